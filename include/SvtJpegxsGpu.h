@@ -1,0 +1,54 @@
+/*
+ * SvtJpegxsGpu.h - GPU extensions of the JPEG XS C API.
+ *
+ * These entry points have no counterpart in the reference API; the
+ * reference-compatible entry points (SvtJpegxsEnc.h, SvtJpegxsDec.h) need
+ * none of them.  They let a caller that already works on the GPU keep its
+ * data there and measure the pipeline:
+ *  - image planes and bitstream buffers passed to send_picture/send_frame may
+ *    be device pointers of the current CUDA device (detected automatically);
+ *  - set_stream binds a handle's GPU work to the caller's CUDA stream;
+ *  - set_timing / read_timing accumulate per-stage GPU time measured with
+ *    CUDA events on the stream the work is launched on.
+ */
+#ifndef SVT_JPEGXS_GPU_H
+#define SVT_JPEGXS_GPU_H
+
+#include "SvtJpegxsDec.h"
+#include "SvtJpegxsEnc.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Encoder stages: 0 host-to-device copy, 1 wavelet transform, 2 rate
+ * control, 3 quantization and packing, 4 device-to-host copy. */
+#define SVT_JPEGXS_GPU_ENC_STAGES 5
+/* Decoder stages: 0 host-to-device copy, 1 unpacking and dequantization,
+ * 2 inverse wavelet transform and output scaling, 3 device-to-host copy. */
+#define SVT_JPEGXS_GPU_DEC_STAGES 4
+
+/* cuda_stream is a cudaStream_t; NULL returns to the handle's own streams
+ * (several frames in flight). */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_set_stream(svt_jpeg_xs_encoder_api_t* enc_api, void* cuda_stream);
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_set_stream(svt_jpeg_xs_decoder_api_t* dec_api, void* cuda_stream);
+
+/* Enabling resets the accumulated stage times. */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_set_timing(svt_jpeg_xs_encoder_api_t* enc_api, uint32_t enable);
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_set_timing(svt_jpeg_xs_decoder_api_t* dec_api, uint32_t enable);
+
+/* Copies up to n accumulated stage times (milliseconds) and returns the
+ * number of frames they cover. */
+PREFIX_API uint64_t svt_jpeg_xs_gpu_encoder_read_timing(svt_jpeg_xs_encoder_api_t* enc_api, double* stage_ms, uint32_t n);
+PREFIX_API uint64_t svt_jpeg_xs_gpu_decoder_read_timing(svt_jpeg_xs_decoder_api_t* dec_api, double* stage_ms, uint32_t n);
+
+/* Quantization and refinement chosen for each precinct row of the most
+ * recently sent picture that has not been returned yet (count >= rows). */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_rc_results(svt_jpeg_xs_encoder_api_t* enc_api, uint8_t* quantization,
+                                                                uint8_t* refinement, uint32_t count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVT_JPEGXS_GPU_H */

@@ -1,0 +1,129 @@
+/*
+ * Internal configuration shared by the host C code and the CUDA kernels.
+ *
+ * A jxs_cfg_t describes one stream configuration: picture geometry, the band
+ * and precinct layout of ISO/IEC 21122 (restating the reference's pi_t,
+ * Source/Lib/Common/Codec/Pi.h:141-180), the weight tables, rate-control
+ * limits, the cached codestream header and the per-slice byte budgets.  It is
+ * plain data so it can be copied to device memory as-is.
+ *
+ * Device data layout ("band-planar"): every band of every component is a 2-D
+ * array covering the whole frame, `h` rows of `pitch` 16-bit sign-magnitude
+ * coefficients (`pitch` a multiple of 8 so rows are 16-byte aligned), at
+ * element offset `coef_off` of one frame buffer.  Precinct row p holds band
+ * rows [p * lines, p * lines + lines_in_precinct).  GCLIs (one byte per group
+ * of 4 coefficients) use the same layout with row pitch `gpitch`.
+ */
+#ifndef JXS_CORE_H
+#define JXS_CORE_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JXS_MAXC 4
+#define JXS_MAXB 10   /* bands per component */
+#define JXS_MAXBL 40  /* bands per picture */
+#define JXS_MAXPK 30  /* packets per precinct */
+#define JXS_NOBAND 0xff
+#define JXS_TRUNC_MAX 15
+#define JXS_PREC_MAX_BYTES 1048575u
+
+/* error codes (SvtJxsErrorType_t values) */
+#define JXS_OK 0
+#define JXS_E_BAD_PARAM ((int32_t)0x80001005)
+#define JXS_E_RESOURCES ((int32_t)0x80001000)
+#define JXS_E_UNDEFINED ((int32_t)0x80001001)
+#define JXS_E_ENC_FRAME ((int32_t)0x80002035)
+#define JXS_E_DEC_PTR ((int32_t)0x80003000)
+#define JXS_E_DEC_BITSTREAM ((int32_t)0x80003001)
+#define JXS_E_DEC_INTERNAL ((int32_t)0x80003002)
+#define JXS_E_DEC_SHORT ((int32_t)0x80003003)
+#define JXS_E_DEC_CONFIG ((int32_t)0x80003004)
+
+typedef struct jxs_band {
+    uint32_t w, h;              /* band size over the whole component */
+    uint32_t x, y;              /* position in the component's wavelet plane */
+    uint32_t lines;             /* band lines per precinct row */
+    uint32_t last_lines;        /* band lines in the last precinct row */
+    uint32_t gcli_w, sig_w;     /* code groups / significance groups per line */
+    uint32_t pitch, gpitch;     /* coefficient / GCLI row pitch */
+    uint64_t coef_off, gcli_off;
+    uint8_t gain, prio, comp, idx;
+    uint32_t gid;               /* position in the codestream band order */
+} jxs_band_t;
+
+typedef struct jxs_comp {
+    uint32_t w, h, sx, sy, dv, dh, nb;
+    uint32_t band0;             /* flat index of band 0 of this component */
+} jxs_comp_t;
+
+typedef struct jxs_packet {
+    uint32_t bs, be, line;      /* global band range [bs, be) and band line */
+} jxs_packet_t;
+
+typedef struct jxs_cfg {
+    uint32_t W, H, nc, fmt, depth, sd;
+    uint32_t dv, dh, prec_h, slice_h, pps, np, nslices;
+    uint32_t nbands_all, nbands;
+    uint8_t g2f[JXS_MAXBL];     /* global band -> flat band index */
+    jxs_comp_t comp[JXS_MAXC];
+    jxs_band_t band[JXS_MAXBL];
+    uint32_t npk;
+    jxs_packet_t pk[JXS_MAXPK];
+    uint32_t short_hdr, lh;
+    uint32_t pk_exist[2];                /* packets present: normal / last precinct row */
+    uint32_t raw_bytes[2][JXS_MAXPK];    /* raw-mode GCLI sub-packet bytes */
+    uint32_t prec_hdr_bytes;             /* ceil((40 + 2 * nbands) / 8) */
+    uint32_t hdrs_bytes[2];              /* precinct header + packet headers */
+    uint32_t qpih, sig, rc_mode, fs, rm, bw, fq;
+    uint8_t max_q, max_r;
+    uint32_t empty[32];                  /* bit r of empty[q]: every band fully truncated */
+    uint32_t lcod;
+    uint8_t hdr[512];
+    uint32_t hdr_len;
+    uint64_t coef_total, gcli_total;     /* per-frame buffer sizes (elements / bytes) */
+    uint32_t max_slice_budget;
+    uint32_t slice_size[8192];           /* bytes of each slice incl. its header (last: incl. EOC) */
+    uint32_t slice_begin[8192];          /* byte offset of each slice in the codestream */
+} jxs_cfg_t;
+
+/* Decoder-side header fields beyond the geometry. */
+typedef struct jxs_hdr_info {
+    uint32_t hdr_len;
+    uint32_t cw, cpih, tnlt;
+} jxs_hdr_info_t;
+
+struct svt_jpeg_xs_encoder_api;
+
+#ifdef __CUDACC__
+#define JXS_HD __host__ __device__
+#else
+#define JXS_HD
+#endif
+
+/* compute_truncation (Source/Lib/Common/Codec/EncDec.c:8-21) */
+static inline JXS_HD uint8_t jxs_truncation(uint8_t gain, uint8_t prio, uint8_t q, uint8_t r) {
+    uint8_t up = prio < r ? 1 : 0;
+    if (q < gain + up) return 0;
+    uint8_t t = (uint8_t)(q - gain - up);
+    return t > JXS_TRUNC_MAX ? JXS_TRUNC_MAX : t;
+}
+
+int32_t jxs_cfg_encoder(jxs_cfg_t* cfg, struct svt_jpeg_xs_encoder_api* api);
+int32_t jxs_cfg_decoder(jxs_cfg_t* cfg, const uint8_t* bs, size_t size, jxs_hdr_info_t* info);
+int32_t jxs_cfg_geometry(jxs_cfg_t* cfg, int for_encoder, uint32_t nc, uint32_t W, uint32_t H, uint32_t dh, uint32_t dv,
+                         uint32_t sd, const uint32_t sx[JXS_MAXC], const uint32_t sy[JXS_MAXC], uint32_t slice_h);
+int32_t jxs_sampling(uint32_t fmt, uint32_t* nc, uint32_t sx[JXS_MAXC], uint32_t sy[JXS_MAXC]);
+uint32_t jxs_frame_bytes_walk(const jxs_cfg_t* cfg, const uint8_t* bs, size_t size, uint32_t hdr_len, uint32_t* prec_off,
+                              int32_t* err);
+void jxs_print_bands(const jxs_cfg_t* cfg);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JXS_CORE_H */

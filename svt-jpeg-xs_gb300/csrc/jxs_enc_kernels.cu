@@ -1,0 +1,961 @@
+/*
+ * Encoder kernels for sm_103a.
+ *
+ *  fwd_dwt_kernel   input scaling + one vertical 5/3 lifting level (in
+ *                   registers, column-parallel) + horizontal lifting of the
+ *                   produced rows (in shared memory) + for the last vertical
+ *                   level all horizontal-only levels; writes 16-bit
+ *                   sign-magnitude coefficients and their GCLIs.
+ *  rc_cost_kernel   per precinct row: GCLI histograms and the byte cost of
+ *                   every (quantization, refinement) candidate.
+ *  rc_select_kernel per slice: the reference's sequential budget carry and
+ *                   binary searches, replayed over the cost table.
+ *  pack_kernel      per precinct row: quantization and bit packing at
+ *                   prefix-summed bit offsets into a shared-memory copy of the
+ *                   precinct, then one coalesced copy to the codestream.
+ *
+ * Integer arithmetic follows the reference one to one (citations inline).
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "jxs_core.h"
+#include "jxs_kernels.cuh"
+
+#define DEV __device__ __forceinline__
+
+/* ------------------------------------------------------------------------ */
+/* shared helpers                                                            */
+/* ------------------------------------------------------------------------ */
+DEV int mirror(int i, int n) {
+    /* symmetric extension without repeating the edge sample */
+    if (i < 0) i = -i;
+    if (i >= n) i = 2 * (n - 1) - i;
+    return i;
+}
+
+DEV int32_t load_src(const DwtJob& J, int row, int x) {
+    const int sh = 20 - J.depth;
+    const int32_t off = 1 << 19;
+    switch (J.src_kind) {
+    case SRC_I32: return ((const int32_t*)J.src)[(long long)row * J.src_pitch + x];
+    case SRC_U8: return ((int32_t)((uint32_t)((const uint8_t*)J.src)[(long long)row * J.src_pitch + x] << sh)) - off;
+    case SRC_U16: {
+        uint32_t v = ((const uint16_t*)J.src)[(long long)row * J.src_pitch + x] & ((1u << J.depth) - 1);
+        return (int32_t)(v << sh) - off;
+    }
+    case SRC_PK8:
+        return ((int32_t)((uint32_t)((const uint8_t*)J.src)[(long long)row * J.src_pitch + 3 * x + J.chan] << sh)) - off;
+    default: {
+        uint32_t v = ((const uint16_t*)J.src)[(long long)row * J.src_pitch + 3 * x + J.chan] & ((1u << J.depth) - 1);
+        return (int32_t)(v << sh) - off;
+    }
+    }
+}
+
+/* image_shift_c (NltEnc.c:12-31): Fq = 8 fractional bits rounded off, no -0 */
+DEV uint32_t to_sm(int32_t v) {
+    if (v >= 0) return (uint32_t)((v + 128) >> 8);
+    uint32_t m = (uint32_t)((-v + 128) >> 8);
+    return m ? (m | 0x8000u) : 0u;
+}
+
+/* Forward 5/3 lifting of rows held in shared memory (Dwt.c:15-40), for all
+ * rows of a block at once.  Elements of a row sit at stride S; n elements. */
+template <typename RowFn>
+DEV void fwd_h_level(RowFn row, int nrows, int n, int S) {
+    const int n2 = n >> 1, n1 = (n + 1) >> 1;
+    for (int t = threadIdx.x; t < nrows * n2; t += blockDim.x) {
+        int r = t / n2, j = t - r * n2;
+        int32_t* p = row(r);
+        int32_t a = p[S * 2 * j];
+        int32_t c = (2 * j + 2 < n) ? p[S * (2 * j + 2)] : a;
+        p[S * (2 * j + 1)] -= (a + c) >> 1;
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < nrows * n1; t += blockDim.x) {
+        int r = t / n1, i = t - r * n1;
+        int32_t* p = row(r);
+        int jp = min(max(i - 1, 0), n2 - 1), jc = min(i, n2 - 1);
+        p[S * 2 * i] += (p[S * (2 * jp + 1)] + p[S * (2 * jc + 1)] + 2) >> 2;
+    }
+    __syncthreads();
+}
+
+/* Writes `n` elements (at p[o + S * k]) of one band row as sign-magnitude
+ * coefficients, 4 per thread, with the GCLI of each 4-group
+ * (gc_precinct_stage_scalar_c, GcStageProcess.c:22-68). */
+DEV void emit_band_row(const int32_t* p, int o, int S, int n, const jxs_band_t& bd, int brow, uint16_t* coef, uint8_t* gcli) {
+    uint16_t* crow = coef + bd.coef_off + (uint64_t)brow * bd.pitch;
+    uint8_t* grow = gcli + bd.gcli_off + (uint64_t)brow * bd.gpitch;
+    const int groups = (n + 3) >> 2;
+    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
+        uint32_t c[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            int idx = 4 * g + k;
+            c[k] = idx < n ? to_sm(p[o + S * idx]) : 0u;
+        }
+        *(uint2*)(crow + 4 * g) = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+        uint32_t m = (c[0] | c[1] | c[2] | c[3]) & 0x7fffu;
+        grow[g] = (uint8_t)(m ? 32 - __clz(m) : 0);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Forward transform, one level per launch.                                  */
+/* ------------------------------------------------------------------------ */
+template <bool VERT>
+__global__ void __launch_bounds__(512) fwd_dwt_kernel(const __grid_constant__ DwtLaunch L, const jxs_band_t* __restrict__ bands,
+                                                      uint16_t* __restrict__ coef, uint8_t* __restrict__ gcli) {
+    extern __shared__ int32_t sm[];
+    int j = 0;
+    while (j + 1 < L.njobs && (int)blockIdx.x >= L.job[j + 1].first_block) j++;
+    const DwtJob& J = L.job[j];
+    const int rb = blockIdx.x - J.first_block;
+    const int w = J.w, h = J.h, sp = J.smem_pitch;
+
+    if (VERT) {
+        const int n1 = (h + 1) >> 1, n2 = h >> 1;
+        const int r0 = rb * J.R;
+        const int rc = min(J.R, n1 - r0);
+        const int hc = max(0, min(J.R, n2 - r0));
+        int32_t* Ls = sm;
+        int32_t* Hs = sm + J.R * sp;
+        /* vertical lifting, one column per thread (Dwt.c:337-398 in frame form) */
+        for (int x = threadIdx.x; x < w; x += blockDim.x) {
+            const int jp = min(max(r0 - 1, 0), n2 - 1);
+            int32_t hprev;
+            {
+                int32_t a = load_src(J, 2 * jp, x), b = load_src(J, 2 * jp + 1, x), c = load_src(J, mirror(2 * jp + 2, h), x);
+                hprev = b - ((a + c) >> 1);
+            }
+            int32_t xe = load_src(J, 2 * r0, x);
+            for (int k = 0; k < rc; k++) {
+                const int i = r0 + k;
+                int32_t hcur, xn = 0;
+                if (i < n2) {
+                    int32_t xo = load_src(J, 2 * i + 1, x);
+                    xn = load_src(J, mirror(2 * i + 2, h), x);
+                    hcur = xo - ((xe + xn) >> 1);
+                    Hs[k * sp + x] = hcur;
+                } else {
+                    hcur = hprev;
+                }
+                Ls[k * sp + x] = xe + ((hprev + hcur + 2) >> 2);
+                hprev = hcur;
+                xe = xn;
+            }
+        }
+        __syncthreads();
+        auto all_rows = [&](int r) { return r < rc ? Ls + r * sp : Hs + (r - rc) * sp; };
+        fwd_h_level(all_rows, rc + hc, w, 1);
+        const int w1 = (w + 1) >> 1, w2 = w >> 1;
+        /* horizontal-only levels on the low rows */
+        int m = w1, S = 2;
+        if (J.last) {
+            auto lrows = [&](int r) { return Ls + r * sp; };
+            for (int e = 0; e < J.nh; e++) {
+                fwd_h_level(lrows, rc, m, S);
+                m = (m + 1) >> 1;
+                S <<= 1;
+            }
+        }
+        /* outputs */
+        for (int k = 0; k < hc; k++) {
+            emit_band_row(Hs + k * sp, 0, 2, w1, bands[J.b_lh], r0 + k, coef, gcli);
+            emit_band_row(Hs + k * sp, 1, 2, w2, bands[J.b_hh], r0 + k, coef, gcli);
+        }
+        for (int k = 0; k < rc; k++) {
+            const int32_t* p = Ls + k * sp;
+            emit_band_row(p, 1, 2, w2, bands[J.b_hl], r0 + k, coef, gcli);
+            if (J.last) {
+                int mm = w1, SS = 2;
+                for (int e = 0; e < J.nh; e++) {
+                    emit_band_row(p, SS, 2 * SS, mm >> 1, bands[J.b_hf[e]], r0 + k, coef, gcli);
+                    mm = (mm + 1) >> 1;
+                    SS <<= 1;
+                }
+                emit_band_row(p, 0, SS, mm, bands[J.b_ll], r0 + k, coef, gcli);
+            } else {
+                int32_t* dst = J.ll + (long long)(r0 + k) * J.ll_pitch;
+                for (int x = threadIdx.x; x < w1; x += blockDim.x) dst[x] = p[2 * x];
+            }
+        }
+    } else {
+        /* no vertical level: horizontal-only levels straight from the input */
+        const int r0 = rb * J.R;
+        const int rc = min(J.R, h - r0);
+        for (int t = threadIdx.x; t < rc * w; t += blockDim.x) {
+            int k = t / w, x = t - k * w;
+            sm[k * sp + x] = load_src(J, r0 + k, x);
+        }
+        __syncthreads();
+        auto rows = [&](int r) { return sm + r * sp; };
+        int m = w, S = 1;
+        for (int e = 0; e < J.nh; e++) {
+            fwd_h_level(rows, rc, m, S);
+            m = (m + 1) >> 1;
+            S <<= 1;
+        }
+        for (int k = 0; k < rc; k++) {
+            const int32_t* p = sm + k * sp;
+            int mm = w, SS = 1;
+            for (int e = 0; e < J.nh; e++) {
+                emit_band_row(p, SS, 2 * SS, mm >> 1, bands[J.b_hf[e]], r0 + k, coef, gcli);
+                mm = (mm + 1) >> 1;
+                SS <<= 1;
+            }
+            emit_band_row(p, 0, SS, mm, bands[J.b_ll], r0 + k, coef, gcli);
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Rate control                                                              */
+/* ------------------------------------------------------------------------ */
+#define RC_MAXBL 80
+
+struct BandLine {
+    uint16_t fb;       /* flat band */
+    uint8_t line, pk;
+    uint32_t row;      /* band row */
+    uint32_t gcli_w, sig_w, w;
+    uint32_t g0;       /* first group in the precinct's flattened group order */
+    uint32_t s0;       /* first significance group in flattened order */
+};
+
+/* Builds the band-line list of precinct row p in codestream order (packet
+ * order, then band order inside the packet).  Returns the count. */
+DEV int build_bandlines(const jxs_cfg_t* cfg, int p, int last, BandLine* bl, uint8_t* blmap /* [fb*4+line] */,
+                        uint32_t* total_groups, uint32_t* total_sig) {
+    int n = 0;
+    uint32_t g0 = 0, s0 = 0;
+    for (int i = 0; i < JXS_MAXBL * 4; i++) blmap[i] = 0xff;
+    for (uint32_t k = 0; k < cfg->npk; k++) {
+        const uint32_t l = cfg->pk[k].line;
+        for (uint32_t gb = cfg->pk[k].bs; gb < cfg->pk[k].be; gb++) {
+            const int fb = cfg->g2f[gb];
+            const jxs_band_t& bd = cfg->band[fb];
+            const uint32_t lines = last ? bd.last_lines : bd.lines;
+            if (l >= lines) continue;
+            BandLine& b = bl[n];
+            b.fb = (uint16_t)fb;
+            b.line = (uint8_t)l;
+            b.pk = (uint8_t)k;
+            b.row = (uint32_t)p * bd.lines + l;
+            b.gcli_w = bd.gcli_w;
+            b.sig_w = bd.sig_w;
+            b.w = bd.w;
+            b.g0 = g0;
+            b.s0 = s0;
+            blmap[fb * 4 + l] = (uint8_t)n;
+            g0 += bd.gcli_w;
+            s0 += bd.sig_w;
+            n++;
+        }
+    }
+    *total_groups = g0;
+    *total_sig = s0;
+    return n;
+}
+
+DEV int find_bl_by_sig(const BandLine* bl, int n, uint32_t s) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (bl[mid].s0 <= s) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+/* Reads up to 8 GCLIs of significance group s of a band line. */
+DEV int load_sig_group(const uint8_t* __restrict__ gcli, const jxs_band_t& bd, const BandLine& b, uint32_t s, uint8_t v[8]) {
+    const uint8_t* row = gcli + bd.gcli_off + (uint64_t)b.row * bd.gpitch + 8 * s;
+    uint2 raw = *(const uint2*)row; /* rows are 16-byte aligned, groups of 8 are 8-byte aligned */
+    const int cnt = min(8, (int)b.gcli_w - (int)(8 * s));
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        uint32_t word = k < 4 ? raw.x : raw.y;
+        v[k] = k < cnt ? (uint8_t)((word >> (8 * (k & 3))) & 0xff) : 0;
+    }
+    return cnt;
+}
+
+/* Byte cost of every (quantization, refinement) candidate of one precinct
+ * row: rate_control_lut_fill, rate_control_calculate_band_best_method and
+ * precinct_get_budget_bytes (RateControl.c:18-154, 457-781). */
+__global__ void __launch_bounds__(256) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
+                                                      uint32_t* __restrict__ cost) {
+    __shared__ BandLine bl[RC_MAXBL];
+    __shared__ uint8_t blmap[JXS_MAXBL * 4];
+    __shared__ uint32_t hist[RC_MAXBL][16];
+    __shared__ uint32_t shist[RC_MAXBL][16];
+    __shared__ int pmax[RC_MAXBL];
+    __shared__ uint32_t t_data[RC_MAXBL][16], t_nosig[RC_MAXBL][16], t_sigg[RC_MAXBL][16];
+    __shared__ uint8_t meth[JXS_MAXBL][16];
+    __shared__ int s_nbl;
+    __shared__ uint32_t s_ng, s_ns;
+
+    const int p = blockIdx.x;
+    const int last = (p + 1 >= (int)cfg->np);
+    if (threadIdx.x == 0) s_nbl = build_bandlines(cfg, p, last, bl, blmap, &s_ng, &s_ns);
+    for (int t = threadIdx.x; t < RC_MAXBL * 16; t += blockDim.x) {
+        hist[t / 16][t % 16] = 0;
+        shist[t / 16][t % 16] = 0;
+    }
+    for (int t = threadIdx.x; t < RC_MAXBL; t += blockDim.x) pmax[t] = -1;
+    __syncthreads();
+    const int nbl = s_nbl;
+    for (uint32_t s = threadIdx.x; s < s_ns; s += blockDim.x) {
+        const int b = find_bl_by_sig(bl, nbl, s);
+        const BandLine& B = bl[b];
+        uint8_t v[8];
+        const int cnt = load_sig_group(gcli, cfg->band[B.fb], B, s - B.s0, v);
+        uint32_t mx = 0;
+        /* nibble counters: at most 8 equal values per group */
+        uint64_t nib = 0;
+        for (int k = 0; k < cnt; k++) {
+            nib += 1ull << (4 * v[k]);
+            mx = max(mx, (uint32_t)v[k]);
+        }
+        while (nib) {
+            int bin = (__ffsll((long long)nib) - 1) >> 2;
+            uint32_t c = (uint32_t)((nib >> (4 * bin)) & 15);
+            atomicAdd(&hist[b][bin], c);
+            nib &= ~(15ull << (4 * bin));
+        }
+        if (cnt == 8) atomicAdd(&shist[b][mx], 1u);
+        else pmax[b] = (int)mx;
+    }
+    __syncthreads();
+    /* per band line and truncation: data bits, GCLI bits without
+     * significance, GCLI bits with significance */
+    for (int t = threadIdx.x; t < nbl * 16; t += blockDim.x) {
+        const int b = t >> 4, g = t & 15;
+        uint32_t data = 0, zero = 0, zs = 0;
+        for (int v = 0; v < 16; v++) {
+            uint32_t c = hist[b][v];
+            if (v > g) data += (uint32_t)(v - g + 1) * c;
+            else {
+                zero += c;
+                zs += shist[b][v];
+            }
+        }
+        uint32_t zeroed = zs * 8;
+        const BandLine& B = bl[b];
+        if (pmax[b] >= 0 && pmax[b] <= g) zeroed += B.gcli_w - (B.gcli_w / 8) * 8;
+        t_data[b][g] = data * 4;
+        t_nosig[b][g] = data + zero;
+        t_sigg[b][g] = data + zero - zeroed;
+    }
+    __syncthreads();
+    /* coding method per band and truncation: significance only if strictly
+     * cheaper (RateControl.c:528-575) */
+    for (int t = threadIdx.x; t < (int)cfg->nbands * 16; t += blockDim.x) {
+        const int fb = t >> 4, g = t & 15;
+        const jxs_band_t& bd = cfg->band[fb];
+        const uint32_t lines = last ? bd.last_lines : bd.lines;
+        uint32_t cn = 0, cs = bd.sig_w * lines;
+        for (uint32_t l = 0; l < lines; l++) {
+            const int b = blmap[fb * 4 + l];
+            cn += t_nosig[b][g];
+            cs += t_sigg[b][g];
+        }
+        meth[fb][g] = (uint8_t)(cfg->sig && cn > cs);
+    }
+    __syncthreads();
+    const int nq = cfg->max_q + 1, nr = cfg->max_r + 1;
+    uint32_t* out = cost + (uint64_t)p * 32 * 32;
+    for (int t = threadIdx.x; t < nq * nr; t += blockDim.x) {
+        const int q = t / nr, r = t - q * nr;
+        uint32_t total = 0;
+        for (uint32_t k = 0; k < cfg->npk; k++) {
+            const uint32_t l = cfg->pk[k].line;
+            uint32_t db = 0, gb = 0, sb = 0;
+            for (uint32_t gband = cfg->pk[k].bs; gband < cfg->pk[k].be; gband++) {
+                const int fb = cfg->g2f[gband];
+                const int b = blmap[fb * 4 + l];
+                if (b == 0xff) continue;
+                const jxs_band_t& bd = cfg->band[fb];
+                const int g = jxs_truncation(bd.gain, bd.prio, (uint8_t)q, (uint8_t)r);
+                db += t_data[b][g];
+                if (meth[fb][g]) {
+                    gb += t_sigg[b][g];
+                    sb += bd.sig_w;
+                } else {
+                    gb += t_nosig[b][g];
+                }
+            }
+            const uint32_t dB = (db + 7) >> 3, gB = (gb + 7) >> 3, sB = (sb + 7) >> 3;
+            total += dB;
+            const uint32_t raw = cfg->raw_bytes[last][k];
+            total += (sB + gB > raw) ? raw : sB + gB;
+        }
+        out[q * 32 + r] = total;
+    }
+}
+
+/* binary_search_init / binary_search_next_step (BinarySearch.c:9-78) */
+struct BSearch {
+    int beg, end, step, best, last, below;
+};
+DEV void bs_init(BSearch& s, int beg, int end, int below, int step) {
+    s.beg = beg; s.end = end; s.below = below; s.best = -1; s.last = -1;
+    s.step = step ? step : (end - beg) / 2;
+}
+enum { BS_BEGIN = 0, BS_TOO_SMALL, BS_TOO_BIG, BS_OUT_OF_RANGE };
+enum { BS_CONTINUE = 0, BS_FOUND, BS_ERROR };
+DEV int bs_next(BSearch& s, int res, int* out) {
+    if (res == BS_TOO_SMALL) {
+        if (s.below && (s.best == -1 || s.best < s.last)) s.best = s.last;
+        if (s.end >= s.last + 1) s.beg = s.last + 1;
+        else {
+            if (s.best == -1) return BS_ERROR;
+            *out = s.best;
+            return BS_FOUND;
+        }
+    } else if (res == BS_TOO_BIG || res == BS_OUT_OF_RANGE) {
+        if (res == BS_TOO_BIG && !s.below && (s.best == -1 || s.best > s.last)) s.best = s.last;
+        if (s.beg <= s.last - 1) s.end = s.last - 1;
+        else {
+            if (s.best == -1) return BS_ERROR;
+            *out = s.best;
+            return BS_FOUND;
+        }
+    }
+    if (s.step > s.end - s.beg) s.step = (s.end - s.beg + 1) / 2;
+    s.last = s.step + s.beg;
+    *out = s.last;
+    return BS_CONTINUE;
+}
+
+/* One block per slice: the slice's precinct budgets with the padding carry
+ * of rate-control mode 1 (PackStageProcess.c:600-684, 293-309) and
+ * rate_control_precinct (RateControl.c:1259-1333) with its binary searches
+ * (:889-1083), evaluated on the cost table. */
+__global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restrict__ cfg, const uint32_t* __restrict__ cost,
+                                                        PrecRC* __restrict__ rc, int* __restrict__ status) {
+    __shared__ uint32_t tbl[32 * 32];
+    __shared__ uint32_t s_carry, s_run;
+    __shared__ int s_err;
+    const int s = blockIdx.x;
+    const int last_slice = (s + 1 == (int)cfg->nslices);
+    const uint32_t slice_budget = cfg->slice_size[s] - 6 - (last_slice ? 2 : 0);
+    const uint32_t first_p = cfg->pps * s;
+    const uint32_t nprec = last_slice ? cfg->np - first_p : cfg->pps;
+    uint32_t min_b = slice_budget / nprec;
+    uint32_t left = slice_budget - min_b * nprec;
+    uint32_t first_b = min_b;
+    if (cfg->rc_mode == 1) {
+        first_b = min(slice_budget, first_b * 110 / 100);
+        if (nprec > 1) {
+            min_b = (slice_budget - first_b) / (nprec - 1);
+            left = slice_budget - min_b * (nprec - 1) - first_b;
+        } else {
+            left = 0;
+        }
+    }
+    if (threadIdx.x == 0) {
+        s_carry = 0;
+        s_run = cfg->slice_begin[s] + 6;
+        s_err = 0;
+    }
+    const int nr = cfg->max_r + 1;
+    for (uint32_t i = 0; i < nprec; i++) {
+        const uint32_t p = first_p + i;
+        __syncthreads();
+        if (s_err) break;
+        for (int t = threadIdx.x; t < (cfg->max_q + 1) * nr; t += blockDim.x) {
+            const int q = t / nr, r = t - q * nr;
+            tbl[q * 32 + r] = cost[(uint64_t)p * 1024 + q * 32 + r];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const int last = (p + 1 >= cfg->np);
+            const uint32_t budget = (i == 0 ? first_b : min_b) + (i < left ? 1 : 0) + s_carry;
+            const uint32_t hdr = cfg->hdrs_bytes[last];
+            int err = 0;
+            if (budget > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
+            else if (budget <= hdr) err = JXS_E_UNDEFINED;
+            int q = 0, r = 0;
+            uint32_t data = 0;
+            if (!err) {
+                const uint32_t avail = budget - hdr;
+                BSearch bs;
+                int step = 6;
+                if (step > cfg->max_q) step = 0;
+                bs_init(bs, 0, cfg->max_q, 0, step);
+                int res, next = BS_BEGIN, v = 0;
+                while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
+                    if (cfg->empty[v] & 1u) next = BS_OUT_OF_RANGE;
+                    else next = tbl[v * 32] > avail ? BS_TOO_SMALL : BS_TOO_BIG;
+                }
+                if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
+                q = v;
+                if (!err) {
+                    step = 6;
+                    if (step >= cfg->max_r) step = 0;
+                    bs_init(bs, 0, cfg->max_r, 1, step);
+                    next = BS_BEGIN;
+                    while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
+                        if ((cfg->empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
+                        else next = tbl[q * 32 + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
+                    }
+                    if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
+                    r = v;
+                    data = tbl[q * 32 + r];
+                }
+                if (!err) {
+                    uint32_t padding = avail - data;
+                    uint32_t total = budget;
+                    if (cfg->rc_mode == 1 && i + 1 < nprec) {
+                        total -= padding;
+                        s_carry = padding;
+                    } else {
+                        s_carry = 0;
+                    }
+                    PrecRC o;
+                    o.total_bytes = total;
+                    o.offset = s_run;
+                    o.data_bytes = data;
+                    o.q = (uint8_t)q;
+                    o.r = (uint8_t)r;
+                    o.first_in_slice = (uint8_t)(i == 0);
+                    o.pad = 0;
+                    rc[p] = o;
+                    s_run += total;
+                }
+            }
+            if (err) {
+                s_err = err;
+                JXS_STATUS_SET(status, err);
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Packing                                                                   */
+/* ------------------------------------------------------------------------ */
+#define PK_THREADS 512
+
+/* OR `n` (<= 32) bits of `v` at bit position `pos` of a big-endian bit
+ * string stored in native byte order.  Writes beyond the precinct's words
+ * are dropped and flagged (they mean the sizes disagree with the rate
+ * control). */
+__shared__ uint32_t pk_nwords;
+__shared__ int pk_overflow;
+DEV void put_bits(uint32_t* buf, uint32_t pos, uint32_t v, uint32_t n) {
+    if (!n) return;
+    const uint32_t w = pos >> 5, sh = pos & 31;
+    if (w + (sh + n > 32 ? 1 : 0) >= pk_nwords) {
+        pk_overflow = 1;
+        return;
+    }
+    if (sh + n <= 32) {
+        atomicOr(&buf[w], __byte_perm(v << (32 - sh - n), 0, 0x0123));
+    } else {
+        const uint32_t n1 = 32 - sh, n2 = n - n1;
+        atomicOr(&buf[w], __byte_perm(v >> n2, 0, 0x0123));
+        atomicOr(&buf[w + 1], __byte_perm(v << (32 - n2), 0, 0x0123));
+    }
+}
+DEV void put_bits64(uint32_t* buf, uint32_t pos, uint64_t v, uint32_t n) {
+    if (n > 32) {
+        put_bits(buf, pos, (uint32_t)(v >> 32), n - 32);
+        put_bits(buf, pos + n - 32, (uint32_t)v, 32);
+    } else {
+        put_bits(buf, pos, (uint32_t)v, n);
+    }
+}
+
+/* quant_deadzone_c / quant_uniform_c (Quant.c:9-45); the reference skips
+ * quantization entirely when gtli is 0 (QuantStageProcess.c:18-31). */
+DEV uint32_t quantize(uint32_t v, uint32_t gcli, uint32_t t, uint32_t uniform) {
+    if (t == 0) return v;
+    const uint32_t sign = v & 0x8000u;
+    uint32_t m = v & 0x7fffu;
+    if (uniform) {
+        const uint32_t s = gcli - t + 1;
+        m = ((((m << s) - m + (1u << gcli)) & 0xffffu) >> (gcli + 1)) & 0xffffu;
+        m = (m << t) & 0xffffu;
+    } else {
+        m = (m >> t) << t;
+    }
+    return m ? (m | sign) : 0u;
+}
+
+struct PackBL {
+    uint16_t fb;
+    uint8_t line, pk, t, meth, raw;
+    uint32_t row, gcli_w, sig_w, w, g0, s0;
+    uint32_t data_bits, nosig_bits, zeroed_bits;
+    uint32_t sig_pos, gcli_pos, data_pos;  /* bit positions inside the precinct */
+    uint32_t vlc_pref, data_pref;          /* flattened prefix at the first group */
+};
+
+/* Block-wide exclusive scan of two counters. */
+DEV void block_scan2(uint32_t a, uint32_t b, uint32_t* ea, uint32_t* eb, uint32_t* wa, uint32_t* wb) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t ia = a, ib = b;
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t ta = __shfl_up_sync(0xffffffffu, ia, o), tb = __shfl_up_sync(0xffffffffu, ib, o);
+        if (lane >= o) { ia += ta; ib += tb; }
+    }
+    if (lane == 31) { wa[warp] = ia; wb[warp] = ib; }
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t va = lane < nw ? wa[lane] : 0, vb = lane < nw ? wb[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t ta = __shfl_up_sync(0xffffffffu, va, o), tb = __shfl_up_sync(0xffffffffu, vb, o);
+            if (lane >= o) { va += ta; vb += tb; }
+        }
+        if (lane < nw) { wa[lane] = va; wb[lane] = vb; }
+    }
+    __syncthreads();
+    const uint32_t ba = warp ? wa[warp - 1] : 0, bb = warp ? wb[warp - 1] : 0;
+    *ea = ba + ia - a;
+    *eb = bb + ib - b;
+    __syncthreads();
+}
+
+DEV int find_bl_by_group(const PackBL* bl, int n, uint32_t g) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (bl[mid].g0 <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+/* pack_precinct (PackPrecinct.c:235-572) for one precinct row; vertical
+ * prediction and sign handling off. */
+__global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
+                                                          const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
+                                                          uint8_t* __restrict__ out, uint32_t cap_words, uint32_t sig_cap,
+                                                          int* status) {
+    extern __shared__ uint32_t buf[];
+    uint8_t* sflag = (uint8_t*)(buf + cap_words); /* per significance group: all GCLIs <= gtli */
+    __shared__ PackBL bl[RC_MAXBL];
+    __shared__ BandLine tmp[RC_MAXBL];
+    __shared__ uint8_t blmap[JXS_MAXBL * 4];
+    __shared__ uint32_t wsa[PK_THREADS / 32], wsb[PK_THREADS / 32];
+    __shared__ int s_nbl, s_ok;
+    __shared__ uint32_t s_ng, s_ns;
+
+    const int p = blockIdx.x;
+    const int last = (p + 1 >= (int)cfg->np);
+    const PrecRC R = rc[p];
+    /* nothing to pack once the rate control failed somewhere in the frame;
+     * the flag is read once so that the whole block takes the same branch */
+    if (threadIdx.x == 0) s_ok = *(volatile int*)status == 0;
+    __syncthreads();
+    if (!s_ok) return;
+    const uint32_t total = R.total_bytes;
+    const uint32_t words = (total + 3) >> 2;
+    if (words > cap_words) {
+        if (threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) buf[i] = 0;
+    if (threadIdx.x == 0) {
+        pk_nwords = words;
+        pk_overflow = 0;
+        int n = build_bandlines(cfg, p, last, tmp, blmap, &s_ng, &s_ns);
+        for (int b = 0; b < n; b++) {
+            const jxs_band_t& bd = cfg->band[tmp[b].fb];
+            PackBL& o = bl[b];
+            o.fb = tmp[b].fb; o.line = tmp[b].line; o.pk = tmp[b].pk;
+            o.row = tmp[b].row; o.gcli_w = tmp[b].gcli_w; o.sig_w = tmp[b].sig_w; o.w = tmp[b].w;
+            o.g0 = tmp[b].g0; o.s0 = tmp[b].s0;
+            o.t = jxs_truncation(bd.gain, bd.prio, R.q, R.r);
+            o.data_bits = o.nosig_bits = o.zeroed_bits = 0;
+        }
+        s_nbl = n;
+    }
+    __syncthreads();
+    const int nbl = s_nbl;
+    if (s_ns > sig_cap) {
+        if (threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        return;
+    }
+    /* per band line: data bits, GCLI bits, significance-zeroed GCLIs */
+    for (uint32_t s = threadIdx.x; s < s_ns; s += blockDim.x) {
+        const int b = find_bl_by_sig((const BandLine*)tmp, nbl, s);
+        const BandLine& B = tmp[b];
+        uint8_t v[8];
+        const int cnt = load_sig_group(gcli, cfg->band[B.fb], B, s - B.s0, v);
+        const uint32_t t = bl[b].t;
+        uint32_t data = 0, nosig = 0, mx = 0;
+        for (int k = 0; k < cnt; k++) {
+            mx = max(mx, (uint32_t)v[k]);
+            if (v[k] > t) {
+                data += 4 * (v[k] - t + 1);
+                nosig += v[k] - t + 1;
+            } else {
+                nosig += 1;
+            }
+        }
+        atomicAdd(&bl[b].data_bits, data);
+        atomicAdd(&bl[b].nosig_bits, nosig);
+        if (mx <= t) atomicAdd(&bl[b].zeroed_bits, (uint32_t)cnt);
+        sflag[s] = (uint8_t)(mx <= t);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        /* method per band (strictly cheaper), then packet sizes and positions */
+        uint8_t meth[JXS_MAXBL];
+        for (uint32_t fb = 0; fb < cfg->nbands; fb++) {
+            const jxs_band_t& bd = cfg->band[fb];
+            const uint32_t lines = last ? bd.last_lines : bd.lines;
+            uint32_t cn = 0, cs = bd.sig_w * lines;
+            for (uint32_t l = 0; l < lines; l++) {
+                const PackBL& b = bl[blmap[fb * 4 + l]];
+                cn += b.nosig_bits;
+                cs += b.nosig_bits - b.zeroed_bits;
+            }
+            meth[fb] = (uint8_t)(cfg->sig && cn > cs);
+        }
+        uint8_t* bytes = (uint8_t*)buf;
+        const uint32_t hdr = cfg->prec_hdr_bytes;
+        const uint32_t lprc = total - hdr;
+        bytes[0] = (uint8_t)(lprc >> 16);
+        bytes[1] = (uint8_t)(lprc >> 8);
+        bytes[2] = (uint8_t)lprc;
+        bytes[3] = R.q;
+        bytes[4] = R.r;
+        uint32_t pos = 40;
+        for (uint32_t gb = 0; gb < cfg->nbands_all; gb++) {
+            const int fb = cfg->g2f[gb];
+            if (fb == JXS_NOBAND) continue;
+            const jxs_band_t& bd = cfg->band[fb];
+            const uint32_t lines = last ? bd.last_lines : bd.lines;
+            const uint32_t d = (lines > 0 && meth[fb]) ? 2u : 0u;
+            bytes[pos >> 3] |= (uint8_t)(d << (6 - (pos & 7)));
+            pos += 2;
+        }
+        pos = hdr * 8;
+        uint32_t vlc_run = 0, data_run = 0;
+        int b = 0;
+        for (uint32_t k = 0; k < cfg->npk; k++) {
+            if (b >= nbl || bl[b].pk != k) continue; /* packet absent in this precinct */
+            int b_end = b;
+            uint32_t db = 0, gbits = 0, sbits = 0;
+            while (b_end < nbl && bl[b_end].pk == k) {
+                PackBL& B = bl[b_end];
+                B.meth = meth[B.fb];
+                db += B.data_bits;
+                gbits += B.meth ? B.nosig_bits - B.zeroed_bits : B.nosig_bits;
+                sbits += B.meth ? B.sig_w : 0;
+                b_end++;
+            }
+            const uint32_t dB = (db + 7) >> 3, gB = (gbits + 7) >> 3, sB = (sbits + 7) >> 3;
+            const uint32_t rawB = cfg->raw_bytes[last][k];
+            const int raw = sB + gB > rawB;
+            const uint32_t gcl_bytes = raw ? rawB : gB;
+            /* packet header (PackHeaders.c:98-127), sign length 0 */
+            const uint32_t hp = pos >> 3;
+            if (hp + 7 > words * 4) {
+                pos = 0xffffffffu; /* inconsistent sizes: rejected below */
+                break;
+            }
+            if (cfg->short_hdr) {
+                bytes[hp + 0] = (uint8_t)((raw << 7) | ((dB >> 8) & 0x7f));
+                bytes[hp + 1] = (uint8_t)dB;
+                bytes[hp + 2] = (uint8_t)(gcl_bytes >> 5);
+                bytes[hp + 3] = (uint8_t)((gcl_bytes & 0x1f) << 3);
+                bytes[hp + 4] = 0;
+                pos += 40;
+            } else {
+                bytes[hp + 0] = (uint8_t)((raw << 7) | ((dB >> 13) & 0x7f));
+                bytes[hp + 1] = (uint8_t)(dB >> 5);
+                bytes[hp + 2] = (uint8_t)(((dB & 0x1f) << 3) | ((gcl_bytes >> 17) & 7));
+                bytes[hp + 3] = (uint8_t)(gcl_bytes >> 9);
+                bytes[hp + 4] = (uint8_t)(gcl_bytes >> 1);
+                bytes[hp + 5] = (uint8_t)((gcl_bytes & 1) << 7);
+                bytes[hp + 6] = 0;
+                pos += 56;
+            }
+            if (raw) {
+                uint32_t gp = pos;
+                for (int x = b; x < b_end; x++) {
+                    bl[x].raw = 1;
+                    bl[x].gcli_pos = gp;
+                    gp += 4 * bl[x].gcli_w;
+                    bl[x].vlc_pref = vlc_run;
+                }
+                pos += rawB * 8;
+            } else {
+                uint32_t sp = pos;
+                for (int x = b; x < b_end; x++) {
+                    bl[x].raw = 0;
+                    bl[x].sig_pos = sp;
+                    if (bl[x].meth) sp += bl[x].sig_w;
+                }
+                pos += sB * 8;
+                uint32_t gp = pos;
+                for (int x = b; x < b_end; x++) {
+                    bl[x].gcli_pos = gp;
+                    bl[x].vlc_pref = vlc_run;
+                    const uint32_t n = bl[x].meth ? bl[x].nosig_bits - bl[x].zeroed_bits : bl[x].nosig_bits;
+                    gp += n;
+                    vlc_run += n;
+                }
+                pos += gB * 8;
+            }
+            uint32_t dp = pos;
+            for (int x = b; x < b_end; x++) {
+                bl[x].data_pos = dp;
+                bl[x].data_pref = data_run;
+                dp += bl[x].data_bits;
+                data_run += bl[x].data_bits;
+            }
+            pos += dB * 8;
+            b = b_end;
+        }
+        /* the packed size must be what the rate control paid for */
+        s_ok = pos != 0xffffffffu && (pos & 7) == 0 && (pos >> 3) <= total && (pos >> 3) == cfg->hdrs_bytes[last] + R.data_bytes;
+        if (!s_ok) JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    const uint32_t uniform = cfg->qpih;
+    /* significance flags: 1 = group fully below the truncation */
+    for (uint32_t s = threadIdx.x; s < s_ns; s += blockDim.x) {
+        const int b = find_bl_by_sig((const BandLine*)tmp, nbl, s);
+        const PackBL& B = bl[b];
+        if (B.raw || !B.meth) continue;
+        if (sflag[s]) put_bits(buf, B.sig_pos + (s - B.s0), 1u, 1);
+    }
+    /* GCLIs and data: each thread owns a contiguous run of groups */
+    const uint32_t G = s_ng;
+    const uint32_t per = (G + blockDim.x - 1) / blockDim.x;
+    const uint32_t g_beg = min(G, threadIdx.x * per), g_end = min(G, g_beg + per);
+    uint32_t sum_v = 0, sum_d = 0;
+    {
+        int b = g_beg < g_end ? find_bl_by_group(bl, nbl, g_beg) : 0;
+        for (uint32_t g = g_beg; g < g_end; g++) {
+            while (b + 1 < nbl && bl[b + 1].g0 <= g) b++;
+            const PackBL& B = bl[b];
+            const jxs_band_t& bd = cfg->band[B.fb];
+            const uint32_t x = g - B.g0;
+            const uint32_t v = gcli[bd.gcli_off + (uint64_t)B.row * bd.gpitch + x];
+            const uint32_t t = B.t;
+            if (v > t) sum_d += 4 * (v - t + 1);
+            if (!B.raw) {
+                const bool skip = B.meth && sflag[B.s0 + (x >> 3)];
+                if (!skip) sum_v += v > t ? v - t + 1 : 1;
+            }
+        }
+    }
+    uint32_t ev, ed;
+    block_scan2(sum_v, sum_d, &ev, &ed, wsa, wsb);
+    {
+        int b = g_beg < g_end ? find_bl_by_group(bl, nbl, g_beg) : 0;
+        for (uint32_t g = g_beg; g < g_end; g++) {
+            while (b + 1 < nbl && bl[b + 1].g0 <= g) b++;
+            const PackBL& B = bl[b];
+            const jxs_band_t& bd = cfg->band[B.fb];
+            const uint32_t x = g - B.g0;
+            const uint32_t v = gcli[bd.gcli_off + (uint64_t)B.row * bd.gpitch + x];
+            const uint32_t t = B.t;
+            if (B.raw) {
+                put_bits(buf, B.gcli_pos + 4 * x, v, 4);
+            } else {
+                const bool skip = B.meth && sflag[B.s0 + (x >> 3)];
+                if (!skip) {
+                    /* unary code: (v - t) ones then a zero (PackPrecinct.h:25-39) */
+                    const uint32_t n = v > t ? v - t : 0;
+                    put_bits(buf, B.gcli_pos + (ev - B.vlc_pref), ((1u << n) - 1) << 1, n + 1);
+                    ev += n + 1;
+                }
+            }
+            if (v > t) {
+                /* data: sign nibble then bit-planes v-1 .. t, coefficient 0 in
+                 * the most significant bit (pack_data_c, PackPrecinct.c:128-198) */
+                const uint16_t* crow = coef + bd.coef_off + (uint64_t)B.row * bd.pitch + 4 * x;
+                const uint2 raw4 = *(const uint2*)crow;
+                uint32_t c[4] = {raw4.x & 0xffffu, raw4.x >> 16, raw4.y & 0xffffu, raw4.y >> 16};
+                uint32_t signs = 0;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    c[k] = (4 * x + k < B.w) ? quantize(c[k], v, t, uniform) : 0u;
+                    signs = (signs << 1) | (c[k] >> 15);
+                }
+                uint64_t code = signs;
+                for (int bit = (int)v - 1; bit >= (int)t; bit--) {
+                    const uint32_t nib = (((c[0] >> bit) & 1u) << 3) | (((c[1] >> bit) & 1u) << 2) | (((c[2] >> bit) & 1u) << 1) |
+                                         ((c[3] >> bit) & 1u);
+                    code = (code << 4) | nib;
+                }
+                const uint32_t nbits = 4 * (v - t + 1);
+                put_bits64(buf, B.data_pos + (ed - B.data_pref), code, nbits);
+                ed += nbits;
+            }
+        }
+    }
+    __syncthreads();
+    if (pk_overflow) {
+        if (threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        return;
+    }
+    /* copy out; slice header, codestream header and EOC around it */
+    const uint8_t* bytes = (const uint8_t*)buf;
+    uint8_t* dst = out + R.offset;
+    for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) dst[i] = bytes[i];
+    if (threadIdx.x == 0) {
+        if (R.first_in_slice) {
+            const uint32_t s = p / cfg->pps;
+            uint8_t* sh = dst - 6;
+            sh[0] = 0xff; sh[1] = 0x20; sh[2] = 0; sh[3] = 4;
+            sh[4] = (uint8_t)(s >> 8); sh[5] = (uint8_t)s;
+        }
+        if (p + 1 == (int)cfg->np) {
+            dst[total] = 0xff;
+            dst[total + 1] = 0x11;
+        }
+    }
+    if (p == 0)
+        for (uint32_t i = threadIdx.x; i < cfg->hdr_len; i += blockDim.x) out[i] = cfg->hdr[i];
+}
+
+/* ------------------------------------------------------------------------ */
+/* host-side launchers                                                       */
+/* ------------------------------------------------------------------------ */
+extern "C" cudaError_t jxs_launch_fwd_dwt(const DwtLaunch* L, int vert, int nblocks, size_t smem, const jxs_band_t* bands,
+                                          uint16_t* coef, uint8_t* gcli, cudaStream_t st) {
+    static size_t configured[2] = {0, 0};
+    if (smem > configured[vert]) {
+        cudaError_t e = vert ? cudaFuncSetAttribute(fwd_dwt_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                             : cudaFuncSetAttribute(fwd_dwt_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured[vert] = smem;
+    }
+    if (vert) fwd_dwt_kernel<true><<<nblocks, 512, smem, st>>>(*L, bands, coef, gcli);
+    else fwd_dwt_kernel<false><<<nblocks, 512, smem, st>>>(*L, bands, coef, gcli);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
+                                     PrecRC* rc, int* status, cudaStream_t st) {
+    rc_cost_kernel<<<np, 256, 0, st>>>(dcfg, gcli, cost);
+    rc_select_kernel<<<nslices, 128, 0, st>>>(dcfg, cost, rc, status);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
+                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, uint32_t sig_cap, int* status,
+                                       cudaStream_t st) {
+    size_t smem = (size_t)cap_words * 4 + sig_cap;
+    static size_t configured = 0;
+    if (smem > configured) {
+        cudaError_t e = cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    pack_kernel<<<np, PK_THREADS, smem, st>>>(dcfg, coef, gcli, rc, out, cap_words, sig_cap, status);
+    return cudaGetLastError();
+}

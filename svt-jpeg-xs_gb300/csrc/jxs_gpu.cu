@@ -1,0 +1,722 @@
+/*
+ * Launch orchestration: per-slot device buffers, streams and the kernel
+ * sequences of one encode or decode.
+ *
+ * Encode of one frame on a slot's stream:
+ *   [H2D planes] -> fwd_dwt (one launch per vertical level, all components)
+ *   -> rc_cost -> rc_select -> pack -> [D2H codestream] -> D2H status
+ * Decode:
+ *   [H2D codestream] + H2D precinct offsets -> unpack
+ *   -> inv_dwt (one launch per vertical level, deepest first; the first
+ *   level writes the output samples) -> [D2H planes] -> D2H status
+ */
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "SvtJpegxs.h"
+#include "jxs_gpu.h"
+#include "jxs_kernels.cuh"
+
+extern "C" cudaError_t jxs_launch_fwd_dwt(const DwtLaunch* L, int vert, int nblocks, size_t smem, const jxs_band_t* bands,
+                                          uint16_t* coef, uint8_t* gcli, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
+                                     PrecRC* rc, int* status, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
+                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, uint32_t sig_cap, int* status,
+                                       cudaStream_t st);
+extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, const uint32_t* prec_off, int16_t* coef,
+                                         uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_inv_dwt(const DwtLaunch* L, int vert, int nblocks, size_t smem, const jxs_band_t* bands,
+                                          const int16_t* coef, int fq, int bw, int depth, cudaStream_t st);
+
+#define CK(x)                                                                                      \
+    do {                                                                                           \
+        cudaError_t e_ = (x);                                                                      \
+        if (e_ != cudaSuccess) {                                                                   \
+            fprintf(stderr, "jxs: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return JXS_E_RESOURCES;                                                                \
+        }                                                                                          \
+    } while (0)
+
+static const size_t kLevelSmemTarget = 64 * 1024;
+static const size_t kInvSmemTarget = 100 * 1024;
+static const size_t kSmemMax = 220 * 1024;
+
+extern "C" int jxs_gpu_is_device_ptr(const void* p) {
+    if (!p) return 0;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+extern "C" void* jxs_gpu_host_alloc(size_t n) {
+    void* p = NULL;
+    if (cudaMallocHost(&p, n) != cudaSuccess) {
+        cudaGetLastError();
+        return malloc(n);
+    }
+    return p;
+}
+
+extern "C" void jxs_gpu_host_free(void* p) {
+    if (!p) return;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) == cudaSuccess && a.type == cudaMemoryTypeHost) {
+        cudaFreeHost(p);
+    } else {
+        cudaGetLastError();
+        free(p);
+    }
+}
+
+extern "C" int jxs_gpu_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+static inline uint32_t div_up(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
+
+/* size of component c at vertical level v (region transformed by level v) */
+static void level_dims(const jxs_comp_t& cp, int v, uint32_t* w, uint32_t* h) {
+    uint32_t ww = cp.w, hh = cp.h;
+    for (int i = 0; i < v; i++) {
+        ww = (ww + 1) / 2;
+        hh = (hh + 1) / 2;
+    }
+    *w = ww;
+    *h = hh;
+}
+
+static uint32_t bytes_per_sample(const jxs_cfg_t* c) { return c->depth <= 8 ? 1 : 2; }
+
+/* address of the band table inside the device copy of the configuration */
+static const jxs_band_t* dev_bands(const jxs_cfg_t* dcfg) {
+    return (const jxs_band_t*)((const char*)dcfg + offsetof(jxs_cfg_t, band));
+}
+
+/* Fills the band indices of a job for vertical level v of component c
+ * (bands of level v: HH = nb-1-3v, LH = HH-1, HL = HH-2; then one high band
+ * per horizontal-only level and the final low band). */
+static void job_bands(const jxs_cfg_t* cfg, int c, int v, DwtJob* J) {
+    const jxs_comp_t& cp = cfg->comp[c];
+    const int b0 = cp.band0;
+    if (cp.dv == 0) {
+        J->last = 1;
+        J->nh = cp.dh;
+        for (uint32_t e = 0; e < cp.dh; e++) J->b_hf[e] = b0 + (int)cp.nb - 1 - (int)e;
+        J->b_ll = b0;
+        return;
+    }
+    const int L = (int)cp.nb - 1 - 3 * v;
+    J->b_hh = b0 + L;
+    J->b_lh = b0 + L - 1;
+    J->b_hl = b0 + L - 2;
+    J->last = (v + 1 == (int)cp.dv);
+    J->nh = J->last ? (int)(cp.dh - cp.dv) : 0;
+    for (int e = 0; e < J->nh; e++) J->b_hf[e] = b0 + L - 3 - e;
+    J->b_ll = b0 + L - 3 - J->nh;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Encoder                                                                   */
+/* ------------------------------------------------------------------------ */
+struct EncSlot {
+    cudaStream_t st;
+    cudaEvent_t done;
+    uint8_t* in_stage;      /* staging for host planes */
+    uint64_t in_off[JXS_MAXC];
+    uint16_t* coef;
+    uint8_t* gcli;
+    int32_t* ll[JXS_MAXC];
+    uint32_t* cost;
+    PrecRC* rc;
+    int* status;
+    uint8_t* out_stage;
+    int* status_h;
+    int busy;
+    cudaEvent_t tev[6];
+    int timed;
+};
+
+/* encoder stages timed with CUDA events: H2D, transform, rate control, packing, D2H */
+#define ENC_STAGES 5
+
+struct jxs_gpu_enc {
+    jxs_cfg_t cfg;
+    jxs_cfg_t* dcfg;
+    int nslots;
+    EncSlot slot[8];
+    uint32_t cap_words, sig_cap;
+    cudaStream_t user_stream;
+    int timing;
+    double stage_ms[ENC_STAGES];
+    uint64_t timed_frames;
+    std::mutex mu;
+};
+
+static inline cudaStream_t enc_stream(const jxs_gpu_enc_t* e, const EncSlot* s) { return e->user_stream ? e->user_stream : s->st; }
+
+static int32_t enc_slot_alloc(jxs_gpu_enc_t* e, EncSlot* s) {
+    const jxs_cfg_t* c = &e->cfg;
+    memset(s, 0, sizeof(*s));
+    CK(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
+    uint64_t in_bytes = 0;
+    const uint32_t bps = bytes_per_sample(c);
+    if (c->fmt == COLOUR_FORMAT_PACKED_YUV444_OR_RGB) {
+        s->in_off[0] = 0;
+        in_bytes = (uint64_t)c->W * c->H * 3 * bps;
+    } else {
+        for (uint32_t k = 0; k < c->nc; k++) {
+            s->in_off[k] = in_bytes;
+            in_bytes += ((uint64_t)c->comp[k].w * c->comp[k].h * bps + 255) & ~255ull;
+        }
+    }
+    CK(cudaMalloc(&s->in_stage, in_bytes));
+    CK(cudaMalloc(&s->coef, c->coef_total * sizeof(uint16_t) + 64));
+    CK(cudaMalloc(&s->gcli, c->gcli_total + 64));
+    for (uint32_t k = 0; k < c->nc; k++) {
+        if (c->comp[k].dv == 2) {
+            uint32_t w, h;
+            level_dims(c->comp[k], 1, &w, &h);
+            CK(cudaMalloc(&s->ll[k], (size_t)w * h * sizeof(int32_t)));
+        }
+    }
+    CK(cudaMalloc(&s->cost, (size_t)c->np * 1024 * sizeof(uint32_t)));
+    CK(cudaMalloc(&s->rc, (size_t)c->np * sizeof(PrecRC)));
+    CK(cudaMalloc(&s->status, 64));
+    CK(cudaMalloc(&s->out_stage, c->lcod + 64));
+    CK(cudaMallocHost(&s->status_h, 64));
+    *s->status_h = 0;
+    for (int i = 0; i < 6; i++) CK(cudaEventCreate(&s->tev[i]));
+    return JXS_OK;
+}
+
+static void enc_slot_free(EncSlot* s) {
+    if (s->st) cudaStreamSynchronize(s->st);
+    cudaFree(s->in_stage);
+    cudaFree(s->coef);
+    cudaFree(s->gcli);
+    for (int k = 0; k < JXS_MAXC; k++) cudaFree(s->ll[k]);
+    cudaFree(s->cost);
+    cudaFree(s->rc);
+    cudaFree(s->status);
+    cudaFree(s->out_stage);
+    if (s->status_h) cudaFreeHost(s->status_h);
+    for (int i = 0; i < 6; i++)
+        if (s->tev[i]) cudaEventDestroy(s->tev[i]);
+    if (s->done) cudaEventDestroy(s->done);
+    if (s->st) cudaStreamDestroy(s->st);
+    memset(s, 0, sizeof(*s));
+}
+
+extern "C" void jxs_gpu_enc_destroy(jxs_gpu_enc_t* e) {
+    if (!e) return;
+    for (int i = 0; i < e->nslots; i++) enc_slot_free(&e->slot[i]);
+    cudaFree(e->dcfg);
+    delete e;
+}
+
+extern "C" jxs_gpu_enc_t* jxs_gpu_enc_create(const jxs_cfg_t* cfg, int nslots, int32_t* err) {
+    *err = JXS_OK;
+    if (jxs_gpu_device_count() == 0) {
+        fprintf(stderr, "jxs: no CUDA device available; this library has no CPU fallback\n");
+        *err = JXS_E_RESOURCES;
+        return NULL;
+    }
+    if (nslots < 1) nslots = 1;
+    if (nslots > 8) nslots = 8;
+    jxs_gpu_enc_t* e = new jxs_gpu_enc_t();
+    memset(&e->slot, 0, sizeof(e->slot));
+    e->cfg = *cfg;
+    e->nslots = 0;
+    /* the packing kernel stages a whole precinct in shared memory: bound it by
+     * the largest slice budget and the significance groups of one precinct */
+    uint32_t sig = 0;
+    for (uint32_t b = 0; b < cfg->nbands; b++) sig += cfg->band[b].sig_w * cfg->band[b].lines;
+    e->sig_cap = (sig + 16) & ~15u;
+    e->cap_words = div_up(cfg->max_slice_budget, 4) + 4;
+    if ((size_t)e->cap_words * 4 + e->sig_cap > kSmemMax) {
+        fprintf(stderr, "jxs: precincts of this configuration (%u bytes per slice) exceed the on-chip packing buffer\n",
+                cfg->max_slice_budget);
+        delete e;
+        *err = JXS_E_BAD_PARAM;
+        return NULL;
+    }
+    if (cudaMalloc(&e->dcfg, sizeof(jxs_cfg_t)) != cudaSuccess ||
+        cudaMemcpy(e->dcfg, cfg, sizeof(jxs_cfg_t), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        delete e;
+        *err = JXS_E_RESOURCES;
+        return NULL;
+    }
+    for (int i = 0; i < nslots; i++) {
+        if (enc_slot_alloc(e, &e->slot[i]) != JXS_OK) {
+            e->nslots = i + 1;
+            jxs_gpu_enc_destroy(e);
+            *err = JXS_E_RESOURCES;
+            return NULL;
+        }
+    }
+    e->nslots = nslots;
+    return e;
+}
+
+static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], const uint32_t strides[4], uint8_t* out) {
+    const jxs_cfg_t* c = &e->cfg;
+    const int packed = c->fmt == COLOUR_FORMAT_PACKED_YUV444_OR_RGB;
+    const uint32_t bps = bytes_per_sample(c);
+    const cudaStream_t st = enc_stream(e, s);
+    s->timed = e->timing;
+#define TMARK(i) \
+    if (s->timed) CK(cudaEventRecord(s->tev[i], st))
+    TMARK(0);
+    CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
+    /* sources of the first level: caller device planes read in place, host
+     * planes staged with one 2-D copy each */
+    const void* src[JXS_MAXC];
+    long long pitch[JXS_MAXC];
+    const int nplanes = packed ? 1 : (int)c->nc;
+    for (int k = 0; k < nplanes; k++) {
+        const uint32_t w = packed ? c->W * 3 : c->comp[k].w, h = packed ? c->H : c->comp[k].h;
+        if (jxs_gpu_is_device_ptr(planes[k])) {
+            src[k] = planes[k];
+            pitch[k] = strides[k];
+        } else {
+            uint8_t* d = s->in_stage + s->in_off[k];
+            CK(cudaMemcpy2DAsync(d, (size_t)w * bps, planes[k], (size_t)strides[k] * bps, (size_t)w * bps, h,
+                                 cudaMemcpyHostToDevice, st));
+            src[k] = d;
+            pitch[k] = w;
+        }
+    }
+    TMARK(1);
+    /* forward transform: one launch per vertical level index */
+    uint32_t max_dv = 0;
+    for (uint32_t k = 0; k < c->nc; k++) max_dv = c->comp[k].dv > max_dv ? c->comp[k].dv : max_dv;
+    for (int pass = 0; pass <= (int)max_dv; pass++) {
+        /* pass max_dv handles components without vertical levels */
+        const int vert = pass < (int)max_dv;
+        DwtLaunch L;
+        memset(&L, 0, sizeof(L));
+        int blocks = 0;
+        size_t smem = 0;
+        for (uint32_t k = 0; k < c->nc; k++) {
+            const jxs_comp_t& cp = c->comp[k];
+            if (vert ? (int)cp.dv <= pass : cp.dv != 0) continue;
+            const int v = vert ? pass : 0;
+            DwtJob& J = L.job[L.njobs++];
+            J.comp = (int)k;
+            uint32_t w, h;
+            level_dims(cp, v, &w, &h);
+            J.w = (int)w;
+            J.h = (int)h;
+            J.smem_pitch = (int)w;
+            job_bands(c, (int)k, v, &J);
+            if (v == 0) {
+                J.src = src[packed ? 0 : k];
+                J.src_pitch = pitch[packed ? 0 : k];
+                J.src_kind = packed ? (bps == 1 ? SRC_PK8 : SRC_PK16) : (bps == 1 ? SRC_U8 : SRC_U16);
+                J.chan = packed ? (int)k : 0;
+            } else {
+                J.src = s->ll[k];
+                J.src_pitch = (long long)((cp.w + 1) / 2);
+                J.src_kind = SRC_I32;
+            }
+            J.depth = (int)c->depth;
+            if (vert && !J.last) {
+                J.ll = s->ll[k];
+                J.ll_pitch = (int)((w + 1) / 2);
+            }
+            const size_t row_bytes = (size_t)w * 4;
+            int R = (int)(kLevelSmemTarget / ((vert ? 2 : 1) * row_bytes));
+            if (R < 1) R = 1;
+            const uint32_t units = vert ? (h + 1) / 2 : h;
+            if ((uint32_t)R > units) R = (int)units;
+            J.R = R;
+            J.first_block = blocks;
+            J.nblocks = (int)div_up(units, (uint32_t)R);
+            blocks += J.nblocks;
+            const size_t need = (size_t)(vert ? 2 : 1) * R * row_bytes;
+            smem = need > smem ? need : smem;
+        }
+        if (!L.njobs) continue;
+        if (smem > kSmemMax) return JXS_E_BAD_PARAM;
+        CK(jxs_launch_fwd_dwt(&L, vert, blocks, smem, dev_bands(e->dcfg), s->coef, s->gcli, st));
+    }
+    TMARK(2);
+    CK(jxs_launch_rc(e->dcfg, c->np, c->nslices, s->gcli, s->cost, s->rc, s->status, st));
+    TMARK(3);
+    const int out_dev = jxs_gpu_is_device_ptr(out);
+    uint8_t* dst = out_dev ? out : s->out_stage;
+    CK(jxs_launch_pack(e->dcfg, c->np, s->coef, s->gcli, s->rc, dst, e->cap_words, e->sig_cap, s->status, st));
+    TMARK(4);
+    if (!out_dev) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TMARK(5);
+#undef TMARK
+    CK(cudaEventRecord(s->done, st));
+    return JXS_OK;
+}
+
+extern "C" int32_t jxs_gpu_enc_submit(jxs_gpu_enc_t* e, int slot, void* const planes[4], const uint32_t strides[4], uint8_t* out) {
+    if (!e || slot < 0 || slot >= e->nslots) return JXS_E_BAD_PARAM;
+    EncSlot* s = &e->slot[slot];
+    s->busy = 1;
+    return enc_run(e, s, planes, strides, out);
+}
+
+extern "C" int32_t jxs_gpu_enc_wait(jxs_gpu_enc_t* e, int slot) {
+    EncSlot* s = &e->slot[slot];
+    if (cudaEventSynchronize(s->done) != cudaSuccess) {
+        fprintf(stderr, "jxs: encode failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+        return JXS_E_ENC_FRAME;
+    }
+    s->busy = 0;
+    if (s->timed) {
+        float ms[ENC_STAGES];
+        for (int i = 0; i < ENC_STAGES; i++)
+            if (cudaEventElapsedTime(&ms[i], s->tev[i], s->tev[i + 1]) != cudaSuccess) ms[i] = 0.f;
+        std::lock_guard<std::mutex> g(e->mu);
+        for (int i = 0; i < ENC_STAGES; i++) e->stage_ms[i] += ms[i];
+        e->timed_frames++;
+        s->timed = 0;
+    }
+    return *s->status_h ? JXS_E_ENC_FRAME : JXS_OK;
+}
+
+extern "C" void jxs_gpu_enc_set_stream(jxs_gpu_enc_t* e, void* stream) { e->user_stream = (cudaStream_t)stream; }
+
+extern "C" void jxs_gpu_enc_set_timing(jxs_gpu_enc_t* e, int on) {
+    std::lock_guard<std::mutex> g(e->mu);
+    e->timing = on;
+    for (int i = 0; i < ENC_STAGES; i++) e->stage_ms[i] = 0;
+    e->timed_frames = 0;
+}
+
+extern "C" uint64_t jxs_gpu_enc_read_timing(jxs_gpu_enc_t* e, double* ms, int n) {
+    std::lock_guard<std::mutex> g(e->mu);
+    for (int i = 0; i < n && i < ENC_STAGES; i++) ms[i] = e->stage_ms[i];
+    return e->timed_frames;
+}
+
+extern "C" int jxs_gpu_enc_ready(jxs_gpu_enc_t* e, int slot) {
+    cudaError_t r = cudaEventQuery(e->slot[slot].done);
+    if (r == cudaErrorNotReady) return 0;
+    return 1;
+}
+
+extern "C" int32_t jxs_gpu_enc_rc_results(jxs_gpu_enc_t* e, int slot, uint8_t* q, uint8_t* r) {
+    EncSlot* s = &e->slot[slot];
+    const uint32_t np = e->cfg.np;
+    PrecRC* h = (PrecRC*)malloc(sizeof(PrecRC) * np);
+    if (!h) return JXS_E_RESOURCES;
+    cudaStreamSynchronize(enc_stream(e, s));
+    if (cudaMemcpy(h, s->rc, sizeof(PrecRC) * np, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        free(h);
+        return JXS_E_RESOURCES;
+    }
+    for (uint32_t i = 0; i < np; i++) {
+        q[i] = h[i].q;
+        r[i] = h[i].r;
+    }
+    free(h);
+    return JXS_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Decoder                                                                   */
+/* ------------------------------------------------------------------------ */
+struct DecSlot {
+    cudaStream_t st;
+    cudaEvent_t done;
+    uint8_t* bs;
+    uint32_t bs_cap;
+    uint32_t* prec_off;
+    int16_t* coef;
+    int32_t* ll[JXS_MAXC];
+    uint8_t* out_stage;
+    uint64_t out_off[JXS_MAXC];
+    int* status;
+    int* status_h;
+    uint32_t* prec_off_h;
+    cudaEvent_t tev[5];
+    int timed;
+};
+
+/* decoder stages timed with CUDA events: H2D, unpack, inverse transform, D2H */
+#define DEC_STAGES 4
+
+struct jxs_gpu_dec {
+    jxs_cfg_t cfg;
+    jxs_cfg_t* dcfg;
+    int nslots;
+    DecSlot slot[8];
+    uint32_t cap_bytes, cap_groups;
+    cudaStream_t user_stream;
+    int timing;
+    double stage_ms[DEC_STAGES];
+    uint64_t timed_frames;
+    std::mutex mu;
+};
+
+static inline cudaStream_t dec_stream(const jxs_gpu_dec_t* d, const DecSlot* s) { return d->user_stream ? d->user_stream : s->st; }
+
+static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
+    const jxs_cfg_t* c = &d->cfg;
+    memset(s, 0, sizeof(*s));
+    CK(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
+    s->bs_cap = c->lcod + 4096;
+    CK(cudaMalloc(&s->bs, s->bs_cap + 64));
+    CK(cudaMalloc(&s->prec_off, (size_t)c->np * sizeof(uint32_t)));
+    CK(cudaMallocHost(&s->prec_off_h, (size_t)c->np * sizeof(uint32_t)));
+    CK(cudaMalloc(&s->coef, c->coef_total * sizeof(int16_t) + 64));
+    for (uint32_t k = 0; k < c->nc; k++) {
+        if (c->comp[k].dv == 2) {
+            uint32_t w, h;
+            level_dims(c->comp[k], 1, &w, &h);
+            CK(cudaMalloc(&s->ll[k], (size_t)w * h * sizeof(int32_t)));
+        }
+    }
+    uint64_t ob = 0;
+    const uint32_t bps = bytes_per_sample(c);
+    for (uint32_t k = 0; k < c->nc; k++) {
+        s->out_off[k] = ob;
+        ob += ((uint64_t)c->comp[k].w * c->comp[k].h * bps + 255) & ~255ull;
+    }
+    CK(cudaMalloc(&s->out_stage, ob));
+    CK(cudaMalloc(&s->status, 64));
+    CK(cudaMallocHost(&s->status_h, 64));
+    *s->status_h = 0;
+    for (int i = 0; i < 5; i++) CK(cudaEventCreate(&s->tev[i]));
+    return JXS_OK;
+}
+
+static void dec_slot_free(DecSlot* s) {
+    if (s->st) cudaStreamSynchronize(s->st);
+    cudaFree(s->bs);
+    cudaFree(s->prec_off);
+    if (s->prec_off_h) cudaFreeHost(s->prec_off_h);
+    cudaFree(s->coef);
+    for (int k = 0; k < JXS_MAXC; k++) cudaFree(s->ll[k]);
+    cudaFree(s->out_stage);
+    cudaFree(s->status);
+    if (s->status_h) cudaFreeHost(s->status_h);
+    for (int i = 0; i < 5; i++)
+        if (s->tev[i]) cudaEventDestroy(s->tev[i]);
+    if (s->done) cudaEventDestroy(s->done);
+    if (s->st) cudaStreamDestroy(s->st);
+    memset(s, 0, sizeof(*s));
+}
+
+extern "C" void jxs_gpu_dec_destroy(jxs_gpu_dec_t* d) {
+    if (!d) return;
+    for (int i = 0; i < d->nslots; i++) dec_slot_free(&d->slot[i]);
+    cudaFree(d->dcfg);
+    delete d;
+}
+
+extern "C" jxs_gpu_dec_t* jxs_gpu_dec_create(const jxs_cfg_t* cfg, int nslots, int32_t* err) {
+    *err = JXS_OK;
+    if (jxs_gpu_device_count() == 0) {
+        fprintf(stderr, "jxs: no CUDA device available; this library has no CPU fallback\n");
+        *err = JXS_E_RESOURCES;
+        return NULL;
+    }
+    if (nslots < 1) nslots = 1;
+    if (nslots > 8) nslots = 8;
+    jxs_gpu_dec_t* d = new jxs_gpu_dec_t();
+    memset(&d->slot, 0, sizeof(d->slot));
+    d->cfg = *cfg;
+    uint32_t groups = 0;
+    for (uint32_t b = 0; b < cfg->nbands; b++) groups += cfg->band[b].gcli_w * cfg->band[b].lines;
+    d->cap_groups = (groups + 64) & ~31u;
+    /* the on-chip copy of a precinct: constant-bit-rate streams give every
+     * slice its share of Lcod, so a precinct fits in a slice's share with
+     * margin; whatever does not fit is reported as an invalid stream */
+    const size_t fixed = (size_t)d->cap_groups * 6 + 64;
+    uint64_t cap = (uint64_t)cfg->lcod / (cfg->nslices ? cfg->nslices : 1);
+    cap = cap + cap / 4 + 4096;
+    if (cap > cfg->lcod + 64ull) cap = cfg->lcod + 64ull;
+    if (cap + fixed > kSmemMax) cap = kSmemMax > fixed + 4096 ? kSmemMax - fixed : 4096;
+    d->cap_bytes = (uint32_t)cap & ~15u;
+    if (cudaMalloc(&d->dcfg, sizeof(jxs_cfg_t)) != cudaSuccess ||
+        cudaMemcpy(d->dcfg, cfg, sizeof(jxs_cfg_t), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        delete d;
+        *err = JXS_E_RESOURCES;
+        return NULL;
+    }
+    for (int i = 0; i < nslots; i++) {
+        if (dec_slot_alloc(d, &d->slot[i]) != JXS_OK) {
+            d->nslots = i + 1;
+            jxs_gpu_dec_destroy(d);
+            *err = JXS_E_RESOURCES;
+            return NULL;
+        }
+    }
+    d->nslots = nslots;
+    return d;
+}
+
+static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t size, const uint32_t* prec_off,
+                       void* const planes[4], const uint32_t strides[4]) {
+    const jxs_cfg_t* c = &d->cfg;
+    const uint32_t bps = bytes_per_sample(c);
+    const cudaStream_t st = dec_stream(d, s);
+    s->timed = d->timing;
+#define TMARK(i) \
+    if (s->timed) CK(cudaEventRecord(s->tev[i], st))
+    TMARK(0);
+    CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
+    const uint8_t* dbs = bs;
+    if (!jxs_gpu_is_device_ptr(bs)) {
+        if (size > s->bs_cap) {
+            CK(cudaStreamSynchronize(st));
+            cudaFree(s->bs);
+            s->bs_cap = size + 4096;
+            CK(cudaMalloc(&s->bs, s->bs_cap + 64));
+        }
+        CK(cudaMemcpyAsync(s->bs, bs, size, cudaMemcpyHostToDevice, st));
+        dbs = s->bs;
+    }
+    /* the previous use of prec_off_h by this slot has completed: slots are
+     * reused only after their completion was observed */
+    memcpy(s->prec_off_h, prec_off, sizeof(uint32_t) * c->np);
+    CK(cudaMemcpyAsync(s->prec_off, s->prec_off_h, sizeof(uint32_t) * c->np, cudaMemcpyHostToDevice, st));
+    TMARK(1);
+    CK(jxs_launch_unpack(d->dcfg, dbs, s->prec_off, s->coef, c->np, d->cap_bytes, d->cap_groups, s->status, st));
+    TMARK(2);
+
+    int out_dev[JXS_MAXC];
+    for (uint32_t k = 0; k < c->nc; k++) out_dev[k] = jxs_gpu_is_device_ptr(planes[k]);
+    uint32_t max_dv = 0;
+    for (uint32_t k = 0; k < c->nc; k++) max_dv = c->comp[k].dv > max_dv ? c->comp[k].dv : max_dv;
+    /* deepest vertical level first; the components without vertical levels last */
+    for (int pass = (int)max_dv - 1; pass >= -1; pass--) {
+        const int vert = pass >= 0;
+        DwtLaunch L;
+        memset(&L, 0, sizeof(L));
+        int blocks = 0;
+        size_t smem = 0;
+        for (uint32_t k = 0; k < c->nc; k++) {
+            const jxs_comp_t& cp = c->comp[k];
+            if (vert ? (int)cp.dv <= pass : cp.dv != 0) continue;
+            const int v = vert ? pass : 0;
+            DwtJob& J = L.job[L.njobs++];
+            J.comp = (int)k;
+            uint32_t w, h;
+            level_dims(cp, v, &w, &h);
+            J.w = (int)w;
+            J.h = (int)h;
+            J.smem_pitch = (int)w;
+            job_bands(c, (int)k, v, &J);
+            if (vert && !J.last) {
+                J.src = s->ll[k];
+                J.src_pitch = (long long)((cp.w + 1) / 2);
+            }
+            if (v == 0) {
+                J.out_kind = bps == 1 ? 1 : 2;
+                if (out_dev[k]) {
+                    J.dst = planes[k];
+                    J.dst_pitch = strides[k];
+                } else {
+                    J.dst = s->out_stage + s->out_off[k];
+                    J.dst_pitch = cp.w;
+                }
+            } else {
+                J.out_kind = 0;
+                J.ll = s->ll[k];
+                J.ll_pitch = (int)w;
+            }
+            const size_t row_bytes = (size_t)w * 4;
+            int R;
+            if (vert) {
+                R = (int)((kInvSmemTarget / row_bytes - 3) / 2);
+                if (kInvSmemTarget / row_bytes < 5) R = 1;
+            } else {
+                R = (int)(kLevelSmemTarget / row_bytes);
+            }
+            if (R < 1) R = 1;
+            const uint32_t units = vert ? (h + 1) / 2 : h;
+            if ((uint32_t)R > units) R = (int)units;
+            J.R = R;
+            J.first_block = blocks;
+            J.nblocks = (int)div_up(units, (uint32_t)R);
+            blocks += J.nblocks;
+            const size_t need = vert ? (size_t)(2 * R + 3) * row_bytes : (size_t)R * row_bytes;
+            smem = need > smem ? need : smem;
+        }
+        if (!L.njobs) continue;
+        if (smem > kSmemMax) return JXS_E_BAD_PARAM;
+        CK(jxs_launch_inv_dwt(&L, vert, blocks, smem, dev_bands(d->dcfg), s->coef, (int)c->fq, (int)c->bw, (int)c->depth, st));
+    }
+    TMARK(3);
+    for (uint32_t k = 0; k < c->nc; k++) {
+        if (out_dev[k]) continue;
+        const jxs_comp_t& cp = c->comp[k];
+        CK(cudaMemcpy2DAsync(planes[k], (size_t)strides[k] * bps, s->out_stage + s->out_off[k], (size_t)cp.w * bps,
+                             (size_t)cp.w * bps, cp.h, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TMARK(4);
+#undef TMARK
+    CK(cudaEventRecord(s->done, st));
+    return JXS_OK;
+}
+
+extern "C" int32_t jxs_gpu_dec_submit(jxs_gpu_dec_t* d, int slot, const uint8_t* bs, uint32_t size, const uint32_t* prec_off,
+                                      void* const planes[4], const uint32_t strides[4]) {
+    if (!d || slot < 0 || slot >= d->nslots) return JXS_E_BAD_PARAM;
+    return dec_run(d, &d->slot[slot], bs, size, prec_off, planes, strides);
+}
+
+extern "C" int32_t jxs_gpu_dec_wait(jxs_gpu_dec_t* d, int slot) {
+    DecSlot* s = &d->slot[slot];
+    if (cudaEventSynchronize(s->done) != cudaSuccess) {
+        fprintf(stderr, "jxs: decode failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+        return JXS_E_DEC_INTERNAL;
+    }
+    if (s->timed) {
+        float ms[DEC_STAGES];
+        for (int i = 0; i < DEC_STAGES; i++)
+            if (cudaEventElapsedTime(&ms[i], s->tev[i], s->tev[i + 1]) != cudaSuccess) ms[i] = 0.f;
+        std::lock_guard<std::mutex> g(d->mu);
+        for (int i = 0; i < DEC_STAGES; i++) d->stage_ms[i] += ms[i];
+        d->timed_frames++;
+        s->timed = 0;
+    }
+    return *s->status_h;
+}
+
+extern "C" void jxs_gpu_dec_set_stream(jxs_gpu_dec_t* d, void* stream) { d->user_stream = (cudaStream_t)stream; }
+
+extern "C" void jxs_gpu_dec_set_timing(jxs_gpu_dec_t* d, int on) {
+    std::lock_guard<std::mutex> g(d->mu);
+    d->timing = on;
+    for (int i = 0; i < DEC_STAGES; i++) d->stage_ms[i] = 0;
+    d->timed_frames = 0;
+}
+
+extern "C" uint64_t jxs_gpu_dec_read_timing(jxs_gpu_dec_t* d, double* ms, int n) {
+    std::lock_guard<std::mutex> g(d->mu);
+    for (int i = 0; i < n && i < DEC_STAGES; i++) ms[i] = d->stage_ms[i];
+    return d->timed_frames;
+}
+
+extern "C" int jxs_gpu_dec_ready(jxs_gpu_dec_t* d, int slot) {
+    cudaError_t r = cudaEventQuery(d->slot[slot].done);
+    return r == cudaErrorNotReady ? 0 : 1;
+}

@@ -1,0 +1,69 @@
+/*
+ * Thin C-ABI between the host C library and the CUDA code.
+ *
+ * An encoder or decoder owns `nslots` independent frame slots; each slot has
+ * its own device buffers and CUDA stream, so up to `nslots` frames are in
+ * flight at once (host-to-device copy of one frame overlaps the kernels of
+ * another).  Planes and bitstreams passed in may be host or device pointers.
+ */
+#ifndef JXS_GPU_H
+#define JXS_GPU_H
+
+#include <stdint.h>
+
+#include "jxs_core.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct jxs_gpu_enc jxs_gpu_enc_t;
+typedef struct jxs_gpu_dec jxs_gpu_dec_t;
+
+/* Encoder ---------------------------------------------------------------- */
+jxs_gpu_enc_t* jxs_gpu_enc_create(const jxs_cfg_t* cfg, int nslots, int32_t* err);
+void jxs_gpu_enc_destroy(jxs_gpu_enc_t* e);
+/* Queues the encode of one frame on `slot`.  `out` receives cfg->lcod bytes. */
+int32_t jxs_gpu_enc_submit(jxs_gpu_enc_t* e, int slot, void* const planes[4], const uint32_t strides[4], uint8_t* out);
+/* Blocks until the slot's frame is done; returns its status (0 or an error code). */
+int32_t jxs_gpu_enc_wait(jxs_gpu_enc_t* e, int slot);
+/* 1 when the slot's frame is done, 0 while it is in flight. */
+int jxs_gpu_enc_ready(jxs_gpu_enc_t* e, int slot);
+/* Per-precinct quantization/refinement of the slot's last frame (host copies). */
+int32_t jxs_gpu_enc_rc_results(jxs_gpu_enc_t* e, int slot, uint8_t* q, uint8_t* r);
+
+/* Decoder ---------------------------------------------------------------- */
+jxs_gpu_dec_t* jxs_gpu_dec_create(const jxs_cfg_t* cfg, int nslots, int32_t* err);
+void jxs_gpu_dec_destroy(jxs_gpu_dec_t* d);
+/* Queues the decode of one frame whose precincts start at prec_off (host
+ * array, cfg->np entries, from jxs_frame_bytes_walk). */
+int32_t jxs_gpu_dec_submit(jxs_gpu_dec_t* d, int slot, const uint8_t* bs, uint32_t size, const uint32_t* prec_off,
+                           void* const planes[4], const uint32_t strides[4]);
+int32_t jxs_gpu_dec_wait(jxs_gpu_dec_t* d, int slot);
+int jxs_gpu_dec_ready(jxs_gpu_dec_t* d, int slot);
+
+/* Binds all work of the handle to a caller stream (cudaStream_t); NULL
+ * returns to the per-slot streams. */
+void jxs_gpu_enc_set_stream(jxs_gpu_enc_t* e, void* stream);
+void jxs_gpu_dec_set_stream(jxs_gpu_dec_t* d, void* stream);
+/* Stage timing with CUDA events on the launching stream.  Encoder stages:
+ * H2D, transform, rate control, packing, D2H.  Decoder stages: H2D, unpack,
+ * inverse transform, D2H.  read returns the frames timed since enabling. */
+void jxs_gpu_enc_set_timing(jxs_gpu_enc_t* e, int on);
+uint64_t jxs_gpu_enc_read_timing(jxs_gpu_enc_t* e, double* ms, int n);
+void jxs_gpu_dec_set_timing(jxs_gpu_dec_t* d, int on);
+uint64_t jxs_gpu_dec_read_timing(jxs_gpu_dec_t* d, double* ms, int n);
+
+/* 1 if p is memory of this process's current CUDA device. */
+int jxs_gpu_is_device_ptr(const void* p);
+/* Page-locked host allocation (falls back to malloc without a GPU). */
+void* jxs_gpu_host_alloc(size_t n);
+void jxs_gpu_host_free(void* p);
+/* Number of GPUs visible (0 when none). */
+int jxs_gpu_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

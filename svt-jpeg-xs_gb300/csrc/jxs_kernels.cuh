@@ -1,0 +1,61 @@
+/*
+ * Launch descriptors shared by the kernels (jxs_enc_kernels.cu,
+ * jxs_dec_kernels.cu) and the launcher (jxs_gpu.cu).
+ */
+#ifndef JXS_KERNELS_CUH
+#define JXS_KERNELS_CUH
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "jxs_core.h"
+
+/* Source sample formats of the first transform level. */
+enum {
+    SRC_I32 = 0,    /* int32 low-pass plane of the previous level */
+    SRC_U8 = 1,     /* planar 8-bit */
+    SRC_U16 = 2,    /* planar 9..16-bit little endian */
+    SRC_PK8 = 3,    /* packed 3 x 8-bit */
+    SRC_PK16 = 4    /* packed 3 x 16-bit */
+};
+
+/* One component's share of a transform-level launch.  Blocks
+ * [first_block, first_block + nblocks) of the grid belong to it. */
+struct DwtJob {
+    int comp;
+    int first_block, nblocks;
+    int R;              /* row pairs (vertical level) or rows (horizontal only) per block */
+    int w, h;           /* size of the region transformed at this level */
+    int last;           /* last vertical level: continue with the horizontal-only levels */
+    int nh;             /* horizontal-only levels run after this one */
+    int src_kind, depth, chan;
+    const void* src;    /* level input (samples or int32 low band) */
+    long long src_pitch;/* elements */
+    int32_t* ll;        /* int32 low band for the next vertical level (forward) or from the deeper level (inverse) */
+    int ll_pitch;
+    int b_hl, b_lh, b_hh;   /* flat band indices produced by this vertical level */
+    int b_hf[5];            /* high band of each horizontal-only level */
+    int b_ll;               /* final low band */
+    int smem_pitch;         /* int32 elements per shared-memory row */
+    /* inverse only: destination plane */
+    void* dst;
+    long long dst_pitch;
+    int out_kind;           /* 0: int32 ll, 1: u8 plane, 2: u16 plane */
+};
+
+struct DwtLaunch {
+    int njobs;
+    DwtJob job[JXS_MAXC];
+};
+
+/* Encoder rate-control outputs per precinct row. */
+struct PrecRC {
+    uint32_t total_bytes;  /* bytes written for the precinct (header to last data byte, incl. trailing padding) */
+    uint32_t offset;       /* absolute byte offset of the precinct in the codestream */
+    uint32_t data_bytes;   /* sub-packet bytes chosen by the rate control (cross-check for packing) */
+    uint8_t q, r, first_in_slice, pad;
+};
+
+#define JXS_STATUS_SET(ptr, code) atomicCAS((int*)(ptr), 0, (int)(code))
+
+#endif
