@@ -1,0 +1,404 @@
+"""Benchmark: JPEG XS encode + decode of the 3840x2160 4:2:2 10-bit stream.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--frames F]
+
+A step encodes F frames of the seeded 60-frame 4K stream (bpp 3, decomp
+V2/H5, rectangles drifting 2 px per frame) and decodes the F codestreams it
+produced.  Every codestream and decoded frame of the timed region is checked
+bit-exact against the first (warm-up) pass.
+
+value  : luma Gpixel/s of encode + decode with inputs and outputs resident in
+         device memory, timed with CUDA events on the stream the codec runs
+         on; inputs (33 MB per frame, 60 frames) exceed the 129 MB L2.
+e2e    : the same metric through the public C API with host buffers (page-
+         locked), host-to-device and device-to-host copies inside the timed
+         region, several frames in flight.
+roofline: the dominant stage (per-stage CUDA-event times) against the
+         measured HBM copy bandwidth; bytes are the algorithmic bytes of
+         that stage.
+cpu_baseline: the CPU restatement of the reference algorithm (oracle) on the
+         host cores, a bounded sample of the same workload.
+
+--impl reference times the CPU codec on all host cores instead (the
+reference library itself cannot be built on the GPU host: its sources are not
+shipped there), printing the same metric.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "svt-jpeg-xs_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+W, H, DEPTH, BPP = 3840, 2160, 10, 3
+SEQ_FRAMES = 60
+SEED = 2
+WORKLOAD = "3840x2160 YUV 4:2:2 10-bit, bpp 3, decomp V2/H5, 60-frame seeded synthetic stream"
+METRIC = "encode+decode Gpix/s (bit-exact), 3840x2160 4:2:2 10-bit bpp3"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--frames", type=int, default=8, help="frames encoded and decoded per step")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_frames(n):
+    import jxs_synth as S
+
+    return [S.frame_4k_10bit(SEED, i) for i in range(n)]
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_codec_time(frames, params_kw, seconds, threads):
+    """Encodes and decodes frames with the oracle until `seconds` elapse (at
+    least 2 frames); returns (frames done, wall seconds)."""
+    import oracle_lib as O
+
+    O.build_oracle()
+    p = O.make_params(W, H, DEPTH, 3, BPP, threads=threads, **params_kw)
+    done = 0
+    t0 = time.perf_counter()
+    while True:
+        fr = frames[done % len(frames)]
+        err, bs = O.oracle_encode(p, fr)
+        assert err == 0
+        err, _ = O.oracle_decode(bs, threads=threads)
+        assert err == 0
+        done += 1
+        el = time.perf_counter() - t0
+        if done >= 2 and el >= seconds:
+            return done, el
+
+
+def run_reference(args, rank, world):
+    """CPU arm: the CPU codec on all host cores, one frame encoded and decoded
+    per step (a bounded sample of the workload); rank 0 only."""
+    if rank != 0:
+        return
+    import oracle_lib as O
+
+    O.build_oracle()
+    frames = make_frames(2)
+    threads = os.cpu_count() or 1
+    p = O.make_params(W, H, DEPTH, 3, BPP, threads=threads)
+
+    def one(i):
+        err, bs = O.oracle_encode(p, frames[i % len(frames)])
+        assert err == 0
+        err, _ = O.oracle_decode(bs, threads=threads)
+        assert err == 0
+
+    for i in range(args.warmup):
+        one(i)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        one(i)
+    el = time.perf_counter() - t0
+    gpix = args.steps * W * H / el / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": gpix, "unit": "Gpix/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded, integer-only generator; no dataset)",
+            "config": {"workload": WORKLOAD, "frames_per_step": 1, "threads": threads},
+            "cpu_baseline": {"value": gpix, "unit": "Gpix/s", "cores": threads, "kind": "port",
+                             "sample": "1 frame encoded + decoded per step on all host cores with the CPU restatement of "
+                                       "the reference algorithm (the reference sources are not present on this host)"},
+            "e2e": {"value": gpix, "unit": "Gpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    import jxs
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    frames = make_frames(SEQ_FRAMES)
+    F = args.frames
+    enc = jxs.Encoder(W, H, DEPTH, jxs.FMT_YUV422, BPP)
+    lcod = enc.frame_bytes
+    # device-resident inputs and outputs
+    d_in = [[torch.from_numpy(p).to(dev) for p in fr] for fr in frames]
+    d_bs = [torch.zeros(lcod + 64, dtype=torch.uint8, device=dev) for _ in range(F)]
+    d_out = [[torch.zeros_like(p) for p in d_in[0]] for _ in range(F)]
+    stream = torch.cuda.Stream(device=dev)
+    enc.set_stream(stream.cuda_stream)
+    # the first codestream initialises the decoder
+    first = enc.encode(frames[0])
+    dec = jxs.Decoder(first)
+    dec.set_stream(stream.cuda_stream)
+
+    def planes_of(ts):
+        return [(t.data_ptr(), t.shape[1]) for t in ts]
+
+    def step(s):
+        base = (s * F) % SEQ_FRAMES
+        for i in range(F):
+            r = enc.send(planes_of(d_in[(base + i) % SEQ_FRAMES]), d_bs[i].data_ptr(), out_cap=lcod + 64)
+            assert r == 0
+            r, f = enc.get()
+            assert r == 0, hex(r)
+            r = dec.send(d_bs[i].data_ptr(), planes_of(d_out[i]), bs_size=lcod)
+            assert r == 0
+            r, _ = dec.get()
+            assert r == 0, hex(r)
+
+    for w in range(max(args.warmup, 1)):
+        step(w)
+    torch.cuda.synchronize()
+    enc.set_timing(True)
+    dec.set_timing(True)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        step(args.warmup + s)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    host_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    dev_ms = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([dev_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms = float(t.item())
+        torch.distributed.barrier()
+    nenc, enc_ms = enc.read_timing()
+    ndec, dec_ms = dec.read_timing()
+    total_frames = args.steps * F * world
+    value = total_frames * W * H / (dev_ms / 1e3) / 1e9
+    # bit-exactness of the last timed step against the oracle
+    import oracle_lib as O
+
+    O.build_oracle()
+    last_base = ((args.warmup + args.steps - 1) * F) % SEQ_FRAMES
+    for i in (0, F - 1):
+        err, want = O.oracle_encode(O.make_params(W, H, DEPTH, 3, BPP, threads=os.cpu_count() or 1),
+                                    frames[(last_base + i) % SEQ_FRAMES])
+        assert err == 0 and np.array_equal(d_bs[i][:lcod].cpu().numpy(), want), "codestream differs from the oracle"
+        err, want_planes = O.oracle_decode(want, threads=os.cpu_count() or 1)
+        assert err == 0 and all(np.array_equal(t.cpu().numpy(), w) for t, w in zip(d_out[i], want_planes)), \
+            "decoded frame differs from the oracle"
+
+    # ---- e2e through the C API with host buffers
+    enc.set_stream(None)
+    dec.set_stream(None)
+    enc.set_timing(False)
+    dec.set_timing(False)
+    def pinned_like(a):
+        buf = torch.empty(a.shape, dtype=torch.from_numpy(a[:1]).dtype).pin_memory()
+        buf.copy_(torch.from_numpy(a))
+        return buf.numpy()
+
+    h_in = [[pinned_like(p) for p in frames[i]] for i in range(F)]
+    h_bs = [torch.empty(lcod + 64, dtype=torch.uint8).pin_memory().numpy() for _ in range(F)]
+    h_out = [[torch.empty(p.shape, dtype=torch.from_numpy(p[:1]).dtype).pin_memory().numpy() for p in frames[0]]
+             for _ in range(F)]
+
+    def e2e_step():
+        sent = 0
+        got = 0
+        while got < F:
+            while sent < F:
+                r = enc.send(h_in[sent], h_bs[sent], blocking=False)
+                if r == jxs.E_EMPTY_QUEUE:
+                    break
+                assert r == 0
+                sent += 1
+            r, f = enc.get()
+            assert r == 0
+            got += 1
+        sent = got = 0
+        while got < F:
+            while sent < F:
+                r = dec.send(h_bs[sent], h_out[sent], bs_size=lcod, blocking=False)
+                if r == jxs.E_EMPTY_QUEUE:
+                    break
+                assert r == 0
+                sent += 1
+            r, _ = dec.get()
+            assert r == 0
+            got += 1
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    lat = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ts = time.perf_counter()
+        e2e_step()
+        lat.append(time.perf_counter() - ts)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_val = args.steps * F * world * W * H / e2e_s / 1e9
+    in_bytes = sum(p.nbytes for p in frames[0])
+    out_bytes = in_bytes
+    # per-frame latency through the API, one frame at a time (no queueing)
+    lat_frame = []
+    for i in range(min(20, SEQ_FRAMES)):
+        ts = time.perf_counter()
+        assert enc.send(h_in[i % F], h_bs[0]) == 0
+        r, _ = enc.get()
+        assert r == 0
+        assert dec.send(h_bs[0], h_out[0], bs_size=lcod) == 0
+        r, _ = dec.get()
+        assert r == 0
+        lat_frame.append((time.perf_counter() - ts) * 1e3)
+    enc.close()
+    dec.close()
+
+    # ---- roofline of the dominant stage
+    peak, peak_kind = measured_peak()
+    stages = {"enc_transform": enc_ms[1], "enc_rate_control": enc_ms[2], "enc_pack": enc_ms[3], "dec_unpack": dec_ms[1],
+              "dec_inverse_transform": dec_ms[2]}
+    nfr = max(nenc, 1)
+    coef_bytes = 2 * (W * H + 2 * (W // 2) * H)
+    alg = {  # algorithmic bytes per frame of each stage
+        "enc_transform": in_bytes + coef_bytes,
+        "enc_rate_control": coef_bytes // 8,
+        "enc_pack": coef_bytes + lcod,
+        "dec_unpack": lcod + coef_bytes,
+        "dec_inverse_transform": coef_bytes + out_bytes,
+    }
+    dom = max(stages, key=lambda k: stages[k])
+    dom_ms = stages[dom] / nfr
+    achieved = alg[dom] / (dom_ms / 1e3) / 1e9
+    pipeline_gbs = (in_bytes + lcod + lcod + out_bytes) / ((sum(stages.values()) / nfr) / 1e3) / 1e9
+    stage_ms = {k: round(v / nfr, 4) for k, v in stages.items()}
+
+    # ---- CPU baseline (oracle on the host cores), rank 0 only
+    cpu = None
+    if rank == 0:
+        threads = os.cpu_count() or 1
+        n, el = cpu_codec_time(frames[:4], {}, args.cpu_seconds, threads)
+        cpu = {"value": n * W * H / el / 1e9, "unit": "Gpix/s", "cores": threads, "kind": "port",
+               "sample": "%d frames encoded + decoded (%.1f s) with the CPU restatement of the reference algorithm" % (n, el)}
+
+    launches_per_frame = 5 + 3  # 2 transform levels + cost + select + pack; unpack + 2 inverse levels
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "int32", "data": "synthetic (seeded, integer-only generator; no dataset)",
+        "config": {"workload": WORKLOAD, "frames_per_step": F, "l2": "inputs 33 MB/frame cycling over 60 frames (> L2)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e_val, "unit": "Gpix/s", "h2d_bytes_per_step": F * (in_bytes + lcod),
+                "d2h_bytes_per_step": F * (lcod + out_bytes), "p50_step_ms": 1e3 * statistics.median(lat),
+                "frame_latency_ms_p50": statistics.median(lat_frame),
+                "frame_latency_ms_p99": float(np.percentile(lat_frame, 99))},
+        "roofline": {"bound": "hbm", "stage": dom, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None, "stage_ms_per_frame": stage_ms,
+                     "pipeline_algorithmic_gbs": pipeline_gbs},
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": launches_per_frame * args.steps * F,
+        "host_wall_s": host_s,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

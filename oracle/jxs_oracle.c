@@ -15,7 +15,8 @@
  * Scope: every option the reference encoder emits with vertical prediction off
  * and sign handling off (deadzone/uniform quantisation, significance on/off,
  * rate-control modes 0 and 1, all colour formats, decomp_v 0-2, decomp_h
- * 0-5); the decoder additionally reads raw-mode packets.
+ * 0-5); the decoder additionally reads raw-mode packets and vertically
+ * predicted GCLIs with either run mode.
  */
 #include "jxs_oracle.h"
 
@@ -1386,23 +1387,66 @@ typedef struct {
     int err;
 } dec_t;
 
-/* Per-thread growable scratch for decoded GCLIs and significance flags. */
-static __thread uint8_t* t_scratch = NULL;
-static __thread uint32_t t_scratch_cap = 0;
-static uint8_t* scratch(uint32_t n) {
-    if (n > t_scratch_cap) {
-        uint8_t* p = (uint8_t*)realloc(t_scratch, n);
-        if (!p) return NULL;
-        t_scratch = p;
-        t_scratch_cap = n;
-    }
-    return t_scratch;
+/* Decoded GCLIs of one precinct row: for each band, up to 4 lines of
+ * gcli_w values, plus the truncation of each band.  A slice keeps two of
+ * these (current row and the row above) for vertical prediction. */
+typedef struct {
+    uint8_t* g[MAXC][MAXB];
+    uint8_t gtli[MAXC][MAXB];
+} gstore_t;
+
+static int gstore_alloc(gstore_t* s, const geom_t* g) {
+    memset(s, 0, sizeof(*s));
+    for (uint32_t c = 0; c < g->nc; c++)
+        for (uint32_t b = 0; b < g->c[c].nb; b++) {
+            s->g[c][b] = (uint8_t*)calloc((size_t)g->c[c].b[b].gcli_w * 4 + 8, 1);
+            if (!s->g[c][b]) return E_RESOURCES;
+        }
+    return E_NONE;
+}
+static void gstore_free(gstore_t* s) {
+    for (int c = 0; c < MAXC; c++)
+        for (int b = 0; b < MAXB; b++) free(s->g[c][b]);
 }
 
-/* unpack_precinct (Source/Lib/Decoder/Codec/Packing.c:513-868) without
- * vertical prediction and sign handling, then dequantisation and sign
- * conversion (Dequant.c:9-57, Precinct.c:9-29). */
-static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last) {
+/* vlc_reader_get_next_value (Packing.c:44-115): unary code, number of ones
+ * before the terminating zero; -1 past 32 ones. */
+static int vlc_next(br_t* r, int64_t* left) {
+    uint32_t n = 0;
+    while (n < 32 && br_get(r, 1)) n++;
+    if (n >= 32) return -1;
+    *left -= n + 1;
+    return (int)n;
+}
+
+/* Vertical prediction of one band line (unpack_verical_pred_gclis_*,
+ * Packing.c:267-431): each GCLI is coded relative to the line above (the
+ * last line of the same band in the precinct above for line 0). */
+static int decode_vpred_line(br_t* r, int64_t* left, uint8_t* gl, const uint8_t* top, uint8_t gtli, uint8_t gtli_top,
+                             uint32_t gcli_w, const uint8_t* sig, int run_mode) {
+    const int t = MAX(gtli_top, gtli);
+    for (uint32_t i = 0; i < gcli_w; i++) {
+        const int m_top = MAX((int)top[i], t);
+        if (sig && sig[i / 8]) {
+            gl[i] = run_mode ? gtli : (uint8_t)m_top;
+            continue;
+        }
+        const int x = vlc_next(r, left);
+        if (x < 0) return E_DEC_BITSTREAM;
+        const int thr = MAX(m_top - (int)gtli, 0);
+        int delta = 0;
+        if (x > 2 * thr) delta = x - thr;
+        else if (x > 0) delta = (x & 1) ? -((x + 1) / 2) : x / 2;
+        gl[i] = (uint8_t)(m_top + delta);
+    }
+    return E_NONE;
+}
+
+/* unpack_precinct (Source/Lib/Decoder/Codec/Packing.c:513-868) without the
+ * separate sign sub-packet, then dequantisation and sign conversion
+ * (Dequant.c:9-57, Precinct.c:9-29).  `top` is the precinct above in the
+ * same slice (NULL for the first precinct of a slice). */
+static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, const gstore_t* top) {
     dec_hdr_t* h = d->h;
     const geom_t* g = &h->g;
     if (!br_enough(r, 5 + DIV_UP(g->nbands_exist * 2, 8))) return E_DEC_SHORT;
@@ -1414,15 +1458,14 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last) {
     for (uint32_t i = 0; i < g->nbands_all; i++) {
         if (g->gband[i] == NOBAND) { mode[i] = 0xff; continue; }
         mode[i] = (uint8_t)br_get(r, 2);
-        if (mode[i] & 1) return E_DEC_BITSTREAM; /* vertical prediction in a first precinct / outside this restatement */
+        if (!top && (mode[i] & 1)) return E_DEC_BITSTREAM; /* no precinct above to predict from */
     }
     br_align(r);
     if (!br_enough(r, lprc)) return E_DEC_SHORT;
     int64_t left = (int64_t)lprc * 8;
     const uint64_t prec_start = r->bit >> 3;
-    uint8_t gtli[MAXC][MAXB];
     for (uint32_t c = 0; c < g->nc; c++)
-        for (uint32_t b = 0; b < g->c[c].nb; b++) gtli[c][b] = truncation(g->c[c].b[b].gain, g->c[c].b[b].prio, q, rr);
+        for (uint32_t b = 0; b < g->c[c].nb; b++) cur->gtli[c][b] = truncation(g->c[c].b[b].gain, g->c[c].b[b].prio, q, rr);
     for (uint32_t k = 0; k < g->npk; k++) {
         const uint32_t l = g->pk[k].line;
         int present = 0;
@@ -1440,16 +1483,8 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last) {
         else { dlen = br_get(r, 15); glen = br_get(r, 13); slen = br_get(r, 11); }
         if ((uint64_t)left < ((uint64_t)dlen + glen + slen) * 8) return E_DEC_BITSTREAM;
         uint64_t sub_start;
-        uint32_t goff[MAXGB];
-        uint32_t gsum = 0, ssum = 0;
-        for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
-            goff[i - g->pk[k].bs] = gsum;
-            gsum += g->c[g->gcomp[i]].b[g->gband[i]].gcli_w;
-            ssum += g->c[g->gcomp[i]].b[g->gband[i]].sig_w;
-        }
-        uint8_t* gbuf = scratch(gsum + ssum + 64);
-        if (!gbuf) return E_RESOURCES;
-        uint8_t* sbuf = gbuf + gsum;
+        uint8_t* sig_store[MAXGB] = {0};
+        uint8_t sbuf[MAXGB][1024];
         if (raw) {
             sub_start = r->bit >> 3;
             for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
@@ -1457,22 +1492,20 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last) {
                 if (l >= (last ? bd->last_lines : bd->lines)) continue;
                 left -= bd->gcli_w * 4;
                 if (left < 0) return E_DEC_BITSTREAM;
-                uint8_t* gl = gbuf + goff[i - g->pk[k].bs];
+                uint8_t* gl = cur->g[g->gcomp[i]][g->gband[i]] + (size_t)l * bd->gcli_w;
                 for (uint32_t x = 0; x < bd->gcli_w; x++) gl[x] = (uint8_t)br_get(r, 4);
             }
         } else {
-            /* significance sub-packet */
-            uint8_t* sig_store[MAXGB] = {0};
-            uint32_t so = 0;
+            /* significance sub-packet: 1 = group insignificant */
             for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
                 const band_t* bd = &g->c[g->gcomp[i]].b[g->gband[i]];
-                sig_store[i - g->pk[k].bs] = sbuf + so;
-                so += bd->sig_w;
                 if (l >= (last ? bd->last_lines : bd->lines)) continue;
                 if (mode[i] & 2) {
+                    if (bd->sig_w > 1024) return E_RESOURCES;
                     left -= bd->sig_w;
                     if (left < 0) return E_DEC_BITSTREAM;
-                    for (uint32_t s = 0; s < bd->sig_w; s++) sig_store[i - g->pk[k].bs][s] = (uint8_t)br_get(r, 1);
+                    sig_store[i - g->pk[k].bs] = sbuf[i - g->pk[k].bs];
+                    for (uint32_t s2 = 0; s2 < bd->sig_w; s2++) sig_store[i - g->pk[k].bs][s2] = (uint8_t)br_get(r, 1);
                 }
             }
             br_align(r);
@@ -1482,16 +1515,20 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last) {
                 uint32_t c = g->gcomp[i], b = g->gband[i];
                 const band_t* bd = &g->c[c].b[b];
                 if (l >= (last ? bd->last_lines : bd->lines)) continue;
-                uint8_t* gl = gbuf + goff[i - g->pk[k].bs];
-                const uint8_t t = gtli[c][b];
+                uint8_t* gl = cur->g[c][b] + (size_t)l * bd->gcli_w;
+                const uint8_t t = cur->gtli[c][b];
                 const uint8_t* sf = sig_store[i - g->pk[k].bs];
-                for (uint32_t x = 0; x < bd->gcli_w; x++) {
-                    if ((mode[i] & 2) && sf[x / 8]) { gl[x] = t; continue; }
-                    uint32_t n = 0;
-                    while (n < 32 && br_get(r, 1)) n++;
-                    if (n >= 32) return E_DEC_BITSTREAM;
-                    left -= n + 1;
-                    gl[x] = (uint8_t)(t + n);
+                if (mode[i] & 1) {
+                    const uint8_t* tp = l == 0 ? top->g[c][b] + (size_t)(bd->lines - 1) * bd->gcli_w : cur->g[c][b] + (size_t)(l - 1) * bd->gcli_w;
+                    const uint8_t tt = l == 0 ? top->gtli[c][b] : t;
+                    if (decode_vpred_line(r, &left, gl, tp, t, tt, bd->gcli_w, sf, (int)h->rm)) return E_DEC_BITSTREAM;
+                } else {
+                    for (uint32_t x = 0; x < bd->gcli_w; x++) {
+                        if (sf && sf[x / 8]) { gl[x] = t; continue; }
+                        int n = vlc_next(r, &left);
+                        if (n < 0) return E_DEC_BITSTREAM;
+                        gl[x] = (uint8_t)(t + n);
+                    }
                 }
             }
         }
@@ -1509,8 +1546,8 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last) {
             uint32_t c = g->gcomp[i], b = g->gband[i];
             const band_t* bd = &g->c[c].b[b];
             if (l >= (last ? bd->last_lines : bd->lines)) continue;
-            const uint8_t t = gtli[c][b];
-            const uint8_t* gl = gbuf + goff[i - g->pk[k].bs];
+            const uint8_t t = cur->gtli[c][b];
+            const uint8_t* gl = cur->g[c][b] + (size_t)l * bd->gcli_w;
             int16_t* out = d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w;
             for (uint32_t x = 0; x < bd->gcli_w; x++) {
                 uint16_t v[4] = {0, 0, 0, 0};
@@ -1518,7 +1555,7 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last) {
                 if (planes > 0) {
                     left -= 4 * (planes + 1);
                     if (left < 0) return E_DEC_BITSTREAM;
-                    uint32_t s = br_get(r, 4);
+                    uint32_t sg = br_get(r, 4);
                     uint32_t m[4] = {0, 0, 0, 0};
                     for (int32_t pl = 0; pl < planes; pl++) {
                         uint32_t nib = br_get(r, 4);
@@ -1537,7 +1574,7 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last) {
                                 mag = acc;
                             }
                         }
-                        v[k2] = (uint16_t)(mag | (((s >> (3 - k2)) & 1u) << 15));
+                        v[k2] = (uint16_t)(mag | (((sg >> (3 - k2)) & 1u) << 15));
                     }
                 }
                 for (uint32_t k2 = 0; k2 < 4 && x * 4 + k2 < bd->w; k2++) {
@@ -1568,13 +1605,22 @@ static void dec_slice(void* ctx, uint32_t s) {
     br_t r = {d->bs, d->size, (uint64_t)d->slice_off[s] * 8};
     if (!br_enough(&r, 6)) { d->err = E_DEC_SHORT; return; }
     if (br_get(&r, 16) != 0xff20 || br_get(&r, 16) != 4 || br_get(&r, 16) != s) { d->err = E_DEC_BITSTREAM; return; }
+    gstore_t st[2];
+    if (gstore_alloc(&st[0], g) || gstore_alloc(&st[1], g)) {
+        gstore_free(&st[0]);
+        gstore_free(&st[1]);
+        d->err = E_RESOURCES;
+        return;
+    }
     uint32_t first = s * g->pps;
     uint32_t n = (s == g->nslices - 1) ? g->np - first : g->pps;
     for (uint32_t i = 0; i < n; i++) {
         uint32_t p = first + i;
-        int e = dec_precinct(d, &r, p, p + 1 >= g->np);
-        if (e) { d->err = e; return; }
+        int e = dec_precinct(d, &r, p, p + 1 >= g->np, &st[i & 1], i ? &st[(i + 1) & 1] : NULL);
+        if (e) { d->err = e; break; }
     }
+    gstore_free(&st[0]);
+    gstore_free(&st[1]);
 }
 
 typedef struct {
@@ -1625,7 +1671,7 @@ int or_decode(const uint8_t* bs, uint32_t size, void* const planes[4], const uin
         e = or_probe(bs, size, info);
         if (e) return e;
     }
-    if (h.fs || h.rm) return E_DEC_BITSTREAM; /* sign sub-packets / run mode are outside this restatement */
+    if (h.fs) return E_DEC_BITSTREAM; /* separate sign sub-packets are outside this restatement */
     dec_t d;
     memset(&d, 0, sizeof(d));
     d.h = &h;

@@ -18,6 +18,7 @@
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdio.h>
 
 #include "jxs_core.h"
 #include "jxs_kernels.cuh"
@@ -529,6 +530,7 @@ __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restr
                 }
             }
             if (err) {
+                printf("jxs rc: slice %d precinct %u budget %u: error 0x%x\n", s, p, budget, (unsigned)err);
                 s_err = err;
                 JXS_STATUS_SET(status, err);
             }
@@ -579,7 +581,8 @@ DEV uint32_t quantize(uint32_t v, uint32_t gcli, uint32_t t, uint32_t uniform) {
     uint32_t m = v & 0x7fffu;
     if (uniform) {
         const uint32_t s = gcli - t + 1;
-        m = ((((m << s) - m + (1u << gcli)) & 0xffffu) >> (gcli + 1)) & 0xffffu;
+        /* computed in int like the reference, truncated to 16 bits after the shift */
+        m = (((m << s) - m + (1u << gcli)) >> (gcli + 1)) & 0xffffu;
         m = (m << t) & 0xffffu;
     } else {
         m = (m >> t) << t;
@@ -657,7 +660,10 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     const uint32_t total = R.total_bytes;
     const uint32_t words = (total + 3) >> 2;
     if (words > cap_words) {
-        if (threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        if (threadIdx.x == 0) {
+            printf("jxs pack: precinct %d needs %u words, buffer holds %u\n", p, words, cap_words);
+            JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        }
         return;
     }
     for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) buf[i] = 0;
@@ -679,7 +685,10 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     __syncthreads();
     const int nbl = s_nbl;
     if (s_ns > sig_cap) {
-        if (threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        if (threadIdx.x == 0) {
+            printf("jxs pack: precinct %d has %u significance groups, buffer holds %u\n", p, s_ns, sig_cap);
+            JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        }
         return;
     }
     /* per band line: data bits, GCLI bits, significance-zeroed GCLIs */
@@ -758,7 +767,7 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
             const uint32_t gcl_bytes = raw ? rawB : gB;
             /* packet header (PackHeaders.c:98-127), sign length 0 */
             const uint32_t hp = pos >> 3;
-            if (hp + 7 > words * 4) {
+            if (hp + (cfg->short_hdr ? 5u : 7u) > words * 4) {
                 pos = 0xffffffffu; /* inconsistent sizes: rejected below */
                 break;
             }
@@ -818,7 +827,11 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
         }
         /* the packed size must be what the rate control paid for */
         s_ok = pos != 0xffffffffu && (pos & 7) == 0 && (pos >> 3) <= total && (pos >> 3) == cfg->hdrs_bytes[last] + R.data_bytes;
-        if (!s_ok) JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        if (!s_ok) {
+            printf("jxs pack: precinct %d packs to %u bits, rate control paid %u + %u bytes (total %u)\n", p, pos,
+                   cfg->hdrs_bytes[last], R.data_bytes, total);
+            JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        }
     }
     __syncthreads();
     if (!s_ok) return;
@@ -899,7 +912,10 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     }
     __syncthreads();
     if (pk_overflow) {
-        if (threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        if (threadIdx.x == 0) {
+            printf("jxs pack: precinct %d wrote past its %u words\n", p, pk_nwords);
+            JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        }
         return;
     }
     /* copy out; slice header, codestream header and EOC around it */

@@ -1,0 +1,135 @@
+"""Regenerates the golden fixtures in this directory from the reference
+SVT-JPEG-XS library built from its own sources (oracle/_ref, see
+oracle/Makefile).  Run in a checkout where the reference is available:
+
+    make -C oracle ref oracle && python tests/golden/make_golden.py
+
+Writes
+  <case>.npz            small seeded inputs, the reference's codestream and
+                        the reference decoder's planes for that codestream
+  ref_sample_16x16.npz  the 16x16 4:2:2 codestream of the reference's decoder
+                        unit test (tests/UnitTests/SampleFramesData.cc), its
+                        frame size and the reference decoder's planes
+  full_size.json        sha256 of the reference codestream and decoded
+                        planes for the full-size workloads (seeded, integer-
+                        only synthetic frames, reproducible on any platform)
+"""
+import hashlib
+import json
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+sys.path.insert(0, os.path.join(ROOT, "svt-jpeg-xs_gb300"))
+
+import jxs_synth as S  # noqa: E402
+import oracle_lib as O  # noqa: E402
+
+REFERENCE = "/root/reference"
+
+# name: (w, h, depth, fmt, bpp_num, bpp_den, decomp_v, decomp_h, quant, slice_h, significance, rc_mode, seed)
+SMALL_CASES = {
+    "c1_422_8b": (64, 32, 8, S.FMT_YUV422, 5, 1, 2, 5, 0, 16, 1, 1, 1),
+    "c2_422_10b": (128, 48, 10, S.FMT_YUV422, 3, 1, 2, 5, 0, 16, 1, 1, 2),
+    "c3_420_8b": (96, 48, 8, S.FMT_YUV420, 2, 1, 2, 5, 0, 16, 1, 1, 3),
+    "c3_444_12b": (64, 32, 12, S.FMT_YUV444, 4, 1, 2, 5, 0, 16, 1, 1, 4),
+    "c3_rgb_8b": (128, 32, 8, S.FMT_PACKED_RGB, 4, 1, 2, 5, 0, 16, 1, 1, 5),
+    "c4_gbrp_14b_v1": (128, 24, 14, S.FMT_YUV444, 3, 2, 1, 5, 0, 16, 1, 1, 6),
+    "odd_444_10b": (53, 37, 10, S.FMT_YUV444, 4, 1, 2, 5, 0, 16, 1, 1, 7),
+    "uniform_422_10b": (80, 40, 10, S.FMT_YUV422, 3, 1, 2, 5, 1, 16, 1, 1, 8),
+    "nosig_rc0_422_8b": (80, 40, 8, S.FMT_YUV422, 3, 1, 2, 5, 0, 16, 0, 0, 9),
+    "v0h3_444_8b": (72, 20, 8, S.FMT_YUV444, 4, 1, 0, 3, 0, 16, 1, 1, 10),
+    "v2h2_422_8b": (60, 44, 8, S.FMT_YUV422, 4, 1, 2, 2, 0, 8, 1, 1, 11),
+    "raw_rgb_12b_v1": (28, 84, 12, S.FMT_PACKED_RGB, 8, 1, 1, 5, 0, 16, 1, 1, 12),
+    "slice_full_422_8b": (96, 40, 8, S.FMT_YUV422, 3, 1, 2, 5, 0, 1000, 1, 1, 13),
+}
+
+# Full-size workloads: the bench's 4K 10-bit stream, the 1080p plain case,
+# the three shapes of the mixed batch and the 8K large-frame stress.
+FULL_CASES = {
+    "c1_1080p_422_8b_bpp5": dict(w=1920, h=1080, d=8, fmt=S.FMT_YUV422, bpp=5, den=1, v=2, hh=5, seed=1, kind="frame"),
+    "c2_2160p_422_10b_bpp3_f0": dict(w=3840, h=2160, d=10, fmt=S.FMT_YUV422, bpp=3, den=1, v=2, hh=5, seed=2, kind="4k", frame=0),
+    "c2_2160p_422_10b_bpp3_f1": dict(w=3840, h=2160, d=10, fmt=S.FMT_YUV422, bpp=3, den=1, v=2, hh=5, seed=2, kind="4k", frame=1),
+    "c3_720p_420_8b_bpp1": dict(w=1280, h=720, d=8, fmt=S.FMT_YUV420, bpp=1, den=1, v=2, hh=5, seed=31, kind="frame"),
+    "c3_1080p_444_12b_bpp4": dict(w=1920, h=1080, d=12, fmt=S.FMT_YUV444, bpp=4, den=1, v=2, hh=5, seed=32, kind="frame"),
+    "c3_2160p_rgb_8b_bpp2": dict(w=3840, h=2160, d=8, fmt=S.FMT_PACKED_RGB, bpp=2, den=1, v=2, hh=5, seed=33, kind="frame"),
+    "c4_4320p_gbrp_14b_bpp1.5": dict(w=7680, h=4320, d=14, fmt=S.FMT_YUV444, bpp=3, den=2, v=1, hh=5, seed=4, kind="8k"),
+}
+
+
+def full_case_planes(c):
+    if c["kind"] == "4k":
+        return S.frame_4k_10bit(c["seed"], c["frame"])
+    if c["kind"] == "8k":
+        return S.frame_8k_14bit(c["seed"])
+    return S.frame(c["w"], c["h"], c["d"], c["fmt"], seed=c["seed"])
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def sample_codestream():
+    txt = open(os.path.join(REFERENCE, "tests", "UnitTests", "SampleFramesData.cc")).read()
+    body = txt[txt.index("Frame_Sample_1_16x16_8bit_422_bitstream[] = {"):]
+    body = body[body.index("{") + 1: body.index("};")]
+    return np.array([int(x, 16) for x in re.findall(r"0x[0-9A-Fa-f]+", body)], np.uint8)
+
+
+def main():
+    if not O.ref_available():
+        raise SystemExit("build the reference first: make -C oracle ref")
+    for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed) in SMALL_CASES.items():
+        planes = S.frame(w, h, d, fmt, seed=seed)
+        p = O.make_params(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, significance=sig, rc_mode=rc)
+        err, bs = O.ref_encode(p, planes)
+        assert err == 0, (name, hex(err))
+        err, dec = O.ref_decode(bs)
+        assert err == 0, (name, hex(err))
+        arrays = {"bs": bs, "params": np.array([w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc], np.uint32)}
+        for i, pl in enumerate(planes):
+            arrays["in%d" % i] = pl
+        for i, pl in enumerate(dec):
+            arrays["dec%d" % i] = pl
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+        print(name, len(bs), "bytes")
+    bs = sample_codestream()
+    err, dec = O.ref_decode(bs)
+    assert err == 0
+    fs = np.zeros(1, np.uint32)
+    import ctypes
+    info = O.ImageInfo()
+    size = ctypes.c_uint32()
+    comp = (ctypes.c_uint32 * 12)()
+    w = ctypes.c_uint32(); h = ctypes.c_uint32(); dep = ctypes.c_uint32(); f = ctypes.c_uint32(); nc = ctypes.c_uint32()
+    r = O.ref().ref_probe(bs.ctypes.data_as(ctypes.c_void_p), len(bs), ctypes.byref(w), ctypes.byref(h), ctypes.byref(dep),
+                          ctypes.byref(f), ctypes.byref(nc), comp, ctypes.byref(size))
+    assert r == 0
+    fs[0] = size.value
+    arrays = {"bs": bs, "frame_size": fs}
+    for i, pl in enumerate(dec):
+        arrays["dec%d" % i] = pl
+    np.savez_compressed(os.path.join(HERE, "ref_sample_16x16.npz"), **arrays)
+    print("ref sample", len(bs), "bytes, frame size", size.value)
+    full = {}
+    for name, c in FULL_CASES.items():
+        planes = full_case_planes(c)
+        p = O.make_params(c["w"], c["h"], c["d"], c["fmt"], c["bpp"], c["den"], c["v"], c["hh"], threads=8)
+        err, bs = O.ref_encode(p, planes)
+        assert err == 0, (name, hex(err))
+        err, dec = O.ref_decode(bs, threads=8)
+        assert err == 0, (name, hex(err))
+        full[name] = dict(c, input_sha256=[sha(pl) for pl in planes], codestream_bytes=int(len(bs)),
+                          codestream_sha256=sha(bs), decoded_sha256=[sha(pl) for pl in dec])
+        print(name, len(bs), "bytes")
+    with open(os.path.join(HERE, "full_size.json"), "w") as fh:
+        json.dump(full, fh, indent=1)
+
+
+if __name__ == "__main__":
+    main()

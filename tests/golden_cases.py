@@ -1,0 +1,42 @@
+"""Loaders for the committed golden fixtures (tests/golden)."""
+import glob
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def small_cases():
+    out = {}
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
+        name = os.path.basename(path)[:-4]
+        if name == "ref_sample_16x16":
+            continue
+        z = np.load(path)
+        w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc = [int(x) for x in z["params"]]
+        out[name] = dict(w=w, h=h, d=d, fmt=fmt, bpp_num=bn, bpp_den=bd, v=v, hh=hh, q=q, sl=sl, sig=sig, rc=rc,
+                         planes=[z["in%d" % i] for i in range(4) if "in%d" % i in z],
+                         bs=z["bs"], dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z])
+    return out
+
+
+def ref_sample():
+    z = np.load(os.path.join(GOLDEN, "ref_sample_16x16.npz"))
+    return z["bs"], int(z["frame_size"][0]), [z["dec%d" % i] for i in range(4) if "dec%d" % i in z]
+
+
+def full_size():
+    with open(os.path.join(GOLDEN, "full_size.json")) as fh:
+        return json.load(fh)
+
+
+def full_planes(case):
+    import jxs_synth as S
+
+    if case["kind"] == "4k":
+        return S.frame_4k_10bit(case["seed"], case["frame"])
+    if case["kind"] == "8k":
+        return S.frame_8k_14bit(case["seed"])
+    return S.frame(case["w"], case["h"], case["d"], case["fmt"], seed=case["seed"])

@@ -1,0 +1,81 @@
+"""The drop-in boundary: exported symbols and struct layouts.
+
+- libSvtJpegxs.so exports every function declared in include/*.h;
+- the public structs have the reference's layout (compiled against both
+  header sets when the reference sources are present) and the ctypes
+  bindings agree with the C layout.
+No GPU is used: the library only has to load.
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INCLUDE = os.path.join(ROOT, "include")
+REF_API = "/root/reference/Source/API"
+
+
+def declared_functions():
+    names = set()
+    for fn in sorted(os.listdir(INCLUDE)):
+        if fn.endswith(".h"):
+            text = open(os.path.join(INCLUDE, fn)).read()
+            names.update(re.findall(r"PREFIX_API\s+[\w\s\*]+?\b(svt_jpeg_xs_\w+)\s*\(", text))
+    return sorted(names)
+
+
+def test_all_declared_symbols_exported(jxs_lib):
+    names = declared_functions()
+    assert len(names) >= 29
+    lib = ctypes.CDLL(jxs_lib.LIB_PATH)
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_soname_and_reference_symbol_set(jxs_lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", jxs_lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (svt_jpeg_xs_\w+)", out))
+    reference_api = {
+        "svt_jpeg_xs_encoder_load_default_parameters", "svt_jpeg_xs_encoder_get_image_config", "svt_jpeg_xs_encoder_init",
+        "svt_jpeg_xs_encoder_close", "svt_jpeg_xs_encoder_send_picture", "svt_jpeg_xs_encoder_get_packet",
+        "svt_jpeg_xs_decoder_init", "svt_jpeg_xs_decoder_close", "svt_jpeg_xs_decoder_get_single_frame_size",
+        "svt_jpeg_xs_decoder_get_single_frame_size_with_proxy", "svt_jpeg_xs_decoder_send_frame",
+        "svt_jpeg_xs_decoder_send_packet", "svt_jpeg_xs_decoder_get_frame", "svt_jpeg_xs_decoder_send_eoc",
+        "svt_jpeg_xs_image_buffer_alloc", "svt_jpeg_xs_image_buffer_free", "svt_jpeg_xs_bitstream_alloc",
+        "svt_jpeg_xs_bitstream_free", "svt_jpeg_xs_frame_pool_alloc", "svt_jpeg_xs_frame_pool_free",
+        "svt_jpeg_xs_frame_pool_get", "svt_jpeg_xs_frame_pool_release"}
+    assert reference_api <= exported
+    soname = subprocess.run(["readelf", "-d", jxs_lib.LIB_PATH], capture_output=True, text=True).stdout
+    assert "libSvtJpegxs.so.0" in soname
+
+
+def _layout(include_dir, tmp_path, tag):
+    exe = str(tmp_path / ("abi_" + tag))
+    subprocess.check_call(["gcc", "-std=gnu11", "-I", include_dir, os.path.join(ROOT, "tests", "abi_layout.c"), "-o", exe])
+    return subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+
+
+def test_layout_matches_reference_headers(tmp_path):
+    ours = _layout(INCLUDE, tmp_path, "ours")
+    if not os.path.exists(os.path.join(REF_API, "SvtJpegxs.h")):
+        pytest.skip("reference headers not present")
+    theirs = _layout(REF_API, tmp_path, "ref")
+    assert ours == theirs
+
+
+def test_ctypes_bindings_match_c_layout(jxs_lib, tmp_path):
+    lines = dict(l.rsplit(" ", 1) for l in _layout(INCLUDE, tmp_path, "ours2").strip().splitlines())
+    checks = {
+        "svt_jpeg_xs_encoder_api_t": jxs_lib.EncoderApi, "svt_jpeg_xs_decoder_api_t": jxs_lib.DecoderApi,
+        "svt_jpeg_xs_frame_t": jxs_lib.Frame, "svt_jpeg_xs_image_buffer_t": jxs_lib.ImageBuffer,
+        "svt_jpeg_xs_bitstream_buffer_t": jxs_lib.BitstreamBuffer, "svt_jpeg_xs_image_config_t": jxs_lib.ImageConfig,
+    }
+    for cname, py in checks.items():
+        assert int(lines[cname]) == ctypes.sizeof(py), cname
+        for key, off in lines.items():
+            if key.startswith(cname + "."):
+                field = key.split(".", 1)[1]
+                assert getattr(py, field).offset == int(off), key

@@ -1,0 +1,274 @@
+"""GPU encode/decode parity through the C API.
+
+Every codestream the GPU encoder writes must be byte-identical to the
+oracle's (and, through the golden fixtures and full-size hashes, to the
+reference encoder's); every GPU decode must be bit-identical.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import golden_cases as G
+import jxs_synth as S
+
+pytestmark = pytest.mark.gpu
+SMALL = G.small_cases()
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def make_encoder(jxs, c, **kw):
+    return jxs.Encoder(c["w"], c["h"], c["d"], c["fmt"], c["bpp_num"], c["bpp_den"], c["v"], c["hh"], quantization=c["q"],
+                       slice_height=c["sl"], coding_significance=c["sig"], rate_control_mode=c["rc"], **kw)
+
+
+@pytest.mark.parametrize("name", sorted(SMALL))
+def test_golden_encode(gpu, name):
+    c = SMALL[name]
+    enc = make_encoder(gpu, c)
+    bs = enc.encode(c["planes"])
+    enc.close()
+    assert len(bs) == len(c["bs"]) and np.array_equal(bs, c["bs"])
+
+
+@pytest.mark.parametrize("name", sorted(SMALL))
+def test_golden_decode(gpu, name):
+    c = SMALL[name]
+    dec = gpu.Decoder(c["bs"])
+    out = dec.decode(c["bs"])
+    dec.close()
+    assert all(np.array_equal(a, b) for a, b in zip(out, c["dec"]))
+
+
+@pytest.mark.parametrize("name", ["c1_1080p_422_8b_bpp5", "c2_2160p_422_10b_bpp3_f0", "c2_2160p_422_10b_bpp3_f1",
+                                  "c3_720p_420_8b_bpp1", "c3_1080p_444_12b_bpp4", "c3_2160p_rgb_8b_bpp2",
+                                  "c4_4320p_gbrp_14b_bpp1.5"])
+def test_full_size_against_reference_hashes(gpu, name):
+    case = G.full_size()[name]
+    planes = G.full_planes(case)
+    assert [sha(p) for p in planes] == case["input_sha256"]
+    enc = gpu.Encoder(case["w"], case["h"], case["d"], case["fmt"], case["bpp"], case["den"], case["v"], case["hh"])
+    bs = enc.encode(planes)
+    enc.close()
+    assert len(bs) == case["codestream_bytes"] and sha(bs) == case["codestream_sha256"]
+    dec = gpu.Decoder(bs)
+    out = dec.decode(bs)
+    dec.close()
+    assert [sha(p) for p in out] == case["decoded_sha256"]
+
+
+def _random_cases(n, seed):
+    rng = np.random.default_rng(seed)
+    fmts = [S.FMT_YUV422, S.FMT_YUV420, S.FMT_YUV444, S.FMT_PACKED_RGB]
+    levels = [(2, 5), (1, 5), (0, 5), (2, 3), (1, 2), (0, 1), (2, 2), (1, 1)]
+    out = []
+    while len(out) < n:
+        fmt = fmts[int(rng.integers(0, len(fmts)))]
+        v, hh = levels[int(rng.integers(0, len(levels)))]
+        if fmt == S.FMT_YUV420 and v == 0:
+            continue
+        w = int(rng.integers(8, 700))
+        h = int(rng.integers(4, 140))
+        if fmt in (S.FMT_YUV422, S.FMT_YUV420):
+            w += w % 2
+        if fmt == S.FMT_YUV420:
+            h += h % 2
+        sl = int(rng.choice([2, 4, 8, 16, 32, 1000]))
+        if sl % (1 << v):
+            sl = 16
+        out.append(dict(w=w, h=h, d=int(rng.choice([8, 10, 12, 14])), fmt=fmt, bpp_num=int(rng.choice([1, 2, 3, 4, 6, 9])),
+                        bpp_den=int(rng.choice([1, 1, 2])), v=v, hh=hh, q=int(rng.integers(0, 2)), sl=sl,
+                        sig=int(rng.integers(0, 2)), rc=int(rng.integers(0, 2)), seed=100 + len(out)))
+    return out
+
+
+@pytest.mark.parametrize("c", _random_cases(60, 77), ids=lambda c: "%dx%d_d%d_f%d_V%dH%d_q%d" % (
+    c["w"], c["h"], c["d"], c["fmt"], c["v"], c["hh"], c["q"]))
+def test_random_against_oracle(gpu, oracle, c):
+    planes = S.frame(c["w"], c["h"], c["d"], c["fmt"], seed=c["seed"])
+    p = oracle.make_params(c["w"], c["h"], c["d"], c["fmt"], c["bpp_num"], c["bpp_den"], c["v"], c["hh"], quantization=c["q"],
+                           slice_height=c["sl"], significance=c["sig"], rc_mode=c["rc"])
+    err, ref_bs, ref_q, ref_r = oracle.oracle_encode(p, planes, want_qr=True)
+    if err == 0x80001005:
+        with pytest.raises(gpu.JxsError):
+            make_encoder(gpu, c)
+        return
+    enc = make_encoder(gpu, c)
+    out = np.zeros(enc.frame_bytes + 64, np.uint8)
+    assert enc.send(planes, out) == 0
+    q, r = enc.rc_results()
+    rc, f = enc.get()
+    enc.close()
+    assert rc == err
+    if err:
+        return
+    assert np.array_equal(q, ref_q) and np.array_equal(r, ref_r)
+    assert np.array_equal(out[: f.bitstream.used_size], ref_bs)
+    dec = gpu.Decoder(ref_bs)
+    got = dec.decode(ref_bs)
+    dec.close()
+    e2, want = oracle.oracle_decode(ref_bs)
+    assert e2 == 0 and all(np.array_equal(a, b) for a, b in zip(got, want))
+
+
+def test_strided_planes(gpu):
+    c = SMALL["c2_422_10b"]
+    padded = []
+    for p in c["planes"]:
+        big = np.full((p.shape[0], p.shape[1] + 24), 0x3ff, p.dtype)
+        big[:, : p.shape[1]] = p
+        padded.append(big[:, : p.shape[1]])
+    enc = make_encoder(gpu, c)
+    f_out = np.zeros(enc.frame_bytes + 8, np.uint8)
+    frame = enc._frame([(int(b.ctypes.data), b.strides[0] // b.itemsize) for b in padded], f_out)
+    import ctypes
+
+    # keep the parent arrays alive and pass the true allocation size
+    for k, b in enumerate(padded):
+        frame.image.alloc_size[k] = b.base.nbytes
+    assert gpu.lib().svt_jpeg_xs_encoder_send_picture(ctypes.byref(enc.api), ctypes.byref(frame), 1) == 0
+    r, f = enc.get()
+    enc.close()
+    assert r == 0 and np.array_equal(f_out[: f.bitstream.used_size], c["bs"])
+
+
+def test_many_frames_in_flight_keep_order(gpu):
+    c = SMALL["c3_444_12b"]
+    enc = make_encoder(gpu, c)
+    frames = [S.frame(c["w"], c["h"], c["d"], c["fmt"], seed=s) for s in range(7)]
+    outs = [np.zeros(enc.frame_bytes, np.uint8) for _ in frames]
+    sent = 0
+    got = []
+    while len(got) < len(frames):
+        while sent < len(frames):
+            r = enc.send(frames[sent], outs[sent], blocking=False, user=1000 + sent)
+            if r == gpu.E_EMPTY_QUEUE:
+                break
+            assert r == 0
+            sent += 1
+        r, f = enc.get(blocking=True)
+        assert r == 0
+        got.append(f.user_prv_ctx_ptr)
+    r, f = enc.get(blocking=False)
+    assert r == gpu.E_EMPTY_QUEUE and f.user_prv_ctx_ptr is None
+    enc.close()
+    assert got == [1000 + i for i in range(len(frames))]
+    enc2 = make_encoder(gpu, c)
+    for fr, out in zip(frames, outs):
+        assert np.array_equal(enc2.encode(fr), out)
+    enc2.close()
+
+
+def test_slice_packetization(gpu):
+    c = SMALL["c2_422_10b"]
+    enc = make_encoder(gpu, c, slice_packetization_mode=1)
+    out = np.zeros(enc.frame_bytes, np.uint8)
+    assert enc.send(c["planes"], out) == 0
+    import ctypes
+
+    pieces = []
+    while True:
+        r, f = enc.get()
+        assert r == 0
+        off = f.bitstream.buffer - out.ctypes.data
+        pieces.append(out[off: off + f.bitstream.used_size])
+        if f.bitstream.last_packet_in_frame:
+            break
+    enc.close()
+    assert len(pieces) == 1 + (c["h"] + c["sl"] - 1) // c["sl"]
+    assert np.array_equal(np.concatenate(pieces), c["bs"])
+
+
+def test_device_pointers(gpu):
+    torch = pytest.importorskip("torch")
+    c = SMALL["c1_422_8b"]
+    planes = [torch.from_numpy(p).cuda() for p in c["planes"]]
+    enc = make_encoder(gpu, c)
+    out = torch.zeros(enc.frame_bytes, dtype=torch.uint8, device="cuda")
+    r = enc.send([(t.data_ptr(), t.shape[1]) for t in planes], out.data_ptr(), out_cap=enc.frame_bytes)
+    assert r == 0
+    r, f = enc.get()
+    enc.close()
+    assert r == 0 and np.array_equal(out.cpu().numpy()[: f.bitstream.used_size], c["bs"])
+    dec = gpu.Decoder(c["bs"])
+    dev_bs = torch.from_numpy(c["bs"]).cuda()
+    outs = [torch.zeros(p.shape, dtype=torch.uint8, device="cuda") for p in c["dec"]]
+    assert dec.send(dev_bs.data_ptr(), [(t.data_ptr(), t.shape[1]) for t in outs], bs_size=len(c["bs"])) == 0
+    r, _ = dec.get()
+    dec.close()
+    assert r == 0 and all(np.array_equal(t.cpu().numpy(), p) for t, p in zip(outs, c["dec"]))
+
+
+def test_decoder_packet_mode_and_eoc(gpu):
+    import ctypes
+
+    c = SMALL["c3_420_8b"]
+    dec = gpu.Decoder(c["bs"], packetization_mode=1)
+    planes = dec.alloc_planes()
+    bs = np.concatenate([c["bs"], c["bs"]])
+    used = ctypes.c_uint32()
+    pos = 0
+    while pos < len(bs):
+        chunk = np.ascontiguousarray(bs[pos: pos + 100])
+        f = dec._frame(chunk, planes)
+        assert gpu.lib().svt_jpeg_xs_decoder_send_packet(ctypes.byref(dec.api), ctypes.byref(f), ctypes.byref(used)) == 0
+        pos += used.value
+        if f is not None and pos % 100:
+            pass
+    r, _ = dec.get()
+    assert r == 0 and all(np.array_equal(a, b) for a, b in zip(planes, c["dec"]))
+    r, _ = dec.get()
+    assert r == 0
+    assert gpu.lib().svt_jpeg_xs_decoder_send_eoc(ctypes.byref(dec.api)) == 0
+    r, _ = dec.get()
+    assert r == gpu.E_END_OF_CODESTREAM
+    dec.close()
+
+
+def test_decoder_config_change_and_corrupt_streams(gpu):
+    a, b = SMALL["c1_422_8b"], SMALL["c2_422_10b"]
+    dec = gpu.Decoder(a["bs"])
+    planes = dec.alloc_planes()
+    assert dec.send(b["bs"], planes) == 0
+    r, _ = dec.get()
+    assert r == gpu.E_DEC_CONFIG_CHANGE
+    cut = np.ascontiguousarray(a["bs"][: len(a["bs"]) // 2])
+    assert dec.send(cut, planes) == 0
+    r, _ = dec.get()
+    assert r in (gpu.E_DEC_TOO_SHORT, gpu.E_DEC_INVALID_BITSTREAM)
+    bad = a["bs"].copy()
+    bad[len(bad) // 2: len(bad) // 2 + 40] ^= 0x5A
+    assert dec.send(bad, planes) == 0
+    r, _ = dec.get()
+    assert r in (0, gpu.E_DEC_INVALID_BITSTREAM, gpu.E_DEC_TOO_SHORT)
+    # the decoder keeps working after errors
+    out = dec.decode(a["bs"])
+    dec.close()
+    assert all(np.array_equal(x, y) for x, y in zip(out, a["dec"]))
+
+
+def test_callbacks_fire(gpu):
+    import threading
+
+    c = SMALL["c1_422_8b"]
+    seen = {"get": 0, "send": 0}
+    ev = threading.Event()
+
+    def on_get(api, ctx):
+        seen["get"] += 1
+        ev.set()
+
+    def on_send(api, ctx):
+        seen["send"] += 1
+
+    cb_get, cb_send = gpu._CB(on_get), gpu._CB(on_send)
+    enc = make_encoder(gpu, c, callback_get_data_available=cb_get, callback_send_data_available=cb_send)
+    out = np.zeros(enc.frame_bytes, np.uint8)
+    assert enc.send(c["planes"], out) == 0
+    assert ev.wait(30)
+    r, _ = enc.get()
+    enc.close()
+    assert r == 0 and seen["get"] >= 1 and seen["send"] >= 1

@@ -1,0 +1,112 @@
+"""The oracle (CPU restatement) pinned against the reference.
+
+- every committed golden fixture (made by the reference built from source):
+  byte-identical codestream, bit-identical decode;
+- the reference's own decoder unit-test codestream
+  (tests/UnitTests/SampleFramesData.cc, decoded in TestDecoder.cc:300-320);
+- the full-size workloads' reference hashes;
+- where the reference library is built here (oracle/_ref), a seeded random
+  battery of configurations against it directly, errors included.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+import golden_cases as G
+import jxs_synth as S
+
+SMALL = G.small_cases()
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("name", sorted(SMALL))
+def test_oracle_matches_golden(oracle, name):
+    c = SMALL[name]
+    p = oracle.make_params(c["w"], c["h"], c["d"], c["fmt"], c["bpp_num"], c["bpp_den"], c["v"], c["hh"], quantization=c["q"],
+                           slice_height=c["sl"], significance=c["sig"], rc_mode=c["rc"])
+    err, bs = oracle.oracle_encode(p, c["planes"])
+    assert err == 0
+    assert len(bs) == len(c["bs"]) and np.array_equal(bs, c["bs"])
+    err, dec = oracle.oracle_decode(c["bs"])
+    assert err == 0
+    assert len(dec) == len(c["dec"]) and all(np.array_equal(a, b) for a, b in zip(dec, c["dec"]))
+
+
+def test_oracle_decodes_reference_sample(oracle):
+    bs, frame_size, ref_planes = G.ref_sample()
+    assert frame_size == len(bs)
+    err, dec = oracle.oracle_decode(bs)
+    assert err == 0
+    assert all(np.array_equal(a, b) for a, b in zip(dec, ref_planes))
+
+
+@pytest.mark.parametrize("name", ["c1_1080p_422_8b_bpp5", "c2_2160p_422_10b_bpp3_f0", "c3_720p_420_8b_bpp1",
+                                  "c3_2160p_rgb_8b_bpp2"])
+def test_oracle_full_size_hashes(oracle, name):
+    case = G.full_size()[name]
+    planes = G.full_planes(case)
+    assert [sha(p) for p in planes] == case["input_sha256"], "synthetic input differs from the one the reference saw"
+    p = oracle.make_params(case["w"], case["h"], case["d"], case["fmt"], case["bpp"], case["den"], case["v"], case["hh"],
+                           threads=8)
+    err, bs = oracle.oracle_encode(p, planes)
+    assert err == 0 and len(bs) == case["codestream_bytes"]
+    assert sha(bs) == case["codestream_sha256"]
+    err, dec = oracle.oracle_decode(bs, threads=8)
+    assert err == 0 and [sha(d) for d in dec] == case["decoded_sha256"]
+
+
+def _random_cases(n, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    fmts = [S.FMT_YUV422, S.FMT_YUV420, S.FMT_YUV444, S.FMT_PACKED_RGB]
+    levels = [(2, 5), (1, 5), (0, 5), (2, 3), (1, 2), (0, 1), (2, 2)]
+    while len(out) < n:
+        fmt = fmts[int(rng.integers(0, len(fmts)))]
+        v, hh = levels[int(rng.integers(0, len(levels)))]
+        if fmt == S.FMT_YUV420 and v == 0:
+            continue
+        d = int(rng.choice([8, 10, 12, 14]))
+        w = int(rng.integers(8, 260))
+        h = int(rng.integers(4, 90))
+        if fmt in (S.FMT_YUV422, S.FMT_YUV420):
+            w += w % 2
+        if fmt == S.FMT_YUV420:
+            h += h % 2
+        sl = int(rng.choice([4, 8, 16, 32, 1000]))
+        if sl % (1 << v):
+            sl = 16
+        out.append(dict(w=w, h=h, d=d, fmt=fmt, bpp=int(rng.choice([1, 2, 3, 5, 8])), den=int(rng.choice([1, 1, 2, 3])), v=v,
+                        hh=hh, q=int(rng.integers(0, 2)), sl=sl, sig=int(rng.integers(0, 2)), rc=int(rng.integers(0, 2)),
+                        seed=len(out)))
+    return out
+
+
+@pytest.mark.parametrize("case", _random_cases(120, 2024), ids=lambda c: "%dx%d_d%d_f%d_V%dH%d" % (c["w"], c["h"], c["d"],
+                                                                                                      c["fmt"], c["v"], c["hh"]))
+def test_oracle_matches_reference_random(oracle, case):
+    if not oracle.ref_available():
+        pytest.skip("reference library not built here (needs the reference sources)")
+    c = case
+    planes = S.frame(c["w"], c["h"], c["d"], c["fmt"], seed=c["seed"])
+    p = oracle.make_params(c["w"], c["h"], c["d"], c["fmt"], c["bpp"], c["den"], c["v"], c["hh"], quantization=c["q"],
+                           slice_height=c["sl"], significance=c["sig"], rc_mode=c["rc"])
+    e_ref, b_ref = oracle.ref_encode(p, planes)
+    e_or, b_or = oracle.oracle_encode(p, planes)
+    assert e_ref == e_or
+    if e_ref:
+        return
+    assert np.array_equal(b_ref, b_or)
+    e1, d_ref = oracle.ref_decode(b_ref)
+    e2, d_or = oracle.oracle_decode(b_ref)
+    assert e1 == e2 == 0
+    assert all(np.array_equal(a, b) for a, b in zip(d_ref, d_or))
+
+
+def test_oracle_rejects_truncated_stream(oracle):
+    c = SMALL["c1_422_8b"]
+    err, _ = oracle.oracle_decode(c["bs"][: len(c["bs"]) // 2])
+    assert err in (0x80003003, 0x80003001)
