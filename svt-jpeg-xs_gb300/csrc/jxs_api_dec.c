@@ -266,6 +266,12 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_decoder_init(uint64_t version_api_major
  * finds the precinct offsets and queues the GPU work for `slot`. */
 static int32_t submit_picture_locked(dec_prv_t* p, int slot, const uint8_t* bs, uint32_t size, svt_jpeg_xs_frame_t* f) {
     if (!bs || !size) return JXS_E_DEC_PTR;
+    if (jxs_gpu_is_device_ptr(bs)) {
+        /* codestream already on the GPU: header check and precinct walk run there */
+        void* planes[4] = {f->image.data_yuv[0], f->image.data_yuv[1], f->image.data_yuv[2], f->image.data_yuv[3]};
+        uint32_t strides[4] = {f->image.stride[0], f->image.stride[1], f->image.stride[2], f->image.stride[3]};
+        return jxs_gpu_dec_submit(p->gpu, slot, bs, size, NULL, planes, strides);
+    }
     jxs_hdr_info_t info;
     int32_t r = jxs_cfg_decoder(p->tmp_cfg, bs, size, &info);
     if (r) return r;

@@ -396,6 +396,39 @@ static void write_header(jxs_cfg_t* g) {
     g->hdr_len = (w.bit + 7) >> 3;
 }
 
+/* Slice byte budgets: every slice's byte range is fixed by Lcod before any
+ * pixel is seen (EncHandle.c:760-809).  The decoder uses the same split to
+ * predict where slices start in constant-bit-rate codestreams. */
+int32_t jxs_cfg_slices(jxs_cfg_t* g) {
+    g->max_slice_budget = 0;
+    uint32_t hdrs = g->hdr_len + 2 + 6 * g->nslices;
+    if (g->lcod == 0 || hdrs >= g->lcod) return JXS_E_BAD_PARAM;
+    uint32_t all = g->lcod - hdrs;
+    uint32_t last_prec = g->pps - (g->nslices * g->pps - g->np);
+    uint32_t min_prec = all / g->np;
+    uint32_t min_slice = min_prec * g->pps;
+    uint32_t last_slice = min_prec * last_prec;
+    uint32_t left = all - last_slice - min_slice * (g->nslices - 1);
+    if (g->nslices > 1) min_slice += (uint32_t)(((uint64_t)left * (g->nslices - 1) * g->pps / g->np) / (g->nslices - 1));
+    last_slice += (uint32_t)((uint64_t)left * last_prec / g->np);
+    left = all - last_slice - min_slice * (g->nslices - 1);
+    uint32_t bytes_left = g->lcod - g->hdr_len, begin = g->hdr_len;
+    for (uint32_t i = 0; i < g->nslices; i++) {
+        uint32_t sz;
+        if (i + 1 != g->nslices) {
+            sz = min_slice + (i < left ? 1 : 0) + 6;
+            bytes_left -= sz;
+        } else {
+            sz = bytes_left;
+        }
+        g->slice_size[i] = sz;
+        g->slice_begin[i] = begin;
+        begin += sz;
+        g->max_slice_budget = MAX(g->max_slice_budget, sz);
+    }
+    return JXS_OK;
+}
+
 int32_t jxs_cfg_encoder(jxs_cfg_t* g, struct svt_jpeg_xs_encoder_api* api) {
     memset(g, 0, sizeof(*g));
     uint32_t nc, sx[JXS_MAXC], sy[JXS_MAXC];
@@ -455,35 +488,7 @@ int32_t jxs_cfg_encoder(jxs_cfg_t* g, struct svt_jpeg_xs_encoder_api* api) {
     rc_limits(g);
     write_header(g);
 
-    /* slice byte budgets: every slice's byte range is fixed before any pixel
-     * is seen (EncHandle.c:760-809) */
-    uint32_t hdrs = g->hdr_len + 2 + 6 * g->nslices;
-    if (hdrs >= g->lcod) return JXS_E_BAD_PARAM;
-    uint32_t all = g->lcod - hdrs;
-    uint32_t last_prec = g->pps - (g->nslices * g->pps - g->np);
-    uint32_t min_prec = all / g->np;
-    uint32_t min_slice = min_prec * g->pps;
-    uint32_t last_slice = min_prec * last_prec;
-    uint32_t left = all - last_slice - min_slice * (g->nslices - 1);
-    if (g->nslices > 1) min_slice += (uint32_t)(((uint64_t)left * (g->nslices - 1) * g->pps / g->np) / (g->nslices - 1));
-    last_slice += (uint32_t)((uint64_t)left * last_prec / g->np);
-    left = all - last_slice - min_slice * (g->nslices - 1);
-    uint32_t bytes_left = g->lcod - g->hdr_len, begin = g->hdr_len;
-    g->max_slice_budget = 0;
-    for (uint32_t i = 0; i < g->nslices; i++) {
-        uint32_t s;
-        if (i + 1 != g->nslices) {
-            s = min_slice + (i < left ? 1 : 0) + 6;
-            bytes_left -= s;
-        } else {
-            s = bytes_left;
-        }
-        g->slice_size[i] = s;
-        g->slice_begin[i] = begin;
-        begin += s;
-        g->max_slice_budget = MAX(g->max_slice_budget, s);
-    }
-    return JXS_OK;
+    return jxs_cfg_slices(g);
 }
 
 /* ---- decoder header parsing (ParseHeader.c:20-617) ---- */
@@ -627,7 +632,10 @@ int32_t jxs_cfg_decoder(jxs_cfg_t* g, const uint8_t* bs, size_t size, jxs_hdr_in
     info->hdr_len = (uint32_t)r.pos;
     info->cw = cw;
     g->hdr_len = (uint32_t)r.pos;
-    if (g->hdr_len <= sizeof(g->hdr)) memcpy(g->hdr, bs, g->hdr_len);
+    if (g->hdr_len > sizeof(g->hdr)) return JXS_E_DEC_BITSTREAM;
+    memcpy(g->hdr, bs, g->hdr_len);
+    /* predicted slice starts for constant-bit-rate streams (checked on use) */
+    if (jxs_cfg_slices(g) != JXS_OK) g->max_slice_budget = 0;
     return JXS_OK;
 }
 

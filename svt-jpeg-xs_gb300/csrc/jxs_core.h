@@ -86,7 +86,7 @@ typedef struct jxs_cfg {
     uint8_t hdr[512];
     uint32_t hdr_len;
     uint64_t coef_total, gcli_total;     /* per-frame buffer sizes (elements / bytes) */
-    uint32_t max_slice_budget;
+    uint32_t max_slice_budget;           /* 0 when slice starts cannot be predicted (decoder) */
     uint32_t slice_size[8192];           /* bytes of each slice incl. its header (last: incl. EOC) */
     uint32_t slice_begin[8192];          /* byte offset of each slice in the codestream */
 } jxs_cfg_t;
@@ -114,6 +114,7 @@ static inline JXS_HD uint8_t jxs_truncation(uint8_t gain, uint8_t prio, uint8_t 
 }
 
 int32_t jxs_cfg_encoder(jxs_cfg_t* cfg, struct svt_jpeg_xs_encoder_api* api);
+int32_t jxs_cfg_slices(jxs_cfg_t* cfg);
 int32_t jxs_cfg_decoder(jxs_cfg_t* cfg, const uint8_t* bs, size_t size, jxs_hdr_info_t* info);
 int32_t jxs_cfg_geometry(jxs_cfg_t* cfg, int for_encoder, uint32_t nc, uint32_t W, uint32_t H, uint32_t dh, uint32_t dv,
                          uint32_t sd, const uint32_t sx[JXS_MAXC], const uint32_t sy[JXS_MAXC], uint32_t slice_h);

@@ -116,6 +116,9 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
 
     const int p = blockIdx.x;
     const int last = (p + 1 >= (int)cfg->np);
+    if (threadIdx.x == 0) s_err = *(volatile int*)status;
+    __syncthreads();
+    if (s_err) return; /* the precinct offsets could not be found */
     const uint8_t* src = bs + prec_off[p];
     if (threadIdx.x == 0) {
         s_err = 0;
@@ -579,9 +582,96 @@ __global__ void __launch_bounds__(512) inv_dwt_kernel(const __grid_constant__ Dw
     }
 }
 
+
+/* ------------------------------------------------------------------------ */
+/* Precinct offsets of a device-resident codestream                          */
+/* ------------------------------------------------------------------------ */
+DEV uint32_t be24(const uint8_t* p) { return ((uint32_t)p[0] << 16) | ((uint32_t)p[1] << 8) | p[2]; }
+
+/* One thread per slice: the slice is expected where the constant-bit-rate
+ * split of Lcod puts it (EncHandle.c:760-809); its precincts are found by
+ * following the 24-bit precinct lengths, and the walk must end exactly at
+ * the next slice (or at EOC).  Any mismatch raises *walk_bad. */
+__global__ void walk_slices_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t size,
+                                   uint32_t* __restrict__ prec_off, int* walk_bad) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= cfg->nslices) return;
+    if (cfg->max_slice_budget == 0) {
+        *walk_bad = 1;
+        return;
+    }
+    uint64_t off = cfg->slice_begin[s];
+    if (off + 6 > size || bs[off] != 0xff || bs[off + 1] != 0x20 || bs[off + 2] != 0 || bs[off + 3] != 4 ||
+        (((uint32_t)bs[off + 4] << 8) | bs[off + 5]) != s) {
+        atomicExch(walk_bad, 1);
+        return;
+    }
+    off += 6;
+    const uint32_t first = s * cfg->pps, n = (s + 1 == cfg->nslices) ? cfg->np - first : cfg->pps;
+    for (uint32_t i = 0; i < n; i++) {
+        if (off + cfg->prec_hdr_bytes > size) {
+            atomicExch(walk_bad, 1);
+            return;
+        }
+        const uint32_t lprc = be24(bs + off);
+        if (lprc > JXS_PREC_MAX_BYTES) {
+            atomicExch(walk_bad, 1);
+            return;
+        }
+        prec_off[first + i] = (uint32_t)off;
+        off += cfg->prec_hdr_bytes + lprc;
+    }
+    const int ok = (s + 1 < cfg->nslices) ? off == cfg->slice_begin[s + 1]
+                                          : (off + 2 <= size && bs[off] == 0xff && bs[off + 1] == 0x11);
+    if (!ok) atomicExch(walk_bad, 1);
+}
+
+/* Fallback when the prediction failed: one thread walks the whole codestream
+ * from the header (get_slice_size, DecThreadInit.c:35-131). */
+__global__ void walk_sequential_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t size,
+                                       uint32_t* __restrict__ prec_off, const int* walk_bad, int* status) {
+    if (!*walk_bad) return;
+    uint64_t off = cfg->hdr_len;
+    for (uint32_t s = 0; s < cfg->nslices; s++) {
+        if (off + 6 > size) {
+            JXS_STATUS_SET(status, JXS_E_DEC_SHORT);
+            return;
+        }
+        if (bs[off] != 0xff || bs[off + 1] != 0x20 || bs[off + 2] != 0 || bs[off + 3] != 4 ||
+            (((uint32_t)bs[off + 4] << 8) | bs[off + 5]) != s) {
+            JXS_STATUS_SET(status, JXS_E_DEC_BITSTREAM);
+            return;
+        }
+        off += 6;
+        const uint32_t first = s * cfg->pps, n = (s + 1 == cfg->nslices) ? cfg->np - first : cfg->pps;
+        for (uint32_t i = 0; i < n; i++) {
+            if (off + cfg->prec_hdr_bytes > size) {
+                JXS_STATUS_SET(status, JXS_E_DEC_SHORT);
+                return;
+            }
+            const uint32_t lprc = be24(bs + off);
+            if (lprc > JXS_PREC_MAX_BYTES) {
+                JXS_STATUS_SET(status, JXS_E_DEC_BITSTREAM);
+                return;
+            }
+            prec_off[first + i] = (uint32_t)off;
+            off += cfg->prec_hdr_bytes + lprc;
+        }
+    }
+    if (off + 2 > size) JXS_STATUS_SET(status, JXS_E_DEC_SHORT);
+    else if (bs[off] != 0xff || bs[off + 1] != 0x11) JXS_STATUS_SET(status, JXS_E_DEC_BITSTREAM);
+}
+
 /* ------------------------------------------------------------------------ */
 /* host-side launchers                                                       */
 /* ------------------------------------------------------------------------ */
+extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, const uint8_t* bs, uint32_t size, uint32_t* prec_off,
+                                       int* walk_bad, int* status, cudaStream_t st) {
+    walk_slices_kernel<<<(nslices + 127) / 128, 128, 0, st>>>(dcfg, bs, size, prec_off, walk_bad);
+    walk_sequential_kernel<<<1, 1, 0, st>>>(dcfg, bs, size, prec_off, walk_bad, status);
+    return cudaGetLastError();
+}
+
 extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, const uint32_t* prec_off, int16_t* coef,
                                          uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status, cudaStream_t st) {
     size_t smem = (size_t)cap_bytes + 16 + 2ull * cap_groups + 16 + 4ull * cap_groups;

@@ -30,6 +30,8 @@ extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const
                                        cudaStream_t st);
 extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, const uint32_t* prec_off, int16_t* coef,
                                          uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, const uint8_t* bs, uint32_t size, uint32_t* prec_off,
+                                       int* walk_bad, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_inv_dwt(const DwtLaunch* L, int vert, int nblocks, size_t smem, const jxs_band_t* bands,
                                           const int16_t* coef, int fq, int bw, int depth, cudaStream_t st);
 
@@ -451,6 +453,8 @@ struct DecSlot {
     int* status;
     int* status_h;
     uint32_t* prec_off_h;
+    uint8_t* hdr_h;       /* header of a device-resident codestream, checked at completion */
+    int hdr_check;
     cudaEvent_t tev[5];
     int timed;
 };
@@ -482,6 +486,7 @@ static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
     CK(cudaMalloc(&s->bs, s->bs_cap + 64));
     CK(cudaMalloc(&s->prec_off, (size_t)c->np * sizeof(uint32_t)));
     CK(cudaMallocHost(&s->prec_off_h, (size_t)c->np * sizeof(uint32_t)));
+    CK(cudaMallocHost(&s->hdr_h, sizeof(c->hdr)));
     CK(cudaMalloc(&s->coef, c->coef_total * sizeof(int16_t) + 64));
     for (uint32_t k = 0; k < c->nc; k++) {
         if (c->comp[k].dv == 2) {
@@ -509,6 +514,7 @@ static void dec_slot_free(DecSlot* s) {
     cudaFree(s->bs);
     cudaFree(s->prec_off);
     if (s->prec_off_h) cudaFreeHost(s->prec_off_h);
+    if (s->hdr_h) cudaFreeHost(s->hdr_h);
     cudaFree(s->coef);
     for (int k = 0; k < JXS_MAXC; k++) cudaFree(s->ll[k]);
     cudaFree(s->out_stage);
@@ -582,7 +588,16 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
     TMARK(0);
     CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
     const uint8_t* dbs = bs;
-    if (!jxs_gpu_is_device_ptr(bs)) {
+    s->hdr_check = 0;
+    if (!prec_off) {
+        /* device-resident codestream: header compared at completion, precinct
+         * offsets found on the GPU */
+        if (!jxs_gpu_is_device_ptr(bs) || size < c->hdr_len) return JXS_E_DEC_PTR;
+        CK(cudaMemcpyAsync(s->hdr_h, bs, c->hdr_len, cudaMemcpyDeviceToHost, st));
+        s->hdr_check = 1;
+        CK(cudaMemsetAsync(s->status + 1, 0, sizeof(int), st));
+        CK(jxs_launch_walk(d->dcfg, c->nslices, bs, size, s->prec_off, s->status + 1, s->status, st));
+    } else if (!jxs_gpu_is_device_ptr(bs)) {
         if (size > s->bs_cap) {
             CK(cudaStreamSynchronize(st));
             cudaFree(s->bs);
@@ -592,10 +607,12 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         CK(cudaMemcpyAsync(s->bs, bs, size, cudaMemcpyHostToDevice, st));
         dbs = s->bs;
     }
-    /* the previous use of prec_off_h by this slot has completed: slots are
-     * reused only after their completion was observed */
-    memcpy(s->prec_off_h, prec_off, sizeof(uint32_t) * c->np);
-    CK(cudaMemcpyAsync(s->prec_off, s->prec_off_h, sizeof(uint32_t) * c->np, cudaMemcpyHostToDevice, st));
+    if (prec_off) {
+        /* the previous use of prec_off_h by this slot has completed: slots are
+         * reused only after their completion was observed */
+        memcpy(s->prec_off_h, prec_off, sizeof(uint32_t) * c->np);
+        CK(cudaMemcpyAsync(s->prec_off, s->prec_off_h, sizeof(uint32_t) * c->np, cudaMemcpyHostToDevice, st));
+    }
     TMARK(1);
     CK(jxs_launch_unpack(d->dcfg, dbs, s->prec_off, s->coef, c->np, d->cap_bytes, d->cap_groups, s->status, st));
     TMARK(2);
@@ -697,6 +714,13 @@ extern "C" int32_t jxs_gpu_dec_wait(jxs_gpu_dec_t* d, int slot) {
         for (int i = 0; i < DEC_STAGES; i++) d->stage_ms[i] += ms[i];
         d->timed_frames++;
         s->timed = 0;
+    }
+    if (s->hdr_check) {
+        /* every header byte but Lcod (12..15) must match the stream's */
+        s->hdr_check = 0;
+        const jxs_cfg_t* c = &d->cfg;
+        if (memcmp(s->hdr_h, c->hdr, 12) != 0 || memcmp(s->hdr_h + 16, c->hdr + 16, c->hdr_len - 16) != 0)
+            return JXS_E_DEC_CONFIG;
     }
     return *s->status_h;
 }

@@ -36,7 +36,9 @@ int32_t jxs_gpu_enc_rc_results(jxs_gpu_enc_t* e, int slot, uint8_t* q, uint8_t* 
 jxs_gpu_dec_t* jxs_gpu_dec_create(const jxs_cfg_t* cfg, int nslots, int32_t* err);
 void jxs_gpu_dec_destroy(jxs_gpu_dec_t* d);
 /* Queues the decode of one frame whose precincts start at prec_off (host
- * array, cfg->np entries, from jxs_frame_bytes_walk). */
+ * array, cfg->np entries, from jxs_frame_bytes_walk).  With prec_off NULL the
+ * codestream must be in device memory: its precincts are located on the GPU
+ * and its header is compared with the stream's when the frame completes. */
 int32_t jxs_gpu_dec_submit(jxs_gpu_dec_t* d, int slot, const uint8_t* bs, uint32_t size, const uint32_t* prec_off,
                            void* const planes[4], const uint32_t strides[4]);
 int32_t jxs_gpu_dec_wait(jxs_gpu_dec_t* d, int slot);

@@ -198,6 +198,20 @@ def test_device_pointers(gpu):
     outs = [torch.zeros(p.shape, dtype=torch.uint8, device="cuda") for p in c["dec"]]
     assert dec.send(dev_bs.data_ptr(), [(t.data_ptr(), t.shape[1]) for t in outs], bs_size=len(c["bs"])) == 0
     r, _ = dec.get()
+    assert r == 0 and all(np.array_equal(t.cpu().numpy(), p) for t, p in zip(outs, c["dec"]))
+    # a device codestream of another configuration is reported when the frame completes
+    other = torch.from_numpy(SMALL["c2_422_10b"]["bs"]).cuda()
+    assert dec.send(other.data_ptr(), [(t.data_ptr(), t.shape[1]) for t in outs], bs_size=other.numel()) == 0
+    r, _ = dec.get()
+    assert r == gpu.E_DEC_CONFIG_CHANGE
+    # a truncated device codestream fails without touching memory past its end
+    cut = dev_bs[: len(c["bs"]) // 2].clone()
+    assert dec.send(cut.data_ptr(), [(t.data_ptr(), t.shape[1]) for t in outs], bs_size=cut.numel()) == 0
+    r, _ = dec.get()
+    assert r != 0
+    # and the decoder still works afterwards
+    assert dec.send(dev_bs.data_ptr(), [(t.data_ptr(), t.shape[1]) for t in outs], bs_size=len(c["bs"])) == 0
+    r, _ = dec.get()
     dec.close()
     assert r == 0 and all(np.array_equal(t.cpu().numpy(), p) for t, p in zip(outs, c["dec"]))
 
