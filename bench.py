@@ -48,11 +48,13 @@ METRIC = "encode+decode Gpix/s (bit-exact), 3840x2160 4:2:2 10-bit bpp3"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=8, help="frames encoded and decoded per step")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget (0: not measured)")
+    ap.add_argument("--seq-frames", type=int, default=SEQ_FRAMES,
+                    help="distinct frames of the stream cycled through (each 33 MB; 4 or more keep inputs above L2)")
     return ap.parse_args()
 
 
@@ -198,7 +200,8 @@ def run_ours(args, rank, world, local):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=dev)
-    frames = make_frames(SEQ_FRAMES)
+    nseq = max(4, args.seq_frames)
+    frames = make_frames(nseq)
     F = args.frames
     enc = jxs.Encoder(W, H, DEPTH, jxs.FMT_YUV422, BPP)
     lcod = enc.frame_bytes
@@ -217,16 +220,30 @@ def run_ours(args, rank, world, local):
         return [(t.data_ptr(), t.shape[1]) for t in ts]
 
     def step(s):
-        base = (s * F) % SEQ_FRAMES
+        # every call is queued on one stream: decode i follows encode i, and
+        # results are collected only when a codec's queue is full
+        base = (s * F) % nseq
+        pend = [0, 0]
+
+        def submit(codec, k, *a, **kw):
+            while True:
+                r = codec.send(*a, blocking=False, **kw)
+                if r != jxs.E_EMPTY_QUEUE:
+                    assert r == 0, hex(r)
+                    pend[k] += 1
+                    return
+                r, _ = codec.get()
+                assert r == 0, hex(r)
+                pend[k] -= 1
+
         for i in range(F):
-            r = enc.send(planes_of(d_in[(base + i) % SEQ_FRAMES]), d_bs[i].data_ptr(), out_cap=lcod + 64)
-            assert r == 0
-            r, f = enc.get()
-            assert r == 0, hex(r)
-            r = dec.send(d_bs[i].data_ptr(), planes_of(d_out[i]), bs_size=lcod)
-            assert r == 0
-            r, _ = dec.get()
-            assert r == 0, hex(r)
+            submit(enc, 0, planes_of(d_in[(base + i) % nseq]), d_bs[i].data_ptr(), out_cap=lcod + 64)
+            submit(dec, 1, d_bs[i].data_ptr(), planes_of(d_out[i]), bs_size=lcod)
+        for k, codec in ((0, enc), (1, dec)):
+            while pend[k]:
+                r, _ = codec.get()
+                assert r == 0, hex(r)
+                pend[k] -= 1
 
     for w in range(max(args.warmup, 1)):
         step(w)
@@ -262,10 +279,10 @@ def run_ours(args, rank, world, local):
     import oracle_lib as O
 
     O.build_oracle()
-    last_base = ((args.warmup + args.steps - 1) * F) % SEQ_FRAMES
+    last_base = ((args.warmup + args.steps - 1) * F) % nseq
     for i in (0, F - 1):
         err, want = O.oracle_encode(O.make_params(W, H, DEPTH, 3, BPP, threads=os.cpu_count() or 1),
-                                    frames[(last_base + i) % SEQ_FRAMES])
+                                    frames[(last_base + i) % nseq])
         assert err == 0 and np.array_equal(d_bs[i][:lcod].cpu().numpy(), want), "codestream differs from the oracle"
         err, want_planes = O.oracle_decode(want, threads=os.cpu_count() or 1)
         assert err == 0 and all(np.array_equal(t.cpu().numpy(), w) for t, w in zip(d_out[i], want_planes)), \
@@ -327,7 +344,7 @@ def run_ours(args, rank, world, local):
     out_bytes = in_bytes
     # per-frame latency through the API, one frame at a time (no queueing)
     lat_frame = []
-    for i in range(min(20, SEQ_FRAMES)):
+    for i in range(20):
         ts = time.perf_counter()
         assert enc.send(h_in[i % F], h_bs[0]) == 0
         r, _ = enc.get()
@@ -360,7 +377,7 @@ def run_ours(args, rank, world, local):
 
     # ---- CPU baseline (oracle on the host cores), rank 0 only
     cpu = None
-    if rank == 0:
+    if rank == 0 and args.cpu_seconds > 0:
         threads = os.cpu_count() or 1
         n, el = cpu_codec_time(frames[:4], {}, args.cpu_seconds, threads)
         cpu = {"value": n * W * H / el / 1e9, "unit": "Gpix/s", "cores": threads, "kind": "port",
@@ -371,7 +388,7 @@ def run_ours(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": "Gpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic (seeded, integer-only generator; no dataset)",
-        "config": {"workload": WORKLOAD, "frames_per_step": F, "l2": "inputs 33 MB/frame cycling over 60 frames (> L2)",
+        "config": {"workload": WORKLOAD, "frames_per_step": F, "l2": "inputs 33 MB/frame cycling over %d frames (> L2)" % nseq,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_val, "unit": "Gpix/s", "h2d_bytes_per_step": F * (in_bytes + lcod),
                 "d2h_bytes_per_step": F * (lcod + out_bytes), "p50_step_ms": 1e3 * statistics.median(lat),
