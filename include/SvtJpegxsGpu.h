@@ -47,6 +47,33 @@ PREFIX_API uint64_t svt_jpeg_xs_gpu_decoder_read_timing(svt_jpeg_xs_decoder_api_
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_rc_results(svt_jpeg_xs_encoder_api_t* enc_api, uint8_t* quantization,
                                                                 uint8_t* refinement, uint32_t count);
 
+/* Size in bytes (header through EOC) and precinct byte offsets of the frame
+ * that starts at dev_bitstream, a device pointer of the current device, read
+ * with the configuration the decoder was initialised with.  No counterpart in
+ * the reference API: svt_jpeg_xs_decoder_get_single_frame_size answers the
+ * size question for host buffers.
+ *
+ * This entry point allocates nothing, on the device or the host. It is for
+ * callers that may not allocate while they run: a receive thread that gets
+ * codestreams straight into GPU memory at line rate, or a server held to a
+ * device-memory budget fixed at admission. Its scratch is a fixed
+ * file-scope device array, so:
+ *   - frames of more than 4096 precincts are rejected with
+ *     SvtJxsErrorBadParameter (and a message on stderr);
+ *   - calls are serialised process-wide, because overlapping walks would
+ *     race on the shared scratch;
+ *   - the first call on a device resolves the scratch's address and may load
+ *     the module, so make it before any stream capture begins.
+ * precinct_offsets may be NULL. Otherwise precinct_capacity must be at least
+ * the frame's precinct count, and the offsets are written there. The call
+ * runs on cuda_stream (NULL: the default stream) and returns when the results
+ * are on the host. A header that differs from the decoder's (Lcod aside)
+ * returns SvtJxsErrorDecoderConfigChange. */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_locate_frame(svt_jpeg_xs_decoder_api_t* dec_api, const void* dev_bitstream,
+                                                                  uint32_t bitstream_size, uint32_t* frame_size,
+                                                                  uint32_t* precinct_offsets, uint32_t precinct_capacity,
+                                                                  void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,6 +15,7 @@
 #include <string.h>
 
 #include "SvtJpegxsDec.h"
+#include "SvtJpegxsGpu.h"
 #include "jxs_core.h"
 #include "jxs_gpu.h"
 #include "jxs_queue.h"
@@ -414,4 +415,14 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_set_timing(svt_jpeg_xs_deco
 PREFIX_API uint64_t svt_jpeg_xs_gpu_decoder_read_timing(svt_jpeg_xs_decoder_api_t* dec_api, double* stage_ms, uint32_t n) {
     if (!dec_api || !dec_api->private_ptr || !stage_ms) return 0;
     return jxs_gpu_dec_read_timing(((dec_prv_t*)dec_api->private_ptr)->gpu, stage_ms, (int)n);
+}
+
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_locate_frame(svt_jpeg_xs_decoder_api_t* dec_api, const void* dev_bitstream,
+                                                                  uint32_t bitstream_size, uint32_t* frame_size,
+                                                                  uint32_t* precinct_offsets, uint32_t precinct_capacity,
+                                                                  void* cuda_stream) {
+    if (!dec_api || !dec_api->private_ptr || !dev_bitstream || !frame_size) return SvtJxsErrorDecoderInvalidPointer;
+    dec_prv_t* p = (dec_prv_t*)dec_api->private_ptr;
+    return (SvtJxsErrorType_t)jxs_gpu_dec_locate_noalloc(p->gpu, dev_bitstream, bitstream_size, frame_size, precinct_offsets,
+                                                         precinct_capacity, cuda_stream);
 }

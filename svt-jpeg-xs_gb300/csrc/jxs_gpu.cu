@@ -527,6 +527,12 @@ static void dec_slot_free(DecSlot* s) {
     memset(s, 0, sizeof(*s));
 }
 
+extern "C" const jxs_cfg_t* jxs_gpu_dec_cfg(jxs_gpu_dec_t* d, const jxs_cfg_t** dev_cfg) {
+    if (!d) return NULL;
+    if (dev_cfg) *dev_cfg = d->dcfg;
+    return &d->cfg;
+}
+
 extern "C" void jxs_gpu_dec_destroy(jxs_gpu_dec_t* d) {
     if (!d) return;
     for (int i = 0; i < d->nslots; i++) dec_slot_free(&d->slot[i]);

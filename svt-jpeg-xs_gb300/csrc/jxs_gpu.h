@@ -58,6 +58,15 @@ uint64_t jxs_gpu_dec_read_timing(jxs_gpu_dec_t* d, double* ms, int n);
 
 /* 1 if p is memory of this process's current CUDA device. */
 int jxs_gpu_is_device_ptr(const void* p);
+
+/* Host and device copies of a decoder's configuration. */
+const jxs_cfg_t* jxs_gpu_dec_cfg(jxs_gpu_dec_t* d, const jxs_cfg_t** dev_cfg);
+
+/* Frame size and precinct offsets of a device-resident codestream, with no
+ * allocation (jxs_noalloc.cu).  prec_off may be NULL; otherwise it receives
+ * cfg->np offsets and cap must be at least that. */
+int32_t jxs_gpu_dec_locate_noalloc(jxs_gpu_dec_t* d, const void* dev_bs, uint32_t size, uint32_t* frame_size,
+                                   uint32_t* prec_off, uint32_t cap, void* stream);
 /* Page-locked host allocation (falls back to malloc without a GPU). */
 void* jxs_gpu_host_alloc(size_t n);
 void jxs_gpu_host_free(void* p);

@@ -138,6 +138,9 @@ def lib():
         L.svt_jpeg_xs_gpu_decoder_read_timing.argtypes = [ctypes.POINTER(DecoderApi), ctypes.POINTER(ctypes.c_double), u32]
         L.svt_jpeg_xs_gpu_decoder_read_timing.restype = ctypes.c_uint64
         L.svt_jpeg_xs_gpu_encoder_rc_results.argtypes = [ctypes.POINTER(EncoderApi), ctypes.c_void_p, ctypes.c_void_p, u32]
+        L.svt_jpeg_xs_gpu_decoder_locate_frame.argtypes = [ctypes.POINTER(DecoderApi), ctypes.c_void_p, u32, ctypes.POINTER(u32),
+                                                          ctypes.c_void_p, u32, ctypes.c_void_p]
+        L.svt_jpeg_xs_gpu_decoder_locate_frame.restype = u32
         L.svt_jpeg_xs_image_buffer_alloc.argtypes = [ctypes.POINTER(ImageConfig)]
         L.svt_jpeg_xs_image_buffer_alloc.restype = ctypes.POINTER(ImageBuffer)
         L.svt_jpeg_xs_image_buffer_free.argtypes = [ctypes.POINTER(ImageBuffer)]
