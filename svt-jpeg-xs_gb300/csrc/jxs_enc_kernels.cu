@@ -1,11 +1,6 @@
 /*
- * Encoder kernels for sm_103a.
+ * Encoder kernels for sm_103a (the forward transform is in jxs_fwd_dwt.cu).
  *
- *  fwd_dwt_kernel   input scaling + one vertical 5/3 lifting level (in
- *                   registers, column-parallel) + horizontal lifting of the
- *                   produced rows (in shared memory) + for the last vertical
- *                   level all horizontal-only levels; writes 16-bit
- *                   sign-magnitude coefficients and their GCLIs.
  *  rc_cost_kernel   per precinct row: GCLI histograms and the byte cost of
  *                   every (quantization, refinement) candidate.
  *  rc_select_kernel per slice: the reference's sequential budget carry and
@@ -24,193 +19,6 @@
 #include "jxs_kernels.cuh"
 
 #define DEV __device__ __forceinline__
-
-/* ------------------------------------------------------------------------ */
-/* shared helpers                                                            */
-/* ------------------------------------------------------------------------ */
-DEV int mirror(int i, int n) {
-    /* symmetric extension without repeating the edge sample */
-    if (i < 0) i = -i;
-    if (i >= n) i = 2 * (n - 1) - i;
-    return i;
-}
-
-DEV int32_t load_src(const DwtJob& J, int row, int x) {
-    const int sh = 20 - J.depth;
-    const int32_t off = 1 << 19;
-    switch (J.src_kind) {
-    case SRC_I32: return ((const int32_t*)J.src)[(long long)row * J.src_pitch + x];
-    case SRC_U8: return ((int32_t)((uint32_t)((const uint8_t*)J.src)[(long long)row * J.src_pitch + x] << sh)) - off;
-    case SRC_U16: {
-        uint32_t v = ((const uint16_t*)J.src)[(long long)row * J.src_pitch + x] & ((1u << J.depth) - 1);
-        return (int32_t)(v << sh) - off;
-    }
-    case SRC_PK8:
-        return ((int32_t)((uint32_t)((const uint8_t*)J.src)[(long long)row * J.src_pitch + 3 * x + J.chan] << sh)) - off;
-    default: {
-        uint32_t v = ((const uint16_t*)J.src)[(long long)row * J.src_pitch + 3 * x + J.chan] & ((1u << J.depth) - 1);
-        return (int32_t)(v << sh) - off;
-    }
-    }
-}
-
-/* image_shift_c (NltEnc.c:12-31): Fq = 8 fractional bits rounded off, no -0 */
-DEV uint32_t to_sm(int32_t v) {
-    if (v >= 0) return (uint32_t)((v + 128) >> 8);
-    uint32_t m = (uint32_t)((-v + 128) >> 8);
-    return m ? (m | 0x8000u) : 0u;
-}
-
-/* Forward 5/3 lifting of rows held in shared memory (Dwt.c:15-40), for all
- * rows of a block at once.  Elements of a row sit at stride S; n elements. */
-template <typename RowFn>
-DEV void fwd_h_level(RowFn row, int nrows, int n, int S) {
-    const int n2 = n >> 1, n1 = (n + 1) >> 1;
-    for (int t = threadIdx.x; t < nrows * n2; t += blockDim.x) {
-        int r = t / n2, j = t - r * n2;
-        int32_t* p = row(r);
-        int32_t a = p[S * 2 * j];
-        int32_t c = (2 * j + 2 < n) ? p[S * (2 * j + 2)] : a;
-        p[S * (2 * j + 1)] -= (a + c) >> 1;
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < nrows * n1; t += blockDim.x) {
-        int r = t / n1, i = t - r * n1;
-        int32_t* p = row(r);
-        int jp = min(max(i - 1, 0), n2 - 1), jc = min(i, n2 - 1);
-        p[S * 2 * i] += (p[S * (2 * jp + 1)] + p[S * (2 * jc + 1)] + 2) >> 2;
-    }
-    __syncthreads();
-}
-
-/* Writes `n` elements (at p[o + S * k]) of one band row as sign-magnitude
- * coefficients, 4 per thread, with the GCLI of each 4-group
- * (gc_precinct_stage_scalar_c, GcStageProcess.c:22-68). */
-DEV void emit_band_row(const int32_t* p, int o, int S, int n, const jxs_band_t& bd, int brow, uint16_t* coef, uint8_t* gcli) {
-    uint16_t* crow = coef + bd.coef_off + (uint64_t)brow * bd.pitch;
-    uint8_t* grow = gcli + bd.gcli_off + (uint64_t)brow * bd.gpitch;
-    const int groups = (n + 3) >> 2;
-    for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-        uint32_t c[4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            int idx = 4 * g + k;
-            c[k] = idx < n ? to_sm(p[o + S * idx]) : 0u;
-        }
-        *(uint2*)(crow + 4 * g) = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
-        uint32_t m = (c[0] | c[1] | c[2] | c[3]) & 0x7fffu;
-        grow[g] = (uint8_t)(m ? 32 - __clz(m) : 0);
-    }
-}
-
-/* ------------------------------------------------------------------------ */
-/* Forward transform, one level per launch.                                  */
-/* ------------------------------------------------------------------------ */
-template <bool VERT>
-__global__ void __launch_bounds__(512) fwd_dwt_kernel(const __grid_constant__ DwtLaunch L, const jxs_band_t* __restrict__ bands,
-                                                      uint16_t* __restrict__ coef, uint8_t* __restrict__ gcli) {
-    extern __shared__ int32_t sm[];
-    int j = 0;
-    while (j + 1 < L.njobs && (int)blockIdx.x >= L.job[j + 1].first_block) j++;
-    const DwtJob& J = L.job[j];
-    const int rb = blockIdx.x - J.first_block;
-    const int w = J.w, h = J.h, sp = J.smem_pitch;
-
-    if (VERT) {
-        const int n1 = (h + 1) >> 1, n2 = h >> 1;
-        const int r0 = rb * J.R;
-        const int rc = min(J.R, n1 - r0);
-        const int hc = max(0, min(J.R, n2 - r0));
-        int32_t* Ls = sm;
-        int32_t* Hs = sm + J.R * sp;
-        /* vertical lifting, one column per thread (Dwt.c:337-398 in frame form) */
-        for (int x = threadIdx.x; x < w; x += blockDim.x) {
-            const int jp = min(max(r0 - 1, 0), n2 - 1);
-            int32_t hprev;
-            {
-                int32_t a = load_src(J, 2 * jp, x), b = load_src(J, 2 * jp + 1, x), c = load_src(J, mirror(2 * jp + 2, h), x);
-                hprev = b - ((a + c) >> 1);
-            }
-            int32_t xe = load_src(J, 2 * r0, x);
-            for (int k = 0; k < rc; k++) {
-                const int i = r0 + k;
-                int32_t hcur, xn = 0;
-                if (i < n2) {
-                    int32_t xo = load_src(J, 2 * i + 1, x);
-                    xn = load_src(J, mirror(2 * i + 2, h), x);
-                    hcur = xo - ((xe + xn) >> 1);
-                    Hs[k * sp + x] = hcur;
-                } else {
-                    hcur = hprev;
-                }
-                Ls[k * sp + x] = xe + ((hprev + hcur + 2) >> 2);
-                hprev = hcur;
-                xe = xn;
-            }
-        }
-        __syncthreads();
-        auto all_rows = [&](int r) { return r < rc ? Ls + r * sp : Hs + (r - rc) * sp; };
-        fwd_h_level(all_rows, rc + hc, w, 1);
-        const int w1 = (w + 1) >> 1, w2 = w >> 1;
-        /* horizontal-only levels on the low rows */
-        int m = w1, S = 2;
-        if (J.last) {
-            auto lrows = [&](int r) { return Ls + r * sp; };
-            for (int e = 0; e < J.nh; e++) {
-                fwd_h_level(lrows, rc, m, S);
-                m = (m + 1) >> 1;
-                S <<= 1;
-            }
-        }
-        /* outputs */
-        for (int k = 0; k < hc; k++) {
-            emit_band_row(Hs + k * sp, 0, 2, w1, bands[J.b_lh], r0 + k, coef, gcli);
-            emit_band_row(Hs + k * sp, 1, 2, w2, bands[J.b_hh], r0 + k, coef, gcli);
-        }
-        for (int k = 0; k < rc; k++) {
-            const int32_t* p = Ls + k * sp;
-            emit_band_row(p, 1, 2, w2, bands[J.b_hl], r0 + k, coef, gcli);
-            if (J.last) {
-                int mm = w1, SS = 2;
-                for (int e = 0; e < J.nh; e++) {
-                    emit_band_row(p, SS, 2 * SS, mm >> 1, bands[J.b_hf[e]], r0 + k, coef, gcli);
-                    mm = (mm + 1) >> 1;
-                    SS <<= 1;
-                }
-                emit_band_row(p, 0, SS, mm, bands[J.b_ll], r0 + k, coef, gcli);
-            } else {
-                int32_t* dst = J.ll + (long long)(r0 + k) * J.ll_pitch;
-                for (int x = threadIdx.x; x < w1; x += blockDim.x) dst[x] = p[2 * x];
-            }
-        }
-    } else {
-        /* no vertical level: horizontal-only levels straight from the input */
-        const int r0 = rb * J.R;
-        const int rc = min(J.R, h - r0);
-        for (int t = threadIdx.x; t < rc * w; t += blockDim.x) {
-            int k = t / w, x = t - k * w;
-            sm[k * sp + x] = load_src(J, r0 + k, x);
-        }
-        __syncthreads();
-        auto rows = [&](int r) { return sm + r * sp; };
-        int m = w, S = 1;
-        for (int e = 0; e < J.nh; e++) {
-            fwd_h_level(rows, rc, m, S);
-            m = (m + 1) >> 1;
-            S <<= 1;
-        }
-        for (int k = 0; k < rc; k++) {
-            const int32_t* p = sm + k * sp;
-            int mm = w, SS = 1;
-            for (int e = 0; e < J.nh; e++) {
-                emit_band_row(p, SS, 2 * SS, mm >> 1, bands[J.b_hf[e]], r0 + k, coef, gcli);
-                mm = (mm + 1) >> 1;
-                SS <<= 1;
-            }
-            emit_band_row(p, 0, SS, mm, bands[J.b_ll], r0 + k, coef, gcli);
-        }
-    }
-}
 
 /* ------------------------------------------------------------------------ */
 /* Rate control                                                              */
@@ -941,20 +749,6 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
 /* ------------------------------------------------------------------------ */
 /* host-side launchers                                                       */
 /* ------------------------------------------------------------------------ */
-extern "C" cudaError_t jxs_launch_fwd_dwt(const DwtLaunch* L, int vert, int nblocks, size_t smem, const jxs_band_t* bands,
-                                          uint16_t* coef, uint8_t* gcli, cudaStream_t st) {
-    static size_t configured[2] = {0, 0};
-    if (smem > configured[vert]) {
-        cudaError_t e = vert ? cudaFuncSetAttribute(fwd_dwt_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                             : cudaFuncSetAttribute(fwd_dwt_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured[vert] = smem;
-    }
-    if (vert) fwd_dwt_kernel<true><<<nblocks, 512, smem, st>>>(*L, bands, coef, gcli);
-    else fwd_dwt_kernel<false><<<nblocks, 512, smem, st>>>(*L, bands, coef, gcli);
-    return cudaGetLastError();
-}
-
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
                                      PrecRC* rc, int* status, cudaStream_t st) {
     rc_cost_kernel<<<np, 256, 0, st>>>(dcfg, gcli, cost);

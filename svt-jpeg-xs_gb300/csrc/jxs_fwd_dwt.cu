@@ -1,0 +1,341 @@
+/*
+ * Forward 5/3 wavelet transform for sm_103a.
+ *
+ *  fwd_v_kernel  one vertical level and the horizontal level that follows
+ *                it, on a tile of FV_ROWPAIRS row pairs x FV_COLS columns of
+ *                one component.  Vertical lifting runs in registers, one
+ *                thread per column pair.  The resulting low and high rows go
+ *                to shared memory with a 2-column halo on each side.  Each
+ *                row is then lifted horizontally by one warp: lanes hold 4
+ *                consecutive samples and exchange the neighbours they need
+ *                with shuffles.  Outputs: the HL, LH and HH bands as 16-bit
+ *                sign-magnitude coefficients with the GCLI of every
+ *                4-coefficient group, and the int32 LL plane for the next
+ *                level.
+ *  fwd_h_kernel  the horizontal-only levels below the last vertical level
+ *                (or all levels of a component without vertical
+ *                decomposition): one warp per row, every level in shared
+ *                memory, the high band of each level and the final LL band
+ *                emitted as coefficients + GCLIs.
+ *
+ * Arithmetic (bit-exact with the reference):
+ *  - input scaling: v = ((x & (2^d - 1)) << (20 - d)) - 2^19 (NltEnc.c:33-72);
+ *  - lifting: d[i] = x[2i+1] - ((x[2i] + x[2i+2]) >> 1),
+ *    s[i] = x[2i] + ((d[i-1] + d[i] + 2) >> 2), with whole-sample symmetric
+ *    extension at both ends (Dwt.c:15-40 horizontally, :337-398 vertically;
+ *    the reference's edge special cases are what the mirrored samples give);
+ *  - vertical before horizontal at every level, the low band of a level
+ *    being the next level's input (Dwt.c:550-1142, frame form);
+ *  - sign-magnitude with Fq = 8: m = (|v| + 128) >> 8, no negative zero
+ *    (NltEnc.c:12-31);
+ *  - GCLI = bit length of the OR of a group's magnitudes
+ *    (GcStageProcess.c:42-68).
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "jxs_core.h"
+#include "jxs_kernels.cuh"
+
+#define DEV __device__ __forceinline__
+#define FULL 0xffffffffu
+
+/* ------------------------------------------------------------------------ */
+/* helpers                                                                   */
+/* ------------------------------------------------------------------------ */
+/* whole-sample symmetric extension of index i into [0, n) */
+DEV int mirror_idx(int i, int n) {
+    if (n == 1) return 0;
+    const int p = 2 * (n - 1);
+    i %= p;
+    if (i < 0) i += p;
+    return i < n ? i : p - i;
+}
+
+DEV uint32_t to_sm(int32_t v) {
+    if (v >= 0) return (uint32_t)((v + 128) >> 8);
+    const uint32_t m = (uint32_t)((-v + 128) >> 8);
+    return m ? (m | 0x8000u) : 0u;
+}
+
+template <int SRC>
+DEV int32_t scale_in(uint32_t raw, int depth) {
+    if (SRC == SRC_I32) return (int32_t)raw;
+    const uint32_t mask = (1u << depth) - 1u;
+    return (int32_t)((raw & mask) << (20 - depth)) - (1 << 19);
+}
+
+/* one sample of the level input at (row y, column x), both in range */
+template <int SRC>
+DEV int32_t load1(const void* src, long long pitch, int chan, int depth, int y, int x) {
+    const long long row = (long long)y * pitch;
+    if (SRC == SRC_I32) return ((const int32_t*)src)[row + x];
+    if (SRC == SRC_U8) return scale_in<SRC>(((const uint8_t*)src)[row + x], depth);
+    if (SRC == SRC_U16) return scale_in<SRC>(((const uint16_t*)src)[row + x], depth);
+    if (SRC == SRC_PK8) return scale_in<SRC>(((const uint8_t*)src)[row + 3 * x + chan], depth);
+    return scale_in<SRC>(((const uint16_t*)src)[row + 3 * x + chan], depth);
+}
+
+/* two horizontally adjacent samples (x even, x + 1 < width) with one load
+ * where the layout allows it */
+template <int SRC>
+DEV void load2(const void* src, long long pitch, int chan, int depth, int y, int x, bool vec, int32_t& a, int32_t& b) {
+    const long long row = (long long)y * pitch;
+    if (vec && SRC == SRC_I32) {
+        const int2 v = *(const int2*)((const int32_t*)src + row + x);
+        a = v.x;
+        b = v.y;
+    } else if (vec && SRC == SRC_U16) {
+        const uint32_t v = *(const uint32_t*)((const uint16_t*)src + row + x);
+        a = scale_in<SRC>(v & 0xffffu, depth);
+        b = scale_in<SRC>(v >> 16, depth);
+    } else if (vec && SRC == SRC_U8) {
+        const uint32_t v = *(const uint16_t*)((const uint8_t*)src + row + x);
+        a = scale_in<SRC>(v & 0xffu, depth);
+        b = scale_in<SRC>(v >> 8, depth);
+    } else {
+        a = load1<SRC>(src, pitch, chan, depth, y, x);
+        b = load1<SRC>(src, pitch, chan, depth, y, x + 1);
+    }
+}
+
+/* Writes coefficients j, j+1 (j even) of row `row` of band bd, and, from the
+ * even lane of each lane pair, the GCLI of the 4-group the pair covers.
+ * Values at j >= width are written as zero; nothing past the last group. */
+DEV void emit2(const jxs_band_t& bd, int row, int j, int32_t a, int32_t b, uint16_t* __restrict__ coef,
+               uint8_t* __restrict__ gcli) {
+    const int w = (int)bd.w;
+    const uint32_t ca = j < w ? to_sm(a) : 0u, cb = j + 1 < w ? to_sm(b) : 0u;
+    uint32_t m = (ca | cb) & 0x7fffu;
+    m |= __shfl_xor_sync(FULL, m, 1);
+    if (j < 4 * (int)bd.gcli_w && j >= 0) {
+        *(uint32_t*)(coef + bd.coef_off + (uint64_t)row * bd.pitch + j) = ca | (cb << 16);
+        if (!(j & 2)) gcli[bd.gcli_off + (uint64_t)row * bd.gpitch + (j >> 2)] = (uint8_t)(m ? 32 - __clz(m) : 0);
+    }
+}
+
+/* One horizontal lifting pass of a row held in shared memory, by one warp.
+ * x points at sample 0 of the pass; x[-2], x[-1] and the samples past the
+ * last pair needed hold the (mirrored or neighbouring-tile) halo.  `npairs`
+ * output pairs (s[j], d[j]) for j in [0, npairs) are produced, npairs a
+ * multiple of 2; lane l of iteration it owns j = 64*it + 2l and 2l + 1.
+ * Reads x[-2 .. 2*npairs + 3]; outputs past the valid width may depend on
+ * samples past x[2*npairs + 1] and are discarded by the caller.
+ * x must be 16-byte aligned. */
+template <typename Out>
+DEV void warp_lift_fwd(const int32_t* x, int npairs, Out out) {
+    const int lane = threadIdx.x & 31;
+    /* d[-1] from the halo */
+    int32_t carry = x[-1] - ((x[-2] + x[0]) >> 1);
+    for (int base = 0; base < npairs; base += 64) {
+        const int j = base + 2 * lane;
+        int4 v = make_int4(0, 0, 0, 0);
+        /* the lane just past the last pair still loads: its first sample is
+         * the right neighbour of the previous lane */
+        if (j <= npairs) v = *(const int4*)(x + 2 * j);
+        int32_t nxt = __shfl_down_sync(FULL, v.x, 1);
+        if (lane == 31) nxt = j < npairs ? x[2 * j + 4] : 0;
+        const int32_t d0 = v.y - ((v.x + v.z) >> 1);
+        const int32_t d1 = v.w - ((v.z + nxt) >> 1);
+        int32_t dm = __shfl_up_sync(FULL, d1, 1);
+        if (lane == 0) dm = carry;
+        carry = __shfl_sync(FULL, d1, 31);
+        const int32_t s0 = v.x + ((dm + d0 + 2) >> 2);
+        const int32_t s1 = v.z + ((d0 + d1 + 2) >> 2);
+        out(j, s0, s1, d0, d1);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* vertical level + one horizontal level                                     */
+/* ------------------------------------------------------------------------ */
+#define FV_THREADS 128
+#define FV_COLS (2 * FV_THREADS)          /* output columns of the level input per tile */
+#define FV_ROWPAIRS 8
+#define FV_SROW (FV_COLS + 8)             /* shared row: 4 front words (2 pad, 2 halo), FV_COLS, 2 halo, 2 pad */
+
+template <int SRC>
+__global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant__ FwdVLaunch L, const jxs_band_t* __restrict__ bands,
+                                                           uint16_t* __restrict__ coef, uint8_t* __restrict__ gcli) {
+    __shared__ __align__(16) int32_t sL[FV_ROWPAIRS][FV_SROW];
+    __shared__ __align__(16) int32_t sH[FV_ROWPAIRS][FV_SROW];
+    int jb = 0;
+    while (jb + 1 < L.njobs && (int)blockIdx.x >= L.job[jb + 1].first_block) jb++;
+    const FwdVJob& J = L.job[jb];
+    const int t = blockIdx.x - J.first_block;
+    const int ty = t / J.col_tiles, tx = t - ty * J.col_tiles;
+    const int w = J.w, h = J.h, depth = L.depth;
+    const int n1 = (h + 1) >> 1, n2 = h >> 1;
+    const int r0 = ty * FV_ROWPAIRS;
+    const int c0 = tx * FV_COLS;
+    const int rc = min(FV_ROWPAIRS, n1 - r0); /* low rows of this tile */
+    const int hc = max(0, min(FV_ROWPAIRS, n2 - r0));
+
+    /* output pairs j in [c0/2, c0/2 + npairs) of the level's bands; lifting
+     * them reads input columns c0 - 2 .. c0 + 2 npairs */
+    const int w1 = (w + 1) >> 1;
+    const int npairs = min(FV_COLS / 2, ((w1 - c0 / 2) + 1) & ~1);
+    const int jc = c0 >> 1;
+    /* vertical lifting: column pair cp covers input columns c0 - 2 + 2cp, +1 */
+    const int ncp = npairs + 2;
+    int ys[2 * FV_ROWPAIRS + 3];
+#pragma unroll
+    for (int k = 0; k < 2 * FV_ROWPAIRS + 3; k++) ys[k] = mirror_idx(2 * r0 - 2 + k, h);
+    for (int cp = threadIdx.x; cp < ncp; cp += FV_THREADS) {
+        const int xa = c0 - 2 + 2 * cp;
+        const bool inside = xa >= 0 && xa + 1 < w;
+        const int ma = mirror_idx(xa, w), mb = mirror_idx(xa + 1, w);
+        int32_t a[2 * FV_ROWPAIRS + 3], b[2 * FV_ROWPAIRS + 3];
+#pragma unroll
+        for (int k = 0; k < 2 * FV_ROWPAIRS + 3; k++) {
+            if (inside) {
+                load2<SRC>(J.src, J.src_pitch, J.chan, depth, ys[k], xa, J.vec, a[k], b[k]);
+            } else {
+                a[k] = load1<SRC>(J.src, J.src_pitch, J.chan, depth, ys[k], ma);
+                b[k] = load1<SRC>(J.src, J.src_pitch, J.chan, depth, ys[k], mb);
+            }
+        }
+        int32_t hpa = a[1] - ((a[0] + a[2]) >> 1), hpb = b[1] - ((b[0] + b[2]) >> 1);
+#pragma unroll
+        for (int k = 0; k < FV_ROWPAIRS; k++) {
+            const int e = 2 + 2 * k; /* x[2i] of pair r0 + k */
+            const int32_t ha = a[e + 1] - ((a[e] + a[e + 2]) >> 1), hb = b[e + 1] - ((b[e] + b[e + 2]) >> 1);
+            const int32_t la = a[e] + ((hpa + ha + 2) >> 2), lb = b[e] + ((hpb + hb + 2) >> 2);
+            *(int2*)&sL[k][2 + 2 * cp] = make_int2(la, lb);
+            *(int2*)&sH[k][2 + 2 * cp] = make_int2(ha, hb);
+            hpa = ha;
+            hpb = hb;
+        }
+    }
+    __syncthreads();
+
+    /* horizontal lifting, one warp per row; the tile's output pairs are
+     * j in [c0/2, c0/2 + npairs) of the level's bands */
+    const int warp = threadIdx.x >> 5;
+    const jxs_band_t bhl = bands[J.b_hl], blh = bands[J.b_lh], bhh = bands[J.b_hh];
+    for (int r = warp; r < rc + hc; r += FV_THREADS / 32) {
+        if (r < rc) {
+            const int row = r0 + r;
+            int32_t* ll = J.ll ? J.ll + (long long)row * J.ll_pitch : nullptr;
+            const int lw = w1;
+            warp_lift_fwd(&sL[r][4], npairs, [&](int j, int32_t s0, int32_t s1, int32_t d0, int32_t d1) {
+                const int jj = jc + j;
+                emit2(bhl, row, jj, d0, d1, coef, gcli);
+                if (ll && jj < lw) {
+                    if (jj + 1 < lw) *(int2*)(ll + jj) = make_int2(s0, s1);
+                    else ll[jj] = s0;
+                }
+            });
+        } else {
+            const int row = r0 + r - rc;
+            warp_lift_fwd(&sH[r - rc][4], npairs, [&](int j, int32_t s0, int32_t s1, int32_t d0, int32_t d1) {
+                const int jj = jc + j;
+                emit2(blh, row, jj, s0, s1, coef, gcli);
+                emit2(bhh, row, jj, d0, d1, coef, gcli);
+            });
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* horizontal-only levels                                                    */
+/* ------------------------------------------------------------------------ */
+#define FH_MAX_WARPS 4
+
+/* fills the 2-sample halo on both sides of a row of n samples at x */
+DEV void fill_halo(int32_t* x, int n, int lane) {
+    if (lane < 4) {
+        const int i = lane < 2 ? -2 + lane : n + lane - 2;
+        x[i] = x[mirror_idx(i, n)];
+    }
+}
+
+template <int SRC>
+__global__ void __launch_bounds__(FH_MAX_WARPS * 32) fwd_h_kernel(const __grid_constant__ FwdHLaunch L, const jxs_band_t* __restrict__ bands,
+                                                              uint16_t* __restrict__ coef, uint8_t* __restrict__ gcli) {
+    extern __shared__ __align__(16) int32_t hsm[];
+    int jb = 0;
+    while (jb + 1 < L.njobs && (int)blockIdx.x >= L.job[jb + 1].first_block) jb++;
+    const FwdHJob& J = L.job[jb];
+    const jxs_band_t bl = bands[J.b_ll];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int row = (blockIdx.x - J.first_block) * L.rows_per_block + warp;
+    if (row >= J.h) return;
+    const int n = J.w;
+    /* per warp: buffer A (n + 8 words) and buffer B (n/2 + 8 words) */
+    int32_t* bufA = hsm + warp * L.warp_words + 4;
+    int32_t* bufB = bufA + ((n + 8 + 3) & ~3);
+    for (int x = lane; x < n; x += 32) bufA[x] = load1<SRC>(J.src, J.src_pitch, J.chan, L.depth, row, x);
+    __syncwarp();
+    fill_halo(bufA, n, lane);
+    __syncwarp();
+    int32_t* cur = bufA;
+    int32_t* nxt = bufB;
+    int m = n;
+    for (int e = 0; e < J.nh; e++) {
+        if (m == 1) break; /* nothing left to split: the remaining high bands are empty */
+        const jxs_band_t bd = bands[J.b_hf[e]];
+        const int m1 = (m + 1) >> 1;
+        const int npairs = (m1 + 1) & ~1;
+        int32_t* dst = nxt;
+        warp_lift_fwd(cur, npairs, [&](int j, int32_t s0, int32_t s1, int32_t d0, int32_t d1) {
+            emit2(bd, row, j, d0, d1, coef, gcli);
+            if (j < m1) {
+                dst[j] = s0;
+                if (j + 1 < m1) dst[j + 1] = s1;
+            }
+        });
+        __syncwarp();
+        fill_halo(dst, m1, lane);
+        __syncwarp();
+        nxt = cur;
+        cur = dst;
+        m = m1;
+    }
+    /* final low band */
+    for (int j0 = 0; j0 < m; j0 += 64) {
+        const int j = j0 + 2 * lane;
+        const int32_t a = j < m ? cur[j] : 0, b = j + 1 < m ? cur[j + 1] : 0;
+        emit2(bl, row, j, a, b, coef, gcli);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* launchers                                                                 */
+/* ------------------------------------------------------------------------ */
+extern "C" int jxs_fwd_v_tile_rows(void) { return FV_ROWPAIRS; }
+extern "C" int jxs_fwd_v_tile_cols(void) { return FV_COLS; }
+extern "C" int jxs_fwd_h_max_rows_per_block(void) { return FH_MAX_WARPS; }
+
+extern "C" cudaError_t jxs_launch_fwd_v(const FwdVLaunch* L, int src_kind, int nblocks, const jxs_band_t* bands, uint16_t* coef,
+                                        uint8_t* gcli, cudaStream_t st) {
+    switch (src_kind) {
+    case SRC_I32: fwd_v_kernel<SRC_I32><<<nblocks, FV_THREADS, 0, st>>>(*L, bands, coef, gcli); break;
+    case SRC_U8: fwd_v_kernel<SRC_U8><<<nblocks, FV_THREADS, 0, st>>>(*L, bands, coef, gcli); break;
+    case SRC_U16: fwd_v_kernel<SRC_U16><<<nblocks, FV_THREADS, 0, st>>>(*L, bands, coef, gcli); break;
+    case SRC_PK8: fwd_v_kernel<SRC_PK8><<<nblocks, FV_THREADS, 0, st>>>(*L, bands, coef, gcli); break;
+    default: fwd_v_kernel<SRC_PK16><<<nblocks, FV_THREADS, 0, st>>>(*L, bands, coef, gcli); break;
+    }
+    return cudaGetLastError();
+}
+
+template <int SRC>
+static cudaError_t launch_h(const FwdHLaunch* L, int nblocks, size_t smem, const jxs_band_t* bands, uint16_t* coef, uint8_t* gcli,
+                            cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(fwd_h_kernel<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    fwd_h_kernel<SRC><<<nblocks, L->rows_per_block * 32, smem, st>>>(*L, bands, coef, gcli);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t jxs_launch_fwd_h(const FwdHLaunch* L, int src_kind, int nblocks, const jxs_band_t* bands, uint16_t* coef,
+                                        uint8_t* gcli, cudaStream_t st) {
+    const size_t smem = (size_t)L->warp_words * L->rows_per_block * sizeof(int32_t);
+    switch (src_kind) {
+    case SRC_I32: return launch_h<SRC_I32>(L, nblocks, smem, bands, coef, gcli, st);
+    case SRC_U8: return launch_h<SRC_U8>(L, nblocks, smem, bands, coef, gcli, st);
+    case SRC_U16: return launch_h<SRC_U16>(L, nblocks, smem, bands, coef, gcli, st);
+    case SRC_PK8: return launch_h<SRC_PK8>(L, nblocks, smem, bands, coef, gcli, st);
+    default: return launch_h<SRC_PK16>(L, nblocks, smem, bands, coef, gcli, st);
+    }
+}

@@ -21,8 +21,13 @@
 #include "jxs_gpu.h"
 #include "jxs_kernels.cuh"
 
-extern "C" cudaError_t jxs_launch_fwd_dwt(const DwtLaunch* L, int vert, int nblocks, size_t smem, const jxs_band_t* bands,
-                                          uint16_t* coef, uint8_t* gcli, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_fwd_v(const FwdVLaunch* L, int src_kind, int nblocks, const jxs_band_t* bands, uint16_t* coef,
+                                        uint8_t* gcli, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_fwd_h(const FwdHLaunch* L, int src_kind, int nblocks, const jxs_band_t* bands, uint16_t* coef,
+                                        uint8_t* gcli, cudaStream_t st);
+extern "C" int jxs_fwd_v_tile_rows(void);
+extern "C" int jxs_fwd_v_tile_cols(void);
+extern "C" int jxs_fwd_h_max_rows_per_block(void);
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
                                      PrecRC* rc, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
@@ -140,7 +145,8 @@ struct EncSlot {
     uint64_t in_off[JXS_MAXC];
     uint16_t* coef;
     uint8_t* gcli;
-    int32_t* ll[JXS_MAXC];
+    int32_t* ll[2][JXS_MAXC];   /* int32 low band after vertical level 0 / 1 */
+    int ll_pitch[2][JXS_MAXC];
     uint32_t* cost;
     PrecRC* rc;
     int* status;
@@ -189,10 +195,11 @@ static int32_t enc_slot_alloc(jxs_gpu_enc_t* e, EncSlot* s) {
     CK(cudaMalloc(&s->coef, c->coef_total * sizeof(uint16_t) + 64));
     CK(cudaMalloc(&s->gcli, c->gcli_total + 64));
     for (uint32_t k = 0; k < c->nc; k++) {
-        if (c->comp[k].dv == 2) {
+        for (uint32_t v = 0; v < c->comp[k].dv && v < 2; v++) {
             uint32_t w, h;
-            level_dims(c->comp[k], 1, &w, &h);
-            CK(cudaMalloc(&s->ll[k], (size_t)w * h * sizeof(int32_t)));
+            level_dims(c->comp[k], (int)v + 1, &w, &h);
+            s->ll_pitch[v][k] = (int)((w + 3) & ~3u);
+            CK(cudaMalloc(&s->ll[v][k], (size_t)s->ll_pitch[v][k] * h * sizeof(int32_t) + 64));
         }
     }
     CK(cudaMalloc(&s->cost, (size_t)c->np * 1024 * sizeof(uint32_t)));
@@ -210,7 +217,8 @@ static void enc_slot_free(EncSlot* s) {
     cudaFree(s->in_stage);
     cudaFree(s->coef);
     cudaFree(s->gcli);
-    for (int k = 0; k < JXS_MAXC; k++) cudaFree(s->ll[k]);
+    for (int v = 0; v < 2; v++)
+        for (int k = 0; k < JXS_MAXC; k++) cudaFree(s->ll[v][k]);
     cudaFree(s->cost);
     cudaFree(s->rc);
     cudaFree(s->status);
@@ -304,58 +312,92 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
         }
     }
     TMARK(1);
-    /* forward transform: one launch per vertical level index */
+    /* forward transform: one launch per vertical level, then the
+     * horizontal-only levels of every component (one launch per source
+     * kind) */
     uint32_t max_dv = 0;
     for (uint32_t k = 0; k < c->nc; k++) max_dv = c->comp[k].dv > max_dv ? c->comp[k].dv : max_dv;
-    for (int pass = 0; pass <= (int)max_dv; pass++) {
-        /* pass max_dv handles components without vertical levels */
-        const int vert = pass < (int)max_dv;
-        DwtLaunch L;
+    const int level0_kind = packed ? (bps == 1 ? SRC_PK8 : SRC_PK16) : (bps == 1 ? SRC_U8 : SRC_U16);
+    const uint32_t vcols = (uint32_t)jxs_fwd_v_tile_cols(), vrows = (uint32_t)jxs_fwd_v_tile_rows();
+    for (int v = 0; v < (int)max_dv; v++) {
+        FwdVLaunch L;
         memset(&L, 0, sizeof(L));
+        L.depth = (int)c->depth;
         int blocks = 0;
-        size_t smem = 0;
         for (uint32_t k = 0; k < c->nc; k++) {
             const jxs_comp_t& cp = c->comp[k];
-            if (vert ? (int)cp.dv <= pass : cp.dv != 0) continue;
-            const int v = vert ? pass : 0;
-            DwtJob& J = L.job[L.njobs++];
-            J.comp = (int)k;
+            if ((int)cp.dv <= v) continue;
+            FwdVJob& J = L.job[L.njobs++];
             uint32_t w, h;
             level_dims(cp, v, &w, &h);
             J.w = (int)w;
             J.h = (int)h;
-            J.smem_pitch = (int)w;
-            job_bands(c, (int)k, v, &J);
             if (v == 0) {
+                const int pk = packed ? 0 : (int)k;
+                J.src = src[pk];
+                J.src_pitch = pitch[pk];
+                J.chan = packed ? (int)k : 0;
+                J.vec = !packed && ((uintptr_t)src[pk] % (2 * bps)) == 0 && (pitch[pk] % 2) == 0;
+            } else {
+                J.src = s->ll[v - 1][k];
+                J.src_pitch = s->ll_pitch[v - 1][k];
+                J.vec = 1;
+            }
+            J.ll = s->ll[v][k];
+            J.ll_pitch = s->ll_pitch[v][k];
+            const int top = (int)cp.band0 + (int)cp.nb - 1 - 3 * v;
+            J.b_hh = top;
+            J.b_lh = top - 1;
+            J.b_hl = top - 2;
+            J.col_tiles = (int)div_up(w, vcols);
+            J.first_block = blocks;
+            blocks += J.col_tiles * (int)div_up((h + 1) / 2, vrows);
+        }
+        CK(jxs_launch_fwd_v(&L, v == 0 ? level0_kind : SRC_I32, blocks, dev_bands(e->dcfg), s->coef, s->gcli, st));
+    }
+    for (int pass = 0; pass < 2; pass++) {
+        /* pass 0: components with vertical levels (input: their last int32
+         * low band); pass 1: components without (input: the samples) */
+        FwdHLaunch L;
+        memset(&L, 0, sizeof(L));
+        L.depth = (int)c->depth;
+        int maxw = 0;
+        for (uint32_t k = 0; k < c->nc; k++) {
+            const jxs_comp_t& cp = c->comp[k];
+            if ((cp.dv > 0) != (pass == 0)) continue;
+            FwdHJob& J = L.job[L.njobs++];
+            uint32_t w, h;
+            level_dims(cp, (int)cp.dv, &w, &h);
+            J.w = (int)w;
+            J.h = (int)h;
+            if (cp.dv > 0) {
+                J.src = s->ll[cp.dv - 1][k];
+                J.src_pitch = s->ll_pitch[cp.dv - 1][k];
+            } else {
                 J.src = src[packed ? 0 : k];
                 J.src_pitch = pitch[packed ? 0 : k];
-                J.src_kind = packed ? (bps == 1 ? SRC_PK8 : SRC_PK16) : (bps == 1 ? SRC_U8 : SRC_U16);
                 J.chan = packed ? (int)k : 0;
-            } else {
-                J.src = s->ll[k];
-                J.src_pitch = (long long)((cp.w + 1) / 2);
-                J.src_kind = SRC_I32;
             }
-            J.depth = (int)c->depth;
-            if (vert && !J.last) {
-                J.ll = s->ll[k];
-                J.ll_pitch = (int)((w + 1) / 2);
-            }
-            const size_t row_bytes = (size_t)w * 4;
-            int R = (int)(kLevelSmemTarget / ((vert ? 2 : 1) * row_bytes));
-            if (R < 1) R = 1;
-            const uint32_t units = vert ? (h + 1) / 2 : h;
-            if ((uint32_t)R > units) R = (int)units;
-            J.R = R;
-            J.first_block = blocks;
-            J.nblocks = (int)div_up(units, (uint32_t)R);
-            blocks += J.nblocks;
-            const size_t need = (size_t)(vert ? 2 : 1) * R * row_bytes;
-            smem = need > smem ? need : smem;
+            DwtJob bj;
+            memset(&bj, 0, sizeof(bj));
+            job_bands(c, (int)k, cp.dv > 0 ? (int)cp.dv - 1 : 0, &bj);
+            J.nh = bj.nh;
+            for (int e2 = 0; e2 < 5; e2++) J.b_hf[e2] = bj.b_hf[e2];
+            J.b_ll = bj.b_ll;
+            maxw = (int)w > maxw ? (int)w : maxw;
         }
         if (!L.njobs) continue;
-        if (smem > kSmemMax) return JXS_E_BAD_PARAM;
-        CK(jxs_launch_fwd_dwt(&L, vert, blocks, smem, dev_bands(e->dcfg), s->coef, s->gcli, st));
+        L.warp_words = 4 + ((maxw + 8 + 3) & ~3) + (((maxw + 1) / 2 + 8 + 3) & ~3) + 4;
+        int rpb = jxs_fwd_h_max_rows_per_block();
+        while (rpb > 1 && (size_t)L.warp_words * rpb * 4 > kSmemMax) rpb >>= 1;
+        if ((size_t)L.warp_words * rpb * 4 > kSmemMax) return JXS_E_BAD_PARAM;
+        L.rows_per_block = rpb;
+        int blocks = 0;
+        for (int i = 0; i < L.njobs; i++) {
+            L.job[i].first_block = blocks;
+            blocks += (int)div_up((uint32_t)L.job[i].h, (uint32_t)rpb);
+        }
+        CK(jxs_launch_fwd_h(&L, pass == 0 ? SRC_I32 : level0_kind, blocks, dev_bands(e->dcfg), s->coef, s->gcli, st));
     }
     TMARK(2);
     CK(jxs_launch_rc(e->dcfg, c->np, c->nslices, s->gcli, s->cost, s->rc, s->status, st));

@@ -48,6 +48,44 @@ struct DwtLaunch {
     DwtJob job[JXS_MAXC];
 };
 
+/* Forward transform, one vertical level (jxs_fwd_dwt.cu): one component's
+ * share of the launch; its tiles are blocks [first_block, first_block +
+ * row_tiles * col_tiles). */
+struct FwdVJob {
+    const void* src;        /* level input: samples (level 0) or the int32 low band of the previous level */
+    long long src_pitch;    /* elements */
+    int chan;               /* packed input: channel of this component */
+    int vec;                /* two adjacent samples may be read with one load */
+    int w, h;               /* level input size */
+    int col_tiles, first_block;
+    int32_t* ll;            /* int32 low band written for the next level */
+    int ll_pitch;           /* elements, a multiple of 4 */
+    int b_hl, b_lh, b_hh;   /* flat band indices */
+};
+struct FwdVLaunch {
+    int njobs, depth;
+    FwdVJob job[JXS_MAXC];
+};
+
+/* Forward transform, horizontal-only levels: rows [0, h) of a w-wide
+ * plane, rows_per_block rows (one warp each) per block. */
+struct FwdHJob {
+    const void* src;
+    long long src_pitch;
+    int chan;
+    int w, h;
+    int first_block;
+    int nh;                 /* levels */
+    int b_hf[5];            /* high band of each level */
+    int b_ll;               /* final low band */
+};
+struct FwdHLaunch {
+    int njobs, depth;
+    int rows_per_block;
+    int warp_words;         /* shared-memory words per warp */
+    FwdHJob job[JXS_MAXC];
+};
+
 /* Encoder rate-control outputs per precinct row. */
 struct PrecRC {
     uint32_t total_bytes;  /* bytes written for the precinct (header to last data byte, incl. trailing padding) */
