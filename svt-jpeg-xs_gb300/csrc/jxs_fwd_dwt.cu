@@ -45,6 +45,7 @@
 /* ------------------------------------------------------------------------ */
 /* whole-sample symmetric extension of index i into [0, n) */
 DEV int mirror_idx(int i, int n) {
+    if ((unsigned)i < (unsigned)n) return i;
     if (n == 1) return 0;
     const int p = 2 * (n - 1);
     i %= p;
@@ -99,50 +100,69 @@ DEV void load2(const void* src, long long pitch, int chan, int depth, int y, int
     }
 }
 
-/* Writes coefficients j, j+1 (j even) of row `row` of band bd, and, from the
- * even lane of each lane pair, the GCLI of the 4-group the pair covers.
- * Values at j >= width are written as zero; nothing past the last group. */
-DEV void emit2(const jxs_band_t& bd, int row, int j, int32_t a, int32_t b, uint16_t* __restrict__ coef,
-               uint8_t* __restrict__ gcli) {
-    const int w = (int)bd.w;
-    const uint32_t ca = j < w ? to_sm(a) : 0u, cb = j + 1 < w ? to_sm(b) : 0u;
-    uint32_t m = (ca | cb) & 0x7fffu;
-    m |= __shfl_xor_sync(FULL, m, 1);
-    if (j < 4 * (int)bd.gcli_w && j >= 0) {
-        *(uint32_t*)(coef + bd.coef_off + (uint64_t)row * bd.pitch + j) = ca | (cb << 16);
-        if (!(j & 2)) gcli[bd.gcli_off + (uint64_t)row * bd.gpitch + (j >> 2)] = (uint8_t)(m ? 32 - __clz(m) : 0);
-    }
+/* One lane's 4-coefficient group of a band row: coefficients j..j+3 (j a
+ * multiple of 4) as sign-magnitude plus the group's GCLI.  crow / grow are
+ * the band row's coefficient and GCLI rows; w its width, gw its groups.
+ * Coefficients past the width are written as zero; nothing past the last
+ * group. */
+struct BandRow {
+    uint16_t* crow;
+    uint8_t* grow;
+    int w, gw;
+};
+DEV BandRow band_row(const jxs_band_t& bd, int row, uint16_t* coef, uint8_t* gcli) {
+    BandRow r;
+    r.crow = coef + bd.coef_off + (uint64_t)row * bd.pitch;
+    r.grow = gcli + bd.gcli_off + (uint64_t)row * bd.gpitch;
+    r.w = (int)bd.w;
+    r.gw = (int)bd.gcli_w;
+    return r;
+}
+DEV void emit4(const BandRow& b, int j, int32_t v0, int32_t v1, int32_t v2, int32_t v3) {
+    if ((j >> 2) >= b.gw) return;
+    const uint32_t c0 = to_sm(v0), c1 = j + 1 < b.w ? to_sm(v1) : 0u, c2 = j + 2 < b.w ? to_sm(v2) : 0u,
+                   c3 = j + 3 < b.w ? to_sm(v3) : 0u;
+    *(uint2*)(b.crow + j) = make_uint2(c0 | (c1 << 16), c2 | (c3 << 16));
+    const uint32_t m = (c0 | c1 | c2 | c3) & 0x7fffu;
+    b.grow[j >> 2] = (uint8_t)(32 - __clz(m));
 }
 
 /* One horizontal lifting pass of a row held in shared memory, by one warp.
  * x points at sample 0 of the pass; x[-2], x[-1] and the samples past the
- * last pair needed hold the (mirrored or neighbouring-tile) halo.  `npairs`
- * output pairs (s[j], d[j]) for j in [0, npairs) are produced, npairs a
- * multiple of 2; lane l of iteration it owns j = 64*it + 2l and 2l + 1.
- * Reads x[-2 .. 2*npairs + 3]; outputs past the valid width may depend on
- * samples past x[2*npairs + 1] and are discarded by the caller.
- * x must be 16-byte aligned. */
+ * last pair needed hold the (mirrored or neighbouring-tile) halo.  Output
+ * pairs (s[j], d[j]) for j in [0, npairs) are produced; lane l of iteration
+ * it owns j = 128*it + 4l .. +3 and passes them to out(j, s[4], d[4]).
+ * Reads x[-2 .. 8 * ceil(npairs / 4) + 7] at most; outputs past the valid
+ * width may depend on samples past x[2 * npairs + 1] and are discarded by
+ * the caller.  x must be 16-byte aligned. */
 template <typename Out>
 DEV void warp_lift_fwd(const int32_t* x, int npairs, Out out) {
     const int lane = threadIdx.x & 31;
-    /* d[-1] from the halo */
-    int32_t carry = x[-1] - ((x[-2] + x[0]) >> 1);
-    for (int base = 0; base < npairs; base += 64) {
-        const int j = base + 2 * lane;
-        int4 v = make_int4(0, 0, 0, 0);
+    int32_t carry = x[-1] - ((x[-2] + x[0]) >> 1); /* d[-1] */
+    for (int base = 0; base < npairs; base += 128) {
+        const int j = base + 4 * lane;
+        int4 a = make_int4(0, 0, 0, 0), b = a;
         /* the lane just past the last pair still loads: its first sample is
          * the right neighbour of the previous lane */
-        if (j <= npairs) v = *(const int4*)(x + 2 * j);
-        int32_t nxt = __shfl_down_sync(FULL, v.x, 1);
-        if (lane == 31) nxt = j < npairs ? x[2 * j + 4] : 0;
-        const int32_t d0 = v.y - ((v.x + v.z) >> 1);
-        const int32_t d1 = v.w - ((v.z + nxt) >> 1);
-        int32_t dm = __shfl_up_sync(FULL, d1, 1);
+        if (j <= npairs) {
+            a = *(const int4*)(x + 2 * j);
+            b = *(const int4*)(x + 2 * j + 4);
+        }
+        int32_t nxt = __shfl_down_sync(FULL, a.x, 1);
+        if (lane == 31) nxt = j < npairs ? x[2 * j + 8] : 0;
+        int32_t d[4], sv[4];
+        d[0] = a.y - ((a.x + a.z) >> 1);
+        d[1] = a.w - ((a.z + b.x) >> 1);
+        d[2] = b.y - ((b.x + b.z) >> 1);
+        d[3] = b.w - ((b.z + nxt) >> 1);
+        int32_t dm = __shfl_up_sync(FULL, d[3], 1);
         if (lane == 0) dm = carry;
-        carry = __shfl_sync(FULL, d1, 31);
-        const int32_t s0 = v.x + ((dm + d0 + 2) >> 2);
-        const int32_t s1 = v.z + ((d0 + d1 + 2) >> 2);
-        out(j, s0, s1, d0, d1);
+        carry = __shfl_sync(FULL, d[3], 31);
+        sv[0] = a.x + ((dm + d[0] + 2) >> 2);
+        sv[1] = a.z + ((d[0] + d[1] + 2) >> 2);
+        sv[2] = b.x + ((d[1] + d[2] + 2) >> 2);
+        sv[3] = b.z + ((d[2] + d[3] + 2) >> 2);
+        if (j < npairs) out(j, sv, d);
     }
 }
 
@@ -150,12 +170,12 @@ DEV void warp_lift_fwd(const int32_t* x, int npairs, Out out) {
 /* vertical level + one horizontal level                                     */
 /* ------------------------------------------------------------------------ */
 #define FV_THREADS 128
-#define FV_COLS (2 * FV_THREADS)          /* output columns of the level input per tile */
+#define FV_COLS (2 * FV_THREADS - 8)      /* level-input columns per tile: tile + 4 halo columns in one pass */
 #define FV_ROWPAIRS 8
-#define FV_SROW (FV_COLS + 8)             /* shared row: 4 front words (2 pad, 2 halo), FV_COLS, 2 halo, 2 pad */
+#define FV_SROW (FV_COLS + 16)            /* shared row: 4 front words (2 pad, 2 halo), FV_COLS, halo, slack */
 
 template <int SRC>
-__global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant__ FwdVLaunch L, const jxs_band_t* __restrict__ bands,
+__global__ void __launch_bounds__(FV_THREADS, 8) fwd_v_kernel(const __grid_constant__ FwdVLaunch L, const jxs_band_t* __restrict__ bands,
                                                            uint16_t* __restrict__ coef, uint8_t* __restrict__ gcli) {
     __shared__ __align__(16) int32_t sL[FV_ROWPAIRS][FV_SROW];
     __shared__ __align__(16) int32_t sH[FV_ROWPAIRS][FV_SROW];
@@ -181,7 +201,7 @@ __global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant
     int ys[2 * FV_ROWPAIRS + 3];
 #pragma unroll
     for (int k = 0; k < 2 * FV_ROWPAIRS + 3; k++) ys[k] = mirror_idx(2 * r0 - 2 + k, h);
-    for (int cp = threadIdx.x; cp < ncp; cp += FV_THREADS) {
+    for (int cp = threadIdx.x; cp < ncp; cp += FV_THREADS) { /* a single pass: ncp <= FV_THREADS */
         const int xa = c0 - 2 + 2 * cp;
         const bool inside = xa >= 0 && xa + 1 < w;
         const int ma = mirror_idx(xa, w), mb = mirror_idx(xa + 1, w);
@@ -212,26 +232,28 @@ __global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant
     /* horizontal lifting, one warp per row; the tile's output pairs are
      * j in [c0/2, c0/2 + npairs) of the level's bands */
     const int warp = threadIdx.x >> 5;
-    const jxs_band_t bhl = bands[J.b_hl], blh = bands[J.b_lh], bhh = bands[J.b_hh];
     for (int r = warp; r < rc + hc; r += FV_THREADS / 32) {
         if (r < rc) {
             const int row = r0 + r;
-            int32_t* ll = J.ll ? J.ll + (long long)row * J.ll_pitch : nullptr;
-            const int lw = w1;
-            warp_lift_fwd(&sL[r][4], npairs, [&](int j, int32_t s0, int32_t s1, int32_t d0, int32_t d1) {
+            const BandRow bhl = band_row(bands[J.b_hl], row, coef, gcli);
+            int32_t* ll = J.ll + (long long)row * J.ll_pitch;
+            warp_lift_fwd(&sL[r][4], npairs, [&](int j, const int32_t* sv, const int32_t* d) {
                 const int jj = jc + j;
-                emit2(bhl, row, jj, d0, d1, coef, gcli);
-                if (ll && jj < lw) {
-                    if (jj + 1 < lw) *(int2*)(ll + jj) = make_int2(s0, s1);
-                    else ll[jj] = s0;
+                emit4(bhl, jj, d[0], d[1], d[2], d[3]);
+                if (jj + 3 < w1) {
+                    *(int4*)(ll + jj) = make_int4(sv[0], sv[1], sv[2], sv[3]);
+                } else {
+                    for (int q = 0; q < 4; q++)
+                        if (jj + q < w1) ll[jj + q] = sv[q];
                 }
             });
         } else {
             const int row = r0 + r - rc;
-            warp_lift_fwd(&sH[r - rc][4], npairs, [&](int j, int32_t s0, int32_t s1, int32_t d0, int32_t d1) {
-                const int jj = jc + j;
-                emit2(blh, row, jj, s0, s1, coef, gcli);
-                emit2(bhh, row, jj, d0, d1, coef, gcli);
+            const BandRow blh = band_row(bands[J.b_lh], row, coef, gcli);
+            const BandRow bhh = band_row(bands[J.b_hh], row, coef, gcli);
+            warp_lift_fwd(&sH[r - rc][4], npairs, [&](int j, const int32_t* sv, const int32_t* d) {
+                emit4(blh, jc + j, sv[0], sv[1], sv[2], sv[3]);
+                emit4(bhh, jc + j, d[0], d[1], d[2], d[3]);
             });
         }
     }
@@ -257,7 +279,6 @@ __global__ void __launch_bounds__(FH_MAX_WARPS * 32) fwd_h_kernel(const __grid_c
     int jb = 0;
     while (jb + 1 < L.njobs && (int)blockIdx.x >= L.job[jb + 1].first_block) jb++;
     const FwdHJob& J = L.job[jb];
-    const jxs_band_t bl = bands[J.b_ll];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = (blockIdx.x - J.first_block) * L.rows_per_block + warp;
     if (row >= J.h) return;
@@ -274,15 +295,16 @@ __global__ void __launch_bounds__(FH_MAX_WARPS * 32) fwd_h_kernel(const __grid_c
     int m = n;
     for (int e = 0; e < J.nh; e++) {
         if (m == 1) break; /* nothing left to split: the remaining high bands are empty */
-        const jxs_band_t bd = bands[J.b_hf[e]];
+        const BandRow bd = band_row(bands[J.b_hf[e]], row, coef, gcli);
         const int m1 = (m + 1) >> 1;
-        const int npairs = (m1 + 1) & ~1;
         int32_t* dst = nxt;
-        warp_lift_fwd(cur, npairs, [&](int j, int32_t s0, int32_t s1, int32_t d0, int32_t d1) {
-            emit2(bd, row, j, d0, d1, coef, gcli);
-            if (j < m1) {
-                dst[j] = s0;
-                if (j + 1 < m1) dst[j + 1] = s1;
+        warp_lift_fwd(cur, m1, [&](int j, const int32_t* sv, const int32_t* d) {
+            emit4(bd, j, d[0], d[1], d[2], d[3]);
+            if (j + 3 < m1) {
+                *(int4*)(dst + j) = make_int4(sv[0], sv[1], sv[2], sv[3]);
+            } else {
+                for (int q = 0; q < 4; q++)
+                    if (j + q < m1) dst[j + q] = sv[q];
             }
         });
         __syncwarp();
@@ -293,10 +315,11 @@ __global__ void __launch_bounds__(FH_MAX_WARPS * 32) fwd_h_kernel(const __grid_c
         m = m1;
     }
     /* final low band */
-    for (int j0 = 0; j0 < m; j0 += 64) {
-        const int j = j0 + 2 * lane;
-        const int32_t a = j < m ? cur[j] : 0, b = j + 1 < m ? cur[j + 1] : 0;
-        emit2(bl, row, j, a, b, coef, gcli);
+    const BandRow bl = band_row(bands[J.b_ll], row, coef, gcli);
+    for (int j = 4 * lane; j < m; j += 128) {
+        int32_t v[4];
+        for (int q = 0; q < 4; q++) v[q] = j + q < m ? cur[j + q] : 0;
+        emit4(bl, j, v[0], v[1], v[2], v[3]);
     }
 }
 
