@@ -40,6 +40,53 @@ int32_t jxs_sampling(uint32_t fmt, uint32_t* nc, uint32_t sx[JXS_MAXC], uint32_t
 
 /* Per-component band tree, global band numbering, packets and precinct
  * lines (Pi.c:131-406 for one precinct column). */
+/* Band lines of the normal and the last precinct row in codestream order,
+ * and their split into segments (packet order of Pi.c:189-406). */
+static int32_t cfg_blines(jxs_cfg_t* g) {
+    uint32_t sg = 128;
+    for (;;) {
+        int fits = 1;
+        for (int t = 0; t < 2; t++) {
+            uint32_t n = 0, ns = 0;
+            for (uint32_t k = 0; k < g->npk; k++) {
+                const uint32_t l = g->pk[k].line;
+                for (uint32_t gb = g->pk[k].bs; gb < g->pk[k].be; gb++) {
+                    const uint32_t fb = g->g2f[gb];
+                    if (fb == JXS_NOBAND) continue;
+                    const jxs_band_t* bd = &g->band[fb];
+                    if (l >= (t ? bd->last_lines : bd->lines)) continue;
+                    if (n >= JXS_MAXBLINES) return JXS_E_BAD_PARAM;
+                    jxs_bline_t* b = &g->bline[t][n++];
+                    b->fb = (uint8_t)fb;
+                    b->line = (uint8_t)l;
+                    b->pk = (uint8_t)k;
+                    b->pad = 0;
+                    b->gcli_w = bd->gcli_w;
+                    b->sig_w = bd->sig_w;
+                    b->w = bd->w;
+                    b->seg0 = ns;
+                    b->nseg = (bd->gcli_w + sg - 1) / sg;
+                    if (b->nseg == 0) b->nseg = 1;
+                    for (uint32_t i = 0; i < b->nseg; i++, ns++) {
+                        if (ns < JXS_MAXSEG) {
+                            g->seg[t][ns].bl = (uint16_t)(n - 1);
+                            g->seg[t][ns].pad = 0;
+                            g->seg[t][ns].g0 = i * sg;
+                        }
+                    }
+                }
+            }
+            g->nbline[t] = n;
+            g->nseg[t] = ns;
+            if (ns > JXS_MAXSEG) fits = 0;
+        }
+        if (fits) break;
+        sg *= 2;
+    }
+    g->seg_groups = sg;
+    return JXS_OK;
+}
+
 int32_t jxs_cfg_geometry(jxs_cfg_t* g, int for_encoder, uint32_t nc, uint32_t W, uint32_t H, uint32_t dh, uint32_t dv,
                          uint32_t sd, const uint32_t sx[JXS_MAXC], const uint32_t sy[JXS_MAXC], uint32_t slice_h) {
     if (sd > nc || dv > dh || dh > 5 || dv > 2 || nc > JXS_MAXC || nc < 1 || slice_h == 0) return JXS_E_BAD_PARAM;
@@ -197,7 +244,7 @@ int32_t jxs_cfg_geometry(jxs_cfg_t* g, int for_encoder, uint32_t nc, uint32_t W,
         }
         g->pk_exist[t] = for_encoder ? (t == 0 ? g->npk : cnt) : cnt;
     }
-    return JXS_OK;
+    return cfg_blines(g);
 }
 
 /* ---- weight tables (gains / priorities per codestream band) ---- */

@@ -65,6 +65,21 @@ typedef struct jxs_packet {
     uint32_t bs, be, line;      /* global band range [bs, be) and band line */
 } jxs_packet_t;
 
+/* One band line of a precinct row, in codestream order (packet order, then
+ * band order inside the packet).  Its GCLI groups are split into segments
+ * of jxs_cfg_t.seg_groups groups that the kernels process one warp each. */
+#define JXS_MAXBLINES 80
+#define JXS_MAXSEG 512
+typedef struct jxs_bline {
+    uint8_t fb, line, pk, pad;  /* flat band, line inside the precinct row, packet */
+    uint32_t gcli_w, sig_w, w;  /* groups, significance groups, coefficients */
+    uint32_t seg0, nseg;        /* its segments */
+} jxs_bline_t;
+typedef struct jxs_seg {
+    uint16_t bl, pad;           /* band line */
+    uint32_t g0;                /* first group, a multiple of seg_groups */
+} jxs_seg_t;
+
 typedef struct jxs_cfg {
     uint32_t W, H, nc, fmt, depth, sd;
     uint32_t dv, dh, prec_h, slice_h, pps, np, nslices;
@@ -86,6 +101,11 @@ typedef struct jxs_cfg {
     uint8_t hdr[512];
     uint32_t hdr_len;
     uint64_t coef_total, gcli_total;     /* per-frame buffer sizes (elements / bytes) */
+    uint32_t nbline[2];                  /* band lines: normal / last precinct row */
+    jxs_bline_t bline[2][JXS_MAXBLINES];
+    uint32_t seg_groups;                 /* groups per segment, a multiple of 32 */
+    uint32_t nseg[2];
+    jxs_seg_t seg[2][JXS_MAXSEG];
     uint32_t max_slice_budget;           /* 0 when slice starts cannot be predicted (decoder) */
     uint32_t slice_size[8192];           /* bytes of each slice incl. its header (last: incl. EOC) */
     uint32_t slice_begin[8192];          /* byte offset of each slice in the codestream */

@@ -350,6 +350,8 @@ __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restr
 /* Packing                                                                   */
 /* ------------------------------------------------------------------------ */
 #define PK_THREADS 512
+#define PK_WARPS (PK_THREADS / 32)
+#define FULL 0xffffffffu
 
 /* OR `n` (<= 32) bits of `v` at bit position `pos` of a big-endian bit
  * string stored in native byte order.  Writes beyond the precinct's words
@@ -381,81 +383,82 @@ DEV void put_bits64(uint32_t* buf, uint32_t pos, uint64_t v, uint32_t n) {
     }
 }
 
-/* quant_deadzone_c / quant_uniform_c (Quant.c:9-45); the reference skips
- * quantization entirely when gtli is 0 (QuantStageProcess.c:18-31). */
-DEV uint32_t quantize(uint32_t v, uint32_t gcli, uint32_t t, uint32_t uniform) {
-    if (t == 0) return v;
-    const uint32_t sign = v & 0x8000u;
-    uint32_t m = v & 0x7fffu;
-    if (uniform) {
-        const uint32_t s = gcli - t + 1;
-        /* computed in int like the reference, truncated to 16 bits after the shift */
-        m = (((m << s) - m + (1u << gcli)) >> (gcli + 1)) & 0xffffu;
-        m = (m << t) & 0xffffu;
-    } else {
-        m = (m >> t) << t;
+DEV uint32_t warp_excl_scan(uint32_t x, uint32_t* total) {
+    const int lane = threadIdx.x & 31;
+    uint32_t inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += y;
     }
-    return m ? (m | sign) : 0u;
+    *total = __shfl_sync(FULL, inc, 31);
+    return inc - x;
 }
 
-struct PackBL {
-    uint16_t fb;
-    uint8_t line, pk, t, meth, raw;
-    uint32_t row, gcli_w, sig_w, w, g0, s0;
-    uint32_t data_bits, nosig_bits, zeroed_bits;
-    uint32_t sig_pos, gcli_pos, data_pos;  /* bit positions inside the precinct */
-    uint32_t vlc_pref, data_pref;          /* flattened prefix at the first group */
+/* Data bits of one 4-coefficient group with GCLI v > gtli t
+ * (pack_data_c, PackPrecinct.c:128-198): the sign nibble (coefficient 0 in
+ * the most significant bit) followed by bit-planes v-1 .. t, each a nibble.
+ * Quantization (Quant.c:9-45) is skipped for t == 0 like the reference
+ * (QuantStageProcess.c:18-31); a sign is sent only for a non-zero
+ * quantized magnitude.  lut[b] spreads the 8 bits of b to every 4th bit. */
+DEV uint64_t data_chunk(uint2 raw4, int wleft, uint32_t v, uint32_t t, uint32_t uniform, const uint32_t* lut) {
+    const uint32_t c[4] = {raw4.x & 0xffffu, raw4.x >> 16, raw4.y & 0xffffu, raw4.y >> 16};
+    uint32_t P[4], signs = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const uint32_t cc = k < wleft ? c[k] : 0u;
+        const uint32_t m = cc & 0x7fffu;
+        uint32_t q;
+        if (t == 0) {
+            q = m;
+        } else if (uniform) {
+            /* computed in int like the reference, truncated to 16 bits */
+            q = (((m << (v - t + 1)) - m + (1u << v)) >> (v + 1)) & 0xffffu;
+            q = ((q << t) & 0xffffu) >> t;
+        } else {
+            q = m >> t;
+        }
+        P[k] = q;
+        signs = (signs << 1) | (q ? (cc >> 15) : 0u);
+    }
+    const uint32_t np = v - t;
+    uint64_t planes = (lut[P[0] & 255] << 3) | (lut[P[1] & 255] << 2) | (lut[P[2] & 255] << 1) | lut[P[3] & 255];
+    if (np > 8)
+        planes |= (uint64_t)((lut[P[0] >> 8] << 3) | (lut[P[1] >> 8] << 2) | (lut[P[2] >> 8] << 1) | lut[P[3] >> 8]) << 32;
+    return ((uint64_t)signs << (4 * np)) | planes;
+}
+
+/* Per band line of the precinct being packed. */
+struct PkLine {
+    uint32_t sig_pos, gcli_pos, data_pos; /* bit positions in the shared-memory precinct */
+    uint32_t data, vlc, zero;             /* data bits, VLC bits without significance, groups in insignificant significance groups */
+    uint8_t meth, raw, pad0, pad1;
 };
 
-/* Block-wide exclusive scan of two counters. */
-DEV void block_scan2(uint32_t a, uint32_t b, uint32_t* ea, uint32_t* eb, uint32_t* wa, uint32_t* wb) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint32_t ia = a, ib = b;
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t ta = __shfl_up_sync(0xffffffffu, ia, o), tb = __shfl_up_sync(0xffffffffu, ib, o);
-        if (lane >= o) { ia += ta; ib += tb; }
-    }
-    if (lane == 31) { wa[warp] = ia; wb[warp] = ib; }
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t va = lane < nw ? wa[lane] : 0, vb = lane < nw ? wb[lane] : 0;
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t ta = __shfl_up_sync(0xffffffffu, va, o), tb = __shfl_up_sync(0xffffffffu, vb, o);
-            if (lane >= o) { va += ta; vb += tb; }
-        }
-        if (lane < nw) { wa[lane] = va; wb[lane] = vb; }
-    }
-    __syncthreads();
-    const uint32_t ba = warp ? wa[warp - 1] : 0, bb = warp ? wb[warp - 1] : 0;
-    *ea = ba + ia - a;
-    *eb = bb + ib - b;
-    __syncthreads();
-}
-
-DEV int find_bl_by_group(const PackBL* bl, int n, uint32_t g) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (bl[mid].g0 <= g) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 /* pack_precinct (PackPrecinct.c:235-572) for one precinct row; vertical
- * prediction and sign handling off. */
+ * prediction and sign handling off.
+ *
+ * The precinct is assembled in shared memory, `lead` bytes into the buffer
+ * so that buffer byte i lands on the 16-byte aligned address
+ * out + offset - lead + i, then copied out.  Band lines are split into
+ * segments of seg_groups groups, one warp per segment:
+ *   pass A  each segment's data bits, VLC bits and groups lying in
+ *           insignificant significance groups, at the precinct's gtli;
+ *   layout  thread 0: coding method per band (significance only if strictly
+ *           cheaper), packet headers, raw fallback, sub-packet positions,
+ *           each segment's start in its GCLI and data sub-packets;
+ *   pass B  each lane one group: significance flags, the unary GCLI code and
+ *           the data bits, at positions from a warp prefix sum, OR-ed into
+ *           the buffer. */
 __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
                                                           const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
-                                                          uint8_t* __restrict__ out, uint32_t cap_words, uint32_t sig_cap,
-                                                          int* status) {
-    extern __shared__ uint32_t buf[];
-    uint8_t* sflag = (uint8_t*)(buf + cap_words); /* per significance group: all GCLIs <= gtli */
-    __shared__ PackBL bl[RC_MAXBL];
-    __shared__ BandLine tmp[RC_MAXBL];
-    __shared__ uint8_t blmap[JXS_MAXBL * 4];
-    __shared__ uint32_t wsa[PK_THREADS / 32], wsb[PK_THREADS / 32];
-    __shared__ int s_nbl, s_ok;
-    __shared__ uint32_t s_ng, s_ns;
+                                                          uint8_t* __restrict__ out, uint32_t cap_words, int* status) {
+    extern __shared__ __align__(16) uint32_t buf[];
+    __shared__ uint32_t s_data[JXS_MAXSEG], s_vlc[JXS_MAXSEG], s_zero[JXS_MAXSEG];
+    __shared__ PkLine pl[JXS_MAXBLINES];
+    __shared__ uint8_t tb[JXS_MAXBL];
+    __shared__ uint32_t lut[256];
+    __shared__ int s_ok;
 
     const int p = blockIdx.x;
     const int last = (p + 1 >= (int)cfg->np);
@@ -466,7 +469,8 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     __syncthreads();
     if (!s_ok) return;
     const uint32_t total = R.total_bytes;
-    const uint32_t words = (total + 3) >> 2;
+    const uint32_t lead = (uint32_t)((uintptr_t)(out + R.offset) & 15);
+    const uint32_t words = ((lead + total + 15) >> 4) << 2;
     if (words > cap_words) {
         if (threadIdx.x == 0) {
             printf("jxs pack: precinct %d needs %u words, buffer holds %u\n", p, words, cap_words);
@@ -475,68 +479,85 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
         return;
     }
     for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) buf[i] = 0;
+    for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) {
+        uint32_t x = 0;
+        for (int k = 0; k < 8; k++) x |= ((i >> k) & 1u) << (4 * k);
+        lut[i] = x;
+    }
+    for (uint32_t fb = threadIdx.x; fb < cfg->nbands; fb += blockDim.x)
+        tb[fb] = jxs_truncation(cfg->band[fb].gain, cfg->band[fb].prio, R.q, R.r);
     if (threadIdx.x == 0) {
         pk_nwords = words;
         pk_overflow = 0;
-        int n = build_bandlines(cfg, p, last, tmp, blmap, &s_ng, &s_ns);
-        for (int b = 0; b < n; b++) {
-            const jxs_band_t& bd = cfg->band[tmp[b].fb];
-            PackBL& o = bl[b];
-            o.fb = tmp[b].fb; o.line = tmp[b].line; o.pk = tmp[b].pk;
-            o.row = tmp[b].row; o.gcli_w = tmp[b].gcli_w; o.sig_w = tmp[b].sig_w; o.w = tmp[b].w;
-            o.g0 = tmp[b].g0; o.s0 = tmp[b].s0;
-            o.t = jxs_truncation(bd.gain, bd.prio, R.q, R.r);
-            o.data_bits = o.nosig_bits = o.zeroed_bits = 0;
-        }
-        s_nbl = n;
     }
     __syncthreads();
-    const int nbl = s_nbl;
-    if (s_ns > sig_cap) {
-        if (threadIdx.x == 0) {
-            printf("jxs pack: precinct %d has %u significance groups, buffer holds %u\n", p, s_ns, sig_cap);
-            JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
-        }
-        return;
-    }
-    /* per band line: data bits, GCLI bits, significance-zeroed GCLIs */
-    for (uint32_t s = threadIdx.x; s < s_ns; s += blockDim.x) {
-        const int b = find_bl_by_sig((const BandLine*)tmp, nbl, s);
-        const BandLine& B = tmp[b];
-        uint8_t v[8];
-        const int cnt = load_sig_group(gcli, cfg->band[B.fb], B, s - B.s0, v);
-        const uint32_t t = bl[b].t;
-        uint32_t data = 0, nosig = 0, mx = 0;
-        for (int k = 0; k < cnt; k++) {
-            mx = max(mx, (uint32_t)v[k]);
-            if (v[k] > t) {
-                data += 4 * (v[k] - t + 1);
-                nosig += v[k] - t + 1;
-            } else {
-                nosig += 1;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t nseg = cfg->nseg[last], SG = cfg->seg_groups;
+    const jxs_seg_t* segs = cfg->seg[last];
+    const jxs_bline_t* bls = cfg->bline[last];
+
+    /* pass A */
+    for (uint32_t sidx = warp; sidx < nseg; sidx += PK_WARPS) {
+        const jxs_seg_t sg = segs[sidx];
+        const jxs_bline_t B = bls[sg.bl];
+        const jxs_band_t& bd = cfg->band[B.fb];
+        const uint32_t t = tb[B.fb];
+        const uint8_t* grow = gcli + bd.gcli_off + (uint64_t)(p * bd.lines + B.line) * bd.gpitch;
+        const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+        uint32_t dsum = 0, vsum = 0, zsum = 0;
+        for (uint32_t base = sg.g0; base < gend; base += 32) {
+            const uint32_t g = base + lane;
+            const bool valid = g < gend;
+            const uint32_t v = valid ? grow[g] : 0u;
+            uint32_t mx = v;
+            mx = max(mx, __shfl_xor_sync(FULL, mx, 1));
+            mx = max(mx, __shfl_xor_sync(FULL, mx, 2));
+            mx = max(mx, __shfl_xor_sync(FULL, mx, 4));
+            if (valid) {
+                dsum += v > t ? 4 * (v - t + 1) : 0u;
+                vsum += v > t ? v - t + 1 : 1u;
+                zsum += mx <= t;
             }
         }
-        atomicAdd(&bl[b].data_bits, data);
-        atomicAdd(&bl[b].nosig_bits, nosig);
-        if (mx <= t) atomicAdd(&bl[b].zeroed_bits, (uint32_t)cnt);
-        sflag[s] = (uint8_t)(mx <= t);
+        dsum = __reduce_add_sync(FULL, dsum);
+        vsum = __reduce_add_sync(FULL, vsum);
+        zsum = __reduce_add_sync(FULL, zsum);
+        if (lane == 0) {
+            s_data[sidx] = dsum;
+            s_vlc[sidx] = vsum;
+            s_zero[sidx] = zsum;
+        }
     }
     __syncthreads();
+
+    /* layout */
     if (threadIdx.x == 0) {
-        /* method per band (strictly cheaper), then packet sizes and positions */
+        const uint32_t nbl = cfg->nbline[last];
+        uint32_t cn[JXS_MAXBL], cs[JXS_MAXBL];
         uint8_t meth[JXS_MAXBL];
         for (uint32_t fb = 0; fb < cfg->nbands; fb++) {
-            const jxs_band_t& bd = cfg->band[fb];
-            const uint32_t lines = last ? bd.last_lines : bd.lines;
-            uint32_t cn = 0, cs = bd.sig_w * lines;
-            for (uint32_t l = 0; l < lines; l++) {
-                const PackBL& b = bl[blmap[fb * 4 + l]];
-                cn += b.nosig_bits;
-                cs += b.nosig_bits - b.zeroed_bits;
-            }
-            meth[fb] = (uint8_t)(cfg->sig && cn > cs);
+            cn[fb] = 0;
+            cs[fb] = 0;
         }
-        uint8_t* bytes = (uint8_t*)buf;
+        for (uint32_t b = 0; b < nbl; b++) {
+            const jxs_bline_t& B = bls[b];
+            uint32_t d = 0, v = 0, z = 0;
+            for (uint32_t i = B.seg0; i < B.seg0 + B.nseg; i++) {
+                d += s_data[i];
+                v += s_vlc[i];
+                z += s_zero[i];
+            }
+            pl[b].data = d;
+            pl[b].vlc = v;
+            pl[b].zero = z;
+            cn[B.fb] += v;
+            cs[B.fb] += v - z + B.sig_w;
+        }
+        /* coding method per band: significance only if strictly cheaper
+         * (RateControl.c:528-575) */
+        for (uint32_t fb = 0; fb < cfg->nbands; fb++) meth[fb] = (uint8_t)(cfg->sig && cn[fb] > cs[fb]);
+        uint8_t* bytes = (uint8_t*)buf + lead;
         const uint32_t hdr = cfg->prec_hdr_bytes;
         const uint32_t lprc = total - hdr;
         bytes[0] = (uint8_t)(lprc >> 16);
@@ -554,19 +575,19 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
             bytes[pos >> 3] |= (uint8_t)(d << (6 - (pos & 7)));
             pos += 2;
         }
-        pos = hdr * 8;
-        uint32_t vlc_run = 0, data_run = 0;
-        int b = 0;
-        for (uint32_t k = 0; k < cfg->npk; k++) {
-            if (b >= nbl || bl[b].pk != k) continue; /* packet absent in this precinct */
-            int b_end = b;
+        pos = (lead + hdr) * 8;
+        uint32_t b = 0;
+        int ok = 1;
+        for (uint32_t k = 0; k < cfg->npk && ok; k++) {
+            if (b >= nbl || bls[b].pk != k) continue; /* packet absent in this precinct */
+            uint32_t b_end = b;
             uint32_t db = 0, gbits = 0, sbits = 0;
-            while (b_end < nbl && bl[b_end].pk == k) {
-                PackBL& B = bl[b_end];
-                B.meth = meth[B.fb];
-                db += B.data_bits;
-                gbits += B.meth ? B.nosig_bits - B.zeroed_bits : B.nosig_bits;
-                sbits += B.meth ? B.sig_w : 0;
+            while (b_end < nbl && bls[b_end].pk == k) {
+                PkLine& L = pl[b_end];
+                L.meth = meth[bls[b_end].fb];
+                db += L.data;
+                gbits += L.meth ? L.vlc - L.zero : L.vlc;
+                sbits += L.meth ? bls[b_end].sig_w : 0;
                 b_end++;
             }
             const uint32_t dB = (db + 7) >> 3, gB = (gbits + 7) >> 3, sB = (sbits + 7) >> 3;
@@ -576,146 +597,130 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
             /* packet header (PackHeaders.c:98-127), sign length 0 */
             const uint32_t hp = pos >> 3;
             if (hp + (cfg->short_hdr ? 5u : 7u) > words * 4) {
-                pos = 0xffffffffu; /* inconsistent sizes: rejected below */
+                ok = 0;
                 break;
             }
+            uint8_t* hb = (uint8_t*)buf + hp;
             if (cfg->short_hdr) {
-                bytes[hp + 0] = (uint8_t)((raw << 7) | ((dB >> 8) & 0x7f));
-                bytes[hp + 1] = (uint8_t)dB;
-                bytes[hp + 2] = (uint8_t)(gcl_bytes >> 5);
-                bytes[hp + 3] = (uint8_t)((gcl_bytes & 0x1f) << 3);
-                bytes[hp + 4] = 0;
+                hb[0] = (uint8_t)((raw << 7) | ((dB >> 8) & 0x7f));
+                hb[1] = (uint8_t)dB;
+                hb[2] = (uint8_t)(gcl_bytes >> 5);
+                hb[3] = (uint8_t)((gcl_bytes & 0x1f) << 3);
+                hb[4] = 0;
                 pos += 40;
             } else {
-                bytes[hp + 0] = (uint8_t)((raw << 7) | ((dB >> 13) & 0x7f));
-                bytes[hp + 1] = (uint8_t)(dB >> 5);
-                bytes[hp + 2] = (uint8_t)(((dB & 0x1f) << 3) | ((gcl_bytes >> 17) & 7));
-                bytes[hp + 3] = (uint8_t)(gcl_bytes >> 9);
-                bytes[hp + 4] = (uint8_t)(gcl_bytes >> 1);
-                bytes[hp + 5] = (uint8_t)((gcl_bytes & 1) << 7);
-                bytes[hp + 6] = 0;
+                hb[0] = (uint8_t)((raw << 7) | ((dB >> 13) & 0x7f));
+                hb[1] = (uint8_t)(dB >> 5);
+                hb[2] = (uint8_t)(((dB & 0x1f) << 3) | ((gcl_bytes >> 17) & 7));
+                hb[3] = (uint8_t)(gcl_bytes >> 9);
+                hb[4] = (uint8_t)(gcl_bytes >> 1);
+                hb[5] = (uint8_t)((gcl_bytes & 1) << 7);
+                hb[6] = 0;
                 pos += 56;
             }
             if (raw) {
                 uint32_t gp = pos;
-                for (int x = b; x < b_end; x++) {
-                    bl[x].raw = 1;
-                    bl[x].gcli_pos = gp;
-                    gp += 4 * bl[x].gcli_w;
-                    bl[x].vlc_pref = vlc_run;
+                for (uint32_t x = b; x < b_end; x++) {
+                    pl[x].raw = 1;
+                    pl[x].gcli_pos = gp;
+                    gp += 4 * bls[x].gcli_w;
                 }
                 pos += rawB * 8;
             } else {
                 uint32_t sp = pos;
-                for (int x = b; x < b_end; x++) {
-                    bl[x].raw = 0;
-                    bl[x].sig_pos = sp;
-                    if (bl[x].meth) sp += bl[x].sig_w;
+                for (uint32_t x = b; x < b_end; x++) {
+                    pl[x].raw = 0;
+                    pl[x].sig_pos = sp;
+                    if (pl[x].meth) sp += bls[x].sig_w;
                 }
                 pos += sB * 8;
                 uint32_t gp = pos;
-                for (int x = b; x < b_end; x++) {
-                    bl[x].gcli_pos = gp;
-                    bl[x].vlc_pref = vlc_run;
-                    const uint32_t n = bl[x].meth ? bl[x].nosig_bits - bl[x].zeroed_bits : bl[x].nosig_bits;
-                    gp += n;
-                    vlc_run += n;
+                for (uint32_t x = b; x < b_end; x++) {
+                    pl[x].gcli_pos = gp;
+                    gp += pl[x].meth ? pl[x].vlc - pl[x].zero : pl[x].vlc;
                 }
                 pos += gB * 8;
             }
             uint32_t dp = pos;
-            for (int x = b; x < b_end; x++) {
-                bl[x].data_pos = dp;
-                bl[x].data_pref = data_run;
-                dp += bl[x].data_bits;
-                data_run += bl[x].data_bits;
+            for (uint32_t x = b; x < b_end; x++) {
+                pl[x].data_pos = dp;
+                dp += pl[x].data;
             }
             pos += dB * 8;
             b = b_end;
         }
+        /* each segment's start in its band line's GCLI and data sub-packets */
+        for (uint32_t x = 0; x < nbl && ok; x++) {
+            const jxs_bline_t& B = bls[x];
+            uint32_t vp = pl[x].gcli_pos, dp = pl[x].data_pos;
+            for (uint32_t i = B.seg0; i < B.seg0 + B.nseg; i++) {
+                const uint32_t vb = pl[x].meth ? s_vlc[i] - s_zero[i] : s_vlc[i], d = s_data[i];
+                s_vlc[i] = vp;
+                s_data[i] = dp;
+                vp += vb;
+                dp += d;
+            }
+        }
         /* the packed size must be what the rate control paid for */
-        s_ok = pos != 0xffffffffu && (pos & 7) == 0 && (pos >> 3) <= total && (pos >> 3) == cfg->hdrs_bytes[last] + R.data_bytes;
+        const uint32_t end = pos / 8 - lead;
+        s_ok = ok && (pos & 7) == 0 && end <= total && end == cfg->hdrs_bytes[last] + R.data_bytes;
         if (!s_ok) {
-            printf("jxs pack: precinct %d packs to %u bits, rate control paid %u + %u bytes (total %u)\n", p, pos,
+            printf("jxs pack: precinct %d packs to %u bytes, rate control paid %u + %u bytes (total %u)\n", p, end,
                    cfg->hdrs_bytes[last], R.data_bytes, total);
             JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
         }
     }
     __syncthreads();
     if (!s_ok) return;
+
+    /* pass B */
     const uint32_t uniform = cfg->qpih;
-    /* significance flags: 1 = group fully below the truncation */
-    for (uint32_t s = threadIdx.x; s < s_ns; s += blockDim.x) {
-        const int b = find_bl_by_sig((const BandLine*)tmp, nbl, s);
-        const PackBL& B = bl[b];
-        if (B.raw || !B.meth) continue;
-        if (sflag[s]) put_bits(buf, B.sig_pos + (s - B.s0), 1u, 1);
-    }
-    /* GCLIs and data: each thread owns a contiguous run of groups */
-    const uint32_t G = s_ng;
-    const uint32_t per = (G + blockDim.x - 1) / blockDim.x;
-    const uint32_t g_beg = min(G, threadIdx.x * per), g_end = min(G, g_beg + per);
-    uint32_t sum_v = 0, sum_d = 0;
-    {
-        int b = g_beg < g_end ? find_bl_by_group(bl, nbl, g_beg) : 0;
-        for (uint32_t g = g_beg; g < g_end; g++) {
-            while (b + 1 < nbl && bl[b + 1].g0 <= g) b++;
-            const PackBL& B = bl[b];
-            const jxs_band_t& bd = cfg->band[B.fb];
-            const uint32_t x = g - B.g0;
-            const uint32_t v = gcli[bd.gcli_off + (uint64_t)B.row * bd.gpitch + x];
-            const uint32_t t = B.t;
-            if (v > t) sum_d += 4 * (v - t + 1);
-            if (!B.raw) {
-                const bool skip = B.meth && sflag[B.s0 + (x >> 3)];
-                if (!skip) sum_v += v > t ? v - t + 1 : 1;
-            }
-        }
-    }
-    uint32_t ev, ed;
-    block_scan2(sum_v, sum_d, &ev, &ed, wsa, wsb);
-    {
-        int b = g_beg < g_end ? find_bl_by_group(bl, nbl, g_beg) : 0;
-        for (uint32_t g = g_beg; g < g_end; g++) {
-            while (b + 1 < nbl && bl[b + 1].g0 <= g) b++;
-            const PackBL& B = bl[b];
-            const jxs_band_t& bd = cfg->band[B.fb];
-            const uint32_t x = g - B.g0;
-            const uint32_t v = gcli[bd.gcli_off + (uint64_t)B.row * bd.gpitch + x];
-            const uint32_t t = B.t;
-            if (B.raw) {
-                put_bits(buf, B.gcli_pos + 4 * x, v, 4);
+    for (uint32_t sidx = warp; sidx < nseg; sidx += PK_WARPS) {
+        const jxs_seg_t sg = segs[sidx];
+        const jxs_bline_t B = bls[sg.bl];
+        const PkLine L = pl[sg.bl];
+        const jxs_band_t& bd = cfg->band[B.fb];
+        const uint32_t t = tb[B.fb];
+        const uint64_t row = (uint64_t)(p * bd.lines + B.line);
+        const uint8_t* grow = gcli + bd.gcli_off + row * bd.gpitch;
+        const uint16_t* crow = coef + bd.coef_off + row * bd.pitch;
+        const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+        uint32_t vpos = s_vlc[sidx], dpos = s_data[sidx];
+        for (uint32_t base = sg.g0; base < gend; base += 32) {
+            const uint32_t g = base + lane;
+            const bool valid = g < gend;
+            const uint32_t v = valid ? grow[g] : 0u;
+            uint32_t mx = v;
+            mx = max(mx, __shfl_xor_sync(FULL, mx, 1));
+            mx = max(mx, __shfl_xor_sync(FULL, mx, 2));
+            mx = max(mx, __shfl_xor_sync(FULL, mx, 4));
+            uint32_t vlen = 0;
+            if (L.raw) {
+                if (valid) put_bits(buf, L.gcli_pos + 4 * g, v, 4);
             } else {
-                const bool skip = B.meth && sflag[B.s0 + (x >> 3)];
-                if (!skip) {
-                    /* unary code: (v - t) ones then a zero (PackPrecinct.h:25-39) */
-                    const uint32_t n = v > t ? v - t : 0;
-                    put_bits(buf, B.gcli_pos + (ev - B.vlc_pref), ((1u << n) - 1) << 1, n + 1);
-                    ev += n + 1;
+                const bool insig = mx <= t;
+                if (L.meth) {
+                    /* significance flags, 1 = insignificant: lanes 0, 8, 16, 24 */
+                    const uint32_t bal = __ballot_sync(FULL, valid && (lane & 7) == 0 && insig);
+                    if (lane == 0) {
+                        const uint32_t nsg = min(4u, (gend - base + 7) >> 3);
+                        const uint32_t bits = ((bal & 1u) << 3) | (((bal >> 8) & 1u) << 2) | (((bal >> 16) & 1u) << 1) | ((bal >> 24) & 1u);
+                        if (bits >> (4 - nsg)) put_bits(buf, L.sig_pos + (base >> 3), bits >> (4 - nsg), nsg);
+                    }
                 }
+                if (valid && !(L.meth && insig)) vlen = v > t ? v - t + 1 : 1u;
             }
-            if (v > t) {
-                /* data: sign nibble then bit-planes v-1 .. t, coefficient 0 in
-                 * the most significant bit (pack_data_c, PackPrecinct.c:128-198) */
-                const uint16_t* crow = coef + bd.coef_off + (uint64_t)B.row * bd.pitch + 4 * x;
-                const uint2 raw4 = *(const uint2*)crow;
-                uint32_t c[4] = {raw4.x & 0xffffu, raw4.x >> 16, raw4.y & 0xffffu, raw4.y >> 16};
-                uint32_t signs = 0;
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    c[k] = (4 * x + k < B.w) ? quantize(c[k], v, t, uniform) : 0u;
-                    signs = (signs << 1) | (c[k] >> 15);
-                }
-                uint64_t code = signs;
-                for (int bit = (int)v - 1; bit >= (int)t; bit--) {
-                    const uint32_t nib = (((c[0] >> bit) & 1u) << 3) | (((c[1] >> bit) & 1u) << 2) | (((c[2] >> bit) & 1u) << 1) |
-                                         ((c[3] >> bit) & 1u);
-                    code = (code << 4) | nib;
-                }
-                const uint32_t nbits = 4 * (v - t + 1);
-                put_bits64(buf, B.data_pos + (ed - B.data_pref), code, nbits);
-                ed += nbits;
+            const uint32_t dlen = (valid && v > t) ? 4 * (v - t + 1) : 0u;
+            uint32_t tot;
+            const uint32_t ex = warp_excl_scan((dlen << 16) | vlen, &tot);
+            /* unary code: (v - t) ones then a zero (PackPrecinct.h:25-39) */
+            if (vlen) put_bits(buf, vpos + (ex & 0xffffu), ((1u << (vlen - 1)) - 1u) << 1, vlen);
+            if (dlen) {
+                const uint2 raw4 = *(const uint2*)(crow + 4 * g);
+                put_bits64(buf, dpos + (ex >> 16), data_chunk(raw4, (int)B.w - 4 * (int)g, v, t, uniform, lut), dlen);
             }
+            vpos += tot & 0xffffu;
+            dpos += tot >> 16;
         }
     }
     __syncthreads();
@@ -726,11 +731,21 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
         }
         return;
     }
-    /* copy out; slice header, codestream header and EOC around it */
+    /* copy out: whole 16-byte chunks where the precinct covers them, single
+     * bytes at its two ends; slice header, codestream header and EOC around */
     const uint8_t* bytes = (const uint8_t*)buf;
-    uint8_t* dst = out + R.offset;
-    for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) dst[i] = bytes[i];
+    uint8_t* gbase = out + R.offset - lead;
+    const uint32_t nbytes = lead + total;
+    for (uint32_t c = threadIdx.x; c < (nbytes + 15) >> 4; c += blockDim.x) {
+        const uint32_t b0 = c << 4;
+        if (b0 >= lead && b0 + 16 <= nbytes) {
+            *(uint4*)(gbase + b0) = *(const uint4*)(bytes + b0);
+        } else {
+            for (uint32_t i = max(b0, lead); i < min(b0 + 16, nbytes); i++) gbase[i] = bytes[i];
+        }
+    }
     if (threadIdx.x == 0) {
+        uint8_t* dst = out + R.offset;
         if (R.first_in_slice) {
             const uint32_t s = p / cfg->pps;
             uint8_t* sh = dst - 6;
@@ -757,15 +772,10 @@ extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_
 }
 
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
-                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, uint32_t sig_cap, int* status,
-                                       cudaStream_t st) {
-    size_t smem = (size_t)cap_words * 4 + sig_cap;
-    static size_t configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
-    pack_kernel<<<np, PK_THREADS, smem, st>>>(dcfg, coef, gcli, rc, out, cap_words, sig_cap, status);
+                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st) {
+    const size_t smem = (size_t)cap_words * 4;
+    cudaError_t e = cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    pack_kernel<<<np, PK_THREADS, smem, st>>>(dcfg, coef, gcli, rc, out, cap_words, status);
     return cudaGetLastError();
 }

@@ -31,8 +31,7 @@ extern "C" int jxs_fwd_h_max_rows_per_block(void);
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
                                      PrecRC* rc, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
-                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, uint32_t sig_cap, int* status,
-                                       cudaStream_t st);
+                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, const uint32_t* prec_off, int16_t* coef,
                                          uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, const uint8_t* bs, uint32_t size, uint32_t* prec_off,
@@ -165,7 +164,7 @@ struct jxs_gpu_enc {
     jxs_cfg_t* dcfg;
     int nslots;
     EncSlot slot[8];
-    uint32_t cap_words, sig_cap;
+    uint32_t cap_words;
     cudaStream_t user_stream;
     int timing;
     double stage_ms[ENC_STAGES];
@@ -251,13 +250,11 @@ extern "C" jxs_gpu_enc_t* jxs_gpu_enc_create(const jxs_cfg_t* cfg, int nslots, i
     memset(&e->slot, 0, sizeof(e->slot));
     e->cfg = *cfg;
     e->nslots = 0;
-    /* the packing kernel stages a whole precinct in shared memory: bound it by
-     * the largest slice budget and the significance groups of one precinct */
-    uint32_t sig = 0;
-    for (uint32_t b = 0; b < cfg->nbands; b++) sig += cfg->band[b].sig_w * cfg->band[b].lines;
-    e->sig_cap = (sig + 16) & ~15u;
-    e->cap_words = div_up(cfg->max_slice_budget, 4) + 4;
-    if ((size_t)e->cap_words * 4 + e->sig_cap > kSmemMax) {
+    /* the packing kernel stages a whole precinct in shared memory, starting
+     * up to 15 bytes into the buffer for aligned stores: bound it by the
+     * largest slice budget */
+    e->cap_words = 4 * div_up(cfg->max_slice_budget + 15, 16) + 4;
+    if ((size_t)e->cap_words * 4 > kSmemMax - 16 * 1024) {
         fprintf(stderr, "jxs: precincts of this configuration (%u bytes per slice) exceed the on-chip packing buffer\n",
                 cfg->max_slice_budget);
         delete e;
@@ -404,7 +401,7 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
     TMARK(3);
     const int out_dev = jxs_gpu_is_device_ptr(out);
     uint8_t* dst = out_dev ? out : s->out_stage;
-    CK(jxs_launch_pack(e->dcfg, c->np, s->coef, s->gcli, s->rc, dst, e->cap_words, e->sig_cap, s->status, st));
+    CK(jxs_launch_pack(e->dcfg, c->np, s->coef, s->gcli, s->rc, dst, e->cap_words, s->status, st));
     TMARK(4);
     if (!out_dev) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
