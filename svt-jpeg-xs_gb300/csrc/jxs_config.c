@@ -47,7 +47,7 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
     for (;;) {
         int fits = 1;
         for (int t = 0; t < 2; t++) {
-            uint32_t n = 0, ns = 0;
+            uint32_t n = 0, ns = 0, gsum = 0;
             for (uint32_t k = 0; k < g->npk; k++) {
                 const uint32_t l = g->pk[k].line;
                 for (uint32_t gb = g->pk[k].bs; gb < g->pk[k].be; gb++) {
@@ -64,6 +64,8 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
                     b->gcli_w = bd->gcli_w;
                     b->sig_w = bd->sig_w;
                     b->w = bd->w;
+                    b->gbase = gsum;
+                    gsum += bd->gcli_w;
                     b->seg0 = ns;
                     b->nseg = (bd->gcli_w + sg - 1) / sg;
                     if (b->nseg == 0) b->nseg = 1;

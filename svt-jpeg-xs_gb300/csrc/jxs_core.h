@@ -74,6 +74,7 @@ typedef struct jxs_bline {
     uint8_t fb, line, pk, pad;  /* flat band, line inside the precinct row, packet */
     uint32_t gcli_w, sig_w, w;  /* groups, significance groups, coefficients */
     uint32_t seg0, nseg;        /* its segments */
+    uint32_t gbase;             /* its first group in the precinct's band-line order */
 } jxs_bline_t;
 typedef struct jxs_seg {
     uint16_t bl, pad;           /* band line */

@@ -22,54 +22,53 @@
 #include "jxs_kernels.cuh"
 
 #define DEV __device__ __forceinline__
-#define UK_THREADS 256
-#define UK_MAXBL 80
 
-struct DecBL {
-    uint16_t fb;
-    uint8_t line, pk, t, mode, raw;
-    uint32_t row, gcli_w, sig_w, w;
-    uint32_t g0, s0;
-    uint32_t sig_pos, gcli_pos; /* bit positions inside the precinct */
+#define UK_THREADS 512
+#define UK_WARPS (UK_THREADS / 32)
+#define FULL 0xffffffffu
+
+/* Per band line of the precinct being unpacked. */
+struct UkLine {
+    uint32_t sig_pos;           /* bit position of its significance flags */
+    uint8_t t, meth, raw, pk;
+};
+/* Per packet. */
+struct UkPk {
+    uint32_t gpos, gbits;       /* GCLI sub-packet: bit position and length */
+    uint32_t dpos, dbits;       /* data sub-packet */
+    uint32_t wbase, nwords;     /* its 32-bit words in the concatenated GCLI word list (VLC packets) */
+    uint32_t zbase, nzero;      /* rank of its first zero bit among all VLC zeros; zeros in its range */
+    uint32_t ncoded;            /* unary codewords */
+    uint32_t raw, present;
 };
 
-struct DecPk {
-    uint32_t gcli_pos, gcli_bits, data_pos, data_bits;
-    uint32_t b_beg, b_end, g_beg, g_end;
-    uint32_t raw;
-};
+/* 32 bits of a big-endian bit string held in shared memory, starting at
+ * bit `pos`; the buffer must be readable 8 bytes past pos / 8. */
+DEV uint32_t be_word(const uint8_t* b, uint32_t wi) { return __byte_perm(((const uint32_t*)b)[wi], 0, 0x0123); }
+DEV uint32_t bits32_at(const uint8_t* b, uint32_t pos) {
+    const uint32_t wi = pos >> 5;
+    return __funnelshift_l(be_word(b, wi + 1), be_word(b, wi), pos & 31);
+}
 
-DEV uint32_t bit_at(const uint8_t* p, uint32_t pos) { return (p[pos >> 3] >> (7 - (pos & 7))) & 1u; }
+/* every 4th bit (positions 0, 4, ..., 28) gathered into bits 0..7 */
+DEV uint32_t compact4(uint32_t x) {
+    x &= 0x11111111u;
+    x = (x | (x >> 3)) & 0x03030303u;
+    x = (x | (x >> 6)) & 0x000f000fu;
+    x = (x | (x >> 12)) & 0x000000ffu;
+    return x;
+}
 
-/* Up to 64 bits starting at `pos` (MSB first). Reads bytes up to pos/8 + 8. */
-DEV uint64_t bits64(const uint8_t* p, uint32_t pos, uint32_t n) {
-    const uint32_t b = pos >> 3, sh = pos & 7;
-    uint64_t v = 0;
+DEV uint32_t warp_excl_scan(uint32_t x, uint32_t* total) {
+    const int lane = threadIdx.x & 31;
+    uint32_t inc = x;
 #pragma unroll
-    for (int k = 0; k < 8; k++) v = (v << 8) | p[b + k];
-    uint64_t extra = p[b + 8];
-    v = (v << sh) | (extra >> (8 - sh) & ((1u << sh) - 1));
-    return n == 64 ? v : (v >> (64 - n));
-}
-
-DEV int find_dbl_by_group(const DecBL* bl, int n, uint32_t g) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (bl[mid].g0 <= g) lo = mid;
-        else hi = mid - 1;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(FULL, inc, o);
+        if (lane >= o) inc += y;
     }
-    return lo;
-}
-
-DEV int find_dbl_by_sig(const DecBL* bl, int n, uint32_t s) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (bl[mid].s0 <= s) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
+    *total = __shfl_sync(FULL, inc, 31);
+    return inc - x;
 }
 
 /* Block-wide exclusive scan of one counter; returns the block total. */
@@ -77,7 +76,7 @@ DEV uint32_t block_scan1(uint32_t a, uint32_t* ea, uint32_t* ws) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     uint32_t ia = a;
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t t = __shfl_up_sync(0xffffffffu, ia, o);
+        uint32_t t = __shfl_up_sync(FULL, ia, o);
         if (lane >= o) ia += t;
     }
     if (lane == 31) ws[warp] = ia;
@@ -85,7 +84,7 @@ DEV uint32_t block_scan1(uint32_t a, uint32_t* ea, uint32_t* ws) {
     if (warp == 0) {
         uint32_t v = lane < nw ? ws[lane] : 0;
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+            uint32_t t = __shfl_up_sync(FULL, v, o);
             if (lane >= o) v += t;
         }
         if (lane < nw) ws[lane] = v;
@@ -97,97 +96,147 @@ DEV uint32_t block_scan1(uint32_t a, uint32_t* ea, uint32_t* ws) {
     return total;
 }
 
-/* dynamic shared memory: [precinct bytes (cap_bytes + 16)] [GCLI per group (cap_groups)]
- * [significance flag per significance group (cap_groups)] [zero positions (4 B x cap_groups)] */
+/* One group's coefficients from its data bits (unpack_data_c,
+ * Packing.c:134-219): sign nibble (coefficient 0 in the most significant
+ * bit), then bit-planes gcli-1 .. gtli; planes placed at << gtli
+ * (Packing.c:117-132), deadzone or uniform dequantization (Dequant.c:9-57)
+ * and sign-magnitude to two's complement (inv_sign_c, Precinct.c:9-14). */
+DEV void decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uint32_t uniform, int32_t out[4]) {
+    const uint32_t sgn = (uint32_t)(chunk >> (4 * np)) & 15u;
+    const uint64_t planes = np >= 16 ? chunk : chunk & ((1ull << (4 * np)) - 1);
+    const uint32_t lo = (uint32_t)planes, hi = (uint32_t)(planes >> 32);
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        uint32_t m = compact4(lo >> (3 - c));
+        if (np > 8) m |= compact4(hi >> (3 - c)) << 8;
+        uint32_t mag = (m << t) & 0xffffu;
+        if (t > 0 && (mag & 0x7fffu)) {
+            if (!uniform) {
+                mag |= 1u << (t - 1);
+            } else {
+                /* inv_quant_uniform (Dequant.c:23-43) */
+                uint32_t val = mag & 0x7fffu, acc = 0;
+                const uint32_t sc = gv - t + 1;
+                for (; val > 0; val >>= sc) acc = (acc + val) & 0xffffu;
+                mag = acc;
+            }
+        }
+        const uint32_t sm = (mag | (((sgn >> (3 - c)) & 1u) << 15)) & 0xffffu;
+        out[c] = (sm & 0x8000u) ? -(int32_t)(sm & 0x7fffu) : (int32_t)sm;
+    }
+}
+
+/* unpack_precinct (Packing.c:513-868) for one precinct row; vertical
+ * prediction and separate sign sub-packets are rejected.
+ *
+ * Dynamic shared memory: [precinct bytes: cap_bytes + 32, stream byte i at
+ * i + lead so that 16-byte chunks are aligned] [GCLI per group: cap_groups]
+ * [end bit of each unary codeword: 4 x cap_groups].
+ *
+ *   copy    the precinct's bytes into shared memory;
+ *   parse   thread 0: precinct header, packet headers, sub-packet positions
+ *           with the reference's length checks;
+ *   pass 1  warp per segment: groups with a unary codeword (the
+ *           significance flags drop the insignificant ones); raw GCLIs;
+ *   zeros   block pass over the VLC sub-packets: codeword c of a packet ends
+ *           at the c-th zero bit of its sub-packet (unpack_pred_zero_gclis_*,
+ *           Packing.c:435-511);
+ *   pass 2  warp per segment: GCLI = gtli + ones in the codeword; data bits;
+ *   pass 3  warp per segment: data bits at warp-scanned offsets, decoded and
+ *           written as int16 coefficients (8 bytes per lane, coalesced). */
 __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs,
-                                                            const uint32_t* __restrict__ prec_off, int16_t* __restrict__ coef,
-                                                            uint32_t cap_bytes, uint32_t cap_groups, int* status) {
+                                                            uint32_t bs_size, const uint32_t* __restrict__ prec_off,
+                                                            int16_t* __restrict__ coef, uint32_t cap_bytes, uint32_t cap_groups,
+                                                            int* status) {
     extern __shared__ __align__(16) uint8_t dsm[];
     uint8_t* pbuf = dsm;
-    uint8_t* gcl = dsm + cap_bytes + 16;
-    uint8_t* sflag = gcl + cap_groups;
-    uint32_t* zpos = (uint32_t*)(((uintptr_t)(sflag + cap_groups) + 15) & ~(uintptr_t)15);
-    __shared__ DecBL bl[UK_MAXBL];
-    __shared__ DecPk pk[JXS_MAXPK];
-    __shared__ uint32_t pk_pref[JXS_MAXPK];
-    __shared__ uint32_t ws[UK_THREADS / 32];
-    __shared__ int s_nbl, s_err;
-    __shared__ uint32_t s_total, s_ng, s_ns;
+    uint8_t* gcl = dsm + cap_bytes + 32;
+    uint32_t* zend = (uint32_t*)(((uintptr_t)(gcl + cap_groups) + 15) & ~(uintptr_t)15);
+    __shared__ UkLine ln[JXS_MAXBLINES];
+    __shared__ UkPk pk[JXS_MAXPK];
+    __shared__ uint32_t s_cnt[JXS_MAXSEG], s_base[JXS_MAXSEG];
+    __shared__ uint32_t ws[UK_WARPS];
+    __shared__ int s_err;
+    __shared__ uint32_t s_total, s_lead, s_tw, s_npk;
 
     const int p = blockIdx.x;
     const int last = (p + 1 >= (int)cfg->np);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) s_err = *(volatile int*)status;
     __syncthreads();
     if (s_err) return; /* the precinct offsets could not be found */
-    const uint8_t* src = bs + prec_off[p];
+    const uint32_t off = prec_off[p];
     if (threadIdx.x == 0) {
         s_err = 0;
-        const uint32_t lprc = ((uint32_t)src[0] << 16) | ((uint32_t)src[1] << 8) | src[2];
-        s_total = cfg->prec_hdr_bytes + lprc;
-        if (lprc > JXS_PREC_MAX_BYTES || s_total > cap_bytes) s_err = JXS_E_DEC_BITSTREAM;
+        if ((uint64_t)off + cfg->prec_hdr_bytes > bs_size) {
+            s_err = JXS_E_DEC_SHORT;
+        } else {
+            const uint32_t lprc = ((uint32_t)bs[off] << 16) | ((uint32_t)bs[off + 1] << 8) | bs[off + 2];
+            s_total = cfg->prec_hdr_bytes + lprc;
+            s_lead = (uint32_t)((uintptr_t)(bs + off) & 15);
+            if (lprc > JXS_PREC_MAX_BYTES || s_total + 48 > cap_bytes) s_err = JXS_E_DEC_BITSTREAM;
+            else if ((uint64_t)off + s_total > bs_size) s_err = JXS_E_DEC_SHORT;
+        }
     }
     __syncthreads();
     if (s_err) {
         if (threadIdx.x == 0) JXS_STATUS_SET(status, s_err);
         return;
     }
-    const uint32_t total = s_total;
-    for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) pbuf[i] = src[i];
-    for (uint32_t i = threadIdx.x; i < 16; i += blockDim.x) pbuf[total + i] = 0;
+    const uint32_t total = s_total, lead = s_lead;
+    {
+        /* aligned 16-byte chunks inside the precinct, single bytes at its
+         * ends; 32 zero bytes after it for the bit readers */
+        const uint8_t* gsrc = bs + off - lead;
+        const uint32_t nbytes = lead + total, nch = (nbytes + 15) >> 4;
+        for (uint32_t c = threadIdx.x; c < nch + 2; c += blockDim.x) {
+            const uint32_t b0 = c << 4;
+            if (b0 >= lead && b0 + 16 <= nbytes) {
+                *(uint4*)(pbuf + b0) = *(const uint4*)(gsrc + b0);
+            } else {
+                for (uint32_t i = b0; i < b0 + 16; i++) pbuf[i] = (i >= lead && i < nbytes) ? gsrc[i] : 0;
+            }
+        }
+    }
     __syncthreads();
 
+    const uint32_t nbl = cfg->nbline[last], nseg = cfg->nseg[last], SG = cfg->seg_groups;
+    const jxs_bline_t* bls = cfg->bline[last];
+    const jxs_seg_t* segs = cfg->seg[last];
+    /* parse */
     if (threadIdx.x == 0) {
         int err = 0;
-        const uint8_t q = pbuf[3], r = pbuf[4];
+        const uint8_t* h0 = pbuf + lead;
+        const uint8_t q = h0[3], r = h0[4];
         const uint32_t lprc = total - cfg->prec_hdr_bytes;
-        /* band coding modes D[p,b], 2 bits per existing band */
         uint8_t mode[JXS_MAXBL];
         uint32_t pos = 40;
         for (uint32_t gb = 0; gb < cfg->nbands_all; gb++) {
             const int fb = cfg->g2f[gb];
             if (fb == JXS_NOBAND) continue;
-            mode[fb] = (uint8_t)((pbuf[pos >> 3] >> (6 - (pos & 7))) & 3);
+            mode[fb] = (uint8_t)((h0[pos >> 3] >> (6 - (pos & 7))) & 3);
             pos += 2;
             if (mode[fb] & 1) err = JXS_E_DEC_BITSTREAM; /* vertical prediction is not part of this decoder */
         }
-        /* band lines in packet order */
-        int n = 0;
-        uint32_t g0 = 0, s0 = 0;
-        for (uint32_t k = 0; k < cfg->npk; k++) {
-            const uint32_t l = cfg->pk[k].line;
-            for (uint32_t gb = cfg->pk[k].bs; gb < cfg->pk[k].be; gb++) {
-                const int fb = cfg->g2f[gb];
-                const jxs_band_t& bd = cfg->band[fb];
-                if (l >= (last ? bd.last_lines : bd.lines)) continue;
-                DecBL& b = bl[n++];
-                b.fb = (uint16_t)fb; b.line = (uint8_t)l; b.pk = (uint8_t)k;
-                b.t = jxs_truncation(bd.gain, bd.prio, q, r);
-                b.mode = mode[fb];
-                b.row = (uint32_t)p * bd.lines + l;
-                b.gcli_w = bd.gcli_w; b.sig_w = bd.sig_w; b.w = bd.w;
-                b.g0 = g0; b.s0 = s0;
-                g0 += bd.gcli_w;
-                s0 += bd.sig_w;
-            }
+        for (uint32_t x = 0; x < nbl; x++) {
+            const jxs_band_t& bd = cfg->band[bls[x].fb];
+            ln[x].t = jxs_truncation(bd.gain, bd.prio, q, r);
+            ln[x].meth = (mode[bls[x].fb] & 2) ? 1 : 0;
+            ln[x].pk = bls[x].pk;
         }
-        s_nbl = n;
-        s_ng = g0;
-        s_ns = s0;
-        if (g0 > cap_groups) err = JXS_E_DEC_INTERNAL;
-        /* packet headers and sub-packet positions */
         const int long_hdr = cfg->lh || !cfg->short_hdr;
         int64_t left = (int64_t)lprc * 8;
-        uint32_t bpos = cfg->prec_hdr_bytes; /* bytes */
-        int b = 0;
-        for (uint32_t k = 0; k < cfg->npk && !err; k++) {
-            DecPk& P = pk[k];
-            P.b_beg = P.b_end = b;
-            P.g_beg = P.g_end = (b < n) ? bl[b].g0 : g0;
-            P.gcli_bits = P.data_bits = 0;
+        uint32_t bpos = lead + cfg->prec_hdr_bytes; /* bytes */
+        uint32_t b = 0, tw = 0;
+        for (uint32_t k = 0; k < cfg->npk; k++) {
+            UkPk& P = pk[k];
+            P.present = 0;
+            P.gbits = P.dbits = P.nwords = P.ncoded = P.nzero = 0;
             P.raw = 0;
-            if (b >= n || bl[b].pk != k) continue;
-            int be = b;
-            while (be < n && bl[be].pk == k) be++;
+            P.wbase = tw;
+            if (err || b >= nbl || bls[b].pk != k) continue;
+            uint32_t be = b;
+            while (be < nbl && bls[be].pk == k) be++;
             const uint32_t hb = long_hdr ? 7 : 5;
             left -= hb * 8;
             if (left < 0) { err = JXS_E_DEC_BITSTREAM; break; }
@@ -208,25 +257,19 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
             if ((uint64_t)left < ((uint64_t)dlen + glen + slen) * 8) { err = JXS_E_DEC_BITSTREAM; break; }
             P.raw = raw;
             if (raw) {
-                uint32_t gp = bpos * 8, need = 0;
-                for (int x = b; x < be; x++) {
-                    bl[x].raw = 1;
-                    bl[x].gcli_pos = gp;
-                    gp += 4 * bl[x].gcli_w;
-                    need += 4 * bl[x].gcli_w;
+                uint32_t need = 0;
+                for (uint32_t x = b; x < be; x++) {
+                    ln[x].raw = 1;
+                    need += 4 * bls[x].gcli_w;
                 }
-                left -= need;
-                if (left < 0 || need > glen * 8) { err = JXS_E_DEC_BITSTREAM; break; }
-                left -= (int64_t)glen * 8 - need; /* skipped padding inside the sub-packet */
+                if (need > glen * 8) { err = JXS_E_DEC_BITSTREAM; break; }
+                left -= (int64_t)glen * 8;
             } else {
-                uint32_t sp = bpos * 8, sbits = 0;
-                for (int x = b; x < be; x++) {
-                    bl[x].raw = 0;
-                    bl[x].sig_pos = sp;
-                    if (bl[x].mode & 2) {
-                        sp += bl[x].sig_w;
-                        sbits += bl[x].sig_w;
-                    }
+                uint32_t sbits = 0;
+                for (uint32_t x = b; x < be; x++) {
+                    ln[x].raw = 0;
+                    ln[x].sig_pos = bpos * 8 + sbits;
+                    if (ln[x].meth) sbits += bls[x].sig_w;
                 }
                 left -= sbits;
                 if (left < 0) { err = JXS_E_DEC_BITSTREAM; break; }
@@ -234,20 +277,124 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
                 bpos += (sbits + 7) >> 3;
                 left -= (int64_t)glen * 8;
             }
-            P.gcli_pos = bpos * 8;
-            P.gcli_bits = glen * 8;
+            P.gpos = bpos * 8;
+            P.gbits = glen * 8;
             bpos += glen;
-            P.data_pos = bpos * 8;
-            P.data_bits = dlen * 8;
+            P.dpos = bpos * 8;
+            P.dbits = dlen * 8;
             bpos += dlen;
             left -= (int64_t)dlen * 8;
-            bpos += cfg->fs ? slen : 0;
             if (cfg->fs) err = JXS_E_DEC_BITSTREAM; /* separate sign sub-packets are not part of this decoder */
-            if (left < 0 || bpos > total) { err = JXS_E_DEC_BITSTREAM; break; }
-            P.b_beg = b; P.b_end = be;
-            P.g_beg = bl[b].g0;
-            P.g_end = (be < n) ? bl[be].g0 : g0;
+            bpos += slen;
+            if (left < 0 || bpos > lead + total) { err = JXS_E_DEC_BITSTREAM; break; }
+            P.present = 1;
+            if (!raw) {
+                P.nwords = (P.gbits + 31) >> 5;
+                tw += P.nwords;
+            }
             b = be;
+        }
+        s_tw = tw;
+        s_npk = cfg->npk;
+        s_err = err;
+    }
+    __syncthreads();
+    if (s_err) {
+        if (threadIdx.x == 0) JXS_STATUS_SET(status, s_err);
+        return;
+    }
+
+    /* pass 1: codewords per segment; raw GCLIs and insignificant groups */
+    for (uint32_t sidx = warp; sidx < nseg; sidx += UK_WARPS) {
+        const jxs_seg_t sg = segs[sidx];
+        const jxs_bline_t B = bls[sg.bl];
+        const UkLine L = ln[sg.bl];
+        const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+        uint32_t cnt = 0;
+        for (uint32_t base = sg.g0; base < gend; base += 32) {
+            const uint32_t g = base + lane;
+            if (g < gend) {
+                if (L.raw) {
+                    const uint32_t pos = pk[L.pk].gpos + 4 * g;
+                    gcl[B.gbase + g] = (uint8_t)((pbuf[pos >> 3] >> (4 - (pos & 7))) & 15);
+                } else {
+                    const uint32_t sp = L.sig_pos + (g >> 3);
+                    const bool insig = L.meth && ((pbuf[sp >> 3] >> (7 - (sp & 7))) & 1);
+                    if (insig) gcl[B.gbase + g] = L.t;
+                    cnt += !insig;
+                }
+            }
+        }
+        cnt = __reduce_add_sync(FULL, cnt);
+        if (lane == 0) s_cnt[sidx] = cnt;
+    }
+    __syncthreads();
+    /* codeword base of every segment inside its packet */
+    if (threadIdx.x == 0) {
+        for (uint32_t x = 0; x < nbl; x++) {
+            if (ln[x].raw) continue;
+            UkPk& P = pk[ln[x].pk];
+            for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
+                s_base[i] = P.ncoded;
+                P.ncoded += s_cnt[i];
+            }
+        }
+    }
+    /* zero bits of the VLC sub-packets: count, scan, record positions */
+    const uint32_t tw = s_tw, npk = s_npk;
+    const uint32_t per = (tw + blockDim.x - 1) / blockDim.x;
+    const uint32_t wa = min(tw, threadIdx.x * per), we = min(tw, wa + per);
+    uint32_t zc = 0;
+    {
+        uint32_t k = 0;
+        for (uint32_t wi = wa; wi < we; wi++) {
+            while (k + 1 < npk && (!pk[k].present || pk[k].raw || wi >= pk[k].wbase + pk[k].nwords)) k++;
+            const uint32_t i = wi - pk[k].wbase;
+            const uint32_t valid = min(32u, pk[k].gbits - 32 * i);
+            uint32_t z = ~bits32_at(pbuf, pk[k].gpos + 32 * i);
+            if (valid < 32) z &= ~(0xffffffffu >> valid);
+            zc += __popc(z);
+        }
+    }
+    uint32_t z0;
+    const uint32_t ztotal = block_scan1(zc, &z0, ws);
+    {
+        uint32_t k = 0;
+        for (uint32_t wi = wa; wi < we; wi++) {
+            while (k + 1 < npk && (!pk[k].present || pk[k].raw || wi >= pk[k].wbase + pk[k].nwords)) k++;
+            const uint32_t i = wi - pk[k].wbase;
+            if (i == 0) pk[k].zbase = z0;
+            const uint32_t valid = min(32u, pk[k].gbits - 32 * i);
+            uint32_t z = ~bits32_at(pbuf, pk[k].gpos + 32 * i);
+            if (valid < 32) z &= ~(0xffffffffu >> valid);
+            while (z) {
+                const uint32_t lz = __clz(z);
+                if (z0 < cap_groups) zend[z0] = pk[k].gpos + 32 * i + lz;
+                z0++;
+                z &= ~(0x80000000u >> lz);
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int err = 0;
+        for (uint32_t k = 0; k < npk; k++) {
+            UkPk& P = pk[k];
+            if (!P.present || P.raw) continue;
+            if (P.nwords == 0) {
+                P.zbase = 0;
+                P.nzero = 0;
+            } else {
+                /* zeros of this packet: up to the next VLC packet's first zero */
+                uint32_t znext = ztotal;
+                for (uint32_t k2 = k + 1; k2 < npk; k2++)
+                    if (pk[k2].present && !pk[k2].raw && pk[k2].nwords) {
+                        znext = pk[k2].zbase;
+                        break;
+                    }
+                P.nzero = znext - P.zbase;
+            }
+            if (P.ncoded > P.nzero || (P.ncoded && P.zbase + P.ncoded > cap_groups)) err = JXS_E_DEC_BITSTREAM;
         }
         s_err = err;
     }
@@ -256,186 +403,101 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
         if (threadIdx.x == 0) JXS_STATUS_SET(status, s_err);
         return;
     }
-    const int nbl = s_nbl;
-    const uint32_t G = s_ng;
-    /* significance flags (1 = group insignificant) and raw GCLIs */
-    for (uint32_t s = threadIdx.x; s < s_ns; s += blockDim.x) {
-        const DecBL& B = bl[find_dbl_by_sig(bl, nbl, s)];
-        sflag[s] = (!B.raw && (B.mode & 2)) ? (uint8_t)bit_at(pbuf, B.sig_pos + (s - B.s0)) : 0;
-    }
-    for (uint32_t g = threadIdx.x; g < G; g += blockDim.x) {
-        const DecBL& B = bl[find_dbl_by_group(bl, nbl, g)];
-        if (B.raw) {
-            const uint32_t pos = B.gcli_pos + 4 * (g - B.g0);
-            gcl[g] = (uint8_t)((pbuf[pos >> 3] >> (4 - (pos & 7))) & 15);
-        }
-    }
-    __syncthreads();
-    /* unary-coded GCLIs, one packet at a time: codeword j ends at the j-th
-     * zero bit of the sub-packet (unpack_pred_zero_gclis_*, Packing.c:435-511) */
-    for (uint32_t k = 0; k < cfg->npk; k++) {
-        const DecPk P = pk[k];
-        if (P.b_beg == P.b_end || P.raw) continue;
-        /* codeword index of each coded group */
-        const uint32_t ng = P.g_end - P.g_beg;
-        const uint32_t per = (ng + blockDim.x - 1) / blockDim.x;
-        const uint32_t a = min(ng, threadIdx.x * per), e = min(ng, a + per);
-        uint32_t cnt = 0;
-        int bidx = a < e ? find_dbl_by_group(bl, nbl, P.g_beg + a) : 0;
-        for (uint32_t i = a; i < e; i++) {
-            const uint32_t g = P.g_beg + i;
-            while (bidx + 1 < nbl && bl[bidx + 1].g0 <= g) bidx++;
-            const DecBL& B = bl[bidx];
-            cnt += !((B.mode & 2) && sflag[B.s0 + ((g - B.g0) >> 3)]);
-        }
-        uint32_t cw0;
-        const uint32_t ncw = block_scan1(cnt, &cw0, ws);
-        /* zero positions */
-        const uint32_t nbits = P.gcli_bits, nwords = (nbits + 31) >> 5;
-        const uint32_t wper = (nwords + blockDim.x - 1) / blockDim.x;
-        const uint32_t wa = min(nwords, threadIdx.x * wper), we = min(nwords, wa + wper);
-        uint32_t zc = 0;
-        for (uint32_t wi = wa; wi < we; wi++) {
-            const uint32_t bit0 = P.gcli_pos + 32 * wi;
-            uint32_t word = (uint32_t)(bits64(pbuf, bit0, 32));
-            const uint32_t valid = min(32u, nbits - 32 * wi);
-            uint32_t z = ~word;
-            if (valid < 32) z &= ~(0xffffffffu >> valid);
-            zc += __popc(z);
-        }
-        uint32_t z0;
-        const uint32_t nz = block_scan1(zc, &z0, ws);
-        for (uint32_t wi = wa; wi < we; wi++) {
-            const uint32_t bit0 = P.gcli_pos + 32 * wi;
-            uint32_t word = (uint32_t)(bits64(pbuf, bit0, 32));
-            const uint32_t valid = min(32u, nbits - 32 * wi);
-            uint32_t z = ~word;
-            if (valid < 32) z &= ~(0xffffffffu >> valid);
-            while (z) {
-                const uint32_t lead = __clz(z);
-                if (z0 < ncw) zpos[z0] = 32 * wi + lead;
-                z0++;
-                z &= ~(0x80000000u >> lead);
+
+    /* pass 2: GCLIs from codeword ends; data bits per segment */
+    int bad = 0;
+    for (uint32_t sidx = warp; sidx < nseg; sidx += UK_WARPS) {
+        const jxs_seg_t sg = segs[sidx];
+        const jxs_bline_t B = bls[sg.bl];
+        const UkLine L = ln[sg.bl];
+        const UkPk P = pk[L.pk];
+        const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+        uint32_t cw = s_base[sidx], dsum = 0;
+        for (uint32_t base = sg.g0; base < gend; base += 32) {
+            const uint32_t g = base + lane;
+            const bool valid = g < gend;
+            uint32_t v = 0;
+            bool coded = false;
+            if (valid && !L.raw) {
+                const uint32_t sp = L.sig_pos + (g >> 3);
+                coded = !(L.meth && ((pbuf[sp >> 3] >> (7 - (sp & 7))) & 1));
             }
-        }
-        if (nz < ncw) {
-            if (threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_DEC_BITSTREAM);
-            return; /* uniform across the block: nz and ncw are block totals */
-        }
-        __syncthreads();
-        bidx = a < e ? find_dbl_by_group(bl, nbl, P.g_beg + a) : 0;
-        uint32_t cw = cw0;
-        int bad = 0;
-        for (uint32_t i = a; i < e; i++) {
-            const uint32_t g = P.g_beg + i;
-            while (bidx + 1 < nbl && bl[bidx + 1].g0 <= g) bidx++;
-            const DecBL& B = bl[bidx];
-            if ((B.mode & 2) && sflag[B.s0 + ((g - B.g0) >> 3)]) {
-                gcl[g] = B.t;
-            } else {
-                const uint32_t start = cw ? zpos[cw - 1] + 1 : 0;
-                const uint32_t ones = zpos[cw] - start;
-                if (ones > 31) bad = 1;
-                gcl[g] = (uint8_t)(B.t + ones);
-                cw++;
-            }
-        }
-        /* bits used must fit the declared sub-packet length */
-        if (ncw && threadIdx.x == 0 && zpos[ncw - 1] + 1 > nbits) bad = 1;
-        if (__syncthreads_or(bad)) {
-            if (threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_DEC_BITSTREAM);
-            return;
-        }
-    }
-    /* data: bit lengths, block scan, per-packet bases, decode */
-    const uint32_t per = (G + blockDim.x - 1) / blockDim.x;
-    const uint32_t ga = min(G, threadIdx.x * per), ge = min(G, ga + per);
-    uint32_t dsum = 0;
-    for (uint32_t g = ga; g < ge; g++) {
-        const DecBL& B = bl[find_dbl_by_group(bl, nbl, g)];
-        const int planes = (int)gcl[g] - (int)B.t;
-        if (planes > 0) dsum += 4 * (planes + 1);
-    }
-    uint32_t d0;
-    block_scan1(dsum, &d0, ws);
-    {
-        uint32_t run = d0;
-        for (uint32_t g = ga; g < ge; g++) {
-            const DecBL& B = bl[find_dbl_by_group(bl, nbl, g)];
-            if (g == B.g0 && pk[B.pk].b_beg == (uint32_t)(&B - bl)) pk_pref[B.pk] = run;
-            const int planes = (int)gcl[g] - (int)B.t;
-            if (planes > 0) run += 4 * (planes + 1);
-        }
-    }
-    __syncthreads();
-    {
-        uint32_t run = d0;
-        int bidx = ga < ge ? find_dbl_by_group(bl, nbl, ga) : 0;
-        int bad = 0;
-        const uint32_t uniform = cfg->qpih;
-        for (uint32_t g = ga; g < ge; g++) {
-            while (bidx + 1 < nbl && bl[bidx + 1].g0 <= g) bidx++;
-            const DecBL& B = bl[bidx];
-            const DecPk& P = pk[B.pk];
-            const jxs_band_t& bd = cfg->band[B.fb];
-            const uint32_t x = g - B.g0;
-            const uint32_t t = B.t, gv = gcl[g];
-            const int planes = (int)gv - (int)t;
-            int32_t out[4] = {0, 0, 0, 0};
-            if (planes > 0) {
-                const uint32_t nb = 4 * (planes + 1);
-                const uint32_t off = run - pk_pref[B.pk];
-                if (off + nb > P.data_bits) bad = 1;
-                else {
-                    const uint32_t pos = P.data_pos + off;
-                    uint32_t m[4] = {0, 0, 0, 0}, sgn;
-                    /* first nibble: signs; then planes gcli-1 .. gtli */
-                    if (nb <= 64) {
-                        uint64_t v = bits64(pbuf, pos, nb);
-                        sgn = (uint32_t)(v >> (nb - 4)) & 15;
-                        for (int pl = planes - 1; pl >= 0; pl--) {
-                            const uint32_t nib = (uint32_t)(v >> (4 * pl)) & 15;
-                            m[0] = (m[0] << 1) | (nib >> 3);
-                            m[1] = (m[1] << 1) | ((nib >> 2) & 1);
-                            m[2] = (m[2] << 1) | ((nib >> 1) & 1);
-                            m[3] = (m[3] << 1) | (nib & 1);
-                        }
-                    } else {
-                        sgn = (uint32_t)bits64(pbuf, pos, 4);
-                        for (int pl = 0; pl < planes; pl++) {
-                            const uint32_t nib = (uint32_t)bits64(pbuf, pos + 4 + 4 * pl, 4);
-                            m[0] = (m[0] << 1) | (nib >> 3);
-                            m[1] = (m[1] << 1) | ((nib >> 2) & 1);
-                            m[2] = (m[2] << 1) | ((nib >> 1) & 1);
-                            m[3] = (m[3] << 1) | (nib & 1);
-                        }
-                    }
-#pragma unroll
-                    for (int c = 0; c < 4; c++) {
-                        uint32_t mag = (m[c] << t) & 0xffffu;
-                        if (t > 0 && (mag & 0x7fffu)) {
-                            if (!uniform) {
-                                mag |= 1u << (t - 1);
-                            } else {
-                                /* inv_quant_uniform (Dequant.c:23-43) */
-                                uint32_t val = mag & 0x7fffu, acc = 0;
-                                const uint32_t sc = gv - t + 1;
-                                for (; val > 0; val >>= sc) acc = (acc + val) & 0xffffu;
-                                mag = acc;
-                            }
-                        }
-                        const uint32_t sm = (mag | (((sgn >> (3 - c)) & 1u) << 15)) & 0xffffu;
-                        out[c] = (sm & 0x8000u) ? -(int32_t)(sm & 0x7fffu) : (int32_t)sm;
-                    }
+            const uint32_t bal = __ballot_sync(FULL, coded);
+            if (coded) {
+                const uint32_t c = cw + __popc(bal & ((1u << lane) - 1));
+                const uint32_t zr = P.zbase + c;
+                const uint32_t start = c ? zend[zr - 1] + 1 : P.gpos;
+                const uint32_t ones = zend[zr] - start;
+                v = L.t + ones;
+                if (v > 15) {
+                    bad = 1;
+                    v = 15;
                 }
-                run += nb;
+                gcl[B.gbase + g] = (uint8_t)v;
+            } else if (valid) {
+                v = gcl[B.gbase + g];
             }
-            int16_t* crow = coef + bd.coef_off + (uint64_t)B.row * bd.pitch + 4 * x;
-            *(uint2*)crow = make_uint2(((uint32_t)out[0] & 0xffffu) | ((uint32_t)out[1] << 16),
-                                       ((uint32_t)out[2] & 0xffffu) | ((uint32_t)out[3] << 16));
+            cw += __popc(bal);
+            if (valid && v > L.t) dsum += 4 * (v - L.t + 1);
         }
-        if (bad) JXS_STATUS_SET(status, JXS_E_DEC_BITSTREAM);
+        dsum = __reduce_add_sync(FULL, dsum);
+        if (lane == 0) s_cnt[sidx] = dsum;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (uint32_t k = 0; k < npk; k++) pk[k].ncoded = 0; /* reused: data bits so far */
+        for (uint32_t x = 0; x < nbl; x++) {
+            UkPk& P = pk[ln[x].pk];
+            for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
+                s_base[i] = P.ncoded;
+                P.ncoded += s_cnt[i];
+            }
+        }
+        int err = 0;
+        for (uint32_t k = 0; k < npk; k++)
+            if (pk[k].present && pk[k].ncoded > pk[k].dbits) err = JXS_E_DEC_BITSTREAM;
+        s_err = err;
+    }
+    __syncthreads();
+    if (s_err) {
+        if (threadIdx.x == 0) JXS_STATUS_SET(status, s_err);
+        return;
+    }
+
+    /* pass 3: data */
+    const uint32_t uniform = cfg->qpih;
+    for (uint32_t sidx = warp; sidx < nseg; sidx += UK_WARPS) {
+        const jxs_seg_t sg = segs[sidx];
+        const jxs_bline_t B = bls[sg.bl];
+        const UkLine L = ln[sg.bl];
+        const UkPk P = pk[L.pk];
+        const jxs_band_t& bd = cfg->band[B.fb];
+        int16_t* crow = coef + bd.coef_off + (uint64_t)(p * bd.lines + B.line) * bd.pitch;
+        const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+        uint32_t dpos = P.dpos + s_base[sidx];
+        for (uint32_t base = sg.g0; base < gend; base += 32) {
+            const uint32_t g = base + lane;
+            const bool valid = g < gend;
+            const uint32_t v = valid ? gcl[B.gbase + g] : 0u;
+            const uint32_t np = v > L.t ? v - L.t : 0u;
+            const uint32_t len = np ? 4 * (np + 1) : 0u;
+            uint32_t tot;
+            const uint32_t ex = warp_excl_scan(len, &tot);
+            int32_t o[4] = {0, 0, 0, 0};
+            if (len) {
+                const uint32_t pos = dpos + ex;
+                const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
+                decode_group(win >> (64 - len), np, L.t, v, uniform, o);
+            }
+            if (valid) {
+                const int wl = (int)B.w - 4 * (int)g;
+                *(uint2*)(crow + 4 * g) = make_uint2(((uint32_t)o[0] & 0xffffu) | ((uint32_t)(wl > 1 ? o[1] : 0) << 16),
+                                                     ((uint32_t)(wl > 2 ? o[2] : 0) & 0xffffu) | ((uint32_t)(wl > 3 ? o[3] : 0) << 16));
+            }
+            dpos += tot;
+        }
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_DEC_BITSTREAM);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -672,16 +734,13 @@ extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, 
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, const uint32_t* prec_off, int16_t* coef,
-                                         uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status, cudaStream_t st) {
-    size_t smem = (size_t)cap_bytes + 16 + 2ull * cap_groups + 16 + 4ull * cap_groups;
-    static size_t configured = 0;
-    if (smem > configured) {
-        cudaError_t e = cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
-    unpack_kernel<<<np, UK_THREADS, smem, st>>>(dcfg, bs, prec_off, coef, cap_bytes, cap_groups, status);
+extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
+                                         int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status,
+                                         cudaStream_t st) {
+    const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 4ull * cap_groups;
+    cudaError_t e = cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    unpack_kernel<<<np, UK_THREADS, smem, st>>>(dcfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status);
     return cudaGetLastError();
 }
 

@@ -32,8 +32,9 @@ extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_
                                      PrecRC* rc, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
                                        const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st);
-extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, const uint32_t* prec_off, int16_t* coef,
-                                         uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
+                                         int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status,
+                                         cudaStream_t st);
 extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, const uint8_t* bs, uint32_t size, uint32_t* prec_off,
                                        int* walk_bad, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_inv_dwt(const DwtLaunch* L, int vert, int nblocks, size_t smem, const jxs_band_t* bands,
@@ -601,7 +602,8 @@ extern "C" jxs_gpu_dec_t* jxs_gpu_dec_create(const jxs_cfg_t* cfg, int nslots, i
     uint64_t cap = (uint64_t)cfg->lcod / (cfg->nslices ? cfg->nslices : 1);
     cap = cap + cap / 4 + 4096;
     if (cap > cfg->lcod + 64ull) cap = cfg->lcod + 64ull;
-    if (cap + fixed > kSmemMax) cap = kSmemMax > fixed + 4096 ? kSmemMax - fixed : 4096;
+    const size_t room = kSmemMax - 8 * 1024; /* static shared memory of the unpacking kernel */
+    if (cap + fixed > room) cap = room > fixed + 4096 ? room - fixed : 4096;
     d->cap_bytes = (uint32_t)cap & ~15u;
     if (cudaMalloc(&d->dcfg, sizeof(jxs_cfg_t)) != cudaSuccess ||
         cudaMemcpy(d->dcfg, cfg, sizeof(jxs_cfg_t), cudaMemcpyHostToDevice) != cudaSuccess) {
@@ -659,7 +661,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         CK(cudaMemcpyAsync(s->prec_off, s->prec_off_h, sizeof(uint32_t) * c->np, cudaMemcpyHostToDevice, st));
     }
     TMARK(1);
-    CK(jxs_launch_unpack(d->dcfg, dbs, s->prec_off, s->coef, c->np, d->cap_bytes, d->cap_groups, s->status, st));
+    CK(jxs_launch_unpack(d->dcfg, dbs, size, s->prec_off, s->coef, c->np, d->cap_bytes, d->cap_groups, s->status, st));
     TMARK(2);
 
     int out_dev[JXS_MAXC];
