@@ -29,7 +29,7 @@
 
 /* Per band line of the precinct being unpacked. */
 struct UkLine {
-    uint32_t sig_pos;           /* bit position of its significance flags */
+    uint32_t sig_pos;           /* bit position of its significance flags; raw packets: of its 4-bit GCLIs */
     uint8_t t, meth, raw, pk;
 };
 /* Per packet. */
@@ -260,6 +260,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
                 uint32_t need = 0;
                 for (uint32_t x = b; x < be; x++) {
                     ln[x].raw = 1;
+                    ln[x].sig_pos = bpos * 8 + need;
                     need += 4 * bls[x].gcli_w;
                 }
                 if (need > glen * 8) { err = JXS_E_DEC_BITSTREAM; break; }
@@ -315,7 +316,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
             const uint32_t g = base + lane;
             if (g < gend) {
                 if (L.raw) {
-                    const uint32_t pos = pk[L.pk].gpos + 4 * g;
+                    const uint32_t pos = L.sig_pos + 4 * g;
                     gcl[B.gbase + g] = (uint8_t)((pbuf[pos >> 3] >> (4 - (pos & 7))) & 15);
                 } else {
                     const uint32_t sp = L.sig_pos + (g >> 3);
