@@ -25,6 +25,7 @@
 
 #define UK_THREADS 512
 #define UK_WARPS (UK_THREADS / 32)
+#define UK_ZCAP(cap_groups) ((cap_groups) + 8 * JXS_MAXPK + 32)
 #define FULL 0xffffffffu
 
 /* Per band line of the precinct being unpacked. */
@@ -131,7 +132,7 @@ DEV void decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uint
  *
  * Dynamic shared memory: [precinct bytes: cap_bytes + 32, stream byte i at
  * i + lead so that 16-byte chunks are aligned] [GCLI per group: cap_groups]
- * [end bit of each unary codeword: 4 x cap_groups].
+ * [end bit of every zero of the VLC sub-packets: 4 x UK_ZCAP(cap_groups)].
  *
  *   copy    the precinct's bytes into shared memory;
  *   parse   thread 0: precinct header, packet headers, sub-packet positions
@@ -152,6 +153,8 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     uint8_t* pbuf = dsm;
     uint8_t* gcl = dsm + cap_bytes + 32;
     uint32_t* zend = (uint32_t*)(((uintptr_t)(gcl + cap_groups) + 15) & ~(uintptr_t)15);
+    /* zero bits: one per codeword plus up to 7 padding bits per packet */
+    const uint32_t zcap = UK_ZCAP(cap_groups);
     __shared__ UkLine ln[JXS_MAXBLINES];
     __shared__ UkPk pk[JXS_MAXPK];
     __shared__ uint32_t s_cnt[JXS_MAXSEG], s_base[JXS_MAXSEG];
@@ -370,7 +373,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
             if (valid < 32) z &= ~(0xffffffffu >> valid);
             while (z) {
                 const uint32_t lz = __clz(z);
-                if (z0 < cap_groups) zend[z0] = pk[k].gpos + 32 * i + lz;
+                if (z0 < zcap) zend[z0] = pk[k].gpos + 32 * i + lz;
                 z0++;
                 z &= ~(0x80000000u >> lz);
             }
@@ -395,7 +398,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
                     }
                 P.nzero = znext - P.zbase;
             }
-            if (P.ncoded > P.nzero || (P.ncoded && P.zbase + P.ncoded > cap_groups)) err = JXS_E_DEC_BITSTREAM;
+            if (P.ncoded > P.nzero || (P.ncoded && P.zbase + P.ncoded > zcap)) err = JXS_E_DEC_BITSTREAM;
         }
         s_err = err;
     }
@@ -738,7 +741,7 @@ extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, 
 extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
                                          int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status,
                                          cudaStream_t st) {
-    const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 4ull * cap_groups;
+    const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 4ull * UK_ZCAP(cap_groups);
     cudaError_t e = cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     unpack_kernel<<<np, UK_THREADS, smem, st>>>(dcfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status);
