@@ -8,12 +8,8 @@
  *                  dequantizes and writes int16 coefficients
  *                  (unpack_precinct, Packing.c:513-868; Dequant.c:9-57;
  *                  Precinct.c:9-29).
- *  inv_dwt_kernel  one vertical 5/3 level per launch: rebuilds the rows it
- *                  needs from the bands (inverse horizontal lifting in shared
- *                  memory), lifts vertically and writes the next level's
- *                  low band or, for the first level, the output samples with
- *                  the linear output scaling fused (Idwt.c:11-287,
- *                  DwtDecoder.c:322-406, NltDec.c:242-264).
+ *  walk_*_kernel   precinct offsets of a device-resident codestream.
+ * The inverse transform is in jxs_inv_dwt.cu.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -505,151 +501,6 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
 }
 
 /* ------------------------------------------------------------------------ */
-/* Inverse transform                                                         */
-/* ------------------------------------------------------------------------ */
-/* Inverse 5/3 lifting of rows in shared memory, stride S, n elements
- * (idwt_horizontal_line_*_c, Idwt.c:11-53). */
-template <typename RowFn>
-DEV void inv_h_level(RowFn row, int nrows, int n, int S) {
-    const int n2 = n >> 1, n1 = (n + 1) >> 1;
-    for (int t = threadIdx.x; t < nrows * n1; t += blockDim.x) {
-        int r = t / n1, i = t - r * n1;
-        int32_t* p = row(r);
-        int jp = min(max(i - 1, 0), n2 - 1), jc = min(i, n2 - 1);
-        p[S * 2 * i] -= (p[S * (2 * jp + 1)] + p[S * (2 * jc + 1)] + 2) >> 2;
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < nrows * n2; t += blockDim.x) {
-        int r = t / n2, j = t - r * n2;
-        int32_t* p = row(r);
-        int32_t a = p[S * 2 * j];
-        int32_t c = (2 * j + 2 < n) ? p[S * (2 * j + 2)] : a;
-        p[S * (2 * j + 1)] += (a + c) >> 1;
-    }
-    __syncthreads();
-}
-
-DEV void place_band(int32_t* p, int o, int S, int n, const jxs_band_t& bd, int brow, const int16_t* coef, int fq) {
-    const int16_t* crow = coef + bd.coef_off + (uint64_t)brow * bd.pitch;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) p[o + S * k] = (int32_t)((uint32_t)(int32_t)crow[k] << fq);
-}
-
-/* linear_output_scaling_*_line_c (NltDec.c:242-264) */
-DEV void store_out(const DwtJob& J, int y, int x, int32_t v, int bw, int depth) {
-    if (J.out_kind == 0) {
-        J.ll[(long long)y * J.ll_pitch + x] = v;
-        return;
-    }
-    const int zeta = bw - depth;
-    long long t = (long long)v + (1 << (bw - 1));
-    t = (t + ((1ll << zeta) >> 1)) >> zeta;
-    const int m = (1 << depth) - 1;
-    const int o = (int)(t > m ? m : (t < 0 ? 0 : t));
-    if (J.out_kind == 1) ((uint8_t*)J.dst)[(long long)y * J.dst_pitch + x] = (uint8_t)o;
-    else ((uint16_t*)J.dst)[(long long)y * J.dst_pitch + x] = (uint16_t)o;
-}
-
-/* Job fields for the inverse: w, h = size of the region this level rebuilds;
- * R = output row pairs per block; last = deepest vertical level (its low
- * rows come from the bands through the horizontal-only levels); src = int32
- * low band of the deeper level otherwise (src_pitch); ll/ll_pitch = int32
- * destination (out_kind 0) or dst/dst_pitch = output plane (1: 8-bit,
- * 2: 16-bit). */
-template <bool VERT>
-__global__ void __launch_bounds__(512) inv_dwt_kernel(const __grid_constant__ DwtLaunch L, const jxs_band_t* __restrict__ bands,
-                                                      const int16_t* __restrict__ coef, int fq, int bw, int depth) {
-    extern __shared__ int32_t sm[];
-    int j = 0;
-    while (j + 1 < L.njobs && (int)blockIdx.x >= L.job[j + 1].first_block) j++;
-    const DwtJob& J = L.job[j];
-    const int rb = blockIdx.x - J.first_block;
-    const int w = J.w, h = J.h, sp = J.smem_pitch;
-    const int w1 = (w + 1) >> 1, w2 = w >> 1;
-
-    if (VERT) {
-        const int n1 = (h + 1) >> 1, n2 = h >> 1;
-        const int r0 = rb * J.R, r1 = min(r0 + J.R, n1);
-        const int lcount = min(r1 + 1, n1) - r0;
-        const int jlo = min(max(r0 - 1, 0), n2 - 1), jhi = min(max(r1, 0), n2 - 1);
-        const int hcount = jhi - jlo + 1;
-        int32_t* Ls = sm;
-        int32_t* Hs = sm + (J.R + 1) * sp;
-        /* low rows */
-        for (int k = 0; k < lcount; k++) {
-            int32_t* p = Ls + k * sp;
-            const int i = r0 + k;
-            if (J.last) {
-                int m = w1, S = 2;
-                int Sl = 1, ml = w; /* geometry of the deepest low band */
-                for (int e = 0; e < J.nh; e++) {
-                    place_band(p, S, 2 * S, m >> 1, bands[J.b_hf[e]], i, coef, fq);
-                    m = (m + 1) >> 1;
-                    S <<= 1;
-                }
-                Sl = S; ml = m;
-                place_band(p, 0, Sl, ml, bands[J.b_ll], i, coef, fq);
-            } else {
-                const int32_t* srow = (const int32_t*)J.src + (long long)i * J.src_pitch;
-                for (int x = threadIdx.x; x < w1; x += blockDim.x) p[2 * x] = srow[x];
-            }
-            place_band(p, 1, 2, w2, bands[J.b_hl], i, coef, fq);
-        }
-        for (int k = 0; k < hcount; k++) {
-            int32_t* p = Hs + k * sp;
-            place_band(p, 0, 2, w1, bands[J.b_lh], jlo + k, coef, fq);
-            place_band(p, 1, 2, w2, bands[J.b_hh], jlo + k, coef, fq);
-        }
-        __syncthreads();
-        if (J.last && J.nh > 0) {
-            auto lrows = [&](int r) { return Ls + r * sp; };
-            int ms[6];
-            ms[0] = w1;
-            for (int e = 1; e <= J.nh; e++) ms[e] = (ms[e - 1] + 1) >> 1;
-            for (int e = J.nh - 1; e >= 0; e--) inv_h_level(lrows, lcount, ms[e], 2 << e);
-        }
-        auto all_rows = [&](int r) { return r < lcount ? Ls + r * sp : Hs + (r - lcount) * sp; };
-        inv_h_level(all_rows, lcount + hcount, w, 1);
-        /* vertical lifting (idwt_vertical_line_c, Idwt.c:186-263 in frame form) */
-        auto H = [&](int jj, int x) { return Hs[(min(max(jj, 0), n2 - 1) - jlo) * sp + x]; };
-        for (int x = threadIdx.x; x < w; x += blockDim.x) {
-            int32_t xe = Ls[x] - ((H(r0 - 1, x) + H(r0, x) + 2) >> 2);
-            for (int i = r0; i < r1; i++) {
-                store_out(J, 2 * i, x, xe, bw, depth);
-                if (2 * i + 1 < h) {
-                    int32_t xn = xe;
-                    if (2 * i + 2 < h) xn = Ls[(i + 1 - r0) * sp + x] - ((H(i, x) + H(i + 1, x) + 2) >> 2);
-                    store_out(J, 2 * i + 1, x, H(i, x) + ((xe + xn) >> 1), bw, depth);
-                    xe = xn;
-                }
-            }
-        }
-    } else {
-        const int r0 = rb * J.R, rc = min(J.R, h - r0);
-        for (int k = 0; k < rc; k++) {
-            int32_t* p = sm + k * sp;
-            int m = w, S = 1;
-            for (int e = 0; e < J.nh; e++) {
-                place_band(p, S, 2 * S, m >> 1, bands[J.b_hf[e]], r0 + k, coef, fq);
-                m = (m + 1) >> 1;
-                S <<= 1;
-            }
-            place_band(p, 0, S, m, bands[J.b_ll], r0 + k, coef, fq);
-        }
-        __syncthreads();
-        auto rows = [&](int r) { return sm + r * sp; };
-        int ms[6];
-        ms[0] = w;
-        for (int e = 1; e <= J.nh; e++) ms[e] = (ms[e - 1] + 1) >> 1;
-        for (int e = J.nh - 1; e >= 0; e--) inv_h_level(rows, rc, ms[e], 1 << e);
-        for (int t = threadIdx.x; t < rc * w; t += blockDim.x) {
-            const int k = t / w, x = t - k * w;
-            store_out(J, r0 + k, x, sm[k * sp + x], bw, depth);
-        }
-    }
-}
-
-
-/* ------------------------------------------------------------------------ */
 /* Precinct offsets of a device-resident codestream                          */
 /* ------------------------------------------------------------------------ */
 DEV uint32_t be24(const uint8_t* p) { return ((uint32_t)p[0] << 16) | ((uint32_t)p[1] << 8) | p[2]; }
@@ -748,17 +599,3 @@ extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* b
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t jxs_launch_inv_dwt(const DwtLaunch* L, int vert, int nblocks, size_t smem, const jxs_band_t* bands,
-                                          const int16_t* coef, int fq, int bw, int depth, cudaStream_t st) {
-    static size_t configured[2] = {0, 0};
-    cudaError_t e;
-    if (smem > configured[vert]) {
-        e = vert ? cudaFuncSetAttribute(inv_dwt_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
-                 : cudaFuncSetAttribute(inv_dwt_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        configured[vert] = smem;
-    }
-    if (vert) inv_dwt_kernel<true><<<nblocks, 512, smem, st>>>(*L, bands, coef, fq, bw, depth);
-    else inv_dwt_kernel<false><<<nblocks, 512, smem, st>>>(*L, bands, coef, fq, bw, depth);
-    return cudaGetLastError();
-}

@@ -37,8 +37,13 @@ extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* b
                                          cudaStream_t st);
 extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, const uint8_t* bs, uint32_t size, uint32_t* prec_off,
                                        int* walk_bad, int* status, cudaStream_t st);
-extern "C" cudaError_t jxs_launch_inv_dwt(const DwtLaunch* L, int vert, int nblocks, size_t smem, const jxs_band_t* bands,
-                                          const int16_t* coef, int fq, int bw, int depth, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_inv_v(const InvVLaunch* L, int out_kind, int nblocks, const jxs_band_t* bands, const int16_t* coef,
+                                        cudaStream_t st);
+extern "C" cudaError_t jxs_launch_inv_h(const InvHLaunch* L, int out_kind, int nblocks, const jxs_band_t* bands, const int16_t* coef,
+                                        cudaStream_t st);
+extern "C" int jxs_inv_v_tile_rows(void);
+extern "C" int jxs_inv_v_tile_cols(void);
+extern "C" int jxs_inv_h_max_rows_per_block(void);
 
 #define CK(x)                                                                                      \
     do {                                                                                           \
@@ -49,8 +54,6 @@ extern "C" cudaError_t jxs_launch_inv_dwt(const DwtLaunch* L, int vert, int nblo
         }                                                                                          \
     } while (0)
 
-static const size_t kLevelSmemTarget = 64 * 1024;
-static const size_t kInvSmemTarget = 100 * 1024;
 static const size_t kSmemMax = 220 * 1024;
 
 extern "C" int jxs_gpu_is_device_ptr(const void* p) {
@@ -487,7 +490,8 @@ struct DecSlot {
     uint32_t bs_cap;
     uint32_t* prec_off;
     int16_t* coef;
-    int32_t* ll[JXS_MAXC];
+    int32_t* ll[2][JXS_MAXC];   /* int32 low band below vertical level 0 / 1 */
+    int ll_pitch[2][JXS_MAXC];
     uint8_t* out_stage;
     uint64_t out_off[JXS_MAXC];
     int* status;
@@ -529,10 +533,11 @@ static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
     CK(cudaMallocHost(&s->hdr_h, sizeof(c->hdr)));
     CK(cudaMalloc(&s->coef, c->coef_total * sizeof(int16_t) + 64));
     for (uint32_t k = 0; k < c->nc; k++) {
-        if (c->comp[k].dv == 2) {
+        for (uint32_t v = 0; v < c->comp[k].dv && v < 2; v++) {
             uint32_t w, h;
-            level_dims(c->comp[k], 1, &w, &h);
-            CK(cudaMalloc(&s->ll[k], (size_t)w * h * sizeof(int32_t)));
+            level_dims(c->comp[k], (int)v + 1, &w, &h);
+            s->ll_pitch[v][k] = (int)((w + 3) & ~3u);
+            CK(cudaMalloc(&s->ll[v][k], (size_t)s->ll_pitch[v][k] * h * sizeof(int32_t) + 64));
         }
     }
     uint64_t ob = 0;
@@ -556,7 +561,8 @@ static void dec_slot_free(DecSlot* s) {
     if (s->prec_off_h) cudaFreeHost(s->prec_off_h);
     if (s->hdr_h) cudaFreeHost(s->hdr_h);
     cudaFree(s->coef);
-    for (int k = 0; k < JXS_MAXC; k++) cudaFree(s->ll[k]);
+    for (int v = 0; v < 2; v++)
+        for (int k = 0; k < JXS_MAXC; k++) cudaFree(s->ll[v][k]);
     cudaFree(s->out_stage);
     cudaFree(s->status);
     if (s->status_h) cudaFreeHost(s->status_h);
@@ -668,64 +674,97 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
     for (uint32_t k = 0; k < c->nc; k++) out_dev[k] = jxs_gpu_is_device_ptr(planes[k]);
     uint32_t max_dv = 0;
     for (uint32_t k = 0; k < c->nc; k++) max_dv = c->comp[k].dv > max_dv ? c->comp[k].dv : max_dv;
-    /* deepest vertical level first; the components without vertical levels last */
-    for (int pass = (int)max_dv - 1; pass >= -1; pass--) {
-        const int vert = pass >= 0;
-        DwtLaunch L;
+    /* horizontal-only levels of every component (into the int32 low band of
+     * its last vertical level, or straight to the output plane), then the
+     * vertical levels from the deepest up */
+    auto out_ptr = [&](uint32_t k, void** dst, long long* pitch) {
+        if (out_dev[k]) {
+            *dst = planes[k];
+            *pitch = strides[k];
+        } else {
+            *dst = s->out_stage + s->out_off[k];
+            *pitch = c->comp[k].w;
+        }
+    };
+    const int sample_kind = bps == 1 ? 1 : 2;
+    for (int pass = 0; pass < 2; pass++) {
+        /* pass 0: components with vertical levels; pass 1: without */
+        InvHLaunch L;
         memset(&L, 0, sizeof(L));
-        int blocks = 0;
-        size_t smem = 0;
+        L.depth = (int)c->depth;
+        L.bw = (int)c->bw;
+        L.fq = (int)c->fq;
+        int maxw = 0;
         for (uint32_t k = 0; k < c->nc; k++) {
             const jxs_comp_t& cp = c->comp[k];
-            if (vert ? (int)cp.dv <= pass : cp.dv != 0) continue;
-            const int v = vert ? pass : 0;
-            DwtJob& J = L.job[L.njobs++];
-            J.comp = (int)k;
+            if ((cp.dv > 0) != (pass == 0)) continue;
+            InvHJob& J = L.job[L.njobs++];
+            uint32_t w, h;
+            level_dims(cp, (int)cp.dv, &w, &h);
+            J.w = (int)w;
+            J.h = (int)h;
+            DwtJob bj;
+            memset(&bj, 0, sizeof(bj));
+            job_bands(c, (int)k, cp.dv > 0 ? (int)cp.dv - 1 : 0, &bj);
+            J.nh = bj.nh;
+            for (int e2 = 0; e2 < 5; e2++) J.b_hf[e2] = bj.b_hf[e2];
+            J.b_ll = bj.b_ll;
+            if (cp.dv > 0) {
+                J.dst = s->ll[cp.dv - 1][k];
+                J.dst_pitch = s->ll_pitch[cp.dv - 1][k];
+            } else {
+                out_ptr(k, &J.dst, &J.dst_pitch);
+            }
+            maxw = (int)w > maxw ? (int)w : maxw;
+        }
+        if (!L.njobs) continue;
+        L.warp_words = 2 * ((((maxw + 1) / 2) + 8 + 3) & ~3);
+        int rpb = jxs_inv_h_max_rows_per_block();
+        while (rpb > 1 && (size_t)L.warp_words * rpb * 4 > kSmemMax) rpb >>= 1;
+        if ((size_t)L.warp_words * rpb * 4 > kSmemMax) return JXS_E_BAD_PARAM;
+        L.rows_per_block = rpb;
+        int blocks = 0;
+        for (int i2 = 0; i2 < L.njobs; i2++) {
+            L.job[i2].first_block = blocks;
+            blocks += (int)div_up((uint32_t)L.job[i2].h, (uint32_t)rpb);
+        }
+        CK(jxs_launch_inv_h(&L, pass == 0 ? 0 : sample_kind, blocks, dev_bands(d->dcfg), s->coef, st));
+    }
+    const uint32_t vcols = (uint32_t)jxs_inv_v_tile_cols(), vrows = (uint32_t)jxs_inv_v_tile_rows();
+    for (int v = (int)max_dv - 1; v >= 0; v--) {
+        InvVLaunch L;
+        memset(&L, 0, sizeof(L));
+        L.depth = (int)c->depth;
+        L.bw = (int)c->bw;
+        L.fq = (int)c->fq;
+        int blocks = 0;
+        for (uint32_t k = 0; k < c->nc; k++) {
+            const jxs_comp_t& cp = c->comp[k];
+            if ((int)cp.dv <= v) continue;
+            InvVJob& J = L.job[L.njobs++];
             uint32_t w, h;
             level_dims(cp, v, &w, &h);
             J.w = (int)w;
             J.h = (int)h;
-            J.smem_pitch = (int)w;
-            job_bands(c, (int)k, v, &J);
-            if (vert && !J.last) {
-                J.src = s->ll[k];
-                J.src_pitch = (long long)((cp.w + 1) / 2);
-            }
-            if (v == 0) {
-                J.out_kind = bps == 1 ? 1 : 2;
-                if (out_dev[k]) {
-                    J.dst = planes[k];
-                    J.dst_pitch = strides[k];
-                } else {
-                    J.dst = s->out_stage + s->out_off[k];
-                    J.dst_pitch = cp.w;
-                }
+            J.ll = s->ll[v][k];
+            J.ll_pitch = s->ll_pitch[v][k];
+            const int top = (int)cp.band0 + (int)cp.nb - 1 - 3 * v;
+            J.b_hh = top;
+            J.b_lh = top - 1;
+            J.b_hl = top - 2;
+            if (v > 0) {
+                J.dst = s->ll[v - 1][k];
+                J.dst_pitch = s->ll_pitch[v - 1][k];
+                J.vec = 1;
             } else {
-                J.out_kind = 0;
-                J.ll = s->ll[k];
-                J.ll_pitch = (int)w;
+                out_ptr(k, &J.dst, &J.dst_pitch);
+                J.vec = ((uintptr_t)J.dst % (2 * bps)) == 0 && (J.dst_pitch % 2) == 0;
             }
-            const size_t row_bytes = (size_t)w * 4;
-            int R;
-            if (vert) {
-                R = (int)((kInvSmemTarget / row_bytes - 3) / 2);
-                if (kInvSmemTarget / row_bytes < 5) R = 1;
-            } else {
-                R = (int)(kLevelSmemTarget / row_bytes);
-            }
-            if (R < 1) R = 1;
-            const uint32_t units = vert ? (h + 1) / 2 : h;
-            if ((uint32_t)R > units) R = (int)units;
-            J.R = R;
+            J.col_tiles = (int)div_up(w, vcols);
             J.first_block = blocks;
-            J.nblocks = (int)div_up(units, (uint32_t)R);
-            blocks += J.nblocks;
-            const size_t need = vert ? (size_t)(2 * R + 3) * row_bytes : (size_t)R * row_bytes;
-            smem = need > smem ? need : smem;
+            blocks += J.col_tiles * (int)div_up((h + 1) / 2, vrows);
         }
-        if (!L.njobs) continue;
-        if (smem > kSmemMax) return JXS_E_BAD_PARAM;
-        CK(jxs_launch_inv_dwt(&L, vert, blocks, smem, dev_bands(d->dcfg), s->coef, (int)c->fq, (int)c->bw, (int)c->depth, st));
+        CK(jxs_launch_inv_v(&L, v > 0 ? 0 : sample_kind, blocks, dev_bands(d->dcfg), s->coef, st));
     }
     TMARK(3);
     for (uint32_t k = 0; k < c->nc; k++) {

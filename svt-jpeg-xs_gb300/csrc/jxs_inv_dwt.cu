@@ -1,0 +1,373 @@
+/*
+ * Inverse 5/3 wavelet transform for sm_103a.
+ *
+ *  inv_h_kernel  the horizontal-only levels, deepest first: one warp per row
+ *                combines the final LL band with the high band of each level
+ *                (in shared memory) and writes the row of the last vertical
+ *                level's low band, or, for a component without vertical
+ *                levels, the output samples.
+ *  inv_v_kernel  one vertical level on a tile of IV_ROWPAIRS row pairs x
+ *                IV_COLS columns: the low rows (LL + HL) and high rows (LH +
+ *                HH) the tile needs are rebuilt by inverse horizontal lifting,
+ *                one warp per row with 4 pairs per lane, into shared memory;
+ *                then each thread lifts one column pair vertically and writes
+ *                the next level's int32 low band or, for level 0, the output
+ *                samples with the linear output scaling fused.
+ *
+ * Arithmetic (bit-exact with the reference): coefficients are int16 two's
+ * complement scaled by << Fq (Definitions.h:128); inverse lifting
+ * x[2i] = s[i] - ((d[i-1] + d[i] + 2) >> 2), x[2i+1] = d[i] + ((x[2i] +
+ * x[2i+2]) >> 1) with whole-sample symmetric extension (Idwt.c:11-53,
+ * :186-263); linear output scaling v += 2^(Bw-1), v = (v + 2^(zeta-1)) >>
+ * zeta, clamp to [0, 2^d - 1], zeta = Bw - d (NltDec.c:242-264).
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "jxs_core.h"
+#include "jxs_kernels.cuh"
+
+#define DEV __device__ __forceinline__
+#define FULL 0xffffffffu
+
+DEV int32_t dq(int16_t c, int fq) { return (int32_t)((uint32_t)(int32_t)c << fq); }
+
+/* linear_output_scaling (NltDec.c:242-264) */
+DEV uint32_t out_sample(int32_t v, int bw, int depth) {
+    const int zeta = bw - depth;
+    long long t = (long long)v + (1 << (bw - 1));
+    t = (t + ((1ll << zeta) >> 1)) >> zeta;
+    const long long m = (1ll << depth) - 1;
+    return (uint32_t)(t > m ? m : (t < 0 ? 0 : t));
+}
+
+/* One band row of int16 coefficients as int32 << fq; index i < width. */
+struct CoefRow {
+    const int16_t* row;
+    int w;
+};
+DEV CoefRow coef_row(const jxs_band_t& bd, int r, const int16_t* coef) {
+    CoefRow c;
+    c.row = coef + bd.coef_off + (uint64_t)r * bd.pitch;
+    c.w = (int)bd.w;
+    return c;
+}
+
+/* Inverse horizontal lifting of one row by one warp, 4 pairs per lane.
+ * sget(i) / dget(i) return the low / high band value i for i in [0, n1) /
+ * [0, n2) (any value outside); get4(...) variants load four at once.  Pairs
+ * j in [j0, j0 + npairs) are produced (j0 a multiple of 4) and passed to
+ * out(j, xe[4], xo[4]): x[2j + 2q] = xe[q], x[2j + 2q + 1] = xo[q]. */
+template <typename S4, typename D4, typename S1, typename D1, typename Out>
+DEV void warp_lift_inv(int j0, int npairs, int n1, int n2, S4 s4, D4 d4, S1 s1, D1 d1, Out out) {
+    const int lane = threadIdx.x & 31;
+    /* symmetric extension of the high band: d[-1] = d[0], d[n2] = d[n2-1] */
+    auto dm = [&](int i) { return n2 == 0 ? 0 : d1(i < 0 ? 0 : (i >= n2 ? n2 - 1 : i)); };
+    int32_t carry = dm(j0 - 1);
+    for (int base = 0; base < npairs; base += 128) {
+        const int j = j0 + base + 4 * lane;
+        int32_t s[4], d[4];
+        s4(j, s);
+        d4(j, d);
+        /* high values past the band: mirrored */
+#pragma unroll
+        for (int q = 0; q < 4; q++)
+            if (j + q >= n2) d[q] = dm(j + q);
+        int32_t dp = __shfl_up_sync(FULL, d[3], 1);
+        if (lane == 0) dp = carry;
+        carry = __shfl_sync(FULL, d[3], 31);
+        int32_t xe[4], xo[4];
+        xe[0] = s[0] - ((dp + d[0] + 2) >> 2);
+        xe[1] = s[1] - ((d[0] + d[1] + 2) >> 2);
+        xe[2] = s[2] - ((d[1] + d[2] + 2) >> 2);
+        xe[3] = s[3] - ((d[2] + d[3] + 2) >> 2);
+        int32_t xn = __shfl_down_sync(FULL, xe[0], 1);
+        if (lane == 31 && j + 4 < n1) xn = s1(j + 4) - ((d[3] + dm(j + 4) + 2) >> 2);
+        /* x[n] = x[n-2] for even widths: the last even sample is its own
+         * right neighbour */
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            const int32_t nx = (j + q + 1 >= n1) ? xe[q] : (q < 3 ? xe[q + 1] : xn);
+            xo[q] = d[q] + ((xe[q] + nx) >> 1);
+        }
+        if (j < j0 + npairs) out(j, xe, xo);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* horizontal-only levels                                                    */
+/* ------------------------------------------------------------------------ */
+#define IH_MAX_WARPS 4
+
+template <int OUT>
+DEV void store_row8(const InvHJob& J, int row, int x0, int w, const int32_t* v, int bw, int depth) {
+    if (OUT == 0) {
+        int32_t* dst = (int32_t*)J.dst + (long long)row * J.dst_pitch + x0;
+        if (x0 + 7 < w) {
+            *(int4*)dst = make_int4(v[0], v[1], v[2], v[3]);
+            *(int4*)(dst + 4) = make_int4(v[4], v[5], v[6], v[7]);
+        } else {
+            for (int q = 0; q < 8; q++)
+                if (x0 + q < w) dst[q] = v[q];
+        }
+    } else {
+        for (int q = 0; q < 8; q++) {
+            if (x0 + q >= w) break;
+            const uint32_t o = out_sample(v[q], bw, depth);
+            const long long idx = (long long)row * J.dst_pitch + x0 + q;
+            if (OUT == 1) ((uint8_t*)J.dst)[idx] = (uint8_t)o;
+            else ((uint16_t*)J.dst)[idx] = (uint16_t)o;
+        }
+    }
+}
+
+template <int OUT>
+__global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_constant__ InvHLaunch L, const jxs_band_t* __restrict__ bands,
+                                                                  const int16_t* __restrict__ coef) {
+    extern __shared__ __align__(16) int32_t ism[];
+    int jb = 0;
+    while (jb + 1 < L.njobs && (int)blockIdx.x >= L.job[jb + 1].first_block) jb++;
+    const InvHJob& J = L.job[jb];
+    const int warp = threadIdx.x >> 5;
+    const int row = (blockIdx.x - J.first_block) * L.rows_per_block + warp;
+    if (row >= J.h) return;
+    const int fq = L.fq;
+    int32_t* bufA = ism + warp * L.warp_words;
+    int32_t* bufB = bufA + L.warp_words / 2;
+    /* widths of every level's input, m[0] = row width */
+    int m[6];
+    m[0] = J.w;
+    for (int e = 0; e < J.nh; e++) m[e + 1] = (m[e] + 1) >> 1;
+    const CoefRow llr = coef_row(bands[J.b_ll], row, coef);
+    const int32_t* cur = nullptr; /* int32 low band of the level being rebuilt (null: the LL band) */
+    int32_t* nxt = bufA;
+    for (int e = J.nh - 1; e >= -1; e--) {
+        if (e == -1) {
+            /* no horizontal-only level: the LL band is the row */
+            if (J.nh > 0) break;
+            const int w = J.w;
+            for (int x0 = 8 * (threadIdx.x & 31); x0 < w; x0 += 256) {
+                int32_t v[8];
+                for (int q = 0; q < 8; q++) v[q] = x0 + q < w ? dq(llr.row[x0 + q], fq) : 0;
+                store_row8<OUT>(J, row, x0, w, v, L.bw, L.depth);
+            }
+            break;
+        }
+        const int n = m[e], n1 = m[e + 1], n2 = n >> 1;
+        const CoefRow hr = coef_row(bands[J.b_hf[e]], row, coef);
+        const int32_t* sc = cur;
+        auto s4 = [&](int j, int32_t* s) {
+            if (sc) {
+                for (int q = 0; q < 4; q++) s[q] = j + q < n1 ? sc[j + q] : 0;
+            } else {
+                for (int q = 0; q < 4; q++) s[q] = j + q < n1 ? dq(llr.row[j + q], fq) : 0;
+            }
+        };
+        auto s1 = [&](int j) { return sc ? sc[j] : dq(llr.row[j], fq); };
+        auto d4 = [&](int j, int32_t* d) {
+            for (int q = 0; q < 4; q++) d[q] = j + q < n2 ? dq(hr.row[j + q], fq) : 0;
+        };
+        auto d1 = [&](int j) { return dq(hr.row[j], fq); };
+        if (e > 0) {
+            int32_t* dst = nxt;
+            warp_lift_inv(0, n1, n1, n2, s4, d4, s1, d1, [&](int j, const int32_t* xe, const int32_t* xo) {
+                for (int q = 0; q < 4; q++) {
+                    if (2 * (j + q) < n) dst[2 * (j + q)] = xe[q];
+                    if (2 * (j + q) + 1 < n) dst[2 * (j + q) + 1] = xo[q];
+                }
+            });
+            __syncwarp();
+            cur = dst;
+            nxt = (dst == bufA) ? bufB : bufA;
+        } else {
+            warp_lift_inv(0, n1, n1, n2, s4, d4, s1, d1, [&](int j, const int32_t* xe, const int32_t* xo) {
+                const int32_t v[8] = {xe[0], xo[0], xe[1], xo[1], xe[2], xo[2], xe[3], xo[3]};
+                store_row8<OUT>(J, row, 2 * j, n, v, L.bw, L.depth);
+            });
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* vertical level                                                            */
+/* ------------------------------------------------------------------------ */
+#define IV_THREADS 128
+#define IV_COLS (2 * IV_THREADS - 8)      /* output columns per tile */
+#define IV_ROWPAIRS 8
+#define IV_NROWS (2 * IV_ROWPAIRS + 3)    /* low rows r0..r0+R, high rows r0-1..r0+R */
+#define IV_SROW (IV_COLS + 8)
+
+template <int OUT>
+__global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant__ InvVLaunch L, const jxs_band_t* __restrict__ bands,
+                                                           const int16_t* __restrict__ coef) {
+    __shared__ __align__(16) int32_t sx[IV_NROWS][IV_SROW];
+    int jb = 0;
+    while (jb + 1 < L.njobs && (int)blockIdx.x >= L.job[jb + 1].first_block) jb++;
+    const InvVJob& J = L.job[jb];
+    const int t = blockIdx.x - J.first_block;
+    const int ty = t / J.col_tiles, tx = t - ty * J.col_tiles;
+    const int w = J.w, h = J.h, fq = L.fq;
+    const int n1 = (h + 1) >> 1, n2 = h >> 1;
+    const int w1 = (w + 1) >> 1, w2 = w >> 1;
+    const int r0 = ty * IV_ROWPAIRS;
+    const int c0 = tx * IV_COLS;
+    const int warp = threadIdx.x >> 5;
+    const int jc = c0 >> 1;
+    const int npairs = min(IV_COLS / 2, w1 - jc);
+    const int rlo = min(IV_ROWPAIRS + 1, n1 - r0); /* low rows present */
+    /* rows of the tile, rebuilt horizontally: k <= R: low row r0 + k;
+     * k > R: high row r0 - 1 + (k - R - 1), mirrored into [0, n2) */
+    for (int k = warp; k < IV_NROWS; k += IV_THREADS / 32) {
+        int32_t* dst = &sx[k][0];
+        if (k <= IV_ROWPAIRS) {
+            if (k >= rlo) continue;
+            const int i = r0 + k;
+            const int32_t* srow = J.ll + (long long)i * J.ll_pitch;
+            const CoefRow hr = coef_row(bands[J.b_hl], i, coef);
+            warp_lift_inv(
+                jc, npairs, w1, w2,
+                [&](int j, int32_t* s) {
+                    if (j + 3 < w1) {
+                        const int4 v = *(const int4*)(srow + j);
+                        s[0] = v.x; s[1] = v.y; s[2] = v.z; s[3] = v.w;
+                    } else {
+                        for (int q = 0; q < 4; q++) s[q] = j + q < w1 ? srow[j + q] : 0;
+                    }
+                },
+                [&](int j, int32_t* d) {
+                    if (j + 3 < w2) {
+                        const uint2 v = *(const uint2*)(hr.row + j);
+                        d[0] = dq((int16_t)(v.x & 0xffff), fq); d[1] = dq((int16_t)(v.x >> 16), fq);
+                        d[2] = dq((int16_t)(v.y & 0xffff), fq); d[3] = dq((int16_t)(v.y >> 16), fq);
+                    } else {
+                        for (int q = 0; q < 4; q++) d[q] = j + q < w2 ? dq(hr.row[j + q], fq) : 0;
+                    }
+                },
+                [&](int j) { return srow[j]; }, [&](int j) { return dq(hr.row[j], fq); },
+                [&](int j, const int32_t* xe, const int32_t* xo) {
+                    const int x = 2 * (j - jc);
+                    *(int4*)(dst + x) = make_int4(xe[0], xo[0], xe[1], xo[1]);
+                    *(int4*)(dst + x + 4) = make_int4(xe[2], xo[2], xe[3], xo[3]);
+                });
+        } else {
+            if (n2 == 0) continue;
+            int i = r0 - 1 + (k - IV_ROWPAIRS - 1);
+            i = i < 0 ? 0 : (i >= n2 ? n2 - 1 : i);
+            const CoefRow lr = coef_row(bands[J.b_lh], i, coef);
+            const CoefRow hr = coef_row(bands[J.b_hh], i, coef);
+            auto ld4 = [&](const CoefRow& cr, int n, int j, int32_t* o) {
+                if (j + 3 < n) {
+                    const uint2 v = *(const uint2*)(cr.row + j);
+                    o[0] = dq((int16_t)(v.x & 0xffff), fq); o[1] = dq((int16_t)(v.x >> 16), fq);
+                    o[2] = dq((int16_t)(v.y & 0xffff), fq); o[3] = dq((int16_t)(v.y >> 16), fq);
+                } else {
+                    for (int q = 0; q < 4; q++) o[q] = j + q < n ? dq(cr.row[j + q], fq) : 0;
+                }
+            };
+            warp_lift_inv(
+                jc, npairs, w1, w2, [&](int j, int32_t* s) { ld4(lr, w1, j, s); }, [&](int j, int32_t* d) { ld4(hr, w2, j, d); },
+                [&](int j) { return dq(lr.row[j], fq); }, [&](int j) { return dq(hr.row[j], fq); },
+                [&](int j, const int32_t* xe, const int32_t* xo) {
+                    const int x = 2 * (j - jc);
+                    *(int4*)(dst + x) = make_int4(xe[0], xo[0], xe[1], xo[1]);
+                    *(int4*)(dst + x + 4) = make_int4(xe[2], xo[2], xe[3], xo[3]);
+                });
+        }
+    }
+    __syncthreads();
+
+    /* vertical lifting, one column pair per thread */
+    const int cp = threadIdx.x;
+    if (2 * cp >= 2 * npairs) return;
+    const int x = c0 + 2 * cp;
+    const int rend = min(r0 + IV_ROWPAIRS, n1);
+#define LV(i) (*(const int2*)&sx[(i) - r0][2 * cp])
+#define HV(i) (*(const int2*)&sx[IV_ROWPAIRS + 1 + ((i) - (r0 - 1))][2 * cp])
+    int2 hp = n2 ? HV(r0 - 1) : make_int2(0, 0);
+    int2 hc = n2 ? HV(r0) : make_int2(0, 0);
+    int2 l0 = LV(r0);
+    int2 xe = make_int2(l0.x - ((hp.x + hc.x + 2) >> 2), l0.y - ((hp.y + hc.y + 2) >> 2));
+    for (int i = r0; i < rend; i++) {
+        const int y = 2 * i;
+        int2 xo = make_int2(0, 0), xn = xe;
+        if (y + 1 < h) {
+            if (y + 2 < h) {
+                const int2 ln = LV(i + 1), hn = HV(i + 1);
+                xn = make_int2(ln.x - ((hc.x + hn.x + 2) >> 2), ln.y - ((hc.y + hn.y + 2) >> 2));
+                hp = hc;
+                hc = hn;
+            }
+            const int2 hcur = HV(i);
+            xo = make_int2(hcur.x + ((xe.x + xn.x) >> 1), hcur.y + ((xe.y + xn.y) >> 1));
+        }
+        /* outputs (rows y, y + 1; columns x, x + 1) */
+        const bool two = x + 1 < w;
+        if (OUT == 0) {
+            int32_t* d0 = (int32_t*)J.dst + (long long)y * J.dst_pitch + x;
+            if (two) *(int2*)d0 = xe;
+            else d0[0] = xe.x;
+            if (y + 1 < h) {
+                int32_t* d1 = d0 + J.dst_pitch;
+                if (two) *(int2*)d1 = xo;
+                else d1[0] = xo.x;
+            }
+        } else {
+            const int rows = y + 1 < h ? 2 : 1;
+            for (int rr = 0; rr < rows; rr++) {
+                const int2 v = rr ? xo : xe;
+                const long long idx = (long long)(y + rr) * J.dst_pitch + x;
+                const uint32_t a = out_sample(v.x, L.bw, L.depth), b = out_sample(v.y, L.bw, L.depth);
+                if (OUT == 1) {
+                    uint8_t* p = (uint8_t*)J.dst + idx;
+                    if (two && J.vec) *(uint16_t*)p = (uint16_t)(a | (b << 8));
+                    else {
+                        p[0] = (uint8_t)a;
+                        if (two) p[1] = (uint8_t)b;
+                    }
+                } else {
+                    uint16_t* p = (uint16_t*)J.dst + idx;
+                    if (two && J.vec) *(uint32_t*)p = a | (b << 16);
+                    else {
+                        p[0] = (uint16_t)a;
+                        if (two) p[1] = (uint16_t)b;
+                    }
+                }
+            }
+        }
+        xe = xn;
+    }
+#undef LV
+#undef HV
+}
+
+/* ------------------------------------------------------------------------ */
+/* launchers                                                                 */
+/* ------------------------------------------------------------------------ */
+extern "C" int jxs_inv_v_tile_rows(void) { return IV_ROWPAIRS; }
+extern "C" int jxs_inv_v_tile_cols(void) { return IV_COLS; }
+extern "C" int jxs_inv_h_max_rows_per_block(void) { return IH_MAX_WARPS; }
+
+extern "C" cudaError_t jxs_launch_inv_v(const InvVLaunch* L, int out_kind, int nblocks, const jxs_band_t* bands, const int16_t* coef,
+                                        cudaStream_t st) {
+    if (out_kind == 0) inv_v_kernel<0><<<nblocks, IV_THREADS, 0, st>>>(*L, bands, coef);
+    else if (out_kind == 1) inv_v_kernel<1><<<nblocks, IV_THREADS, 0, st>>>(*L, bands, coef);
+    else inv_v_kernel<2><<<nblocks, IV_THREADS, 0, st>>>(*L, bands, coef);
+    return cudaGetLastError();
+}
+
+template <int OUT>
+static cudaError_t launch_ih(const InvHLaunch* L, int nblocks, size_t smem, const jxs_band_t* bands, const int16_t* coef,
+                             cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(inv_h_kernel<OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    inv_h_kernel<OUT><<<nblocks, L->rows_per_block * 32, smem, st>>>(*L, bands, coef);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t jxs_launch_inv_h(const InvHLaunch* L, int out_kind, int nblocks, const jxs_band_t* bands, const int16_t* coef,
+                                        cudaStream_t st) {
+    const size_t smem = (size_t)L->warp_words * L->rows_per_block * sizeof(int32_t);
+    if (out_kind == 0) return launch_ih<0>(L, nblocks, smem, bands, coef, st);
+    if (out_kind == 1) return launch_ih<1>(L, nblocks, smem, bands, coef, st);
+    return launch_ih<2>(L, nblocks, smem, bands, coef, st);
+}

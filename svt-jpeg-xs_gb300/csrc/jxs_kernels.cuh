@@ -86,6 +86,38 @@ struct FwdHLaunch {
     FwdHJob job[JXS_MAXC];
 };
 
+/* Inverse transform, one vertical level (jxs_inv_dwt.cu): rebuilds the
+ * w x h level input from the int32 low band ll and the HL, LH, HH bands. */
+struct InvVJob {
+    int w, h;
+    const int32_t* ll;
+    int ll_pitch;           /* elements, a multiple of 4 */
+    int b_hl, b_lh, b_hh;
+    int col_tiles, first_block;
+    void* dst;              /* int32 low band of the next level up, or the output plane */
+    long long dst_pitch;    /* elements */
+    int vec;                /* two adjacent output samples may be stored at once */
+};
+struct InvVLaunch {
+    int njobs, depth, bw, fq;
+    InvVJob job[JXS_MAXC];
+};
+
+/* Inverse transform, horizontal-only levels: rows [0, h) of width w. */
+struct InvHJob {
+    int w, h;
+    int first_block;
+    int nh;
+    int b_hf[5], b_ll;
+    void* dst;
+    long long dst_pitch;
+};
+struct InvHLaunch {
+    int njobs, depth, bw, fq;
+    int rows_per_block, warp_words;
+    InvHJob job[JXS_MAXC];
+};
+
 /* Encoder rate-control outputs per precinct row. */
 struct PrecRC {
     uint32_t total_bytes;  /* bytes written for the precinct (header to last data byte, incl. trailing padding) */
