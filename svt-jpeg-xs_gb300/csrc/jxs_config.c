@@ -50,12 +50,15 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
             uint32_t n = 0, ns = 0, gsum = 0;
             for (uint32_t k = 0; k < g->npk; k++) {
                 const uint32_t l = g->pk[k].line;
+                g->pk_bl0[t][k] = (uint8_t)n;
+                g->pk_nbl[t][k] = 0;
                 for (uint32_t gb = g->pk[k].bs; gb < g->pk[k].be; gb++) {
                     const uint32_t fb = g->g2f[gb];
                     if (fb == JXS_NOBAND) continue;
                     const jxs_band_t* bd = &g->band[fb];
                     if (l >= (t ? bd->last_lines : bd->lines)) continue;
                     if (n >= JXS_MAXBLINES) return JXS_E_BAD_PARAM;
+                    g->pk_nbl[t][k]++;
                     jxs_bline_t* b = &g->bline[t][n++];
                     b->fb = (uint8_t)fb;
                     b->line = (uint8_t)l;

@@ -104,6 +104,8 @@ typedef struct jxs_cfg {
     uint64_t coef_total, gcli_total;     /* per-frame buffer sizes (elements / bytes) */
     uint32_t nbline[2];                  /* band lines: normal / last precinct row */
     jxs_bline_t bline[2][JXS_MAXBLINES];
+    uint8_t pk_bl0[2][JXS_MAXPK];        /* first band line of each packet (its count in pk_nbl; 0: absent) */
+    uint8_t pk_nbl[2][JXS_MAXPK];
     uint32_t seg_groups;                 /* groups per segment, a multiple of 32 */
     uint32_t nseg[2];
     jxs_seg_t seg[2][JXS_MAXSEG];

@@ -329,16 +329,18 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
         if (lane == 0) s_cnt[sidx] = cnt;
     }
     __syncthreads();
-    /* codeword base of every segment inside its packet */
-    if (threadIdx.x == 0) {
-        for (uint32_t x = 0; x < nbl; x++) {
+    /* codeword base of every segment inside its packet: one lane per packet */
+    if (warp == 0 && lane < (int)cfg->npk) {
+        const uint32_t b0 = cfg->pk_bl0[last][lane], nb = cfg->pk_nbl[last][lane];
+        uint32_t run = 0;
+        for (uint32_t x = b0; x < b0 + nb; x++) {
             if (ln[x].raw) continue;
-            UkPk& P = pk[ln[x].pk];
             for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
-                s_base[i] = P.ncoded;
-                P.ncoded += s_cnt[i];
+                s_base[i] = run;
+                run += s_cnt[i];
             }
         }
+        pk[lane].ncoded = run;
     }
     /* zero bits of the VLC sub-packets: count, scan, record positions */
     const uint32_t tw = s_tw, npk = s_npk;
@@ -376,27 +378,28 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        int err = 0;
-        for (uint32_t k = 0; k < npk; k++) {
+    if (warp == 0) {
+        /* zeros of each VLC packet: up to the next VLC packet's first zero */
+        const uint32_t k = lane;
+        const bool vlc = k < npk && pk[k].present && !pk[k].raw && pk[k].nwords;
+        const uint32_t zb = vlc ? pk[k].zbase : 0u;
+        const uint32_t later = __ballot_sync(FULL, vlc) & ~((2u << k) - 1u);
+        const uint32_t zn = __shfl_sync(FULL, zb, later ? __ffs(later) - 1 : 0);
+        const uint32_t znext = later ? zn : ztotal;
+        bool bad_pk = false;
+        if (k < npk && pk[k].present && !pk[k].raw) {
             UkPk& P = pk[k];
-            if (!P.present || P.raw) continue;
-            if (P.nwords == 0) {
+            if (!P.nwords) {
                 P.zbase = 0;
                 P.nzero = 0;
             } else {
-                /* zeros of this packet: up to the next VLC packet's first zero */
-                uint32_t znext = ztotal;
-                for (uint32_t k2 = k + 1; k2 < npk; k2++)
-                    if (pk[k2].present && !pk[k2].raw && pk[k2].nwords) {
-                        znext = pk[k2].zbase;
-                        break;
-                    }
                 P.nzero = znext - P.zbase;
             }
-            if (P.ncoded > P.nzero || (P.ncoded && P.zbase + P.ncoded > zcap)) err = JXS_E_DEC_BITSTREAM;
+            bad_pk = P.ncoded > P.nzero || (P.ncoded && P.zbase + P.ncoded > zcap);
         }
-        s_err = err;
+        if (lane == 0) s_err = 0;
+        __syncwarp();
+        if (__any_sync(FULL, bad_pk) && lane == 0) s_err = JXS_E_DEC_BITSTREAM;
     }
     __syncthreads();
     if (s_err) {
@@ -444,19 +447,21 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
         if (lane == 0) s_cnt[sidx] = dsum;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (uint32_t k = 0; k < npk; k++) pk[k].ncoded = 0; /* reused: data bits so far */
-        for (uint32_t x = 0; x < nbl; x++) {
-            UkPk& P = pk[ln[x].pk];
-            for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
-                s_base[i] = P.ncoded;
-                P.ncoded += s_cnt[i];
-            }
+    if (warp == 0) {
+        /* data base of every segment inside its packet: one lane per packet */
+        bool bad_pk = false;
+        if (lane < (int)npk) {
+            const uint32_t b0 = cfg->pk_bl0[last][lane], nb = cfg->pk_nbl[last][lane];
+            uint32_t run = 0;
+            for (uint32_t x = b0; x < b0 + nb; x++)
+                for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
+                    s_base[i] = run;
+                    run += s_cnt[i];
+                }
+            bad_pk = pk[lane].present && run > pk[lane].dbits;
         }
-        int err = 0;
-        for (uint32_t k = 0; k < npk; k++)
-            if (pk[k].present && pk[k].ncoded > pk[k].dbits) err = JXS_E_DEC_BITSTREAM;
-        s_err = err;
+        const bool any_bad = __any_sync(FULL, bad_pk);
+        if (lane == 0) s_err = any_bad ? JXS_E_DEC_BITSTREAM : 0;
     }
     __syncthreads();
     if (s_err) {

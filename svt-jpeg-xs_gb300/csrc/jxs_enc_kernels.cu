@@ -444,8 +444,9 @@ struct PkLine {
  * segments of seg_groups groups, one warp per segment:
  *   pass A  each segment's data bits, VLC bits and groups lying in
  *           insignificant significance groups, at the precinct's gtli;
- *   layout  thread 0: coding method per band (significance only if strictly
- *           cheaper), packet headers, raw fallback, sub-packet positions,
+ *   layout  warp 0, lanes over band lines, bands, packets: coding method per
+ *           band (significance only if strictly cheaper), packet headers, raw
+ *           fallback, packet positions by a warp scan, sub-packet positions,
  *           each segment's start in its GCLI and data sub-packets;
  *   pass B  each lane one group: significance flags, the unary GCLI code and
  *           the data bits, at positions from a warp prefix sum, OR-ed into
@@ -456,7 +457,8 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     extern __shared__ __align__(16) uint32_t buf[];
     __shared__ uint32_t s_data[JXS_MAXSEG], s_vlc[JXS_MAXSEG], s_zero[JXS_MAXSEG];
     __shared__ PkLine pl[JXS_MAXBLINES];
-    __shared__ uint8_t tb[JXS_MAXBL];
+    __shared__ uint8_t tb[JXS_MAXBL], s_meth[JXS_MAXBL];
+    __shared__ uint32_t s_cn[JXS_MAXBL], s_cs[JXS_MAXBL];
     __shared__ uint32_t lut[256];
     __shared__ int s_ok;
 
@@ -484,8 +486,11 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
         for (int k = 0; k < 8; k++) x |= ((i >> k) & 1u) << (4 * k);
         lut[i] = x;
     }
-    for (uint32_t fb = threadIdx.x; fb < cfg->nbands; fb += blockDim.x)
+    for (uint32_t fb = threadIdx.x; fb < cfg->nbands; fb += blockDim.x) {
         tb[fb] = jxs_truncation(cfg->band[fb].gain, cfg->band[fb].prio, R.q, R.r);
+        s_cn[fb] = 0;
+        s_cs[fb] = 0;
+    }
     if (threadIdx.x == 0) {
         pk_nwords = words;
         pk_overflow = 0;
@@ -531,16 +536,10 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     }
     __syncthreads();
 
-    /* layout */
-    if (threadIdx.x == 0) {
+    /* layout, by warp 0 with lanes over band lines, bands and packets */
+    if (warp == 0) {
         const uint32_t nbl = cfg->nbline[last];
-        uint32_t cn[JXS_MAXBL], cs[JXS_MAXBL];
-        uint8_t meth[JXS_MAXBL];
-        for (uint32_t fb = 0; fb < cfg->nbands; fb++) {
-            cn[fb] = 0;
-            cs[fb] = 0;
-        }
-        for (uint32_t b = 0; b < nbl; b++) {
+        for (uint32_t b = lane; b < nbl; b += 32) {
             const jxs_bline_t& B = bls[b];
             uint32_t d = 0, v = 0, z = 0;
             for (uint32_t i = B.seg0; i < B.seg0 + B.nseg; i++) {
@@ -551,76 +550,57 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
             pl[b].data = d;
             pl[b].vlc = v;
             pl[b].zero = z;
-            cn[B.fb] += v;
-            cs[B.fb] += v - z + B.sig_w;
+            atomicAdd(&s_cn[B.fb], v);
+            atomicAdd(&s_cs[B.fb], v - z + B.sig_w);
         }
+        __syncwarp();
         /* coding method per band: significance only if strictly cheaper
          * (RateControl.c:528-575) */
-        for (uint32_t fb = 0; fb < cfg->nbands; fb++) meth[fb] = (uint8_t)(cfg->sig && cn[fb] > cs[fb]);
-        uint8_t* bytes = (uint8_t*)buf + lead;
-        const uint32_t hdr = cfg->prec_hdr_bytes;
-        const uint32_t lprc = total - hdr;
-        bytes[0] = (uint8_t)(lprc >> 16);
-        bytes[1] = (uint8_t)(lprc >> 8);
-        bytes[2] = (uint8_t)lprc;
-        bytes[3] = R.q;
-        bytes[4] = R.r;
-        uint32_t pos = 40;
-        for (uint32_t gb = 0; gb < cfg->nbands_all; gb++) {
-            const int fb = cfg->g2f[gb];
-            if (fb == JXS_NOBAND) continue;
-            const jxs_band_t& bd = cfg->band[fb];
-            const uint32_t lines = last ? bd.last_lines : bd.lines;
-            const uint32_t d = (lines > 0 && meth[fb]) ? 2u : 0u;
-            bytes[pos >> 3] |= (uint8_t)(d << (6 - (pos & 7)));
-            pos += 2;
+        for (uint32_t fb = lane; fb < cfg->nbands; fb += 32) s_meth[fb] = (uint8_t)(cfg->sig && s_cn[fb] > s_cs[fb]);
+        __syncwarp();
+        /* one lane per packet: sub-packet sizes, raw fallback, header */
+        const uint32_t k = lane;
+        const uint32_t nb = k < cfg->npk ? cfg->pk_nbl[last][k] : 0u, b0 = k < cfg->npk ? cfg->pk_bl0[last][k] : 0u;
+        uint32_t db = 0, gbits = 0, sbits = 0;
+        for (uint32_t x = b0; x < b0 + nb; x++) {
+            const uint8_t m = s_meth[bls[x].fb];
+            pl[x].meth = m;
+            db += pl[x].data;
+            gbits += m ? pl[x].vlc - pl[x].zero : pl[x].vlc;
+            sbits += m ? bls[x].sig_w : 0u;
         }
-        pos = (lead + hdr) * 8;
-        uint32_t b = 0;
-        int ok = 1;
-        for (uint32_t k = 0; k < cfg->npk && ok; k++) {
-            if (b >= nbl || bls[b].pk != k) continue; /* packet absent in this precinct */
-            uint32_t b_end = b;
-            uint32_t db = 0, gbits = 0, sbits = 0;
-            while (b_end < nbl && bls[b_end].pk == k) {
-                PkLine& L = pl[b_end];
-                L.meth = meth[bls[b_end].fb];
-                db += L.data;
-                gbits += L.meth ? L.vlc - L.zero : L.vlc;
-                sbits += L.meth ? bls[b_end].sig_w : 0;
-                b_end++;
-            }
-            const uint32_t dB = (db + 7) >> 3, gB = (gbits + 7) >> 3, sB = (sbits + 7) >> 3;
-            const uint32_t rawB = cfg->raw_bytes[last][k];
-            const int raw = sB + gB > rawB;
-            const uint32_t gcl_bytes = raw ? rawB : gB;
+        const uint32_t dB = (db + 7) >> 3, gB = (gbits + 7) >> 3, sB = (sbits + 7) >> 3;
+        const uint32_t rawB = nb ? cfg->raw_bytes[last][k] : 0u;
+        const int raw = nb && sB + gB > rawB;
+        const uint32_t gcl_bytes = raw ? rawB : gB;
+        const uint32_t hb = nb ? (cfg->short_hdr ? 5u : 7u) : 0u;
+        const uint32_t pk_bytes = nb ? hb + (raw ? rawB : sB + gB) + dB : 0u;
+        uint32_t pk_total;
+        const uint32_t hdr = cfg->prec_hdr_bytes;
+        const uint32_t start = lead + hdr + warp_excl_scan(pk_bytes, &pk_total);
+        const int fits = start + hb <= words * 4;
+        if (nb && fits) {
             /* packet header (PackHeaders.c:98-127), sign length 0 */
-            const uint32_t hp = pos >> 3;
-            if (hp + (cfg->short_hdr ? 5u : 7u) > words * 4) {
-                ok = 0;
-                break;
-            }
-            uint8_t* hb = (uint8_t*)buf + hp;
+            uint8_t* h = (uint8_t*)buf + start;
             if (cfg->short_hdr) {
-                hb[0] = (uint8_t)((raw << 7) | ((dB >> 8) & 0x7f));
-                hb[1] = (uint8_t)dB;
-                hb[2] = (uint8_t)(gcl_bytes >> 5);
-                hb[3] = (uint8_t)((gcl_bytes & 0x1f) << 3);
-                hb[4] = 0;
-                pos += 40;
+                h[0] = (uint8_t)((raw << 7) | ((dB >> 8) & 0x7f));
+                h[1] = (uint8_t)dB;
+                h[2] = (uint8_t)(gcl_bytes >> 5);
+                h[3] = (uint8_t)((gcl_bytes & 0x1f) << 3);
+                h[4] = 0;
             } else {
-                hb[0] = (uint8_t)((raw << 7) | ((dB >> 13) & 0x7f));
-                hb[1] = (uint8_t)(dB >> 5);
-                hb[2] = (uint8_t)(((dB & 0x1f) << 3) | ((gcl_bytes >> 17) & 7));
-                hb[3] = (uint8_t)(gcl_bytes >> 9);
-                hb[4] = (uint8_t)(gcl_bytes >> 1);
-                hb[5] = (uint8_t)((gcl_bytes & 1) << 7);
-                hb[6] = 0;
-                pos += 56;
+                h[0] = (uint8_t)((raw << 7) | ((dB >> 13) & 0x7f));
+                h[1] = (uint8_t)(dB >> 5);
+                h[2] = (uint8_t)(((dB & 0x1f) << 3) | ((gcl_bytes >> 17) & 7));
+                h[3] = (uint8_t)(gcl_bytes >> 9);
+                h[4] = (uint8_t)(gcl_bytes >> 1);
+                h[5] = (uint8_t)((gcl_bytes & 1) << 7);
+                h[6] = 0;
             }
+            uint32_t pos = (start + hb) * 8;
             if (raw) {
                 uint32_t gp = pos;
-                for (uint32_t x = b; x < b_end; x++) {
+                for (uint32_t x = b0; x < b0 + nb; x++) {
                     pl[x].raw = 1;
                     pl[x].gcli_pos = gp;
                     gp += 4 * bls[x].gcli_w;
@@ -628,46 +608,71 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
                 pos += rawB * 8;
             } else {
                 uint32_t sp = pos;
-                for (uint32_t x = b; x < b_end; x++) {
+                for (uint32_t x = b0; x < b0 + nb; x++) {
                     pl[x].raw = 0;
                     pl[x].sig_pos = sp;
                     if (pl[x].meth) sp += bls[x].sig_w;
                 }
                 pos += sB * 8;
                 uint32_t gp = pos;
-                for (uint32_t x = b; x < b_end; x++) {
+                for (uint32_t x = b0; x < b0 + nb; x++) {
                     pl[x].gcli_pos = gp;
                     gp += pl[x].meth ? pl[x].vlc - pl[x].zero : pl[x].vlc;
                 }
                 pos += gB * 8;
             }
+            /* data sub-packet; each segment's start in its band line's GCLI
+             * and data bits */
             uint32_t dp = pos;
-            for (uint32_t x = b; x < b_end; x++) {
+            for (uint32_t x = b0; x < b0 + nb; x++) {
                 pl[x].data_pos = dp;
+                const jxs_bline_t& B = bls[x];
+                uint32_t vp = pl[x].gcli_pos, sdp = dp;
+                for (uint32_t i = B.seg0; i < B.seg0 + B.nseg; i++) {
+                    const uint32_t vb = pl[x].meth ? s_vlc[i] - s_zero[i] : s_vlc[i], d = s_data[i];
+                    s_vlc[i] = vp;
+                    s_data[i] = sdp;
+                    vp += vb;
+                    sdp += d;
+                }
                 dp += pl[x].data;
             }
-            pos += dB * 8;
-            b = b_end;
         }
-        /* each segment's start in its band line's GCLI and data sub-packets */
-        for (uint32_t x = 0; x < nbl && ok; x++) {
-            const jxs_bline_t& B = bls[x];
-            uint32_t vp = pl[x].gcli_pos, dp = pl[x].data_pos;
-            for (uint32_t i = B.seg0; i < B.seg0 + B.nseg; i++) {
-                const uint32_t vb = pl[x].meth ? s_vlc[i] - s_zero[i] : s_vlc[i], d = s_data[i];
-                s_vlc[i] = vp;
-                s_data[i] = dp;
-                vp += vb;
-                dp += d;
+        /* precinct header: Lprc, Q, R as bytes first, then the 2-bit band
+         * coding modes D[p,b] of every existing band */
+        if (lane == 0) {
+            uint8_t* bytes = (uint8_t*)buf + lead;
+            const uint32_t lprc = total - hdr;
+            bytes[0] = (uint8_t)(lprc >> 16);
+            bytes[1] = (uint8_t)(lprc >> 8);
+            bytes[2] = (uint8_t)lprc;
+            bytes[3] = R.q;
+            bytes[4] = R.r;
+        }
+        __syncwarp();
+        uint32_t idx0 = 0;
+        for (uint32_t gb0 = 0; gb0 < cfg->nbands_all; gb0 += 32) {
+            const uint32_t gb = gb0 + lane;
+            const int fb = gb < cfg->nbands_all ? cfg->g2f[gb] : JXS_NOBAND;
+            const bool ex = fb != JXS_NOBAND;
+            const uint32_t bal = __ballot_sync(FULL, ex);
+            if (ex) {
+                const jxs_band_t& bd = cfg->band[fb];
+                const uint32_t lines = last ? bd.last_lines : bd.lines;
+                if (lines > 0 && s_meth[fb]) put_bits(buf, lead * 8 + 40 + 2 * (idx0 + __popc(bal & ((1u << lane) - 1))), 2u, 2);
             }
+            idx0 += __popc(bal);
         }
         /* the packed size must be what the rate control paid for */
-        const uint32_t end = pos / 8 - lead;
-        s_ok = ok && (pos & 7) == 0 && end <= total && end == cfg->hdrs_bytes[last] + R.data_bytes;
-        if (!s_ok) {
-            printf("jxs pack: precinct %d packs to %u bytes, rate control paid %u + %u bytes (total %u)\n", p, end,
-                   cfg->hdrs_bytes[last], R.data_bytes, total);
-            JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+        const int all_fit = __all_sync(FULL, fits || !nb);
+        if (lane == 0) {
+            const uint32_t end = hdr + pk_total;
+            s_ok = all_fit && end <= total && end == cfg->hdrs_bytes[last] + R.data_bytes;
+            if (!s_ok) {
+                printf("jxs pack: precinct %d packs to %u bytes, rate control paid %u + %u bytes (total %u)\n", p, end,
+                       cfg->hdrs_bytes[last], R.data_bytes, total);
+                JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
+            }
         }
     }
     __syncthreads();
