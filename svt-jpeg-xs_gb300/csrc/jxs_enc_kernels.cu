@@ -23,184 +23,140 @@
 /* ------------------------------------------------------------------------ */
 /* Rate control                                                              */
 /* ------------------------------------------------------------------------ */
-#define RC_MAXBL 80
-
-struct BandLine {
-    uint16_t fb;       /* flat band */
-    uint8_t line, pk;
-    uint32_t row;      /* band row */
-    uint32_t gcli_w, sig_w, w;
-    uint32_t g0;       /* first group in the precinct's flattened group order */
-    uint32_t s0;       /* first significance group in flattened order */
-};
-
-/* Builds the band-line list of precinct row p in codestream order (packet
- * order, then band order inside the packet).  Returns the count. */
-DEV int build_bandlines(const jxs_cfg_t* cfg, int p, int last, BandLine* bl, uint8_t* blmap /* [fb*4+line] */,
-                        uint32_t* total_groups, uint32_t* total_sig) {
-    int n = 0;
-    uint32_t g0 = 0, s0 = 0;
-    for (int i = 0; i < JXS_MAXBL * 4; i++) blmap[i] = 0xff;
-    for (uint32_t k = 0; k < cfg->npk; k++) {
-        const uint32_t l = cfg->pk[k].line;
-        for (uint32_t gb = cfg->pk[k].bs; gb < cfg->pk[k].be; gb++) {
-            const int fb = cfg->g2f[gb];
-            const jxs_band_t& bd = cfg->band[fb];
-            const uint32_t lines = last ? bd.last_lines : bd.lines;
-            if (l >= lines) continue;
-            BandLine& b = bl[n];
-            b.fb = (uint16_t)fb;
-            b.line = (uint8_t)l;
-            b.pk = (uint8_t)k;
-            b.row = (uint32_t)p * bd.lines + l;
-            b.gcli_w = bd.gcli_w;
-            b.sig_w = bd.sig_w;
-            b.w = bd.w;
-            b.g0 = g0;
-            b.s0 = s0;
-            blmap[fb * 4 + l] = (uint8_t)n;
-            g0 += bd.gcli_w;
-            s0 += bd.sig_w;
-            n++;
-        }
-    }
-    *total_groups = g0;
-    *total_sig = s0;
-    return n;
-}
-
-DEV int find_bl_by_sig(const BandLine* bl, int n, uint32_t s) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        int mid = (lo + hi + 1) >> 1;
-        if (bl[mid].s0 <= s) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-/* Reads up to 8 GCLIs of significance group s of a band line. */
-DEV int load_sig_group(const uint8_t* __restrict__ gcli, const jxs_band_t& bd, const BandLine& b, uint32_t s, uint8_t v[8]) {
-    const uint8_t* row = gcli + bd.gcli_off + (uint64_t)b.row * bd.gpitch + 8 * s;
-    uint2 raw = *(const uint2*)row; /* rows are 16-byte aligned, groups of 8 are 8-byte aligned */
-    const int cnt = min(8, (int)b.gcli_w - (int)(8 * s));
-#pragma unroll
-    for (int k = 0; k < 8; k++) {
-        uint32_t word = k < 4 ? raw.x : raw.y;
-        v[k] = k < cnt ? (uint8_t)((word >> (8 * (k & 3))) & 0xff) : 0;
-    }
-    return cnt;
-}
+#define FULL 0xffffffffu
+#define RC_THREADS 512
+#define RC_WARPS (RC_THREADS / 32)
 
 /* Byte cost of every (quantization, refinement) candidate of one precinct
  * row: rate_control_lut_fill, rate_control_calculate_band_best_method and
- * precinct_get_budget_bytes (RateControl.c:18-154, 457-781). */
-__global__ void __launch_bounds__(256) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
-                                                      uint32_t* __restrict__ cost) {
-    __shared__ BandLine bl[RC_MAXBL];
-    __shared__ uint8_t blmap[JXS_MAXBL * 4];
-    __shared__ uint32_t hist[RC_MAXBL][16];
-    __shared__ uint32_t shist[RC_MAXBL][16];
-    __shared__ int pmax[RC_MAXBL];
-    __shared__ uint32_t t_data[RC_MAXBL][16], t_nosig[RC_MAXBL][16], t_sigg[RC_MAXBL][16];
-    __shared__ uint8_t meth[JXS_MAXBL][16];
-    __shared__ int s_nbl;
-    __shared__ uint32_t s_ng, s_ns;
+ * precinct_get_budget_bytes (RateControl.c:18-154, 457-781).
+ *   histograms  warp per segment: GCLI histogram of every band line
+ *               (warp-aggregated shared atomics), histogram of the maxima of
+ *               full significance groups, maximum of the partial last group;
+ *   tables      thread per band line: for every gtli t, data bits, GCLI bits
+ *               without significance and with it (suffix sums over the
+ *               histogram); per band, significance coding at t only if
+ *               strictly cheaper over all its lines;
+ *   costs       thread per (Q, R): per packet, data / significance / GCLI
+ *               bytes rounded separately, raw fallback when cheaper. */
+__global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
+                                                           uint32_t* __restrict__ cost) {
+    __shared__ uint32_t hist[JXS_MAXBLINES][16], shist[JXS_MAXBLINES][16];
+    __shared__ int pmax[JXS_MAXBLINES];
+    __shared__ uint32_t tdat[JXS_MAXBLINES][16], tnos[JXS_MAXBLINES][16], tsig[JXS_MAXBLINES][16];
+    __shared__ uint32_t cn[JXS_MAXBL][16], cs[JXS_MAXBL][16];
+    __shared__ uint16_t meth[JXS_MAXBL];
+    __shared__ uint8_t lgain[JXS_MAXBLINES], lprio[JXS_MAXBLINES], lfb[JXS_MAXBLINES];
+    __shared__ uint32_t lsig[JXS_MAXBLINES], lraw[JXS_MAXPK];
 
     const int p = blockIdx.x;
     const int last = (p + 1 >= (int)cfg->np);
-    if (threadIdx.x == 0) s_nbl = build_bandlines(cfg, p, last, bl, blmap, &s_ng, &s_ns);
-    for (int t = threadIdx.x; t < RC_MAXBL * 16; t += blockDim.x) {
-        hist[t / 16][t % 16] = 0;
-        shist[t / 16][t % 16] = 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t nbl = cfg->nbline[last], nseg = cfg->nseg[last], SG = cfg->seg_groups;
+    const jxs_bline_t* bls = cfg->bline[last];
+    const jxs_seg_t* segs = cfg->seg[last];
+    for (uint32_t i = threadIdx.x; i < nbl * 16; i += blockDim.x) {
+        hist[i >> 4][i & 15] = 0;
+        shist[i >> 4][i & 15] = 0;
     }
-    for (int t = threadIdx.x; t < RC_MAXBL; t += blockDim.x) pmax[t] = -1;
-    __syncthreads();
-    const int nbl = s_nbl;
-    for (uint32_t s = threadIdx.x; s < s_ns; s += blockDim.x) {
-        const int b = find_bl_by_sig(bl, nbl, s);
-        const BandLine& B = bl[b];
-        uint8_t v[8];
-        const int cnt = load_sig_group(gcli, cfg->band[B.fb], B, s - B.s0, v);
-        uint32_t mx = 0;
-        /* nibble counters: at most 8 equal values per group */
-        uint64_t nib = 0;
-        for (int k = 0; k < cnt; k++) {
-            nib += 1ull << (4 * v[k]);
-            mx = max(mx, (uint32_t)v[k]);
-        }
-        while (nib) {
-            int bin = (__ffsll((long long)nib) - 1) >> 2;
-            uint32_t c = (uint32_t)((nib >> (4 * bin)) & 15);
-            atomicAdd(&hist[b][bin], c);
-            nib &= ~(15ull << (4 * bin));
-        }
-        if (cnt == 8) atomicAdd(&shist[b][mx], 1u);
-        else pmax[b] = (int)mx;
+    for (uint32_t i = threadIdx.x; i < cfg->nbands * 16; i += blockDim.x) {
+        cn[i >> 4][i & 15] = 0;
+        cs[i >> 4][i & 15] = 0;
     }
+    for (uint32_t x = threadIdx.x; x < nbl; x += blockDim.x) {
+        const jxs_band_t& bd = cfg->band[bls[x].fb];
+        pmax[x] = -1;
+        lgain[x] = bd.gain;
+        lprio[x] = bd.prio;
+        lfb[x] = bls[x].fb;
+        lsig[x] = bls[x].sig_w;
+    }
+    for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) lraw[k] = cfg->raw_bytes[last][k];
     __syncthreads();
-    /* per band line and truncation: data bits, GCLI bits without
-     * significance, GCLI bits with significance */
-    for (int t = threadIdx.x; t < nbl * 16; t += blockDim.x) {
-        const int b = t >> 4, g = t & 15;
-        uint32_t data = 0, zero = 0, zs = 0;
-        for (int v = 0; v < 16; v++) {
-            uint32_t c = hist[b][v];
-            if (v > g) data += (uint32_t)(v - g + 1) * c;
-            else {
-                zero += c;
-                zs += shist[b][v];
+
+    /* histograms */
+    for (uint32_t sidx = warp; sidx < nseg; sidx += RC_WARPS) {
+        const jxs_seg_t sg = segs[sidx];
+        const uint32_t x = sg.bl;
+        const jxs_bline_t B = bls[x];
+        const jxs_band_t& bd = cfg->band[B.fb];
+        const uint8_t* grow = gcli + bd.gcli_off + (uint64_t)(p * bd.lines + B.line) * bd.gpitch;
+        const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+        for (uint32_t base = sg.g0; base < gend; base += 32) {
+            const uint32_t g = base + lane;
+            const bool valid = g < gend;
+            const uint32_t v = valid ? grow[g] : 0u;
+            const uint32_t peers = __match_any_sync(FULL, valid ? v : 16u);
+            if (valid && __ffs(peers) - 1 == lane) atomicAdd(&hist[x][v], __popc(peers));
+            uint32_t mx = v;
+            mx = max(mx, __shfl_xor_sync(FULL, mx, 1));
+            mx = max(mx, __shfl_xor_sync(FULL, mx, 2));
+            mx = max(mx, __shfl_xor_sync(FULL, mx, 4));
+            const uint32_t vb = __ballot_sync(FULL, valid);
+            if ((lane & 7) == 0 && valid) {
+                if (__popc((vb >> lane) & 0xffu) == 8) atomicAdd(&shist[x][mx], 1u);
+                else pmax[x] = (int)mx; /* the partial last significance group of the line */
             }
         }
-        uint32_t zeroed = zs * 8;
-        const BandLine& B = bl[b];
-        if (pmax[b] >= 0 && pmax[b] <= g) zeroed += B.gcli_w - (B.gcli_w / 8) * 8;
-        t_data[b][g] = data * 4;
-        t_nosig[b][g] = data + zero;
-        t_sigg[b][g] = data + zero - zeroed;
     }
     __syncthreads();
-    /* coding method per band and truncation: significance only if strictly
-     * cheaper (RateControl.c:528-575) */
-    for (int t = threadIdx.x; t < (int)cfg->nbands * 16; t += blockDim.x) {
-        const int fb = t >> 4, g = t & 15;
-        const jxs_band_t& bd = cfg->band[fb];
-        const uint32_t lines = last ? bd.last_lines : bd.lines;
-        uint32_t cn = 0, cs = bd.sig_w * lines;
-        for (uint32_t l = 0; l < lines; l++) {
-            const int b = blmap[fb * 4 + l];
-            cn += t_nosig[b][g];
-            cs += t_sigg[b][g];
+
+    /* per band line and gtli t: data bits, GCLI bits without / with
+     * significance coding */
+    for (uint32_t x = threadIdx.x; x < nbl; x += blockDim.x) {
+        const uint32_t N = bls[x].gcli_w, partial = N & 7u;
+        int S0 = 0, S1 = 0;
+        for (int t = 15; t >= 0; t--) {
+            const int dsum = S1 - (t - 1) * S0; /* sum over v > t of (v - t + 1) h[v] */
+            tdat[x][t] = 4u * (uint32_t)dsum;
+            tnos[x][t] = (uint32_t)dsum + N - (uint32_t)S0;
+            S0 += (int)hist[x][t];
+            S1 += t * (int)hist[x][t];
         }
-        meth[fb][g] = (uint8_t)(cfg->sig && cn > cs);
+        uint32_t Z = 0;
+        const int pm = pmax[x];
+        const uint32_t fb = lfb[x];
+        for (int t = 0; t < 16; t++) {
+            Z += shist[x][t];
+            const uint32_t zer = 8 * Z + ((pm >= 0 && pm <= t) ? partial : 0u);
+            tsig[x][t] = tnos[x][t] - zer;
+            atomicAdd(&cn[fb][t], tnos[x][t]);
+            atomicAdd(&cs[fb][t], tsig[x][t] + lsig[x]);
+        }
     }
     __syncthreads();
+    /* coding method per band and t: significance only if strictly cheaper
+     * (RateControl.c:528-575) */
+    for (uint32_t fb = threadIdx.x; fb < cfg->nbands; fb += blockDim.x) {
+        uint32_t m = 0;
+        if (cfg->sig)
+            for (int t = 0; t < 16; t++) m |= (cn[fb][t] > cs[fb][t] ? 1u : 0u) << t;
+        meth[fb] = (uint16_t)m;
+    }
+    __syncthreads();
+
     const int nq = cfg->max_q + 1, nr = cfg->max_r + 1;
     uint32_t* out = cost + (uint64_t)p * 32 * 32;
-    for (int t = threadIdx.x; t < nq * nr; t += blockDim.x) {
-        const int q = t / nr, r = t - q * nr;
+    for (int e = threadIdx.x; e < nq * nr; e += blockDim.x) {
+        const int q = e / nr, r = e - q * nr;
         uint32_t total = 0;
         for (uint32_t k = 0; k < cfg->npk; k++) {
-            const uint32_t l = cfg->pk[k].line;
+            const uint32_t b0 = cfg->pk_bl0[last][k], nb = cfg->pk_nbl[last][k];
+            if (!nb) continue;
             uint32_t db = 0, gb = 0, sb = 0;
-            for (uint32_t gband = cfg->pk[k].bs; gband < cfg->pk[k].be; gband++) {
-                const int fb = cfg->g2f[gband];
-                const int b = blmap[fb * 4 + l];
-                if (b == 0xff) continue;
-                const jxs_band_t& bd = cfg->band[fb];
-                const int g = jxs_truncation(bd.gain, bd.prio, (uint8_t)q, (uint8_t)r);
-                db += t_data[b][g];
-                if (meth[fb][g]) {
-                    gb += t_sigg[b][g];
-                    sb += bd.sig_w;
+            for (uint32_t x = b0; x < b0 + nb; x++) {
+                const int g = lgain[x] + (lprio[x] < r ? 1 : 0);
+                const int t = q < g ? 0 : min(q - g, 15);
+                db += tdat[x][t];
+                if ((meth[lfb[x]] >> t) & 1u) {
+                    gb += tsig[x][t];
+                    sb += lsig[x];
                 } else {
-                    gb += t_nosig[b][g];
+                    gb += tnos[x][t];
                 }
             }
             const uint32_t dB = (db + 7) >> 3, gB = (gb + 7) >> 3, sB = (sb + 7) >> 3;
-            total += dB;
-            const uint32_t raw = cfg->raw_bytes[last][k];
-            total += (sB + gB > raw) ? raw : sB + gB;
+            total += dB + min(lraw[k], sB + gB);
         }
         out[q * 32 + r] = total;
     }
@@ -243,10 +199,13 @@ DEV int bs_next(BSearch& s, int res, int* out) {
 /* One block per slice: the slice's precinct budgets with the padding carry
  * of rate-control mode 1 (PackStageProcess.c:600-684, 293-309) and
  * rate_control_precinct (RateControl.c:1259-1333) with its binary searches
- * (:889-1083), evaluated on the cost table. */
+ * (:889-1083), evaluated on the cost tables.  The tables of up to RS_CHUNK
+ * precincts are loaded in one go; thread 0 then runs their searches in
+ * order. */
+#define RS_CHUNK 8
 __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restrict__ cfg, const uint32_t* __restrict__ cost,
                                                         PrecRC* __restrict__ rc, int* __restrict__ status) {
-    __shared__ uint32_t tbl[32 * 32];
+    extern __shared__ uint32_t tbl[]; /* [RS_CHUNK][nq][nr] */
     __shared__ uint32_t s_carry, s_run;
     __shared__ int s_err;
     const int s = blockIdx.x;
@@ -271,76 +230,81 @@ __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restr
         s_run = cfg->slice_begin[s] + 6;
         s_err = 0;
     }
-    const int nr = cfg->max_r + 1;
-    for (uint32_t i = 0; i < nprec; i++) {
-        const uint32_t p = first_p + i;
+    const int nq = cfg->max_q + 1, nr = cfg->max_r + 1, nt = nq * nr;
+    for (uint32_t c0 = 0; c0 < nprec; c0 += RS_CHUNK) {
+        const uint32_t cnt = min((uint32_t)RS_CHUNK, nprec - c0);
         __syncthreads();
         if (s_err) break;
-        for (int t = threadIdx.x; t < (cfg->max_q + 1) * nr; t += blockDim.x) {
-            const int q = t / nr, r = t - q * nr;
-            tbl[q * 32 + r] = cost[(uint64_t)p * 1024 + q * 32 + r];
+        for (int e = threadIdx.x; e < (int)cnt * nt; e += blockDim.x) {
+            const int i = e / nt, qr = e - i * nt, q = qr / nr, r = qr - q * nr;
+            tbl[e] = cost[(uint64_t)(first_p + c0 + i) * 1024 + q * 32 + r];
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            const int last = (p + 1 >= cfg->np);
-            const uint32_t budget = (i == 0 ? first_b : min_b) + (i < left ? 1 : 0) + s_carry;
-            const uint32_t hdr = cfg->hdrs_bytes[last];
-            int err = 0;
-            if (budget > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
-            else if (budget <= hdr) err = JXS_E_UNDEFINED;
-            int q = 0, r = 0;
-            uint32_t data = 0;
-            if (!err) {
-                const uint32_t avail = budget - hdr;
-                BSearch bs;
-                int step = 6;
-                if (step > cfg->max_q) step = 0;
-                bs_init(bs, 0, cfg->max_q, 0, step);
-                int res, next = BS_BEGIN, v = 0;
-                while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
-                    if (cfg->empty[v] & 1u) next = BS_OUT_OF_RANGE;
-                    else next = tbl[v * 32] > avail ? BS_TOO_SMALL : BS_TOO_BIG;
-                }
-                if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
-                q = v;
+            for (uint32_t ii = 0; ii < cnt && !s_err; ii++) {
+                const uint32_t i = c0 + ii;
+                const uint32_t p = first_p + i;
+                const uint32_t* T = tbl + ii * nt;
+                const int last = (p + 1 >= cfg->np);
+                const uint32_t budget = (i == 0 ? first_b : min_b) + (i < left ? 1 : 0) + s_carry;
+                const uint32_t hdr = cfg->hdrs_bytes[last];
+                int err = 0;
+                if (budget > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
+                else if (budget <= hdr) err = JXS_E_UNDEFINED;
+                int q = 0, r = 0;
+                uint32_t data = 0;
                 if (!err) {
-                    step = 6;
-                    if (step >= cfg->max_r) step = 0;
-                    bs_init(bs, 0, cfg->max_r, 1, step);
-                    next = BS_BEGIN;
+                    const uint32_t avail = budget - hdr;
+                    BSearch bs;
+                    int step = 6;
+                    if (step > cfg->max_q) step = 0;
+                    bs_init(bs, 0, cfg->max_q, 0, step);
+                    int res, next = BS_BEGIN, v = 0;
                     while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
-                        if ((cfg->empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
-                        else next = tbl[q * 32 + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
+                        if (cfg->empty[v] & 1u) next = BS_OUT_OF_RANGE;
+                        else next = T[v * nr] > avail ? BS_TOO_SMALL : BS_TOO_BIG;
                     }
                     if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
-                    r = v;
-                    data = tbl[q * 32 + r];
-                }
-                if (!err) {
-                    uint32_t padding = avail - data;
-                    uint32_t total = budget;
-                    if (cfg->rc_mode == 1 && i + 1 < nprec) {
-                        total -= padding;
-                        s_carry = padding;
-                    } else {
-                        s_carry = 0;
+                    q = v;
+                    if (!err) {
+                        step = 6;
+                        if (step >= cfg->max_r) step = 0;
+                        bs_init(bs, 0, cfg->max_r, 1, step);
+                        next = BS_BEGIN;
+                        while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
+                            if ((cfg->empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
+                            else next = T[q * nr + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
+                        }
+                        if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
+                        r = v;
+                        data = T[q * nr + r];
                     }
-                    PrecRC o;
-                    o.total_bytes = total;
-                    o.offset = s_run;
-                    o.data_bytes = data;
-                    o.q = (uint8_t)q;
-                    o.r = (uint8_t)r;
-                    o.first_in_slice = (uint8_t)(i == 0);
-                    o.pad = 0;
-                    rc[p] = o;
-                    s_run += total;
+                    if (!err) {
+                        uint32_t padding = avail - data;
+                        uint32_t total = budget;
+                        if (cfg->rc_mode == 1 && i + 1 < nprec) {
+                            total -= padding;
+                            s_carry = padding;
+                        } else {
+                            s_carry = 0;
+                        }
+                        PrecRC o;
+                        o.total_bytes = total;
+                        o.offset = s_run;
+                        o.data_bytes = data;
+                        o.q = (uint8_t)q;
+                        o.r = (uint8_t)r;
+                        o.first_in_slice = (uint8_t)(i == 0);
+                        o.pad = 0;
+                        rc[p] = o;
+                        s_run += total;
+                    }
                 }
-            }
-            if (err) {
-                printf("jxs rc: slice %d precinct %u budget %u: error 0x%x\n", s, p, budget, (unsigned)err);
-                s_err = err;
-                JXS_STATUS_SET(status, err);
+                if (err) {
+                    printf("jxs rc: slice %d precinct %u budget %u: error 0x%x\n", s, p, budget, (unsigned)err);
+                    s_err = err;
+                    JXS_STATUS_SET(status, err);
+                }
             }
         }
     }
@@ -351,7 +315,6 @@ __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restr
 /* ------------------------------------------------------------------------ */
 #define PK_THREADS 512
 #define PK_WARPS (PK_THREADS / 32)
-#define FULL 0xffffffffu
 
 /* OR `n` (<= 32) bits of `v` at bit position `pos` of a big-endian bit
  * string stored in native byte order.  Writes beyond the precinct's words
@@ -771,8 +734,8 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
 /* ------------------------------------------------------------------------ */
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
                                      PrecRC* rc, int* status, cudaStream_t st) {
-    rc_cost_kernel<<<np, 256, 0, st>>>(dcfg, gcli, cost);
-    rc_select_kernel<<<nslices, 128, 0, st>>>(dcfg, cost, rc, status);
+    rc_cost_kernel<<<np, RC_THREADS, 0, st>>>(dcfg, gcli, cost);
+    rc_select_kernel<<<nslices, 128, RS_CHUNK * 32 * 32 * sizeof(uint32_t), st>>>(dcfg, cost, rc, status);
     return cudaGetLastError();
 }
 
