@@ -83,6 +83,20 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
             }
             g->nbline[t] = n;
             g->nseg[t] = ns;
+            /* each packet's band lines by ascending priority (insertion sort) */
+            for (uint32_t k = 0; k < g->npk; k++) {
+                const uint32_t b0 = g->pk_bl0[t][k], nb = g->pk_nbl[t][k];
+                for (uint32_t i = 0; i < nb; i++) g->pk_order[t][b0 + i] = (uint8_t)(b0 + i);
+                for (uint32_t i = 1; i < nb; i++) {
+                    const uint8_t x = g->pk_order[t][b0 + i];
+                    uint32_t j = i;
+                    while (j > 0 && g->band[g->bline[t][g->pk_order[t][b0 + j - 1]].fb].prio > g->band[g->bline[t][x].fb].prio) {
+                        g->pk_order[t][b0 + j] = g->pk_order[t][b0 + j - 1];
+                        j--;
+                    }
+                    g->pk_order[t][b0 + j] = x;
+                }
+            }
             if (ns > JXS_MAXSEG) fits = 0;
         }
         if (fits) break;

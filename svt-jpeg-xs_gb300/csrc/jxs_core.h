@@ -106,6 +106,7 @@ typedef struct jxs_cfg {
     jxs_bline_t bline[2][JXS_MAXBLINES];
     uint8_t pk_bl0[2][JXS_MAXPK];        /* first band line of each packet (its count in pk_nbl; 0: absent) */
     uint8_t pk_nbl[2][JXS_MAXPK];
+    uint8_t pk_order[2][JXS_MAXBLINES];  /* band lines of each packet (from pk_bl0) in ascending band priority */
     uint32_t seg_groups;                 /* groups per segment, a multiple of 32 */
     uint32_t nseg[2];
     jxs_seg_t seg[2][JXS_MAXSEG];

@@ -37,8 +37,9 @@
  *               without significance and with it (suffix sums over the
  *               histogram); per band, significance coding at t only if
  *               strictly cheaper over all its lines;
- *   costs       thread per (Q, R): per packet, data / significance / GCLI
- *               bytes rounded separately, raw fallback when cheaper. */
+ *   costs       per packet, data / significance / GCLI bytes rounded
+ *               separately, raw fallback when cheaper; summed over packets
+ *               for every (Q, R). */
 __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
                                                            uint32_t* __restrict__ cost) {
     __shared__ uint32_t hist[JXS_MAXBLINES][16], shist[JXS_MAXBLINES][16];
@@ -48,6 +49,7 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
     __shared__ uint16_t meth[JXS_MAXBL];
     __shared__ uint8_t lgain[JXS_MAXBLINES], lprio[JXS_MAXBLINES], lfb[JXS_MAXBLINES];
     __shared__ uint32_t lsig[JXS_MAXBLINES], lraw[JXS_MAXPK];
+    __shared__ uint32_t dC[32][32]; /* per Q: cost at R = 0, then its changes at each R */
 
     const int p = blockIdx.x;
     const int last = (p + 1 >= (int)cfg->np);
@@ -74,7 +76,8 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
     for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) lraw[k] = cfg->raw_bytes[last][k];
     __syncthreads();
 
-    /* histograms */
+    /* histograms: per lane, 8-bit counters packed four to a register,
+     * summed over the warp every 4 iterations (at most 128 per bin) */
     for (uint32_t sidx = warp; sidx < nseg; sidx += RC_WARPS) {
         const jxs_seg_t sg = segs[sidx];
         const uint32_t x = sg.bl;
@@ -82,20 +85,42 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
         const jxs_band_t& bd = cfg->band[B.fb];
         const uint8_t* grow = gcli + bd.gcli_off + (uint64_t)(p * bd.lines + B.line) * bd.gpitch;
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+        uint32_t h[4] = {0, 0, 0, 0}, sh[4] = {0, 0, 0, 0};
+        int it = 0;
         for (uint32_t base = sg.g0; base < gend; base += 32) {
             const uint32_t g = base + lane;
             const bool valid = g < gend;
             const uint32_t v = valid ? grow[g] : 0u;
-            const uint32_t peers = __match_any_sync(FULL, valid ? v : 16u);
-            if (valid && __ffs(peers) - 1 == lane) atomicAdd(&hist[x][v], __popc(peers));
+            const uint32_t inc = valid ? 1u << (8 * (v & 3)) : 0u;
+#pragma unroll
+            for (int r = 0; r < 4; r++) h[r] += (v >> 2) == (uint32_t)r ? inc : 0u;
             uint32_t mx = v;
             mx = max(mx, __shfl_xor_sync(FULL, mx, 1));
             mx = max(mx, __shfl_xor_sync(FULL, mx, 2));
             mx = max(mx, __shfl_xor_sync(FULL, mx, 4));
             const uint32_t vb = __ballot_sync(FULL, valid);
             if ((lane & 7) == 0 && valid) {
-                if (__popc((vb >> lane) & 0xffu) == 8) atomicAdd(&shist[x][mx], 1u);
-                else pmax[x] = (int)mx; /* the partial last significance group of the line */
+                if (__popc((vb >> lane) & 0xffu) == 8) {
+                    const uint32_t si = 1u << (8 * (mx & 3));
+#pragma unroll
+                    for (int r = 0; r < 4; r++) sh[r] += (mx >> 2) == (uint32_t)r ? si : 0u;
+                } else {
+                    pmax[x] = (int)mx; /* the partial last significance group of the line */
+                }
+            }
+            if (++it == 4 || base + 32 >= gend) {
+                it = 0;
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    const uint32_t hs = __reduce_add_sync(FULL, h[r]), ss = __reduce_add_sync(FULL, sh[r]);
+                    if (lane < 4) {
+                        const uint32_t c = (hs >> (8 * lane)) & 0xffu, cs2 = (ss >> (8 * lane)) & 0xffu;
+                        if (c) atomicAdd(&hist[x][4 * r + lane], c);
+                        if (cs2) atomicAdd(&shist[x][4 * r + lane], cs2);
+                    }
+                    h[r] = 0;
+                    sh[r] = 0;
+                }
             }
         }
     }
@@ -135,30 +160,56 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
     }
     __syncthreads();
 
+    /* costs: band priorities are distinct, so raising R by one lowers the
+     * gtli of one band only; each (Q, packet) thread adds its packet's cost
+     * at R = 0 and its change at every R where one of its band lines drops,
+     * and the table is a prefix sum over R */
     const int nq = cfg->max_q + 1, nr = cfg->max_r + 1;
-    uint32_t* out = cost + (uint64_t)p * 32 * 32;
-    for (int e = threadIdx.x; e < nq * nr; e += blockDim.x) {
-        const int q = e / nr, r = e - q * nr;
-        uint32_t total = 0;
-        for (uint32_t k = 0; k < cfg->npk; k++) {
-            const uint32_t b0 = cfg->pk_bl0[last][k], nb = cfg->pk_nbl[last][k];
-            if (!nb) continue;
-            uint32_t db = 0, gb = 0, sb = 0;
-            for (uint32_t x = b0; x < b0 + nb; x++) {
-                const int g = lgain[x] + (lprio[x] < r ? 1 : 0);
-                const int t = q < g ? 0 : min(q - g, 15);
-                db += tdat[x][t];
-                if ((meth[lfb[x]] >> t) & 1u) {
-                    gb += tsig[x][t];
-                    sb += lsig[x];
-                } else {
-                    gb += tnos[x][t];
-                }
+    for (int e = threadIdx.x; e < nq * 32; e += blockDim.x) dC[e >> 5][e & 31] = 0;
+    __syncthreads();
+    const uint32_t npk = cfg->npk;
+    for (uint32_t e = threadIdx.x; e < (uint32_t)nq * npk; e += blockDim.x) {
+        const int q = (int)(e / npk);
+        const uint32_t k = e - (uint32_t)q * npk;
+        const uint32_t b0 = cfg->pk_bl0[last][k], nb = cfg->pk_nbl[last][k];
+        if (!nb) continue;
+        uint32_t db = 0, gb = 0, sb = 0;
+        for (uint32_t x = b0; x < b0 + nb; x++) {
+            const int g = lgain[x];
+            const int t = q < g ? 0 : min(q - g, 15);
+            db += tdat[x][t];
+            if ((meth[lfb[x]] >> t) & 1u) {
+                gb += tsig[x][t];
+                sb += lsig[x];
+            } else {
+                gb += tnos[x][t];
             }
-            const uint32_t dB = (db + 7) >> 3, gB = (gb + 7) >> 3, sB = (sb + 7) >> 3;
-            total += dB + min(lraw[k], sB + gB);
         }
-        out[q * 32 + r] = total;
+        uint32_t c = ((db + 7) >> 3) + min(lraw[k], ((sb + 7) >> 3) + ((gb + 7) >> 3));
+        atomicAdd(&dC[q][0], c);
+        for (uint32_t i = 0; i < nb; i++) {
+            const uint32_t x = cfg->pk_order[last][b0 + i];
+            const int rf = lprio[x] + 1; /* the line's gtli drops by one for R >= priority + 1 */
+            if (rf >= nr) break;
+            const int g = lgain[x];
+            const int t0 = q < g ? 0 : min(q - g, 15), t1 = q < g + 1 ? 0 : min(q - g - 1, 15);
+            const uint32_t m0 = (meth[lfb[x]] >> t0) & 1u, m1 = (meth[lfb[x]] >> t1) & 1u;
+            db += tdat[x][t1] - tdat[x][t0];
+            gb += (m1 ? tsig[x][t1] : tnos[x][t1]) - (m0 ? tsig[x][t0] : tnos[x][t0]);
+            sb += (m1 ? lsig[x] : 0u) - (m0 ? lsig[x] : 0u);
+            const uint32_t c1 = ((db + 7) >> 3) + min(lraw[k], ((sb + 7) >> 3) + ((gb + 7) >> 3));
+            atomicAdd(&dC[q][rf], c1 - c);
+            c = c1;
+        }
+    }
+    __syncthreads();
+    uint32_t* out = cost + (uint64_t)p * 32 * 32;
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        uint32_t run = 0;
+        for (int r = 0; r < nr; r++) {
+            run += dC[q][r];
+            out[q * 32 + r] = run;
+        }
     }
 }
 
