@@ -83,20 +83,6 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
             }
             g->nbline[t] = n;
             g->nseg[t] = ns;
-            /* each packet's band lines by ascending priority (insertion sort) */
-            for (uint32_t k = 0; k < g->npk; k++) {
-                const uint32_t b0 = g->pk_bl0[t][k], nb = g->pk_nbl[t][k];
-                for (uint32_t i = 0; i < nb; i++) g->pk_order[t][b0 + i] = (uint8_t)(b0 + i);
-                for (uint32_t i = 1; i < nb; i++) {
-                    const uint8_t x = g->pk_order[t][b0 + i];
-                    uint32_t j = i;
-                    while (j > 0 && g->band[g->bline[t][g->pk_order[t][b0 + j - 1]].fb].prio > g->band[g->bline[t][x].fb].prio) {
-                        g->pk_order[t][b0 + j] = g->pk_order[t][b0 + j - 1];
-                        j--;
-                    }
-                    g->pk_order[t][b0 + j] = x;
-                }
-            }
             if (ns > JXS_MAXSEG) fits = 0;
         }
         if (fits) break;
@@ -104,6 +90,25 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
     }
     g->seg_groups = sg;
     return JXS_OK;
+}
+
+/* Each packet's band lines by ascending band priority (the order in which
+ * a growing refinement R lowers their gtli); needs the weight tables. */
+static void cfg_pk_order(jxs_cfg_t* g) {
+    for (int t = 0; t < 2; t++)
+        for (uint32_t k = 0; k < g->npk; k++) {
+            const uint32_t b0 = g->pk_bl0[t][k], nb = g->pk_nbl[t][k];
+            for (uint32_t i = 0; i < nb; i++) g->pk_order[t][b0 + i] = (uint8_t)(b0 + i);
+            for (uint32_t i = 1; i < nb; i++) {
+                const uint8_t x = g->pk_order[t][b0 + i];
+                uint32_t j = i;
+                while (j > 0 && g->band[g->bline[t][g->pk_order[t][b0 + j - 1]].fb].prio > g->band[g->bline[t][x].fb].prio) {
+                    g->pk_order[t][b0 + j] = g->pk_order[t][b0 + j - 1];
+                    j--;
+                }
+                g->pk_order[t][b0 + j] = x;
+            }
+        }
 }
 
 int32_t jxs_cfg_geometry(jxs_cfg_t* g, int for_encoder, uint32_t nc, uint32_t W, uint32_t H, uint32_t dh, uint32_t dv,
@@ -554,6 +559,7 @@ int32_t jxs_cfg_encoder(jxs_cfg_t* g, struct svt_jpeg_xs_encoder_api* api) {
     rc_limits(g);
     write_header(g);
 
+    cfg_pk_order(g);
     return jxs_cfg_slices(g);
 }
 
@@ -701,6 +707,7 @@ int32_t jxs_cfg_decoder(jxs_cfg_t* g, const uint8_t* bs, size_t size, jxs_hdr_in
     if (g->hdr_len > sizeof(g->hdr)) return JXS_E_DEC_BITSTREAM;
     memcpy(g->hdr, bs, g->hdr_len);
     /* predicted slice starts for constant-bit-rate streams (checked on use) */
+    cfg_pk_order(g);
     if (jxs_cfg_slices(g) != JXS_OK) g->max_slice_budget = 0;
     return JXS_OK;
 }
