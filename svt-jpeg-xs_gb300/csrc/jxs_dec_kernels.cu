@@ -97,30 +97,50 @@ DEV uint32_t block_scan1(uint32_t a, uint32_t* ea, uint32_t* ws) {
  * Packing.c:134-219): sign nibble (coefficient 0 in the most significant
  * bit), then bit-planes gcli-1 .. gtli; planes placed at << gtli
  * (Packing.c:117-132), deadzone or uniform dequantization (Dequant.c:9-57)
- * and sign-magnitude to two's complement (inv_sign_c, Precinct.c:9-14). */
-DEV void decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uint32_t uniform, int32_t out[4]) {
+ * and sign-magnitude to two's complement (inv_sign_c, Precinct.c:9-14).
+ * Returns the four int16 results packed two per word, coefficient 0 in the
+ * low half of .x; coefficients at or past `wl` (remaining width) are 0. */
+DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uint32_t uniform, int wl) {
     const uint32_t sgn = (uint32_t)(chunk >> (4 * np)) & 15u;
-    const uint64_t planes = np >= 16 ? chunk : chunk & ((1ull << (4 * np)) - 1);
+    const uint64_t planes = chunk & ((1ull << (4 * np)) - 1);
     const uint32_t lo = (uint32_t)planes, hi = (uint32_t)(planes >> 32);
+    uint32_t m[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) {
-        uint32_t m = compact4(lo >> (3 - c));
-        if (np > 8) m |= compact4(hi >> (3 - c)) << 8;
-        uint32_t mag = (m << t) & 0xffffu;
-        if (t > 0 && (mag & 0x7fffu)) {
-            if (!uniform) {
-                mag |= 1u << (t - 1);
-            } else {
-                /* inv_quant_uniform (Dequant.c:23-43) */
-                uint32_t val = mag & 0x7fffu, acc = 0;
-                const uint32_t sc = gv - t + 1;
-                for (; val > 0; val >>= sc) acc = (acc + val) & 0xffffu;
-                mag = acc;
-            }
+        m[c] = compact4(lo >> (3 - c));
+        if (np > 8) m[c] |= compact4(hi >> (3 - c)) << 8;
+    }
+    /* keep[] zeroes coefficients past the band width */
+    const uint32_t keepA = (wl > 1 ? 0xffff0000u : 0u) | 0xffffu, keepB = (wl > 2 ? 0xffffu : 0u) | (wl > 3 ? 0xffff0000u : 0u);
+    if (!uniform || t == 0) {
+        /* two coefficients per word: m << t stays below 2^15 */
+        uint32_t A = (m[0] | (m[1] << 16)) << t, B = (m[2] | (m[3] << 16)) << t;
+        if (t > 0) {
+            const uint32_t half = (1u << (t - 1)) * 0x00010001u;
+            A |= __vcmpne2(A, 0u) & half;
+            B |= __vcmpne2(B, 0u) & half;
+        }
+        const uint32_t nA = ((sgn & 8u) ? 0xffffu : 0u) | ((sgn & 4u) ? 0xffff0000u : 0u);
+        const uint32_t nB = ((sgn & 2u) ? 0xffffu : 0u) | ((sgn & 1u) ? 0xffff0000u : 0u);
+        A = (A & ~nA) | (__vsub2(0u, A) & nA);
+        B = (B & ~nB) | (__vsub2(0u, B) & nB);
+        return make_uint2(A & keepA, B & keepB);
+    }
+    uint32_t o[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        uint32_t mag = (m[c] << t) & 0xffffu;
+        if (mag & 0x7fffu) {
+            /* inv_quant_uniform (Dequant.c:23-43) */
+            uint32_t val = mag & 0x7fffu, acc = 0;
+            const uint32_t sc = gv - t + 1;
+            for (; val > 0; val >>= sc) acc = (acc + val) & 0xffffu;
+            mag = acc;
         }
         const uint32_t sm = (mag | (((sgn >> (3 - c)) & 1u) << 15)) & 0xffffu;
-        out[c] = (sm & 0x8000u) ? -(int32_t)(sm & 0x7fffu) : (int32_t)sm;
+        o[c] = (uint32_t)((sm & 0x8000u) ? -(int32_t)(sm & 0x7fffu) : (int32_t)sm) & 0xffffu;
     }
+    return make_uint2((o[0] | (o[1] << 16)) & keepA, (o[2] | (o[3] << 16)) & keepB);
 }
 
 /* unpack_precinct (Packing.c:513-868) for one precinct row; vertical
@@ -488,17 +508,13 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
             const uint32_t len = np ? 4 * (np + 1) : 0u;
             uint32_t tot;
             const uint32_t ex = warp_excl_scan(len, &tot);
-            int32_t o[4] = {0, 0, 0, 0};
+            uint2 o = make_uint2(0u, 0u);
             if (len) {
                 const uint32_t pos = dpos + ex;
                 const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
-                decode_group(win >> (64 - len), np, L.t, v, uniform, o);
+                o = decode_group(win >> (64 - len), np, L.t, v, uniform, (int)B.w - 4 * (int)g);
             }
-            if (valid) {
-                const int wl = (int)B.w - 4 * (int)g;
-                *(uint2*)(crow + 4 * g) = make_uint2(((uint32_t)o[0] & 0xffffu) | ((uint32_t)(wl > 1 ? o[1] : 0) << 16),
-                                                     ((uint32_t)(wl > 2 ? o[2] : 0) & 0xffffu) | ((uint32_t)(wl > 3 ? o[3] : 0) << 16));
-            }
+            if (valid) *(uint2*)(crow + 4 * g) = o;
             dpos += tot;
         }
     }
