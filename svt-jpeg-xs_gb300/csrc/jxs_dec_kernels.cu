@@ -31,6 +31,7 @@ struct UkLine {
 };
 /* Per packet. */
 struct UkPk {
+    uint32_t spos;              /* first bit after the packet header */
     uint32_t gpos, gbits;       /* GCLI sub-packet: bit position and length */
     uint32_t dpos, dbits;       /* data sub-packet */
     uint32_t wbase, nwords;     /* its 32-bit words in the concatenated GCLI word list (VLC packets) */
@@ -93,6 +94,14 @@ DEV uint32_t block_scan1(uint32_t a, uint32_t* ea, uint32_t* ws) {
     return total;
 }
 
+/* Next segment for a warp from a shared queue (the warps balance segments
+ * of different lengths between them). */
+DEV uint32_t next_seg(uint32_t* ctr, int lane) {
+    uint32_t v = 0;
+    if (lane == 0) v = atomicAdd(ctr, 1u);
+    return __shfl_sync(FULL, v, 0);
+}
+
 /* One group's coefficients from its data bits (unpack_data_c,
  * Packing.c:134-219): sign nibble (coefficient 0 in the most significant
  * bit), then bit-planes gcli-1 .. gtli; planes placed at << gtli
@@ -148,7 +157,8 @@ DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uin
  *
  * Dynamic shared memory: [precinct bytes: cap_bytes + 32, stream byte i at
  * i + lead so that 16-byte chunks are aligned] [GCLI per group: cap_groups]
- * [end bit of every zero of the VLC sub-packets: 4 x UK_ZCAP(cap_groups)].
+ * [every zero bit of the VLC sub-packets, as a 16-bit offset in its
+ * sub-packet: 2 x UK_ZCAP(cap_groups)].
  *
  *   copy    the precinct's bytes into shared memory;
  *   parse   thread 0: precinct header, packet headers, sub-packet positions
@@ -168,11 +178,14 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     extern __shared__ __align__(16) uint8_t dsm[];
     uint8_t* pbuf = dsm;
     uint8_t* gcl = dsm + cap_bytes + 32;
-    uint32_t* zend = (uint32_t*)(((uintptr_t)(gcl + cap_groups) + 15) & ~(uintptr_t)15);
+    uint16_t* zend = (uint16_t*)(((uintptr_t)(gcl + cap_groups) + 15) & ~(uintptr_t)15);
     /* zero bits: one per codeword plus up to 7 padding bits per packet */
     const uint32_t zcap = UK_ZCAP(cap_groups);
     __shared__ UkLine ln[JXS_MAXBLINES];
     __shared__ UkPk pk[JXS_MAXPK];
+    __shared__ uint8_t s_mode[JXS_MAXBL];
+    __shared__ uint32_t s_pksb[JXS_MAXPK], s_pkrb[JXS_MAXPK];
+    __shared__ uint32_t s_next[3]; /* segment queues of the three warp passes */
     __shared__ uint32_t s_cnt[JXS_MAXSEG], s_base[JXS_MAXSEG];
     __shared__ uint32_t ws[UK_WARPS];
     __shared__ int s_err;
@@ -182,6 +195,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     const int last = (p + 1 >= (int)cfg->np);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) s_err = *(volatile int*)status;
+    if (threadIdx.x < 3) s_next[threadIdx.x] = 0;
     __syncthreads();
     if (s_err) return; /* the precinct offsets could not be found */
     const uint32_t off = prec_off[p];
@@ -222,101 +236,124 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     const uint32_t nbl = cfg->nbline[last], nseg = cfg->nseg[last], SG = cfg->seg_groups;
     const jxs_bline_t* bls = cfg->bline[last];
     const jxs_seg_t* segs = cfg->seg[last];
-    /* parse */
-    if (threadIdx.x == 0) {
-        int err = 0;
+    /* parse, by warp 0: band modes and per-line fields in parallel, the
+     * packet headers in order by lane 0, then every line's positions */
+    if (warp == 0) {
         const uint8_t* h0 = pbuf + lead;
         const uint8_t q = h0[3], r = h0[4];
-        const uint32_t lprc = total - cfg->prec_hdr_bytes;
-        uint8_t mode[JXS_MAXBL];
-        uint32_t pos = 40;
-        for (uint32_t gb = 0; gb < cfg->nbands_all; gb++) {
-            const int fb = cfg->g2f[gb];
-            if (fb == JXS_NOBAND) continue;
-            mode[fb] = (uint8_t)((h0[pos >> 3] >> (6 - (pos & 7))) & 3);
-            pos += 2;
-            if (mode[fb] & 1) err = JXS_E_DEC_BITSTREAM; /* vertical prediction is not part of this decoder */
+        int err = 0;
+        /* band coding modes D[p,b], 2 bits per existing band */
+        uint32_t idx0 = 0;
+        for (uint32_t gb0 = 0; gb0 < cfg->nbands_all; gb0 += 32) {
+            const uint32_t gb = gb0 + lane;
+            const int fb = gb < cfg->nbands_all ? cfg->g2f[gb] : JXS_NOBAND;
+            const bool ex = fb != JXS_NOBAND;
+            const uint32_t bal = __ballot_sync(FULL, ex);
+            if (ex) {
+                const uint32_t pos = 40 + 2 * (idx0 + __popc(bal & ((1u << lane) - 1)));
+                s_mode[fb] = (uint8_t)((h0[pos >> 3] >> (6 - (pos & 7))) & 3);
+                if (s_mode[fb] & 1) err = JXS_E_DEC_BITSTREAM; /* vertical prediction is not part of this decoder */
+            }
+            idx0 += __popc(bal);
         }
-        for (uint32_t x = 0; x < nbl; x++) {
+        __syncwarp();
+        for (uint32_t x = lane; x < nbl; x += 32) {
             const jxs_band_t& bd = cfg->band[bls[x].fb];
             ln[x].t = jxs_truncation(bd.gain, bd.prio, q, r);
-            ln[x].meth = (mode[bls[x].fb] & 2) ? 1 : 0;
+            ln[x].meth = (s_mode[bls[x].fb] & 2) ? 1 : 0;
             ln[x].pk = bls[x].pk;
         }
-        const int long_hdr = cfg->lh || !cfg->short_hdr;
-        int64_t left = (int64_t)lprc * 8;
-        uint32_t bpos = lead + cfg->prec_hdr_bytes; /* bytes */
-        uint32_t b = 0, tw = 0;
-        for (uint32_t k = 0; k < cfg->npk; k++) {
-            UkPk& P = pk[k];
-            P.present = 0;
-            P.gbits = P.dbits = P.nwords = P.ncoded = P.nzero = 0;
-            P.raw = 0;
-            P.wbase = tw;
-            if (err || b >= nbl || bls[b].pk != k) continue;
-            uint32_t be = b;
-            while (be < nbl && bls[be].pk == k) be++;
-            const uint32_t hb = long_hdr ? 7 : 5;
-            left -= hb * 8;
-            if (left < 0) { err = JXS_E_DEC_BITSTREAM; break; }
-            const uint8_t* h = pbuf + bpos;
-            uint32_t raw, dlen, glen, slen;
-            if (long_hdr) {
-                raw = h[0] >> 7;
-                dlen = ((uint32_t)(h[0] & 0x7f) << 13) | ((uint32_t)h[1] << 5) | (h[2] >> 3);
-                glen = ((uint32_t)(h[2] & 7) << 17) | ((uint32_t)h[3] << 9) | ((uint32_t)h[4] << 1) | (h[5] >> 7);
-                slen = ((uint32_t)(h[5] & 0x7f) << 8) | h[6];
-            } else {
-                raw = h[0] >> 7;
-                dlen = ((uint32_t)(h[0] & 0x7f) << 8) | h[1];
-                glen = ((uint32_t)h[2] << 5) | (h[3] >> 3);
-                slen = ((uint32_t)(h[3] & 7) << 8) | h[4];
+        __syncwarp();
+        /* per packet: significance bits and raw GCLI bits it must hold */
+        uint32_t sb = 0, rb = 0;
+        if (lane < (int)cfg->npk) {
+            const uint32_t b0 = cfg->pk_bl0[last][lane], nb = cfg->pk_nbl[last][lane];
+            for (uint32_t x = b0; x < b0 + nb; x++) {
+                if (ln[x].meth) sb += bls[x].sig_w;
+                rb += 4 * bls[x].gcli_w;
             }
-            bpos += hb;
-            if ((uint64_t)left < ((uint64_t)dlen + glen + slen) * 8) { err = JXS_E_DEC_BITSTREAM; break; }
-            P.raw = raw;
-            if (raw) {
-                uint32_t need = 0;
-                for (uint32_t x = b; x < be; x++) {
-                    ln[x].raw = 1;
-                    ln[x].sig_pos = bpos * 8 + need;
-                    need += 4 * bls[x].gcli_w;
-                }
-                if (need > glen * 8) { err = JXS_E_DEC_BITSTREAM; break; }
-                left -= (int64_t)glen * 8;
-            } else {
-                uint32_t sbits = 0;
-                for (uint32_t x = b; x < be; x++) {
-                    ln[x].raw = 0;
-                    ln[x].sig_pos = bpos * 8 + sbits;
-                    if (ln[x].meth) sbits += bls[x].sig_w;
-                }
-                left -= sbits;
-                if (left < 0) { err = JXS_E_DEC_BITSTREAM; break; }
-                left -= left & 7;
-                bpos += (sbits + 7) >> 3;
-                left -= (int64_t)glen * 8;
-            }
-            P.gpos = bpos * 8;
-            P.gbits = glen * 8;
-            bpos += glen;
-            P.dpos = bpos * 8;
-            P.dbits = dlen * 8;
-            bpos += dlen;
-            left -= (int64_t)dlen * 8;
-            if (cfg->fs) err = JXS_E_DEC_BITSTREAM; /* separate sign sub-packets are not part of this decoder */
-            bpos += slen;
-            if (left < 0 || bpos > lead + total) { err = JXS_E_DEC_BITSTREAM; break; }
-            P.present = 1;
-            if (!raw) {
-                P.nwords = (P.gbits + 31) >> 5;
-                tw += P.nwords;
-            }
-            b = be;
+            s_pksb[lane] = sb;
+            s_pkrb[lane] = rb;
         }
-        s_tw = tw;
-        s_npk = cfg->npk;
-        s_err = err;
+        __syncwarp();
+        if (lane == 0) {
+            const uint32_t lprc = total - cfg->prec_hdr_bytes;
+            const int long_hdr = cfg->lh || !cfg->short_hdr;
+            int64_t left = (int64_t)lprc * 8;
+            uint32_t bpos = lead + cfg->prec_hdr_bytes; /* bytes */
+            uint32_t tw = 0;
+            for (uint32_t k = 0; k < cfg->npk; k++) {
+                UkPk& P = pk[k];
+                P.present = 0;
+                P.gbits = P.dbits = P.nwords = P.ncoded = P.nzero = 0;
+                P.raw = 0;
+                P.wbase = tw;
+                if (err || !cfg->pk_nbl[last][k]) continue;
+                const uint32_t hb = long_hdr ? 7 : 5;
+                left -= hb * 8;
+                if (left < 0) { err = JXS_E_DEC_BITSTREAM; break; }
+                const uint8_t* h = pbuf + bpos;
+                uint32_t raw, dlen, glen, slen;
+                if (long_hdr) {
+                    raw = h[0] >> 7;
+                    dlen = ((uint32_t)(h[0] & 0x7f) << 13) | ((uint32_t)h[1] << 5) | (h[2] >> 3);
+                    glen = ((uint32_t)(h[2] & 7) << 17) | ((uint32_t)h[3] << 9) | ((uint32_t)h[4] << 1) | (h[5] >> 7);
+                    slen = ((uint32_t)(h[5] & 0x7f) << 8) | h[6];
+                } else {
+                    raw = h[0] >> 7;
+                    dlen = ((uint32_t)(h[0] & 0x7f) << 8) | h[1];
+                    glen = ((uint32_t)h[2] << 5) | (h[3] >> 3);
+                    slen = ((uint32_t)(h[3] & 7) << 8) | h[4];
+                }
+                bpos += hb;
+                if ((uint64_t)left < ((uint64_t)dlen + glen + slen) * 8) { err = JXS_E_DEC_BITSTREAM; break; }
+                P.raw = raw;
+                P.spos = bpos * 8;
+                if (raw) {
+                    if (s_pkrb[k] > glen * 8) { err = JXS_E_DEC_BITSTREAM; break; }
+                    left -= (int64_t)glen * 8;
+                } else {
+                    left -= s_pksb[k];
+                    if (left < 0) { err = JXS_E_DEC_BITSTREAM; break; }
+                    left -= left & 7;
+                    bpos += (s_pksb[k] + 7) >> 3;
+                    left -= (int64_t)glen * 8;
+                    /* codeword ends are kept as 16-bit offsets in the sub-packet */
+                    if (glen * 8 > 65535u) { err = JXS_E_DEC_BITSTREAM; break; }
+                }
+                P.gpos = bpos * 8;
+                P.gbits = glen * 8;
+                bpos += glen;
+                P.dpos = bpos * 8;
+                P.dbits = dlen * 8;
+                bpos += dlen;
+                left -= (int64_t)dlen * 8;
+                if (cfg->fs) err = JXS_E_DEC_BITSTREAM; /* separate sign sub-packets are not part of this decoder */
+                bpos += slen;
+                if (left < 0 || bpos > lead + total) { err = JXS_E_DEC_BITSTREAM; break; }
+                P.present = 1;
+                if (!raw) {
+                    P.nwords = (P.gbits + 31) >> 5;
+                    tw += P.nwords;
+                }
+            }
+            s_tw = tw;
+            s_npk = cfg->npk;
+        }
+        err = __reduce_or_sync(FULL, (uint32_t)err) ? JXS_E_DEC_BITSTREAM : 0;
+        __syncwarp();
+        /* line positions: significance flags, or raw GCLIs for raw packets */
+        if (!err && lane < (int)cfg->npk && pk[lane].present) {
+            const UkPk& P = pk[lane];
+            const uint32_t b0 = cfg->pk_bl0[last][lane], nb = cfg->pk_nbl[last][lane];
+            uint32_t run = P.spos;
+            for (uint32_t x = b0; x < b0 + nb; x++) {
+                ln[x].raw = (uint8_t)P.raw;
+                ln[x].sig_pos = run;
+                run += P.raw ? 4 * bls[x].gcli_w : (ln[x].meth ? bls[x].sig_w : 0u);
+            }
+        }
+        if (lane == 0) s_err = err;
     }
     __syncthreads();
     if (s_err) {
@@ -325,7 +362,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     }
 
     /* pass 1: codewords per segment; raw GCLIs and insignificant groups */
-    for (uint32_t sidx = warp; sidx < nseg; sidx += UK_WARPS) {
+    for (uint32_t sidx = next_seg(&s_next[0], lane); sidx < nseg; sidx = next_seg(&s_next[0], lane)) {
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
         const UkLine L = ln[sg.bl];
@@ -391,7 +428,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
             if (valid < 32) z &= ~(0xffffffffu >> valid);
             while (z) {
                 const uint32_t lz = __clz(z);
-                if (z0 < zcap) zend[z0] = pk[k].gpos + 32 * i + lz;
+                if (z0 < zcap) zend[z0] = (uint16_t)(32 * i + lz);
                 z0++;
                 z &= ~(0x80000000u >> lz);
             }
@@ -429,7 +466,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
 
     /* pass 2: GCLIs from codeword ends; data bits per segment */
     int bad = 0;
-    for (uint32_t sidx = warp; sidx < nseg; sidx += UK_WARPS) {
+    for (uint32_t sidx = next_seg(&s_next[1], lane); sidx < nseg; sidx = next_seg(&s_next[1], lane)) {
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
         const UkLine L = ln[sg.bl];
@@ -449,7 +486,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
             if (coded) {
                 const uint32_t c = cw + __popc(bal & ((1u << lane) - 1));
                 const uint32_t zr = P.zbase + c;
-                const uint32_t start = c ? zend[zr - 1] + 1 : P.gpos;
+                const uint32_t start = c ? zend[zr - 1] + 1u : 0u;
                 const uint32_t ones = zend[zr] - start;
                 v = L.t + ones;
                 if (v > 15) {
@@ -491,7 +528,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
 
     /* pass 3: data */
     const uint32_t uniform = cfg->qpih;
-    for (uint32_t sidx = warp; sidx < nseg; sidx += UK_WARPS) {
+    for (uint32_t sidx = next_seg(&s_next[2], lane); sidx < nseg; sidx = next_seg(&s_next[2], lane)) {
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
         const UkLine L = ln[sg.bl];
@@ -613,7 +650,7 @@ extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, 
 extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
                                          int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status,
                                          cudaStream_t st) {
-    const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 4ull * UK_ZCAP(cap_groups);
+    const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 2ull * UK_ZCAP(cap_groups);
     cudaError_t e = cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     unpack_kernel<<<np, UK_THREADS, smem, st>>>(dcfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status);

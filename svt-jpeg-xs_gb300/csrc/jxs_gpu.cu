@@ -604,9 +604,9 @@ extern "C" jxs_gpu_dec_t* jxs_gpu_dec_create(const jxs_cfg_t* cfg, int nslots, i
     /* the on-chip copy of a precinct: constant-bit-rate streams give every
      * slice its share of Lcod, so a precinct fits in a slice's share with
      * margin; whatever does not fit is reported as an invalid stream */
-    const size_t fixed = (size_t)d->cap_groups * 6 + 4 * (8 * JXS_MAXPK + 32) + 64;
+    const size_t fixed = (size_t)d->cap_groups * 3 + 2 * (8 * JXS_MAXPK + 32) + 64;
     uint64_t cap = (uint64_t)cfg->lcod / (cfg->nslices ? cfg->nslices : 1);
-    cap = cap + cap / 4 + 4096;
+    cap = (cfg->max_slice_budget ? cfg->max_slice_budget : cap + cap / 4) + 4096;
     if (cap > cfg->lcod + 64ull) cap = cfg->lcod + 64ull;
     const size_t room = kSmemMax - 8 * 1024; /* static shared memory of the unpacking kernel */
     if (cap + fixed > room) cap = room > fixed + 4096 ? room - fixed : 4096;
