@@ -48,13 +48,19 @@ DEV uint32_t bits32_at(const uint8_t* b, uint32_t pos) {
     return __funnelshift_l(be_word(b, wi + 1), be_word(b, wi), pos & 31);
 }
 
-/* every 4th bit (positions 0, 4, ..., 28) gathered into bits 0..7 */
-DEV uint32_t compact4(uint32_t x) {
-    x &= 0x11111111u;
-    x = (x | (x >> 3)) & 0x03030303u;
-    x = (x | (x >> 6)) & 0x000f000fu;
-    x = (x | (x >> 12)) & 0x000000ffu;
-    return x;
+/* Transpose of the 8 x 4 bit matrix in a word: bit 4k + j moves to bit
+ * 8j + k (k: nibble = bit-plane, j: bit in the nibble), so that byte 3 - c
+ * collects the 8 plane bits of coefficient c.  Four swaps of index bits
+ * ((4,1), (3,0), (2,1), (1,0)) as masked delta swaps. */
+DEV uint32_t dswap(uint32_t x, int d, uint32_t m) {
+    const uint32_t t = ((x >> d) ^ x) & m;
+    return x ^ t ^ (t << d);
+}
+DEV uint32_t planes_to_coefs(uint32_t x) {
+    x = dswap(x, 14, 0x0000ccccu);
+    x = dswap(x, 7, 0x00aa00aau);
+    x = dswap(x, 2, 0x0c0c0c0cu);
+    return dswap(x, 1, 0x22222222u);
 }
 
 DEV uint32_t warp_excl_scan(uint32_t x, uint32_t* total) {
@@ -112,18 +118,19 @@ DEV uint32_t next_seg(uint32_t* ctr, int lane) {
 DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uint32_t uniform, int wl) {
     const uint32_t sgn = (uint32_t)(chunk >> (4 * np)) & 15u;
     const uint64_t planes = chunk & ((1ull << (4 * np)) - 1);
-    const uint32_t lo = (uint32_t)planes, hi = (uint32_t)(planes >> 32);
-    uint32_t m[4];
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-        m[c] = compact4(lo >> (3 - c));
-        if (np > 8) m[c] |= compact4(hi >> (3 - c)) << 8;
+    /* the plane bits of coefficients 0, 1 / 2, 3 as 16-bit pairs */
+    const uint32_t tl = planes_to_coefs((uint32_t)planes);
+    uint32_t P01 = __byte_perm(tl, 0u, 0x4243), P23 = __byte_perm(tl, 0u, 0x4041);
+    if (np > 8) {
+        const uint32_t th = planes_to_coefs((uint32_t)(planes >> 32));
+        P01 |= __byte_perm(th, 0u, 0x4243) << 8;
+        P23 |= __byte_perm(th, 0u, 0x4041) << 8;
     }
     /* keep[] zeroes coefficients past the band width */
     const uint32_t keepA = (wl > 1 ? 0xffff0000u : 0u) | 0xffffu, keepB = (wl > 2 ? 0xffffu : 0u) | (wl > 3 ? 0xffff0000u : 0u);
     if (!uniform || t == 0) {
         /* two coefficients per word: m << t stays below 2^15 */
-        uint32_t A = (m[0] | (m[1] << 16)) << t, B = (m[2] | (m[3] << 16)) << t;
+        uint32_t A = P01 << t, B = P23 << t;
         if (t > 0) {
             const uint32_t half = (1u << (t - 1)) * 0x00010001u;
             A |= __vcmpne2(A, 0u) & half;
@@ -135,6 +142,7 @@ DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uin
         B = (B & ~nB) | (__vsub2(0u, B) & nB);
         return make_uint2(A & keepA, B & keepB);
     }
+    const uint32_t m[4] = {P01 & 0xffffu, P01 >> 16, P23 & 0xffffu, P23 >> 16};
     uint32_t o[4];
 #pragma unroll
     for (int c = 0; c < 4; c++) {
@@ -185,7 +193,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     __shared__ UkPk pk[JXS_MAXPK];
     __shared__ uint8_t s_mode[JXS_MAXBL];
     __shared__ uint32_t s_pksb[JXS_MAXPK], s_pkrb[JXS_MAXPK];
-    __shared__ uint32_t s_next[3]; /* segment queues of the three warp passes */
+    __shared__ uint32_t s_next[2]; /* segment queues of the two warp passes */
     __shared__ uint32_t s_cnt[JXS_MAXSEG], s_base[JXS_MAXSEG];
     __shared__ uint32_t ws[UK_WARPS];
     __shared__ int s_err;
@@ -195,7 +203,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     const int last = (p + 1 >= (int)cfg->np);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) s_err = *(volatile int*)status;
-    if (threadIdx.x < 3) s_next[threadIdx.x] = 0;
+    if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
     __syncthreads();
     if (s_err) return; /* the precinct offsets could not be found */
     const uint32_t off = prec_off[p];
@@ -353,6 +361,45 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
                 run += P.raw ? 4 * bls[x].gcli_w : (ln[x].meth ? bls[x].sig_w : 0u);
             }
         }
+        __syncwarp();
+        /* codewords of every segment: its groups minus those in
+         * insignificant significance groups (flags: 1 = insignificant) */
+        if (!err) {
+            for (uint32_t sidx = lane; sidx < nseg; sidx += 32) {
+                const jxs_seg_t sg = segs[sidx];
+                const jxs_bline_t& B = bls[sg.bl];
+                const UkLine& L = ln[sg.bl];
+                const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+                uint32_t cnt = 0;
+                if (!L.raw) {
+                    cnt = gend - sg.g0;
+                    if (L.meth) {
+                        for (uint32_t s0 = sg.g0 >> 3; s0 < ((gend + 7) >> 3); s0 += 32) {
+                            const uint32_t ns = min(32u, ((gend + 7) >> 3) - s0);
+                            const uint32_t fl = bits32_at(pbuf, L.sig_pos + s0) >> (32 - ns);
+                            cnt -= 8 * __popc(fl);
+                            /* a flagged partial last group counts its own size */
+                            if ((fl & 1u) && 8 * (s0 + ns) > B.gcli_w) cnt += 8 * (s0 + ns) - B.gcli_w;
+                        }
+                    }
+                }
+                s_cnt[sidx] = cnt;
+            }
+            __syncwarp();
+            /* codeword base of every segment inside its packet: one lane per packet */
+            if (lane < (int)cfg->npk) {
+                const uint32_t b0 = cfg->pk_bl0[last][lane], nb = cfg->pk_nbl[last][lane];
+                uint32_t run = 0;
+                for (uint32_t x = b0; x < b0 + nb; x++) {
+                    if (ln[x].raw) continue;
+                    for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
+                        s_base[i] = run;
+                        run += s_cnt[i];
+                    }
+                }
+                pk[lane].ncoded = run;
+            }
+        }
         if (lane == 0) s_err = err;
     }
     __syncthreads();
@@ -361,44 +408,6 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
         return;
     }
 
-    /* pass 1: codewords per segment; raw GCLIs and insignificant groups */
-    for (uint32_t sidx = next_seg(&s_next[0], lane); sidx < nseg; sidx = next_seg(&s_next[0], lane)) {
-        const jxs_seg_t sg = segs[sidx];
-        const jxs_bline_t B = bls[sg.bl];
-        const UkLine L = ln[sg.bl];
-        const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
-        uint32_t cnt = 0;
-        for (uint32_t base = sg.g0; base < gend; base += 32) {
-            const uint32_t g = base + lane;
-            if (g < gend) {
-                if (L.raw) {
-                    const uint32_t pos = L.sig_pos + 4 * g;
-                    gcl[B.gbase + g] = (uint8_t)((pbuf[pos >> 3] >> (4 - (pos & 7))) & 15);
-                } else {
-                    const uint32_t sp = L.sig_pos + (g >> 3);
-                    const bool insig = L.meth && ((pbuf[sp >> 3] >> (7 - (sp & 7))) & 1);
-                    if (insig) gcl[B.gbase + g] = L.t;
-                    cnt += !insig;
-                }
-            }
-        }
-        cnt = __reduce_add_sync(FULL, cnt);
-        if (lane == 0) s_cnt[sidx] = cnt;
-    }
-    __syncthreads();
-    /* codeword base of every segment inside its packet: one lane per packet */
-    if (warp == 0 && lane < (int)cfg->npk) {
-        const uint32_t b0 = cfg->pk_bl0[last][lane], nb = cfg->pk_nbl[last][lane];
-        uint32_t run = 0;
-        for (uint32_t x = b0; x < b0 + nb; x++) {
-            if (ln[x].raw) continue;
-            for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
-                s_base[i] = run;
-                run += s_cnt[i];
-            }
-        }
-        pk[lane].ncoded = run;
-    }
     /* zero bits of the VLC sub-packets: count, scan, record positions */
     const uint32_t tw = s_tw, npk = s_npk;
     const uint32_t per = (tw + blockDim.x - 1) / blockDim.x;
@@ -466,7 +475,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
 
     /* pass 2: GCLIs from codeword ends; data bits per segment */
     int bad = 0;
-    for (uint32_t sidx = next_seg(&s_next[1], lane); sidx < nseg; sidx = next_seg(&s_next[1], lane)) {
+    for (uint32_t sidx = next_seg(&s_next[0], lane); sidx < nseg; sidx = next_seg(&s_next[0], lane)) {
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
         const UkLine L = ln[sg.bl];
@@ -478,9 +487,15 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
             const bool valid = g < gend;
             uint32_t v = 0;
             bool coded = false;
-            if (valid && !L.raw) {
-                const uint32_t sp = L.sig_pos + (g >> 3);
-                coded = !(L.meth && ((pbuf[sp >> 3] >> (7 - (sp & 7))) & 1));
+            if (valid) {
+                if (L.raw) {
+                    const uint32_t pos = L.sig_pos + 4 * g;
+                    v = (pbuf[pos >> 3] >> (4 - (pos & 7))) & 15u;
+                } else {
+                    const uint32_t sp = L.sig_pos + (g >> 3);
+                    coded = !(L.meth && ((pbuf[sp >> 3] >> (7 - (sp & 7))) & 1));
+                    if (!coded) v = L.t;
+                }
             }
             const uint32_t bal = __ballot_sync(FULL, coded);
             if (coded) {
@@ -493,10 +508,8 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
                     bad = 1;
                     v = 15;
                 }
-                gcl[B.gbase + g] = (uint8_t)v;
-            } else if (valid) {
-                v = gcl[B.gbase + g];
             }
+            if (valid) gcl[B.gbase + g] = (uint8_t)v;
             cw += __popc(bal);
             if (valid && v > L.t) dsum += 4 * (v - L.t + 1);
         }
@@ -528,7 +541,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
 
     /* pass 3: data */
     const uint32_t uniform = cfg->qpih;
-    for (uint32_t sidx = next_seg(&s_next[2], lane); sidx < nseg; sidx = next_seg(&s_next[2], lane)) {
+    for (uint32_t sidx = next_seg(&s_next[1], lane); sidx < nseg; sidx = next_seg(&s_next[1], lane)) {
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
         const UkLine L = ln[sg.bl];

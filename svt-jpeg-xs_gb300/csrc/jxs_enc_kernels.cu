@@ -409,13 +409,28 @@ DEV uint32_t warp_excl_scan(uint32_t x, uint32_t* total) {
     return inc - x;
 }
 
+/* Inverse of the 8 x 4 bit-matrix transpose: byte 3 - c holds the 8 plane
+ * bits of coefficient c; bit k of it moves to bit 4k + 3 - c (nibble k =
+ * plane k, coefficient 0 in its most significant bit).  Masked delta swaps
+ * of index bits (1,0), (2,1), (3,0), (4,1). */
+DEV uint32_t dswap(uint32_t x, int d, uint32_t m) {
+    const uint32_t t = ((x >> d) ^ x) & m;
+    return x ^ t ^ (t << d);
+}
+DEV uint32_t coefs_to_planes(uint32_t x) {
+    x = dswap(x, 1, 0x22222222u);
+    x = dswap(x, 2, 0x0c0c0c0cu);
+    x = dswap(x, 7, 0x00aa00aau);
+    return dswap(x, 14, 0x0000ccccu);
+}
+
 /* Data bits of one 4-coefficient group with GCLI v > gtli t
  * (pack_data_c, PackPrecinct.c:128-198): the sign nibble (coefficient 0 in
  * the most significant bit) followed by bit-planes v-1 .. t, each a nibble.
  * Quantization (Quant.c:9-45) is skipped for t == 0 like the reference
  * (QuantStageProcess.c:18-31); a sign is sent only for a non-zero
- * quantized magnitude.  lut[b] spreads the 8 bits of b to every 4th bit. */
-DEV uint64_t data_chunk(uint2 raw4, int wleft, uint32_t v, uint32_t t, uint32_t uniform, const uint32_t* lut) {
+ * quantized magnitude. */
+DEV uint64_t data_chunk(uint2 raw4, int wleft, uint32_t v, uint32_t t, uint32_t uniform) {
     const uint32_t c[4] = {raw4.x & 0xffffu, raw4.x >> 16, raw4.y & 0xffffu, raw4.y >> 16};
     uint32_t P[4], signs = 0;
 #pragma unroll
@@ -436,9 +451,9 @@ DEV uint64_t data_chunk(uint2 raw4, int wleft, uint32_t v, uint32_t t, uint32_t 
         signs = (signs << 1) | (q ? (cc >> 15) : 0u);
     }
     const uint32_t np = v - t;
-    uint64_t planes = (lut[P[0] & 255] << 3) | (lut[P[1] & 255] << 2) | (lut[P[2] & 255] << 1) | lut[P[3] & 255];
+    uint64_t planes = coefs_to_planes(((P[0] & 255u) << 24) | ((P[1] & 255u) << 16) | ((P[2] & 255u) << 8) | (P[3] & 255u));
     if (np > 8)
-        planes |= (uint64_t)((lut[P[0] >> 8] << 3) | (lut[P[1] >> 8] << 2) | (lut[P[2] >> 8] << 1) | lut[P[3] >> 8]) << 32;
+        planes |= (uint64_t)coefs_to_planes(((P[0] >> 8) << 24) | ((P[1] >> 8) << 16) | ((P[2] >> 8) << 8) | (P[3] >> 8)) << 32;
     return ((uint64_t)signs << (4 * np)) | planes;
 }
 
@@ -473,7 +488,6 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     __shared__ PkLine pl[JXS_MAXBLINES];
     __shared__ uint8_t tb[JXS_MAXBL], s_meth[JXS_MAXBL];
     __shared__ uint32_t s_cn[JXS_MAXBL], s_cs[JXS_MAXBL];
-    __shared__ uint32_t lut[256];
     __shared__ int s_ok;
 
     const int p = blockIdx.x;
@@ -495,11 +509,6 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
         return;
     }
     for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) buf[i] = 0;
-    for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) {
-        uint32_t x = 0;
-        for (int k = 0; k < 8; k++) x |= ((i >> k) & 1u) << (4 * k);
-        lut[i] = x;
-    }
     for (uint32_t fb = threadIdx.x; fb < cfg->nbands; fb += blockDim.x) {
         tb[fb] = jxs_truncation(cfg->band[fb].gain, cfg->band[fb].prio, R.q, R.r);
         s_cn[fb] = 0;
@@ -736,7 +745,7 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
             if (vlen) put_bits(buf, vpos + (ex & 0xffffu), ((1u << (vlen - 1)) - 1u) << 1, vlen);
             if (dlen) {
                 const uint2 raw4 = *(const uint2*)(crow + 4 * g);
-                put_bits64(buf, dpos + (ex >> 16), data_chunk(raw4, (int)B.w - 4 * (int)g, v, t, uniform, lut), dlen);
+                put_bits64(buf, dpos + (ex >> 16), data_chunk(raw4, (int)B.w - 4 * (int)g, v, t, uniform), dlen);
             }
             vpos += tot & 0xffffu;
             dpos += tot >> 16;
