@@ -367,34 +367,21 @@ __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restr
 #define PK_THREADS 512
 #define PK_WARPS (PK_THREADS / 32)
 
-/* OR `n` (<= 32) bits of `v` at bit position `pos` of a big-endian bit
- * string stored in native byte order.  Writes beyond the precinct's words
- * are dropped and flagged (they mean the sizes disagree with the rate
- * control). */
-__shared__ uint32_t pk_nwords;
-__shared__ int pk_overflow;
-DEV void put_bits(uint32_t* buf, uint32_t pos, uint32_t v, uint32_t n) {
-    if (!n) return;
-    const uint32_t w = pos >> 5, sh = pos & 31;
-    if (w + (sh + n > 32 ? 1 : 0) >= pk_nwords) {
-        pk_overflow = 1;
+/* OR the low `n` bits (1..64) of `v` into a big-endian bit string stored in
+ * native byte order (byte i of the string is byte i of the buffer), at bit
+ * `pos`.  Bits past the buffer's `nw` words are not written and set `ovf`
+ * (the sizes would disagree with the rate control). */
+DEV void put_bits(uint32_t* buf, uint32_t nw, uint32_t pos, uint64_t v, uint32_t n, int& ovf) {
+    if (((pos + n - 1) >> 5) >= nw) {
+        ovf = 1;
         return;
     }
-    if (sh + n <= 32) {
-        atomicOr(&buf[w], __byte_perm(v << (32 - sh - n), 0, 0x0123));
-    } else {
-        const uint32_t n1 = 32 - sh, n2 = n - n1;
-        atomicOr(&buf[w], __byte_perm(v >> n2, 0, 0x0123));
-        atomicOr(&buf[w + 1], __byte_perm(v << (32 - n2), 0, 0x0123));
-    }
-}
-DEV void put_bits64(uint32_t* buf, uint32_t pos, uint64_t v, uint32_t n) {
-    if (n > 32) {
-        put_bits(buf, pos, (uint32_t)(v >> 32), n - 32);
-        put_bits(buf, pos + n - 32, (uint32_t)v, 32);
-    } else {
-        put_bits(buf, pos, (uint32_t)v, n);
-    }
+    const uint64_t a = v << (64 - n); /* left-aligned */
+    const uint32_t hi = (uint32_t)(a >> 32), lo = (uint32_t)a;
+    const uint32_t w = pos >> 5, sh = pos & 31;
+    atomicOr(&buf[w], __byte_perm(hi >> sh, 0, 0x0123));
+    if (sh + n > 32) atomicOr(&buf[w + 1], __byte_perm(__funnelshift_r(lo, hi, sh), 0, 0x0123));
+    if (sh + n > 64) atomicOr(&buf[w + 2], __byte_perm(lo << (32 - sh), 0, 0x0123));
 }
 
 DEV uint32_t warp_excl_scan(uint32_t x, uint32_t* total) {
@@ -508,6 +495,7 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
         }
         return;
     }
+    int ovf = 0;
     for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) buf[i] = 0;
     for (uint32_t fb = threadIdx.x; fb < cfg->nbands; fb += blockDim.x) {
         tb[fb] = jxs_truncation(cfg->band[fb].gain, cfg->band[fb].prio, R.q, R.r);
@@ -515,8 +503,6 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
         s_cs[fb] = 0;
     }
     if (threadIdx.x == 0) {
-        pk_nwords = words;
-        pk_overflow = 0;
     }
     __syncthreads();
 
@@ -682,7 +668,7 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
             if (ex) {
                 const jxs_band_t& bd = cfg->band[fb];
                 const uint32_t lines = last ? bd.last_lines : bd.lines;
-                if (lines > 0 && s_meth[fb]) put_bits(buf, lead * 8 + 40 + 2 * (idx0 + __popc(bal & ((1u << lane) - 1))), 2u, 2);
+                if (lines > 0 && s_meth[fb]) put_bits(buf, words, lead * 8 + 40 + 2 * (idx0 + __popc(bal & ((1u << lane) - 1))), 2u, 2, ovf);
             }
             idx0 += __popc(bal);
         }
@@ -724,7 +710,7 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
             mx = max(mx, __shfl_xor_sync(FULL, mx, 4));
             uint32_t vlen = 0;
             if (L.raw) {
-                if (valid) put_bits(buf, L.gcli_pos + 4 * g, v, 4);
+                if (valid) put_bits(buf, words, L.gcli_pos + 4 * g, v, 4, ovf);
             } else {
                 const bool insig = mx <= t;
                 if (L.meth) {
@@ -733,7 +719,7 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
                     if (lane == 0) {
                         const uint32_t nsg = min(4u, (gend - base + 7) >> 3);
                         const uint32_t bits = ((bal & 1u) << 3) | (((bal >> 8) & 1u) << 2) | (((bal >> 16) & 1u) << 1) | ((bal >> 24) & 1u);
-                        if (bits >> (4 - nsg)) put_bits(buf, L.sig_pos + (base >> 3), bits >> (4 - nsg), nsg);
+                        if (bits >> (4 - nsg)) put_bits(buf, words, L.sig_pos + (base >> 3), bits >> (4 - nsg), nsg, ovf);
                     }
                 }
                 if (valid && !(L.meth && insig)) vlen = v > t ? v - t + 1 : 1u;
@@ -742,19 +728,18 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
             uint32_t tot;
             const uint32_t ex = warp_excl_scan((dlen << 16) | vlen, &tot);
             /* unary code: (v - t) ones then a zero (PackPrecinct.h:25-39) */
-            if (vlen) put_bits(buf, vpos + (ex & 0xffffu), ((1u << (vlen - 1)) - 1u) << 1, vlen);
+            if (vlen) put_bits(buf, words, vpos + (ex & 0xffffu), ((1u << (vlen - 1)) - 1u) << 1, vlen, ovf);
             if (dlen) {
                 const uint2 raw4 = *(const uint2*)(crow + 4 * g);
-                put_bits64(buf, dpos + (ex >> 16), data_chunk(raw4, (int)B.w - 4 * (int)g, v, t, uniform), dlen);
+                put_bits(buf, words, dpos + (ex >> 16), data_chunk(raw4, (int)B.w - 4 * (int)g, v, t, uniform), dlen, ovf);
             }
             vpos += tot & 0xffffu;
             dpos += tot >> 16;
         }
     }
-    __syncthreads();
-    if (pk_overflow) {
+    if (__syncthreads_or(ovf)) {
         if (threadIdx.x == 0) {
-            printf("jxs pack: precinct %d wrote past its %u words\n", p, pk_nwords);
+            printf("jxs pack: precinct %d wrote past its %u words\n", p, words);
             JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
         }
         return;
