@@ -418,29 +418,38 @@ DEV uint32_t coefs_to_planes(uint32_t x) {
  * (QuantStageProcess.c:18-31); a sign is sent only for a non-zero
  * quantized magnitude. */
 DEV uint64_t data_chunk(uint2 raw4, int wleft, uint32_t v, uint32_t t, uint32_t uniform) {
-    const uint32_t c[4] = {raw4.x & 0xffffu, raw4.x >> 16, raw4.y & 0xffffu, raw4.y >> 16};
-    uint32_t P[4], signs = 0;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const uint32_t cc = k < wleft ? c[k] : 0u;
-        const uint32_t m = cc & 0x7fffu;
-        uint32_t q;
-        if (t == 0) {
-            q = m;
-        } else if (uniform) {
-            /* computed in int like the reference, truncated to 16 bits */
-            q = (((m << (v - t + 1)) - m + (1u << v)) >> (v + 1)) & 0xffffu;
-            q = ((q << t) & 0xffffu) >> t;
-        } else {
-            q = m >> t;
-        }
-        P[k] = q;
-        signs = (signs << 1) | (q ? (cc >> 15) : 0u);
-    }
     const uint32_t np = v - t;
-    uint64_t planes = coefs_to_planes(((P[0] & 255u) << 24) | ((P[1] & 255u) << 16) | ((P[2] & 255u) << 8) | (P[3] & 255u));
-    if (np > 8)
-        planes |= (uint64_t)coefs_to_planes(((P[0] >> 8) << 24) | ((P[1] >> 8) << 16) | ((P[2] >> 8) << 8) | (P[3] >> 8)) << 32;
+    /* coefficients past the band width are zero */
+    uint32_t c01 = raw4.x & ((wleft > 1 ? 0xffff0000u : 0u) | 0xffffu);
+    uint32_t c23 = raw4.y & ((wleft > 2 ? 0xffffu : 0u) | (wleft > 3 ? 0xffff0000u : 0u));
+    uint32_t P01, P23;
+    if (t == 0) {
+        P01 = c01 & 0x7fff7fffu;
+        P23 = c23 & 0x7fff7fffu;
+    } else if (!uniform) {
+        /* deadzone: magnitude >> t, two coefficients per word */
+        const uint32_t keep = (0x7fffu >> t) * 0x00010001u;
+        P01 = ((c01 & 0x7fff7fffu) >> t) & keep;
+        P23 = ((c23 & 0x7fff7fffu) >> t) & keep;
+    } else {
+        uint32_t q[4];
+        const uint32_t c[4] = {c01 & 0xffffu, c01 >> 16, c23 & 0xffffu, c23 >> 16};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint32_t m = c[k] & 0x7fffu;
+            /* computed in int like the reference, truncated to 16 bits */
+            const uint32_t u = (((m << (v - t + 1)) - m + (1u << v)) >> (v + 1)) & 0xffffu;
+            q[k] = ((u << t) & 0xffffu) >> t;
+        }
+        P01 = q[0] | (q[1] << 16);
+        P23 = q[2] | (q[3] << 16);
+    }
+    /* signs of the non-zero quantized values, coefficient 0 first */
+    const uint32_t s01 = __vcmpne2(P01, 0u) & c01 & 0x80008000u, s23 = __vcmpne2(P23, 0u) & c23 & 0x80008000u;
+    const uint32_t signs = ((s01 >> 12) & 8u) | ((s01 >> 29) & 4u) | ((s23 >> 14) & 2u) | (s23 >> 31);
+    /* byte 3 - c of the word = low 8 plane bits of coefficient c */
+    uint64_t planes = coefs_to_planes(__byte_perm(P01, P23, 0x0246));
+    if (np > 8) planes |= (uint64_t)coefs_to_planes(__byte_perm(P01, P23, 0x1357)) << 32;
     return ((uint64_t)signs << (4 * np)) | planes;
 }
 
