@@ -476,7 +476,7 @@ struct PkLine {
  *   pass B  each lane one group: significance flags, the unary GCLI code and
  *           the data bits, at positions from a warp prefix sum, OR-ed into
  *           the buffer. */
-__global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
+__global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
                                                           const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
                                                           uint8_t* __restrict__ out, uint32_t cap_words, int* status) {
     extern __shared__ __align__(16) uint32_t buf[];
@@ -484,6 +484,10 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     __shared__ PkLine pl[JXS_MAXBLINES];
     __shared__ uint8_t tb[JXS_MAXBL], s_meth[JXS_MAXBL];
     __shared__ uint32_t s_cn[JXS_MAXBL], s_cs[JXS_MAXBL];
+    __shared__ uint32_t s_lg[JXS_MAXBLINES], s_ls[JXS_MAXBLINES];       /* per line: GCLI / significance bits */
+    __shared__ uint32_t s_pks[JXS_MAXPK], s_pkg[JXS_MAXPK], s_pkd[JXS_MAXPK]; /* per packet: sub-packet starts */
+    __shared__ uint8_t s_pkr[JXS_MAXPK];
+    __shared__ uint32_t s_vst[JXS_MAXSEG], s_dst[JXS_MAXSEG];        /* per segment: GCLI / data bit starts */
     __shared__ int s_ok;
 
     const int p = blockIdx.x;
@@ -520,7 +524,8 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     const jxs_seg_t* segs = cfg->seg[last];
     const jxs_bline_t* bls = cfg->bline[last];
 
-    /* pass A */
+    /* pass A: each lane 4 consecutive groups (one 4-byte GCLI load), a warp
+     * 128 groups per step */
     for (uint32_t sidx = warp; sidx < nseg; sidx += PK_WARPS) {
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
@@ -529,18 +534,22 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
         const uint8_t* grow = gcli + bd.gcli_off + (uint64_t)(p * bd.lines + B.line) * bd.gpitch;
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
         uint32_t dsum = 0, vsum = 0, zsum = 0;
-        for (uint32_t base = sg.g0; base < gend; base += 32) {
-            const uint32_t g = base + lane;
-            const bool valid = g < gend;
-            const uint32_t v = valid ? grow[g] : 0u;
-            uint32_t mx = v;
-            mx = max(mx, __shfl_xor_sync(FULL, mx, 1));
-            mx = max(mx, __shfl_xor_sync(FULL, mx, 2));
-            mx = max(mx, __shfl_xor_sync(FULL, mx, 4));
-            if (valid) {
-                dsum += v > t ? 4 * (v - t + 1) : 0u;
-                vsum += v > t ? v - t + 1 : 1u;
-                zsum += mx <= t;
+        for (uint32_t base = sg.g0; base < gend; base += 128) {
+            const uint32_t g = base + 4 * lane;
+            const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
+            const uint32_t w4 = nv ? *(const uint32_t*)(grow + g) : 0u;
+            uint32_t m = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) m = max(m, k < (int)nv ? (w4 >> (8 * k)) & 255u : 0u);
+            const uint32_t mx = max(m, __shfl_xor_sync(FULL, m, 1)); /* significance group: 2 lanes */
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                if (k < (int)nv) {
+                    const uint32_t v = (w4 >> (8 * k)) & 255u;
+                    dsum += v > t ? 4 * (v - t + 1) : 0u;
+                    vsum += v > t ? v - t + 1 : 1u;
+                    zsum += mx <= t;
+                }
             }
         }
         dsum = __reduce_add_sync(FULL, dsum);
@@ -554,7 +563,7 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     }
     __syncthreads();
 
-    /* layout, by warp 0 with lanes over band lines, bands and packets */
+    /* layout, by warp 0: lanes over band lines, bands, packets, segments */
     if (warp == 0) {
         const uint32_t nbl = cfg->nbline[last];
         for (uint32_t b = lane; b < nbl; b += 32) {
@@ -576,16 +585,22 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
          * (RateControl.c:528-575) */
         for (uint32_t fb = lane; fb < cfg->nbands; fb += 32) s_meth[fb] = (uint8_t)(cfg->sig && s_cn[fb] > s_cs[fb]);
         __syncwarp();
+        /* per line: GCLI and significance bits with the band's method */
+        for (uint32_t b = lane; b < nbl; b += 32) {
+            const uint8_t m = s_meth[bls[b].fb];
+            pl[b].meth = m;
+            s_lg[b] = m ? pl[b].vlc - pl[b].zero : pl[b].vlc;
+            s_ls[b] = m ? bls[b].sig_w : 0u;
+        }
+        __syncwarp();
         /* one lane per packet: sub-packet sizes, raw fallback, header */
         const uint32_t k = lane;
         const uint32_t nb = k < cfg->npk ? cfg->pk_nbl[last][k] : 0u, b0 = k < cfg->npk ? cfg->pk_bl0[last][k] : 0u;
         uint32_t db = 0, gbits = 0, sbits = 0;
         for (uint32_t x = b0; x < b0 + nb; x++) {
-            const uint8_t m = s_meth[bls[x].fb];
-            pl[x].meth = m;
             db += pl[x].data;
-            gbits += m ? pl[x].vlc - pl[x].zero : pl[x].vlc;
-            sbits += m ? bls[x].sig_w : 0u;
+            gbits += s_lg[x];
+            sbits += s_ls[x];
         }
         const uint32_t dB = (db + 7) >> 3, gB = (gbits + 7) >> 3, sB = (sbits + 7) >> 3;
         const uint32_t rawB = nb ? cfg->raw_bytes[last][k] : 0u;
@@ -615,46 +630,41 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
                 h[5] = (uint8_t)((gcl_bytes & 1) << 7);
                 h[6] = 0;
             }
-            uint32_t pos = (start + hb) * 8;
-            if (raw) {
-                uint32_t gp = pos;
-                for (uint32_t x = b0; x < b0 + nb; x++) {
-                    pl[x].raw = 1;
-                    pl[x].gcli_pos = gp;
-                    gp += 4 * bls[x].gcli_w;
-                }
-                pos += rawB * 8;
-            } else {
-                uint32_t sp = pos;
-                for (uint32_t x = b0; x < b0 + nb; x++) {
-                    pl[x].raw = 0;
-                    pl[x].sig_pos = sp;
-                    if (pl[x].meth) sp += bls[x].sig_w;
-                }
-                pos += sB * 8;
-                uint32_t gp = pos;
-                for (uint32_t x = b0; x < b0 + nb; x++) {
-                    pl[x].gcli_pos = gp;
-                    gp += pl[x].meth ? pl[x].vlc - pl[x].zero : pl[x].vlc;
-                }
-                pos += gB * 8;
+            /* sub-packet starts: significance, GCLIs, data */
+            const uint32_t p0 = (start + hb) * 8;
+            s_pks[k] = p0;
+            s_pkg[k] = raw ? p0 : p0 + sB * 8;
+            s_pkd[k] = p0 + (raw ? rawB : sB + gB) * 8;
+            s_pkr[k] = (uint8_t)raw;
+        }
+        __syncwarp();
+        /* per line: positions inside its packet's sub-packets */
+        for (uint32_t x = lane; x < nbl; x += 32) {
+            const uint32_t kk = bls[x].pk, xb0 = cfg->pk_bl0[last][kk];
+            uint32_t sp = 0, gp = 0, dp = 0;
+            const int r = s_pkr[kk];
+            for (uint32_t y = xb0; y < x; y++) {
+                sp += s_ls[y];
+                gp += r ? 4 * bls[y].gcli_w : s_lg[y];
+                dp += pl[y].data;
             }
-            /* data sub-packet; each segment's start in its band line's GCLI
-             * and data bits */
-            uint32_t dp = pos;
-            for (uint32_t x = b0; x < b0 + nb; x++) {
-                pl[x].data_pos = dp;
-                const jxs_bline_t& B = bls[x];
-                uint32_t vp = pl[x].gcli_pos, sdp = dp;
-                for (uint32_t i = B.seg0; i < B.seg0 + B.nseg; i++) {
-                    const uint32_t vb = pl[x].meth ? s_vlc[i] - s_zero[i] : s_vlc[i], d = s_data[i];
-                    s_vlc[i] = vp;
-                    s_data[i] = sdp;
-                    vp += vb;
-                    sdp += d;
-                }
-                dp += pl[x].data;
+            pl[x].raw = (uint8_t)r;
+            pl[x].sig_pos = s_pks[kk] + sp;
+            pl[x].gcli_pos = s_pkg[kk] + gp;
+            pl[x].data_pos = s_pkd[kk] + dp;
+        }
+        __syncwarp();
+        /* per segment: its start in its line's GCLI and data bits */
+        for (uint32_t i = lane; i < nseg; i += 32) {
+            const uint32_t x = segs[i].bl;
+            const uint8_t m = pl[x].meth;
+            uint32_t vp = pl[x].gcli_pos, dp = pl[x].data_pos;
+            for (uint32_t j = bls[x].seg0; j < i; j++) {
+                vp += m ? s_vlc[j] - s_zero[j] : s_vlc[j];
+                dp += s_data[j];
             }
+            s_vst[i] = vp;
+            s_dst[i] = dp;
         }
         /* precinct header: Lprc, Q, R as bytes first, then the 2-bit band
          * coding modes D[p,b] of every existing band */
@@ -696,7 +706,8 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
     __syncthreads();
     if (!s_ok) return;
 
-    /* pass B */
+    /* pass B: each lane 4 consecutive groups; its unary codes are joined
+     * into one write, its data chunks into writes of up to 64 bits */
     const uint32_t uniform = cfg->qpih;
     for (uint32_t sidx = warp; sidx < nseg; sidx += PK_WARPS) {
         const jxs_seg_t sg = segs[sidx];
@@ -708,39 +719,81 @@ __global__ void __launch_bounds__(PK_THREADS) pack_kernel(const jxs_cfg_t* __res
         const uint8_t* grow = gcli + bd.gcli_off + row * bd.gpitch;
         const uint16_t* crow = coef + bd.coef_off + row * bd.pitch;
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
-        uint32_t vpos = s_vlc[sidx], dpos = s_data[sidx];
-        for (uint32_t base = sg.g0; base < gend; base += 32) {
-            const uint32_t g = base + lane;
-            const bool valid = g < gend;
-            const uint32_t v = valid ? grow[g] : 0u;
-            uint32_t mx = v;
-            mx = max(mx, __shfl_xor_sync(FULL, mx, 1));
-            mx = max(mx, __shfl_xor_sync(FULL, mx, 2));
-            mx = max(mx, __shfl_xor_sync(FULL, mx, 4));
-            uint32_t vlen = 0;
+        uint32_t vpos = s_vst[sidx], dpos = s_dst[sidx];
+        for (uint32_t base = sg.g0; base < gend; base += 128) {
+            const uint32_t g = base + 4 * lane;
+            const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
+            const uint32_t w4 = nv ? *(const uint32_t*)(grow + g) : 0u;
+            uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0;
+            if (nv) {
+                c0 = *(const uint4*)(crow + 4 * g);
+                c1 = *(const uint4*)(crow + 4 * g + 8);
+            }
+            uint32_t v[4], m = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                v[k] = k < (int)nv ? (w4 >> (8 * k)) & 255u : 0u;
+                m = max(m, v[k]);
+            }
+            const uint32_t mx = max(m, __shfl_xor_sync(FULL, m, 1));
+            const bool insig = mx <= t;
+            uint64_t vacc = 0;
+            uint32_t vl = 0;
             if (L.raw) {
-                if (valid) put_bits(buf, words, L.gcli_pos + 4 * g, v, 4, ovf);
+                /* raw GCLIs: the lane's nibbles in one write */
+                if (nv) put_bits(buf, words, L.gcli_pos + 4 * g, ((v[0] << 12) | (v[1] << 8) | (v[2] << 4) | v[3]) >> (4 * (4 - nv)), 4 * nv, ovf);
             } else {
-                const bool insig = mx <= t;
                 if (L.meth) {
-                    /* significance flags, 1 = insignificant: lanes 0, 8, 16, 24 */
-                    const uint32_t bal = __ballot_sync(FULL, valid && (lane & 7) == 0 && insig);
+                    /* significance flags, 1 = insignificant: even lanes lead a group of 8 */
+                    const uint32_t bal = __ballot_sync(FULL, nv && !(lane & 1) && insig);
                     if (lane == 0) {
-                        const uint32_t nsg = min(4u, (gend - base + 7) >> 3);
-                        const uint32_t bits = ((bal & 1u) << 3) | (((bal >> 8) & 1u) << 2) | (((bal >> 16) & 1u) << 1) | ((bal >> 24) & 1u);
-                        if (bits >> (4 - nsg)) put_bits(buf, words, L.sig_pos + (base >> 3), bits >> (4 - nsg), nsg, ovf);
+                        const uint32_t nsg = min(16u, (gend - base + 7) >> 3);
+                        uint32_t bits = 0;
+                        for (uint32_t i2 = 0; i2 < nsg; i2++) bits = (bits << 1) | ((bal >> (2 * i2)) & 1u);
+                        if (bits) put_bits(buf, words, L.sig_pos + (base >> 3), bits, nsg, ovf);
                     }
                 }
-                if (valid && !(L.meth && insig)) vlen = v > t ? v - t + 1 : 1u;
+                if (!(L.meth && insig)) {
+                    /* unary codes: (v - t) ones then a zero (PackPrecinct.h:25-39) */
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        if (k < (int)nv) {
+                            const uint32_t n = v[k] > t ? v[k] - t + 1 : 1u;
+                            vacc = (vacc << n) | (((1ull << (n - 1)) - 1) << 1);
+                            vl += n;
+                        }
+                    }
+                }
             }
-            const uint32_t dlen = (valid && v > t) ? 4 * (v - t + 1) : 0u;
+            uint32_t dl = 0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) dl += (k < (int)nv && v[k] > t) ? 4 * (v[k] - t + 1) : 0u;
             uint32_t tot;
-            const uint32_t ex = warp_excl_scan((dlen << 16) | vlen, &tot);
-            /* unary code: (v - t) ones then a zero (PackPrecinct.h:25-39) */
-            if (vlen) put_bits(buf, words, vpos + (ex & 0xffffu), ((1u << (vlen - 1)) - 1u) << 1, vlen, ovf);
-            if (dlen) {
-                const uint2 raw4 = *(const uint2*)(crow + 4 * g);
-                put_bits(buf, words, dpos + (ex >> 16), data_chunk(raw4, (int)B.w - 4 * (int)g, v, t, uniform), dlen, ovf);
+            const uint32_t ex = warp_excl_scan((dl << 16) | vl, &tot);
+            if (vl) put_bits(buf, words, vpos + (ex & 0xffffu), vacc, vl, ovf);
+            if (dl) {
+                /* data bits of the groups with gcli > gtli (pack_data_c,
+                 * PackPrecinct.c:128-198), joined while they fit 64 bits */
+                uint32_t pos = dpos + (ex >> 16);
+                uint64_t acc = 0;
+                uint32_t an = 0;
+                const uint2 cw[4] = {make_uint2(c0.x, c0.y), make_uint2(c0.z, c0.w), make_uint2(c1.x, c1.y), make_uint2(c1.z, c1.w)};
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (k < (int)nv && v[k] > t) {
+                        const uint32_t n = 4 * (v[k] - t + 1);
+                        const uint64_t ch = data_chunk(cw[k], (int)B.w - 4 * (int)(g + k), v[k], t, uniform);
+                        if (an + n > 64) {
+                            put_bits(buf, words, pos, acc, an, ovf);
+                            pos += an;
+                            acc = 0;
+                            an = 0;
+                        }
+                        acc = n == 64 ? ch : (acc << n) | ch;
+                        an += n;
+                    }
+                }
+                if (an) put_bits(buf, words, pos, acc, an, ovf);
             }
             vpos += tot & 0xffffu;
             dpos += tot >> 16;
