@@ -482,12 +482,19 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __
     extern __shared__ __align__(16) uint32_t buf[];
     __shared__ uint32_t s_data[JXS_MAXSEG], s_vlc[JXS_MAXSEG], s_zero[JXS_MAXSEG];
     __shared__ PkLine pl[JXS_MAXBLINES];
-    __shared__ uint8_t tb[JXS_MAXBL], s_meth[JXS_MAXBL];
+    __shared__ uint8_t s_meth[JXS_MAXBL];
     __shared__ uint32_t s_cn[JXS_MAXBL], s_cs[JXS_MAXBL];
     __shared__ uint32_t s_lg[JXS_MAXBLINES], s_ls[JXS_MAXBLINES];       /* per line: GCLI / significance bits */
     __shared__ uint32_t s_pks[JXS_MAXPK], s_pkg[JXS_MAXPK], s_pkd[JXS_MAXPK]; /* per packet: sub-packet starts */
     __shared__ uint8_t s_pkr[JXS_MAXPK];
     __shared__ uint32_t s_vst[JXS_MAXSEG], s_dst[JXS_MAXSEG];        /* per segment: GCLI / data bit starts */
+    /* this precinct kind's tables, staged from the configuration */
+    __shared__ jxs_seg_t s_seg[JXS_MAXSEG];
+    __shared__ jxs_bline_t s_bl[JXS_MAXBLINES];
+    __shared__ uint64_t s_grow[JXS_MAXBLINES], s_crow[JXS_MAXBLINES]; /* per line: GCLI / coefficient row offsets */
+    __shared__ uint8_t s_lt[JXS_MAXBLINES];                            /* per line: gtli */
+    __shared__ uint8_t s_pkbl0[JXS_MAXPK], s_pknbl[JXS_MAXPK];
+    __shared__ uint32_t s_praw[JXS_MAXPK];
     __shared__ int s_ok;
 
     const int p = blockIdx.x;
@@ -511,9 +518,28 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __
     int ovf = 0;
     for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) buf[i] = 0;
     for (uint32_t fb = threadIdx.x; fb < cfg->nbands; fb += blockDim.x) {
-        tb[fb] = jxs_truncation(cfg->band[fb].gain, cfg->band[fb].prio, R.q, R.r);
         s_cn[fb] = 0;
         s_cs[fb] = 0;
+    }
+    {
+        const uint32_t ns = cfg->nseg[last], nl = cfg->nbline[last];
+        for (uint32_t i = threadIdx.x; i < ns * (sizeof(jxs_seg_t) / 4); i += blockDim.x)
+            ((uint32_t*)s_seg)[i] = ((const uint32_t*)cfg->seg[last])[i];
+        for (uint32_t i = threadIdx.x; i < nl * (sizeof(jxs_bline_t) / 4); i += blockDim.x)
+            ((uint32_t*)s_bl)[i] = ((const uint32_t*)cfg->bline[last])[i];
+        for (uint32_t x = threadIdx.x; x < nl; x += blockDim.x) {
+            const jxs_bline_t& B = cfg->bline[last][x];
+            const jxs_band_t& bd = cfg->band[B.fb];
+            const uint64_t row = (uint64_t)(p * bd.lines + B.line);
+            s_grow[x] = bd.gcli_off + row * bd.gpitch;
+            s_crow[x] = bd.coef_off + row * bd.pitch;
+            s_lt[x] = jxs_truncation(bd.gain, bd.prio, R.q, R.r);
+        }
+        for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) {
+            s_pkbl0[k] = cfg->pk_bl0[last][k];
+            s_pknbl[k] = cfg->pk_nbl[last][k];
+            s_praw[k] = cfg->raw_bytes[last][k];
+        }
     }
     if (threadIdx.x == 0) {
     }
@@ -521,18 +547,16 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t nseg = cfg->nseg[last], SG = cfg->seg_groups;
-    const jxs_seg_t* segs = cfg->seg[last];
-    const jxs_bline_t* bls = cfg->bline[last];
+    const jxs_seg_t* segs = s_seg;
+    const jxs_bline_t* bls = s_bl;
 
     /* pass A: each lane 4 consecutive groups (one 4-byte GCLI load), a warp
      * 128 groups per step */
     for (uint32_t sidx = warp; sidx < nseg; sidx += PK_WARPS) {
         const jxs_seg_t sg = segs[sidx];
-        const jxs_bline_t B = bls[sg.bl];
-        const jxs_band_t& bd = cfg->band[B.fb];
-        const uint32_t t = tb[B.fb];
-        const uint8_t* grow = gcli + bd.gcli_off + (uint64_t)(p * bd.lines + B.line) * bd.gpitch;
-        const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+        const uint32_t t = s_lt[sg.bl];
+        const uint8_t* grow = gcli + s_grow[sg.bl];
+        const uint32_t gend = min(sg.g0 + SG, bls[sg.bl].gcli_w);
         uint32_t dsum = 0, vsum = 0, zsum = 0;
         for (uint32_t base = sg.g0; base < gend; base += 128) {
             const uint32_t g = base + 4 * lane;
@@ -595,7 +619,7 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __
         __syncwarp();
         /* one lane per packet: sub-packet sizes, raw fallback, header */
         const uint32_t k = lane;
-        const uint32_t nb = k < cfg->npk ? cfg->pk_nbl[last][k] : 0u, b0 = k < cfg->npk ? cfg->pk_bl0[last][k] : 0u;
+        const uint32_t nb = k < cfg->npk ? s_pknbl[k] : 0u, b0 = k < cfg->npk ? s_pkbl0[k] : 0u;
         uint32_t db = 0, gbits = 0, sbits = 0;
         for (uint32_t x = b0; x < b0 + nb; x++) {
             db += pl[x].data;
@@ -603,7 +627,7 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __
             sbits += s_ls[x];
         }
         const uint32_t dB = (db + 7) >> 3, gB = (gbits + 7) >> 3, sB = (sbits + 7) >> 3;
-        const uint32_t rawB = nb ? cfg->raw_bytes[last][k] : 0u;
+        const uint32_t rawB = nb ? s_praw[k] : 0u;
         const int raw = nb && sB + gB > rawB;
         const uint32_t gcl_bytes = raw ? rawB : gB;
         const uint32_t hb = nb ? (cfg->short_hdr ? 5u : 7u) : 0u;
@@ -640,7 +664,7 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __
         __syncwarp();
         /* per line: positions inside its packet's sub-packets */
         for (uint32_t x = lane; x < nbl; x += 32) {
-            const uint32_t kk = bls[x].pk, xb0 = cfg->pk_bl0[last][kk];
+            const uint32_t kk = bls[x].pk, xb0 = s_pkbl0[kk];
             uint32_t sp = 0, gp = 0, dp = 0;
             const int r = s_pkr[kk];
             for (uint32_t y = xb0; y < x; y++) {
@@ -713,11 +737,9 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
         const PkLine L = pl[sg.bl];
-        const jxs_band_t& bd = cfg->band[B.fb];
-        const uint32_t t = tb[B.fb];
-        const uint64_t row = (uint64_t)(p * bd.lines + B.line);
-        const uint8_t* grow = gcli + bd.gcli_off + row * bd.gpitch;
-        const uint16_t* crow = coef + bd.coef_off + row * bd.pitch;
+        const uint32_t t = s_lt[sg.bl];
+        const uint8_t* grow = gcli + s_grow[sg.bl];
+        const uint16_t* crow = coef + s_crow[sg.bl];
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
         uint32_t vpos = s_vst[sidx], dpos = s_dst[sidx];
         for (uint32_t base = sg.g0; base < gend; base += 128) {
