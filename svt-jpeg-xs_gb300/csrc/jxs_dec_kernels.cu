@@ -194,6 +194,11 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     __shared__ uint8_t s_mode[JXS_MAXBL];
     __shared__ uint32_t s_pksb[JXS_MAXPK], s_pkrb[JXS_MAXPK];
     __shared__ uint32_t s_next[2]; /* segment queues of the two warp passes */
+    /* this precinct kind's tables, staged from the configuration */
+    __shared__ jxs_seg_t s_seg[JXS_MAXSEG];
+    __shared__ jxs_bline_t s_bl[JXS_MAXBLINES];
+    __shared__ uint64_t s_crow[JXS_MAXBLINES]; /* per line: coefficient row offset */
+    __shared__ uint8_t s_pkbl0[JXS_MAXPK], s_pknbl[JXS_MAXPK];
     __shared__ uint32_t s_cnt[JXS_MAXSEG], s_base[JXS_MAXSEG];
     __shared__ uint32_t ws[UK_WARPS];
     __shared__ int s_err;
@@ -226,6 +231,22 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     }
     const uint32_t total = s_total, lead = s_lead;
     {
+        const uint32_t ns = cfg->nseg[last], nl = cfg->nbline[last];
+        for (uint32_t i = threadIdx.x; i < ns * (sizeof(jxs_seg_t) / 4); i += blockDim.x)
+            ((uint32_t*)s_seg)[i] = ((const uint32_t*)cfg->seg[last])[i];
+        for (uint32_t i = threadIdx.x; i < nl * (sizeof(jxs_bline_t) / 4); i += blockDim.x)
+            ((uint32_t*)s_bl)[i] = ((const uint32_t*)cfg->bline[last])[i];
+        for (uint32_t x = threadIdx.x; x < nl; x += blockDim.x) {
+            const jxs_bline_t& B = cfg->bline[last][x];
+            const jxs_band_t& bd = cfg->band[B.fb];
+            s_crow[x] = bd.coef_off + (uint64_t)(p * bd.lines + B.line) * bd.pitch;
+        }
+        for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) {
+            s_pkbl0[k] = cfg->pk_bl0[last][k];
+            s_pknbl[k] = cfg->pk_nbl[last][k];
+        }
+    }
+    {
         /* aligned 16-byte chunks inside the precinct, single bytes at its
          * ends; 32 zero bytes after it for the bit readers */
         const uint8_t* gsrc = bs + off - lead;
@@ -242,8 +263,8 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     __syncthreads();
 
     const uint32_t nbl = cfg->nbline[last], nseg = cfg->nseg[last], SG = cfg->seg_groups;
-    const jxs_bline_t* bls = cfg->bline[last];
-    const jxs_seg_t* segs = cfg->seg[last];
+    const jxs_bline_t* bls = s_bl;
+    const jxs_seg_t* segs = s_seg;
     /* parse, by warp 0: band modes and per-line fields in parallel, the
      * packet headers in order by lane 0, then every line's positions */
     if (warp == 0) {
@@ -275,7 +296,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
         /* per packet: significance bits and raw GCLI bits it must hold */
         uint32_t sb = 0, rb = 0;
         if (lane < (int)cfg->npk) {
-            const uint32_t b0 = cfg->pk_bl0[last][lane], nb = cfg->pk_nbl[last][lane];
+            const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
             for (uint32_t x = b0; x < b0 + nb; x++) {
                 if (ln[x].meth) sb += bls[x].sig_w;
                 rb += 4 * bls[x].gcli_w;
@@ -296,7 +317,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
                 P.gbits = P.dbits = P.nwords = P.ncoded = P.nzero = 0;
                 P.raw = 0;
                 P.wbase = tw;
-                if (err || !cfg->pk_nbl[last][k]) continue;
+                if (err || !s_pknbl[k]) continue;
                 const uint32_t hb = long_hdr ? 7 : 5;
                 left -= hb * 8;
                 if (left < 0) { err = JXS_E_DEC_BITSTREAM; break; }
@@ -353,7 +374,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
         /* line positions: significance flags, or raw GCLIs for raw packets */
         if (!err && lane < (int)cfg->npk && pk[lane].present) {
             const UkPk& P = pk[lane];
-            const uint32_t b0 = cfg->pk_bl0[last][lane], nb = cfg->pk_nbl[last][lane];
+            const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
             uint32_t run = P.spos;
             for (uint32_t x = b0; x < b0 + nb; x++) {
                 ln[x].raw = (uint8_t)P.raw;
@@ -388,7 +409,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
             __syncwarp();
             /* codeword base of every segment inside its packet: one lane per packet */
             if (lane < (int)cfg->npk) {
-                const uint32_t b0 = cfg->pk_bl0[last][lane], nb = cfg->pk_nbl[last][lane];
+                const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
                 uint32_t run = 0;
                 for (uint32_t x = b0; x < b0 + nb; x++) {
                     if (ln[x].raw) continue;
@@ -521,7 +542,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
         /* data base of every segment inside its packet: one lane per packet */
         bool bad_pk = false;
         if (lane < (int)npk) {
-            const uint32_t b0 = cfg->pk_bl0[last][lane], nb = cfg->pk_nbl[last][lane];
+            const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
             uint32_t run = 0;
             for (uint32_t x = b0; x < b0 + nb; x++)
                 for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
@@ -546,8 +567,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
         const jxs_bline_t B = bls[sg.bl];
         const UkLine L = ln[sg.bl];
         const UkPk P = pk[L.pk];
-        const jxs_band_t& bd = cfg->band[B.fb];
-        int16_t* crow = coef + bd.coef_off + (uint64_t)(p * bd.lines + B.line) * bd.pitch;
+        int16_t* crow = coef + s_crow[sg.bl];
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
         uint32_t dpos = P.dpos + s_base[sidx];
         for (uint32_t base = sg.g0; base < gend; base += 32) {

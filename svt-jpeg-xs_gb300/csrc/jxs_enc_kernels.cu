@@ -50,13 +50,26 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
     __shared__ uint8_t lgain[JXS_MAXBLINES], lprio[JXS_MAXBLINES], lfb[JXS_MAXBLINES];
     __shared__ uint32_t lsig[JXS_MAXBLINES], lraw[JXS_MAXPK];
     __shared__ uint32_t dC[32][32]; /* per Q: cost at R = 0, then its changes at each R */
+    /* this precinct kind's tables, staged from the configuration */
+    __shared__ jxs_seg_t s_seg[JXS_MAXSEG];
+    __shared__ jxs_bline_t s_bl[JXS_MAXBLINES];
+    __shared__ uint64_t s_grow[JXS_MAXBLINES];
+    __shared__ uint8_t s_pkbl0[JXS_MAXPK], s_pknbl[JXS_MAXPK], s_order[JXS_MAXBLINES];
 
     const int p = blockIdx.x;
     const int last = (p + 1 >= (int)cfg->np);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t nbl = cfg->nbline[last], nseg = cfg->nseg[last], SG = cfg->seg_groups;
-    const jxs_bline_t* bls = cfg->bline[last];
-    const jxs_seg_t* segs = cfg->seg[last];
+    const jxs_bline_t* bls = s_bl;
+    const jxs_seg_t* segs = s_seg;
+    for (uint32_t i = threadIdx.x; i < nseg * (sizeof(jxs_seg_t) / 4); i += blockDim.x)
+        ((uint32_t*)s_seg)[i] = ((const uint32_t*)cfg->seg[last])[i];
+    for (uint32_t i = threadIdx.x; i < nbl * (sizeof(jxs_bline_t) / 4); i += blockDim.x)
+        ((uint32_t*)s_bl)[i] = ((const uint32_t*)cfg->bline[last])[i];
+    for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) {
+        s_pkbl0[k] = cfg->pk_bl0[last][k];
+        s_pknbl[k] = cfg->pk_nbl[last][k];
+    }
     for (uint32_t i = threadIdx.x; i < nbl * 16; i += blockDim.x) {
         hist[i >> 4][i & 15] = 0;
         shist[i >> 4][i & 15] = 0;
@@ -66,12 +79,15 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
         cs[i >> 4][i & 15] = 0;
     }
     for (uint32_t x = threadIdx.x; x < nbl; x += blockDim.x) {
-        const jxs_band_t& bd = cfg->band[bls[x].fb];
+        const jxs_bline_t& B = cfg->bline[last][x];
+        const jxs_band_t& bd = cfg->band[B.fb];
         pmax[x] = -1;
         lgain[x] = bd.gain;
         lprio[x] = bd.prio;
-        lfb[x] = bls[x].fb;
-        lsig[x] = bls[x].sig_w;
+        lfb[x] = B.fb;
+        lsig[x] = B.sig_w;
+        s_grow[x] = bd.gcli_off + (uint64_t)(p * bd.lines + B.line) * bd.gpitch;
+        s_order[x] = cfg->pk_order[last][x];
     }
     for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) lraw[k] = cfg->raw_bytes[last][k];
     __syncthreads();
@@ -81,10 +97,8 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
     for (uint32_t sidx = warp; sidx < nseg; sidx += RC_WARPS) {
         const jxs_seg_t sg = segs[sidx];
         const uint32_t x = sg.bl;
-        const jxs_bline_t B = bls[x];
-        const jxs_band_t& bd = cfg->band[B.fb];
-        const uint8_t* grow = gcli + bd.gcli_off + (uint64_t)(p * bd.lines + B.line) * bd.gpitch;
-        const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+        const uint8_t* grow = gcli + s_grow[x];
+        const uint32_t gend = min(sg.g0 + SG, bls[x].gcli_w);
         uint32_t h[4] = {0, 0, 0, 0}, sh[4] = {0, 0, 0, 0};
         int it = 0;
         for (uint32_t base = sg.g0; base < gend; base += 32) {
@@ -171,7 +185,7 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
     for (uint32_t e = threadIdx.x; e < (uint32_t)nq * npk; e += blockDim.x) {
         const int q = (int)(e / npk);
         const uint32_t k = e - (uint32_t)q * npk;
-        const uint32_t b0 = cfg->pk_bl0[last][k], nb = cfg->pk_nbl[last][k];
+        const uint32_t b0 = s_pkbl0[k], nb = s_pknbl[k];
         if (!nb) continue;
         uint32_t db = 0, gb = 0, sb = 0;
         for (uint32_t x = b0; x < b0 + nb; x++) {
@@ -188,7 +202,7 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
         uint32_t c = ((db + 7) >> 3) + min(lraw[k], ((sb + 7) >> 3) + ((gb + 7) >> 3));
         atomicAdd(&dC[q][0], c);
         for (uint32_t i = 0; i < nb; i++) {
-            const uint32_t x = cfg->pk_order[last][b0 + i];
+            const uint32_t x = s_order[b0 + i];
             const int rf = lprio[x] + 1; /* the line's gtli drops by one for R >= priority + 1 */
             if (rf >= nr) break;
             const int g = lgain[x];
@@ -259,7 +273,9 @@ __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restr
     extern __shared__ uint32_t tbl[]; /* [RS_CHUNK][nq][nr] */
     __shared__ uint32_t s_carry, s_run;
     __shared__ int s_err;
+    __shared__ uint32_t s_empty[32];
     const int s = blockIdx.x;
+    if (threadIdx.x < 32) s_empty[threadIdx.x] = cfg->empty[threadIdx.x];
     const int last_slice = (s + 1 == (int)cfg->nslices);
     const uint32_t slice_budget = cfg->slice_size[s] - 6 - (last_slice ? 2 : 0);
     const uint32_t first_p = cfg->pps * s;
@@ -282,6 +298,8 @@ __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restr
         s_err = 0;
     }
     const int nq = cfg->max_q + 1, nr = cfg->max_r + 1, nt = nq * nr;
+    const int max_q = cfg->max_q, max_r = cfg->max_r, rc_mode = (int)cfg->rc_mode;
+    const uint32_t np_all = cfg->np, hdrs0 = cfg->hdrs_bytes[0], hdrs1 = cfg->hdrs_bytes[1];
     for (uint32_t c0 = 0; c0 < nprec; c0 += RS_CHUNK) {
         const uint32_t cnt = min((uint32_t)RS_CHUNK, nprec - c0);
         __syncthreads();
@@ -296,9 +314,9 @@ __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restr
                 const uint32_t i = c0 + ii;
                 const uint32_t p = first_p + i;
                 const uint32_t* T = tbl + ii * nt;
-                const int last = (p + 1 >= cfg->np);
+                const int last = (p + 1 >= np_all);
                 const uint32_t budget = (i == 0 ? first_b : min_b) + (i < left ? 1 : 0) + s_carry;
-                const uint32_t hdr = cfg->hdrs_bytes[last];
+                const uint32_t hdr = last ? hdrs1 : hdrs0;
                 int err = 0;
                 if (budget > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
                 else if (budget <= hdr) err = JXS_E_UNDEFINED;
@@ -308,22 +326,22 @@ __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restr
                     const uint32_t avail = budget - hdr;
                     BSearch bs;
                     int step = 6;
-                    if (step > cfg->max_q) step = 0;
-                    bs_init(bs, 0, cfg->max_q, 0, step);
+                    if (step > max_q) step = 0;
+                    bs_init(bs, 0, max_q, 0, step);
                     int res, next = BS_BEGIN, v = 0;
                     while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
-                        if (cfg->empty[v] & 1u) next = BS_OUT_OF_RANGE;
+                        if (s_empty[v] & 1u) next = BS_OUT_OF_RANGE;
                         else next = T[v * nr] > avail ? BS_TOO_SMALL : BS_TOO_BIG;
                     }
                     if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
                     q = v;
                     if (!err) {
                         step = 6;
-                        if (step >= cfg->max_r) step = 0;
-                        bs_init(bs, 0, cfg->max_r, 1, step);
+                        if (step >= max_r) step = 0;
+                        bs_init(bs, 0, max_r, 1, step);
                         next = BS_BEGIN;
                         while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
-                            if ((cfg->empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
+                            if ((s_empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
                             else next = T[q * nr + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
                         }
                         if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
@@ -333,7 +351,7 @@ __global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restr
                     if (!err) {
                         uint32_t padding = avail - data;
                         uint32_t total = budget;
-                        if (cfg->rc_mode == 1 && i + 1 < nprec) {
+                        if (rc_mode == 1 && i + 1 < nprec) {
                             total -= padding;
                             s_carry = padding;
                         } else {

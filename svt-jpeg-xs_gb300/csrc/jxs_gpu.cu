@@ -608,7 +608,7 @@ extern "C" jxs_gpu_dec_t* jxs_gpu_dec_create(const jxs_cfg_t* cfg, int nslots, i
     uint64_t cap = (uint64_t)cfg->lcod / (cfg->nslices ? cfg->nslices : 1);
     cap = (cfg->max_slice_budget ? cfg->max_slice_budget : cap + cap / 4) + 4096;
     if (cap > cfg->lcod + 64ull) cap = cfg->lcod + 64ull;
-    const size_t room = kSmemMax - 8 * 1024; /* static shared memory of the unpacking kernel */
+    const size_t room = kSmemMax - 16 * 1024; /* static shared memory of the unpacking kernel */
     if (cap + fixed > room) cap = room > fixed + 4096 ? room - fixed : 4096;
     d->cap_bytes = (uint32_t)cap & ~15u;
     if (cudaMalloc(&d->dcfg, sizeof(jxs_cfg_t)) != cudaSuccess ||
