@@ -174,88 +174,173 @@ DEV void warp_lift_fwd(const int32_t* x, int npairs, Out out) {
 #define FV_ROWPAIRS 8
 #define FV_SROW (FV_COLS + 16)            /* shared row: 4 front words (2 pad, 2 halo), FV_COLS, halo, slack */
 
-template <int SRC>
-__global__ void __launch_bounds__(FV_THREADS, 8) fwd_v_kernel(const __grid_constant__ FwdVLaunch L, const jxs_band_t* __restrict__ bands,
-                                                           uint16_t* __restrict__ coef, uint8_t* __restrict__ gcli) {
-    __shared__ __align__(16) int32_t sL[FV_ROWPAIRS][FV_SROW];
-    __shared__ __align__(16) int32_t sH[FV_ROWPAIRS][FV_SROW];
-    int jb = 0;
-    while (jb + 1 < L.njobs && (int)blockIdx.x >= L.job[jb + 1].first_block) jb++;
-    const FwdVJob& J = L.job[jb];
-    const int t = blockIdx.x - J.first_block;
-    const int ty = t / J.col_tiles, tx = t - ty * J.col_tiles;
-    const int w = J.w, h = J.h, depth = L.depth;
-    const int n1 = (h + 1) >> 1, n2 = h >> 1;
-    const int r0 = ty * FV_ROWPAIRS;
-    const int c0 = tx * FV_COLS;
-    const int rc = min(FV_ROWPAIRS, n1 - r0); /* low rows of this tile */
-    const int hc = max(0, min(FV_ROWPAIRS, n2 - r0));
+#define FV_NR (2 * FV_ROWPAIRS + 3)       /* input rows per tile: 2 above, 2 R, 1 below */
 
+/* Raw input of one column pair in the staging buffer: the two samples as
+ * read (16-bit sources: packed in one word) or the two int32 low-band
+ * values. */
+template <int SRC> struct FvIn { typedef uint32_t T; };
+template <> struct FvIn<SRC_I32> { typedef int2 T; };
+
+DEV void cp_async4(void* smem, const void* g) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(g));
+}
+DEV void cp_async8(void* smem, const void* g) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(g));
+}
+DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+DEV void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
+
+/* One tile of a vertical-level launch. */
+struct FvTile {
+    int jb, r0, c0, npairs, ncp, rc, hc;
+};
+DEV FvTile fv_tile(const FwdVLaunch& L, int t) {
+    FvTile T;
+    int jb = 0;
+    while (jb + 1 < L.njobs && t >= L.job[jb + 1].first_block) jb++;
+    const FwdVJob& J = L.job[jb];
+    const int u = t - J.first_block;
+    const int ty = u / J.col_tiles, tx = u - ty * J.col_tiles;
+    const int n1 = (J.h + 1) >> 1, n2 = J.h >> 1, w1 = (J.w + 1) >> 1;
+    T.jb = jb;
+    T.r0 = ty * FV_ROWPAIRS;
+    T.c0 = tx * FV_COLS;
     /* output pairs j in [c0/2, c0/2 + npairs) of the level's bands; lifting
-     * them reads input columns c0 - 2 .. c0 + 2 npairs */
-    const int w1 = (w + 1) >> 1;
-    const int npairs = min(FV_COLS / 2, ((w1 - c0 / 2) + 1) & ~1);
-    const int jc = c0 >> 1;
-    /* vertical lifting: column pair cp covers input columns c0 - 2 + 2cp, +1 */
-    const int ncp = npairs + 2;
-    int ys[2 * FV_ROWPAIRS + 3];
-#pragma unroll
-    for (int k = 0; k < 2 * FV_ROWPAIRS + 3; k++) ys[k] = mirror_idx(2 * r0 - 2 + k, h);
-    for (int cp = threadIdx.x; cp < ncp; cp += FV_THREADS) { /* a single pass: ncp <= FV_THREADS */
-        const int xa = c0 - 2 + 2 * cp;
-        const bool inside = xa >= 0 && xa + 1 < w;
-        const int ma = mirror_idx(xa, w), mb = mirror_idx(xa + 1, w);
-        int32_t a[2 * FV_ROWPAIRS + 3], b[2 * FV_ROWPAIRS + 3];
-#pragma unroll
-        for (int k = 0; k < 2 * FV_ROWPAIRS + 3; k++) {
-            if (inside) {
-                load2<SRC>(J.src, J.src_pitch, J.chan, depth, ys[k], xa, J.vec, a[k], b[k]);
-            } else {
-                a[k] = load1<SRC>(J.src, J.src_pitch, J.chan, depth, ys[k], ma);
-                b[k] = load1<SRC>(J.src, J.src_pitch, J.chan, depth, ys[k], mb);
-            }
-        }
-        int32_t hpa = a[1] - ((a[0] + a[2]) >> 1), hpb = b[1] - ((b[0] + b[2]) >> 1);
-#pragma unroll
-        for (int k = 0; k < FV_ROWPAIRS; k++) {
-            const int e = 2 + 2 * k; /* x[2i] of pair r0 + k */
-            const int32_t ha = a[e + 1] - ((a[e] + a[e + 2]) >> 1), hb = b[e + 1] - ((b[e] + b[e + 2]) >> 1);
-            const int32_t la = a[e] + ((hpa + ha + 2) >> 2), lb = b[e] + ((hpb + hb + 2) >> 2);
-            *(int2*)&sL[k][2 + 2 * cp] = make_int2(la, lb);
-            *(int2*)&sH[k][2 + 2 * cp] = make_int2(ha, hb);
-            hpa = ha;
-            hpb = hb;
+     * them reads input columns c0 - 2 .. c0 + 2 npairs + 1 */
+    T.npairs = min(FV_COLS / 2, ((w1 - T.c0 / 2) + 1) & ~1);
+    T.ncp = T.npairs + 2;
+    T.rc = min(FV_ROWPAIRS, n1 - T.r0);
+    T.hc = max(0, min(FV_ROWPAIRS, n2 - T.r0));
+    return T;
+}
+
+/* Stages the input of tile t into buffer `in` (FV_NR rows x column pairs):
+ * asynchronous copies where the pair is inside the plane and aligned,
+ * ordinary loads (with the symmetric extension) elsewhere. */
+template <int SRC>
+DEV void fv_stage(const FwdVLaunch& L, int t, typename FvIn<SRC>::T* in) {
+    const FvTile T = fv_tile(L, t);
+    const FwdVJob& J = L.job[T.jb];
+    const int cp = threadIdx.x;
+    if (cp >= T.ncp) return;
+    const int w = J.w, h = J.h;
+    const int xa = T.c0 - 2 + 2 * cp;
+    const bool inside = xa >= 0 && xa + 1 < w;
+    const bool async = inside && J.vec && (SRC == SRC_U16 || SRC == SRC_I32);
+    const int ma = mirror_idx(xa, w), mb = mirror_idx(xa + 1, w);
+#pragma unroll 4
+    for (int k = 0; k < FV_NR; k++) {
+        const int y = mirror_idx(2 * T.r0 - 2 + k, h);
+        typename FvIn<SRC>::T* dst = in + k * FV_THREADS + cp;
+        const long long row = (long long)y * J.src_pitch;
+        if (SRC == SRC_I32) {
+            const int32_t* src = (const int32_t*)J.src + row;
+            if (async) cp_async8(dst, src + xa);
+            else *(int2*)dst = make_int2(src[ma], src[mb]);
+        } else if (SRC == SRC_U16) {
+            const uint16_t* src = (const uint16_t*)J.src + row;
+            if (async) cp_async4(dst, src + xa);
+            else *(uint32_t*)dst = (uint32_t)src[ma] | ((uint32_t)src[mb] << 16);
+        } else if (SRC == SRC_U8) {
+            const uint8_t* src = (const uint8_t*)J.src + row;
+            *(uint32_t*)dst = (uint32_t)src[ma] | ((uint32_t)src[mb] << 16);
+        } else if (SRC == SRC_PK8) {
+            const uint8_t* src = (const uint8_t*)J.src + row;
+            *(uint32_t*)dst = (uint32_t)src[3 * ma + J.chan] | ((uint32_t)src[3 * mb + J.chan] << 16);
+        } else {
+            const uint16_t* src = (const uint16_t*)J.src + row;
+            *(uint32_t*)dst = (uint32_t)src[3 * ma + J.chan] | ((uint32_t)src[3 * mb + J.chan] << 16);
         }
     }
-    __syncthreads();
+}
 
-    /* horizontal lifting, one warp per row; the tile's output pairs are
-     * j in [c0/2, c0/2 + npairs) of the level's bands */
+/* Persistent: each block walks tiles t = blockIdx.x, + gridDim.x, ...; the
+ * next tile's input is staged (asynchronous copies) while the current one is
+ * lifted. */
+template <int SRC>
+__global__ void __launch_bounds__(FV_THREADS, 6) fwd_v_kernel(const __grid_constant__ FwdVLaunch L, const jxs_band_t* __restrict__ bands,
+                                                           uint16_t* __restrict__ coef, uint8_t* __restrict__ gcli) {
+    typedef typename FvIn<SRC>::T InT;
+    extern __shared__ __align__(16) unsigned char fv_dyn[];
+    InT* inbuf = (InT*)fv_dyn; /* [2][FV_NR][FV_THREADS] */
+    __shared__ __align__(16) int32_t sL[FV_ROWPAIRS][FV_SROW];
+    __shared__ __align__(16) int32_t sH[FV_ROWPAIRS][FV_SROW];
+    const int depth = L.depth;
     const int warp = threadIdx.x >> 5;
-    for (int r = warp; r < rc + hc; r += FV_THREADS / 32) {
-        if (r < rc) {
-            const int row = r0 + r;
-            const BandRow bhl = band_row(bands[J.b_hl], row, coef, gcli);
-            int32_t* ll = J.ll + (long long)row * J.ll_pitch;
-            warp_lift_fwd(&sL[r][4], npairs, [&](int j, const int32_t* sv, const int32_t* d) {
-                const int jj = jc + j;
-                emit4(bhl, jj, d[0], d[1], d[2], d[3]);
-                if (jj + 3 < w1) {
-                    *(int4*)(ll + jj) = make_int4(sv[0], sv[1], sv[2], sv[3]);
+    int t = blockIdx.x, buf = 0;
+    if (t < L.ntiles) fv_stage<SRC>(L, t, inbuf);
+    cp_async_commit();
+    for (; t < L.ntiles; t += gridDim.x) {
+        const int tn = t + gridDim.x;
+        if (tn < L.ntiles) fv_stage<SRC>(L, tn, inbuf + (buf ^ 1) * FV_NR * FV_THREADS);
+        cp_async_commit();
+        cp_async_wait1();
+        __syncthreads();
+        const FvTile T = fv_tile(L, t);
+        const FwdVJob& J = L.job[T.jb];
+        const InT* in = inbuf + buf * FV_NR * FV_THREADS;
+        /* vertical lifting, one column pair per thread */
+        const int cp = threadIdx.x;
+        if (cp < T.ncp) {
+            int32_t a[FV_NR], b[FV_NR];
+#pragma unroll
+            for (int k = 0; k < FV_NR; k++) {
+                const InT v = in[k * FV_THREADS + cp];
+                if (SRC == SRC_I32) {
+                    a[k] = ((const int2*)&v)->x;
+                    b[k] = ((const int2*)&v)->y;
                 } else {
-                    for (int q = 0; q < 4; q++)
-                        if (jj + q < w1) ll[jj + q] = sv[q];
+                    const uint32_t r = *(const uint32_t*)&v;
+                    a[k] = scale_in<SRC>(r & 0xffffu, depth);
+                    b[k] = scale_in<SRC>(r >> 16, depth);
                 }
-            });
-        } else {
-            const int row = r0 + r - rc;
-            const BandRow blh = band_row(bands[J.b_lh], row, coef, gcli);
-            const BandRow bhh = band_row(bands[J.b_hh], row, coef, gcli);
-            warp_lift_fwd(&sH[r - rc][4], npairs, [&](int j, const int32_t* sv, const int32_t* d) {
-                emit4(blh, jc + j, sv[0], sv[1], sv[2], sv[3]);
-                emit4(bhh, jc + j, d[0], d[1], d[2], d[3]);
-            });
+            }
+            int32_t hpa = a[1] - ((a[0] + a[2]) >> 1), hpb = b[1] - ((b[0] + b[2]) >> 1);
+#pragma unroll
+            for (int k = 0; k < FV_ROWPAIRS; k++) {
+                const int e = 2 + 2 * k; /* x[2i] of pair r0 + k */
+                const int32_t ha = a[e + 1] - ((a[e] + a[e + 2]) >> 1), hb = b[e + 1] - ((b[e] + b[e + 2]) >> 1);
+                const int32_t la = a[e] + ((hpa + ha + 2) >> 2), lb = b[e] + ((hpb + hb + 2) >> 2);
+                *(int2*)&sL[k][2 + 2 * cp] = make_int2(la, lb);
+                *(int2*)&sH[k][2 + 2 * cp] = make_int2(ha, hb);
+                hpa = ha;
+                hpb = hb;
+            }
         }
+        __syncthreads();
+
+        /* horizontal lifting, one warp per row; the tile's output pairs are
+         * j in [c0/2, c0/2 + npairs) of the level's bands */
+        const int w1 = (J.w + 1) >> 1;
+        const int jc = T.c0 >> 1;
+        for (int r = warp; r < T.rc + T.hc; r += FV_THREADS / 32) {
+            if (r < T.rc) {
+                const int row = T.r0 + r;
+                const BandRow bhl = band_row(bands[J.b_hl], row, coef, gcli);
+                int32_t* ll = J.ll + (long long)row * J.ll_pitch;
+                warp_lift_fwd(&sL[r][4], T.npairs, [&](int j, const int32_t* sv, const int32_t* d) {
+                    const int jj = jc + j;
+                    emit4(bhl, jj, d[0], d[1], d[2], d[3]);
+                    if (jj + 3 < w1) {
+                        *(int4*)(ll + jj) = make_int4(sv[0], sv[1], sv[2], sv[3]);
+                    } else {
+                        for (int q = 0; q < 4; q++)
+                            if (jj + q < w1) ll[jj + q] = sv[q];
+                    }
+                });
+            } else {
+                const int row = T.r0 + r - T.rc;
+                const BandRow blh = band_row(bands[J.b_lh], row, coef, gcli);
+                const BandRow bhh = band_row(bands[J.b_hh], row, coef, gcli);
+                warp_lift_fwd(&sH[r - T.rc][4], T.npairs, [&](int j, const int32_t* sv, const int32_t* d) {
+                    emit4(blh, jc + j, sv[0], sv[1], sv[2], sv[3]);
+                    emit4(bhh, jc + j, d[0], d[1], d[2], d[3]);
+                });
+            }
+        }
+        __syncthreads();
+        buf ^= 1;
     }
 }
 
@@ -330,16 +415,30 @@ extern "C" int jxs_fwd_v_tile_rows(void) { return FV_ROWPAIRS; }
 extern "C" int jxs_fwd_v_tile_cols(void) { return FV_COLS; }
 extern "C" int jxs_fwd_h_max_rows_per_block(void) { return FH_MAX_WARPS; }
 
-extern "C" cudaError_t jxs_launch_fwd_v(const FwdVLaunch* L, int src_kind, int nblocks, const jxs_band_t* bands, uint16_t* coef,
+template <int SRC>
+static cudaError_t launch_v(const FwdVLaunch* L, int ntiles, const jxs_band_t* bands, uint16_t* coef, uint8_t* gcli, cudaStream_t st) {
+    const size_t smem = 2 * FV_NR * FV_THREADS * sizeof(typename FvIn<SRC>::T);
+    cudaError_t e = cudaFuncSetAttribute(fwd_v_kernel<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd_v_kernel<SRC>, FV_THREADS, smem)) != cudaSuccess) return e;
+    int blocks = sms * (per_sm > 0 ? per_sm : 1);
+    if (blocks > ntiles) blocks = ntiles;
+    fwd_v_kernel<SRC><<<blocks, FV_THREADS, smem, st>>>(*L, bands, coef, gcli);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t jxs_launch_fwd_v(const FwdVLaunch* L, int src_kind, int ntiles, const jxs_band_t* bands, uint16_t* coef,
                                         uint8_t* gcli, cudaStream_t st) {
     switch (src_kind) {
-    case SRC_I32: fwd_v_kernel<SRC_I32><<<nblocks, FV_THREADS, 0, st>>>(*L, bands, coef, gcli); break;
-    case SRC_U8: fwd_v_kernel<SRC_U8><<<nblocks, FV_THREADS, 0, st>>>(*L, bands, coef, gcli); break;
-    case SRC_U16: fwd_v_kernel<SRC_U16><<<nblocks, FV_THREADS, 0, st>>>(*L, bands, coef, gcli); break;
-    case SRC_PK8: fwd_v_kernel<SRC_PK8><<<nblocks, FV_THREADS, 0, st>>>(*L, bands, coef, gcli); break;
-    default: fwd_v_kernel<SRC_PK16><<<nblocks, FV_THREADS, 0, st>>>(*L, bands, coef, gcli); break;
+    case SRC_I32: return launch_v<SRC_I32>(L, ntiles, bands, coef, gcli, st);
+    case SRC_U8: return launch_v<SRC_U8>(L, ntiles, bands, coef, gcli, st);
+    case SRC_U16: return launch_v<SRC_U16>(L, ntiles, bands, coef, gcli, st);
+    case SRC_PK8: return launch_v<SRC_PK8>(L, ntiles, bands, coef, gcli, st);
+    default: return launch_v<SRC_PK16>(L, ntiles, bands, coef, gcli, st);
     }
-    return cudaGetLastError();
 }
 
 template <int SRC>

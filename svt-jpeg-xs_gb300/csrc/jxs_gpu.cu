@@ -354,6 +354,7 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
             J.first_block = blocks;
             blocks += J.col_tiles * (int)div_up((h + 1) / 2, vrows);
         }
+        L.ntiles = blocks;
         CK(jxs_launch_fwd_v(&L, v == 0 ? level0_kind : SRC_I32, blocks, dev_bands(e->dcfg), s->coef, s->gcli, st));
     }
     for (int pass = 0; pass < 2; pass++) {

@@ -64,6 +64,7 @@ struct FwdVJob {
 };
 struct FwdVLaunch {
     int njobs, depth;
+    int ntiles;             /* tiles of all jobs; job j owns [first_block, next job's first_block) */
     FwdVJob job[JXS_MAXC];
 };
 
