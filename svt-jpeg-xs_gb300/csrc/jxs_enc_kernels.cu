@@ -3,8 +3,9 @@
  *
  *  rc_cost_kernel   per precinct row: GCLI histograms and the byte cost of
  *                   every (quantization, refinement) candidate.
- *  rc_select_kernel per slice: the reference's sequential budget carry and
- *                   binary searches, replayed over the cost table.
+ *                   The block that completes a slice then replays the
+ *                   reference's sequential budget carry and binary searches
+ *                   for that slice over the cost tables.
  *  pack_kernel      per precinct row: quantization and bit packing at
  *                   prefix-summed bit offsets into a shared-memory copy of the
  *                   precinct, then one coalesced copy to the codestream.
@@ -26,6 +27,157 @@
 #define FULL 0xffffffffu
 #define RC_THREADS 512
 #define RC_WARPS (RC_THREADS / 32)
+#define RC_AREA_WORDS (5 * JXS_MAXBLINES * 16)
+
+/* binary_search_init / binary_search_next_step (BinarySearch.c:9-78) */
+struct BSearch {
+    int beg, end, step, best, last, below;
+};
+DEV void bs_init(BSearch& s, int beg, int end, int below, int step) {
+    s.beg = beg; s.end = end; s.below = below; s.best = -1; s.last = -1;
+    s.step = step ? step : (end - beg) / 2;
+}
+enum { BS_BEGIN = 0, BS_TOO_SMALL, BS_TOO_BIG, BS_OUT_OF_RANGE };
+enum { BS_CONTINUE = 0, BS_FOUND, BS_ERROR };
+DEV int bs_next(BSearch& s, int res, int* out) {
+    if (res == BS_TOO_SMALL) {
+        if (s.below && (s.best == -1 || s.best < s.last)) s.best = s.last;
+        if (s.end >= s.last + 1) s.beg = s.last + 1;
+        else {
+            if (s.best == -1) return BS_ERROR;
+            *out = s.best;
+            return BS_FOUND;
+        }
+    } else if (res == BS_TOO_BIG || res == BS_OUT_OF_RANGE) {
+        if (res == BS_TOO_BIG && !s.below && (s.best == -1 || s.best > s.last)) s.best = s.last;
+        if (s.beg <= s.last - 1) s.end = s.last - 1;
+        else {
+            if (s.best == -1) return BS_ERROR;
+            *out = s.best;
+            return BS_FOUND;
+        }
+    }
+    if (s.step > s.end - s.beg) s.step = (s.end - s.beg + 1) / 2;
+    s.last = s.step + s.beg;
+    *out = s.last;
+    return BS_CONTINUE;
+}
+
+/* One slice's precinct budgets with the padding carry of rate-control
+ * mode 1 (PackStageProcess.c:600-684, 293-309) and rate_control_precinct
+ * (RateControl.c:1259-1333) with its binary searches (:889-1083), evaluated
+ * on the slice's cost tables.  Run by a whole block: the tables of up to
+ * `area_words / (nq * nr)` precincts are read (through L2) into `area` at a
+ * time; thread 0 then runs their searches in order. */
+DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* __restrict__ cost, uint32_t* area,
+                      uint32_t area_words, PrecRC* __restrict__ rc, int* __restrict__ status) {
+    __shared__ uint32_t s_carry, s_run;
+    __shared__ int s_err;
+    __shared__ uint32_t s_empty[32];
+    if (threadIdx.x < 32) s_empty[threadIdx.x] = cfg->empty[threadIdx.x];
+    const int last_slice = (s + 1 == (int)cfg->nslices);
+    const uint32_t slice_budget = cfg->slice_size[s] - 6 - (last_slice ? 2 : 0);
+    const uint32_t first_p = cfg->pps * s;
+    const uint32_t nprec = last_slice ? cfg->np - first_p : cfg->pps;
+    uint32_t min_b = slice_budget / nprec;
+    uint32_t left = slice_budget - min_b * nprec;
+    uint32_t first_b = min_b;
+    if (cfg->rc_mode == 1) {
+        first_b = min(slice_budget, first_b * 110 / 100);
+        if (nprec > 1) {
+            min_b = (slice_budget - first_b) / (nprec - 1);
+            left = slice_budget - min_b * (nprec - 1) - first_b;
+        } else {
+            left = 0;
+        }
+    }
+    if (threadIdx.x == 0) {
+        s_carry = 0;
+        s_run = cfg->slice_begin[s] + 6;
+        s_err = 0;
+    }
+    const int nq = cfg->max_q + 1, nr = cfg->max_r + 1, nt = nq * nr;
+    const int max_q = cfg->max_q, max_r = cfg->max_r, rc_mode = (int)cfg->rc_mode;
+    const uint32_t np_all = cfg->np, hdrs0 = cfg->hdrs_bytes[0], hdrs1 = cfg->hdrs_bytes[1];
+    const uint32_t chunk = area_words / (uint32_t)nt;
+    for (uint32_t c0 = 0; c0 < nprec; c0 += chunk) {
+        const uint32_t cnt = min(chunk, nprec - c0);
+        __syncthreads();
+        if (s_err) break;
+        for (int e = threadIdx.x; e < (int)cnt * nt; e += blockDim.x) {
+            const int i = e / nt, qr = e - i * nt, q = qr / nr, r = qr - q * nr;
+            area[e] = __ldcg(cost + (uint64_t)(first_p + c0 + i) * 1024 + q * 32 + r);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (uint32_t ii = 0; ii < cnt && !s_err; ii++) {
+                const uint32_t i = c0 + ii;
+                const uint32_t p = first_p + i;
+                const uint32_t* T = area + ii * nt;
+                const int last = (p + 1 >= np_all);
+                const uint32_t budget = (i == 0 ? first_b : min_b) + (i < left ? 1 : 0) + s_carry;
+                const uint32_t hdr = last ? hdrs1 : hdrs0;
+                int err = 0;
+                if (budget > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
+                else if (budget <= hdr) err = JXS_E_UNDEFINED;
+                int q = 0, r = 0;
+                uint32_t data = 0;
+                if (!err) {
+                    const uint32_t avail = budget - hdr;
+                    BSearch bs;
+                    int step = 6;
+                    if (step > max_q) step = 0;
+                    bs_init(bs, 0, max_q, 0, step);
+                    int res, next = BS_BEGIN, v = 0;
+                    while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
+                        if (s_empty[v] & 1u) next = BS_OUT_OF_RANGE;
+                        else next = T[v * nr] > avail ? BS_TOO_SMALL : BS_TOO_BIG;
+                    }
+                    if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
+                    q = v;
+                    if (!err) {
+                        step = 6;
+                        if (step >= max_r) step = 0;
+                        bs_init(bs, 0, max_r, 1, step);
+                        next = BS_BEGIN;
+                        while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
+                            if ((s_empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
+                            else next = T[q * nr + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
+                        }
+                        if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
+                        r = v;
+                        data = T[q * nr + r];
+                    }
+                    if (!err) {
+                        uint32_t padding = avail - data;
+                        uint32_t total = budget;
+                        if (rc_mode == 1 && i + 1 < nprec) {
+                            total -= padding;
+                            s_carry = padding;
+                        } else {
+                            s_carry = 0;
+                        }
+                        PrecRC o;
+                        o.total_bytes = total;
+                        o.offset = s_run;
+                        o.data_bytes = data;
+                        o.q = (uint8_t)q;
+                        o.r = (uint8_t)r;
+                        o.first_in_slice = (uint8_t)(i == 0);
+                        o.pad = 0;
+                        rc[p] = o;
+                        s_run += total;
+                    }
+                }
+                if (err) {
+                    printf("jxs rc: slice %d precinct %u budget %u: error 0x%x\\n", s, p, budget, (unsigned)err);
+                    s_err = err;
+                    JXS_STATUS_SET(status, err);
+                }
+            }
+        }
+    }
+}
 
 /* Byte cost of every (quantization, refinement) candidate of one precinct
  * row: rate_control_lut_fill, rate_control_calculate_band_best_method and
@@ -41,10 +193,18 @@
  *               separately, raw fallback when cheaper; summed over packets
  *               for every (Q, R). */
 __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
-                                                           uint32_t* __restrict__ cost) {
-    __shared__ uint32_t hist[JXS_MAXBLINES][16], shist[JXS_MAXBLINES][16];
+                                                           uint32_t* __restrict__ cost, uint32_t* __restrict__ slice_done,
+                                                           PrecRC* __restrict__ rc, int* __restrict__ status) {
+    /* per band line: GCLI and significance-maximum histograms, then per gtli
+     * data / GCLI bits without and with significance; the area is reused by
+     * the slice selection at the end */
+    __shared__ __align__(16) uint32_t s_area[RC_AREA_WORDS];
+    uint32_t(*hist)[16] = (uint32_t(*)[16])s_area;
+    uint32_t(*shist)[16] = (uint32_t(*)[16])(s_area + JXS_MAXBLINES * 16);
+    uint32_t(*tdat)[16] = (uint32_t(*)[16])(s_area + 2 * JXS_MAXBLINES * 16);
+    uint32_t(*tnos)[16] = (uint32_t(*)[16])(s_area + 3 * JXS_MAXBLINES * 16);
+    uint32_t(*tsig)[16] = (uint32_t(*)[16])(s_area + 4 * JXS_MAXBLINES * 16);
     __shared__ int pmax[JXS_MAXBLINES];
-    __shared__ uint32_t tdat[JXS_MAXBLINES][16], tnos[JXS_MAXBLINES][16], tsig[JXS_MAXBLINES][16];
     __shared__ uint32_t cn[JXS_MAXBL][16], cs[JXS_MAXBL][16];
     __shared__ uint16_t meth[JXS_MAXBL];
     __shared__ uint8_t lgain[JXS_MAXBLINES], lprio[JXS_MAXBLINES], lfb[JXS_MAXBLINES];
@@ -225,158 +385,20 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
             out[q * 32 + r] = run;
         }
     }
-}
-
-/* binary_search_init / binary_search_next_step (BinarySearch.c:9-78) */
-struct BSearch {
-    int beg, end, step, best, last, below;
-};
-DEV void bs_init(BSearch& s, int beg, int end, int below, int step) {
-    s.beg = beg; s.end = end; s.below = below; s.best = -1; s.last = -1;
-    s.step = step ? step : (end - beg) / 2;
-}
-enum { BS_BEGIN = 0, BS_TOO_SMALL, BS_TOO_BIG, BS_OUT_OF_RANGE };
-enum { BS_CONTINUE = 0, BS_FOUND, BS_ERROR };
-DEV int bs_next(BSearch& s, int res, int* out) {
-    if (res == BS_TOO_SMALL) {
-        if (s.below && (s.best == -1 || s.best < s.last)) s.best = s.last;
-        if (s.end >= s.last + 1) s.beg = s.last + 1;
-        else {
-            if (s.best == -1) return BS_ERROR;
-            *out = s.best;
-            return BS_FOUND;
-        }
-    } else if (res == BS_TOO_BIG || res == BS_OUT_OF_RANGE) {
-        if (res == BS_TOO_BIG && !s.below && (s.best == -1 || s.best > s.last)) s.best = s.last;
-        if (s.beg <= s.last - 1) s.end = s.last - 1;
-        else {
-            if (s.best == -1) return BS_ERROR;
-            *out = s.best;
-            return BS_FOUND;
-        }
-    }
-    if (s.step > s.end - s.beg) s.step = (s.end - s.beg + 1) / 2;
-    s.last = s.step + s.beg;
-    *out = s.last;
-    return BS_CONTINUE;
-}
-
-/* One block per slice: the slice's precinct budgets with the padding carry
- * of rate-control mode 1 (PackStageProcess.c:600-684, 293-309) and
- * rate_control_precinct (RateControl.c:1259-1333) with its binary searches
- * (:889-1083), evaluated on the cost tables.  The tables of up to RS_CHUNK
- * precincts are loaded in one go; thread 0 then runs their searches in
- * order. */
-#define RS_CHUNK 8
-__global__ void __launch_bounds__(128) rc_select_kernel(const jxs_cfg_t* __restrict__ cfg, const uint32_t* __restrict__ cost,
-                                                        PrecRC* __restrict__ rc, int* __restrict__ status) {
-    extern __shared__ uint32_t tbl[]; /* [RS_CHUNK][nq][nr] */
-    __shared__ uint32_t s_carry, s_run;
-    __shared__ int s_err;
-    __shared__ uint32_t s_empty[32];
-    const int s = blockIdx.x;
-    if (threadIdx.x < 32) s_empty[threadIdx.x] = cfg->empty[threadIdx.x];
-    const int last_slice = (s + 1 == (int)cfg->nslices);
-    const uint32_t slice_budget = cfg->slice_size[s] - 6 - (last_slice ? 2 : 0);
+    /* the block that completes a slice runs the slice's selection: tables
+     * published with a fence, blocks counted per slice */
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    const uint32_t s = (uint32_t)p / cfg->pps;
     const uint32_t first_p = cfg->pps * s;
-    const uint32_t nprec = last_slice ? cfg->np - first_p : cfg->pps;
-    uint32_t min_b = slice_budget / nprec;
-    uint32_t left = slice_budget - min_b * nprec;
-    uint32_t first_b = min_b;
-    if (cfg->rc_mode == 1) {
-        first_b = min(slice_budget, first_b * 110 / 100);
-        if (nprec > 1) {
-            min_b = (slice_budget - first_b) / (nprec - 1);
-            left = slice_budget - min_b * (nprec - 1) - first_b;
-        } else {
-            left = 0;
-        }
-    }
-    if (threadIdx.x == 0) {
-        s_carry = 0;
-        s_run = cfg->slice_begin[s] + 6;
-        s_err = 0;
-    }
-    const int nq = cfg->max_q + 1, nr = cfg->max_r + 1, nt = nq * nr;
-    const int max_q = cfg->max_q, max_r = cfg->max_r, rc_mode = (int)cfg->rc_mode;
-    const uint32_t np_all = cfg->np, hdrs0 = cfg->hdrs_bytes[0], hdrs1 = cfg->hdrs_bytes[1];
-    for (uint32_t c0 = 0; c0 < nprec; c0 += RS_CHUNK) {
-        const uint32_t cnt = min((uint32_t)RS_CHUNK, nprec - c0);
-        __syncthreads();
-        if (s_err) break;
-        for (int e = threadIdx.x; e < (int)cnt * nt; e += blockDim.x) {
-            const int i = e / nt, qr = e - i * nt, q = qr / nr, r = qr - q * nr;
-            tbl[e] = cost[(uint64_t)(first_p + c0 + i) * 1024 + q * 32 + r];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (uint32_t ii = 0; ii < cnt && !s_err; ii++) {
-                const uint32_t i = c0 + ii;
-                const uint32_t p = first_p + i;
-                const uint32_t* T = tbl + ii * nt;
-                const int last = (p + 1 >= np_all);
-                const uint32_t budget = (i == 0 ? first_b : min_b) + (i < left ? 1 : 0) + s_carry;
-                const uint32_t hdr = last ? hdrs1 : hdrs0;
-                int err = 0;
-                if (budget > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
-                else if (budget <= hdr) err = JXS_E_UNDEFINED;
-                int q = 0, r = 0;
-                uint32_t data = 0;
-                if (!err) {
-                    const uint32_t avail = budget - hdr;
-                    BSearch bs;
-                    int step = 6;
-                    if (step > max_q) step = 0;
-                    bs_init(bs, 0, max_q, 0, step);
-                    int res, next = BS_BEGIN, v = 0;
-                    while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
-                        if (s_empty[v] & 1u) next = BS_OUT_OF_RANGE;
-                        else next = T[v * nr] > avail ? BS_TOO_SMALL : BS_TOO_BIG;
-                    }
-                    if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
-                    q = v;
-                    if (!err) {
-                        step = 6;
-                        if (step >= max_r) step = 0;
-                        bs_init(bs, 0, max_r, 1, step);
-                        next = BS_BEGIN;
-                        while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
-                            if ((s_empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
-                            else next = T[q * nr + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
-                        }
-                        if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
-                        r = v;
-                        data = T[q * nr + r];
-                    }
-                    if (!err) {
-                        uint32_t padding = avail - data;
-                        uint32_t total = budget;
-                        if (rc_mode == 1 && i + 1 < nprec) {
-                            total -= padding;
-                            s_carry = padding;
-                        } else {
-                            s_carry = 0;
-                        }
-                        PrecRC o;
-                        o.total_bytes = total;
-                        o.offset = s_run;
-                        o.data_bytes = data;
-                        o.q = (uint8_t)q;
-                        o.r = (uint8_t)r;
-                        o.first_in_slice = (uint8_t)(i == 0);
-                        o.pad = 0;
-                        rc[p] = o;
-                        s_run += total;
-                    }
-                }
-                if (err) {
-                    printf("jxs rc: slice %d precinct %u budget %u: error 0x%x\n", s, p, budget, (unsigned)err);
-                    s_err = err;
-                    JXS_STATUS_SET(status, err);
-                }
-            }
-        }
-    }
+    const uint32_t nprec = (s + 1 == cfg->nslices) ? cfg->np - first_p : cfg->pps;
+    if (threadIdx.x == 0) s_last = atomicAdd(&slice_done[s], 1u) + 1 == nprec;
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    select_slice(cfg, (int)s, cost, s_area, RC_AREA_WORDS, rc, status);
+    if (threadIdx.x == 0) slice_done[s] = 0; /* ready for the next frame */
 }
 
 /* ------------------------------------------------------------------------ */
@@ -880,9 +902,9 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __
 /* host-side launchers                                                       */
 /* ------------------------------------------------------------------------ */
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
-                                     PrecRC* rc, int* status, cudaStream_t st) {
-    rc_cost_kernel<<<np, RC_THREADS, 0, st>>>(dcfg, gcli, cost);
-    rc_select_kernel<<<nslices, 128, RS_CHUNK * 32 * 32 * sizeof(uint32_t), st>>>(dcfg, cost, rc, status);
+                                     uint32_t* slice_done, PrecRC* rc, int* status, cudaStream_t st) {
+    (void)nslices;
+    rc_cost_kernel<<<np, RC_THREADS, 0, st>>>(dcfg, gcli, cost, slice_done, rc, status);
     return cudaGetLastError();
 }
 

@@ -257,7 +257,8 @@ DEV void fv_stage(const FwdVLaunch& L, int t, typename FvIn<SRC>::T* in) {
 
 /* Persistent: each block walks tiles t = blockIdx.x, + gridDim.x, ...; the
  * next tile's input is staged (asynchronous copies) while the current one is
- * lifted. */
+ * lifted.  With `persistent` false (int32 low bands, still in L2) the grid
+ * has one block per tile and a single buffer. */
 template <int SRC>
 __global__ void __launch_bounds__(FV_THREADS, 6) fwd_v_kernel(const __grid_constant__ FwdVLaunch L, const jxs_band_t* __restrict__ bands,
                                                            uint16_t* __restrict__ coef, uint8_t* __restrict__ gcli) {
@@ -268,12 +269,13 @@ __global__ void __launch_bounds__(FV_THREADS, 6) fwd_v_kernel(const __grid_const
     __shared__ __align__(16) int32_t sH[FV_ROWPAIRS][FV_SROW];
     const int depth = L.depth;
     const int warp = threadIdx.x >> 5;
+    const bool persistent = gridDim.x < (unsigned)L.ntiles;
     int t = blockIdx.x, buf = 0;
     if (t < L.ntiles) fv_stage<SRC>(L, t, inbuf);
     cp_async_commit();
     for (; t < L.ntiles; t += gridDim.x) {
         const int tn = t + gridDim.x;
-        if (tn < L.ntiles) fv_stage<SRC>(L, tn, inbuf + (buf ^ 1) * FV_NR * FV_THREADS);
+        if (persistent && tn < L.ntiles) fv_stage<SRC>(L, tn, inbuf + (buf ^ 1) * FV_NR * FV_THREADS);
         cp_async_commit();
         cp_async_wait1();
         __syncthreads();
@@ -417,14 +419,17 @@ extern "C" int jxs_fwd_h_max_rows_per_block(void) { return FH_MAX_WARPS; }
 
 template <int SRC>
 static cudaError_t launch_v(const FwdVLaunch* L, int ntiles, const jxs_band_t* bands, uint16_t* coef, uint8_t* gcli, cudaStream_t st) {
-    const size_t smem = 2 * FV_NR * FV_THREADS * sizeof(typename FvIn<SRC>::T);
+    /* int32 inputs (the previous level's low band, in L2): one block per
+     * tile, one buffer; sample planes: persistent, double-buffered */
+    const bool persistent = SRC != SRC_I32;
+    const size_t smem = (persistent ? 2 : 1) * FV_NR * FV_THREADS * sizeof(typename FvIn<SRC>::T);
     cudaError_t e = cudaFuncSetAttribute(fwd_v_kernel<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd_v_kernel<SRC>, FV_THREADS, smem)) != cudaSuccess) return e;
-    int blocks = sms * (per_sm > 0 ? per_sm : 1);
+    int blocks = persistent ? sms * (per_sm > 0 ? per_sm : 1) : ntiles;
     if (blocks > ntiles) blocks = ntiles;
     fwd_v_kernel<SRC><<<blocks, FV_THREADS, smem, st>>>(*L, bands, coef, gcli);
     return cudaGetLastError();

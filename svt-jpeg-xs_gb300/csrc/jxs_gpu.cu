@@ -29,7 +29,7 @@ extern "C" int jxs_fwd_v_tile_rows(void);
 extern "C" int jxs_fwd_v_tile_cols(void);
 extern "C" int jxs_fwd_h_max_rows_per_block(void);
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
-                                     PrecRC* rc, int* status, cudaStream_t st);
+                                     uint32_t* slice_done, PrecRC* rc, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
                                        const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
@@ -151,6 +151,7 @@ struct EncSlot {
     int32_t* ll[2][JXS_MAXC];   /* int32 low band after vertical level 0 / 1 */
     int ll_pitch[2][JXS_MAXC];
     uint32_t* cost;
+    uint32_t* slice_done;   /* per slice: cost blocks finished (back to 0 after each frame) */
     PrecRC* rc;
     int* status;
     uint8_t* out_stage;
@@ -206,6 +207,8 @@ static int32_t enc_slot_alloc(jxs_gpu_enc_t* e, EncSlot* s) {
         }
     }
     CK(cudaMalloc(&s->cost, (size_t)c->np * 1024 * sizeof(uint32_t)));
+    CK(cudaMalloc(&s->slice_done, (size_t)c->nslices * sizeof(uint32_t)));
+    CK(cudaMemset(s->slice_done, 0, (size_t)c->nslices * sizeof(uint32_t)));
     CK(cudaMalloc(&s->rc, (size_t)c->np * sizeof(PrecRC)));
     CK(cudaMalloc(&s->status, 64));
     CK(cudaMalloc(&s->out_stage, c->lcod + 64));
@@ -223,6 +226,7 @@ static void enc_slot_free(EncSlot* s) {
     for (int v = 0; v < 2; v++)
         for (int k = 0; k < JXS_MAXC; k++) cudaFree(s->ll[v][k]);
     cudaFree(s->cost);
+    cudaFree(s->slice_done);
     cudaFree(s->rc);
     cudaFree(s->status);
     cudaFree(s->out_stage);
@@ -402,7 +406,7 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
         CK(jxs_launch_fwd_h(&L, pass == 0 ? SRC_I32 : level0_kind, blocks, dev_bands(e->dcfg), s->coef, s->gcli, st));
     }
     TMARK(2);
-    CK(jxs_launch_rc(e->dcfg, c->np, c->nslices, s->gcli, s->cost, s->rc, s->status, st));
+    CK(jxs_launch_rc(e->dcfg, c->np, c->nslices, s->gcli, s->cost, s->slice_done, s->rc, s->status, st));
     TMARK(3);
     const int out_dev = jxs_gpu_is_device_ptr(out);
     uint8_t* dst = out_dev ? out : s->out_stage;
