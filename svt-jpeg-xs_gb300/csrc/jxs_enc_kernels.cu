@@ -252,29 +252,33 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
     for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) lraw[k] = cfg->raw_bytes[last][k];
     __syncthreads();
 
-    /* histograms: per lane, 8-bit counters packed four to a register,
-     * summed over the warp every 4 iterations (at most 128 per bin) */
+    /* histograms: each lane 4 consecutive groups (one 4-byte load), 8-bit
+     * counters packed four to a register, summed over the warp per 128
+     * groups (at most 128 per bin) */
     for (uint32_t sidx = warp; sidx < nseg; sidx += RC_WARPS) {
         const jxs_seg_t sg = segs[sidx];
         const uint32_t x = sg.bl;
         const uint8_t* grow = gcli + s_grow[x];
         const uint32_t gend = min(sg.g0 + SG, bls[x].gcli_w);
-        uint32_t h[4] = {0, 0, 0, 0}, sh[4] = {0, 0, 0, 0};
-        int it = 0;
-        for (uint32_t base = sg.g0; base < gend; base += 32) {
-            const uint32_t g = base + lane;
-            const bool valid = g < gend;
-            const uint32_t v = valid ? grow[g] : 0u;
-            const uint32_t inc = valid ? 1u << (8 * (v & 3)) : 0u;
+        for (uint32_t base = sg.g0; base < gend; base += 128) {
+            const uint32_t g = base + 4 * lane;
+            const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
+            const uint32_t w4 = nv ? *(const uint32_t*)(grow + g) : 0u;
+            uint32_t h[4] = {0, 0, 0, 0}, m = 0;
 #pragma unroll
-            for (int r = 0; r < 4; r++) h[r] += (v >> 2) == (uint32_t)r ? inc : 0u;
-            uint32_t mx = v;
-            mx = max(mx, __shfl_xor_sync(FULL, mx, 1));
-            mx = max(mx, __shfl_xor_sync(FULL, mx, 2));
-            mx = max(mx, __shfl_xor_sync(FULL, mx, 4));
-            const uint32_t vb = __ballot_sync(FULL, valid);
-            if ((lane & 7) == 0 && valid) {
-                if (__popc((vb >> lane) & 0xffu) == 8) {
+            for (int k = 0; k < 4; k++) {
+                const uint32_t v = (w4 >> (8 * k)) & 255u;
+                const uint32_t inc = k < (int)nv ? 1u << (8 * (v & 3)) : 0u;
+#pragma unroll
+                for (int r = 0; r < 4; r++) h[r] += (v >> 2) == (uint32_t)r ? inc : 0u;
+                if (k < (int)nv) m = max(m, v);
+            }
+            /* significance group: 8 groups in lanes 2i, 2i+1 */
+            const uint32_t mx = max(m, __shfl_xor_sync(FULL, m, 1));
+            const uint32_t nvp = nv + __shfl_xor_sync(FULL, nv, 1);
+            uint32_t sh[4] = {0, 0, 0, 0};
+            if (!(lane & 1) && nv) {
+                if (nvp == 8) {
                     const uint32_t si = 1u << (8 * (mx & 3));
 #pragma unroll
                     for (int r = 0; r < 4; r++) sh[r] += (mx >> 2) == (uint32_t)r ? si : 0u;
@@ -282,18 +286,13 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
                     pmax[x] = (int)mx; /* the partial last significance group of the line */
                 }
             }
-            if (++it == 4 || base + 32 >= gend) {
-                it = 0;
 #pragma unroll
-                for (int r = 0; r < 4; r++) {
-                    const uint32_t hs = __reduce_add_sync(FULL, h[r]), ss = __reduce_add_sync(FULL, sh[r]);
-                    if (lane < 4) {
-                        const uint32_t c = (hs >> (8 * lane)) & 0xffu, cs2 = (ss >> (8 * lane)) & 0xffu;
-                        if (c) atomicAdd(&hist[x][4 * r + lane], c);
-                        if (cs2) atomicAdd(&shist[x][4 * r + lane], cs2);
-                    }
-                    h[r] = 0;
-                    sh[r] = 0;
+            for (int r = 0; r < 4; r++) {
+                const uint32_t hs = __reduce_add_sync(FULL, h[r]), ss = __reduce_add_sync(FULL, sh[r]);
+                if (lane < 4) {
+                    const uint32_t c = (hs >> (8 * lane)) & 0xffu, cs2 = (ss >> (8 * lane)) & 0xffu;
+                    if (c) atomicAdd(&hist[x][4 * r + lane], c);
+                    if (cs2) atomicAdd(&shist[x][4 * r + lane], cs2);
                 }
             }
         }
