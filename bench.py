@@ -8,14 +8,17 @@ produced.  Every codestream and decoded frame of the timed region is checked
 bit-exact against the first (warm-up) pass.
 
 value  : luma Gpixel/s of encode + decode with inputs and outputs resident in
-         device memory, timed with CUDA events on the stream the codec runs
-         on; inputs (33 MB per frame, 60 frames) exceed the 129 MB L2.
+         device memory. `--streams` encoder/decoder pairs each run on their
+         own CUDA stream (frame i of a step on pair i % streams); the time is
+         taken with CUDA events from an event on the main stream that every
+         pair's stream waits for to an event recorded after joining them.
+         Inputs (33 MB per frame, 60 frames) exceed the 129 MB L2.
 e2e    : the same metric through the public C API with host buffers (page-
          locked), host-to-device and device-to-host copies inside the timed
          region, several frames in flight.
-roofline: the dominant stage (per-stage CUDA-event times) against the
-         measured HBM copy bandwidth; bytes are the algorithmic bytes of
-         that stage.
+roofline: the dominant stage (per-stage CUDA-event times from a separate
+         single-stream pass) against the measured HBM copy bandwidth; bytes
+         are the algorithmic bytes of that stage.
 cpu_baseline: the CPU restatement of the reference algorithm (oracle) on the
          host cores, a bounded sample of the same workload.
 
@@ -52,6 +55,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=8, help="frames encoded and decoded per step")
+    ap.add_argument("--streams", type=int, default=3, help="encoder/decoder pairs, each on its own CUDA stream")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget (0: not measured)")
     ap.add_argument("--seq-frames", type=int, default=SEQ_FRAMES,
                     help="distinct frames of the stream cycled through (each 33 MB; 4 or more keep inputs above L2)")
@@ -203,65 +207,88 @@ def run_ours(args, rank, world, local):
     nseq = max(4, args.seq_frames)
     frames = make_frames(nseq)
     F = args.frames
-    enc = jxs.Encoder(W, H, DEPTH, jxs.FMT_YUV422, BPP)
-    lcod = enc.frame_bytes
+    NS = max(1, args.streams)
+    # NS encoder/decoder pairs, each bound to its own stream: frame i of a
+    # step goes to pair i % NS, so its encode and decode share a stream and
+    # the pairs overlap on the device
+    streams = [torch.cuda.Stream(device=dev) for _ in range(NS)]
+    encs = [jxs.Encoder(W, H, DEPTH, jxs.FMT_YUV422, BPP) for _ in range(NS)]
+    lcod = encs[0].frame_bytes
     # device-resident inputs and outputs
     d_in = [[torch.from_numpy(p).to(dev) for p in fr] for fr in frames]
     d_bs = [torch.zeros(lcod + 64, dtype=torch.uint8, device=dev) for _ in range(F)]
     d_out = [[torch.zeros_like(p) for p in d_in[0]] for _ in range(F)]
-    stream = torch.cuda.Stream(device=dev)
-    enc.set_stream(stream.cuda_stream)
-    # the first codestream initialises the decoder
-    first = enc.encode(frames[0])
-    dec = jxs.Decoder(first)
-    dec.set_stream(stream.cuda_stream)
+    # the first codestream initialises the decoders
+    first = encs[0].encode(frames[0])
+    decs = [jxs.Decoder(first) for _ in range(NS)]
+    for k in range(NS):
+        encs[k].set_stream(streams[k].cuda_stream)
+        decs[k].set_stream(streams[k].cuda_stream)
 
     def planes_of(ts):
         return [(t.data_ptr(), t.shape[1]) for t in ts]
 
-    def step(s):
-        # every call is queued on one stream: decode i follows encode i, and
-        # results are collected only when a codec's queue is full
+    def step(s, npairs):
+        # every call is queued on its pair's stream: decode i follows encode
+        # i, and results are collected only when a codec's queue is full
         base = (s * F) % nseq
-        pend = [0, 0]
+        pend = {}
 
-        def submit(codec, k, *a, **kw):
+        def submit(codec, *a, **kw):
             while True:
                 r = codec.send(*a, blocking=False, **kw)
                 if r != jxs.E_EMPTY_QUEUE:
                     assert r == 0, hex(r)
-                    pend[k] += 1
+                    pend[id(codec)] = pend.get(id(codec), 0) + 1
                     return
                 r, _ = codec.get()
                 assert r == 0, hex(r)
-                pend[k] -= 1
+                pend[id(codec)] -= 1
 
         for i in range(F):
-            submit(enc, 0, planes_of(d_in[(base + i) % nseq]), d_bs[i].data_ptr(), out_cap=lcod + 64)
-            submit(dec, 1, d_bs[i].data_ptr(), planes_of(d_out[i]), bs_size=lcod)
-        for k, codec in ((0, enc), (1, dec)):
-            while pend[k]:
+            k = i % npairs
+            submit(encs[k], planes_of(d_in[(base + i) % nseq]), d_bs[i].data_ptr(), out_cap=lcod + 64)
+            submit(decs[k], d_bs[i].data_ptr(), planes_of(d_out[i]), bs_size=lcod)
+        for codec in encs[:npairs] + decs[:npairs]:
+            while pend.get(id(codec), 0):
                 r, _ = codec.get()
                 assert r == 0, hex(r)
-                pend[k] -= 1
+                pend[id(codec)] -= 1
 
     for w in range(max(args.warmup, 1)):
-        step(w)
+        step(w, NS)
     torch.cuda.synchronize()
-    enc.set_timing(True)
-    dec.set_timing(True)
+    # per-stage CUDA-event times, one stream (pair 0 alone)
+    encs[0].set_timing(True)
+    decs[0].set_timing(True)
+    for s in range(max(3, args.steps // 4)):
+        step(args.warmup + s, 1)
+    torch.cuda.synchronize()
+    nenc, enc_ms = encs[0].read_timing()
+    ndec, dec_ms = decs[0].read_timing()
+    encs[0].set_timing(False)
+    decs[0].set_timing(False)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    # throughput: all pairs, timed from an event on the main stream that every
+    # pair's stream waits for, to one recorded after all of them
+    main = torch.cuda.current_stream(dev)
     clocks = ClockSampler(local)
     clocks.start()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
-    ev0.record(stream)
+    ev0.record(main)
+    for st in streams:
+        st.wait_event(ev0)
     t0 = time.perf_counter()
     for s in range(args.steps):
-        step(args.warmup + s)
-    ev1.record(stream)
+        step(args.warmup + s, NS)
+    for st in streams:
+        e = torch.cuda.Event()
+        e.record(st)
+        main.wait_event(e)
+    ev1.record(main)
     torch.cuda.synchronize()
     host_s = time.perf_counter() - t0
     clk = clocks.stop()
@@ -271,8 +298,6 @@ def run_ours(args, rank, world, local):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         dev_ms = float(t.item())
         torch.distributed.barrier()
-    nenc, enc_ms = enc.read_timing()
-    ndec, dec_ms = dec.read_timing()
     total_frames = args.steps * F * world
     value = total_frames * W * H / (dev_ms / 1e3) / 1e9
     # bit-exactness of the last timed step against the oracle
@@ -288,11 +313,11 @@ def run_ours(args, rank, world, local):
         assert err == 0 and all(np.array_equal(t.cpu().numpy(), w) for t, w in zip(d_out[i], want_planes)), \
             "decoded frame differs from the oracle"
 
-    # ---- e2e through the C API with host buffers
+    # ---- e2e through the C API with host buffers: pair 0 on its own slot
+    # streams (3 frames in flight)
+    enc, dec = encs[0], decs[0]
     enc.set_stream(None)
     dec.set_stream(None)
-    enc.set_timing(False)
-    dec.set_timing(False)
     def pinned_like(a):
         buf = torch.empty(a.shape, dtype=torch.from_numpy(a[:1]).dtype).pin_memory()
         buf.copy_(torch.from_numpy(a))
@@ -353,8 +378,8 @@ def run_ours(args, rank, world, local):
         r, _ = dec.get()
         assert r == 0
         lat_frame.append((time.perf_counter() - ts) * 1e3)
-    enc.close()
-    dec.close()
+    for codec in encs + decs:
+        codec.close()
 
     # ---- roofline of the dominant stage
     peak, peak_kind = measured_peak()
@@ -383,12 +408,14 @@ def run_ours(args, rank, world, local):
         cpu = {"value": n * W * H / el / 1e9, "unit": "Gpix/s", "cores": threads, "kind": "port",
                "sample": "%d frames encoded + decoded (%.1f s) with the CPU restatement of the reference algorithm" % (n, el)}
 
-    launches_per_frame = 5 + 3  # 2 transform levels + cost + select + pack; unpack + 2 inverse levels
+    # per frame: 2 vertical + 1 horizontal transform, rate control, pack;
+    # 2 precinct walks (device codestreams), unpack, 1 horizontal + 2 vertical inverse
+    launches_per_frame = 5 + 6
     line = {
         "metric": METRIC, "value": value, "unit": "Gpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic (seeded, integer-only generator; no dataset)",
-        "config": {"workload": WORKLOAD, "frames_per_step": F, "l2": "inputs 33 MB/frame cycling over %d frames (> L2)" % nseq,
+        "config": {"workload": WORKLOAD, "frames_per_step": F, "streams": NS, "l2": "inputs 33 MB/frame cycling over %d frames (> L2)" % nseq,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_val, "unit": "Gpix/s", "h2d_bytes_per_step": F * (in_bytes + lcod),
                 "d2h_bytes_per_step": F * (lcod + out_bytes), "p50_step_ms": 1e3 * statistics.median(lat),

@@ -33,6 +33,15 @@ extern "C" {
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_set_stream(svt_jpeg_xs_encoder_api_t* enc_api, void* cuda_stream);
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_set_stream(svt_jpeg_xs_decoder_api_t* dec_api, void* cuda_stream);
 
+/* Frame slot i of the handle runs on cuda_streams[i % count] (count = 0:
+ * back to the handle's own streams).  A handle keeps 3 frames in flight, so
+ * with 3 streams consecutive frames overlap on the device; an encoder and a
+ * decoder bound to the same streams put frame i of both on the same stream. */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_set_streams(svt_jpeg_xs_encoder_api_t* enc_api, void* const* cuda_streams,
+                                                                 uint32_t count);
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_set_streams(svt_jpeg_xs_decoder_api_t* dec_api, void* const* cuda_streams,
+                                                                 uint32_t count);
+
 /* Enabling resets the accumulated stage times. */
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_set_timing(svt_jpeg_xs_encoder_api_t* enc_api, uint32_t enable);
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_set_timing(svt_jpeg_xs_decoder_api_t* dec_api, uint32_t enable);

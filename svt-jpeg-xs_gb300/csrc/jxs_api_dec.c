@@ -406,6 +406,13 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_set_stream(svt_jpeg_xs_deco
     return SvtJxsErrorNone;
 }
 
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_set_streams(svt_jpeg_xs_decoder_api_t* dec_api, void* const* cuda_streams,
+                                                                 uint32_t count) {
+    if (!dec_api || !dec_api->private_ptr || (count && !cuda_streams)) return SvtJxsErrorBadParameter;
+    jxs_gpu_dec_set_streams(((dec_prv_t*)dec_api->private_ptr)->gpu, cuda_streams, (int)count);
+    return SvtJxsErrorNone;
+}
+
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_set_timing(svt_jpeg_xs_decoder_api_t* dec_api, uint32_t enable) {
     if (!dec_api || !dec_api->private_ptr) return SvtJxsErrorBadParameter;
     jxs_gpu_dec_set_timing(((dec_prv_t*)dec_api->private_ptr)->gpu, (int)enable);

@@ -256,6 +256,13 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_set_stream(svt_jpeg_xs_enco
     return SvtJxsErrorNone;
 }
 
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_set_streams(svt_jpeg_xs_encoder_api_t* enc_api, void* const* cuda_streams,
+                                                                 uint32_t count) {
+    if (!enc_api || !enc_api->private_ptr || (count && !cuda_streams)) return SvtJxsErrorBadParameter;
+    jxs_gpu_enc_set_streams(((enc_prv_t*)enc_api->private_ptr)->gpu, cuda_streams, (int)count);
+    return SvtJxsErrorNone;
+}
+
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_set_timing(svt_jpeg_xs_encoder_api_t* enc_api, uint32_t enable) {
     if (!enc_api || !enc_api->private_ptr) return SvtJxsErrorBadParameter;
     jxs_gpu_enc_set_timing(((enc_prv_t*)enc_api->private_ptr)->gpu, (int)enable);

@@ -170,14 +170,17 @@ struct jxs_gpu_enc {
     int nslots;
     EncSlot slot[8];
     uint32_t cap_words;
-    cudaStream_t user_stream;
+    cudaStream_t user_stream[8]; /* per slot; null: the slot's own stream */
     int timing;
     double stage_ms[ENC_STAGES];
     uint64_t timed_frames;
     std::mutex mu;
 };
 
-static inline cudaStream_t enc_stream(const jxs_gpu_enc_t* e, const EncSlot* s) { return e->user_stream ? e->user_stream : s->st; }
+static inline cudaStream_t enc_stream(const jxs_gpu_enc_t* e, const EncSlot* s) {
+    const cudaStream_t u = e->user_stream[s - e->slot];
+    return u ? u : s->st;
+}
 
 static int32_t enc_slot_alloc(jxs_gpu_enc_t* e, EncSlot* s) {
     const jxs_cfg_t* c = &e->cfg;
@@ -446,7 +449,13 @@ extern "C" int32_t jxs_gpu_enc_wait(jxs_gpu_enc_t* e, int slot) {
     return *s->status_h ? JXS_E_ENC_FRAME : JXS_OK;
 }
 
-extern "C" void jxs_gpu_enc_set_stream(jxs_gpu_enc_t* e, void* stream) { e->user_stream = (cudaStream_t)stream; }
+extern "C" void jxs_gpu_enc_set_stream(jxs_gpu_enc_t* e, void* stream) {
+    for (int i = 0; i < 8; i++) e->user_stream[i] = (cudaStream_t)stream;
+}
+extern "C" void jxs_gpu_enc_set_streams(jxs_gpu_enc_t* e, void* const* streams, int n) {
+    for (int i = 0; i < 8; i++) e->user_stream[i] = n > 0 ? (cudaStream_t)streams[i % n] : (cudaStream_t)0;
+}
+extern "C" int jxs_gpu_enc_slots(jxs_gpu_enc_t* e) { return e->nslots; }
 
 extern "C" void jxs_gpu_enc_set_timing(jxs_gpu_enc_t* e, int on) {
     std::lock_guard<std::mutex> g(e->mu);
@@ -517,14 +526,17 @@ struct jxs_gpu_dec {
     int nslots;
     DecSlot slot[8];
     uint32_t cap_bytes, cap_groups;
-    cudaStream_t user_stream;
+    cudaStream_t user_stream[8]; /* per slot; null: the slot's own stream */
     int timing;
     double stage_ms[DEC_STAGES];
     uint64_t timed_frames;
     std::mutex mu;
 };
 
-static inline cudaStream_t dec_stream(const jxs_gpu_dec_t* d, const DecSlot* s) { return d->user_stream ? d->user_stream : s->st; }
+static inline cudaStream_t dec_stream(const jxs_gpu_dec_t* d, const DecSlot* s) {
+    const cudaStream_t u = d->user_stream[s - d->slot];
+    return u ? u : s->st;
+}
 
 static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
     const jxs_cfg_t* c = &d->cfg;
@@ -816,7 +828,13 @@ extern "C" int32_t jxs_gpu_dec_wait(jxs_gpu_dec_t* d, int slot) {
     return *s->status_h;
 }
 
-extern "C" void jxs_gpu_dec_set_stream(jxs_gpu_dec_t* d, void* stream) { d->user_stream = (cudaStream_t)stream; }
+extern "C" void jxs_gpu_dec_set_stream(jxs_gpu_dec_t* d, void* stream) {
+    for (int i = 0; i < 8; i++) d->user_stream[i] = (cudaStream_t)stream;
+}
+extern "C" void jxs_gpu_dec_set_streams(jxs_gpu_dec_t* d, void* const* streams, int n) {
+    for (int i = 0; i < 8; i++) d->user_stream[i] = n > 0 ? (cudaStream_t)streams[i % n] : (cudaStream_t)0;
+}
+extern "C" int jxs_gpu_dec_slots(jxs_gpu_dec_t* d) { return d->nslots; }
 
 extern "C" void jxs_gpu_dec_set_timing(jxs_gpu_dec_t* d, int on) {
     std::lock_guard<std::mutex> g(d->mu);

@@ -48,6 +48,11 @@ int jxs_gpu_dec_ready(jxs_gpu_dec_t* d, int slot);
  * returns to the per-slot streams. */
 void jxs_gpu_enc_set_stream(jxs_gpu_enc_t* e, void* stream);
 void jxs_gpu_dec_set_stream(jxs_gpu_dec_t* d, void* stream);
+/* slot i runs on streams[i % n]; n = 0 returns to the slots' own streams */
+void jxs_gpu_enc_set_streams(jxs_gpu_enc_t* e, void* const* streams, int n);
+void jxs_gpu_dec_set_streams(jxs_gpu_dec_t* d, void* const* streams, int n);
+int jxs_gpu_enc_slots(jxs_gpu_enc_t* e);
+int jxs_gpu_dec_slots(jxs_gpu_dec_t* d);
 /* Stage timing with CUDA events on the launching stream.  Encoder stages:
  * H2D, transform, rate control, packing, D2H.  Decoder stages: H2D, unpack,
  * inverse transform, D2H.  read returns the frames timed since enabling. */

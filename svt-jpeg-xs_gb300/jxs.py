@@ -106,6 +106,7 @@ def lib():
                      "svt_jpeg_xs_decoder_send_packet", "svt_jpeg_xs_decoder_send_eoc",
                      "svt_jpeg_xs_decoder_get_single_frame_size", "svt_jpeg_xs_decoder_get_single_frame_size_with_proxy",
                      "svt_jpeg_xs_gpu_encoder_set_stream", "svt_jpeg_xs_gpu_decoder_set_stream",
+                     "svt_jpeg_xs_gpu_encoder_set_streams", "svt_jpeg_xs_gpu_decoder_set_streams",
                      "svt_jpeg_xs_gpu_encoder_set_timing", "svt_jpeg_xs_gpu_decoder_set_timing",
                      "svt_jpeg_xs_gpu_encoder_rc_results", "svt_jpeg_xs_frame_pool_get"):
             getattr(L, name).restype = u32
@@ -131,6 +132,8 @@ def lib():
             ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(ImageConfig), ctypes.POINTER(u32), u32, ctypes.c_int32]
         L.svt_jpeg_xs_gpu_encoder_set_stream.argtypes = [ctypes.POINTER(EncoderApi), ctypes.c_void_p]
         L.svt_jpeg_xs_gpu_decoder_set_stream.argtypes = [ctypes.POINTER(DecoderApi), ctypes.c_void_p]
+        L.svt_jpeg_xs_gpu_encoder_set_streams.argtypes = [ctypes.POINTER(EncoderApi), ctypes.c_void_p, u32]
+        L.svt_jpeg_xs_gpu_decoder_set_streams.argtypes = [ctypes.POINTER(DecoderApi), ctypes.c_void_p, u32]
         L.svt_jpeg_xs_gpu_encoder_set_timing.argtypes = [ctypes.POINTER(EncoderApi), u32]
         L.svt_jpeg_xs_gpu_decoder_set_timing.argtypes = [ctypes.POINTER(DecoderApi), u32]
         L.svt_jpeg_xs_gpu_encoder_read_timing.argtypes = [ctypes.POINTER(EncoderApi), ctypes.POINTER(ctypes.c_double), u32]
@@ -278,6 +281,10 @@ class Encoder:
     def set_stream(self, stream_handle):
         _check("set_stream", lib().svt_jpeg_xs_gpu_encoder_set_stream(ctypes.byref(self.api), stream_handle or None))
 
+    def set_streams(self, stream_handles):
+        arr = (ctypes.c_void_p * max(1, len(stream_handles)))(*stream_handles)
+        _check("set_streams", lib().svt_jpeg_xs_gpu_encoder_set_streams(ctypes.byref(self.api), arr, len(stream_handles)))
+
     def set_timing(self, on):
         _check("set_timing", lib().svt_jpeg_xs_gpu_encoder_set_timing(ctypes.byref(self.api), 1 if on else 0))
 
@@ -362,6 +369,10 @@ class Decoder:
 
     def set_stream(self, stream_handle):
         _check("set_stream", lib().svt_jpeg_xs_gpu_decoder_set_stream(ctypes.byref(self.api), stream_handle or None))
+
+    def set_streams(self, stream_handles):
+        arr = (ctypes.c_void_p * max(1, len(stream_handles)))(*stream_handles)
+        _check("set_streams", lib().svt_jpeg_xs_gpu_decoder_set_streams(ctypes.byref(self.api), arr, len(stream_handles)))
 
     def set_timing(self, on):
         _check("set_timing", lib().svt_jpeg_xs_gpu_decoder_set_timing(ctypes.byref(self.api), 1 if on else 0))
