@@ -51,7 +51,7 @@ METRIC = "encode+decode Gpix/s (bit-exact), 3840x2160 4:2:2 10-bit bpp3"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=8, help="frames encoded and decoded per step")
@@ -313,45 +313,58 @@ def run_ours(args, rank, world, local):
         assert err == 0 and all(np.array_equal(t.cpu().numpy(), w) for t, w in zip(d_out[i], want_planes)), \
             "decoded frame differs from the oracle"
 
-    # ---- e2e through the C API with host buffers: pair 0 on its own slot
-    # streams (3 frames in flight)
+    # ---- e2e through the C API with host buffers: every pair on its own slot
+    # streams (3 frames in flight per codec); the latency probe uses pair 0
     enc, dec = encs[0], decs[0]
-    enc.set_stream(None)
-    dec.set_stream(None)
     def pinned_like(a):
         buf = torch.empty(a.shape, dtype=torch.from_numpy(a[:1]).dtype).pin_memory()
         buf.copy_(torch.from_numpy(a))
         return buf.numpy()
 
-    h_in = [[pinned_like(p) for p in frames[i]] for i in range(F)]
+    h_in = [[pinned_like(p) for p in frames[i % nseq]] for i in range(F)]
     h_bs = [torch.empty(lcod + 64, dtype=torch.uint8).pin_memory().numpy() for _ in range(F)]
     h_out = [[torch.empty(p.shape, dtype=torch.from_numpy(p[:1]).dtype).pin_memory().numpy() for p in frames[0]]
              for _ in range(F)]
 
+    for k in range(NS):
+        encs[k].set_stream(None)
+        decs[k].set_stream(None)
+
     def e2e_step():
-        sent = 0
-        got = 0
-        while got < F:
-            while sent < F:
-                r = enc.send(h_in[sent], h_bs[sent], blocking=False)
-                if r == jxs.E_EMPTY_QUEUE:
-                    break
-                assert r == 0
-                sent += 1
-            r, f = enc.get()
-            assert r == 0
-            got += 1
-        sent = got = 0
-        while got < F:
-            while sent < F:
-                r = dec.send(h_bs[sent], h_out[sent], bs_size=lcod, blocking=False)
-                if r == jxs.E_EMPTY_QUEUE:
-                    break
-                assert r == 0
-                sent += 1
-            r, _ = dec.get()
-            assert r == 0
-            got += 1
+        # frame i on pair i % NS: encode from host planes, the codestream back
+        # to the host, decode from it into host planes; every codec keeps its
+        # queue full and results are polled without blocking
+        nxt_enc = list(range(NS))            # next frame to encode per pair
+        enc_q = [[] for _ in range(NS)]      # frames in each encoder, in order
+        ready = [[] for _ in range(NS)]      # encoded frames waiting for the decoder
+        dec_q = [[] for _ in range(NS)]
+        done = 0
+        while done < F:
+            for k in range(NS):
+                while nxt_enc[k] < F:
+                    i = nxt_enc[k]
+                    if encs[k].send(h_in[i], h_bs[i], blocking=False) == jxs.E_EMPTY_QUEUE:
+                        break
+                    enc_q[k].append(i)
+                    nxt_enc[k] += NS
+                while enc_q[k]:
+                    r, _ = encs[k].get(blocking=False)
+                    if r == jxs.E_EMPTY_QUEUE:
+                        break
+                    assert r == 0, hex(r)
+                    ready[k].append(enc_q[k].pop(0))
+                while ready[k]:
+                    i = ready[k][0]
+                    if decs[k].send(h_bs[i], h_out[i], bs_size=lcod, blocking=False) == jxs.E_EMPTY_QUEUE:
+                        break
+                    dec_q[k].append(ready[k].pop(0))
+                while dec_q[k]:
+                    r, _ = decs[k].get(blocking=False)
+                    if r == jxs.E_EMPTY_QUEUE:
+                        break
+                    assert r == 0, hex(r)
+                    dec_q[k].pop(0)
+                    done += 1
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
