@@ -47,6 +47,43 @@ SEED = 2
 WORKLOAD = "3840x2160 YUV 4:2:2 10-bit, bpp 3, decomp V2/H5, 60-frame seeded synthetic stream"
 METRIC = "encode+decode Gpix/s (bit-exact), 3840x2160 4:2:2 10-bit bpp3"
 
+# kernel launches of one frame, in launch order (per-kernel CUDA-event times)
+ENC_KERNELS = ["fwd_v_level0", "fwd_v_level1", "fwd_h", "rc_cost", "pack"]
+DEC_KERNELS = ["walk", "unpack", "inv_h", "inv_v_level1", "inv_v_level0"]
+
+# DRAM bytes (read + write) of one launch of each kernel on this workload,
+# from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum; ncu
+# flushes caches before each launch, so these are cold-cache figures)
+KERNEL_DRAM_BYTES = {"fwd_v_level0": 34_390_000, "fwd_v_level1": 16_630_000, "fwd_h": 4_160_000, "rc_cost": 4_220_000,
+                     "pack": 37_800_000, "unpack": 3_200_000, "inv_h": 2_100_000, "inv_v_level1": 10_400_000,
+                     "inv_v_level0": 42_600_000}
+
+
+def kernel_bytes(lcod):
+    """Algorithmic bytes of one launch of each kernel for the 4:2:2 V2/H5
+    geometry: samples 2 bytes, coefficients 2 bytes, GCLIs 1 byte per 4
+    coefficients, int32 low bands 4 bytes."""
+    comps = [(W, H), (W // 2, H), (W // 2, H)]
+    out = {k: 0 for k in ENC_KERNELS + DEC_KERNELS if k != "walk"}
+    total_coef = 0
+    for (w, h) in comps:
+        w1, h1 = (w + 1) // 2, (h + 1) // 2
+        w2, h2 = (w1 + 1) // 2, (h1 + 1) // 2
+        b0 = w * h - w1 * h1          # level-0 high bands
+        b1 = w1 * h1 - w2 * h2        # level-1 high bands
+        b2 = w2 * h2                  # horizontal-only bands + final LL
+        total_coef += w * h
+        out["fwd_v_level0"] += 2 * w * h + 2 * b0 + b0 // 4 + 4 * w1 * h1
+        out["fwd_v_level1"] += 4 * w1 * h1 + 2 * b1 + b1 // 4 + 4 * w2 * h2
+        out["fwd_h"] += 4 * b2 + 2 * b2 + b2 // 4
+        out["inv_h"] += 2 * b2 + 4 * b2
+        out["inv_v_level1"] += 4 * w2 * h2 + 2 * b1 + 4 * w1 * h1
+        out["inv_v_level0"] += 4 * w1 * h1 + 2 * b0 + 2 * w * h
+    out["rc_cost"] = total_coef // 4
+    out["pack"] = 2 * total_coef + total_coef // 4 + lcod
+    out["unpack"] = lcod + 2 * total_coef
+    return out
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -266,6 +303,8 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     nenc, enc_ms = encs[0].read_timing()
     ndec, dec_ms = decs[0].read_timing()
+    kenc = encs[0].read_kernel_timing()
+    kdec = decs[0].read_kernel_timing()
     encs[0].set_timing(False)
     decs[0].set_timing(False)
     if world > 1:
@@ -394,24 +433,20 @@ def run_ours(args, rank, world, local):
     for codec in encs + decs:
         codec.close()
 
-    # ---- roofline of the dominant stage
+    # ---- roofline of the dominant kernel
     peak, peak_kind = measured_peak()
     stages = {"enc_transform": enc_ms[1], "enc_rate_control": enc_ms[2], "enc_pack": enc_ms[3], "dec_unpack": dec_ms[1],
               "dec_inverse_transform": dec_ms[2]}
     nfr = max(nenc, 1)
-    coef_bytes = 2 * (W * H + 2 * (W // 2) * H)
-    alg = {  # algorithmic bytes per frame of each stage
-        "enc_transform": in_bytes + coef_bytes,
-        "enc_rate_control": coef_bytes // 8,
-        "enc_pack": coef_bytes + lcod,
-        "dec_unpack": lcod + coef_bytes,
-        "dec_inverse_transform": coef_bytes + out_bytes,
-    }
-    dom = max(stages, key=lambda k: stages[k])
-    dom_ms = stages[dom] / nfr
-    achieved = alg[dom] / (dom_ms / 1e3) / 1e9
-    pipeline_gbs = (in_bytes + lcod + lcod + out_bytes) / ((sum(stages.values()) / nfr) / 1e3) / 1e9
     stage_ms = {k: round(v / nfr, 4) for k, v in stages.items()}
+    kb = kernel_bytes(lcod)
+    kern_ms = {}
+    for names, times in ((ENC_KERNELS, kenc), (DEC_KERNELS, kdec)):
+        for name, t in zip(names, times):
+            kern_ms[name] = t / nfr
+    dom = max((k for k in kern_ms if k in kb), key=lambda k: kern_ms[k])
+    achieved = kb[dom] / (kern_ms[dom] / 1e3) / 1e9
+    pipeline_gbs = (in_bytes + lcod + lcod + out_bytes) / ((sum(stages.values()) / nfr) / 1e3) / 1e9
 
     # ---- CPU baseline (oracle on the host cores), rank 0 only
     cpu = None
@@ -434,8 +469,9 @@ def run_ours(args, rank, world, local):
                 "d2h_bytes_per_step": F * (lcod + out_bytes), "p50_step_ms": 1e3 * statistics.median(lat),
                 "frame_latency_ms_p50": statistics.median(lat_frame),
                 "frame_latency_ms_p99": float(np.percentile(lat_frame, 99))},
-        "roofline": {"bound": "hbm", "stage": dom, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": None, "stage_ms_per_frame": stage_ms,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": KERNEL_DRAM_BYTES.get(dom), "algorithmic_bytes": kb[dom],
+                     "kernel_ms_per_frame": {k: round(v, 4) for k, v in kern_ms.items()}, "stage_ms_per_frame": stage_ms,
                      "pipeline_algorithmic_gbs": pipeline_gbs},
         "cpu_baseline": cpu,
         "clocks": clk,

@@ -51,6 +51,15 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_set_timing(svt_jpeg_xs_deco
 PREFIX_API uint64_t svt_jpeg_xs_gpu_encoder_read_timing(svt_jpeg_xs_encoder_api_t* enc_api, double* stage_ms, uint32_t n);
 PREFIX_API uint64_t svt_jpeg_xs_gpu_decoder_read_timing(svt_jpeg_xs_decoder_api_t* dec_api, double* stage_ms, uint32_t n);
 
+/* Accumulated milliseconds of each kernel launch of a frame, in launch order
+ * (timing mode): encoder - the vertical transform levels, the horizontal-
+ * only levels, rate control, packing; decoder - the precinct walk (device
+ * codestreams only), unpacking, the inverse horizontal-only levels, the
+ * inverse vertical levels from the deepest up.  Returns the launches per
+ * frame. */
+PREFIX_API uint32_t svt_jpeg_xs_gpu_encoder_read_kernel_timing(svt_jpeg_xs_encoder_api_t* enc_api, double* kernel_ms, uint32_t n);
+PREFIX_API uint32_t svt_jpeg_xs_gpu_decoder_read_kernel_timing(svt_jpeg_xs_decoder_api_t* dec_api, double* kernel_ms, uint32_t n);
+
 /* Quantization and refinement chosen for each precinct row of the most
  * recently sent picture that has not been returned yet (count >= rows). */
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_rc_results(svt_jpeg_xs_encoder_api_t* enc_api, uint8_t* quantization,

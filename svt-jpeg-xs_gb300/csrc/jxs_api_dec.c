@@ -433,3 +433,8 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_locate_frame(svt_jpeg_xs_de
     return (SvtJxsErrorType_t)jxs_gpu_dec_locate_noalloc(p->gpu, dev_bitstream, bitstream_size, frame_size, precinct_offsets,
                                                          precinct_capacity, cuda_stream);
 }
+
+PREFIX_API uint32_t svt_jpeg_xs_gpu_decoder_read_kernel_timing(svt_jpeg_xs_decoder_api_t* dec_api, double* kernel_ms, uint32_t n) {
+    if (!dec_api || !dec_api->private_ptr || !kernel_ms) return 0;
+    return (uint32_t)jxs_gpu_dec_read_kernel_timing(((dec_prv_t*)dec_api->private_ptr)->gpu, kernel_ms, (int)n);
+}

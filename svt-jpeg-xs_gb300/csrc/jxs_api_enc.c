@@ -273,3 +273,8 @@ PREFIX_API uint64_t svt_jpeg_xs_gpu_encoder_read_timing(svt_jpeg_xs_encoder_api_
     if (!enc_api || !enc_api->private_ptr || !stage_ms) return 0;
     return jxs_gpu_enc_read_timing(((enc_prv_t*)enc_api->private_ptr)->gpu, stage_ms, (int)n);
 }
+
+PREFIX_API uint32_t svt_jpeg_xs_gpu_encoder_read_kernel_timing(svt_jpeg_xs_encoder_api_t* enc_api, double* kernel_ms, uint32_t n) {
+    if (!enc_api || !enc_api->private_ptr || !kernel_ms) return 0;
+    return (uint32_t)jxs_gpu_enc_read_kernel_timing(((enc_prv_t*)enc_api->private_ptr)->gpu, kernel_ms, (int)n);
+}

@@ -55,6 +55,12 @@ extern "C" int jxs_inv_h_max_rows_per_block(void);
     } while (0)
 
 static const size_t kSmemMax = 220 * 1024;
+/* timing mode: events around every kernel of a frame */
+#define JXS_KEV 17
+#define KMARK()                                                          \
+    do {                                                                 \
+        if (s->timed && s->nkev < JXS_KEV) CK(cudaEventRecord(s->kev[s->nkev++], st)); \
+    } while (0)
 
 extern "C" int jxs_gpu_is_device_ptr(const void* p) {
     if (!p) return 0;
@@ -158,6 +164,8 @@ struct EncSlot {
     int* status_h;
     int busy;
     cudaEvent_t tev[6];
+    cudaEvent_t kev[JXS_KEV];   /* timing mode: before the first kernel and after each */
+    int nkev;
     int timed;
 };
 
@@ -173,6 +181,8 @@ struct jxs_gpu_enc {
     cudaStream_t user_stream[8]; /* per slot; null: the slot's own stream */
     int timing;
     double stage_ms[ENC_STAGES];
+    double kern_ms[JXS_KEV];
+    int nkern;
     uint64_t timed_frames;
     std::mutex mu;
 };
@@ -218,6 +228,7 @@ static int32_t enc_slot_alloc(jxs_gpu_enc_t* e, EncSlot* s) {
     CK(cudaMallocHost(&s->status_h, 64));
     *s->status_h = 0;
     for (int i = 0; i < 6; i++) CK(cudaEventCreate(&s->tev[i]));
+    for (int i = 0; i < JXS_KEV; i++) CK(cudaEventCreate(&s->kev[i]));
     return JXS_OK;
 }
 
@@ -236,6 +247,8 @@ static void enc_slot_free(EncSlot* s) {
     if (s->status_h) cudaFreeHost(s->status_h);
     for (int i = 0; i < 6; i++)
         if (s->tev[i]) cudaEventDestroy(s->tev[i]);
+    for (int i = 0; i < JXS_KEV; i++)
+        if (s->kev[i]) cudaEventDestroy(s->kev[i]);
     if (s->done) cudaEventDestroy(s->done);
     if (s->st) cudaStreamDestroy(s->st);
     memset(s, 0, sizeof(*s));
@@ -320,6 +333,8 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
         }
     }
     TMARK(1);
+    s->nkev = 0;
+    KMARK();
     /* forward transform: one launch per vertical level, then the
      * horizontal-only levels of every component (one launch per source
      * kind) */
@@ -363,6 +378,7 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
         }
         L.ntiles = blocks;
         CK(jxs_launch_fwd_v(&L, v == 0 ? level0_kind : SRC_I32, blocks, dev_bands(e->dcfg), s->coef, s->gcli, st));
+        KMARK();
     }
     for (int pass = 0; pass < 2; pass++) {
         /* pass 0: components with vertical levels (input: their last int32
@@ -407,13 +423,16 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
             blocks += (int)div_up((uint32_t)L.job[i].h, (uint32_t)rpb);
         }
         CK(jxs_launch_fwd_h(&L, pass == 0 ? SRC_I32 : level0_kind, blocks, dev_bands(e->dcfg), s->coef, s->gcli, st));
+        KMARK();
     }
     TMARK(2);
     CK(jxs_launch_rc(e->dcfg, c->np, c->nslices, s->gcli, s->cost, s->slice_done, s->rc, s->status, st));
+    KMARK();
     TMARK(3);
     const int out_dev = jxs_gpu_is_device_ptr(out);
     uint8_t* dst = out_dev ? out : s->out_stage;
     CK(jxs_launch_pack(e->dcfg, c->np, s->coef, s->gcli, s->rc, dst, e->cap_words, s->status, st));
+    KMARK();
     TMARK(4);
     if (!out_dev) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));
     CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -443,6 +462,11 @@ extern "C" int32_t jxs_gpu_enc_wait(jxs_gpu_enc_t* e, int slot) {
             if (cudaEventElapsedTime(&ms[i], s->tev[i], s->tev[i + 1]) != cudaSuccess) ms[i] = 0.f;
         std::lock_guard<std::mutex> g(e->mu);
         for (int i = 0; i < ENC_STAGES; i++) e->stage_ms[i] += ms[i];
+        for (int i = 0; i + 1 < s->nkev; i++) {
+            float k = 0.f;
+            if (cudaEventElapsedTime(&k, s->kev[i], s->kev[i + 1]) == cudaSuccess) e->kern_ms[i] += k;
+        }
+        e->nkern = s->nkev > 0 ? s->nkev - 1 : 0;
         e->timed_frames++;
         s->timed = 0;
     }
@@ -461,7 +485,14 @@ extern "C" void jxs_gpu_enc_set_timing(jxs_gpu_enc_t* e, int on) {
     std::lock_guard<std::mutex> g(e->mu);
     e->timing = on;
     for (int i = 0; i < ENC_STAGES; i++) e->stage_ms[i] = 0;
+    for (int i = 0; i < JXS_KEV; i++) e->kern_ms[i] = 0;
     e->timed_frames = 0;
+}
+
+extern "C" int jxs_gpu_enc_read_kernel_timing(jxs_gpu_enc_t* e, double* ms, int n) {
+    std::lock_guard<std::mutex> g(e->mu);
+    for (int i = 0; i < n && i < JXS_KEV; i++) ms[i] = e->kern_ms[i];
+    return e->nkern;
 }
 
 extern "C" uint64_t jxs_gpu_enc_read_timing(jxs_gpu_enc_t* e, double* ms, int n) {
@@ -514,6 +545,8 @@ struct DecSlot {
     uint8_t* hdr_h;       /* header of a device-resident codestream, checked at completion */
     int hdr_check;
     cudaEvent_t tev[5];
+    cudaEvent_t kev[JXS_KEV];
+    int nkev;
     int timed;
 };
 
@@ -529,6 +562,8 @@ struct jxs_gpu_dec {
     cudaStream_t user_stream[8]; /* per slot; null: the slot's own stream */
     int timing;
     double stage_ms[DEC_STAGES];
+    double kern_ms[JXS_KEV];
+    int nkern;
     uint64_t timed_frames;
     std::mutex mu;
 };
@@ -568,6 +603,7 @@ static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
     CK(cudaMallocHost(&s->status_h, 64));
     *s->status_h = 0;
     for (int i = 0; i < 5; i++) CK(cudaEventCreate(&s->tev[i]));
+    for (int i = 0; i < JXS_KEV; i++) CK(cudaEventCreate(&s->kev[i]));
     return JXS_OK;
 }
 
@@ -585,6 +621,10 @@ static void dec_slot_free(DecSlot* s) {
     if (s->status_h) cudaFreeHost(s->status_h);
     for (int i = 0; i < 5; i++)
         if (s->tev[i]) cudaEventDestroy(s->tev[i]);
+    for (int i = 0; i < JXS_KEV; i++)
+        if (s->kev[i]) cudaEventDestroy(s->kev[i]);
+    for (int i = 0; i < JXS_KEV; i++)
+        if (s->kev[i]) cudaEventDestroy(s->kev[i]);
     if (s->done) cudaEventDestroy(s->done);
     if (s->st) cudaStreamDestroy(s->st);
     memset(s, 0, sizeof(*s));
@@ -659,6 +699,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
     CK(cudaMemsetAsync(s->status, 0, sizeof(int), st));
     const uint8_t* dbs = bs;
     s->hdr_check = 0;
+    s->nkev = 0;
     if (!prec_off) {
         /* device-resident codestream: header compared at completion, precinct
          * offsets found on the GPU */
@@ -666,6 +707,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         CK(cudaMemcpyAsync(s->hdr_h, bs, c->hdr_len, cudaMemcpyDeviceToHost, st));
         s->hdr_check = 1;
         CK(cudaMemsetAsync(s->status + 1, 0, sizeof(int), st));
+        KMARK();
         CK(jxs_launch_walk(d->dcfg, c->nslices, bs, size, s->prec_off, s->status + 1, s->status, st));
     } else if (!jxs_gpu_is_device_ptr(bs)) {
         if (size > s->bs_cap) {
@@ -684,7 +726,9 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         CK(cudaMemcpyAsync(s->prec_off, s->prec_off_h, sizeof(uint32_t) * c->np, cudaMemcpyHostToDevice, st));
     }
     TMARK(1);
+    KMARK();
     CK(jxs_launch_unpack(d->dcfg, dbs, size, s->prec_off, s->coef, c->np, d->cap_bytes, d->cap_groups, s->status, st));
+    KMARK();
     TMARK(2);
 
     int out_dev[JXS_MAXC];
@@ -746,6 +790,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
             blocks += (int)div_up((uint32_t)L.job[i2].h, (uint32_t)rpb);
         }
         CK(jxs_launch_inv_h(&L, pass == 0 ? 0 : sample_kind, blocks, dev_bands(d->dcfg), s->coef, st));
+        KMARK();
     }
     const uint32_t vcols = (uint32_t)jxs_inv_v_tile_cols(), vrows = (uint32_t)jxs_inv_v_tile_rows();
     for (int v = (int)max_dv - 1; v >= 0; v--) {
@@ -782,6 +827,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
             blocks += J.col_tiles * (int)div_up((h + 1) / 2, vrows);
         }
         CK(jxs_launch_inv_v(&L, v > 0 ? 0 : sample_kind, blocks, dev_bands(d->dcfg), s->coef, st));
+        KMARK();
     }
     TMARK(3);
     for (uint32_t k = 0; k < c->nc; k++) {
@@ -815,6 +861,13 @@ extern "C" int32_t jxs_gpu_dec_wait(jxs_gpu_dec_t* d, int slot) {
             if (cudaEventElapsedTime(&ms[i], s->tev[i], s->tev[i + 1]) != cudaSuccess) ms[i] = 0.f;
         std::lock_guard<std::mutex> g(d->mu);
         for (int i = 0; i < DEC_STAGES; i++) d->stage_ms[i] += ms[i];
+        /* kernels in launch order: the precinct walk (device codestreams
+         * only), unpack, the inverse transform launches */
+        for (int i = 0; i + 1 < s->nkev; i++) {
+            float k = 0.f;
+            if (cudaEventElapsedTime(&k, s->kev[i], s->kev[i + 1]) == cudaSuccess) d->kern_ms[i] += k;
+        }
+        d->nkern = s->nkev > 0 ? s->nkev - 1 : 0;
         d->timed_frames++;
         s->timed = 0;
     }
@@ -840,7 +893,14 @@ extern "C" void jxs_gpu_dec_set_timing(jxs_gpu_dec_t* d, int on) {
     std::lock_guard<std::mutex> g(d->mu);
     d->timing = on;
     for (int i = 0; i < DEC_STAGES; i++) d->stage_ms[i] = 0;
+    for (int i = 0; i < JXS_KEV; i++) d->kern_ms[i] = 0;
     d->timed_frames = 0;
+}
+
+extern "C" int jxs_gpu_dec_read_kernel_timing(jxs_gpu_dec_t* d, double* ms, int n) {
+    std::lock_guard<std::mutex> g(d->mu);
+    for (int i = 0; i < n && i < JXS_KEV; i++) ms[i] = d->kern_ms[i];
+    return d->nkern;
 }
 
 extern "C" uint64_t jxs_gpu_dec_read_timing(jxs_gpu_dec_t* d, double* ms, int n) {

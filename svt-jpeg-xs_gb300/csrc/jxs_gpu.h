@@ -52,6 +52,10 @@ void jxs_gpu_dec_set_stream(jxs_gpu_dec_t* d, void* stream);
 void jxs_gpu_enc_set_streams(jxs_gpu_enc_t* e, void* const* streams, int n);
 void jxs_gpu_dec_set_streams(jxs_gpu_dec_t* d, void* const* streams, int n);
 int jxs_gpu_enc_slots(jxs_gpu_enc_t* e);
+/* timing mode: accumulated milliseconds of each kernel launch of a frame in
+ * launch order; returns the launches per frame */
+int jxs_gpu_enc_read_kernel_timing(jxs_gpu_enc_t* e, double* ms, int n);
+int jxs_gpu_dec_read_kernel_timing(jxs_gpu_dec_t* d, double* ms, int n);
 int jxs_gpu_dec_slots(jxs_gpu_dec_t* d);
 /* Stage timing with CUDA events on the launching stream.  Encoder stages:
  * H2D, transform, rate control, packing, D2H.  Decoder stages: H2D, unpack,

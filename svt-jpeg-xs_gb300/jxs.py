@@ -140,6 +140,10 @@ def lib():
         L.svt_jpeg_xs_gpu_encoder_read_timing.restype = ctypes.c_uint64
         L.svt_jpeg_xs_gpu_decoder_read_timing.argtypes = [ctypes.POINTER(DecoderApi), ctypes.POINTER(ctypes.c_double), u32]
         L.svt_jpeg_xs_gpu_decoder_read_timing.restype = ctypes.c_uint64
+        L.svt_jpeg_xs_gpu_encoder_read_kernel_timing.argtypes = [ctypes.POINTER(EncoderApi), ctypes.POINTER(ctypes.c_double), u32]
+        L.svt_jpeg_xs_gpu_encoder_read_kernel_timing.restype = u32
+        L.svt_jpeg_xs_gpu_decoder_read_kernel_timing.argtypes = [ctypes.POINTER(DecoderApi), ctypes.POINTER(ctypes.c_double), u32]
+        L.svt_jpeg_xs_gpu_decoder_read_kernel_timing.restype = u32
         L.svt_jpeg_xs_gpu_encoder_rc_results.argtypes = [ctypes.POINTER(EncoderApi), ctypes.c_void_p, ctypes.c_void_p, u32]
         L.svt_jpeg_xs_gpu_decoder_locate_frame.argtypes = [ctypes.POINTER(DecoderApi), ctypes.c_void_p, u32, ctypes.POINTER(u32),
                                                           ctypes.c_void_p, u32, ctypes.c_void_p]
@@ -288,6 +292,11 @@ class Encoder:
     def set_timing(self, on):
         _check("set_timing", lib().svt_jpeg_xs_gpu_encoder_set_timing(ctypes.byref(self.api), 1 if on else 0))
 
+    def read_kernel_timing(self):
+        ms = (ctypes.c_double * 16)()
+        n = lib().svt_jpeg_xs_gpu_encoder_read_kernel_timing(ctypes.byref(self.api), ms, 16)
+        return [ms[i] for i in range(n)]
+
     def read_timing(self):
         ms = (ctypes.c_double * 5)()
         n = lib().svt_jpeg_xs_gpu_encoder_read_timing(ctypes.byref(self.api), ms, 5)
@@ -376,6 +385,11 @@ class Decoder:
 
     def set_timing(self, on):
         _check("set_timing", lib().svt_jpeg_xs_gpu_decoder_set_timing(ctypes.byref(self.api), 1 if on else 0))
+
+    def read_kernel_timing(self):
+        ms = (ctypes.c_double * 16)()
+        n = lib().svt_jpeg_xs_gpu_decoder_read_kernel_timing(ctypes.byref(self.api), ms, 16)
+        return [ms[i] for i in range(n)]
 
     def read_timing(self):
         ms = (ctypes.c_double * 4)()
