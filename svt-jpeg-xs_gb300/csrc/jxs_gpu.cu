@@ -623,8 +623,6 @@ static void dec_slot_free(DecSlot* s) {
         if (s->tev[i]) cudaEventDestroy(s->tev[i]);
     for (int i = 0; i < JXS_KEV; i++)
         if (s->kev[i]) cudaEventDestroy(s->kev[i]);
-    for (int i = 0; i < JXS_KEV; i++)
-        if (s->kev[i]) cudaEventDestroy(s->kev[i]);
     if (s->done) cudaEventDestroy(s->done);
     if (s->st) cudaStreamDestroy(s->st);
     memset(s, 0, sizeof(*s));
