@@ -92,6 +92,74 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_locate_frame(svt_jpeg_xs_de
                                                                   uint32_t* precinct_offsets, uint32_t precinct_capacity,
                                                                   void* cuda_stream);
 
+/* ------------------------------------------------------------------------
+ * Batched form.  A batch object encodes or decodes up to
+ * SVT_JPEGXS_GPU_BATCH_MAX frames per call, of any mix of sizes, colour
+ * formats and bit depths: frame i uses the configuration of the i-th handle.
+ * Each stage runs as one kernel launch over all frames of the batch; the
+ * launches are captured into a CUDA graph that is replayed while the batch's
+ * buffers and launch parameters stay the same.  Every frame position owns a
+ * working set carved from the object's device budget (device_bytes); a
+ * batch that does not fit returns SvtJxsErrorInsufficientResources.
+ *
+ * A batch call queues the work and returns; svt_jpeg_xs_gpu_batch_wait
+ * completes it (one batch in flight per object; use several objects to
+ * overlap batches).  Planes and codestreams may be host or device memory of
+ * the current device.  Outputs are identical, byte for byte, to those of
+ * send_picture / send_frame on the same handles.  A batch object is used from
+ * one thread at a time.
+ * ------------------------------------------------------------------------ */
+#define SVT_JPEGXS_GPU_BATCH_MAX 64
+
+typedef struct svt_jpeg_xs_gpu_batch svt_jpeg_xs_gpu_batch_t;
+
+typedef struct svt_jpeg_xs_gpu_batch_info {
+    float last_gpu_ms;         /* device time of the last batch (CUDA events around its launches) */
+    uint32_t last_launches;    /* kernel launches of the last batch */
+    uint64_t graph_hits;       /* batches replayed from a cached graph */
+    uint64_t graph_builds;     /* graphs instantiated */
+    uint64_t graph_updates;    /* cached graphs updated in place with new parameters */
+    int32_t tune[5];           /* launch shapes of the last batch, as for set_tune */
+    uint64_t device_bytes, device_used, device_peak; /* device budget */
+} svt_jpeg_xs_gpu_batch_info_t;
+
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_create(uint64_t device_bytes, svt_jpeg_xs_gpu_batch_t** batch);
+PREFIX_API void svt_jpeg_xs_gpu_batch_destroy(svt_jpeg_xs_gpu_batch_t* batch);
+
+/* use_graph (default 1): capture and replay CUDA graphs.  autotune (default
+ * 0): the first batch of each new composition of handles first times a set
+ * of launch shapes and keeps the fastest for that composition (blocking;
+ * the outputs of every candidate are identical). */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_set_options(svt_jpeg_xs_gpu_batch_t* batch, uint32_t use_graph,
+                                                               uint32_t autotune);
+
+/* Fixes the launch shapes of every batch: tune[0] independent chains the
+ * frames are split into (1-4), tune[1] frames ordered largest first,
+ * tune[2] blocks per SM of the first transform level (0: as many as fit),
+ * tune[3] / tune[4] rows per block of the forward / inverse
+ * horizontal-only levels (1-4). */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_set_tune(svt_jpeg_xs_gpu_batch_t* batch, const int32_t* tune);
+
+/* Encodes frames[i] with enc[i]'s configuration into frames[i]->bitstream
+ * (used_size is set to the frame size). */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_encode(svt_jpeg_xs_gpu_batch_t* batch, svt_jpeg_xs_encoder_api_t* const* enc,
+                                                          svt_jpeg_xs_frame_t* const* frames, uint32_t n, void* cuda_stream);
+
+/* Decodes frames[i]->bitstream (used_size bytes) with dec[i]'s stream
+ * configuration into frames[i]->image. */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_decode(svt_jpeg_xs_gpu_batch_t* batch, svt_jpeg_xs_decoder_api_t* const* dec,
+                                                          svt_jpeg_xs_frame_t* const* frames, uint32_t n, void* cuda_stream);
+
+/* Blocks until the batch in flight completes.  status (may be NULL) receives
+ * SVT_JPEGXS_GPU_BATCH_MAX entries, the first n of them the per-frame
+ * results; returns the first error, or SvtJxsErrorNone. */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_wait(svt_jpeg_xs_gpu_batch_t* batch, SvtJxsErrorType_t* status);
+
+/* 1 when no batch is in flight or it has completed. */
+PREFIX_API uint32_t svt_jpeg_xs_gpu_batch_ready(svt_jpeg_xs_gpu_batch_t* batch);
+
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_get_info(svt_jpeg_xs_gpu_batch_t* batch, svt_jpeg_xs_gpu_batch_info_t* info);
+
 #ifdef __cplusplus
 }
 #endif

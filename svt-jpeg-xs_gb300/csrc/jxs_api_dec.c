@@ -17,6 +17,7 @@
 #include "SvtJpegxsDec.h"
 #include "SvtJpegxsGpu.h"
 #include "jxs_core.h"
+#include "jxs_batch.h"
 #include "jxs_gpu.h"
 #include "jxs_queue.h"
 
@@ -437,4 +438,54 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_decoder_locate_frame(svt_jpeg_xs_de
 PREFIX_API uint32_t svt_jpeg_xs_gpu_decoder_read_kernel_timing(svt_jpeg_xs_decoder_api_t* dec_api, double* kernel_ms, uint32_t n) {
     if (!dec_api || !dec_api->private_ptr || !kernel_ms) return 0;
     return (uint32_t)jxs_gpu_dec_read_kernel_timing(((dec_prv_t*)dec_api->private_ptr)->gpu, kernel_ms, (int)n);
+}
+
+/* Batched decode (SvtJpegxsGpu.h).  Host codestreams are parsed and walked
+ * here as send_frame does (header checked against the decoder's stream,
+ * precinct offsets by jxs_frame_bytes_walk); device codestreams are located
+ * on the GPU and their headers checked when the batch completes. */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_decode(svt_jpeg_xs_gpu_batch_t* batch, svt_jpeg_xs_decoder_api_t* const* dec,
+                                                          svt_jpeg_xs_frame_t* const* frames, uint32_t n, void* cuda_stream) {
+    if (!batch || !dec || !frames || n == 0 || n > SVT_JPEGXS_GPU_BATCH_MAX) return SvtJxsErrorBadParameter;
+    jxs_gpu_batch_t* b = (jxs_gpu_batch_t*)batch;
+    jxs_gpu_dec_t* gpu[SVT_JPEGXS_GPU_BATCH_MAX];
+    const uint8_t* bs[SVT_JPEGXS_GPU_BATCH_MAX];
+    uint32_t size[SVT_JPEGXS_GPU_BATCH_MAX];
+    int walked[SVT_JPEGXS_GPU_BATCH_MAX];
+    void* planes[SVT_JPEGXS_GPU_BATCH_MAX][4];
+    uint32_t strides[SVT_JPEGXS_GPU_BATCH_MAX][4];
+    for (uint32_t i = 0; i < n; i++) {
+        if (!dec[i] || !dec[i]->private_ptr || !frames[i]) return SvtJxsErrorDecoderInvalidPointer;
+        dec_prv_t* p = (dec_prv_t*)dec[i]->private_ptr;
+        if (p->packet_mode) return SvtJxsErrorUndefined;
+        const svt_jpeg_xs_frame_t* f = frames[i];
+        SvtJxsErrorType_t e = check_planes(p, f);
+        if (e) return e;
+        gpu[i] = p->gpu;
+        bs[i] = f->bitstream.buffer;
+        size[i] = f->bitstream.used_size;
+        if (!bs[i] || !size[i]) return SvtJxsErrorDecoderInvalidPointer;
+        walked[i] = 0;
+        if (!jxs_gpu_is_device_ptr(bs[i])) {
+            uint32_t* prec = jxs_gpu_batch_prec_buffer(b, i, p->cfg->np);
+            if (!prec) return SvtJxsErrorInsufficientResources;
+            jxs_hdr_info_t info;
+            pthread_mutex_lock(&p->send_mu);
+            int32_t r = jxs_cfg_decoder(p->tmp_cfg, bs[i], size[i], &info);
+            if (!r && (info.hdr_len != p->info.hdr_len || memcmp(bs[i], p->cfg->hdr, 12) != 0 ||
+                       memcmp(bs[i] + 16, p->cfg->hdr + 16, info.hdr_len - 16) != 0))
+                r = JXS_E_DEC_CONFIG;
+            if (!r) jxs_frame_bytes_walk(p->cfg, bs[i], size[i], info.hdr_len, prec, &r);
+            pthread_mutex_unlock(&p->send_mu);
+            if (r) return (SvtJxsErrorType_t)r;
+            walked[i] = 1;
+        }
+        for (int k = 0; k < 4; k++) {
+            planes[i][k] = f->image.data_yuv[k];
+            strides[i][k] = f->image.stride[k];
+        }
+    }
+    const int32_t r = jxs_gpu_batch_decode(b, gpu, n, bs, size, walked, (void* const(*)[4])planes, (const uint32_t(*)[4])strides,
+                                           cuda_stream);
+    return (SvtJxsErrorType_t)r;
 }

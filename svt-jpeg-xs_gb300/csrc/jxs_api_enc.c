@@ -14,6 +14,8 @@
 
 #include "SvtJpegxsEnc.h"
 #include "jxs_core.h"
+#include "SvtJpegxsGpu.h"
+#include "jxs_batch.h"
 #include "jxs_gpu.h"
 #include "jxs_queue.h"
 
@@ -163,11 +165,8 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_encoder_init(uint64_t version_api_major
     return SvtJxsErrorNone;
 }
 
-PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_encoder_send_picture(svt_jpeg_xs_encoder_api_t* enc_api, svt_jpeg_xs_frame_t* in,
-                                                              uint8_t blocking_flag) {
-    if (!enc_api || !enc_api->private_ptr || !in) return SvtJxsErrorBadParameter;
-    enc_prv_t* p = (enc_prv_t*)enc_api->private_ptr;
-    const jxs_cfg_t* c = p->cfg;
+/* send_picture's checks of a frame (EncHandle.c:955-990) */
+static SvtJxsErrorType_t check_frame(const jxs_cfg_t* c, const svt_jpeg_xs_frame_t* in) {
     if (in->bitstream.allocation_size < c->lcod || !in->bitstream.buffer) return SvtJxsErrorBadParameter;
     const uint32_t ps = c->depth <= 8 ? 1 : 2;
     for (uint32_t k = 0; k < c->nc; k++) {
@@ -178,6 +177,15 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_encoder_send_picture(svt_jpeg_xs_encode
             min_size = (uint64_t)in->image.stride[0] * ps * (c->H - 1) + (uint64_t)c->W * 3 * ps;
         if (in->image.alloc_size[k] < min_size) return SvtJxsErrorBadParameter;
     }
+    return SvtJxsErrorNone;
+}
+
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_encoder_send_picture(svt_jpeg_xs_encoder_api_t* enc_api, svt_jpeg_xs_frame_t* in,
+                                                              uint8_t blocking_flag) {
+    if (!enc_api || !enc_api->private_ptr || !in) return SvtJxsErrorBadParameter;
+    enc_prv_t* p = (enc_prv_t*)enc_api->private_ptr;
+    const SvtJxsErrorType_t bad = check_frame(p->cfg, in);
+    if (bad) return bad;
     const int slot = jxs_queue_acquire(&p->q, blocking_flag);
     if (slot < 0) return SvtJxsErrorNoErrorEmptyQueue;
     p->frame[slot] = *in;
@@ -277,4 +285,35 @@ PREFIX_API uint64_t svt_jpeg_xs_gpu_encoder_read_timing(svt_jpeg_xs_encoder_api_
 PREFIX_API uint32_t svt_jpeg_xs_gpu_encoder_read_kernel_timing(svt_jpeg_xs_encoder_api_t* enc_api, double* kernel_ms, uint32_t n) {
     if (!enc_api || !enc_api->private_ptr || !kernel_ms) return 0;
     return (uint32_t)jxs_gpu_enc_read_kernel_timing(((enc_prv_t*)enc_api->private_ptr)->gpu, kernel_ms, (int)n);
+}
+
+/* Batched encode (SvtJpegxsGpu.h): frame i with the configuration of
+ * enc[i].  The frames are checked as send_picture checks them; none of them
+ * goes through the handle's queue, so a handle may serve batches and
+ * send_picture alike. */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_encode(svt_jpeg_xs_gpu_batch_t* batch, svt_jpeg_xs_encoder_api_t* const* enc,
+                                                          svt_jpeg_xs_frame_t* const* frames, uint32_t n, void* cuda_stream) {
+    if (!batch || !enc || !frames || n == 0 || n > SVT_JPEGXS_GPU_BATCH_MAX) return SvtJxsErrorBadParameter;
+    jxs_gpu_enc_t* gpu[SVT_JPEGXS_GPU_BATCH_MAX];
+    void* planes[SVT_JPEGXS_GPU_BATCH_MAX][4];
+    uint32_t strides[SVT_JPEGXS_GPU_BATCH_MAX][4];
+    uint8_t* out[SVT_JPEGXS_GPU_BATCH_MAX];
+    for (uint32_t i = 0; i < n; i++) {
+        if (!enc[i] || !enc[i]->private_ptr || !frames[i]) return SvtJxsErrorBadParameter;
+        const enc_prv_t* p = (const enc_prv_t*)enc[i]->private_ptr;
+        const SvtJxsErrorType_t bad = check_frame(p->cfg, frames[i]);
+        if (bad) return bad;
+        gpu[i] = p->gpu;
+        for (int k = 0; k < 4; k++) {
+            planes[i][k] = frames[i]->image.data_yuv[k];
+            strides[i][k] = frames[i]->image.stride[k];
+        }
+        out[i] = frames[i]->bitstream.buffer;
+        /* constant bit rate: every frame is exactly Lcod bytes */
+        frames[i]->bitstream.used_size = p->cfg->lcod;
+        frames[i]->bitstream.last_packet_in_frame = 1;
+    }
+    const int32_t r = jxs_gpu_batch_encode((jxs_gpu_batch_t*)batch, gpu, n, (void* const(*)[4])planes,
+                                           (const uint32_t(*)[4])strides, out, cuda_stream);
+    return (SvtJxsErrorType_t)r;
 }

@@ -179,10 +179,9 @@ DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uin
  *   pass 2  warp per segment: GCLI = gtli + ones in the codeword; data bits;
  *   pass 3  warp per segment: data bits at warp-scanned offsets, decoded and
  *           written as int16 coefficients (8 bytes per lane, coalesced). */
-__global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs,
-                                                            uint32_t bs_size, const uint32_t* __restrict__ prec_off,
-                                                            int16_t* __restrict__ coef, uint32_t cap_bytes, uint32_t cap_groups,
-                                                            int* status) {
+__device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t bs_size,
+                                            const uint32_t* __restrict__ prec_off, int16_t* __restrict__ coef,
+                                            uint32_t cap_bytes, uint32_t cap_groups, int* status, const int p) {
     extern __shared__ __align__(16) uint8_t dsm[];
     uint8_t* pbuf = dsm;
     uint8_t* gcl = dsm + cap_bytes + 32;
@@ -204,7 +203,6 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
     __shared__ int s_err;
     __shared__ uint32_t s_total, s_lead, s_tw, s_npk;
 
-    const int p = blockIdx.x;
     const int last = (p + 1 >= (int)cfg->np);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) s_err = *(volatile int*)status;
@@ -600,9 +598,8 @@ DEV uint32_t be24(const uint8_t* p) { return ((uint32_t)p[0] << 16) | ((uint32_t
  * split of Lcod puts it (EncHandle.c:760-809); its precincts are found by
  * following the 24-bit precinct lengths, and the walk must end exactly at
  * the next slice (or at EOC).  Any mismatch raises *walk_bad. */
-__global__ void walk_slices_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t size,
-                                   uint32_t* __restrict__ prec_off, int* walk_bad) {
-    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+DEV void walk_slice(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t size,
+                    uint32_t* __restrict__ prec_off, int* walk_bad, const uint32_t s) {
     if (s >= cfg->nslices) return;
     if (cfg->max_slice_budget == 0) {
         *walk_bad = 1;
@@ -636,8 +633,8 @@ __global__ void walk_slices_kernel(const jxs_cfg_t* __restrict__ cfg, const uint
 
 /* Fallback when the prediction failed: one thread walks the whole codestream
  * from the header (get_slice_size, DecThreadInit.c:35-131). */
-__global__ void walk_sequential_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t size,
-                                       uint32_t* __restrict__ prec_off, const int* walk_bad, int* status) {
+DEV void walk_sequential(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t size,
+                         uint32_t* __restrict__ prec_off, const int* walk_bad, int* status) {
     if (!*walk_bad) return;
     uint64_t off = cfg->hdr_len;
     for (uint32_t s = 0; s < cfg->nslices; s++) {
@@ -671,6 +668,56 @@ __global__ void walk_sequential_kernel(const jxs_cfg_t* __restrict__ cfg, const 
 }
 
 /* ------------------------------------------------------------------------ */
+/* kernels: one frame, or a batch of frames                                  */
+/* ------------------------------------------------------------------------ */
+__global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs,
+                                                            uint32_t bs_size, const uint32_t* __restrict__ prec_off,
+                                                            int16_t* __restrict__ coef, uint32_t cap_bytes, uint32_t cap_groups,
+                                                            int* status) {
+    unpack_body(cfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status, (int)blockIdx.x);
+}
+
+/* cap_bytes / cap_groups: the largest of the batch's frames (shared-memory
+ * layout of the launch) */
+__global__ void __launch_bounds__(UK_THREADS) unpack_batch_kernel(const __grid_constant__ DecPrecLaunch L, uint32_t cap_bytes,
+                                                                  uint32_t cap_groups) {
+    const DecPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
+    unpack_body(F.cfg, F.bs, F.bs_size, F.prec_off, F.coef, cap_bytes, cap_groups, F.status, (int)blockIdx.x - F.first_block);
+}
+
+__global__ void walk_slices_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t size,
+                                   uint32_t* __restrict__ prec_off, int* walk_bad) {
+    walk_slice(cfg, bs, size, prec_off, walk_bad, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__global__ void walk_sequential_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t size,
+                                       uint32_t* __restrict__ prec_off, const int* walk_bad, int* status) {
+    walk_sequential(cfg, bs, size, prec_off, walk_bad, status);
+}
+
+/* one thread per slice of every frame of the batch */
+__global__ void walk_slices_batch_kernel(const __grid_constant__ DecPrecLaunch L) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= L.nslices) return;
+    int lo = 0, hi = L.nframes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (g >= L.job[mid].first_slice) lo = mid;
+        else hi = mid - 1;
+    }
+    const DecPrecFrame& F = L.job[lo];
+    walk_slice(F.cfg, F.bs, F.bs_size, F.prec_off, F.status + 1, (uint32_t)(g - F.first_slice));
+}
+
+/* one thread per frame of the batch */
+__global__ void walk_sequential_batch_kernel(const __grid_constant__ DecPrecLaunch L) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= L.nframes) return;
+    const DecPrecFrame& F = L.job[f];
+    walk_sequential(F.cfg, F.bs, F.bs_size, F.prec_off, F.status + 1, F.status);
+}
+
+/* ------------------------------------------------------------------------ */
 /* host-side launchers                                                       */
 /* ------------------------------------------------------------------------ */
 extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, const uint8_t* bs, uint32_t size, uint32_t* prec_off,
@@ -690,3 +737,19 @@ extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* b
     return cudaGetLastError();
 }
 
+
+extern "C" cudaError_t jxs_launch_walk_batch(const DecPrecLaunch* L, cudaStream_t st) {
+    if (L->nframes <= 0) return cudaSuccess;
+    walk_slices_batch_kernel<<<(L->nslices + 127) / 128, 128, 0, st>>>(*L);
+    walk_sequential_batch_kernel<<<(L->nframes + 31) / 32, 32, 0, st>>>(*L);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t jxs_launch_unpack_batch(const DecPrecLaunch* L, uint32_t cap_bytes, uint32_t cap_groups, cudaStream_t st) {
+    const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 2ull * UK_ZCAP(cap_groups);
+    cudaError_t e = cudaFuncSetAttribute(unpack_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (L->nblocks <= 0) return cudaSuccess;
+    unpack_batch_kernel<<<L->nblocks, UK_THREADS, smem, st>>>(*L, cap_bytes, cap_groups);
+    return cudaGetLastError();
+}

@@ -192,9 +192,9 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
  *   costs       per packet, data / significance / GCLI bytes rounded
  *               separately, raw fallback when cheaper; summed over packets
  *               for every (Q, R). */
-__global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
-                                                           uint32_t* __restrict__ cost, uint32_t* __restrict__ slice_done,
-                                                           PrecRC* __restrict__ rc, int* __restrict__ status) {
+__device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
+                                             uint32_t* __restrict__ cost, uint32_t* __restrict__ slice_done,
+                                             PrecRC* __restrict__ rc, int* __restrict__ status, const int p) {
     /* per band line: GCLI and significance-maximum histograms, then per gtli
      * data / GCLI bits without and with significance; the area is reused by
      * the slice selection at the end */
@@ -216,7 +216,6 @@ __global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __
     __shared__ uint64_t s_grow[JXS_MAXBLINES];
     __shared__ uint8_t s_pkbl0[JXS_MAXPK], s_pknbl[JXS_MAXPK], s_order[JXS_MAXBLINES];
 
-    const int p = blockIdx.x;
     const int last = (p + 1 >= (int)cfg->np);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t nbl = cfg->nbline[last], nseg = cfg->nseg[last], SG = cfg->seg_groups;
@@ -515,9 +514,9 @@ struct PkLine {
  *   pass B  each lane one group: significance flags, the unary GCLI code and
  *           the data bits, at positions from a warp prefix sum, OR-ed into
  *           the buffer. */
-__global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
-                                                          const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
-                                                          uint8_t* __restrict__ out, uint32_t cap_words, int* status) {
+__device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
+                                          const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
+                                          uint8_t* __restrict__ out, uint32_t cap_words, int* status, const int p) {
     extern __shared__ __align__(16) uint32_t buf[];
     __shared__ uint32_t s_data[JXS_MAXSEG], s_vlc[JXS_MAXSEG], s_zero[JXS_MAXSEG];
     __shared__ PkLine pl[JXS_MAXBLINES];
@@ -536,7 +535,6 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __
     __shared__ uint32_t s_praw[JXS_MAXPK];
     __shared__ int s_ok;
 
-    const int p = blockIdx.x;
     const int last = (p + 1 >= (int)cfg->np);
     const PrecRC R = rc[p];
     /* nothing to pack once the rate control failed somewhere in the frame;
@@ -898,6 +896,31 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __
 }
 
 /* ------------------------------------------------------------------------ */
+/* kernels: one frame, or a batch of frames (block -> frame by its first block) */
+/* ------------------------------------------------------------------------ */
+__global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
+                                                           uint32_t* __restrict__ cost, uint32_t* __restrict__ slice_done,
+                                                           PrecRC* __restrict__ rc, int* __restrict__ status) {
+    rc_cost_body(cfg, gcli, cost, slice_done, rc, status, (int)blockIdx.x);
+}
+
+__global__ void __launch_bounds__(RC_THREADS) rc_cost_batch_kernel(const __grid_constant__ EncPrecLaunch L) {
+    const EncPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
+    rc_cost_body(F.cfg, F.gcli, F.cost, F.slice_done, F.rc, F.status, (int)blockIdx.x - F.first_block);
+}
+
+__global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
+                                                          const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
+                                                          uint8_t* __restrict__ out, uint32_t cap_words, int* status) {
+    pack_body(cfg, coef, gcli, rc, out, cap_words, status, (int)blockIdx.x);
+}
+
+__global__ void __launch_bounds__(PK_THREADS, 3) pack_batch_kernel(const __grid_constant__ EncPrecLaunch L, uint32_t cap_words) {
+    const EncPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
+    pack_body(F.cfg, F.coef, F.gcli, F.rc, F.out, cap_words, F.status, (int)blockIdx.x - F.first_block);
+}
+
+/* ------------------------------------------------------------------------ */
 /* host-side launchers                                                       */
 /* ------------------------------------------------------------------------ */
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
@@ -913,5 +936,20 @@ extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const
     cudaError_t e = cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     pack_kernel<<<np, PK_THREADS, smem, st>>>(dcfg, coef, gcli, rc, out, cap_words, status);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, cudaStream_t st) {
+    if (L->nblocks <= 0) return cudaSuccess;
+    rc_cost_batch_kernel<<<L->nblocks, RC_THREADS, 0, st>>>(*L);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t jxs_launch_pack_batch(const EncPrecLaunch* L, uint32_t cap_words, cudaStream_t st) {
+    const size_t smem = (size_t)cap_words * 4;
+    cudaError_t e = cudaFuncSetAttribute(pack_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (L->nblocks <= 0) return cudaSuccess;
+    pack_batch_kernel<<<L->nblocks, PK_THREADS, smem, st>>>(*L, cap_words);
     return cudaGetLastError();
 }

@@ -195,10 +195,10 @@ DEV void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
 struct FvTile {
     int jb, r0, c0, npairs, ncp, rc, hc;
 };
-DEV FvTile fv_tile(const FwdVLaunch& L, int t) {
+template <int NJ>
+DEV FvTile fv_tile(const FwdVLaunchN<NJ>& L, int t) {
     FvTile T;
-    int jb = 0;
-    while (jb + 1 < L.njobs && t >= L.job[jb + 1].first_block) jb++;
+    const int jb = find_job<NJ>(L.job, L.njobs, t);
     const FwdVJob& J = L.job[jb];
     const int u = t - J.first_block;
     const int ty = u / J.col_tiles, tx = u - ty * J.col_tiles;
@@ -218,8 +218,8 @@ DEV FvTile fv_tile(const FwdVLaunch& L, int t) {
 /* Stages the input of tile t into buffer `in` (FV_NR rows x column pairs):
  * asynchronous copies where the pair is inside the plane and aligned,
  * ordinary loads (with the symmetric extension) elsewhere. */
-template <int SRC>
-DEV void fv_stage(const FwdVLaunch& L, int t, typename FvIn<SRC>::T* in) {
+template <int SRC, int NJ>
+DEV void fv_stage(const FwdVLaunchN<NJ>& L, int t, typename FvIn<SRC>::T* in) {
     const FvTile T = fv_tile(L, t);
     const FwdVJob& J = L.job[T.jb];
     const int cp = threadIdx.x;
@@ -259,28 +259,27 @@ DEV void fv_stage(const FwdVLaunch& L, int t, typename FvIn<SRC>::T* in) {
  * next tile's input is staged (asynchronous copies) while the current one is
  * lifted.  With `persistent` false (int32 low bands, still in L2) the grid
  * has one block per tile and a single buffer. */
-template <int SRC>
-__global__ void __launch_bounds__(FV_THREADS, 6) fwd_v_kernel(const __grid_constant__ FwdVLaunch L, const jxs_band_t* __restrict__ bands,
-                                                           uint16_t* __restrict__ coef, uint8_t* __restrict__ gcli) {
+template <int SRC, int NJ>
+__global__ void __launch_bounds__(FV_THREADS, 6) fwd_v_kernel(const __grid_constant__ FwdVLaunchN<NJ> L) {
     typedef typename FvIn<SRC>::T InT;
     extern __shared__ __align__(16) unsigned char fv_dyn[];
     InT* inbuf = (InT*)fv_dyn; /* [2][FV_NR][FV_THREADS] */
     __shared__ __align__(16) int32_t sL[FV_ROWPAIRS][FV_SROW];
     __shared__ __align__(16) int32_t sH[FV_ROWPAIRS][FV_SROW];
-    const int depth = L.depth;
     const int warp = threadIdx.x >> 5;
     const bool persistent = gridDim.x < (unsigned)L.ntiles;
     int t = blockIdx.x, buf = 0;
-    if (t < L.ntiles) fv_stage<SRC>(L, t, inbuf);
+    if (t < L.ntiles) fv_stage<SRC, NJ>(L, t, inbuf);
     cp_async_commit();
     for (; t < L.ntiles; t += gridDim.x) {
         const int tn = t + gridDim.x;
-        if (persistent && tn < L.ntiles) fv_stage<SRC>(L, tn, inbuf + (buf ^ 1) * FV_NR * FV_THREADS);
+        if (persistent && tn < L.ntiles) fv_stage<SRC, NJ>(L, tn, inbuf + (buf ^ 1) * FV_NR * FV_THREADS);
         cp_async_commit();
         cp_async_wait1();
         __syncthreads();
         const FvTile T = fv_tile(L, t);
         const FwdVJob& J = L.job[T.jb];
+        const int depth = J.depth;
         const InT* in = inbuf + buf * FV_NR * FV_THREADS;
         /* vertical lifting, one column pair per thread */
         const int cp = threadIdx.x;
@@ -319,7 +318,7 @@ __global__ void __launch_bounds__(FV_THREADS, 6) fwd_v_kernel(const __grid_const
         for (int r = warp; r < T.rc + T.hc; r += FV_THREADS / 32) {
             if (r < T.rc) {
                 const int row = T.r0 + r;
-                const BandRow bhl = band_row(bands[J.b_hl], row, coef, gcli);
+                const BandRow bhl = band_row(J.bands[J.b_hl], row, J.coef, J.gcli);
                 int32_t* ll = J.ll + (long long)row * J.ll_pitch;
                 warp_lift_fwd(&sL[r][4], T.npairs, [&](int j, const int32_t* sv, const int32_t* d) {
                     const int jj = jc + j;
@@ -333,8 +332,8 @@ __global__ void __launch_bounds__(FV_THREADS, 6) fwd_v_kernel(const __grid_const
                 });
             } else {
                 const int row = T.r0 + r - T.rc;
-                const BandRow blh = band_row(bands[J.b_lh], row, coef, gcli);
-                const BandRow bhh = band_row(bands[J.b_hh], row, coef, gcli);
+                const BandRow blh = band_row(J.bands[J.b_lh], row, J.coef, J.gcli);
+                const BandRow bhh = band_row(J.bands[J.b_hh], row, J.coef, J.gcli);
                 warp_lift_fwd(&sH[r - T.rc][4], T.npairs, [&](int j, const int32_t* sv, const int32_t* d) {
                     emit4(blh, jc + j, sv[0], sv[1], sv[2], sv[3]);
                     emit4(bhh, jc + j, d[0], d[1], d[2], d[3]);
@@ -359,13 +358,10 @@ DEV void fill_halo(int32_t* x, int n, int lane) {
     }
 }
 
-template <int SRC>
-__global__ void __launch_bounds__(FH_MAX_WARPS * 32) fwd_h_kernel(const __grid_constant__ FwdHLaunch L, const jxs_band_t* __restrict__ bands,
-                                                              uint16_t* __restrict__ coef, uint8_t* __restrict__ gcli) {
+template <int SRC, int NJ>
+__global__ void __launch_bounds__(FH_MAX_WARPS * 32) fwd_h_kernel(const __grid_constant__ FwdHLaunchN<NJ> L) {
     extern __shared__ __align__(16) int32_t hsm[];
-    int jb = 0;
-    while (jb + 1 < L.njobs && (int)blockIdx.x >= L.job[jb + 1].first_block) jb++;
-    const FwdHJob& J = L.job[jb];
+    const FwdHJob& J = L.job[find_job<NJ>(L.job, L.njobs, (int)blockIdx.x)];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int row = (blockIdx.x - J.first_block) * L.rows_per_block + warp;
     if (row >= J.h) return;
@@ -373,7 +369,7 @@ __global__ void __launch_bounds__(FH_MAX_WARPS * 32) fwd_h_kernel(const __grid_c
     /* per warp: buffer A (n + 8 words) and buffer B (n/2 + 8 words) */
     int32_t* bufA = hsm + warp * L.warp_words + 4;
     int32_t* bufB = bufA + ((n + 8 + 3) & ~3);
-    for (int x = lane; x < n; x += 32) bufA[x] = load1<SRC>(J.src, J.src_pitch, J.chan, L.depth, row, x);
+    for (int x = lane; x < n; x += 32) bufA[x] = load1<SRC>(J.src, J.src_pitch, J.chan, J.depth, row, x);
     __syncwarp();
     fill_halo(bufA, n, lane);
     __syncwarp();
@@ -382,7 +378,7 @@ __global__ void __launch_bounds__(FH_MAX_WARPS * 32) fwd_h_kernel(const __grid_c
     int m = n;
     for (int e = 0; e < J.nh; e++) {
         if (m == 1) break; /* nothing left to split: the remaining high bands are empty */
-        const BandRow bd = band_row(bands[J.b_hf[e]], row, coef, gcli);
+        const BandRow bd = band_row(J.bands[J.b_hf[e]], row, J.coef, J.gcli);
         const int m1 = (m + 1) >> 1;
         int32_t* dst = nxt;
         warp_lift_fwd(cur, m1, [&](int j, const int32_t* sv, const int32_t* d) {
@@ -402,7 +398,7 @@ __global__ void __launch_bounds__(FH_MAX_WARPS * 32) fwd_h_kernel(const __grid_c
         m = m1;
     }
     /* final low band */
-    const BandRow bl = band_row(bands[J.b_ll], row, coef, gcli);
+    const BandRow bl = band_row(J.bands[J.b_ll], row, J.coef, J.gcli);
     for (int j = 4 * lane; j < m; j += 128) {
         int32_t v[4];
         for (int q = 0; q < 4; q++) v[q] = j + q < m ? cur[j + q] : 0;
@@ -417,52 +413,74 @@ extern "C" int jxs_fwd_v_tile_rows(void) { return FV_ROWPAIRS; }
 extern "C" int jxs_fwd_v_tile_cols(void) { return FV_COLS; }
 extern "C" int jxs_fwd_h_max_rows_per_block(void) { return FH_MAX_WARPS; }
 
-template <int SRC>
-static cudaError_t launch_v(const FwdVLaunch* L, int ntiles, const jxs_band_t* bands, uint16_t* coef, uint8_t* gcli, cudaStream_t st) {
+template <int SRC, int NJ>
+static cudaError_t launch_v(const FwdVLaunchN<NJ>* L, int grid_per_sm, cudaStream_t st) {
     /* int32 inputs (the previous level's low band, in L2): one block per
-     * tile, one buffer; sample planes: persistent, double-buffered */
+     * tile, one buffer; sample planes: persistent, double-buffered, with
+     * grid_per_sm blocks per SM (0: as many as fit) */
     const bool persistent = SRC != SRC_I32;
     const size_t smem = (persistent ? 2 : 1) * FV_NR * FV_THREADS * sizeof(typename FvIn<SRC>::T);
-    cudaError_t e = cudaFuncSetAttribute(fwd_v_kernel<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(fwd_v_kernel<SRC, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0, per_sm = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd_v_kernel<SRC>, FV_THREADS, smem)) != cudaSuccess) return e;
-    int blocks = persistent ? sms * (per_sm > 0 ? per_sm : 1) : ntiles;
-    if (blocks > ntiles) blocks = ntiles;
-    fwd_v_kernel<SRC><<<blocks, FV_THREADS, smem, st>>>(*L, bands, coef, gcli);
+    int blocks = L->ntiles;
+    if (persistent) {
+        int dev = 0, sms = 0, per_sm = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd_v_kernel<SRC, NJ>, FV_THREADS, smem)) != cudaSuccess)
+            return e;
+        if (per_sm < 1) per_sm = 1;
+        if (grid_per_sm > 0 && grid_per_sm < per_sm) per_sm = grid_per_sm;
+        blocks = sms * per_sm;
+        if (blocks > L->ntiles) blocks = L->ntiles;
+    }
+    if (blocks <= 0) return cudaSuccess;
+    fwd_v_kernel<SRC, NJ><<<blocks, FV_THREADS, smem, st>>>(*L);
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t jxs_launch_fwd_v(const FwdVLaunch* L, int src_kind, int ntiles, const jxs_band_t* bands, uint16_t* coef,
-                                        uint8_t* gcli, cudaStream_t st) {
+template <int NJ>
+static cudaError_t launch_v_kind(const FwdVLaunchN<NJ>* L, int src_kind, int grid_per_sm, cudaStream_t st) {
     switch (src_kind) {
-    case SRC_I32: return launch_v<SRC_I32>(L, ntiles, bands, coef, gcli, st);
-    case SRC_U8: return launch_v<SRC_U8>(L, ntiles, bands, coef, gcli, st);
-    case SRC_U16: return launch_v<SRC_U16>(L, ntiles, bands, coef, gcli, st);
-    case SRC_PK8: return launch_v<SRC_PK8>(L, ntiles, bands, coef, gcli, st);
-    default: return launch_v<SRC_PK16>(L, ntiles, bands, coef, gcli, st);
+    case SRC_I32: return launch_v<SRC_I32, NJ>(L, grid_per_sm, st);
+    case SRC_U8: return launch_v<SRC_U8, NJ>(L, grid_per_sm, st);
+    case SRC_U16: return launch_v<SRC_U16, NJ>(L, grid_per_sm, st);
+    case SRC_PK8: return launch_v<SRC_PK8, NJ>(L, grid_per_sm, st);
+    default: return launch_v<SRC_PK16, NJ>(L, grid_per_sm, st);
     }
 }
 
-template <int SRC>
-static cudaError_t launch_h(const FwdHLaunch* L, int nblocks, size_t smem, const jxs_band_t* bands, uint16_t* coef, uint8_t* gcli,
-                            cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(fwd_h_kernel<SRC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    fwd_h_kernel<SRC><<<nblocks, L->rows_per_block * 32, smem, st>>>(*L, bands, coef, gcli);
-    return cudaGetLastError();
+extern "C" cudaError_t jxs_launch_fwd_v(const FwdVLaunch* L, int src_kind, int grid_per_sm, cudaStream_t st) {
+    return launch_v_kind<JXS_MAXC>(L, src_kind, grid_per_sm, st);
+}
+extern "C" cudaError_t jxs_launch_fwd_v_batch(const FwdVLaunchB* L, int src_kind, int grid_per_sm, cudaStream_t st) {
+    return launch_v_kind<JXS_BATCH_JOBS>(L, src_kind, grid_per_sm, st);
 }
 
-extern "C" cudaError_t jxs_launch_fwd_h(const FwdHLaunch* L, int src_kind, int nblocks, const jxs_band_t* bands, uint16_t* coef,
-                                        uint8_t* gcli, cudaStream_t st) {
+template <int SRC, int NJ>
+static cudaError_t launch_h(const FwdHLaunchN<NJ>* L, int nblocks, cudaStream_t st) {
     const size_t smem = (size_t)L->warp_words * L->rows_per_block * sizeof(int32_t);
+    cudaError_t e = cudaFuncSetAttribute(fwd_h_kernel<SRC, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (nblocks <= 0) return cudaSuccess;
+    fwd_h_kernel<SRC, NJ><<<nblocks, L->rows_per_block * 32, smem, st>>>(*L);
+    return cudaGetLastError();
+}
+
+template <int NJ>
+static cudaError_t launch_h_kind(const FwdHLaunchN<NJ>* L, int src_kind, int nblocks, cudaStream_t st) {
     switch (src_kind) {
-    case SRC_I32: return launch_h<SRC_I32>(L, nblocks, smem, bands, coef, gcli, st);
-    case SRC_U8: return launch_h<SRC_U8>(L, nblocks, smem, bands, coef, gcli, st);
-    case SRC_U16: return launch_h<SRC_U16>(L, nblocks, smem, bands, coef, gcli, st);
-    case SRC_PK8: return launch_h<SRC_PK8>(L, nblocks, smem, bands, coef, gcli, st);
-    default: return launch_h<SRC_PK16>(L, nblocks, smem, bands, coef, gcli, st);
+    case SRC_I32: return launch_h<SRC_I32, NJ>(L, nblocks, st);
+    case SRC_U8: return launch_h<SRC_U8, NJ>(L, nblocks, st);
+    case SRC_U16: return launch_h<SRC_U16, NJ>(L, nblocks, st);
+    case SRC_PK8: return launch_h<SRC_PK8, NJ>(L, nblocks, st);
+    default: return launch_h<SRC_PK16, NJ>(L, nblocks, st);
     }
+}
+
+extern "C" cudaError_t jxs_launch_fwd_h(const FwdHLaunch* L, int src_kind, int nblocks, cudaStream_t st) {
+    return launch_h_kind<JXS_MAXC>(L, src_kind, nblocks, st);
+}
+extern "C" cudaError_t jxs_launch_fwd_h_batch(const FwdHLaunchB* L, int src_kind, int nblocks, cudaStream_t st) {
+    return launch_h_kind<JXS_BATCH_JOBS>(L, src_kind, nblocks, st);
 }

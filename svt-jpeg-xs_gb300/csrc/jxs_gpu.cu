@@ -15,35 +15,14 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "SvtJpegxs.h"
+#include "jxs_batch.h"
 #include "jxs_gpu.h"
 #include "jxs_kernels.cuh"
-
-extern "C" cudaError_t jxs_launch_fwd_v(const FwdVLaunch* L, int src_kind, int nblocks, const jxs_band_t* bands, uint16_t* coef,
-                                        uint8_t* gcli, cudaStream_t st);
-extern "C" cudaError_t jxs_launch_fwd_h(const FwdHLaunch* L, int src_kind, int nblocks, const jxs_band_t* bands, uint16_t* coef,
-                                        uint8_t* gcli, cudaStream_t st);
-extern "C" int jxs_fwd_v_tile_rows(void);
-extern "C" int jxs_fwd_v_tile_cols(void);
-extern "C" int jxs_fwd_h_max_rows_per_block(void);
-extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
-                                     uint32_t* slice_done, PrecRC* rc, int* status, cudaStream_t st);
-extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
-                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st);
-extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
-                                         int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status,
-                                         cudaStream_t st);
-extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, const uint8_t* bs, uint32_t size, uint32_t* prec_off,
-                                       int* walk_bad, int* status, cudaStream_t st);
-extern "C" cudaError_t jxs_launch_inv_v(const InvVLaunch* L, int out_kind, int nblocks, const jxs_band_t* bands, const int16_t* coef,
-                                        cudaStream_t st);
-extern "C" cudaError_t jxs_launch_inv_h(const InvHLaunch* L, int out_kind, int nblocks, const jxs_band_t* bands, const int16_t* coef,
-                                        cudaStream_t st);
-extern "C" int jxs_inv_v_tile_rows(void);
-extern "C" int jxs_inv_v_tile_cols(void);
-extern "C" int jxs_inv_h_max_rows_per_block(void);
+#include "jxs_plan.cuh"
 
 #define CK(x)                                                                                      \
     do {                                                                                           \
@@ -54,7 +33,6 @@ extern "C" int jxs_inv_h_max_rows_per_block(void);
         }                                                                                          \
     } while (0)
 
-static const size_t kSmemMax = 220 * 1024;
 /* timing mode: events around every kernel of a frame */
 #define JXS_KEV 17
 #define KMARK()                                                          \
@@ -101,49 +79,6 @@ extern "C" int jxs_gpu_device_count(void) {
     return n;
 }
 
-static inline uint32_t div_up(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
-
-/* size of component c at vertical level v (region transformed by level v) */
-static void level_dims(const jxs_comp_t& cp, int v, uint32_t* w, uint32_t* h) {
-    uint32_t ww = cp.w, hh = cp.h;
-    for (int i = 0; i < v; i++) {
-        ww = (ww + 1) / 2;
-        hh = (hh + 1) / 2;
-    }
-    *w = ww;
-    *h = hh;
-}
-
-static uint32_t bytes_per_sample(const jxs_cfg_t* c) { return c->depth <= 8 ? 1 : 2; }
-
-/* address of the band table inside the device copy of the configuration */
-static const jxs_band_t* dev_bands(const jxs_cfg_t* dcfg) {
-    return (const jxs_band_t*)((const char*)dcfg + offsetof(jxs_cfg_t, band));
-}
-
-/* Fills the band indices of a job for vertical level v of component c
- * (bands of level v: HH = nb-1-3v, LH = HH-1, HL = HH-2; then one high band
- * per horizontal-only level and the final low band). */
-static void job_bands(const jxs_cfg_t* cfg, int c, int v, DwtJob* J) {
-    const jxs_comp_t& cp = cfg->comp[c];
-    const int b0 = cp.band0;
-    if (cp.dv == 0) {
-        J->last = 1;
-        J->nh = cp.dh;
-        for (uint32_t e = 0; e < cp.dh; e++) J->b_hf[e] = b0 + (int)cp.nb - 1 - (int)e;
-        J->b_ll = b0;
-        return;
-    }
-    const int L = (int)cp.nb - 1 - 3 * v;
-    J->b_hh = b0 + L;
-    J->b_lh = b0 + L - 1;
-    J->b_hl = b0 + L - 2;
-    J->last = (v + 1 == (int)cp.dv);
-    J->nh = J->last ? (int)(cp.dh - cp.dv) : 0;
-    for (int e = 0; e < J->nh; e++) J->b_hf[e] = b0 + L - 3 - e;
-    J->b_ll = b0 + L - 3 - J->nh;
-}
-
 /* ------------------------------------------------------------------------ */
 /* Encoder                                                                   */
 /* ------------------------------------------------------------------------ */
@@ -184,8 +119,11 @@ struct jxs_gpu_enc {
     double kern_ms[JXS_KEV];
     int nkern;
     uint64_t timed_frames;
+    uint64_t serial;             /* process-unique: identifies the handle's layout to the batch engine */
     std::mutex mu;
 };
+
+static std::atomic<uint64_t> g_serial{1};
 
 static inline cudaStream_t enc_stream(const jxs_gpu_enc_t* e, const EncSlot* s) {
     const cudaStream_t u = e->user_stream[s - e->slot];
@@ -274,6 +212,7 @@ extern "C" jxs_gpu_enc_t* jxs_gpu_enc_create(const jxs_cfg_t* cfg, int nslots, i
     memset(&e->slot, 0, sizeof(e->slot));
     e->cfg = *cfg;
     e->nslots = 0;
+    e->serial = g_serial++;
     /* the packing kernel stages a whole precinct in shared memory, starting
      * up to 15 bytes into the buffer for aligned stores: bound it by the
      * largest slice budget */
@@ -338,91 +277,40 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
     /* forward transform: one launch per vertical level, then the
      * horizontal-only levels of every component (one launch per source
      * kind) */
-    uint32_t max_dv = 0;
-    for (uint32_t k = 0; k < c->nc; k++) max_dv = c->comp[k].dv > max_dv ? c->comp[k].dv : max_dv;
-    const int level0_kind = packed ? (bps == 1 ? SRC_PK8 : SRC_PK16) : (bps == 1 ? SRC_U8 : SRC_U16);
-    const uint32_t vcols = (uint32_t)jxs_fwd_v_tile_cols(), vrows = (uint32_t)jxs_fwd_v_tile_rows();
-    for (int v = 0; v < (int)max_dv; v++) {
+    FrameBufs fb;
+    memset(&fb, 0, sizeof(fb));
+    fb.coef = s->coef;
+    fb.gcli = s->gcli;
+    memcpy(fb.ll, s->ll, sizeof(fb.ll));
+    memcpy(fb.ll_pitch, s->ll_pitch, sizeof(fb.ll_pitch));
+    FramePlanes in;
+    memset(&in, 0, sizeof(in));
+    for (int k = 0; k < nplanes; k++) {
+        in.p[k] = (void*)src[k];
+        in.pitch[k] = pitch[k];
+    }
+    const int level0_kind = enc_level0_kind(c);
+    const int max_dv = (int)cfg_max_dv(c);
+    for (int v = 0; v < max_dv; v++) {
         FwdVLaunch L;
         memset(&L, 0, sizeof(L));
-        L.depth = (int)c->depth;
-        int blocks = 0;
-        for (uint32_t k = 0; k < c->nc; k++) {
-            const jxs_comp_t& cp = c->comp[k];
-            if ((int)cp.dv <= v) continue;
-            FwdVJob& J = L.job[L.njobs++];
-            uint32_t w, h;
-            level_dims(cp, v, &w, &h);
-            J.w = (int)w;
-            J.h = (int)h;
-            if (v == 0) {
-                const int pk = packed ? 0 : (int)k;
-                J.src = src[pk];
-                J.src_pitch = pitch[pk];
-                J.chan = packed ? (int)k : 0;
-                J.vec = !packed && ((uintptr_t)src[pk] % (2 * bps)) == 0 && (pitch[pk] % 2) == 0;
-            } else {
-                J.src = s->ll[v - 1][k];
-                J.src_pitch = s->ll_pitch[v - 1][k];
-                J.vec = 1;
-            }
-            J.ll = s->ll[v][k];
-            J.ll_pitch = s->ll_pitch[v][k];
-            const int top = (int)cp.band0 + (int)cp.nb - 1 - 3 * v;
-            J.b_hh = top;
-            J.b_lh = top - 1;
-            J.b_hl = top - 2;
-            J.col_tiles = (int)div_up(w, vcols);
-            J.first_block = blocks;
-            blocks += J.col_tiles * (int)div_up((h + 1) / 2, vrows);
+        int tiles[JXS_MAXC];
+        L.njobs = plan_fwd_v(c, e->dcfg, fb, in, v, L.job, tiles);
+        for (int i = 0; i < L.njobs; i++) {
+            L.job[i].first_block = L.ntiles;
+            L.ntiles += tiles[i];
         }
-        L.ntiles = blocks;
-        CK(jxs_launch_fwd_v(&L, v == 0 ? level0_kind : SRC_I32, blocks, dev_bands(e->dcfg), s->coef, s->gcli, st));
+        CK(jxs_launch_fwd_v(&L, v == 0 ? level0_kind : SRC_I32, 0, st));
         KMARK();
     }
     for (int pass = 0; pass < 2; pass++) {
-        /* pass 0: components with vertical levels (input: their last int32
-         * low band); pass 1: components without (input: the samples) */
         FwdHLaunch L;
         memset(&L, 0, sizeof(L));
-        L.depth = (int)c->depth;
-        int maxw = 0;
-        for (uint32_t k = 0; k < c->nc; k++) {
-            const jxs_comp_t& cp = c->comp[k];
-            if ((cp.dv > 0) != (pass == 0)) continue;
-            FwdHJob& J = L.job[L.njobs++];
-            uint32_t w, h;
-            level_dims(cp, (int)cp.dv, &w, &h);
-            J.w = (int)w;
-            J.h = (int)h;
-            if (cp.dv > 0) {
-                J.src = s->ll[cp.dv - 1][k];
-                J.src_pitch = s->ll_pitch[cp.dv - 1][k];
-            } else {
-                J.src = src[packed ? 0 : k];
-                J.src_pitch = pitch[packed ? 0 : k];
-                J.chan = packed ? (int)k : 0;
-            }
-            DwtJob bj;
-            memset(&bj, 0, sizeof(bj));
-            job_bands(c, (int)k, cp.dv > 0 ? (int)cp.dv - 1 : 0, &bj);
-            J.nh = bj.nh;
-            for (int e2 = 0; e2 < 5; e2++) J.b_hf[e2] = bj.b_hf[e2];
-            J.b_ll = bj.b_ll;
-            maxw = (int)w > maxw ? (int)w : maxw;
-        }
+        L.njobs = plan_fwd_h(c, e->dcfg, fb, in, pass, L.job);
         if (!L.njobs) continue;
-        L.warp_words = 4 + ((maxw + 8 + 3) & ~3) + (((maxw + 1) / 2 + 8 + 3) & ~3) + 4;
-        int rpb = jxs_fwd_h_max_rows_per_block();
-        while (rpb > 1 && (size_t)L.warp_words * rpb * 4 > kSmemMax) rpb >>= 1;
-        if ((size_t)L.warp_words * rpb * 4 > kSmemMax) return JXS_E_BAD_PARAM;
-        L.rows_per_block = rpb;
-        int blocks = 0;
-        for (int i = 0; i < L.njobs; i++) {
-            L.job[i].first_block = blocks;
-            blocks += (int)div_up((uint32_t)L.job[i].h, (uint32_t)rpb);
-        }
-        CK(jxs_launch_fwd_h(&L, pass == 0 ? SRC_I32 : level0_kind, blocks, dev_bands(e->dcfg), s->coef, s->gcli, st));
+        const int blocks = fwd_h_layout(L, jxs_fwd_h_max_rows_per_block());
+        if (blocks < 0) return JXS_E_BAD_PARAM;
+        CK(jxs_launch_fwd_h(&L, pass == 0 ? SRC_I32 : level0_kind, blocks, st));
         KMARK();
     }
     TMARK(2);
@@ -565,6 +453,7 @@ struct jxs_gpu_dec {
     double kern_ms[JXS_KEV];
     int nkern;
     uint64_t timed_frames;
+    uint64_t serial;
     std::mutex mu;
 };
 
@@ -653,6 +542,7 @@ extern "C" jxs_gpu_dec_t* jxs_gpu_dec_create(const jxs_cfg_t* cfg, int nslots, i
     jxs_gpu_dec_t* d = new jxs_gpu_dec_t();
     memset(&d->slot, 0, sizeof(d->slot));
     d->cfg = *cfg;
+    d->serial = g_serial++;
     uint32_t groups = 0;
     for (uint32_t b = 0; b < cfg->nbands; b++) groups += cfg->band[b].gcli_w * cfg->band[b].lines;
     d->cap_groups = (groups + 64) & ~31u;
@@ -731,100 +621,46 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
 
     int out_dev[JXS_MAXC];
     for (uint32_t k = 0; k < c->nc; k++) out_dev[k] = jxs_gpu_is_device_ptr(planes[k]);
-    uint32_t max_dv = 0;
-    for (uint32_t k = 0; k < c->nc; k++) max_dv = c->comp[k].dv > max_dv ? c->comp[k].dv : max_dv;
     /* horizontal-only levels of every component (into the int32 low band of
      * its last vertical level, or straight to the output plane), then the
      * vertical levels from the deepest up */
-    auto out_ptr = [&](uint32_t k, void** dst, long long* pitch) {
+    FrameBufs fb;
+    memset(&fb, 0, sizeof(fb));
+    fb.coef = s->coef;
+    memcpy(fb.ll, s->ll, sizeof(fb.ll));
+    memcpy(fb.ll_pitch, s->ll_pitch, sizeof(fb.ll_pitch));
+    FramePlanes out;
+    memset(&out, 0, sizeof(out));
+    for (uint32_t k = 0; k < c->nc; k++) {
         if (out_dev[k]) {
-            *dst = planes[k];
-            *pitch = strides[k];
+            out.p[k] = planes[k];
+            out.pitch[k] = strides[k];
         } else {
-            *dst = s->out_stage + s->out_off[k];
-            *pitch = c->comp[k].w;
+            out.p[k] = s->out_stage + s->out_off[k];
+            out.pitch[k] = c->comp[k].w;
         }
-    };
-    const int sample_kind = bps == 1 ? 1 : 2;
+    }
+    const int sample_kind = dec_sample_kind(c);
     for (int pass = 0; pass < 2; pass++) {
-        /* pass 0: components with vertical levels; pass 1: without */
         InvHLaunch L;
         memset(&L, 0, sizeof(L));
-        L.depth = (int)c->depth;
-        L.bw = (int)c->bw;
-        L.fq = (int)c->fq;
-        int maxw = 0;
-        for (uint32_t k = 0; k < c->nc; k++) {
-            const jxs_comp_t& cp = c->comp[k];
-            if ((cp.dv > 0) != (pass == 0)) continue;
-            InvHJob& J = L.job[L.njobs++];
-            uint32_t w, h;
-            level_dims(cp, (int)cp.dv, &w, &h);
-            J.w = (int)w;
-            J.h = (int)h;
-            DwtJob bj;
-            memset(&bj, 0, sizeof(bj));
-            job_bands(c, (int)k, cp.dv > 0 ? (int)cp.dv - 1 : 0, &bj);
-            J.nh = bj.nh;
-            for (int e2 = 0; e2 < 5; e2++) J.b_hf[e2] = bj.b_hf[e2];
-            J.b_ll = bj.b_ll;
-            if (cp.dv > 0) {
-                J.dst = s->ll[cp.dv - 1][k];
-                J.dst_pitch = s->ll_pitch[cp.dv - 1][k];
-            } else {
-                out_ptr(k, &J.dst, &J.dst_pitch);
-            }
-            maxw = (int)w > maxw ? (int)w : maxw;
-        }
+        L.njobs = plan_inv_h(c, d->dcfg, fb, out, pass, L.job);
         if (!L.njobs) continue;
-        L.warp_words = 2 * ((((maxw + 1) / 2) + 8 + 3) & ~3);
-        int rpb = jxs_inv_h_max_rows_per_block();
-        while (rpb > 1 && (size_t)L.warp_words * rpb * 4 > kSmemMax) rpb >>= 1;
-        if ((size_t)L.warp_words * rpb * 4 > kSmemMax) return JXS_E_BAD_PARAM;
-        L.rows_per_block = rpb;
-        int blocks = 0;
-        for (int i2 = 0; i2 < L.njobs; i2++) {
-            L.job[i2].first_block = blocks;
-            blocks += (int)div_up((uint32_t)L.job[i2].h, (uint32_t)rpb);
-        }
-        CK(jxs_launch_inv_h(&L, pass == 0 ? 0 : sample_kind, blocks, dev_bands(d->dcfg), s->coef, st));
+        const int blocks = inv_h_layout(L, jxs_inv_h_max_rows_per_block());
+        if (blocks < 0) return JXS_E_BAD_PARAM;
+        CK(jxs_launch_inv_h(&L, pass == 0 ? 0 : sample_kind, blocks, st));
         KMARK();
     }
-    const uint32_t vcols = (uint32_t)jxs_inv_v_tile_cols(), vrows = (uint32_t)jxs_inv_v_tile_rows();
-    for (int v = (int)max_dv - 1; v >= 0; v--) {
+    for (int v = (int)cfg_max_dv(c) - 1; v >= 0; v--) {
         InvVLaunch L;
         memset(&L, 0, sizeof(L));
-        L.depth = (int)c->depth;
-        L.bw = (int)c->bw;
-        L.fq = (int)c->fq;
-        int blocks = 0;
-        for (uint32_t k = 0; k < c->nc; k++) {
-            const jxs_comp_t& cp = c->comp[k];
-            if ((int)cp.dv <= v) continue;
-            InvVJob& J = L.job[L.njobs++];
-            uint32_t w, h;
-            level_dims(cp, v, &w, &h);
-            J.w = (int)w;
-            J.h = (int)h;
-            J.ll = s->ll[v][k];
-            J.ll_pitch = s->ll_pitch[v][k];
-            const int top = (int)cp.band0 + (int)cp.nb - 1 - 3 * v;
-            J.b_hh = top;
-            J.b_lh = top - 1;
-            J.b_hl = top - 2;
-            if (v > 0) {
-                J.dst = s->ll[v - 1][k];
-                J.dst_pitch = s->ll_pitch[v - 1][k];
-                J.vec = 1;
-            } else {
-                out_ptr(k, &J.dst, &J.dst_pitch);
-                J.vec = ((uintptr_t)J.dst % (2 * bps)) == 0 && (J.dst_pitch % 2) == 0;
-            }
-            J.col_tiles = (int)div_up(w, vcols);
-            J.first_block = blocks;
-            blocks += J.col_tiles * (int)div_up((h + 1) / 2, vrows);
+        int tiles[JXS_MAXC], blocks = 0;
+        L.njobs = plan_inv_v(c, d->dcfg, fb, out, v, L.job, tiles);
+        for (int i = 0; i < L.njobs; i++) {
+            L.job[i].first_block = blocks;
+            blocks += tiles[i];
         }
-        CK(jxs_launch_inv_v(&L, v > 0 ? 0 : sample_kind, blocks, dev_bands(d->dcfg), s->coef, st));
+        CK(jxs_launch_inv_v(&L, v > 0 ? 0 : sample_kind, blocks, st));
         KMARK();
     }
     TMARK(3);
@@ -911,3 +747,21 @@ extern "C" int jxs_gpu_dec_ready(jxs_gpu_dec_t* d, int slot) {
     cudaError_t r = cudaEventQuery(d->slot[slot].done);
     return r == cudaErrorNotReady ? 0 : 1;
 }
+
+extern "C" const jxs_cfg_t* jxs_gpu_enc_info(jxs_gpu_enc_t* e, const jxs_cfg_t** dev_cfg, uint32_t* cap_words) {
+    if (!e) return NULL;
+    if (dev_cfg) *dev_cfg = e->dcfg;
+    if (cap_words) *cap_words = e->cap_words;
+    return &e->cfg;
+}
+extern "C" uint64_t jxs_gpu_enc_serial(jxs_gpu_enc_t* e) { return e ? e->serial : 0; }
+
+extern "C" const jxs_cfg_t* jxs_gpu_dec_info(jxs_gpu_dec_t* d, const jxs_cfg_t** dev_cfg, uint32_t* cap_bytes,
+                                             uint32_t* cap_groups) {
+    if (!d) return NULL;
+    if (dev_cfg) *dev_cfg = d->dcfg;
+    if (cap_bytes) *cap_bytes = d->cap_bytes;
+    if (cap_groups) *cap_groups = d->cap_groups;
+    return &d->cfg;
+}
+extern "C" uint64_t jxs_gpu_dec_serial(jxs_gpu_dec_t* d) { return d ? d->serial : 0; }

@@ -121,17 +121,16 @@ DEV void store_row8(const InvHJob& J, int row, int x0, int w, const int32_t* v, 
     }
 }
 
-template <int OUT>
-__global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_constant__ InvHLaunch L, const jxs_band_t* __restrict__ bands,
-                                                                  const int16_t* __restrict__ coef) {
+template <int OUT, int NJ>
+__global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_constant__ InvHLaunchN<NJ> L) {
     extern __shared__ __align__(16) int32_t ism[];
-    int jb = 0;
-    while (jb + 1 < L.njobs && (int)blockIdx.x >= L.job[jb + 1].first_block) jb++;
-    const InvHJob& J = L.job[jb];
+    const InvHJob& J = L.job[find_job<NJ>(L.job, L.njobs, (int)blockIdx.x)];
+    const jxs_band_t* __restrict__ bands = J.bands;
+    const int16_t* __restrict__ coef = J.coef;
     const int warp = threadIdx.x >> 5;
     const int row = (blockIdx.x - J.first_block) * L.rows_per_block + warp;
     if (row >= J.h) return;
-    const int fq = L.fq;
+    const int fq = J.fq;
     int32_t* bufA = ism + warp * L.warp_words;
     int32_t* bufB = bufA + L.warp_words / 2;
     /* widths of every level's input, m[0] = row width */
@@ -149,7 +148,7 @@ __global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_c
             for (int x0 = 8 * (threadIdx.x & 31); x0 < w; x0 += 256) {
                 int32_t v[8];
                 for (int q = 0; q < 8; q++) v[q] = x0 + q < w ? dq(llr.row[x0 + q], fq) : 0;
-                store_row8<OUT>(J, row, x0, w, v, L.bw, L.depth);
+                store_row8<OUT>(J, row, x0, w, v, J.bw, J.depth);
             }
             break;
         }
@@ -182,7 +181,7 @@ __global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_c
         } else {
             warp_lift_inv(0, n1, n1, n2, s4, d4, s1, d1, [&](int j, const int32_t* xe, const int32_t* xo) {
                 const int32_t v[8] = {xe[0], xo[0], xe[1], xo[1], xe[2], xo[2], xe[3], xo[3]};
-                store_row8<OUT>(J, row, 2 * j, n, v, L.bw, L.depth);
+                store_row8<OUT>(J, row, 2 * j, n, v, J.bw, J.depth);
             });
         }
     }
@@ -197,16 +196,15 @@ __global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_c
 #define IV_NROWS (2 * IV_ROWPAIRS + 3)    /* low rows r0..r0+R, high rows r0-1..r0+R */
 #define IV_SROW (IV_COLS + 8)
 
-template <int OUT>
-__global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant__ InvVLaunch L, const jxs_band_t* __restrict__ bands,
-                                                           const int16_t* __restrict__ coef) {
+template <int OUT, int NJ>
+__global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant__ InvVLaunchN<NJ> L) {
     __shared__ __align__(16) int32_t sx[IV_NROWS][IV_SROW];
-    int jb = 0;
-    while (jb + 1 < L.njobs && (int)blockIdx.x >= L.job[jb + 1].first_block) jb++;
-    const InvVJob& J = L.job[jb];
+    const InvVJob& J = L.job[find_job<NJ>(L.job, L.njobs, (int)blockIdx.x)];
+    const jxs_band_t* __restrict__ bands = J.bands;
+    const int16_t* __restrict__ coef = J.coef;
     const int t = blockIdx.x - J.first_block;
     const int ty = t / J.col_tiles, tx = t - ty * J.col_tiles;
-    const int w = J.w, h = J.h, fq = L.fq;
+    const int w = J.w, h = J.h, fq = J.fq;
     const int n1 = (h + 1) >> 1, n2 = h >> 1;
     const int w1 = (w + 1) >> 1, w2 = w >> 1;
     const int r0 = ty * IV_ROWPAIRS;
@@ -316,7 +314,7 @@ __global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant
             for (int rr = 0; rr < rows; rr++) {
                 const int2 v = rr ? xo : xe;
                 const long long idx = (long long)(y + rr) * J.dst_pitch + x;
-                const uint32_t a = out_sample(v.x, L.bw, L.depth), b = out_sample(v.y, L.bw, L.depth);
+                const uint32_t a = out_sample(v.x, J.bw, J.depth), b = out_sample(v.y, J.bw, J.depth);
                 if (OUT == 1) {
                     uint8_t* p = (uint8_t*)J.dst + idx;
                     if (two && J.vec) *(uint16_t*)p = (uint16_t)(a | (b << 8));
@@ -347,27 +345,41 @@ extern "C" int jxs_inv_v_tile_rows(void) { return IV_ROWPAIRS; }
 extern "C" int jxs_inv_v_tile_cols(void) { return IV_COLS; }
 extern "C" int jxs_inv_h_max_rows_per_block(void) { return IH_MAX_WARPS; }
 
-extern "C" cudaError_t jxs_launch_inv_v(const InvVLaunch* L, int out_kind, int nblocks, const jxs_band_t* bands, const int16_t* coef,
-                                        cudaStream_t st) {
-    if (out_kind == 0) inv_v_kernel<0><<<nblocks, IV_THREADS, 0, st>>>(*L, bands, coef);
-    else if (out_kind == 1) inv_v_kernel<1><<<nblocks, IV_THREADS, 0, st>>>(*L, bands, coef);
-    else inv_v_kernel<2><<<nblocks, IV_THREADS, 0, st>>>(*L, bands, coef);
+template <int OUT, int NJ>
+static cudaError_t launch_iv(const InvVLaunchN<NJ>* L, int nblocks, cudaStream_t st) {
+    if (nblocks <= 0) return cudaSuccess;
+    inv_v_kernel<OUT, NJ><<<nblocks, IV_THREADS, 0, st>>>(*L);
     return cudaGetLastError();
 }
 
-template <int OUT>
-static cudaError_t launch_ih(const InvHLaunch* L, int nblocks, size_t smem, const jxs_band_t* bands, const int16_t* coef,
-                             cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(inv_h_kernel<OUT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    inv_h_kernel<OUT><<<nblocks, L->rows_per_block * 32, smem, st>>>(*L, bands, coef);
-    return cudaGetLastError();
+extern "C" cudaError_t jxs_launch_inv_v(const InvVLaunch* L, int out_kind, int nblocks, cudaStream_t st) {
+    if (out_kind == 0) return launch_iv<0, JXS_MAXC>(L, nblocks, st);
+    if (out_kind == 1) return launch_iv<1, JXS_MAXC>(L, nblocks, st);
+    return launch_iv<2, JXS_MAXC>(L, nblocks, st);
+}
+extern "C" cudaError_t jxs_launch_inv_v_batch(const InvVLaunchB* L, int out_kind, int nblocks, cudaStream_t st) {
+    if (out_kind == 0) return launch_iv<0, JXS_BATCH_JOBS>(L, nblocks, st);
+    if (out_kind == 1) return launch_iv<1, JXS_BATCH_JOBS>(L, nblocks, st);
+    return launch_iv<2, JXS_BATCH_JOBS>(L, nblocks, st);
 }
 
-extern "C" cudaError_t jxs_launch_inv_h(const InvHLaunch* L, int out_kind, int nblocks, const jxs_band_t* bands, const int16_t* coef,
-                                        cudaStream_t st) {
+template <int OUT, int NJ>
+static cudaError_t launch_ih(const InvHLaunchN<NJ>* L, int nblocks, cudaStream_t st) {
     const size_t smem = (size_t)L->warp_words * L->rows_per_block * sizeof(int32_t);
-    if (out_kind == 0) return launch_ih<0>(L, nblocks, smem, bands, coef, st);
-    if (out_kind == 1) return launch_ih<1>(L, nblocks, smem, bands, coef, st);
-    return launch_ih<2>(L, nblocks, smem, bands, coef, st);
+    cudaError_t e = cudaFuncSetAttribute(inv_h_kernel<OUT, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    if (nblocks <= 0) return cudaSuccess;
+    inv_h_kernel<OUT, NJ><<<nblocks, L->rows_per_block * 32, smem, st>>>(*L);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t jxs_launch_inv_h(const InvHLaunch* L, int out_kind, int nblocks, cudaStream_t st) {
+    if (out_kind == 0) return launch_ih<0, JXS_MAXC>(L, nblocks, st);
+    if (out_kind == 1) return launch_ih<1, JXS_MAXC>(L, nblocks, st);
+    return launch_ih<2, JXS_MAXC>(L, nblocks, st);
+}
+extern "C" cudaError_t jxs_launch_inv_h_batch(const InvHLaunchB* L, int out_kind, int nblocks, cudaStream_t st) {
+    if (out_kind == 0) return launch_ih<0, JXS_BATCH_JOBS>(L, nblocks, st);
+    if (out_kind == 1) return launch_ih<1, JXS_BATCH_JOBS>(L, nblocks, st);
+    return launch_ih<2, JXS_BATCH_JOBS>(L, nblocks, st);
 }

@@ -43,10 +43,11 @@ struct DwtJob {
     int out_kind;           /* 0: int32 ll, 1: u8 plane, 2: u16 plane */
 };
 
-struct DwtLaunch {
-    int njobs;
-    DwtJob job[JXS_MAXC];
-};
+/* Job capacity of one transform launch in the per-frame form (one job per
+ * component) and in the batched form (jobs of many frames). */
+#define JXS_BATCH_JOBS 96
+/* Frames of one per-precinct launch in the batched form. */
+#define JXS_BATCH_FRAMES 64
 
 /* Forward transform, one vertical level (jxs_fwd_dwt.cu): one component's
  * share of the launch; its tiles are blocks [first_block, first_block +
@@ -61,12 +62,18 @@ struct FwdVJob {
     int32_t* ll;            /* int32 low band written for the next level */
     int ll_pitch;           /* elements, a multiple of 4 */
     int b_hl, b_lh, b_hh;   /* flat band indices */
+    int depth;              /* sample bit depth of the frame */
+    const jxs_band_t* bands;/* the frame's band table (device copy of its configuration) */
+    uint16_t* coef;         /* the frame's coefficient and GCLI planes */
+    uint8_t* gcli;
 };
-struct FwdVLaunch {
-    int njobs, depth;
+template <int NJ> struct FwdVLaunchN {
+    int njobs;
     int ntiles;             /* tiles of all jobs; job j owns [first_block, next job's first_block) */
-    FwdVJob job[JXS_MAXC];
+    FwdVJob job[NJ];
 };
+typedef FwdVLaunchN<JXS_MAXC> FwdVLaunch;
+typedef FwdVLaunchN<JXS_BATCH_JOBS> FwdVLaunchB;
 
 /* Forward transform, horizontal-only levels: rows [0, h) of a w-wide
  * plane, rows_per_block rows (one warp each) per block. */
@@ -79,13 +86,19 @@ struct FwdHJob {
     int nh;                 /* levels */
     int b_hf[5];            /* high band of each level */
     int b_ll;               /* final low band */
+    int depth;
+    const jxs_band_t* bands;
+    uint16_t* coef;
+    uint8_t* gcli;
 };
-struct FwdHLaunch {
-    int njobs, depth;
+template <int NJ> struct FwdHLaunchN {
+    int njobs;
     int rows_per_block;
     int warp_words;         /* shared-memory words per warp */
-    FwdHJob job[JXS_MAXC];
+    FwdHJob job[NJ];
 };
+typedef FwdHLaunchN<JXS_MAXC> FwdHLaunch;
+typedef FwdHLaunchN<JXS_BATCH_JOBS> FwdHLaunchB;
 
 /* Inverse transform, one vertical level (jxs_inv_dwt.cu): rebuilds the
  * w x h level input from the int32 low band ll and the HL, LH, HH bands. */
@@ -98,11 +111,16 @@ struct InvVJob {
     void* dst;              /* int32 low band of the next level up, or the output plane */
     long long dst_pitch;    /* elements */
     int vec;                /* two adjacent output samples may be stored at once */
+    int depth, bw, fq;
+    const jxs_band_t* bands;
+    const int16_t* coef;
 };
-struct InvVLaunch {
-    int njobs, depth, bw, fq;
-    InvVJob job[JXS_MAXC];
+template <int NJ> struct InvVLaunchN {
+    int njobs;
+    InvVJob job[NJ];
 };
+typedef InvVLaunchN<JXS_MAXC> InvVLaunch;
+typedef InvVLaunchN<JXS_BATCH_JOBS> InvVLaunchB;
 
 /* Inverse transform, horizontal-only levels: rows [0, h) of width w. */
 struct InvHJob {
@@ -112,12 +130,35 @@ struct InvHJob {
     int b_hf[5], b_ll;
     void* dst;
     long long dst_pitch;
+    int depth, bw, fq;
+    const jxs_band_t* bands;
+    const int16_t* coef;
 };
-struct InvHLaunch {
-    int njobs, depth, bw, fq;
+template <int NJ> struct InvHLaunchN {
+    int njobs;
     int rows_per_block, warp_words;
-    InvHJob job[JXS_MAXC];
+    InvHJob job[NJ];
 };
+typedef InvHLaunchN<JXS_MAXC> InvHLaunch;
+typedef InvHLaunchN<JXS_BATCH_JOBS> InvHLaunchB;
+
+/* Job of block b: the last job whose first_block is <= b.  Linear for the
+ * per-frame launches (at most 4 jobs), binary for batched ones. */
+template <int NJ, class JOB>
+__device__ __forceinline__ int find_job(const JOB* job, int njobs, int b) {
+    if (NJ <= JXS_MAXC) {
+        int jb = 0;
+        while (jb + 1 < njobs && b >= job[jb + 1].first_block) jb++;
+        return jb;
+    }
+    int lo = 0, hi = njobs - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (b >= job[mid].first_block) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
 
 /* Encoder rate-control outputs per precinct row. */
 struct PrecRC {
@@ -125,6 +166,42 @@ struct PrecRC {
     uint32_t offset;       /* absolute byte offset of the precinct in the codestream */
     uint32_t data_bytes;   /* sub-packet bytes chosen by the rate control (cross-check for packing) */
     uint8_t q, r, first_in_slice, pad;
+};
+
+/* Batched per-precinct launches (rate control, packing, unpacking): one
+ * entry per frame.  Blocks [first_block, next frame's first_block) are the
+ * frame's precincts; the kernels find their frame with find_job. */
+struct EncPrecFrame {
+    const jxs_cfg_t* cfg;   /* device copy of the frame's configuration */
+    const uint16_t* coef;
+    const uint8_t* gcli;
+    uint32_t* cost;
+    uint32_t* slice_done;
+    PrecRC* rc;
+    uint8_t* out;           /* codestream */
+    int* status;
+    int first_block;
+};
+struct EncPrecLaunch {
+    int nframes;
+    int nblocks;
+    EncPrecFrame job[JXS_BATCH_FRAMES];
+};
+
+struct DecPrecFrame {
+    const jxs_cfg_t* cfg;
+    const uint8_t* bs;      /* codestream */
+    uint32_t bs_size;
+    uint32_t* prec_off;     /* precinct byte offsets */
+    int16_t* coef;
+    int* status;            /* status[0]: frame status; status[1]: the slice walk found a mismatch */
+    int first_block;        /* unpacking: first precinct block */
+    int first_slice;        /* walk: first slice thread */
+};
+struct DecPrecLaunch {
+    int nframes;
+    int nblocks, nslices;
+    DecPrecFrame job[JXS_BATCH_FRAMES];
 };
 
 #define JXS_STATUS_SET(ptr, code) atomicCAS((int*)(ptr), 0, (int)(code))

@@ -92,6 +92,15 @@ class DecoderApi(ctypes.Structure):
 _lib = None
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("last_gpu_ms", ctypes.c_float), ("last_launches", ctypes.c_uint32), ("graph_hits", ctypes.c_uint64),
+                ("graph_builds", ctypes.c_uint64), ("graph_updates", ctypes.c_uint64), ("tune", ctypes.c_int32 * 5),
+                ("device_bytes", ctypes.c_uint64), ("device_used", ctypes.c_uint64), ("device_peak", ctypes.c_uint64)]
+
+
+BATCH_MAX = 64
+
+
 def lib():
     """The loaded libSvtJpegxs.so; raises if the extension was not built."""
     global _lib
@@ -148,6 +157,24 @@ def lib():
         L.svt_jpeg_xs_gpu_decoder_locate_frame.argtypes = [ctypes.POINTER(DecoderApi), ctypes.c_void_p, u32, ctypes.POINTER(u32),
                                                           ctypes.c_void_p, u32, ctypes.c_void_p]
         L.svt_jpeg_xs_gpu_decoder_locate_frame.restype = u32
+        L.svt_jpeg_xs_gpu_batch_create.argtypes = [ctypes.c_uint64, ctypes.POINTER(ctypes.c_void_p)]
+        L.svt_jpeg_xs_gpu_batch_create.restype = u32
+        L.svt_jpeg_xs_gpu_batch_destroy.argtypes = [ctypes.c_void_p]
+        L.svt_jpeg_xs_gpu_batch_destroy.restype = None
+        L.svt_jpeg_xs_gpu_batch_set_options.argtypes = [ctypes.c_void_p, u32, u32]
+        L.svt_jpeg_xs_gpu_batch_set_options.restype = u32
+        L.svt_jpeg_xs_gpu_batch_set_tune.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32)]
+        L.svt_jpeg_xs_gpu_batch_set_tune.restype = u32
+        L.svt_jpeg_xs_gpu_batch_encode.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, u32, ctypes.c_void_p]
+        L.svt_jpeg_xs_gpu_batch_encode.restype = u32
+        L.svt_jpeg_xs_gpu_batch_decode.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, u32, ctypes.c_void_p]
+        L.svt_jpeg_xs_gpu_batch_decode.restype = u32
+        L.svt_jpeg_xs_gpu_batch_wait.argtypes = [ctypes.c_void_p, ctypes.POINTER(u32)]
+        L.svt_jpeg_xs_gpu_batch_wait.restype = u32
+        L.svt_jpeg_xs_gpu_batch_ready.argtypes = [ctypes.c_void_p]
+        L.svt_jpeg_xs_gpu_batch_ready.restype = u32
+        L.svt_jpeg_xs_gpu_batch_get_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchInfo)]
+        L.svt_jpeg_xs_gpu_batch_get_info.restype = u32
         L.svt_jpeg_xs_image_buffer_alloc.argtypes = [ctypes.POINTER(ImageConfig)]
         L.svt_jpeg_xs_image_buffer_alloc.restype = ctypes.POINTER(ImageBuffer)
         L.svt_jpeg_xs_image_buffer_free.argtypes = [ctypes.POINTER(ImageBuffer)]
@@ -395,3 +422,73 @@ class Decoder:
         ms = (ctypes.c_double * 4)()
         n = lib().svt_jpeg_xs_gpu_decoder_read_timing(ctypes.byref(self.api), ms, 4)
         return int(n), list(ms)
+
+
+class Batch:
+    """Batched encode/decode (svt_jpeg_xs_gpu_batch_*): frame i of a call uses
+    the configuration of the i-th Encoder / Decoder.  One batch in flight per
+    object; encode()/decode() queue it, wait() completes it."""
+
+    def __init__(self, device_bytes, use_graph=True, autotune=False):
+        self.h = ctypes.c_void_p()
+        _check("batch_create", lib().svt_jpeg_xs_gpu_batch_create(int(device_bytes), ctypes.byref(self.h)))
+        self.set_options(use_graph, autotune)
+        self._keep = None
+        self.n = 0
+
+    def close(self):
+        if self.h:
+            lib().svt_jpeg_xs_gpu_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_options(self, use_graph=True, autotune=False):
+        _check("batch_set_options", lib().svt_jpeg_xs_gpu_batch_set_options(self.h, 1 if use_graph else 0, 1 if autotune else 0))
+
+    def set_tune(self, chains=1, heavy_first=0, grid_per_sm=0, fwd_rows=4, inv_rows=4):
+        t = (ctypes.c_int32 * 5)(chains, heavy_first, grid_per_sm, fwd_rows, inv_rows)
+        _check("batch_set_tune", lib().svt_jpeg_xs_gpu_batch_set_tune(self.h, t))
+
+    def encode(self, encoders, planes_list, outs, out_caps=None, stream=None):
+        """Queues encoders[i].encode(planes_list[i]) into outs[i] (numpy array
+        or device pointer with out_caps[i] bytes)."""
+        n = len(encoders)
+        frames = [e._frame(p, o, out_caps[i] if out_caps else None) for i, (e, p, o) in enumerate(zip(encoders, planes_list, outs))]
+        apis = (ctypes.c_void_p * n)(*[ctypes.addressof(e.api) for e in encoders])
+        fps = (ctypes.c_void_p * n)(*[ctypes.addressof(f) for f in frames])
+        self._keep = (frames, apis, fps, planes_list, outs)
+        self.n = n
+        return lib().svt_jpeg_xs_gpu_batch_encode(self.h, apis, fps, n, stream)
+
+    def decode(self, decoders, bitstreams, planes_list, sizes=None, stream=None):
+        """Queues decoders[i].decode(bitstreams[i]) into planes_list[i] (numpy
+        arrays or (device_ptr, stride) tuples); device codestreams need sizes."""
+        n = len(decoders)
+        frames = [d._frame(b, p, sizes[i] if sizes else None) for i, (d, b, p) in enumerate(zip(decoders, bitstreams, planes_list))]
+        apis = (ctypes.c_void_p * n)(*[ctypes.addressof(d.api) for d in decoders])
+        fps = (ctypes.c_void_p * n)(*[ctypes.addressof(f) for f in frames])
+        self._keep = (frames, apis, fps, bitstreams, planes_list)
+        self.n = n
+        return lib().svt_jpeg_xs_gpu_batch_decode(self.h, apis, fps, n, stream)
+
+    def wait(self):
+        """(first error or 0, per-frame statuses)"""
+        st = (ctypes.c_uint32 * BATCH_MAX)()
+        r = lib().svt_jpeg_xs_gpu_batch_wait(self.h, st)
+        self._keep = None
+        return r, [st[i] for i in range(self.n)]
+
+    def ready(self):
+        return bool(lib().svt_jpeg_xs_gpu_batch_ready(self.h))
+
+    def info(self):
+        i = BatchInfo()
+        _check("batch_get_info", lib().svt_jpeg_xs_gpu_batch_get_info(self.h, ctypes.byref(i)))
+        return {"last_gpu_ms": i.last_gpu_ms, "last_launches": i.last_launches, "graph_hits": i.graph_hits,
+                "graph_builds": i.graph_builds, "graph_updates": i.graph_updates, "tune": list(i.tune),
+                "device_bytes": i.device_bytes, "device_used": i.device_used, "device_peak": i.device_peak}
