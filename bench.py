@@ -230,6 +230,76 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_batched(args, jxs, torch, dev, frames, d_in, lcod, enc, dec, nseq):
+    """Batched encode + decode of the stream, device-resident; returns the
+    device time of args.steps steps and the last step's outputs."""
+    F = args.frames
+    NB = 2
+    streams = [torch.cuda.Stream(device=dev) for _ in range(NB)]
+    bat_e = [jxs.Batch(F * (200 << 20), autotune=True) for _ in range(NB)]
+    bat_d = [jxs.Batch(F * (120 << 20), autotune=True) for _ in range(NB)]
+    d_bs = [[torch.zeros(lcod + 64, dtype=torch.uint8, device=dev) for _ in range(F)] for _ in range(NB)]
+    d_out = [[[torch.zeros_like(p) for p in d_in[0]] for _ in range(F)] for _ in range(NB)]
+    busy = [False] * NB
+
+    def planes_of(ts):
+        return [(t.data_ptr(), t.shape[1]) for t in ts]
+
+    def finish(k):
+        if busy[k]:
+            r, _ = bat_e[k].wait()
+            assert r == 0, hex(r)
+            r, _ = bat_d[k].wait()
+            assert r == 0, hex(r)
+            busy[k] = False
+
+    def step(s):
+        k = s % NB
+        finish(k)
+        base = (s * F) % nseq
+        st = streams[k].cuda_stream
+        r = bat_e[k].encode([enc] * F, [planes_of(d_in[(base + i) % nseq]) for i in range(F)],
+                            [t.data_ptr() for t in d_bs[k]], out_caps=[lcod + 64] * F, stream=st)
+        assert r == 0, hex(r)
+        r = bat_d[k].decode([dec] * F, [t.data_ptr() for t in d_bs[k]], [planes_of(o) for o in d_out[k]],
+                            sizes=[lcod] * F, stream=st)
+        assert r == 0, hex(r)
+        busy[k] = True
+
+    for w in range(max(args.warmup, NB)):
+        step(w)
+    for k in range(NB):
+        finish(k)
+    torch.cuda.synchronize()
+    main = torch.cuda.current_stream(dev)
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(main)
+    for st in streams:
+        st.wait_event(ev0)
+    w0 = max(args.warmup, NB)
+    for s in range(args.steps):
+        step(w0 + s)
+    for st in streams:
+        e = torch.cuda.Event()
+        e.record(st)
+        main.wait_event(e)
+    ev1.record(main)
+    torch.cuda.synchronize()
+    for k in range(NB):
+        finish(k)
+    dev_ms = ev0.elapsed_time(ev1)
+    last = (w0 + args.steps - 1) % NB
+    ie, idd = bat_e[last].info(), bat_d[last].info()
+    out = {"dev_ms": dev_ms, "last_base": ((w0 + args.steps - 1) * F) % nseq, "bs": d_bs[last], "out": d_out[last],
+           "enc_tune": ie["tune"], "dec_tune": idd["tune"], "launches_per_step": ie["last_launches"] + idd["last_launches"],
+           "graph_hits": ie["graph_hits"] + idd["graph_hits"], "enc_batch_gpu_ms": ie["last_gpu_ms"],
+           "dec_batch_gpu_ms": idd["last_gpu_ms"]}
+    for b in bat_e + bat_d:
+        b.close()
+    return out
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -352,6 +422,28 @@ def run_ours(args, rank, world, local):
         assert err == 0 and all(np.array_equal(t.cpu().numpy(), w) for t, w in zip(d_out[i], want_planes)), \
             "decoded frame differs from the oracle"
 
+    # ---- batched form: one batch encode + one batch decode of the step's F
+    # frames per step (one launch per stage over all F frames, replayed as a
+    # CUDA graph), two batch pairs alternating on two streams so that one
+    # step's launches queue behind the other's; launch shapes autotuned on
+    # the first (warm-up) batch
+    clocks_b = ClockSampler(local)
+    clocks_b.start()
+    bat = run_batched(args, jxs, torch, dev, frames, d_in, lcod, encs[0], decs[0], nseq)
+    clk_b = clocks_b.stop()
+    for i in (0, F - 1):
+        err, want = O.oracle_encode(O.make_params(W, H, DEPTH, 3, BPP, threads=os.cpu_count() or 1),
+                                    frames[(bat["last_base"] + i) % nseq])
+        assert err == 0 and np.array_equal(bat["bs"][i][:lcod].cpu().numpy(), want), "batched codestream differs from the oracle"
+        err, want_planes = O.oracle_decode(want, threads=os.cpu_count() or 1)
+        assert err == 0 and all(np.array_equal(t.cpu().numpy(), w) for t, w in zip(bat["out"][i], want_planes)), \
+            "batched decoded frame differs from the oracle"
+    if world > 1:
+        t = torch.tensor([bat["dev_ms"]], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        bat["dev_ms"] = float(t.item())
+    batched_value = args.steps * F * world * W * H / (bat["dev_ms"] / 1e3) / 1e9
+
     # ---- e2e through the C API with host buffers: every pair on its own slot
     # streams (3 frames in flight per codec); the latency probe uses pair 0
     enc, dec = encs[0], decs[0]
@@ -459,9 +551,12 @@ def run_ours(args, rank, world, local):
     # per frame: 2 vertical + 1 horizontal transform, rate control, pack;
     # 2 precinct walks (device codestreams), unpack, 1 horizontal + 2 vertical inverse
     launches_per_frame = 5 + 6
+    head_batched = batched_value >= value
+    head_ms = bat["dev_ms"] if head_batched else dev_ms
+    head_clk = clk_b if head_batched else clk
     line = {
-        "metric": METRIC, "value": value, "unit": "Gpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "metric": METRIC, "value": max(value, batched_value), "unit": "Gpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": head_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "int32", "data": "synthetic (seeded, integer-only generator; no dataset)",
         "config": {"workload": WORKLOAD, "frames_per_step": F, "streams": NS, "l2": "inputs 33 MB/frame cycling over %d frames (> L2)" % nseq,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
@@ -473,9 +568,16 @@ def run_ours(args, rank, world, local):
                      "peak_source": peak_kind, "traffic": KERNEL_DRAM_BYTES.get(dom), "algorithmic_bytes": kb[dom],
                      "kernel_ms_per_frame": {k: round(v, 4) for k, v in kern_ms.items()}, "stage_ms_per_frame": stage_ms,
                      "pipeline_algorithmic_gbs": pipeline_gbs},
+        "per_frame": {"value": value, "unit": "Gpix/s", "streams": NS, "launches_per_frame": launches_per_frame},
+        "batched": {"value": batched_value, "unit": "Gpix/s", "frames_per_batch": F,
+                    "launches_per_step": bat["launches_per_step"], "graph_replays": bat["graph_hits"],
+                    "tune_encode": bat["enc_tune"], "tune_decode": bat["dec_tune"],
+                    "last_batch_gpu_ms": {"encode": bat["enc_batch_gpu_ms"], "decode": bat["dec_batch_gpu_ms"]}},
+        "headline_path": "batched" if head_batched else "per_frame",
         "cpu_baseline": cpu,
-        "clocks": clk,
-        "gpu_launches": launches_per_frame * args.steps * F,
+        "clocks": head_clk,
+        "clocks_other_path": clk if head_batched else clk_b,
+        "gpu_launches": (bat["launches_per_step"] if head_batched else launches_per_frame * F) * args.steps,
         "host_wall_s": host_s,
     }
     if rank == 0:
