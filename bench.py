@@ -94,6 +94,8 @@ def parse():
     ap.add_argument("--frames", type=int, default=8, help="frames encoded and decoded per step")
     ap.add_argument("--streams", type=int, default=3, help="encoder/decoder pairs, each on its own CUDA stream")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget (0: not measured)")
+    ap.add_argument("--workload", default="stream4k", choices=["stream4k", "mixed48", "8k"],
+                    help="stream4k: the default line; mixed48 / 8k: batched form against the per-frame path")
     ap.add_argument("--seq-frames", type=int, default=SEQ_FRAMES,
                     help="distinct frames of the stream cycled through (each 33 MB; 4 or more keep inputs above L2)")
     return ap.parse_args()
@@ -586,11 +588,209 @@ def run_ours(args, rank, world, local):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# other workloads (not the default line): the mixed 48-frame batch and the
+# 8K 14-bit stress batch, batched form against the per-frame path
+# ---------------------------------------------------------------------------
+# (w, h, depth, format, bpp numerator, bpp denominator, decomp V, decomp H, content seed)
+SHAPES_MIXED = [(1280, 720, 8, 2, 1, 1, 2, 5, 31), (1920, 1080, 12, 4, 4, 1, 2, 5, 32), (3840, 2160, 8, 21, 2, 1, 2, 5, 33)]
+SHAPE_8K = (7680, 4320, 14, 4, 3, 2, 1, 5, 4)
+
+
+def workload_frames(name):
+    """(shape list, per-position shape index, planes per shape, description)"""
+    import jxs_synth as S
+
+    if name == "mixed48":
+        rng = np.random.default_rng(3)
+        order = [int(x) for x in rng.permutation([0] * 16 + [1] * 16 + [2] * 16)]
+        contents = []
+        for (w, h, d, fmt, _, _, _, _, seed) in SHAPES_MIXED:
+            contents.append([S.frame(w, h, d, fmt, seed=seed + 100 * j) for j in range(2)])
+        desc = ("48 frames, shape order from seed 3: 16 x 1280x720 4:2:0 8-bit bpp 1, 16 x 1920x1080 4:4:4 12-bit bpp 4, "
+                "16 x 3840x2160 packed RGB 8-bit bpp 2; decomp V2/H5; 2 seeded contents per shape, alternating")
+        return SHAPES_MIXED, order, contents, desc
+    contents = [[S.frame_8k_14bit(SHAPE_8K[8] + j) for j in range(2)]]
+    desc = "8 frames 7680x4320 gbrp 14-bit bpp 1.5, decomp V1/H5, uniform noise in one quadrant; 2 seeded contents"
+    return [SHAPE_8K], [0] * 8, contents, desc
+
+
+def run_workload(args, name, local):
+    import torch
+
+    import jxs
+    import oracle_lib as O
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    shapes, order, contents, desc = workload_frames(name)
+    n = len(order)
+    pix = sum(shapes[k][0] * shapes[k][1] for k in order)
+    NS = 3
+    # per shape: NS encoder/decoder pairs (per-frame path) and the pair the batches use
+    encs = [[jxs.Encoder(w, h, d, fmt, bn, bd, v, hh) for _ in range(NS)] for (w, h, d, fmt, bn, bd, v, hh, _) in shapes]
+    first = [encs[k][0].encode(contents[k][0]) for k in range(len(shapes))]
+    decs = [[jxs.Decoder(first[k]) for _ in range(NS)] for k in range(len(shapes))]
+    streams = [torch.cuda.Stream(device=dev) for _ in range(NS)]
+    for k in range(len(shapes)):
+        for j in range(NS):
+            encs[k][j].set_stream(streams[j].cuda_stream)
+            decs[k][j].set_stream(streams[j].cuda_stream)
+    d_in = [[torch.from_numpy(p).to(dev) for p in contents[order[i]][(i // len(shapes)) % 2]] for i in range(n)]
+    lcod = [encs[order[i]][0].frame_bytes for i in range(n)]
+    d_bs = [torch.zeros(lcod[i] + 64, dtype=torch.uint8, device=dev) for i in range(n)]
+    d_out = [[torch.zeros_like(p) for p in d_in[i]] for i in range(n)]
+    # decoded planes of packed RGB input come back planar
+    for i in range(n):
+        if shapes[order[i]][3] == 21:
+            w, h = shapes[order[i]][0], shapes[order[i]][1]
+            dt = d_in[i][0].dtype
+            d_out[i] = [torch.zeros((h, w), dtype=dt, device=dev) for _ in range(3)]
+
+    def planes_of(ts):
+        return [(t.data_ptr(), t.shape[1]) for t in ts]
+
+    main = torch.cuda.current_stream(dev)
+
+    def timed(fn, steps):
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(main)
+        for st in streams:
+            st.wait_event(ev0)
+        lat = []
+        for _ in range(steps):
+            lat.extend(fn())
+        for st in streams:
+            e = torch.cuda.Event()
+            e.record(st)
+            main.wait_event(e)
+        ev1.record(main)
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1), lat
+
+    # ---- per-frame path: all n frames submitted at once, frame i on pair
+    # i % NS of its shape; a codec whose queue is full hands back its oldest
+    # frame before it takes the next
+    def per_frame_step(decode_only=False):
+        t0 = time.perf_counter()
+        lat = []
+        pend = {}
+
+        def get_one(codec, is_dec):
+            r, _ = codec.get()
+            assert r == 0, hex(r)
+            pend[id(codec)][1].pop(0)
+            if is_dec:
+                lat.append((time.perf_counter() - t0) * 1e3)
+
+        def submit(codec, is_dec, i, *a, **kw):
+            while True:
+                r = codec.send(*a, blocking=False, **kw)
+                if r != jxs.E_EMPTY_QUEUE:
+                    assert r == 0, hex(r)
+                    pend.setdefault(id(codec), (codec, []))[1].append((i, is_dec))
+                    return
+                get_one(codec, is_dec)
+
+        for i in range(n):
+            k, j = order[i], i % NS
+            if not decode_only:
+                submit(encs[k][j], False, i, planes_of(d_in[i]), d_bs[i].data_ptr(), out_cap=lcod[i] + 64)
+            submit(decs[k][j], True, i, d_bs[i].data_ptr(), planes_of(d_out[i]), bs_size=lcod[i])
+        for codec, q in list(pend.values()):
+            while q:
+                get_one(codec, q[0][1])
+        return lat
+
+    for _ in range(max(1, args.warmup)):
+        per_frame_step()
+    pf_ms, pf_lat = timed(per_frame_step, args.steps)
+    pf_dec_ms, pf_dec_lat = timed(lambda: per_frame_step(True), args.steps)
+
+    # ---- batched form: one batch encode + one batch decode of all n frames
+    for k in range(len(shapes)):
+        for j in range(NS):
+            encs[k][j].set_stream(None)
+            decs[k][j].set_stream(None)
+    be = jxs.Batch(n * (700 << 20 if name == "8k" else 160 << 20), autotune=True)
+    bd = jxs.Batch(n * (600 << 20 if name == "8k" else 100 << 20), autotune=True)
+    st = streams[0].cuda_stream
+    e_list = [encs[order[i]][0] for i in range(n)]
+    dl = [decs[order[i]][0] for i in range(n)]
+
+    def batch_step(decode_only=False):
+        t0 = time.perf_counter()
+        if not decode_only:
+            assert be.encode(e_list, [planes_of(d_in[i]) for i in range(n)], [t.data_ptr() for t in d_bs],
+                             out_caps=[x + 64 for x in lcod], stream=st) == 0
+        assert bd.decode(dl, [t.data_ptr() for t in d_bs], [planes_of(o) for o in d_out], sizes=lcod, stream=st) == 0
+        if not decode_only:
+            r, _ = be.wait()
+            assert r == 0, hex(r)
+        r, _ = bd.wait()
+        assert r == 0, hex(r)
+        done = (time.perf_counter() - t0) * 1e3
+        return [done] * n
+
+    for _ in range(max(1, args.warmup)):
+        batch_step()
+    b_ms, b_lat = timed(batch_step, args.steps)
+    b_dec_ms, b_dec_lat = timed(lambda: batch_step(True), args.steps)
+    launches = be.info()["last_launches"] + bd.info()["last_launches"]
+    tunes = {"encode": be.info()["tune"], "decode": bd.info()["tune"]}
+
+    # bit-exactness: one frame of each shape against the oracle
+    checked = set()
+    for i in range(n):
+        k = order[i]
+        if k in checked:
+            continue
+        checked.add(k)
+        w, h, d, fmt, bn, bdn, v, hh, _ = shapes[k]
+        planes = contents[k][(i // len(shapes)) % 2]
+        err, want = O.oracle_encode(O.make_params(w, h, d, fmt, bn, bdn, v, hh, threads=os.cpu_count() or 1), planes)
+        assert err == 0 and np.array_equal(d_bs[i][: lcod[i]].cpu().numpy(), want), "codestream differs from the oracle"
+        err, wp = O.oracle_decode(want, threads=os.cpu_count() or 1)
+        assert err == 0 and all(np.array_equal(t.cpu().numpy(), x) for t, x in zip(d_out[i], wp)), "decode differs"
+    be.close()
+    bd.close()
+    for row in encs + decs:
+        for c in row:
+            c.close()
+
+    def pct(a, q):
+        return float(np.percentile(a, q))
+
+    steps = args.steps
+    line = {
+        "workload": name, "metric": "encode+decode Gpix/s (bit-exact) and frame latency, batched vs per-frame", "unit": "Gpix/s",
+        "value": steps * pix / (b_ms / 1e3) / 1e9, "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+        "higher_is_better": True, "dtype": "int32", "data": "synthetic (seeded, integer-only generator; no dataset)",
+        "config": {"workload": desc, "frames": n, "luma_pixels_per_step": pix},
+        "batched": {"gpix_s": steps * pix / (b_ms / 1e3) / 1e9, "frames_s": steps * n / (b_ms / 1e3),
+                    "ms_per_step": b_ms / steps, "frame_latency_ms_p50": pct(b_lat, 50), "frame_latency_ms_p99": pct(b_lat, 99),
+                    "decode_only_gpix_s": steps * pix / (b_dec_ms / 1e3) / 1e9, "decode_only_latency_ms_p99": pct(b_dec_lat, 99),
+                    "launches_per_step": launches, "tune": tunes},
+        "per_frame": {"gpix_s": steps * pix / (pf_ms / 1e3) / 1e9, "frames_s": steps * n / (pf_ms / 1e3),
+                      "ms_per_step": pf_ms / steps, "frame_latency_ms_p50": pct(pf_lat, 50),
+                      "frame_latency_ms_p99": pct(pf_lat, 99), "decode_only_gpix_s": steps * pix / (pf_dec_ms / 1e3) / 1e9,
+                      "decode_only_latency_ms_p99": pct(pf_dec_lat, 99), "streams": NS},
+        "latency_definition": "all frames of a step submitted at once; a frame's latency is submit to its result on the host",
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload != "stream4k":
+        if rank == 0:
+            run_workload(args, args.workload, local)
         return
     run_ours(args, rank, world, local)
 
