@@ -160,6 +160,67 @@ PREFIX_API uint32_t svt_jpeg_xs_gpu_batch_ready(svt_jpeg_xs_gpu_batch_t* batch);
 
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_get_info(svt_jpeg_xs_gpu_batch_t* batch, svt_jpeg_xs_gpu_batch_info_t* info);
 
+/* ------------------------------------------------------------------------
+ * Serving loop.  Encode and decode requests from many streams are run by a
+ * scheduler thread of the library:
+ *   SVT_JPEGXS_GPU_SERVER_BATCHED: continuous batching.  `lanes` encode
+ *     lanes and `lanes` decode lanes (CUDA streams) each take the waiting
+ *     requests of their kind, oldest first, up to max_batch and as many as
+ *     the device budget (device_bytes) admits, as one batch; requests that
+ *     arrive while the lanes are busy join the next batch.  A request that
+ *     can never fit completes with SvtJxsErrorInsufficientResources.
+ *   SVT_JPEGXS_GPU_SERVER_PER_FRAME: the plain per-frame path; each request
+ *     goes to a free frame slot of its stream's handle when it arrives.
+ * A stream is one encoder or decoder handle (its configuration); register
+ * all streams before the first submit, and do not use those handles for
+ * send_picture / send_frame while the server runs.  Planes and codestreams
+ * of requests are device memory of the current device and stay untouched
+ * by the caller until the request completes.  Outputs are identical to those
+ * of the same handles' send_picture / send_frame.
+ * ------------------------------------------------------------------------ */
+#define SVT_JPEGXS_GPU_SERVER_BATCHED 0
+#define SVT_JPEGXS_GPU_SERVER_PER_FRAME 1
+
+typedef struct svt_jpeg_xs_gpu_server svt_jpeg_xs_gpu_server_t;
+
+typedef struct svt_jpeg_xs_gpu_request {
+    int32_t stream;            /* id from add_encoder / add_decoder */
+    uint64_t tag;              /* returned with the completion */
+    void* planes[4];           /* encode: input planes; decode: output planes */
+    uint32_t strides[4];       /* samples */
+    void* bitstream;           /* encode: output (Lcod bytes); decode: input */
+    uint32_t bitstream_size;   /* decode: codestream bytes */
+} svt_jpeg_xs_gpu_request_t;
+
+typedef struct svt_jpeg_xs_gpu_completion {
+    uint64_t tag;
+    int32_t stream;
+    SvtJxsErrorType_t status;
+    int64_t t_arrive_ns;       /* submit, host steady clock */
+    int64_t t_start_ns;        /* launched on the device */
+    int64_t t_done_ns;         /* completion seen by the scheduler */
+} svt_jpeg_xs_gpu_completion_t;
+
+typedef struct svt_jpeg_xs_gpu_server_stats {
+    uint64_t batches, batched_frames, max_batch_seen;
+    uint64_t deferred;         /* admissions postponed for lack of device memory */
+    uint64_t device_bytes, device_used, device_peak;
+} svt_jpeg_xs_gpu_server_stats_t;
+
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_server_create(uint64_t device_bytes, uint32_t mode, uint32_t lanes,
+                                                           uint32_t max_batch, svt_jpeg_xs_gpu_server_t** server);
+PREFIX_API void svt_jpeg_xs_gpu_server_destroy(svt_jpeg_xs_gpu_server_t* server);
+/* Return the stream id, or -1. */
+PREFIX_API int32_t svt_jpeg_xs_gpu_server_add_encoder(svt_jpeg_xs_gpu_server_t* server, svt_jpeg_xs_encoder_api_t* enc_api);
+PREFIX_API int32_t svt_jpeg_xs_gpu_server_add_decoder(svt_jpeg_xs_gpu_server_t* server, svt_jpeg_xs_decoder_api_t* dec_api);
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_server_submit(svt_jpeg_xs_gpu_server_t* server, const svt_jpeg_xs_gpu_request_t* req);
+/* Moves up to max completions to out, oldest first; returns how many. */
+PREFIX_API uint32_t svt_jpeg_xs_gpu_server_poll(svt_jpeg_xs_gpu_server_t* server, svt_jpeg_xs_gpu_completion_t* out, uint32_t max);
+/* Requests submitted and not yet completed. */
+PREFIX_API uint64_t svt_jpeg_xs_gpu_server_pending(svt_jpeg_xs_gpu_server_t* server);
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_server_get_stats(svt_jpeg_xs_gpu_server_t* server,
+                                                              svt_jpeg_xs_gpu_server_stats_t* stats);
+
 #ifdef __cplusplus
 }
 #endif

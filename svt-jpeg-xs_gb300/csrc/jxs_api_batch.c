@@ -7,7 +7,9 @@
 #include <string.h>
 
 #include "SvtJpegxsGpu.h"
+#include "jxs_api_internal.h"
 #include "jxs_batch.h"
+#include "jxs_server.h"
 
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_create(uint64_t device_bytes, svt_jpeg_xs_gpu_batch_t** batch) {
     if (!batch || !device_bytes) return SvtJxsErrorBadParameter;
@@ -60,5 +62,86 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_get_info(svt_jpeg_xs_gpu_batc
     info->device_bytes = i.arena_bytes;
     info->device_used = i.arena_used;
     info->device_peak = i.arena_peak;
+    return SvtJxsErrorNone;
+}
+
+/* ------------------------------------------------------------------------ */
+/* serving loop                                                              */
+/* ------------------------------------------------------------------------ */
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_server_create(uint64_t device_bytes, uint32_t mode, uint32_t lanes,
+                                                           uint32_t max_batch, svt_jpeg_xs_gpu_server_t** server) {
+    if (!server || (mode != SVT_JPEGXS_GPU_SERVER_BATCHED && mode != SVT_JPEGXS_GPU_SERVER_PER_FRAME)) return SvtJxsErrorBadParameter;
+    if (mode == SVT_JPEGXS_GPU_SERVER_BATCHED && !device_bytes) return SvtJxsErrorBadParameter;
+    int32_t err = 0;
+    *server = (svt_jpeg_xs_gpu_server_t*)jxs_server_create(device_bytes, (int)mode, (int)lanes, (int)max_batch, &err);
+    return *server ? SvtJxsErrorNone : (SvtJxsErrorType_t)err;
+}
+
+PREFIX_API void svt_jpeg_xs_gpu_server_destroy(svt_jpeg_xs_gpu_server_t* server) { jxs_server_destroy((jxs_server_t*)server); }
+
+PREFIX_API int32_t svt_jpeg_xs_gpu_server_add_encoder(svt_jpeg_xs_gpu_server_t* server, svt_jpeg_xs_encoder_api_t* enc_api) {
+    jxs_gpu_enc_t* e = jxs_api_enc_gpu(enc_api);
+    if (!server || !e) return -1;
+    return jxs_server_add_stream((jxs_server_t*)server, e, NULL);
+}
+
+PREFIX_API int32_t svt_jpeg_xs_gpu_server_add_decoder(svt_jpeg_xs_gpu_server_t* server, svt_jpeg_xs_decoder_api_t* dec_api) {
+    jxs_gpu_dec_t* d = jxs_api_dec_gpu(dec_api);
+    if (!server || !d) return -1;
+    return jxs_server_add_stream((jxs_server_t*)server, NULL, d);
+}
+
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_server_submit(svt_jpeg_xs_gpu_server_t* server, const svt_jpeg_xs_gpu_request_t* req) {
+    if (!server || !req) return SvtJxsErrorBadParameter;
+    jxs_srv_request_t r;
+    memset(&r, 0, sizeof(r));
+    r.stream = req->stream;
+    r.tag = req->tag;
+    for (int k = 0; k < 4; k++) {
+        r.planes[k] = req->planes[k];
+        r.strides[k] = req->strides[k];
+    }
+    r.bitstream = req->bitstream;
+    r.bitstream_size = req->bitstream_size;
+    return (SvtJxsErrorType_t)jxs_server_submit((jxs_server_t*)server, &r);
+}
+
+PREFIX_API uint32_t svt_jpeg_xs_gpu_server_poll(svt_jpeg_xs_gpu_server_t* server, svt_jpeg_xs_gpu_completion_t* out, uint32_t max) {
+    if (!server || !out) return 0;
+    jxs_srv_done_t d[256];
+    uint32_t total = 0;
+    while (total < max) {
+        const int want = (int)((max - total) < 256 ? (max - total) : 256);
+        const int n = jxs_server_poll((jxs_server_t*)server, d, want);
+        for (int i = 0; i < n; i++) {
+            svt_jpeg_xs_gpu_completion_t* c = &out[total + i];
+            c->tag = d[i].tag;
+            c->stream = d[i].stream;
+            c->status = (SvtJxsErrorType_t)d[i].status;
+            c->t_arrive_ns = d[i].t_arrive_ns;
+            c->t_start_ns = d[i].t_start_ns;
+            c->t_done_ns = d[i].t_done_ns;
+        }
+        total += (uint32_t)n;
+        if (n < want) break;
+    }
+    return total;
+}
+
+PREFIX_API uint64_t svt_jpeg_xs_gpu_server_pending(svt_jpeg_xs_gpu_server_t* server) {
+    return server ? jxs_server_pending((jxs_server_t*)server) : 0;
+}
+
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_server_get_stats(svt_jpeg_xs_gpu_server_t* server, svt_jpeg_xs_gpu_server_stats_t* st) {
+    if (!server || !st) return SvtJxsErrorBadParameter;
+    jxs_srv_stats_t s;
+    jxs_server_stats((jxs_server_t*)server, &s);
+    st->batches = s.batches;
+    st->batched_frames = s.batched_frames;
+    st->max_batch_seen = s.max_batch_seen;
+    st->deferred = s.deferred;
+    st->device_bytes = s.device_bytes;
+    st->device_used = s.device_used;
+    st->device_peak = s.device_peak;
     return SvtJxsErrorNone;
 }

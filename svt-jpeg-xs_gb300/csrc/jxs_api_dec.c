@@ -17,6 +17,7 @@
 #include "SvtJpegxsDec.h"
 #include "SvtJpegxsGpu.h"
 #include "jxs_core.h"
+#include "jxs_api_internal.h"
 #include "jxs_batch.h"
 #include "jxs_gpu.h"
 #include "jxs_queue.h"
@@ -488,4 +489,10 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_decode(svt_jpeg_xs_gpu_batch_
     const int32_t r = jxs_gpu_batch_decode(b, gpu, n, bs, size, walked, (void* const(*)[4])planes, (const uint32_t(*)[4])strides,
                                            cuda_stream);
     return (SvtJxsErrorType_t)r;
+}
+
+jxs_gpu_dec_t* jxs_api_dec_gpu(svt_jpeg_xs_decoder_api_t* dec_api) {
+    if (!dec_api || !dec_api->private_ptr) return NULL;
+    dec_prv_t* p = (dec_prv_t*)dec_api->private_ptr;
+    return p->packet_mode ? NULL : p->gpu;
 }

@@ -15,6 +15,7 @@
 #include "SvtJpegxsEnc.h"
 #include "jxs_core.h"
 #include "SvtJpegxsGpu.h"
+#include "jxs_api_internal.h"
 #include "jxs_batch.h"
 #include "jxs_gpu.h"
 #include "jxs_queue.h"
@@ -316,4 +317,9 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_encode(svt_jpeg_xs_gpu_batch_
     const int32_t r = jxs_gpu_batch_encode((jxs_gpu_batch_t*)batch, gpu, n, (void* const(*)[4])planes,
                                            (const uint32_t(*)[4])strides, out, cuda_stream);
     return (SvtJxsErrorType_t)r;
+}
+
+jxs_gpu_enc_t* jxs_api_enc_gpu(svt_jpeg_xs_encoder_api_t* enc_api) {
+    if (!enc_api || !enc_api->private_ptr) return NULL;
+    return ((enc_prv_t*)enc_api->private_ptr)->gpu;
 }

@@ -316,6 +316,7 @@ struct jxs_gpu_batch {
     std::vector<const jxs_cfg_t*> cfgs;
     /* graphs and tuning */
     int use_graph = 1, autotune = 0;
+    int release_after_wait = 0; /* serving: working sets go back to the arena when a batch completes */
     GraphEntry cache[GRAPH_CACHE];
     uint64_t clock = 0, graph_hits = 0, graph_builds = 0, graph_updates = 0;
     std::map<std::string, Tune> tuned;
@@ -781,6 +782,53 @@ extern "C" void jxs_gpu_batch_set_options(jxs_gpu_batch_t* b, int use_graph, int
     b->autotune = autotune;
 }
 
+extern "C" void jxs_gpu_batch_set_release(jxs_gpu_batch_t* b, int on) { b->release_after_wait = on; }
+
+extern "C" uint64_t jxs_gpu_batch_enc_work_bytes(jxs_gpu_enc_t* e) {
+    EncWork w;
+    const jxs_cfg_t* c = jxs_gpu_enc_info(e, nullptr, nullptr);
+    return c ? round256(enc_work_layout(c, nullptr, &w)) : 0;
+}
+
+extern "C" uint64_t jxs_gpu_batch_dec_work_bytes(jxs_gpu_dec_t* d) {
+    DecWork w;
+    const jxs_cfg_t* c = jxs_gpu_dec_info(d, nullptr, nullptr, nullptr);
+    return c ? round256(dec_work_layout(c, nullptr, &w)) : 0;
+}
+
+/* Lays out the working sets of positions 0..n-1 for the given handles
+ * (exactly one of enc / dec non-NULL); returns how many leading positions
+ * now hold one.  Stops at the first that does not fit in the arena. */
+static int32_t ensure_enc(jxs_gpu_batch_t* b, uint32_t i, jxs_gpu_enc_t* e, cudaStream_t st);
+static int32_t ensure_dec(jxs_gpu_batch_t* b, uint32_t i, jxs_gpu_dec_t* d, cudaStream_t st);
+
+extern "C" uint32_t jxs_gpu_batch_reserve(jxs_gpu_batch_t* b, jxs_gpu_enc_t* const* enc, jxs_gpu_dec_t* const* dec, uint32_t n,
+                                          void* stream) {
+    if (!b || b->pending || n > JXS_BATCH_FRAMES) return 0;
+    /* the stream the batch will run on: a new position's counters are reset
+     * there, ahead of its kernels */
+    const cudaStream_t st = stream ? (cudaStream_t)stream : b->st;
+    uint32_t k = 0;
+    for (; k < n; k++) {
+        const int32_t r = enc ? ensure_enc(b, k, enc[k], st) : ensure_dec(b, k, dec[k], st);
+        if (r != JXS_OK) break;
+    }
+    return k;
+}
+
+static void release_all(jxs_gpu_batch_t* b) {
+    for (EncWork& w : b->enc) {
+        if (w.mem) jxs_arena_free(b->arena, w.mem, w.bytes);
+        w.mem = nullptr;
+        w.serial = 0;
+    }
+    for (DecWork& w : b->dec) {
+        if (w.mem) jxs_arena_free(b->arena, w.mem, w.bytes);
+        w.mem = nullptr;
+        w.serial = 0;
+    }
+}
+
 extern "C" void jxs_gpu_batch_set_tune(jxs_gpu_batch_t* b, const int* t5) {
     /* fixes the launch shapes of every signature (autotune results dropped) */
     Tune t = {std::max(1, std::min(t5[0], MAX_CHAINS)), t5[1] != 0, std::max(0, t5[2]), std::max(1, std::min(t5[3], 4)),
@@ -801,6 +849,54 @@ static Tune tune_for(jxs_gpu_batch_t* b, const std::string& sig, int* found) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* working sets of the positions                                             */
+/* ------------------------------------------------------------------------ */
+static int32_t ensure_enc(jxs_gpu_batch_t* b, uint32_t i, jxs_gpu_enc_t* e, cudaStream_t st) {
+    if (b->enc.size() <= i) b->enc.resize(i + 1);
+    const jxs_cfg_t* c = jxs_gpu_enc_info(e, nullptr, nullptr);
+    if (!c) return JXS_E_BAD_PARAM;
+    const uint64_t serial = jxs_gpu_enc_serial(e);
+    EncWork& w = b->enc[i];
+    if (w.serial == serial && w.mem) return JXS_OK;
+    /* the position's previous working set may still be read by work queued
+     * on this stream */
+    BCK(cudaStreamSynchronize(st));
+    release_enc(b, &w);
+    w.bytes = enc_work_layout(c, nullptr, &w);
+    w.mem = (uint8_t*)jxs_arena_alloc(b->arena, w.bytes);
+    if (!w.mem) {
+        w.bytes = 0;
+        return JXS_E_RESOURCES;
+    }
+    enc_work_layout(c, w.mem, &w);
+    BCK(cudaMemsetAsync(w.slice_done, 0, (size_t)c->nslices * sizeof(uint32_t), st));
+    w.serial = serial;
+    return JXS_OK;
+}
+
+static int32_t ensure_dec(jxs_gpu_batch_t* b, uint32_t i, jxs_gpu_dec_t* d, cudaStream_t st) {
+    if (b->dec.size() <= i) b->dec.resize(i + 1);
+    const jxs_cfg_t* c = jxs_gpu_dec_info(d, nullptr, nullptr, nullptr);
+    if (!c) return JXS_E_DEC_PTR;
+    const uint64_t serial = jxs_gpu_dec_serial(d);
+    DecWork& w = b->dec[i];
+    if (w.serial == serial && w.mem) return JXS_OK;
+    BCK(cudaStreamSynchronize(st));
+    if (w.mem) jxs_arena_free(b->arena, w.mem, w.bytes);
+    w.mem = nullptr;
+    w.serial = 0;
+    w.bytes = dec_work_layout(c, nullptr, &w);
+    w.mem = (uint8_t*)jxs_arena_alloc(b->arena, w.bytes);
+    if (!w.mem) {
+        w.bytes = 0;
+        return JXS_E_RESOURCES;
+    }
+    dec_work_layout(c, w.mem, &w);
+    w.serial = serial;
+    return JXS_OK;
+}
+
+/* ------------------------------------------------------------------------ */
 /* encode                                                                    */
 /* ------------------------------------------------------------------------ */
 extern "C" int32_t jxs_gpu_batch_encode(jxs_gpu_batch_t* b, jxs_gpu_enc_t* const* enc, uint32_t n, void* const (*planes)[4],
@@ -818,22 +914,13 @@ extern "C" int32_t jxs_gpu_batch_encode(jxs_gpu_batch_t* b, jxs_gpu_enc_t* const
         const jxs_cfg_t* c = jxs_gpu_enc_info(enc[i], &dcfg, &items[i].cap_words);
         if (!c) return JXS_E_BAD_PARAM;
         const uint64_t serial = jxs_gpu_enc_serial(enc[i]);
-        EncWork& w = b->enc[i];
-        if (w.serial != serial || !w.mem) {
-            BCK(cudaStreamSynchronize(st));
-            release_enc(b, &w);
-            w.bytes = enc_work_layout(c, nullptr, &w);
-            w.mem = (uint8_t*)jxs_arena_alloc(b->arena, w.bytes);
-            if (!w.mem) {
-                fprintf(stderr, "jxs batch: frame %u needs %llu device bytes; the batch's device budget is exhausted\n", i,
-                        (unsigned long long)w.bytes);
-                w.bytes = 0;
-                return JXS_E_RESOURCES;
-            }
-            enc_work_layout(c, w.mem, &w);
-            BCK(cudaMemsetAsync(w.slice_done, 0, (size_t)c->nslices * sizeof(uint32_t), st));
-            w.serial = serial;
+        const int32_t er = ensure_enc(b, i, enc[i], st);
+        if (er != JXS_OK) {
+            if (er == JXS_E_RESOURCES)
+                fprintf(stderr, "jxs batch: frame %u does not fit in the batch's device budget\n", i);
+            return er;
         }
+        EncWork& w = b->enc[i];
         EncItem& e = items[i];
         e.c = c;
         e.dcfg = dcfg;
@@ -939,23 +1026,13 @@ extern "C" int32_t jxs_gpu_batch_decode(jxs_gpu_batch_t* b, jxs_gpu_dec_t* const
         const jxs_cfg_t* c = jxs_gpu_dec_info(dec[i], &dcfg, &cb, &cg);
         if (!c || !bs[i]) return JXS_E_DEC_PTR;
         const uint64_t serial = jxs_gpu_dec_serial(dec[i]);
-        DecWork& w = b->dec[i];
-        if (w.serial != serial || !w.mem) {
-            BCK(cudaStreamSynchronize(st));
-            if (w.mem) jxs_arena_free(b->arena, w.mem, w.bytes);
-            w.mem = nullptr;
-            w.bytes = dec_work_layout(c, nullptr, &w);
-            w.mem = (uint8_t*)jxs_arena_alloc(b->arena, w.bytes);
-            if (!w.mem) {
-                fprintf(stderr, "jxs batch: frame %u needs %llu device bytes; the batch's device budget is exhausted\n", i,
-                        (unsigned long long)w.bytes);
-                w.bytes = 0;
-                w.serial = 0;
-                return JXS_E_RESOURCES;
-            }
-            dec_work_layout(c, w.mem, &w);
-            w.serial = serial;
+        const int32_t er = ensure_dec(b, i, dec[i], st);
+        if (er != JXS_OK) {
+            if (er == JXS_E_RESOURCES)
+                fprintf(stderr, "jxs batch: frame %u does not fit in the batch's device budget\n", i);
+            return er;
         }
+        DecWork& w = b->dec[i];
         if (!w.hdr_h && cudaMallocHost(&w.hdr_h, sizeof(c->hdr)) != cudaSuccess) {
             cudaGetLastError();
             w.hdr_h = nullptr;
@@ -1065,6 +1142,7 @@ extern "C" int32_t jxs_gpu_batch_wait(jxs_gpu_batch_t* b, int32_t* status) {
         fprintf(stderr, "jxs batch: %s\n", cudaGetErrorString(cudaGetLastError()));
         for (uint32_t i = 0; i < b->n; i++)
             if (status) status[i] = b->kind ? JXS_E_DEC_INTERNAL : JXS_E_ENC_FRAME;
+        if (b->release_after_wait) release_all(b);
         return JXS_E_RESOURCES;
     }
     if (cudaEventElapsedTime(&b->last_ms, b->t0, b->t1) != cudaSuccess) {
@@ -1085,6 +1163,7 @@ extern "C" int32_t jxs_gpu_batch_wait(jxs_gpu_batch_t* b, int32_t* status) {
         if (status) status[i] = s;
         if (s && !worst) worst = s;
     }
+    if (b->release_after_wait) release_all(b);
     return worst;
 }
 

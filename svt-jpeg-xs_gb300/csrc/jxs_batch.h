@@ -40,6 +40,16 @@ void jxs_gpu_batch_destroy(jxs_gpu_batch_t* b);
 /* use_graph: capture and replay CUDA graphs (default 1); autotune: tune the
  * launch shapes the first time a batch signature is seen (default 0) */
 void jxs_gpu_batch_set_options(jxs_gpu_batch_t* b, int use_graph, int autotune);
+/* serving: the positions' working sets return to the arena when a batch
+ * completes (wait), so the arena holds exactly the batches in flight */
+void jxs_gpu_batch_set_release(jxs_gpu_batch_t* b, int on);
+/* device bytes of one encoder / decoder position of the handle's configuration */
+uint64_t jxs_gpu_batch_enc_work_bytes(jxs_gpu_enc_t* e);
+uint64_t jxs_gpu_batch_dec_work_bytes(jxs_gpu_dec_t* d);
+/* Lays out positions 0..n-1 for enc[i] (or dec[i]; the other NULL) ahead of
+ * a batch call on `stream`; returns how many leading positions fit in the
+ * arena. */
+uint32_t jxs_gpu_batch_reserve(jxs_gpu_batch_t* b, jxs_gpu_enc_t* const* enc, jxs_gpu_dec_t* const* dec, uint32_t n, void* stream);
 /* fixed launch shapes for every batch: chains, heavy-first, blocks per SM,
  * forward / inverse rows per block */
 void jxs_gpu_batch_set_tune(jxs_gpu_batch_t* b, const int* tune5);

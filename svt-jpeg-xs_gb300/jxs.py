@@ -101,6 +101,26 @@ class BatchInfo(ctypes.Structure):
 BATCH_MAX = 64
 
 
+class ServerRequest(ctypes.Structure):
+    _fields_ = [("stream", ctypes.c_int32), ("tag", ctypes.c_uint64), ("planes", ctypes.c_void_p * 4),
+                ("strides", ctypes.c_uint32 * 4), ("bitstream", ctypes.c_void_p), ("bitstream_size", ctypes.c_uint32)]
+
+
+class ServerCompletion(ctypes.Structure):
+    _fields_ = [("tag", ctypes.c_uint64), ("stream", ctypes.c_int32), ("status", ctypes.c_uint32),
+                ("t_arrive_ns", ctypes.c_int64), ("t_start_ns", ctypes.c_int64), ("t_done_ns", ctypes.c_int64)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("batches", ctypes.c_uint64), ("batched_frames", ctypes.c_uint64), ("max_batch_seen", ctypes.c_uint64),
+                ("deferred", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64), ("device_used", ctypes.c_uint64),
+                ("device_peak", ctypes.c_uint64)]
+
+
+SERVER_BATCHED = 0
+SERVER_PER_FRAME = 1
+
+
 def lib():
     """The loaded libSvtJpegxs.so; raises if the extension was not built."""
     global _lib
@@ -175,6 +195,22 @@ def lib():
         L.svt_jpeg_xs_gpu_batch_ready.restype = u32
         L.svt_jpeg_xs_gpu_batch_get_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchInfo)]
         L.svt_jpeg_xs_gpu_batch_get_info.restype = u32
+        L.svt_jpeg_xs_gpu_server_create.argtypes = [ctypes.c_uint64, u32, u32, u32, ctypes.POINTER(ctypes.c_void_p)]
+        L.svt_jpeg_xs_gpu_server_create.restype = u32
+        L.svt_jpeg_xs_gpu_server_destroy.argtypes = [ctypes.c_void_p]
+        L.svt_jpeg_xs_gpu_server_destroy.restype = None
+        L.svt_jpeg_xs_gpu_server_add_encoder.argtypes = [ctypes.c_void_p, ctypes.POINTER(EncoderApi)]
+        L.svt_jpeg_xs_gpu_server_add_encoder.restype = ctypes.c_int32
+        L.svt_jpeg_xs_gpu_server_add_decoder.argtypes = [ctypes.c_void_p, ctypes.POINTER(DecoderApi)]
+        L.svt_jpeg_xs_gpu_server_add_decoder.restype = ctypes.c_int32
+        L.svt_jpeg_xs_gpu_server_submit.argtypes = [ctypes.c_void_p, ctypes.POINTER(ServerRequest)]
+        L.svt_jpeg_xs_gpu_server_submit.restype = u32
+        L.svt_jpeg_xs_gpu_server_poll.argtypes = [ctypes.c_void_p, ctypes.POINTER(ServerCompletion), u32]
+        L.svt_jpeg_xs_gpu_server_poll.restype = u32
+        L.svt_jpeg_xs_gpu_server_pending.argtypes = [ctypes.c_void_p]
+        L.svt_jpeg_xs_gpu_server_pending.restype = ctypes.c_uint64
+        L.svt_jpeg_xs_gpu_server_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ServerStats)]
+        L.svt_jpeg_xs_gpu_server_get_stats.restype = u32
         L.svt_jpeg_xs_image_buffer_alloc.argtypes = [ctypes.POINTER(ImageConfig)]
         L.svt_jpeg_xs_image_buffer_alloc.restype = ctypes.POINTER(ImageBuffer)
         L.svt_jpeg_xs_image_buffer_free.argtypes = [ctypes.POINTER(ImageBuffer)]
@@ -492,3 +528,61 @@ class Batch:
         return {"last_gpu_ms": i.last_gpu_ms, "last_launches": i.last_launches, "graph_hits": i.graph_hits,
                 "graph_builds": i.graph_builds, "graph_updates": i.graph_updates, "tune": list(i.tune),
                 "device_bytes": i.device_bytes, "device_used": i.device_used, "device_peak": i.device_peak}
+
+
+class Server:
+    """Serving loop (svt_jpeg_xs_gpu_server_*): requests on device buffers
+    from many streams, batched continuously (SERVER_BATCHED) or run frame by
+    frame on each stream's handle (SERVER_PER_FRAME)."""
+
+    def __init__(self, device_bytes, mode=SERVER_BATCHED, lanes=2, max_batch=16):
+        self.h = ctypes.c_void_p()
+        _check("server_create", lib().svt_jpeg_xs_gpu_server_create(int(device_bytes), mode, lanes, max_batch, ctypes.byref(self.h)))
+        self._buf = (ServerCompletion * 4096)()
+
+    def close(self):
+        if self.h:
+            lib().svt_jpeg_xs_gpu_server_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_encoder(self, enc):
+        sid = lib().svt_jpeg_xs_gpu_server_add_encoder(self.h, ctypes.byref(enc.api))
+        if sid < 0:
+            raise JxsError("server_add_encoder", E_BAD_PARAMETER)
+        return sid
+
+    def add_decoder(self, dec):
+        sid = lib().svt_jpeg_xs_gpu_server_add_decoder(self.h, ctypes.byref(dec.api))
+        if sid < 0:
+            raise JxsError("server_add_decoder", E_BAD_PARAMETER)
+        return sid
+
+    def submit(self, stream, tag, planes, bitstream, bitstream_size=0):
+        """planes: (device_ptr, stride) tuples; bitstream: device pointer"""
+        r = ServerRequest()
+        r.stream, r.tag = stream, tag
+        for k, (ptr, stride) in enumerate(planes):
+            r.planes[k] = ptr
+            r.strides[k] = stride
+        r.bitstream = bitstream
+        r.bitstream_size = bitstream_size
+        return lib().svt_jpeg_xs_gpu_server_submit(self.h, ctypes.byref(r))
+
+    def poll(self):
+        """completed requests: (tag, stream, status, t_arrive_ns, t_start_ns, t_done_ns)"""
+        n = lib().svt_jpeg_xs_gpu_server_poll(self.h, self._buf, len(self._buf))
+        return [(c.tag, c.stream, c.status, c.t_arrive_ns, c.t_start_ns, c.t_done_ns) for c in self._buf[:n]]
+
+    def pending(self):
+        return int(lib().svt_jpeg_xs_gpu_server_pending(self.h))
+
+    def stats(self):
+        st = ServerStats()
+        _check("server_get_stats", lib().svt_jpeg_xs_gpu_server_get_stats(self.h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
