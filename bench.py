@@ -94,8 +94,12 @@ def parse():
     ap.add_argument("--frames", type=int, default=8, help="frames encoded and decoded per step")
     ap.add_argument("--streams", type=int, default=3, help="encoder/decoder pairs, each on its own CUDA stream")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline sample budget (0: not measured)")
-    ap.add_argument("--workload", default="stream4k", choices=["stream4k", "mixed48", "8k"],
-                    help="stream4k: the default line; mixed48 / 8k: batched form against the per-frame path")
+    ap.add_argument("--workload", default="stream4k", choices=["stream4k", "mixed48", "8k", "serve"],
+                    help="stream4k: the default line; mixed48 / 8k: batched form against the per-frame path; "
+                         "serve: the serving loop against the per-frame path")
+    ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: seconds of arrivals")
+    ap.add_argument("--serve-lanes", type=int, default=2, help="serve: encode lanes (and as many decode lanes)")
+    ap.add_argument("--serve-max-batch", type=int, default=16, help="serve: requests per batch at most")
     ap.add_argument("--seq-frames", type=int, default=SEQ_FRAMES,
                     help="distinct frames of the stream cycled through (each 33 MB; 4 or more keep inputs above L2)")
     return ap.parse_args()
@@ -782,11 +786,153 @@ def run_workload(args, name, local):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# serving workload: 24 Poisson streams, 2000 frames/s in total, encode and
+# decode 50/50, continuous batching under a 40 GB budget against the
+# per-frame path, on the same arrival schedule
+# ---------------------------------------------------------------------------
+SERVE_TYPES = [(1920, 540, 10, 3, 5, 41), (1920, 1080, 8, 3, 3, 42), (3840, 2160, 10, 3, 2, 43)]  # w, h, depth, fmt, bpp, seed
+
+
+def run_serve(args, local):
+    import torch
+
+    import jxs
+    import jxs_synth as S
+    import oracle_lib as O
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    O.build_oracle()
+    rng = np.random.default_rng(5)
+    nstreams, rate, seconds = 24, 2000.0, args.serve_seconds
+    types = [int(rng.integers(0, len(SERVE_TYPES))) for _ in range(nstreams)]
+    kinds = ["enc" if i % 2 == 0 else "dec" for i in range(nstreams)]
+    # two seeded frames per type, on the device; decode inputs are the
+    # oracle's codestreams of the same frames
+    frames, codestreams = {}, {}
+    for t, (w, h, d, fmt, bpp, seed) in enumerate(SERVE_TYPES):
+        frames[t] = [S.frame(w, h, d, fmt, seed=seed + 10 * j) for j in range(2)]
+        p = O.make_params(w, h, d, fmt, bpp, threads=os.cpu_count() or 1)
+        codestreams[t] = []
+        for fr in frames[t]:
+            err, bs = O.oracle_encode(p, fr)
+            assert err == 0
+            codestreams[t].append(bs)
+    d_frames = {t: [[torch.from_numpy(p).to(dev) for p in fr] for fr in frames[t]] for t in frames}
+    d_bs = {t: [torch.from_numpy(b).to(dev) for b in codestreams[t]] for t in codestreams}
+    # arrivals: per stream exponential gaps, merged
+    arrivals = []
+    for sidx in range(nstreams):
+        t = 0.0
+        while True:
+            t += rng.exponential(nstreams / rate)
+            if t >= seconds:
+                break
+            arrivals.append((t, sidx))
+    arrivals.sort()
+    depth = 32  # output buffers per stream (ring)
+
+    def run(mode):
+        server = jxs.Server(40 << 30, mode, lanes=args.serve_lanes, max_batch=args.serve_max_batch)
+        handles, sids, outs = [], [], []
+        for sidx in range(nstreams):
+            w, h, d, fmt, bpp, _ = SERVE_TYPES[types[sidx]]
+            if kinds[sidx] == "enc":
+                hnd = jxs.Encoder(w, h, d, fmt, bpp)
+                sids.append(server.add_encoder(hnd))
+                outs.append([torch.zeros(hnd.frame_bytes, dtype=torch.uint8, device=dev) for _ in range(depth)])
+            else:
+                hnd = jxs.Decoder(codestreams[types[sidx]][0])
+                sids.append(server.add_decoder(hnd))
+                outs.append([[torch.zeros_like(p) for p in d_frames[types[sidx]][0]] for _ in range(depth)])
+            handles.append(hnd)
+        # warm-up: one request per stream
+        for sidx in range(nstreams):
+            submit(server, sidx, sids, outs, 0, 1 << 40 | sidx)
+        while server.pending():
+            time.sleep(0.001)
+        server.poll()
+        done, meta = [], {}
+        seq = [0] * nstreams
+        t0 = time.perf_counter()
+        for n, (ta, sidx) in enumerate(arrivals):
+            while time.perf_counter() - t0 < ta:
+                pass
+            k = seq[sidx]
+            seq[sidx] += 1
+            meta[n] = (sidx, k)
+            assert submit(server, sidx, sids, outs, k, n) == 0
+            if n % 16 == 0:
+                done.extend(server.poll())
+        while server.pending():
+            done.extend(server.poll())
+            time.sleep(0.0002)
+        done.extend(server.poll())
+        st = server.stats()
+        # the last request of every stream against its result alone
+        checks = 0
+        last = {}
+        for n, (sidx, k) in meta.items():
+            last[sidx] = (n, k)
+        for sidx, (n, k) in last.items():
+            t = types[sidx]
+            if kinds[sidx] == "enc":
+                want = codestreams[t][k % 2]
+                assert np.array_equal(outs[sidx][k % depth].cpu().numpy(), want), "served codestream differs"
+            else:
+                err, want = O.oracle_decode(codestreams[t][k % 2], threads=os.cpu_count() or 1)
+                assert err == 0 and all(np.array_equal(a.cpu().numpy(), b) for a, b in zip(outs[sidx][k % depth], want)), \
+                    "served decode differs"
+            checks += 1
+        server.close()
+        for hnd in handles:
+            hnd.close()
+        assert len(done) == len(arrivals) and all(x[2] == 0 for x in done), "a request failed"
+        lat = np.array([(x[5] - x[3]) / 1e6 for x in done])
+        span = (max(x[5] for x in done) - min(x[3] for x in done)) / 1e9
+        pix = sum(SERVE_TYPES[types[sidx]][0] * SERVE_TYPES[types[sidx]][1] for _, sidx in arrivals)
+        out = {"gpix_s": pix / span / 1e9, "frames_s": len(done) / span, "frame_latency_ms_p50": float(np.percentile(lat, 50)),
+               "frame_latency_ms_p99": float(np.percentile(lat, 99)), "frame_latency_ms_max": float(lat.max()),
+               "requests": len(done), "checked_bit_exact": checks}
+        if mode == jxs.SERVER_BATCHED:
+            out.update({"batches": st["batches"], "mean_batch": st["batched_frames"] / max(1, st["batches"]),
+                        "max_batch": st["max_batch_seen"], "deferred_for_memory": st["deferred"],
+                        "device_peak_bytes": st["device_peak"], "device_budget_bytes": st["device_bytes"]})
+        return out
+
+    def submit(server, sidx, sids, outs, k, tag):
+        t = types[sidx]
+        if kinds[sidx] == "enc":
+            planes = [(p.data_ptr(), p.shape[1]) for p in d_frames[t][k % 2]]
+            return server.submit(sids[sidx], tag, planes, outs[sidx][k % depth].data_ptr())
+        planes = [(p.data_ptr(), p.shape[1]) for p in outs[sidx][k % depth]]
+        b = d_bs[t][k % 2]
+        return server.submit(sids[sidx], tag, planes, b.data_ptr(), b.numel())
+
+    batched = run(jxs.SERVER_BATCHED)
+    per_frame = run(jxs.SERVER_PER_FRAME)
+    line = {"workload": "serve", "metric": "served encode/decode Gpix/s and p50/p99 frame latency, batched vs per-frame",
+            "unit": "Gpix/s", "value": batched["gpix_s"], "n_gpus": 1, "higher_is_better": True, "dtype": "int32",
+            "data": "synthetic (seeded, integer-only generator; no dataset); decode requests use the oracle's codestreams",
+            "config": {"workload": "24 streams, Poisson arrivals totalling %.0f frames/s for %.1f s; stream types from seed 5 "
+                                   "(1920x540 4:2:2 10-bit bpp 5, 1920x1080 4:2:2 8-bit bpp 3, 3840x2160 4:2:2 10-bit bpp 2); "
+                                   "even streams encode, odd streams decode; device budget 40 GB" % (rate, seconds),
+                       "stream_types": types, "lanes": args.serve_lanes, "max_batch": args.serve_max_batch},
+            "batched": batched, "per_frame": per_frame,
+            "latency_definition": "request submit to completion seen by the server's scheduler (host steady clock)"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "serve":
+        if rank == 0:
+            run_serve(args, local)
         return
     if args.workload != "stream4k":
         if rank == 0:
