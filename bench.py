@@ -98,6 +98,8 @@ def parse():
                     help="stream4k: the default line; mixed48 / 8k: batched form against the per-frame path; "
                          "serve: the serving loop against the per-frame path")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: seconds of arrivals")
+    ap.add_argument("--serve-rates", default="2000,6000,10000",
+                    help="serve: offered frames/s; the first is the headline, the others a load sweep")
     ap.add_argument("--serve-lanes", type=int, default=2, help="serve: encode lanes (and as many decode lanes)")
     ap.add_argument("--serve-max-batch", type=int, default=16, help="serve: requests per batch at most")
     ap.add_argument("--seq-frames", type=int, default=SEQ_FRAMES,
@@ -805,7 +807,8 @@ def run_serve(args, local):
     dev = torch.device("cuda", local)
     O.build_oracle()
     rng = np.random.default_rng(5)
-    nstreams, rate, seconds = 24, 2000.0, args.serve_seconds
+    nstreams, seconds = 24, args.serve_seconds
+    rate = float(args.serve_rates.split(",")[0])
     types = [int(rng.integers(0, len(SERVE_TYPES))) for _ in range(nstreams)]
     kinds = ["enc" if i % 2 == 0 else "dec" for i in range(nstreams)]
     # two seeded frames per type, on the device; decode inputs are the
@@ -821,19 +824,23 @@ def run_serve(args, local):
             codestreams[t].append(bs)
     d_frames = {t: [[torch.from_numpy(p).to(dev) for p in fr] for fr in frames[t]] for t in frames}
     d_bs = {t: [torch.from_numpy(b).to(dev) for b in codestreams[t]] for t in codestreams}
-    # arrivals: per stream exponential gaps, merged
-    arrivals = []
-    for sidx in range(nstreams):
-        t = 0.0
-        while True:
-            t += rng.exponential(nstreams / rate)
-            if t >= seconds:
-                break
-            arrivals.append((t, sidx))
-    arrivals.sort()
-    depth = 32  # output buffers per stream (ring)
+    def arrivals_at(rate):
+        # per stream exponential gaps at rate / nstreams, merged
+        r = np.random.default_rng(6)
+        arr = []
+        for sidx in range(nstreams):
+            t = 0.0
+            while True:
+                t += r.exponential(nstreams / rate)
+                if t >= seconds:
+                    break
+                arr.append((t, sidx))
+        arr.sort()
+        return arr
 
-    def run(mode):
+    depth = 64  # output buffers per stream (ring)
+
+    def run(mode, arrivals):
         server = jxs.Server(40 << 30, mode, lanes=args.serve_lanes, max_batch=args.serve_max_batch)
         handles, sids, outs = [], [], []
         for sidx in range(nstreams):
@@ -910,10 +917,16 @@ def run_serve(args, local):
         b = d_bs[t][k % 2]
         return server.submit(sids[sidx], tag, planes, b.data_ptr(), b.numel())
 
-    batched = run(jxs.SERVER_BATCHED)
-    per_frame = run(jxs.SERVER_PER_FRAME)
+    rates = [float(x) for x in args.serve_rates.split(",")]
+    sweep = []
+    for r in rates:
+        arr = arrivals_at(r)
+        sweep.append({"offered_frames_s": r, "batched": run(jxs.SERVER_BATCHED, arr),
+                      "per_frame": run(jxs.SERVER_PER_FRAME, arr)})
+    batched, per_frame = sweep[0]["batched"], sweep[0]["per_frame"]
     line = {"workload": "serve", "metric": "served encode/decode Gpix/s and p50/p99 frame latency, batched vs per-frame",
             "unit": "Gpix/s", "value": batched["gpix_s"], "n_gpus": 1, "higher_is_better": True, "dtype": "int32",
+            "load_sweep": sweep[1:],
             "data": "synthetic (seeded, integer-only generator; no dataset); decode requests use the oracle's codestreams",
             "config": {"workload": "24 streams, Poisson arrivals totalling %.0f frames/s for %.1f s; stream types from seed 5 "
                                    "(1920x540 4:2:2 10-bit bpp 5, 1920x1080 4:2:2 8-bit bpp 3, 3840x2160 4:2:2 10-bit bpp 2); "

@@ -784,6 +784,14 @@ extern "C" void jxs_gpu_batch_set_options(jxs_gpu_batch_t* b, int use_graph, int
 
 extern "C" void jxs_gpu_batch_set_release(jxs_gpu_batch_t* b, int on) { b->release_after_wait = on; }
 
+static void release_all(jxs_gpu_batch_t* b);
+
+extern "C" int jxs_gpu_batch_release(jxs_gpu_batch_t* b) {
+    if (!b || b->pending) return 0;
+    release_all(b);
+    return 1;
+}
+
 extern "C" uint64_t jxs_gpu_batch_enc_work_bytes(jxs_gpu_enc_t* e) {
     EncWork w;
     const jxs_cfg_t* c = jxs_gpu_enc_info(e, nullptr, nullptr);

@@ -43,6 +43,9 @@ void jxs_gpu_batch_set_options(jxs_gpu_batch_t* b, int use_graph, int autotune);
 /* serving: the positions' working sets return to the arena when a batch
  * completes (wait), so the arena holds exactly the batches in flight */
 void jxs_gpu_batch_set_release(jxs_gpu_batch_t* b, int on);
+/* returns every position's working set to the arena now (nothing in
+ * flight); 0 if a batch is in flight */
+int jxs_gpu_batch_release(jxs_gpu_batch_t* b);
 /* device bytes of one encoder / decoder position of the handle's configuration */
 uint64_t jxs_gpu_batch_enc_work_bytes(jxs_gpu_enc_t* e);
 uint64_t jxs_gpu_batch_dec_work_bytes(jxs_gpu_dec_t* d);

@@ -16,8 +16,9 @@
  *                 Requests that arrive while every lane is
  *                 busy wait for the next free lane, so the batch size follows
  *                 the load: one request alone runs at once, a burst runs
- *                 together.  A lane's working sets return to the arena when
- *                 its batches complete.
+ *                 together.  A lane keeps its working sets for its next batch;
+ *                 when a batch does not fit, the idle lanes give theirs back
+ *                 to the arena first.
  *   per-frame     the plain drop-in path: every request goes to a free frame
  *                 slot of its stream's own handle as soon as it arrives
  *                 (jxs_gpu_enc_submit / jxs_gpu_dec_submit), several frames
@@ -137,8 +138,18 @@ static int lane_launch(jxs_server_t* s, SrvLane& L) {
     }
     /* admission by the device budget: the leading requests whose working
      * sets fit; the others go back to the head of the queue */
-    const uint32_t n = L.kind == 0 ? jxs_gpu_batch_reserve(L.b, eh.data(), nullptr, n0, L.st)
-                                   : jxs_gpu_batch_reserve(L.b, nullptr, dh.data(), n0, L.st);
+    auto reserve = [&]() {
+        return L.kind == 0 ? jxs_gpu_batch_reserve(L.b, eh.data(), nullptr, n0, L.st)
+                           : jxs_gpu_batch_reserve(L.b, nullptr, dh.data(), n0, L.st);
+    };
+    uint32_t n = reserve();
+    if (n < n0) {
+        /* idle lanes keep their working sets for the next batch of the same
+         * shapes; under memory pressure they give them back first */
+        for (SrvLane& o : s->lanes)
+            if (!o.busy) jxs_gpu_batch_release(o.b);
+        n = reserve();
+    }
     if (n < n0) {
         std::lock_guard<std::mutex> g(s->mu);
         s->deferred += n0 - n;
@@ -301,10 +312,10 @@ extern "C" jxs_server_t* jxs_server_create(uint64_t device_bytes, int mode, int 
                 *err = JXS_E_RESOURCES;
                 return nullptr;
             }
-            /* parameters change with every mix of requests: launch directly;
-             * working sets back to the arena when a batch completes */
+            /* parameters change with every mix of requests: launch directly.
+             * Working sets stay with their positions between batches and go
+             * back to the arena when another lane needs the memory */
             jxs_gpu_batch_set_options(L.b, 0, 0);
-            jxs_gpu_batch_set_release(L.b, 1);
         }
     }
     return s;

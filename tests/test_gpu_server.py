@@ -81,7 +81,7 @@ def test_server_mixed_streams_same_alone_and_in_mix(gpu, mode):
     st = server.stats()
     if mode == "batched":
         assert st["batched_frames"] == len(jobs) and st["max_batch_seen"] > 1 and st["batches"] < len(jobs)
-        assert st["device_used"] == 0
+        assert st["device_peak"] <= st["device_bytes"]
     server.close()
     for x in list(encs.values()) + list(decs.values()):
         x.close()
