@@ -100,7 +100,7 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: seconds of arrivals")
     ap.add_argument("--serve-rates", default="2000,6000,10000",
                     help="serve: offered frames/s; the first is the headline, the others a load sweep")
-    ap.add_argument("--serve-lanes", type=int, default=2, help="serve: encode lanes (and as many decode lanes)")
+    ap.add_argument("--serve-lanes", type=int, default=4, help="serve: encode lanes (and as many decode lanes)")
     ap.add_argument("--serve-max-batch", type=int, default=16, help="serve: requests per batch at most")
     ap.add_argument("--seq-frames", type=int, default=SEQ_FRAMES,
                     help="distinct frames of the stream cycled through (each 33 MB; 4 or more keep inputs above L2)")

@@ -309,6 +309,15 @@ struct jxs_gpu_batch {
     int* status_h = nullptr;
     std::vector<EncWork> enc;
     std::vector<DecWork> dec;
+    /* idle working sets, kept for positions that need the same handle's
+     * layout again; freed when the arena runs short */
+    struct Idle {
+        int kind; /* 0 encoder, 1 decoder */
+        uint64_t serial;
+        uint8_t* mem;
+        uint64_t bytes;
+    };
+    std::vector<Idle> idle;
     /* the call in flight */
     int pending = 0, kind = 0;
     uint32_t n = 0;
@@ -739,6 +748,8 @@ extern "C" jxs_gpu_batch_t* jxs_gpu_batch_create(uint64_t device_bytes, jxs_aren
     return b;
 }
 
+static void release_idle(jxs_gpu_batch_t* b);
+
 static void release_enc(jxs_gpu_batch_t* b, EncWork* w) {
     if (w->mem) jxs_arena_free(b->arena, w->mem, w->bytes);
     w->mem = nullptr;
@@ -760,6 +771,7 @@ extern "C" void jxs_gpu_batch_destroy(jxs_gpu_batch_t* b) {
     if (b->st) cudaStreamSynchronize(b->st);
     for (EncWork& w : b->enc) release_enc(b, &w);
     for (DecWork& w : b->dec) release_dec(b, &w);
+    release_idle(b);
     for (GraphEntry& g : b->cache)
         if (g.exec) cudaGraphExecDestroy(g.exec);
     for (int c = 0; c < MAX_CHAINS; c++) {
@@ -824,6 +836,11 @@ extern "C" uint32_t jxs_gpu_batch_reserve(jxs_gpu_batch_t* b, jxs_gpu_enc_t* con
     return k;
 }
 
+static void release_idle(jxs_gpu_batch_t* b) {
+    for (const auto& x : b->idle) jxs_arena_free(b->arena, x.mem, x.bytes);
+    b->idle.clear();
+}
+
 static void release_all(jxs_gpu_batch_t* b) {
     for (EncWork& w : b->enc) {
         if (w.mem) jxs_arena_free(b->arena, w.mem, w.bytes);
@@ -835,6 +852,29 @@ static void release_all(jxs_gpu_batch_t* b) {
         w.mem = nullptr;
         w.serial = 0;
     }
+    release_idle(b);
+}
+
+/* A working set for a position that needs `serial`'s layout: an idle one of
+ * that layout, else a new one from the arena (idle sets of other layouts are
+ * freed first when the arena is short).  No batch of this object is in flight
+ * when positions change, so no set handed over here is still being read. */
+static uint8_t* take_set(jxs_gpu_batch_t* b, int kind, uint64_t serial, uint64_t bytes, int* fresh) {
+    *fresh = 0;
+    for (size_t k = 0; k < b->idle.size(); k++) {
+        if (b->idle[k].kind == kind && b->idle[k].serial == serial) {
+            uint8_t* m = b->idle[k].mem;
+            b->idle.erase(b->idle.begin() + (long)k);
+            return m;
+        }
+    }
+    uint8_t* m = (uint8_t*)jxs_arena_alloc(b->arena, bytes);
+    if (!m && !b->idle.empty()) {
+        release_idle(b);
+        m = (uint8_t*)jxs_arena_alloc(b->arena, bytes);
+    }
+    *fresh = m != nullptr;
+    return m;
 }
 
 extern "C" void jxs_gpu_batch_set_tune(jxs_gpu_batch_t* b, const int* t5) {
@@ -866,18 +906,20 @@ static int32_t ensure_enc(jxs_gpu_batch_t* b, uint32_t i, jxs_gpu_enc_t* e, cuda
     const uint64_t serial = jxs_gpu_enc_serial(e);
     EncWork& w = b->enc[i];
     if (w.serial == serial && w.mem) return JXS_OK;
-    /* the position's previous working set may still be read by work queued
-     * on this stream */
-    BCK(cudaStreamSynchronize(st));
-    release_enc(b, &w);
+    if (w.mem) b->idle.push_back({0, w.serial, w.mem, w.bytes});
+    w.mem = nullptr;
+    w.serial = 0;
     w.bytes = enc_work_layout(c, nullptr, &w);
-    w.mem = (uint8_t*)jxs_arena_alloc(b->arena, w.bytes);
+    int fresh = 0;
+    w.mem = take_set(b, 0, serial, w.bytes, &fresh);
     if (!w.mem) {
         w.bytes = 0;
         return JXS_E_RESOURCES;
     }
     enc_work_layout(c, w.mem, &w);
-    BCK(cudaMemsetAsync(w.slice_done, 0, (size_t)c->nslices * sizeof(uint32_t), st));
+    /* a new set's slice counters start at zero; a reused one's were reset by
+     * the kernels of its last frame */
+    if (fresh) BCK(cudaMemsetAsync(w.slice_done, 0, (size_t)c->nslices * sizeof(uint32_t), st));
     w.serial = serial;
     return JXS_OK;
 }
@@ -889,12 +931,13 @@ static int32_t ensure_dec(jxs_gpu_batch_t* b, uint32_t i, jxs_gpu_dec_t* d, cuda
     const uint64_t serial = jxs_gpu_dec_serial(d);
     DecWork& w = b->dec[i];
     if (w.serial == serial && w.mem) return JXS_OK;
-    BCK(cudaStreamSynchronize(st));
-    if (w.mem) jxs_arena_free(b->arena, w.mem, w.bytes);
+    (void)st;
+    if (w.mem) b->idle.push_back({1, w.serial, w.mem, w.bytes});
     w.mem = nullptr;
     w.serial = 0;
     w.bytes = dec_work_layout(c, nullptr, &w);
-    w.mem = (uint8_t*)jxs_arena_alloc(b->arena, w.bytes);
+    int fresh = 0;
+    w.mem = take_set(b, 1, serial, w.bytes, &fresh);
     if (!w.mem) {
         w.bytes = 0;
         return JXS_E_RESOURCES;
