@@ -897,10 +897,14 @@ def run_serve(args, local):
             hnd.close()
         assert len(done) == len(arrivals) and all(x[2] == 0 for x in done), "a request failed"
         lat = np.array([(x[5] - x[3]) / 1e6 for x in done])
+        queue = np.array([(x[4] - x[3]) / 1e6 for x in done])
+        service = np.array([(x[5] - x[4]) / 1e6 for x in done])
         span = (max(x[5] for x in done) - min(x[3] for x in done)) / 1e9
         pix = sum(SERVE_TYPES[types[sidx]][0] * SERVE_TYPES[types[sidx]][1] for _, sidx in arrivals)
         out = {"gpix_s": pix / span / 1e9, "frames_s": len(done) / span, "frame_latency_ms_p50": float(np.percentile(lat, 50)),
                "frame_latency_ms_p99": float(np.percentile(lat, 99)), "frame_latency_ms_max": float(lat.max()),
+               "queue_ms_p50": float(np.percentile(queue, 50)), "queue_ms_p99": float(np.percentile(queue, 99)),
+               "service_ms_p50": float(np.percentile(service, 50)), "service_ms_p99": float(np.percentile(service, 99)),
                "requests": len(done), "checked_bit_exact": checks}
         if mode == jxs.SERVER_BATCHED:
             out.update({"batches": st["batches"], "mean_batch": st["batched_frames"] / max(1, st["batches"]),

@@ -159,7 +159,7 @@ struct DecWork {
     uint64_t out_off[JXS_MAXC];
     uint32_t* prec_off_h = nullptr; /* page-locked: precinct offsets of a host codestream */
     uint32_t prec_cap = 0;
-    uint8_t* hdr_h = nullptr;       /* page-locked: header of a device codestream */
+    uint8_t* hdr_h = nullptr;       /* header of a device codestream (in the batch's page-locked pool) */
 };
 
 /* Lays out (base NULL: only sizes) the encoder working set of one frame. */
@@ -226,7 +226,24 @@ static uint64_t dec_work_layout(const jxs_cfg_t* c, uint8_t* base, DecWork* w) {
 /* ------------------------------------------------------------------------ */
 /* plans: the launches of one batch                                          */
 /* ------------------------------------------------------------------------ */
-enum { OP_FWD_V, OP_FWD_H, OP_RC, OP_PACK, OP_WALK, OP_UNPACK, OP_INV_H, OP_INV_V };
+/* Ops ending in _S carry the per-frame launch structure (at most 4 jobs)
+ * and those ending in 1 one frame's arguments: a stage of one or two frames
+ * then launches with a few hundred bytes of parameters instead of the
+ * batched tables (about 9 KB), which costs host time on every launch. */
+enum {
+    OP_FWD_V, OP_FWD_H, OP_RC, OP_PACK, OP_WALK, OP_UNPACK, OP_INV_H, OP_INV_V,
+    OP_FWD_V_S, OP_FWD_H_S, OP_INV_H_S, OP_INV_V_S, OP_RC1, OP_PACK1, OP_WALK1, OP_UNPACK1
+};
+
+/* The per-frame launch structure holding the (at most JXS_MAXC) jobs of a
+ * batched one; both have the same fields before the job table. */
+template <class SMALL, class BIG>
+static void shrink(SMALL* sm, const BIG* big) {
+    static_assert(offsetof(SMALL, job) == offsetof(BIG, job), "launch headers differ");
+    memset(sm, 0, sizeof(*sm));
+    memcpy(sm, big, offsetof(BIG, job));
+    memcpy(sm->job, big->job, (size_t)big->njobs * sizeof(big->job[0]));
+}
 
 struct Op {
     int type, kind, chain, nblocks;
@@ -307,6 +324,7 @@ struct jxs_gpu_batch {
     cudaEvent_t fork = nullptr, join[MAX_CHAINS] = {}, done = nullptr, t0 = nullptr, t1 = nullptr;
     int* status_d = nullptr;
     int* status_h = nullptr;
+    uint8_t* hdr_pool = nullptr; /* page-locked: one codestream header per position */
     std::vector<EncWork> enc;
     std::vector<DecWork> dec;
     /* idle working sets, kept for positions that need the same handle's
@@ -366,7 +384,13 @@ static int32_t plan_encode_chain(const std::vector<EncItem>& it, const std::vect
             FwdVLaunchB* L = (FwdVLaunchB*)scratch.data();
             memset(L, 0, sizeof(*L));
             auto flush = [&]() {
-                if (L->njobs) P->add(OP_FWD_V, kind, chain, L->ntiles, (uint32_t)t.grid_per_sm, 0, L, sizeof(*L));
+                if (L->njobs > JXS_MAXC) {
+                    P->add(OP_FWD_V, kind, chain, L->ntiles, (uint32_t)t.grid_per_sm, 0, L, sizeof(*L));
+                } else if (L->njobs) {
+                    FwdVLaunch sm;
+                    shrink(&sm, L);
+                    P->add(OP_FWD_V_S, kind, chain, L->ntiles, (uint32_t)t.grid_per_sm, 0, &sm, sizeof(sm));
+                }
                 memset(L, 0, sizeof(*L));
             };
             for (int f : fr) {
@@ -396,7 +420,12 @@ static int32_t plan_encode_chain(const std::vector<EncItem>& it, const std::vect
                 if (L->njobs) {
                     const int blocks = fwd_h_layout(*L, t.fh_rpb);
                     if (blocks < 0) err = JXS_E_BAD_PARAM;
-                    else P->add(OP_FWD_H, kind, chain, blocks, 0, 0, L, sizeof(*L));
+                    else if (L->njobs > JXS_MAXC) P->add(OP_FWD_H, kind, chain, blocks, 0, 0, L, sizeof(*L));
+                    else {
+                        FwdHLaunch sm;
+                        shrink(&sm, L);
+                        P->add(OP_FWD_H_S, kind, chain, blocks, 0, 0, &sm, sizeof(sm));
+                    }
                 }
                 memset(L, 0, sizeof(*L));
             };
@@ -419,7 +448,8 @@ static int32_t plan_encode_chain(const std::vector<EncItem>& it, const std::vect
         memset(L, 0, sizeof(*L));
         uint32_t cap = 0;
         auto flush = [&]() {
-            if (L->nframes) P->add(op == 0 ? OP_RC : OP_PACK, 0, chain, L->nblocks, cap, 0, L, sizeof(*L));
+            if (L->nframes > 1) P->add(op == 0 ? OP_RC : OP_PACK, 0, chain, L->nblocks, cap, 0, L, sizeof(*L));
+            else if (L->nframes) P->add(op == 0 ? OP_RC1 : OP_PACK1, 0, chain, L->nblocks, cap, 0, &L->job[0], sizeof(L->job[0]));
             memset(L, 0, sizeof(*L));
             cap = 0;
         };
@@ -454,14 +484,16 @@ static int32_t plan_decode_chain(const std::vector<DecItem>& it, const std::vect
         auto flush = [&]() {
             if (L->nframes) {
                 if (op == 0) {
-                    P->add(OP_WALK, 0, chain, L->nslices, 0, 0, L, sizeof(*L));
+                    if (L->nframes > 1) P->add(OP_WALK, 0, chain, L->nslices, 0, 0, L, sizeof(*L));
+                    else P->add(OP_WALK1, 0, chain, L->nslices, 0, 0, &L->job[0], sizeof(L->job[0]));
                 } else {
                     /* one shared-memory layout for the launch: the largest
                      * precinct buffer that leaves room for the rest */
                     const size_t fixed = (size_t)cg * 3 + 2 * (8 * JXS_MAXPK + 32) + 64;
                     const size_t room = kSmemMax - 16 * 1024;
                     if (cb + fixed > room) cb = room > fixed + 4096 ? (uint32_t)(room - fixed) : 4096;
-                    P->add(OP_UNPACK, 0, chain, L->nblocks, cb & ~15u, cg, L, sizeof(*L));
+                    if (L->nframes > 1) P->add(OP_UNPACK, 0, chain, L->nblocks, cb & ~15u, cg, L, sizeof(*L));
+                    else P->add(OP_UNPACK1, 0, chain, L->nblocks, cb & ~15u, cg, &L->job[0], sizeof(L->job[0]));
                 }
             }
             memset(L, 0, sizeof(*L));
@@ -498,7 +530,12 @@ static int32_t plan_decode_chain(const std::vector<DecItem>& it, const std::vect
                 if (L->njobs) {
                     const int blocks = inv_h_layout(*L, t.ih_rpb);
                     if (blocks < 0) err = JXS_E_BAD_PARAM;
-                    else P->add(OP_INV_H, ok, chain, blocks, 0, 0, L, sizeof(*L));
+                    else if (L->njobs > JXS_MAXC) P->add(OP_INV_H, ok, chain, blocks, 0, 0, L, sizeof(*L));
+                    else {
+                        InvHLaunch sm;
+                        shrink(&sm, L);
+                        P->add(OP_INV_H_S, ok, chain, blocks, 0, 0, &sm, sizeof(sm));
+                    }
                 }
                 memset(L, 0, sizeof(*L));
             };
@@ -523,7 +560,13 @@ static int32_t plan_decode_chain(const std::vector<DecItem>& it, const std::vect
             memset(L, 0, sizeof(*L));
             int blocks = 0;
             auto flush = [&]() {
-                if (L->njobs) P->add(OP_INV_V, ok, chain, blocks, 0, 0, L, sizeof(*L));
+                if (L->njobs > JXS_MAXC) {
+                    P->add(OP_INV_V, ok, chain, blocks, 0, 0, L, sizeof(*L));
+                } else if (L->njobs) {
+                    InvVLaunch sm;
+                    shrink(&sm, L);
+                    P->add(OP_INV_V_S, ok, chain, blocks, 0, 0, &sm, sizeof(sm));
+                }
                 memset(L, 0, sizeof(*L));
                 blocks = 0;
             };
@@ -568,6 +611,30 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         case OP_UNPACK: e = jxs_launch_unpack_batch((const DecPrecLaunch*)d, o.a, o.b, s); break;
         case OP_INV_H: e = jxs_launch_inv_h_batch((const InvHLaunchB*)d, o.kind, o.nblocks, s); break;
         case OP_INV_V: e = jxs_launch_inv_v_batch((const InvVLaunchB*)d, o.kind, o.nblocks, s); break;
+        case OP_FWD_V_S: e = jxs_launch_fwd_v((const FwdVLaunch*)d, o.kind, (int)o.a, s); break;
+        case OP_FWD_H_S: e = jxs_launch_fwd_h((const FwdHLaunch*)d, o.kind, o.nblocks, s); break;
+        case OP_INV_H_S: e = jxs_launch_inv_h((const InvHLaunch*)d, o.kind, o.nblocks, s); break;
+        case OP_INV_V_S: e = jxs_launch_inv_v((const InvVLaunch*)d, o.kind, o.nblocks, s); break;
+        case OP_RC1: {
+            const EncPrecFrame* F = (const EncPrecFrame*)d;
+            e = jxs_launch_rc(F->cfg, (uint32_t)o.nblocks, 0, F->gcli, F->cost, F->slice_done, F->rc, F->status, s);
+            break;
+        }
+        case OP_PACK1: {
+            const EncPrecFrame* F = (const EncPrecFrame*)d;
+            e = jxs_launch_pack(F->cfg, (uint32_t)o.nblocks, F->coef, F->gcli, F->rc, F->out, o.a, F->status, s);
+            break;
+        }
+        case OP_WALK1: {
+            const DecPrecFrame* F = (const DecPrecFrame*)d;
+            e = jxs_launch_walk(F->cfg, (uint32_t)o.nblocks, F->bs, F->bs_size, F->prec_off, F->status + 1, F->status, s);
+            break;
+        }
+        case OP_UNPACK1: {
+            const DecPrecFrame* F = (const DecPrecFrame*)d;
+            e = jxs_launch_unpack(F->cfg, F->bs, F->bs_size, F->prec_off, F->coef, (uint32_t)o.nblocks, o.a, o.b, F->status, s);
+            break;
+        }
         }
         BCK(e);
     }
@@ -739,6 +806,7 @@ extern "C" jxs_gpu_batch_t* jxs_gpu_batch_create(uint64_t device_bytes, jxs_aren
     ok = ok && cudaEventCreate(&b->t0) == cudaSuccess && cudaEventCreate(&b->t1) == cudaSuccess;
     ok = ok && cudaMalloc(&b->status_d, 2 * JXS_BATCH_FRAMES * sizeof(int)) == cudaSuccess;
     ok = ok && cudaMallocHost(&b->status_h, 2 * JXS_BATCH_FRAMES * sizeof(int)) == cudaSuccess;
+    ok = ok && cudaMallocHost(&b->hdr_pool, (size_t)JXS_BATCH_FRAMES * sizeof(((jxs_cfg_t*)0)->hdr)) == cudaSuccess;
     if (!ok) {
         cudaGetLastError();
         jxs_gpu_batch_destroy(b);
@@ -760,7 +828,6 @@ static void release_dec(jxs_gpu_batch_t* b, DecWork* w) {
     w->mem = nullptr;
     w->serial = 0;
     if (w->prec_off_h) cudaFreeHost(w->prec_off_h);
-    if (w->hdr_h) cudaFreeHost(w->hdr_h);
     w->prec_off_h = nullptr;
     w->hdr_h = nullptr;
     w->prec_cap = 0;
@@ -784,6 +851,7 @@ extern "C" void jxs_gpu_batch_destroy(jxs_gpu_batch_t* b) {
     if (b->t1) cudaEventDestroy(b->t1);
     cudaFree(b->status_d);
     if (b->status_h) cudaFreeHost(b->status_h);
+    if (b->hdr_pool) cudaFreeHost(b->hdr_pool);
     if (b->st) cudaStreamDestroy(b->st);
     if (b->own_arena) jxs_arena_destroy(b->arena);
     delete b;
@@ -1084,11 +1152,7 @@ extern "C" int32_t jxs_gpu_batch_decode(jxs_gpu_batch_t* b, jxs_gpu_dec_t* const
             return er;
         }
         DecWork& w = b->dec[i];
-        if (!w.hdr_h && cudaMallocHost(&w.hdr_h, sizeof(c->hdr)) != cudaSuccess) {
-            cudaGetLastError();
-            w.hdr_h = nullptr;
-            return JXS_E_RESOURCES;
-        }
+        w.hdr_h = b->hdr_pool + (size_t)i * sizeof(c->hdr);
         DecItem& d = items[i];
         d.c = c;
         d.dcfg = dcfg;
