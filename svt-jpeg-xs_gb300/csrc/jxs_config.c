@@ -68,7 +68,7 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
                     b->sig_w = bd->sig_w;
                     b->w = bd->w;
                     b->gbase = gsum;
-                    gsum += bd->gcli_w;
+                    gsum += (bd->gcli_w + 3) & ~3u; /* 4-aligned: 32-bit access to 4 groups */
                     b->seg0 = ns;
                     b->nseg = (bd->gcli_w + sg - 1) / sg;
                     if (b->nseg == 0) b->nseg = 1;

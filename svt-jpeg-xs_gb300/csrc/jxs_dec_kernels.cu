@@ -492,8 +492,12 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         return;
     }
 
-    /* pass 2: GCLIs from codeword ends; data bits per segment */
+    /* pass 2: GCLIs from codeword ends; data bits per segment.  Each lane
+     * takes 4 consecutive groups: they share one significance flag, so
+     * either all of them carry a codeword or none (only the segment's last
+     * lane may hold fewer than 4 groups, and no lane after it holds any). */
     int bad = 0;
+    const uint32_t lt_mask = (1u << lane) - 1u;
     for (uint32_t sidx = next_seg(&s_next[0], lane); sidx < nseg; sidx = next_seg(&s_next[0], lane)) {
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
@@ -501,36 +505,55 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         const UkPk P = pk[L.pk];
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
         uint32_t cw = s_base[sidx], dsum = 0;
-        for (uint32_t base = sg.g0; base < gend; base += 32) {
-            const uint32_t g = base + lane;
-            const bool valid = g < gend;
-            uint32_t v = 0;
+        for (uint32_t base = sg.g0; base < gend; base += 128) {
+            const uint32_t g0 = base + 4 * lane;
+            const uint32_t nv = g0 < gend ? min(4u, gend - g0) : 0u;
+            uint32_t v4 = 0;
             bool coded = false;
-            if (valid) {
+            if (nv) {
                 if (L.raw) {
-                    const uint32_t pos = L.sig_pos + 4 * g;
-                    v = (pbuf[pos >> 3] >> (4 - (pos & 7))) & 15u;
+                    /* 4 raw 4-bit GCLIs, group g0 in the top nibble */
+                    const uint32_t w = bits32_at(pbuf, L.sig_pos + 4 * g0);
+                    v4 = __byte_perm(((w >> 28) & 15u) | (((w >> 24) & 15u) << 8), ((w >> 20) & 15u) | (((w >> 16) & 15u) << 8),
+                                     0x5410);
                 } else {
-                    const uint32_t sp = L.sig_pos + (g >> 3);
+                    const uint32_t sp = L.sig_pos + (g0 >> 3);
                     coded = !(L.meth && ((pbuf[sp >> 3] >> (7 - (sp & 7))) & 1));
-                    if (!coded) v = L.t;
+                    if (!coded) v4 = L.t * 0x01010101u;
                 }
             }
             const uint32_t bal = __ballot_sync(FULL, coded);
             if (coded) {
-                const uint32_t c = cw + __popc(bal & ((1u << lane) - 1));
+                /* codeword c + q ends at the (c + q)-th zero bit */
+                const uint32_t c = cw + 4 * __popc(bal & lt_mask);
                 const uint32_t zr = P.zbase + c;
-                const uint32_t start = c ? zend[zr - 1] + 1u : 0u;
-                const uint32_t ones = zend[zr] - start;
-                v = L.t + ones;
-                if (v > 15) {
-                    bad = 1;
-                    v = 15;
+                int prev = c ? (int)zend[zr - 1] : -1;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if (q < (int)nv) {
+                        const int e = (int)zend[zr + q];
+                        uint32_t v = L.t + (uint32_t)(e - prev - 1);
+                        if (v > 15) {
+                            bad = 1;
+                            v = 15;
+                        }
+                        v4 |= v << (8 * q);
+                        prev = e;
+                    }
                 }
             }
-            if (valid) gcl[B.gbase + g] = (uint8_t)v;
-            cw += __popc(bal);
-            if (valid && v > L.t) dsum += 4 * (v - L.t + 1);
+            uint8_t* gdst = gcl + B.gbase + g0;
+            if (nv == 4) {
+                *(uint32_t*)gdst = v4;
+            } else {
+                for (uint32_t q = 0; q < nv; q++) gdst[q] = (uint8_t)(v4 >> (8 * q));
+            }
+            cw += __reduce_add_sync(FULL, coded ? nv : 0u);
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t v = (v4 >> (8 * q)) & 255u;
+                if (q < (int)nv && v > L.t) dsum += 4 * (v - L.t + 1);
+            }
         }
         dsum = __reduce_add_sync(FULL, dsum);
         if (lane == 0) s_cnt[sidx] = dsum;
@@ -558,7 +581,8 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         return;
     }
 
-    /* pass 3: data */
+    /* pass 3: data, 4 consecutive groups per lane: one warp scan of their
+     * bit lengths, two 16-byte stores of their 16 coefficients */
     const uint32_t uniform = cfg->qpih;
     for (uint32_t sidx = next_seg(&s_next[1], lane); sidx < nseg; sidx = next_seg(&s_next[1], lane)) {
         const jxs_seg_t sg = segs[sidx];
@@ -567,22 +591,48 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         const UkPk P = pk[L.pk];
         int16_t* crow = coef + s_crow[sg.bl];
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+        const uint32_t t = L.t;
         uint32_t dpos = P.dpos + s_base[sidx];
-        for (uint32_t base = sg.g0; base < gend; base += 32) {
-            const uint32_t g = base + lane;
-            const bool valid = g < gend;
-            const uint32_t v = valid ? gcl[B.gbase + g] : 0u;
-            const uint32_t np = v > L.t ? v - L.t : 0u;
-            const uint32_t len = np ? 4 * (np + 1) : 0u;
-            uint32_t tot;
-            const uint32_t ex = warp_excl_scan(len, &tot);
-            uint2 o = make_uint2(0u, 0u);
-            if (len) {
-                const uint32_t pos = dpos + ex;
-                const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
-                o = decode_group(win >> (64 - len), np, L.t, v, uniform, (int)B.w - 4 * (int)g);
+        for (uint32_t base = sg.g0; base < gend; base += 128) {
+            const uint32_t g0 = base + 4 * lane;
+            const uint32_t nv = g0 < gend ? min(4u, gend - g0) : 0u;
+            const uint8_t* gsrc = gcl + B.gbase + g0;
+            uint32_t v4 = 0;
+            if (nv == 4) {
+                v4 = *(const uint32_t*)gsrc;
+            } else {
+                for (uint32_t q = 0; q < nv; q++) v4 |= (uint32_t)gsrc[q] << (8 * q);
             }
-            if (valid) *(uint2*)(crow + 4 * g) = o;
+            uint32_t len[4], sum = 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t v = (v4 >> (8 * q)) & 255u;
+                len[q] = v > t ? 4 * (v - t + 1) : 0u;
+                sum += len[q];
+            }
+            uint32_t tot;
+            const uint32_t ex = warp_excl_scan(sum, &tot);
+            uint32_t pos = dpos + ex;
+            uint2 o[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                o[q] = make_uint2(0u, 0u);
+                if (len[q]) {
+                    const uint32_t v = (v4 >> (8 * q)) & 255u;
+                    const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
+                    o[q] = decode_group(win >> (64 - len[q]), v - t, t, v, uniform, (int)B.w - 4 * (int)(g0 + q));
+                }
+                pos += len[q];
+            }
+            int16_t* cdst = crow + 4 * g0;
+            if (nv == 4) {
+                *(uint4*)cdst = make_uint4(o[0].x, o[0].y, o[1].x, o[1].y);
+                *(uint4*)(cdst + 8) = make_uint4(o[2].x, o[2].y, o[3].x, o[3].y);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    if (q < (int)nv) *(uint2*)(cdst + 4 * q) = o[q];
+            }
             dpos += tot;
         }
     }

@@ -545,7 +545,8 @@ extern "C" jxs_gpu_dec_t* jxs_gpu_dec_create(const jxs_cfg_t* cfg, int nslots, i
     d->serial = g_serial++;
     uint32_t groups = 0;
     for (uint32_t b = 0; b < cfg->nbands; b++) groups += cfg->band[b].gcli_w * cfg->band[b].lines;
-    d->cap_groups = (groups + 64) & ~31u;
+    /* + up to 3 groups of alignment per band line (jxs_bline_t.gbase) */
+    d->cap_groups = (groups + 3 * JXS_MAXBLINES + 64) & ~31u;
     /* the on-chip copy of a precinct: constant-bit-rate streams give every
      * slice its share of Lcod, so a precinct fits in a slice's share with
      * margin; whatever does not fit is reported as an invalid stream */
