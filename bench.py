@@ -343,15 +343,28 @@ def run_ours(args, rank, world, local):
     def planes_of(ts):
         return [(t.data_ptr(), t.shape[1]) for t in ts]
 
+    # frame structures built once and sent repeatedly, as a C caller would
+    enc_frames, dec_frames = {}, {}
+
+    def enc_frame(j, i):
+        if (j, i) not in enc_frames:
+            enc_frames[(j, i)] = encs[0].make_frame(planes_of(d_in[j]), d_bs[i].data_ptr(), out_cap=lcod + 64)
+        return enc_frames[(j, i)]
+
+    def dec_frame(i):
+        if i not in dec_frames:
+            dec_frames[i] = decs[0].make_frame(d_bs[i].data_ptr(), planes_of(d_out[i]), bs_size=lcod)
+        return dec_frames[i]
+
     def step(s, npairs):
         # every call is queued on its pair's stream: decode i follows encode
         # i, and results are collected only when a codec's queue is full
         base = (s * F) % nseq
         pend = {}
 
-        def submit(codec, *a, **kw):
+        def submit(codec, frame):
             while True:
-                r = codec.send(*a, blocking=False, **kw)
+                r = codec.send_frame(frame, blocking=False)
                 if r != jxs.E_EMPTY_QUEUE:
                     assert r == 0, hex(r)
                     pend[id(codec)] = pend.get(id(codec), 0) + 1
@@ -362,8 +375,8 @@ def run_ours(args, rank, world, local):
 
         for i in range(F):
             k = i % npairs
-            submit(encs[k], planes_of(d_in[(base + i) % nseq]), d_bs[i].data_ptr(), out_cap=lcod + 64)
-            submit(decs[k], d_bs[i].data_ptr(), planes_of(d_out[i]), bs_size=lcod)
+            submit(encs[k], enc_frame((base + i) % nseq, i))
+            submit(decs[k], dec_frame(i))
         for codec in encs[:npairs] + decs[:npairs]:
             while pend.get(id(codec), 0):
                 r, _ = codec.get()
@@ -468,6 +481,8 @@ def run_ours(args, rank, world, local):
     for k in range(NS):
         encs[k].set_stream(None)
         decs[k].set_stream(None)
+    h_enc_frames = [enc.make_frame(h_in[i], h_bs[i]) for i in range(F)]
+    h_dec_frames = [dec.make_frame(h_bs[i], h_out[i], bs_size=lcod) for i in range(F)]
 
     def e2e_step():
         # frame i on pair i % NS: encode from host planes, the codestream back
@@ -482,7 +497,7 @@ def run_ours(args, rank, world, local):
             for k in range(NS):
                 while nxt_enc[k] < F:
                     i = nxt_enc[k]
-                    if encs[k].send(h_in[i], h_bs[i], blocking=False) == jxs.E_EMPTY_QUEUE:
+                    if encs[k].send_frame(h_enc_frames[i], blocking=False) == jxs.E_EMPTY_QUEUE:
                         break
                     enc_q[k].append(i)
                     nxt_enc[k] += NS
@@ -494,7 +509,7 @@ def run_ours(args, rank, world, local):
                     ready[k].append(enc_q[k].pop(0))
                 while ready[k]:
                     i = ready[k][0]
-                    if decs[k].send(h_bs[i], h_out[i], bs_size=lcod, blocking=False) == jxs.E_EMPTY_QUEUE:
+                    if decs[k].send_frame(h_dec_frames[i], blocking=False) == jxs.E_EMPTY_QUEUE:
                         break
                     dec_q[k].append(ready[k].pop(0))
                 while dec_q[k]:

@@ -581,8 +581,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         return;
     }
 
-    /* pass 3: data, 4 consecutive groups per lane: one warp scan of their
-     * bit lengths, two 16-byte stores of their 16 coefficients */
+    /* pass 3: data */
     const uint32_t uniform = cfg->qpih;
     for (uint32_t sidx = next_seg(&s_next[1], lane); sidx < nseg; sidx = next_seg(&s_next[1], lane)) {
         const jxs_seg_t sg = segs[sidx];
@@ -591,48 +590,22 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         const UkPk P = pk[L.pk];
         int16_t* crow = coef + s_crow[sg.bl];
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
-        const uint32_t t = L.t;
         uint32_t dpos = P.dpos + s_base[sidx];
-        for (uint32_t base = sg.g0; base < gend; base += 128) {
-            const uint32_t g0 = base + 4 * lane;
-            const uint32_t nv = g0 < gend ? min(4u, gend - g0) : 0u;
-            const uint8_t* gsrc = gcl + B.gbase + g0;
-            uint32_t v4 = 0;
-            if (nv == 4) {
-                v4 = *(const uint32_t*)gsrc;
-            } else {
-                for (uint32_t q = 0; q < nv; q++) v4 |= (uint32_t)gsrc[q] << (8 * q);
-            }
-            uint32_t len[4], sum = 0;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const uint32_t v = (v4 >> (8 * q)) & 255u;
-                len[q] = v > t ? 4 * (v - t + 1) : 0u;
-                sum += len[q];
-            }
+        for (uint32_t base = sg.g0; base < gend; base += 32) {
+            const uint32_t g = base + lane;
+            const bool valid = g < gend;
+            const uint32_t v = valid ? gcl[B.gbase + g] : 0u;
+            const uint32_t np = v > L.t ? v - L.t : 0u;
+            const uint32_t len = np ? 4 * (np + 1) : 0u;
             uint32_t tot;
-            const uint32_t ex = warp_excl_scan(sum, &tot);
-            uint32_t pos = dpos + ex;
-            uint2 o[4];
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                o[q] = make_uint2(0u, 0u);
-                if (len[q]) {
-                    const uint32_t v = (v4 >> (8 * q)) & 255u;
-                    const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
-                    o[q] = decode_group(win >> (64 - len[q]), v - t, t, v, uniform, (int)B.w - 4 * (int)(g0 + q));
-                }
-                pos += len[q];
+            const uint32_t ex = warp_excl_scan(len, &tot);
+            uint2 o = make_uint2(0u, 0u);
+            if (len) {
+                const uint32_t pos = dpos + ex;
+                const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
+                o = decode_group(win >> (64 - len), np, L.t, v, uniform, (int)B.w - 4 * (int)g);
             }
-            int16_t* cdst = crow + 4 * g0;
-            if (nv == 4) {
-                *(uint4*)cdst = make_uint4(o[0].x, o[0].y, o[1].x, o[1].y);
-                *(uint4*)(cdst + 8) = make_uint4(o[2].x, o[2].y, o[3].x, o[3].y);
-            } else {
-#pragma unroll
-                for (int q = 0; q < 4; q++)
-                    if (q < (int)nv) *(uint2*)(cdst + 4 * q) = o[q];
-            }
+            if (valid) *(uint2*)(crow + 4 * g) = o;
             dpos += tot;
         }
     }
@@ -781,7 +754,8 @@ extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* b
                                          int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status,
                                          cudaStream_t st) {
     const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 2ull * UK_ZCAP(cap_groups);
-    cudaError_t e = cudaFuncSetAttribute(unpack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static std::atomic<int> attr[JXS_MAX_DEV];
+    cudaError_t e = jxs_smem_attr(unpack_kernel, (int)smem, attr);
     if (e != cudaSuccess) return e;
     unpack_kernel<<<np, UK_THREADS, smem, st>>>(dcfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status);
     return cudaGetLastError();
@@ -797,7 +771,8 @@ extern "C" cudaError_t jxs_launch_walk_batch(const DecPrecLaunch* L, cudaStream_
 
 extern "C" cudaError_t jxs_launch_unpack_batch(const DecPrecLaunch* L, uint32_t cap_bytes, uint32_t cap_groups, cudaStream_t st) {
     const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 2ull * UK_ZCAP(cap_groups);
-    cudaError_t e = cudaFuncSetAttribute(unpack_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static std::atomic<int> attr[JXS_MAX_DEV];
+    cudaError_t e = jxs_smem_attr(unpack_batch_kernel, (int)smem, attr);
     if (e != cudaSuccess) return e;
     if (L->nblocks <= 0) return cudaSuccess;
     unpack_batch_kernel<<<L->nblocks, UK_THREADS, smem, st>>>(*L, cap_bytes, cap_groups);

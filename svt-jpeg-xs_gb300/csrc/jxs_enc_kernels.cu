@@ -933,7 +933,8 @@ extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
                                        const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st) {
     const size_t smem = (size_t)cap_words * 4;
-    cudaError_t e = cudaFuncSetAttribute(pack_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static std::atomic<int> attr[JXS_MAX_DEV];
+    cudaError_t e = jxs_smem_attr(pack_kernel, (int)smem, attr);
     if (e != cudaSuccess) return e;
     pack_kernel<<<np, PK_THREADS, smem, st>>>(dcfg, coef, gcli, rc, out, cap_words, status);
     return cudaGetLastError();
@@ -947,7 +948,8 @@ extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, cudaStream_t 
 
 extern "C" cudaError_t jxs_launch_pack_batch(const EncPrecLaunch* L, uint32_t cap_words, cudaStream_t st) {
     const size_t smem = (size_t)cap_words * 4;
-    cudaError_t e = cudaFuncSetAttribute(pack_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static std::atomic<int> attr[JXS_MAX_DEV];
+    cudaError_t e = jxs_smem_attr(pack_batch_kernel, (int)smem, attr);
     if (e != cudaSuccess) return e;
     if (L->nblocks <= 0) return cudaSuccess;
     pack_batch_kernel<<<L->nblocks, PK_THREADS, smem, st>>>(*L, cap_words);

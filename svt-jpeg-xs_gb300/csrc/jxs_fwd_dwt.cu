@@ -420,15 +420,29 @@ static cudaError_t launch_v(const FwdVLaunchN<NJ>* L, int grid_per_sm, cudaStrea
      * grid_per_sm blocks per SM (0: as many as fit) */
     const bool persistent = SRC != SRC_I32;
     const size_t smem = (persistent ? 2 : 1) * FV_NR * FV_THREADS * sizeof(typename FvIn<SRC>::T);
-    cudaError_t e = cudaFuncSetAttribute(fwd_v_kernel<SRC, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static std::atomic<int> attr[JXS_MAX_DEV];
+    cudaError_t e = jxs_smem_attr(fwd_v_kernel<SRC, NJ>, (int)smem, attr);
     if (e != cudaSuccess) return e;
     int blocks = L->ntiles;
     if (persistent) {
+        /* SMs and resident blocks per SM, queried once per device */
+        static std::atomic<int> q_sms[JXS_MAX_DEV], q_per_sm[JXS_MAX_DEV];
         int dev = 0, sms = 0, per_sm = 0;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd_v_kernel<SRC, NJ>, FV_THREADS, smem)) != cudaSuccess)
-            return e;
+        const bool cached = dev >= 0 && dev < JXS_MAX_DEV && q_sms[dev].load() > 0;
+        if (cached) {
+            sms = q_sms[dev].load();
+            per_sm = q_per_sm[dev].load();
+        } else {
+            if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd_v_kernel<SRC, NJ>, FV_THREADS, smem)) !=
+                cudaSuccess)
+                return e;
+            if (dev >= 0 && dev < JXS_MAX_DEV) {
+                q_per_sm[dev].store(per_sm);
+                q_sms[dev].store(sms);
+            }
+        }
         if (per_sm < 1) per_sm = 1;
         if (grid_per_sm > 0 && grid_per_sm < per_sm) per_sm = grid_per_sm;
         blocks = sms * per_sm;
@@ -460,7 +474,8 @@ extern "C" cudaError_t jxs_launch_fwd_v_batch(const FwdVLaunchB* L, int src_kind
 template <int SRC, int NJ>
 static cudaError_t launch_h(const FwdHLaunchN<NJ>* L, int nblocks, cudaStream_t st) {
     const size_t smem = (size_t)L->warp_words * L->rows_per_block * sizeof(int32_t);
-    cudaError_t e = cudaFuncSetAttribute(fwd_h_kernel<SRC, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static std::atomic<int> attr[JXS_MAX_DEV];
+    cudaError_t e = jxs_smem_attr(fwd_h_kernel<SRC, NJ>, (int)smem, attr);
     if (e != cudaSuccess) return e;
     if (nblocks <= 0) return cudaSuccess;
     fwd_h_kernel<SRC, NJ><<<nblocks, L->rows_per_block * 32, smem, st>>>(*L);

@@ -366,7 +366,8 @@ extern "C" cudaError_t jxs_launch_inv_v_batch(const InvVLaunchB* L, int out_kind
 template <int OUT, int NJ>
 static cudaError_t launch_ih(const InvHLaunchN<NJ>* L, int nblocks, cudaStream_t st) {
     const size_t smem = (size_t)L->warp_words * L->rows_per_block * sizeof(int32_t);
-    cudaError_t e = cudaFuncSetAttribute(inv_h_kernel<OUT, NJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static std::atomic<int> attr[JXS_MAX_DEV];
+    cudaError_t e = jxs_smem_attr(inv_h_kernel<OUT, NJ>, (int)smem, attr);
     if (e != cudaSuccess) return e;
     if (nblocks <= 0) return cudaSuccess;
     inv_h_kernel<OUT, NJ><<<nblocks, L->rows_per_block * 32, smem, st>>>(*L);

@@ -8,6 +8,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "jxs_core.h"
 
 /* Source sample formats of the first transform level. */
@@ -203,6 +205,25 @@ struct DecPrecLaunch {
     int nblocks, nslices;
     DecPrecFrame job[JXS_BATCH_FRAMES];
 };
+
+/* Launch-time queries cached per device: a kernel's dynamic shared-memory
+ * limit is raised only when a launch needs more than was set before, so the
+ * steady state costs no driver call. */
+#define JXS_MAX_DEV 16
+template <class K>
+static inline cudaError_t jxs_smem_attr(K kern, int bytes, std::atomic<int>* cache) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < JXS_MAX_DEV && cache[dev].load(std::memory_order_relaxed) >= bytes) return cudaSuccess;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess && dev >= 0 && dev < JXS_MAX_DEV) {
+        int cur = cache[dev].load(std::memory_order_relaxed);
+        while (cur < bytes && !cache[dev].compare_exchange_weak(cur, bytes)) {
+        }
+    }
+    return e;
+}
 
 #define JXS_STATUS_SET(ptr, code) atomicCAS((int*)(ptr), 0, (int)(code))
 

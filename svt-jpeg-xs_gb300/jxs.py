@@ -326,6 +326,13 @@ class Encoder:
         f = self._frame(planes, out, out_cap, user)
         return lib().svt_jpeg_xs_encoder_send_picture(ctypes.byref(self.api), ctypes.byref(f), 1 if blocking else 0)
 
+    def make_frame(self, planes, out, out_cap=None):
+        """A frame structure to send repeatedly (the API copies it per call)."""
+        return self._frame(planes, out, out_cap)
+
+    def send_frame(self, frame, blocking=True):
+        return lib().svt_jpeg_xs_encoder_send_picture(ctypes.byref(self.api), ctypes.byref(frame), 1 if blocking else 0)
+
     def get(self, blocking=True):
         f = Frame()
         r = lib().svt_jpeg_xs_encoder_get_packet(ctypes.byref(self.api), ctypes.byref(f), 1 if blocking else 0)
@@ -425,6 +432,13 @@ class Decoder:
     def send(self, bs, planes, bs_size=None, blocking=True, user=None):
         f = self._frame(bs, planes, bs_size, user)
         return lib().svt_jpeg_xs_decoder_send_frame(ctypes.byref(self.api), ctypes.byref(f), 1 if blocking else 0)
+
+    def make_frame(self, bs, planes, bs_size=None):
+        """A frame structure to send repeatedly (the API copies it per call)."""
+        return self._frame(bs, planes, bs_size)
+
+    def send_frame(self, frame, blocking=True):
+        return lib().svt_jpeg_xs_decoder_send_frame(ctypes.byref(self.api), ctypes.byref(frame), 1 if blocking else 0)
 
     def get(self, blocking=True):
         f = Frame()
