@@ -466,41 +466,48 @@ def run_ours(args, rank, world, local):
     batched_value = args.steps * F * world * W * H / (bat["dev_ms"] / 1e3) / 1e9
 
     # ---- e2e through the C API with host buffers: every pair on its own slot
-    # streams (3 frames in flight per codec); the latency probe uses pair 0
+    # streams (3 frames in flight per codec), one continuous pipeline over
+    # the timed frames; the latency probe uses pair 0
     enc, dec = encs[0], decs[0]
     def pinned_like(a):
         buf = torch.empty(a.shape, dtype=torch.from_numpy(a[:1]).dtype).pin_memory()
         buf.copy_(torch.from_numpy(a))
         return buf.numpy()
 
-    h_in = [[pinned_like(p) for p in frames[i % nseq]] for i in range(F)]
-    h_bs = [torch.empty(lcod + 64, dtype=torch.uint8).pin_memory().numpy() for _ in range(F)]
+    # a ring of R page-locked buffer sets: frame n uses set n % R
+    R = 2 * F
+    h_in = [[pinned_like(p) for p in frames[i % nseq]] for i in range(R)]
+    h_bs = [torch.empty(lcod + 64, dtype=torch.uint8).pin_memory().numpy() for _ in range(R)]
     h_out = [[torch.empty(p.shape, dtype=torch.from_numpy(p[:1]).dtype).pin_memory().numpy() for p in frames[0]]
-             for _ in range(F)]
+             for _ in range(R)]
 
     for k in range(NS):
         encs[k].set_stream(None)
         decs[k].set_stream(None)
-    h_enc_frames = [enc.make_frame(h_in[i], h_bs[i]) for i in range(F)]
-    h_dec_frames = [dec.make_frame(h_bs[i], h_out[i], bs_size=lcod) for i in range(F)]
+    h_enc_frames = [enc.make_frame(h_in[i], h_bs[i]) for i in range(R)]
+    h_dec_frames = [dec.make_frame(h_bs[i], h_out[i], bs_size=lcod) for i in range(R)]
 
-    def e2e_step():
-        # frame i on pair i % NS: encode from host planes, the codestream back
-        # to the host, decode from it into host planes; every codec keeps its
-        # queue full and results are polled without blocking
-        nxt_enc = list(range(NS))            # next frame to encode per pair
+    def e2e_run(nframes):
+        """Frames 0..nframes-1 as one continuous pipeline: frame n on pair
+        n % NS and buffer set n % R, encoded from host planes, its codestream
+        back to the host, decoded from there into host planes.  A set is
+        reused once the frame before it is decoded; every codec keeps its
+        queue full and results are polled without blocking.  Returns the
+        times at which every F-th frame completed."""
+        done = [False] * nframes
+        nxt, ndone = 0, 0
         enc_q = [[] for _ in range(NS)]      # frames in each encoder, in order
         ready = [[] for _ in range(NS)]      # encoded frames waiting for the decoder
         dec_q = [[] for _ in range(NS)]
-        done = 0
-        while done < F:
+        marks = []
+        while ndone < nframes:
+            while nxt < nframes and (nxt < R or done[nxt - R]):
+                k = nxt % NS
+                if encs[k].send_frame(h_enc_frames[nxt % R], blocking=False) == jxs.E_EMPTY_QUEUE:
+                    break
+                enc_q[k].append(nxt)
+                nxt += 1
             for k in range(NS):
-                while nxt_enc[k] < F:
-                    i = nxt_enc[k]
-                    if encs[k].send_frame(h_enc_frames[i], blocking=False) == jxs.E_EMPTY_QUEUE:
-                        break
-                    enc_q[k].append(i)
-                    nxt_enc[k] += NS
                 while enc_q[k]:
                     r, _ = encs[k].get(blocking=False)
                     if r == jxs.E_EMPTY_QUEUE:
@@ -508,8 +515,8 @@ def run_ours(args, rank, world, local):
                     assert r == 0, hex(r)
                     ready[k].append(enc_q[k].pop(0))
                 while ready[k]:
-                    i = ready[k][0]
-                    if decs[k].send_frame(h_dec_frames[i], blocking=False) == jxs.E_EMPTY_QUEUE:
+                    n = ready[k][0]
+                    if decs[k].send_frame(h_dec_frames[n % R], blocking=False) == jxs.E_EMPTY_QUEUE:
                         break
                     dec_q[k].append(ready[k].pop(0))
                 while dec_q[k]:
@@ -517,20 +524,19 @@ def run_ours(args, rank, world, local):
                     if r == jxs.E_EMPTY_QUEUE:
                         break
                     assert r == 0, hex(r)
-                    dec_q[k].pop(0)
-                    done += 1
+                    done[dec_q[k].pop(0)] = True
+                    ndone += 1
+                    if ndone % F == 0:
+                        marks.append(time.perf_counter())
+        return marks
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
+    e2e_run(max(1, args.warmup) * F)
     torch.cuda.synchronize()
-    lat = []
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        ts = time.perf_counter()
-        e2e_step()
-        lat.append(time.perf_counter() - ts)
+    marks = e2e_run(args.steps * F)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    lat = list(np.diff([t0] + marks))
     e2e_val = args.steps * F * world * W * H / e2e_s / 1e9
     in_bytes = sum(p.nbytes for p in frames[0])
     out_bytes = in_bytes
