@@ -202,32 +202,44 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     __shared__ uint32_t ws[UK_WARPS];
     __shared__ int s_err;
     __shared__ uint32_t s_total, s_lead, s_tw, s_npk;
+    __shared__ uint8_t s_g2f[JXS_MAXBL];          /* global band -> flat band */
+    __shared__ uint16_t s_lgp[JXS_MAXBLINES];      /* per line: band gain | priority << 8 */
+    __shared__ uint32_t s_sc[8];                   /* nbands_all, npk, long headers, separate signs, precinct header bytes,
+                                                      band lines, segments, groups per segment */
 
     const int last = (p + 1 >= (int)cfg->np);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x == 0) s_err = *(volatile int*)status;
-    if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
-    __syncthreads();
-    if (s_err) return; /* the precinct offsets could not be found */
-    const uint32_t off = prec_off[p];
+    /* thread 0: the frame's status and the precinct's length field; every
+     * thread meanwhile stages this precinct kind's tables and the scalars
+     * the parse needs, so that no single-warp phase waits on device memory */
     if (threadIdx.x == 0) {
-        s_err = 0;
-        if ((uint64_t)off + cfg->prec_hdr_bytes > bs_size) {
-            s_err = JXS_E_DEC_SHORT;
+        int err = *(volatile int*)status; /* set: the precinct offsets could not be found */
+        s_sc[0] = cfg->nbands_all;
+        s_sc[1] = cfg->npk;
+        s_sc[2] = cfg->lh || !cfg->short_hdr;
+        s_sc[3] = cfg->fs;
+        s_sc[4] = cfg->prec_hdr_bytes;
+        s_sc[5] = cfg->nbline[last];
+        s_sc[6] = cfg->nseg[last];
+        s_sc[7] = cfg->seg_groups;
+        if (!err) {
+            const uint32_t off = prec_off[p], phb = cfg->prec_hdr_bytes;
+            if ((uint64_t)off + phb > bs_size) {
+                err = JXS_E_DEC_SHORT;
+            } else {
+                const uint32_t lprc = ((uint32_t)bs[off] << 16) | ((uint32_t)bs[off + 1] << 8) | bs[off + 2];
+                s_total = phb + lprc;
+                s_lead = (uint32_t)((uintptr_t)(bs + off) & 15);
+                if (lprc > JXS_PREC_MAX_BYTES || s_total + 48 > cap_bytes) err = JXS_E_DEC_BITSTREAM;
+                else if ((uint64_t)off + s_total > bs_size) err = JXS_E_DEC_SHORT;
+            }
+            if (err) JXS_STATUS_SET(status, err);
         } else {
-            const uint32_t lprc = ((uint32_t)bs[off] << 16) | ((uint32_t)bs[off + 1] << 8) | bs[off + 2];
-            s_total = cfg->prec_hdr_bytes + lprc;
-            s_lead = (uint32_t)((uintptr_t)(bs + off) & 15);
-            if (lprc > JXS_PREC_MAX_BYTES || s_total + 48 > cap_bytes) s_err = JXS_E_DEC_BITSTREAM;
-            else if ((uint64_t)off + s_total > bs_size) s_err = JXS_E_DEC_SHORT;
+            err = -1; /* already reported */
         }
+        s_err = err;
     }
-    __syncthreads();
-    if (s_err) {
-        if (threadIdx.x == 0) JXS_STATUS_SET(status, s_err);
-        return;
-    }
-    const uint32_t total = s_total, lead = s_lead;
+    if (threadIdx.x < 2) s_next[threadIdx.x] = 0;
     {
         const uint32_t ns = cfg->nseg[last], nl = cfg->nbline[last];
         for (uint32_t i = threadIdx.x; i < ns * (sizeof(jxs_seg_t) / 4); i += blockDim.x)
@@ -238,12 +250,18 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             const jxs_bline_t& B = cfg->bline[last][x];
             const jxs_band_t& bd = cfg->band[B.fb];
             s_crow[x] = bd.coef_off + (uint64_t)(p * bd.lines + B.line) * bd.pitch;
+            s_lgp[x] = (uint16_t)(bd.gain | (bd.prio << 8));
         }
         for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) {
             s_pkbl0[k] = cfg->pk_bl0[last][k];
             s_pknbl[k] = cfg->pk_nbl[last][k];
         }
+        for (uint32_t gb = threadIdx.x; gb < cfg->nbands_all; gb += blockDim.x) s_g2f[gb] = cfg->g2f[gb];
     }
+    __syncthreads();
+    if (s_err) return;
+    const uint32_t off = prec_off[p];
+    const uint32_t total = s_total, lead = s_lead;
     {
         /* aligned 16-byte chunks inside the precinct, single bytes at its
          * ends; 32 zero bytes after it for the bit readers */
@@ -260,7 +278,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     }
     __syncthreads();
 
-    const uint32_t nbl = cfg->nbline[last], nseg = cfg->nseg[last], SG = cfg->seg_groups;
+    const uint32_t nbl = s_sc[5], nseg = s_sc[6], SG = s_sc[7];
     const jxs_bline_t* bls = s_bl;
     const jxs_seg_t* segs = s_seg;
     /* parse, by warp 0: band modes and per-line fields in parallel, the
@@ -271,9 +289,10 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         int err = 0;
         /* band coding modes D[p,b], 2 bits per existing band */
         uint32_t idx0 = 0;
-        for (uint32_t gb0 = 0; gb0 < cfg->nbands_all; gb0 += 32) {
+        const uint32_t nbands_all = s_sc[0], npk_c = s_sc[1];
+        for (uint32_t gb0 = 0; gb0 < nbands_all; gb0 += 32) {
             const uint32_t gb = gb0 + lane;
-            const int fb = gb < cfg->nbands_all ? cfg->g2f[gb] : JXS_NOBAND;
+            const int fb = gb < nbands_all ? s_g2f[gb] : JXS_NOBAND;
             const bool ex = fb != JXS_NOBAND;
             const uint32_t bal = __ballot_sync(FULL, ex);
             if (ex) {
@@ -285,15 +304,14 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         }
         __syncwarp();
         for (uint32_t x = lane; x < nbl; x += 32) {
-            const jxs_band_t& bd = cfg->band[bls[x].fb];
-            ln[x].t = jxs_truncation(bd.gain, bd.prio, q, r);
+            ln[x].t = jxs_truncation((uint8_t)(s_lgp[x] & 255u), (uint8_t)(s_lgp[x] >> 8), q, r);
             ln[x].meth = (s_mode[bls[x].fb] & 2) ? 1 : 0;
             ln[x].pk = bls[x].pk;
         }
         __syncwarp();
         /* per packet: significance bits and raw GCLI bits it must hold */
         uint32_t sb = 0, rb = 0;
-        if (lane < (int)cfg->npk) {
+        if (lane < (int)npk_c) {
             const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
             for (uint32_t x = b0; x < b0 + nb; x++) {
                 if (ln[x].meth) sb += bls[x].sig_w;
@@ -304,12 +322,12 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         }
         __syncwarp();
         if (lane == 0) {
-            const uint32_t lprc = total - cfg->prec_hdr_bytes;
-            const int long_hdr = cfg->lh || !cfg->short_hdr;
+            const uint32_t lprc = total - s_sc[4];
+            const int long_hdr = (int)s_sc[2];
             int64_t left = (int64_t)lprc * 8;
-            uint32_t bpos = lead + cfg->prec_hdr_bytes; /* bytes */
+            uint32_t bpos = lead + s_sc[4]; /* bytes */
             uint32_t tw = 0;
-            for (uint32_t k = 0; k < cfg->npk; k++) {
+            for (uint32_t k = 0; k < npk_c; k++) {
                 UkPk& P = pk[k];
                 P.present = 0;
                 P.gbits = P.dbits = P.nwords = P.ncoded = P.nzero = 0;
@@ -355,7 +373,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                 P.dbits = dlen * 8;
                 bpos += dlen;
                 left -= (int64_t)dlen * 8;
-                if (cfg->fs) err = JXS_E_DEC_BITSTREAM; /* separate sign sub-packets are not part of this decoder */
+                if (s_sc[3]) err = JXS_E_DEC_BITSTREAM; /* separate sign sub-packets are not part of this decoder */
                 bpos += slen;
                 if (left < 0 || bpos > lead + total) { err = JXS_E_DEC_BITSTREAM; break; }
                 P.present = 1;
@@ -365,12 +383,12 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                 }
             }
             s_tw = tw;
-            s_npk = cfg->npk;
+            s_npk = npk_c;
         }
         err = __reduce_or_sync(FULL, (uint32_t)err) ? JXS_E_DEC_BITSTREAM : 0;
         __syncwarp();
         /* line positions: significance flags, or raw GCLIs for raw packets */
-        if (!err && lane < (int)cfg->npk && pk[lane].present) {
+        if (!err && lane < (int)npk_c && pk[lane].present) {
             const UkPk& P = pk[lane];
             const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
             uint32_t run = P.spos;
@@ -406,7 +424,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             }
             __syncwarp();
             /* codeword base of every segment inside its packet: one lane per packet */
-            if (lane < (int)cfg->npk) {
+            if (lane < (int)npk_c) {
                 const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
                 uint32_t run = 0;
                 for (uint32_t x = b0; x < b0 + nb; x++) {

@@ -533,6 +533,11 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
     __shared__ uint8_t s_lt[JXS_MAXBLINES];                            /* per line: gtli */
     __shared__ uint8_t s_pkbl0[JXS_MAXPK], s_pknbl[JXS_MAXPK];
     __shared__ uint32_t s_praw[JXS_MAXPK];
+    __shared__ uint8_t s_g2f[JXS_MAXBL];                               /* global band -> flat band */
+    __shared__ uint8_t s_blines[JXS_MAXBL];                            /* lines of each band in this precinct kind */
+    /* configuration scalars of the layout, loaded with the tables so that the
+     * single-warp layout waits on no device-memory read */
+    __shared__ uint32_t s_nbands, s_nbands_all, s_npk, s_sig, s_short, s_phb, s_hdrs, s_nbl;
     __shared__ int s_ok;
 
     const int last = (p + 1 >= (int)cfg->np);
@@ -577,8 +582,19 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             s_pknbl[k] = cfg->pk_nbl[last][k];
             s_praw[k] = cfg->raw_bytes[last][k];
         }
+        for (uint32_t gb = threadIdx.x; gb < cfg->nbands_all; gb += blockDim.x) s_g2f[gb] = cfg->g2f[gb];
+        for (uint32_t fb = threadIdx.x; fb < cfg->nbands; fb += blockDim.x)
+            s_blines[fb] = (uint8_t)(last ? cfg->band[fb].last_lines : cfg->band[fb].lines);
     }
     if (threadIdx.x == 0) {
+        s_nbands = cfg->nbands;
+        s_nbands_all = cfg->nbands_all;
+        s_npk = cfg->npk;
+        s_sig = cfg->sig;
+        s_short = cfg->short_hdr;
+        s_phb = cfg->prec_hdr_bytes;
+        s_hdrs = cfg->hdrs_bytes[last];
+        s_nbl = cfg->nbline[last];
     }
     __syncthreads();
 
@@ -626,7 +642,7 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
 
     /* layout, by warp 0: lanes over band lines, bands, packets, segments */
     if (warp == 0) {
-        const uint32_t nbl = cfg->nbline[last];
+        const uint32_t nbl = s_nbl;
         for (uint32_t b = lane; b < nbl; b += 32) {
             const jxs_bline_t& B = bls[b];
             uint32_t d = 0, v = 0, z = 0;
@@ -644,7 +660,7 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
         __syncwarp();
         /* coding method per band: significance only if strictly cheaper
          * (RateControl.c:528-575) */
-        for (uint32_t fb = lane; fb < cfg->nbands; fb += 32) s_meth[fb] = (uint8_t)(cfg->sig && s_cn[fb] > s_cs[fb]);
+        for (uint32_t fb = lane; fb < s_nbands; fb += 32) s_meth[fb] = (uint8_t)(s_sig && s_cn[fb] > s_cs[fb]);
         __syncwarp();
         /* per line: GCLI and significance bits with the band's method */
         for (uint32_t b = lane; b < nbl; b += 32) {
@@ -656,7 +672,7 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
         __syncwarp();
         /* one lane per packet: sub-packet sizes, raw fallback, header */
         const uint32_t k = lane;
-        const uint32_t nb = k < cfg->npk ? s_pknbl[k] : 0u, b0 = k < cfg->npk ? s_pkbl0[k] : 0u;
+        const uint32_t nb = k < s_npk ? s_pknbl[k] : 0u, b0 = k < s_npk ? s_pkbl0[k] : 0u;
         uint32_t db = 0, gbits = 0, sbits = 0;
         for (uint32_t x = b0; x < b0 + nb; x++) {
             db += pl[x].data;
@@ -667,16 +683,16 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
         const uint32_t rawB = nb ? s_praw[k] : 0u;
         const int raw = nb && sB + gB > rawB;
         const uint32_t gcl_bytes = raw ? rawB : gB;
-        const uint32_t hb = nb ? (cfg->short_hdr ? 5u : 7u) : 0u;
+        const uint32_t hb = nb ? (s_short ? 5u : 7u) : 0u;
         const uint32_t pk_bytes = nb ? hb + (raw ? rawB : sB + gB) + dB : 0u;
         uint32_t pk_total;
-        const uint32_t hdr = cfg->prec_hdr_bytes;
+        const uint32_t hdr = s_phb;
         const uint32_t start = lead + hdr + warp_excl_scan(pk_bytes, &pk_total);
         const int fits = start + hb <= words * 4;
         if (nb && fits) {
             /* packet header (PackHeaders.c:98-127), sign length 0 */
             uint8_t* h = (uint8_t*)buf + start;
-            if (cfg->short_hdr) {
+            if (s_short) {
                 h[0] = (uint8_t)((raw << 7) | ((dB >> 8) & 0x7f));
                 h[1] = (uint8_t)dB;
                 h[2] = (uint8_t)(gcl_bytes >> 5);
@@ -740,26 +756,23 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
         }
         __syncwarp();
         uint32_t idx0 = 0;
-        for (uint32_t gb0 = 0; gb0 < cfg->nbands_all; gb0 += 32) {
+        for (uint32_t gb0 = 0; gb0 < s_nbands_all; gb0 += 32) {
             const uint32_t gb = gb0 + lane;
-            const int fb = gb < cfg->nbands_all ? cfg->g2f[gb] : JXS_NOBAND;
+            const int fb = gb < s_nbands_all ? s_g2f[gb] : JXS_NOBAND;
             const bool ex = fb != JXS_NOBAND;
             const uint32_t bal = __ballot_sync(FULL, ex);
-            if (ex) {
-                const jxs_band_t& bd = cfg->band[fb];
-                const uint32_t lines = last ? bd.last_lines : bd.lines;
-                if (lines > 0 && s_meth[fb]) put_bits(buf, words, lead * 8 + 40 + 2 * (idx0 + __popc(bal & ((1u << lane) - 1))), 2u, 2, ovf);
-            }
+            if (ex && s_blines[fb] > 0 && s_meth[fb])
+                put_bits(buf, words, lead * 8 + 40 + 2 * (idx0 + __popc(bal & ((1u << lane) - 1))), 2u, 2, ovf);
             idx0 += __popc(bal);
         }
         /* the packed size must be what the rate control paid for */
         const int all_fit = __all_sync(FULL, fits || !nb);
         if (lane == 0) {
             const uint32_t end = hdr + pk_total;
-            s_ok = all_fit && end <= total && end == cfg->hdrs_bytes[last] + R.data_bytes;
+            s_ok = all_fit && end <= total && end == s_hdrs + R.data_bytes;
             if (!s_ok) {
                 printf("jxs pack: precinct %d packs to %u bytes, rate control paid %u + %u bytes (total %u)\n", p, end,
-                       cfg->hdrs_bytes[last], R.data_bytes, total);
+                       s_hdrs, R.data_bytes, total);
                 JXS_STATUS_SET(status, JXS_E_ENC_FRAME);
             }
         }
