@@ -1267,6 +1267,9 @@ extern "C" int32_t jxs_gpu_batch_wait(jxs_gpu_batch_t* b, int32_t* status) {
     int32_t worst = JXS_OK;
     for (uint32_t i = 0; i < b->n; i++) {
         int32_t s = b->status_h[2 * i];
+        /* vertical prediction needs slice-ordered decoding, which the batched
+         * form does not run: decode such frames with send_frame */
+        if (s == JXS_E_DEC_VPRED) s = JXS_E_DEC_BITSTREAM;
         if (b->kind == 0) {
             s = s ? JXS_E_ENC_FRAME : JXS_OK;
         } else if (b->hdr_check[i] && s == JXS_OK) {

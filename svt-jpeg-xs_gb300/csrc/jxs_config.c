@@ -89,6 +89,25 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
         sg *= 2;
     }
     g->seg_groups = sg;
+    /* the line above each band line, for vertical prediction */
+    for (int t = 0; t < 2; t++) {
+        for (uint32_t x = 0; x < g->nbline[t]; x++) {
+            const jxs_bline_t* b = &g->bline[t][x];
+            const int prev = b->line == 0;
+            const int tt = prev ? 0 : t;
+            const uint32_t want = prev ? g->band[b->fb].lines - 1 : b->line - 1u;
+            g->top_bl[t][x] = 0xff;
+            g->top_prev[t][x] = (uint8_t)prev;
+            g->top_gbase[t][x] = 0;
+            for (uint32_t y = 0; y < g->nbline[tt]; y++) {
+                if (g->bline[tt][y].fb == b->fb && g->bline[tt][y].line == want) {
+                    g->top_bl[t][x] = (uint8_t)y;
+                    g->top_gbase[t][x] = g->bline[tt][y].gbase;
+                    break;
+                }
+            }
+        }
+    }
     return JXS_OK;
 }
 

@@ -43,6 +43,10 @@ extern "C" {
 #define JXS_E_DEC_INTERNAL ((int32_t)0x80003002)
 #define JXS_E_DEC_SHORT ((int32_t)0x80003003)
 #define JXS_E_DEC_CONFIG ((int32_t)0x80003004)
+/* internal, never returned to a caller: a precinct uses vertical prediction,
+ * which the per-precinct unpacking cannot resolve; the frame is decoded
+ * again slice by slice */
+#define JXS_E_DEC_VPRED ((int32_t)0x800030ff)
 
 typedef struct jxs_band {
     uint32_t w, h;              /* band size over the whole component */
@@ -107,6 +111,12 @@ typedef struct jxs_cfg {
     uint8_t pk_bl0[2][JXS_MAXPK];        /* first band line of each packet (its count in pk_nbl; 0: absent) */
     uint8_t pk_nbl[2][JXS_MAXPK];
     uint8_t pk_order[2][JXS_MAXBLINES];  /* band lines of each packet (from pk_bl0) in ascending band priority */
+    /* vertical prediction: the band line above each band line (same band,
+     * line - 1 in the same precinct; for line 0 the band's last line in the
+     * precinct row above, a normal row), and where its GCLIs start */
+    uint8_t top_bl[2][JXS_MAXBLINES];    /* band line index (in the normal row's table when top_prev) */
+    uint8_t top_prev[2][JXS_MAXBLINES];  /* 1: in the precinct row above */
+    uint32_t top_gbase[2][JXS_MAXBLINES];
     uint32_t seg_groups;                 /* groups per segment, a multiple of 32 */
     uint32_t nseg[2];
     jxs_seg_t seg[2][JXS_MAXSEG];

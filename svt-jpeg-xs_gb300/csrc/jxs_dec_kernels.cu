@@ -28,6 +28,7 @@
 struct UkLine {
     uint32_t sig_pos;           /* bit position of its significance flags; raw packets: of its 4-bit GCLIs */
     uint8_t t, meth, raw, pk;
+    uint8_t vp, pad0, pad1, pad2; /* vp: GCLIs predicted from the line above */
 };
 /* Per packet. */
 struct UkPk {
@@ -181,7 +182,8 @@ DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uin
  *           written as int16 coefficients (8 bytes per lane, coalesced). */
 __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t bs_size,
                                             const uint32_t* __restrict__ prec_off, int16_t* __restrict__ coef,
-                                            uint32_t cap_bytes, uint32_t cap_groups, int* status, const int p) {
+                                            uint32_t cap_bytes, uint32_t cap_groups, int* status, const int p,
+                                            uint8_t* top_gcl, uint8_t* top_t, const int vp_ok) {
     extern __shared__ __align__(16) uint8_t dsm[];
     uint8_t* pbuf = dsm;
     uint8_t* gcl = dsm + cap_bytes + 32;
@@ -204,8 +206,11 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     __shared__ uint32_t s_total, s_lead, s_tw, s_npk;
     __shared__ uint8_t s_g2f[JXS_MAXBL];          /* global band -> flat band */
     __shared__ uint16_t s_lgp[JXS_MAXBLINES];      /* per line: band gain | priority << 8 */
-    __shared__ uint32_t s_sc[8];                   /* nbands_all, npk, long headers, separate signs, precinct header bytes,
-                                                      band lines, segments, groups per segment */
+    __shared__ uint32_t s_sc[9];                   /* nbands_all, npk, long headers, separate signs, precinct header bytes,
+                                                      band lines, segments, groups per segment, run mode */
+    __shared__ uint8_t s_topbl[JXS_MAXBLINES], s_topprev[JXS_MAXBLINES]; /* vertical prediction: the line above */
+    __shared__ uint32_t s_topg[JXS_MAXBLINES];
+    __shared__ int s_hasvp;
 
     const int last = (p + 1 >= (int)cfg->np);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -222,6 +227,8 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         s_sc[5] = cfg->nbline[last];
         s_sc[6] = cfg->nseg[last];
         s_sc[7] = cfg->seg_groups;
+        s_sc[8] = cfg->rm;
+        s_hasvp = 0;
         if (!err) {
             const uint32_t off = prec_off[p], phb = cfg->prec_hdr_bytes;
             if ((uint64_t)off + phb > bs_size) {
@@ -251,6 +258,9 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             const jxs_band_t& bd = cfg->band[B.fb];
             s_crow[x] = bd.coef_off + (uint64_t)(p * bd.lines + B.line) * bd.pitch;
             s_lgp[x] = (uint16_t)(bd.gain | (bd.prio << 8));
+            s_topbl[x] = cfg->top_bl[last][x];
+            s_topprev[x] = cfg->top_prev[last][x];
+            s_topg[x] = cfg->top_gbase[last][x];
         }
         for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) {
             s_pkbl0[k] = cfg->pk_bl0[last][k];
@@ -286,7 +296,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     if (warp == 0) {
         const uint8_t* h0 = pbuf + lead;
         const uint8_t q = h0[3], r = h0[4];
-        int err = 0;
+        int err = 0, vp_seen = 0;
         /* band coding modes D[p,b], 2 bits per existing band */
         uint32_t idx0 = 0;
         const uint32_t nbands_all = s_sc[0], npk_c = s_sc[1];
@@ -298,7 +308,10 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             if (ex) {
                 const uint32_t pos = 40 + 2 * (idx0 + __popc(bal & ((1u << lane) - 1)));
                 s_mode[fb] = (uint8_t)((h0[pos >> 3] >> (6 - (pos & 7))) & 3);
-                if (s_mode[fb] & 1) err = JXS_E_DEC_BITSTREAM; /* vertical prediction is not part of this decoder */
+                /* vertical prediction: resolved here when the precinct row
+                 * above is known (slice-ordered decoding), else the frame is
+                 * decoded again that way; never in a slice's first row */
+                if (s_mode[fb] & 1) vp_seen = 1;
             }
             idx0 += __popc(bal);
         }
@@ -306,6 +319,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         for (uint32_t x = lane; x < nbl; x += 32) {
             ln[x].t = jxs_truncation((uint8_t)(s_lgp[x] & 255u), (uint8_t)(s_lgp[x] >> 8), q, r);
             ln[x].meth = (s_mode[bls[x].fb] & 2) ? 1 : 0;
+            ln[x].vp = (s_mode[bls[x].fb] & 1) ? 1 : 0;
             ln[x].pk = bls[x].pk;
         }
         __syncwarp();
@@ -386,6 +400,10 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             s_npk = npk_c;
         }
         err = __reduce_or_sync(FULL, (uint32_t)err) ? JXS_E_DEC_BITSTREAM : 0;
+        if (!err && __any_sync(FULL, vp_seen)) {
+            if (!top_gcl) err = JXS_E_DEC_VPRED;
+            else if (!vp_ok) err = JXS_E_DEC_BITSTREAM; /* no precinct row above to predict from */
+        }
         __syncwarp();
         /* line positions: significance flags, or raw GCLIs for raw packets */
         if (!err && lane < (int)npk_c && pk[lane].present) {
@@ -394,11 +412,17 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             uint32_t run = P.spos;
             for (uint32_t x = b0; x < b0 + nb; x++) {
                 ln[x].raw = (uint8_t)P.raw;
+                if (P.raw) ln[x].vp = 0;
                 ln[x].sig_pos = run;
                 run += P.raw ? 4 * bls[x].gcli_w : (ln[x].meth ? bls[x].sig_w : 0u);
             }
         }
         __syncwarp();
+        if (!err) {
+            bool hv = false;
+            for (uint32_t x = lane; x < nbl; x += 32) hv |= ln[x].vp != 0;
+            if (__any_sync(FULL, hv) && lane == 0) s_hasvp = 1;
+        }
         /* codewords of every segment: its groups minus those in
          * insignificant significance groups (flags: 1 = insignificant) */
         if (!err) {
@@ -537,7 +561,9 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                 } else {
                     const uint32_t sp = L.sig_pos + (g0 >> 3);
                     coded = !(L.meth && ((pbuf[sp >> 3] >> (7 - (sp & 7))) & 1));
-                    if (!coded) v4 = L.t * 0x01010101u;
+                    /* predicted lines keep the codeword value (0xff: no
+                     * codeword) until the line above is known */
+                    if (!coded) v4 = L.vp ? 0xffffffffu : L.t * 0x01010101u;
                 }
             }
             const uint32_t bal = __ballot_sync(FULL, coded);
@@ -550,10 +576,10 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                 for (int q = 0; q < 4; q++) {
                     if (q < (int)nv) {
                         const int e = (int)zend[zr + q];
-                        uint32_t v = L.t + (uint32_t)(e - prev - 1);
-                        if (v > 15) {
+                        uint32_t v = (L.vp ? 0u : L.t) + (uint32_t)(e - prev - 1);
+                        if (v > (L.vp ? 31u : 15u)) {
                             bad = 1;
-                            v = 15;
+                            v = L.vp ? 31u : 15u;
                         }
                         v4 |= v << (8 * q);
                         prev = e;
@@ -570,13 +596,58 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const uint32_t v = (v4 >> (8 * q)) & 255u;
-                if (q < (int)nv && v > L.t) dsum += 4 * (v - L.t + 1);
+                if (!L.vp && q < (int)nv && v > L.t) dsum += 4 * (v - L.t + 1);
             }
         }
         dsum = __reduce_add_sync(FULL, dsum);
         if (lane == 0) s_cnt[sidx] = dsum;
     }
     __syncthreads();
+    if (s_hasvp) {
+        /* vertical prediction (unpack_verical_pred_gclis_*, Packing.c:267-431):
+         * GCLI = the predictor max(top, max(gtli_top, gtli)) moved by the
+         * codeword value; without a codeword (insignificant group) the
+         * predictor, or gtli in run mode.  Line levels in order: line l reads
+         * line l - 1 of its band (line 0: the row above, top_gcl). */
+        const uint32_t rm = s_sc[8];
+        for (uint32_t lvl = 0; lvl < 4; lvl++) {
+            for (uint32_t sidx = warp; sidx < nseg; sidx += UK_WARPS) {
+                const jxs_seg_t sg = segs[sidx];
+                const jxs_bline_t B = bls[sg.bl];
+                const UkLine L = ln[sg.bl];
+                if (!L.vp || B.line != lvl) continue;
+                const uint32_t tb = s_topbl[sg.bl];
+                const int from_prev = s_topprev[sg.bl];
+                const uint8_t* src = (from_prev ? top_gcl : gcl) + s_topg[sg.bl];
+                const uint32_t tt = max(from_prev ? (uint32_t)top_t[tb] : (uint32_t)ln[tb].t, (uint32_t)L.t);
+                const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+                uint32_t dsum = 0;
+                for (uint32_t g = sg.g0 + lane; g < gend; g += 32) {
+                    const uint32_t x = gcl[B.gbase + g];
+                    const uint32_t mt = max((uint32_t)src[g], tt);
+                    uint32_t v;
+                    if (x == 0xffu) {
+                        v = rm ? L.t : mt;
+                    } else {
+                        const uint32_t thr = mt > L.t ? mt - L.t : 0u;
+                        int d = 0;
+                        if (x > 2 * thr) d = (int)(x - thr);
+                        else if (x > 0) d = (x & 1) ? -(int)((x + 1) >> 1) : (int)(x >> 1);
+                        v = (uint32_t)((int)mt + d);
+                    }
+                    if (v > 15) {
+                        bad = 1;
+                        v = 15;
+                    }
+                    gcl[B.gbase + g] = (uint8_t)v;
+                    if (v > L.t) dsum += 4 * (v - L.t + 1);
+                }
+                dsum = __reduce_add_sync(FULL, dsum);
+                if (lane == 0) s_cnt[sidx] = dsum;
+            }
+            __syncthreads();
+        }
+    }
     if (warp == 0) {
         /* data base of every segment inside its packet: one lane per packet */
         bool bad_pk = false;
@@ -628,6 +699,11 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         }
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_DEC_BITSTREAM);
+    if (top_gcl) {
+        /* slice-ordered decoding: this row is the next one's row above */
+        for (uint32_t i = threadIdx.x; i < (cap_groups >> 2); i += blockDim.x) ((uint32_t*)top_gcl)[i] = ((const uint32_t*)gcl)[i];
+        for (uint32_t x = threadIdx.x; x < nbl; x += blockDim.x) top_t[x] = ln[x].t;
+    }
 }
 
 /* ------------------------------------------------------------------------ */
@@ -715,7 +791,7 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
                                                             uint32_t bs_size, const uint32_t* __restrict__ prec_off,
                                                             int16_t* __restrict__ coef, uint32_t cap_bytes, uint32_t cap_groups,
                                                             int* status) {
-    unpack_body(cfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status, (int)blockIdx.x);
+    unpack_body(cfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status, (int)blockIdx.x, nullptr, nullptr, 0);
 }
 
 /* cap_bytes / cap_groups: the largest of the batch's frames (shared-memory
@@ -723,7 +799,28 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __r
 __global__ void __launch_bounds__(UK_THREADS) unpack_batch_kernel(const __grid_constant__ DecPrecLaunch L, uint32_t cap_bytes,
                                                                   uint32_t cap_groups) {
     const DecPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
-    unpack_body(F.cfg, F.bs, F.bs_size, F.prec_off, F.coef, cap_bytes, cap_groups, F.status, (int)blockIdx.x - F.first_block);
+    unpack_body(F.cfg, F.bs, F.bs_size, F.prec_off, F.coef, cap_bytes, cap_groups, F.status, (int)blockIdx.x - F.first_block,
+                nullptr, nullptr, 0);
+}
+
+/* Streams with vertical prediction: one block per slice, its precinct rows
+ * in order, each predicting from the row above (kept in shared memory after
+ * the zero-bit table: cap_groups bytes). */
+__global__ void __launch_bounds__(UK_THREADS) unpack_vpred_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs,
+                                                                  uint32_t bs_size, const uint32_t* __restrict__ prec_off,
+                                                                  int16_t* __restrict__ coef, uint32_t cap_bytes,
+                                                                  uint32_t cap_groups, int* status) {
+    extern __shared__ __align__(16) uint8_t dsm[];
+    __shared__ uint8_t top_t[JXS_MAXBLINES];
+    uint8_t* top_gcl = (uint8_t*)(((uintptr_t)(dsm + cap_bytes + 32 + cap_groups) + 15) & ~(uintptr_t)15) + 2 * UK_ZCAP(cap_groups);
+    top_gcl = (uint8_t*)(((uintptr_t)top_gcl + 15) & ~(uintptr_t)15);
+    const uint32_t s = blockIdx.x;
+    const uint32_t first = s * cfg->pps, end = min(cfg->np, first + cfg->pps);
+    for (uint32_t p = first; p < end; p++) {
+        unpack_body(cfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status, (int)p, top_gcl, top_t, p != first);
+        __syncthreads();
+        if (*(volatile int*)status) break;
+    }
 }
 
 __global__ void walk_slices_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t size,
@@ -794,5 +891,16 @@ extern "C" cudaError_t jxs_launch_unpack_batch(const DecPrecLaunch* L, uint32_t 
     if (e != cudaSuccess) return e;
     if (L->nblocks <= 0) return cudaSuccess;
     unpack_batch_kernel<<<L->nblocks, UK_THREADS, smem, st>>>(*L, cap_bytes, cap_groups);
+    return cudaGetLastError();
+}
+
+extern "C" cudaError_t jxs_launch_unpack_vpred(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
+                                               int16_t* coef, uint32_t nslices, uint32_t cap_bytes, uint32_t cap_groups, int* status,
+                                               cudaStream_t st) {
+    const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 2ull * UK_ZCAP(cap_groups) + 16 + cap_groups;
+    static std::atomic<int> attr[JXS_MAX_DEV];
+    cudaError_t e = jxs_smem_attr(unpack_vpred_kernel, (int)smem, attr);
+    if (e != cudaSuccess) return e;
+    unpack_vpred_kernel<<<nslices, UK_THREADS, smem, st>>>(dcfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status);
     return cudaGetLastError();
 }

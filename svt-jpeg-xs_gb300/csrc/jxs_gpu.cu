@@ -432,6 +432,13 @@ struct DecSlot {
     uint32_t* prec_off_h;
     uint8_t* hdr_h;       /* header of a device-resident codestream, checked at completion */
     int hdr_check;
+    /* the frame's arguments, for a second decode slice by slice when it
+     * turns out to use vertical prediction */
+    const uint8_t* arg_bs;  /* device codestream (the caller's or the slot's copy) */
+    uint32_t arg_size;
+    int arg_walked;         /* precinct offsets in prec_off_h */
+    void* arg_planes[4];
+    uint32_t arg_strides[4];
     cudaEvent_t tev[5];
     cudaEvent_t kev[JXS_KEV];
     int nkev;
@@ -454,6 +461,7 @@ struct jxs_gpu_dec {
     int nkern;
     uint64_t timed_frames;
     uint64_t serial;
+    int vpred;                   /* decode slice by slice: the stream uses vertical prediction */
     std::mutex mu;
 };
 
@@ -611,12 +619,22 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
     if (prec_off) {
         /* the previous use of prec_off_h by this slot has completed: slots are
          * reused only after their completion was observed */
-        memcpy(s->prec_off_h, prec_off, sizeof(uint32_t) * c->np);
+        if (prec_off != s->prec_off_h) memcpy(s->prec_off_h, prec_off, sizeof(uint32_t) * c->np);
         CK(cudaMemcpyAsync(s->prec_off, s->prec_off_h, sizeof(uint32_t) * c->np, cudaMemcpyHostToDevice, st));
+    }
+    s->arg_bs = dbs;
+    s->arg_size = size;
+    s->arg_walked = prec_off != NULL;
+    for (int k = 0; k < 4; k++) {
+        s->arg_planes[k] = planes[k];
+        s->arg_strides[k] = strides[k];
     }
     TMARK(1);
     KMARK();
-    CK(jxs_launch_unpack(d->dcfg, dbs, size, s->prec_off, s->coef, c->np, d->cap_bytes, d->cap_groups, s->status, st));
+    if (d->vpred)
+        CK(jxs_launch_unpack_vpred(d->dcfg, dbs, size, s->prec_off, s->coef, c->nslices, d->cap_bytes, d->cap_groups, s->status, st));
+    else
+        CK(jxs_launch_unpack(d->dcfg, dbs, size, s->prec_off, s->coef, c->np, d->cap_bytes, d->cap_groups, s->status, st));
     KMARK();
     TMARK(2);
 
@@ -689,6 +707,18 @@ extern "C" int32_t jxs_gpu_dec_wait(jxs_gpu_dec_t* d, int slot) {
     if (cudaEventSynchronize(s->done) != cudaSuccess) {
         fprintf(stderr, "jxs: decode failed: %s\n", cudaGetErrorString(cudaGetLastError()));
         return JXS_E_DEC_INTERNAL;
+    }
+    if (*s->status_h == JXS_E_DEC_VPRED) {
+        /* the frame uses vertical prediction: decode it again slice by slice,
+         * and the stream's later frames that way from the start */
+        d->vpred = 1;
+        const int32_t r = dec_run(d, s, s->arg_bs, s->arg_size, s->arg_walked ? s->prec_off_h : NULL, s->arg_planes,
+                                  s->arg_strides);
+        if (r != JXS_OK) return r;
+        if (cudaEventSynchronize(s->done) != cudaSuccess) {
+            fprintf(stderr, "jxs: decode failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+            return JXS_E_DEC_INTERNAL;
+        }
     }
     if (s->timed) {
         float ms[DEC_STAGES];

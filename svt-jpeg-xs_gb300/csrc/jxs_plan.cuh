@@ -34,6 +34,9 @@ extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* b
                                          int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status,
                                          cudaStream_t st);
 extern "C" cudaError_t jxs_launch_unpack_batch(const DecPrecLaunch* L, uint32_t cap_bytes, uint32_t cap_groups, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_unpack_vpred(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
+                                               int16_t* coef, uint32_t nslices, uint32_t cap_bytes, uint32_t cap_groups, int* status,
+                                               cudaStream_t st);
 extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, const uint8_t* bs, uint32_t size, uint32_t* prec_off,
                                        int* walk_bad, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_walk_batch(const DecPrecLaunch* L, cudaStream_t st);

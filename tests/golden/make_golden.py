@@ -2,11 +2,14 @@
 SVT-JPEG-XS library built from its own sources (oracle/_ref, see
 oracle/Makefile).  Run in a checkout where the reference is available:
 
-    make -C oracle ref oracle && python tests/golden/make_golden.py
+    make -C oracle ref oracle && python tests/golden/make_golden.py [--vpred-only]
 
 Writes
   <case>.npz            small seeded inputs, the reference's codestream and
                         the reference decoder's planes for that codestream
+  vpred*.npz            the same for the reference encoder's vertical
+                        prediction modes (the product's encoder does not
+                        emit them; its decoder must read them)
   ref_sample_16x16.npz  the 16x16 4:2:2 codestream of the reference's decoder
                         unit test (tests/UnitTests/SampleFramesData.cc), its
                         frame size and the reference decoder's planes
@@ -49,6 +52,19 @@ SMALL_CASES = {
     "slice_full_422_8b": (96, 40, 8, S.FMT_YUV422, 3, 1, 2, 5, 0, 1000, 1, 1, 13),
 }
 
+# Vertical prediction (coding_vertical_prediction_mode 1 and 2 of the reference
+# encoder), decoded by the reference decoder; several precinct rows per
+# slice so that rows predict from the row above.
+# name: (w, h, depth, fmt, bpp_num, bpp_den, decomp_v, decomp_h, quant, slice_h, significance, rc_mode, seed, vpred_mode)
+VPRED_CASES = {
+    "vpred1_422_8b": (128, 64, 8, S.FMT_YUV422, 3, 1, 2, 5, 0, 32, 1, 1, 21, 1),
+    "vpred2_422_10b": (96, 48, 10, S.FMT_YUV422, 4, 1, 2, 5, 0, 48, 1, 1, 22, 2),
+    "vpred1_444_8b": (80, 40, 8, S.FMT_YUV444, 5, 1, 2, 4, 0, 40, 1, 1, 23, 1),
+    "vpred2_420_8b": (64, 64, 8, S.FMT_YUV420, 4, 1, 2, 5, 0, 64, 1, 1, 24, 2),
+    "vpred1_nosig_uniform_422_12b": (72, 32, 12, S.FMT_YUV422, 6, 1, 2, 3, 1, 32, 0, 1, 25, 1),
+    "vpred2_rgb_8b": (64, 48, 8, S.FMT_PACKED_RGB, 4, 1, 2, 5, 0, 48, 1, 1, 26, 2),
+}
+
 # Full-size workloads: the bench's 4K 10-bit stream, the 1080p plain case,
 # the three shapes of the mixed batch and the 8K large-frame stress.
 FULL_CASES = {
@@ -81,9 +97,31 @@ def sample_codestream():
     return np.array([int(x, 16) for x in re.findall(r"0x[0-9A-Fa-f]+", body)], np.uint8)
 
 
+def make_vpred():
+    for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed, vpm) in VPRED_CASES.items():
+        planes = S.frame(w, h, d, fmt, seed=seed)
+        p = O.make_params(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, significance=sig, rc_mode=rc)
+        p.coding_vertical_prediction_mode = vpm
+        err, bs = O.ref_encode(p, planes)
+        assert err == 0, (name, hex(err))
+        err, dec = O.ref_decode(bs)
+        assert err == 0, (name, hex(err))
+        arrays = {"bs": bs, "params": np.array([w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, vpm], np.uint32)}
+        for i, pl in enumerate(planes):
+            arrays["in%d" % i] = pl
+        for i, pl in enumerate(dec):
+            arrays["dec%d" % i] = pl
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+        print(name, len(bs), "bytes")
+
+
 def main():
     if not O.ref_available():
         raise SystemExit("build the reference first: make -C oracle ref")
+    if "--vpred-only" in sys.argv:
+        make_vpred()
+        return
+    make_vpred()
     for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed) in SMALL_CASES.items():
         planes = S.frame(w, h, d, fmt, seed=seed)
         p = O.make_params(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, significance=sig, rc_mode=rc)

@@ -12,13 +12,25 @@ def small_cases():
     out = {}
     for path in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         name = os.path.basename(path)[:-4]
-        if name == "ref_sample_16x16":
+        if name == "ref_sample_16x16" or name.startswith("vpred"):
             continue
         z = np.load(path)
         w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc = [int(x) for x in z["params"]]
         out[name] = dict(w=w, h=h, d=d, fmt=fmt, bpp_num=bn, bpp_den=bd, v=v, hh=hh, q=q, sl=sl, sig=sig, rc=rc,
                          planes=[z["in%d" % i] for i in range(4) if "in%d" % i in z],
                          bs=z["bs"], dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z])
+    return out
+
+
+def vpred_cases():
+    """Codestreams of the reference encoder with vertical prediction, with
+    their inputs and the reference decoder's planes."""
+    out = {}
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "vpred*.npz"))):
+        z = np.load(path)
+        out[os.path.basename(path)[:-4]] = dict(params=[int(x) for x in z["params"]], bs=z["bs"],
+                                                planes=[z["in%d" % i] for i in range(4) if "in%d" % i in z],
+                                                dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z])
     return out
 
 

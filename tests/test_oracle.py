@@ -110,3 +110,12 @@ def test_oracle_rejects_truncated_stream(oracle):
     c = SMALL["c1_422_8b"]
     err, _ = oracle.oracle_decode(c["bs"][: len(c["bs"]) // 2])
     assert err in (0x80003003, 0x80003001)
+
+
+def test_oracle_vertical_prediction_fixtures(oracle):
+    """The oracle decodes the reference encoder's vertical-prediction
+    codestreams bit-exact with the reference decoder (fixtures)."""
+    for name, c in G.vpred_cases().items():
+        err, planes = oracle.oracle_decode(c["bs"])
+        assert err == 0, name
+        assert all(np.array_equal(a, b) for a, b in zip(planes, c["dec"])), name
