@@ -239,6 +239,21 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def whole_job(local_ms, local_units, world, device):
+    """Replicas: every rank times its own share; the job takes as long as the
+    slowest rank (max over ranks of the CUDA-event times) and did the units
+    of all ranks.  Returns (max ms, total units); no collective for one rank."""
+    if world <= 1:
+        return local_ms, local_units
+    import torch
+
+    t = torch.tensor([float(local_ms), float(local_units)], dtype=torch.float64, device=device)
+    mx = t.clone()
+    torch.distributed.all_reduce(mx, op=torch.distributed.ReduceOp.MAX)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.SUM)
+    return float(mx[0].item()), int(round(t[1].item()))
+
+
 def run_batched(args, jxs, torch, dev, frames, d_in, lcod, enc, dec, nseq):
     """Batched encode + decode of the stream, device-resident; returns the
     device time of args.steps steps and the last step's outputs."""
@@ -423,13 +438,9 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     host_s = time.perf_counter() - t0
     clk = clocks.stop()
-    dev_ms = ev0.elapsed_time(ev1)
+    dev_ms, total_frames = whole_job(ev0.elapsed_time(ev1), args.steps * F, world, dev)
     if world > 1:
-        t = torch.tensor([dev_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms = float(t.item())
         torch.distributed.barrier()
-    total_frames = args.steps * F * world
     value = total_frames * W * H / (dev_ms / 1e3) / 1e9
     # bit-exactness of the last timed step against the oracle
     import oracle_lib as O
@@ -460,11 +471,8 @@ def run_ours(args, rank, world, local):
         err, want_planes = O.oracle_decode(want, threads=os.cpu_count() or 1)
         assert err == 0 and all(np.array_equal(t.cpu().numpy(), w) for t, w in zip(bat["out"][i], want_planes)), \
             "batched decoded frame differs from the oracle"
-    if world > 1:
-        t = torch.tensor([bat["dev_ms"]], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        bat["dev_ms"] = float(t.item())
-    batched_value = args.steps * F * world * W * H / (bat["dev_ms"] / 1e3) / 1e9
+    bat["dev_ms"], bat_frames = whole_job(bat["dev_ms"], args.steps * F, world, dev)
+    batched_value = bat_frames * W * H / (bat["dev_ms"] / 1e3) / 1e9
 
     # ---- e2e through the C API with host buffers: every pair on its own slot
     # streams (3 frames in flight per codec), one continuous pipeline over
