@@ -103,15 +103,35 @@ int ref_probe(const uint8_t* bs, uint32_t size, uint32_t* width, uint32_t* heigh
     return 0;
 }
 
-/* Decodes one frame into caller planes (stride = component width). */
-int ref_decode(const uint8_t* bs, uint32_t size, void* const planes[4], const uint32_t alloc_sizes[4], uint32_t threads_num) {
+/* Image configuration of a codestream decoded at a proxy resolution
+ * (proxy: 0 full, 1 half, 2 quarter). */
+int ref_probe_proxy(const uint8_t* bs, uint32_t size, uint32_t proxy, uint32_t* comps, uint32_t comp_info[12]) {
+    svt_jpeg_xs_image_config_t cfg;
+    uint32_t frame_size = 0;
+    memset(&cfg, 0, sizeof(cfg));
+    SvtJxsErrorType_t err = svt_jpeg_xs_decoder_get_single_frame_size_with_proxy(bs, size, &cfg, &frame_size, 0,
+                                                                                 (proxy_mode_t)proxy);
+    if (err) return (int)err;
+    *comps = cfg.components_num;
+    for (int c = 0; c < 4; c++) {
+        comp_info[3 * c + 0] = cfg.components[c].width;
+        comp_info[3 * c + 1] = cfg.components[c].height;
+        comp_info[3 * c + 2] = cfg.components[c].byte_size;
+    }
+    return 0;
+}
+
+/* Decodes one frame into caller planes (stride = component width) at a
+ * proxy resolution. */
+int ref_decode_proxy(const uint8_t* bs, uint32_t size, void* const planes[4], const uint32_t alloc_sizes[4], uint32_t threads_num,
+                     uint32_t proxy) {
     svt_jpeg_xs_decoder_api_t dec;
     memset(&dec, 0, sizeof(dec));
     dec.use_cpu_flags = 0;
     dec.verbose = 0;
     dec.threads_num = threads_num;
     dec.packetization_mode = 0;
-    dec.proxy_mode = proxy_mode_full;
+    dec.proxy_mode = (proxy_mode_t)proxy;
     svt_jpeg_xs_image_config_t cfg;
     SvtJxsErrorType_t err = svt_jpeg_xs_decoder_init(SVT_JPEGXS_API_VER_MAJOR, SVT_JPEGXS_API_VER_MINOR, &dec, bs, size, &cfg);
     if (err) return (int)err;
@@ -135,4 +155,9 @@ int ref_decode(const uint8_t* bs, uint32_t size, void* const planes[4], const ui
     err = svt_jpeg_xs_decoder_get_frame(&dec, &out, 1);
     svt_jpeg_xs_decoder_close(&dec);
     return (int)err;
+}
+
+/* Decodes one frame into caller planes (stride = component width). */
+int ref_decode(const uint8_t* bs, uint32_t size, void* const planes[4], const uint32_t alloc_sizes[4], uint32_t threads_num) {
+    return ref_decode_proxy(bs, size, planes, alloc_sizes, threads_num, 0);
 }

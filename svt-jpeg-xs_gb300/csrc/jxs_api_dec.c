@@ -57,10 +57,13 @@ static void fill_image_config(const jxs_cfg_t* c, svt_jpeg_xs_image_config_t* o)
     o->format = (ColourFormat_t)c->fmt;
     o->components_num = (uint8_t)c->nc;
     const uint32_t ps = c->depth <= 8 ? 1 : 2;
+    /* proxy decoding: the reduced output (ParseHeader.c:813-829) */
+    o->width = (c->W + (1u << c->proxy) - 1) >> c->proxy;
+    o->height = (c->H + (1u << c->proxy) - 1) >> c->proxy;
     for (uint32_t k = 0; k < c->nc; k++) {
-        o->components[k].width = c->comp[k].w;
-        o->components[k].height = c->comp[k].h;
-        o->components[k].byte_size = c->comp[k].w * c->comp[k].h * ps;
+        o->components[k].width = jxs_out_w(c, k);
+        o->components[k].height = jxs_out_h(c, k);
+        o->components[k].byte_size = jxs_out_w(c, k) * jxs_out_h(c, k) * ps;
     }
 }
 
@@ -218,10 +221,7 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_decoder_init(uint64_t version_api_major
     if (!dec_api) return SvtJxsErrorBadParameter;
     dec_api->private_ptr = NULL;
     if (!bitstream_buf || !codestream_size) return SvtJxsErrorDecoderInvalidPointer;
-    if (dec_api->proxy_mode != proxy_mode_full) {
-        /* reduced-resolution decoding is not part of this implementation */
-        return SvtJxsErrorBadParameter;
-    }
+    if (dec_api->proxy_mode >= proxy_mode_max) return SvtJxsErrorBadParameter;
     dec_prv_t* p = (dec_prv_t*)calloc(1, sizeof(dec_prv_t));
     if (!p) return SvtJxsErrorInsufficientResources;
     p->cfg = (jxs_cfg_t*)calloc(1, sizeof(jxs_cfg_t));
@@ -239,6 +239,21 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_decoder_init(uint64_t version_api_major
         free(p);
         return (SvtJxsErrorType_t)r;
     }
+    /* proxy decoding: every component needs as many vertical and horizontal
+     * levels as the output drops (pi_update_proxy_mode, Pi.c:567-626) */
+    const uint32_t ss = dec_api->proxy_mode == proxy_mode_half ? 1u : dec_api->proxy_mode == proxy_mode_quarter ? 2u : 0u;
+    int proxy_ok = ss <= p->cfg->dv && ss <= p->cfg->dh;
+    for (uint32_t k = 0; k < p->cfg->nc; k++) proxy_ok = proxy_ok && ss <= p->cfg->comp[k].dv && ss <= p->cfg->comp[k].dh;
+    if (!proxy_ok) {
+        if (dec_api->verbose >= VERBOSE_ERRORS)
+            fprintf(stderr, "svt-jpeg-xs-gpu: proxy mode %d needs %u decomposition levels in every component\n",
+                    (int)dec_api->proxy_mode, ss);
+        free(p->cfg);
+        free(p->tmp_cfg);
+        free(p);
+        return SvtJxsErrorBadParameter;
+    }
+    p->cfg->proxy = ss;
     p->prec_off = (uint32_t*)malloc(sizeof(uint32_t) * p->cfg->np);
     p->gpu = jxs_gpu_dec_create(p->cfg, DEC_SLOTS, &r);
     if (!p->gpu || !p->prec_off) {
@@ -302,7 +317,7 @@ static SvtJxsErrorType_t check_planes(const dec_prv_t* p, const svt_jpeg_xs_fram
     const uint32_t ps = c->depth <= 8 ? 1 : 2;
     for (uint32_t k = 0; k < c->nc; k++) {
         if (!f->image.data_yuv[k]) return SvtJxsErrorBadParameter;
-        uint64_t min_size = (uint64_t)f->image.stride[k] * ps * (c->comp[k].h - 1) + (uint64_t)c->comp[k].w * ps;
+        uint64_t min_size = (uint64_t)f->image.stride[k] * ps * (jxs_out_h(c, k) - 1) + (uint64_t)jxs_out_w(c, k) * ps;
         if (f->image.alloc_size[k] < min_size) return SvtJxsErrorBadParameter;
     }
     return SvtJxsErrorNone;

@@ -217,7 +217,7 @@ static uint64_t dec_work_layout(const jxs_cfg_t* c, uint8_t* base, DecWork* w) {
     memset(w->out_off, 0, sizeof(w->out_off));
     for (uint32_t k = 0; k < c->nc; k++) {
         w->out_off[k] = ob;
-        ob += round256((uint64_t)c->comp[k].w * c->comp[k].h * bps);
+        ob += round256((uint64_t)jxs_out_w(c, k) * jxs_out_h(c, k) * bps);
     }
     w->out_stage = take(ob);
     return off;
@@ -553,9 +553,10 @@ static int32_t plan_decode_chain(const std::vector<DecItem>& it, const std::vect
             if (err) return err;
         }
     }
-    /* vertical levels from the deepest up; level 0 writes the samples */
+    /* vertical levels from the deepest up; the output level (0, or the proxy
+     * level) writes the samples */
     for (int v = 1; v >= 0; v--) {
-        for (int ok = (v > 0 ? 0 : 1); ok <= (v > 0 ? 0 : 2); ok++) {
+        for (int ok = 0; ok <= 2; ok++) {
             InvVLaunchB* L = (InvVLaunchB*)scratch.data();
             memset(L, 0, sizeof(*L));
             int blocks = 0;
@@ -574,7 +575,7 @@ static int32_t plan_decode_chain(const std::vector<DecItem>& it, const std::vect
             int tiles[JXS_MAXC];
             for (int f : fr) {
                 const DecItem& d = it[f];
-                if (v == 0 && dec_sample_kind(d.c) != ok) continue;
+                if ((v > (int)d.c->proxy ? 0 : dec_sample_kind(d.c)) != ok) continue;
                 const int nj = plan_inv_v(d.c, d.dcfg, d.w->fb, d.out, v, vj, tiles);
                 for (int j = 0; j < nj; j++) {
                     if (L->njobs == JXS_BATCH_JOBS) flush();
@@ -1191,7 +1192,7 @@ extern "C" int32_t jxs_gpu_batch_decode(jxs_gpu_batch_t* b, jxs_gpu_dec_t* const
                 d.out.pitch[k] = strides[i][k];
             } else {
                 d.out.p[k] = w.out_stage + w.out_off[k];
-                d.out.pitch[k] = c->comp[k].w;
+                d.out.pitch[k] = jxs_out_w(c, k);
             }
         }
         weight[i] = c->coef_total;
@@ -1229,9 +1230,9 @@ extern "C" int32_t jxs_gpu_batch_decode(jxs_gpu_batch_t* b, jxs_gpu_dec_t* const
         const uint32_t bps = bytes_per_sample(d.c);
         for (uint32_t k = 0; k < d.c->nc; k++) {
             if (d.out.p[k] == planes[i][k]) continue;
-            const jxs_comp_t& cp = d.c->comp[k];
-            BCK(cudaMemcpy2DAsync(planes[i][k], (size_t)strides[i][k] * bps, d.out.p[k], (size_t)cp.w * bps, (size_t)cp.w * bps,
-                                  cp.h, cudaMemcpyDeviceToHost, st));
+            const uint32_t ow = jxs_out_w(d.c, k), oh = jxs_out_h(d.c, k);
+            BCK(cudaMemcpy2DAsync(planes[i][k], (size_t)strides[i][k] * bps, d.out.p[k], (size_t)ow * bps, (size_t)ow * bps, oh,
+                                  cudaMemcpyDeviceToHost, st));
         }
     }
     BCK(cudaMemcpyAsync(b->status_h, b->status_d, 2 * (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -121,9 +121,19 @@ typedef struct jxs_cfg {
     uint32_t nseg[2];
     jxs_seg_t seg[2][JXS_MAXSEG];
     uint32_t max_slice_budget;           /* 0 when slice starts cannot be predicted (decoder) */
+    uint32_t proxy;                      /* decoder: output at 1/2^proxy resolution (proxy modes, Pi.c:567-626) */
     uint32_t slice_size[8192];           /* bytes of each slice incl. its header (last: incl. EOC) */
     uint32_t slice_begin[8192];          /* byte offset of each slice in the codestream */
 } jxs_cfg_t;
+
+/* Decoded output size of component k: full size, or the proxy resolution
+ * (Pi.c:599-615, ParseHeader.c:813-829). */
+static inline uint32_t jxs_out_w(const jxs_cfg_t* c, uint32_t k) {
+    return (c->comp[k].w + (1u << c->proxy) - 1) >> c->proxy;
+}
+static inline uint32_t jxs_out_h(const jxs_cfg_t* c, uint32_t k) {
+    return (c->comp[k].h + (1u << c->proxy) - 1) >> c->proxy;
+}
 
 /* Decoder-side header fields beyond the geometry. */
 typedef struct jxs_hdr_info {

@@ -493,7 +493,7 @@ static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
     const uint32_t bps = bytes_per_sample(c);
     for (uint32_t k = 0; k < c->nc; k++) {
         s->out_off[k] = ob;
-        ob += ((uint64_t)c->comp[k].w * c->comp[k].h * bps + 255) & ~255ull;
+        ob += ((uint64_t)jxs_out_w(c, k) * jxs_out_h(c, k) * bps + 255) & ~255ull;
     }
     CK(cudaMalloc(&s->out_stage, ob));
     CK(cudaMalloc(&s->status, 64));
@@ -656,7 +656,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
             out.pitch[k] = strides[k];
         } else {
             out.p[k] = s->out_stage + s->out_off[k];
-            out.pitch[k] = c->comp[k].w;
+            out.pitch[k] = jxs_out_w(c, k);
         }
     }
     const int sample_kind = dec_sample_kind(c);
@@ -670,7 +670,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         CK(jxs_launch_inv_h(&L, pass == 0 ? 0 : sample_kind, blocks, st));
         KMARK();
     }
-    for (int v = (int)cfg_max_dv(c) - 1; v >= 0; v--) {
+    for (int v = (int)cfg_max_dv(c) - 1; v >= (int)c->proxy; v--) {
         InvVLaunch L;
         memset(&L, 0, sizeof(L));
         int tiles[JXS_MAXC], blocks = 0;
@@ -679,15 +679,16 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
             L.job[i].first_block = blocks;
             blocks += tiles[i];
         }
-        CK(jxs_launch_inv_v(&L, v > 0 ? 0 : sample_kind, blocks, st));
+        if (!L.njobs) continue;
+        CK(jxs_launch_inv_v(&L, v > (int)c->proxy ? 0 : sample_kind, blocks, st));
         KMARK();
     }
     TMARK(3);
     for (uint32_t k = 0; k < c->nc; k++) {
         if (out_dev[k]) continue;
-        const jxs_comp_t& cp = c->comp[k];
-        CK(cudaMemcpy2DAsync(planes[k], (size_t)strides[k] * bps, s->out_stage + s->out_off[k], (size_t)cp.w * bps,
-                             (size_t)cp.w * bps, cp.h, cudaMemcpyDeviceToHost, st));
+        const uint32_t ow = jxs_out_w(c, k), oh = jxs_out_h(c, k);
+        CK(cudaMemcpy2DAsync(planes[k], (size_t)strides[k] * bps, s->out_stage + s->out_off[k], (size_t)ow * bps, (size_t)ow * bps,
+                             oh, cudaMemcpyDeviceToHost, st));
     }
     CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
     TMARK(4);

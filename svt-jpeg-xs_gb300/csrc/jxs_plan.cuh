@@ -227,15 +227,17 @@ static inline int plan_fwd_h(const jxs_cfg_t* c, const jxs_cfg_t* dcfg, const Fr
     return n;
 }
 
-/* Inverse horizontal-only jobs: pass 0 the components with vertical levels
- * (output: the int32 low band of their last vertical level, kind 0), pass 1
- * those without (output: the samples, dec_sample_kind). */
+/* Inverse horizontal-only jobs: pass 0 the components whose output comes
+ * from a vertical level (output: the int32 low band of their last vertical
+ * level, kind 0), pass 1 the others (output: the samples, dec_sample_kind):
+ * components without vertical levels, and under proxy decoding those whose
+ * output level is their last vertical level (dv == proxy). */
 static inline int plan_inv_h(const jxs_cfg_t* c, const jxs_cfg_t* dcfg, const FrameBufs& b, const FramePlanes& out, int pass,
                              InvHJob* jobs) {
     int n = 0;
     for (uint32_t k = 0; k < c->nc; k++) {
         const jxs_comp_t& cp = c->comp[k];
-        if ((cp.dv > 0) != (pass == 0)) continue;
+        if ((cp.dv > c->proxy) != (pass == 0)) continue;
         InvHJob& J = jobs[n++];
         memset(&J, 0, sizeof(J));
         uint32_t w, h;
@@ -248,7 +250,7 @@ static inline int plan_inv_h(const jxs_cfg_t* c, const jxs_cfg_t* dcfg, const Fr
         J.nh = bj.nh;
         for (int e = 0; e < 5; e++) J.b_hf[e] = bj.b_hf[e];
         J.b_ll = bj.b_ll;
-        if (cp.dv > 0) {
+        if (cp.dv > c->proxy) {
             J.dst = b.ll[cp.dv - 1][k];
             J.dst_pitch = b.ll_pitch[cp.dv - 1][k];
         } else {
@@ -265,7 +267,8 @@ static inline int plan_inv_h(const jxs_cfg_t* c, const jxs_cfg_t* dcfg, const Fr
 }
 
 /* Inverse jobs of vertical level v (output: the int32 low band of level v-1,
- * or the samples for v = 0); *tiles receives each job's block count. */
+ * or the samples for v = proxy, the output level); levels below the output
+ * level have no jobs.  *tiles receives each job's block count. */
 static inline int plan_inv_v(const jxs_cfg_t* c, const jxs_cfg_t* dcfg, const FrameBufs& b, const FramePlanes& out, int v,
                              InvVJob* jobs, int* tiles) {
     const uint32_t bps = bytes_per_sample(c);
@@ -273,7 +276,7 @@ static inline int plan_inv_v(const jxs_cfg_t* c, const jxs_cfg_t* dcfg, const Fr
     int n = 0;
     for (uint32_t k = 0; k < c->nc; k++) {
         const jxs_comp_t& cp = c->comp[k];
-        if ((int)cp.dv <= v) continue;
+        if ((int)cp.dv <= v || v < (int)c->proxy) continue;
         InvVJob& J = jobs[n];
         memset(&J, 0, sizeof(J));
         uint32_t w, h;
@@ -286,7 +289,7 @@ static inline int plan_inv_v(const jxs_cfg_t* c, const jxs_cfg_t* dcfg, const Fr
         J.b_hh = top;
         J.b_lh = top - 1;
         J.b_hl = top - 2;
-        if (v > 0) {
+        if (v > (int)c->proxy) {
             J.dst = b.ll[v - 1][k];
             J.dst_pitch = b.ll_pitch[v - 1][k];
             J.vec = 1;

@@ -384,10 +384,11 @@ def frame_size(bs, fast=0):
 class Decoder:
     """GPU decoder behind the reference C API; initialised from a codestream."""
 
-    def __init__(self, first_codestream, packetization_mode=0, verbose=0):
+    def __init__(self, first_codestream, packetization_mode=0, verbose=0, proxy_mode=0):
         self.api = DecoderApi()
         self.api.verbose = verbose
         self.api.packetization_mode = packetization_mode
+        self.api.proxy_mode = proxy_mode
         self.config = ImageConfig()
         buf = np.ascontiguousarray(first_codestream, dtype=np.uint8)
         _check("decoder_init", lib().svt_jpeg_xs_decoder_init(API_MAJOR, API_MINOR, ctypes.byref(self.api), buf.ctypes.data,

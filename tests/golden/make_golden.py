@@ -2,7 +2,7 @@
 SVT-JPEG-XS library built from its own sources (oracle/_ref, see
 oracle/Makefile).  Run in a checkout where the reference is available:
 
-    make -C oracle ref oracle && python tests/golden/make_golden.py [--vpred-only]
+    make -C oracle ref oracle && python tests/golden/make_golden.py [--vpred-only | --proxy-only]
 
 Writes
   <case>.npz            small seeded inputs, the reference's codestream and
@@ -10,6 +10,8 @@ Writes
   vpred*.npz            the same for the reference encoder's vertical
                         prediction modes (the product's encoder does not
                         emit them; its decoder must read them)
+  proxy<m>_<case>.npz   the reference decoder's proxy output (m = 1 half,
+                        2 quarter resolution) for a small case's codestream
   ref_sample_16x16.npz  the 16x16 4:2:2 codestream of the reference's decoder
                         unit test (tests/UnitTests/SampleFramesData.cc), its
                         frame size and the reference decoder's planes
@@ -97,6 +99,27 @@ def sample_codestream():
     return np.array([int(x, 16) for x in re.findall(r"0x[0-9A-Fa-f]+", body)], np.uint8)
 
 
+# Proxy decoding: the reference decoder's half- and quarter-resolution
+# output for codestreams of the small cases (proxy 2 needs two vertical
+# levels in every component).
+PROXY_CASES = [("c1_422_8b", 1), ("c1_422_8b", 2), ("c2_422_10b", 1), ("c2_422_10b", 2), ("c3_420_8b", 1),
+               ("c3_444_12b", 2), ("c3_rgb_8b", 1), ("odd_444_10b", 1), ("odd_444_10b", 2), ("c4_gbrp_14b_v1", 1),
+               ("uniform_422_10b", 2)]
+
+
+def make_proxy():
+    for name, proxy in PROXY_CASES:
+        z = np.load(os.path.join(HERE, name + ".npz"))
+        bs = z["bs"]
+        err, dec = O.ref_decode_proxy(bs, proxy)
+        assert err == 0, (name, proxy, hex(err))
+        arrays = {"bs": bs, "proxy": np.array([proxy], np.uint32)}
+        for i, pl in enumerate(dec):
+            arrays["dec%d" % i] = pl
+        np.savez_compressed(os.path.join(HERE, "proxy%d_%s.npz" % (proxy, name)), **arrays)
+        print("proxy", proxy, name, [p.shape for p in dec])
+
+
 def make_vpred():
     for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed, vpm) in VPRED_CASES.items():
         planes = S.frame(w, h, d, fmt, seed=seed)
@@ -121,6 +144,9 @@ def main():
     if "--vpred-only" in sys.argv:
         make_vpred()
         return
+    if "--proxy-only" in sys.argv:
+        make_proxy()
+        return
     make_vpred()
     for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed) in SMALL_CASES.items():
         planes = S.frame(w, h, d, fmt, seed=seed)
@@ -136,6 +162,7 @@ def main():
             arrays["dec%d" % i] = pl
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
         print(name, len(bs), "bytes")
+    make_proxy()
     bs = sample_codestream()
     err, dec = O.ref_decode(bs)
     assert err == 0

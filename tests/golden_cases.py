@@ -12,13 +12,24 @@ def small_cases():
     out = {}
     for path in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         name = os.path.basename(path)[:-4]
-        if name == "ref_sample_16x16" or name.startswith("vpred"):
+        if name == "ref_sample_16x16" or name.startswith("vpred") or name.startswith("proxy"):
             continue
         z = np.load(path)
         w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc = [int(x) for x in z["params"]]
         out[name] = dict(w=w, h=h, d=d, fmt=fmt, bpp_num=bn, bpp_den=bd, v=v, hh=hh, q=q, sl=sl, sig=sig, rc=rc,
                          planes=[z["in%d" % i] for i in range(4) if "in%d" % i in z],
                          bs=z["bs"], dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z])
+    return out
+
+
+def proxy_cases():
+    """Codestreams of the small cases with the reference decoder's half (1)
+    or quarter (2) resolution output."""
+    out = {}
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "proxy*.npz"))):
+        z = np.load(path)
+        out[os.path.basename(path)[:-4]] = dict(proxy=int(z["proxy"][0]), bs=z["bs"],
+                                                dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z])
     return out
 
 

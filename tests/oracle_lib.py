@@ -142,6 +142,22 @@ def ref_encode(params, planes):
     return err & 0xffffffff, out[:sz.value].copy()
 
 
+def ref_decode_proxy(bs, proxy, threads=1):
+    """The reference decoder at a proxy resolution (1 half, 2 quarter)."""
+    buf = np.ascontiguousarray(bs, dtype=np.uint8)
+    comps = ctypes.c_uint32()
+    info = (ctypes.c_uint32 * 12)()
+    err = ref().ref_probe_proxy(buf.ctypes.data_as(ctypes.c_void_p), len(buf), proxy, ctypes.byref(comps), info)
+    if err:
+        return err & 0xffffffff, None
+    e0, full = probe(bs)
+    dt = np.uint8 if full.bit_depth <= 8 else np.uint16
+    planes = [np.zeros((info[3 * c + 1], info[3 * c]), dt) for c in range(comps.value)]
+    ptrs, _, allocs = _plane_args(planes)
+    err = ref().ref_decode_proxy(buf.ctypes.data_as(ctypes.c_void_p), len(buf), ptrs, allocs, threads, proxy)
+    return err & 0xffffffff, planes
+
+
 def ref_decode(bs, threads=1):
     err, info = probe(bs)
     if err:

@@ -326,3 +326,52 @@ def test_vertical_prediction_device_codestream(gpu):
         r, _ = dec.get()
         assert r == 0 and all(np.array_equal(t.cpu().numpy(), p) for t, p in zip(outs, c["dec"]))
     dec.close()
+
+
+@pytest.mark.parametrize("name", sorted(G.proxy_cases()))
+def test_proxy_decode_matches_reference(gpu, name):
+    """Half (1) and quarter (2) resolution decoding, bit-exact with the
+    reference decoder's proxy output."""
+    c = G.proxy_cases()[name]
+    dec = gpu.Decoder(c["bs"], proxy_mode=c["proxy"])
+    assert [(dec.config.components[k].height, dec.config.components[k].width) for k in range(dec.config.components_num)] == \
+        [p.shape for p in c["dec"]]
+    out = dec.decode(c["bs"])
+    dec.close()
+    assert all(np.array_equal(a, b) for a, b in zip(out, c["dec"])), name
+
+
+def test_proxy_batched_and_device(gpu):
+    """Proxy decoding through the batch API, mixed with full-resolution
+    frames, and into device planes."""
+    torch = pytest.importorskip("torch")
+    cases = G.proxy_cases()
+    names = ["proxy1_c1_422_8b", "proxy2_c2_422_10b", "proxy1_c3_420_8b"]
+    decs = [gpu.Decoder(cases[n]["bs"], proxy_mode=cases[n]["proxy"]) for n in names]
+    full = SMALL["c3_444_12b"]
+    decs.append(gpu.Decoder(full["bs"]))
+    bss = [cases[n]["bs"] for n in names] + [full["bs"]]
+    wants = [cases[n]["dec"] for n in names] + [full["dec"]]
+    batch = gpu.Batch(1 << 30)
+    planes = [d.alloc_planes() for d in decs]
+    assert batch.decode(decs, bss, planes) == 0
+    r, st = batch.wait()
+    assert r == 0 and st == [0] * len(decs)
+    for out, want in zip(planes, wants):
+        assert all(np.array_equal(a, b) for a, b in zip(out, want))
+    batch.close()
+    d = decs[0]
+    dout = [torch.zeros(p.shape, dtype=torch.uint8, device="cuda") for p in wants[0]]
+    assert d.send(bss[0], [(t.data_ptr(), t.shape[1]) for t in dout]) == 0
+    r, _ = d.get()
+    assert r == 0 and all(np.array_equal(t.cpu().numpy(), p) for t, p in zip(dout, wants[0]))
+    for x in decs:
+        x.close()
+
+
+def test_proxy_needs_enough_levels(gpu):
+    """Quarter resolution of a stream with one vertical level is refused
+    (pi_update_proxy_mode)."""
+    c = SMALL["c4_gbrp_14b_v1"]
+    with pytest.raises(gpu.JxsError):
+        gpu.Decoder(c["bs"], proxy_mode=2)
