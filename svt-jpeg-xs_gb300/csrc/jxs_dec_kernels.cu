@@ -35,6 +35,7 @@ struct UkPk {
     uint32_t spos;              /* first bit after the packet header */
     uint32_t gpos, gbits;       /* GCLI sub-packet: bit position and length */
     uint32_t dpos, dbits;       /* data sub-packet */
+    uint32_t sgpos, sgbits;     /* sign sub-packet (separate signs, Fs = 1) */
     uint32_t wbase, nwords;     /* its 32-bit words in the concatenated GCLI word list (VLC packets) */
     uint32_t zbase, nzero;      /* rank of its first zero bit among all VLC zeros; zeros in its range */
     uint32_t ncoded;            /* unary codewords */
@@ -116,9 +117,15 @@ DEV uint32_t next_seg(uint32_t* ctr, int lane) {
  * and sign-magnitude to two's complement (inv_sign_c, Precinct.c:9-14).
  * Returns the four int16 results packed two per word, coefficient 0 in the
  * low half of .x; coefficients at or past `wl` (remaining width) are 0. */
-DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uint32_t uniform, int wl) {
-    const uint32_t sgn = (uint32_t)(chunk >> (4 * np)) & 15u;
-    const uint64_t planes = chunk & ((1ull << (4 * np)) - 1);
+DEV uint2 group_finish(uint32_t A, uint32_t B, uint32_t sgn, uint32_t uniform, int wl);
+
+/* The dequantized magnitudes of a group's four coefficients from its plane
+ * bits, as 16-bit pairs: coefficients 0 | 1 << 16 in *A, 2 | 3 << 16 in *B.
+ * The plane bits are planes v-1 .. gtli as nibbles, coefficient 0 in each
+ * nibble's most significant bit (Packing.c:117-132), placed at << gtli, then
+ * deadzone or uniform dequantization (Dequant.c:9-57).  Returns the mask of
+ * non-zero magnitudes (bit 3 - c for coefficient c). */
+DEV uint32_t group_mags(uint64_t planes, uint32_t np, uint32_t t, uint32_t gv, uint32_t uniform, uint32_t* A, uint32_t* B) {
     /* the plane bits of coefficients 0, 1 / 2, 3 as 16-bit pairs */
     const uint32_t tl = planes_to_coefs((uint32_t)planes);
     uint32_t P01 = __byte_perm(tl, 0u, 0x4243), P23 = __byte_perm(tl, 0u, 0x4041);
@@ -127,21 +134,19 @@ DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uin
         P01 |= __byte_perm(th, 0u, 0x4243) << 8;
         P23 |= __byte_perm(th, 0u, 0x4041) << 8;
     }
-    /* keep[] zeroes coefficients past the band width */
-    const uint32_t keepA = (wl > 1 ? 0xffff0000u : 0u) | 0xffffu, keepB = (wl > 2 ? 0xffffu : 0u) | (wl > 3 ? 0xffff0000u : 0u);
+    const uint32_t nz01 = __vcmpne2(P01, 0u), nz23 = __vcmpne2(P23, 0u);
+    const uint32_t nz = ((nz01 & 1u) << 3) | ((nz01 >> 16 & 1u) << 2) | ((nz23 & 1u) << 1) | (nz23 >> 16 & 1u);
     if (!uniform || t == 0) {
         /* two coefficients per word: m << t stays below 2^15 */
-        uint32_t A = P01 << t, B = P23 << t;
+        uint32_t a = P01 << t, b = P23 << t;
         if (t > 0) {
             const uint32_t half = (1u << (t - 1)) * 0x00010001u;
-            A |= __vcmpne2(A, 0u) & half;
-            B |= __vcmpne2(B, 0u) & half;
+            a |= __vcmpne2(a, 0u) & half;
+            b |= __vcmpne2(b, 0u) & half;
         }
-        const uint32_t nA = ((sgn & 8u) ? 0xffffu : 0u) | ((sgn & 4u) ? 0xffff0000u : 0u);
-        const uint32_t nB = ((sgn & 2u) ? 0xffffu : 0u) | ((sgn & 1u) ? 0xffff0000u : 0u);
-        A = (A & ~nA) | (__vsub2(0u, A) & nA);
-        B = (B & ~nB) | (__vsub2(0u, B) & nB);
-        return make_uint2(A & keepA, B & keepB);
+        *A = a;
+        *B = b;
+        return nz;
     }
     const uint32_t m[4] = {P01 & 0xffffu, P01 >> 16, P23 & 0xffffu, P23 >> 16};
     uint32_t o[4];
@@ -155,10 +160,45 @@ DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uin
             for (; val > 0; val >>= sc) acc = (acc + val) & 0xffffu;
             mag = acc;
         }
-        const uint32_t sm = (mag | (((sgn >> (3 - c)) & 1u) << 15)) & 0xffffu;
+        o[c] = mag;
+    }
+    *A = o[0] | (o[1] << 16);
+    *B = o[2] | (o[3] << 16);
+    return nz;
+}
+
+/* Sign-magnitude to two's complement (inv_sign_c, Precinct.c:9-14): sign
+ * bit 3 - c of `sgn` for coefficient c; coefficients at or past `wl`
+ * (remaining width) are 0.  Returns the four int16 results packed two per
+ * word, coefficient 0 in the low half of .x. */
+DEV uint2 group_finish(uint32_t A, uint32_t B, uint32_t sgn, uint32_t uniform, int wl) {
+    const uint32_t keepA = (wl > 1 ? 0xffff0000u : 0u) | 0xffffu, keepB = (wl > 2 ? 0xffffu : 0u) | (wl > 3 ? 0xffff0000u : 0u);
+    if (!uniform) {
+        /* deadzone magnitudes stay below 2^15 */
+        const uint32_t nA = ((sgn & 8u) ? 0xffffu : 0u) | ((sgn & 4u) ? 0xffff0000u : 0u);
+        const uint32_t nB = ((sgn & 2u) ? 0xffffu : 0u) | ((sgn & 1u) ? 0xffff0000u : 0u);
+        A = (A & ~nA) | (__vsub2(0u, A) & nA);
+        B = (B & ~nB) | (__vsub2(0u, B) & nB);
+        return make_uint2(A & keepA, B & keepB);
+    }
+    const uint32_t mg[4] = {A & 0xffffu, A >> 16, B & 0xffffu, B >> 16};
+    uint32_t o[4];
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const uint32_t sm = (mg[c] | (((sgn >> (3 - c)) & 1u) << 15)) & 0xffffu;
         o[c] = (uint32_t)((sm & 0x8000u) ? -(int32_t)(sm & 0x7fffu) : (int32_t)sm) & 0xffffu;
     }
     return make_uint2((o[0] | (o[1] << 16)) & keepA, (o[2] | (o[3] << 16)) & keepB);
+}
+
+/* One group's coefficients from its data bits with the signs joined to the
+ * data (unpack_data_c, Packing.c:134-219): the sign nibble (coefficient 0 in
+ * its most significant bit), then the plane nibbles. */
+DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uint32_t uniform, int wl) {
+    const uint32_t sgn = (uint32_t)(chunk >> (4 * np)) & 15u;
+    uint32_t A, B;
+    group_mags(chunk & ((1ull << (4 * np)) - 1), np, t, gv, uniform, &A, &B);
+    return group_finish(A, B, sgn, uniform && t != 0, wl);
 }
 
 /* unpack_precinct (Packing.c:513-868) for one precinct row; vertical
@@ -211,6 +251,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     __shared__ uint8_t s_topbl[JXS_MAXBLINES], s_topprev[JXS_MAXBLINES]; /* vertical prediction: the line above */
     __shared__ uint32_t s_topg[JXS_MAXBLINES];
     __shared__ int s_hasvp;
+    __shared__ uint32_t s_nz[JXS_MAXSEG], s_sgb[JXS_MAXSEG]; /* separate signs: per segment, count and first bit */
 
     const int last = (p + 1 >= (int)cfg->np);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -387,8 +428,10 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                 P.dbits = dlen * 8;
                 bpos += dlen;
                 left -= (int64_t)dlen * 8;
-                if (s_sc[3]) err = JXS_E_DEC_BITSTREAM; /* separate sign sub-packets are not part of this decoder */
+                P.sgpos = bpos * 8;
+                P.sgbits = slen * 8;
                 bpos += slen;
+                left -= (int64_t)slen * 8;
                 if (left < 0 || bpos > lead + total) { err = JXS_E_DEC_BITSTREAM; break; }
                 P.present = 1;
                 if (!raw) {
@@ -540,6 +583,8 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
      * lane may hold fewer than 4 groups, and no lane after it holds any). */
     int bad = 0;
     const uint32_t lt_mask = (1u << lane) - 1u;
+    /* a group's data: its sign nibble (signs with the data) and its planes */
+    const uint32_t fs = s_sc[3], nib_sign = fs ? 0u : 1u;
     for (uint32_t sidx = next_seg(&s_next[0], lane); sidx < nseg; sidx = next_seg(&s_next[0], lane)) {
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
@@ -596,7 +641,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 const uint32_t v = (v4 >> (8 * q)) & 255u;
-                if (!L.vp && q < (int)nv && v > L.t) dsum += 4 * (v - L.t + 1);
+                if (!L.vp && q < (int)nv && v > L.t) dsum += 4 * (v - L.t + nib_sign);
             }
         }
         dsum = __reduce_add_sync(FULL, dsum);
@@ -640,7 +685,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                         v = 15;
                     }
                     gcl[B.gbase + g] = (uint8_t)v;
-                    if (v > L.t) dsum += 4 * (v - L.t + 1);
+                    if (v > L.t) dsum += 4 * (v - L.t + nib_sign);
                 }
                 dsum = __reduce_add_sync(FULL, dsum);
                 if (lane == 0) s_cnt[sidx] = dsum;
@@ -672,6 +717,63 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
 
     /* pass 3: data */
     const uint32_t uniform = cfg->qpih;
+    if (fs) {
+        /* separate signs (unpack_sign, Packing.c:221-247): a sign bit for
+         * every non-zero magnitude, band lines of the packet in order and each
+         * line in coefficient order (the last group's padding coefficients
+         * last).  Count them per segment, give each segment its first sign
+         * bit in the packet's sign sub-packet, then decode with the signs. */
+        for (uint32_t sidx = next_seg(&s_next[1], lane); sidx < nseg; sidx = next_seg(&s_next[1], lane)) {
+            const jxs_seg_t sg = segs[sidx];
+            const jxs_bline_t B = bls[sg.bl];
+            const UkLine L = ln[sg.bl];
+            const UkPk P = pk[L.pk];
+            const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+            uint32_t dpos = P.dpos + s_base[sidx], nzs = 0;
+            for (uint32_t base = sg.g0; base < gend; base += 32) {
+                const uint32_t g = base + lane;
+                const uint32_t v = g < gend ? gcl[B.gbase + g] : 0u;
+                const uint32_t np = v > L.t ? v - L.t : 0u;
+                const uint32_t len = 4 * np;
+                uint32_t tot;
+                const uint32_t ex = warp_excl_scan(len, &tot);
+                if (len) {
+                    const uint32_t pos = dpos + ex;
+                    const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
+                    uint32_t A, B2;
+                    nzs += __popc(group_mags(win >> (64 - len), np, L.t, v, uniform, &A, &B2));
+                }
+                dpos += tot;
+            }
+            nzs = __reduce_add_sync(FULL, nzs);
+            if (lane == 0) s_nz[sidx] = nzs;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            /* first sign bit of every segment inside its packet: one lane per packet */
+            bool bad_pk = false;
+            if (lane < (int)npk) {
+                const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
+                uint32_t run = 0;
+                for (uint32_t x = b0; x < b0 + nb; x++)
+                    for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
+                        s_sgb[i] = run;
+                        run += s_nz[i];
+                    }
+                bad_pk = pk[lane].present && run > pk[lane].sgbits;
+            }
+            const bool any_bad = __any_sync(FULL, bad_pk);
+            if (lane == 0) {
+                s_err = any_bad ? JXS_E_DEC_BITSTREAM : 0;
+                s_next[1] = 0;
+            }
+        }
+        __syncthreads();
+        if (s_err) {
+            if (threadIdx.x == 0) JXS_STATUS_SET(status, s_err);
+            return;
+        }
+    }
     for (uint32_t sidx = next_seg(&s_next[1], lane); sidx < nseg; sidx = next_seg(&s_next[1], lane)) {
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
@@ -680,19 +782,46 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         int16_t* crow = coef + s_crow[sg.bl];
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
         uint32_t dpos = P.dpos + s_base[sidx];
+        uint32_t spos = fs ? P.sgpos + s_sgb[sidx] : 0u;
         for (uint32_t base = sg.g0; base < gend; base += 32) {
             const uint32_t g = base + lane;
             const bool valid = g < gend;
             const uint32_t v = valid ? gcl[B.gbase + g] : 0u;
             const uint32_t np = v > L.t ? v - L.t : 0u;
-            const uint32_t len = np ? 4 * (np + 1) : 0u;
+            const uint32_t len = np ? 4 * (np + nib_sign) : 0u;
             uint32_t tot;
             const uint32_t ex = warp_excl_scan(len, &tot);
             uint2 o = make_uint2(0u, 0u);
-            if (len) {
-                const uint32_t pos = dpos + ex;
-                const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
-                o = decode_group(win >> (64 - len), np, L.t, v, uniform, (int)B.w - 4 * (int)g);
+            if (!fs) {
+                if (len) {
+                    const uint32_t pos = dpos + ex;
+                    const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
+                    o = decode_group(win >> (64 - len), np, L.t, v, uniform, (int)B.w - 4 * (int)g);
+                }
+            } else {
+                uint32_t A = 0, B2 = 0, nz = 0;
+                if (len) {
+                    const uint32_t pos = dpos + ex;
+                    const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
+                    nz = group_mags(win >> (64 - len), np, L.t, v, uniform, &A, &B2);
+                }
+                /* this group's sign bits follow those of the lanes before it */
+                uint32_t stot;
+                const uint32_t sex = warp_excl_scan(__popc(nz), &stot);
+                uint32_t sgn = 0;
+                if (nz) {
+                    const uint32_t sw = bits32_at(pbuf, spos + sex);
+                    uint32_t k = 0;
+#pragma unroll
+                    for (int c = 3; c >= 0; c--) {
+                        if (nz & (1u << c)) {
+                            sgn |= ((sw >> (31 - k)) & 1u) << c;
+                            k++;
+                        }
+                    }
+                }
+                if (len) o = group_finish(A, B2, sgn, uniform && L.t != 0, (int)B.w - 4 * (int)g);
+                spos += stot;
             }
             if (valid) *(uint2*)(crow + 4 * g) = o;
             dpos += tot;

@@ -2,7 +2,7 @@
 SVT-JPEG-XS library built from its own sources (oracle/_ref, see
 oracle/Makefile).  Run in a checkout where the reference is available:
 
-    make -C oracle ref oracle && python tests/golden/make_golden.py [--vpred-only | --proxy-only]
+    make -C oracle ref oracle && python tests/golden/make_golden.py [--vpred-only | --proxy-only | --signs-only]
 
 Writes
   <case>.npz            small seeded inputs, the reference's codestream and
@@ -10,6 +10,9 @@ Writes
   vpred*.npz            the same for the reference encoder's vertical
                         prediction modes (the product's encoder does not
                         emit them; its decoder must read them)
+  signs*.npz            codestreams with separate sign sub-packets
+                        (coding_signs_handling 1 / 2), with inputs and the
+                        reference decoder's planes
   proxy<m>_<case>.npz   the reference decoder's proxy output (m = 1 half,
                         2 quarter resolution) for a small case's codestream
   ref_sample_16x16.npz  the 16x16 4:2:2 codestream of the reference's decoder
@@ -120,6 +123,38 @@ def make_proxy():
         print("proxy", proxy, name, [p.shape for p in dec])
 
 
+# Separate sign sub-packets (coding_signs_handling 1 fast, 2 full), with
+# and without vertical prediction, decoded by the reference decoder.
+# name: (w, h, depth, fmt, bpp_num, bpp_den, decomp_v, decomp_h, quant, slice_h, significance, rc_mode, seed, signs, vpred_mode)
+SIGN_CASES = {
+    "signs1_422_8b": (64, 32, 8, S.FMT_YUV422, 5, 1, 2, 5, 0, 16, 1, 1, 31, 1, 0),
+    "signs2_422_10b": (128, 48, 10, S.FMT_YUV422, 3, 1, 2, 5, 0, 16, 1, 1, 32, 2, 0),
+    "signs2_444_12b_odd": (53, 37, 12, S.FMT_YUV444, 4, 1, 2, 5, 0, 16, 1, 1, 33, 2, 0),
+    "signs1_rgb_8b_uniform": (96, 32, 8, S.FMT_PACKED_RGB, 4, 1, 2, 5, 1, 16, 1, 1, 34, 1, 0),
+    "signs2_vpred1_422_8b": (128, 64, 8, S.FMT_YUV422, 3, 1, 2, 5, 0, 32, 1, 1, 35, 2, 1),
+    "signs1_nosig_420_8b": (96, 48, 8, S.FMT_YUV420, 3, 1, 2, 5, 0, 16, 0, 1, 36, 1, 0),
+}
+
+
+def make_signs():
+    for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed, sg, vpm) in SIGN_CASES.items():
+        planes = S.frame(w, h, d, fmt, seed=seed)
+        p = O.make_params(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, significance=sig, rc_mode=rc)
+        p.coding_signs_handling = sg
+        p.coding_vertical_prediction_mode = vpm
+        err, bs = O.ref_encode(p, planes)
+        assert err == 0, (name, hex(err))
+        err, dec = O.ref_decode(bs)
+        assert err == 0, (name, hex(err))
+        arrays = {"bs": bs, "params": np.array([w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, sg, vpm], np.uint32)}
+        for i, pl in enumerate(planes):
+            arrays["in%d" % i] = pl
+        for i, pl in enumerate(dec):
+            arrays["dec%d" % i] = pl
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+        print(name, len(bs), "bytes")
+
+
 def make_vpred():
     for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed, vpm) in VPRED_CASES.items():
         planes = S.frame(w, h, d, fmt, seed=seed)
@@ -147,7 +182,11 @@ def main():
     if "--proxy-only" in sys.argv:
         make_proxy()
         return
+    if "--signs-only" in sys.argv:
+        make_signs()
+        return
     make_vpred()
+    make_signs()
     for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed) in SMALL_CASES.items():
         planes = S.frame(w, h, d, fmt, seed=seed)
         p = O.make_params(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, significance=sig, rc_mode=rc)

@@ -12,7 +12,7 @@ def small_cases():
     out = {}
     for path in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         name = os.path.basename(path)[:-4]
-        if name == "ref_sample_16x16" or name.startswith("vpred") or name.startswith("proxy"):
+        if name == "ref_sample_16x16" or name.startswith(("vpred", "proxy", "signs")):
             continue
         z = np.load(path)
         w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc = [int(x) for x in z["params"]]
@@ -29,6 +29,18 @@ def proxy_cases():
     for path in sorted(glob.glob(os.path.join(GOLDEN, "proxy*.npz"))):
         z = np.load(path)
         out[os.path.basename(path)[:-4]] = dict(proxy=int(z["proxy"][0]), bs=z["bs"],
+                                                dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z])
+    return out
+
+
+def sign_cases():
+    """Codestreams of the reference encoder with separate sign sub-packets,
+    with their inputs and the reference decoder's planes."""
+    out = {}
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "signs*.npz"))):
+        z = np.load(path)
+        out[os.path.basename(path)[:-4]] = dict(params=[int(x) for x in z["params"]], bs=z["bs"],
+                                                planes=[z["in%d" % i] for i in range(4) if "in%d" % i in z],
                                                 dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z])
     return out
 

@@ -375,3 +375,22 @@ def test_proxy_needs_enough_levels(gpu):
     c = SMALL["c4_gbrp_14b_v1"]
     with pytest.raises(gpu.JxsError):
         gpu.Decoder(c["bs"], proxy_mode=2)
+
+
+@pytest.mark.parametrize("name", sorted(G.sign_cases()))
+def test_separate_signs_golden_decode(gpu, name):
+    """Codestreams with separate sign sub-packets (the reference encoder's
+    coding_signs_handling 1 and 2, one with vertical prediction too):
+    decoded bit-exact with the reference decoder, per frame and batched."""
+    c = G.sign_cases()[name]
+    dec = gpu.Decoder(c["bs"])
+    out = dec.decode(c["bs"])
+    assert all(np.array_equal(a, b) for a, b in zip(out, c["dec"])), name
+    if c["params"][13] == 0:
+        batch = gpu.Batch(1 << 28)
+        planes = [dec.alloc_planes()]
+        assert batch.decode([dec], [c["bs"]], planes) == 0
+        r, st = batch.wait()
+        assert r == 0 and all(np.array_equal(a, b) for a, b in zip(planes[0], c["dec"])), name
+        batch.close()
+    dec.close()
