@@ -570,7 +570,6 @@ static int enc_configure(enc_t* e, const or_enc_params_t* p) {
     if (mw == 0 || mh == 0) return E_BAD_PARAM;
     /* This restatement covers vertical prediction off and signs off. */
     if (c->coding_vertical_prediction_mode != 0 || c->coding_signs_handling != 0) return E_BAD_PARAM;
-    if (c->rate_control_mode > 1) return E_BAD_PARAM;
     int r = geom_compute(&e->g, 1, nc, c->width, c->height, c->decomp_h, c->decomp_v, 0, sx, sy, c->slice_height);
     if (r) return r;
     if (weights_assign(&e->g, c->colour_format)) return E_BAD_PARAM;
@@ -1058,8 +1057,132 @@ typedef struct {
     enc_t* e;
 } slice_job_t;
 
-/* pack_stage_kernel for RC modes 0 and 1 (PackStageProcess.c:567-749,
- * process_precinct :274-338). */
+/* Precinct header + packet header bytes (rate_control_get_headers_bytes,
+ * RateControl.c:258-272). */
+static uint32_t prec_hdr_bytes(const geom_t* g, int last) {
+    return DIV_UP(5 * 8 + g->nbands_exist * 2, 8) + DIV_UP((g->short_hdr ? 40 : 56) * g->pk_exist[last], 8);
+}
+
+/* RC modes 2 and 3, per-slice common quantization: the budget of each
+ * precinct of the slice (process_slice, PackStageProcess.c:339-483;
+ * rate_control_slice_quantization_fast_no_vpred_no_sign_full,
+ * RateControl.c:1336-1425, with its binary searches :1086-1209).  One
+ * (Q, R) for the whole slice by the same searches as a precinct's, on the
+ * summed data bytes; the last precinct takes the remaining bytes; mode 3
+ * raises every precinct to a quarter of the largest; then 10 % of the first
+ * precinct's budget and an even share of what is left move out of the last
+ * precinct's padding. */
+static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec, uint32_t slice_budget, uint32_t* total) {
+    const geom_t* g = &e->g;
+    if (DIV_UP(slice_budget, nprec) > PREC_MAX_BYTES) return E_ENC_FRAME;
+    prec_stats_t* st = (prec_stats_t*)malloc(sizeof(prec_stats_t) * nprec);
+    prec_cost_t pc;
+    if (!st) return E_RESOURCES;
+    uint32_t headers = 0;
+    for (uint32_t i = 0; i < nprec; i++) {
+        const int last = first_p + i + 1 >= g->np;
+        prec_stats(e, first_p + i, last, &st[i]);
+        total[i] = prec_hdr_bytes(g, last);
+        headers += total[i];
+    }
+    if (slice_budget <= headers) {
+        free(st);
+        return E_UNDEFINED;
+    }
+    const uint32_t avail = slice_budget - headers;
+    bsearch_t s;
+    uint32_t step = 6;
+    if (step > e->max_q) step = 0;
+    bs_init(&s, 0, e->max_q, 0, step);
+    int res, next = BS_BEGIN;
+    uint32_t qv = 0;
+    while ((res = bs_next(&s, next, &qv)) == BS_CONTINUE) {
+        if (all_truncated(g, (uint8_t)qv, 0)) { next = BS_OUT_OF_RANGE; continue; }
+        uint32_t sum = 0;
+        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, (uint8_t)qv, 0, &pc);
+        next = sum > avail ? BS_TOO_SMALL : BS_TOO_BIG;
+    }
+    if (res != BS_FOUND) {
+        free(st);
+        return E_ENC_FRAME;
+    }
+    const uint8_t q = (uint8_t)qv;
+    step = 6;
+    if (step >= e->max_r) step = 0;
+    bs_init(&s, 0, e->max_r, 1, step);
+    next = BS_BEGIN;
+    uint32_t rv = 0;
+    while ((res = bs_next(&s, next, &rv)) == BS_CONTINUE) {
+        if (all_truncated(g, q, (uint8_t)rv)) { next = BS_OUT_OF_RANGE; continue; }
+        uint32_t sum = 0;
+        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc);
+        next = sum <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
+    }
+    if (res != BS_FOUND) {
+        free(st);
+        return E_ENC_FRAME;
+    }
+    uint32_t pad_last = avail;
+    for (uint32_t i = 0; i < nprec; i++) {
+        const uint32_t d = prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc);
+        pad_last -= d;
+        total[i] += d;
+    }
+    free(st);
+    total[nprec - 1] += pad_last;
+    if (e->prm.rate_control_mode == 3) {
+        /* RC_CBR_PER_SLICE_COMMON_QUANT_MAX_RATE: no precinct below a quarter
+         * of the largest (padding excluded) */
+        uint32_t max_size = 0;
+        for (uint32_t i = 0; i < nprec; i++) {
+            const uint32_t ds = total[i] - (i + 1 == nprec ? pad_last : 0);
+            if (ds > max_size) max_size = ds;
+        }
+        const uint32_t min_size = max_size / 4;
+        uint32_t need = 0;
+        for (uint32_t i = 0; i < nprec; i++) {
+            const uint32_t ds = total[i] - (i + 1 == nprec ? pad_last : 0);
+            if (ds < min_size) {
+                total[i] += min_size - ds;
+                need += min_size - ds;
+            }
+        }
+        if (need) {
+            if (pad_last >= need) {
+                pad_last -= need;
+                total[nprec - 1] -= need;
+            } else {
+                need -= pad_last;
+                total[nprec - 1] -= pad_last;
+                pad_last = 0;
+                while (need)
+                    for (uint32_t i = 0; i < nprec && need; i++) {
+                        need--;
+                        total[i]--;
+                    }
+            }
+        }
+    }
+    if (pad_last > 0) {
+        uint32_t add_first = total[0] * 10 / 100;
+        if (add_first > pad_last) add_first = pad_last;
+        pad_last -= add_first;
+        total[nprec - 1] -= add_first;
+        total[0] += add_first;
+        if (pad_last) {
+            total[nprec - 1] -= pad_last;
+            const uint32_t each = pad_last / nprec, extra = pad_last - each * nprec;
+            for (uint32_t i = 0; i < nprec; i++) total[i] += each + (i < extra ? 1 : 0);
+        }
+    }
+    return E_NONE;
+}
+
+/* pack_stage_kernel (PackStageProcess.c:567-749): RC modes 0 and 1
+ * (process_precinct :274-338) split the slice evenly (mode 1: the first
+ * precinct 10 % more); modes 2 and 3 (process_slice :339-565) split it by a
+ * slice-wide quantization.  Then each precinct's own search, with padding
+ * moved to the next precinct in modes 1-3. */
 static void enc_slice(void* ctx, uint32_t s) {
     enc_t* e = ((slice_job_t*)ctx)->e;
     const geom_t* g = &e->g;
@@ -1082,6 +1205,16 @@ static void enc_slice(void* ctx, uint32_t s) {
             left = 0;
         }
     }
+    uint32_t* common = NULL;
+    if (e->prm.rate_control_mode >= 2) {
+        common = (uint32_t*)malloc(sizeof(uint32_t) * nprec);
+        int err = common ? slice_common_budgets(e, first_p, nprec, slice_budget, common) : E_RESOURCES;
+        if (err) {
+            free(common);
+            e->slice_err = err;
+            return;
+        }
+    }
     bw_t w = {e->out + begin, 0};
     uint32_t carry = 0;
     prec_stats_t st;
@@ -1089,18 +1222,20 @@ static void enc_slice(void* ctx, uint32_t s) {
     for (uint32_t i = 0; i < nprec; i++) {
         uint32_t p = first_p + i;
         int last = (p + 1 >= g->np);
-        uint32_t budget = (i == 0 ? first_b : min_b) + (i < left ? 1 : 0) + carry;
+        uint32_t budget = (common ? common[i] : (i == 0 ? first_b : min_b) + (i < left ? 1 : 0)) + carry;
         prec_stats(e, p, last, &st);
         uint8_t q = 0, r = 0;
         uint32_t data = 0, hdr = 0;
         int err = prec_rc(e, &st, last, budget, &q, &r, &data, &hdr, &pc);
         if (err) {
+            free(common);
             e->slice_err = err;
             return;
         }
         uint32_t padding = budget - hdr - data;
         uint32_t total = budget;
-        if (e->prm.rate_control_mode == 1 && i + 1 < nprec) {
+        /* modes 1-3 move a precinct's padding to the next one */
+        if (e->prm.rate_control_mode >= 1 && i + 1 < nprec) {
             total -= padding;
             carry = padding;
             padding = 0;
@@ -1118,6 +1253,7 @@ static void enc_slice(void* ctx, uint32_t s) {
         for (uint64_t z = used; z < total; z++) bw_put(&w, 0, 8);
     }
     if (last_slice) bw_put(&w, 0xff11, 16); /* EOC */
+    free(common);
 }
 
 static void enc_free(enc_t* e) {

@@ -99,6 +99,115 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
     const int nq = cfg->max_q + 1, nr = cfg->max_r + 1, nt = nq * nr;
     const int max_q = cfg->max_q, max_r = cfg->max_r, rc_mode = (int)cfg->rc_mode;
     const uint32_t np_all = cfg->np, hdrs0 = cfg->hdrs_bytes[0], hdrs1 = cfg->hdrs_bytes[1];
+    if (rc_mode >= 2) {
+        /* RC modes 2 and 3, per-slice common quantization (process_slice,
+         * PackStageProcess.c:339-483; RateControl.c:1086-1209, 1336-1425):
+         * the data bytes of every (Q, R) summed over the slice's precincts,
+         * one (Q, R) for the slice by the precinct searches, then the budget
+         * of each precinct; kept in rc[p].total_bytes for the loop below */
+        __syncthreads();
+        for (int e = threadIdx.x; e < nt; e += blockDim.x) {
+            const int q = e / nr, r = e - q * nr;
+            uint32_t sum = 0;
+            for (uint32_t i = 0; i < nprec; i++) sum += __ldcg(cost + (uint64_t)(first_p + i) * 1024 + q * 32 + r);
+            area[e] = sum;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            int err = 0;
+            uint32_t headers = 0;
+            for (uint32_t i = 0; i < nprec; i++) headers += first_p + i + 1 >= np_all ? hdrs1 : hdrs0;
+            if ((slice_budget + nprec - 1) / nprec > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
+            else if (slice_budget <= headers) err = JXS_E_UNDEFINED;
+            int q = 0, r = 0;
+            if (!err) {
+                const uint32_t avail = slice_budget - headers;
+                BSearch bs;
+                int step = 6;
+                if (step > max_q) step = 0;
+                bs_init(bs, 0, max_q, 0, step);
+                int res, next = BS_BEGIN, v = 0;
+                while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
+                    if (s_empty[v] & 1u) next = BS_OUT_OF_RANGE;
+                    else next = area[v * nr] > avail ? BS_TOO_SMALL : BS_TOO_BIG;
+                }
+                if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
+                q = v;
+                if (!err) {
+                    step = 6;
+                    if (step >= max_r) step = 0;
+                    bs_init(bs, 0, max_r, 1, step);
+                    next = BS_BEGIN;
+                    while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
+                        if ((s_empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
+                        else next = area[q * nr + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
+                    }
+                    if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
+                    r = v;
+                }
+                if (!err) {
+                    /* each precinct its headers and data at (Q, R); the last
+                     * also the slice's remaining bytes */
+                    uint32_t pad_last = avail;
+                    for (uint32_t i = 0; i < nprec; i++) {
+                        const uint32_t p = first_p + i;
+                        const uint32_t d = __ldcg(cost + (uint64_t)p * 1024 + q * 32 + r);
+                        pad_last -= d;
+                        rc[p].total_bytes = (p + 1 >= np_all ? hdrs1 : hdrs0) + d;
+                    }
+                    rc[first_p + nprec - 1].total_bytes += pad_last;
+                    if (rc_mode == 3) {
+                        /* RC_CBR_PER_SLICE_COMMON_QUANT_MAX_RATE: no precinct
+                         * below a quarter of the largest, padding excluded */
+                        uint32_t max_size = 0;
+                        for (uint32_t i = 0; i < nprec; i++)
+                            max_size = max(max_size, rc[first_p + i].total_bytes - (i + 1 == nprec ? pad_last : 0u));
+                        const uint32_t min_size = max_size / 4;
+                        uint32_t need = 0;
+                        for (uint32_t i = 0; i < nprec; i++) {
+                            const uint32_t ds = rc[first_p + i].total_bytes - (i + 1 == nprec ? pad_last : 0u);
+                            if (ds < min_size) {
+                                rc[first_p + i].total_bytes += min_size - ds;
+                                need += min_size - ds;
+                            }
+                        }
+                        if (need) {
+                            if (pad_last >= need) {
+                                pad_last -= need;
+                                rc[first_p + nprec - 1].total_bytes -= need;
+                            } else {
+                                need -= pad_last;
+                                rc[first_p + nprec - 1].total_bytes -= pad_last;
+                                pad_last = 0;
+                                /* the rest one byte at a time, round robin */
+                                const uint32_t each = need / nprec, extra = need - each * nprec;
+                                for (uint32_t i = 0; i < nprec; i++) rc[first_p + i].total_bytes -= each + (i < extra ? 1u : 0u);
+                            }
+                        }
+                    }
+                    if (pad_last > 0) {
+                        /* the first precinct 10 % more, the rest of the padding
+                         * shared evenly */
+                        uint32_t add_first = rc[first_p].total_bytes * 10 / 100;
+                        if (add_first > pad_last) add_first = pad_last;
+                        pad_last -= add_first;
+                        rc[first_p + nprec - 1].total_bytes -= add_first;
+                        rc[first_p].total_bytes += add_first;
+                        if (pad_last) {
+                            rc[first_p + nprec - 1].total_bytes -= pad_last;
+                            const uint32_t each = pad_last / nprec, extra = pad_last - each * nprec;
+                            for (uint32_t i = 0; i < nprec; i++) rc[first_p + i].total_bytes += each + (i < extra ? 1u : 0u);
+                        }
+                    }
+                }
+            }
+            if (err) {
+                printf("jxs rc: slice %d (common quantization): error 0x%x\n", s, (unsigned)err);
+                s_err = err;
+                JXS_STATUS_SET(status, err);
+            }
+        }
+    }
     const uint32_t chunk = area_words / (uint32_t)nt;
     for (uint32_t c0 = 0; c0 < nprec; c0 += chunk) {
         const uint32_t cnt = min(chunk, nprec - c0);
@@ -115,7 +224,8 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
                 const uint32_t p = first_p + i;
                 const uint32_t* T = area + ii * nt;
                 const int last = (p + 1 >= np_all);
-                const uint32_t budget = (i == 0 ? first_b : min_b) + (i < left ? 1 : 0) + s_carry;
+                const uint32_t budget =
+                    (rc_mode >= 2 ? rc[p].total_bytes : (i == 0 ? first_b : min_b) + (i < left ? 1 : 0)) + s_carry;
                 const uint32_t hdr = last ? hdrs1 : hdrs0;
                 int err = 0;
                 if (budget > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
@@ -151,7 +261,7 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
                     if (!err) {
                         uint32_t padding = avail - data;
                         uint32_t total = budget;
-                        if (rc_mode == 1 && i + 1 < nprec) {
+                        if (rc_mode >= 1 && i + 1 < nprec) {
                             total -= padding;
                             s_carry = padding;
                         } else {

@@ -394,3 +394,39 @@ def test_separate_signs_golden_decode(gpu, name):
         assert r == 0 and all(np.array_equal(a, b) for a, b in zip(planes[0], c["dec"])), name
         batch.close()
     dec.close()
+
+
+def _rc_mode_cases(n, seed):
+    out = []
+    for c in _random_cases(n, seed):
+        c = dict(c)
+        c["rc"] = 2 + (c["seed"] % 2)
+        out.append(c)
+    return out
+
+
+@pytest.mark.parametrize("c", _rc_mode_cases(40, 91), ids=lambda c: "rc%d_%dx%d_d%d_f%d_V%dH%d_sl%d" % (
+    c["rc"], c["w"], c["h"], c["d"], c["fmt"], c["v"], c["hh"], c["sl"]))
+def test_rc_modes_2_3_against_oracle(gpu, oracle, c):
+    """Rate-control modes 2 and 3 (per-slice common quantization, and its
+    max-rate variant): codestreams and per-precinct (Q, R) byte-exact with
+    the oracle, which matches the reference encoder on these modes."""
+    planes = S.frame(c["w"], c["h"], c["d"], c["fmt"], seed=c["seed"])
+    p = oracle.make_params(c["w"], c["h"], c["d"], c["fmt"], c["bpp_num"], c["bpp_den"], c["v"], c["hh"], quantization=c["q"],
+                           slice_height=c["sl"], significance=c["sig"], rc_mode=c["rc"])
+    err, ref_bs, ref_q, ref_r = oracle.oracle_encode(p, planes, want_qr=True)
+    if err == 0x80001005:
+        with pytest.raises(gpu.JxsError):
+            make_encoder(gpu, c)
+        return
+    enc = make_encoder(gpu, c)
+    out = np.zeros(enc.frame_bytes + 64, np.uint8)
+    assert enc.send(planes, out) == 0
+    q, r = enc.rc_results()
+    rc, f = enc.get()
+    enc.close()
+    assert rc == err
+    if err:
+        return
+    assert np.array_equal(q, ref_q) and np.array_equal(r, ref_r)
+    assert np.array_equal(out[: f.bitstream.used_size], ref_bs)

@@ -119,3 +119,31 @@ def test_oracle_vertical_prediction_fixtures(oracle):
         err, planes = oracle.oracle_decode(c["bs"])
         assert err == 0, name
         assert all(np.array_equal(a, b) for a, b in zip(planes, c["dec"])), name
+
+
+def _rc_mode_cases(n, seed):
+    """Random configurations under rate-control modes 2 and 3 (per-slice
+    common quantization, and its max-rate variant)."""
+    out = []
+    for c in _random_cases(n, seed):
+        c = dict(c)
+        c["rc"] = 2 + (c["seed"] % 2)
+        out.append(c)
+    return out
+
+
+@pytest.mark.parametrize("case", _rc_mode_cases(80, 2025), ids=lambda c: "rc%d_%dx%d_d%d_f%d_V%dH%d_sl%d" % (
+    c["rc"], c["w"], c["h"], c["d"], c["fmt"], c["v"], c["hh"], c["sl"]))
+def test_oracle_rc_modes_2_3_match_reference(oracle, case):
+    if not oracle.ref_available():
+        pytest.skip("reference library not built here (needs the reference sources)")
+    c = case
+    planes = S.frame(c["w"], c["h"], c["d"], c["fmt"], seed=c["seed"])
+    p = oracle.make_params(c["w"], c["h"], c["d"], c["fmt"], c["bpp"], c["den"], c["v"], c["hh"], quantization=c["q"],
+                           slice_height=c["sl"], significance=c["sig"], rc_mode=c["rc"])
+    e_ref, b_ref = oracle.ref_encode(p, planes)
+    e_or, b_or = oracle.oracle_encode(p, planes)
+    assert e_ref == e_or
+    if e_ref:
+        return
+    assert np.array_equal(b_ref, b_or)
