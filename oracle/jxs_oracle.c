@@ -568,8 +568,8 @@ static int enc_configure(enc_t* e, const or_enc_params_t* p) {
         else { mh = 0; break; }
     }
     if (mw == 0 || mh == 0) return E_BAD_PARAM;
-    /* This restatement covers vertical prediction off and signs off. */
-    if (c->coding_vertical_prediction_mode != 0 || c->coding_signs_handling != 0) return E_BAD_PARAM;
+    /* This restatement covers the encoder with vertical prediction off. */
+    if (c->coding_vertical_prediction_mode != 0) return E_BAD_PARAM;
     int r = geom_compute(&e->g, 1, nc, c->width, c->height, c->decomp_h, c->decomp_v, 0, sx, sy, c->slice_height);
     if (r) return r;
     if (weights_assign(&e->g, c->colour_format)) return E_BAD_PARAM;
@@ -637,7 +637,7 @@ static void enc_write_header(enc_t* e) {
     bw_put(&w, !g->short_hdr, 1);              /* Lh */
     bw_put(&w, 1, 1);                          /* Rl */
     bw_put(&w, e->prm.quantization, 2);        /* Qpih */
-    bw_put(&w, 0, 2);                          /* Fs */
+    bw_put(&w, e->prm.coding_signs_handling ? 1 : 0, 2); /* Fs */
     bw_put(&w, 0, 2);                          /* Rm */
     bw_put(&w, 0xff13, 16);                    /* CDT */
     bw_put(&w, 2 * g->nc + 2, 16);
@@ -750,6 +750,9 @@ typedef struct {
     uint32_t hist[MAXC][MAXB][2][16];
     uint32_t sighist[MAXC][MAXB][2][16];
     int partial_max[MAXC][MAXB][2]; /* max of the trailing partial significance group, -1 if none */
+    /* sign handling: per band line, coefficients by the number of gtli values
+     * (0, 1, ...) at which their quantized value is non-zero */
+    uint32_t nzhist[MAXC][MAXB][2][17];
     uint32_t lines[MAXC][MAXB];
 } prec_stats_t;
 
@@ -758,9 +761,29 @@ typedef struct {
     uint8_t sig_method[MAXC][MAXB];
     uint32_t data_bits[MAXC][MAXB][2], gcli_bits[MAXC][MAXB][2], sig_bits[MAXC][MAXB][2];
     uint8_t raw[MAXPK];
-    uint32_t pk_data[MAXPK], pk_gcli[MAXPK], pk_sig[MAXPK];
+    uint32_t pk_data[MAXPK], pk_gcli[MAXPK], pk_sig[MAXPK], pk_sign[MAXPK];
     uint32_t total;
 } prec_cost_t;
+
+enum { SIGNS_OFF = 0, SIGNS_FAST = 1, SIGNS_FULL = 2 };
+
+/* Number of gtli values t (from 0 up) at which a coefficient of magnitude m
+ * in a group with GCLI g stays non-zero after quantization: deadzone keeps
+ * m >> t (rate_control_lut_fill, RateControl.c:124-137, counts bits(m));
+ * uniform keeps ((m << (g - t + 1)) - m + 2^g) >> (g + 1)
+ * (rate_control_sign_coding_get_sum_nonzero_coeff_c, RateControl.c:366-455),
+ * which falls as t grows. */
+static uint32_t nz_levels(uint32_t m, uint32_t g, uint32_t uniform) {
+    if (!m) return 0;
+    if (!uniform) {
+        uint32_t n = 0;
+        while (m >> n) n++;
+        return n;
+    }
+    uint32_t n = 0;
+    while (n < g && (((m << (g - n + 1)) - m + (1u << g)) >> (g + 1)) != 0) n++;
+    return n;
+}
 
 static void prec_stats(const enc_t* e, uint32_t p, int last, prec_stats_t* st) {
     const geom_t* g = &e->g;
@@ -778,15 +801,24 @@ static void prec_stats(const enc_t* e, uint32_t p, int last, prec_stats_t* st) {
                 uint32_t full = bd->gcli_w / 8;
                 for (uint32_t i = 0; i < full; i++) st->sighist[c][b][l][sm[i]]++;
                 st->partial_max[c][b][l] = (full < bd->sig_w) ? sm[full] : -1;
+                if (e->prm.coding_signs_handling) {
+                    const uint16_t* cf = e->coef[c][b] + (size_t)row * bd->w;
+                    for (uint32_t i = 0; i < bd->w; i++)
+                        st->nzhist[c][b][l][nz_levels(cf[i] & 0x7fffu, gl[i / 4], e->prm.quantization)]++;
+                }
             }
         }
 }
 
 /* precinct_get_budget_bytes + rate_control_calculate_band_best_method
  * (RateControl.c:457-781) for one (quantization, refinement), no vertical
- * prediction and no sign handling. */
-static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint8_t q, uint8_t r, prec_cost_t* pc) {
+ * prediction.  With sign handling the data bits leave out the sign nibbles
+ * and each packet adds a sign sub-packet: SIGNS_FAST counts every
+ * coefficient of a group above gtli, SIGNS_FULL only those that stay
+ * non-zero (RateControl.c:505-523). */
+static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint8_t q, uint8_t r, prec_cost_t* pc, int smode) {
     const geom_t* g = &e->g;
+    uint32_t sign_bits[MAXC][MAXB][2];
     for (uint32_t c = 0; c < g->nc; c++)
         for (uint32_t b = 0; b < g->c[c].nb; b++) {
             const band_t* bd = &g->c[c].b[b];
@@ -797,12 +829,22 @@ static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint
             uint32_t nosig[2], total_nosig = 0, total_sig = bd->sig_w * lines, gsig[2];
             for (uint32_t l = 0; l < lines; l++) {
                 const uint32_t* h = st->hist[c][b][l];
-                uint32_t data = 0, zero = 0;
+                uint32_t data = 0, zero = 0, above = 0;
                 for (uint32_t v = 0; v <= TRUNC_MAX; v++) {
-                    if (v > t) data += (v - t + 1) * h[v];
-                    else zero += h[v];
+                    if (v > t) {
+                        data += (v - t + 1) * h[v];
+                        above += h[v];
+                    } else {
+                        zero += h[v];
+                    }
                 }
-                pc->data_bits[c][b][l] = data * 4;
+                pc->data_bits[c][b][l] = (data - (smode ? above : 0)) * 4;
+                sign_bits[c][b][l] = 0;
+                if (smode == SIGNS_FAST) {
+                    sign_bits[c][b][l] = 4 * above;
+                } else if (smode == SIGNS_FULL) {
+                    for (uint32_t n = t + 1; n <= 16; n++) sign_bits[c][b][l] += st->nzhist[c][b][l][n];
+                }
                 nosig[l] = data + zero;
                 total_nosig += nosig[l];
                 uint32_t zeroed = 0;
@@ -822,18 +864,20 @@ static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint
         }
     uint32_t total = 0;
     for (uint32_t k = 0; k < g->npk; k++) {
-        uint32_t db = 0, gb = 0, sb = 0;
+        uint32_t db = 0, gb = 0, sb = 0, nb = 0;
         for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
             uint32_t c = g->gcomp[i], b = g->gband[i], l = g->pk[k].line;
             if (l < st->lines[c][b]) {
                 db += pc->data_bits[c][b][l];
                 gb += pc->gcli_bits[c][b][l];
                 sb += pc->sig_bits[c][b][l];
+                nb += sign_bits[c][b][l];
             }
         }
         uint32_t dB = DIV_UP(db, 8), gB = DIV_UP(gb, 8), sB = DIV_UP(sb, 8);
         pc->pk_data[k] = dB;
-        total += dB;
+        pc->pk_sign[k] = DIV_UP(nb, 8);
+        total += dB + pc->pk_sign[k];
         if (sB + gB > g->raw_bytes[last][k]) {
             pc->raw[k] = 1;
             pc->pk_sig[k] = 0;
@@ -897,6 +941,10 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
     uint32_t avail = budget - hdr;
     *hdr_bytes = hdr;
 
+    /* the quantization search counts signs the fast way; SIGNS_FULL then
+     * steps from its result with exact sign counts (RateControl.c:909-1015) */
+    const int smode = (int)e->prm.coding_signs_handling;
+    const int sfast = smode == SIGNS_FULL ? SIGNS_FAST : smode;
     bsearch_t s;
     uint32_t step = 6;
     if (step > e->max_q) step = 0;
@@ -905,10 +953,26 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
     uint32_t qv = 0;
     while ((res = bs_next(&s, next, &qv)) == BS_CONTINUE) {
         if (all_truncated(g, (uint8_t)qv, 0)) { next = BS_OUT_OF_RANGE; continue; }
-        next = prec_cost(e, st, last, (uint8_t)qv, 0, pc) > avail ? BS_TOO_SMALL : BS_TOO_BIG;
+        next = prec_cost(e, st, last, (uint8_t)qv, 0, pc, sfast) > avail ? BS_TOO_SMALL : BS_TOO_BIG;
     }
     if (res != BS_FOUND) return E_ENC_FRAME;
     uint8_t q = (uint8_t)qv;
+    if (smode == SIGNS_FULL) {
+        /* lower quantizations while they fit, else the first higher that fits */
+        int best = -1;
+        for (int qt = (int)q - 1; qt >= 0; qt--) {
+            if (all_truncated(g, (uint8_t)qt, 0) || prec_cost(e, st, last, (uint8_t)qt, 0, pc, smode) > avail) break;
+            best = qt;
+        }
+        if (best < 0)
+            for (uint32_t qt = q; qt <= e->max_q; qt++)
+                if (!all_truncated(g, (uint8_t)qt, 0) && prec_cost(e, st, last, (uint8_t)qt, 0, pc, smode) <= avail) {
+                    best = (int)qt;
+                    break;
+                }
+        if (best < 0) return E_ENC_FRAME;
+        q = (uint8_t)best;
+    }
 
     step = 6;
     if (step >= e->max_r) step = 0;
@@ -920,7 +984,7 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
     while ((res = bs_next(&s, next, &rv)) == BS_CONTINUE) {
         last_tested = -1;
         if (all_truncated(g, q, (uint8_t)rv)) { next = BS_OUT_OF_RANGE; continue; }
-        uint32_t cst = prec_cost(e, st, last, q, (uint8_t)rv, pc);
+        uint32_t cst = prec_cost(e, st, last, q, (uint8_t)rv, pc, smode);
         last_tested = (int32_t)rv;
         last_cost = cst;
         next = cst <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
@@ -929,7 +993,7 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
     (void)last_tested;
     (void)last_cost;
     /* The pack step needs the per-packet decisions of the chosen pair. */
-    *data_bytes = prec_cost(e, st, last, q, (uint8_t)rv, pc);
+    *data_bytes = prec_cost(e, st, last, q, (uint8_t)rv, pc, smode);
     *q_out = q;
     *r_out = (uint8_t)rv;
     return E_NONE;
@@ -952,8 +1016,12 @@ static inline uint16_t quantize(uint16_t v, uint8_t gcli, uint8_t t, uint32_t un
 }
 
 /* pack_precinct (Source/Lib/Encoder/Codec/PackPrecinct.c:235-572), vertical
- * prediction and sign handling off. */
-static void prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc, uint8_t q, uint8_t r, uint32_t total_bytes,
+ * prediction off.  With sign handling the data sub-packet carries no sign
+ * nibbles and a sign sub-packet follows it: one bit per non-zero quantized
+ * coefficient of the groups above gtli (pack_sign_c, :200-233).  Returns
+ * non-zero when a sign sub-packet differs from the size the rate control
+ * computed. */
+static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc, uint8_t q, uint8_t r, uint32_t total_bytes,
                       bw_t* w) {
     const geom_t* g = &e->g;
     uint32_t hdr_len = DIV_UP(5 * 8 + 2 * g->nbands_exist, 8);
@@ -968,6 +1036,7 @@ static void prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* p
     }
     bw_align(w);
     const uint32_t uniform = e->prm.quantization;
+    const int signs_sep = e->prm.coding_signs_handling != 0;
     uint16_t qbuf[4];
     for (uint32_t k = 0; k < g->npk; k++) {
         const uint32_t l = g->pk[k].line;
@@ -982,12 +1051,12 @@ static void prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* p
             bw_put(w, pc->raw[k], 1);
             bw_put(w, pc->pk_data[k], 15);
             bw_put(w, pc->pk_gcli[k], 13);
-            bw_put(w, 0, 11);
+            bw_put(w, pc->pk_sign[k], 11);
         } else {
             bw_put(w, pc->raw[k], 1);
             bw_put(w, pc->pk_data[k], 20);
             bw_put(w, pc->pk_gcli[k], 20);
-            bw_put(w, 0, 15);
+            bw_put(w, pc->pk_sign[k], 15);
         }
         if (pc->raw[k]) {
             for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
@@ -1023,7 +1092,7 @@ static void prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* p
             }
             bw_align(w);
         }
-        /* data sub-packet: pack_data_c (PackPrecinct.c:128-198), sign_flag 0 */
+        /* data sub-packet: pack_data_c (PackPrecinct.c:128-198) */
         for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
             uint32_t c = g->gcomp[i], b = g->gband[i];
             const band_t* bd = &g->c[c].b[b];
@@ -1041,7 +1110,7 @@ static void prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* p
                 }
                 uint32_t signs = 0;
                 for (uint32_t k2 = 0; k2 < 4; k2++) signs = (signs << 1) | (qbuf[k2] >> 15);
-                bw_put(w, signs, 4);
+                if (!signs_sep) bw_put(w, signs, 4);
                 for (int bit = gl[x] - 1; bit >= t; bit--) {
                     uint32_t nib = 0;
                     for (uint32_t k2 = 0; k2 < 4; k2++) nib = (nib << 1) | ((qbuf[k2] >> bit) & 1u);
@@ -1050,7 +1119,31 @@ static void prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* p
             }
         }
         bw_align(w);
+        if (!signs_sep) continue;
+        /* sign sub-packet: pack_sign_c (PackPrecinct.c:200-233) */
+        uint32_t nbits = 0;
+        for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
+            uint32_t c = g->gcomp[i], b = g->gband[i];
+            const band_t* bd = &g->c[c].b[b];
+            if (l >= (last ? bd->last_lines : bd->lines)) continue;
+            const uint8_t t = pc->gtli[c][b];
+            const size_t row = (size_t)(p * bd->lines + l);
+            const uint8_t* gl = e->gcli[c][b] + row * bd->gcli_w;
+            const uint16_t* cf = e->coef[c][b] + row * bd->w;
+            for (uint32_t xi = 0; xi < bd->w; xi++) {
+                const uint8_t gv = gl[xi / 4];
+                if (gv <= t) continue;
+                const uint16_t qv = t ? quantize(cf[xi], gv, t, uniform) : cf[xi];
+                if (qv) {
+                    bw_put(w, qv >> 15, 1);
+                    nbits++;
+                }
+            }
+        }
+        bw_align(w);
+        if (DIV_UP(nbits, 8) != pc->pk_sign[k]) return E_ENC_FRAME;
     }
+    return E_NONE;
 }
 
 typedef struct {
@@ -1077,6 +1170,8 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     if (DIV_UP(slice_budget, nprec) > PREC_MAX_BYTES) return E_ENC_FRAME;
     prec_stats_t* st = (prec_stats_t*)malloc(sizeof(prec_stats_t) * nprec);
     prec_cost_t pc;
+    /* signs counted the fast way for the whole slice (RateControl.c:1341-1343) */
+    const int sfast = e->prm.coding_signs_handling ? SIGNS_FAST : SIGNS_OFF;
     if (!st) return E_RESOURCES;
     uint32_t headers = 0;
     for (uint32_t i = 0; i < nprec; i++) {
@@ -1099,7 +1194,7 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     while ((res = bs_next(&s, next, &qv)) == BS_CONTINUE) {
         if (all_truncated(g, (uint8_t)qv, 0)) { next = BS_OUT_OF_RANGE; continue; }
         uint32_t sum = 0;
-        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, (uint8_t)qv, 0, &pc);
+        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, (uint8_t)qv, 0, &pc, sfast);
         next = sum > avail ? BS_TOO_SMALL : BS_TOO_BIG;
     }
     if (res != BS_FOUND) {
@@ -1115,7 +1210,7 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     while ((res = bs_next(&s, next, &rv)) == BS_CONTINUE) {
         if (all_truncated(g, q, (uint8_t)rv)) { next = BS_OUT_OF_RANGE; continue; }
         uint32_t sum = 0;
-        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc);
+        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc, sfast);
         next = sum <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
     }
     if (res != BS_FOUND) {
@@ -1124,7 +1219,7 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     }
     uint32_t pad_last = avail;
     for (uint32_t i = 0; i < nprec; i++) {
-        const uint32_t d = prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc);
+        const uint32_t d = prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc, sfast);
         pad_last -= d;
         total[i] += d;
     }
@@ -1164,7 +1259,8 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
         }
     }
     if (pad_last > 0) {
-        uint32_t add_first = total[0] * 10 / 100;
+        /* 20 % with fast signs, else 10 % (PackStageProcess.c:34-35, 432-446) */
+        uint32_t add_first = total[0] * (e->prm.coding_signs_handling == SIGNS_FAST ? 20 : 10) / 100;
         if (add_first > pad_last) add_first = pad_last;
         pad_last -= add_first;
         total[nprec - 1] -= add_first;
@@ -1196,7 +1292,8 @@ static void enc_slice(void* ctx, uint32_t s) {
     uint32_t left = slice_budget - min_b * nprec;
     uint32_t first_b = min_b;
     if (e->prm.rate_control_mode == 1) {
-        first_b = first_b * 110 / 100;
+        /* 20 % more with fast signs, else 10 % (PackStageProcess.c:34-35, 614-622) */
+        first_b = first_b * (e->prm.coding_signs_handling == SIGNS_FAST ? 120 : 110) / 100;
         first_b = MIN(slice_budget, first_b);
         if (nprec > 1) {
             min_b = (slice_budget - first_b) / (nprec - 1);
@@ -1234,10 +1331,18 @@ static void enc_slice(void* ctx, uint32_t s) {
         }
         uint32_t padding = budget - hdr - data;
         uint32_t total = budget;
+        /* fast signs: the sign sub-packets shrink to the signs actually sent;
+         * the bytes they free (PackPrecinct.c:513-536) are cut from the
+         * precinct with its padding, or left as padding in the slice's last
+         * precinct and in mode 0 (PackStageProcess.c:293-333) */
+        uint32_t retrieve = 0;
+        if (e->prm.coding_signs_handling == SIGNS_FAST) {
+            retrieve = data - prec_cost(e, &st, last, q, r, &pc, SIGNS_FULL);
+        }
         /* modes 1-3 move a precinct's padding to the next one */
         if (e->prm.rate_control_mode >= 1 && i + 1 < nprec) {
-            total -= padding;
-            carry = padding;
+            total -= padding + retrieve;
+            carry = padding + retrieve;
             padding = 0;
         }
         if (e->q_out) e->q_out[p] = q;
@@ -1248,7 +1353,11 @@ static void enc_slice(void* ctx, uint32_t s) {
             bw_put(&w, s, 16);
         }
         uint64_t start = w.bit;
-        prec_pack(e, p, last, &pc, q, r, total, &w);
+        if (prec_pack(e, p, last, &pc, q, r, total, &w) || ((w.bit - start) >> 3) != hdr + data - retrieve) {
+            free(common);
+            e->slice_err = E_ENC_FRAME;
+            return;
+        }
         uint64_t used = (w.bit - start) >> 3;
         for (uint64_t z = used; z < total; z++) bw_put(&w, 0, 8);
     }
@@ -1578,8 +1687,8 @@ static int decode_vpred_line(br_t* r, int64_t* left, uint8_t* gl, const uint8_t*
     return E_NONE;
 }
 
-/* unpack_precinct (Source/Lib/Decoder/Codec/Packing.c:513-868) without the
- * separate sign sub-packet, then dequantisation and sign conversion
+/* unpack_precinct (Source/Lib/Decoder/Codec/Packing.c:513-868), then
+ * dequantisation and sign conversion
  * (Dequant.c:9-57, Precinct.c:9-29).  `top` is the precinct above in the
  * same slice (NULL for the first precinct of a slice). */
 static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, const gstore_t* top) {
@@ -1676,7 +1785,9 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, 
             if (lo > 0 && br_enough(r, (uint32_t)lo)) { r->bit += (uint64_t)lo * 8; left -= lo * 8; }
             else return E_DEC_BITSTREAM;
         }
-        /* data sub-packet: unpack_data_c (Packing.c:134-219), sign_flag 0 */
+        /* data sub-packet: unpack_data_c (Packing.c:134-219).  Values are
+         * kept in sign-magnitude form until the packet's signs are known. */
+        uint32_t leftover_nz[MAXGB] = {0};
         sub_start = r->bit >> 3;
         for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
             uint32_t c = g->gcomp[i], b = g->gband[i];
@@ -1684,39 +1795,24 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, 
             if (l >= (last ? bd->last_lines : bd->lines)) continue;
             const uint8_t t = cur->gtli[c][b];
             const uint8_t* gl = cur->g[c][b] + (size_t)l * bd->gcli_w;
-            int16_t* out = d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w;
+            uint16_t* out = (uint16_t*)d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w;
             for (uint32_t x = 0; x < bd->gcli_w; x++) {
                 uint16_t v[4] = {0, 0, 0, 0};
                 int32_t planes = (int32_t)gl[x] - t;
                 if (planes > 0) {
-                    left -= 4 * (planes + 1);
+                    left -= 4 * (planes + (h->fs ? 0 : 1));
                     if (left < 0) return E_DEC_BITSTREAM;
-                    uint32_t sg = br_get(r, 4);
+                    uint32_t sg = h->fs ? 0 : br_get(r, 4);
                     uint32_t m[4] = {0, 0, 0, 0};
                     for (int32_t pl = 0; pl < planes; pl++) {
                         uint32_t nib = br_get(r, 4);
                         for (int k2 = 0; k2 < 4; k2++) m[k2] = (m[k2] << 1) | ((nib >> (3 - k2)) & 1u);
                     }
-                    for (int k2 = 0; k2 < 4; k2++) {
-                        uint16_t mag = (uint16_t)(m[k2] << t);
-                        /* inv_quant_deadzone / inv_quant_uniform (Dequant.c:9-43) */
-                        if (t > 0 && mag) {
-                            if (h->qpih == 0) {
-                                mag |= (uint16_t)(1u << (t - 1));
-                            } else {
-                                uint16_t val = mag, acc = 0;
-                                uint8_t sc = (uint8_t)(gl[x] - t + 1);
-                                for (; val > 0; val >>= sc) acc = (uint16_t)(acc + val);
-                                mag = acc;
-                            }
-                        }
-                        v[k2] = (uint16_t)(mag | (((sg >> (3 - k2)) & 1u) << 15));
-                    }
+                    for (int k2 = 0; k2 < 4; k2++) v[k2] = (uint16_t)((uint16_t)(m[k2] << t) | (((sg >> (3 - k2)) & 1u) << 15));
                 }
-                for (uint32_t k2 = 0; k2 < 4 && x * 4 + k2 < bd->w; k2++) {
-                    uint16_t val = v[k2];
-                    /* inv_sign_c, Precinct.c:9-14 */
-                    out[x * 4 + k2] = (int16_t)((val & 0x8000) ? -(int32_t)(val & 0x7fff) : (int32_t)val);
+                for (uint32_t k2 = 0; k2 < 4; k2++) {
+                    if (x * 4 + k2 < bd->w) out[x * 4 + k2] = v[k2];
+                    else leftover_nz[i - g->pk[k].bs] += v[k2] != 0; /* its sign is sent too (Packing.c:200-215) */
                 }
             }
         }
@@ -1727,6 +1823,62 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, 
             int64_t lo = (int64_t)dlen - used;
             if (lo > 0 && br_enough(r, (uint32_t)lo)) { r->bit += (uint64_t)lo * 8; left -= lo * 8; }
             else return E_DEC_BITSTREAM;
+        }
+        if (h->fs) {
+            /* sign sub-packet: unpack_sign (Packing.c:221-247), one bit per
+             * non-zero magnitude, then the signs of the padding coefficients */
+            sub_start = r->bit >> 3;
+            for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
+                uint32_t c = g->gcomp[i], b = g->gband[i];
+                const band_t* bd = &g->c[c].b[b];
+                if (l >= (last ? bd->last_lines : bd->lines)) continue;
+                uint16_t* out = (uint16_t*)d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w;
+                for (uint32_t x = 0; x < bd->w; x++) {
+                    if (!out[x]) continue;
+                    if (--left < 0) return E_DEC_BITSTREAM;
+                    if (!br_enough(r, 1)) return E_DEC_SHORT;
+                    out[x] |= (uint16_t)(br_get(r, 1) << 15);
+                }
+                const uint32_t lo = leftover_nz[i - g->pk[k].bs];
+                if (lo && (bd->w % 4)) {
+                    left -= lo;
+                    if (left < 0) return E_DEC_BITSTREAM;
+                    r->bit += lo;
+                }
+            }
+            br_align(r);
+            left -= left & 7;
+            used = (int64_t)(r->bit >> 3) - (int64_t)sub_start;
+            if (used != (int64_t)slen) {
+                int64_t lo = (int64_t)slen - used;
+                if (lo > 0 && br_enough(r, (uint32_t)lo)) { r->bit += (uint64_t)lo * 8; left -= lo * 8; }
+                else return E_DEC_BITSTREAM;
+            }
+        }
+        /* inv_quant_deadzone / inv_quant_uniform (Dequant.c:9-43), then
+         * inv_sign_c (Precinct.c:9-14) */
+        for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
+            uint32_t c = g->gcomp[i], b = g->gband[i];
+            const band_t* bd = &g->c[c].b[b];
+            if (l >= (last ? bd->last_lines : bd->lines)) continue;
+            const uint8_t t = cur->gtli[c][b];
+            const uint8_t* gl = cur->g[c][b] + (size_t)l * bd->gcli_w;
+            int16_t* out = d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w;
+            for (uint32_t x = 0; x < bd->w; x++) {
+                const uint16_t raw = (uint16_t)out[x];
+                uint16_t mag = raw & 0x7fff;
+                if (t > 0 && mag) {
+                    if (h->qpih == 0) {
+                        mag |= (uint16_t)(1u << (t - 1));
+                    } else {
+                        uint16_t val = mag, acc = 0;
+                        uint8_t sc = (uint8_t)(gl[x / 4] - t + 1);
+                        for (; val > 0; val >>= sc) acc = (uint16_t)(acc + val);
+                        mag = acc;
+                    }
+                }
+                out[x] = (int16_t)((raw & 0x8000) ? -(int32_t)(mag & 0x7fff) : (int32_t)mag);
+            }
         }
     }
     int64_t pad = (int64_t)lprc - ((int64_t)(r->bit >> 3) - (int64_t)prec_start);
@@ -1807,7 +1959,6 @@ int or_decode(const uint8_t* bs, uint32_t size, void* const planes[4], const uin
         e = or_probe(bs, size, info);
         if (e) return e;
     }
-    if (h.fs) return E_DEC_BITSTREAM; /* separate sign sub-packets are outside this restatement */
     dec_t d;
     memset(&d, 0, sizeof(d));
     d.h = &h;

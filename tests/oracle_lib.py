@@ -30,9 +30,9 @@ class ImageInfo(ctypes.Structure):
 
 
 def make_params(width, height, depth, fmt, bpp_num, bpp_den=1, decomp_v=2, decomp_h=5, quantization=0, slice_height=16,
-                rc_mode=1, significance=1, threads=1):
+                rc_mode=1, significance=1, threads=1, signs=0, vpred=0):
     return EncParams(width, height, depth, fmt, bpp_num, bpp_den, decomp_v, decomp_h, quantization, slice_height, rc_mode,
-                     significance, 0, 0, threads)
+                     significance, signs, vpred, threads)
 
 
 def build_oracle():

@@ -147,3 +147,64 @@ def test_oracle_rc_modes_2_3_match_reference(oracle, case):
     if e_ref:
         return
     assert np.array_equal(b_ref, b_or)
+
+
+def test_oracle_encodes_sign_fixtures(oracle):
+    """The oracle's encoder with separate sign sub-packets (fast and full
+    strategies) reproduces the reference encoder's codestreams byte for
+    byte (fixtures; vertical prediction excluded)."""
+    n = 0
+    for name, c in G.sign_cases().items():
+        w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, sg, vpm = c["params"]
+        if vpm:
+            continue
+        p = oracle.make_params(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, significance=sig, rc_mode=rc,
+                               signs=sg)
+        err, bs = oracle.oracle_encode(p, c["planes"])
+        assert err == 0, name
+        assert np.array_equal(bs, c["bs"]), name
+        n += 1
+    assert n >= 5
+
+
+def _sign_cases(n, seed):
+    """Random configurations with sign handling: fast and full strategies
+    under every rate-control mode, both quantizers."""
+    out = []
+    for c in _random_cases(n, seed):
+        c = dict(c)
+        c["signs"] = 1 + (c["seed"] % 2)
+        c["rc"] = (c["seed"] // 2) % 4
+        out.append(c)
+    return out
+
+
+@pytest.mark.parametrize("case", _sign_cases(80, 2026), ids=lambda c: "s%d_rc%d_q%d_%dx%d_d%d_f%d_V%dH%d" % (
+    c["signs"], c["rc"], c["q"], c["w"], c["h"], c["d"], c["fmt"], c["v"], c["hh"]))
+def test_oracle_signs_match_reference(oracle, case):
+    if not oracle.ref_available():
+        pytest.skip("reference library not built here (needs the reference sources)")
+    c = case
+    planes = S.frame(c["w"], c["h"], c["d"], c["fmt"], seed=c["seed"])
+    p = oracle.make_params(c["w"], c["h"], c["d"], c["fmt"], c["bpp"], c["den"], c["v"], c["hh"], quantization=c["q"],
+                           slice_height=c["sl"], significance=c["sig"], rc_mode=c["rc"], signs=c["signs"])
+    e_ref, b_ref = oracle.ref_encode(p, planes)
+    e_or, b_or = oracle.oracle_encode(p, planes)
+    assert e_ref == e_or
+    if e_ref:
+        return
+    assert np.array_equal(b_ref, b_or)
+    e2, d_or = oracle.oracle_decode(b_ref)
+    e1, d_ref = oracle.ref_decode(b_ref)
+    assert e1 == e2 == 0
+    assert all(np.array_equal(a, b) for a, b in zip(d_ref, d_or))
+
+
+def test_oracle_decodes_sign_fixtures(oracle):
+    """The oracle decodes the reference encoder's sign sub-packet
+    codestreams (vertical prediction included) bit-exact with the
+    reference decoder."""
+    for name, c in G.sign_cases().items():
+        err, planes = oracle.oracle_decode(c["bs"])
+        assert err == 0, name
+        assert all(np.array_equal(a, b) for a, b in zip(planes, c["dec"])), name
