@@ -189,7 +189,7 @@ static uint64_t enc_work_layout(const jxs_cfg_t* c, uint8_t* base, EncWork* w) {
     ll_layout(c, w->fb.ll_pitch, llsz);
     for (int v = 0; v < 2; v++)
         for (int k = 0; k < JXS_MAXC; k++) w->fb.ll[v][k] = llsz[v][k] ? (int32_t*)take(llsz[v][k]) : nullptr;
-    w->cost = (uint32_t*)take((uint64_t)c->np * 1024 * sizeof(uint32_t));
+    w->cost = (uint32_t*)take((uint64_t)c->np * 1024 * sizeof(uint32_t) * (c->fs ? 2 : 1));
     w->slice_done = (uint32_t*)take((uint64_t)c->nslices * sizeof(uint32_t));
     w->rc = (PrecRC*)take((uint64_t)c->np * sizeof(PrecRC));
     w->out_stage = take((uint64_t)c->lcod + 64);
@@ -618,7 +618,7 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         case OP_INV_V_S: e = jxs_launch_inv_v((const InvVLaunch*)d, o.kind, o.nblocks, s); break;
         case OP_RC1: {
             const EncPrecFrame* F = (const EncPrecFrame*)d;
-            e = jxs_launch_rc(F->cfg, (uint32_t)o.nblocks, 0, F->gcli, F->cost, F->slice_done, F->rc, F->status, s);
+            e = jxs_launch_rc(F->cfg, (uint32_t)o.nblocks, 0, F->gcli, F->coef, F->cost, F->slice_done, F->rc, F->status, s);
             break;
         }
         case OP_PACK1: {

@@ -556,10 +556,9 @@ int32_t jxs_cfg_encoder(jxs_cfg_t* g, struct svt_jpeg_xs_encoder_api* api) {
         else { mh = 0; break; }
     }
     if (mw == 0 || mh == 0) return JXS_E_BAD_PARAM;
-    /* The GPU encoder implements vertical prediction off and sign handling
-     * off, with every rate-control mode (0-3). */
-    if (api->coding_vertical_prediction_mode != 0 || api->coding_signs_handling != 0 || api->rate_control_mode > 3)
-        return JXS_E_BAD_PARAM;
+    /* The GPU encoder implements vertical prediction off, with every
+     * rate-control mode (0-3) and sign handling off, fast or full. */
+    if (api->coding_vertical_prediction_mode != 0 || api->rate_control_mode > 3) return JXS_E_BAD_PARAM;
 
     int32_t r = jxs_cfg_geometry(g, 1, nc, api->source_width, api->source_height, api->ndecomp_h, api->ndecomp_v, 0, sx, sy,
                                  api->slice_height);
@@ -569,7 +568,8 @@ int32_t jxs_cfg_encoder(jxs_cfg_t* g, struct svt_jpeg_xs_encoder_api* api) {
     g->qpih = api->quantization;
     g->sig = !!api->coding_significance;
     g->rc_mode = api->rate_control_mode;
-    g->fs = 0;
+    g->signs = api->coding_signs_handling;
+    g->fs = g->signs ? 1 : 0; /* hdr_Fs (EncHandle.c:278) */
     g->rm = 0;
     g->bw = 20;
     g->fq = 8;

@@ -27,7 +27,7 @@
 #define FULL 0xffffffffu
 #define RC_THREADS 512
 #define RC_WARPS (RC_THREADS / 32)
-#define RC_AREA_WORDS (5 * JXS_MAXBLINES * 16)
+#define RC_AREA_WORDS (6 * JXS_MAXBLINES * 16)
 
 /* binary_search_init / binary_search_next_step (BinarySearch.c:9-78) */
 struct BSearch {
@@ -68,7 +68,16 @@ DEV int bs_next(BSearch& s, int res, int* out) {
  * (RateControl.c:1259-1333) with its binary searches (:889-1083), evaluated
  * on the slice's cost tables.  Run by a whole block: the tables of up to
  * `area_words / (nq * nr)` precincts are read (through L2) into `area` at a
- * time; thread 0 then runs their searches in order. */
+ * time; thread 0 then runs their searches in order.
+ *
+ * With sign handling each precinct has two tables: signs counted the fast
+ * way (every coefficient of a group above gtli) and exactly.  The
+ * quantization search runs on the fast table; the full strategy then steps
+ * from its result on the exact table and searches the refinement there.
+ * The fast strategy sends only the signs it needs: the bytes this frees are
+ * cut from the precinct and carried to the next one with its padding, or
+ * stay as padding in a slice's last precinct and in mode 0
+ * (PackPrecinct.c:513-536, PackStageProcess.c:293-333, 526-560). */
 DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* __restrict__ cost, uint32_t* area,
                       uint32_t area_words, PrecRC* __restrict__ rc, int* __restrict__ status) {
     __shared__ uint32_t s_carry, s_run;
@@ -82,8 +91,11 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
     uint32_t min_b = slice_budget / nprec;
     uint32_t left = slice_budget - min_b * nprec;
     uint32_t first_b = min_b;
+    const uint32_t signs = cfg->signs;
     if (cfg->rc_mode == 1) {
-        first_b = min(slice_budget, first_b * 110 / 100);
+        /* the first precinct 20 % more with fast signs, else 10 %
+         * (PackStageProcess.c:34-35, 614-622) */
+        first_b = min(slice_budget, first_b * (signs == 1 ? 120u : 110u) / 100);
         if (nprec > 1) {
             min_b = (slice_budget - first_b) / (nprec - 1);
             left = slice_budget - min_b * (nprec - 1) - first_b;
@@ -188,7 +200,7 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
                     if (pad_last > 0) {
                         /* the first precinct 10 % more, the rest of the padding
                          * shared evenly */
-                        uint32_t add_first = rc[first_p].total_bytes * 10 / 100;
+                        uint32_t add_first = rc[first_p].total_bytes * (signs == 1 ? 20u : 10u) / 100;
                         if (add_first > pad_last) add_first = pad_last;
                         pad_last -= add_first;
                         rc[first_p + nprec - 1].total_bytes -= add_first;
@@ -208,21 +220,26 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
             }
         }
     }
-    const uint32_t chunk = area_words / (uint32_t)nt;
+    /* per precinct its table, and with sign handling the exact-sign table
+     * after it */
+    const int ntab = signs ? 2 : 1;
+    const uint32_t chunk = area_words / (uint32_t)(nt * ntab);
     for (uint32_t c0 = 0; c0 < nprec; c0 += chunk) {
         const uint32_t cnt = min(chunk, nprec - c0);
         __syncthreads();
         if (s_err) break;
-        for (int e = threadIdx.x; e < (int)cnt * nt; e += blockDim.x) {
-            const int i = e / nt, qr = e - i * nt, q = qr / nr, r = qr - q * nr;
-            area[e] = __ldcg(cost + (uint64_t)(first_p + c0 + i) * 1024 + q * 32 + r);
+        for (int e = threadIdx.x; e < (int)cnt * nt * ntab; e += blockDim.x) {
+            const int i = e / (nt * ntab), rest = e - i * nt * ntab, tb = rest / nt, qr = rest - tb * nt, q = qr / nr,
+                      r = qr - q * nr;
+            area[e] = __ldcg(cost + ((uint64_t)tb * np_all + first_p + c0 + i) * 1024 + q * 32 + r);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             for (uint32_t ii = 0; ii < cnt && !s_err; ii++) {
                 const uint32_t i = c0 + ii;
                 const uint32_t p = first_p + i;
-                const uint32_t* T = area + ii * nt;
+                const uint32_t* T = area + ii * nt * ntab;
+                const uint32_t* F = signs ? T + nt : T; /* exact signs */
                 const int last = (p + 1 >= np_all);
                 const uint32_t budget =
                     (rc_mode >= 2 ? rc[p].total_bytes : (i == 0 ? first_b : min_b) + (i < left ? 1 : 0)) + s_carry;
@@ -245,6 +262,25 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
                     }
                     if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
                     q = v;
+                    if (!err && signs == 2) {
+                        /* full signs: lower quantizations while they fit,
+                         * else the first higher one that fits
+                         * (RateControl.c:936-1015) */
+                        int best = -1;
+                        for (int qt = q - 1; qt >= 0; qt--) {
+                            if ((s_empty[qt] & 1u) || F[qt * nr] > avail) break;
+                            best = qt;
+                        }
+                        if (best < 0)
+                            for (int qt = q; qt <= max_q; qt++)
+                                if (!(s_empty[qt] & 1u) && F[qt * nr] <= avail) {
+                                    best = qt;
+                                    break;
+                                }
+                        if (best < 0) err = JXS_E_ENC_FRAME;
+                        q = best;
+                    }
+                    const uint32_t* TR = signs == 2 ? F : T; /* the refinement search's table */
                     if (!err) {
                         step = 6;
                         if (step >= max_r) step = 0;
@@ -252,25 +288,27 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
                         next = BS_BEGIN;
                         while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
                             if ((s_empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
-                            else next = T[q * nr + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
+                            else next = TR[q * nr + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
                         }
                         if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
                         r = v;
-                        data = T[q * nr + r];
+                        data = TR[q * nr + r];
                     }
                     if (!err) {
                         uint32_t padding = avail - data;
                         uint32_t total = budget;
+                        /* fast signs: the bytes of signs not sent */
+                        const uint32_t retrieve = signs == 1 ? T[q * nr + r] - F[q * nr + r] : 0u;
                         if (rc_mode >= 1 && i + 1 < nprec) {
-                            total -= padding;
-                            s_carry = padding;
+                            total -= padding + retrieve;
+                            s_carry = padding + retrieve;
                         } else {
                             s_carry = 0;
                         }
                         PrecRC o;
                         o.total_bytes = total;
                         o.offset = s_run;
-                        o.data_bytes = data;
+                        o.data_bytes = data - retrieve; /* the sub-packet bytes packed */
                         o.q = (uint8_t)q;
                         o.r = (uint8_t)r;
                         o.first_in_slice = (uint8_t)(i == 0);
@@ -289,6 +327,21 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
     }
 }
 
+/* Number of gtli values t (from 0 up) at which a coefficient of magnitude m
+ * in a group with GCLI g stays non-zero after quantization
+ * (rate_control_lut_fill, RateControl.c:124-137, and
+ * rate_control_sign_coding_get_sum_nonzero_coeff_c, :366-455): the bits of
+ * m for deadzone quantization; for uniform quantization the value
+ * ((m << (g - t + 1)) - m + 2^g) >> (g + 1) falls as t grows and is non-zero
+ * while m (2^(g-t+1) - 1) >= 2^g. */
+DEV uint32_t nz_levels(uint32_t m, uint32_t g, uint32_t uniform) {
+    if (!m) return 0;
+    if (!uniform) return 32 - __clz(m);
+    uint32_t n = 0;
+    while (n < g && m * ((2u << (g - n)) - 1u) >= (1u << g)) n++;
+    return n;
+}
+
 /* Byte cost of every (quantization, refinement) candidate of one precinct
  * row: rate_control_lut_fill, rate_control_calculate_band_best_method and
  * precinct_get_budget_bytes (RateControl.c:18-154, 457-781).
@@ -303,17 +356,24 @@ DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* 
  *               separately, raw fallback when cheaper; summed over packets
  *               for every (Q, R). */
 __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
-                                             uint32_t* __restrict__ cost, uint32_t* __restrict__ slice_done,
-                                             PrecRC* __restrict__ rc, int* __restrict__ status, const int p) {
-    /* per band line: GCLI and significance-maximum histograms, then per gtli
-     * data / GCLI bits without and with significance; the area is reused by
-     * the slice selection at the end */
+                                             const uint16_t* __restrict__ coef, uint32_t* __restrict__ cost,
+                                             uint32_t* __restrict__ slice_done, PrecRC* __restrict__ rc,
+                                             int* __restrict__ status, const int p) {
+    /* per band line: GCLI and significance-maximum histograms (with sign
+     * handling also the coefficients by non-zero levels), then per gtli data
+     * / GCLI bits without and with significance and the sign bits; the area
+     * is reused by the slice selection at the end */
     __shared__ __align__(16) uint32_t s_area[RC_AREA_WORDS];
-    uint32_t(*hist)[16] = (uint32_t(*)[16])s_area;
-    uint32_t(*shist)[16] = (uint32_t(*)[16])(s_area + JXS_MAXBLINES * 16);
+    uint32_t(*hist)[16] = (uint32_t(*)[16])s_area;                          /* later: fast sign bits per t */
+    uint32_t(*shist)[16] = (uint32_t(*)[16])(s_area + JXS_MAXBLINES * 16);  /* later: full-sign cost changes */
     uint32_t(*tdat)[16] = (uint32_t(*)[16])(s_area + 2 * JXS_MAXBLINES * 16);
     uint32_t(*tnos)[16] = (uint32_t(*)[16])(s_area + 3 * JXS_MAXBLINES * 16);
     uint32_t(*tsig)[16] = (uint32_t(*)[16])(s_area + 4 * JXS_MAXBLINES * 16);
+    uint32_t(*nzh)[16] = (uint32_t(*)[16])(s_area + 5 * JXS_MAXBLINES * 16);  /* later: full sign bits per t */
+    uint32_t(*tfs)[16] = hist;
+    uint32_t(*tnz)[16] = nzh;
+    uint32_t(*dF)[32] = (uint32_t(*)[32])shist;
+    const uint32_t fs = cfg->fs, uniform = cfg->qpih;
     __shared__ int pmax[JXS_MAXBLINES];
     __shared__ uint32_t cn[JXS_MAXBL][16], cs[JXS_MAXBL][16];
     __shared__ uint16_t meth[JXS_MAXBL];
@@ -342,6 +402,7 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     for (uint32_t i = threadIdx.x; i < nbl * 16; i += blockDim.x) {
         hist[i >> 4][i & 15] = 0;
         shist[i >> 4][i & 15] = 0;
+        nzh[i >> 4][i & 15] = 0;
     }
     for (uint32_t i = threadIdx.x; i < cfg->nbands * 16; i += blockDim.x) {
         cn[i >> 4][i & 15] = 0;
@@ -369,6 +430,11 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
         const uint32_t x = sg.bl;
         const uint8_t* grow = gcli + s_grow[x];
         const uint32_t gend = min(sg.g0 + SG, bls[x].gcli_w);
+        const uint16_t* crow = nullptr;
+        if (fs) {
+            const jxs_band_t& bd = cfg->band[lfb[x]];
+            crow = coef + bd.coef_off + (uint64_t)(p * bd.lines + bls[x].line) * bd.pitch;
+        }
         for (uint32_t base = sg.g0; base < gend; base += 128) {
             const uint32_t g = base + 4 * lane;
             const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
@@ -404,6 +470,35 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
                     if (cs2) atomicAdd(&shist[x][4 * r + lane], cs2);
                 }
             }
+            if (fs) {
+                /* sign handling: the lane's 16 coefficients (inside the band
+                 * width) by the number of gtli values at which they stay
+                 * non-zero; 16-bit counters two to a register */
+                uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0;
+                if (nv) {
+                    c0 = *(const uint4*)(crow + 4 * g);
+                    c1 = *(const uint4*)(crow + 4 * g + 8);
+                }
+                const uint32_t cw[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+                const int wleft = (int)bls[x].w - 4 * (int)g;
+                uint32_t zc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+                for (int i = 0; i < 16; i++) {
+                    const uint32_t m = (cw[i >> 1] >> (16 * (i & 1))) & 0x7fffu;
+                    const uint32_t v = (w4 >> (8 * (i >> 2))) & 255u;
+                    const uint32_t n = i < wleft && (i >> 2) < (int)nv ? nz_levels(m, v, uniform) : 0u;
+#pragma unroll
+                    for (int r = 0; r < 8; r++) zc[r] += (n >> 1) == (uint32_t)r ? 1u << (16 * (n & 1)) : 0u;
+                }
+#pragma unroll
+                for (int r = 0; r < 8; r++) {
+                    const uint32_t zs = __reduce_add_sync(FULL, zc[r]);
+                    if (lane < 2) {
+                        const uint32_t c = (zs >> (16 * lane)) & 0xffffu;
+                        if (c) atomicAdd(&nzh[x][2 * r + lane], c);
+                    }
+                }
+            }
         }
     }
     __syncthreads();
@@ -413,12 +508,21 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     for (uint32_t x = threadIdx.x; x < nbl; x += blockDim.x) {
         const uint32_t N = bls[x].gcli_w, partial = N & 7u;
         int S0 = 0, S1 = 0;
+        uint32_t Z1 = 0;
         for (int t = 15; t >= 0; t--) {
             const int dsum = S1 - (t - 1) * S0; /* sum over v > t of (v - t + 1) h[v] */
-            tdat[x][t] = 4u * (uint32_t)dsum;
+            const uint32_t h = hist[x][t];
+            /* with sign handling the data leave out the sign nibbles
+             * (RateControl.c:156-210): fast signs count 4 per group above
+             * t, full signs the coefficients that stay non-zero */
+            tdat[x][t] = 4u * (uint32_t)(dsum - (fs ? S0 : 0));
             tnos[x][t] = (uint32_t)dsum + N - (uint32_t)S0;
-            S0 += (int)hist[x][t];
-            S1 += t * (int)hist[x][t];
+            tfs[x][t] = 4u * (uint32_t)S0;
+            const uint32_t zh = nzh[x][t];
+            tnz[x][t] = Z1;
+            Z1 += zh;
+            S0 += (int)h;
+            S1 += t * (int)h;
         }
         uint32_t Z = 0;
         const int pm = pmax[x];
@@ -447,15 +551,20 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
      * at R = 0 and its change at every R where one of its band lines drops,
      * and the table is a prefix sum over R */
     const int nq = cfg->max_q + 1, nr = cfg->max_r + 1;
-    for (int e = threadIdx.x; e < nq * 32; e += blockDim.x) dC[e >> 5][e & 31] = 0;
+    for (int e = threadIdx.x; e < nq * 32; e += blockDim.x) {
+        dC[e >> 5][e & 31] = 0;
+        dF[e >> 5][e & 31] = 0;
+    }
     __syncthreads();
+    /* with sign handling each packet adds its sign sub-packet, rounded on
+     * its own: fast signs in dC, full signs in dF (RateControl.c:745-756) */
     const uint32_t npk = cfg->npk;
     for (uint32_t e = threadIdx.x; e < (uint32_t)nq * npk; e += blockDim.x) {
         const int q = (int)(e / npk);
         const uint32_t k = e - (uint32_t)q * npk;
         const uint32_t b0 = s_pkbl0[k], nb = s_pknbl[k];
         if (!nb) continue;
-        uint32_t db = 0, gb = 0, sb = 0;
+        uint32_t db = 0, gb = 0, sb = 0, fb = 0, zb = 0;
         for (uint32_t x = b0; x < b0 + nb; x++) {
             const int g = lgain[x];
             const int t = q < g ? 0 : min(q - g, 15);
@@ -466,9 +575,15 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
             } else {
                 gb += tnos[x][t];
             }
+            if (fs) {
+                fb += tfs[x][t];
+                zb += tnz[x][t];
+            }
         }
-        uint32_t c = ((db + 7) >> 3) + min(lraw[k], ((sb + 7) >> 3) + ((gb + 7) >> 3));
+        const uint32_t base = ((db + 7) >> 3) + min(lraw[k], ((sb + 7) >> 3) + ((gb + 7) >> 3));
+        uint32_t c = base + (fs ? (fb + 7) >> 3 : 0u), cf = base + ((zb + 7) >> 3);
         atomicAdd(&dC[q][0], c);
+        if (fs) atomicAdd(&dF[q][0], cf);
         for (uint32_t i = 0; i < nb; i++) {
             const uint32_t x = s_order[b0 + i];
             const int rf = lprio[x] + 1; /* the line's gtli drops by one for R >= priority + 1 */
@@ -479,18 +594,32 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
             db += tdat[x][t1] - tdat[x][t0];
             gb += (m1 ? tsig[x][t1] : tnos[x][t1]) - (m0 ? tsig[x][t0] : tnos[x][t0]);
             sb += (m1 ? lsig[x] : 0u) - (m0 ? lsig[x] : 0u);
-            const uint32_t c1 = ((db + 7) >> 3) + min(lraw[k], ((sb + 7) >> 3) + ((gb + 7) >> 3));
+            const uint32_t base1 = ((db + 7) >> 3) + min(lraw[k], ((sb + 7) >> 3) + ((gb + 7) >> 3));
+            uint32_t c1 = base1;
+            if (fs) {
+                fb += tfs[x][t1] - tfs[x][t0];
+                zb += tnz[x][t1] - tnz[x][t0];
+                c1 += (fb + 7) >> 3;
+                const uint32_t cf1 = base1 + ((zb + 7) >> 3);
+                atomicAdd(&dF[q][rf], cf1 - cf);
+                cf = cf1;
+            }
             atomicAdd(&dC[q][rf], c1 - c);
             c = c1;
         }
     }
     __syncthreads();
     uint32_t* out = cost + (uint64_t)p * 32 * 32;
+    uint32_t* outf = cost + ((uint64_t)cfg->np + p) * 32 * 32;
     for (int q = threadIdx.x; q < nq; q += blockDim.x) {
-        uint32_t run = 0;
+        uint32_t run = 0, runf = 0;
         for (int r = 0; r < nr; r++) {
             run += dC[q][r];
             out[q * 32 + r] = run;
+            if (fs) {
+                runf += dF[q][r];
+                outf[q * 32 + r] = runf;
+            }
         }
     }
     /* the block that completes a slice runs the slice's selection: tables
@@ -560,13 +689,15 @@ DEV uint32_t coefs_to_planes(uint32_t x) {
 }
 
 /* Data bits of one 4-coefficient group with GCLI v > gtli t
- * (pack_data_c, PackPrecinct.c:128-198): the sign nibble (coefficient 0 in
- * the most significant bit) followed by bit-planes v-1 .. t, each a nibble.
- * Quantization (Quant.c:9-45) is skipped for t == 0 like the reference
- * (QuantStageProcess.c:18-31); a sign is sent only for a non-zero
- * quantized magnitude. */
-DEV uint64_t data_chunk(uint2 raw4, int wleft, uint32_t v, uint32_t t, uint32_t uniform) {
-    const uint32_t np = v - t;
+ * (pack_data_c, PackPrecinct.c:128-198): bit-planes v-1 .. t, each a
+ * nibble (coefficient 0 in the most significant bit).  Quantization
+ * (Quant.c:9-45) is skipped for t == 0 like the reference
+ * (QuantStageProcess.c:18-31).  `signs` receives the sign nibble, which has
+ * a bit only for a non-zero quantized magnitude, and `nzm` the non-zero
+ * magnitudes, both with coefficient 0 in bit 3.  Without sign handling the
+ * sign nibble leads the group's data; with it the signs of the non-zero
+ * magnitudes go to the packet's sign sub-packet (pack_sign_c, :200-233). */
+DEV uint64_t data_chunk(uint2 raw4, int wleft, uint32_t v, uint32_t t, uint32_t uniform, uint32_t& signs, uint32_t& nzm) {
     /* coefficients past the band width are zero */
     uint32_t c01 = raw4.x & ((wleft > 1 ? 0xffff0000u : 0u) | 0xffffu);
     uint32_t c23 = raw4.y & ((wleft > 2 ? 0xffffu : 0u) | (wleft > 3 ? 0xffff0000u : 0u));
@@ -592,24 +723,26 @@ DEV uint64_t data_chunk(uint2 raw4, int wleft, uint32_t v, uint32_t t, uint32_t 
         P01 = q[0] | (q[1] << 16);
         P23 = q[2] | (q[3] << 16);
     }
-    /* signs of the non-zero quantized values, coefficient 0 first */
-    const uint32_t s01 = __vcmpne2(P01, 0u) & c01 & 0x80008000u, s23 = __vcmpne2(P23, 0u) & c23 & 0x80008000u;
-    const uint32_t signs = ((s01 >> 12) & 8u) | ((s01 >> 29) & 4u) | ((s23 >> 14) & 2u) | (s23 >> 31);
+    const uint32_t n01 = __vcmpne2(P01, 0u), n23 = __vcmpne2(P23, 0u);
+    nzm = ((n01 << 3) & 8u) | ((n01 >> 14) & 4u) | ((n23 << 1) & 2u) | (n23 >> 31);
+    const uint32_t s01 = n01 & c01 & 0x80008000u, s23 = n23 & c23 & 0x80008000u;
+    signs = ((s01 >> 12) & 8u) | ((s01 >> 29) & 4u) | ((s23 >> 14) & 2u) | (s23 >> 31);
     /* byte 3 - c of the word = low 8 plane bits of coefficient c */
     uint64_t planes = coefs_to_planes(__byte_perm(P01, P23, 0x0246));
-    if (np > 8) planes |= (uint64_t)coefs_to_planes(__byte_perm(P01, P23, 0x1357)) << 32;
-    return ((uint64_t)signs << (4 * np)) | planes;
+    if (v - t > 8) planes |= (uint64_t)coefs_to_planes(__byte_perm(P01, P23, 0x1357)) << 32;
+    return planes;
 }
 
 /* Per band line of the precinct being packed. */
 struct PkLine {
-    uint32_t sig_pos, gcli_pos, data_pos; /* bit positions in the shared-memory precinct */
-    uint32_t data, vlc, zero;             /* data bits, VLC bits without significance, groups in insignificant significance groups */
+    uint32_t sig_pos, gcli_pos, data_pos, sign_pos; /* bit positions in the shared-memory precinct */
+    uint32_t data, vlc, zero, nz; /* data bits, VLC bits without significance, groups in insignificant significance
+                                     groups, signs sent in the sign sub-packet */
     uint8_t meth, raw, pad0, pad1;
 };
 
 /* pack_precinct (PackPrecinct.c:235-572) for one precinct row; vertical
- * prediction and sign handling off.
+ * prediction off.
  *
  * The precinct is assembled in shared memory, `lead` bytes into the buffer
  * so that buffer byte i lands on the 16-byte aligned address
@@ -628,14 +761,14 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                                           const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
                                           uint8_t* __restrict__ out, uint32_t cap_words, int* status, const int p) {
     extern __shared__ __align__(16) uint32_t buf[];
-    __shared__ uint32_t s_data[JXS_MAXSEG], s_vlc[JXS_MAXSEG], s_zero[JXS_MAXSEG];
+    __shared__ uint32_t s_data[JXS_MAXSEG], s_vlc[JXS_MAXSEG], s_zero[JXS_MAXSEG], s_nz[JXS_MAXSEG];
     __shared__ PkLine pl[JXS_MAXBLINES];
     __shared__ uint8_t s_meth[JXS_MAXBL];
     __shared__ uint32_t s_cn[JXS_MAXBL], s_cs[JXS_MAXBL];
     __shared__ uint32_t s_lg[JXS_MAXBLINES], s_ls[JXS_MAXBLINES];       /* per line: GCLI / significance bits */
-    __shared__ uint32_t s_pks[JXS_MAXPK], s_pkg[JXS_MAXPK], s_pkd[JXS_MAXPK]; /* per packet: sub-packet starts */
+    __shared__ uint32_t s_pks[JXS_MAXPK], s_pkg[JXS_MAXPK], s_pkd[JXS_MAXPK], s_pkn[JXS_MAXPK]; /* per packet: sub-packet starts */
     __shared__ uint8_t s_pkr[JXS_MAXPK];
-    __shared__ uint32_t s_vst[JXS_MAXSEG], s_dst[JXS_MAXSEG];        /* per segment: GCLI / data bit starts */
+    __shared__ uint32_t s_vst[JXS_MAXSEG], s_dst[JXS_MAXSEG], s_nst[JXS_MAXSEG]; /* per segment: GCLI / data / sign bit starts */
     /* this precinct kind's tables, staged from the configuration */
     __shared__ jxs_seg_t s_seg[JXS_MAXSEG];
     __shared__ jxs_bline_t s_bl[JXS_MAXBLINES];
@@ -714,13 +847,17 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
     const jxs_bline_t* bls = s_bl;
 
     /* pass A: each lane 4 consecutive groups (one 4-byte GCLI load), a warp
-     * 128 groups per step */
+     * 128 groups per step; with sign handling also the non-zero quantized
+     * coefficients, whose signs go to the sign sub-packets */
+    const uint32_t fs = cfg->fs, uniform = cfg->qpih;
     for (uint32_t sidx = warp; sidx < nseg; sidx += PK_WARPS) {
         const jxs_seg_t sg = segs[sidx];
         const uint32_t t = s_lt[sg.bl];
         const uint8_t* grow = gcli + s_grow[sg.bl];
+        const uint16_t* crow = coef + s_crow[sg.bl];
+        const int bw = (int)bls[sg.bl].w;
         const uint32_t gend = min(sg.g0 + SG, bls[sg.bl].gcli_w);
-        uint32_t dsum = 0, vsum = 0, zsum = 0;
+        uint32_t dsum = 0, vsum = 0, zsum = 0, nsum = 0;
         for (uint32_t base = sg.g0; base < gend; base += 128) {
             const uint32_t g = base + 4 * lane;
             const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
@@ -733,19 +870,34 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             for (int k = 0; k < 4; k++) {
                 if (k < (int)nv) {
                     const uint32_t v = (w4 >> (8 * k)) & 255u;
-                    dsum += v > t ? 4 * (v - t + 1) : 0u;
+                    dsum += v > t ? 4 * (v - t + 1 - fs) : 0u;
                     vsum += v > t ? v - t + 1 : 1u;
                     zsum += mx <= t;
+                }
+            }
+            if (fs && m > t) {
+                const uint4 c0 = *(const uint4*)(crow + 4 * g), c1 = *(const uint4*)(crow + 4 * g + 8);
+                const uint2 cw[4] = {make_uint2(c0.x, c0.y), make_uint2(c0.z, c0.w), make_uint2(c1.x, c1.y), make_uint2(c1.z, c1.w)};
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const uint32_t v = (w4 >> (8 * k)) & 255u;
+                    if (k < (int)nv && v > t) {
+                        uint32_t sgn, nzm;
+                        (void)data_chunk(cw[k], bw - 4 * (int)(g + k), v, t, uniform, sgn, nzm);
+                        nsum += __popc(nzm);
+                    }
                 }
             }
         }
         dsum = __reduce_add_sync(FULL, dsum);
         vsum = __reduce_add_sync(FULL, vsum);
         zsum = __reduce_add_sync(FULL, zsum);
+        nsum = __reduce_add_sync(FULL, nsum);
         if (lane == 0) {
             s_data[sidx] = dsum;
             s_vlc[sidx] = vsum;
             s_zero[sidx] = zsum;
+            s_nz[sidx] = nsum;
         }
     }
     __syncthreads();
@@ -755,15 +907,17 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
         const uint32_t nbl = s_nbl;
         for (uint32_t b = lane; b < nbl; b += 32) {
             const jxs_bline_t& B = bls[b];
-            uint32_t d = 0, v = 0, z = 0;
+            uint32_t d = 0, v = 0, z = 0, n = 0;
             for (uint32_t i = B.seg0; i < B.seg0 + B.nseg; i++) {
                 d += s_data[i];
                 v += s_vlc[i];
                 z += s_zero[i];
+                n += s_nz[i];
             }
             pl[b].data = d;
             pl[b].vlc = v;
             pl[b].zero = z;
+            pl[b].nz = n;
             atomicAdd(&s_cn[B.fb], v);
             atomicAdd(&s_cs[B.fb], v - z + B.sig_w);
         }
@@ -783,75 +937,81 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
         /* one lane per packet: sub-packet sizes, raw fallback, header */
         const uint32_t k = lane;
         const uint32_t nb = k < s_npk ? s_pknbl[k] : 0u, b0 = k < s_npk ? s_pkbl0[k] : 0u;
-        uint32_t db = 0, gbits = 0, sbits = 0;
+        uint32_t db = 0, gbits = 0, sbits = 0, nbits = 0;
         for (uint32_t x = b0; x < b0 + nb; x++) {
             db += pl[x].data;
             gbits += s_lg[x];
             sbits += s_ls[x];
+            nbits += pl[x].nz;
         }
-        const uint32_t dB = (db + 7) >> 3, gB = (gbits + 7) >> 3, sB = (sbits + 7) >> 3;
+        const uint32_t dB = (db + 7) >> 3, gB = (gbits + 7) >> 3, sB = (sbits + 7) >> 3, nB = (nbits + 7) >> 3;
         const uint32_t rawB = nb ? s_praw[k] : 0u;
         const int raw = nb && sB + gB > rawB;
         const uint32_t gcl_bytes = raw ? rawB : gB;
         const uint32_t hb = nb ? (s_short ? 5u : 7u) : 0u;
-        const uint32_t pk_bytes = nb ? hb + (raw ? rawB : sB + gB) + dB : 0u;
+        const uint32_t pk_bytes = nb ? hb + (raw ? rawB : sB + gB) + dB + nB : 0u;
         uint32_t pk_total;
         const uint32_t hdr = s_phb;
         const uint32_t start = lead + hdr + warp_excl_scan(pk_bytes, &pk_total);
         const int fits = start + hb <= words * 4;
         if (nb && fits) {
-            /* packet header (PackHeaders.c:98-127), sign length 0 */
+            /* packet header (PackHeaders.c:98-127) */
             uint8_t* h = (uint8_t*)buf + start;
             if (s_short) {
                 h[0] = (uint8_t)((raw << 7) | ((dB >> 8) & 0x7f));
                 h[1] = (uint8_t)dB;
                 h[2] = (uint8_t)(gcl_bytes >> 5);
-                h[3] = (uint8_t)((gcl_bytes & 0x1f) << 3);
-                h[4] = 0;
+                h[3] = (uint8_t)(((gcl_bytes & 0x1f) << 3) | ((nB >> 8) & 7));
+                h[4] = (uint8_t)nB;
             } else {
                 h[0] = (uint8_t)((raw << 7) | ((dB >> 13) & 0x7f));
                 h[1] = (uint8_t)(dB >> 5);
                 h[2] = (uint8_t)(((dB & 0x1f) << 3) | ((gcl_bytes >> 17) & 7));
                 h[3] = (uint8_t)(gcl_bytes >> 9);
                 h[4] = (uint8_t)(gcl_bytes >> 1);
-                h[5] = (uint8_t)((gcl_bytes & 1) << 7);
-                h[6] = 0;
+                h[5] = (uint8_t)(((gcl_bytes & 1) << 7) | ((nB >> 8) & 0x7f));
+                h[6] = (uint8_t)nB;
             }
-            /* sub-packet starts: significance, GCLIs, data */
+            /* sub-packet starts: significance, GCLIs, data, signs */
             const uint32_t p0 = (start + hb) * 8;
             s_pks[k] = p0;
             s_pkg[k] = raw ? p0 : p0 + sB * 8;
             s_pkd[k] = p0 + (raw ? rawB : sB + gB) * 8;
+            s_pkn[k] = s_pkd[k] + dB * 8;
             s_pkr[k] = (uint8_t)raw;
         }
         __syncwarp();
         /* per line: positions inside its packet's sub-packets */
         for (uint32_t x = lane; x < nbl; x += 32) {
             const uint32_t kk = bls[x].pk, xb0 = s_pkbl0[kk];
-            uint32_t sp = 0, gp = 0, dp = 0;
+            uint32_t sp = 0, gp = 0, dp = 0, np = 0;
             const int r = s_pkr[kk];
             for (uint32_t y = xb0; y < x; y++) {
                 sp += s_ls[y];
                 gp += r ? 4 * bls[y].gcli_w : s_lg[y];
                 dp += pl[y].data;
+                np += pl[y].nz;
             }
             pl[x].raw = (uint8_t)r;
             pl[x].sig_pos = s_pks[kk] + sp;
             pl[x].gcli_pos = s_pkg[kk] + gp;
             pl[x].data_pos = s_pkd[kk] + dp;
+            pl[x].sign_pos = s_pkn[kk] + np;
         }
         __syncwarp();
         /* per segment: its start in its line's GCLI and data bits */
         for (uint32_t i = lane; i < nseg; i += 32) {
             const uint32_t x = segs[i].bl;
             const uint8_t m = pl[x].meth;
-            uint32_t vp = pl[x].gcli_pos, dp = pl[x].data_pos;
+            uint32_t vp = pl[x].gcli_pos, dp = pl[x].data_pos, np = pl[x].sign_pos;
             for (uint32_t j = bls[x].seg0; j < i; j++) {
                 vp += m ? s_vlc[j] - s_zero[j] : s_vlc[j];
                 dp += s_data[j];
+                np += s_nz[j];
             }
             s_vst[i] = vp;
             s_dst[i] = dp;
+            s_nst[i] = np;
         }
         /* precinct header: Lprc, Q, R as bytes first, then the 2-bit band
          * coding modes D[p,b] of every existing band */
@@ -891,8 +1051,8 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
     if (!s_ok) return;
 
     /* pass B: each lane 4 consecutive groups; its unary codes are joined
-     * into one write, its data chunks into writes of up to 64 bits */
-    const uint32_t uniform = cfg->qpih;
+     * into one write, its data chunks into writes of up to 64 bits, its
+     * signs (with sign handling) into one write */
     for (uint32_t sidx = warp; sidx < nseg; sidx += PK_WARPS) {
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
@@ -901,7 +1061,7 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
         const uint8_t* grow = gcli + s_grow[sg.bl];
         const uint16_t* crow = coef + s_crow[sg.bl];
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
-        uint32_t vpos = s_vst[sidx], dpos = s_dst[sidx];
+        uint32_t vpos = s_vst[sidx], dpos = s_dst[sidx], npos = s_nst[sidx];
         for (uint32_t base = sg.g0; base < gend; base += 128) {
             const uint32_t g = base + 4 * lane;
             const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
@@ -949,10 +1109,11 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             }
             uint32_t dl = 0;
 #pragma unroll
-            for (int k = 0; k < 4; k++) dl += (k < (int)nv && v[k] > t) ? 4 * (v[k] - t + 1) : 0u;
+            for (int k = 0; k < 4; k++) dl += (k < (int)nv && v[k] > t) ? 4 * (v[k] - t + 1 - fs) : 0u;
             uint32_t tot;
             const uint32_t ex = warp_excl_scan((dl << 16) | vl, &tot);
             if (vl) put_bits(buf, words, vpos + (ex & 0xffffu), vacc, vl, ovf);
+            uint32_t sbits = 0, sn = 0;
             if (dl) {
                 /* data bits of the groups with gcli > gtli (pack_data_c,
                  * PackPrecinct.c:128-198), joined while they fit 64 bits */
@@ -963,8 +1124,21 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     if (k < (int)nv && v[k] > t) {
-                        const uint32_t n = 4 * (v[k] - t + 1);
-                        const uint64_t ch = data_chunk(cw[k], (int)B.w - 4 * (int)(g + k), v[k], t, uniform);
+                        const uint32_t np = v[k] - t, n = 4 * (np + 1 - fs);
+                        uint32_t sgn, nzm;
+                        uint64_t ch = data_chunk(cw[k], (int)B.w - 4 * (int)(g + k), v[k], t, uniform, sgn, nzm);
+                        if (fs) {
+                            /* the signs of the non-zero magnitudes, coefficient 0 first */
+#pragma unroll
+                            for (int j = 3; j >= 0; j--) {
+                                if ((nzm >> j) & 1u) {
+                                    sbits = (sbits << 1) | ((sgn >> j) & 1u);
+                                    sn++;
+                                }
+                            }
+                        } else {
+                            ch |= (uint64_t)sgn << (4 * np);
+                        }
                         if (an + n > 64) {
                             put_bits(buf, words, pos, acc, an, ovf);
                             pos += an;
@@ -979,6 +1153,13 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             }
             vpos += tot & 0xffffu;
             dpos += tot >> 16;
+            if (fs) {
+                /* sign sub-packet (pack_sign_c, PackPrecinct.c:200-233) */
+                uint32_t stot;
+                const uint32_t sx = warp_excl_scan(sn, &stot);
+                if (sn) put_bits(buf, words, npos + sx, sbits, sn, ovf);
+                npos += stot;
+            }
         }
     }
     if (__syncthreads_or(ovf)) {
@@ -1021,15 +1202,16 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
 /* ------------------------------------------------------------------------ */
 /* kernels: one frame, or a batch of frames (block -> frame by its first block) */
 /* ------------------------------------------------------------------------ */
-__global__ void __launch_bounds__(RC_THREADS) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
-                                                           uint32_t* __restrict__ cost, uint32_t* __restrict__ slice_done,
-                                                           PrecRC* __restrict__ rc, int* __restrict__ status) {
-    rc_cost_body(cfg, gcli, cost, slice_done, rc, status, (int)blockIdx.x);
+__global__ void __launch_bounds__(RC_THREADS, 3) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
+                                                           const uint16_t* __restrict__ coef, uint32_t* __restrict__ cost,
+                                                           uint32_t* __restrict__ slice_done, PrecRC* __restrict__ rc,
+                                                           int* __restrict__ status) {
+    rc_cost_body(cfg, gcli, coef, cost, slice_done, rc, status, (int)blockIdx.x);
 }
 
-__global__ void __launch_bounds__(RC_THREADS) rc_cost_batch_kernel(const __grid_constant__ EncPrecLaunch L) {
+__global__ void __launch_bounds__(RC_THREADS, 3) rc_cost_batch_kernel(const __grid_constant__ EncPrecLaunch L) {
     const EncPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
-    rc_cost_body(F.cfg, F.gcli, F.cost, F.slice_done, F.rc, F.status, (int)blockIdx.x - F.first_block);
+    rc_cost_body(F.cfg, F.gcli, F.coef, F.cost, F.slice_done, F.rc, F.status, (int)blockIdx.x - F.first_block);
 }
 
 __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
@@ -1046,10 +1228,11 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_batch_kernel(const __grid_
 /* ------------------------------------------------------------------------ */
 /* host-side launchers                                                       */
 /* ------------------------------------------------------------------------ */
-extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli, uint32_t* cost,
-                                     uint32_t* slice_done, PrecRC* rc, int* status, cudaStream_t st) {
+extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli,
+                                     const uint16_t* coef, uint32_t* cost, uint32_t* slice_done, PrecRC* rc, int* status,
+                                     cudaStream_t st) {
     (void)nslices;
-    rc_cost_kernel<<<np, RC_THREADS, 0, st>>>(dcfg, gcli, cost, slice_done, rc, status);
+    rc_cost_kernel<<<np, RC_THREADS, 0, st>>>(dcfg, gcli, coef, cost, slice_done, rc, status);
     return cudaGetLastError();
 }
 

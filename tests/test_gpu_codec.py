@@ -430,3 +430,68 @@ def test_rc_modes_2_3_against_oracle(gpu, oracle, c):
         return
     assert np.array_equal(q, ref_q) and np.array_equal(r, ref_r)
     assert np.array_equal(out[: f.bitstream.used_size], ref_bs)
+
+
+@pytest.mark.parametrize("name", sorted(n for n, c in G.sign_cases().items() if c["params"][13] == 0))
+def test_separate_signs_golden_encode(gpu, name):
+    """The encoder with sign handling (fast and full strategies) reproduces
+    the reference encoder's codestreams byte for byte, per frame and
+    batched."""
+    c = G.sign_cases()[name]
+    w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, sg, vpm = c["params"]
+    enc = gpu.Encoder(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, coding_significance=sig,
+                      rate_control_mode=rc, coding_signs_handling=sg)
+    bs = enc.encode(c["planes"])
+    assert np.array_equal(bs, c["bs"]), name
+    batch = gpu.Batch(1 << 28)
+    outs = [np.zeros(enc.frame_bytes, np.uint8)]
+    assert batch.encode([enc], [c["planes"]], outs) == 0
+    r, st = batch.wait()
+    assert r == 0 and np.array_equal(outs[0], c["bs"]), name
+    batch.close()
+    enc.close()
+
+
+def _sign_cases(n, seed):
+    out = []
+    for c in _random_cases(n, seed):
+        c = dict(c)
+        c["signs"] = 1 + (c["seed"] % 2)
+        c["rc"] = (c["seed"] // 2) % 4
+        out.append(c)
+    return out
+
+
+@pytest.mark.parametrize("c", _sign_cases(48, 93), ids=lambda c: "s%d_rc%d_q%d_%dx%d_d%d_f%d_V%dH%d" % (
+    c["signs"], c["rc"], c["q"], c["w"], c["h"], c["d"], c["fmt"], c["v"], c["hh"]))
+def test_signs_against_oracle(gpu, oracle, c):
+    """Sign handling under every rate-control mode: codestreams and
+    per-precinct (Q, R) byte-exact with the oracle (which matches the
+    reference encoder on these modes), and the decode of the GPU's
+    codestream bit-exact with the oracle's decode."""
+    planes = S.frame(c["w"], c["h"], c["d"], c["fmt"], seed=c["seed"])
+    p = oracle.make_params(c["w"], c["h"], c["d"], c["fmt"], c["bpp_num"], c["bpp_den"], c["v"], c["hh"], quantization=c["q"],
+                           slice_height=c["sl"], significance=c["sig"], rc_mode=c["rc"], signs=c["signs"])
+    err, ref_bs, ref_q, ref_r = oracle.oracle_encode(p, planes, want_qr=True)
+    if err == 0x80001005:
+        with pytest.raises(gpu.JxsError):
+            make_encoder(gpu, c, coding_signs_handling=c["signs"])
+        return
+    enc = make_encoder(gpu, c, coding_signs_handling=c["signs"])
+    out = np.zeros(enc.frame_bytes + 64, np.uint8)
+    assert enc.send(planes, out) == 0
+    q, r = enc.rc_results()
+    rc, f = enc.get()
+    enc.close()
+    assert rc == err
+    if err:
+        return
+    assert np.array_equal(q, ref_q) and np.array_equal(r, ref_r)
+    bs = out[: f.bitstream.used_size]
+    assert np.array_equal(bs, ref_bs)
+    e2, want = oracle.oracle_decode(bs)
+    assert e2 == 0
+    dec = gpu.Decoder(bs)
+    got = dec.decode(bs)
+    dec.close()
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
