@@ -446,12 +446,14 @@ static int32_t plan_encode_chain(const std::vector<EncItem>& it, const std::vect
     for (int op = 0; op < 2; op++) {
         EncPrecLaunch* L = (EncPrecLaunch*)scratch.data();
         memset(L, 0, sizeof(*L));
-        uint32_t cap = 0;
+        uint32_t cap = 0, signs = 0; /* signs: a frame of the launch has sign handling */
         auto flush = [&]() {
-            if (L->nframes > 1) P->add(op == 0 ? OP_RC : OP_PACK, 0, chain, L->nblocks, cap, 0, L, sizeof(*L));
-            else if (L->nframes) P->add(op == 0 ? OP_RC1 : OP_PACK1, 0, chain, L->nblocks, cap, 0, &L->job[0], sizeof(L->job[0]));
+            if (L->nframes > 1) P->add(op == 0 ? OP_RC : OP_PACK, 0, chain, L->nblocks, cap, signs, L, sizeof(*L));
+            else if (L->nframes)
+                P->add(op == 0 ? OP_RC1 : OP_PACK1, 0, chain, L->nblocks, cap, signs, &L->job[0], sizeof(L->job[0]));
             memset(L, 0, sizeof(*L));
             cap = 0;
+            signs = 0;
         };
         for (int f : fr) {
             const EncItem& e = it[f];
@@ -468,6 +470,7 @@ static int32_t plan_encode_chain(const std::vector<EncItem>& it, const std::vect
             F.first_block = L->nblocks;
             L->nblocks += (int)e.c->np;
             cap = std::max(cap, e.cap_words);
+            signs |= e.c->fs;
         }
         flush();
     }
@@ -606,7 +609,7 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         switch (o.type) {
         case OP_FWD_V: e = jxs_launch_fwd_v_batch((const FwdVLaunchB*)d, o.kind, (int)o.a, s); break;
         case OP_FWD_H: e = jxs_launch_fwd_h_batch((const FwdHLaunchB*)d, o.kind, o.nblocks, s); break;
-        case OP_RC: e = jxs_launch_rc_batch((const EncPrecLaunch*)d, s); break;
+        case OP_RC: e = jxs_launch_rc_batch((const EncPrecLaunch*)d, (int)o.b, s); break;
         case OP_PACK: e = jxs_launch_pack_batch((const EncPrecLaunch*)d, o.a, s); break;
         case OP_WALK: e = jxs_launch_walk_batch((const DecPrecLaunch*)d, s); break;
         case OP_UNPACK: e = jxs_launch_unpack_batch((const DecPrecLaunch*)d, o.a, o.b, s); break;
@@ -618,7 +621,8 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         case OP_INV_V_S: e = jxs_launch_inv_v((const InvVLaunch*)d, o.kind, o.nblocks, s); break;
         case OP_RC1: {
             const EncPrecFrame* F = (const EncPrecFrame*)d;
-            e = jxs_launch_rc(F->cfg, (uint32_t)o.nblocks, 0, F->gcli, F->coef, F->cost, F->slice_done, F->rc, F->status, s);
+            e = jxs_launch_rc(F->cfg, (uint32_t)o.nblocks, 0, F->gcli, F->coef, F->cost, F->slice_done, F->rc, F->status, (int)o.b,
+                              s);
             break;
         }
         case OP_PACK1: {

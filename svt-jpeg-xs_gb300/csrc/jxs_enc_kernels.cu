@@ -27,7 +27,9 @@
 #define FULL 0xffffffffu
 #define RC_THREADS 512
 #define RC_WARPS (RC_THREADS / 32)
-#define RC_AREA_WORDS (6 * JXS_MAXBLINES * 16)
+/* shared area of the rate control: 5 tables of 16 words per band line, 6
+ * with sign handling */
+#define RC_AREA_WORDS(signs) (((signs) ? 6 : 5) * JXS_MAXBLINES * 16)
 
 /* binary_search_init / binary_search_next_step (BinarySearch.c:9-78) */
 struct BSearch {
@@ -355,6 +357,7 @@ DEV uint32_t nz_levels(uint32_t m, uint32_t g, uint32_t uniform) {
  *   costs       per packet, data / significance / GCLI bytes rounded
  *               separately, raw fallback when cheaper; summed over packets
  *               for every (Q, R). */
+template <bool SIGNS>
 __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
                                              const uint16_t* __restrict__ coef, uint32_t* __restrict__ cost,
                                              uint32_t* __restrict__ slice_done, PrecRC* __restrict__ rc,
@@ -363,17 +366,19 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
      * handling also the coefficients by non-zero levels), then per gtli data
      * / GCLI bits without and with significance and the sign bits; the area
      * is reused by the slice selection at the end */
-    __shared__ __align__(16) uint32_t s_area[RC_AREA_WORDS];
+    __shared__ __align__(16) uint32_t s_area[RC_AREA_WORDS(SIGNS)];
     uint32_t(*hist)[16] = (uint32_t(*)[16])s_area;                          /* later: fast sign bits per t */
     uint32_t(*shist)[16] = (uint32_t(*)[16])(s_area + JXS_MAXBLINES * 16);  /* later: full-sign cost changes */
     uint32_t(*tdat)[16] = (uint32_t(*)[16])(s_area + 2 * JXS_MAXBLINES * 16);
     uint32_t(*tnos)[16] = (uint32_t(*)[16])(s_area + 3 * JXS_MAXBLINES * 16);
     uint32_t(*tsig)[16] = (uint32_t(*)[16])(s_area + 4 * JXS_MAXBLINES * 16);
-    uint32_t(*nzh)[16] = (uint32_t(*)[16])(s_area + 5 * JXS_MAXBLINES * 16);  /* later: full sign bits per t */
+    uint32_t(*nzh)[16] = (uint32_t(*)[16])(s_area + (SIGNS ? 5 : 0) * JXS_MAXBLINES * 16); /* later: full sign bits per t */
     uint32_t(*tfs)[16] = hist;
     uint32_t(*tnz)[16] = nzh;
     uint32_t(*dF)[32] = (uint32_t(*)[32])shist;
-    const uint32_t fs = cfg->fs, uniform = cfg->qpih;
+    /* SIGNS: the launch may hold frames with sign handling (compiled out
+     * otherwise) */
+    const uint32_t fs = SIGNS ? cfg->fs : 0u, uniform = cfg->qpih;
     __shared__ int pmax[JXS_MAXBLINES];
     __shared__ uint32_t cn[JXS_MAXBL][16], cs[JXS_MAXBL][16];
     __shared__ uint16_t meth[JXS_MAXBL];
@@ -402,7 +407,7 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     for (uint32_t i = threadIdx.x; i < nbl * 16; i += blockDim.x) {
         hist[i >> 4][i & 15] = 0;
         shist[i >> 4][i & 15] = 0;
-        nzh[i >> 4][i & 15] = 0;
+        if (SIGNS) nzh[i >> 4][i & 15] = 0;
     }
     for (uint32_t i = threadIdx.x; i < cfg->nbands * 16; i += blockDim.x) {
         cn[i >> 4][i & 15] = 0;
@@ -517,10 +522,12 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
              * t, full signs the coefficients that stay non-zero */
             tdat[x][t] = 4u * (uint32_t)(dsum - (fs ? S0 : 0));
             tnos[x][t] = (uint32_t)dsum + N - (uint32_t)S0;
-            tfs[x][t] = 4u * (uint32_t)S0;
-            const uint32_t zh = nzh[x][t];
-            tnz[x][t] = Z1;
-            Z1 += zh;
+            if (SIGNS) {
+                tfs[x][t] = 4u * (uint32_t)S0;
+                const uint32_t zh = nzh[x][t];
+                tnz[x][t] = Z1;
+                Z1 += zh;
+            }
             S0 += (int)h;
             S1 += t * (int)h;
         }
@@ -553,7 +560,7 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     const int nq = cfg->max_q + 1, nr = cfg->max_r + 1;
     for (int e = threadIdx.x; e < nq * 32; e += blockDim.x) {
         dC[e >> 5][e & 31] = 0;
-        dF[e >> 5][e & 31] = 0;
+        if (SIGNS) dF[e >> 5][e & 31] = 0;
     }
     __syncthreads();
     /* with sign handling each packet adds its sign sub-packet, rounded on
@@ -634,7 +641,7 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    select_slice(cfg, (int)s, cost, s_area, RC_AREA_WORDS, rc, status);
+    select_slice(cfg, (int)s, cost, s_area, RC_AREA_WORDS(SIGNS), rc, status);
     if (threadIdx.x == 0) slice_done[s] = 0; /* ready for the next frame */
 }
 
@@ -1202,16 +1209,18 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
 /* ------------------------------------------------------------------------ */
 /* kernels: one frame, or a batch of frames (block -> frame by its first block) */
 /* ------------------------------------------------------------------------ */
+template <bool SIGNS>
 __global__ void __launch_bounds__(RC_THREADS, 3) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
                                                            const uint16_t* __restrict__ coef, uint32_t* __restrict__ cost,
                                                            uint32_t* __restrict__ slice_done, PrecRC* __restrict__ rc,
                                                            int* __restrict__ status) {
-    rc_cost_body(cfg, gcli, coef, cost, slice_done, rc, status, (int)blockIdx.x);
+    rc_cost_body<SIGNS>(cfg, gcli, coef, cost, slice_done, rc, status, (int)blockIdx.x);
 }
 
+template <bool SIGNS>
 __global__ void __launch_bounds__(RC_THREADS, 3) rc_cost_batch_kernel(const __grid_constant__ EncPrecLaunch L) {
     const EncPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
-    rc_cost_body(F.cfg, F.gcli, F.coef, F.cost, F.slice_done, F.rc, F.status, (int)blockIdx.x - F.first_block);
+    rc_cost_body<SIGNS>(F.cfg, F.gcli, F.coef, F.cost, F.slice_done, F.rc, F.status, (int)blockIdx.x - F.first_block);
 }
 
 __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
@@ -1230,9 +1239,10 @@ __global__ void __launch_bounds__(PK_THREADS, 3) pack_batch_kernel(const __grid_
 /* ------------------------------------------------------------------------ */
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli,
                                      const uint16_t* coef, uint32_t* cost, uint32_t* slice_done, PrecRC* rc, int* status,
-                                     cudaStream_t st) {
+                                     int signs, cudaStream_t st) {
     (void)nslices;
-    rc_cost_kernel<<<np, RC_THREADS, 0, st>>>(dcfg, gcli, coef, cost, slice_done, rc, status);
+    if (signs) rc_cost_kernel<true><<<np, RC_THREADS, 0, st>>>(dcfg, gcli, coef, cost, slice_done, rc, status);
+    else rc_cost_kernel<false><<<np, RC_THREADS, 0, st>>>(dcfg, gcli, coef, cost, slice_done, rc, status);
     return cudaGetLastError();
 }
 
@@ -1246,9 +1256,10 @@ extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, cudaStream_t st) {
+extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, int signs, cudaStream_t st) {
     if (L->nblocks <= 0) return cudaSuccess;
-    rc_cost_batch_kernel<<<L->nblocks, RC_THREADS, 0, st>>>(*L);
+    if (signs) rc_cost_batch_kernel<true><<<L->nblocks, RC_THREADS, 0, st>>>(*L);
+    else rc_cost_batch_kernel<false><<<L->nblocks, RC_THREADS, 0, st>>>(*L);
     return cudaGetLastError();
 }
 

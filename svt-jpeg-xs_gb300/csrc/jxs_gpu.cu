@@ -315,7 +315,7 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
         KMARK();
     }
     TMARK(2);
-    CK(jxs_launch_rc(e->dcfg, c->np, c->nslices, s->gcli, s->coef, s->cost, s->slice_done, s->rc, s->status, st));
+    CK(jxs_launch_rc(e->dcfg, c->np, c->nslices, s->gcli, s->coef, s->cost, s->slice_done, s->rc, s->status, (int)c->fs, st));
     KMARK();
     TMARK(3);
     const int out_dev = jxs_gpu_is_device_ptr(out);

@@ -26,8 +26,8 @@ extern "C" int jxs_fwd_v_tile_cols(void);
 extern "C" int jxs_fwd_h_max_rows_per_block(void);
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli,
                                      const uint16_t* coef, uint32_t* cost, uint32_t* slice_done, PrecRC* rc, int* status,
-                                     cudaStream_t st);
-extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, cudaStream_t st);
+                                     int signs, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, int signs, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
                                        const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_pack_batch(const EncPrecLaunch* L, uint32_t cap_words, cudaStream_t st);
