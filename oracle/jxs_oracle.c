@@ -568,8 +568,6 @@ static int enc_configure(enc_t* e, const or_enc_params_t* p) {
         else { mh = 0; break; }
     }
     if (mw == 0 || mh == 0) return E_BAD_PARAM;
-    /* This restatement covers the encoder with vertical prediction off. */
-    if (c->coding_vertical_prediction_mode != 0) return E_BAD_PARAM;
     int r = geom_compute(&e->g, 1, nc, c->width, c->height, c->decomp_h, c->decomp_v, 0, sx, sy, c->slice_height);
     if (r) return r;
     if (weights_assign(&e->g, c->colour_format)) return E_BAD_PARAM;
@@ -638,7 +636,7 @@ static void enc_write_header(enc_t* e) {
     bw_put(&w, 1, 1);                          /* Rl */
     bw_put(&w, e->prm.quantization, 2);        /* Qpih */
     bw_put(&w, e->prm.coding_signs_handling ? 1 : 0, 2); /* Fs */
-    bw_put(&w, 0, 2);                          /* Rm */
+    bw_put(&w, e->prm.coding_vertical_prediction_mode == 2 ? 1 : 0, 2); /* Rm (EncHandle.c:250-253) */
     bw_put(&w, 0xff13, 16);                    /* CDT */
     bw_put(&w, 2 * g->nc + 2, 16);
     for (uint32_t c = 0; c < g->nc; c++) {
@@ -756,9 +754,16 @@ typedef struct {
     uint32_t lines[MAXC][MAXB];
 } prec_stats_t;
 
+/* Vertical prediction: the precinct row above in the same slice (its
+ * GCLIs and final gtli per band), NULL for a slice's first row. */
+typedef struct {
+    uint32_t p;               /* its precinct row */
+    uint8_t gtli[MAXC][MAXB]; /* its gtli per band */
+} vp_top_t;
+
 typedef struct {
     uint8_t gtli[MAXC][MAXB];
-    uint8_t sig_method[MAXC][MAXB];
+    uint8_t sig_method[MAXC][MAXB]; /* D[p,b]: bit 1 significance, bit 0 vertical prediction */
     uint32_t data_bits[MAXC][MAXB][2], gcli_bits[MAXC][MAXB][2], sig_bits[MAXC][MAXB][2];
     uint8_t raw[MAXPK];
     uint32_t pk_data[MAXPK], pk_gcli[MAXPK], pk_sig[MAXPK], pk_sign[MAXPK];
@@ -816,7 +821,47 @@ static void prec_stats(const enc_t* e, uint32_t p, int last, prec_stats_t* st) {
  * and each packet adds a sign sub-packet: SIGNS_FAST counts every
  * coefficient of a group above gtli, SIGNS_FULL only those that stay
  * non-zero (RateControl.c:505-523). */
-static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint8_t q, uint8_t r, prec_cost_t* pc, int smode) {
+/* vlc_encode_get_bits (PackPrecinct.h:86-104): ones of the unary code of
+ * x for the vertical prediction range (r, t). */
+static uint32_t vlc_vp_bits(int32_t x, int32_t r, int32_t t) {
+    int32_t mx = r - t;
+    if (mx < 0) mx = 0;
+    if (x > mx) return (uint32_t)(x + mx);
+    x *= 2;
+    return (uint32_t)(x < 0 ? -x - 1 : x);
+}
+
+/* GCLI line `cur` coded from the line above `top` (rate_control_calc_vpred_
+ * cost_nosigf_c / _sigf_c, RateControl.c:290-347): the unary bits of every
+ * GCLI, and the significance groups that need no code (run mode Rm: groups
+ * with every GCLI <= gtli; otherwise groups predicted exactly).  Returns
+ * the bits without significance; `*reduction` the bits the skipped groups
+ * save; `flags` (optional) one byte per significance group. */
+static uint32_t vp_line_cost(const uint8_t* cur, const uint8_t* top, uint32_t gcli_w, uint32_t sig_w, int gtli, int gtli_top,
+                             int rm, uint32_t* reduction, uint8_t* flags, uint8_t* bits_out) {
+    const int gmax = MAX(gtli, gtli_top);
+    uint32_t total = 0, red = 0;
+    for (uint32_t s2 = 0; s2 < sig_w; s2++) {
+        const uint32_t i0 = s2 * 8, i1 = MIN(i0 + 8, gcli_w);
+        int flag = 1;
+        uint32_t grp = 0;
+        for (uint32_t i = i0; i < i1; i++) {
+            const int m_top = MAX((int)top[i], gmax), gv = MAX((int)cur[i], gtli);
+            const uint32_t b = vlc_vp_bits(gv - m_top, m_top, gtli);
+            if (bits_out) bits_out[i] = (uint8_t)b;
+            grp += b + 1;
+            if (rm ? ((int)cur[i] > gtli) : (m_top != gv)) flag = 0;
+        }
+        total += grp;
+        if (flag) red += grp;
+        if (flags) flags[s2] = (uint8_t)flag;
+    }
+    *reduction = red;
+    return total;
+}
+
+static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint8_t q, uint8_t r, prec_cost_t* pc, int smode,
+                          uint32_t p, const vp_top_t* top) {
     const geom_t* g = &e->g;
     uint32_t sign_bits[MAXC][MAXB][2];
     for (uint32_t c = 0; c < g->nc; c++)
@@ -855,11 +900,42 @@ static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint
                 gsig[l] = nosig[l] - zeroed;
                 total_sig += gsig[l];
             }
-            int use_sig = e->prm.coding_significance && total_nosig > total_sig;
-            pc->sig_method[c][b] = (uint8_t)use_sig;
+            /* the cheapest coding of the band's GCLIs, a later method only
+             * if strictly cheaper (RateControl.c:526-676) */
+            int method = 0;
+            uint32_t best = total_nosig;
+            if (e->prm.coding_significance && best > total_sig) {
+                method = 2;
+                best = total_sig;
+            }
+            uint32_t vnos[2] = {0, 0}, vsig[2] = {0, 0};
+            if (top) {
+                uint32_t tot_vn = 0, tot_vs = 0;
+                for (uint32_t l = 0; l < lines; l++) {
+                    const size_t row = (size_t)(p * bd->lines + l);
+                    const uint8_t* cur = e->gcli[c][b] + row * bd->gcli_w;
+                    const uint8_t* tl = l ? cur - bd->gcli_w : e->gcli[c][b] + ((size_t)top->p * bd->lines + bd->lines - 1) * bd->gcli_w;
+                    const int tt = l ? t : top->gtli[c][b];
+                    uint32_t red = 0;
+                    vnos[l] = vp_line_cost(cur, tl, bd->gcli_w, bd->sig_w, t, tt, e->prm.coding_vertical_prediction_mode == 2,
+                                           &red, NULL, NULL);
+                    vsig[l] = vnos[l] - red;
+                    tot_vn += vnos[l];
+                    tot_vs += vsig[l] + bd->sig_w;
+                }
+                if (best > tot_vn) {
+                    method = 1;
+                    best = tot_vn;
+                }
+                if (e->prm.coding_significance && best > tot_vs) {
+                    method = 3;
+                    best = tot_vs;
+                }
+            }
+            pc->sig_method[c][b] = (uint8_t)method;
             for (uint32_t l = 0; l < lines; l++) {
-                pc->gcli_bits[c][b][l] = use_sig ? gsig[l] : nosig[l];
-                pc->sig_bits[c][b][l] = use_sig ? bd->sig_w : 0;
+                pc->gcli_bits[c][b][l] = method == 0 ? nosig[l] : method == 2 ? gsig[l] : method == 1 ? vnos[l] : vsig[l];
+                pc->sig_bits[c][b][l] = (method & 2) ? bd->sig_w : 0;
             }
         }
     uint32_t total = 0;
@@ -931,7 +1007,7 @@ static int bs_next(bsearch_t* s, int res, uint32_t* out) {
 /* rate_control_precinct (RateControl.c:1259-1333) with the binary searches of
  * RateControl.c:889-1083.  Returns 0 and fills q, r, data_bytes, headers. */
 static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t budget, uint8_t* q_out, uint8_t* r_out,
-                   uint32_t* data_bytes, uint32_t* hdr_bytes, prec_cost_t* pc) {
+                   uint32_t* data_bytes, uint32_t* hdr_bytes, prec_cost_t* pc, uint32_t p, const vp_top_t* top) {
     const geom_t* g = &e->g;
     if (budget > PREC_MAX_BYTES) return E_ENC_FRAME;
     uint32_t hdr = DIV_UP(5 * 8 + g->nbands_exist * 2, 8);
@@ -953,20 +1029,20 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
     uint32_t qv = 0;
     while ((res = bs_next(&s, next, &qv)) == BS_CONTINUE) {
         if (all_truncated(g, (uint8_t)qv, 0)) { next = BS_OUT_OF_RANGE; continue; }
-        next = prec_cost(e, st, last, (uint8_t)qv, 0, pc, sfast) > avail ? BS_TOO_SMALL : BS_TOO_BIG;
+        next = prec_cost(e, st, last, (uint8_t)qv, 0, pc, sfast, p, NULL) > avail ? BS_TOO_SMALL : BS_TOO_BIG;
     }
     if (res != BS_FOUND) return E_ENC_FRAME;
     uint8_t q = (uint8_t)qv;
-    if (smode == SIGNS_FULL) {
+    if (smode == SIGNS_FULL || e->prm.coding_vertical_prediction_mode) {
         /* lower quantizations while they fit, else the first higher that fits */
         int best = -1;
         for (int qt = (int)q - 1; qt >= 0; qt--) {
-            if (all_truncated(g, (uint8_t)qt, 0) || prec_cost(e, st, last, (uint8_t)qt, 0, pc, smode) > avail) break;
+            if (all_truncated(g, (uint8_t)qt, 0) || prec_cost(e, st, last, (uint8_t)qt, 0, pc, smode, p, top) > avail) break;
             best = qt;
         }
         if (best < 0)
             for (uint32_t qt = q; qt <= e->max_q; qt++)
-                if (!all_truncated(g, (uint8_t)qt, 0) && prec_cost(e, st, last, (uint8_t)qt, 0, pc, smode) <= avail) {
+                if (!all_truncated(g, (uint8_t)qt, 0) && prec_cost(e, st, last, (uint8_t)qt, 0, pc, smode, p, top) <= avail) {
                     best = (int)qt;
                     break;
                 }
@@ -984,7 +1060,7 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
     while ((res = bs_next(&s, next, &rv)) == BS_CONTINUE) {
         last_tested = -1;
         if (all_truncated(g, q, (uint8_t)rv)) { next = BS_OUT_OF_RANGE; continue; }
-        uint32_t cst = prec_cost(e, st, last, q, (uint8_t)rv, pc, smode);
+        uint32_t cst = prec_cost(e, st, last, q, (uint8_t)rv, pc, smode, p, top);
         last_tested = (int32_t)rv;
         last_cost = cst;
         next = cst <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
@@ -993,7 +1069,7 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
     (void)last_tested;
     (void)last_cost;
     /* The pack step needs the per-packet decisions of the chosen pair. */
-    *data_bytes = prec_cost(e, st, last, q, (uint8_t)rv, pc, smode);
+    *data_bytes = prec_cost(e, st, last, q, (uint8_t)rv, pc, smode, p, top);
     *q_out = q;
     *r_out = (uint8_t)rv;
     return E_NONE;
@@ -1015,14 +1091,14 @@ static inline uint16_t quantize(uint16_t v, uint8_t gcli, uint8_t t, uint32_t un
     return m ? (uint16_t)(m | sign) : 0;
 }
 
-/* pack_precinct (Source/Lib/Encoder/Codec/PackPrecinct.c:235-572), vertical
- * prediction off.  With sign handling the data sub-packet carries no sign
+/* pack_precinct (Source/Lib/Encoder/Codec/PackPrecinct.c:235-572).  `top`
+ * is the row above for vertically predicted bands.  With sign handling the data sub-packet carries no sign
  * nibbles and a sign sub-packet follows it: one bit per non-zero quantized
  * coefficient of the groups above gtli (pack_sign_c, :200-233).  Returns
  * non-zero when a sign sub-packet differs from the size the rate control
  * computed. */
 static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc, uint8_t q, uint8_t r, uint32_t total_bytes,
-                      bw_t* w) {
+                     bw_t* w, const vp_top_t* top) {
     const geom_t* g = &e->g;
     uint32_t hdr_len = DIV_UP(5 * 8 + 2 * g->nbands_exist, 8);
     bw_put(w, total_bytes - hdr_len, 24);
@@ -1032,7 +1108,7 @@ static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc
         if (g->gband[i] == NOBAND) continue;
         uint32_t c = g->gcomp[i], b = g->gband[i];
         uint32_t lines = last ? g->c[c].b[b].last_lines : g->c[c].b[b].lines;
-        bw_put(w, (lines > 0 && pc->sig_method[c][b]) ? 2 : 0, 2);
+        bw_put(w, lines > 0 ? pc->sig_method[c][b] : 0, 2);
     }
     bw_align(w);
     const uint32_t uniform = e->prm.quantization;
@@ -1068,12 +1144,28 @@ static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc
             }
             bw_align(w);
         } else {
+            /* vertical prediction of a line: its codes and flags
+             * (pack_bitplane_count_vpred_*, PackPrecinct.c:47-74) */
+            uint8_t vbits[MAXGB][2048], vflags[MAXGB][256];
             for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
                 uint32_t c = g->gcomp[i], b = g->gband[i];
                 const band_t* bd = &g->c[c].b[b];
-                if (l >= (last ? bd->last_lines : bd->lines) || !pc->sig_method[c][b]) continue;
+                if (l >= (last ? bd->last_lines : bd->lines) || !(pc->sig_method[c][b] & 1)) continue;
+                if (bd->gcli_w > 2048 || bd->sig_w > 256) return E_RESOURCES;
+                const size_t row = (size_t)(p * bd->lines + l);
+                const uint8_t* cur = e->gcli[c][b] + row * bd->gcli_w;
+                const uint8_t* tl = l ? cur - bd->gcli_w : e->gcli[c][b] + ((size_t)top->p * bd->lines + bd->lines - 1) * bd->gcli_w;
+                uint32_t red;
+                vp_line_cost(cur, tl, bd->gcli_w, bd->sig_w, pc->gtli[c][b], l ? pc->gtli[c][b] : top->gtli[c][b],
+                             e->prm.coding_vertical_prediction_mode == 2, &red, vflags[i - g->pk[k].bs], vbits[i - g->pk[k].bs]);
+            }
+            for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
+                uint32_t c = g->gcomp[i], b = g->gband[i];
+                const band_t* bd = &g->c[c].b[b];
+                if (l >= (last ? bd->last_lines : bd->lines) || !(pc->sig_method[c][b] & 2)) continue;
                 const uint8_t* sm = e->sigmax[c][b] + (size_t)(p * bd->lines + l) * bd->sig_w;
-                for (uint32_t s = 0; s < bd->sig_w; s++) bw_put(w, sm[s] <= pc->gtli[c][b], 1);
+                for (uint32_t s = 0; s < bd->sig_w; s++)
+                    bw_put(w, (pc->sig_method[c][b] & 1) ? vflags[i - g->pk[k].bs][s] : sm[s] <= pc->gtli[c][b], 1);
             }
             bw_align(w);
             for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
@@ -1081,13 +1173,20 @@ static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc
                 const band_t* bd = &g->c[c].b[b];
                 if (l >= (last ? bd->last_lines : bd->lines)) continue;
                 const uint8_t t = pc->gtli[c][b];
+                const uint8_t meth = pc->sig_method[c][b];
                 const uint8_t* gl = e->gcli[c][b] + (size_t)(p * bd->lines + l) * bd->gcli_w;
                 const uint8_t* sm = e->sigmax[c][b] + (size_t)(p * bd->lines + l) * bd->sig_w;
                 for (uint32_t x = 0; x < bd->gcli_w; x++) {
-                    if (pc->sig_method[c][b] && sm[x / 8] <= t) continue;
-                    uint32_t n = gl[x] > t ? (uint32_t)(gl[x] - t) : 0;
+                    uint32_t n;
+                    if (meth & 1) {
+                        if ((meth & 2) && vflags[i - g->pk[k].bs][x / 8]) continue;
+                        n = vbits[i - g->pk[k].bs][x];
+                    } else {
+                        if ((meth & 2) && sm[x / 8] <= t) continue;
+                        n = gl[x] > t ? (uint32_t)(gl[x] - t) : 0;
+                    }
                     /* unary: n ones then a zero (vlc_encode_pack_bits, PackPrecinct.h:25-39) */
-                    bw_put(w, ((1u << n) - 1) << 1, n + 1);
+                    bw_put(w, (uint32_t)(((1ull << n) - 1) << 1), n + 1);
                 }
             }
             bw_align(w);
@@ -1194,7 +1293,7 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     while ((res = bs_next(&s, next, &qv)) == BS_CONTINUE) {
         if (all_truncated(g, (uint8_t)qv, 0)) { next = BS_OUT_OF_RANGE; continue; }
         uint32_t sum = 0;
-        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, (uint8_t)qv, 0, &pc, sfast);
+        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, (uint8_t)qv, 0, &pc, sfast, first_p + i, NULL);
         next = sum > avail ? BS_TOO_SMALL : BS_TOO_BIG;
     }
     if (res != BS_FOUND) {
@@ -1210,7 +1309,7 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     while ((res = bs_next(&s, next, &rv)) == BS_CONTINUE) {
         if (all_truncated(g, q, (uint8_t)rv)) { next = BS_OUT_OF_RANGE; continue; }
         uint32_t sum = 0;
-        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc, sfast);
+        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc, sfast, first_p + i, NULL);
         next = sum <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
     }
     if (res != BS_FOUND) {
@@ -1219,7 +1318,7 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     }
     uint32_t pad_last = avail;
     for (uint32_t i = 0; i < nprec; i++) {
-        const uint32_t d = prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc, sfast);
+        const uint32_t d = prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc, sfast, first_p + i, NULL);
         pad_last -= d;
         total[i] += d;
     }
@@ -1316,6 +1415,9 @@ static void enc_slice(void* ctx, uint32_t s) {
     uint32_t carry = 0;
     prec_stats_t st;
     prec_cost_t pc;
+    /* vertical prediction: the row above in the slice, with its final gtli */
+    vp_top_t top_rows[2];
+    const vp_top_t* top = NULL;
     for (uint32_t i = 0; i < nprec; i++) {
         uint32_t p = first_p + i;
         int last = (p + 1 >= g->np);
@@ -1323,7 +1425,7 @@ static void enc_slice(void* ctx, uint32_t s) {
         prec_stats(e, p, last, &st);
         uint8_t q = 0, r = 0;
         uint32_t data = 0, hdr = 0;
-        int err = prec_rc(e, &st, last, budget, &q, &r, &data, &hdr, &pc);
+        int err = prec_rc(e, &st, last, budget, &q, &r, &data, &hdr, &pc, p, top);
         if (err) {
             free(common);
             e->slice_err = err;
@@ -1337,7 +1439,7 @@ static void enc_slice(void* ctx, uint32_t s) {
          * precinct and in mode 0 (PackStageProcess.c:293-333) */
         uint32_t retrieve = 0;
         if (e->prm.coding_signs_handling == SIGNS_FAST) {
-            retrieve = data - prec_cost(e, &st, last, q, r, &pc, SIGNS_FULL);
+            retrieve = data - prec_cost(e, &st, last, q, r, &pc, SIGNS_FULL, p, top);
         }
         /* modes 1-3 move a precinct's padding to the next one */
         if (e->prm.rate_control_mode >= 1 && i + 1 < nprec) {
@@ -1353,10 +1455,16 @@ static void enc_slice(void* ctx, uint32_t s) {
             bw_put(&w, s, 16);
         }
         uint64_t start = w.bit;
-        if (prec_pack(e, p, last, &pc, q, r, total, &w) || ((w.bit - start) >> 3) != hdr + data - retrieve) {
+        if (prec_pack(e, p, last, &pc, q, r, total, &w, top) || ((w.bit - start) >> 3) != hdr + data - retrieve) {
             free(common);
             e->slice_err = E_ENC_FRAME;
             return;
+        }
+        if (e->prm.coding_vertical_prediction_mode) {
+            vp_top_t* nt = &top_rows[i & 1];
+            nt->p = p;
+            memcpy(nt->gtli, pc.gtli, sizeof(nt->gtli));
+            top = nt;
         }
         uint64_t used = (w.bit - start) >> 3;
         for (uint64_t z = used; z < total; z++) bw_put(&w, 0, 8);
