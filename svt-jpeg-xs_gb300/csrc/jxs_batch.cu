@@ -189,7 +189,7 @@ static uint64_t enc_work_layout(const jxs_cfg_t* c, uint8_t* base, EncWork* w) {
     ll_layout(c, w->fb.ll_pitch, llsz);
     for (int v = 0; v < 2; v++)
         for (int k = 0; k < JXS_MAXC; k++) w->fb.ll[v][k] = llsz[v][k] ? (int32_t*)take(llsz[v][k]) : nullptr;
-    w->cost = (uint32_t*)take((uint64_t)c->np * 1024 * sizeof(uint32_t) * (c->fs ? 2 : 1));
+    w->cost = (uint32_t*)take(jxs_cost_bytes(c));
     w->slice_done = (uint32_t*)take((uint64_t)c->nslices * sizeof(uint32_t));
     w->rc = (PrecRC*)take((uint64_t)c->np * sizeof(PrecRC));
     w->out_stage = take((uint64_t)c->lcod + 64);
@@ -446,7 +446,7 @@ static int32_t plan_encode_chain(const std::vector<EncItem>& it, const std::vect
     for (int op = 0; op < 2; op++) {
         EncPrecLaunch* L = (EncPrecLaunch*)scratch.data();
         memset(L, 0, sizeof(*L));
-        uint32_t cap = 0, signs = 0; /* signs: a frame of the launch has sign handling */
+        uint32_t cap = 0, signs = 0; /* rate-control variant: bit 0 sign handling, bit 1 vertical prediction */
         auto flush = [&]() {
             if (L->nframes > 1) P->add(op == 0 ? OP_RC : OP_PACK, 0, chain, L->nblocks, cap, signs, L, sizeof(*L));
             else if (L->nframes)
@@ -470,7 +470,7 @@ static int32_t plan_encode_chain(const std::vector<EncItem>& it, const std::vect
             F.first_block = L->nblocks;
             L->nblocks += (int)e.c->np;
             cap = std::max(cap, e.cap_words);
-            signs |= e.c->fs;
+            signs |= (e.c->fs ? 1u : 0u) | (e.c->vpred ? 2u : 0u);
         }
         flush();
     }
@@ -610,7 +610,7 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         case OP_FWD_V: e = jxs_launch_fwd_v_batch((const FwdVLaunchB*)d, o.kind, (int)o.a, s); break;
         case OP_FWD_H: e = jxs_launch_fwd_h_batch((const FwdHLaunchB*)d, o.kind, o.nblocks, s); break;
         case OP_RC: e = jxs_launch_rc_batch((const EncPrecLaunch*)d, (int)o.b, s); break;
-        case OP_PACK: e = jxs_launch_pack_batch((const EncPrecLaunch*)d, o.a, s); break;
+        case OP_PACK: e = jxs_launch_pack_batch((const EncPrecLaunch*)d, o.a, (int)o.b, s); break;
         case OP_WALK: e = jxs_launch_walk_batch((const DecPrecLaunch*)d, s); break;
         case OP_UNPACK: e = jxs_launch_unpack_batch((const DecPrecLaunch*)d, o.a, o.b, s); break;
         case OP_INV_H: e = jxs_launch_inv_h_batch((const InvHLaunchB*)d, o.kind, o.nblocks, s); break;
@@ -627,7 +627,7 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         }
         case OP_PACK1: {
             const EncPrecFrame* F = (const EncPrecFrame*)d;
-            e = jxs_launch_pack(F->cfg, (uint32_t)o.nblocks, F->coef, F->gcli, F->rc, F->out, o.a, F->status, s);
+            e = jxs_launch_pack(F->cfg, (uint32_t)o.nblocks, F->coef, F->gcli, F->rc, F->out, o.a, F->status, (int)o.b, s);
             break;
         }
         case OP_WALK1: {

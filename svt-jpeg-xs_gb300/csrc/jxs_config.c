@@ -556,9 +556,7 @@ int32_t jxs_cfg_encoder(jxs_cfg_t* g, struct svt_jpeg_xs_encoder_api* api) {
         else { mh = 0; break; }
     }
     if (mw == 0 || mh == 0) return JXS_E_BAD_PARAM;
-    /* The GPU encoder implements vertical prediction off, with every
-     * rate-control mode (0-3) and sign handling off, fast or full. */
-    if (api->coding_vertical_prediction_mode != 0 || api->rate_control_mode > 3) return JXS_E_BAD_PARAM;
+    if (api->rate_control_mode > 3) return JXS_E_BAD_PARAM;
 
     int32_t r = jxs_cfg_geometry(g, 1, nc, api->source_width, api->source_height, api->ndecomp_h, api->ndecomp_v, 0, sx, sy,
                                  api->slice_height);
@@ -570,7 +568,8 @@ int32_t jxs_cfg_encoder(jxs_cfg_t* g, struct svt_jpeg_xs_encoder_api* api) {
     g->rc_mode = api->rate_control_mode;
     g->signs = api->coding_signs_handling;
     g->fs = g->signs ? 1 : 0; /* hdr_Fs (EncHandle.c:278) */
-    g->rm = 0;
+    g->vpred = api->coding_vertical_prediction_mode;
+    g->rm = g->vpred == 2 ? 1 : 0; /* hdr_Rm (EncHandle.c:250-253) */
     g->bw = 20;
     g->fq = 8;
     g->lcod = (uint32_t)bpf;

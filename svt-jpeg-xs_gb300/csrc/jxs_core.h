@@ -101,6 +101,7 @@ typedef struct jxs_cfg {
     uint32_t hdrs_bytes[2];              /* precinct header + packet headers */
     uint32_t qpih, sig, rc_mode, fs, rm, bw, fq;
     uint32_t signs;                      /* encoder sign handling: 0 off, 1 fast, 2 full */
+    uint32_t vpred;                      /* encoder vertical prediction: 0 off, 1 (Rm 0), 2 (Rm 1, zero coefficients) */
     uint8_t max_q, max_r;
     uint32_t empty[32];                  /* bit r of empty[q]: every band fully truncated */
     uint32_t lcod;

@@ -65,265 +65,512 @@ DEV int bs_next(BSearch& s, int res, int* out) {
     return BS_CONTINUE;
 }
 
-/* One slice's precinct budgets with the padding carry of rate-control
- * mode 1 (PackStageProcess.c:600-684, 293-309) and rate_control_precinct
- * (RateControl.c:1259-1333) with its binary searches (:889-1083), evaluated
- * on the slice's cost tables.  Run by a whole block: the tables of up to
- * `area_words / (nq * nr)` precincts are read (through L2) into `area` at a
- * time; thread 0 then runs their searches in order.
- *
- * With sign handling each precinct has two tables: signs counted the fast
- * way (every coefficient of a group above gtli) and exactly.  The
- * quantization search runs on the fast table; the full strategy then steps
- * from its result on the exact table and searches the refinement there.
- * The fast strategy sends only the signs it needs: the bytes this frees are
- * cut from the precinct and carried to the next one with its padding, or
- * stay as padding in a slice's last precinct and in mode 0
- * (PackPrecinct.c:513-536, PackStageProcess.c:293-333, 526-560). */
+/* A slice's even split of its budget over its precincts
+ * (PackStageProcess.c:600-684): mode 1 gives the first precinct 10 % more
+ * (20 % with fast signs, :34-35). */
+struct SliceSplit {
+    uint32_t slice_budget, first_p, nprec, first_b, min_b, left;
+};
+DEV SliceSplit slice_split(const jxs_cfg_t* __restrict__ cfg, int s) {
+    SliceSplit o;
+    const int last_slice = (s + 1 == (int)cfg->nslices);
+    o.slice_budget = cfg->slice_size[s] - 6 - (last_slice ? 2 : 0);
+    o.first_p = cfg->pps * s;
+    o.nprec = last_slice ? cfg->np - o.first_p : cfg->pps;
+    o.min_b = o.slice_budget / o.nprec;
+    o.left = o.slice_budget - o.min_b * o.nprec;
+    o.first_b = o.min_b;
+    if (cfg->rc_mode == 1) {
+        o.first_b = min(o.slice_budget, o.first_b * (cfg->signs == 1 ? 120u : 110u) / 100);
+        if (o.nprec > 1) {
+            o.min_b = (o.slice_budget - o.first_b) / (o.nprec - 1);
+            o.left = o.slice_budget - o.min_b * (o.nprec - 1) - o.first_b;
+        } else {
+            o.left = 0;
+        }
+    }
+    return o;
+}
+
+/* The precinct searches of rate_control_precinct (RateControl.c:1259-1333,
+ * binary searches :889-1083), by one thread on tables in shared memory
+ * ([q * nr + r]): the quantization by binary
+ * search on T[q * nr]; with `scan` (full signs, vertical prediction) then
+ * lower quantizations while TS fits, else the first higher one that fits
+ * (:936-1015); the refinement by binary search on TS.  Returns an error
+ * code, 0 when q, r and data (TS at (q, r)) are set. */
+DEV int prec_search(const uint32_t* T, const uint32_t* TS, int ld, int scan, int nr, int max_q, int max_r,
+                    const uint32_t* __restrict__ s_empty, uint32_t avail, int& q, int& r, uint32_t& data) {
+    BSearch bs;
+    int step = 6;
+    if (step > max_q) step = 0;
+    bs_init(bs, 0, max_q, 0, step);
+    int res, next = BS_BEGIN, v = 0;
+    while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
+        if (s_empty[v] & 1u) next = BS_OUT_OF_RANGE;
+        else next = T[v * nr] > avail ? BS_TOO_SMALL : BS_TOO_BIG;
+    }
+    if (res != BS_FOUND) return JXS_E_ENC_FRAME;
+    q = v;
+    if (scan) {
+        int best = -1;
+        for (int qt = q - 1; qt >= 0; qt--) {
+            if ((s_empty[qt] & 1u) || TS[qt * ld] > avail) break;
+            best = qt;
+        }
+        if (best < 0)
+            for (int qt = q; qt <= max_q; qt++)
+                if (!(s_empty[qt] & 1u) && TS[qt * ld] <= avail) {
+                    best = qt;
+                    break;
+                }
+        if (best < 0) return JXS_E_ENC_FRAME;
+        q = best;
+    }
+    step = 6;
+    if (step >= max_r) step = 0;
+    bs_init(bs, 0, max_r, 1, step);
+    next = BS_BEGIN;
+    while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
+        if ((s_empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
+        else next = TS[q * ld + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
+    }
+    if (res != BS_FOUND) return JXS_E_ENC_FRAME;
+    r = v;
+    data = TS[q * ld + r];
+    return 0;
+}
+
+/* RC modes 2 and 3, per-slice common quantization (process_slice,
+ * PackStageProcess.c:339-483; RateControl.c:1086-1209, 1336-1425): the
+ * (fast-sign) data bytes of every (Q, R) summed over the slice's precincts
+ * into `area`, one (Q, R) for the slice by the precinct searches, then the
+ * budget of each precinct, kept in rc[p].total_bytes.  Run by a whole
+ * block; returns the error (every thread). */
+DEV int slice_common(const jxs_cfg_t* __restrict__ cfg, int s, const SliceSplit& sp, const uint32_t* __restrict__ cost,
+                     uint32_t* area, const uint32_t* __restrict__ s_empty, PrecRC* __restrict__ rc, int* __restrict__ status) {
+    __shared__ int s_cerr;
+    const int nq = cfg->max_q + 1, nr = cfg->max_r + 1, nt = nq * nr;
+    const int max_q = cfg->max_q, max_r = cfg->max_r, rc_mode = (int)cfg->rc_mode;
+    const uint32_t np_all = cfg->np, hdrs0 = cfg->hdrs_bytes[0], hdrs1 = cfg->hdrs_bytes[1];
+    const uint32_t first_p = sp.first_p, nprec = sp.nprec, slice_budget = sp.slice_budget;
+    __syncthreads();
+    for (int e = threadIdx.x; e < nt; e += blockDim.x) {
+        const int q = e / nr, r = e - q * nr;
+        uint32_t sum = 0;
+        for (uint32_t i = 0; i < nprec; i++) sum += __ldcg(cost + (uint64_t)(first_p + i) * 1024 + q * 32 + r);
+        area[e] = sum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int err = 0;
+        uint32_t headers = 0;
+        for (uint32_t i = 0; i < nprec; i++) headers += first_p + i + 1 >= np_all ? hdrs1 : hdrs0;
+        if ((slice_budget + nprec - 1) / nprec > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
+        else if (slice_budget <= headers) err = JXS_E_UNDEFINED;
+        int q = 0, r = 0;
+        uint32_t dsum = 0;
+        if (!err) err = prec_search(area, area, nr, 0, nr, max_q, max_r, s_empty, slice_budget - headers, q, r, dsum);
+        if (!err) {
+            /* each precinct its headers and data at (Q, R); the last also
+             * the slice's remaining bytes */
+            uint32_t pad_last = slice_budget - headers;
+            for (uint32_t i = 0; i < nprec; i++) {
+                const uint32_t p = first_p + i;
+                const uint32_t d = __ldcg(cost + (uint64_t)p * 1024 + q * 32 + r);
+                pad_last -= d;
+                rc[p].total_bytes = (p + 1 >= np_all ? hdrs1 : hdrs0) + d;
+            }
+            rc[first_p + nprec - 1].total_bytes += pad_last;
+            if (rc_mode == 3) {
+                /* RC_CBR_PER_SLICE_COMMON_QUANT_MAX_RATE: no precinct below a
+                 * quarter of the largest, padding excluded */
+                uint32_t max_size = 0;
+                for (uint32_t i = 0; i < nprec; i++)
+                    max_size = max(max_size, rc[first_p + i].total_bytes - (i + 1 == nprec ? pad_last : 0u));
+                const uint32_t min_size = max_size / 4;
+                uint32_t need = 0;
+                for (uint32_t i = 0; i < nprec; i++) {
+                    const uint32_t ds = rc[first_p + i].total_bytes - (i + 1 == nprec ? pad_last : 0u);
+                    if (ds < min_size) {
+                        rc[first_p + i].total_bytes += min_size - ds;
+                        need += min_size - ds;
+                    }
+                }
+                if (need) {
+                    if (pad_last >= need) {
+                        pad_last -= need;
+                        rc[first_p + nprec - 1].total_bytes -= need;
+                    } else {
+                        need -= pad_last;
+                        rc[first_p + nprec - 1].total_bytes -= pad_last;
+                        pad_last = 0;
+                        /* the rest one byte at a time, round robin */
+                        const uint32_t each = need / nprec, extra = need - each * nprec;
+                        for (uint32_t i = 0; i < nprec; i++) rc[first_p + i].total_bytes -= each + (i < extra ? 1u : 0u);
+                    }
+                }
+            }
+            if (pad_last > 0) {
+                /* the first precinct 10 % more (20 % with fast signs), the
+                 * rest of the padding shared evenly */
+                uint32_t add_first = rc[first_p].total_bytes * (cfg->signs == 1 ? 20u : 10u) / 100;
+                if (add_first > pad_last) add_first = pad_last;
+                pad_last -= add_first;
+                rc[first_p + nprec - 1].total_bytes -= add_first;
+                rc[first_p].total_bytes += add_first;
+                if (pad_last) {
+                    rc[first_p + nprec - 1].total_bytes -= pad_last;
+                    const uint32_t each = pad_last / nprec, extra = pad_last - each * nprec;
+                    for (uint32_t i = 0; i < nprec; i++) rc[first_p + i].total_bytes += each + (i < extra ? 1u : 0u);
+                }
+            }
+        }
+        if (err) {
+            printf("jxs rc: slice %d (common quantization): error 0x%x\n", s, (unsigned)err);
+            JXS_STATUS_SET(status, err);
+        }
+        s_cerr = err;
+    }
+    __syncthreads();
+    return s_cerr;
+}
+
+/* One precinct's budget, searches and padding carry; thread 0.  `T` is the
+ * table of the quantization search, `F` the exact-sign table (fast signs:
+ * the bytes of the signs not sent are T - F at the chosen (Q, R)), `TS` the
+ * table of the scan and the refinement search (row stride `ld`); all in
+ * shared memory.
+ * Modes 1-3 carry the padding (and fast signs' unsent sign bytes) to the
+ * next precinct of the slice; a slice's last precinct and mode 0 keep them
+ * as zero bytes (PackStageProcess.c:293-333, 526-560,
+ * PackPrecinct.c:513-536).  Returns an error code. */
+DEV int prec_select(const jxs_cfg_t* __restrict__ cfg, int s, uint32_t i, const SliceSplit& sp, const uint32_t* T,
+                    const uint32_t* F, const uint32_t* TS, int ld, int scan, const uint32_t* __restrict__ s_empty, uint32_t& carry,
+                    uint32_t& run, PrecRC* __restrict__ rc, int* __restrict__ status) {
+    const uint32_t p = sp.first_p + i;
+    const int last = (p + 1 >= cfg->np);
+    const uint32_t budget =
+        (cfg->rc_mode >= 2 ? rc[p].total_bytes : (i == 0 ? sp.first_b : sp.min_b) + (i < sp.left ? 1 : 0)) + carry;
+    const uint32_t hdr = cfg->hdrs_bytes[last];
+    const int nr = cfg->max_r + 1;
+    int err = 0;
+    if (budget > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
+    else if (budget <= hdr) err = JXS_E_UNDEFINED;
+    int q = 0, r = 0;
+    uint32_t data = 0;
+    if (!err) err = prec_search(T, TS, ld, scan, nr, cfg->max_q, cfg->max_r, s_empty, budget - hdr, q, r, data);
+    if (!err) {
+        const uint32_t padding = budget - hdr - data;
+        uint32_t total = budget;
+        const uint32_t retrieve = cfg->signs == 1 ? T[q * nr + r] - F[q * nr + r] : 0u;
+        if (cfg->rc_mode >= 1 && i + 1 < sp.nprec) {
+            total -= padding + retrieve;
+            carry = padding + retrieve;
+        } else {
+            carry = 0;
+        }
+        PrecRC o;
+        o.total_bytes = total;
+        o.offset = run;
+        o.data_bytes = data - retrieve; /* the sub-packet bytes packed */
+        o.q = (uint8_t)q;
+        o.r = (uint8_t)r;
+        o.first_in_slice = (uint8_t)(i == 0);
+        o.pad = 0;
+        rc[p] = o;
+        run += total;
+    } else {
+        printf("jxs rc: slice %d precinct %u budget %u: error 0x%x\n", s, p, budget, (unsigned)err);
+        JXS_STATUS_SET(status, err);
+    }
+    return err;
+}
+
+/* One slice's selection without vertical prediction, on the slice's cost
+ * tables: the tables of up to `area_words / (nq * nr * tables)` precincts
+ * are read (through L2) into `area` at a time; thread 0 then runs their
+ * searches in order.  With sign handling each precinct has two tables:
+ * signs counted the fast way (every coefficient of a group above gtli) and
+ * exactly; the quantization search runs on the fast one, the full strategy
+ * then scans and searches the refinement on the exact one. */
 DEV void select_slice(const jxs_cfg_t* __restrict__ cfg, int s, const uint32_t* __restrict__ cost, uint32_t* area,
                       uint32_t area_words, PrecRC* __restrict__ rc, int* __restrict__ status) {
     __shared__ uint32_t s_carry, s_run;
     __shared__ int s_err;
     __shared__ uint32_t s_empty[32];
     if (threadIdx.x < 32) s_empty[threadIdx.x] = cfg->empty[threadIdx.x];
-    const int last_slice = (s + 1 == (int)cfg->nslices);
-    const uint32_t slice_budget = cfg->slice_size[s] - 6 - (last_slice ? 2 : 0);
-    const uint32_t first_p = cfg->pps * s;
-    const uint32_t nprec = last_slice ? cfg->np - first_p : cfg->pps;
-    uint32_t min_b = slice_budget / nprec;
-    uint32_t left = slice_budget - min_b * nprec;
-    uint32_t first_b = min_b;
-    const uint32_t signs = cfg->signs;
-    if (cfg->rc_mode == 1) {
-        /* the first precinct 20 % more with fast signs, else 10 %
-         * (PackStageProcess.c:34-35, 614-622) */
-        first_b = min(slice_budget, first_b * (signs == 1 ? 120u : 110u) / 100);
-        if (nprec > 1) {
-            min_b = (slice_budget - first_b) / (nprec - 1);
-            left = slice_budget - min_b * (nprec - 1) - first_b;
-        } else {
-            left = 0;
-        }
-    }
+    const SliceSplit sp = slice_split(cfg, s);
     if (threadIdx.x == 0) {
         s_carry = 0;
         s_run = cfg->slice_begin[s] + 6;
         s_err = 0;
     }
     const int nq = cfg->max_q + 1, nr = cfg->max_r + 1, nt = nq * nr;
-    const int max_q = cfg->max_q, max_r = cfg->max_r, rc_mode = (int)cfg->rc_mode;
-    const uint32_t np_all = cfg->np, hdrs0 = cfg->hdrs_bytes[0], hdrs1 = cfg->hdrs_bytes[1];
-    if (rc_mode >= 2) {
-        /* RC modes 2 and 3, per-slice common quantization (process_slice,
-         * PackStageProcess.c:339-483; RateControl.c:1086-1209, 1336-1425):
-         * the data bytes of every (Q, R) summed over the slice's precincts,
-         * one (Q, R) for the slice by the precinct searches, then the budget
-         * of each precinct; kept in rc[p].total_bytes for the loop below */
-        __syncthreads();
-        for (int e = threadIdx.x; e < nt; e += blockDim.x) {
-            const int q = e / nr, r = e - q * nr;
-            uint32_t sum = 0;
-            for (uint32_t i = 0; i < nprec; i++) sum += __ldcg(cost + (uint64_t)(first_p + i) * 1024 + q * 32 + r);
-            area[e] = sum;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            int err = 0;
-            uint32_t headers = 0;
-            for (uint32_t i = 0; i < nprec; i++) headers += first_p + i + 1 >= np_all ? hdrs1 : hdrs0;
-            if ((slice_budget + nprec - 1) / nprec > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
-            else if (slice_budget <= headers) err = JXS_E_UNDEFINED;
-            int q = 0, r = 0;
-            if (!err) {
-                const uint32_t avail = slice_budget - headers;
-                BSearch bs;
-                int step = 6;
-                if (step > max_q) step = 0;
-                bs_init(bs, 0, max_q, 0, step);
-                int res, next = BS_BEGIN, v = 0;
-                while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
-                    if (s_empty[v] & 1u) next = BS_OUT_OF_RANGE;
-                    else next = area[v * nr] > avail ? BS_TOO_SMALL : BS_TOO_BIG;
-                }
-                if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
-                q = v;
-                if (!err) {
-                    step = 6;
-                    if (step >= max_r) step = 0;
-                    bs_init(bs, 0, max_r, 1, step);
-                    next = BS_BEGIN;
-                    while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
-                        if ((s_empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
-                        else next = area[q * nr + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
-                    }
-                    if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
-                    r = v;
-                }
-                if (!err) {
-                    /* each precinct its headers and data at (Q, R); the last
-                     * also the slice's remaining bytes */
-                    uint32_t pad_last = avail;
-                    for (uint32_t i = 0; i < nprec; i++) {
-                        const uint32_t p = first_p + i;
-                        const uint32_t d = __ldcg(cost + (uint64_t)p * 1024 + q * 32 + r);
-                        pad_last -= d;
-                        rc[p].total_bytes = (p + 1 >= np_all ? hdrs1 : hdrs0) + d;
-                    }
-                    rc[first_p + nprec - 1].total_bytes += pad_last;
-                    if (rc_mode == 3) {
-                        /* RC_CBR_PER_SLICE_COMMON_QUANT_MAX_RATE: no precinct
-                         * below a quarter of the largest, padding excluded */
-                        uint32_t max_size = 0;
-                        for (uint32_t i = 0; i < nprec; i++)
-                            max_size = max(max_size, rc[first_p + i].total_bytes - (i + 1 == nprec ? pad_last : 0u));
-                        const uint32_t min_size = max_size / 4;
-                        uint32_t need = 0;
-                        for (uint32_t i = 0; i < nprec; i++) {
-                            const uint32_t ds = rc[first_p + i].total_bytes - (i + 1 == nprec ? pad_last : 0u);
-                            if (ds < min_size) {
-                                rc[first_p + i].total_bytes += min_size - ds;
-                                need += min_size - ds;
-                            }
-                        }
-                        if (need) {
-                            if (pad_last >= need) {
-                                pad_last -= need;
-                                rc[first_p + nprec - 1].total_bytes -= need;
-                            } else {
-                                need -= pad_last;
-                                rc[first_p + nprec - 1].total_bytes -= pad_last;
-                                pad_last = 0;
-                                /* the rest one byte at a time, round robin */
-                                const uint32_t each = need / nprec, extra = need - each * nprec;
-                                for (uint32_t i = 0; i < nprec; i++) rc[first_p + i].total_bytes -= each + (i < extra ? 1u : 0u);
-                            }
-                        }
-                    }
-                    if (pad_last > 0) {
-                        /* the first precinct 10 % more, the rest of the padding
-                         * shared evenly */
-                        uint32_t add_first = rc[first_p].total_bytes * (signs == 1 ? 20u : 10u) / 100;
-                        if (add_first > pad_last) add_first = pad_last;
-                        pad_last -= add_first;
-                        rc[first_p + nprec - 1].total_bytes -= add_first;
-                        rc[first_p].total_bytes += add_first;
-                        if (pad_last) {
-                            rc[first_p + nprec - 1].total_bytes -= pad_last;
-                            const uint32_t each = pad_last / nprec, extra = pad_last - each * nprec;
-                            for (uint32_t i = 0; i < nprec; i++) rc[first_p + i].total_bytes += each + (i < extra ? 1u : 0u);
-                        }
-                    }
-                }
-            }
-            if (err) {
-                printf("jxs rc: slice %d (common quantization): error 0x%x\n", s, (unsigned)err);
-                s_err = err;
-                JXS_STATUS_SET(status, err);
-            }
-        }
-    }
-    /* per precinct its table, and with sign handling the exact-sign table
-     * after it */
+    const uint32_t np_all = cfg->np, signs = cfg->signs;
+    __syncthreads();
+    if (cfg->rc_mode >= 2 && slice_common(cfg, s, sp, cost, area, s_empty, rc, status)) return;
     const int ntab = signs ? 2 : 1;
     const uint32_t chunk = area_words / (uint32_t)(nt * ntab);
-    for (uint32_t c0 = 0; c0 < nprec; c0 += chunk) {
-        const uint32_t cnt = min(chunk, nprec - c0);
+    for (uint32_t c0 = 0; c0 < sp.nprec; c0 += chunk) {
+        const uint32_t cnt = min(chunk, sp.nprec - c0);
         __syncthreads();
         if (s_err) break;
         for (int e = threadIdx.x; e < (int)cnt * nt * ntab; e += blockDim.x) {
             const int i = e / (nt * ntab), rest = e - i * nt * ntab, tb = rest / nt, qr = rest - tb * nt, q = qr / nr,
                       r = qr - q * nr;
-            area[e] = __ldcg(cost + ((uint64_t)tb * np_all + first_p + c0 + i) * 1024 + q * 32 + r);
+            area[e] = __ldcg(cost + ((uint64_t)tb * np_all + sp.first_p + c0 + i) * 1024 + q * 32 + r);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             for (uint32_t ii = 0; ii < cnt && !s_err; ii++) {
-                const uint32_t i = c0 + ii;
-                const uint32_t p = first_p + i;
                 const uint32_t* T = area + ii * nt * ntab;
                 const uint32_t* F = signs ? T + nt : T; /* exact signs */
-                const int last = (p + 1 >= np_all);
-                const uint32_t budget =
-                    (rc_mode >= 2 ? rc[p].total_bytes : (i == 0 ? first_b : min_b) + (i < left ? 1 : 0)) + s_carry;
-                const uint32_t hdr = last ? hdrs1 : hdrs0;
-                int err = 0;
-                if (budget > JXS_PREC_MAX_BYTES) err = JXS_E_ENC_FRAME;
-                else if (budget <= hdr) err = JXS_E_UNDEFINED;
-                int q = 0, r = 0;
-                uint32_t data = 0;
-                if (!err) {
-                    const uint32_t avail = budget - hdr;
-                    BSearch bs;
-                    int step = 6;
-                    if (step > max_q) step = 0;
-                    bs_init(bs, 0, max_q, 0, step);
-                    int res, next = BS_BEGIN, v = 0;
-                    while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
-                        if (s_empty[v] & 1u) next = BS_OUT_OF_RANGE;
-                        else next = T[v * nr] > avail ? BS_TOO_SMALL : BS_TOO_BIG;
-                    }
-                    if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
-                    q = v;
-                    if (!err && signs == 2) {
-                        /* full signs: lower quantizations while they fit,
-                         * else the first higher one that fits
-                         * (RateControl.c:936-1015) */
-                        int best = -1;
-                        for (int qt = q - 1; qt >= 0; qt--) {
-                            if ((s_empty[qt] & 1u) || F[qt * nr] > avail) break;
-                            best = qt;
+                uint32_t carry = s_carry, run = s_run;
+                s_err = prec_select(cfg, s, c0 + ii, sp, T, F, signs == 2 ? F : T, nr, signs == 2, s_empty, carry, run, rc, status);
+                s_carry = carry;
+                s_run = run;
+            }
+        }
+    }
+}
+
+/* Vertical prediction (RateControl.c:586-676): line tables stored by every
+ * precinct's block for the ordered selection, and the shared regions of
+ * that selection */
+#define RC_LT_REGION (JXS_MAXBLINES * 16)
+#define RC_LT_WORDS (5 * RC_LT_REGION) /* data, GCLI bits, GCLI bits with significance, fast / full sign bits */
+#define RC_VP_REGIONS 10
+
+/* vlc_encode_get_bits (PackPrecinct.h:86-104): ones of the unary code of a
+ * GCLI difference x for the vertical prediction range (r, t). */
+DEV uint32_t vlc_vp_bits(int x, int r, int t) {
+    const int mx = max(r - t, 0);
+    if (x > mx) return (uint32_t)(x + mx);
+    x *= 2;
+    return (uint32_t)(x < 0 ? -x - 1 : x);
+}
+
+/* One slice's selection with vertical prediction, precinct after precinct
+ * (the costs of a row depend on the gtli chosen for the row above,
+ * RateControl.c:586-676), by the block that completes the slice.  Per
+ * precinct:
+ *   tables   its line tables and (fast-sign) cost tables from the other
+ *            blocks;
+ *   vpred    warp per segment: for every gtli t, the unary bits of each
+ *            GCLI coded from the line above (line 0: the band's last line
+ *            in the row above, with that row's gtli) and the bits the
+ *            significance groups without code save (run mode Rm: groups
+ *            with every GCLI <= t; else groups predicted exactly);
+ *   methods  per band and t: no significance, significance, prediction,
+ *            prediction with significance; a later one only if strictly
+ *            cheaper;
+ *   costs    as in the parallel pass, with those methods and exact signs
+ *            for the full strategy;
+ *   search   thread 0: quantization on the plain table, then the scan and
+ *            refinement on the prediction table (:909-1083). */
+template <typename Stage>
+DEV void select_slice_vpred(const jxs_cfg_t* __restrict__ cfg, int s, const uint8_t* __restrict__ gcli,
+                            const uint32_t* __restrict__ cost, uint32_t* area, PrecRC* __restrict__ rc,
+                            int* __restrict__ status, Stage& stage_kind, const uint8_t* lgain, const uint8_t* lprio,
+                            const uint8_t* lfb, const uint32_t* lsig, const uint32_t* lraw, const jxs_bline_t* bls,
+                            const jxs_seg_t* segs, const uint8_t* s_pkbl0, const uint8_t* s_pknbl, const uint8_t* s_order) {
+    __shared__ uint32_t s_carry, s_run;
+    __shared__ int s_err;
+    __shared__ uint32_t s_empty[32];
+    __shared__ uint8_t s_gtop[JXS_MAXBL], s_bl0[JXS_MAXBL], s_bl1[JXS_MAXBL];
+    __shared__ uint32_t s_methv[JXS_MAXBL]; /* per band: 2 bits per t */
+    uint32_t(*vtfs)[16] = (uint32_t(*)[16])area;
+    uint32_t(*dV)[32] = (uint32_t(*)[32])(area + RC_LT_REGION);
+    uint32_t(*vtdat)[16] = (uint32_t(*)[16])(area + 2 * RC_LT_REGION);
+    uint32_t(*vtnos)[16] = (uint32_t(*)[16])(area + 3 * RC_LT_REGION);
+    uint32_t(*vtsig)[16] = (uint32_t(*)[16])(area + 4 * RC_LT_REGION);
+    uint32_t(*vtnz)[16] = (uint32_t(*)[16])(area + 5 * RC_LT_REGION);
+    uint32_t(*vnos)[16] = (uint32_t(*)[16])(area + 6 * RC_LT_REGION);
+    uint32_t(*vred)[16] = (uint32_t(*)[16])(area + 7 * RC_LT_REGION);
+    uint32_t* Ts = area + 8 * RC_LT_REGION;
+    uint32_t* Fs = area + 9 * RC_LT_REGION;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x < 32) s_empty[threadIdx.x] = cfg->empty[threadIdx.x];
+    const SliceSplit sp = slice_split(cfg, s);
+    if (threadIdx.x == 0) {
+        s_carry = 0;
+        s_run = cfg->slice_begin[s] + 6;
+        s_err = 0;
+    }
+    const int nq = cfg->max_q + 1, nr = cfg->max_r + 1, nt = nq * nr;
+    const uint32_t np_all = cfg->np, signs = cfg->signs, fs = cfg->fs, SG = cfg->seg_groups, npk = cfg->npk;
+    const uint32_t nbands = cfg->nbands, sig = cfg->sig;
+    const int rm = cfg->rm;
+    __syncthreads();
+    if (cfg->rc_mode >= 2 && slice_common(cfg, s, sp, cost, Ts, s_empty, rc, status)) return;
+    int kind_staged = -1;
+    for (uint32_t i = 0; i < sp.nprec; i++) {
+        const uint32_t p = sp.first_p + i;
+        const int kind = (p + 1 >= np_all);
+        __syncthreads();
+        if (s_err) break;
+        if (kind != kind_staged) {
+            stage_kind(kind);
+            kind_staged = kind;
+            __syncthreads();
+        }
+        const uint32_t nbl = cfg->nbline[kind], nseg = cfg->nseg[kind];
+        /* the lines of each band (at most two per precinct row) */
+        for (uint32_t fb = threadIdx.x; fb < nbands; fb += blockDim.x) {
+            s_bl0[fb] = 0xff;
+            s_bl1[fb] = 0xff;
+            s_methv[fb] = 0;
+        }
+        __syncthreads();
+        for (uint32_t x = threadIdx.x; x < nbl; x += blockDim.x) {
+            if (bls[x].line == 0) s_bl0[bls[x].fb] = (uint8_t)x;
+            else s_bl1[bls[x].fb] = (uint8_t)x;
+        }
+        /* this row's tables from the other blocks */
+        const uint32_t* lt = cost + (uint64_t)np_all * 1024 * (fs ? 2 : 1) + (uint64_t)p * RC_LT_WORDS;
+        for (uint32_t k = threadIdx.x; k < nbl * 16; k += blockDim.x) {
+            const uint32_t x = k >> 4, t = k & 15;
+            vtdat[x][t] = __ldcg(lt + k);
+            vtnos[x][t] = __ldcg(lt + RC_LT_REGION + k);
+            vtsig[x][t] = __ldcg(lt + 2 * RC_LT_REGION + k);
+            if (fs) {
+                vtfs[x][t] = __ldcg(lt + 3 * RC_LT_REGION + k);
+                vtnz[x][t] = __ldcg(lt + 4 * RC_LT_REGION + k);
+            }
+            vnos[x][t] = 0;
+            vred[x][t] = 0;
+        }
+        for (int e = threadIdx.x; e < nt; e += blockDim.x) {
+            const int q = e / nr, r = e - q * nr;
+            Ts[e] = __ldcg(cost + (uint64_t)p * 1024 + q * 32 + r);
+            if (fs) Fs[e] = __ldcg(cost + ((uint64_t)np_all + p) * 1024 + q * 32 + r);
+        }
+        for (int e = threadIdx.x; e < nq * 32; e += blockDim.x) dV[e >> 5][e & 31] = 0;
+        __syncthreads();
+        /* vertical prediction costs of every line, for every t */
+        if (i > 0) {
+            for (uint32_t sidx = warp; sidx < nseg; sidx += RC_WARPS) {
+                const jxs_seg_t sg = segs[sidx];
+                const uint32_t x = sg.bl;
+                const jxs_bline_t B = bls[x];
+                const jxs_band_t& bd = cfg->band[B.fb];
+                const uint8_t* cur = gcli + bd.gcli_off + (uint64_t)(p * bd.lines + B.line) * bd.gpitch;
+                const uint8_t* top = cur - bd.gpitch; /* the row above: the previous line, for line 0 in the row above */
+                const int gtt = B.line ? -1 : (int)s_gtop[B.fb];
+                const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+                for (uint32_t base = sg.g0; base < gend; base += 128) {
+                    const uint32_t g = base + 4 * lane;
+                    const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
+                    const uint32_t wc = nv ? *(const uint32_t*)(cur + g) : 0u, wt = nv ? *(const uint32_t*)(top + g) : 0u;
+                    for (int t = 0; t < 16; t++) {
+                        const int gmax = max(t, gtt);
+                        uint32_t sum = 0, flag = 1;
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            if (k < (int)nv) {
+                                const int c = (int)((wc >> (8 * k)) & 255u), tp = (int)((wt >> (8 * k)) & 255u);
+                                const int mt = max(tp, gmax), gv = max(c, t);
+                                sum += vlc_vp_bits(gv - mt, mt, t) + 1;
+                                flag &= rm ? (uint32_t)(c <= t) : (uint32_t)(mt == gv);
+                            }
                         }
-                        if (best < 0)
-                            for (int qt = q; qt <= max_q; qt++)
-                                if (!(s_empty[qt] & 1u) && F[qt * nr] <= avail) {
-                                    best = qt;
-                                    break;
-                                }
-                        if (best < 0) err = JXS_E_ENC_FRAME;
-                        q = best;
-                    }
-                    const uint32_t* TR = signs == 2 ? F : T; /* the refinement search's table */
-                    if (!err) {
-                        step = 6;
-                        if (step >= max_r) step = 0;
-                        bs_init(bs, 0, max_r, 1, step);
-                        next = BS_BEGIN;
-                        while ((res = bs_next(bs, next, &v)) == BS_CONTINUE) {
-                            if ((s_empty[q] >> v) & 1u) next = BS_OUT_OF_RANGE;
-                            else next = TR[q * nr + v] <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
+                        /* significance group of 8 GCLIs: lanes 2j, 2j + 1 */
+                        const uint32_t f2 = flag & __shfl_xor_sync(FULL, flag, 1);
+                        const uint32_t s2 = sum + __shfl_xor_sync(FULL, sum, 1);
+                        const uint32_t red = (!(lane & 1) && f2) ? s2 : 0u;
+                        const uint32_t tot = __reduce_add_sync(FULL, sum), rtot = __reduce_add_sync(FULL, red);
+                        if (lane == 0) {
+                            if (tot) atomicAdd(&vnos[x][t], tot);
+                            if (rtot) atomicAdd(&vred[x][t], rtot);
                         }
-                        if (res != BS_FOUND) err = JXS_E_ENC_FRAME;
-                        r = v;
-                        data = TR[q * nr + r];
-                    }
-                    if (!err) {
-                        uint32_t padding = avail - data;
-                        uint32_t total = budget;
-                        /* fast signs: the bytes of signs not sent */
-                        const uint32_t retrieve = signs == 1 ? T[q * nr + r] - F[q * nr + r] : 0u;
-                        if (rc_mode >= 1 && i + 1 < nprec) {
-                            total -= padding + retrieve;
-                            s_carry = padding + retrieve;
-                        } else {
-                            s_carry = 0;
-                        }
-                        PrecRC o;
-                        o.total_bytes = total;
-                        o.offset = s_run;
-                        o.data_bytes = data - retrieve; /* the sub-packet bytes packed */
-                        o.q = (uint8_t)q;
-                        o.r = (uint8_t)r;
-                        o.first_in_slice = (uint8_t)(i == 0);
-                        o.pad = 0;
-                        rc[p] = o;
-                        s_run += total;
                     }
                 }
-                if (err) {
-                    printf("jxs rc: slice %d precinct %u budget %u: error 0x%x\\n", s, p, budget, (unsigned)err);
-                    s_err = err;
-                    JXS_STATUS_SET(status, err);
+            }
+        }
+        __syncthreads();
+        /* coding method per band and t (RateControl.c:526-676) */
+        for (uint32_t e = threadIdx.x; e < nbands * 16; e += blockDim.x) {
+            const uint32_t fb = e >> 4, t = e & 15;
+            const uint32_t x0 = s_bl0[fb], x1 = s_bl1[fb];
+            if (x0 == 0xff) continue;
+            uint32_t cnv = vtnos[x0][t], csv = vtsig[x0][t] + lsig[x0], vn = vnos[x0][t], vs = vnos[x0][t] - vred[x0][t] + lsig[x0];
+            if (x1 != 0xff) {
+                cnv += vtnos[x1][t];
+                csv += vtsig[x1][t] + lsig[x1];
+                vn += vnos[x1][t];
+                vs += vnos[x1][t] - vred[x1][t] + lsig[x1];
+            }
+            uint32_t m = 0, best = cnv;
+            if (sig && best > csv) {
+                m = 2;
+                best = csv;
+            }
+            if (i > 0) {
+                if (best > vn) {
+                    m = 1;
+                    best = vn;
                 }
+                if (sig && best > vs) m = 3;
+            }
+            atomicOr(&s_methv[fb], m << (2 * t));
+        }
+        __syncthreads();
+        /* costs with those methods, per (Q, packet) as in the parallel pass */
+        auto gbits = [&](uint32_t x, uint32_t m, int t) -> uint32_t {
+            return m == 0 ? vtnos[x][t] : m == 2 ? vtsig[x][t] : m == 1 ? vnos[x][t] : vnos[x][t] - vred[x][t];
+        };
+        auto nbits = [&](uint32_t x, int t) -> uint32_t { return signs == 2 ? vtnz[x][t] : signs == 1 ? vtfs[x][t] : 0u; };
+        for (uint32_t e = threadIdx.x; e < (uint32_t)nq * npk; e += blockDim.x) {
+            const int q = (int)(e / npk);
+            const uint32_t k = e - (uint32_t)q * npk;
+            const uint32_t b0 = s_pkbl0[k], nb = s_pknbl[k];
+            if (!nb) continue;
+            uint32_t db = 0, gb = 0, sb = 0, zb = 0;
+            for (uint32_t x = b0; x < b0 + nb; x++) {
+                const int g = lgain[x];
+                const int t = q < g ? 0 : min(q - g, 15);
+                const uint32_t m = (s_methv[lfb[x]] >> (2 * t)) & 3u;
+                db += vtdat[x][t];
+                gb += gbits(x, m, t);
+                sb += (m & 2u) ? lsig[x] : 0u;
+                zb += nbits(x, t);
+            }
+            uint32_t c = ((db + 7) >> 3) + min(lraw[k], ((sb + 7) >> 3) + ((gb + 7) >> 3)) + ((zb + 7) >> 3);
+            atomicAdd(&dV[q][0], c);
+            for (uint32_t j = 0; j < nb; j++) {
+                const uint32_t x = s_order[b0 + j];
+                const int rf = lprio[x] + 1;
+                if (rf >= nr) break;
+                const int g = lgain[x];
+                const int t0 = q < g ? 0 : min(q - g, 15), t1 = q < g + 1 ? 0 : min(q - g - 1, 15);
+                const uint32_t m0 = (s_methv[lfb[x]] >> (2 * t0)) & 3u, m1 = (s_methv[lfb[x]] >> (2 * t1)) & 3u;
+                db += vtdat[x][t1] - vtdat[x][t0];
+                gb += gbits(x, m1, t1) - gbits(x, m0, t0);
+                sb += ((m1 & 2u) ? lsig[x] : 0u) - ((m0 & 2u) ? lsig[x] : 0u);
+                zb += nbits(x, t1) - nbits(x, t0);
+                const uint32_t c1 = ((db + 7) >> 3) + min(lraw[k], ((sb + 7) >> 3) + ((gb + 7) >> 3)) + ((zb + 7) >> 3);
+                atomicAdd(&dV[q][rf], c1 - c);
+                c = c1;
+            }
+        }
+        __syncthreads();
+        for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+            uint32_t run = 0;
+            for (int r = 0; r < nr; r++) {
+                run += dV[q][r];
+                dV[q][r] = run;
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t carry = s_carry, run = s_run;
+            s_err = prec_select(cfg, s, i, sp, Ts, fs ? Fs : Ts, &dV[0][0], 32, 1, s_empty, carry, run, rc, status);
+            s_carry = carry;
+            s_run = run;
+            if (!s_err) {
+                const PrecRC o = rc[p];
+                for (uint32_t fb = 0; fb < nbands; fb++) s_gtop[fb] = jxs_truncation(cfg->band[fb].gain, cfg->band[fb].prio, o.q, o.r);
             }
         }
     }
@@ -357,7 +604,7 @@ DEV uint32_t nz_levels(uint32_t m, uint32_t g, uint32_t uniform) {
  *   costs       per packet, data / significance / GCLI bytes rounded
  *               separately, raw fallback when cheaper; summed over packets
  *               for every (Q, R). */
-template <bool SIGNS>
+template <bool SIGNS, bool VPRED>
 __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
                                              const uint16_t* __restrict__ coef, uint32_t* __restrict__ cost,
                                              uint32_t* __restrict__ slice_done, PrecRC* __restrict__ rc,
@@ -365,8 +612,11 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     /* per band line: GCLI and significance-maximum histograms (with sign
      * handling also the coefficients by non-zero levels), then per gtli data
      * / GCLI bits without and with significance and the sign bits; the area
-     * is reused by the slice selection at the end */
-    __shared__ __align__(16) uint32_t s_area[RC_AREA_WORDS(SIGNS)];
+     * is reused by the slice selection at the end (with vertical prediction
+     * it is dynamic shared memory of RC_VP_REGIONS regions) */
+    __shared__ __align__(16) uint32_t s_area_st[VPRED ? 4 : RC_AREA_WORDS(SIGNS)];
+    extern __shared__ __align__(16) uint32_t rc_dyn[];
+    uint32_t* s_area = VPRED ? rc_dyn : s_area_st;
     uint32_t(*hist)[16] = (uint32_t(*)[16])s_area;                          /* later: fast sign bits per t */
     uint32_t(*shist)[16] = (uint32_t(*)[16])(s_area + JXS_MAXBLINES * 16);  /* later: full-sign cost changes */
     uint32_t(*tdat)[16] = (uint32_t(*)[16])(s_area + 2 * JXS_MAXBLINES * 16);
@@ -376,8 +626,8 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     uint32_t(*tfs)[16] = hist;
     uint32_t(*tnz)[16] = nzh;
     uint32_t(*dF)[32] = (uint32_t(*)[32])shist;
-    /* SIGNS: the launch may hold frames with sign handling (compiled out
-     * otherwise) */
+    /* SIGNS: the launch may hold frames with sign handling; VPRED: with
+     * vertical prediction (compiled out otherwise) */
     const uint32_t fs = SIGNS ? cfg->fs : 0u, uniform = cfg->qpih;
     __shared__ int pmax[JXS_MAXBLINES];
     __shared__ uint32_t cn[JXS_MAXBL][16], cs[JXS_MAXBL][16];
@@ -396,14 +646,29 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     const uint32_t nbl = cfg->nbline[last], nseg = cfg->nseg[last], SG = cfg->seg_groups;
     const jxs_bline_t* bls = s_bl;
     const jxs_seg_t* segs = s_seg;
-    for (uint32_t i = threadIdx.x; i < nseg * (sizeof(jxs_seg_t) / 4); i += blockDim.x)
-        ((uint32_t*)s_seg)[i] = ((const uint32_t*)cfg->seg[last])[i];
-    for (uint32_t i = threadIdx.x; i < nbl * (sizeof(jxs_bline_t) / 4); i += blockDim.x)
-        ((uint32_t*)s_bl)[i] = ((const uint32_t*)cfg->bline[last])[i];
-    for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) {
-        s_pkbl0[k] = cfg->pk_bl0[last][k];
-        s_pknbl[k] = cfg->pk_nbl[last][k];
-    }
+    /* the tables of a precinct kind (normal / last row) */
+    auto stage_kind = [&](int kind) {
+        const uint32_t nb = cfg->nbline[kind], ns = cfg->nseg[kind];
+        for (uint32_t i = threadIdx.x; i < ns * (sizeof(jxs_seg_t) / 4); i += blockDim.x)
+            ((uint32_t*)s_seg)[i] = ((const uint32_t*)cfg->seg[kind])[i];
+        for (uint32_t i = threadIdx.x; i < nb * (sizeof(jxs_bline_t) / 4); i += blockDim.x)
+            ((uint32_t*)s_bl)[i] = ((const uint32_t*)cfg->bline[kind])[i];
+        for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) {
+            s_pkbl0[k] = cfg->pk_bl0[kind][k];
+            s_pknbl[k] = cfg->pk_nbl[kind][k];
+            lraw[k] = cfg->raw_bytes[kind][k];
+        }
+        for (uint32_t x = threadIdx.x; x < nb; x += blockDim.x) {
+            const jxs_bline_t& B = cfg->bline[kind][x];
+            const jxs_band_t& bd = cfg->band[B.fb];
+            lgain[x] = bd.gain;
+            lprio[x] = bd.prio;
+            lfb[x] = B.fb;
+            lsig[x] = B.sig_w;
+            s_order[x] = cfg->pk_order[kind][x];
+        }
+    };
+    stage_kind(last);
     for (uint32_t i = threadIdx.x; i < nbl * 16; i += blockDim.x) {
         hist[i >> 4][i & 15] = 0;
         shist[i >> 4][i & 15] = 0;
@@ -417,14 +682,8 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
         const jxs_bline_t& B = cfg->bline[last][x];
         const jxs_band_t& bd = cfg->band[B.fb];
         pmax[x] = -1;
-        lgain[x] = bd.gain;
-        lprio[x] = bd.prio;
-        lfb[x] = B.fb;
-        lsig[x] = B.sig_w;
         s_grow[x] = bd.gcli_off + (uint64_t)(p * bd.lines + B.line) * bd.gpitch;
-        s_order[x] = cfg->pk_order[last][x];
     }
-    for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) lraw[k] = cfg->raw_bytes[last][k];
     __syncthreads();
 
     /* histograms: each lane 4 consecutive groups (one 4-byte load), 8-bit
@@ -543,6 +802,20 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
         }
     }
     __syncthreads();
+    if (VPRED && cfg->vpred) {
+        /* the line tables, for the slice's selection in precinct order */
+        uint32_t* lt = cost + (uint64_t)cfg->np * 1024 * (cfg->fs ? 2 : 1) + (uint64_t)p * RC_LT_WORDS;
+        for (uint32_t i = threadIdx.x; i < nbl * 16; i += blockDim.x) {
+            const uint32_t x = i >> 4, t = i & 15;
+            lt[i] = tdat[x][t];
+            lt[RC_LT_REGION + i] = tnos[x][t];
+            lt[2 * RC_LT_REGION + i] = tsig[x][t];
+            if (fs) {
+                lt[3 * RC_LT_REGION + i] = tfs[x][t];
+                lt[4 * RC_LT_REGION + i] = tnz[x][t];
+            }
+        }
+    }
     /* coding method per band and t: significance only if strictly cheaper
      * (RateControl.c:528-575) */
     for (uint32_t fb = threadIdx.x; fb < cfg->nbands; fb += blockDim.x) {
@@ -641,7 +914,13 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     __syncthreads();
     if (!s_last) return;
     __threadfence();
-    select_slice(cfg, (int)s, cost, s_area, RC_AREA_WORDS(SIGNS), rc, status);
+    if constexpr (VPRED) {
+        if (cfg->vpred) select_slice_vpred(cfg, (int)s, gcli, cost, s_area, rc, status, stage_kind, lgain, lprio, lfb, lsig,
+                                           lraw, s_bl, s_seg, s_pkbl0, s_pknbl, s_order);
+        else select_slice(cfg, (int)s, cost, s_area, RC_VP_REGIONS * RC_LT_REGION, rc, status);
+    } else {
+        select_slice(cfg, (int)s, cost, s_area, RC_AREA_WORDS(SIGNS), rc, status);
+    }
     if (threadIdx.x == 0) slice_done[s] = 0; /* ready for the next frame */
 }
 
@@ -748,8 +1027,7 @@ struct PkLine {
     uint8_t meth, raw, pad0, pad1;
 };
 
-/* pack_precinct (PackPrecinct.c:235-572) for one precinct row; vertical
- * prediction off.
+/* pack_precinct (PackPrecinct.c:235-572) for one precinct row.
  *
  * The precinct is assembled in shared memory, `lead` bytes into the buffer
  * so that buffer byte i lands on the 16-byte aligned address
@@ -763,7 +1041,15 @@ struct PkLine {
  *           each segment's start in its GCLI and data sub-packets;
  *   pass B  each lane one group: significance flags, the unary GCLI code and
  *           the data bits, at positions from a warp prefix sum, OR-ed into
- *           the buffer. */
+ *           the buffer.
+ * VPRED (frames with vertical prediction; compiled out otherwise): a
+ * precinct row below another of its slice also sums, per segment, the
+ * codes of its GCLIs predicted from the line above at its gtli (line 0:
+ * from the row above, with that row's gtli) and the groups that need no
+ * code; the layout chooses among the four codings per band like the rate
+ * control (RateControl.c:526-676), and pass B writes the prediction codes
+ * (pack_bitplane_count_vpred_*, PackPrecinct.c:47-74). */
+template <bool VPRED>
 __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
                                           const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
                                           uint8_t* __restrict__ out, uint32_t cap_words, int* status, const int p) {
@@ -772,6 +1058,11 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
     __shared__ PkLine pl[JXS_MAXBLINES];
     __shared__ uint8_t s_meth[JXS_MAXBL];
     __shared__ uint32_t s_cn[JXS_MAXBL], s_cs[JXS_MAXBL];
+    __shared__ uint32_t s_vn[VPRED ? JXS_MAXSEG : 1], s_vr[VPRED ? JXS_MAXSEG : 1]; /* per segment: prediction bits */
+    __shared__ uint32_t s_cv[VPRED ? JXS_MAXBL : 1], s_cvs[VPRED ? JXS_MAXBL : 1];   /* per band: prediction totals */
+    __shared__ int8_t s_gtt[VPRED ? JXS_MAXBLINES : 1];                            /* per line: gtli of the line above (-1: this row's) */
+    __shared__ uint32_t s_lvn[VPRED ? JXS_MAXBLINES : 1], s_lvr[VPRED ? JXS_MAXBLINES : 1]; /* per line: prediction bits */
+    __shared__ uint32_t s_gp[VPRED ? JXS_MAXBLINES : 1];                           /* per line: GCLI row pitch */
     __shared__ uint32_t s_lg[JXS_MAXBLINES], s_ls[JXS_MAXBLINES];       /* per line: GCLI / significance bits */
     __shared__ uint32_t s_pks[JXS_MAXPK], s_pkg[JXS_MAXPK], s_pkd[JXS_MAXPK], s_pkn[JXS_MAXPK]; /* per packet: sub-packet starts */
     __shared__ uint8_t s_pkr[JXS_MAXPK];
@@ -812,7 +1103,14 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
     for (uint32_t fb = threadIdx.x; fb < cfg->nbands; fb += blockDim.x) {
         s_cn[fb] = 0;
         s_cs[fb] = 0;
+        if (VPRED) {
+            s_cv[fb] = 0;
+            s_cvs[fb] = 0;
+        }
     }
+    /* vertical prediction applies below the first row of a slice */
+    const int vp = VPRED && cfg->vpred && !R.first_in_slice;
+    const int rmode = cfg->rm;
     {
         const uint32_t ns = cfg->nseg[last], nl = cfg->nbline[last];
         for (uint32_t i = threadIdx.x; i < ns * (sizeof(jxs_seg_t) / 4); i += blockDim.x)
@@ -826,6 +1124,10 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             s_grow[x] = bd.gcli_off + row * bd.gpitch;
             s_crow[x] = bd.coef_off + row * bd.pitch;
             s_lt[x] = jxs_truncation(bd.gain, bd.prio, R.q, R.r);
+            if (VPRED) {
+                s_gp[x] = bd.gpitch;
+                s_gtt[x] = (int8_t)(vp && B.line == 0 ? jxs_truncation(bd.gain, bd.prio, rc[p - 1].q, rc[p - 1].r) : -1);
+            }
         }
         for (uint32_t k = threadIdx.x; k < cfg->npk; k += blockDim.x) {
             s_pkbl0[k] = cfg->pk_bl0[last][k];
@@ -864,11 +1166,30 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
         const uint16_t* crow = coef + s_crow[sg.bl];
         const int bw = (int)bls[sg.bl].w;
         const uint32_t gend = min(sg.g0 + SG, bls[sg.bl].gcli_w);
-        uint32_t dsum = 0, vsum = 0, zsum = 0, nsum = 0;
+        uint32_t dsum = 0, vsum = 0, zsum = 0, nsum = 0, pnsum = 0, prsum = 0;
         for (uint32_t base = sg.g0; base < gend; base += 128) {
             const uint32_t g = base + 4 * lane;
             const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
             const uint32_t w4 = nv ? *(const uint32_t*)(grow + g) : 0u;
+            if (VPRED && vp) {
+                /* GCLIs predicted from the line above: code bits, and the
+                 * groups of 8 that need none (lanes 2j, 2j + 1) */
+                const uint32_t wt = nv ? *(const uint32_t*)(grow - s_gp[sg.bl] + g) : 0u;
+                const int gmax = max((int)t, (int)s_gtt[sg.bl]);
+                uint32_t sum = 0, flag = 1;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (k < (int)nv) {
+                        const int c = (int)((w4 >> (8 * k)) & 255u), tp = (int)((wt >> (8 * k)) & 255u);
+                        const int mt = max(tp, gmax), gv = max(c, (int)t);
+                        sum += vlc_vp_bits(gv - mt, mt, (int)t) + 1;
+                        flag &= rmode ? (uint32_t)(c <= (int)t) : (uint32_t)(mt == gv);
+                    }
+                }
+                const uint32_t f2 = flag & __shfl_xor_sync(FULL, flag, 1), s2 = sum + __shfl_xor_sync(FULL, sum, 1);
+                pnsum += sum;
+                prsum += (!(lane & 1) && f2) ? s2 : 0u;
+            }
             uint32_t m = 0;
 #pragma unroll
             for (int k = 0; k < 4; k++) m = max(m, k < (int)nv ? (w4 >> (8 * k)) & 255u : 0u);
@@ -900,11 +1221,19 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
         vsum = __reduce_add_sync(FULL, vsum);
         zsum = __reduce_add_sync(FULL, zsum);
         nsum = __reduce_add_sync(FULL, nsum);
+        if (VPRED) {
+            pnsum = __reduce_add_sync(FULL, pnsum);
+            prsum = __reduce_add_sync(FULL, prsum);
+        }
         if (lane == 0) {
             s_data[sidx] = dsum;
             s_vlc[sidx] = vsum;
             s_zero[sidx] = zsum;
             s_nz[sidx] = nsum;
+            if (VPRED) {
+                s_vn[sidx] = pnsum;
+                s_vr[sidx] = prsum;
+            }
         }
     }
     __syncthreads();
@@ -927,18 +1256,44 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             pl[b].nz = n;
             atomicAdd(&s_cn[B.fb], v);
             atomicAdd(&s_cs[B.fb], v - z + B.sig_w);
+            if (VPRED && vp) {
+                uint32_t vn = 0, vr = 0;
+                for (uint32_t i = B.seg0; i < B.seg0 + B.nseg; i++) {
+                    vn += s_vn[i];
+                    vr += s_vr[i];
+                }
+                s_lvn[b] = vn;
+                s_lvr[b] = vr;
+                atomicAdd(&s_cv[B.fb], vn);
+                atomicAdd(&s_cvs[B.fb], vn - vr + B.sig_w);
+            }
         }
         __syncwarp();
-        /* coding method per band: significance only if strictly cheaper
-         * (RateControl.c:528-575) */
-        for (uint32_t fb = lane; fb < s_nbands; fb += 32) s_meth[fb] = (uint8_t)(s_sig && s_cn[fb] > s_cs[fb]);
+        /* coding method per band, D[p,b] (bit 1 significance, bit 0
+         * prediction): a later one only if strictly cheaper
+         * (RateControl.c:526-676) */
+        for (uint32_t fb = lane; fb < s_nbands; fb += 32) {
+            uint32_t m = 0, best = s_cn[fb];
+            if (s_sig && best > s_cs[fb]) {
+                m = 2;
+                best = s_cs[fb];
+            }
+            if (VPRED && vp) {
+                if (best > s_cv[fb]) {
+                    m = 1;
+                    best = s_cv[fb];
+                }
+                if (s_sig && best > s_cvs[fb]) m = 3;
+            }
+            s_meth[fb] = (uint8_t)m;
+        }
         __syncwarp();
         /* per line: GCLI and significance bits with the band's method */
         for (uint32_t b = lane; b < nbl; b += 32) {
             const uint8_t m = s_meth[bls[b].fb];
             pl[b].meth = m;
-            s_lg[b] = m ? pl[b].vlc - pl[b].zero : pl[b].vlc;
-            s_ls[b] = m ? bls[b].sig_w : 0u;
+            s_lg[b] = m == 0 ? pl[b].vlc : m == 2 ? pl[b].vlc - pl[b].zero : m == 1 ? s_lvn[VPRED ? b : 0] : s_lvn[VPRED ? b : 0] - s_lvr[VPRED ? b : 0];
+            s_ls[b] = (m & 2) ? bls[b].sig_w : 0u;
         }
         __syncwarp();
         /* one lane per packet: sub-packet sizes, raw fallback, header */
@@ -1012,7 +1367,7 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             const uint8_t m = pl[x].meth;
             uint32_t vp = pl[x].gcli_pos, dp = pl[x].data_pos, np = pl[x].sign_pos;
             for (uint32_t j = bls[x].seg0; j < i; j++) {
-                vp += m ? s_vlc[j] - s_zero[j] : s_vlc[j];
+                vp += m == 0 ? s_vlc[j] : m == 2 ? s_vlc[j] - s_zero[j] : m == 1 ? s_vn[VPRED ? j : 0] : s_vn[VPRED ? j : 0] - s_vr[VPRED ? j : 0];
                 dp += s_data[j];
                 np += s_nz[j];
             }
@@ -1039,7 +1394,7 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             const bool ex = fb != JXS_NOBAND;
             const uint32_t bal = __ballot_sync(FULL, ex);
             if (ex && s_blines[fb] > 0 && s_meth[fb])
-                put_bits(buf, words, lead * 8 + 40 + 2 * (idx0 + __popc(bal & ((1u << lane) - 1))), 2u, 2, ovf);
+                put_bits(buf, words, lead * 8 + 40 + 2 * (idx0 + __popc(bal & ((1u << lane) - 1))), s_meth[fb], 2, ovf);
             idx0 += __popc(bal);
         }
         /* the packed size must be what the rate control paid for */
@@ -1085,14 +1440,34 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                 m = max(m, v[k]);
             }
             const uint32_t mx = max(m, __shfl_xor_sync(FULL, m, 1));
-            const bool insig = mx <= t;
-            uint64_t vacc = 0;
+            /* a significance group without codes: all GCLIs <= gtli, or with
+             * prediction the group's flag */
+            bool insig = mx <= t;
+            uint32_t n4[4] = {0, 0, 0, 0}; /* prediction: each GCLI's code length */
+            uint64_t vacc = 0;             /* otherwise: the lane's codes joined */
             uint32_t vl = 0;
+            if (VPRED && (L.meth & 1) && !L.raw) {
+                /* codes predicted from the line above (vlc_encode,
+                 * PackPrecinct.h:41-65) */
+                const uint32_t wt = nv ? *(const uint32_t*)(grow - s_gp[VPRED ? sg.bl : 0] + g) : 0u;
+                const int gmax = max((int)t, (int)s_gtt[VPRED ? sg.bl : 0]);
+                uint32_t flag = 1;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (k < (int)nv) {
+                        const int c = (int)v[k], tp = (int)((wt >> (8 * k)) & 255u);
+                        const int mt = max(tp, gmax), gv = max(c, (int)t);
+                        n4[k] = vlc_vp_bits(gv - mt, mt, (int)t) + 1;
+                        flag &= rmode ? (uint32_t)(c <= (int)t) : (uint32_t)(mt == gv);
+                    }
+                }
+                insig = (flag & __shfl_xor_sync(FULL, flag, 1)) != 0;
+            }
             if (L.raw) {
                 /* raw GCLIs: the lane's nibbles in one write */
                 if (nv) put_bits(buf, words, L.gcli_pos + 4 * g, ((v[0] << 12) | (v[1] << 8) | (v[2] << 4) | v[3]) >> (4 * (4 - nv)), 4 * nv, ovf);
             } else {
-                if (L.meth) {
+                if (L.meth & 2) {
                     /* significance flags, 1 = insignificant: even lanes lead a group of 8 */
                     const uint32_t bal = __ballot_sync(FULL, nv && !(lane & 1) && insig);
                     if (lane == 0) {
@@ -1102,14 +1477,19 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                         if (bits) put_bits(buf, words, L.sig_pos + (base >> 3), bits, nsg, ovf);
                     }
                 }
-                if (!(L.meth && insig)) {
-                    /* unary codes: (v - t) ones then a zero (PackPrecinct.h:25-39) */
+                if (!((L.meth & 2) && insig)) {
+                    if (VPRED && (L.meth & 1)) {
 #pragma unroll
-                    for (int k = 0; k < 4; k++) {
-                        if (k < (int)nv) {
-                            const uint32_t n = v[k] > t ? v[k] - t + 1 : 1u;
-                            vacc = (vacc << n) | (((1ull << (n - 1)) - 1) << 1);
-                            vl += n;
+                        for (int k = 0; k < 4; k++) vl += n4[k];
+                    } else {
+                        /* unary codes: (v - t) ones then a zero (PackPrecinct.h:25-39) */
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            if (k < (int)nv) {
+                                const uint32_t n = v[k] > t ? v[k] - t + 1 : 1u;
+                                vacc = (vacc << n) | (((1ull << (n - 1)) - 1) << 1);
+                                vl += n;
+                            }
                         }
                     }
                 }
@@ -1119,7 +1499,31 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             for (int k = 0; k < 4; k++) dl += (k < (int)nv && v[k] > t) ? 4 * (v[k] - t + 1 - fs) : 0u;
             uint32_t tot;
             const uint32_t ex = warp_excl_scan((dl << 16) | vl, &tot);
-            if (vl) put_bits(buf, words, vpos + (ex & 0xffffu), vacc, vl, ovf);
+            if (vl) {
+                if (VPRED && (L.meth & 1)) {
+                    /* prediction codes (up to 31 bits each): n - 1 ones then
+                     * a zero, joined while they fit 64 bits */
+                    uint32_t pos = vpos + (ex & 0xffffu), an = 0;
+                    uint64_t acc = 0;
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        const uint32_t n = n4[k];
+                        if (n) {
+                            if (an + n > 64) {
+                                put_bits(buf, words, pos, acc, an, ovf);
+                                pos += an;
+                                acc = 0;
+                                an = 0;
+                            }
+                            acc = (acc << n) | (((1ull << (n - 1)) - 1) << 1);
+                            an += n;
+                        }
+                    }
+                    if (an) put_bits(buf, words, pos, acc, an, ovf);
+                } else {
+                    put_bits(buf, words, vpos + (ex & 0xffffu), vacc, vl, ovf);
+                }
+            }
             uint32_t sbits = 0, sn = 0;
             if (dl) {
                 /* data bits of the groups with gcli > gtli (pack_data_c,
@@ -1209,66 +1613,115 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
 /* ------------------------------------------------------------------------ */
 /* kernels: one frame, or a batch of frames (block -> frame by its first block) */
 /* ------------------------------------------------------------------------ */
-template <bool SIGNS>
+template <bool SIGNS, bool VPRED>
 __global__ void __launch_bounds__(RC_THREADS, 3) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
                                                            const uint16_t* __restrict__ coef, uint32_t* __restrict__ cost,
                                                            uint32_t* __restrict__ slice_done, PrecRC* __restrict__ rc,
                                                            int* __restrict__ status) {
-    rc_cost_body<SIGNS>(cfg, gcli, coef, cost, slice_done, rc, status, (int)blockIdx.x);
+    rc_cost_body<SIGNS, VPRED>(cfg, gcli, coef, cost, slice_done, rc, status, (int)blockIdx.x);
 }
 
-template <bool SIGNS>
+template <bool SIGNS, bool VPRED>
 __global__ void __launch_bounds__(RC_THREADS, 3) rc_cost_batch_kernel(const __grid_constant__ EncPrecLaunch L) {
     const EncPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
-    rc_cost_body<SIGNS>(F.cfg, F.gcli, F.coef, F.cost, F.slice_done, F.rc, F.status, (int)blockIdx.x - F.first_block);
+    rc_cost_body<SIGNS, VPRED>(F.cfg, F.gcli, F.coef, F.cost, F.slice_done, F.rc, F.status, (int)blockIdx.x - F.first_block);
 }
 
+template <bool VPRED>
 __global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
                                                           const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
                                                           uint8_t* __restrict__ out, uint32_t cap_words, int* status) {
-    pack_body(cfg, coef, gcli, rc, out, cap_words, status, (int)blockIdx.x);
+    pack_body<VPRED>(cfg, coef, gcli, rc, out, cap_words, status, (int)blockIdx.x);
 }
 
+template <bool VPRED>
 __global__ void __launch_bounds__(PK_THREADS, 3) pack_batch_kernel(const __grid_constant__ EncPrecLaunch L, uint32_t cap_words) {
     const EncPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
-    pack_body(F.cfg, F.coef, F.gcli, F.rc, F.out, cap_words, F.status, (int)blockIdx.x - F.first_block);
+    pack_body<VPRED>(F.cfg, F.coef, F.gcli, F.rc, F.out, cap_words, F.status, (int)blockIdx.x - F.first_block);
 }
 
 /* ------------------------------------------------------------------------ */
 /* host-side launchers                                                       */
 /* ------------------------------------------------------------------------ */
+/* The rate-control variants: `modes` bit 0 = a frame of the launch has
+ * sign handling, bit 1 = vertical prediction (dynamic shared memory for
+ * the ordered selection). */
+#define RC_VP_SMEM (RC_VP_REGIONS * RC_LT_REGION * 4)
+template <bool S, bool V>
+static cudaError_t rc_one(const jxs_cfg_t* dcfg, uint32_t np, const uint8_t* gcli, const uint16_t* coef, uint32_t* cost,
+                          uint32_t* slice_done, PrecRC* rc, int* status, cudaStream_t st) {
+    if (V) {
+        static std::atomic<int> attr[JXS_MAX_DEV];
+        cudaError_t e = jxs_smem_attr(rc_cost_kernel<S, V>, RC_VP_SMEM, attr);
+        if (e != cudaSuccess) return e;
+    }
+    rc_cost_kernel<S, V><<<np, RC_THREADS, V ? RC_VP_SMEM : 0, st>>>(dcfg, gcli, coef, cost, slice_done, rc, status);
+    return cudaGetLastError();
+}
+template <bool S, bool V>
+static cudaError_t rc_batch_one(const EncPrecLaunch* L, cudaStream_t st) {
+    if (V) {
+        static std::atomic<int> attr[JXS_MAX_DEV];
+        cudaError_t e = jxs_smem_attr(rc_cost_batch_kernel<S, V>, RC_VP_SMEM, attr);
+        if (e != cudaSuccess) return e;
+    }
+    rc_cost_batch_kernel<S, V><<<L->nblocks, RC_THREADS, V ? RC_VP_SMEM : 0, st>>>(*L);
+    return cudaGetLastError();
+}
+
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli,
                                      const uint16_t* coef, uint32_t* cost, uint32_t* slice_done, PrecRC* rc, int* status,
-                                     int signs, cudaStream_t st) {
+                                     int modes, cudaStream_t st) {
     (void)nslices;
-    if (signs) rc_cost_kernel<true><<<np, RC_THREADS, 0, st>>>(dcfg, gcli, coef, cost, slice_done, rc, status);
-    else rc_cost_kernel<false><<<np, RC_THREADS, 0, st>>>(dcfg, gcli, coef, cost, slice_done, rc, status);
+    switch (modes & 3) {
+    case 0: return rc_one<false, false>(dcfg, np, gcli, coef, cost, slice_done, rc, status, st);
+    case 1: return rc_one<true, false>(dcfg, np, gcli, coef, cost, slice_done, rc, status, st);
+    case 2: return rc_one<false, true>(dcfg, np, gcli, coef, cost, slice_done, rc, status, st);
+    default: return rc_one<true, true>(dcfg, np, gcli, coef, cost, slice_done, rc, status, st);
+    }
+}
+
+template <bool V>
+static cudaError_t pack_one(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli, const PrecRC* rc,
+                            uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st) {
+    const size_t smem = (size_t)cap_words * 4;
+    static std::atomic<int> attr[JXS_MAX_DEV];
+    cudaError_t e = jxs_smem_attr(pack_kernel<V>, (int)smem, attr);
+    if (e != cudaSuccess) return e;
+    pack_kernel<V><<<np, PK_THREADS, smem, st>>>(dcfg, coef, gcli, rc, out, cap_words, status);
     return cudaGetLastError();
 }
 
+/* `modes` bit 1: a frame of the launch has vertical prediction */
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
-                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st) {
+                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, int modes,
+                                       cudaStream_t st) {
+    if (modes & 2) return pack_one<true>(dcfg, np, coef, gcli, rc, out, cap_words, status, st);
+    return pack_one<false>(dcfg, np, coef, gcli, rc, out, cap_words, status, st);
+}
+
+extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, int modes, cudaStream_t st) {
+    if (L->nblocks <= 0) return cudaSuccess;
+    switch (modes & 3) {
+    case 0: return rc_batch_one<false, false>(L, st);
+    case 1: return rc_batch_one<true, false>(L, st);
+    case 2: return rc_batch_one<false, true>(L, st);
+    default: return rc_batch_one<true, true>(L, st);
+    }
+}
+
+template <bool V>
+static cudaError_t pack_batch_one(const EncPrecLaunch* L, uint32_t cap_words, cudaStream_t st) {
     const size_t smem = (size_t)cap_words * 4;
     static std::atomic<int> attr[JXS_MAX_DEV];
-    cudaError_t e = jxs_smem_attr(pack_kernel, (int)smem, attr);
+    cudaError_t e = jxs_smem_attr(pack_batch_kernel<V>, (int)smem, attr);
     if (e != cudaSuccess) return e;
-    pack_kernel<<<np, PK_THREADS, smem, st>>>(dcfg, coef, gcli, rc, out, cap_words, status);
+    if (L->nblocks <= 0) return cudaSuccess;
+    pack_batch_kernel<V><<<L->nblocks, PK_THREADS, smem, st>>>(*L, cap_words);
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, int signs, cudaStream_t st) {
-    if (L->nblocks <= 0) return cudaSuccess;
-    if (signs) rc_cost_batch_kernel<true><<<L->nblocks, RC_THREADS, 0, st>>>(*L);
-    else rc_cost_batch_kernel<false><<<L->nblocks, RC_THREADS, 0, st>>>(*L);
-    return cudaGetLastError();
-}
-
-extern "C" cudaError_t jxs_launch_pack_batch(const EncPrecLaunch* L, uint32_t cap_words, cudaStream_t st) {
-    const size_t smem = (size_t)cap_words * 4;
-    static std::atomic<int> attr[JXS_MAX_DEV];
-    cudaError_t e = jxs_smem_attr(pack_batch_kernel, (int)smem, attr);
-    if (e != cudaSuccess) return e;
-    if (L->nblocks <= 0) return cudaSuccess;
-    pack_batch_kernel<<<L->nblocks, PK_THREADS, smem, st>>>(*L, cap_words);
-    return cudaGetLastError();
+extern "C" cudaError_t jxs_launch_pack_batch(const EncPrecLaunch* L, uint32_t cap_words, int modes, cudaStream_t st) {
+    if (modes & 2) return pack_batch_one<true>(L, cap_words, st);
+    return pack_batch_one<false>(L, cap_words, st);
 }

@@ -157,8 +157,7 @@ static int32_t enc_slot_alloc(jxs_gpu_enc_t* e, EncSlot* s) {
             CK(cudaMalloc(&s->ll[v][k], (size_t)s->ll_pitch[v][k] * h * sizeof(int32_t) + 64));
         }
     }
-    /* with sign handling a second table: the costs with exact sign counts */
-    CK(cudaMalloc(&s->cost, (size_t)c->np * 1024 * sizeof(uint32_t) * (c->fs ? 2 : 1)));
+        CK(cudaMalloc(&s->cost, jxs_cost_bytes(c)));
     CK(cudaMalloc(&s->slice_done, (size_t)c->nslices * sizeof(uint32_t)));
     CK(cudaMemset(s->slice_done, 0, (size_t)c->nslices * sizeof(uint32_t)));
     CK(cudaMalloc(&s->rc, (size_t)c->np * sizeof(PrecRC)));
@@ -315,12 +314,13 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
         KMARK();
     }
     TMARK(2);
-    CK(jxs_launch_rc(e->dcfg, c->np, c->nslices, s->gcli, s->coef, s->cost, s->slice_done, s->rc, s->status, (int)c->fs, st));
+    CK(jxs_launch_rc(e->dcfg, c->np, c->nslices, s->gcli, s->coef, s->cost, s->slice_done, s->rc, s->status,
+                     (c->fs ? 1 : 0) | (c->vpred ? 2 : 0), st));
     KMARK();
     TMARK(3);
     const int out_dev = jxs_gpu_is_device_ptr(out);
     uint8_t* dst = out_dev ? out : s->out_stage;
-    CK(jxs_launch_pack(e->dcfg, c->np, s->coef, s->gcli, s->rc, dst, e->cap_words, s->status, st));
+    CK(jxs_launch_pack(e->dcfg, c->np, s->coef, s->gcli, s->rc, dst, e->cap_words, s->status, c->vpred ? 2 : 0, st));
     KMARK();
     TMARK(4);
     if (!out_dev) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));

@@ -26,11 +26,12 @@ extern "C" int jxs_fwd_v_tile_cols(void);
 extern "C" int jxs_fwd_h_max_rows_per_block(void);
 extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_t nslices, const uint8_t* gcli,
                                      const uint16_t* coef, uint32_t* cost, uint32_t* slice_done, PrecRC* rc, int* status,
-                                     int signs, cudaStream_t st);
-extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, int signs, cudaStream_t st);
+                                     int modes, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, int modes, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
-                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st);
-extern "C" cudaError_t jxs_launch_pack_batch(const EncPrecLaunch* L, uint32_t cap_words, cudaStream_t st);
+                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, int modes,
+                                       cudaStream_t st);
+extern "C" cudaError_t jxs_launch_pack_batch(const EncPrecLaunch* L, uint32_t cap_words, int modes, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
                                          int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status,
                                          cudaStream_t st);
@@ -50,6 +51,14 @@ extern "C" int jxs_inv_v_tile_cols(void);
 extern "C" int jxs_inv_h_max_rows_per_block(void);
 
 static const size_t kSmemMax = 220 * 1024;
+
+/* Rate-control tables of a frame: per precinct row the byte cost of every
+ * (Q, R); with sign handling a second set with exact sign counts; with
+ * vertical prediction the per-line tables of the ordered selection
+ * (5 x 80 x 16 words per row). */
+static inline size_t jxs_cost_bytes(const jxs_cfg_t* c) {
+    return ((size_t)c->np * 1024 * (c->fs ? 2 : 1) + (c->vpred ? (size_t)c->np * 5 * JXS_MAXBLINES * 16 : 0)) * sizeof(uint32_t);
+}
 
 static inline uint32_t div_up(uint32_t a, uint32_t b) { return (a + b - 1) / b; }
 

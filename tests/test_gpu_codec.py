@@ -495,3 +495,82 @@ def test_signs_against_oracle(gpu, oracle, c):
     got = dec.decode(bs)
     dec.close()
     assert all(np.array_equal(a, b) for a, b in zip(got, want))
+
+
+def _vpred_fixtures():
+    out = {}
+    for name, c in G.vpred_cases().items():
+        w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, vpm = c["params"]
+        out[name] = (c, dict(w=w, h=h, d=d, fmt=fmt, bn=bn, bd=bd, v=v, hh=hh, q=q, sl=sl, sig=sig, rc=rc, sg=0, vpm=vpm))
+    for name, c in G.sign_cases().items():
+        w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, sg, vpm = c["params"]
+        if vpm:
+            out[name] = (c, dict(w=w, h=h, d=d, fmt=fmt, bn=bn, bd=bd, v=v, hh=hh, q=q, sl=sl, sig=sig, rc=rc, sg=sg, vpm=vpm))
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(_vpred_fixtures()))
+def test_vertical_prediction_golden_encode(gpu, name):
+    """The encoder with vertical prediction (modes 1 and 2; one case with
+    full signs) reproduces the reference encoder's codestreams byte for
+    byte, per frame and batched."""
+    c, k = _vpred_fixtures()[name]
+    enc = gpu.Encoder(k["w"], k["h"], k["d"], k["fmt"], k["bn"], k["bd"], k["v"], k["hh"], quantization=k["q"],
+                      slice_height=k["sl"], coding_significance=k["sig"], rate_control_mode=k["rc"],
+                      coding_signs_handling=k["sg"], coding_vertical_prediction_mode=k["vpm"])
+    bs = enc.encode(c["planes"])
+    assert np.array_equal(bs, c["bs"]), name
+    batch = gpu.Batch(1 << 28)
+    outs = [np.zeros(enc.frame_bytes, np.uint8)]
+    assert batch.encode([enc], [c["planes"]], outs) == 0
+    r, st = batch.wait()
+    assert r == 0 and np.array_equal(outs[0], c["bs"]), name
+    batch.close()
+    enc.close()
+
+
+def _vpred_random(n, seed):
+    out = []
+    for c in _random_cases(n, seed):
+        c = dict(c)
+        c["vpred"] = 1 + (c["seed"] % 2)
+        c["rc"] = (c["seed"] // 2) % 4
+        c["signs"] = (c["seed"] // 8) % 3
+        out.append(c)
+    return out
+
+
+@pytest.mark.parametrize("c", _vpred_random(48, 95), ids=lambda c: "vp%d_s%d_rc%d_%dx%d_d%d_f%d_V%dH%d_sl%d" % (
+    c["vpred"], c["signs"], c["rc"], c["w"], c["h"], c["d"], c["fmt"], c["v"], c["hh"], c["sl"]))
+def test_vertical_prediction_against_oracle(gpu, oracle, c):
+    """Vertical prediction with every rate-control mode and sign strategy:
+    codestreams and per-precinct (Q, R) byte-exact with the oracle (which
+    matches the reference encoder on these modes), and the GPU decode of
+    the codestream bit-exact with the oracle's decode."""
+    planes = S.frame(c["w"], c["h"], c["d"], c["fmt"], seed=c["seed"])
+    p = oracle.make_params(c["w"], c["h"], c["d"], c["fmt"], c["bpp_num"], c["bpp_den"], c["v"], c["hh"], quantization=c["q"],
+                           slice_height=c["sl"], significance=c["sig"], rc_mode=c["rc"], signs=c["signs"], vpred=c["vpred"])
+    err, ref_bs, ref_q, ref_r = oracle.oracle_encode(p, planes, want_qr=True)
+    kw = dict(coding_signs_handling=c["signs"], coding_vertical_prediction_mode=c["vpred"])
+    if err == 0x80001005:
+        with pytest.raises(gpu.JxsError):
+            make_encoder(gpu, c, **kw)
+        return
+    enc = make_encoder(gpu, c, **kw)
+    out = np.zeros(enc.frame_bytes + 64, np.uint8)
+    assert enc.send(planes, out) == 0
+    q, r = enc.rc_results()
+    rc, f = enc.get()
+    enc.close()
+    assert rc == err
+    if err:
+        return
+    assert np.array_equal(q, ref_q) and np.array_equal(r, ref_r)
+    bs = out[: f.bitstream.used_size]
+    assert np.array_equal(bs, ref_bs)
+    e2, want = oracle.oracle_decode(bs)
+    assert e2 == 0
+    dec = gpu.Decoder(bs)
+    got = dec.decode(bs)
+    dec.close()
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
