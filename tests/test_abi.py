@@ -79,3 +79,24 @@ def test_ctypes_bindings_match_c_layout(jxs_lib, tmp_path):
             if key.startswith(cname + "."):
                 field = key.split(".", 1)[1]
                 assert getattr(py, field).offset == int(off), key
+
+
+def test_plugins_compile_and_link(jxs_lib, tmp_path):
+    """The reference's FFmpeg and IMTL plugins' use of the API (types,
+    constants, struct members, functions in their call forms;
+    tests/plugin_api.c) compiles against include/ and links against
+    libSvtJpegxs.so with no unresolved symbol."""
+    lib_dir = os.path.dirname(jxs_lib.LIB_PATH)
+    so = str(tmp_path / "libplugin_api.so")
+    subprocess.check_call(["gcc", "-std=gnu11", "-Wall", "-Werror", "-shared", "-fPIC", "-I", INCLUDE,
+                           os.path.join(ROOT, "tests", "plugin_api.c"), "-o", so, "-L", lib_dir, "-lSvtJpegxs",
+                           "-Wl,--no-undefined", "-Wl,-rpath," + lib_dir])
+    undefined = subprocess.run(["nm", "-D", "--undefined-only", so], capture_output=True, text=True).stdout
+    used = set(re.findall(r"(svt_jpeg_xs_\w+)", undefined))
+    assert used == {"svt_jpeg_xs_encoder_load_default_parameters", "svt_jpeg_xs_encoder_init", "svt_jpeg_xs_encoder_send_picture",
+                    "svt_jpeg_xs_encoder_get_packet", "svt_jpeg_xs_encoder_close",
+                    "svt_jpeg_xs_decoder_get_single_frame_size_with_proxy", "svt_jpeg_xs_decoder_init",
+                    "svt_jpeg_xs_decoder_send_frame", "svt_jpeg_xs_decoder_get_frame", "svt_jpeg_xs_decoder_close"}
+    out = subprocess.run(["nm", "-D", "--defined-only", jxs_lib.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (svt_jpeg_xs_\w+)", out))
+    assert used <= exported
