@@ -58,8 +58,9 @@
 
 /* ------------------------------------------------------------------------ */
 /* Geometry: restates pi_compute / calc_packet_inclusion /                    */
-/* calc_precinct_dimension (Source/Lib/Common/Codec/Pi.c:21-406) for one      */
-/* precinct column (Cw = 0, the only value the reference encoder writes).     */
+/* calc_precinct_dimension (Source/Lib/Common/Codec/Pi.c:21-406).  Cw = 0     */
+/* (the only value the reference encoder writes) gives one precinct per row;  */
+/* Cw > 0 splits every row into columns of 8 Cw max(Sx) 2^NLx samples.       */
 /* ------------------------------------------------------------------------ */
 typedef struct {
     uint32_t w, h, x, y;
@@ -68,6 +69,10 @@ typedef struct {
     uint32_t gcli_w, sig_w;
     uint8_t gain, prio;
     uint32_t gid;
+    /* precinct columns: coefficients, groups and significance groups of a
+     * normal / the last column, and the row strides of the encoder's GCLI
+     * and significance-maximum planes (each column grouped on its own) */
+    uint32_t wn, wl, gwn, gwl, swn, swl, gstride, sstride;
 } band_t;
 
 typedef struct {
@@ -81,6 +86,7 @@ typedef struct {
 
 typedef struct {
     uint32_t nc, W, H, dv, dh, sd, prec_h, slice_h, pps, np, nslices;
+    uint32_t cw, ncol;             /* precinct width (Cw) and precincts per row; np counts rows */
     uint32_t nbands_all, nbands_exist;
     uint8_t gcomp[MAXGB], gband[MAXGB];
     uint32_t npk;
@@ -88,8 +94,26 @@ typedef struct {
     int short_hdr;
     comp_t c[MAXC];
     uint32_t pk_exist[2];          /* packets present in a normal / the last precinct row */
-    uint32_t raw_bytes[2][MAXPK];  /* raw-mode GCLI sub-packet bytes, normal / last */
+    uint32_t raw_bytes[4][MAXPK];  /* raw-mode GCLI sub-packet bytes per precinct kind (pkind) */
 } geom_t;
+
+/* A precinct's kind: bit 0 the last row, bit 1 the last of several columns
+ * (PRECINCT_NORMAL / _LAST_NORMAL / _NORMAL_LAST / _LAST, Pi.h). */
+static inline int pkind(const geom_t* g, int last_row, uint32_t col) {
+    return last_row + ((g->ncol > 1 && col + 1 == g->ncol) ? 2 : 0);
+}
+
+/* A band's part in precinct column `col`: coefficients, groups and
+ * significance groups, and where they start in the band's rows. */
+typedef struct {
+    uint32_t w, gw, sw, x0, g0, s0;
+} bview_t;
+static inline bview_t bview(const geom_t* g, const band_t* bd, uint32_t col) {
+    const int lc = col + 1 == g->ncol;
+    bview_t v = {lc ? bd->wl : bd->wn, lc ? bd->gwl : bd->gwn, lc ? bd->swl : bd->swn, col * bd->wn, col * bd->gwn,
+                 col * bd->swn};
+    return v;
+}
 
 static int sampling(uint32_t fmt, uint32_t* nc, uint32_t sx[MAXC], uint32_t sy[MAXC]) {
     /* format_get_sampling_factory, Pi.c:521-565 */
@@ -106,8 +130,9 @@ static int sampling(uint32_t fmt, uint32_t* nc, uint32_t sx[MAXC], uint32_t sy[M
 }
 
 static int geom_compute(geom_t* g, int for_encoder, uint32_t nc, uint32_t W, uint32_t H, uint32_t dh, uint32_t dv, uint32_t sd,
-                        const uint32_t sx[MAXC], const uint32_t sy[MAXC], uint32_t slice_h) {
+                        const uint32_t sx[MAXC], const uint32_t sy[MAXC], uint32_t slice_h, uint32_t cw) {
     memset(g, 0, sizeof(*g));
+    g->cw = cw;
     if (sd > nc || dv > dh || dh > 5 || dv > 2 || nc > MAXC || slice_h == 0) return E_BAD_PARAM;
     g->nc = nc; g->W = W; g->H = H; g->dh = dh; g->dv = dv; g->sd = sd;
     const uint32_t ncd = nc - sd;
@@ -216,14 +241,38 @@ static int geom_compute(geom_t* g, int for_encoder, uint32_t nc, uint32_t W, uin
     g->npk = n;
     g->short_hdr = (W * nc) < 32752;
 
-    /* calc_precinct_dimension, Pi.c:21-129 (precinct_width = 0) */
+    /* calc_precinct_dimension, Pi.c:21-129 */
     g->np = DIV_UP(H, 1u << dv);
+    g->ncol = 1;
+    uint32_t cs = 0;
+    if (cw) {
+        uint32_t sx_max = 0;
+        for (uint32_t c = 0; c < nc; c++) sx_max = MAX(sx_max, g->c[c].sx);
+        cs = 8 * cw * sx_max * (1u << dh);
+        g->ncol = DIV_UP(W, cs);
+        if (g->ncol >= 130) return E_BAD_PARAM; /* MAX_PRECINCT_IN_LINE, Decoder.c:294 */
+    }
     for (uint32_t c = 0; c < nc; c++)
         for (uint32_t b = 0; b < g->c[c].nb; b++) {
             band_t* bd = &g->c[c].b[b];
             bd->last_lines = bd->h - (g->np - 1) * bd->lines;
             bd->gcli_w = DIV_UP(bd->w, 4);
             bd->sig_w = DIV_UP(bd->gcli_w, 8);
+            bd->wn = bd->w; /* one column: it is the last one, of the band's width */
+            if (cw && g->ncol > 1) {
+                const uint64_t num = (uint64_t)cs * bd->w, den = (uint64_t)g->c[c].sx * g->c[c].w;
+                bd->wn = (uint32_t)((bd->w % 2) ? num / den : (num + den - 1) / den);
+                /* a last column without coefficients is outside this
+                 * restatement (the reference's width_last would wrap) */
+                if ((uint64_t)(g->ncol - 1) * bd->wn >= bd->w) return E_BAD_PARAM;
+            }
+            bd->wl = bd->w - (g->ncol - 1) * bd->wn;
+            bd->gwn = DIV_UP(bd->wn, 4);
+            bd->gwl = DIV_UP(bd->wl, 4);
+            bd->swn = DIV_UP(bd->gwn, 8);
+            bd->swl = DIV_UP(bd->gwl, 8);
+            bd->gstride = (g->ncol - 1) * bd->gwn + bd->gwl;
+            bd->sstride = (g->ncol - 1) * bd->swn + bd->swl;
         }
     if (for_encoder) {
         g->pk_exist[0] = g->npk;
@@ -235,13 +284,13 @@ static int geom_compute(geom_t* g, int for_encoder, uint32_t nc, uint32_t W, uin
             cnt += present;
         }
         g->pk_exist[1] = cnt;
-        for (int t = 0; t < 2; t++)
+        for (int t = 0; t < 4; t++)
             for (uint32_t k = 0; k < g->npk; k++) {
                 uint32_t bits = 0;
                 for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
                     band_t* bd = &g->c[g->gcomp[i]].b[g->gband[i]];
-                    uint32_t lines = t ? bd->last_lines : bd->lines;
-                    if (g->pk[k].line < lines) bits += bd->gcli_w * 4;
+                    uint32_t lines = (t & 1) ? bd->last_lines : bd->lines;
+                    if (g->pk[k].line < lines) bits += ((t & 2) ? bd->gwl : bd->gwn) * 4;
                 }
                 g->raw_bytes[t][k] = DIV_UP(bits, 8);
             }
@@ -568,7 +617,7 @@ static int enc_configure(enc_t* e, const or_enc_params_t* p) {
         else { mh = 0; break; }
     }
     if (mw == 0 || mh == 0) return E_BAD_PARAM;
-    int r = geom_compute(&e->g, 1, nc, c->width, c->height, c->decomp_h, c->decomp_v, 0, sx, sy, c->slice_height);
+    int r = geom_compute(&e->g, 1, nc, c->width, c->height, c->decomp_h, c->decomp_v, 0, sx, sy, c->slice_height, c->precinct_width);
     if (r) return r;
     if (weights_assign(&e->g, c->colour_format)) return E_BAD_PARAM;
     e->fmt = c->colour_format;
@@ -623,7 +672,7 @@ static void enc_write_header(enc_t* e) {
     bw_put(&w, 0, 16);                         /* Plev */
     bw_put(&w, g->W, 16);
     bw_put(&w, g->H, 16);
-    bw_put(&w, 0, 16);                         /* Cw */
+    bw_put(&w, g->cw, 16);                     /* Cw */
     bw_put(&w, g->pps, 16);                    /* Hsl */
     bw_put(&w, g->nc, 8);
     bw_put(&w, 4, 8);                          /* Ng */
@@ -718,24 +767,27 @@ static void enc_dwt_one(void* ctx, uint32_t c) {
             for (uint32_t x = 0; x < bd->w; x++) o[(size_t)y * bd->w + x] = to_sm(a[(size_t)(bd->y + y) * w + bd->x + x]);
         /* gc_precinct_stage_scalar_c and gc_precinct_sigflags_max_c
          * (GcStageProcess.c:22-97) */
-        for (uint32_t y = 0; y < bd->h; y++) {
-            const uint16_t* row = o + (size_t)y * bd->w;
-            uint8_t* gl = e->gcli[c][b] + (size_t)y * bd->gcli_w;
-            for (uint32_t gi = 0; gi < bd->gcli_w; gi++) {
-                uint16_t m = 0;
-                for (uint32_t k = gi * 4; k < MIN(gi * 4 + 4, bd->w); k++) m |= row[k];
-                m = (uint16_t)(m << 1);
-                uint8_t v = 0;
-                while (m >> v) v++;
-                gl[gi] = m ? (uint8_t)(v - 1) : 0;
+        /* each precinct column grouped from its own first coefficient */
+        for (uint32_t y = 0; y < bd->h; y++)
+            for (uint32_t col = 0; col < e->g.ncol; col++) {
+                const bview_t v = bview(&e->g, bd, col);
+                const uint16_t* row = o + (size_t)y * bd->w + v.x0;
+                uint8_t* gl = e->gcli[c][b] + (size_t)y * bd->gstride + v.g0;
+                for (uint32_t gi = 0; gi < v.gw; gi++) {
+                    uint16_t m = 0;
+                    for (uint32_t k = gi * 4; k < MIN(gi * 4 + 4, v.w); k++) m |= row[k];
+                    m = (uint16_t)(m << 1);
+                    uint8_t nb = 0;
+                    while (m >> nb) nb++;
+                    gl[gi] = m ? (uint8_t)(nb - 1) : 0;
+                }
+                uint8_t* sm = e->sigmax[c][b] + (size_t)y * bd->sstride + v.s0;
+                for (uint32_t s = 0; s < v.sw; s++) {
+                    uint8_t mx = 0;
+                    for (uint32_t k = s * 8; k < MIN(s * 8 + 8, v.gw); k++) mx = MAX(mx, gl[k]);
+                    sm[s] = mx;
+                }
             }
-            uint8_t* sm = e->sigmax[c][b] + (size_t)y * bd->sig_w;
-            for (uint32_t s = 0; s < bd->sig_w; s++) {
-                uint8_t mx = 0;
-                for (uint32_t k = s * 8; k < MIN(s * 8 + 8, bd->gcli_w); k++) mx = MAX(mx, gl[k]);
-                sm[s] = mx;
-            }
-        }
     }
     free(a);
 }
@@ -790,25 +842,26 @@ static uint32_t nz_levels(uint32_t m, uint32_t g, uint32_t uniform) {
     return n;
 }
 
-static void prec_stats(const enc_t* e, uint32_t p, int last, prec_stats_t* st) {
+static void prec_stats(const enc_t* e, uint32_t p, uint32_t col, int last, prec_stats_t* st) {
     const geom_t* g = &e->g;
     memset(st, 0, sizeof(*st));
     for (uint32_t c = 0; c < g->nc; c++)
         for (uint32_t b = 0; b < g->c[c].nb; b++) {
             const band_t* bd = &g->c[c].b[b];
+            const bview_t v = bview(g, bd, col);
             uint32_t lines = last ? bd->last_lines : bd->lines;
             st->lines[c][b] = lines;
             for (uint32_t l = 0; l < lines; l++) {
                 uint32_t row = p * bd->lines + l;
-                const uint8_t* gl = e->gcli[c][b] + (size_t)row * bd->gcli_w;
-                for (uint32_t i = 0; i < bd->gcli_w; i++) st->hist[c][b][l][gl[i]]++;
-                const uint8_t* sm = e->sigmax[c][b] + (size_t)row * bd->sig_w;
-                uint32_t full = bd->gcli_w / 8;
+                const uint8_t* gl = e->gcli[c][b] + (size_t)row * bd->gstride + v.g0;
+                for (uint32_t i = 0; i < v.gw; i++) st->hist[c][b][l][gl[i]]++;
+                const uint8_t* sm = e->sigmax[c][b] + (size_t)row * bd->sstride + v.s0;
+                uint32_t full = v.gw / 8;
                 for (uint32_t i = 0; i < full; i++) st->sighist[c][b][l][sm[i]]++;
-                st->partial_max[c][b][l] = (full < bd->sig_w) ? sm[full] : -1;
+                st->partial_max[c][b][l] = (full < v.sw) ? sm[full] : -1;
                 if (e->prm.coding_signs_handling) {
-                    const uint16_t* cf = e->coef[c][b] + (size_t)row * bd->w;
-                    for (uint32_t i = 0; i < bd->w; i++)
+                    const uint16_t* cf = e->coef[c][b] + (size_t)row * bd->w + v.x0;
+                    for (uint32_t i = 0; i < v.w; i++)
                         st->nzhist[c][b][l][nz_levels(cf[i] & 0x7fffu, gl[i / 4], e->prm.quantization)]++;
                 }
             }
@@ -861,8 +914,9 @@ static uint32_t vp_line_cost(const uint8_t* cur, const uint8_t* top, uint32_t gc
 }
 
 static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint8_t q, uint8_t r, prec_cost_t* pc, int smode,
-                          uint32_t p, const vp_top_t* top) {
+                          uint32_t p, uint32_t col, const vp_top_t* top) {
     const geom_t* g = &e->g;
+    const int kind = pkind(g, last, col);
     uint32_t sign_bits[MAXC][MAXB][2];
     for (uint32_t c = 0; c < g->nc; c++)
         for (uint32_t b = 0; b < g->c[c].nb; b++) {
@@ -871,7 +925,8 @@ static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint
             pc->gtli[c][b] = t;
             uint32_t lines = st->lines[c][b];
             if (!lines) continue;
-            uint32_t nosig[2], total_nosig = 0, total_sig = bd->sig_w * lines, gsig[2];
+            const bview_t v = bview(g, bd, col);
+            uint32_t nosig[2], total_nosig = 0, total_sig = v.sw * lines, gsig[2];
             for (uint32_t l = 0; l < lines; l++) {
                 const uint32_t* h = st->hist[c][b][l];
                 uint32_t data = 0, zero = 0, above = 0;
@@ -896,7 +951,7 @@ static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint
                 for (uint32_t v = 0; v <= t; v++) zeroed += st->sighist[c][b][l][v];
                 zeroed *= 8;
                 if (st->partial_max[c][b][l] >= 0 && (uint32_t)st->partial_max[c][b][l] <= t)
-                    zeroed += bd->gcli_w - (bd->gcli_w / 8) * 8;
+                    zeroed += v.gw - (v.gw / 8) * 8;
                 gsig[l] = nosig[l] - zeroed;
                 total_sig += gsig[l];
             }
@@ -913,15 +968,15 @@ static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint
                 uint32_t tot_vn = 0, tot_vs = 0;
                 for (uint32_t l = 0; l < lines; l++) {
                     const size_t row = (size_t)(p * bd->lines + l);
-                    const uint8_t* cur = e->gcli[c][b] + row * bd->gcli_w;
-                    const uint8_t* tl = l ? cur - bd->gcli_w : e->gcli[c][b] + ((size_t)top->p * bd->lines + bd->lines - 1) * bd->gcli_w;
+                    const uint8_t* cur = e->gcli[c][b] + row * bd->gstride + v.g0;
+                    const uint8_t* tl = l ? cur - bd->gstride : e->gcli[c][b] + ((size_t)top->p * bd->lines + bd->lines - 1) * bd->gstride + v.g0;
                     const int tt = l ? t : top->gtli[c][b];
                     uint32_t red = 0;
-                    vnos[l] = vp_line_cost(cur, tl, bd->gcli_w, bd->sig_w, t, tt, e->prm.coding_vertical_prediction_mode == 2,
+                    vnos[l] = vp_line_cost(cur, tl, v.gw, v.sw, t, tt, e->prm.coding_vertical_prediction_mode == 2,
                                            &red, NULL, NULL);
                     vsig[l] = vnos[l] - red;
                     tot_vn += vnos[l];
-                    tot_vs += vsig[l] + bd->sig_w;
+                    tot_vs += vsig[l] + v.sw;
                 }
                 if (best > tot_vn) {
                     method = 1;
@@ -935,7 +990,7 @@ static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint
             pc->sig_method[c][b] = (uint8_t)method;
             for (uint32_t l = 0; l < lines; l++) {
                 pc->gcli_bits[c][b][l] = method == 0 ? nosig[l] : method == 2 ? gsig[l] : method == 1 ? vnos[l] : vsig[l];
-                pc->sig_bits[c][b][l] = (method & 2) ? bd->sig_w : 0;
+                pc->sig_bits[c][b][l] = (method & 2) ? v.sw : 0;
             }
         }
     uint32_t total = 0;
@@ -954,10 +1009,10 @@ static uint32_t prec_cost(const enc_t* e, const prec_stats_t* st, int last, uint
         pc->pk_data[k] = dB;
         pc->pk_sign[k] = DIV_UP(nb, 8);
         total += dB + pc->pk_sign[k];
-        if (sB + gB > g->raw_bytes[last][k]) {
+        if (sB + gB > g->raw_bytes[kind][k]) {
             pc->raw[k] = 1;
             pc->pk_sig[k] = 0;
-            pc->pk_gcli[k] = g->raw_bytes[last][k];
+            pc->pk_gcli[k] = g->raw_bytes[kind][k];
         } else {
             pc->raw[k] = 0;
             pc->pk_sig[k] = sB;
@@ -1007,7 +1062,7 @@ static int bs_next(bsearch_t* s, int res, uint32_t* out) {
 /* rate_control_precinct (RateControl.c:1259-1333) with the binary searches of
  * RateControl.c:889-1083.  Returns 0 and fills q, r, data_bytes, headers. */
 static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t budget, uint8_t* q_out, uint8_t* r_out,
-                   uint32_t* data_bytes, uint32_t* hdr_bytes, prec_cost_t* pc, uint32_t p, const vp_top_t* top) {
+                   uint32_t* data_bytes, uint32_t* hdr_bytes, prec_cost_t* pc, uint32_t p, uint32_t col, const vp_top_t* top) {
     const geom_t* g = &e->g;
     if (budget > PREC_MAX_BYTES) return E_ENC_FRAME;
     uint32_t hdr = DIV_UP(5 * 8 + g->nbands_exist * 2, 8);
@@ -1029,7 +1084,7 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
     uint32_t qv = 0;
     while ((res = bs_next(&s, next, &qv)) == BS_CONTINUE) {
         if (all_truncated(g, (uint8_t)qv, 0)) { next = BS_OUT_OF_RANGE; continue; }
-        next = prec_cost(e, st, last, (uint8_t)qv, 0, pc, sfast, p, NULL) > avail ? BS_TOO_SMALL : BS_TOO_BIG;
+        next = prec_cost(e, st, last, (uint8_t)qv, 0, pc, sfast, p, col, NULL) > avail ? BS_TOO_SMALL : BS_TOO_BIG;
     }
     if (res != BS_FOUND) return E_ENC_FRAME;
     uint8_t q = (uint8_t)qv;
@@ -1037,12 +1092,12 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
         /* lower quantizations while they fit, else the first higher that fits */
         int best = -1;
         for (int qt = (int)q - 1; qt >= 0; qt--) {
-            if (all_truncated(g, (uint8_t)qt, 0) || prec_cost(e, st, last, (uint8_t)qt, 0, pc, smode, p, top) > avail) break;
+            if (all_truncated(g, (uint8_t)qt, 0) || prec_cost(e, st, last, (uint8_t)qt, 0, pc, smode, p, col, top) > avail) break;
             best = qt;
         }
         if (best < 0)
             for (uint32_t qt = q; qt <= e->max_q; qt++)
-                if (!all_truncated(g, (uint8_t)qt, 0) && prec_cost(e, st, last, (uint8_t)qt, 0, pc, smode, p, top) <= avail) {
+                if (!all_truncated(g, (uint8_t)qt, 0) && prec_cost(e, st, last, (uint8_t)qt, 0, pc, smode, p, col, top) <= avail) {
                     best = (int)qt;
                     break;
                 }
@@ -1060,7 +1115,7 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
     while ((res = bs_next(&s, next, &rv)) == BS_CONTINUE) {
         last_tested = -1;
         if (all_truncated(g, q, (uint8_t)rv)) { next = BS_OUT_OF_RANGE; continue; }
-        uint32_t cst = prec_cost(e, st, last, q, (uint8_t)rv, pc, smode, p, top);
+        uint32_t cst = prec_cost(e, st, last, q, (uint8_t)rv, pc, smode, p, col, top);
         last_tested = (int32_t)rv;
         last_cost = cst;
         next = cst <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
@@ -1069,7 +1124,7 @@ static int prec_rc(const enc_t* e, const prec_stats_t* st, int last, uint32_t bu
     (void)last_tested;
     (void)last_cost;
     /* The pack step needs the per-packet decisions of the chosen pair. */
-    *data_bytes = prec_cost(e, st, last, q, (uint8_t)rv, pc, smode, p, top);
+    *data_bytes = prec_cost(e, st, last, q, (uint8_t)rv, pc, smode, p, col, top);
     *q_out = q;
     *r_out = (uint8_t)rv;
     return E_NONE;
@@ -1097,8 +1152,8 @@ static inline uint16_t quantize(uint16_t v, uint8_t gcli, uint8_t t, uint32_t un
  * coefficient of the groups above gtli (pack_sign_c, :200-233).  Returns
  * non-zero when a sign sub-packet differs from the size the rate control
  * computed. */
-static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc, uint8_t q, uint8_t r, uint32_t total_bytes,
-                     bw_t* w, const vp_top_t* top) {
+static int prec_pack(const enc_t* e, uint32_t p, uint32_t col, int last, const prec_cost_t* pc, uint8_t q, uint8_t r,
+                     uint32_t total_bytes, bw_t* w, const vp_top_t* top) {
     const geom_t* g = &e->g;
     uint32_t hdr_len = DIV_UP(5 * 8 + 2 * g->nbands_exist, 8);
     bw_put(w, total_bytes - hdr_len, 24);
@@ -1139,8 +1194,9 @@ static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc
                 uint32_t c = g->gcomp[i], b = g->gband[i];
                 const band_t* bd = &g->c[c].b[b];
                 if (l >= (last ? bd->last_lines : bd->lines)) continue;
-                const uint8_t* gl = e->gcli[c][b] + (size_t)(p * bd->lines + l) * bd->gcli_w;
-                for (uint32_t x = 0; x < bd->gcli_w; x++) bw_put(w, gl[x], 4);
+                const bview_t v = bview(g, bd, col);
+                const uint8_t* gl = e->gcli[c][b] + (size_t)(p * bd->lines + l) * bd->gstride + v.g0;
+                for (uint32_t x = 0; x < v.gw; x++) bw_put(w, gl[x], 4);
             }
             bw_align(w);
         } else {
@@ -1151,20 +1207,22 @@ static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc
                 uint32_t c = g->gcomp[i], b = g->gband[i];
                 const band_t* bd = &g->c[c].b[b];
                 if (l >= (last ? bd->last_lines : bd->lines) || !(pc->sig_method[c][b] & 1)) continue;
-                if (bd->gcli_w > 2048 || bd->sig_w > 256) return E_RESOURCES;
+                const bview_t v = bview(g, bd, col);
+                if (v.gw > 2048 || v.sw > 256) return E_RESOURCES;
                 const size_t row = (size_t)(p * bd->lines + l);
-                const uint8_t* cur = e->gcli[c][b] + row * bd->gcli_w;
-                const uint8_t* tl = l ? cur - bd->gcli_w : e->gcli[c][b] + ((size_t)top->p * bd->lines + bd->lines - 1) * bd->gcli_w;
+                const uint8_t* cur = e->gcli[c][b] + row * bd->gstride + v.g0;
+                const uint8_t* tl = l ? cur - bd->gstride : e->gcli[c][b] + ((size_t)top->p * bd->lines + bd->lines - 1) * bd->gstride + v.g0;
                 uint32_t red;
-                vp_line_cost(cur, tl, bd->gcli_w, bd->sig_w, pc->gtli[c][b], l ? pc->gtli[c][b] : top->gtli[c][b],
+                vp_line_cost(cur, tl, v.gw, v.sw, pc->gtli[c][b], l ? pc->gtli[c][b] : top->gtli[c][b],
                              e->prm.coding_vertical_prediction_mode == 2, &red, vflags[i - g->pk[k].bs], vbits[i - g->pk[k].bs]);
             }
             for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
                 uint32_t c = g->gcomp[i], b = g->gband[i];
                 const band_t* bd = &g->c[c].b[b];
                 if (l >= (last ? bd->last_lines : bd->lines) || !(pc->sig_method[c][b] & 2)) continue;
-                const uint8_t* sm = e->sigmax[c][b] + (size_t)(p * bd->lines + l) * bd->sig_w;
-                for (uint32_t s = 0; s < bd->sig_w; s++)
+                const bview_t v = bview(g, bd, col);
+                const uint8_t* sm = e->sigmax[c][b] + (size_t)(p * bd->lines + l) * bd->sstride + v.s0;
+                for (uint32_t s = 0; s < v.sw; s++)
                     bw_put(w, (pc->sig_method[c][b] & 1) ? vflags[i - g->pk[k].bs][s] : sm[s] <= pc->gtli[c][b], 1);
             }
             bw_align(w);
@@ -1174,9 +1232,10 @@ static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc
                 if (l >= (last ? bd->last_lines : bd->lines)) continue;
                 const uint8_t t = pc->gtli[c][b];
                 const uint8_t meth = pc->sig_method[c][b];
-                const uint8_t* gl = e->gcli[c][b] + (size_t)(p * bd->lines + l) * bd->gcli_w;
-                const uint8_t* sm = e->sigmax[c][b] + (size_t)(p * bd->lines + l) * bd->sig_w;
-                for (uint32_t x = 0; x < bd->gcli_w; x++) {
+                const bview_t v = bview(g, bd, col);
+                const uint8_t* gl = e->gcli[c][b] + (size_t)(p * bd->lines + l) * bd->gstride + v.g0;
+                const uint8_t* sm = e->sigmax[c][b] + (size_t)(p * bd->lines + l) * bd->sstride + v.s0;
+                for (uint32_t x = 0; x < v.gw; x++) {
                     uint32_t n;
                     if (meth & 1) {
                         if ((meth & 2) && vflags[i - g->pk[k].bs][x / 8]) continue;
@@ -1198,14 +1257,15 @@ static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc
             if (l >= (last ? bd->last_lines : bd->lines)) continue;
             const uint8_t t = pc->gtli[c][b];
             const size_t row = (size_t)(p * bd->lines + l);
-            const uint8_t* gl = e->gcli[c][b] + row * bd->gcli_w;
-            const uint16_t* cf = e->coef[c][b] + row * bd->w;
-            for (uint32_t x = 0; x < bd->gcli_w; x++) {
+            const bview_t v = bview(g, bd, col);
+            const uint8_t* gl = e->gcli[c][b] + row * bd->gstride + v.g0;
+            const uint16_t* cf = e->coef[c][b] + row * bd->w + v.x0;
+            for (uint32_t x = 0; x < v.gw; x++) {
                 if (gl[x] <= t) continue;
                 for (uint32_t k2 = 0; k2 < 4; k2++) {
                     uint32_t xi = x * 4 + k2;
-                    uint16_t v = xi < bd->w ? cf[xi] : 0;
-                    qbuf[k2] = t ? quantize(v, gl[x], t, uniform) : v;
+                    uint16_t cv = xi < v.w ? cf[xi] : 0;
+                    qbuf[k2] = t ? quantize(cv, gl[x], t, uniform) : cv;
                 }
                 uint32_t signs = 0;
                 for (uint32_t k2 = 0; k2 < 4; k2++) signs = (signs << 1) | (qbuf[k2] >> 15);
@@ -1227,9 +1287,10 @@ static int prec_pack(const enc_t* e, uint32_t p, int last, const prec_cost_t* pc
             if (l >= (last ? bd->last_lines : bd->lines)) continue;
             const uint8_t t = pc->gtli[c][b];
             const size_t row = (size_t)(p * bd->lines + l);
-            const uint8_t* gl = e->gcli[c][b] + row * bd->gcli_w;
-            const uint16_t* cf = e->coef[c][b] + row * bd->w;
-            for (uint32_t xi = 0; xi < bd->w; xi++) {
+            const bview_t v = bview(g, bd, col);
+            const uint8_t* gl = e->gcli[c][b] + row * bd->gstride + v.g0;
+            const uint16_t* cf = e->coef[c][b] + row * bd->w + v.x0;
+            for (uint32_t xi = 0; xi < v.w; xi++) {
                 const uint8_t gv = gl[xi / 4];
                 if (gv <= t) continue;
                 const uint16_t qv = t ? quantize(cf[xi], gv, t, uniform) : cf[xi];
@@ -1273,10 +1334,13 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     const int sfast = e->prm.coding_signs_handling ? SIGNS_FAST : SIGNS_OFF;
     if (!st) return E_RESOURCES;
     uint32_t headers = 0;
+    /* precinct i of the slice: row first_p + i / ncol, column i % ncol */
+#define PREC_ROW(i) (first_p + (i) / g->ncol)
+#define PREC_COL(i) ((i) % g->ncol)
+#define PREC_LAST(i) (PREC_ROW(i) + 1 >= g->np)
     for (uint32_t i = 0; i < nprec; i++) {
-        const int last = first_p + i + 1 >= g->np;
-        prec_stats(e, first_p + i, last, &st[i]);
-        total[i] = prec_hdr_bytes(g, last);
+        prec_stats(e, PREC_ROW(i), PREC_COL(i), PREC_LAST(i), &st[i]);
+        total[i] = prec_hdr_bytes(g, PREC_LAST(i));
         headers += total[i];
     }
     if (slice_budget <= headers) {
@@ -1293,7 +1357,7 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     while ((res = bs_next(&s, next, &qv)) == BS_CONTINUE) {
         if (all_truncated(g, (uint8_t)qv, 0)) { next = BS_OUT_OF_RANGE; continue; }
         uint32_t sum = 0;
-        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, (uint8_t)qv, 0, &pc, sfast, first_p + i, NULL);
+        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], PREC_LAST(i), (uint8_t)qv, 0, &pc, sfast, PREC_ROW(i), PREC_COL(i), NULL);
         next = sum > avail ? BS_TOO_SMALL : BS_TOO_BIG;
     }
     if (res != BS_FOUND) {
@@ -1309,7 +1373,7 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     while ((res = bs_next(&s, next, &rv)) == BS_CONTINUE) {
         if (all_truncated(g, q, (uint8_t)rv)) { next = BS_OUT_OF_RANGE; continue; }
         uint32_t sum = 0;
-        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc, sfast, first_p + i, NULL);
+        for (uint32_t i = 0; i < nprec; i++) sum += prec_cost(e, &st[i], PREC_LAST(i), q, (uint8_t)rv, &pc, sfast, PREC_ROW(i), PREC_COL(i), NULL);
         next = sum <= avail ? BS_TOO_SMALL : BS_TOO_BIG;
     }
     if (res != BS_FOUND) {
@@ -1318,7 +1382,7 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     }
     uint32_t pad_last = avail;
     for (uint32_t i = 0; i < nprec; i++) {
-        const uint32_t d = prec_cost(e, &st[i], first_p + i + 1 >= g->np, q, (uint8_t)rv, &pc, sfast, first_p + i, NULL);
+        const uint32_t d = prec_cost(e, &st[i], PREC_LAST(i), q, (uint8_t)rv, &pc, sfast, PREC_ROW(i), PREC_COL(i), NULL);
         pad_last -= d;
         total[i] += d;
     }
@@ -1372,6 +1436,9 @@ static int slice_common_budgets(const enc_t* e, uint32_t first_p, uint32_t nprec
     }
     return E_NONE;
 }
+#undef PREC_ROW
+#undef PREC_COL
+#undef PREC_LAST
 
 /* pack_stage_kernel (PackStageProcess.c:567-749): RC modes 0 and 1
  * (process_precinct :274-338) split the slice evenly (mode 1: the first
@@ -1385,8 +1452,9 @@ static void enc_slice(void* ctx, uint32_t s) {
     for (uint32_t i = 0; i < s; i++) begin += e->slice_sizes[i];
     const int last_slice = s == g->nslices - 1;
     uint32_t slice_budget = e->slice_sizes[s] - 6 - (last_slice ? 2 : 0);
-    uint32_t first_p = g->pps * s;
-    uint32_t nprec = last_slice ? g->np - first_p : g->pps;
+    uint32_t first_p = g->pps * s; /* first precinct row */
+    /* precincts of the slice: rows x columns, row after row */
+    uint32_t nprec = (last_slice ? g->np - first_p : g->pps) * g->ncol;
     uint32_t min_b = slice_budget / nprec;
     uint32_t left = slice_budget - min_b * nprec;
     uint32_t first_b = min_b;
@@ -1415,19 +1483,26 @@ static void enc_slice(void* ctx, uint32_t s) {
     uint32_t carry = 0;
     prec_stats_t st;
     prec_cost_t pc;
-    /* vertical prediction: the row above in the slice, with its final gtli */
-    vp_top_t top_rows[2];
-    const vp_top_t* top = NULL;
+    /* vertical prediction: the precinct above in the slice (same column),
+     * with its final gtli */
+    vp_top_t* tops = (vp_top_t*)malloc(sizeof(vp_top_t) * g->ncol);
+    if (!tops) {
+        free(common);
+        e->slice_err = E_RESOURCES;
+        return;
+    }
     for (uint32_t i = 0; i < nprec; i++) {
-        uint32_t p = first_p + i;
+        const uint32_t p = first_p + i / g->ncol, col = i % g->ncol;
         int last = (p + 1 >= g->np);
+        const vp_top_t* top = (e->prm.coding_vertical_prediction_mode && i >= g->ncol) ? &tops[col] : NULL;
         uint32_t budget = (common ? common[i] : (i == 0 ? first_b : min_b) + (i < left ? 1 : 0)) + carry;
-        prec_stats(e, p, last, &st);
+        prec_stats(e, p, col, last, &st);
         uint8_t q = 0, r = 0;
         uint32_t data = 0, hdr = 0;
-        int err = prec_rc(e, &st, last, budget, &q, &r, &data, &hdr, &pc, p, top);
+        int err = prec_rc(e, &st, last, budget, &q, &r, &data, &hdr, &pc, p, col, top);
         if (err) {
             free(common);
+            free(tops);
             e->slice_err = err;
             return;
         }
@@ -1439,7 +1514,7 @@ static void enc_slice(void* ctx, uint32_t s) {
          * precinct and in mode 0 (PackStageProcess.c:293-333) */
         uint32_t retrieve = 0;
         if (e->prm.coding_signs_handling == SIGNS_FAST) {
-            retrieve = data - prec_cost(e, &st, last, q, r, &pc, SIGNS_FULL, p, top);
+            retrieve = data - prec_cost(e, &st, last, q, r, &pc, SIGNS_FULL, p, col, top);
         }
         /* modes 1-3 move a precinct's padding to the next one */
         if (e->prm.rate_control_mode >= 1 && i + 1 < nprec) {
@@ -1447,30 +1522,30 @@ static void enc_slice(void* ctx, uint32_t s) {
             carry = padding + retrieve;
             padding = 0;
         }
-        if (e->q_out) e->q_out[p] = q;
-        if (e->r_out) e->r_out[p] = r;
+        if (e->q_out) e->q_out[p * g->ncol + col] = q;
+        if (e->r_out) e->r_out[p * g->ncol + col] = r;
         if (i == 0) { /* write_slice_header, PackHeaders.c:91-96 */
             bw_put(&w, 0xff20, 16);
             bw_put(&w, 4, 16);
             bw_put(&w, s, 16);
         }
         uint64_t start = w.bit;
-        if (prec_pack(e, p, last, &pc, q, r, total, &w, top) || ((w.bit - start) >> 3) != hdr + data - retrieve) {
+        if (prec_pack(e, p, col, last, &pc, q, r, total, &w, top) || ((w.bit - start) >> 3) != hdr + data - retrieve) {
             free(common);
+            free(tops);
             e->slice_err = E_ENC_FRAME;
             return;
         }
         if (e->prm.coding_vertical_prediction_mode) {
-            vp_top_t* nt = &top_rows[i & 1];
-            nt->p = p;
-            memcpy(nt->gtli, pc.gtli, sizeof(nt->gtli));
-            top = nt;
+            tops[col].p = p;
+            memcpy(tops[col].gtli, pc.gtli, sizeof(tops[col].gtli));
         }
         uint64_t used = (w.bit - start) >> 3;
         for (uint64_t z = used; z < total; z++) bw_put(&w, 0, 8);
     }
     if (last_slice) bw_put(&w, 0xff11, 16); /* EOC */
     free(common);
+    free(tops);
 }
 
 static void enc_free(enc_t* e) {
@@ -1488,8 +1563,8 @@ static int enc_alloc(enc_t* e) {
         for (uint32_t b = 0; b < e->g.c[c].nb; b++) {
             band_t* bd = &e->g.c[c].b[b];
             e->coef[c][b] = (uint16_t*)malloc(sizeof(uint16_t) * (size_t)bd->w * bd->h);
-            e->gcli[c][b] = (uint8_t*)malloc((size_t)bd->gcli_w * bd->h);
-            e->sigmax[c][b] = (uint8_t*)malloc((size_t)bd->sig_w * bd->h);
+            e->gcli[c][b] = (uint8_t*)malloc((size_t)bd->gstride * bd->h);
+            e->sigmax[c][b] = (uint8_t*)malloc((size_t)bd->sstride * bd->h);
             if (!e->coef[c][b] || !e->gcli[c][b] || !e->sigmax[c][b]) return E_RESOURCES;
         }
     return E_NONE;
@@ -1681,8 +1756,7 @@ static int dec_parse_header(const uint8_t* bs, uint32_t size, dec_hdr_t* h) {
     }
     if (!have_cdt || !have_wgt) return E_DEC_BITSTREAM;
     if (h->cpih) return E_DEC_BITSTREAM;
-    if (cw != 0) return E_DEC_BITSTREAM; /* multi-column precincts are outside this restatement */
-    int e = geom_compute(&h->g, 0, nc, W, H, dh, dv, sd, sx, sy, hsl * (1u << dv));
+    int e = geom_compute(&h->g, 0, nc, W, H, dh, dv, sd, sx, sy, hsl * (1u << dv), cw);
     if (e) return e;
     /* copy_weights_table, Decoder.c:35-50 */
     uint32_t k = 0;
@@ -1752,7 +1826,7 @@ static int gstore_alloc(gstore_t* s, const geom_t* g) {
     memset(s, 0, sizeof(*s));
     for (uint32_t c = 0; c < g->nc; c++)
         for (uint32_t b = 0; b < g->c[c].nb; b++) {
-            s->g[c][b] = (uint8_t*)calloc((size_t)g->c[c].b[b].gcli_w * 4 + 8, 1);
+            s->g[c][b] = (uint8_t*)calloc((size_t)MAX(g->c[c].b[b].gwn, g->c[c].b[b].gwl) * 4 + 8, 1);
             if (!s->g[c][b]) return E_RESOURCES;
         }
     return E_NONE;
@@ -1799,7 +1873,7 @@ static int decode_vpred_line(br_t* r, int64_t* left, uint8_t* gl, const uint8_t*
  * dequantisation and sign conversion
  * (Dequant.c:9-57, Precinct.c:9-29).  `top` is the precinct above in the
  * same slice (NULL for the first precinct of a slice). */
-static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, const gstore_t* top) {
+static int dec_precinct(dec_t* d, br_t* r, uint32_t p, uint32_t col, int last, gstore_t* cur, const gstore_t* top) {
     dec_hdr_t* h = d->h;
     const geom_t* g = &h->g;
     if (!br_enough(r, 5 + DIV_UP(g->nbands_exist * 2, 8))) return E_DEC_SHORT;
@@ -1843,10 +1917,11 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, 
             for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
                 const band_t* bd = &g->c[g->gcomp[i]].b[g->gband[i]];
                 if (l >= (last ? bd->last_lines : bd->lines)) continue;
-                left -= bd->gcli_w * 4;
+                const bview_t v = bview(g, bd, col);
+                left -= v.gw * 4;
                 if (left < 0) return E_DEC_BITSTREAM;
-                uint8_t* gl = cur->g[g->gcomp[i]][g->gband[i]] + (size_t)l * bd->gcli_w;
-                for (uint32_t x = 0; x < bd->gcli_w; x++) gl[x] = (uint8_t)br_get(r, 4);
+                uint8_t* gl = cur->g[g->gcomp[i]][g->gband[i]] + (size_t)l * v.gw;
+                for (uint32_t x = 0; x < v.gw; x++) gl[x] = (uint8_t)br_get(r, 4);
             }
         } else {
             /* significance sub-packet: 1 = group insignificant */
@@ -1854,11 +1929,12 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, 
                 const band_t* bd = &g->c[g->gcomp[i]].b[g->gband[i]];
                 if (l >= (last ? bd->last_lines : bd->lines)) continue;
                 if (mode[i] & 2) {
-                    if (bd->sig_w > 1024) return E_RESOURCES;
-                    left -= bd->sig_w;
+                    const bview_t v = bview(g, bd, col);
+                    if (v.sw > 1024) return E_RESOURCES;
+                    left -= v.sw;
                     if (left < 0) return E_DEC_BITSTREAM;
                     sig_store[i - g->pk[k].bs] = sbuf[i - g->pk[k].bs];
-                    for (uint32_t s2 = 0; s2 < bd->sig_w; s2++) sig_store[i - g->pk[k].bs][s2] = (uint8_t)br_get(r, 1);
+                    for (uint32_t s2 = 0; s2 < v.sw; s2++) sig_store[i - g->pk[k].bs][s2] = (uint8_t)br_get(r, 1);
                 }
             }
             br_align(r);
@@ -1868,15 +1944,16 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, 
                 uint32_t c = g->gcomp[i], b = g->gband[i];
                 const band_t* bd = &g->c[c].b[b];
                 if (l >= (last ? bd->last_lines : bd->lines)) continue;
-                uint8_t* gl = cur->g[c][b] + (size_t)l * bd->gcli_w;
+                const bview_t v = bview(g, bd, col);
+                uint8_t* gl = cur->g[c][b] + (size_t)l * v.gw;
                 const uint8_t t = cur->gtli[c][b];
                 const uint8_t* sf = sig_store[i - g->pk[k].bs];
                 if (mode[i] & 1) {
-                    const uint8_t* tp = l == 0 ? top->g[c][b] + (size_t)(bd->lines - 1) * bd->gcli_w : cur->g[c][b] + (size_t)(l - 1) * bd->gcli_w;
+                    const uint8_t* tp = l == 0 ? top->g[c][b] + (size_t)(bd->lines - 1) * v.gw : cur->g[c][b] + (size_t)(l - 1) * v.gw;
                     const uint8_t tt = l == 0 ? top->gtli[c][b] : t;
-                    if (decode_vpred_line(r, &left, gl, tp, t, tt, bd->gcli_w, sf, (int)h->rm)) return E_DEC_BITSTREAM;
+                    if (decode_vpred_line(r, &left, gl, tp, t, tt, v.gw, sf, (int)h->rm)) return E_DEC_BITSTREAM;
                 } else {
-                    for (uint32_t x = 0; x < bd->gcli_w; x++) {
+                    for (uint32_t x = 0; x < v.gw; x++) {
                         if (sf && sf[x / 8]) { gl[x] = t; continue; }
                         int n = vlc_next(r, &left);
                         if (n < 0) return E_DEC_BITSTREAM;
@@ -1902,10 +1979,11 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, 
             const band_t* bd = &g->c[c].b[b];
             if (l >= (last ? bd->last_lines : bd->lines)) continue;
             const uint8_t t = cur->gtli[c][b];
-            const uint8_t* gl = cur->g[c][b] + (size_t)l * bd->gcli_w;
-            uint16_t* out = (uint16_t*)d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w;
-            for (uint32_t x = 0; x < bd->gcli_w; x++) {
-                uint16_t v[4] = {0, 0, 0, 0};
+            const bview_t v = bview(g, bd, col);
+            const uint8_t* gl = cur->g[c][b] + (size_t)l * v.gw;
+            uint16_t* out = (uint16_t*)d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w + v.x0;
+            for (uint32_t x = 0; x < v.gw; x++) {
+                uint16_t vv[4] = {0, 0, 0, 0};
                 int32_t planes = (int32_t)gl[x] - t;
                 if (planes > 0) {
                     left -= 4 * (planes + (h->fs ? 0 : 1));
@@ -1916,11 +1994,11 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, 
                         uint32_t nib = br_get(r, 4);
                         for (int k2 = 0; k2 < 4; k2++) m[k2] = (m[k2] << 1) | ((nib >> (3 - k2)) & 1u);
                     }
-                    for (int k2 = 0; k2 < 4; k2++) v[k2] = (uint16_t)((uint16_t)(m[k2] << t) | (((sg >> (3 - k2)) & 1u) << 15));
+                    for (int k2 = 0; k2 < 4; k2++) vv[k2] = (uint16_t)((uint16_t)(m[k2] << t) | (((sg >> (3 - k2)) & 1u) << 15));
                 }
                 for (uint32_t k2 = 0; k2 < 4; k2++) {
-                    if (x * 4 + k2 < bd->w) out[x * 4 + k2] = v[k2];
-                    else leftover_nz[i - g->pk[k].bs] += v[k2] != 0; /* its sign is sent too (Packing.c:200-215) */
+                    if (x * 4 + k2 < v.w) out[x * 4 + k2] = vv[k2];
+                    else leftover_nz[i - g->pk[k].bs] += vv[k2] != 0; /* its sign is sent too (Packing.c:200-215) */
                 }
             }
         }
@@ -1940,15 +2018,16 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, 
                 uint32_t c = g->gcomp[i], b = g->gband[i];
                 const band_t* bd = &g->c[c].b[b];
                 if (l >= (last ? bd->last_lines : bd->lines)) continue;
-                uint16_t* out = (uint16_t*)d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w;
-                for (uint32_t x = 0; x < bd->w; x++) {
+                const bview_t v = bview(g, bd, col);
+                uint16_t* out = (uint16_t*)d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w + v.x0;
+                for (uint32_t x = 0; x < v.w; x++) {
                     if (!out[x]) continue;
                     if (--left < 0) return E_DEC_BITSTREAM;
                     if (!br_enough(r, 1)) return E_DEC_SHORT;
                     out[x] |= (uint16_t)(br_get(r, 1) << 15);
                 }
                 const uint32_t lo = leftover_nz[i - g->pk[k].bs];
-                if (lo && (bd->w % 4)) {
+                if (lo && (v.w % 4)) {
                     left -= lo;
                     if (left < 0) return E_DEC_BITSTREAM;
                     r->bit += lo;
@@ -1970,9 +2049,10 @@ static int dec_precinct(dec_t* d, br_t* r, uint32_t p, int last, gstore_t* cur, 
             const band_t* bd = &g->c[c].b[b];
             if (l >= (last ? bd->last_lines : bd->lines)) continue;
             const uint8_t t = cur->gtli[c][b];
-            const uint8_t* gl = cur->g[c][b] + (size_t)l * bd->gcli_w;
-            int16_t* out = d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w;
-            for (uint32_t x = 0; x < bd->w; x++) {
+            const bview_t v = bview(g, bd, col);
+            const uint8_t* gl = cur->g[c][b] + (size_t)l * v.gw;
+            int16_t* out = d->coef[c][b] + (size_t)(p * bd->lines + l) * bd->w + v.x0;
+            for (uint32_t x = 0; x < v.w; x++) {
                 const uint16_t raw = (uint16_t)out[x];
                 uint16_t mag = raw & 0x7fff;
                 if (t > 0 && mag) {
@@ -2001,22 +2081,22 @@ static void dec_slice(void* ctx, uint32_t s) {
     br_t r = {d->bs, d->size, (uint64_t)d->slice_off[s] * 8};
     if (!br_enough(&r, 6)) { d->err = E_DEC_SHORT; return; }
     if (br_get(&r, 16) != 0xff20 || br_get(&r, 16) != 4 || br_get(&r, 16) != s) { d->err = E_DEC_BITSTREAM; return; }
-    gstore_t st[2];
-    if (gstore_alloc(&st[0], g) || gstore_alloc(&st[1], g)) {
-        gstore_free(&st[0]);
-        gstore_free(&st[1]);
-        d->err = E_RESOURCES;
-        return;
-    }
+    /* the precincts of a row, column after column (Decoder.c:537-580);
+     * each column keeps the row above's GCLIs for vertical prediction */
+    const uint32_t ncol = g->ncol;
+    gstore_t* st = (gstore_t*)calloc(2 * (size_t)ncol, sizeof(gstore_t));
+    int err = st ? E_NONE : E_RESOURCES;
+    for (uint32_t k = 0; k < 2 * ncol && !err; k++) err = gstore_alloc(&st[k], g);
     uint32_t first = s * g->pps;
     uint32_t n = (s == g->nslices - 1) ? g->np - first : g->pps;
-    for (uint32_t i = 0; i < n; i++) {
+    for (uint32_t i = 0; i < n && !err; i++) {
         uint32_t p = first + i;
-        int e = dec_precinct(d, &r, p, p + 1 >= g->np, &st[i & 1], i ? &st[(i + 1) & 1] : NULL);
-        if (e) { d->err = e; break; }
+        for (uint32_t col = 0; col < ncol && !err; col++)
+            err = dec_precinct(d, &r, p, col, p + 1 >= g->np, &st[2 * col + (i & 1)], i ? &st[2 * col + ((i + 1) & 1)] : NULL);
     }
-    gstore_free(&st[0]);
-    gstore_free(&st[1]);
+    if (err) d->err = err;
+    for (uint32_t k = 0; st && k < 2 * ncol; k++) gstore_free(&st[k]);
+    free(st);
 }
 
 typedef struct {
@@ -2082,7 +2162,7 @@ int or_decode(const uint8_t* bs, uint32_t size, void* const planes[4], const uin
         d.slice_off[s] = (uint32_t)off;
         off += 6;
         uint32_t first = s * g->pps;
-        uint32_t n = (s == g->nslices - 1) ? g->np - first : g->pps;
+        uint32_t n = ((s == g->nslices - 1) ? g->np - first : g->pps) * g->ncol;
         for (uint32_t i = 0; i < n; i++) {
             if (off + 3 > size) { free(d.slice_off); return E_DEC_SHORT; }
             uint32_t lprc = ((uint32_t)bs[off] << 16) | ((uint32_t)bs[off + 1] << 8) | bs[off + 2];

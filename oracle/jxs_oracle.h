@@ -21,6 +21,8 @@ typedef struct or_enc_params {
     uint32_t quantization, slice_height, rate_control_mode;
     uint32_t coding_significance, coding_signs_handling, coding_vertical_prediction_mode;
     uint32_t threads_num;
+    uint32_t precinct_width; /* Cw: 0 (the reference encoder's only value), or > 0 for
+                                multi-column test codestreams */
 } or_enc_params_t;
 
 typedef struct or_image_info {

@@ -254,7 +254,7 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_decoder_init(uint64_t version_api_major
         return SvtJxsErrorBadParameter;
     }
     p->cfg->proxy = ss;
-    p->prec_off = (uint32_t*)malloc(sizeof(uint32_t) * p->cfg->np);
+    p->prec_off = (uint32_t*)malloc(sizeof(uint32_t) * p->cfg->nprec);
     p->gpu = jxs_gpu_dec_create(p->cfg, DEC_SLOTS, &r);
     if (!p->gpu || !p->prec_off) {
         jxs_gpu_dec_destroy(p->gpu);
@@ -483,7 +483,7 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_decode(svt_jpeg_xs_gpu_batch_
         if (!bs[i] || !size[i]) return SvtJxsErrorDecoderInvalidPointer;
         walked[i] = 0;
         if (!jxs_gpu_is_device_ptr(bs[i])) {
-            uint32_t* prec = jxs_gpu_batch_prec_buffer(b, i, p->cfg->np);
+            uint32_t* prec = jxs_gpu_batch_prec_buffer(b, i, p->cfg->nprec);
             if (!prec) return SvtJxsErrorInsufficientResources;
             jxs_hdr_info_t info;
             pthread_mutex_lock(&p->send_mu);

@@ -206,7 +206,7 @@ static uint64_t dec_work_layout(const jxs_cfg_t* c, uint8_t* base, DecWork* w) {
     memset(&w->fb, 0, sizeof(w->fb));
     w->bs_cap = c->lcod + 4096;
     w->bs = take((uint64_t)w->bs_cap + 64);
-    w->prec_off = (uint32_t*)take((uint64_t)c->np * sizeof(uint32_t));
+    w->prec_off = (uint32_t*)take((uint64_t)c->nprec * sizeof(uint32_t));
     w->fb.coef = take(c->coef_total * sizeof(int16_t) + 64);
     uint64_t llsz[2][JXS_MAXC];
     ll_layout(c, w->fb.ll_pitch, llsz);
@@ -515,7 +515,7 @@ static int32_t plan_decode_chain(const std::vector<DecItem>& it, const std::vect
             F.status = d.status;
             F.first_block = L->nblocks;
             F.first_slice = L->nslices;
-            L->nblocks += (int)d.c->np;
+            L->nblocks += (int)d.c->nprec;
             L->nslices += (int)d.c->nslices;
             cb = std::max(cb, d.cap_bytes);
             cg = std::max(cg, d.cap_groups);
@@ -1169,8 +1169,8 @@ extern "C" int32_t jxs_gpu_batch_decode(jxs_gpu_batch_t* b, jxs_gpu_dec_t* const
         const int dev = jxs_gpu_is_device_ptr(bs[i]);
         if (host_walked && host_walked[i]) {
             /* precinct offsets found on the host (jxs_frame_bytes_walk) */
-            if (!w.prec_off_h || w.prec_cap < c->np) return JXS_E_BAD_PARAM;
-            BCK(cudaMemcpyAsync(w.prec_off, w.prec_off_h, (size_t)c->np * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+            if (!w.prec_off_h || w.prec_cap < c->nprec) return JXS_E_BAD_PARAM;
+            BCK(cudaMemcpyAsync(w.prec_off, w.prec_off_h, (size_t)c->nprec * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
             d.walk = 0;
         } else {
             if (!dev || size[i] < c->hdr_len) return JXS_E_DEC_PTR;

@@ -46,7 +46,7 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
     uint32_t sg = 128;
     for (;;) {
         int fits = 1;
-        for (int t = 0; t < 2; t++) {
+        for (int t = 0; t < 4; t++) {
             uint32_t n = 0, ns = 0, gsum = 0;
             for (uint32_t k = 0; k < g->npk; k++) {
                 const uint32_t l = g->pk[k].line;
@@ -56,21 +56,22 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
                     const uint32_t fb = g->g2f[gb];
                     if (fb == JXS_NOBAND) continue;
                     const jxs_band_t* bd = &g->band[fb];
-                    if (l >= (t ? bd->last_lines : bd->lines)) continue;
+                    if (l >= ((t & 1) ? bd->last_lines : bd->lines)) continue;
                     if (n >= JXS_MAXBLINES) return JXS_E_BAD_PARAM;
+                    const uint32_t w = (t & 2) ? bd->cwl : bd->cwn, gw = DIV_UP(w, 4);
                     g->pk_nbl[t][k]++;
                     jxs_bline_t* b = &g->bline[t][n++];
                     b->fb = (uint8_t)fb;
                     b->line = (uint8_t)l;
                     b->pk = (uint8_t)k;
                     b->pad = 0;
-                    b->gcli_w = bd->gcli_w;
-                    b->sig_w = bd->sig_w;
-                    b->w = bd->w;
+                    b->gcli_w = gw;
+                    b->sig_w = DIV_UP(gw, 8);
+                    b->w = w;
                     b->gbase = gsum;
-                    gsum += (bd->gcli_w + 3) & ~3u; /* 4-aligned: 32-bit access to 4 groups */
+                    gsum += (gw + 3) & ~3u; /* 4-aligned: 32-bit access to 4 groups */
                     b->seg0 = ns;
-                    b->nseg = (bd->gcli_w + sg - 1) / sg;
+                    b->nseg = (gw + sg - 1) / sg;
                     if (b->nseg == 0) b->nseg = 1;
                     for (uint32_t i = 0; i < b->nseg; i++, ns++) {
                         if (ns < JXS_MAXSEG) {
@@ -89,12 +90,14 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
         sg *= 2;
     }
     g->seg_groups = sg;
-    /* the line above each band line, for vertical prediction */
-    for (int t = 0; t < 2; t++) {
+    /* the line above each band line, for vertical prediction (line 0: the
+     * band's last line in the precinct above, a normal row of the same
+     * column kind) */
+    for (int t = 0; t < 4; t++) {
         for (uint32_t x = 0; x < g->nbline[t]; x++) {
             const jxs_bline_t* b = &g->bline[t][x];
             const int prev = b->line == 0;
-            const int tt = prev ? 0 : t;
+            const int tt = prev ? (t & 2) : t;
             const uint32_t want = prev ? g->band[b->fb].lines - 1 : b->line - 1u;
             g->top_bl[t][x] = 0xff;
             g->top_prev[t][x] = (uint8_t)prev;
@@ -114,7 +117,7 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
 /* Each packet's band lines by ascending band priority (the order in which
  * a growing refinement R lowers their gtli); needs the weight tables. */
 static void cfg_pk_order(jxs_cfg_t* g) {
-    for (int t = 0; t < 2; t++)
+    for (int t = 0; t < 4; t++)
         for (uint32_t k = 0; k < g->npk; k++) {
             const uint32_t b0 = g->pk_bl0[t][k], nb = g->pk_nbl[t][k];
             for (uint32_t i = 0; i < nb; i++) g->pk_order[t][b0 + i] = (uint8_t)(b0 + i);
@@ -131,7 +134,7 @@ static void cfg_pk_order(jxs_cfg_t* g) {
 }
 
 int32_t jxs_cfg_geometry(jxs_cfg_t* g, int for_encoder, uint32_t nc, uint32_t W, uint32_t H, uint32_t dh, uint32_t dv,
-                         uint32_t sd, const uint32_t sx[JXS_MAXC], const uint32_t sy[JXS_MAXC], uint32_t slice_h) {
+                         uint32_t sd, const uint32_t sx[JXS_MAXC], const uint32_t sy[JXS_MAXC], uint32_t slice_h, uint32_t cw) {
     if (sd > nc || dv > dh || dh > 5 || dv > 2 || nc > JXS_MAXC || nc < 1 || slice_h == 0) return JXS_E_BAD_PARAM;
     g->nc = nc; g->W = W; g->H = H; g->dh = dh; g->dv = dv; g->sd = sd;
     const uint32_t ncd = nc - sd;
@@ -251,14 +254,37 @@ int32_t jxs_cfg_geometry(jxs_cfg_t* g, int for_encoder, uint32_t nc, uint32_t W,
     g->npk = n;
     g->short_hdr = (W * nc) < 32752;
 
-    /* precinct rows and buffer layout (Pi.c:21-129, precinct_width 0) */
+    /* precinct rows and columns, buffer layout (calc_precinct_dimension,
+     * Pi.c:21-129): Cw > 0 splits each row into columns of
+     * 8 Cw max(Sx) 2^NLx samples */
     g->np = DIV_UP(H, 1u << dv);
+    g->cw = cw;
+    g->ncol = 1;
+    uint32_t cs = 0;
+    if (cw) {
+        uint32_t sx_max = 0;
+        for (uint32_t c = 0; c < nc; c++) sx_max = sx[c] > sx_max ? sx[c] : sx_max;
+        cs = 8 * cw * sx_max * (1u << dh);
+        g->ncol = DIV_UP(W, cs);
+        if (g->ncol >= 130) return JXS_E_BAD_PARAM; /* MAX_PRECINCT_IN_LINE, Decoder.c:294 */
+    }
+    g->nprec = g->np * g->ncol;
     uint64_t coff = 0, goff = 0;
     for (uint32_t i = 0; i < g->nbands; i++) {
         jxs_band_t* bd = &g->band[i];
         bd->last_lines = bd->h - (g->np - 1) * bd->lines;
         bd->gcli_w = DIV_UP(bd->w, 4);
         bd->sig_w = DIV_UP(bd->gcli_w, 8);
+        bd->cwn = bd->w; /* one column: it is the last one, of the band's width */
+        if (cw && g->ncol > 1) {
+            const jxs_comp_t* cp = &g->comp[bd->comp];
+            const uint64_t num = (uint64_t)cs * bd->w, den = (uint64_t)cp->sx * cp->w;
+            bd->cwn = (uint32_t)((bd->w % 2) ? num / den : (num + den - 1) / den);
+            /* a last column without coefficients (the reference's width_last
+             * would wrap) is refused */
+            if ((uint64_t)(g->ncol - 1) * bd->cwn >= bd->w) return JXS_E_BAD_PARAM;
+        }
+        bd->cwl = bd->w - (g->ncol - 1) * bd->cwn;
         bd->pitch = ALIGN_UP(bd->w, 8);
         bd->gpitch = ALIGN_UP(bd->gcli_w, 16);
         bd->coef_off = coff;
@@ -269,23 +295,23 @@ int32_t jxs_cfg_geometry(jxs_cfg_t* g, int for_encoder, uint32_t nc, uint32_t W,
     g->coef_total = coff;
     g->gcli_total = goff;
     g->prec_hdr_bytes = DIV_UP(40 + 2 * g->nbands, 8);
-    for (int t = 0; t < 2; t++) {
+    for (int t = 0; t < 4; t++) {
         uint32_t cnt = 0;
         for (uint32_t k = 0; k < g->npk; k++) {
             uint32_t bits = 0;
             int present = 0;
             for (uint32_t i = g->pk[k].bs; i < g->pk[k].be; i++) {
                 const jxs_band_t* bd = &g->band[g->g2f[i]];
-                uint32_t lines = t ? bd->last_lines : bd->lines;
+                uint32_t lines = (t & 1) ? bd->last_lines : bd->lines;
                 if (g->pk[k].line < lines) {
                     present = 1;
-                    bits += bd->gcli_w * 4;
+                    bits += DIV_UP((t & 2) ? bd->cwl : bd->cwn, 4) * 4;
                 }
             }
             g->raw_bytes[t][k] = DIV_UP(bits, 8);
             cnt += present;
         }
-        g->pk_exist[t] = for_encoder ? (t == 0 ? g->npk : cnt) : cnt;
+        if (t < 2) g->pk_exist[t] = for_encoder ? (t == 0 ? g->npk : cnt) : cnt;
     }
     return cfg_blines(g);
 }
@@ -558,8 +584,9 @@ int32_t jxs_cfg_encoder(jxs_cfg_t* g, struct svt_jpeg_xs_encoder_api* api) {
     if (mw == 0 || mh == 0) return JXS_E_BAD_PARAM;
     if (api->rate_control_mode > 3) return JXS_E_BAD_PARAM;
 
+    /* the reference encoder writes Cw = 0 (EncHandle.c:401) */
     int32_t r = jxs_cfg_geometry(g, 1, nc, api->source_width, api->source_height, api->ndecomp_h, api->ndecomp_v, 0, sx, sy,
-                                 api->slice_height);
+                                 api->slice_height, 0);
     if (r) return r;
     g->fmt = api->colour_format;
     g->depth = api->input_bit_depth;
@@ -693,9 +720,9 @@ int32_t jxs_cfg_decoder(jxs_cfg_t* g, const uint8_t* bs, size_t size, jxs_hdr_in
         }
     }
     if (!have_cdt || !have_wgt) return JXS_E_DEC_BITSTREAM;
-    if (info->cpih || cw) return JXS_E_DEC_BITSTREAM;
+    if (info->cpih) return JXS_E_DEC_BITSTREAM;
     if (dv > 31) return JXS_E_DEC_BITSTREAM;
-    int32_t e = jxs_cfg_geometry(g, 0, nc, W, H, dh, dv, sd, sx, sy, hsl * (1u << dv));
+    int32_t e = jxs_cfg_geometry(g, 0, nc, W, H, dh, dv, sd, sx, sy, hsl * (1u << dv), cw);
     if (e) return e;
     uint32_t k = 0;
     for (uint32_t i = 0; i < g->nbands_all; i++) {
@@ -745,7 +772,8 @@ uint32_t jxs_frame_bytes_walk(const jxs_cfg_t* g, const uint8_t* bs, size_t size
             return 0;
         }
         off += 6;
-        uint32_t first = s * g->pps, n = (s + 1 == g->nslices) ? g->np - first : g->pps;
+        /* the slice's precincts: rows x columns, row after row */
+        uint32_t first = s * g->pps * g->ncol, n = ((s + 1 == g->nslices) ? g->np - s * g->pps : g->pps) * g->ncol;
         for (uint32_t i = 0; i < n; i++) {
             if (off + g->prec_hdr_bytes > size) { *err = JXS_E_DEC_SHORT; return 0; }
             uint32_t lprc = ((uint32_t)bs[off] << 16) | ((uint32_t)bs[off + 1] << 8) | bs[off + 2];

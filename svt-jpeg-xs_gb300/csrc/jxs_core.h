@@ -55,6 +55,7 @@ typedef struct jxs_band {
     uint32_t last_lines;        /* band lines in the last precinct row */
     uint32_t gcli_w, sig_w;     /* code groups / significance groups per line */
     uint32_t pitch, gpitch;     /* coefficient / GCLI row pitch */
+    uint32_t cwn, cwl;          /* coefficients per line in a normal / the last precinct column (w when Cw = 0) */
     uint64_t coef_off, gcli_off;
     uint8_t gain, prio, comp, idx;
     uint32_t gid;               /* position in the codestream band order */
@@ -88,6 +89,7 @@ typedef struct jxs_seg {
 typedef struct jxs_cfg {
     uint32_t W, H, nc, fmt, depth, sd;
     uint32_t dv, dh, prec_h, slice_h, pps, np, nslices;
+    uint32_t cw, ncol, nprec;   /* precinct width Cw, precincts per row (Cw = 0: 1), precincts (np rows x ncol) */
     uint32_t nbands_all, nbands;
     uint8_t g2f[JXS_MAXBL];     /* global band -> flat band index */
     jxs_comp_t comp[JXS_MAXC];
@@ -96,7 +98,7 @@ typedef struct jxs_cfg {
     jxs_packet_t pk[JXS_MAXPK];
     uint32_t short_hdr, lh;
     uint32_t pk_exist[2];                /* packets present: normal / last precinct row */
-    uint32_t raw_bytes[2][JXS_MAXPK];    /* raw-mode GCLI sub-packet bytes */
+    uint32_t raw_bytes[4][JXS_MAXPK];    /* raw-mode GCLI sub-packet bytes per precinct kind (jxs_pkind) */
     uint32_t prec_hdr_bytes;             /* ceil((40 + 2 * nbands) / 8) */
     uint32_t hdrs_bytes[2];              /* precinct header + packet headers */
     uint32_t qpih, sig, rc_mode, fs, rm, bw, fq;
@@ -108,20 +110,22 @@ typedef struct jxs_cfg {
     uint8_t hdr[512];
     uint32_t hdr_len;
     uint64_t coef_total, gcli_total;     /* per-frame buffer sizes (elements / bytes) */
-    uint32_t nbline[2];                  /* band lines: normal / last precinct row */
-    jxs_bline_t bline[2][JXS_MAXBLINES];
-    uint8_t pk_bl0[2][JXS_MAXPK];        /* first band line of each packet (its count in pk_nbl; 0: absent) */
-    uint8_t pk_nbl[2][JXS_MAXPK];
-    uint8_t pk_order[2][JXS_MAXBLINES];  /* band lines of each packet (from pk_bl0) in ascending band priority */
+    /* tables per precinct kind (jxs_pkind): normal, last row, last column,
+     * last row and column */
+    uint32_t nbline[4];                  /* band lines */
+    jxs_bline_t bline[4][JXS_MAXBLINES];
+    uint8_t pk_bl0[4][JXS_MAXPK];        /* first band line of each packet (its count in pk_nbl; 0: absent) */
+    uint8_t pk_nbl[4][JXS_MAXPK];
+    uint8_t pk_order[4][JXS_MAXBLINES];  /* band lines of each packet (from pk_bl0) in ascending band priority */
     /* vertical prediction: the band line above each band line (same band,
      * line - 1 in the same precinct; for line 0 the band's last line in the
      * precinct row above, a normal row), and where its GCLIs start */
-    uint8_t top_bl[2][JXS_MAXBLINES];    /* band line index (in the normal row's table when top_prev) */
-    uint8_t top_prev[2][JXS_MAXBLINES];  /* 1: in the precinct row above */
-    uint32_t top_gbase[2][JXS_MAXBLINES];
+    uint8_t top_bl[4][JXS_MAXBLINES];    /* band line index (in the normal row's table when top_prev) */
+    uint8_t top_prev[4][JXS_MAXBLINES];  /* 1: in the precinct row above */
+    uint32_t top_gbase[4][JXS_MAXBLINES];
     uint32_t seg_groups;                 /* groups per segment, a multiple of 32 */
-    uint32_t nseg[2];
-    jxs_seg_t seg[2][JXS_MAXSEG];
+    uint32_t nseg[4];
+    jxs_seg_t seg[4][JXS_MAXSEG];
     uint32_t max_slice_budget;           /* 0 when slice starts cannot be predicted (decoder) */
     uint32_t proxy;                      /* decoder: output at 1/2^proxy resolution (proxy modes, Pi.c:567-626) */
     uint32_t slice_size[8192];           /* bytes of each slice incl. its header (last: incl. EOC) */
@@ -162,8 +166,16 @@ static inline JXS_HD uint8_t jxs_truncation(uint8_t gain, uint8_t prio, uint8_t 
 int32_t jxs_cfg_encoder(jxs_cfg_t* cfg, struct svt_jpeg_xs_encoder_api* api);
 int32_t jxs_cfg_slices(jxs_cfg_t* cfg);
 int32_t jxs_cfg_decoder(jxs_cfg_t* cfg, const uint8_t* bs, size_t size, jxs_hdr_info_t* info);
+/* A precinct's kind: bit 0 the last row, bit 1 the last of several columns
+ * (PRECINCT_NORMAL / _LAST_NORMAL / _NORMAL_LAST / _LAST, Pi.h); p counts
+ * precincts row after row, ncol per row. */
+static inline JXS_HD int jxs_pkind(const jxs_cfg_t* c, uint32_t p) {
+    const uint32_t row = p / c->ncol, col = p - row * c->ncol;
+    return (row + 1 >= c->np ? 1 : 0) | (c->ncol > 1 && col + 1 == c->ncol ? 2 : 0);
+}
+
 int32_t jxs_cfg_geometry(jxs_cfg_t* cfg, int for_encoder, uint32_t nc, uint32_t W, uint32_t H, uint32_t dh, uint32_t dv,
-                         uint32_t sd, const uint32_t sx[JXS_MAXC], const uint32_t sy[JXS_MAXC], uint32_t slice_h);
+                         uint32_t sd, const uint32_t sx[JXS_MAXC], const uint32_t sy[JXS_MAXC], uint32_t slice_h, uint32_t cw);
 int32_t jxs_sampling(uint32_t fmt, uint32_t* nc, uint32_t sx[JXS_MAXC], uint32_t sy[JXS_MAXC]);
 uint32_t jxs_frame_bytes_walk(const jxs_cfg_t* cfg, const uint8_t* bs, size_t size, uint32_t hdr_len, uint32_t* prec_off,
                               int32_t* err);

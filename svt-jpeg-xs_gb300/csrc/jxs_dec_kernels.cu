@@ -253,7 +253,10 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     __shared__ int s_hasvp;
     __shared__ uint32_t s_nz[JXS_MAXSEG], s_sgb[JXS_MAXSEG]; /* separate signs: per segment, count and first bit */
 
-    const int last = (p + 1 >= (int)cfg->np);
+    /* the precinct kind's tables (last row / last of several columns) */
+    const int last = jxs_pkind(cfg, (uint32_t)p);
+    const uint32_t prow = (uint32_t)p / cfg->ncol, pcol = (uint32_t)p - prow * cfg->ncol;
+    const int one_col = cfg->ncol == 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     /* thread 0: the frame's status and the precinct's length field; every
      * thread meanwhile stages this precinct kind's tables and the scalars
@@ -297,7 +300,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         for (uint32_t x = threadIdx.x; x < nl; x += blockDim.x) {
             const jxs_bline_t& B = cfg->bline[last][x];
             const jxs_band_t& bd = cfg->band[B.fb];
-            s_crow[x] = bd.coef_off + (uint64_t)(p * bd.lines + B.line) * bd.pitch;
+            s_crow[x] = bd.coef_off + (uint64_t)(prow * bd.lines + B.line) * bd.pitch + (uint64_t)pcol * bd.cwn;
             s_lgp[x] = (uint16_t)(bd.gain | (bd.prio << 8));
             s_topbl[x] = cfg->top_bl[last][x];
             s_topprev[x] = cfg->top_prev[last][x];
@@ -823,7 +826,19 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                 if (len) o = group_finish(A, B2, sgn, uniform && L.t != 0, (int)B.w - 4 * (int)g);
                 spos += stot;
             }
-            if (valid) *(uint2*)(crow + 4 * g) = o;
+            if (valid) {
+                if (one_col) {
+                    *(uint2*)(crow + 4 * g) = o; /* the band row's padding takes the last group's tail */
+                } else {
+                    /* a column starts anywhere in the row and ends where the
+                     * next begins: the group's coefficients inside it only */
+                    const int wl = (int)B.w - 4 * (int)g;
+                    crow[4 * g] = (int16_t)(o.x & 0xffffu);
+                    if (wl > 1) crow[4 * g + 1] = (int16_t)(o.x >> 16);
+                    if (wl > 2) crow[4 * g + 2] = (int16_t)(o.y & 0xffffu);
+                    if (wl > 3) crow[4 * g + 3] = (int16_t)(o.y >> 16);
+                }
+            }
             dpos += tot;
         }
     }
@@ -858,7 +873,9 @@ DEV void walk_slice(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict
         return;
     }
     off += 6;
-    const uint32_t first = s * cfg->pps, n = (s + 1 == cfg->nslices) ? cfg->np - first : cfg->pps;
+    /* the slice's precincts: rows x columns, row after row */
+    const uint32_t first = s * cfg->pps * cfg->ncol,
+                   n = ((s + 1 == cfg->nslices) ? cfg->np - s * cfg->pps : cfg->pps) * cfg->ncol;
     for (uint32_t i = 0; i < n; i++) {
         if (off + cfg->prec_hdr_bytes > size) {
             atomicExch(walk_bad, 1);
@@ -894,7 +911,8 @@ DEV void walk_sequential(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __res
             return;
         }
         off += 6;
-        const uint32_t first = s * cfg->pps, n = (s + 1 == cfg->nslices) ? cfg->np - first : cfg->pps;
+        const uint32_t first = s * cfg->pps * cfg->ncol,
+                       n = ((s + 1 == cfg->nslices) ? cfg->np - s * cfg->pps : cfg->pps) * cfg->ncol;
         for (uint32_t i = 0; i < n; i++) {
             if (off + cfg->prec_hdr_bytes > size) {
                 JXS_STATUS_SET(status, JXS_E_DEC_SHORT);
@@ -934,7 +952,8 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_batch_kernel(const __grid_c
 
 /* Streams with vertical prediction: one block per slice, its precinct rows
  * in order, each predicting from the row above (kept in shared memory after
- * the zero-bit table: cap_groups bytes). */
+ * the zero-bit table: cap_groups bytes); with several precinct columns,
+ * column after column (the precinct above is in the same column). */
 __global__ void __launch_bounds__(UK_THREADS) unpack_vpred_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs,
                                                                   uint32_t bs_size, const uint32_t* __restrict__ prec_off,
                                                                   int16_t* __restrict__ coef, uint32_t cap_bytes,
@@ -943,12 +962,15 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_vpred_kernel(const jxs_cfg_
     __shared__ uint8_t top_t[JXS_MAXBLINES];
     uint8_t* top_gcl = (uint8_t*)(((uintptr_t)(dsm + cap_bytes + 32 + cap_groups) + 15) & ~(uintptr_t)15) + 2 * UK_ZCAP(cap_groups);
     top_gcl = (uint8_t*)(((uintptr_t)top_gcl + 15) & ~(uintptr_t)15);
-    const uint32_t s = blockIdx.x;
+    const uint32_t s = blockIdx.x, ncol = cfg->ncol;
     const uint32_t first = s * cfg->pps, end = min(cfg->np, first + cfg->pps);
-    for (uint32_t p = first; p < end; p++) {
-        unpack_body(cfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status, (int)p, top_gcl, top_t, p != first);
-        __syncthreads();
-        if (*(volatile int*)status) break;
+    for (uint32_t col = 0; col < ncol; col++) {
+        for (uint32_t row = first; row < end; row++) {
+            unpack_body(cfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status, (int)(row * ncol + col), top_gcl, top_t,
+                        row != first);
+            __syncthreads();
+            if (*(volatile int*)status) return;
+        }
     }
 }
 

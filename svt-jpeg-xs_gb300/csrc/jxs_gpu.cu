@@ -478,8 +478,8 @@ static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
     CK(cudaEventCreateWithFlags(&s->done, cudaEventDisableTiming));
     s->bs_cap = c->lcod + 4096;
     CK(cudaMalloc(&s->bs, s->bs_cap + 64));
-    CK(cudaMalloc(&s->prec_off, (size_t)c->np * sizeof(uint32_t)));
-    CK(cudaMallocHost(&s->prec_off_h, (size_t)c->np * sizeof(uint32_t)));
+    CK(cudaMalloc(&s->prec_off, (size_t)c->nprec * sizeof(uint32_t)));
+    CK(cudaMallocHost(&s->prec_off_h, (size_t)c->nprec * sizeof(uint32_t)));
     CK(cudaMallocHost(&s->hdr_h, sizeof(c->hdr)));
     CK(cudaMalloc(&s->coef, c->coef_total * sizeof(int16_t) + 64));
     for (uint32_t k = 0; k < c->nc; k++) {
@@ -620,8 +620,8 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
     if (prec_off) {
         /* the previous use of prec_off_h by this slot has completed: slots are
          * reused only after their completion was observed */
-        if (prec_off != s->prec_off_h) memcpy(s->prec_off_h, prec_off, sizeof(uint32_t) * c->np);
-        CK(cudaMemcpyAsync(s->prec_off, s->prec_off_h, sizeof(uint32_t) * c->np, cudaMemcpyHostToDevice, st));
+        if (prec_off != s->prec_off_h) memcpy(s->prec_off_h, prec_off, sizeof(uint32_t) * c->nprec);
+        CK(cudaMemcpyAsync(s->prec_off, s->prec_off_h, sizeof(uint32_t) * c->nprec, cudaMemcpyHostToDevice, st));
     }
     s->arg_bs = dbs;
     s->arg_size = size;
@@ -635,7 +635,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
     if (d->vpred)
         CK(jxs_launch_unpack_vpred(d->dcfg, dbs, size, s->prec_off, s->coef, c->nslices, d->cap_bytes, d->cap_groups, s->status, st));
     else
-        CK(jxs_launch_unpack(d->dcfg, dbs, size, s->prec_off, s->coef, c->np, d->cap_bytes, d->cap_groups, s->status, st));
+        CK(jxs_launch_unpack(d->dcfg, dbs, size, s->prec_off, s->coef, c->nprec, d->cap_bytes, d->cap_groups, s->status, st));
     KMARK();
     TMARK(2);
 

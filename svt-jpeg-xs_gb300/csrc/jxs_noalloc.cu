@@ -75,7 +75,9 @@ static __device__ uint64_t walk_one_slice(const jxs_cfg_t* cfg, const uint8_t* b
                                           uint32_t* offs) {
     if (!slice_header_at(bs, off, size, s)) return 0;
     off += 6;
-    const uint32_t first = s * cfg->pps, n = (s + 1 == cfg->nslices) ? cfg->np - first : cfg->pps;
+    /* the slice's precincts: rows x columns, row after row */
+    const uint32_t first = s * cfg->pps * cfg->ncol,
+                   n = ((s + 1 == cfg->nslices) ? cfg->np - s * cfg->pps : cfg->pps) * cfg->ncol;
     for (uint32_t i = 0; i < n; i++) {
         if (off + cfg->prec_hdr_bytes > size || first + i >= NOALLOC_MAX_PRECINCTS) return 0;
         const uint32_t lprc = rd24(bs + off);
@@ -139,14 +141,14 @@ extern "C" int32_t jxs_gpu_dec_locate_noalloc(jxs_gpu_dec_t* d, const void* dev_
     if (!c || !dev_bs || !frame_size) return JXS_E_DEC_PTR;
     *frame_size = 0;
     if (!jxs_gpu_is_device_ptr(dev_bs)) return JXS_E_DEC_PTR;
-    if (c->np > NOALLOC_MAX_PRECINCTS) {
+    if (c->nprec > NOALLOC_MAX_PRECINCTS) {
         fprintf(stderr,
                 "svt_jpeg_xs_gpu_decoder_locate_frame: the frame has %u precincts; this entry point holds at most %u\n",
-                c->np, NOALLOC_MAX_PRECINCTS);
+                c->nprec, NOALLOC_MAX_PRECINCTS);
         return JXS_E_BAD_PARAM;
     }
-    if (prec_off && cap < c->np) {
-        fprintf(stderr, "svt_jpeg_xs_gpu_decoder_locate_frame: room for %u precinct offsets, the frame has %u\n", cap, c->np);
+    if (prec_off && cap < c->nprec) {
+        fprintf(stderr, "svt_jpeg_xs_gpu_decoder_locate_frame: room for %u precinct offsets, the frame has %u\n", cap, c->nprec);
         return JXS_E_BAD_PARAM;
     }
     if (size < c->hdr_len) return JXS_E_DEC_SHORT;
@@ -173,7 +175,7 @@ extern "C" int32_t jxs_gpu_dec_locate_noalloc(jxs_gpu_dec_t* d, const void* dev_
         return JXS_E_UNDEFINED;
     if (res[0]) return (int32_t)res[0];
     if (prec_off) {
-        if (cudaMemcpyAsync(prec_off, scratch + NOALLOC_HEAD_WORDS, (size_t)c->np * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+        if (cudaMemcpyAsync(prec_off, scratch + NOALLOC_HEAD_WORDS, (size_t)c->nprec * sizeof(uint32_t), cudaMemcpyDeviceToHost,
                             st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess)
             return JXS_E_UNDEFINED;

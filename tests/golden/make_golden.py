@@ -2,17 +2,19 @@
 SVT-JPEG-XS library built from its own sources (oracle/_ref, see
 oracle/Makefile).  Run in a checkout where the reference is available:
 
-    make -C oracle ref oracle && python tests/golden/make_golden.py [--vpred-only | --proxy-only | --signs-only]
+    make -C oracle ref oracle && python tests/golden/make_golden.py [--vpred-only | --proxy-only | --signs-only | --cw-only]
 
 Writes
   <case>.npz            small seeded inputs, the reference's codestream and
                         the reference decoder's planes for that codestream
   vpred*.npz            the same for the reference encoder's vertical
-                        prediction modes (the product's encoder does not
-                        emit them; its decoder must read them)
+                        prediction modes
   signs*.npz            codestreams with separate sign sub-packets
                         (coding_signs_handling 1 / 2), with inputs and the
                         reference decoder's planes
+  cw*.npz               multi-column precinct codestreams (Cw > 0) from the
+                        oracle's encoder (the reference encoder writes only
+                        Cw = 0) and the reference decoder's planes
   proxy<m>_<case>.npz   the reference decoder's proxy output (m = 1 half,
                         2 quarter resolution) for a small case's codestream
   ref_sample_16x16.npz  the 16x16 4:2:2 codestream of the reference's decoder
@@ -173,9 +175,44 @@ def make_vpred():
         print(name, len(bs), "bytes")
 
 
+# Multi-column precincts (Cw > 0).  The reference encoder always writes
+# Cw = 0 (EncHandle.c:401), so these codestreams come from the oracle's
+# encoder; the reference decoder's planes are the expected output.
+# name: (w, h, depth, fmt, bpp_num, bpp_den, decomp_v, decomp_h, quant, slice_h, significance, rc_mode, seed, signs,
+#        vpred_mode, cw)
+CW_CASES = {
+    "cw1_422_8b": (1200, 16, 8, S.FMT_YUV422, 4, 1, 2, 5, 0, 16, 1, 1, 41, 0, 0, 1),
+    "cw2_444_10b_h3": (300, 40, 10, S.FMT_YUV444, 4, 1, 2, 3, 0, 16, 1, 0, 42, 0, 0, 2),
+    "cw1_420_8b_signs2": (600, 32, 8, S.FMT_YUV420, 4, 1, 2, 3, 0, 16, 1, 1, 43, 2, 0, 1),
+    "cw3_rgb_12b_v1_uniform": (401, 24, 12, S.FMT_PACKED_RGB, 5, 1, 1, 2, 1, 8, 0, 1, 44, 0, 0, 3),
+    "cw1_422_10b_vpred1": (320, 48, 10, S.FMT_YUV422, 3, 1, 2, 3, 0, 48, 1, 1, 45, 0, 1, 1),
+    "cw2_444_8b_vpred2_rc3": (400, 40, 8, S.FMT_YUV444, 5, 1, 1, 4, 0, 40, 1, 3, 46, 1, 2, 2),
+    "cw1_422_8b_v0": (180, 12, 8, S.FMT_YUV422, 4, 1, 0, 3, 0, 4, 1, 2, 47, 0, 0, 1),
+}
+
+
+def make_cw():
+    for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed, sg, vpm, cw) in CW_CASES.items():
+        planes = S.frame(w, h, d, fmt, seed=seed)
+        p = O.make_params(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, significance=sig, rc_mode=rc, signs=sg,
+                          vpred=vpm, cw=cw)
+        err, bs = O.oracle_encode(p, planes)
+        assert err == 0, (name, hex(err))
+        err, dec = O.ref_decode(bs)
+        assert err == 0, (name, hex(err))
+        arrays = {"bs": bs, "params": np.array([w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, sg, vpm, cw], np.uint32)}
+        for i, pl in enumerate(dec):
+            arrays["dec%d" % i] = pl
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+        print(name, len(bs), "bytes")
+
+
 def main():
     if not O.ref_available():
         raise SystemExit("build the reference first: make -C oracle ref")
+    if "--cw-only" in sys.argv:
+        make_cw()
+        return
     if "--vpred-only" in sys.argv:
         make_vpred()
         return
@@ -187,6 +224,7 @@ def main():
         return
     make_vpred()
     make_signs()
+    make_cw()
     for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed) in SMALL_CASES.items():
         planes = S.frame(w, h, d, fmt, seed=seed)
         p = O.make_params(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, significance=sig, rc_mode=rc)

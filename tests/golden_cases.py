@@ -12,7 +12,7 @@ def small_cases():
     out = {}
     for path in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         name = os.path.basename(path)[:-4]
-        if name == "ref_sample_16x16" or name.startswith(("vpred", "proxy", "signs")):
+        if name == "ref_sample_16x16" or name.startswith(("vpred", "proxy", "signs", "cw")):
             continue
         z = np.load(path)
         w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc = [int(x) for x in z["params"]]
@@ -41,6 +41,17 @@ def sign_cases():
         z = np.load(path)
         out[os.path.basename(path)[:-4]] = dict(params=[int(x) for x in z["params"]], bs=z["bs"],
                                                 planes=[z["in%d" % i] for i in range(4) if "in%d" % i in z],
+                                                dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z])
+    return out
+
+
+def cw_cases():
+    """Multi-column precinct codestreams (Cw > 0) made by the oracle's
+    encoder, with the reference decoder's planes."""
+    out = {}
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "cw*.npz"))):
+        z = np.load(path)
+        out[os.path.basename(path)[:-4]] = dict(params=[int(x) for x in z["params"]], bs=z["bs"],
                                                 dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z])
     return out
 

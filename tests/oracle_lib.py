@@ -16,7 +16,8 @@ ORACLE_SO = os.path.join(ORACLE_DIR, "_build", "libjxsoracle.so")
 REF_SO = os.path.join(ORACLE_DIR, "_ref", "libjxsref.so")
 
 _FIELDS = ("width height bit_depth colour_format bpp_num bpp_den decomp_v decomp_h quantization slice_height "
-           "rate_control_mode coding_significance coding_signs_handling coding_vertical_prediction_mode threads_num").split()
+           "rate_control_mode coding_significance coding_signs_handling coding_vertical_prediction_mode threads_num "
+           "precinct_width").split()
 
 
 class EncParams(ctypes.Structure):
@@ -30,9 +31,11 @@ class ImageInfo(ctypes.Structure):
 
 
 def make_params(width, height, depth, fmt, bpp_num, bpp_den=1, decomp_v=2, decomp_h=5, quantization=0, slice_height=16,
-                rc_mode=1, significance=1, threads=1, signs=0, vpred=0):
+                rc_mode=1, significance=1, threads=1, signs=0, vpred=0, cw=0):
+    """cw > 0 (precinct columns) only for the oracle's own test codestreams:
+    the reference encoder always writes Cw = 0."""
     return EncParams(width, height, depth, fmt, bpp_num, bpp_den, decomp_v, decomp_h, quantization, slice_height, rc_mode,
-                     significance, signs, vpred, threads)
+                     significance, signs, vpred, threads, cw)
 
 
 def build_oracle():
@@ -88,8 +91,8 @@ def oracle_encode(params, planes, want_qr=False):
     out = np.zeros(cap, np.uint8)
     sz = ctypes.c_uint32()
     rows = (params.height + (1 << params.decomp_v) - 1) >> params.decomp_v
-    q = np.zeros(rows, np.uint8)
-    r = np.zeros(rows, np.uint8)
+    q = np.zeros(rows * (130 if params.precinct_width else 1), np.uint8)  # per precinct: rows x columns (< 130)
+    r = np.zeros_like(q)
     err = oracle().or_encode(ctypes.byref(params), ptrs, strides, out.ctypes.data_as(ctypes.c_void_p), cap,
                              ctypes.byref(sz), q.ctypes.data_as(ctypes.c_void_p), r.ctypes.data_as(ctypes.c_void_p))
     err &= 0xffffffff
