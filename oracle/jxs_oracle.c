@@ -580,6 +580,7 @@ typedef struct {
     uint8_t* q_out;
     uint8_t* r_out;
     int slice_err;
+    int32_t* rct[MAXC]; /* Cpih = 1: the scaled input after the forward colour transform */
 } enc_t;
 
 /* encoder_init_configuration (Source/Lib/Encoder/Codec/EncHandle.c:128-454). */
@@ -601,6 +602,8 @@ static int enc_configure(enc_t* e, const or_enc_params_t* p) {
     if (c->coding_vertical_prediction_mode >= 3) return E_BAD_PARAM;
     if (c->coding_signs_handling > 2) return E_BAD_PARAM;
     if (c->width < 4) return E_BAD_PARAM;
+    if (c->cpih > 1 || c->tnlt > 2) return E_BAD_PARAM;
+    if (c->cpih && c->colour_format != FMT_YUV444 && c->colour_format != FMT_PACKED_RGB) return E_BAD_PARAM;
     if ((c->colour_format == FMT_YUV422 || c->colour_format == FMT_YUV420) && (c->width % 2)) return E_BAD_PARAM;
     if (c->colour_format == FMT_YUV420 && (c->height % 2)) return E_BAD_PARAM;
     if (c->decomp_v > 2 || c->decomp_h > 5 || c->decomp_h < c->decomp_v) return E_BAD_PARAM;
@@ -662,7 +665,8 @@ static void enc_write_header(enc_t* e) {
     bw_put(&w, 0xff10, 16);                    /* SOC */
     bw_put(&w, 0xff50, 16);                    /* CAP */
     bw_put(&w, DIV_UP(16 + 9, 8), 16);
-    uint8_t cap[9] = {0, 0, 0, 0, (uint8_t)(e->fmt == FMT_YUV420), 0, 0, 0, 1 /* Rl */};
+    uint8_t cap[9] = {0, 0, (uint8_t)(e->prm.tnlt == 1), (uint8_t)(e->prm.tnlt == 2), (uint8_t)(e->fmt == FMT_YUV420), 0, 0, 0,
+                      1 /* Rl */};
     for (int i = 0; i < 9; i++) bw_put(&w, cap[i], 1);
     bw_align(&w);
     bw_put(&w, 0xff12, 16);                    /* PIH */
@@ -679,7 +683,7 @@ static void enc_write_header(enc_t* e) {
     bw_put(&w, 8, 8);                          /* Ss */
     bw_put(&w, BW, 8);
     bw_put(&w, (FQ << 4) | 4, 8);              /* Fq | Br */
-    bw_put(&w, 0, 8);                          /* Fslc | Ppoc | Cpih */
+    bw_put(&w, e->prm.cpih, 8);                /* Fslc | Ppoc | Cpih */
     bw_put(&w, (g->dh << 4) | g->dv, 8);
     bw_put(&w, !g->short_hdr, 1);              /* Lh */
     bw_put(&w, 1, 1);                          /* Rl */
@@ -700,6 +704,22 @@ static void enc_write_header(enc_t* e) {
         band_t* bd = &g->c[g->gcomp[i]].b[g->gband[i]];
         bw_put(&w, bd->gain, 8);
         bw_put(&w, bd->prio, 8);
+    }
+    if (e->prm.tnlt == 1) { /* NLT, quadratic */
+        bw_put(&w, 0xff16, 16);
+        bw_put(&w, 5, 16);
+        bw_put(&w, 1, 8);
+        bw_put(&w, e->prm.nlt_sigma & 1, 1);
+        bw_put(&w, e->prm.nlt_alpha & 0x7fff, 15);
+    } else if (e->prm.tnlt == 2) { /* NLT, extended */
+        bw_put(&w, 0xff16, 16);
+        bw_put(&w, 12, 16);
+        bw_put(&w, 2, 8);
+        bw_put(&w, e->prm.nlt_t1 >> 16, 16);
+        bw_put(&w, e->prm.nlt_t1 & 0xffff, 16);
+        bw_put(&w, e->prm.nlt_t2 >> 16, 16);
+        bw_put(&w, e->prm.nlt_t2 & 0xffff, 16);
+        bw_put(&w, e->prm.nlt_e, 8);
     }
     bw_align(&w);
     e->hdr_len = (uint32_t)(w.bit >> 3);
@@ -742,15 +762,13 @@ typedef struct {
     const uint32_t* strides;
 } dwt_job_t;
 
-static void enc_dwt_one(void* ctx, uint32_t c) {
-    dwt_job_t* j = (dwt_job_t*)ctx;
-    enc_t* e = j->e;
-    comp_t* cp = &e->g.c[c];
-    uint32_t w = cp->w, h = cp->h, d = e->depth;
-    int32_t* a = (int32_t*)malloc(sizeof(int32_t) * (size_t)w * h);
+/* linear_input_scaling_line_{8,16}bit_c (NltEnc.c:33-72) of component c */
+static void enc_scale_input(const enc_t* e, void* const* planes, const uint32_t* strides, uint32_t c, int32_t* a) {
+    const comp_t* cp = &e->g.c[c];
+    const uint32_t w = cp->w, h = cp->h, d = e->depth;
     const int packed = e->fmt == FMT_PACKED_RGB;
-    const void* src = packed ? j->planes[0] : j->planes[c];
-    const uint32_t stride = packed ? j->strides[0] : j->strides[c];
+    const void* src = packed ? planes[0] : planes[c];
+    const uint32_t stride = packed ? strides[0] : strides[c];
     const int32_t off = 1 << (BW - 1);
     const uint32_t sh = BW - d;
     for (uint32_t y = 0; y < h; y++)
@@ -759,6 +777,37 @@ static void enc_dwt_one(void* ctx, uint32_t c) {
             uint32_t s = d <= 8 ? ((const uint8_t*)src)[idx] : (((const uint16_t*)src)[idx] & ((1u << d) - 1));
             a[(size_t)y * w + x] = (int32_t)(s << sh) - off;
         }
+}
+
+/* Forward reversible colour transform (inverse of Mct.c:137-153):
+ * (R, G, B) -> (G + ((B - G + R - G) >> 2), B - G, R - G). */
+static int enc_forward_rct(enc_t* e, void* const* planes, const uint32_t* strides) {
+    const size_t n = (size_t)e->g.c[0].w * e->g.c[0].h;
+    for (uint32_t c = 0; c < 3; c++) {
+        e->rct[c] = (int32_t*)malloc(sizeof(int32_t) * n);
+        if (!e->rct[c]) return E_RESOURCES;
+        enc_scale_input(e, planes, strides, c, e->rct[c]);
+    }
+    for (size_t i = 0; i < n; i++) {
+        const int32_t r = e->rct[0][i], g = e->rct[1][i], b = e->rct[2][i];
+        e->rct[1][i] = b - g;
+        e->rct[2][i] = r - g;
+        e->rct[0][i] = g + ((b - g + r - g) >> 2);
+    }
+    return E_NONE;
+}
+
+static void enc_dwt_one(void* ctx, uint32_t c) {
+    dwt_job_t* j = (dwt_job_t*)ctx;
+    enc_t* e = j->e;
+    comp_t* cp = &e->g.c[c];
+    uint32_t w = cp->w, h = cp->h;
+    int32_t* a = (int32_t*)malloc(sizeof(int32_t) * (size_t)w * h);
+    if (e->rct[c]) {
+        memcpy(a, e->rct[c], sizeof(int32_t) * (size_t)w * h);
+    } else {
+        enc_scale_input(e, j->planes, j->strides, c, a);
+    }
     fwd_component(a, w, h, cp->dv, cp->dh);
     for (uint32_t b = 0; b < cp->nb; b++) {
         band_t* bd = &cp->b[b];
@@ -1549,12 +1598,14 @@ static void enc_slice(void* ctx, uint32_t s) {
 }
 
 static void enc_free(enc_t* e) {
-    for (int c = 0; c < MAXC; c++)
+    for (int c = 0; c < MAXC; c++) {
         for (int b = 0; b < MAXB; b++) {
             free(e->coef[c][b]);
             free(e->gcli[c][b]);
             free(e->sigmax[c][b]);
         }
+        free(e->rct[c]);
+    }
     free(e->slice_sizes);
 }
 
@@ -1592,6 +1643,10 @@ int or_encode(const or_enc_params_t* p, void* const planes[4], const uint32_t st
     r = enc_alloc(&e);
     if (r) { enc_free(&e); return r; }
     uint32_t threads = p->threads_num ? p->threads_num : 1;
+    if (e.prm.cpih == 1) {
+        r = enc_forward_rct(&e, planes, strides);
+        if (r) { enc_free(&e); return r; }
+    }
     dwt_job_t dj = {&e, planes, strides};
     parallel_for(e.g.nc, threads, enc_dwt_one, &dj);
     memcpy(out, e.hdr, e.hdr_len);
@@ -1652,13 +1707,14 @@ static inline void br_align(br_t* r) { r->bit = (r->bit + 7) & ~(uint64_t)7; }
 typedef struct {
     geom_t g;
     uint32_t lcod, depth[MAXC], qpih, fs, rm, bw, fq, lh, rl, nc, cpih, tnlt;
+    uint32_t nlt_sigma, nlt_alpha, nlt_t1, nlt_t2, nlt_e; /* non-linearity parameters (NLT marker) */
     uint32_t hdr_len;
     uint8_t gain[MAXGB], prio[MAXGB];
 } dec_hdr_t;
 
 /* get_header and its marker readers (Source/Lib/Decoder/Codec/ParseHeader.c:
- * 20-617) for the markers this project's and the reference's encoders write;
- * NLT/CWD/CTS/CRG/COM are parsed and, where they change decoding, rejected. */
+ * 20-617).  The Star-Tetrix transform (Cpih = 3, CTS/CRG markers) is
+ * rejected; everything else is parsed. */
 static int dec_parse_header(const uint8_t* bs, uint32_t size, dec_hdr_t* h) {
     memset(h, 0, sizeof(*h));
     br_t r = {bs, size, 0};
@@ -1729,16 +1785,27 @@ static int dec_parse_header(const uint8_t* bs, uint32_t size, dec_hdr_t* h) {
                 h->gain[i] = (uint8_t)br_get(&r, 8);
                 h->prio[i] = (uint8_t)br_get(&r, 8);
             }
-        } else if (m == 0xff16) { /* NLT */
+        } else if (m == 0xff16) { /* NLT, get_nonlinearity (ParseHeader.c:373-405) */
             if (!br_enough(&r, 3)) return E_DEC_SHORT;
             br_get(&r, 16);
             h->tnlt = br_get(&r, 8);
-            return E_DEC_BITSTREAM; /* non-linear output is outside this restatement */
+            if (h->tnlt == 1) {
+                if (!br_enough(&r, 2)) return E_DEC_SHORT;
+                h->nlt_sigma = br_get(&r, 1);
+                h->nlt_alpha = br_get(&r, 15);
+            } else if (h->tnlt == 2) {
+                if (!br_enough(&r, 9)) return E_DEC_SHORT;
+                h->nlt_t1 = br_get(&r, 32);
+                h->nlt_t2 = br_get(&r, 32);
+                h->nlt_e = br_get(&r, 8);
+            } else {
+                return E_DEC_BITSTREAM;
+            }
         } else if (m == 0xff17) { /* CWD */
             if (!br_enough(&r, 3)) return E_DEC_SHORT;
             if (br_get(&r, 16) != 3) return E_DEC_BITSTREAM;
             sd = br_get(&r, 8);
-        } else if (m == 0xff18 || m == 0xff19) { /* CTS / CRG: colour transforms are outside this restatement */
+        } else if (m == 0xff18 || m == 0xff19) { /* CTS / CRG: the Star-Tetrix transform is outside this restatement */
             return E_DEC_BITSTREAM;
         } else if (m == 0xff15) { /* COM */
             if (!br_enough(&r, 4)) return E_DEC_SHORT;
@@ -1755,7 +1822,10 @@ static int dec_parse_header(const uint8_t* bs, uint32_t size, dec_hdr_t* h) {
         }
     }
     if (!have_cdt || !have_wgt) return E_DEC_BITSTREAM;
-    if (h->cpih) return E_DEC_BITSTREAM;
+    if (h->cpih == 3) return E_DEC_BITSTREAM; /* Star-Tetrix: outside this restatement */
+    if (h->cpih) /* the colour transform needs equal sampling (ParseHeader.c:584-594) */
+        for (uint32_t c = 1; c < nc; c++)
+            if (sx[c] != sx[0] || sy[c] != sy[0]) return E_DEC_BITSTREAM;
     int e = geom_compute(&h->g, 0, nc, W, H, dh, dv, sd, sx, sy, hsl * (1u << dv), cw);
     if (e) return e;
     /* copy_weights_table, Decoder.c:35-50 */
@@ -1807,6 +1877,7 @@ int or_probe(const uint8_t* bs, uint32_t size, or_image_info_t* info) {
 
 typedef struct {
     dec_hdr_t* h;
+    int32_t* mct[MAXC]; /* Cpih != 0: each component after the inverse transform */
     const uint8_t* bs;
     uint32_t size;
     uint32_t* slice_off;
@@ -2105,6 +2176,72 @@ typedef struct {
     const uint32_t* strides;
 } idwt_job_t;
 
+static inline int32_t clamp_i64(int64_t v, int32_t m) { return (int32_t)(v > m ? m : v < 0 ? 0 : v); }
+
+/* Output scaling of one sample of the inverse transform by the NLT
+ * marker's non-linearity (nlt_inverse_transform_line_*, NltDec.c:22-194,
+ * 366-406): linear, quadratic (Tnlt = 1) or extended (Tnlt = 2), with the
+ * first component's depth. */
+static int32_t nlt_sample(const dec_hdr_t* h, int64_t v) {
+    const int32_t bw = (int32_t)h->bw, depth = (int32_t)h->depth[0], m = (1 << depth) - 1, clampv = (1 << bw) - 1;
+    v += ((int64_t)1 << bw) >> 1;
+    if (h->tnlt == 1) {
+        const int32_t zeta = 2 * bw - depth;
+        const int32_t dco = (int32_t)h->nlt_alpha - (int32_t)h->nlt_sigma * (1 << 15);
+        const int64_t q = (int64_t)clamp_i64(v, clampv);
+        const int64_t v2 = (q * q + (((int64_t)1 << zeta) >> 1)) >> zeta;
+        return clamp_i64(v2 + dco, m);
+    }
+    if (h->tnlt == 2) {
+        const int32_t zeta = 2 * bw - depth;
+        const int32_t t1 = (int32_t)h->nlt_t1, t2 = (int32_t)h->nlt_t2, e = (int32_t)h->nlt_e;
+        const int32_t b1 = (int32_t)((int64_t)t1 + (1 << (bw - e - 1)));
+        const int64_t b2 = (int64_t)t1 * t1, b3 = (int64_t)t2 - ((int64_t)1 << (bw - e - 1));
+        const int64_t a1 = b2 + (int64_t)t1 * ((int64_t)1 << (bw - e)) + ((int64_t)1 << (2 * bw - 2 - 2 * e));
+        const int64_t a3 = b2 + (int64_t)t2 * ((int64_t)1 << (bw - e)) - ((int64_t)1 << (2 * bw - 2 - 2 * e));
+        if (v < t1) {
+            const int64_t q = clamp_i64((int64_t)b1 - v, clampv);
+            v = a1 - q * q;
+        } else if (v < t2) {
+            v = v * ((int64_t)1 << (bw - e)) + b2;
+        } else {
+            const int64_t q = clamp_i64(v - b3, clampv);
+            v = a3 + q * q;
+        }
+        return clamp_i64((v + (((int64_t)1 << zeta) >> 1)) >> zeta, m);
+    }
+    const int32_t zeta = bw - depth;
+    return clamp_i64((v + (((int64_t)1 << zeta) >> 1)) >> zeta, m);
+}
+
+/* With a colour transform (Cpih = 1): the inverse reversible colour
+ * transform of components 0-2 (inverse_rct, Mct.c:137-153) of the whole
+ * frame, then every component's output scaling (svt_jpeg_xs_decode_final,
+ * Decoder.c:707-798). */
+static void dec_mct_nlt(dec_t* d, void* const planes[4], const uint32_t strides[4]) {
+    const dec_hdr_t* h = d->h;
+    const geom_t* g = &h->g;
+    const uint32_t w = g->c[0].w, ht = g->c[0].h;
+    const size_t n = (size_t)w * ht;
+    if (h->cpih == 1) {
+        int32_t *c0 = d->mct[0], *c1 = d->mct[1], *c2 = d->mct[2];
+        for (size_t i = 0; i < n; i++) {
+            const int32_t i0 = c0[i], i1 = c1[i], i2 = c2[i];
+            const int32_t o1 = i0 - ((i1 + i2) >> 2);
+            c0[i] = o1 + i2;
+            c1[i] = o1;
+            c2[i] = o1 + i1;
+        }
+    }
+    for (uint32_t c = 0; c < g->nc; c++)
+        for (uint32_t y = 0; y < ht; y++)
+            for (uint32_t x = 0; x < w; x++) {
+                const int32_t o = nlt_sample(h, d->mct[c][(size_t)y * w + x]);
+                if (h->depth[0] <= 8) ((uint8_t*)planes[c])[(size_t)y * strides[c] + x] = (uint8_t)o;
+                else ((uint16_t*)planes[c])[(size_t)y * strides[c] + x] = (uint16_t)o;
+            }
+}
+
 /* Inverse transform of one component (coefficients << Fq, DwtDecoder.c:
  * 322-406) and linear output scaling (linear_output_scaling_*_line_c,
  * NltDec.c:242-264). */
@@ -2122,15 +2259,16 @@ static void dec_idwt_one(void* ctx, uint32_t c) {
                 a[(size_t)(bd->y + y) * w + bd->x + x] = (int32_t)((uint32_t)(int32_t)d->coef[c][b][(size_t)y * bd->w + x] << d->h->fq);
     }
     inv_component(a, w, h, cp->dv, cp->dh);
+    if (d->h->cpih) {
+        /* kept for the colour transform and the output non-linearity
+         * (svt_jpeg_xs_decode_final, Decoder.c:707-798) */
+        d->mct[c] = a;
+        return;
+    }
     const uint32_t depth = d->h->depth[0];
-    const int32_t zeta = (int32_t)d->h->bw - (int32_t)depth;
-    const int32_t m = (1 << depth) - 1;
     for (uint32_t y = 0; y < h; y++)
         for (uint32_t x = 0; x < w; x++) {
-            int64_t v = a[(size_t)y * w + x];
-            v += (1 << d->h->bw) >> 1;
-            v = (v + ((1ll << zeta) >> 1)) >> zeta;
-            int32_t o = (int32_t)(v > m ? m : v < 0 ? 0 : v);
+            const int32_t o = nlt_sample(d->h, a[(size_t)y * w + x]);
             if (depth == 8) ((uint8_t*)j->planes[c])[(size_t)y * j->strides[c] + x] = (uint8_t)o;
             else ((uint16_t*)j->planes[c])[(size_t)y * j->strides[c] + x] = (uint16_t)o;
         }
@@ -2178,7 +2316,9 @@ int or_decode(const uint8_t* bs, uint32_t size, void* const planes[4], const uin
     if (!d.err) {
         idwt_job_t j = {&d, planes, strides};
         parallel_for(g->nc, threads, dec_idwt_one, &j);
+        if (h.cpih) dec_mct_nlt(&d, planes, strides);
     }
+    for (uint32_t c = 0; c < g->nc; c++) free(d.mct[c]);
     for (uint32_t c = 0; c < g->nc; c++)
         for (uint32_t b = 0; b < g->c[c].nb; b++) free(d.coef[c][b]);
     free(d.slice_off);

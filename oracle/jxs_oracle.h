@@ -23,6 +23,11 @@ typedef struct or_enc_params {
     uint32_t threads_num;
     uint32_t precinct_width; /* Cw: 0 (the reference encoder's only value), or > 0 for
                                 multi-column test codestreams */
+    /* decoder test codestreams only (the reference encoder writes neither):
+     * Cpih = 1 applies the reversible colour transform before the wavelet
+     * transform; tnlt 1 / 2 writes an NLT marker (quadratic / extended
+     * output non-linearity) with the given parameters */
+    uint32_t cpih, tnlt, nlt_sigma, nlt_alpha, nlt_t1, nlt_t2, nlt_e;
 } or_enc_params_t;
 
 typedef struct or_image_info {

@@ -1149,6 +1149,8 @@ extern "C" int32_t jxs_gpu_batch_decode(jxs_gpu_batch_t* b, jxs_gpu_dec_t* const
         uint32_t cb = 0, cg = 0;
         const jxs_cfg_t* c = jxs_gpu_dec_info(dec[i], &dcfg, &cb, &cg);
         if (!c || !bs[i]) return JXS_E_DEC_PTR;
+        /* colour transforms and non-linear outputs decode per frame only */
+        if (dec_needs_nlt_pass(c)) return JXS_E_BAD_PARAM;
         const uint64_t serial = jxs_gpu_dec_serial(dec[i]);
         const int32_t er = ensure_dec(b, i, dec[i], st);
         if (er != JXS_OK) {

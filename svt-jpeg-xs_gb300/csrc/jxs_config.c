@@ -651,6 +651,8 @@ int32_t jxs_cfg_decoder(jxs_cfg_t* g, const uint8_t* bs, size_t size, jxs_hdr_in
     if ((v >> 7) != 0 || ((v >> 4) & 7) != 0) return JXS_E_DEC_BITSTREAM;
     info->cpih = v & 15;
     if (info->cpih != 0 && info->cpih != 1 && info->cpih != 3) return JXS_E_DEC_BITSTREAM;
+    /* the Star-Tetrix transform (Cpih = 3) is not part of this implementation */
+    if (info->cpih == 3) return JXS_E_DEC_BITSTREAM;
     v = hr_u8(&r);
     uint32_t dh = v >> 4, dv = v & 15;
     v = hr_u8(&r);
@@ -693,18 +695,31 @@ int32_t jxs_cfg_decoder(jxs_cfg_t* g, const uint8_t* bs, size_t size, jxs_hdr_in
                 prio[i] = (uint8_t)hr_u8(&r);
             }
         } else if (m == 0xff16) {
+            /* NLT: quadratic (sigma, alpha) or extended (T1, T2, E) output
+             * non-linearity (get_nonlinearity, ParseHeader.c:373-405) */
             if (!hr_has(&r, 3)) return JXS_E_DEC_SHORT;
             hr_u16(&r);
             info->tnlt = hr_u8(&r);
-            /* Quadratic and extended output non-linearities are not part of
-             * this implementation. */
-            return JXS_E_DEC_BITSTREAM;
+            if (info->tnlt == 1) {
+                if (!hr_has(&r, 2)) return JXS_E_DEC_SHORT;
+                const uint32_t q = hr_u16(&r);
+                g->nlt_sigma = q >> 15;
+                g->nlt_alpha = q & 0x7fff;
+            } else if (info->tnlt == 2) {
+                if (!hr_has(&r, 9)) return JXS_E_DEC_SHORT;
+                g->nlt_t1 = hr_u32(&r);
+                g->nlt_t2 = hr_u32(&r);
+                g->nlt_e = hr_u8(&r);
+            } else {
+                return JXS_E_DEC_BITSTREAM;
+            }
+            g->tnlt = info->tnlt;
         } else if (m == 0xff17) {
             if (!hr_has(&r, 3)) return JXS_E_DEC_SHORT;
             if (hr_u16(&r) != 3) return JXS_E_DEC_BITSTREAM;
             sd = hr_u8(&r);
         } else if (m == 0xff18 || m == 0xff19) {
-            return JXS_E_DEC_BITSTREAM; /* colour transforms are not part of this implementation */
+            return JXS_E_DEC_BITSTREAM; /* CTS / CRG: only with the Star-Tetrix transform, not part of this implementation */
         } else if (m == 0xff15) {
             if (!hr_has(&r, 4)) return JXS_E_DEC_SHORT;
             uint32_t len = hr_u16(&r);
@@ -720,7 +735,14 @@ int32_t jxs_cfg_decoder(jxs_cfg_t* g, const uint8_t* bs, size_t size, jxs_hdr_in
         }
     }
     if (!have_cdt || !have_wgt) return JXS_E_DEC_BITSTREAM;
-    if (info->cpih) return JXS_E_DEC_BITSTREAM;
+    if (info->cpih) {
+        /* the colour transform needs three components of equal sampling
+         * (ParseHeader.c:584-594, Mct.c:137-153) */
+        if (nc < 3) return JXS_E_DEC_BITSTREAM;
+        for (uint32_t c = 1; c < nc; c++)
+            if (sx[c] != sx[0] || sy[c] != sy[0]) return JXS_E_DEC_BITSTREAM;
+    }
+    g->cpih = info->cpih;
     if (dv > 31) return JXS_E_DEC_BITSTREAM;
     int32_t e = jxs_cfg_geometry(g, 0, nc, W, H, dh, dv, sd, sx, sy, hsl * (1u << dv), cw);
     if (e) return e;

@@ -128,6 +128,10 @@ typedef struct jxs_cfg {
     jxs_seg_t seg[4][JXS_MAXSEG];
     uint32_t max_slice_budget;           /* 0 when slice starts cannot be predicted (decoder) */
     uint32_t proxy;                      /* decoder: output at 1/2^proxy resolution (proxy modes, Pi.c:567-626) */
+    /* decoder: colour transform Cpih (0 none, 1 reversible RCT) and the NLT
+     * marker's output non-linearity (0 linear, 1 quadratic, 2 extended) */
+    uint32_t cpih, tnlt, nlt_sigma, nlt_alpha, nlt_e;
+    uint32_t nlt_t1, nlt_t2;
     uint32_t slice_size[8192];           /* bytes of each slice incl. its header (last: incl. EOC) */
     uint32_t slice_begin[8192];          /* byte offset of each slice in the codestream */
 } jxs_cfg_t;

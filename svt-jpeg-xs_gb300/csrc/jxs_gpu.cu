@@ -428,6 +428,9 @@ struct DecSlot {
     int ll_pitch[2][JXS_MAXC];
     uint8_t* out_stage;
     uint64_t out_off[JXS_MAXC];
+    int32_t* mct;               /* colour transform / non-linear output: the int32 planes of the last inverse level */
+    uint64_t mct_off[JXS_MAXC];
+    int mct_pitch[JXS_MAXC];
     int* status;
     int* status_h;
     uint32_t* prec_off_h;
@@ -497,6 +500,15 @@ static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
         ob += ((uint64_t)jxs_out_w(c, k) * jxs_out_h(c, k) * bps + 255) & ~255ull;
     }
     CK(cudaMalloc(&s->out_stage, ob));
+    if (dec_needs_nlt_pass(c)) {
+        uint64_t mb = 0;
+        for (uint32_t k = 0; k < c->nc; k++) {
+            s->mct_off[k] = mb;
+            s->mct_pitch[k] = (int)((jxs_out_w(c, k) + 3) & ~3u);
+            mb += ((uint64_t)s->mct_pitch[k] * jxs_out_h(c, k) + 63) & ~63ull;
+        }
+        CK(cudaMalloc(&s->mct, mb * sizeof(int32_t)));
+    }
     CK(cudaMalloc(&s->status, 64));
     CK(cudaMallocHost(&s->status_h, 64));
     *s->status_h = 0;
@@ -515,6 +527,7 @@ static void dec_slot_free(DecSlot* s) {
     for (int v = 0; v < 2; v++)
         for (int k = 0; k < JXS_MAXC; k++) cudaFree(s->ll[v][k]);
     cudaFree(s->out_stage);
+    cudaFree(s->mct);
     cudaFree(s->status);
     if (s->status_h) cudaFreeHost(s->status_h);
     for (int i = 0; i < 5; i++)
@@ -660,11 +673,20 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
             out.pitch[k] = jxs_out_w(c, k);
         }
     }
-    const int sample_kind = dec_sample_kind(c);
+    /* a colour transform or a non-linear output: the last inverse level
+     * writes int32 planes, nlt_out_kernel writes the samples */
+    const int nlt_pass = dec_needs_nlt_pass(c);
+    FramePlanes lout = out;
+    if (nlt_pass)
+        for (uint32_t k = 0; k < c->nc; k++) {
+            lout.p[k] = s->mct + s->mct_off[k];
+            lout.pitch[k] = s->mct_pitch[k];
+        }
+    const int sample_kind = nlt_pass ? 0 : dec_sample_kind(c);
     for (int pass = 0; pass < 2; pass++) {
         InvHLaunch L;
         memset(&L, 0, sizeof(L));
-        L.njobs = plan_inv_h(c, d->dcfg, fb, out, pass, L.job);
+        L.njobs = plan_inv_h(c, d->dcfg, fb, lout, pass, L.job);
         if (!L.njobs) continue;
         const int blocks = inv_h_layout(L, jxs_inv_h_max_rows_per_block());
         if (blocks < 0) return JXS_E_BAD_PARAM;
@@ -675,7 +697,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         InvVLaunch L;
         memset(&L, 0, sizeof(L));
         int tiles[JXS_MAXC], blocks = 0;
-        L.njobs = plan_inv_v(c, d->dcfg, fb, out, v, L.job, tiles);
+        L.njobs = plan_inv_v(c, d->dcfg, fb, lout, v, L.job, tiles);
         for (int i = 0; i < L.njobs; i++) {
             L.job[i].first_block = blocks;
             blocks += tiles[i];
@@ -683,6 +705,11 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         if (!L.njobs) continue;
         CK(jxs_launch_inv_v(&L, v > (int)c->proxy ? 0 : sample_kind, blocks, st));
         KMARK();
+    }
+    if (nlt_pass) {
+        NltOut P;
+        nlt_out_params(c, lout, out, &P);
+        CK(jxs_launch_nlt_out(&P, st));
     }
     TMARK(3);
     for (uint32_t k = 0; k < c->nc; k++) {

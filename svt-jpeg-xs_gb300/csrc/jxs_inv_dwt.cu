@@ -384,3 +384,72 @@ extern "C" cudaError_t jxs_launch_inv_h_batch(const InvHLaunchB* L, int out_kind
     if (out_kind == 1) return launch_ih<1, JXS_BATCH_JOBS>(L, nblocks, st);
     return launch_ih<2, JXS_BATCH_JOBS>(L, nblocks, st);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Colour transform and output non-linearity                                 */
+/* ------------------------------------------------------------------------ */
+/* Streams with a colour transform (Cpih = 1) or an NLT marker: the last
+ * inverse level writes int32 planes, and this kernel turns them into
+ * samples.  Cpih = 1: the inverse reversible colour transform of
+ * components 0-2 (inverse_rct, Mct.c:137-153); then every component's
+ * output scaling (nlt_inverse_transform_line_*, NltDec.c:22-194, 366-406):
+ * linear, quadratic (Tnlt = 1) or extended (Tnlt = 2), with the first
+ * component's depth.  One thread per sample column x, rows over grid.y. */
+DEV int32_t nlt_clamp64(int64_t v, int32_t m) { return (int32_t)(v > m ? m : v < 0 ? 0 : v); }
+
+DEV int32_t nlt_sample(const NltOut& P, int64_t v) {
+    const int32_t bw = P.bw, depth = P.depth, m = (1 << depth) - 1, clampv = (1 << bw) - 1;
+    v += ((int64_t)1 << bw) >> 1;
+    if (P.tnlt == 1) {
+        const int32_t zeta = 2 * bw - depth;
+        const int64_t q = (int64_t)nlt_clamp64(v, clampv);
+        return nlt_clamp64(((q * q + (((int64_t)1 << zeta) >> 1)) >> zeta) + P.dco, m);
+    }
+    if (P.tnlt == 2) {
+        const int32_t zeta = 2 * bw - depth;
+        if (v < P.t1) {
+            const int64_t q = nlt_clamp64((int64_t)P.b1 - v, clampv);
+            v = P.a1 - q * q;
+        } else if (v < P.t2) {
+            v = v * ((int64_t)1 << (bw - P.e)) + P.b2;
+        } else {
+            const int64_t q = nlt_clamp64(v - P.b3, clampv);
+            v = P.a3 + q * q;
+        }
+        return nlt_clamp64((v + (((int64_t)1 << zeta) >> 1)) >> zeta, m);
+    }
+    const int32_t zeta = bw - depth;
+    return nlt_clamp64((v + (((int64_t)1 << zeta) >> 1)) >> zeta, m);
+}
+
+__global__ void __launch_bounds__(256) nlt_out_kernel(const __grid_constant__ NltOut P) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    int32_t v[JXS_MAXC];
+#pragma unroll
+    for (int k = 0; k < JXS_MAXC; k++)
+        v[k] = (k < P.nc && x < P.w[k] && y < P.h[k]) ? P.in[k][(size_t)y * P.in_pitch[k] + x] : 0;
+    if (P.cpih == 1 && x < P.w[0] && y < P.h[0]) {
+        const int32_t o1 = v[0] - ((v[1] + v[2]) >> 2);
+        const int32_t o0 = o1 + v[2], o2 = o1 + v[1];
+        v[0] = o0;
+        v[1] = o1;
+        v[2] = o2;
+    }
+#pragma unroll
+    for (int k = 0; k < JXS_MAXC; k++) {
+        if (k >= P.nc || x >= P.w[k] || y >= P.h[k]) continue;
+        const int32_t o = nlt_sample(P, v[k]);
+        if (P.bps == 1) ((uint8_t*)P.out[k])[(size_t)y * P.out_pitch[k] + x] = (uint8_t)o;
+        else ((uint16_t*)P.out[k])[(size_t)y * P.out_pitch[k] + x] = (uint16_t)o;
+    }
+}
+
+extern "C" cudaError_t jxs_launch_nlt_out(const NltOut* P, cudaStream_t st) {
+    int wmax = 1, hmax = 1;
+    for (int k = 0; k < P->nc; k++) {
+        wmax = max(wmax, P->w[k]);
+        hmax = max(hmax, P->h[k]);
+    }
+    nlt_out_kernel<<<dim3((unsigned)((wmax + 255) / 256), (unsigned)hmax), 256, 0, st>>>(*P);
+    return cudaGetLastError();
+}

@@ -162,6 +162,21 @@ __device__ __forceinline__ int find_job(const JOB* job, int njobs, int b) {
     return lo;
 }
 
+/* The colour transform and output non-linearity of a decoded frame
+ * (nlt_out_kernel): int32 planes in, samples out. */
+struct NltOut {
+    const int32_t* in[JXS_MAXC];
+    long long in_pitch[JXS_MAXC];  /* elements */
+    void* out[JXS_MAXC];
+    long long out_pitch[JXS_MAXC]; /* samples */
+    int w[JXS_MAXC], h[JXS_MAXC];
+    int nc, cpih, tnlt, bw, depth, bps;
+    /* quadratic: dco = alpha - sigma 2^15; extended: thresholds and the
+     * constants of NltDec.c:111-116 */
+    int32_t dco, t1, t2, e, b1;
+    int64_t b2, b3, a1, a3;
+};
+
 /* Encoder rate-control outputs per precinct row. */
 struct PrecRC {
     uint32_t total_bytes;  /* bytes written for the precinct (header to last data byte, incl. trailing padding) */

@@ -46,6 +46,7 @@ extern "C" cudaError_t jxs_launch_inv_v(const InvVLaunch* L, int out_kind, int n
 extern "C" cudaError_t jxs_launch_inv_v_batch(const InvVLaunchB* L, int out_kind, int nblocks, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_inv_h(const InvHLaunch* L, int out_kind, int nblocks, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_inv_h_batch(const InvHLaunchB* L, int out_kind, int nblocks, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_nlt_out(const NltOut* P, cudaStream_t st);
 extern "C" int jxs_inv_v_tile_rows(void);
 extern "C" int jxs_inv_v_tile_cols(void);
 extern "C" int jxs_inv_h_max_rows_per_block(void);
@@ -133,6 +134,43 @@ struct FramePlanes {
     void* p[JXS_MAXC];
     long long pitch[JXS_MAXC];     /* elements */
 };
+
+/* Decoded frames whose last inverse level writes int32 planes for
+ * nlt_out_kernel: a colour transform or a non-linear output. */
+static inline int dec_needs_nlt_pass(const jxs_cfg_t* c) { return c->cpih != 0 || c->tnlt != 0; }
+
+/* The parameters of nlt_out_kernel for a frame: int32 planes `in` (pitch
+ * in elements) to the output planes `out` (NltDec.c:111-116 for the
+ * extended constants). */
+static inline void nlt_out_params(const jxs_cfg_t* c, const FramePlanes& in, const FramePlanes& out, NltOut* P) {
+    memset(P, 0, sizeof(*P));
+    P->nc = (int)c->nc;
+    for (uint32_t k = 0; k < c->nc; k++) {
+        P->in[k] = (const int32_t*)in.p[k];
+        P->in_pitch[k] = in.pitch[k];
+        P->out[k] = out.p[k];
+        P->out_pitch[k] = out.pitch[k];
+        P->w[k] = (int)jxs_out_w(c, k);
+        P->h[k] = (int)jxs_out_h(c, k);
+    }
+    P->cpih = (int)c->cpih;
+    P->tnlt = (int)c->tnlt;
+    P->bw = (int)c->bw;
+    P->depth = (int)c->depth;
+    P->bps = (int)bytes_per_sample(c);
+    P->dco = (int32_t)c->nlt_alpha - (int32_t)c->nlt_sigma * (1 << 15);
+    const int32_t bw = (int32_t)c->bw, e = (int32_t)c->nlt_e;
+    P->t1 = (int32_t)c->nlt_t1;
+    P->t2 = (int32_t)c->nlt_t2;
+    P->e = e;
+    if (c->tnlt == 2) {
+        P->b1 = (int32_t)((int64_t)P->t1 + (1 << (bw - e - 1)));
+        P->b2 = (int64_t)P->t1 * P->t1;
+        P->b3 = (int64_t)P->t2 - ((int64_t)1 << (bw - e - 1));
+        P->a1 = P->b2 + (int64_t)P->t1 * ((int64_t)1 << (bw - e)) + ((int64_t)1 << (2 * bw - 2 - 2 * e));
+        P->a3 = P->b2 + (int64_t)P->t2 * ((int64_t)1 << (bw - e)) - ((int64_t)1 << (2 * bw - 2 - 2 * e));
+    }
+}
 
 /* Bytes of the int32 low bands of one frame, and their pitches. */
 static inline uint64_t ll_layout(const jxs_cfg_t* c, int pitch[2][JXS_MAXC], uint64_t size[2][JXS_MAXC]) {

@@ -2,7 +2,8 @@
 SVT-JPEG-XS library built from its own sources (oracle/_ref, see
 oracle/Makefile).  Run in a checkout where the reference is available:
 
-    make -C oracle ref oracle && python tests/golden/make_golden.py [--vpred-only | --proxy-only | --signs-only | --cw-only]
+    make -C oracle ref oracle && python tests/golden/make_golden.py [--vpred-only | --proxy-only | --signs-only | --cw-only |
+                                                           --mct-only]
 
 Writes
   <case>.npz            small seeded inputs, the reference's codestream and
@@ -15,6 +16,9 @@ Writes
   cw*.npz               multi-column precinct codestreams (Cw > 0) from the
                         oracle's encoder (the reference encoder writes only
                         Cw = 0) and the reference decoder's planes
+  mct*.npz, nlt*.npz    colour transform (Cpih = 1) and output non-linearity
+                        codestreams from the oracle's encoder, with the
+                        reference decoder's planes (full and half resolution)
   proxy<m>_<case>.npz   the reference decoder's proxy output (m = 1 half,
                         2 quarter resolution) for a small case's codestream
   ref_sample_16x16.npz  the 16x16 4:2:2 codestream of the reference's decoder
@@ -207,11 +211,50 @@ def make_cw():
         print(name, len(bs), "bytes")
 
 
+# Colour transform (Cpih = 1, reversible RCT) and output non-linearities
+# (NLT marker: Tnlt 1 quadratic, 2 extended).  The reference encoder writes
+# none of them, so the oracle's encoder writes these codestreams (the RCT
+# applied forward; the NLT marker only changes the decoder's output
+# scaling); the reference decoder's planes, full and at proxy 1, are the
+# expected output.
+# name: (w, h, depth, fmt, bpp_num, decomp_v, decomp_h, quant, slice_h, seed, cpih, tnlt, sigma, alpha, t1, t2, e)
+MCT_CASES = {
+    "mct_rct_444_8b": (96, 32, 8, S.FMT_YUV444, 6, 2, 5, 0, 16, 51, 1, 0, 0, 0, 0, 0, 0),
+    "mct_rct_rgb_10b_quadratic": (120, 24, 10, S.FMT_PACKED_RGB, 8, 1, 3, 1, 8, 52, 1, 1, 1, 1234, 0, 0, 0),
+    "mct_rct_444_12b_extended": (72, 40, 12, S.FMT_YUV444, 5, 2, 2, 0, 16, 53, 1, 2, 0, 0, 300000, 560000, 3),
+    "nlt_quadratic_422_8b": (128, 32, 8, S.FMT_YUV422, 5, 2, 5, 0, 16, 54, 0, 1, 0, 777, 0, 0, 0),
+    "nlt_extended_420_10b": (96, 32, 10, S.FMT_YUV420, 4, 2, 4, 0, 32, 55, 0, 2, 0, 0, 150000, 700000, 2),
+}
+
+
+def make_mct():
+    for name, (w, h, d, fmt, bn, v, hh, q, sl, seed, cpih, tnlt, sg, al, t1, t2, e) in MCT_CASES.items():
+        planes = S.frame(w, h, d, fmt, seed=seed)
+        p = O.make_params(w, h, d, fmt, bn, 1, v, hh, quantization=q, slice_height=sl)
+        p.cpih, p.tnlt, p.nlt_sigma, p.nlt_alpha, p.nlt_t1, p.nlt_t2, p.nlt_e = cpih, tnlt, sg, al, t1, t2, e
+        err, bs = O.oracle_encode(p, planes)
+        assert err == 0, (name, hex(err))
+        err, dec = O.ref_decode(bs)
+        assert err == 0, (name, hex(err))
+        err, dec1 = O.ref_decode_proxy(bs, 1)
+        assert err == 0, (name, hex(err))
+        arrays = {"bs": bs, "params": np.array([w, h, d, fmt, bn, v, hh, q, sl, seed, cpih, tnlt, sg, al, t1, t2, e], np.uint32)}
+        for i, pl in enumerate(dec):
+            arrays["dec%d" % i] = pl
+        for i, pl in enumerate(dec1):
+            arrays["proxy%d" % i] = pl
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+        print(name, len(bs), "bytes")
+
+
 def main():
     if not O.ref_available():
         raise SystemExit("build the reference first: make -C oracle ref")
     if "--cw-only" in sys.argv:
         make_cw()
+        return
+    if "--mct-only" in sys.argv:
+        make_mct()
         return
     if "--vpred-only" in sys.argv:
         make_vpred()
@@ -225,6 +268,7 @@ def main():
     make_vpred()
     make_signs()
     make_cw()
+    make_mct()
     for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed) in SMALL_CASES.items():
         planes = S.frame(w, h, d, fmt, seed=seed)
         p = O.make_params(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, significance=sig, rc_mode=rc)

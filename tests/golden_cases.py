@@ -12,7 +12,7 @@ def small_cases():
     out = {}
     for path in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         name = os.path.basename(path)[:-4]
-        if name == "ref_sample_16x16" or name.startswith(("vpred", "proxy", "signs", "cw")):
+        if name == "ref_sample_16x16" or name.startswith(("vpred", "proxy", "signs", "cw", "mct", "nlt")):
             continue
         z = np.load(path)
         w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc = [int(x) for x in z["params"]]
@@ -53,6 +53,19 @@ def cw_cases():
         z = np.load(path)
         out[os.path.basename(path)[:-4]] = dict(params=[int(x) for x in z["params"]], bs=z["bs"],
                                                 dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z])
+    return out
+
+
+def mct_cases():
+    """Colour transform (Cpih = 1) and output non-linearity codestreams made
+    by the oracle's encoder, with the reference decoder's planes at full
+    and half resolution."""
+    out = {}
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "mct*.npz")) + glob.glob(os.path.join(GOLDEN, "nlt*.npz"))):
+        z = np.load(path)
+        out[os.path.basename(path)[:-4]] = dict(params=[int(x) for x in z["params"]], bs=z["bs"],
+                                                dec=[z["dec%d" % i] for i in range(4) if "dec%d" % i in z],
+                                                proxy=[z["proxy%d" % i] for i in range(4) if "proxy%d" % i in z])
     return out
 
 

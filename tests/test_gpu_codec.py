@@ -642,3 +642,61 @@ def test_multi_column_against_oracle(gpu, oracle, seed):
     got = dec.decode(bs)
     dec.close()
     assert all(np.array_equal(a, b) for a, b in zip(got, want))
+
+
+@pytest.mark.parametrize("name", sorted(G.mct_cases()))
+def test_colour_transform_and_nlt_golden_decode(gpu, name):
+    """Cpih = 1 (reversible colour transform) and NLT markers (quadratic,
+    extended; oracle-made codestreams, which the reference encoder cannot
+    write): decoded bit-exact with the reference decoder, at full and half
+    resolution."""
+    c = G.mct_cases()[name]
+    dec = gpu.Decoder(c["bs"])
+    out = dec.decode(c["bs"])
+    dec.close()
+    assert all(np.array_equal(a, b) for a, b in zip(out, c["dec"])), name
+    dec = gpu.Decoder(c["bs"], proxy_mode=1)
+    out = dec.decode(c["bs"])
+    dec.close()
+    assert all(np.array_equal(a, b) for a, b in zip(out, c["proxy"])), name
+
+
+def test_colour_transform_not_batched(gpu):
+    """Frames with a colour transform or an output non-linearity decode per
+    frame only; the batch API refuses them."""
+    c = G.mct_cases()["mct_rct_444_8b"]
+    dec = gpu.Decoder(c["bs"])
+    batch = gpu.Batch(1 << 28)
+    planes = [dec.alloc_planes()]
+    assert batch.decode([dec], [c["bs"]], planes) != 0
+    batch.close()
+    dec.close()
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_colour_transform_and_nlt_against_oracle(gpu, oracle, seed):
+    rng = np.random.default_rng(950 + seed)
+    fmt = [S.FMT_YUV444, S.FMT_PACKED_RGB, S.FMT_YUV422, S.FMT_YUV420][seed % 4]
+    cpih = 1 if fmt in (S.FMT_YUV444, S.FMT_PACKED_RGB) and seed % 3 else 0
+    v, hh = [(2, 5), (1, 3), (0, 2), (2, 2), (1, 1)][seed % 5]
+    if fmt == S.FMT_YUV420 and v == 0:
+        v = 1
+    d = int(rng.choice([8, 10, 12, 14]))
+    w, h = int(rng.integers(8, 300)) * 2, int(rng.integers(2, 40)) * 2
+    planes = S.frame(w, h, d, fmt, seed=seed)
+    p = oracle.make_params(w, h, d, fmt, int(rng.choice([3, 6, 10])), 1, v, hh, quantization=int(rng.integers(0, 2)),
+                           slice_height=16)
+    p.cpih, p.tnlt = cpih, (seed // 4) % 3
+    p.nlt_sigma, p.nlt_alpha = int(rng.integers(0, 2)), int(rng.integers(0, 1 << 15))
+    p.nlt_t1 = int(rng.integers(1 << 16, 1 << 19))
+    p.nlt_t2 = p.nlt_t1 + int(rng.integers(1, 1 << 19))
+    p.nlt_e = int(rng.integers(1, 6))
+    err, bs = oracle.oracle_encode(p, planes)
+    if err:
+        pytest.skip("encode error 0x%x" % err)
+    e2, want = oracle.oracle_decode(bs)
+    assert e2 == 0
+    dec = gpu.Decoder(bs)
+    got = dec.decode(bs)
+    dec.close()
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
