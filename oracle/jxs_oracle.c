@@ -409,6 +409,16 @@ static int weights_assign(geom_t* g, uint32_t fmt) {
             memcpy(gain, wt444_g[g->dv], 30); memcpy(prio, wt444_p[g->dv], 30); size = wt444_n[g->dv]; have = 1;
         }
     }
+    if (!have && g->nc == 4 && fmt == FMT_4COMP) {
+        /* no weight table exists for four components; the Star-Tetrix test
+         * codestreams use gain 0 and priority = codestream band index */
+        for (uint32_t c = 0; c < g->nc; c++)
+            for (uint32_t b = 0; b < g->c[c].nb; b++) {
+                g->c[c].b[b].gain = 0;
+                g->c[c].b[b].prio = (uint8_t)g->c[c].b[b].gid;
+            }
+        return 0;
+    }
     if (!have) {
         if (g->nc != 3) return -1;
         if (fmt == FMT_YUV422) wt_derive(wt422_g[2], wt422_p[2], g->dv, g->dh, gain, prio, &size);
@@ -602,8 +612,10 @@ static int enc_configure(enc_t* e, const or_enc_params_t* p) {
     if (c->coding_vertical_prediction_mode >= 3) return E_BAD_PARAM;
     if (c->coding_signs_handling > 2) return E_BAD_PARAM;
     if (c->width < 4) return E_BAD_PARAM;
-    if (c->cpih > 1 || c->tnlt > 2) return E_BAD_PARAM;
-    if (c->cpih && c->colour_format != FMT_YUV444 && c->colour_format != FMT_PACKED_RGB) return E_BAD_PARAM;
+    if ((c->cpih != 0 && c->cpih != 1 && c->cpih != 3) || c->tnlt > 2) return E_BAD_PARAM;
+    if (c->cpih == 1 && c->colour_format != FMT_YUV444 && c->colour_format != FMT_PACKED_RGB) return E_BAD_PARAM;
+    if ((c->cpih == 3) != (c->colour_format == FMT_4COMP)) return E_BAD_PARAM;
+    if (c->cpih == 3 && (c->cts_cf > 15 || c->cts_e1 > 15 || c->cts_e2 > 15 || c->cfa_type > 1)) return E_BAD_PARAM;
     if ((c->colour_format == FMT_YUV422 || c->colour_format == FMT_YUV420) && (c->width % 2)) return E_BAD_PARAM;
     if (c->colour_format == FMT_YUV420 && (c->height % 2)) return E_BAD_PARAM;
     if (c->decomp_v > 2 || c->decomp_h > 5 || c->decomp_h < c->decomp_v) return E_BAD_PARAM;
@@ -665,8 +677,8 @@ static void enc_write_header(enc_t* e) {
     bw_put(&w, 0xff10, 16);                    /* SOC */
     bw_put(&w, 0xff50, 16);                    /* CAP */
     bw_put(&w, DIV_UP(16 + 9, 8), 16);
-    uint8_t cap[9] = {0, 0, (uint8_t)(e->prm.tnlt == 1), (uint8_t)(e->prm.tnlt == 2), (uint8_t)(e->fmt == FMT_YUV420), 0, 0, 0,
-                      1 /* Rl */};
+    uint8_t cap[9] = {0, (uint8_t)(e->prm.cpih == 3), (uint8_t)(e->prm.tnlt == 1), (uint8_t)(e->prm.tnlt == 2),
+                      (uint8_t)(e->fmt == FMT_YUV420), 0, 0, 0, 1 /* Rl */};
     for (int i = 0; i < 9; i++) bw_put(&w, cap[i], 1);
     bw_align(&w);
     bw_put(&w, 0xff12, 16);                    /* PIH */
@@ -704,6 +716,20 @@ static void enc_write_header(enc_t* e) {
         band_t* bd = &g->c[g->gcomp[i]].b[g->gband[i]];
         bw_put(&w, bd->gain, 8);
         bw_put(&w, bd->prio, 8);
+    }
+    if (e->prm.cpih == 3) {
+        bw_put(&w, 0xff18, 16); /* CTS */
+        bw_put(&w, 4, 16);
+        bw_put(&w, e->prm.cts_cf, 8);
+        bw_put(&w, (e->prm.cts_e1 << 4) | e->prm.cts_e2, 8);
+        bw_put(&w, 0xff19, 16); /* CRG: component positions of the CFA (Table F.9) */
+        bw_put(&w, 2 + 4 * g->nc, 16);
+        static const uint16_t crg[2][4][2] = {{{0, 0}, {32768, 0}, {0, 32768}, {32768, 32768}},
+                                              {{32768, 0}, {0, 0}, {32768, 32768}, {0, 32768}}};
+        for (uint32_t c = 0; c < g->nc; c++) {
+            bw_put(&w, crg[e->prm.cfa_type][c][0], 16);
+            bw_put(&w, crg[e->prm.cfa_type][c][1], 16);
+        }
     }
     if (e->prm.tnlt == 1) { /* NLT, quadratic */
         bw_put(&w, 0xff16, 16);
@@ -1708,13 +1734,13 @@ typedef struct {
     geom_t g;
     uint32_t lcod, depth[MAXC], qpih, fs, rm, bw, fq, lh, rl, nc, cpih, tnlt;
     uint32_t nlt_sigma, nlt_alpha, nlt_t1, nlt_t2, nlt_e; /* non-linearity parameters (NLT marker) */
+    uint32_t cts, cf, e1, e2, crg, xcrg[MAXC], ycrg[MAXC]; /* Star-Tetrix: CTS and CRG markers */
     uint32_t hdr_len;
     uint8_t gain[MAXGB], prio[MAXGB];
 } dec_hdr_t;
 
 /* get_header and its marker readers (Source/Lib/Decoder/Codec/ParseHeader.c:
- * 20-617).  The Star-Tetrix transform (Cpih = 3, CTS/CRG markers) is
- * rejected; everything else is parsed. */
+ * 20-617). */
 static int dec_parse_header(const uint8_t* bs, uint32_t size, dec_hdr_t* h) {
     memset(h, 0, sizeof(*h));
     br_t r = {bs, size, 0};
@@ -1805,8 +1831,24 @@ static int dec_parse_header(const uint8_t* bs, uint32_t size, dec_hdr_t* h) {
             if (!br_enough(&r, 3)) return E_DEC_SHORT;
             if (br_get(&r, 16) != 3) return E_DEC_BITSTREAM;
             sd = br_get(&r, 8);
-        } else if (m == 0xff18 || m == 0xff19) { /* CTS / CRG: the Star-Tetrix transform is outside this restatement */
-            return E_DEC_BITSTREAM;
+        } else if (m == 0xff18) { /* CTS, get_cts (ParseHeader.c:418-446) */
+            if (h->cts) return E_DEC_BITSTREAM;
+            h->cts = 1;
+            if (!br_enough(&r, 4)) return E_DEC_SHORT;
+            if (br_get(&r, 16) != 4) return E_DEC_BITSTREAM;
+            br_get(&r, 4);
+            h->cf = br_get(&r, 4);
+            h->e1 = br_get(&r, 4);
+            h->e2 = br_get(&r, 4);
+        } else if (m == 0xff19) { /* CRG, get_crg (ParseHeader.c:448-480) */
+            if (h->crg) return E_DEC_BITSTREAM;
+            h->crg = 1;
+            if (!br_enough(&r, 2 + nc * 4)) return E_DEC_SHORT;
+            if (br_get(&r, 16) != 2 + nc * 4 || nc > MAXC) return E_DEC_BITSTREAM;
+            for (uint32_t c = 0; c < nc; c++) {
+                h->xcrg[c] = br_get(&r, 16);
+                h->ycrg[c] = br_get(&r, 16);
+            }
         } else if (m == 0xff15) { /* COM */
             if (!br_enough(&r, 4)) return E_DEC_SHORT;
             uint32_t len = br_get(&r, 16);
@@ -1822,7 +1864,7 @@ static int dec_parse_header(const uint8_t* bs, uint32_t size, dec_hdr_t* h) {
         }
     }
     if (!have_cdt || !have_wgt) return E_DEC_BITSTREAM;
-    if (h->cpih == 3) return E_DEC_BITSTREAM; /* Star-Tetrix: outside this restatement */
+    if (h->cpih == 3 && (!h->cts || !h->crg || nc != 4)) return E_DEC_BITSTREAM;
     if (h->cpih) /* the colour transform needs equal sampling (ParseHeader.c:584-594) */
         for (uint32_t c = 1; c < nc; c++)
             if (sx[c] != sx[0] || sy[c] != sy[0]) return E_DEC_BITSTREAM;
@@ -2214,15 +2256,70 @@ static int32_t nlt_sample(const dec_hdr_t* h, int64_t v) {
     return clamp_i64((v + (((int64_t)1 << zeta) >> 1)) >> zeta, m);
 }
 
-/* With a colour transform (Cpih = 1): the inverse reversible colour
- * transform of components 0-2 (inverse_rct, Mct.c:137-153) of the whole
- * frame, then every component's output scaling (svt_jpeg_xs_decode_final,
+/* Star-Tetrix (ISO/IEC 21122-1 Annex F; Mct.c:14-136): the component
+ * displacement vectors (Table F.10), the component at a displacement
+ * (Table F.11) and the coordinate access with mirroring at the picture
+ * edges and, for Cf = 3, within a line pair (Table F.12). */
+static const int8_t st_disp[2][4][2] = {{{0, 1}, {1, 1}, {0, 0}, {1, 0}}, {{1, 1}, {0, 1}, {1, 0}, {0, 0}}};
+static const uint8_t st_comp[2][2][2] = {{{2, 0}, {3, 1}}, {{3, 1}, {2, 0}}};
+static int32_t st_access(int32_t* const* comps, int c, int x, int y, int w, int h, int rx, int ry, int cf, int ct) {
+    const int dx = st_disp[ct][c][0], dy = st_disp[ct][c][1];
+    if (2 * x + rx + dx < 0 || 2 * x + rx + dx >= 2 * w) rx = -rx;
+    if ((cf == 3 && (ry + dy < 0 || ry + dy > 1)) || 2 * y + ry + dy < 0 || 2 * y + ry + dy >= 2 * h) ry = -ry;
+    const int xx = (2 * x + rx + dx) / 2, yy = (2 * y + ry + dy) / 2;
+    return comps[st_comp[ct][(2 + rx + dx) % 2][(2 + ry + dy) % 2]][(size_t)yy * w + xx];
+}
+
+/* Inverse Star-Tetrix (Tables F.4-F.8; inverse_star_tetrix, Mct.c:120-135):
+ * average, delta, Y and CbCr steps in place, then components 0 <-> 2 and
+ * 1 <-> 3.  Products are taken in 32-bit wrap-around arithmetic like the
+ * reference's int. */
+static void inv_star_tetrix(int32_t* comps[4], int cf, int ct, int e1, int e2, int w, int h) {
+#define ACC(c, rx, ry) st_access(comps, c, x, y, w, h, rx, ry, cf, ct)
+#define MUL(k, v) ((int32_t)((uint32_t)(k) * (uint32_t)(v)))
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++)
+            comps[0][(size_t)y * w + x] -= (ACC(0, -1, -1) + ACC(0, 1, -1) + ACC(0, -1, 1) + ACC(0, 1, 1)) >> 3;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++)
+            comps[3][(size_t)y * w + x] += (ACC(3, -1, -1) + ACC(3, 1, -1) + ACC(3, -1, 1) + ACC(3, 1, 1)) >> 2;
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            comps[0][(size_t)y * w + x] -= (MUL(1 << e2, ACC(0, -1, 0) + ACC(0, 1, 0)) + MUL(1 << e1, ACC(0, 0, -1) + ACC(0, 0, 1))) >> 3;
+            comps[3][(size_t)y * w + x] -= (MUL(1 << e2, ACC(3, 0, -1) + ACC(3, 0, 1)) + MUL(1 << e1, ACC(3, -1, 0) + ACC(3, 1, 0))) >> 3;
+        }
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            comps[1][(size_t)y * w + x] += (ACC(1, -1, 0) + ACC(1, 1, 0) + ACC(1, 0, -1) + ACC(1, 0, 1)) >> 2;
+            comps[2][(size_t)y * w + x] += (ACC(2, -1, 0) + ACC(2, 1, 0) + ACC(2, 0, -1) + ACC(2, 0, 1)) >> 2;
+        }
+#undef ACC
+#undef MUL
+    int32_t* t = comps[0];
+    comps[0] = comps[2];
+    comps[2] = t;
+    t = comps[1];
+    comps[1] = comps[3];
+    comps[3] = t;
+}
+
+/* get_cfa_pattern (Mct.c:155-178): the CFA pattern type from the CRG
+ * marker. */
+static int st_cfa_type(const dec_hdr_t* h) {
+    return (h->xcrg[1] == 32768 && h->ycrg[1] == 0 && h->xcrg[2] == 0 && h->ycrg[2] == 32768) ? 0 : 1;
+}
+
+/* With a colour transform: Cpih = 1, the inverse reversible colour
+ * transform of components 0-2 (inverse_rct, Mct.c:137-153); Cpih = 3, the
+ * inverse Star-Tetrix transform; on the whole frame, then every
+ * component's output scaling (svt_jpeg_xs_decode_final,
  * Decoder.c:707-798). */
 static void dec_mct_nlt(dec_t* d, void* const planes[4], const uint32_t strides[4]) {
     const dec_hdr_t* h = d->h;
     const geom_t* g = &h->g;
     const uint32_t w = g->c[0].w, ht = g->c[0].h;
     const size_t n = (size_t)w * ht;
+    if (h->cpih == 3) inv_star_tetrix(d->mct, (int)h->cf, st_cfa_type(h), (int)h->e1, (int)h->e2, (int)w, (int)ht);
     if (h->cpih == 1) {
         int32_t *c0 = d->mct[0], *c1 = d->mct[1], *c2 = d->mct[2];
         for (size_t i = 0; i < n; i++) {

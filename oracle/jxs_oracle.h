@@ -28,6 +28,10 @@ typedef struct or_enc_params {
      * transform; tnlt 1 / 2 writes an NLT marker (quadratic / extended
      * output non-linearity) with the given parameters */
     uint32_t cpih, tnlt, nlt_sigma, nlt_alpha, nlt_t1, nlt_t2, nlt_e;
+    /* Cpih = 3 (Star-Tetrix, 4 components): CTS Cf / e1 / e2 and the CFA
+     * pattern type of the CRG marker (0 RGGB-like, 1 GRBG-like); written
+     * as is, without the forward transform */
+    uint32_t cts_cf, cts_e1, cts_e2, cfa_type;
 } or_enc_params_t;
 
 typedef struct or_image_info {

@@ -651,8 +651,6 @@ int32_t jxs_cfg_decoder(jxs_cfg_t* g, const uint8_t* bs, size_t size, jxs_hdr_in
     if ((v >> 7) != 0 || ((v >> 4) & 7) != 0) return JXS_E_DEC_BITSTREAM;
     info->cpih = v & 15;
     if (info->cpih != 0 && info->cpih != 1 && info->cpih != 3) return JXS_E_DEC_BITSTREAM;
-    /* the Star-Tetrix transform (Cpih = 3) is not part of this implementation */
-    if (info->cpih == 3) return JXS_E_DEC_BITSTREAM;
     v = hr_u8(&r);
     uint32_t dh = v >> 4, dv = v & 15;
     v = hr_u8(&r);
@@ -662,7 +660,7 @@ int32_t jxs_cfg_decoder(jxs_cfg_t* g, const uint8_t* bs, size_t size, jxs_hdr_in
     g->rm = v & 3;
     if (g->qpih > 1 || g->fs > 1 || g->rm > 1) return JXS_E_DEC_BITSTREAM;
     uint32_t sx[JXS_MAXC] = {1, 1, 1, 1}, sy[JXS_MAXC] = {1, 1, 1, 1}, sd = 0, depth[8] = {0};
-    int have_cdt = 0, have_wgt = 0;
+    int have_cdt = 0, have_wgt = 0, have_cts = 0, have_crg = 0;
     uint8_t gain[JXS_MAXBL], prio[JXS_MAXBL];
     uint32_t nw = 0;
     for (;;) {
@@ -718,8 +716,30 @@ int32_t jxs_cfg_decoder(jxs_cfg_t* g, const uint8_t* bs, size_t size, jxs_hdr_in
             if (!hr_has(&r, 3)) return JXS_E_DEC_SHORT;
             if (hr_u16(&r) != 3) return JXS_E_DEC_BITSTREAM;
             sd = hr_u8(&r);
-        } else if (m == 0xff18 || m == 0xff19) {
-            return JXS_E_DEC_BITSTREAM; /* CTS / CRG: only with the Star-Tetrix transform, not part of this implementation */
+        } else if (m == 0xff18) {
+            /* CTS: Cf, e1, e2 of the Star-Tetrix transform (get_cts,
+             * ParseHeader.c:418-446) */
+            if (have_cts) return JXS_E_DEC_BITSTREAM;
+            have_cts = 1;
+            if (!hr_has(&r, 4)) return JXS_E_DEC_SHORT;
+            if (hr_u16(&r) != 4) return JXS_E_DEC_BITSTREAM;
+            g->cts_cf = hr_u8(&r) & 15;
+            v = hr_u8(&r);
+            g->cts_e1 = v >> 4;
+            g->cts_e2 = v & 15;
+        } else if (m == 0xff19) {
+            /* CRG: component registration; the CFA pattern type of
+             * get_cfa_pattern (Mct.c:155-178, ParseHeader.c:448-480) */
+            if (have_crg) return JXS_E_DEC_BITSTREAM;
+            have_crg = 1;
+            if (!hr_has(&r, 2 + nc * 4)) return JXS_E_DEC_SHORT;
+            if (hr_u16(&r) != 2 + nc * 4 || nc > JXS_MAXC) return JXS_E_DEC_BITSTREAM;
+            uint32_t xc[JXS_MAXC], yc[JXS_MAXC];
+            for (uint32_t c = 0; c < nc; c++) {
+                xc[c] = hr_u16(&r);
+                yc[c] = hr_u16(&r);
+            }
+            g->cfa_type = (nc >= 3 && xc[1] == 32768 && yc[1] == 0 && xc[2] == 0 && yc[2] == 32768) ? 0 : 1;
         } else if (m == 0xff15) {
             if (!hr_has(&r, 4)) return JXS_E_DEC_SHORT;
             uint32_t len = hr_u16(&r);
@@ -736,9 +756,11 @@ int32_t jxs_cfg_decoder(jxs_cfg_t* g, const uint8_t* bs, size_t size, jxs_hdr_in
     }
     if (!have_cdt || !have_wgt) return JXS_E_DEC_BITSTREAM;
     if (info->cpih) {
-        /* the colour transform needs three components of equal sampling
-         * (ParseHeader.c:584-594, Mct.c:137-153) */
+        /* the colour transforms need three (RCT) or four (Star-Tetrix, with
+         * its CTS and CRG markers) components of equal sampling
+         * (ParseHeader.c:584-604, Mct.c:137-153) */
         if (nc < 3) return JXS_E_DEC_BITSTREAM;
+        if (info->cpih == 3 && (nc != 4 || !have_cts || !have_crg)) return JXS_E_DEC_BITSTREAM;
         for (uint32_t c = 1; c < nc; c++)
             if (sx[c] != sx[0] || sy[c] != sy[0]) return JXS_E_DEC_BITSTREAM;
     }

@@ -132,6 +132,7 @@ typedef struct jxs_cfg {
      * marker's output non-linearity (0 linear, 1 quadratic, 2 extended) */
     uint32_t cpih, tnlt, nlt_sigma, nlt_alpha, nlt_e;
     uint32_t nlt_t1, nlt_t2;
+    uint32_t cts_cf, cts_e1, cts_e2, cfa_type; /* Star-Tetrix (Cpih = 3): CTS marker, CFA pattern type from CRG */
     uint32_t slice_size[8192];           /* bytes of each slice incl. its header (last: incl. EOC) */
     uint32_t slice_begin[8192];          /* byte offset of each slice in the codestream */
 } jxs_cfg_t;

@@ -707,8 +707,29 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         KMARK();
     }
     if (nlt_pass) {
+        FramePlanes tin = lout;
+        if (c->cpih == 3) {
+            /* inverse Star-Tetrix in place, then components 0 <-> 2 and
+             * 1 <-> 3 (inverse_star_tetrix, Mct.c:120-135) */
+            StParams T;
+            memset(&T, 0, sizeof(T));
+            for (int k = 0; k < 4; k++) T.c[k] = (int32_t*)lout.p[k];
+            T.pitch = lout.pitch[0];
+            T.w = (int)jxs_out_w(c, 0);
+            T.h = (int)jxs_out_h(c, 0);
+            T.cf = (int)c->cts_cf;
+            T.ct = (int)c->cfa_type;
+            T.e1 = (int)c->cts_e1;
+            T.e2 = (int)c->cts_e2;
+            CK(jxs_launch_star_tetrix(&T, st));
+            const int perm[4] = {2, 3, 0, 1};
+            for (int k = 0; k < 4; k++) {
+                tin.p[k] = lout.p[perm[k]];
+                tin.pitch[k] = lout.pitch[perm[k]];
+            }
+        }
         NltOut P;
-        nlt_out_params(c, lout, out, &P);
+        nlt_out_params(c, tin, out, &P);
         CK(jxs_launch_nlt_out(&P, st));
     }
     TMARK(3);

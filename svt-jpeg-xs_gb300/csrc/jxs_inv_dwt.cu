@@ -453,3 +453,59 @@ extern "C" cudaError_t jxs_launch_nlt_out(const NltOut* P, cudaStream_t st) {
     nlt_out_kernel<<<dim3((unsigned)((wmax + 255) / 256), (unsigned)hmax), 256, 0, st>>>(*P);
     return cudaGetLastError();
 }
+
+/* Inverse Star-Tetrix (Cpih = 3; ISO/IEC 21122-1 Annex F, Mct.c:14-136) on
+ * the int32 planes of the four components, before nlt_out_kernel.  Each of
+ * the four steps updates components that none of its reads touch (the
+ * access function always lands on another component), so one launch per
+ * step is exact in any thread order:
+ *   step 0  average: c0 -= (four diagonal neighbours) >> 3
+ *   step 1  delta:   c3 += (four diagonal neighbours) >> 2
+ *   step 2  Y:       c0, c3 -= (2^e2 (horizontal pair) + 2^e1 (vertical pair)) >> 3
+ *   step 3  CbCr:    c1, c2 += (four direct neighbours) >> 2
+ * then components 0 <-> 2 and 1 <-> 3 (done by the caller's plane order). */
+__constant__ int8_t c_st_disp[2][4][2] = {{{0, 1}, {1, 1}, {0, 0}, {1, 0}}, {{1, 1}, {0, 1}, {1, 0}, {0, 0}}}; /* Table F.10 */
+__constant__ uint8_t c_st_comp[2][2][2] = {{{2, 0}, {3, 1}}, {{3, 1}, {2, 0}}};                            /* Table F.11 */
+
+/* Table F.12: mirrored at the picture edges and, for Cf = 3, within a line
+ * pair */
+DEV int32_t st_access(const StParams& P, int c, int x, int y, int rx, int ry) {
+    const int dx = c_st_disp[P.ct][c][0], dy = c_st_disp[P.ct][c][1];
+    if (2 * x + rx + dx < 0 || 2 * x + rx + dx >= 2 * P.w) rx = -rx;
+    if ((P.cf == 3 && (ry + dy < 0 || ry + dy > 1)) || 2 * y + ry + dy < 0 || 2 * y + ry + dy >= 2 * P.h) ry = -ry;
+    const int xx = (2 * x + rx + dx) / 2, yy = (2 * y + ry + dy) / 2;
+    return P.c[c_st_comp[P.ct][(2 + rx + dx) % 2][(2 + ry + dy) % 2]][(long long)yy * P.pitch + xx];
+}
+
+/* products in 32-bit wrap-around arithmetic like the reference's int */
+DEV int32_t st_mul(int32_t k, int32_t v) { return (int32_t)((uint32_t)k * (uint32_t)v); }
+
+__global__ void __launch_bounds__(256) star_tetrix_kernel(const __grid_constant__ StParams P, int step) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x >= P.w || y >= P.h) return;
+    const long long i = (long long)y * P.pitch + x;
+#define ACC(c, rx, ry) st_access(P, c, x, y, rx, ry)
+    if (step == 0) {
+        P.c[0][i] -= (ACC(0, -1, -1) + ACC(0, 1, -1) + ACC(0, -1, 1) + ACC(0, 1, 1)) >> 3;
+    } else if (step == 1) {
+        P.c[3][i] += (ACC(3, -1, -1) + ACC(3, 1, -1) + ACC(3, -1, 1) + ACC(3, 1, 1)) >> 2;
+    } else if (step == 2) {
+        const int32_t k1 = 1 << P.e1, k2 = 1 << P.e2;
+        P.c[0][i] -= (st_mul(k2, ACC(0, -1, 0) + ACC(0, 1, 0)) + st_mul(k1, ACC(0, 0, -1) + ACC(0, 0, 1))) >> 3;
+        P.c[3][i] -= (st_mul(k2, ACC(3, 0, -1) + ACC(3, 0, 1)) + st_mul(k1, ACC(3, -1, 0) + ACC(3, 1, 0))) >> 3;
+    } else {
+        P.c[1][i] += (ACC(1, -1, 0) + ACC(1, 1, 0) + ACC(1, 0, -1) + ACC(1, 0, 1)) >> 2;
+        P.c[2][i] += (ACC(2, -1, 0) + ACC(2, 1, 0) + ACC(2, 0, -1) + ACC(2, 0, 1)) >> 2;
+    }
+#undef ACC
+}
+
+extern "C" cudaError_t jxs_launch_star_tetrix(const StParams* P, cudaStream_t st) {
+    const dim3 grid((unsigned)((P->w + 255) / 256), (unsigned)P->h);
+    for (int step = 0; step < 4; step++) {
+        star_tetrix_kernel<<<grid, 256, 0, st>>>(*P, step);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}

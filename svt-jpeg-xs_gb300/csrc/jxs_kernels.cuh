@@ -177,6 +177,14 @@ struct NltOut {
     int64_t b2, b3, a1, a3;
 };
 
+/* The inverse Star-Tetrix transform of a decoded frame (star_tetrix_kernel):
+ * four int32 planes of w x h with one pitch, updated in place. */
+struct StParams {
+    int32_t* c[4];
+    long long pitch;
+    int w, h, cf, ct, e1, e2;
+};
+
 /* Encoder rate-control outputs per precinct row. */
 struct PrecRC {
     uint32_t total_bytes;  /* bytes written for the precinct (header to last data byte, incl. trailing padding) */

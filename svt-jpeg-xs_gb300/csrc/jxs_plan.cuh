@@ -47,6 +47,7 @@ extern "C" cudaError_t jxs_launch_inv_v_batch(const InvVLaunchB* L, int out_kind
 extern "C" cudaError_t jxs_launch_inv_h(const InvHLaunch* L, int out_kind, int nblocks, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_inv_h_batch(const InvHLaunchB* L, int out_kind, int nblocks, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_nlt_out(const NltOut* P, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_star_tetrix(const StParams* P, cudaStream_t st);
 extern "C" int jxs_inv_v_tile_rows(void);
 extern "C" int jxs_inv_v_tile_cols(void);
 extern "C" int jxs_inv_h_max_rows_per_block(void);

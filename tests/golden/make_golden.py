@@ -16,7 +16,8 @@ Writes
   cw*.npz               multi-column precinct codestreams (Cw > 0) from the
                         oracle's encoder (the reference encoder writes only
                         Cw = 0) and the reference decoder's planes
-  mct*.npz, nlt*.npz    colour transform (Cpih = 1) and output non-linearity
+  mct*.npz, nlt*.npz    colour transform (Cpih = 1, Star-Tetrix Cpih = 3) and
+                        output non-linearity
                         codestreams from the oracle's encoder, with the
                         reference decoder's planes (full and half resolution)
   proxy<m>_<case>.npz   the reference decoder's proxy output (m = 1 half,
@@ -247,6 +248,38 @@ def make_mct():
         print(name, len(bs), "bytes")
 
 
+# Star-Tetrix (Cpih = 3, four components with CTS / CRG markers), written
+# by the oracle's encoder without the forward transform; the reference
+# decoder's planes (full and half resolution) are the expected output.
+# name: (w, h, depth, bpp_num, decomp_v, decomp_h, quant, slice_h, seed, cf, e1, e2, cfa_type, tnlt)
+ST_CASES = {
+    "mct_st_cf0_rggb_8b": (64, 32, 8, 8, 2, 5, 0, 16, 61, 0, 1, 2, 0, 0),
+    "mct_st_cf3_grbg_10b": (90, 24, 10, 6, 1, 3, 1, 8, 62, 3, 0, 1, 1, 0),
+    "mct_st_cf0_grbg_12b_quadratic": (48, 40, 12, 10, 2, 2, 0, 16, 63, 0, 2, 0, 1, 1),
+}
+
+
+def make_st():
+    for name, (w, h, d, bn, v, hh, q, sl, seed, cf, e1, e2, ct, tnlt) in ST_CASES.items():
+        planes = S.frame(w, h, d, S.FMT_4COMP, seed=seed)
+        p = O.make_params(w, h, d, S.FMT_4COMP, bn, 1, v, hh, quantization=q, slice_height=sl)
+        p.cpih, p.cts_cf, p.cts_e1, p.cts_e2, p.cfa_type = 3, cf, e1, e2, ct
+        p.tnlt, p.nlt_alpha = tnlt, 321
+        err, bs = O.oracle_encode(p, planes)
+        assert err == 0, (name, hex(err))
+        err, dec = O.ref_decode(bs)
+        assert err == 0, (name, hex(err))
+        err, dec1 = O.ref_decode_proxy(bs, 1)
+        assert err == 0, (name, hex(err))
+        arrays = {"bs": bs, "params": np.array([w, h, d, bn, v, hh, q, sl, seed, cf, e1, e2, ct, tnlt], np.uint32)}
+        for i, pl in enumerate(dec):
+            arrays["dec%d" % i] = pl
+        for i, pl in enumerate(dec1):
+            arrays["proxy%d" % i] = pl
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrays)
+        print(name, len(bs), "bytes")
+
+
 def main():
     if not O.ref_available():
         raise SystemExit("build the reference first: make -C oracle ref")
@@ -255,6 +288,7 @@ def main():
         return
     if "--mct-only" in sys.argv:
         make_mct()
+        make_st()
         return
     if "--vpred-only" in sys.argv:
         make_vpred()
@@ -269,6 +303,7 @@ def main():
     make_signs()
     make_cw()
     make_mct()
+    make_st()
     for name, (w, h, d, fmt, bn, bd, v, hh, q, sl, sig, rc, seed) in SMALL_CASES.items():
         planes = S.frame(w, h, d, fmt, seed=seed)
         p = O.make_params(w, h, d, fmt, bn, bd, v, hh, quantization=q, slice_height=sl, significance=sig, rc_mode=rc)

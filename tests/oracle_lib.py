@@ -17,7 +17,7 @@ REF_SO = os.path.join(ORACLE_DIR, "_ref", "libjxsref.so")
 
 _FIELDS = ("width height bit_depth colour_format bpp_num bpp_den decomp_v decomp_h quantization slice_height "
            "rate_control_mode coding_significance coding_signs_handling coding_vertical_prediction_mode threads_num "
-           "precinct_width cpih tnlt nlt_sigma nlt_alpha nlt_t1 nlt_t2 nlt_e").split()
+           "precinct_width cpih tnlt nlt_sigma nlt_alpha nlt_t1 nlt_t2 nlt_e cts_cf cts_e1 cts_e2 cfa_type").split()
 
 
 class EncParams(ctypes.Structure):

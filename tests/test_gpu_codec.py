@@ -700,3 +700,28 @@ def test_colour_transform_and_nlt_against_oracle(gpu, oracle, seed):
     got = dec.decode(bs)
     dec.close()
     assert all(np.array_equal(a, b) for a, b in zip(got, want))
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_star_tetrix_against_oracle(gpu, oracle, seed):
+    """Star-Tetrix (Cpih = 3) codestreams of the oracle's encoder: the GPU
+    decode is bit-exact with the oracle's, which matches the reference
+    decoder on such streams."""
+    rng = np.random.default_rng(1100 + seed)
+    w, h = int(rng.integers(4, 200)) * 2, int(rng.integers(2, 40)) * 2
+    d = int(rng.choice([8, 10, 12]))
+    v, hh = [(2, 5), (1, 3), (0, 2), (2, 2)][seed % 4]
+    planes = S.frame(w, h, d, S.FMT_4COMP, seed=seed)
+    p = oracle.make_params(w, h, d, S.FMT_4COMP, int(rng.choice([4, 8, 12])), 1, v, hh,
+                           quantization=int(rng.integers(0, 2)), slice_height=16)
+    p.cpih, p.cts_cf, p.cts_e1, p.cts_e2, p.cfa_type = 3, [0, 3][seed % 2], int(rng.integers(0, 4)), int(rng.integers(0, 4)), (seed // 2) % 2
+    p.tnlt, p.nlt_alpha, p.nlt_t1, p.nlt_t2, p.nlt_e = (seed // 4) % 3, 500, 200000, 500000, 3
+    err, bs = oracle.oracle_encode(p, planes)
+    if err:
+        pytest.skip("encode error 0x%x" % err)
+    e2, want = oracle.oracle_decode(bs)
+    assert e2 == 0
+    dec = gpu.Decoder(bs)
+    got = dec.decode(bs)
+    dec.close()
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))

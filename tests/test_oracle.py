@@ -358,3 +358,28 @@ def test_oracle_colour_transform_and_nlt_match_reference_decoder(oracle, seed):
     e2, d_or = oracle.oracle_decode(bs)
     assert e1 == e2 == 0
     assert all(np.array_equal(a, b) for a, b in zip(d_ref, d_or))
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_oracle_star_tetrix_matches_reference_decoder(oracle, seed):
+    """Star-Tetrix (Cpih = 3: four components, CTS / CRG markers; both CFA
+    pattern types, Cf 0 and 3): oracle-made codestreams decode to the same
+    planes in the reference decoder and the oracle's."""
+    if not oracle.ref_available():
+        pytest.skip("reference library not built here (needs the reference sources)")
+    rng = np.random.default_rng(1000 + seed)
+    w, h = int(rng.integers(4, 90)) * 2, int(rng.integers(2, 24)) * 2
+    d = int(rng.choice([8, 10, 12]))
+    v, hh = [(2, 5), (1, 3), (0, 2), (2, 2)][seed % 4]
+    planes = S.frame(w, h, d, S.FMT_4COMP, seed=seed)
+    p = oracle.make_params(w, h, d, S.FMT_4COMP, int(rng.choice([4, 8, 12])), 1, v, hh,
+                           quantization=int(rng.integers(0, 2)), slice_height=16)
+    p.cpih, p.cts_cf, p.cts_e1, p.cts_e2, p.cfa_type = 3, [0, 3][seed % 2], int(rng.integers(0, 4)), int(rng.integers(0, 4)), (seed // 2) % 2
+    p.tnlt, p.nlt_alpha, p.nlt_t1, p.nlt_t2, p.nlt_e = (seed // 4) % 3, 500, 200000, 500000, 3
+    err, bs = oracle.oracle_encode(p, planes)
+    if err:
+        return
+    e1, d_ref = oracle.ref_decode(bs)
+    e2, d_or = oracle.oracle_decode(bs)
+    assert e1 == e2 == 0
+    assert all(np.array_equal(a, b) for a, b in zip(d_ref, d_or))
