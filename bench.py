@@ -27,6 +27,7 @@ reference library itself cannot be built on the GPU host: its sources are not
 shipped there), printing the same metric.
 """
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -892,10 +893,16 @@ def run_serve(args, local):
         server.poll()
         done, meta = [], {}
         seq = [0] * nstreams
+        lag = np.zeros(len(arrivals))
+        # the submitting loop must keep to the arrival times: a garbage
+        # collection during it would delay a burst of submissions
+        gc.collect()
+        gc.disable()
         t0 = time.perf_counter()
         for n, (ta, sidx) in enumerate(arrivals):
             while time.perf_counter() - t0 < ta:
                 pass
+            lag[n] = time.perf_counter() - t0 - ta
             k = seq[sidx]
             seq[sidx] += 1
             meta[n] = (sidx, k)
@@ -906,6 +913,7 @@ def run_serve(args, local):
             done.extend(server.poll())
             time.sleep(0.0002)
         done.extend(server.poll())
+        gc.enable()
         st = server.stats()
         # the last request of every stream against its result alone
         checks = 0
@@ -935,6 +943,7 @@ def run_serve(args, local):
                "frame_latency_ms_p99": float(np.percentile(lat, 99)), "frame_latency_ms_max": float(lat.max()),
                "queue_ms_p50": float(np.percentile(queue, 50)), "queue_ms_p99": float(np.percentile(queue, 99)),
                "service_ms_p50": float(np.percentile(service, 50)), "service_ms_p99": float(np.percentile(service, 99)),
+               "submit_lag_ms_p99": float(np.percentile(lag, 99) * 1e3), "submit_lag_ms_max": float(lag.max() * 1e3),
                "requests": len(done), "checked_bit_exact": checks}
         if mode == jxs.SERVER_BATCHED:
             out.update({"batches": st["batches"], "mean_batch": st["batched_frames"] / max(1, st["batches"]),
