@@ -960,12 +960,23 @@ def run_serve(args, local):
         b = d_bs[t][k % 2]
         return server.submit(sids[sidx], tag, planes, b.data_ptr(), b.numel())
 
+    def run_checked(mode, arrivals):
+        # a run whose submitting loop fell behind the arrival times by more
+        # than a millisecond (the host was busy) measured a different load:
+        # it is repeated once and marked
+        out = run(mode, arrivals)
+        if out["submit_lag_ms_max"] > 1.0:
+            first = out["submit_lag_ms_max"]
+            out = run(mode, arrivals)
+            out["repeated_after_submit_lag_ms"] = first
+        return out
+
     rates = [float(x) for x in args.serve_rates.split(",")]
     sweep = []
     for r in rates:
         arr = arrivals_at(r)
-        sweep.append({"offered_frames_s": r, "batched": run(jxs.SERVER_BATCHED, arr),
-                      "per_frame": run(jxs.SERVER_PER_FRAME, arr)})
+        sweep.append({"offered_frames_s": r, "batched": run_checked(jxs.SERVER_BATCHED, arr),
+                      "per_frame": run_checked(jxs.SERVER_PER_FRAME, arr)})
     batched, per_frame = sweep[0]["batched"], sweep[0]["per_frame"]
     line = {"workload": "serve", "metric": "served encode/decode Gpix/s and p50/p99 frame latency, batched vs per-frame",
             "unit": "Gpix/s", "value": batched["gpix_s"], "n_gpus": 1, "higher_is_better": True, "dtype": "int32",
