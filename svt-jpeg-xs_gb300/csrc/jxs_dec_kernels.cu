@@ -23,6 +23,7 @@
 #define UK_WARPS (UK_THREADS / 32)
 #define UK_ZCAP(cap_groups) ((cap_groups) + 8 * JXS_MAXPK + 32)
 #define FULL 0xffffffffu
+static_assert(JXS_MAXSEG <= UK_THREADS, "one thread per segment");
 
 /* Per band line of the precinct being unpacked. */
 struct UkLine {
@@ -108,6 +109,30 @@ DEV uint32_t next_seg(uint32_t* ctr, int lane) {
     uint32_t v = 0;
     if (lane == 0) v = atomicAdd(ctr, 1u);
     return __shfl_sync(FULL, v, 0);
+}
+
+/* Per-packet exclusive running sums of one count per segment.  Segments
+ * are numbered in packet order, so a segment's base inside its packet is the
+ * block-wide exclusive sum up to it minus that of its packet's first
+ * segment.  Thread i holds segment i's count (nseg <= blockDim.x); base[i]
+ * receives its base, ex[0 .. nseg] the block-wide exclusive sums, and
+ * threads k < npk get packet k's total (0 without segments).  Other
+ * threads may read base[] and ex[] after the caller's next barrier. */
+DEV uint32_t seg_bases(uint32_t cnt, uint32_t nseg, uint32_t npk, const jxs_seg_t* segs, const jxs_bline_t* bls,
+                       const uint8_t* pkbl0, const uint8_t* pknbl, uint32_t* ex, uint32_t* base, uint32_t* ws) {
+    const uint32_t i = threadIdx.x;
+    uint32_t e;
+    const uint32_t total = block_scan1(i < nseg ? cnt : 0u, &e, ws);
+    if (i < nseg) ex[i] = e;
+    if (i == 0) ex[nseg] = total;
+    __syncthreads();
+    if (i < nseg) base[i] = e - ex[bls[pkbl0[bls[segs[i].bl].pk]].seg0];
+    uint32_t sum = 0;
+    if (i < npk && pknbl[i]) {
+        const uint32_t b0 = pkbl0[i], lb = b0 + pknbl[i] - 1;
+        sum = ex[bls[lb].seg0 + bls[lb].nseg] - ex[bls[b0].seg0];
+    }
+    return sum;
 }
 
 /* One group's coefficients from its data bits (unpack_data_c,
@@ -240,7 +265,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     __shared__ jxs_bline_t s_bl[JXS_MAXBLINES];
     __shared__ uint64_t s_crow[JXS_MAXBLINES]; /* per line: coefficient row offset */
     __shared__ uint8_t s_pkbl0[JXS_MAXPK], s_pknbl[JXS_MAXPK];
-    __shared__ uint32_t s_cnt[JXS_MAXSEG], s_base[JXS_MAXSEG];
+    __shared__ uint32_t s_cnt[JXS_MAXSEG], s_base[JXS_MAXSEG], s_ex[JXS_MAXSEG + 1];
     __shared__ uint32_t ws[UK_WARPS];
     __shared__ int s_err;
     __shared__ uint32_t s_total, s_lead, s_tw, s_npk;
@@ -469,44 +494,6 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             for (uint32_t x = lane; x < nbl; x += 32) hv |= ln[x].vp != 0;
             if (__any_sync(FULL, hv) && lane == 0) s_hasvp = 1;
         }
-        /* codewords of every segment: its groups minus those in
-         * insignificant significance groups (flags: 1 = insignificant) */
-        if (!err) {
-            for (uint32_t sidx = lane; sidx < nseg; sidx += 32) {
-                const jxs_seg_t sg = segs[sidx];
-                const jxs_bline_t& B = bls[sg.bl];
-                const UkLine& L = ln[sg.bl];
-                const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
-                uint32_t cnt = 0;
-                if (!L.raw) {
-                    cnt = gend - sg.g0;
-                    if (L.meth) {
-                        for (uint32_t s0 = sg.g0 >> 3; s0 < ((gend + 7) >> 3); s0 += 32) {
-                            const uint32_t ns = min(32u, ((gend + 7) >> 3) - s0);
-                            const uint32_t fl = bits32_at(pbuf, L.sig_pos + s0) >> (32 - ns);
-                            cnt -= 8 * __popc(fl);
-                            /* a flagged partial last group counts its own size */
-                            if ((fl & 1u) && 8 * (s0 + ns) > B.gcli_w) cnt += 8 * (s0 + ns) - B.gcli_w;
-                        }
-                    }
-                }
-                s_cnt[sidx] = cnt;
-            }
-            __syncwarp();
-            /* codeword base of every segment inside its packet: one lane per packet */
-            if (lane < (int)npk_c) {
-                const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
-                uint32_t run = 0;
-                for (uint32_t x = b0; x < b0 + nb; x++) {
-                    if (ln[x].raw) continue;
-                    for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
-                        s_base[i] = run;
-                        run += s_cnt[i];
-                    }
-                }
-                pk[lane].ncoded = run;
-            }
-        }
         if (lane == 0) s_err = err;
     }
     __syncthreads();
@@ -515,8 +502,36 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         return;
     }
 
-    /* zero bits of the VLC sub-packets: count, scan, record positions */
+    /* codewords of every segment, one thread each: its groups minus those
+     * in insignificant significance groups (flags: 1 = insignificant); then
+     * the codeword base of every segment inside its packet */
     const uint32_t tw = s_tw, npk = s_npk;
+    {
+        uint32_t cnt = 0;
+        if (threadIdx.x < nseg) {
+            const jxs_seg_t sg = segs[threadIdx.x];
+            const jxs_bline_t& B = bls[sg.bl];
+            const UkLine& L = ln[sg.bl];
+            const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
+            if (!L.raw) {
+                cnt = gend - sg.g0;
+                if (L.meth) {
+                    for (uint32_t s0 = sg.g0 >> 3; s0 < ((gend + 7) >> 3); s0 += 32) {
+                        const uint32_t ns = min(32u, ((gend + 7) >> 3) - s0);
+                        const uint32_t fl = bits32_at(pbuf, L.sig_pos + s0) >> (32 - ns);
+                        cnt -= 8 * __popc(fl);
+                        /* a flagged partial last group counts its own size */
+                        if ((fl & 1u) && 8 * (s0 + ns) > B.gcli_w) cnt += 8 * (s0 + ns) - B.gcli_w;
+                    }
+                }
+            }
+        }
+        const uint32_t ncoded = seg_bases(cnt, nseg, npk, segs, bls, s_pkbl0, s_pknbl, s_ex, s_base, ws);
+        if (threadIdx.x < npk) pk[threadIdx.x].ncoded = ncoded;
+        __syncthreads();
+    }
+
+    /* zero bits of the VLC sub-packets: count, scan, record positions */
     const uint32_t per = (tw + blockDim.x - 1) / blockDim.x;
     const uint32_t wa = min(tw, threadIdx.x * per), we = min(tw, wa + per);
     uint32_t zc = 0;
@@ -696,26 +711,15 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             __syncthreads();
         }
     }
-    if (warp == 0) {
-        /* data base of every segment inside its packet: one lane per packet */
-        bool bad_pk = false;
-        if (lane < (int)npk) {
-            const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
-            uint32_t run = 0;
-            for (uint32_t x = b0; x < b0 + nb; x++)
-                for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
-                    s_base[i] = run;
-                    run += s_cnt[i];
-                }
-            bad_pk = pk[lane].present && run > pk[lane].dbits;
+    {
+        /* data base of every segment inside its packet */
+        const uint32_t dbits = seg_bases(threadIdx.x < nseg ? s_cnt[threadIdx.x] : 0u, nseg, npk, segs, bls, s_pkbl0, s_pknbl,
+                                         s_ex, s_base, ws);
+        const int bad_pk = threadIdx.x < npk && pk[threadIdx.x].present && dbits > pk[threadIdx.x].dbits;
+        if (__syncthreads_or(bad_pk)) {
+            if (threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_DEC_BITSTREAM);
+            return;
         }
-        const bool any_bad = __any_sync(FULL, bad_pk);
-        if (lane == 0) s_err = any_bad ? JXS_E_DEC_BITSTREAM : 0;
-    }
-    __syncthreads();
-    if (s_err) {
-        if (threadIdx.x == 0) JXS_STATUS_SET(status, s_err);
-        return;
     }
 
     /* pass 3: data */
@@ -752,28 +756,13 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             if (lane == 0) s_nz[sidx] = nzs;
         }
         __syncthreads();
-        if (warp == 0) {
-            /* first sign bit of every segment inside its packet: one lane per packet */
-            bool bad_pk = false;
-            if (lane < (int)npk) {
-                const uint32_t b0 = s_pkbl0[lane], nb = s_pknbl[lane];
-                uint32_t run = 0;
-                for (uint32_t x = b0; x < b0 + nb; x++)
-                    for (uint32_t i = bls[x].seg0; i < bls[x].seg0 + bls[x].nseg; i++) {
-                        s_sgb[i] = run;
-                        run += s_nz[i];
-                    }
-                bad_pk = pk[lane].present && run > pk[lane].sgbits;
-            }
-            const bool any_bad = __any_sync(FULL, bad_pk);
-            if (lane == 0) {
-                s_err = any_bad ? JXS_E_DEC_BITSTREAM : 0;
-                s_next[1] = 0;
-            }
-        }
-        __syncthreads();
-        if (s_err) {
-            if (threadIdx.x == 0) JXS_STATUS_SET(status, s_err);
+        /* first sign bit of every segment inside its packet */
+        const uint32_t sbits = seg_bases(threadIdx.x < nseg ? s_nz[threadIdx.x] : 0u, nseg, npk, segs, bls, s_pkbl0, s_pknbl,
+                                         s_ex, s_sgb, ws);
+        const int bad_pk = threadIdx.x < npk && pk[threadIdx.x].present && sbits > pk[threadIdx.x].sgbits;
+        if (threadIdx.x == 0) s_next[1] = 0;
+        if (__syncthreads_or(bad_pk)) {
+            if (threadIdx.x == 0) JXS_STATUS_SET(status, JXS_E_DEC_BITSTREAM);
             return;
         }
     }
