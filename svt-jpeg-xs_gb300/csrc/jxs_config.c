@@ -90,6 +90,24 @@ static int32_t cfg_blines(jxs_cfg_t* g) {
         sg *= 2;
     }
     g->seg_groups = sg;
+    /* work order of the segments: most groups first, so that the warps that
+     * take segments from a queue finish close together */
+    for (int t = 0; t < 4; t++) {
+        const uint32_t n = g->nseg[t];
+        for (uint32_t i = 0; i < n; i++) {
+            const jxs_seg_t* si = &g->seg[t][i];
+            const uint32_t gi = g->bline[t][si->bl].gcli_w - si->g0, ni = gi < sg ? gi : sg;
+            uint32_t j = i;
+            while (j > 0) {
+                const jxs_seg_t* sj = &g->seg[t][g->seg_ord[t][j - 1]];
+                const uint32_t gj = g->bline[t][sj->bl].gcli_w - sj->g0, nj = gj < sg ? gj : sg;
+                if (nj >= ni) break;
+                g->seg_ord[t][j] = g->seg_ord[t][j - 1];
+                j--;
+            }
+            g->seg_ord[t][j] = (uint16_t)i;
+        }
+    }
     /* the line above each band line, for vertical prediction (line 0: the
      * band's last line in the precinct above, a normal row of the same
      * column kind) */

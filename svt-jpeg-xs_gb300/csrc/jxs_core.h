@@ -126,6 +126,7 @@ typedef struct jxs_cfg {
     uint32_t seg_groups;                 /* groups per segment, a multiple of 32 */
     uint32_t nseg[4];
     jxs_seg_t seg[4][JXS_MAXSEG];
+    uint16_t seg_ord[4][JXS_MAXSEG];     /* segments by decreasing group count (warp work queues) */
     uint32_t max_slice_budget;           /* 0 when slice starts cannot be predicted (decoder) */
     uint32_t proxy;                      /* decoder: output at 1/2^proxy resolution (proxy modes, Pi.c:567-626) */
     /* decoder: colour transform Cpih (0 none, 1 reversible RCT) and the NLT

@@ -262,6 +262,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     __shared__ uint32_t s_next[2]; /* segment queues of the two warp passes */
     /* this precinct kind's tables, staged from the configuration */
     __shared__ jxs_seg_t s_seg[JXS_MAXSEG];
+    __shared__ uint16_t s_ord[JXS_MAXSEG];     /* work order of the segments */
     __shared__ jxs_bline_t s_bl[JXS_MAXBLINES];
     __shared__ uint64_t s_crow[JXS_MAXBLINES]; /* per line: coefficient row offset */
     __shared__ uint8_t s_pkbl0[JXS_MAXPK], s_pknbl[JXS_MAXPK];
@@ -322,6 +323,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             ((uint32_t*)s_seg)[i] = ((const uint32_t*)cfg->seg[last])[i];
         for (uint32_t i = threadIdx.x; i < nl * (sizeof(jxs_bline_t) / 4); i += blockDim.x)
             ((uint32_t*)s_bl)[i] = ((const uint32_t*)cfg->bline[last])[i];
+        for (uint32_t i = threadIdx.x; i < ns; i += blockDim.x) s_ord[i] = cfg->seg_ord[last][i];
         for (uint32_t x = threadIdx.x; x < nl; x += blockDim.x) {
             const jxs_bline_t& B = cfg->bline[last][x];
             const jxs_band_t& bd = cfg->band[B.fb];
@@ -603,7 +605,8 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     const uint32_t lt_mask = (1u << lane) - 1u;
     /* a group's data: its sign nibble (signs with the data) and its planes */
     const uint32_t fs = s_sc[3], nib_sign = fs ? 0u : 1u;
-    for (uint32_t sidx = next_seg(&s_next[0], lane); sidx < nseg; sidx = next_seg(&s_next[0], lane)) {
+    for (uint32_t qi = next_seg(&s_next[0], lane); qi < nseg; qi = next_seg(&s_next[0], lane)) {
+        const uint32_t sidx = s_ord[qi];
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
         const UkLine L = ln[sg.bl];
@@ -730,7 +733,8 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
          * line in coefficient order (the last group's padding coefficients
          * last).  Count them per segment, give each segment its first sign
          * bit in the packet's sign sub-packet, then decode with the signs. */
-        for (uint32_t sidx = next_seg(&s_next[1], lane); sidx < nseg; sidx = next_seg(&s_next[1], lane)) {
+        for (uint32_t qi = next_seg(&s_next[1], lane); qi < nseg; qi = next_seg(&s_next[1], lane)) {
+            const uint32_t sidx = s_ord[qi];
             const jxs_seg_t sg = segs[sidx];
             const jxs_bline_t B = bls[sg.bl];
             const UkLine L = ln[sg.bl];
@@ -766,7 +770,8 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             return;
         }
     }
-    for (uint32_t sidx = next_seg(&s_next[1], lane); sidx < nseg; sidx = next_seg(&s_next[1], lane)) {
+    for (uint32_t qi = next_seg(&s_next[1], lane); qi < nseg; qi = next_seg(&s_next[1], lane)) {
+        const uint32_t sidx = s_ord[qi];
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
         const UkLine L = ln[sg.bl];

@@ -930,6 +930,13 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
 #define PK_THREADS 512
 #define PK_WARPS (PK_THREADS / 32)
 
+/* Next entry of a block's shared work queue for a warp. */
+__device__ __forceinline__ uint32_t queue_next(uint32_t* ctr, int lane) {
+    uint32_t v = 0;
+    if (lane == 0) v = atomicAdd(ctr, 1u);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
 /* OR the low `n` bits (1..64) of `v` into a big-endian bit string stored in
  * native byte order (byte i of the string is byte i of the buffer), at bit
  * `pos`.  Bits past the buffer's `nw` words are not written and set `ovf`
@@ -1069,6 +1076,8 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
     __shared__ uint32_t s_vst[JXS_MAXSEG], s_dst[JXS_MAXSEG], s_nst[JXS_MAXSEG]; /* per segment: GCLI / data / sign bit starts */
     /* this precinct kind's tables, staged from the configuration */
     __shared__ jxs_seg_t s_seg[JXS_MAXSEG];
+    __shared__ uint16_t s_ord[JXS_MAXSEG];                              /* work order of the segments */
+    __shared__ uint32_t s_q[2];                                         /* work queues of passes A and B */
     __shared__ jxs_bline_t s_bl[JXS_MAXBLINES];
     __shared__ uint64_t s_grow[JXS_MAXBLINES], s_crow[JXS_MAXBLINES]; /* per line: GCLI / coefficient row offsets */
     __shared__ uint8_t s_lt[JXS_MAXBLINES];                            /* per line: gtli */
@@ -1117,6 +1126,8 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             ((uint32_t*)s_seg)[i] = ((const uint32_t*)cfg->seg[last])[i];
         for (uint32_t i = threadIdx.x; i < nl * (sizeof(jxs_bline_t) / 4); i += blockDim.x)
             ((uint32_t*)s_bl)[i] = ((const uint32_t*)cfg->bline[last])[i];
+        for (uint32_t i = threadIdx.x; i < ns; i += blockDim.x) s_ord[i] = cfg->seg_ord[last][i];
+        if (threadIdx.x < 2) s_q[threadIdx.x] = 0;
         for (uint32_t x = threadIdx.x; x < nl; x += blockDim.x) {
             const jxs_bline_t& B = cfg->bline[last][x];
             const jxs_band_t& bd = cfg->band[B.fb];
@@ -1159,7 +1170,8 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
      * 128 groups per step; with sign handling also the non-zero quantized
      * coefficients, whose signs go to the sign sub-packets */
     const uint32_t fs = cfg->fs, uniform = cfg->qpih;
-    for (uint32_t sidx = warp; sidx < nseg; sidx += PK_WARPS) {
+    for (uint32_t qi = queue_next(&s_q[0], lane); qi < nseg; qi = queue_next(&s_q[0], lane)) {
+        const uint32_t sidx = s_ord[qi];
         const jxs_seg_t sg = segs[sidx];
         const uint32_t t = s_lt[sg.bl];
         const uint8_t* grow = gcli + s_grow[sg.bl];
@@ -1415,7 +1427,8 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
     /* pass B: each lane 4 consecutive groups; its unary codes are joined
      * into one write, its data chunks into writes of up to 64 bits, its
      * signs (with sign handling) into one write */
-    for (uint32_t sidx = warp; sidx < nseg; sidx += PK_WARPS) {
+    for (uint32_t qi = queue_next(&s_q[1], lane); qi < nseg; qi = queue_next(&s_q[1], lane)) {
+        const uint32_t sidx = s_ord[qi];
         const jxs_seg_t sg = segs[sidx];
         const jxs_bline_t B = bls[sg.bl];
         const PkLine L = pl[sg.bl];

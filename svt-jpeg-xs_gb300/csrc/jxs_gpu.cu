@@ -215,9 +215,10 @@ extern "C" jxs_gpu_enc_t* jxs_gpu_enc_create(const jxs_cfg_t* cfg, int nslots, i
     e->serial = g_serial++;
     /* the packing kernel stages a whole precinct in shared memory, starting
      * up to 15 bytes into the buffer for aligned stores: bound it by the
-     * largest slice budget */
+     * largest slice budget (the kernel's static shared memory, up to 34 KB,
+     * comes on top) */
     e->cap_words = 4 * div_up(cfg->max_slice_budget + 15, 16) + 4;
-    if ((size_t)e->cap_words * 4 > kSmemMax - 16 * 1024) {
+    if ((size_t)e->cap_words * 4 > kSmemMax - 28 * 1024) {
         fprintf(stderr, "jxs: precincts of this configuration (%u bytes per slice) exceed the on-chip packing buffer\n",
                 cfg->max_slice_budget);
         delete e;
