@@ -1627,7 +1627,7 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
 /* kernels: one frame, or a batch of frames (block -> frame by its first block) */
 /* ------------------------------------------------------------------------ */
 template <bool SIGNS, bool VPRED>
-__global__ void __launch_bounds__(RC_THREADS, 3) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
+__global__ void __launch_bounds__(RC_THREADS, (SIGNS || VPRED) ? 3 : 4) rc_cost_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ gcli,
                                                            const uint16_t* __restrict__ coef, uint32_t* __restrict__ cost,
                                                            uint32_t* __restrict__ slice_done, PrecRC* __restrict__ rc,
                                                            int* __restrict__ status) {
@@ -1635,20 +1635,20 @@ __global__ void __launch_bounds__(RC_THREADS, 3) rc_cost_kernel(const jxs_cfg_t*
 }
 
 template <bool SIGNS, bool VPRED>
-__global__ void __launch_bounds__(RC_THREADS, 3) rc_cost_batch_kernel(const __grid_constant__ EncPrecLaunch L) {
+__global__ void __launch_bounds__(RC_THREADS, (SIGNS || VPRED) ? 3 : 4) rc_cost_batch_kernel(const __grid_constant__ EncPrecLaunch L) {
     const EncPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
     rc_cost_body<SIGNS, VPRED>(F.cfg, F.gcli, F.coef, F.cost, F.slice_done, F.rc, F.status, (int)blockIdx.x - F.first_block);
 }
 
 template <bool VPRED>
-__global__ void __launch_bounds__(PK_THREADS, 3) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
+__global__ void __launch_bounds__(PK_THREADS, 4) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
                                                           const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
                                                           uint8_t* __restrict__ out, uint32_t cap_words, int* status) {
     pack_body<VPRED>(cfg, coef, gcli, rc, out, cap_words, status, (int)blockIdx.x);
 }
 
 template <bool VPRED>
-__global__ void __launch_bounds__(PK_THREADS, 3) pack_batch_kernel(const __grid_constant__ EncPrecLaunch L, uint32_t cap_words) {
+__global__ void __launch_bounds__(PK_THREADS, 4) pack_batch_kernel(const __grid_constant__ EncPrecLaunch L, uint32_t cap_words) {
     const EncPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
     pack_body<VPRED>(F.cfg, F.coef, F.gcli, F.rc, F.out, cap_words, F.status, (int)blockIdx.x - F.first_block);
 }
