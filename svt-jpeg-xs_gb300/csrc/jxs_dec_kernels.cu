@@ -779,23 +779,64 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         int16_t* crow = coef + s_crow[sg.bl];
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
         uint32_t dpos = P.dpos + s_base[sidx];
-        uint32_t spos = fs ? P.sgpos + s_sgb[sidx] : 0u;
+        if (!fs) {
+            /* signs with the data: each lane two consecutive groups (one
+             * offset scan for both, one 16-byte store where the band row is
+             * a single column) */
+            for (uint32_t base = sg.g0; base < gend; base += 64) {
+                const uint32_t g = base + 2 * lane;
+                const bool va = g < gend, vb = g + 1 < gend;
+                uint32_t v0 = 0, v1 = 0;
+                if (vb) {
+                    const uint32_t pr = *(const uint16_t*)(gcl + B.gbase + g);
+                    v0 = pr & 255u;
+                    v1 = pr >> 8;
+                } else if (va) {
+                    v0 = gcl[B.gbase + g];
+                }
+                const uint32_t np0 = v0 > L.t ? v0 - L.t : 0u, np1 = v1 > L.t ? v1 - L.t : 0u;
+                const uint32_t len0 = np0 ? 4 * (np0 + 1) : 0u, len1 = np1 ? 4 * (np1 + 1) : 0u;
+                uint32_t tot;
+                const uint32_t ex = warp_excl_scan(len0 + len1, &tot);
+                uint2 o0 = make_uint2(0u, 0u), o1 = o0;
+                const int wl = (int)B.w - 4 * (int)g;
+                if (len0) {
+                    const uint32_t pos = dpos + ex;
+                    const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
+                    o0 = decode_group(win >> (64 - len0), np0, L.t, v0, uniform, wl);
+                }
+                if (len1) {
+                    const uint32_t pos = dpos + ex + len0;
+                    const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
+                    o1 = decode_group(win >> (64 - len1), np1, L.t, v1, uniform, wl - 4);
+                }
+                if (one_col) {
+                    /* the band row's padding takes the last group's tail */
+                    if (vb) *(uint4*)(crow + 4 * g) = make_uint4(o0.x, o0.y, o1.x, o1.y);
+                    else if (va) *(uint2*)(crow + 4 * g) = o0;
+                } else {
+                    /* a column starts anywhere in the row and ends where the
+                     * next begins: the groups' coefficients inside it only */
+                    const uint32_t ov[4] = {o0.x, o0.y, o1.x, o1.y};
+#pragma unroll
+                    for (int c = 0; c < 8; c++)
+                        if ((c < 4 ? va : vb) && c < wl) crow[4 * g + c] = (int16_t)((ov[c >> 1] >> (16 * (c & 1))) & 0xffffu);
+                }
+                dpos += tot;
+            }
+            continue;
+        }
+        uint32_t spos = P.sgpos + s_sgb[sidx];
         for (uint32_t base = sg.g0; base < gend; base += 32) {
             const uint32_t g = base + lane;
             const bool valid = g < gend;
             const uint32_t v = valid ? gcl[B.gbase + g] : 0u;
             const uint32_t np = v > L.t ? v - L.t : 0u;
-            const uint32_t len = np ? 4 * (np + nib_sign) : 0u;
+            const uint32_t len = 4 * np; /* separate signs: planes only */
             uint32_t tot;
             const uint32_t ex = warp_excl_scan(len, &tot);
             uint2 o = make_uint2(0u, 0u);
-            if (!fs) {
-                if (len) {
-                    const uint32_t pos = dpos + ex;
-                    const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
-                    o = decode_group(win >> (64 - len), np, L.t, v, uniform, (int)B.w - 4 * (int)g);
-                }
-            } else {
+            {
                 uint32_t A = 0, B2 = 0, nz = 0;
                 if (len) {
                     const uint32_t pos = dpos + ex;
