@@ -135,6 +135,22 @@ DEV uint32_t seg_bases(uint32_t cnt, uint32_t nseg, uint32_t npk, const jxs_seg_
     return sum;
 }
 
+/* Packet header fields (get_packet_header, ParseHeader.c:20-44): raw flag,
+ * data, GCLI and sign sub-packet lengths in bytes; short (5-byte) or long
+ * (7-byte) form. */
+DEV void pk_header(const uint8_t* h, int long_hdr, uint32_t& raw, uint32_t& dlen, uint32_t& glen, uint32_t& slen) {
+    raw = h[0] >> 7;
+    if (long_hdr) {
+        dlen = ((uint32_t)(h[0] & 0x7f) << 13) | ((uint32_t)h[1] << 5) | (h[2] >> 3);
+        glen = ((uint32_t)(h[2] & 7) << 17) | ((uint32_t)h[3] << 9) | ((uint32_t)h[4] << 1) | (h[5] >> 7);
+        slen = ((uint32_t)(h[5] & 0x7f) << 8) | h[6];
+    } else {
+        dlen = ((uint32_t)(h[0] & 0x7f) << 8) | h[1];
+        glen = ((uint32_t)h[2] << 5) | (h[3] >> 3);
+        slen = ((uint32_t)(h[3] & 7) << 8) | h[4];
+    }
+}
+
 /* One group's coefficients from its data bits (unpack_data_c,
  * Packing.c:134-219): sign nibble (coefficient 0 in the most significant
  * bit), then bit-planes gcli-1 .. gtli; planes placed at << gtli
@@ -258,7 +274,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     __shared__ UkLine ln[JXS_MAXBLINES];
     __shared__ UkPk pk[JXS_MAXPK];
     __shared__ uint8_t s_mode[JXS_MAXBL];
-    __shared__ uint32_t s_pksb[JXS_MAXPK], s_pkrb[JXS_MAXPK];
+    __shared__ uint32_t s_pksb[JXS_MAXPK], s_pkrb[JXS_MAXPK], s_hpos[JXS_MAXPK];
     __shared__ uint32_t s_next[2]; /* segment queues of the two warp passes */
     /* this precinct kind's tables, staged from the configuration */
     __shared__ jxs_seg_t s_seg[JXS_MAXSEG];
@@ -406,71 +422,70 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             s_pkrb[lane] = rb;
         }
         __syncwarp();
+        /* packet headers: lane 0 follows the chain of header positions
+         * only; one lane per packet then reads its header again and derives
+         * its sub-packet positions with the reference's checks (every check
+         * bounds the running position, so testing each packet's own end
+         * against the precinct's end is equivalent) */
+        const int long_hdr = (int)s_sc[2];
+        const uint32_t hb = long_hdr ? 7u : 5u, pend_max = lead + total;
         if (lane == 0) {
-            const uint32_t lprc = total - s_sc[4];
-            const int long_hdr = (int)s_sc[2];
-            int64_t left = (int64_t)lprc * 8;
             uint32_t bpos = lead + s_sc[4]; /* bytes */
-            uint32_t tw = 0;
             for (uint32_t k = 0; k < npk_c; k++) {
-                UkPk& P = pk[k];
-                P.present = 0;
-                P.gbits = P.dbits = P.nwords = P.ncoded = P.nzero = 0;
-                P.raw = 0;
-                P.wbase = tw;
-                if (err || !s_pknbl[k]) continue;
-                const uint32_t hb = long_hdr ? 7 : 5;
-                left -= hb * 8;
-                if (left < 0) { err = JXS_E_DEC_BITSTREAM; break; }
-                const uint8_t* h = pbuf + bpos;
+                if (!s_pknbl[k]) continue;
+                if (bpos + hb > pend_max) {
+                    err = JXS_E_DEC_BITSTREAM;
+                    break;
+                }
                 uint32_t raw, dlen, glen, slen;
-                if (long_hdr) {
-                    raw = h[0] >> 7;
-                    dlen = ((uint32_t)(h[0] & 0x7f) << 13) | ((uint32_t)h[1] << 5) | (h[2] >> 3);
-                    glen = ((uint32_t)(h[2] & 7) << 17) | ((uint32_t)h[3] << 9) | ((uint32_t)h[4] << 1) | (h[5] >> 7);
-                    slen = ((uint32_t)(h[5] & 0x7f) << 8) | h[6];
-                } else {
-                    raw = h[0] >> 7;
-                    dlen = ((uint32_t)(h[0] & 0x7f) << 8) | h[1];
-                    glen = ((uint32_t)h[2] << 5) | (h[3] >> 3);
-                    slen = ((uint32_t)(h[3] & 7) << 8) | h[4];
-                }
-                bpos += hb;
-                if ((uint64_t)left < ((uint64_t)dlen + glen + slen) * 8) { err = JXS_E_DEC_BITSTREAM; break; }
-                P.raw = raw;
-                P.spos = bpos * 8;
-                if (raw) {
-                    if (s_pkrb[k] > glen * 8) { err = JXS_E_DEC_BITSTREAM; break; }
-                    left -= (int64_t)glen * 8;
-                } else {
-                    left -= s_pksb[k];
-                    if (left < 0) { err = JXS_E_DEC_BITSTREAM; break; }
-                    left -= left & 7;
-                    bpos += (s_pksb[k] + 7) >> 3;
-                    left -= (int64_t)glen * 8;
-                    /* codeword ends are kept as 16-bit offsets in the sub-packet */
-                    if (glen * 8 > 65535u) { err = JXS_E_DEC_BITSTREAM; break; }
-                }
-                P.gpos = bpos * 8;
-                P.gbits = glen * 8;
-                bpos += glen;
-                P.dpos = bpos * 8;
-                P.dbits = dlen * 8;
-                bpos += dlen;
-                left -= (int64_t)dlen * 8;
-                P.sgpos = bpos * 8;
-                P.sgbits = slen * 8;
-                bpos += slen;
-                left -= (int64_t)slen * 8;
-                if (left < 0 || bpos > lead + total) { err = JXS_E_DEC_BITSTREAM; break; }
-                P.present = 1;
-                if (!raw) {
-                    P.nwords = (P.gbits + 31) >> 5;
-                    tw += P.nwords;
-                }
+                pk_header(pbuf + bpos, long_hdr, raw, dlen, glen, slen);
+                s_hpos[k] = bpos;
+                bpos += hb + (raw ? 0u : (s_pksb[k] + 7) >> 3) + glen + dlen + slen;
             }
-            s_tw = tw;
-            s_npk = npk_c;
+        }
+        err = __shfl_sync(FULL, err, 0);
+        uint32_t nwords = 0;
+        if (lane < (int)npk_c) {
+            UkPk& P = pk[lane];
+            P.present = 0;
+            P.gbits = P.dbits = P.ncoded = P.nzero = 0;
+            P.raw = 0;
+            if (!err && s_pknbl[lane]) {
+                uint32_t raw, dlen, glen, slen;
+                const uint32_t b = s_hpos[lane] + hb;
+                pk_header(pbuf + s_hpos[lane], long_hdr, raw, dlen, glen, slen);
+                uint32_t gp = b;
+                if (raw) {
+                    if (s_pkrb[lane] > glen * 8) err = JXS_E_DEC_BITSTREAM;
+                } else {
+                    gp += (s_pksb[lane] + 7) >> 3;
+                    /* codeword ends are kept as 16-bit offsets in the sub-packet */
+                    if (glen * 8 > 65535u) err = JXS_E_DEC_BITSTREAM;
+                }
+                if ((uint64_t)gp + glen + dlen + slen > pend_max) err = JXS_E_DEC_BITSTREAM;
+                P.raw = raw;
+                P.spos = b * 8;
+                P.gpos = gp * 8;
+                P.gbits = glen * 8;
+                P.dpos = (gp + glen) * 8;
+                P.dbits = dlen * 8;
+                P.sgpos = (gp + glen + dlen) * 8;
+                P.sgbits = slen * 8;
+                P.present = 1;
+                if (!raw) nwords = (P.gbits + 31) >> 5;
+            }
+        }
+        {
+            uint32_t tw;
+            const uint32_t wb = warp_excl_scan(nwords, &tw);
+            if (lane < (int)npk_c) {
+                pk[lane].wbase = wb;
+                pk[lane].nwords = nwords;
+            }
+            if (lane == 0) {
+                s_tw = tw;
+                s_npk = npk_c;
+            }
         }
         err = __reduce_or_sync(FULL, (uint32_t)err) ? JXS_E_DEC_BITSTREAM : 0;
         if (!err && __any_sync(FULL, vp_seen)) {
