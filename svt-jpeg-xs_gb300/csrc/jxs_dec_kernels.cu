@@ -304,6 +304,11 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
      * thread meanwhile stages this precinct kind's tables and the scalars
      * the parse needs, so that no single-warp phase waits on device memory */
     if (threadIdx.x == 0) {
+        /* the precinct's offset and length field are read in bounds before
+         * the frame status, so that the three loads do not wait in turn */
+        const uint32_t off = prec_off[p], phb = cfg->prec_hdr_bytes;
+        const bool inb = (uint64_t)off + phb <= bs_size;
+        const uint32_t lprc = inb ? ((uint32_t)bs[off] << 16) | ((uint32_t)bs[off + 1] << 8) | bs[off + 2] : 0u;
         int err = *(volatile int*)status; /* set: the precinct offsets could not be found */
         s_sc[0] = cfg->nbands_all;
         s_sc[1] = cfg->npk;
@@ -316,11 +321,9 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         s_sc[8] = cfg->rm;
         s_hasvp = 0;
         if (!err) {
-            const uint32_t off = prec_off[p], phb = cfg->prec_hdr_bytes;
-            if ((uint64_t)off + phb > bs_size) {
+            if (!inb) {
                 err = JXS_E_DEC_SHORT;
             } else {
-                const uint32_t lprc = ((uint32_t)bs[off] << 16) | ((uint32_t)bs[off + 1] << 8) | bs[off + 2];
                 s_total = phb + lprc;
                 s_lead = (uint32_t)((uintptr_t)(bs + off) & 15);
                 if (lprc > JXS_PREC_MAX_BYTES || s_total + 48 > cap_bytes) err = JXS_E_DEC_BITSTREAM;
