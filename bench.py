@@ -19,12 +19,14 @@ e2e    : the same metric through the public C API with host buffers (page-
 roofline: the dominant stage (per-stage CUDA-event times from a separate
          single-stream pass) against the measured HBM copy bandwidth; bytes
          are the algorithmic bytes of that stage.
-cpu_baseline: the CPU restatement of the reference algorithm (oracle) on the
-         host cores, a bounded sample of the same workload.
+cpu_baseline: the reference SVT-JPEG-XS library on the host cores (built from
+         its own C sources by build(); threads_num = cores, frames pipelined
+         through its public API), a bounded sample of the same workload;
+         cpu_baseline_port: this project's CPU restatement (the oracle) beside it.
 
---impl reference times the CPU codec on all host cores instead (the
-reference library itself cannot be built on the GPU host: its sources are not
-shipped there), printing the same metric.
+--impl reference times the reference library the same way on all host cores
+instead, printing the same metric (the oracle stands in only where the
+reference could not be built).
 """
 import argparse
 import gc
@@ -204,38 +206,140 @@ def cpu_codec_time(frames, params_kw, seconds, threads):
             return done, el
 
 
+def cpu_model():
+    try:
+        with open("/proc/cpuinfo") as fh:
+            txt = fh.read()
+        for key in ("model name", "CPU part", "Hardware"):
+            for line in txt.splitlines():
+                if line.startswith(key):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.processor() or platform.machine()
+
+
+class RefCodec:
+    """The reference SVT-JPEG-XS library (built from its own C sources into
+    oracle/_ref) driven through its public API like its sample applications:
+    one encoder and one decoder kept open, threads_num = the host's cores, the
+    frames of a step sent with blocking sends while results are collected, so
+    that they overlap in the reference's pipeline.  One step encodes F frames
+    and decodes their codestreams."""
+
+    def __init__(self, frames, threads):
+        import oracle_lib as O
+
+        self.O = O
+        self.frames = frames
+        self.threads = threads
+        self.rs = O.RefStream(O.make_params(W, H, DEPTH, 3, BPP, threads=threads))
+        self.outs = None
+
+    @staticmethod
+    def available():
+        import oracle_lib as O
+
+        return O.ref_available()
+
+    def step(self, base, F):
+        fr = [self.frames[(base + i) % len(self.frames)] for i in range(F)]
+        cs = self.rs.encode(fr)
+        if self.outs is None or len(self.outs) < F:
+            _, info = self.O.probe(cs[0])
+            self.outs = [self.O.alloc_planes(info) for _ in range(F)]
+        self.rs.decode(cs, self.outs[:F])
+        return cs
+
+    def check(self, base):
+        """Frame `base` of a fresh step against the oracle: the reference build
+        on this host must give the same codestream and planes."""
+        cs = self.step(base, 1)
+        err, want = self.O.oracle_encode(self.O.make_params(W, H, DEPTH, 3, BPP, threads=self.threads), self.frames[base])
+        assert err == 0 and np.array_equal(cs[0], want), "reference codestream differs from the oracle"
+        err, planes = self.O.oracle_decode(want, threads=self.threads)
+        assert err == 0 and all(np.array_equal(a, b) for a, b in zip(self.outs[0], planes)), \
+            "reference decode differs from the oracle"
+
+    def close(self):
+        self.rs.close()
+
+
+def reference_sample(frames, F, seconds, threads):
+    """The reference codec on `threads` host cores: steps of F frames until
+    `seconds` elapse (at least 2 steps).  Returns (frames, wall seconds)."""
+    rc = RefCodec(frames, threads)
+    rc.check(0)
+    rc.step(0, F)  # warm-up: worker threads started, buffers touched
+    done, s = 0, 0
+    t0 = time.perf_counter()
+    while True:
+        rc.step(s * F, F)
+        done += F
+        s += 1
+        el = time.perf_counter() - t0
+        if s >= 2 and el >= seconds:
+            rc.close()
+            return done, el
+
+
 def run_reference(args, rank, world):
-    """CPU arm: the CPU codec on all host cores, one frame encoded and decoded
-    per step (a bounded sample of the workload); rank 0 only."""
+    """CPU arm: the reference library on all host cores through its public
+    API, each step F frames encoded and decoded (pipelined); rank 0 only.
+    Where the reference could not be built, the oracle stands in (kind
+    "port")."""
     if rank != 0:
         return
     import oracle_lib as O
 
     O.build_oracle()
-    frames = make_frames(2)
     threads = os.cpu_count() or 1
-    p = O.make_params(W, H, DEPTH, 3, BPP, threads=threads)
+    F = args.frames
+    frames = make_frames(max(2, min(F, 4)))
+    kind = "reference" if RefCodec.available() else "port"
+    if kind == "reference":
+        rc = RefCodec(frames, threads)
+        rc.check(0)
+        # steps of F frames, fewer where the whole run would exceed about
+        # three minutes of CPU time
+        t0 = time.perf_counter()
+        rc.step(0, F)
+        per_frame_s = (time.perf_counter() - t0) / F
+        per_step = max(1, min(F, int(180.0 / (max(1, args.steps + args.warmup) * per_frame_s))))
 
-    def one(i):
-        err, bs = O.oracle_encode(p, frames[i % len(frames)])
-        assert err == 0
-        err, _ = O.oracle_decode(bs, threads=threads)
-        assert err == 0
+        def one(i):
+            rc.step(i * per_step, per_step)
+        sample = ("%d frames encoded + decoded per step by the reference SVT-JPEG-XS library (portable C path, built "
+                  "from its own sources on this host) through its public API, threads_num = %d, frames pipelined"
+                  % (per_step, threads))
+    else:
+        p = O.make_params(W, H, DEPTH, 3, BPP, threads=threads)
 
+        def one(i):
+            err, bs = O.oracle_encode(p, frames[i % len(frames)])
+            assert err == 0
+            err, _ = O.oracle_decode(bs, threads=threads)
+            assert err == 0
+        per_step = 1
+        sample = ("1 frame encoded + decoded per step on all host cores with the CPU restatement of the reference "
+                  "algorithm (the reference library could not be built on this host)")
     for i in range(args.warmup):
         one(i)
     t0 = time.perf_counter()
     for i in range(args.steps):
         one(i)
     el = time.perf_counter() - t0
-    gpix = args.steps * W * H / el / 1e9
+    if kind == "reference":
+        rc.close()
+    gpix = args.steps * per_step * W * H / el / 1e9
     line = {"impl": "reference", "metric": METRIC, "value": gpix, "unit": "Gpix/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded, integer-only generator; no dataset)",
-            "config": {"workload": WORKLOAD, "frames_per_step": 1, "threads": threads},
-            "cpu_baseline": {"value": gpix, "unit": "Gpix/s", "cores": threads, "kind": "port",
-                             "sample": "1 frame encoded + decoded per step on all host cores with the CPU restatement of "
-                                       "the reference algorithm (the reference sources are not present on this host)"},
+            "config": {"workload": WORKLOAD, "frames_per_step": per_step, "threads": threads, "cpu": cpu_model()},
+            "cpu_baseline": {"value": gpix, "unit": "Gpix/s", "cores": threads, "kind": kind, "sample": sample,
+                             "cpu": cpu_model()},
             "e2e": {"value": gpix, "unit": "Gpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -579,13 +683,23 @@ def run_ours(args, rank, world, local):
     achieved = kb[dom] / (kern_ms[dom] / 1e3) / 1e9
     pipeline_gbs = (in_bytes + lcod + lcod + out_bytes) / ((sum(stages.values()) / nfr) / 1e3) / 1e9
 
-    # ---- CPU baseline (oracle on the host cores), rank 0 only
-    cpu = None
+    # ---- CPU baseline, rank 0 only: the reference library on the host
+    # cores through its public API (a bounded sample), and the oracle beside it
+    cpu = cpu_port = None
     if rank == 0 and args.cpu_seconds > 0:
         threads = os.cpu_count() or 1
-        n, el = cpu_codec_time(frames[:4], {}, args.cpu_seconds, threads)
-        cpu = {"value": n * W * H / el / 1e9, "unit": "Gpix/s", "cores": threads, "kind": "port",
-               "sample": "%d frames encoded + decoded (%.1f s) with the CPU restatement of the reference algorithm" % (n, el)}
+        if RefCodec.available():
+            n, el = reference_sample(frames[:4], F, args.cpu_seconds, threads)
+            cpu = {"value": n * W * H / el / 1e9, "unit": "Gpix/s", "cores": threads, "kind": "reference",
+                   "cpu": cpu_model(),
+                   "sample": "%d frames encoded + decoded (%.1f s) by the reference SVT-JPEG-XS library (portable C path) "
+                             "through its public API, threads_num = %d, %d frames pipelined per step" % (n, el, threads, F)}
+        n, el = cpu_codec_time(frames[:4], {}, args.cpu_seconds / 2, threads)
+        cpu_port = {"value": n * W * H / el / 1e9, "unit": "Gpix/s", "cores": threads, "kind": "port",
+                    "sample": "%d frames encoded + decoded (%.1f s) with the CPU restatement of the reference algorithm"
+                              % (n, el)}
+        if cpu is None:
+            cpu, cpu_port = cpu_port, None
 
     # per frame: 2 vertical + 1 horizontal transform, rate control, pack;
     # 2 precinct walks (device codestreams), unpack, 1 horizontal + 2 vertical inverse
@@ -614,6 +728,7 @@ def run_ours(args, rank, world, local):
                     "last_batch_gpu_ms": {"encode": bat["enc_batch_gpu_ms"], "decode": bat["dec_batch_gpu_ms"]}},
         "headline_path": "batched" if head_batched else "per_frame",
         "cpu_baseline": cpu,
+        "cpu_baseline_port": cpu_port,
         "clocks": head_clk,
         "clocks_other_path": clk if head_batched else clk_b,
         "gpu_launches": (bat["launches_per_step"] if head_batched else launches_per_frame * F) * args.steps,

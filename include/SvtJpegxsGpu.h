@@ -81,7 +81,9 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_encoder_rc_results(svt_jpeg_xs_enco
  *   - calls are serialised process-wide, because overlapping walks would
  *     race on the shared scratch;
  *   - the first call on a device resolves the scratch's address and may load
- *     the module, so make it before any stream capture begins.
+ *     the module, so make it before any stream capture begins;
+ *   - the decoder and dev_bitstream must be on the current device, which
+ *     must be the decoder's; otherwise SvtJxsErrorDecoderInvalidPointer.
  * precinct_offsets may be NULL. Otherwise precinct_capacity must be at least
  * the frame's precinct count, and the offsets are written there. The call
  * runs on cuda_stream (NULL: the default stream) and returns when the results

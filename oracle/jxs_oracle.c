@@ -1,9 +1,9 @@
 /*
  * CPU restatement of the SVT-JPEG-XS (ISO/IEC 21122 JPEG XS) encode/decode
  * path.  TEST INFRASTRUCTURE ONLY: the oracle that the GPU product is checked
- * against, and the CPU baseline that bench.py times.  It is pinned against the
- * reference library built from the reference's own sources (oracle/_ref,
- * tests/test_oracle_pin.py) and against tests/golden/.
+ * against, and the CPU restatement bench.py times beside the reference library.
+ * It is pinned against the reference library built from the reference's own
+ * sources (oracle/_ref, tests/test_oracle.py) and against tests/golden/.
  *
  * The reference pipelines its transform precinct by precinct with line
  * buffers; this restatement transforms whole components at once, which the
@@ -12,11 +12,14 @@
  * Everything else follows the reference's integer steps one to one; each
  * function names the reference lines it restates.
  *
- * Scope: every option the reference encoder emits with vertical prediction off
- * and sign handling off (deadzone/uniform quantisation, significance on/off,
- * rate-control modes 0 and 1, all colour formats, decomp_v 0-2, decomp_h
- * 0-5); the decoder additionally reads raw-mode packets and vertically
- * predicted GCLIs with either run mode.
+ * Scope: every option the reference encoder emits: deadzone / uniform
+ * quantisation, significance on/off, rate-control modes 0-3, sign handling
+ * (fast and full), vertical prediction (modes 1 and 2), all colour formats,
+ * decomp_v 0-2, decomp_h 0-5.  The decoder also reads what the reference
+ * decoder reads beyond that: raw-mode packets, multi-column precincts
+ * (Cw > 0), the reversible colour transform and Star-Tetrix, the NLT
+ * marker's output non-linearities and proxy resolutions; the encoder writes
+ * those forms too, to make test codestreams for them.
  */
 #include "jxs_oracle.h"
 

@@ -13,8 +13,10 @@
  * aliases planes 1 and 2 to plane 0, which the packed path never reads
  * (Source/Lib/Encoder/Codec/GcStageProcess.c:427-660).
  */
+#include <pthread.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "SvtJpegxsEnc.h"
@@ -160,4 +162,181 @@ int ref_decode_proxy(const uint8_t* bs, uint32_t size, void* const planes[4], co
 /* Decodes one frame into caller planes (stride = component width). */
 int ref_decode(const uint8_t* bs, uint32_t size, void* const planes[4], const uint32_t alloc_sizes[4], uint32_t threads_num) {
     return ref_decode_proxy(bs, size, planes, alloc_sizes, threads_num, 0);
+}
+
+/* ------------------------------------------------------------------------
+ * Streaming throughput of the reference codec, driven the way its sample
+ * applications drive it (Source/App/EncApp/EncAppMain.c:97-170 and the
+ * decoder app): one encoder and one decoder handle kept open across calls,
+ * threads_num worker threads each (--lp), a sender thread that submits
+ * frames with blocking send_picture / send_frame while the calling thread
+ * collects the results with blocking get_packet / get_frame, so that several
+ * frames are in the reference's pipeline at once.  bench.py times these calls
+ * as the CPU baseline.
+ * ------------------------------------------------------------------------ */
+typedef struct ref_stream {
+    svt_jpeg_xs_encoder_api_t enc;
+    svt_jpeg_xs_decoder_api_t dec;
+    svt_jpeg_xs_image_config_t dcfg;
+    int enc_open, dec_open, packed;
+} ref_stream_t;
+
+/* Opens the encoder with the given parameters; the decoder is opened on the
+ * first ref_stream_decode call, from that call's first codestream. */
+void* ref_stream_open(const ref_enc_params_t* p, int* err) {
+    ref_stream_t* s = (ref_stream_t*)calloc(1, sizeof(*s));
+    if (!s) {
+        *err = (int)SvtJxsErrorInsufficientResources;
+        return NULL;
+    }
+    SvtJxsErrorType_t e = svt_jpeg_xs_encoder_load_default_parameters(SVT_JPEGXS_API_VER_MAJOR, SVT_JPEGXS_API_VER_MINOR, &s->enc);
+    if (!e) {
+        s->enc.source_width = p->width;
+        s->enc.source_height = p->height;
+        s->enc.input_bit_depth = (uint8_t)p->bit_depth;
+        s->enc.colour_format = (ColourFormat_t)p->colour_format;
+        s->enc.bpp_numerator = p->bpp_num;
+        s->enc.bpp_denominator = p->bpp_den;
+        s->enc.ndecomp_v = p->decomp_v;
+        s->enc.ndecomp_h = p->decomp_h;
+        s->enc.quantization = p->quantization;
+        s->enc.slice_height = p->slice_height;
+        s->enc.rate_control_mode = p->rate_control_mode;
+        s->enc.coding_significance = p->coding_significance;
+        s->enc.coding_signs_handling = p->coding_signs_handling;
+        s->enc.coding_vertical_prediction_mode = p->coding_vertical_prediction_mode;
+        s->enc.threads_num = p->threads_num;
+        s->enc.verbose = 0;
+        e = svt_jpeg_xs_encoder_init(SVT_JPEGXS_API_VER_MAJOR, SVT_JPEGXS_API_VER_MINOR, &s->enc);
+    }
+    if (e) {
+        free(s);
+        *err = (int)e;
+        return NULL;
+    }
+    s->enc_open = 1;
+    s->packed = p->colour_format == COLOUR_FORMAT_PACKED_YUV444_OR_RGB;
+    s->dec.threads_num = p->threads_num;
+    *err = 0;
+    return s;
+}
+
+void ref_stream_close(void* h) {
+    ref_stream_t* s = (ref_stream_t*)h;
+    if (!s) return;
+    if (s->enc_open) svt_jpeg_xs_encoder_close(&s->enc);
+    if (s->dec_open) svt_jpeg_xs_decoder_close(&s->dec);
+    free(s);
+}
+
+typedef struct stream_job {
+    ref_stream_t* s;
+    uint32_t n;
+    svt_jpeg_xs_frame_t* frames;
+    int decode;
+    SvtJxsErrorType_t err;
+} stream_job_t;
+
+static void* stream_sender(void* arg) {
+    stream_job_t* j = (stream_job_t*)arg;
+    for (uint32_t i = 0; i < j->n && !j->err; i++) {
+        j->err = j->decode ? svt_jpeg_xs_decoder_send_frame(&j->s->dec, &j->frames[i], 1)
+                           : svt_jpeg_xs_encoder_send_picture(&j->s->enc, &j->frames[i], 1);
+    }
+    return NULL;
+}
+
+/* Runs n prepared frames through the encoder (decode = 0) or the decoder;
+ * frame i carries i + 1 as its user context.  done[i] receives the output
+ * size (encode: codestream bytes) or 1 (decode).  Returns 0 or the first
+ * error. */
+static int stream_run(ref_stream_t* s, uint32_t n, svt_jpeg_xs_frame_t* frames, int decode, uint32_t* done) {
+    stream_job_t j = {s, n, frames, decode, SvtJxsErrorNone};
+    pthread_t th;
+    if (pthread_create(&th, NULL, stream_sender, &j)) return (int)SvtJxsErrorInsufficientResources;
+    int err = 0;
+    for (uint32_t got = 0; got < n;) {
+        svt_jpeg_xs_frame_t res;
+        memset(&res, 0, sizeof(res));
+        SvtJxsErrorType_t e = decode ? svt_jpeg_xs_decoder_get_frame(&s->dec, &res, 1)
+                                     : svt_jpeg_xs_encoder_get_packet(&s->enc, &res, 1);
+        if (e == SvtJxsErrorNoErrorEmptyQueue) continue;
+        if (e != SvtJxsErrorNone) {
+            err = (int)e;
+            break;
+        }
+        const uintptr_t idx = (uintptr_t)res.user_prv_ctx_ptr;
+        if (idx >= 1 && idx <= n) done[idx - 1] = decode ? 1u : res.bitstream.used_size;
+        got++;
+    }
+    pthread_join(th, NULL);
+    if (!err && j.err) err = (int)j.err;
+    return err;
+}
+
+/* Encodes n frames: planes[4 i + c] is plane c of frame i (packed formats:
+ * plane 0 only), codestream i goes to out + i * out_cap; sizes[i] receives
+ * its length. */
+int ref_stream_encode(void* h, uint32_t n, void* const* planes, const uint32_t strides[4], const uint32_t alloc_sizes[4],
+                      uint8_t* out, uint32_t out_cap, uint32_t* sizes) {
+    ref_stream_t* s = (ref_stream_t*)h;
+    svt_jpeg_xs_frame_t* fr = (svt_jpeg_xs_frame_t*)calloc(n ? n : 1, sizeof(*fr));
+    if (!fr) return (int)SvtJxsErrorInsufficientResources;
+    for (uint32_t i = 0; i < n; i++) {
+        for (int c = 0; c < 4; c++) {
+            const int src = s->packed ? 0 : c;
+            fr[i].image.data_yuv[c] = planes[4 * i + src];
+            fr[i].image.stride[c] = strides[src];
+            fr[i].image.alloc_size[c] = alloc_sizes[src];
+        }
+        fr[i].bitstream.buffer = out + (size_t)i * out_cap;
+        fr[i].bitstream.allocation_size = out_cap;
+        fr[i].user_prv_ctx_ptr = (void*)(uintptr_t)(i + 1);
+        sizes[i] = 0;
+    }
+    const int err = stream_run(s, n, fr, 0, sizes);
+    free(fr);
+    return err;
+}
+
+/* Decodes n codestreams (bs[i], sizes[i]) into planes[4 i + c] (stride =
+ * component width, alloc_sizes[c] bytes each). */
+int ref_stream_decode(void* h, uint32_t n, const uint8_t* const* bs, const uint32_t* sizes, void* const* planes,
+                      const uint32_t alloc_sizes[4]) {
+    ref_stream_t* s = (ref_stream_t*)h;
+    if (!n) return 0;
+    if (!s->dec_open) {
+        s->dec.use_cpu_flags = 0;
+        s->dec.verbose = 0;
+        s->dec.packetization_mode = 0;
+        s->dec.proxy_mode = proxy_mode_full;
+        SvtJxsErrorType_t e = svt_jpeg_xs_decoder_init(SVT_JPEGXS_API_VER_MAJOR, SVT_JPEGXS_API_VER_MINOR, &s->dec, bs[0], sizes[0],
+                                                       &s->dcfg);
+        if (e) return (int)e;
+        s->dec_open = 1;
+    }
+    svt_jpeg_xs_frame_t* fr = (svt_jpeg_xs_frame_t*)calloc(n, sizeof(*fr));
+    uint32_t* done = (uint32_t*)calloc(n, sizeof(uint32_t));
+    if (!fr || !done) {
+        free(fr);
+        free(done);
+        return (int)SvtJxsErrorInsufficientResources;
+    }
+    for (uint32_t i = 0; i < n; i++) {
+        for (int c = 0; c < s->dcfg.components_num; c++) {
+            fr[i].image.data_yuv[c] = planes[4 * i + c];
+            fr[i].image.stride[c] = s->dcfg.components[c].width;
+            fr[i].image.alloc_size[c] = alloc_sizes[c];
+        }
+        fr[i].bitstream.buffer = (uint8_t*)bs[i];
+        fr[i].bitstream.allocation_size = sizes[i];
+        fr[i].bitstream.used_size = sizes[i];
+        fr[i].user_prv_ctx_ptr = (void*)(uintptr_t)(i + 1);
+    }
+    int err = stream_run(s, n, fr, 1, done);
+    for (uint32_t i = 0; i < n && !err; i++)
+        if (!done[i]) err = (int)SvtJxsErrorUndefined;
+    free(fr);
+    free(done);
+    return err;
 }

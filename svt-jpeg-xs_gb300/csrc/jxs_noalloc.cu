@@ -33,9 +33,18 @@
  * rejected before any launch, with SvtJxsErrorBadParameter and a message on
  * stderr.
  *
- * The host side takes the scratch's address once per device with
- * cudaGetSymbolAddress. That first call may load the module, so the first
- * call on a device should come before any stream capture starts.
+ * The host side takes the scratch's address with cudaGetSymbolAddress, with
+ * the device current. The first call on a device may load the module, so it
+ * should come before any stream capture starts. The address is looked up
+ * again on every call rather than cached: after cudaDeviceReset, or once the
+ * primary context has been destroyed and created again, the array lives at a
+ * new address, and a cached one could point into some other allocation. The
+ * lookup itself allocates nothing.
+ *
+ * The decoder handle's configuration and the codestream must both be in the
+ * memory of the current device, which must be the decoder's device; a
+ * pointer on another device is refused with SvtJxsErrorDecoderInvalidPointer
+ * before anything is launched.
  *
  * Overlapping calls would race on the shared scratch: two walks in flight at
  * once would write the same words. Every call therefore holds one
@@ -55,7 +64,6 @@
 
 #define NOALLOC_HEAD_WORDS 64u
 #define NOALLOC_MAX_PRECINCTS 4096u
-#define NOALLOC_MAX_DEVICES 64
 #define NOALLOC_THREADS 256
 
 static __device__ __align__(256) uint32_t noalloc_scratch[NOALLOC_HEAD_WORDS + NOALLOC_MAX_PRECINCTS];
@@ -132,7 +140,17 @@ __global__ void __launch_bounds__(NOALLOC_THREADS) locate_frame_kernel(const jxs
 }
 
 static std::mutex g_mu;
-static void* g_addr[NOALLOC_MAX_DEVICES];
+
+/* The device that owns device memory p, or -1 for host memory or an unknown
+ * pointer. */
+static int device_of(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) ? a.device : -1;
+}
 
 extern "C" int32_t jxs_gpu_dec_locate_noalloc(jxs_gpu_dec_t* d, const void* dev_bs, uint32_t size, uint32_t* frame_size,
                                               uint32_t* prec_off, uint32_t cap, void* stream) {
@@ -153,14 +171,22 @@ extern "C" int32_t jxs_gpu_dec_locate_noalloc(jxs_gpu_dec_t* d, const void* dev_
     }
     if (size < c->hdr_len) return JXS_E_DEC_SHORT;
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return JXS_E_UNDEFINED;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return JXS_E_UNDEFINED;
+    /* the kernel reads both, so both must be on the device it runs on */
+    if (device_of(dcfg) != dev || device_of(dev_bs) != dev) {
+        fprintf(stderr,
+                "svt_jpeg_xs_gpu_decoder_locate_frame: the decoder and the codestream must be on the current device (%d)\n",
+                dev);
+        return JXS_E_DEC_PTR;
+    }
     const cudaStream_t st = (cudaStream_t)stream;
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev] && cudaGetSymbolAddress(&g_addr[dev], noalloc_scratch) != cudaSuccess) {
-        g_addr[dev] = NULL;
+    void* addr = NULL;
+    if (cudaGetSymbolAddress(&addr, noalloc_scratch) != cudaSuccess || !addr) {
+        cudaGetLastError();
         return JXS_E_UNDEFINED;
     }
-    uint32_t* scratch = (uint32_t*)g_addr[dev];
+    uint32_t* scratch = (uint32_t*)addr;
     /* the stream's constant header must be the decoder's, Lcod aside */
     uint8_t hdr[sizeof(c->hdr)];
     if (cudaMemcpyAsync(hdr, dev_bs, c->hdr_len, cudaMemcpyDeviceToHost, st) != cudaSuccess ||

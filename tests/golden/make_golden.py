@@ -45,7 +45,7 @@ sys.path.insert(0, os.path.join(ROOT, "svt-jpeg-xs_gb300"))
 import jxs_synth as S  # noqa: E402
 import oracle_lib as O  # noqa: E402
 
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("JXS_REFERENCE", "/root/reference")
 
 # name: (w, h, depth, fmt, bpp_num, bpp_den, decomp_v, decomp_h, quant, slice_h, significance, rc_mode, seed)
 SMALL_CASES = {
@@ -87,6 +87,10 @@ FULL_CASES = {
     "c3_1080p_444_12b_bpp4": dict(w=1920, h=1080, d=12, fmt=S.FMT_YUV444, bpp=4, den=1, v=2, hh=5, seed=32, kind="frame"),
     "c3_2160p_rgb_8b_bpp2": dict(w=3840, h=2160, d=8, fmt=S.FMT_PACKED_RGB, bpp=2, den=1, v=2, hh=5, seed=33, kind="frame"),
     "c4_4320p_gbrp_14b_bpp1.5": dict(w=7680, h=4320, d=14, fmt=S.FMT_YUV444, bpp=3, den=2, v=1, hh=5, seed=4, kind="8k"),
+    # the three stream types of the serving workload
+    "c5_540i_422_10b_bpp5": dict(w=1920, h=540, d=10, fmt=S.FMT_YUV422, bpp=5, den=1, v=2, hh=5, seed=51, kind="frame"),
+    "c5_1080p_422_8b_bpp3": dict(w=1920, h=1080, d=8, fmt=S.FMT_YUV422, bpp=3, den=1, v=2, hh=5, seed=52, kind="frame"),
+    "c5_2160p_422_10b_bpp2": dict(w=3840, h=2160, d=10, fmt=S.FMT_YUV422, bpp=2, den=1, v=2, hh=5, seed=53, kind="frame"),
 }
 
 
@@ -299,6 +303,9 @@ def main():
     if "--signs-only" in sys.argv:
         make_signs()
         return
+    if "--full-only" in sys.argv:
+        make_full()
+        return
     make_vpred()
     make_signs()
     make_cw()
@@ -337,6 +344,12 @@ def main():
         arrays["dec%d" % i] = pl
     np.savez_compressed(os.path.join(HERE, "ref_sample_16x16.npz"), **arrays)
     print("ref sample", len(bs), "bytes, frame size", size.value)
+    make_full()
+
+
+def make_full():
+    """full_size.json: the reference's codestream and decode of every full-size
+    case, as SHA-256 hashes."""
     full = {}
     for name, c in FULL_CASES.items():
         planes = full_case_planes(c)

@@ -170,3 +170,60 @@ def ref_decode(bs, threads=1):
     buf = np.ascontiguousarray(bs, dtype=np.uint8)
     err = ref().ref_decode(buf.ctypes.data_as(ctypes.c_void_p), len(buf), ptrs, allocs, threads)
     return err & 0xffffffff, planes
+
+
+class RefStream:
+    """The reference codec kept open over a stream of frames and driven like
+    its sample applications (a sender thread with blocking sends, results
+    collected as they complete, threads_num workers): the CPU baseline that
+    bench.py times.  encode(frames) returns the codestreams (views into one
+    buffer that the next encode call overwrites); decode(codestreams, outs)
+    fills the preallocated planes."""
+
+    def __init__(self, params):
+        r = ref()
+        r.ref_stream_open.restype = ctypes.c_void_p
+        err = ctypes.c_int()
+        self.h = r.ref_stream_open(ctypes.byref(params), ctypes.byref(err))
+        if not self.h:
+            raise RuntimeError("ref_stream_open failed: 0x%x" % (err.value & 0xffffffff))
+        self.params = params
+        self.cap = max(params.width * params.height * 8, 1 << 16)
+        self._out = None
+
+    def encode(self, frames):
+        n = len(frames)
+        if self._out is None or self._out.size < n * self.cap:
+            self._out = np.zeros(n * self.cap, np.uint8)
+        ptrs = (ctypes.c_void_p * (4 * n))()
+        for i, planes in enumerate(frames):
+            for c, p in enumerate(planes):
+                ptrs[4 * i + c] = p.ctypes.data
+        _, strides, allocs = _plane_args(frames[0])
+        sizes = (ctypes.c_uint32 * n)()
+        err = ref().ref_stream_encode(ctypes.c_void_p(self.h), n, ptrs, strides, allocs,
+                                      self._out.ctypes.data_as(ctypes.c_void_p), self.cap, sizes)
+        if err:
+            raise RuntimeError("ref_stream_encode failed: 0x%x" % (err & 0xffffffff))
+        return [self._out[i * self.cap:i * self.cap + sizes[i]] for i in range(n)]
+
+    def decode(self, codestreams, outs):
+        """Decodes into the preallocated plane lists `outs` (one per codestream)."""
+        n = len(codestreams)
+        bufs = [np.ascontiguousarray(b, dtype=np.uint8) for b in codestreams]
+        bsp = (ctypes.c_void_p * n)(*[b.ctypes.data for b in bufs])
+        sizes = (ctypes.c_uint32 * n)(*[len(b) for b in bufs])
+        ptrs = (ctypes.c_void_p * (4 * n))()
+        for i, planes in enumerate(outs):
+            for c, p in enumerate(planes):
+                ptrs[4 * i + c] = p.ctypes.data
+        _, _, allocs = _plane_args(outs[0])
+        err = ref().ref_stream_decode(ctypes.c_void_p(self.h), n, bsp, sizes, ptrs, allocs)
+        if err:
+            raise RuntimeError("ref_stream_decode failed: 0x%x" % (err & 0xffffffff))
+        return outs
+
+    def close(self):
+        if self.h:
+            ref().ref_stream_close(ctypes.c_void_p(self.h))
+            self.h = None

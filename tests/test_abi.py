@@ -15,7 +15,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
-REF_API = "/root/reference/Source/API"
+REF_API = os.path.join(os.environ.get("JXS_REFERENCE", "/root/reference"), "Source", "API")
 
 
 def declared_functions():

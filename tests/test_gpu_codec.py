@@ -45,7 +45,8 @@ def test_golden_decode(gpu, name):
 
 @pytest.mark.parametrize("name", ["c1_1080p_422_8b_bpp5", "c2_2160p_422_10b_bpp3_f0", "c2_2160p_422_10b_bpp3_f1",
                                   "c3_720p_420_8b_bpp1", "c3_1080p_444_12b_bpp4", "c3_2160p_rgb_8b_bpp2",
-                                  "c4_4320p_gbrp_14b_bpp1.5"])
+                                  "c4_4320p_gbrp_14b_bpp1.5", "c5_540i_422_10b_bpp5", "c5_1080p_422_8b_bpp3",
+                                  "c5_2160p_422_10b_bpp2"])
 def test_full_size_against_reference_hashes(gpu, name):
     case = G.full_size()[name]
     planes = G.full_planes(case)
@@ -614,7 +615,12 @@ def test_multi_column_device_codestream(gpu):
         dec.close()
 
 
-@pytest.mark.parametrize("seed", range(24))
+# seeds whose random layout the oracle's encoder accepts (seeds 2, 3, 6, 15
+# and 26, 27 draw shapes with no valid multi-column layout), so every case runs
+MULTI_COLUMN_SEEDS = [0, 1, 4, 5, 7, 8, 9, 10, 11, 12, 13, 14, 16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 28, 29]
+
+
+@pytest.mark.parametrize("seed", MULTI_COLUMN_SEEDS)
 def test_multi_column_against_oracle(gpu, oracle, seed):
     """Random multi-column codestreams from the oracle's encoder (every
     rate-control mode, signs, vertical prediction): the GPU decode is
@@ -634,8 +640,7 @@ def test_multi_column_against_oracle(gpu, oracle, seed):
                            slice_height=sl, significance=int(rng.integers(0, 2)), rc_mode=seed % 4, signs=(seed // 4) % 3,
                            vpred=(seed // 2) % 3, cw=1 + seed % 3)
     err, bs = oracle.oracle_encode(p, planes)
-    if err:
-        pytest.skip("no valid multi-column layout for this shape (0x%x)" % err)
+    assert err == 0, hex(err)
     e2, want = oracle.oracle_decode(bs)
     assert e2 == 0
     dec = gpu.Decoder(bs)
@@ -673,7 +678,8 @@ def test_colour_transform_not_batched(gpu):
     dec.close()
 
 
-@pytest.mark.parametrize("seed", range(16))
+# seed 15 draws a budget the oracle's encoder cannot meet; 16 replaces it
+@pytest.mark.parametrize("seed", list(range(15)) + [16])
 def test_colour_transform_and_nlt_against_oracle(gpu, oracle, seed):
     rng = np.random.default_rng(950 + seed)
     fmt = [S.FMT_YUV444, S.FMT_PACKED_RGB, S.FMT_YUV422, S.FMT_YUV420][seed % 4]
@@ -692,8 +698,7 @@ def test_colour_transform_and_nlt_against_oracle(gpu, oracle, seed):
     p.nlt_t2 = p.nlt_t1 + int(rng.integers(1, 1 << 19))
     p.nlt_e = int(rng.integers(1, 6))
     err, bs = oracle.oracle_encode(p, planes)
-    if err:
-        pytest.skip("encode error 0x%x" % err)
+    assert err == 0, hex(err)
     e2, want = oracle.oracle_decode(bs)
     assert e2 == 0
     dec = gpu.Decoder(bs)
@@ -717,8 +722,7 @@ def test_star_tetrix_against_oracle(gpu, oracle, seed):
     p.cpih, p.cts_cf, p.cts_e1, p.cts_e2, p.cfa_type = 3, [0, 3][seed % 2], int(rng.integers(0, 4)), int(rng.integers(0, 4)), (seed // 2) % 2
     p.tnlt, p.nlt_alpha, p.nlt_t1, p.nlt_t2, p.nlt_e = (seed // 4) % 3, 500, 200000, 500000, 3
     err, bs = oracle.oracle_encode(p, planes)
-    if err:
-        pytest.skip("encode error 0x%x" % err)
+    assert err == 0, hex(err)
     e2, want = oracle.oracle_decode(bs)
     assert e2 == 0
     dec = gpu.Decoder(bs)

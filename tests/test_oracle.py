@@ -45,7 +45,8 @@ def test_oracle_decodes_reference_sample(oracle):
 
 
 @pytest.mark.parametrize("name", ["c1_1080p_422_8b_bpp5", "c2_2160p_422_10b_bpp3_f0", "c3_720p_420_8b_bpp1",
-                                  "c3_2160p_rgb_8b_bpp2"])
+                                  "c3_2160p_rgb_8b_bpp2", "c5_540i_422_10b_bpp5", "c5_1080p_422_8b_bpp3",
+                                  "c5_2160p_422_10b_bpp2"])
 def test_oracle_full_size_hashes(oracle, name):
     case = G.full_size()[name]
     planes = G.full_planes(case)
@@ -383,3 +384,27 @@ def test_oracle_star_tetrix_matches_reference_decoder(oracle, seed):
     e2, d_or = oracle.oracle_decode(bs)
     assert e1 == e2 == 0
     assert all(np.array_equal(a, b) for a, b in zip(d_ref, d_or))
+
+
+def test_reference_stream_driver_matches_single_frame_calls(oracle):
+    """The streaming driver bench.py times as the CPU baseline (one reference
+    encoder and decoder kept open, frames pipelined on worker threads) gives
+    the codestreams and planes of one-frame reference calls, in order, over
+    two calls in a row."""
+    if not oracle.ref_available():
+        pytest.skip("reference library not built")
+    w, h = 320, 96
+    frames = [S.frame(w, h, 10, S.FMT_YUV422, seed=40 + i) for i in range(5)]
+    rs = oracle.RefStream(oracle.make_params(w, h, 10, S.FMT_YUV422, 3, threads=4))
+    try:
+        for order in (frames, frames[::-1]):
+            cs = [c.copy() for c in rs.encode(order)]
+            outs = [oracle.alloc_planes(oracle.probe(c)[1]) for c in cs]
+            rs.decode(cs, outs)
+            for f, c, out in zip(order, cs, outs):
+                err, want = oracle.ref_encode(oracle.make_params(w, h, 10, S.FMT_YUV422, 3), f)
+                assert err == 0 and np.array_equal(c, want)
+                err, planes = oracle.ref_decode(want)
+                assert err == 0 and all(np.array_equal(a, b) for a, b in zip(out, planes))
+    finally:
+        rs.close()

@@ -19,9 +19,9 @@ W, H = 256, 64          # 4:2:2 8-bit, V2/H5: 30 bands, 16 precinct rows, 4 slic
 PREC_HDR_BYTES = (40 + 2 * 30 + 7) // 8
 
 
-def _encode(jxs, seed, w=W, h=H, **kw):
+def _encode(jxs, seed, w=W, h=H, bpp=3, **kw):
     planes = S.frame(w, h, 8, S.FMT_YUV422, seed=seed)
-    enc = jxs.Encoder(w, h, 8, S.FMT_YUV422, 3, **kw)
+    enc = jxs.Encoder(w, h, 8, S.FMT_YUV422, bpp, **kw)
     bs = enc.encode(planes)
     enc.close()
     return bs
@@ -108,4 +108,43 @@ def test_locate_frame_rejects_more_precincts_than_its_scratch(gpu):
     dev = torch.from_numpy(bs).cuda()
     r, size, _ = _locate(gpu, dec, dev.data_ptr(), dev.numel(), 0)
     assert r == gpu.E_BAD_PARAMETER and size == 0
+    dec.close()
+
+
+def test_locate_frame_walks_in_order_when_slices_are_elsewhere(gpu):
+    """A stream that differs from the decoder's only in Lcod (the same
+    settings at another bpp) has no slice where the decoder's constant-bit-rate
+    split puts it, so the one-thread walk from the header finds the precincts
+    instead; its size and offsets must still match the codestream."""
+    torch = pytest.importorskip("torch")
+    a, b = _encode(gpu, 11), _encode(gpu, 11, bpp=4)
+    assert len(b) != len(a)
+    dec = gpu.Decoder(a)
+    for bs in (b, a, b):
+        dev = torch.from_numpy(np.concatenate([bs, np.zeros(64, np.uint8)])).cuda()
+        r, size, offs = _locate(gpu, dec, dev.data_ptr(), dev.numel(), H // 4)
+        assert r == 0, hex(r)
+        assert size == _host_frame_size(gpu, bs) == len(bs)
+        want, end = _walk_precincts(bs)
+        assert end == size and offs == want
+    dec.close()
+
+
+def test_locate_frame_allocates_no_device_memory(gpu):
+    """After a first call (which loads the module and resolves the scratch's
+    address), further calls leave the device's free memory unchanged."""
+    torch = pytest.importorskip("torch")
+    a = _encode(gpu, 11)
+    dec = gpu.Decoder(a)
+    dev = torch.from_numpy(a).cuda()
+    r, _, _ = _locate(gpu, dec, dev.data_ptr(), dev.numel(), H // 4)
+    assert r == 0
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(8):
+        r, size, _ = _locate(gpu, dec, dev.data_ptr(), dev.numel(), H // 4)
+        assert r == 0 and size == len(a)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
     dec.close()
