@@ -7,8 +7,8 @@
  * IMTL plugins, applications) links against this library unchanged.  The
  * implementation behind it runs on one NVIDIA GB300 GPU.
  */
-#ifndef SVT_JPEGXS_H
-#define SVT_JPEGXS_H
+#ifndef _SVT_JPEG_XS_API_H_
+#define _SVT_JPEG_XS_API_H_
 
 #ifdef __cplusplus
 extern "C" {
@@ -154,4 +154,4 @@ typedef uint64_t CPU_FLAGS;
 }
 #endif
 
-#endif /* SVT_JPEGXS_H */
+#endif /* _SVT_JPEG_XS_API_H_ */

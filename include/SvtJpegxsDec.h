@@ -5,8 +5,8 @@
  * points below are ABI identical to the reference's Source/API/SvtJpegxsDec.h
  * (struct :16-57, functions :59-148).  Decoding runs on the GPU.
  */
-#ifndef SVT_JPEGXS_DEC_H
-#define SVT_JPEGXS_DEC_H
+#ifndef _SVT_JPEG_XS_API_DEC_H_
+#define _SVT_JPEG_XS_API_DEC_H_
 
 #ifdef __cplusplus
 extern "C" {
@@ -81,4 +81,4 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_decoder_send_eoc(svt_jpeg_xs_decoder_ap
 }
 #endif
 
-#endif /* SVT_JPEGXS_DEC_H */
+#endif /* _SVT_JPEG_XS_API_DEC_H_ */

@@ -7,8 +7,8 @@
  * runs on the GPU; the threading, queueing and callback behaviour of the
  * reference is kept (see each function).
  */
-#ifndef SVT_JPEGXS_ENC_H
-#define SVT_JPEGXS_ENC_H
+#ifndef _SVT_JPEG_XS_API_ENC_H_
+#define _SVT_JPEG_XS_API_ENC_H_
 
 #ifdef __cplusplus
 extern "C" {
@@ -93,4 +93,4 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_encoder_get_packet(svt_jpeg_xs_encoder_
 }
 #endif
 
-#endif /* SVT_JPEGXS_ENC_H */
+#endif /* _SVT_JPEG_XS_API_ENC_H_ */

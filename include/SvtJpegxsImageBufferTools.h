@@ -6,8 +6,8 @@
  * (:20-88).  Buffers come from page-locked host memory so that the GPU copies
  * them at full PCIe/C2C speed.
  */
-#ifndef SVT_JPEGXS_IMAGE_BUFFER_TOOLS_H
-#define SVT_JPEGXS_IMAGE_BUFFER_TOOLS_H
+#ifndef _SVT_JPEG_XS_API_IMAGE_BUFFER_TOOLS_H_
+#define _SVT_JPEG_XS_API_IMAGE_BUFFER_TOOLS_H_
 
 #include "SvtJpegxs.h"
 
@@ -51,4 +51,4 @@ PREFIX_API void svt_jpeg_xs_frame_pool_release(svt_jpeg_xs_frame_pool_t* frame_p
 }
 #endif
 
-#endif /* SVT_JPEGXS_IMAGE_BUFFER_TOOLS_H */
+#endif /* _SVT_JPEG_XS_API_IMAGE_BUFFER_TOOLS_H_ */

@@ -307,7 +307,7 @@ struct EncItem {
 struct DecItem {
     const jxs_cfg_t* c;
     const jxs_cfg_t* dcfg;
-    uint32_t cap_bytes, cap_groups;
+    uint32_t cap_bytes, cap_groups, cap_seg;
     const uint8_t* bs; /* device codestream */
     uint32_t size;
     int walk;          /* precinct offsets found on the GPU */
@@ -483,7 +483,7 @@ static int32_t plan_decode_chain(const std::vector<DecItem>& it, const std::vect
     for (int op = 0; op < 2; op++) {
         DecPrecLaunch* L = (DecPrecLaunch*)scratch.data();
         memset(L, 0, sizeof(*L));
-        uint32_t cb = 0, cg = 0;
+        uint32_t cb = 0, cg = 0, cs = 0;
         auto flush = [&]() {
             if (L->nframes) {
                 if (op == 0) {
@@ -492,11 +492,12 @@ static int32_t plan_decode_chain(const std::vector<DecItem>& it, const std::vect
                 } else {
                     /* one shared-memory layout for the launch: the largest
                      * precinct buffer that leaves room for the rest */
-                    const size_t fixed = (size_t)cg * 3 + 2 * (8 * JXS_MAXPK + 32) + 64;
-                    const size_t room = kSmemMax - 16 * 1024;
+                    const size_t fixed = uk_layout(0, cg, cs).end;
+                    const size_t room = kSmemMax - UK_STATIC_SMEM;
                     if (cb + fixed > room) cb = room > fixed + 4096 ? (uint32_t)(room - fixed) : 4096;
-                    if (L->nframes > 1) P->add(OP_UNPACK, 0, chain, L->nblocks, cb & ~15u, cg, L, sizeof(*L));
-                    else P->add(OP_UNPACK1, 0, chain, L->nblocks, cb & ~15u, cg, &L->job[0], sizeof(L->job[0]));
+                    /* the launch's segment capacity travels as the op's kind */
+                    if (L->nframes > 1) P->add(OP_UNPACK, (int)cs, chain, L->nblocks, cb & ~15u, cg, L, sizeof(*L));
+                    else P->add(OP_UNPACK1, (int)cs, chain, L->nblocks, cb & ~15u, cg, &L->job[0], sizeof(L->job[0]));
                 }
             }
             memset(L, 0, sizeof(*L));
@@ -519,6 +520,7 @@ static int32_t plan_decode_chain(const std::vector<DecItem>& it, const std::vect
             L->nslices += (int)d.c->nslices;
             cb = std::max(cb, d.cap_bytes);
             cg = std::max(cg, d.cap_groups);
+            cs = std::max(cs, d.cap_seg);
         }
         flush();
     }
@@ -612,7 +614,7 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         case OP_RC: e = jxs_launch_rc_batch((const EncPrecLaunch*)d, (int)o.b, s); break;
         case OP_PACK: e = jxs_launch_pack_batch((const EncPrecLaunch*)d, o.a, (int)o.b, s); break;
         case OP_WALK: e = jxs_launch_walk_batch((const DecPrecLaunch*)d, s); break;
-        case OP_UNPACK: e = jxs_launch_unpack_batch((const DecPrecLaunch*)d, o.a, o.b, s); break;
+        case OP_UNPACK: e = jxs_launch_unpack_batch((const DecPrecLaunch*)d, o.a, o.b, (uint32_t)o.kind, s); break;
         case OP_INV_H: e = jxs_launch_inv_h_batch((const InvHLaunchB*)d, o.kind, o.nblocks, s); break;
         case OP_INV_V: e = jxs_launch_inv_v_batch((const InvVLaunchB*)d, o.kind, o.nblocks, s); break;
         case OP_FWD_V_S: e = jxs_launch_fwd_v((const FwdVLaunch*)d, o.kind, (int)o.a, s); break;
@@ -627,7 +629,7 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         }
         case OP_PACK1: {
             const EncPrecFrame* F = (const EncPrecFrame*)d;
-            e = jxs_launch_pack(F->cfg, (uint32_t)o.nblocks, F->coef, F->gcli, F->rc, F->out, o.a, F->status, (int)o.b, s);
+            e = jxs_launch_pack(F->cfg, (uint32_t)o.nblocks, F->coef, F->gcli, F->rc, F->cost, F->out, o.a, F->status, (int)o.b, s);
             break;
         }
         case OP_WALK1: {
@@ -637,7 +639,8 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         }
         case OP_UNPACK1: {
             const DecPrecFrame* F = (const DecPrecFrame*)d;
-            e = jxs_launch_unpack(F->cfg, F->bs, F->bs_size, F->prec_off, F->coef, (uint32_t)o.nblocks, o.a, o.b, F->status, s);
+            e = jxs_launch_unpack(F->cfg, F->bs, F->bs_size, F->prec_off, F->coef, (uint32_t)o.nblocks, o.a, o.b, (uint32_t)o.kind,
+                                  F->status, s);
             break;
         }
         }
@@ -885,7 +888,7 @@ extern "C" uint64_t jxs_gpu_batch_enc_work_bytes(jxs_gpu_enc_t* e) {
 
 extern "C" uint64_t jxs_gpu_batch_dec_work_bytes(jxs_gpu_dec_t* d) {
     DecWork w;
-    const jxs_cfg_t* c = jxs_gpu_dec_info(d, nullptr, nullptr, nullptr);
+    const jxs_cfg_t* c = jxs_gpu_dec_info(d, nullptr, nullptr, nullptr, nullptr);
     return c ? round256(dec_work_layout(c, nullptr, &w)) : 0;
 }
 
@@ -999,7 +1002,7 @@ static int32_t ensure_enc(jxs_gpu_batch_t* b, uint32_t i, jxs_gpu_enc_t* e, cuda
 
 static int32_t ensure_dec(jxs_gpu_batch_t* b, uint32_t i, jxs_gpu_dec_t* d, cudaStream_t st) {
     if (b->dec.size() <= i) b->dec.resize(i + 1);
-    const jxs_cfg_t* c = jxs_gpu_dec_info(d, nullptr, nullptr, nullptr);
+    const jxs_cfg_t* c = jxs_gpu_dec_info(d, nullptr, nullptr, nullptr, nullptr);
     if (!c) return JXS_E_DEC_PTR;
     const uint64_t serial = jxs_gpu_dec_serial(d);
     DecWork& w = b->dec[i];
@@ -1146,8 +1149,8 @@ extern "C" int32_t jxs_gpu_batch_decode(jxs_gpu_batch_t* b, jxs_gpu_dec_t* const
     b->cfgs.assign(n, nullptr);
     for (uint32_t i = 0; i < n; i++) {
         const jxs_cfg_t* dcfg = nullptr;
-        uint32_t cb = 0, cg = 0;
-        const jxs_cfg_t* c = jxs_gpu_dec_info(dec[i], &dcfg, &cb, &cg);
+        uint32_t cb = 0, cg = 0, cs = 0;
+        const jxs_cfg_t* c = jxs_gpu_dec_info(dec[i], &dcfg, &cb, &cg, &cs);
         if (!c || !bs[i]) return JXS_E_DEC_PTR;
         /* colour transforms and non-linear outputs decode per frame only */
         if (dec_needs_nlt_pass(c)) return JXS_E_BAD_PARAM;
@@ -1165,6 +1168,7 @@ extern "C" int32_t jxs_gpu_batch_decode(jxs_gpu_batch_t* b, jxs_gpu_dec_t* const
         d.dcfg = dcfg;
         d.cap_bytes = cb;
         d.cap_groups = cg;
+        d.cap_seg = cs;
         d.w = &w;
         d.status = b->status_d + 2 * i;
         d.size = size[i];

@@ -81,7 +81,8 @@ void jxs_gpu_batch_info(jxs_gpu_batch_t* b, jxs_batch_info_t* info);
 /* Encoder / decoder handle internals the batch engine plans with. */
 const jxs_cfg_t* jxs_gpu_enc_info(jxs_gpu_enc_t* e, const jxs_cfg_t** dev_cfg, uint32_t* cap_words);
 uint64_t jxs_gpu_enc_serial(jxs_gpu_enc_t* e);
-const jxs_cfg_t* jxs_gpu_dec_info(jxs_gpu_dec_t* d, const jxs_cfg_t** dev_cfg, uint32_t* cap_bytes, uint32_t* cap_groups);
+const jxs_cfg_t* jxs_gpu_dec_info(jxs_gpu_dec_t* d, const jxs_cfg_t** dev_cfg, uint32_t* cap_bytes, uint32_t* cap_groups,
+                                  uint32_t* cap_seg);
 uint64_t jxs_gpu_dec_serial(jxs_gpu_dec_t* d);
 
 #ifdef __cplusplus

@@ -180,6 +180,23 @@ static inline JXS_HD int jxs_pkind(const jxs_cfg_t* c, uint32_t p) {
     return (row + 1 >= c->np ? 1 : 0) | (c->ncol > 1 && col + 1 == c->ncol ? 2 : 0);
 }
 
+/* The encoder's per-segment histograms, written by the rate control for
+ * packing (segments of at most 128 groups, so that every count fits a byte):
+ * 8 words per segment of every precinct row, after the rate-control tables
+ * (cost tables, exact-sign tables, vertical-prediction line tables).  Words
+ * 0-3: the segment's GCLI histogram, bin v in byte v & 3 of word v >> 2;
+ * words 4-7: its groups by the maximum GCLI of their significance group,
+ * same layout. */
+#define JXS_SEGHIST_WORDS 8
+static inline JXS_HD uint32_t jxs_seg_cap(const jxs_cfg_t* c) {
+    uint32_t n = 1;
+    for (int k = 0; k < 4; k++) n = c->nseg[k] > n ? c->nseg[k] : n;
+    return n;
+}
+static inline JXS_HD uint64_t jxs_seghist_word(const jxs_cfg_t* c) {
+    return (uint64_t)c->np * 1024 * (c->fs ? 2 : 1) + (c->vpred ? (uint64_t)c->np * 5 * JXS_MAXBLINES * 16 : 0);
+}
+
 int32_t jxs_cfg_geometry(jxs_cfg_t* cfg, int for_encoder, uint32_t nc, uint32_t W, uint32_t H, uint32_t dh, uint32_t dv,
                          uint32_t sd, const uint32_t sx[JXS_MAXC], const uint32_t sy[JXS_MAXC], uint32_t slice_h, uint32_t cw);
 int32_t jxs_sampling(uint32_t fmt, uint32_t* nc, uint32_t sx[JXS_MAXC], uint32_t sy[JXS_MAXC]);

@@ -21,7 +21,6 @@
 
 #define UK_THREADS 512
 #define UK_WARPS (UK_THREADS / 32)
-#define UK_ZCAP(cap_groups) ((cap_groups) + 8 * JXS_MAXPK + 32)
 #define FULL 0xffffffffu
 static_assert(JXS_MAXSEG <= UK_THREADS, "one thread per segment");
 
@@ -245,10 +244,10 @@ DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uin
 /* unpack_precinct (Packing.c:513-868) for one precinct row; vertical
  * prediction and separate sign sub-packets are rejected.
  *
- * Dynamic shared memory: [precinct bytes: cap_bytes + 32, stream byte i at
- * i + lead so that 16-byte chunks are aligned] [GCLI per group: cap_groups]
- * [every zero bit of the VLC sub-packets, as a 16-bit offset in its
- * sub-packet: 2 x UK_ZCAP(cap_groups)].
+ * Dynamic shared memory (uk_layout): [precinct bytes: cap_bytes + 32,
+ * stream byte i at i + lead so that 16-byte chunks are aligned] [GCLI per
+ * group: cap_groups] [every zero bit of the VLC sub-packets, as a 16-bit
+ * offset in its sub-packet] [the per-segment arrays, cap_seg segments].
  *
  *   copy    the precinct's bytes into shared memory;
  *   parse   thread 0: precinct header, packet headers, sub-packet positions
@@ -263,12 +262,13 @@ DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uin
  *           written as int16 coefficients (8 bytes per lane, coalesced). */
 __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs, uint32_t bs_size,
                                             const uint32_t* __restrict__ prec_off, int16_t* __restrict__ coef,
-                                            uint32_t cap_bytes, uint32_t cap_groups, int* status, const int p,
+                                            uint32_t cap_bytes, uint32_t cap_groups, uint32_t cap_seg, int* status, const int p,
                                             uint8_t* top_gcl, uint8_t* top_t, const int vp_ok) {
     extern __shared__ __align__(16) uint8_t dsm[];
+    const UkLayout UL = uk_layout(cap_bytes, cap_groups, cap_seg);
     uint8_t* pbuf = dsm;
-    uint8_t* gcl = dsm + cap_bytes + 32;
-    uint16_t* zend = (uint16_t*)(((uintptr_t)(gcl + cap_groups) + 15) & ~(uintptr_t)15);
+    uint8_t* gcl = dsm + UL.gcl;
+    uint16_t* zend = (uint16_t*)(dsm + UL.zend);
     /* zero bits: one per codeword plus up to 7 padding bits per packet */
     const uint32_t zcap = UK_ZCAP(cap_groups);
     __shared__ UkLine ln[JXS_MAXBLINES];
@@ -277,12 +277,18 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     __shared__ uint32_t s_pksb[JXS_MAXPK], s_pkrb[JXS_MAXPK], s_hpos[JXS_MAXPK];
     __shared__ uint32_t s_next[2]; /* segment queues of the two warp passes */
     /* this precinct kind's tables, staged from the configuration */
-    __shared__ jxs_seg_t s_seg[JXS_MAXSEG];
-    __shared__ uint16_t s_ord[JXS_MAXSEG];     /* work order of the segments */
+    /* this precinct kind's segments, their work order and per-segment sums
+     * (dynamic: sized for the launch's largest segment count) */
+    jxs_seg_t* s_seg = (jxs_seg_t*)(dsm + UL.seg);
+    uint16_t* s_ord = (uint16_t*)(dsm + UL.ord);
+    uint32_t* s_cnt = (uint32_t*)(dsm + UL.cnt);
+    uint32_t* s_base = (uint32_t*)(dsm + UL.base);
+    uint32_t* s_ex = (uint32_t*)(dsm + UL.ex);
+    uint32_t* s_nz = (uint32_t*)(dsm + UL.nz);  /* separate signs: per segment, count */
+    uint32_t* s_sgb = (uint32_t*)(dsm + UL.sgb); /* and first bit */
     __shared__ jxs_bline_t s_bl[JXS_MAXBLINES];
     __shared__ uint64_t s_crow[JXS_MAXBLINES]; /* per line: coefficient row offset */
     __shared__ uint8_t s_pkbl0[JXS_MAXPK], s_pknbl[JXS_MAXPK];
-    __shared__ uint32_t s_cnt[JXS_MAXSEG], s_base[JXS_MAXSEG], s_ex[JXS_MAXSEG + 1];
     __shared__ uint32_t ws[UK_WARPS];
     __shared__ int s_err;
     __shared__ uint32_t s_total, s_lead, s_tw, s_npk;
@@ -293,7 +299,6 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     __shared__ uint8_t s_topbl[JXS_MAXBLINES], s_topprev[JXS_MAXBLINES]; /* vertical prediction: the line above */
     __shared__ uint32_t s_topg[JXS_MAXBLINES];
     __shared__ int s_hasvp;
-    __shared__ uint32_t s_nz[JXS_MAXSEG], s_sgb[JXS_MAXSEG]; /* separate signs: per segment, count and first bit */
 
     /* the precinct kind's tables (last row / last of several columns) */
     const int last = jxs_pkind(cfg, (uint32_t)p);
@@ -987,20 +992,22 @@ DEV void walk_sequential(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __res
 /* ------------------------------------------------------------------------ */
 /* kernels: one frame, or a batch of frames                                  */
 /* ------------------------------------------------------------------------ */
-__global__ void __launch_bounds__(UK_THREADS) unpack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs,
-                                                            uint32_t bs_size, const uint32_t* __restrict__ prec_off,
-                                                            int16_t* __restrict__ coef, uint32_t cap_bytes, uint32_t cap_groups,
-                                                            int* status) {
-    unpack_body(cfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status, (int)blockIdx.x, nullptr, nullptr, 0);
+/* 4 blocks of 512 threads per SM where the shared memory allows it (32
+ * registers) */
+__global__ void __launch_bounds__(UK_THREADS, 4) unpack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs,
+                                                               uint32_t bs_size, const uint32_t* __restrict__ prec_off,
+                                                               int16_t* __restrict__ coef, uint32_t cap_bytes, uint32_t cap_groups,
+                                                               uint32_t cap_seg, int* status) {
+    unpack_body(cfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, cap_seg, status, (int)blockIdx.x, nullptr, nullptr, 0);
 }
 
-/* cap_bytes / cap_groups: the largest of the batch's frames (shared-memory
- * layout of the launch) */
-__global__ void __launch_bounds__(UK_THREADS) unpack_batch_kernel(const __grid_constant__ DecPrecLaunch L, uint32_t cap_bytes,
-                                                                  uint32_t cap_groups) {
+/* cap_bytes / cap_groups / cap_seg: the largest of the batch's frames
+ * (shared-memory layout of the launch) */
+__global__ void __launch_bounds__(UK_THREADS, 4) unpack_batch_kernel(const __grid_constant__ DecPrecLaunch L, uint32_t cap_bytes,
+                                                                     uint32_t cap_groups, uint32_t cap_seg) {
     const DecPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
-    unpack_body(F.cfg, F.bs, F.bs_size, F.prec_off, F.coef, cap_bytes, cap_groups, F.status, (int)blockIdx.x - F.first_block,
-                nullptr, nullptr, 0);
+    unpack_body(F.cfg, F.bs, F.bs_size, F.prec_off, F.coef, cap_bytes, cap_groups, cap_seg, F.status,
+                (int)blockIdx.x - F.first_block, nullptr, nullptr, 0);
 }
 
 /* Streams with vertical prediction: one block per slice, its precinct rows
@@ -1010,17 +1017,16 @@ __global__ void __launch_bounds__(UK_THREADS) unpack_batch_kernel(const __grid_c
 __global__ void __launch_bounds__(UK_THREADS) unpack_vpred_kernel(const jxs_cfg_t* __restrict__ cfg, const uint8_t* __restrict__ bs,
                                                                   uint32_t bs_size, const uint32_t* __restrict__ prec_off,
                                                                   int16_t* __restrict__ coef, uint32_t cap_bytes,
-                                                                  uint32_t cap_groups, int* status) {
+                                                                  uint32_t cap_groups, uint32_t cap_seg, int* status) {
     extern __shared__ __align__(16) uint8_t dsm[];
     __shared__ uint8_t top_t[JXS_MAXBLINES];
-    uint8_t* top_gcl = (uint8_t*)(((uintptr_t)(dsm + cap_bytes + 32 + cap_groups) + 15) & ~(uintptr_t)15) + 2 * UK_ZCAP(cap_groups);
-    top_gcl = (uint8_t*)(((uintptr_t)top_gcl + 15) & ~(uintptr_t)15);
+    uint8_t* top_gcl = dsm + uk_layout(cap_bytes, cap_groups, cap_seg).top;
     const uint32_t s = blockIdx.x, ncol = cfg->ncol;
     const uint32_t first = s * cfg->pps, end = min(cfg->np, first + cfg->pps);
     for (uint32_t col = 0; col < ncol; col++) {
         for (uint32_t row = first; row < end; row++) {
-            unpack_body(cfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status, (int)(row * ncol + col), top_gcl, top_t,
-                        row != first);
+            unpack_body(cfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, cap_seg, status, (int)(row * ncol + col), top_gcl,
+                        top_t, row != first);
             __syncthreads();
             if (*(volatile int*)status) return;
         }
@@ -1070,13 +1076,13 @@ extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, 
 }
 
 extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
-                                         int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status,
-                                         cudaStream_t st) {
-    const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 2ull * UK_ZCAP(cap_groups);
+                                         int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, uint32_t cap_seg,
+                                         int* status, cudaStream_t st) {
+    const size_t smem = uk_layout(cap_bytes, cap_groups, cap_seg).end;
     static std::atomic<int> attr[JXS_MAX_DEV];
     cudaError_t e = jxs_smem_attr(unpack_kernel, (int)smem, attr);
     if (e != cudaSuccess) return e;
-    unpack_kernel<<<np, UK_THREADS, smem, st>>>(dcfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status);
+    unpack_kernel<<<np, UK_THREADS, smem, st>>>(dcfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, cap_seg, status);
     return cudaGetLastError();
 }
 
@@ -1088,23 +1094,25 @@ extern "C" cudaError_t jxs_launch_walk_batch(const DecPrecLaunch* L, cudaStream_
     return cudaGetLastError();
 }
 
-extern "C" cudaError_t jxs_launch_unpack_batch(const DecPrecLaunch* L, uint32_t cap_bytes, uint32_t cap_groups, cudaStream_t st) {
-    const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 2ull * UK_ZCAP(cap_groups);
+extern "C" cudaError_t jxs_launch_unpack_batch(const DecPrecLaunch* L, uint32_t cap_bytes, uint32_t cap_groups, uint32_t cap_seg,
+                                               cudaStream_t st) {
+    const size_t smem = uk_layout(cap_bytes, cap_groups, cap_seg).end;
     static std::atomic<int> attr[JXS_MAX_DEV];
     cudaError_t e = jxs_smem_attr(unpack_batch_kernel, (int)smem, attr);
     if (e != cudaSuccess) return e;
     if (L->nblocks <= 0) return cudaSuccess;
-    unpack_batch_kernel<<<L->nblocks, UK_THREADS, smem, st>>>(*L, cap_bytes, cap_groups);
+    unpack_batch_kernel<<<L->nblocks, UK_THREADS, smem, st>>>(*L, cap_bytes, cap_groups, cap_seg);
     return cudaGetLastError();
 }
 
 extern "C" cudaError_t jxs_launch_unpack_vpred(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
-                                               int16_t* coef, uint32_t nslices, uint32_t cap_bytes, uint32_t cap_groups, int* status,
-                                               cudaStream_t st) {
-    const size_t smem = (size_t)cap_bytes + 32 + cap_groups + 16 + 2ull * UK_ZCAP(cap_groups) + 16 + cap_groups;
+                                               int16_t* coef, uint32_t nslices, uint32_t cap_bytes, uint32_t cap_groups,
+                                               uint32_t cap_seg, int* status, cudaStream_t st) {
+    const size_t smem = uk_layout(cap_bytes, cap_groups, cap_seg).top_end;
     static std::atomic<int> attr[JXS_MAX_DEV];
     cudaError_t e = jxs_smem_attr(unpack_vpred_kernel, (int)smem, attr);
     if (e != cudaSuccess) return e;
-    unpack_vpred_kernel<<<nslices, UK_THREADS, smem, st>>>(dcfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, status);
+    unpack_vpred_kernel<<<nslices, UK_THREADS, smem, st>>>(dcfg, bs, bs_size, prec_off, coef, cap_bytes, cap_groups, cap_seg,
+                                                           status);
     return cudaGetLastError();
 }

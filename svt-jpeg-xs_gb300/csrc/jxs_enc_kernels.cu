@@ -595,8 +595,10 @@ DEV uint32_t nz_levels(uint32_t m, uint32_t g, uint32_t uniform) {
  * row: rate_control_lut_fill, rate_control_calculate_band_best_method and
  * precinct_get_budget_bytes (RateControl.c:18-154, 457-781).
  *   histograms  warp per segment: GCLI histogram of every band line
- *               (warp-aggregated shared atomics), histogram of the maxima of
- *               full significance groups, maximum of the partial last group;
+ *               (warp-aggregated shared atomics) and the line's groups by
+ *               the maximum GCLI of their significance group; each segment's
+ *               own two histograms also go to device memory for packing
+ *               (segments of at most 128 groups);
  *   tables      thread per band line: for every gtli t, data bits, GCLI bits
  *               without significance and with it (suffix sums over the
  *               histogram); per band, significance coding at t only if
@@ -618,7 +620,7 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     extern __shared__ __align__(16) uint32_t rc_dyn[];
     uint32_t* s_area = VPRED ? rc_dyn : s_area_st;
     uint32_t(*hist)[16] = (uint32_t(*)[16])s_area;                          /* later: fast sign bits per t */
-    uint32_t(*shist)[16] = (uint32_t(*)[16])(s_area + JXS_MAXBLINES * 16);  /* later: full-sign cost changes */
+    uint32_t(*shist)[16] = (uint32_t(*)[16])(s_area + JXS_MAXBLINES * 16);  /* groups by significance-group maximum; later: full-sign cost changes */
     uint32_t(*tdat)[16] = (uint32_t(*)[16])(s_area + 2 * JXS_MAXBLINES * 16);
     uint32_t(*tnos)[16] = (uint32_t(*)[16])(s_area + 3 * JXS_MAXBLINES * 16);
     uint32_t(*tsig)[16] = (uint32_t(*)[16])(s_area + 4 * JXS_MAXBLINES * 16);
@@ -629,7 +631,6 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     /* SIGNS: the launch may hold frames with sign handling; VPRED: with
      * vertical prediction (compiled out otherwise) */
     const uint32_t fs = SIGNS ? cfg->fs : 0u, uniform = cfg->qpih;
-    __shared__ int pmax[JXS_MAXBLINES];
     __shared__ uint32_t cn[JXS_MAXBL][16], cs[JXS_MAXBL][16];
     __shared__ uint16_t meth[JXS_MAXBL];
     __shared__ uint8_t lgain[JXS_MAXBLINES], lprio[JXS_MAXBLINES], lfb[JXS_MAXBLINES];
@@ -681,14 +682,16 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     for (uint32_t x = threadIdx.x; x < nbl; x += blockDim.x) {
         const jxs_bline_t& B = cfg->bline[last][x];
         const jxs_band_t& bd = cfg->band[B.fb];
-        pmax[x] = -1;
         s_grow[x] = bd.gcli_off + (uint64_t)(p * bd.lines + B.line) * bd.gpitch;
     }
     __syncthreads();
 
     /* histograms: each lane 4 consecutive groups (one 4-byte load), 8-bit
      * counters packed four to a register, summed over the warp per 128
-     * groups (at most 128 per bin) */
+     * groups (at most 128 per bin); a segment of at most 128 groups also
+     * stores its own histograms for packing */
+    uint32_t* seghist = cost + jxs_seghist_word(cfg) + (uint64_t)p * jxs_seg_cap(cfg) * JXS_SEGHIST_WORDS;
+    const bool export_hist = SG <= 128;
     for (uint32_t sidx = warp; sidx < nseg; sidx += RC_WARPS) {
         const jxs_seg_t sg = segs[sidx];
         const uint32_t x = sg.bl;
@@ -712,28 +715,28 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
                 for (int r = 0; r < 4; r++) h[r] += (v >> 2) == (uint32_t)r ? inc : 0u;
                 if (k < (int)nv) m = max(m, v);
             }
-            /* significance group: 8 groups in lanes 2i, 2i+1 */
+            /* significance group: 8 groups in lanes 2i, 2i+1; its groups
+             * (8, or fewer at the end of a line) counted at its maximum */
             const uint32_t mx = max(m, __shfl_xor_sync(FULL, m, 1));
             const uint32_t nvp = nv + __shfl_xor_sync(FULL, nv, 1);
             uint32_t sh[4] = {0, 0, 0, 0};
             if (!(lane & 1) && nv) {
-                if (nvp == 8) {
-                    const uint32_t si = 1u << (8 * (mx & 3));
+                const uint32_t si = nvp << (8 * (mx & 3));
 #pragma unroll
-                    for (int r = 0; r < 4; r++) sh[r] += (mx >> 2) == (uint32_t)r ? si : 0u;
-                } else {
-                    pmax[x] = (int)mx; /* the partial last significance group of the line */
-                }
+                for (int r = 0; r < 4; r++) sh[r] += (mx >> 2) == (uint32_t)r ? si : 0u;
             }
+            uint32_t mine = 0;
 #pragma unroll
             for (int r = 0; r < 4; r++) {
                 const uint32_t hs = __reduce_add_sync(FULL, h[r]), ss = __reduce_add_sync(FULL, sh[r]);
+                mine = lane == r ? hs : (lane == 4 + r ? ss : mine);
                 if (lane < 4) {
                     const uint32_t c = (hs >> (8 * lane)) & 0xffu, cs2 = (ss >> (8 * lane)) & 0xffu;
                     if (c) atomicAdd(&hist[x][4 * r + lane], c);
                     if (cs2) atomicAdd(&shist[x][4 * r + lane], cs2);
                 }
             }
+            if (export_hist && lane < JXS_SEGHIST_WORDS) seghist[sidx * JXS_SEGHIST_WORDS + lane] = mine;
             if (fs) {
                 /* sign handling: the lane's 16 coefficients (inside the band
                  * width) by the number of gtli values at which they stay
@@ -770,7 +773,7 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     /* per band line and gtli t: data bits, GCLI bits without / with
      * significance coding */
     for (uint32_t x = threadIdx.x; x < nbl; x += blockDim.x) {
-        const uint32_t N = bls[x].gcli_w, partial = N & 7u;
+        const uint32_t N = bls[x].gcli_w;
         int S0 = 0, S1 = 0;
         uint32_t Z1 = 0;
         for (int t = 15; t >= 0; t--) {
@@ -790,13 +793,11 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
             S0 += (int)h;
             S1 += t * (int)h;
         }
-        uint32_t Z = 0;
-        const int pm = pmax[x];
+        uint32_t Z = 0; /* groups in significance groups whose maximum is <= t: no GCLI codes */
         const uint32_t fb = lfb[x];
         for (int t = 0; t < 16; t++) {
             Z += shist[x][t];
-            const uint32_t zer = 8 * Z + ((pm >= 0 && pm <= t) ? partial : 0u);
-            tsig[x][t] = tnos[x][t] - zer;
+            tsig[x][t] = tnos[x][t] - Z;
             atomicAdd(&cn[fb][t], tnos[x][t]);
             atomicAdd(&cs[fb][t], tsig[x][t] + lsig[x]);
         }
@@ -1041,7 +1042,11 @@ struct PkLine {
  * out + offset - lead + i, then copied out.  Band lines are split into
  * segments of seg_groups groups, one warp per segment:
  *   pass A  each segment's data bits, VLC bits and groups lying in
- *           insignificant significance groups, at the precinct's gtli;
+ *           insignificant significance groups, at the precinct's gtli: from
+ *           the segment's histograms that the rate control stored (thread
+ *           per segment), or, with sign handling, vertical prediction or
+ *           segments of more than 128 groups, from the GCLIs (warp per
+ *           segment);
  *   layout  warp 0, lanes over band lines, bands, packets: coding method per
  *           band (significance only if strictly cheaper), packet headers, raw
  *           fallback, packet positions by a warp scan, sub-packet positions,
@@ -1059,7 +1064,8 @@ struct PkLine {
 template <bool VPRED>
 __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
                                           const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
-                                          uint8_t* __restrict__ out, uint32_t cap_words, int* status, const int p) {
+                                          const uint32_t* __restrict__ cost, uint8_t* __restrict__ out, uint32_t cap_words,
+                                          int* status, const int p) {
     extern __shared__ __align__(16) uint32_t buf[];
     __shared__ uint32_t s_data[JXS_MAXSEG], s_vlc[JXS_MAXSEG], s_zero[JXS_MAXSEG], s_nz[JXS_MAXSEG];
     __shared__ PkLine pl[JXS_MAXBLINES];
@@ -1170,6 +1176,35 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
      * 128 groups per step; with sign handling also the non-zero quantized
      * coefficients, whose signs go to the sign sub-packets */
     const uint32_t fs = cfg->fs, uniform = cfg->qpih;
+    if (!VPRED && !fs && SG <= 128) {
+        /* from the rate control's histograms: data bits 4 (v - t + 1) and
+         * codes of v - t + 1 bits for groups with GCLI v > t, 1-bit codes
+         * for the others; no codes for the groups of significance groups
+         * whose maximum is <= t */
+        const uint32_t* hist = cost + jxs_seghist_word(cfg) + (uint64_t)p * jxs_seg_cap(cfg) * JXS_SEGHIST_WORDS;
+        for (uint32_t i = threadIdx.x; i < nseg; i += blockDim.x) {
+            const uint4 gh = __ldcg((const uint4*)(hist + i * JXS_SEGHIST_WORDS));
+            const uint4 zh = __ldcg((const uint4*)(hist + i * JXS_SEGHIST_WORDS + 4));
+            const uint32_t t = s_lt[segs[i].bl];
+            const uint32_t gw[4] = {gh.x, gh.y, gh.z, gh.w}, zw[4] = {zh.x, zh.y, zh.z, zh.w};
+            uint32_t d = 0, v = 0, z = 0;
+#pragma unroll
+            for (uint32_t b = 0; b < 16; b++) {
+                const uint32_t c = (gw[b >> 2] >> (8 * (b & 3))) & 255u, cz = (zw[b >> 2] >> (8 * (b & 3))) & 255u;
+                if (b > t) {
+                    d += (b - t + 1) * c;
+                    v += (b - t + 1) * c;
+                } else {
+                    v += c;
+                    z += cz;
+                }
+            }
+            s_data[i] = 4 * d;
+            s_vlc[i] = v;
+            s_zero[i] = z;
+            s_nz[i] = 0;
+        }
+    } else
     for (uint32_t qi = queue_next(&s_q[0], lane); qi < nseg; qi = queue_next(&s_q[0], lane)) {
         const uint32_t sidx = s_ord[qi];
         const jxs_seg_t sg = segs[sidx];
@@ -1643,14 +1678,15 @@ __global__ void __launch_bounds__(RC_THREADS, (SIGNS || VPRED) ? 3 : 4) rc_cost_
 template <bool VPRED>
 __global__ void __launch_bounds__(PK_THREADS, 4) pack_kernel(const jxs_cfg_t* __restrict__ cfg, const uint16_t* __restrict__ coef,
                                                           const uint8_t* __restrict__ gcli, const PrecRC* __restrict__ rc,
-                                                          uint8_t* __restrict__ out, uint32_t cap_words, int* status) {
-    pack_body<VPRED>(cfg, coef, gcli, rc, out, cap_words, status, (int)blockIdx.x);
+                                                          const uint32_t* __restrict__ cost, uint8_t* __restrict__ out,
+                                                          uint32_t cap_words, int* status) {
+    pack_body<VPRED>(cfg, coef, gcli, rc, cost, out, cap_words, status, (int)blockIdx.x);
 }
 
 template <bool VPRED>
 __global__ void __launch_bounds__(PK_THREADS, 4) pack_batch_kernel(const __grid_constant__ EncPrecLaunch L, uint32_t cap_words) {
     const EncPrecFrame& F = L.job[find_job<JXS_BATCH_FRAMES>(L.job, L.nframes, (int)blockIdx.x)];
-    pack_body<VPRED>(F.cfg, F.coef, F.gcli, F.rc, F.out, cap_words, F.status, (int)blockIdx.x - F.first_block);
+    pack_body<VPRED>(F.cfg, F.coef, F.gcli, F.rc, F.cost, F.out, cap_words, F.status, (int)blockIdx.x - F.first_block);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -1696,21 +1732,21 @@ extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_
 
 template <bool V>
 static cudaError_t pack_one(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli, const PrecRC* rc,
-                            uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st) {
+                            const uint32_t* cost, uint8_t* out, uint32_t cap_words, int* status, cudaStream_t st) {
     const size_t smem = (size_t)cap_words * 4;
     static std::atomic<int> attr[JXS_MAX_DEV];
     cudaError_t e = jxs_smem_attr(pack_kernel<V>, (int)smem, attr);
     if (e != cudaSuccess) return e;
-    pack_kernel<V><<<np, PK_THREADS, smem, st>>>(dcfg, coef, gcli, rc, out, cap_words, status);
+    pack_kernel<V><<<np, PK_THREADS, smem, st>>>(dcfg, coef, gcli, rc, cost, out, cap_words, status);
     return cudaGetLastError();
 }
 
 /* `modes` bit 1: a frame of the launch has vertical prediction */
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
-                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, int modes,
-                                       cudaStream_t st) {
-    if (modes & 2) return pack_one<true>(dcfg, np, coef, gcli, rc, out, cap_words, status, st);
-    return pack_one<false>(dcfg, np, coef, gcli, rc, out, cap_words, status, st);
+                                       const PrecRC* rc, const uint32_t* cost, uint8_t* out, uint32_t cap_words, int* status,
+                                       int modes, cudaStream_t st) {
+    if (modes & 2) return pack_one<true>(dcfg, np, coef, gcli, rc, cost, out, cap_words, status, st);
+    return pack_one<false>(dcfg, np, coef, gcli, rc, cost, out, cap_words, status, st);
 }
 
 extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, int modes, cudaStream_t st) {

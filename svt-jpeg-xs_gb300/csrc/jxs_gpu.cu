@@ -321,7 +321,7 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
     TMARK(3);
     const int out_dev = jxs_gpu_is_device_ptr(out);
     uint8_t* dst = out_dev ? out : s->out_stage;
-    CK(jxs_launch_pack(e->dcfg, c->np, s->coef, s->gcli, s->rc, dst, e->cap_words, s->status, c->vpred ? 2 : 0, st));
+    CK(jxs_launch_pack(e->dcfg, c->np, s->coef, s->gcli, s->rc, s->cost, dst, e->cap_words, s->status, c->vpred ? 2 : 0, st));
     KMARK();
     TMARK(4);
     if (!out_dev) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));
@@ -458,7 +458,7 @@ struct jxs_gpu_dec {
     jxs_cfg_t* dcfg;
     int nslots;
     DecSlot slot[8];
-    uint32_t cap_bytes, cap_groups;
+    uint32_t cap_bytes, cap_groups, cap_seg;
     cudaStream_t user_stream[8]; /* per slot; null: the slot's own stream */
     int timing;
     double stage_ms[DEC_STAGES];
@@ -570,16 +570,21 @@ extern "C" jxs_gpu_dec_t* jxs_gpu_dec_create(const jxs_cfg_t* cfg, int nslots, i
     for (uint32_t b = 0; b < cfg->nbands; b++) groups += cfg->band[b].gcli_w * cfg->band[b].lines;
     /* + up to 3 groups of alignment per band line (jxs_bline_t.gbase) */
     d->cap_groups = (groups + 3 * JXS_MAXBLINES + 64) & ~31u;
-    /* the on-chip copy of a precinct: constant-bit-rate streams give every
-     * slice its share of Lcod, so a precinct fits in a slice's share with
-     * margin; whatever does not fit is reported as an invalid stream */
-    const size_t fixed = (size_t)d->cap_groups * 3 + 2 * (8 * JXS_MAXPK + 32) + 64;
+    d->cap_seg = 1;
+    for (int k = 0; k < 4; k++) d->cap_seg = d->cap_seg > cfg->nseg[k] ? d->cap_seg : cfg->nseg[k];
+    /* the on-chip copy of a precinct: in a constant-bit-rate stream a
+     * precinct lies inside its slice, so it needs at most the largest slice
+     * budget (plus the 48 bytes the bit readers may look past its end and
+     * the alignment lead); without that prediction a quarter more than a
+     * slice's share of Lcod.  A precinct that does not fit is reported as an
+     * invalid stream. */
     uint64_t cap = (uint64_t)cfg->lcod / (cfg->nslices ? cfg->nslices : 1);
-    cap = (cfg->max_slice_budget ? cfg->max_slice_budget : cap + cap / 4) + 4096;
+    cap = cfg->max_slice_budget ? cfg->max_slice_budget + 64ull : cap + cap / 4 + 4096;
     if (cap > cfg->lcod + 64ull) cap = cfg->lcod + 64ull;
-    const size_t room = kSmemMax - 16 * 1024; /* static shared memory of the unpacking kernel */
+    const size_t fixed = uk_layout(0, d->cap_groups, d->cap_seg).top_end;
+    const size_t room = kSmemMax - UK_STATIC_SMEM;
     if (cap + fixed > room) cap = room > fixed + 4096 ? room - fixed : 4096;
-    d->cap_bytes = (uint32_t)cap & ~15u;
+    d->cap_bytes = (uint32_t)(cap + 15) & ~15u;
     if (cudaMalloc(&d->dcfg, sizeof(jxs_cfg_t)) != cudaSuccess ||
         cudaMemcpy(d->dcfg, cfg, sizeof(jxs_cfg_t), cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaGetLastError();
@@ -647,9 +652,11 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
     TMARK(1);
     KMARK();
     if (d->vpred)
-        CK(jxs_launch_unpack_vpred(d->dcfg, dbs, size, s->prec_off, s->coef, c->nslices, d->cap_bytes, d->cap_groups, s->status, st));
+        CK(jxs_launch_unpack_vpred(d->dcfg, dbs, size, s->prec_off, s->coef, c->nslices, d->cap_bytes, d->cap_groups, d->cap_seg,
+                                   s->status, st));
     else
-        CK(jxs_launch_unpack(d->dcfg, dbs, size, s->prec_off, s->coef, c->nprec, d->cap_bytes, d->cap_groups, s->status, st));
+        CK(jxs_launch_unpack(d->dcfg, dbs, size, s->prec_off, s->coef, c->nprec, d->cap_bytes, d->cap_groups, d->cap_seg, s->status,
+                             st));
     KMARK();
     TMARK(2);
 
@@ -839,11 +846,12 @@ extern "C" const jxs_cfg_t* jxs_gpu_enc_info(jxs_gpu_enc_t* e, const jxs_cfg_t**
 extern "C" uint64_t jxs_gpu_enc_serial(jxs_gpu_enc_t* e) { return e ? e->serial : 0; }
 
 extern "C" const jxs_cfg_t* jxs_gpu_dec_info(jxs_gpu_dec_t* d, const jxs_cfg_t** dev_cfg, uint32_t* cap_bytes,
-                                             uint32_t* cap_groups) {
+                                             uint32_t* cap_groups, uint32_t* cap_seg) {
     if (!d) return NULL;
     if (dev_cfg) *dev_cfg = d->dcfg;
     if (cap_bytes) *cap_bytes = d->cap_bytes;
     if (cap_groups) *cap_groups = d->cap_groups;
+    if (cap_seg) *cap_seg = d->cap_seg;
     return &d->cfg;
 }
 extern "C" uint64_t jxs_gpu_dec_serial(jxs_gpu_dec_t* d) { return d ? d->serial : 0; }

@@ -32,13 +32,28 @@
 
 DEV int32_t dq(int16_t c, int fq) { return (int32_t)((uint32_t)(int32_t)c << fq); }
 
-/* linear_output_scaling (NltDec.c:242-264) */
-DEV uint32_t out_sample(int32_t v, int bw, int depth) {
-    const int zeta = bw - depth;
-    long long t = (long long)v + (1 << (bw - 1));
-    t = (t + ((1ll << zeta) >> 1)) >> zeta;
-    const long long m = (1ll << depth) - 1;
-    return (uint32_t)(t > m ? m : (t < 0 ? 0 : t));
+/* linear_output_scaling (NltDec.c:242-264).  The reference adds 2^(Bw-1) in
+ * int32, then rounds (v + 2^(zeta-1)) >> zeta in int64 and clamps to
+ * [0, 2^d - 1].  With u = q 2^zeta + r (0 <= r < 2^zeta) the rounded value is
+ * q + ((r + 2^(zeta-1)) >> zeta), so everything stays in 32 bits; the
+ * constants of a launch are computed once (OutScale). */
+struct OutScale {
+    uint32_t half_bw, mask_z, half_z;
+    int zeta, m;
+};
+DEV OutScale out_scale(int bw, int depth) {
+    OutScale s;
+    s.zeta = bw - depth;
+    s.half_bw = (uint32_t)((1ull << bw) >> 1);
+    s.mask_z = (1u << s.zeta) - 1u;
+    s.half_z = (1u << s.zeta) >> 1;
+    s.m = (1 << depth) - 1;
+    return s;
+}
+DEV uint32_t out_sample(int32_t v, const OutScale& s) {
+    const int32_t u = (int32_t)((uint32_t)v + s.half_bw);
+    const int32_t t = (u >> s.zeta) + (int32_t)((((uint32_t)u & s.mask_z) + s.half_z) >> s.zeta);
+    return (uint32_t)min(max(t, 0), s.m);
 }
 
 /* One band row of int16 coefficients as int32 << fq; index i < width. */
@@ -100,7 +115,7 @@ DEV void warp_lift_inv(int j0, int npairs, int n1, int n2, S4 s4, D4 d4, S1 s1, 
 #define IH_MAX_WARPS 4
 
 template <int OUT>
-DEV void store_row8(const InvHJob& J, int row, int x0, int w, const int32_t* v, int bw, int depth) {
+DEV void store_row8(const InvHJob& J, int row, int x0, int w, const int32_t* v, const OutScale& os) {
     if (OUT == 0) {
         int32_t* dst = (int32_t*)J.dst + (long long)row * J.dst_pitch + x0;
         if (x0 + 7 < w) {
@@ -113,7 +128,7 @@ DEV void store_row8(const InvHJob& J, int row, int x0, int w, const int32_t* v, 
     } else {
         for (int q = 0; q < 8; q++) {
             if (x0 + q >= w) break;
-            const uint32_t o = out_sample(v[q], bw, depth);
+            const uint32_t o = out_sample(v[q], os);
             const long long idx = (long long)row * J.dst_pitch + x0 + q;
             if (OUT == 1) ((uint8_t*)J.dst)[idx] = (uint8_t)o;
             else ((uint16_t*)J.dst)[idx] = (uint16_t)o;
@@ -131,6 +146,7 @@ __global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_c
     const int row = (blockIdx.x - J.first_block) * L.rows_per_block + warp;
     if (row >= J.h) return;
     const int fq = J.fq;
+    const OutScale os = out_scale(J.bw, J.depth);
     int32_t* bufA = ism + warp * L.warp_words;
     int32_t* bufB = bufA + L.warp_words / 2;
     /* widths of every level's input, m[0] = row width */
@@ -148,7 +164,7 @@ __global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_c
             for (int x0 = 8 * (threadIdx.x & 31); x0 < w; x0 += 256) {
                 int32_t v[8];
                 for (int q = 0; q < 8; q++) v[q] = x0 + q < w ? dq(llr.row[x0 + q], fq) : 0;
-                store_row8<OUT>(J, row, x0, w, v, J.bw, J.depth);
+                store_row8<OUT>(J, row, x0, w, v, os);
             }
             break;
         }
@@ -181,7 +197,7 @@ __global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_c
         } else {
             warp_lift_inv(0, n1, n1, n2, s4, d4, s1, d1, [&](int j, const int32_t* xe, const int32_t* xo) {
                 const int32_t v[8] = {xe[0], xo[0], xe[1], xo[1], xe[2], xo[2], xe[3], xo[3]};
-                store_row8<OUT>(J, row, 2 * j, n, v, J.bw, J.depth);
+                store_row8<OUT>(J, row, 2 * j, n, v, os);
             });
         }
     }
@@ -279,6 +295,7 @@ __global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant
     if (2 * cp >= 2 * npairs) return;
     const int x = c0 + 2 * cp;
     const int rend = min(r0 + IV_ROWPAIRS, n1);
+    const OutScale os = out_scale(J.bw, J.depth);
 #define LV(i) (*(const int2*)&sx[(i) - r0][2 * cp])
 #define HV(i) (*(const int2*)&sx[IV_ROWPAIRS + 1 + ((i) - (r0 - 1))][2 * cp])
     int2 hp = n2 ? HV(r0 - 1) : make_int2(0, 0);
@@ -314,7 +331,7 @@ __global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant
             for (int rr = 0; rr < rows; rr++) {
                 const int2 v = rr ? xo : xe;
                 const long long idx = (long long)(y + rr) * J.dst_pitch + x;
-                const uint32_t a = out_sample(v.x, J.bw, J.depth), b = out_sample(v.y, J.bw, J.depth);
+                const uint32_t a = out_sample(v.x, os), b = out_sample(v.y, os);
                 if (OUT == 1) {
                     uint8_t* p = (uint8_t*)J.dst + idx;
                     if (two && J.vec) *(uint16_t*)p = (uint16_t)(a | (b << 8));

@@ -229,6 +229,48 @@ struct DecPrecLaunch {
     DecPrecFrame job[JXS_BATCH_FRAMES];
 };
 
+/* Dynamic shared memory of the unpacking kernels (jxs_dec_kernels.cu), laid
+ * out for the largest frame of a launch: the precinct's bytes (cap_bytes +
+ * 32), a GCLI per group (cap_groups), the zero-bit table (a 16-bit offset per
+ * zero: one per codeword plus up to 7 padding bits per packet), then the
+ * per-segment arrays (cap_seg segments): the segment table, its work order,
+ * counts, bases, block-wide sums and, for separate signs, sign counts and
+ * first sign bits.  `end` is the size of one precinct's area; slice-ordered
+ * decoding keeps the row above's GCLIs after it (top, cap_groups bytes). */
+#define UK_ZCAP(cap_groups) ((cap_groups) + 8 * JXS_MAXPK + 32)
+struct UkLayout {
+    uint32_t gcl, zend, seg, cnt, base, ex, nz, sgb, ord, end, top, top_end;
+};
+static inline __host__ __device__ UkLayout uk_layout(uint32_t cap_bytes, uint32_t cap_groups, uint32_t cap_seg) {
+    UkLayout L;
+    uint32_t o = cap_bytes + 32;
+    L.gcl = o;
+    o = (o + cap_groups + 15) & ~15u;
+    L.zend = o;
+    o = (o + 2 * UK_ZCAP(cap_groups) + 15) & ~15u;
+    L.seg = o;
+    o += 8 * cap_seg;
+    L.cnt = o;
+    o += 4 * cap_seg;
+    L.base = o;
+    o += 4 * cap_seg;
+    L.ex = o;
+    o += 4 * (cap_seg + 1);
+    L.nz = o;
+    o += 4 * cap_seg;
+    L.sgb = o;
+    o += 4 * cap_seg;
+    L.ord = o;
+    o = (o + 2 * cap_seg + 15) & ~15u;
+    L.end = o;
+    L.top = o;
+    L.top_end = (o + cap_groups + 15) & ~15u;
+    return L;
+}
+/* Static shared memory of the unpacking kernels at most (the launchers size
+ * the dynamic part against what is left of an SM's shared memory). */
+#define UK_STATIC_SMEM (9 * 1024)
+
 /* Launch-time queries cached per device: a kernel's dynamic shared-memory
  * limit is raised only when a launch needs more than was set before, so the
  * steady state costs no driver call. */

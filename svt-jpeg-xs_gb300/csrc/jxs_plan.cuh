@@ -29,16 +29,17 @@ extern "C" cudaError_t jxs_launch_rc(const jxs_cfg_t* dcfg, uint32_t np, uint32_
                                      int modes, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_rc_batch(const EncPrecLaunch* L, int modes, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_pack(const jxs_cfg_t* dcfg, uint32_t np, const uint16_t* coef, const uint8_t* gcli,
-                                       const PrecRC* rc, uint8_t* out, uint32_t cap_words, int* status, int modes,
-                                       cudaStream_t st);
+                                       const PrecRC* rc, const uint32_t* cost, uint8_t* out, uint32_t cap_words, int* status,
+                                       int modes, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_pack_batch(const EncPrecLaunch* L, uint32_t cap_words, int modes, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_unpack(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
-                                         int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, int* status,
-                                         cudaStream_t st);
-extern "C" cudaError_t jxs_launch_unpack_batch(const DecPrecLaunch* L, uint32_t cap_bytes, uint32_t cap_groups, cudaStream_t st);
-extern "C" cudaError_t jxs_launch_unpack_vpred(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
-                                               int16_t* coef, uint32_t nslices, uint32_t cap_bytes, uint32_t cap_groups, int* status,
+                                         int16_t* coef, uint32_t np, uint32_t cap_bytes, uint32_t cap_groups, uint32_t cap_seg,
+                                         int* status, cudaStream_t st);
+extern "C" cudaError_t jxs_launch_unpack_batch(const DecPrecLaunch* L, uint32_t cap_bytes, uint32_t cap_groups, uint32_t cap_seg,
                                                cudaStream_t st);
+extern "C" cudaError_t jxs_launch_unpack_vpred(const jxs_cfg_t* dcfg, const uint8_t* bs, uint32_t bs_size, const uint32_t* prec_off,
+                                               int16_t* coef, uint32_t nslices, uint32_t cap_bytes, uint32_t cap_groups,
+                                               uint32_t cap_seg, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_walk(const jxs_cfg_t* dcfg, uint32_t nslices, const uint8_t* bs, uint32_t size, uint32_t* prec_off,
                                        int* walk_bad, int* status, cudaStream_t st);
 extern "C" cudaError_t jxs_launch_walk_batch(const DecPrecLaunch* L, cudaStream_t st);
@@ -57,9 +58,10 @@ static const size_t kSmemMax = 220 * 1024;
 /* Rate-control tables of a frame: per precinct row the byte cost of every
  * (Q, R); with sign handling a second set with exact sign counts; with
  * vertical prediction the per-line tables of the ordered selection
- * (5 x 80 x 16 words per row). */
+ * (5 x 80 x 16 words per row); then the per-segment histograms the rate
+ * control hands to packing (JXS_SEGHIST_WORDS per segment of every row). */
 static inline size_t jxs_cost_bytes(const jxs_cfg_t* c) {
-    return ((size_t)c->np * 1024 * (c->fs ? 2 : 1) + (c->vpred ? (size_t)c->np * 5 * JXS_MAXBLINES * 16 : 0)) * sizeof(uint32_t);
+    return ((size_t)jxs_seghist_word(c) + (size_t)c->np * jxs_seg_cap(c) * JXS_SEGHIST_WORDS) * sizeof(uint32_t);
 }
 
 static inline uint32_t div_up(uint32_t a, uint32_t b) { return (a + b - 1) / b; }

@@ -100,3 +100,64 @@ def test_plugins_compile_and_link(jxs_lib, tmp_path):
     out = subprocess.run(["nm", "-D", "--defined-only", jxs_lib.LIB_PATH], capture_output=True, text=True).stdout
     exported = set(re.findall(r" T (svt_jpeg_xs_\w+)", out))
     assert used <= exported
+
+
+def _pkg_config(pc_path, *fields):
+    """pkg-config's --cflags / --libs for one .pc file (no pkg-config tool on
+    the build host): variables expanded, the requested fields joined."""
+    vars_, keys = {}, {}
+    for line in open(pc_path).read().splitlines():
+        line = line.strip()
+        m = re.match(r"^([A-Za-z_][\w.]*)=(.*)$", line)
+        if m:
+            vars_[m.group(1)] = m.group(2).strip()
+            continue
+        m = re.match(r"^([A-Za-z.]+):\s*(.*)$", line)
+        if m:
+            keys[m.group(1)] = m.group(2).strip()
+
+    def expand(v):
+        for _ in range(10):
+            v = re.sub(r"\$\{(\w+)\}", lambda mm: vars_[mm.group(1)], v)
+        return v
+
+    for k in list(vars_):
+        vars_[k] = expand(vars_[k])
+    return keys.get("Version"), " ".join(expand(keys[f]) for f in fields).split()
+
+
+def test_pkg_config_install_layout(jxs_lib, tmp_path):
+    """build() installs the reference's layout: headers under
+    include/svt-jpegxs, libSvtJpegxs.so.0 and SvtJpegxs.pc (the file FFmpeg's
+    --enable-libsvtjpegxs looks up). The plugins' API use compiles and links
+    with exactly the flags the .pc file gives."""
+    import build as pkg_build
+
+    pc = os.path.join(pkg_build.INSTALL, "lib", "pkgconfig", "SvtJpegxs.pc")
+    assert os.path.exists(pc)
+    version, flags = _pkg_config(pc, "Cflags", "Libs")
+    assert version == "0.10.0"
+    inc = [f[2:] for f in flags if f.startswith("-I")]
+    assert len(inc) == 1 and inc[0].endswith(os.path.join("include", "svt-jpegxs"))
+    for h in ("SvtJpegxs.h", "SvtJpegxsEnc.h", "SvtJpegxsDec.h", "SvtJpegxsImageBufferTools.h"):
+        assert open(os.path.join(inc[0], h)).read() == open(os.path.join(INCLUDE, h)).read()
+    libdir = [f[2:] for f in flags if f.startswith("-L")][0]
+    assert os.path.realpath(os.path.join(libdir, "libSvtJpegxs.so")) == os.path.join(libdir, "libSvtJpegxs.so.0")
+    so = str(tmp_path / "libplugin_pc.so")
+    subprocess.check_call(["gcc", "-std=gnu11", "-Wall", "-Werror", "-shared", "-fPIC", os.path.join(ROOT, "tests", "plugin_api.c"),
+                           "-o", so, *flags, "-Wl,--no-undefined", "-Wl,-rpath," + libdir])
+    needed = subprocess.run(["readelf", "-d", so], capture_output=True, text=True).stdout
+    assert "libSvtJpegxs.so.0" in needed
+
+
+def test_include_guards_are_the_references():
+    """Code that tests the reference headers' include-guard macros sees them
+    defined by these headers too."""
+    guards = {"SvtJpegxs.h": "_SVT_JPEG_XS_API_H_", "SvtJpegxsEnc.h": "_SVT_JPEG_XS_API_ENC_H_",
+              "SvtJpegxsDec.h": "_SVT_JPEG_XS_API_DEC_H_",
+              "SvtJpegxsImageBufferTools.h": "_SVT_JPEG_XS_API_IMAGE_BUFFER_TOOLS_H_"}
+    for h, g in guards.items():
+        text = open(os.path.join(INCLUDE, h)).read()
+        assert "#ifndef %s\n#define %s\n" % (g, g) in text, h
+        if os.path.exists(os.path.join(REF_API, h)):
+            assert ("#ifndef %s" % g) in open(os.path.join(REF_API, h)).read(), h
