@@ -1519,9 +1519,15 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                     /* significance flags, 1 = insignificant: even lanes lead a group of 8 */
                     const uint32_t bal = __ballot_sync(FULL, nv && !(lane & 1) && insig);
                     if (lane == 0) {
+                        /* the even lanes' votes compacted (bit i: group of 8
+                         * number i), then reversed: group 0 first */
                         const uint32_t nsg = min(16u, (gend - base + 7) >> 3);
-                        uint32_t bits = 0;
-                        for (uint32_t i2 = 0; i2 < nsg; i2++) bits = (bits << 1) | ((bal >> (2 * i2)) & 1u);
+                        uint32_t x = bal & 0x55555555u;
+                        x = (x | (x >> 1)) & 0x33333333u;
+                        x = (x | (x >> 2)) & 0x0f0f0f0fu;
+                        x = (x | (x >> 4)) & 0x00ff00ffu;
+                        x = (x | (x >> 8)) & 0x0000ffffu;
+                        const uint32_t bits = __brev(x) >> (32 - nsg);
                         if (bits) put_bits(buf, words, L.sig_pos + (base >> 3), bits, nsg, ovf);
                     }
                 }

@@ -206,153 +206,173 @@ __global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_c
 /* ------------------------------------------------------------------------ */
 /* vertical level                                                            */
 /* ------------------------------------------------------------------------ */
-#define IV_THREADS 128
-#define IV_COLS (2 * IV_THREADS - 8)      /* output columns per tile */
+/* A tile is IV_ROWPAIRS row pairs x IV_COLS columns of the level's output;
+ * each of its warps works alone on a strip of IV_WPAIRS column pairs.  Lane
+ * l holds the pairs j0 = first - 2 + 2 l and j0 + 1 (four columns): lanes 1
+ * to 30 produce the strip, lanes 0 and 31 are the halo the lifting needs on
+ * either side.  Every row the vertical lifting reads is rebuilt in
+ * registers by inverse horizontal lifting (the neighbours a lane needs come
+ * by two shuffles), and the vertical lifting runs down the lane's columns;
+ * there is no shared memory and no block barrier. */
+#define IV_WARPS 4
+#define IV_THREADS (32 * IV_WARPS)
+#define IV_WPAIRS 60                       /* output column pairs per warp (a multiple of 2) */
+#define IV_COLS (2 * IV_WPAIRS * IV_WARPS) /* output columns per tile */
 #define IV_ROWPAIRS 8
-#define IV_NROWS (2 * IV_ROWPAIRS + 3)    /* low rows r0..r0+R, high rows r0-1..r0+R */
-#define IV_SROW (IV_COLS + 8)
+
+DEV int clampi(int i, int n) { return i < 0 ? 0 : (i >= n ? n - 1 : i); }
+
+/* Values j, j + 1 (j even) of an int16 band row of n coefficients, as int32
+ * << fq; indices outside [0, n) read the nearest inside (n > 0). */
+DEV void band2(const int16_t* row, int j, int n, int fq, int32_t& a, int32_t& b) {
+    if (j >= 0 && j + 1 < n) {
+        const uint32_t v = *(const uint32_t*)(row + j);
+        a = (int32_t)((uint32_t)(int32_t)(int16_t)(v & 0xffffu) << fq);
+        b = (int32_t)((uint32_t)((int32_t)v >> 16) << fq);
+    } else {
+        a = dq(row[clampi(j, n)], fq);
+        b = dq(row[clampi(j + 1, n)], fq);
+    }
+}
+/* The same for an int32 low band row. */
+DEV void low2(const int32_t* row, int j, int n, int32_t& a, int32_t& b) {
+    if (j >= 0 && j + 1 < n) {
+        const int2 v = *(const int2*)(row + j);
+        a = v.x;
+        b = v.y;
+    } else {
+        a = row[clampi(j, n)];
+        b = row[clampi(j + 1, n)];
+    }
+}
+
+/* Inverse horizontal lifting of one row for this lane's pairs j0, j0 + 1:
+ * low values s0, s1 and high values d0, d1 (the high band read with its
+ * ends repeated: d[-1] = d[0], d[n2] = d[n2 - 1]).  x[2j+1] uses x[2j+2],
+ * or x[2j] itself where 2j + 2 is past the row (j + 1 >= w1).  Returns
+ * x[2 j0 .. 2 j0 + 3]; lanes 0 and 31 get values that only their neighbours
+ * use. */
+DEV int4 hinv(int32_t s0, int32_t s1, int32_t d0, int32_t d1, int j0, int w1) {
+    const int32_t dp = __shfl_up_sync(FULL, d1, 1);
+    const int32_t xe0 = s0 - ((dp + d0 + 2) >> 2);
+    const int32_t xe1 = s1 - ((d0 + d1 + 2) >> 2);
+    const int32_t xen = __shfl_down_sync(FULL, xe0, 1);
+    const int32_t xo0 = d0 + ((xe0 + (j0 + 1 < w1 ? xe1 : xe0)) >> 1);
+    const int32_t xo1 = d1 + ((xe1 + (j0 + 2 < w1 ? xen : xe1)) >> 1);
+    return make_int4(xe0, xo0, xe1, xo1);
+}
+
+DEV int4 add4(int4 a, int4 b) { return make_int4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+/* x - ((a + b + 2) >> 2) and x + ((a + b) >> 1), per column */
+DEV int4 lift_even(int4 x, int4 a, int4 b) {
+    return make_int4(x.x - ((a.x + b.x + 2) >> 2), x.y - ((a.y + b.y + 2) >> 2), x.z - ((a.z + b.z + 2) >> 2),
+                     x.w - ((a.w + b.w + 2) >> 2));
+}
+DEV int4 lift_odd(int4 x, int4 a, int4 b) {
+    return make_int4(x.x + ((a.x + b.x) >> 1), x.y + ((a.y + b.y) >> 1), x.z + ((a.z + b.z) >> 1), x.w + ((a.w + b.w) >> 1));
+}
+
+/* One output row of this lane's four columns x0 .. x0 + 3 (x0 < w). */
+template <int OUT>
+DEV void store4(const InvVJob& J, int y, int x0, int w, int4 v, const OutScale& os) {
+    const bool all4 = x0 + 3 < w;
+    if (OUT == 0) {
+        int32_t* d = (int32_t*)J.dst + (long long)y * J.dst_pitch + x0;
+        if (all4) {
+            *(int4*)d = v;
+        } else {
+            d[0] = v.x;
+            if (x0 + 1 < w) d[1] = v.y;
+            if (x0 + 2 < w) d[2] = v.z;
+        }
+        return;
+    }
+    const uint32_t a = out_sample(v.x, os), b = out_sample(v.y, os), c = out_sample(v.z, os), e = out_sample(v.w, os);
+    if (OUT == 1) {
+        uint8_t* d = (uint8_t*)J.dst + (long long)y * J.dst_pitch + x0;
+        if (all4 && ((uintptr_t)d & 3) == 0) {
+            *(uint32_t*)d = a | (b << 8) | (c << 16) | (e << 24);
+        } else {
+            d[0] = (uint8_t)a;
+            if (x0 + 1 < w) d[1] = (uint8_t)b;
+            if (x0 + 2 < w) d[2] = (uint8_t)c;
+            if (x0 + 3 < w) d[3] = (uint8_t)e;
+        }
+    } else {
+        uint16_t* d = (uint16_t*)J.dst + (long long)y * J.dst_pitch + x0;
+        if (all4 && ((uintptr_t)d & 7) == 0) {
+            *(uint2*)d = make_uint2(a | (b << 16), c | (e << 16));
+        } else {
+            d[0] = (uint16_t)a;
+            if (x0 + 1 < w) d[1] = (uint16_t)b;
+            if (x0 + 2 < w) d[2] = (uint16_t)c;
+            if (x0 + 3 < w) d[3] = (uint16_t)e;
+        }
+    }
+}
 
 template <int OUT, int NJ>
 __global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant__ InvVLaunchN<NJ> L) {
-    __shared__ __align__(16) int32_t sx[IV_NROWS][IV_SROW];
     const InvVJob& J = L.job[find_job<NJ>(L.job, L.njobs, (int)blockIdx.x)];
-    const jxs_band_t* __restrict__ bands = J.bands;
-    const int16_t* __restrict__ coef = J.coef;
     const int t = blockIdx.x - J.first_block;
     const int ty = t / J.col_tiles, tx = t - ty * J.col_tiles;
     const int w = J.w, h = J.h, fq = J.fq;
     const int n1 = (h + 1) >> 1, n2 = h >> 1;
     const int w1 = (w + 1) >> 1, w2 = w >> 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int jw = (tx * IV_WARPS + warp) * IV_WPAIRS; /* first output pair of the strip */
+    if (jw >= w1) return;                              /* the whole warp */
+    const int j0 = jw - 2 + 2 * lane;
     const int r0 = ty * IV_ROWPAIRS;
-    const int c0 = tx * IV_COLS;
-    const int warp = threadIdx.x >> 5;
-    const int jc = c0 >> 1;
-    const int npairs = min(IV_COLS / 2, w1 - jc);
-    const int rlo = min(IV_ROWPAIRS + 1, n1 - r0); /* low rows present */
-    /* rows of the tile, rebuilt horizontally: k <= R: low row r0 + k;
-     * k > R: high row r0 - 1 + (k - R - 1), mirrored into [0, n2) */
-    for (int k = warp; k < IV_NROWS; k += IV_THREADS / 32) {
-        int32_t* dst = &sx[k][0];
-        if (k <= IV_ROWPAIRS) {
-            if (k >= rlo) continue;
-            const int i = r0 + k;
-            const int32_t* srow = J.ll + (long long)i * J.ll_pitch;
-            const CoefRow hr = coef_row(bands[J.b_hl], i, coef);
-            warp_lift_inv(
-                jc, npairs, w1, w2,
-                [&](int j, int32_t* s) {
-                    if (j + 3 < w1) {
-                        const int4 v = *(const int4*)(srow + j);
-                        s[0] = v.x; s[1] = v.y; s[2] = v.z; s[3] = v.w;
-                    } else {
-                        for (int q = 0; q < 4; q++) s[q] = j + q < w1 ? srow[j + q] : 0;
-                    }
-                },
-                [&](int j, int32_t* d) {
-                    if (j + 3 < w2) {
-                        const uint2 v = *(const uint2*)(hr.row + j);
-                        d[0] = dq((int16_t)(v.x & 0xffff), fq); d[1] = dq((int16_t)(v.x >> 16), fq);
-                        d[2] = dq((int16_t)(v.y & 0xffff), fq); d[3] = dq((int16_t)(v.y >> 16), fq);
-                    } else {
-                        for (int q = 0; q < 4; q++) d[q] = j + q < w2 ? dq(hr.row[j + q], fq) : 0;
-                    }
-                },
-                [&](int j) { return srow[j]; }, [&](int j) { return dq(hr.row[j], fq); },
-                [&](int j, const int32_t* xe, const int32_t* xo) {
-                    const int x = 2 * (j - jc);
-                    *(int4*)(dst + x) = make_int4(xe[0], xo[0], xe[1], xo[1]);
-                    *(int4*)(dst + x + 4) = make_int4(xe[2], xo[2], xe[3], xo[3]);
-                });
-        } else {
-            if (n2 == 0) continue;
-            int i = r0 - 1 + (k - IV_ROWPAIRS - 1);
-            i = i < 0 ? 0 : (i >= n2 ? n2 - 1 : i);
-            const CoefRow lr = coef_row(bands[J.b_lh], i, coef);
-            const CoefRow hr = coef_row(bands[J.b_hh], i, coef);
-            auto ld4 = [&](const CoefRow& cr, int n, int j, int32_t* o) {
-                if (j + 3 < n) {
-                    const uint2 v = *(const uint2*)(cr.row + j);
-                    o[0] = dq((int16_t)(v.x & 0xffff), fq); o[1] = dq((int16_t)(v.x >> 16), fq);
-                    o[2] = dq((int16_t)(v.y & 0xffff), fq); o[3] = dq((int16_t)(v.y >> 16), fq);
-                } else {
-                    for (int q = 0; q < 4; q++) o[q] = j + q < n ? dq(cr.row[j + q], fq) : 0;
-                }
-            };
-            warp_lift_inv(
-                jc, npairs, w1, w2, [&](int j, int32_t* s) { ld4(lr, w1, j, s); }, [&](int j, int32_t* d) { ld4(hr, w2, j, d); },
-                [&](int j) { return dq(lr.row[j], fq); }, [&](int j) { return dq(hr.row[j], fq); },
-                [&](int j, const int32_t* xe, const int32_t* xo) {
-                    const int x = 2 * (j - jc);
-                    *(int4*)(dst + x) = make_int4(xe[0], xo[0], xe[1], xo[1]);
-                    *(int4*)(dst + x + 4) = make_int4(xe[2], xo[2], xe[3], xo[3]);
-                });
-        }
-    }
-    __syncthreads();
-
-    /* vertical lifting, one column pair per thread */
-    const int cp = threadIdx.x;
-    if (2 * cp >= 2 * npairs) return;
-    const int x = c0 + 2 * cp;
     const int rend = min(r0 + IV_ROWPAIRS, n1);
+    const jxs_band_t& bHL = J.bands[J.b_hl];
+    const jxs_band_t& bLH = J.bands[J.b_lh];
+    const jxs_band_t& bHH = J.bands[J.b_hh];
+    const int16_t* hl = J.coef + bHL.coef_off;
+    const int16_t* lh = J.coef + bLH.coef_off;
+    const int16_t* hh = J.coef + bHH.coef_off;
+    const uint32_t hl_p = bHL.pitch, lh_p = bLH.pitch, hh_p = bHH.pitch;
     const OutScale os = out_scale(J.bw, J.depth);
-#define LV(i) (*(const int2*)&sx[(i) - r0][2 * cp])
-#define HV(i) (*(const int2*)&sx[IV_ROWPAIRS + 1 + ((i) - (r0 - 1))][2 * cp])
-    int2 hp = n2 ? HV(r0 - 1) : make_int2(0, 0);
-    int2 hc = n2 ? HV(r0) : make_int2(0, 0);
-    int2 l0 = LV(r0);
-    int2 xe = make_int2(l0.x - ((hp.x + hc.x + 2) >> 2), l0.y - ((hp.y + hc.y + 2) >> 2));
+    /* low row i (LL + HL), i < n1; high row i (LH + HH) with i clamped into
+     * [0, n2) (n2 > 0), rebuilt horizontally */
+    auto lowrow = [&](int i) {
+        int32_t s0, s1, d0 = 0, d1 = 0;
+        low2(J.ll + (long long)i * J.ll_pitch, j0, w1, s0, s1);
+        if (w2) band2(hl + (uint64_t)i * hl_p, j0, w2, fq, d0, d1);
+        return hinv(s0, s1, d0, d1, j0, w1);
+    };
+    auto highrow = [&](int i) {
+        i = clampi(i, n2);
+        int32_t s0, s1, d0 = 0, d1 = 0;
+        band2(lh + (uint64_t)i * lh_p, j0, w1, fq, s0, s1);
+        if (w2) band2(hh + (uint64_t)i * hh_p, j0, w2, fq, d0, d1);
+        return hinv(s0, s1, d0, d1, j0, w1);
+    };
+    const int4 zero = make_int4(0, 0, 0, 0);
+    int4 hp = n2 ? highrow(r0 - 1) : zero, hc = n2 ? highrow(r0) : zero;
+    int4 xe = lift_even(lowrow(r0), hp, hc);
+    const bool out_lane = lane >= 1 && lane <= 30 && 2 * j0 < w;
+    const int x0 = 2 * j0;
     for (int i = r0; i < rend; i++) {
         const int y = 2 * i;
-        int2 xo = make_int2(0, 0), xn = xe;
+        int4 xo = zero, xn = xe;
         if (y + 1 < h) {
+            const int4 hcur = hc;
             if (y + 2 < h) {
-                const int2 ln = LV(i + 1), hn = HV(i + 1);
-                xn = make_int2(ln.x - ((hc.x + hn.x + 2) >> 2), ln.y - ((hc.y + hn.y + 2) >> 2));
+                const int4 hn = highrow(i + 1);
+                xn = lift_even(lowrow(i + 1), hc, hn);
                 hp = hc;
                 hc = hn;
             }
-            const int2 hcur = HV(i);
-            xo = make_int2(hcur.x + ((xe.x + xn.x) >> 1), hcur.y + ((xe.y + xn.y) >> 1));
+            xo = lift_odd(hcur, xe, xn);
         }
-        /* outputs (rows y, y + 1; columns x, x + 1) */
-        const bool two = x + 1 < w;
-        if (OUT == 0) {
-            int32_t* d0 = (int32_t*)J.dst + (long long)y * J.dst_pitch + x;
-            if (two) *(int2*)d0 = xe;
-            else d0[0] = xe.x;
-            if (y + 1 < h) {
-                int32_t* d1 = d0 + J.dst_pitch;
-                if (two) *(int2*)d1 = xo;
-                else d1[0] = xo.x;
-            }
-        } else {
-            const int rows = y + 1 < h ? 2 : 1;
-            for (int rr = 0; rr < rows; rr++) {
-                const int2 v = rr ? xo : xe;
-                const long long idx = (long long)(y + rr) * J.dst_pitch + x;
-                const uint32_t a = out_sample(v.x, os), b = out_sample(v.y, os);
-                if (OUT == 1) {
-                    uint8_t* p = (uint8_t*)J.dst + idx;
-                    if (two && J.vec) *(uint16_t*)p = (uint16_t)(a | (b << 8));
-                    else {
-                        p[0] = (uint8_t)a;
-                        if (two) p[1] = (uint8_t)b;
-                    }
-                } else {
-                    uint16_t* p = (uint16_t*)J.dst + idx;
-                    if (two && J.vec) *(uint32_t*)p = a | (b << 16);
-                    else {
-                        p[0] = (uint16_t)a;
-                        if (two) p[1] = (uint16_t)b;
-                    }
-                }
-            }
+        if (out_lane) {
+            store4<OUT>(J, y, x0, w, xe, os);
+            if (y + 1 < h) store4<OUT>(J, y + 1, x0, w, xo, os);
         }
         xe = xn;
     }
-#undef LV
-#undef HV
+    (void)hp;
 }
 
 /* ------------------------------------------------------------------------ */
