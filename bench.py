@@ -106,6 +106,8 @@ def parse():
                     help="serve: offered frames/s; the first is the headline, the others a load sweep")
     ap.add_argument("--serve-lanes", type=int, default=4, help="serve: encode lanes (and as many decode lanes)")
     ap.add_argument("--serve-max-batch", type=int, default=16, help="serve: requests per batch at most")
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="default line without the mixed-batch and serving passes")
     ap.add_argument("--seq-frames", type=int, default=SEQ_FRAMES,
                     help="distinct frames of the stream cycled through (each 33 MB; 4 or more keep inputs above L2)")
     return ap.parse_args()
@@ -283,6 +285,38 @@ def reference_sample(frames, F, seconds, threads):
         if s >= 2 and el >= seconds:
             rc.close()
             return done, el
+
+
+def extras_lines(args, local):
+    """Bounded passes of the mixed 48-frame batch (3 timed steps) and of the
+    serving loop (2000 frames/s offered for 2 s per mode), summarised for the
+    default line: batched vs per-frame throughput and p99 latency."""
+    import copy
+
+    out = {}
+    a = copy.copy(args)
+    a.steps, a.warmup = 3, 1
+    clk = ClockSampler(local)
+    clk.start()
+    m = run_workload(a, "mixed48", local)
+    c = clk.stop()
+    keys = ("gpix_s", "frames_s", "frame_latency_ms_p50", "frame_latency_ms_p99", "decode_only_gpix_s")
+    out["mixed48"] = {"config": m["config"]["workload"], "steps": a.steps,
+                      "batched": {k: m["batched"][k] for k in keys + ("launches_per_step",)},
+                      "per_frame": {k: m["per_frame"][k] for k in keys}, "clocks": c,
+                      "latency_definition": m["latency_definition"]}
+    a = copy.copy(args)
+    a.serve_seconds, a.serve_rates = 2.0, "2000"
+    clk = ClockSampler(local)
+    clk.start()
+    sv = run_serve(a, local)
+    c = clk.stop()
+    keys = ("gpix_s", "frames_s", "frame_latency_ms_p50", "frame_latency_ms_p99", "frame_latency_ms_max", "requests",
+            "submit_lag_ms_max")
+    out["serve"] = {"config": sv["config"]["workload"], "batched": {k: sv["batched"][k] for k in keys + ("mean_batch",)},
+                    "per_frame": {k: sv["per_frame"][k] for k in keys}, "clocks": c,
+                    "latency_definition": sv["latency_definition"]}
+    return out
 
 
 def run_reference(args, rank, world):
@@ -734,6 +768,14 @@ def run_ours(args, rank, world, local):
         "gpu_launches": (bat["launches_per_step"] if head_batched else launches_per_frame * F) * args.steps,
         "host_wall_s": host_s,
     }
+    if rank == 0 and world == 1 and args.extras:
+        # the metric's second half, batched vs per-frame on the other
+        # workloads: a short pass of the mixed 48-frame batch and of the
+        # serving loop at its headline load, each with its own clock record
+        del d_in, d_bs, d_out, h_in, h_bs, h_out, bat
+        gc.collect()
+        torch.cuda.empty_cache()
+        line.update(extras_lines(args, local))
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -931,7 +973,7 @@ def run_workload(args, name, local):
                       "decode_only_latency_ms_p99": pct(pf_dec_lat, 99), "streams": NS},
         "latency_definition": "all frames of a step submitted at once; a frame's latency is submit to its result on the host",
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -1103,7 +1145,7 @@ def run_serve(args, local):
                        "stream_types": types, "lanes": args.serve_lanes, "max_batch": args.serve_max_batch},
             "batched": batched, "per_frame": per_frame,
             "latency_definition": "request submit to completion seen by the server's scheduler (host steady clock)"}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
@@ -1114,11 +1156,11 @@ def main():
         return
     if args.workload == "serve":
         if rank == 0:
-            run_serve(args, local)
+            print(json.dumps(run_serve(args, local)), flush=True)
         return
     if args.workload != "stream4k":
         if rank == 0:
-            run_workload(args, args.workload, local)
+            print(json.dumps(run_workload(args, args.workload, local)), flush=True)
         return
     run_ours(args, rank, world, local)
 

@@ -1067,7 +1067,14 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                                           const uint32_t* __restrict__ cost, uint8_t* __restrict__ out, uint32_t cap_words,
                                           int* status, const int p) {
     extern __shared__ __align__(16) uint32_t buf[];
-    __shared__ uint32_t s_data[JXS_MAXSEG], s_vlc[JXS_MAXSEG], s_zero[JXS_MAXSEG], s_nz[JXS_MAXSEG];
+    /* per segment: data bits, VLC bits, groups without codes, signs; in pass
+     * B the same words hold each warp's list of significant groups */
+    __shared__ uint32_t s_segw[4][JXS_MAXSEG];
+    uint32_t* s_data = s_segw[0];
+    uint32_t* s_vlc = s_segw[1];
+    uint32_t* s_zero = s_segw[2];
+    uint32_t* s_nz = s_segw[3];
+    static_assert(4 * JXS_MAXSEG >= 128 * PK_WARPS, "a list of 128 groups per warp");
     __shared__ PkLine pl[JXS_MAXBLINES];
     __shared__ uint8_t s_meth[JXS_MAXBL];
     __shared__ uint32_t s_cn[JXS_MAXBL], s_cs[JXS_MAXBL];
@@ -1477,7 +1484,7 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
             const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
             const uint32_t w4 = nv ? *(const uint32_t*)(grow + g) : 0u;
             uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0;
-            if (nv) {
+            if (nv && fs) {
                 c0 = *(const uint4*)(crow + 4 * g);
                 c1 = *(const uint4*)(crow + 4 * g + 8);
             }
@@ -1579,7 +1586,41 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                 }
             }
             uint32_t sbits = 0, sn = 0;
-            if (dl) {
+            if (!fs) {
+                /* signs with the data: the warp lists its groups with GCLI
+                 * > gtli (bit offset in the warp's data, group, GCLI), then
+                 * each lane packs one listed group at a time, its sign
+                 * nibble and planes in one write of at most 64 bits; the
+                 * coefficients of the other groups are never read */
+                uint32_t* list = &s_segw[0][0] + 128 * warp;
+                const uint32_t lt = (1u << lane) - 1u;
+                uint32_t cnt = 0, idx = 0, o = ex >> 16;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const bool sk = k < (int)nv && v[k] > t;
+                    const uint32_t bk = __ballot_sync(FULL, sk);
+                    idx += __popc(bk & lt);
+                    cnt += __popc(bk);
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    if (k < (int)nv && v[k] > t) {
+                        list[idx++] = (o << 11) | ((uint32_t)(4 * lane + k) << 4) | v[k];
+                        o += 4 * (v[k] - t + 1);
+                    }
+                }
+                __syncwarp();
+                for (uint32_t r = lane; r < cnt; r += 32) {
+                    const uint32_t e = list[r];
+                    const uint32_t gi = base + ((e >> 4) & 127u), vv = e & 15u, np = vv - t;
+                    const uint2 raw4 = *(const uint2*)(crow + 4 * gi);
+                    uint32_t sgn, nzm;
+                    uint64_t ch = data_chunk(raw4, (int)B.w - 4 * (int)gi, vv, t, uniform, sgn, nzm);
+                    ch |= (uint64_t)sgn << (4 * np);
+                    put_bits(buf, words, dpos + (e >> 11), ch, 4 * (np + 1), ovf);
+                }
+                __syncwarp();
+            } else if (dl) {
                 /* data bits of the groups with gcli > gtli (pack_data_c,
                  * PackPrecinct.c:128-198), joined while they fit 64 bits */
                 uint32_t pos = dpos + (ex >> 16);
