@@ -178,7 +178,7 @@ static uint64_t enc_work_layout(const jxs_cfg_t* c, uint8_t* base, EncWork* w) {
     } else {
         for (uint32_t k = 0; k < c->nc; k++) {
             w->in_off[k] = in_bytes;
-            in_bytes += round256((uint64_t)c->comp[k].w * c->comp[k].h * bps);
+            in_bytes += round256((uint64_t)stage_pitch(c->comp[k].w, bps) * c->comp[k].h * bps);
         }
     }
     memset(&w->fb, 0, sizeof(w->fb));
@@ -217,7 +217,7 @@ static uint64_t dec_work_layout(const jxs_cfg_t* c, uint8_t* base, DecWork* w) {
     memset(w->out_off, 0, sizeof(w->out_off));
     for (uint32_t k = 0; k < c->nc; k++) {
         w->out_off[k] = ob;
-        ob += round256((uint64_t)jxs_out_w(c, k) * jxs_out_h(c, k) * bps);
+        ob += round256((uint64_t)stage_pitch(jxs_out_w(c, k), bps) * jxs_out_h(c, k) * bps);
     }
     w->out_stage = take(ob);
     return off;
@@ -1064,10 +1064,11 @@ extern "C" int32_t jxs_gpu_batch_encode(jxs_gpu_batch_t* b, jxs_gpu_enc_t* const
                 e.in.pitch[k] = strides[i][k];
             } else {
                 uint8_t* d = w.in_stage + w.in_off[k];
-                BCK(cudaMemcpy2DAsync(d, (size_t)pw * bps, planes[i][k], (size_t)strides[i][k] * bps, (size_t)pw * bps, ph,
+                const uint32_t sp = packed ? pw : stage_pitch(pw, bps);
+                BCK(cudaMemcpy2DAsync(d, (size_t)sp * bps, planes[i][k], (size_t)strides[i][k] * bps, (size_t)pw * bps, ph,
                                       cudaMemcpyHostToDevice, st));
                 e.in.p[k] = d;
-                e.in.pitch[k] = pw;
+                e.in.pitch[k] = sp;
             }
         }
         e.out = jxs_gpu_is_device_ptr(out[i]) ? out[i] : w.out_stage;
@@ -1202,7 +1203,7 @@ extern "C" int32_t jxs_gpu_batch_decode(jxs_gpu_batch_t* b, jxs_gpu_dec_t* const
                 d.out.pitch[k] = strides[i][k];
             } else {
                 d.out.p[k] = w.out_stage + w.out_off[k];
-                d.out.pitch[k] = jxs_out_w(c, k);
+                d.out.pitch[k] = stage_pitch(jxs_out_w(c, k), bytes_per_sample(c));
             }
         }
         weight[i] = c->coef_total;
@@ -1241,8 +1242,8 @@ extern "C" int32_t jxs_gpu_batch_decode(jxs_gpu_batch_t* b, jxs_gpu_dec_t* const
         for (uint32_t k = 0; k < d.c->nc; k++) {
             if (d.out.p[k] == planes[i][k]) continue;
             const uint32_t ow = jxs_out_w(d.c, k), oh = jxs_out_h(d.c, k);
-            BCK(cudaMemcpy2DAsync(planes[i][k], (size_t)strides[i][k] * bps, d.out.p[k], (size_t)ow * bps, (size_t)ow * bps, oh,
-                                  cudaMemcpyDeviceToHost, st));
+            BCK(cudaMemcpy2DAsync(planes[i][k], (size_t)strides[i][k] * bps, d.out.p[k], (size_t)d.out.pitch[k] * bps, (size_t)ow * bps,
+                                  oh, cudaMemcpyDeviceToHost, st));
         }
     }
     BCK(cudaMemcpyAsync(b->status_h, b->status_d, 2 * (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -23,6 +23,7 @@
 #define UK_WARPS (UK_THREADS / 32)
 #define FULL 0xffffffffu
 static_assert(JXS_MAXSEG <= UK_THREADS, "one thread per segment");
+static_assert(UK_LIST_BYTES == 4 * 128 * UK_WARPS, "a list of 128 groups per warp");
 
 /* Per band line of the precinct being unpacked. */
 struct UkLine {
@@ -803,48 +804,81 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         const uint32_t gend = min(sg.g0 + SG, B.gcli_w);
         uint32_t dpos = P.dpos + s_base[sidx];
         if (!fs) {
-            /* signs with the data: each lane two consecutive groups (one
-             * offset scan for both, one 16-byte store where the band row is
-             * a single column) */
-            for (uint32_t base = sg.g0; base < gend; base += 64) {
-                const uint32_t g = base + 2 * lane;
-                const bool va = g < gend, vb = g + 1 < gend;
-                uint32_t v0 = 0, v1 = 0;
-                if (vb) {
-                    const uint32_t pr = *(const uint16_t*)(gcl + B.gbase + g);
-                    v0 = pr & 255u;
-                    v1 = pr >> 8;
-                } else if (va) {
-                    v0 = gcl[B.gbase + g];
+            /* signs with the data: each lane 4 consecutive groups.  The lane
+             * writes zeros for its groups, then the warp lists the groups
+             * with data (bit offset in the warp's data, group, GCLI) and each
+             * lane decodes one listed group at a time, so that the decode
+             * work follows the groups that have data */
+            uint32_t* list = (uint32_t*)(dsm + UL.zend) + 128 * warp;
+            const uint32_t t = L.t;
+            for (uint32_t base = sg.g0; base < gend; base += 128) {
+                const uint32_t g = base + 4 * lane;
+                const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
+                uint32_t v4 = 0;
+                if (nv == 4) {
+                    v4 = *(const uint32_t*)(gcl + B.gbase + g);
+                } else {
+                    for (uint32_t q = 0; q < nv; q++) v4 |= (uint32_t)gcl[B.gbase + g + q] << (8 * q);
                 }
-                const uint32_t np0 = v0 > L.t ? v0 - L.t : 0u, np1 = v1 > L.t ? v1 - L.t : 0u;
-                const uint32_t len0 = np0 ? 4 * (np0 + 1) : 0u, len1 = np1 ? 4 * (np1 + 1) : 0u;
+                uint32_t len[4], lsum = 0;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const uint32_t v = (v4 >> (8 * q)) & 255u;
+                    len[q] = (q < (int)nv && v > t) ? 4 * (v - t + 1) : 0u;
+                    lsum += len[q];
+                }
                 uint32_t tot;
-                const uint32_t ex = warp_excl_scan(len0 + len1, &tot);
-                uint2 o0 = make_uint2(0u, 0u), o1 = o0;
-                const int wl = (int)B.w - 4 * (int)g;
-                if (len0) {
-                    const uint32_t pos = dpos + ex;
-                    const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
-                    o0 = decode_group(win >> (64 - len0), np0, L.t, v0, uniform, wl);
-                }
-                if (len1) {
-                    const uint32_t pos = dpos + ex + len0;
-                    const uint64_t win = ((uint64_t)bits32_at(pbuf, pos) << 32) | bits32_at(pbuf, pos + 32);
-                    o1 = decode_group(win >> (64 - len1), np1, L.t, v1, uniform, wl - 4);
-                }
+                uint32_t o = warp_excl_scan(lsum, &tot);
+                /* zeros for the lane's groups (those with data are written
+                 * again below, after the warp barrier) */
                 if (one_col) {
-                    /* the band row's padding takes the last group's tail */
-                    if (vb) *(uint4*)(crow + 4 * g) = make_uint4(o0.x, o0.y, o1.x, o1.y);
-                    else if (va) *(uint2*)(crow + 4 * g) = o0;
+                    if (nv == 4) {
+                        *(uint4*)(crow + 4 * g) = make_uint4(0u, 0u, 0u, 0u);
+                        *(uint4*)(crow + 4 * g + 8) = make_uint4(0u, 0u, 0u, 0u);
+                    } else {
+                        for (uint32_t q = 0; q < nv; q++) *(uint2*)(crow + 4 * (g + q)) = make_uint2(0u, 0u);
+                    }
                 } else {
                     /* a column starts anywhere in the row and ends where the
                      * next begins: the groups' coefficients inside it only */
-                    const uint32_t ov[4] = {o0.x, o0.y, o1.x, o1.y};
-#pragma unroll
-                    for (int c = 0; c < 8; c++)
-                        if ((c < 4 ? va : vb) && c < wl) crow[4 * g + c] = (int16_t)((ov[c >> 1] >> (16 * (c & 1))) & 0xffffu);
+                    const int wl = (int)B.w - 4 * (int)g;
+                    for (int c = 0; c < 4 * (int)nv && c < wl; c++)
+                        if (!len[c >> 2]) crow[4 * g + c] = 0;
                 }
+                uint32_t idx = 0, cnt = 0;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const uint32_t bq = __ballot_sync(FULL, len[q] != 0);
+                    idx += __popc(bq & lt_mask);
+                    cnt += __popc(bq);
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    if (len[q]) {
+                        list[idx++] = (o << 11) | ((uint32_t)(4 * lane + q) << 4) | ((v4 >> (8 * q)) & 15u);
+                        o += len[q];
+                    }
+                }
+                __syncwarp();
+                for (uint32_t r = lane; r < cnt; r += 32) {
+                    const uint32_t e = list[r];
+                    const uint32_t gi = base + ((e >> 4) & 127u), v = e & 15u, np = v - t, ln = 4 * (np + 1);
+                    const uint32_t pos = dpos + (e >> 11);
+                    const uint32_t wi = pos >> 5, sh = pos & 31;
+                    const uint32_t w0 = be_word(pbuf, wi), w1 = be_word(pbuf, wi + 1), w2 = be_word(pbuf, wi + 2);
+                    const uint64_t win = ((uint64_t)__funnelshift_l(w1, w0, sh) << 32) | __funnelshift_l(w2, w1, sh);
+                    const int wl = (int)B.w - 4 * (int)gi;
+                    const uint2 ov = decode_group(win >> (64 - ln), np, t, v, uniform, wl);
+                    if (one_col) {
+                        *(uint2*)(crow + 4 * gi) = ov;
+                    } else {
+                        const uint32_t vv[2] = {ov.x, ov.y};
+#pragma unroll
+                        for (int c = 0; c < 4; c++)
+                            if (c < wl) crow[4 * gi + c] = (int16_t)((vv[c >> 1] >> (16 * (c & 1))) & 0xffffu);
+                    }
+                }
+                __syncwarp();
                 dpos += tot;
             }
             continue;

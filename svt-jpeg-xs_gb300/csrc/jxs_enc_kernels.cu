@@ -706,25 +706,30 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
             const uint32_t g = base + 4 * lane;
             const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
             const uint32_t w4 = nv ? *(const uint32_t*)(grow + g) : 0u;
-            uint32_t h[4] = {0, 0, 0, 0}, m = 0;
+            /* 8-bit counters of GCLIs 0..7 in lo, 8..15 in hi (GCLIs are
+             * below 16): one shift and add per group */
+            uint64_t lo = 0, hi = 0;
+            uint32_t m = 0;
 #pragma unroll
             for (int k = 0; k < 4; k++) {
                 const uint32_t v = (w4 >> (8 * k)) & 255u;
-                const uint32_t inc = k < (int)nv ? 1u << (8 * (v & 3)) : 0u;
-#pragma unroll
-                for (int r = 0; r < 4; r++) h[r] += (v >> 2) == (uint32_t)r ? inc : 0u;
+                const uint64_t inc = k < (int)nv ? 1ull << (8 * (v & 7)) : 0ull;
+                if (v & 8) hi += inc;
+                else lo += inc;
                 if (k < (int)nv) m = max(m, v);
             }
+            const uint32_t h[4] = {(uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32)};
             /* significance group: 8 groups in lanes 2i, 2i+1; its groups
              * (8, or fewer at the end of a line) counted at its maximum */
             const uint32_t mx = max(m, __shfl_xor_sync(FULL, m, 1));
             const uint32_t nvp = nv + __shfl_xor_sync(FULL, nv, 1);
-            uint32_t sh[4] = {0, 0, 0, 0};
+            uint64_t slo = 0, shi = 0;
             if (!(lane & 1) && nv) {
-                const uint32_t si = nvp << (8 * (mx & 3));
-#pragma unroll
-                for (int r = 0; r < 4; r++) sh[r] += (mx >> 2) == (uint32_t)r ? si : 0u;
+                const uint64_t si = (uint64_t)nvp << (8 * (mx & 7));
+                if (mx & 8) shi = si;
+                else slo = si;
             }
+            const uint32_t sh[4] = {(uint32_t)slo, (uint32_t)(slo >> 32), (uint32_t)shi, (uint32_t)(shi >> 32)};
             uint32_t mine = 0;
 #pragma unroll
             for (int r = 0; r < 4; r++) {

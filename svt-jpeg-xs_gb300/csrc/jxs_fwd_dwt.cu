@@ -2,16 +2,13 @@
  * Forward 5/3 wavelet transform for sm_103a.
  *
  *  fwd_v_kernel  one vertical level and the horizontal level that follows
- *                it, on a tile of FV_ROWPAIRS row pairs x FV_COLS columns of
- *                one component.  Vertical lifting runs in registers, one
- *                thread per column pair.  The resulting low and high rows go
- *                to shared memory with a 2-column halo on each side.  Each
- *                row is then lifted horizontally by one warp: lanes hold 4
- *                consecutive samples and exchange the neighbours they need
- *                with shuffles.  Outputs: the HL, LH and HH bands as 16-bit
- *                sign-magnitude coefficients with the GCLI of every
- *                4-coefficient group, and the int32 LL plane for the next
- *                level.
+ *                it.  Each warp streams down a strip of 240 columns (8 per
+ *                lane, plus one halo lane on either side) for 8 row pairs:
+ *                vertical lifting in registers, then horizontal lifting
+ *                across the warp with shuffles.  Outputs: the HL, LH and HH
+ *                bands as 16-bit sign-magnitude coefficients with the GCLI of
+ *                every 4-coefficient group (one group per lane and band row),
+ *                and the int32 LL plane for the next level.
  *  fwd_h_kernel  the horizontal-only levels below the last vertical level
  *                (or all levels of a component without vertical
  *                decomposition): one warp per row, every level in shared
@@ -54,9 +51,8 @@ DEV int mirror_idx(int i, int n) {
 }
 
 DEV uint32_t to_sm(int32_t v) {
-    if (v >= 0) return (uint32_t)((v + 128) >> 8);
-    const uint32_t m = (uint32_t)((-v + 128) >> 8);
-    return m ? (m | 0x8000u) : 0u;
+    const uint32_t m = ((uint32_t)abs(v) + 128u) >> 8;
+    return m ? (m | (((uint32_t)v >> 16) & 0x8000u)) : 0u;
 }
 
 template <int SRC>
@@ -75,29 +71,6 @@ DEV int32_t load1(const void* src, long long pitch, int chan, int depth, int y, 
     if (SRC == SRC_U16) return scale_in<SRC>(((const uint16_t*)src)[row + x], depth);
     if (SRC == SRC_PK8) return scale_in<SRC>(((const uint8_t*)src)[row + 3 * x + chan], depth);
     return scale_in<SRC>(((const uint16_t*)src)[row + 3 * x + chan], depth);
-}
-
-/* two horizontally adjacent samples (x even, x + 1 < width) with one load
- * where the layout allows it */
-template <int SRC>
-DEV void load2(const void* src, long long pitch, int chan, int depth, int y, int x, bool vec, int32_t& a, int32_t& b) {
-    const long long row = (long long)y * pitch;
-    if (vec && SRC == SRC_I32) {
-        const int2 v = *(const int2*)((const int32_t*)src + row + x);
-        a = v.x;
-        b = v.y;
-    } else if (vec && SRC == SRC_U16) {
-        const uint32_t v = *(const uint32_t*)((const uint16_t*)src + row + x);
-        a = scale_in<SRC>(v & 0xffffu, depth);
-        b = scale_in<SRC>(v >> 16, depth);
-    } else if (vec && SRC == SRC_U8) {
-        const uint32_t v = *(const uint16_t*)((const uint8_t*)src + row + x);
-        a = scale_in<SRC>(v & 0xffu, depth);
-        b = scale_in<SRC>(v >> 8, depth);
-    } else {
-        a = load1<SRC>(src, pitch, chan, depth, y, x);
-        b = load1<SRC>(src, pitch, chan, depth, y, x + 1);
-    }
 }
 
 /* One lane's 4-coefficient group of a band row: coefficients j..j+3 (j a
@@ -169,179 +142,212 @@ DEV void warp_lift_fwd(const int32_t* x, int npairs, Out out) {
 /* ------------------------------------------------------------------------ */
 /* vertical level + one horizontal level                                     */
 /* ------------------------------------------------------------------------ */
-#define FV_THREADS 128
-#define FV_COLS (2 * FV_THREADS - 8)      /* level-input columns per tile: tile + 4 halo columns in one pass */
-#define FV_ROWPAIRS 8
-#define FV_SROW (FV_COLS + 16)            /* shared row: 4 front words (2 pad, 2 halo), FV_COLS, halo, slack */
+/* A tile is FV_COLS columns x FV_ROWPAIRS row pairs of the level input; its
+ * warps are stacked vertically, each working alone on FV_WROWPAIRS row pairs
+ * of the tile's column strip.  Lane l holds the 8 columns c0 = first - 8 +
+ * 8 l .. c0 + 7: lanes 1 to 30 produce the strip, lanes 0 and 31 are the
+ * halo the horizontal lifting needs on either side.  Each lane streams down
+ * its 8 columns: two input rows per step, the vertical lifting in registers
+ * (the previous even row and high value are kept), then the horizontal
+ * lifting of the new low and high rows across the warp (the neighbours by
+ * two shuffles).  Every lane's 4 output pairs are one 4-coefficient group of
+ * each band.  No shared memory, no block barrier. */
+#define FV_WARPS 4
+#define FV_THREADS (32 * FV_WARPS)
+#define FV_COLS 240          /* level-input columns of a strip: lanes 1..30, 8 each */
+#define FV_WROWPAIRS 8       /* row pairs per warp */
+#define FV_ROWPAIRS (FV_WROWPAIRS * FV_WARPS)
 
-#define FV_NR (2 * FV_ROWPAIRS + 3)       /* input rows per tile: 2 above, 2 R, 1 below */
+/* Raw samples of one input row for a lane's 8 columns: 16-bit sources hold
+ * two samples per word (column 2k in the low half of word k), int32 sources
+ * one per word. */
+template <int SRC> struct FvRaw { static const int N = 4; };
+template <> struct FvRaw<SRC_I32> { static const int N = 8; };
 
-/* Raw input of one column pair in the staging buffer: the two samples as
- * read (16-bit sources: packed in one word) or the two int32 low-band
- * values. */
-template <int SRC> struct FvIn { typedef uint32_t T; };
-template <> struct FvIn<SRC_I32> { typedef int2 T; };
-
-DEV void cp_async4(void* smem, const void* g) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(g));
-}
-DEV void cp_async8(void* smem, const void* g) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(g));
-}
-DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-DEV void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::); }
-
-/* One tile of a vertical-level launch. */
-struct FvTile {
-    int jb, r0, c0, npairs, ncp, rc, hc;
-};
-template <int NJ>
-DEV FvTile fv_tile(const FwdVLaunchN<NJ>& L, int t) {
-    FvTile T;
-    const int jb = find_job<NJ>(L.job, L.njobs, t);
-    const FwdVJob& J = L.job[jb];
-    const int u = t - J.first_block;
-    const int ty = u / J.col_tiles, tx = u - ty * J.col_tiles;
-    const int n1 = (J.h + 1) >> 1, n2 = J.h >> 1, w1 = (J.w + 1) >> 1;
-    T.jb = jb;
-    T.r0 = ty * FV_ROWPAIRS;
-    T.c0 = tx * FV_COLS;
-    /* output pairs j in [c0/2, c0/2 + npairs) of the level's bands; lifting
-     * them reads input columns c0 - 2 .. c0 + 2 npairs + 1 */
-    T.npairs = min(FV_COLS / 2, ((w1 - T.c0 / 2) + 1) & ~1);
-    T.ncp = T.npairs + 2;
-    T.rc = min(FV_ROWPAIRS, n1 - T.r0);
-    T.hc = max(0, min(FV_ROWPAIRS, n2 - T.r0));
-    return T;
+/* raw value of column x (0 <= x < w) of a row */
+template <int SRC>
+DEV uint32_t raw1(const void* row, int chan, int x) {
+    if (SRC == SRC_I32) return (uint32_t)((const int32_t*)row)[x];
+    if (SRC == SRC_U8) return ((const uint8_t*)row)[x];
+    if (SRC == SRC_U16) return ((const uint16_t*)row)[x];
+    if (SRC == SRC_PK8) return ((const uint8_t*)row)[3 * x + chan];
+    return ((const uint16_t*)row)[3 * x + chan];
 }
 
-/* Stages the input of tile t into buffer `in` (FV_NR rows x column pairs):
- * asynchronous copies where the pair is inside the plane and aligned,
- * ordinary loads (with the symmetric extension) elsewhere. */
-template <int SRC, int NJ>
-DEV void fv_stage(const FwdVLaunchN<NJ>& L, int t, typename FvIn<SRC>::T* in) {
-    const FvTile T = fv_tile(L, t);
-    const FwdVJob& J = L.job[T.jb];
-    const int cp = threadIdx.x;
-    if (cp >= T.ncp) return;
-    const int w = J.w, h = J.h;
-    const int xa = T.c0 - 2 + 2 * cp;
-    const bool inside = xa >= 0 && xa + 1 < w;
-    const bool async = inside && J.vec && (SRC == SRC_U16 || SRC == SRC_I32);
-    const int ma = mirror_idx(xa, w), mb = mirror_idx(xa + 1, w);
-#pragma unroll 4
-    for (int k = 0; k < FV_NR; k++) {
-        const int y = mirror_idx(2 * T.r0 - 2 + k, h);
-        typename FvIn<SRC>::T* dst = in + k * FV_THREADS + cp;
-        const long long row = (long long)y * J.src_pitch;
-        if (SRC == SRC_I32) {
-            const int32_t* src = (const int32_t*)J.src + row;
-            if (async) cp_async8(dst, src + xa);
-            else *(int2*)dst = make_int2(src[ma], src[mb]);
-        } else if (SRC == SRC_U16) {
-            const uint16_t* src = (const uint16_t*)J.src + row;
-            if (async) cp_async4(dst, src + xa);
-            else *(uint32_t*)dst = (uint32_t)src[ma] | ((uint32_t)src[mb] << 16);
-        } else if (SRC == SRC_U8) {
-            const uint8_t* src = (const uint8_t*)J.src + row;
-            *(uint32_t*)dst = (uint32_t)src[ma] | ((uint32_t)src[mb] << 16);
-        } else if (SRC == SRC_PK8) {
-            const uint8_t* src = (const uint8_t*)J.src + row;
-            *(uint32_t*)dst = (uint32_t)src[3 * ma + J.chan] | ((uint32_t)src[3 * mb + J.chan] << 16);
+template <int SRC> DEV size_t src_elem() { return SRC == SRC_I32 ? 4 : (SRC == SRC_U16 || SRC == SRC_PK16) ? 2 : 1; }
+
+/* Loads row y (in range) for the lane's columns c0 .. c0 + 7: one or two
+ * vector loads when `fast` (all 8 columns inside, aligned), else one load per
+ * column with the symmetric extension. */
+template <int SRC>
+DEV void fv_load(const FwdVJob& J, int y, int c0, bool fast, uint32_t* r) {
+    const char* row = (const char*)J.src + (size_t)y * (size_t)J.src_pitch * src_elem<SRC>();
+    if constexpr (SRC == SRC_I32) {
+        if (fast) {
+            const int4 a = *(const int4*)((const int32_t*)row + c0), b = *(const int4*)((const int32_t*)row + c0 + 4);
+            r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
+            r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
         } else {
-            const uint16_t* src = (const uint16_t*)J.src + row;
-            *(uint32_t*)dst = (uint32_t)src[3 * ma + J.chan] | ((uint32_t)src[3 * mb + J.chan] << 16);
+#pragma unroll
+            for (int k = 0; k < 8; k++) r[k] = raw1<SRC>(row, 0, mirror_idx(c0 + k, J.w));
+        }
+    } else if (fast && SRC == SRC_U16) {
+        const uint4 q = *(const uint4*)((const uint16_t*)row + c0);
+        r[0] = q.x; r[1] = q.y; r[2] = q.z; r[3] = q.w;
+    } else if (fast && SRC == SRC_U8) {
+        const uint2 q = *(const uint2*)((const uint8_t*)row + c0);
+        r[0] = __byte_perm(q.x, 0, 0x4140);
+        r[1] = __byte_perm(q.x, 0, 0x4342);
+        r[2] = __byte_perm(q.y, 0, 0x4140);
+        r[3] = __byte_perm(q.y, 0, 0x4342);
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++)
+            r[k] = raw1<SRC>(row, J.chan, mirror_idx(c0 + 2 * k, J.w)) | (raw1<SRC>(row, J.chan, mirror_idx(c0 + 2 * k + 1, J.w)) << 16);
+    }
+}
+
+/* The scaled samples of a raw row: ((x & (2^d - 1)) << (20 - d)) - 2^19 as
+ * one multiply-add (mul = 2^(20 - d)). */
+template <int SRC>
+DEV void fv_decode(const uint32_t* r, uint32_t mask, int32_t mul, int32_t* v) {
+    if constexpr (SRC == SRC_I32) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) v[k] = (int32_t)r[k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            v[2 * k] = (int32_t)(r[k] & mask) * mul - (1 << 19);
+            v[2 * k + 1] = (int32_t)((r[k] >> 16) & mask) * mul - (1 << 19);
         }
     }
 }
 
-/* Persistent: each block walks tiles t = blockIdx.x, + gridDim.x, ...; the
- * next tile's input is staged (asynchronous copies) while the current one is
- * lifted.  With `persistent` false (int32 low bands, still in L2) the grid
- * has one block per tile and a single buffer. */
-template <int SRC, int NJ>
-__global__ void __launch_bounds__(FV_THREADS, 6) fwd_v_kernel(const __grid_constant__ FwdVLaunchN<NJ> L) {
-    typedef typename FvIn<SRC>::T InT;
-    extern __shared__ __align__(16) unsigned char fv_dyn[];
-    InT* inbuf = (InT*)fv_dyn; /* [2][FV_NR][FV_THREADS] */
-    __shared__ __align__(16) int32_t sL[FV_ROWPAIRS][FV_SROW];
-    __shared__ __align__(16) int32_t sH[FV_ROWPAIRS][FV_SROW];
-    const int warp = threadIdx.x >> 5;
-    const bool persistent = gridDim.x < (unsigned)L.ntiles;
-    int t = blockIdx.x, buf = 0;
-    if (t < L.ntiles) fv_stage<SRC, NJ>(L, t, inbuf);
-    cp_async_commit();
-    for (; t < L.ntiles; t += gridDim.x) {
-        const int tn = t + gridDim.x;
-        if (persistent && tn < L.ntiles) fv_stage<SRC, NJ>(L, tn, inbuf + (buf ^ 1) * FV_NR * FV_THREADS);
-        cp_async_commit();
-        cp_async_wait1();
-        __syncthreads();
-        const FvTile T = fv_tile(L, t);
-        const FwdVJob& J = L.job[T.jb];
-        const int depth = J.depth;
-        const InT* in = inbuf + buf * FV_NR * FV_THREADS;
-        /* vertical lifting, one column pair per thread */
-        const int cp = threadIdx.x;
-        if (cp < T.ncp) {
-            int32_t a[FV_NR], b[FV_NR];
-#pragma unroll
-            for (int k = 0; k < FV_NR; k++) {
-                const InT v = in[k * FV_THREADS + cp];
-                if (SRC == SRC_I32) {
-                    a[k] = ((const int2*)&v)->x;
-                    b[k] = ((const int2*)&v)->y;
-                } else {
-                    const uint32_t r = *(const uint32_t*)&v;
-                    a[k] = scale_in<SRC>(r & 0xffffu, depth);
-                    b[k] = scale_in<SRC>(r >> 16, depth);
-                }
-            }
-            int32_t hpa = a[1] - ((a[0] + a[2]) >> 1), hpb = b[1] - ((b[0] + b[2]) >> 1);
-#pragma unroll
-            for (int k = 0; k < FV_ROWPAIRS; k++) {
-                const int e = 2 + 2 * k; /* x[2i] of pair r0 + k */
-                const int32_t ha = a[e + 1] - ((a[e] + a[e + 2]) >> 1), hb = b[e + 1] - ((b[e] + b[e + 2]) >> 1);
-                const int32_t la = a[e] + ((hpa + ha + 2) >> 2), lb = b[e] + ((hpb + hb + 2) >> 2);
-                *(int2*)&sL[k][2 + 2 * cp] = make_int2(la, lb);
-                *(int2*)&sH[k][2 + 2 * cp] = make_int2(ha, hb);
-                hpa = ha;
-                hpb = hb;
-            }
-        }
-        __syncthreads();
+/* Horizontal lifting of one row across the warp: v holds the lane's 8
+ * samples x[2j0 .. 2j0 + 7]; s / d receive its 4 low / high outputs.  The
+ * right neighbour's first sample and the left neighbour's last high value
+ * come by shuffles (lanes 0 and 31 get values only their neighbours use). */
+DEV void fv_hlift(const int32_t* v, int32_t* s, int32_t* d) {
+    const int32_t nx = __shfl_down_sync(FULL, v[0], 1);
+    d[0] = v[1] - ((v[0] + v[2]) >> 1);
+    d[1] = v[3] - ((v[2] + v[4]) >> 1);
+    d[2] = v[5] - ((v[4] + v[6]) >> 1);
+    d[3] = v[7] - ((v[6] + nx) >> 1);
+    const int32_t dm = __shfl_up_sync(FULL, d[3], 1);
+    s[0] = v[0] + ((dm + d[0] + 2) >> 2);
+    s[1] = v[2] + ((d[0] + d[1] + 2) >> 2);
+    s[2] = v[4] + ((d[1] + d[2] + 2) >> 2);
+    s[3] = v[6] + ((d[2] + d[3] + 2) >> 2);
+}
 
-        /* horizontal lifting, one warp per row; the tile's output pairs are
-         * j in [c0/2, c0/2 + npairs) of the level's bands */
-        const int w1 = (J.w + 1) >> 1;
-        const int jc = T.c0 >> 1;
-        for (int r = warp; r < T.rc + T.hc; r += FV_THREADS / 32) {
-            if (r < T.rc) {
-                const int row = T.r0 + r;
-                const BandRow bhl = band_row(J.bands[J.b_hl], row, J.coef, J.gcli);
-                int32_t* ll = J.ll + (long long)row * J.ll_pitch;
-                warp_lift_fwd(&sL[r][4], T.npairs, [&](int j, const int32_t* sv, const int32_t* d) {
-                    const int jj = jc + j;
-                    emit4(bhl, jj, d[0], d[1], d[2], d[3]);
-                    if (jj + 3 < w1) {
-                        *(int4*)(ll + jj) = make_int4(sv[0], sv[1], sv[2], sv[3]);
-                    } else {
-                        for (int q = 0; q < 4; q++)
-                            if (jj + q < w1) ll[jj + q] = sv[q];
-                    }
-                });
+/* One band's output of a strip: coefficient and GCLI rows advanced by one
+ * band row per step. */
+struct FvBand {
+    uint16_t* crow;
+    uint8_t* grow;
+    uint32_t pitch, gpitch;
+    int w, gw;
+};
+DEV FvBand fv_band(const jxs_band_t& bd, int row, uint16_t* coef, uint8_t* gcli) {
+    FvBand b;
+    b.pitch = bd.pitch;
+    b.gpitch = bd.gpitch;
+    b.crow = coef + bd.coef_off + (uint64_t)row * bd.pitch;
+    b.grow = gcli + bd.gcli_off + (uint64_t)row * bd.gpitch;
+    b.w = (int)bd.w;
+    b.gw = (int)bd.gcli_w;
+    return b;
+}
+DEV void fv_emit(const FvBand& b, int j, const int32_t* v) {
+    emit4(BandRow{b.crow, b.grow, b.w, b.gw}, j, v[0], v[1], v[2], v[3]);
+}
+DEV void fv_next(FvBand& b) {
+    b.crow += b.pitch;
+    b.grow += b.gpitch;
+}
+
+template <int SRC, int NJ>
+__global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant__ FwdVLaunchN<NJ> L) {
+    const FwdVJob& J = L.job[find_job<NJ>(L.job, L.njobs, (int)blockIdx.x)];
+    const int u = blockIdx.x - J.first_block;
+    const int ty = u / J.col_tiles, tx = u - ty * J.col_tiles;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int w = J.w, h = J.h, n1 = (h + 1) >> 1, n2 = h >> 1;
+    const int r0 = (ty * FV_WARPS + warp) * FV_WROWPAIRS;
+    if (r0 >= n1) return; /* the whole warp */
+    const int rend = min(r0 + FV_WROWPAIRS, n1);
+    const int c0 = tx * FV_COLS - 8 + 8 * lane;
+    const bool fast = J.vec && c0 >= 0 && c0 + 8 <= w;
+    const uint32_t mask = (1u << J.depth) - 1u;
+    const int32_t mul = 1 << (20 - J.depth);
+    /* output: pairs jj .. jj + 3 of the level's bands (one group), lanes 1..30 */
+    const int jj = c0 >> 1, w1 = (w + 1) >> 1;
+    const bool out_lane = lane >= 1 && lane <= 30 && c0 < w;
+    FvBand bhl = fv_band(J.bands[J.b_hl], r0, J.coef, J.gcli);
+    FvBand blh = fv_band(J.bands[J.b_lh], r0, J.coef, J.gcli);
+    FvBand bhh = fv_band(J.bands[J.b_hh], r0, J.coef, J.gcli);
+    int32_t* ll = J.ll + (size_t)r0 * J.ll_pitch + jj;
+    const int N = FvRaw<SRC>::N;
+
+    /* x[2 r0] and d[r0 - 1] (rows 2 r0 - 2, 2 r0 - 1 mirrored at the top);
+     * rows 2 r0 + 1, 2 r0 + 2 already in flight */
+    int32_t xe[8], dp[8];
+    uint32_t ra[N], rb[N];
+    {
+        uint32_t q0[N], q1[N], q2[N];
+        fv_load<SRC>(J, mirror_idx(2 * r0 - 2, h), c0, fast, q0);
+        fv_load<SRC>(J, mirror_idx(2 * r0 - 1, h), c0, fast, q1);
+        fv_load<SRC>(J, 2 * r0, c0, fast, q2);
+        fv_load<SRC>(J, mirror_idx(2 * r0 + 1, h), c0, fast, ra);
+        fv_load<SRC>(J, mirror_idx(2 * r0 + 2, h), c0, fast, rb);
+        int32_t xa[8], xb[8];
+        fv_decode<SRC>(q0, mask, mul, xa);
+        fv_decode<SRC>(q1, mask, mul, xb);
+        fv_decode<SRC>(q2, mask, mul, xe);
+#pragma unroll
+        for (int k = 0; k < 8; k++) dp[k] = xb[k] - ((xa[k] + xe[k]) >> 1);
+    }
+    for (int i = r0; i < rend; i++) {
+        int32_t xo[8], xn[8];
+        fv_decode<SRC>(ra, mask, mul, xo);
+        fv_decode<SRC>(rb, mask, mul, xn);
+        if (i + 1 < rend) {
+            fv_load<SRC>(J, mirror_idx(2 * i + 3, h), c0, fast, ra);
+            fv_load<SRC>(J, mirror_idx(2 * i + 4, h), c0, fast, rb);
+        }
+        /* vertical lifting: high d[i], low s[i] */
+        int32_t d[8], s[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            d[k] = xo[k] - ((xe[k] + xn[k]) >> 1);
+            s[k] = xe[k] + ((dp[k] + d[k] + 2) >> 2);
+            xe[k] = xn[k];
+            dp[k] = d[k];
+        }
+        /* low row i: LL (int32, next level) and HL */
+        int32_t hs[4], hd[4];
+        fv_hlift(s, hs, hd);
+        if (out_lane) {
+            fv_emit(bhl, jj, hd);
+            if (jj + 3 < w1) {
+                *(int4*)ll = make_int4(hs[0], hs[1], hs[2], hs[3]);
             } else {
-                const int row = T.r0 + r - T.rc;
-                const BandRow blh = band_row(J.bands[J.b_lh], row, J.coef, J.gcli);
-                const BandRow bhh = band_row(J.bands[J.b_hh], row, J.coef, J.gcli);
-                warp_lift_fwd(&sH[r - T.rc][4], T.npairs, [&](int j, const int32_t* sv, const int32_t* d) {
-                    emit4(blh, jc + j, sv[0], sv[1], sv[2], sv[3]);
-                    emit4(bhh, jc + j, d[0], d[1], d[2], d[3]);
-                });
+                for (int q = 0; q < 4; q++)
+                    if (jj + q < w1) ll[q] = hs[q];
             }
         }
-        __syncthreads();
-        buf ^= 1;
+        /* high row i: LH and HH */
+        if (i < n2) {
+            fv_hlift(d, hs, hd);
+            if (out_lane) {
+                fv_emit(blh, jj, hs);
+                fv_emit(bhh, jj, hd);
+            }
+        }
+        fv_next(bhl);
+        fv_next(blh);
+        fv_next(bhh);
+        ll += J.ll_pitch;
     }
 }
 
@@ -415,41 +421,9 @@ extern "C" int jxs_fwd_h_max_rows_per_block(void) { return FH_MAX_WARPS; }
 
 template <int SRC, int NJ>
 static cudaError_t launch_v(const FwdVLaunchN<NJ>* L, int grid_per_sm, cudaStream_t st) {
-    /* int32 inputs (the previous level's low band, in L2): one block per
-     * tile, one buffer; sample planes: persistent, double-buffered, with
-     * grid_per_sm blocks per SM (0: as many as fit) */
-    const bool persistent = SRC != SRC_I32;
-    const size_t smem = (persistent ? 2 : 1) * FV_NR * FV_THREADS * sizeof(typename FvIn<SRC>::T);
-    static std::atomic<int> attr[JXS_MAX_DEV];
-    cudaError_t e = jxs_smem_attr(fwd_v_kernel<SRC, NJ>, (int)smem, attr);
-    if (e != cudaSuccess) return e;
-    int blocks = L->ntiles;
-    if (persistent) {
-        /* SMs and resident blocks per SM, queried once per device */
-        static std::atomic<int> q_sms[JXS_MAX_DEV], q_per_sm[JXS_MAX_DEV];
-        int dev = 0, sms = 0, per_sm = 0;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        const bool cached = dev >= 0 && dev < JXS_MAX_DEV && q_sms[dev].load() > 0;
-        if (cached) {
-            sms = q_sms[dev].load();
-            per_sm = q_per_sm[dev].load();
-        } else {
-            if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fwd_v_kernel<SRC, NJ>, FV_THREADS, smem)) !=
-                cudaSuccess)
-                return e;
-            if (dev >= 0 && dev < JXS_MAX_DEV) {
-                q_per_sm[dev].store(per_sm);
-                q_sms[dev].store(sms);
-            }
-        }
-        if (per_sm < 1) per_sm = 1;
-        if (grid_per_sm > 0 && grid_per_sm < per_sm) per_sm = grid_per_sm;
-        blocks = sms * per_sm;
-        if (blocks > L->ntiles) blocks = L->ntiles;
-    }
-    if (blocks <= 0) return cudaSuccess;
-    fwd_v_kernel<SRC, NJ><<<blocks, FV_THREADS, smem, st>>>(*L);
+    (void)grid_per_sm; /* one block per tile */
+    if (L->ntiles <= 0) return cudaSuccess;
+    fwd_v_kernel<SRC, NJ><<<L->ntiles, FV_THREADS, 0, st>>>(*L);
     return cudaGetLastError();
 }
 

@@ -143,7 +143,7 @@ static int32_t enc_slot_alloc(jxs_gpu_enc_t* e, EncSlot* s) {
     } else {
         for (uint32_t k = 0; k < c->nc; k++) {
             s->in_off[k] = in_bytes;
-            in_bytes += ((uint64_t)c->comp[k].w * c->comp[k].h * bps + 255) & ~255ull;
+            in_bytes += ((uint64_t)stage_pitch(c->comp[k].w, bps) * c->comp[k].h * bps + 255) & ~255ull;
         }
     }
     CK(cudaMalloc(&s->in_stage, in_bytes));
@@ -266,10 +266,11 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
             pitch[k] = strides[k];
         } else {
             uint8_t* d = s->in_stage + s->in_off[k];
-            CK(cudaMemcpy2DAsync(d, (size_t)w * bps, planes[k], (size_t)strides[k] * bps, (size_t)w * bps, h,
+            const uint32_t sp = packed ? w : stage_pitch(w, bps);
+            CK(cudaMemcpy2DAsync(d, (size_t)sp * bps, planes[k], (size_t)strides[k] * bps, (size_t)w * bps, h,
                                  cudaMemcpyHostToDevice, st));
             src[k] = d;
-            pitch[k] = w;
+            pitch[k] = sp;
         }
     }
     TMARK(1);
@@ -498,7 +499,7 @@ static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
     const uint32_t bps = bytes_per_sample(c);
     for (uint32_t k = 0; k < c->nc; k++) {
         s->out_off[k] = ob;
-        ob += ((uint64_t)jxs_out_w(c, k) * jxs_out_h(c, k) * bps + 255) & ~255ull;
+        ob += ((uint64_t)stage_pitch(jxs_out_w(c, k), bps) * jxs_out_h(c, k) * bps + 255) & ~255ull;
     }
     CK(cudaMalloc(&s->out_stage, ob));
     if (dec_needs_nlt_pass(c)) {
@@ -678,7 +679,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
             out.pitch[k] = strides[k];
         } else {
             out.p[k] = s->out_stage + s->out_off[k];
-            out.pitch[k] = jxs_out_w(c, k);
+            out.pitch[k] = stage_pitch(jxs_out_w(c, k), bps);
         }
     }
     /* a colour transform or a non-linear output: the last inverse level
@@ -744,8 +745,8 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
     for (uint32_t k = 0; k < c->nc; k++) {
         if (out_dev[k]) continue;
         const uint32_t ow = jxs_out_w(c, k), oh = jxs_out_h(c, k);
-        CK(cudaMemcpy2DAsync(planes[k], (size_t)strides[k] * bps, s->out_stage + s->out_off[k], (size_t)ow * bps, (size_t)ow * bps,
-                             oh, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpy2DAsync(planes[k], (size_t)strides[k] * bps, s->out_stage + s->out_off[k], (size_t)stage_pitch(ow, bps) * bps,
+                             (size_t)ow * bps, oh, cudaMemcpyDeviceToHost, st));
     }
     CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
     TMARK(4);

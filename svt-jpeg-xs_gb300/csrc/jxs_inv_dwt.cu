@@ -6,13 +6,13 @@
  *                (in shared memory) and writes the row of the last vertical
  *                level's low band, or, for a component without vertical
  *                levels, the output samples.
- *  inv_v_kernel  one vertical level on a tile of IV_ROWPAIRS row pairs x
- *                IV_COLS columns: the low rows (LL + HL) and high rows (LH +
- *                HH) the tile needs are rebuilt by inverse horizontal lifting,
- *                one warp per row with 4 pairs per lane, into shared memory;
- *                then each thread lifts one column pair vertically and writes
- *                the next level's int32 low band or, for level 0, the output
- *                samples with the linear output scaling fused.
+ *  inv_v_kernel  one vertical level: each warp streams down a strip of 240
+ *                output columns (8 per lane, plus one halo lane on either
+ *                side) for 8 row pairs.  Every step rebuilds a low row (LL +
+ *                HL) and a high row (LH + HH) by inverse horizontal lifting
+ *                across the warp, lifts vertically in registers and writes
+ *                two rows of the next level's int32 low band or, for level 0,
+ *                of the output samples with the linear output scaling fused.
  *
  * Arithmetic (bit-exact with the reference): coefficients are int16 two's
  * complement scaled by << Fq (Definitions.h:128); inverse lifting
@@ -206,107 +206,137 @@ __global__ void __launch_bounds__(IH_MAX_WARPS * 32) inv_h_kernel(const __grid_c
 /* ------------------------------------------------------------------------ */
 /* vertical level                                                            */
 /* ------------------------------------------------------------------------ */
-/* A tile is IV_ROWPAIRS row pairs x IV_COLS columns of the level's output;
- * each of its warps works alone on a strip of IV_WPAIRS column pairs.  Lane
- * l holds the pairs j0 = first - 2 + 2 l and j0 + 1 (four columns): lanes 1
- * to 30 produce the strip, lanes 0 and 31 are the halo the lifting needs on
- * either side.  Every row the vertical lifting reads is rebuilt in
- * registers by inverse horizontal lifting (the neighbours a lane needs come
- * by two shuffles), and the vertical lifting runs down the lane's columns;
- * there is no shared memory and no block barrier. */
+/* A tile is IV_COLS columns x IV_ROWPAIRS row pairs of the level's output;
+ * its warps are stacked vertically, each working alone on IV_WROWPAIRS row
+ * pairs of the tile's column strip.  Lane l holds the 8 output columns c0 =
+ * first - 8 + 8 l .. c0 + 7 (band pairs j0 = c0 / 2 .. j0 + 3, one group of
+ * every band): lanes 1 to 30 produce the strip, lanes 0 and 31 are the halo
+ * the lifting needs on either side.  Each step rebuilds the next low row (LL
+ * + HL) and high row (LH + HH) by inverse horizontal lifting across the warp
+ * (the neighbours by two shuffles), lifts vertically in registers (the last
+ * even row and high row are kept) and writes two output rows.  The band rows
+ * of the step after are loaded while this one computes.  No shared memory,
+ * no block barrier. */
 #define IV_WARPS 4
 #define IV_THREADS (32 * IV_WARPS)
-#define IV_WPAIRS 60                       /* output column pairs per warp (a multiple of 2) */
-#define IV_COLS (2 * IV_WPAIRS * IV_WARPS) /* output columns per tile */
-#define IV_ROWPAIRS 8
+#define IV_COLS 240                          /* output columns of a strip: lanes 1..30, 8 each */
+#define IV_WROWPAIRS 8                       /* row pairs per warp */
+#define IV_ROWPAIRS (IV_WROWPAIRS * IV_WARPS)
 
 DEV int clampi(int i, int n) { return i < 0 ? 0 : (i >= n ? n - 1 : i); }
 
-/* Values j, j + 1 (j even) of an int16 band row of n coefficients, as int32
- * << fq; indices outside [0, n) read the nearest inside (n > 0). */
-DEV void band2(const int16_t* row, int j, int n, int fq, int32_t& a, int32_t& b) {
-    if (j >= 0 && j + 1 < n) {
-        const uint32_t v = *(const uint32_t*)(row + j);
-        a = (int32_t)((uint32_t)(int32_t)(int16_t)(v & 0xffffu) << fq);
-        b = (int32_t)((uint32_t)((int32_t)v >> 16) << fq);
-    } else {
-        a = dq(row[clampi(j, n)], fq);
-        b = dq(row[clampi(j + 1, n)], fq);
-    }
+/* Raw band values of one low or high row for the lane's pairs j0 .. j0 + 3:
+ * the low-pass values (int32 low band, or int16 coefficients of the LH band)
+ * and the high-pass int16 coefficients (HL or HH), two per word. */
+struct IvRaw {
+    int4 s;     /* int32 low band values */
+    uint2 sc;   /* or LH coefficients, two per word */
+    uint2 d;    /* HL / HH coefficients, two per word */
+};
+
+/* int16 values j0 .. j0 + 3 of a band row of n (> 0) coefficients, two per
+ * word; indices outside [0, n) read the nearest inside */
+DEV uint2 iv_ld_coef(const int16_t* row, int j0, int n) {
+    if (j0 >= 0 && j0 + 4 <= n) return *(const uint2*)(row + j0);
+    uint32_t v[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) v[q] = (uint16_t)row[clampi(j0 + q, n)];
+    return make_uint2(v[0] | (v[1] << 16), v[2] | (v[3] << 16));
 }
-/* The same for an int32 low band row. */
-DEV void low2(const int32_t* row, int j, int n, int32_t& a, int32_t& b) {
-    if (j >= 0 && j + 1 < n) {
-        const int2 v = *(const int2*)(row + j);
-        a = v.x;
-        b = v.y;
-    } else {
-        a = row[clampi(j, n)];
-        b = row[clampi(j + 1, n)];
-    }
+DEV int4 iv_ld_low(const int32_t* row, int j0, int n) {
+    if (j0 >= 0 && j0 + 4 <= n) return *(const int4*)(row + j0);
+    return make_int4(row[clampi(j0, n)], row[clampi(j0 + 1, n)], row[clampi(j0 + 2, n)], row[clampi(j0 + 3, n)]);
+}
+/* two int16 values of a word as int32 << fq */
+DEV void iv_dq2(uint32_t w, int fq, int32_t& a, int32_t& b) {
+    a = (int32_t)(w << 16) >> (16 - fq);
+    b = (int32_t)(w & 0xffff0000u) >> (16 - fq);
 }
 
-/* Inverse horizontal lifting of one row for this lane's pairs j0, j0 + 1:
- * low values s0, s1 and high values d0, d1 (the high band read with its
- * ends repeated: d[-1] = d[0], d[n2] = d[n2 - 1]).  x[2j+1] uses x[2j+2],
- * or x[2j] itself where 2j + 2 is past the row (j + 1 >= w1).  Returns
- * x[2 j0 .. 2 j0 + 3]; lanes 0 and 31 get values that only their neighbours
- * use. */
-DEV int4 hinv(int32_t s0, int32_t s1, int32_t d0, int32_t d1, int j0, int w1) {
-    const int32_t dp = __shfl_up_sync(FULL, d1, 1);
-    const int32_t xe0 = s0 - ((dp + d0 + 2) >> 2);
-    const int32_t xe1 = s1 - ((d0 + d1 + 2) >> 2);
-    const int32_t xen = __shfl_down_sync(FULL, xe0, 1);
-    const int32_t xo0 = d0 + ((xe0 + (j0 + 1 < w1 ? xe1 : xe0)) >> 1);
-    const int32_t xo1 = d1 + ((xe1 + (j0 + 2 < w1 ? xen : xe1)) >> 1);
-    return make_int4(xe0, xo0, xe1, xo1);
+/* Inverse horizontal lifting of one row across the warp from the lane's low
+ * values s[0..3] and high values d[0..3] (pairs j0 .. j0 + 3): x[2j] = s[j] -
+ * ((d[j-1] + d[j] + 2) >> 2), x[2j+1] = d[j] + ((x[2j] + x[2j+2]) >> 1), with
+ * x[2j] itself in place of x[2j+2] past the row (j + 1 >= w1).  The left
+ * neighbour's last high value and the right neighbour's first even sample
+ * come by shuffles.  x receives the lane's 8 samples. */
+DEV void iv_hrow(const int32_t* s, const int32_t* d, int j0, int w1, int32_t* x) {
+    const int32_t dm = __shfl_up_sync(FULL, d[3], 1);
+    const int32_t e0 = s[0] - ((dm + d[0] + 2) >> 2);
+    const int32_t e1 = s[1] - ((d[0] + d[1] + 2) >> 2);
+    const int32_t e2 = s[2] - ((d[1] + d[2] + 2) >> 2);
+    const int32_t e3 = s[3] - ((d[2] + d[3] + 2) >> 2);
+    const int32_t en = __shfl_down_sync(FULL, e0, 1);
+    x[0] = e0;
+    x[1] = d[0] + ((e0 + (j0 + 1 < w1 ? e1 : e0)) >> 1);
+    x[2] = e1;
+    x[3] = d[1] + ((e1 + (j0 + 2 < w1 ? e2 : e1)) >> 1);
+    x[4] = e2;
+    x[5] = d[2] + ((e2 + (j0 + 3 < w1 ? e3 : e2)) >> 1);
+    x[6] = e3;
+    x[7] = d[3] + ((e3 + (j0 + 4 < w1 ? en : e3)) >> 1);
 }
 
-DEV int4 add4(int4 a, int4 b) { return make_int4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
-/* x - ((a + b + 2) >> 2) and x + ((a + b) >> 1), per column */
-DEV int4 lift_even(int4 x, int4 a, int4 b) {
-    return make_int4(x.x - ((a.x + b.x + 2) >> 2), x.y - ((a.y + b.y + 2) >> 2), x.z - ((a.z + b.z + 2) >> 2),
-                     x.w - ((a.w + b.w + 2) >> 2));
+/* linear_output_scaling of one sample with zeta >= 2: the rounded value
+ * (u + 2^(zeta-1)) >> zeta (u = v + 2^(Bw-1), wrapping like the reference's
+ * int32 addition) equals ((u >> 1) + 2^(zeta-2)) >> (zeta-1), which cannot
+ * overflow; then the clamp to [0, 2^d - 1] */
+struct OutScale8 {
+    uint32_t half_bw;
+    int32_t q;
+    int zm1, m, general;
+    OutScale os;
+};
+DEV OutScale8 out_scale8(int bw, int depth) {
+    OutScale8 s;
+    s.os = out_scale(bw, depth);
+    s.half_bw = s.os.half_bw;
+    s.general = s.os.zeta < 2;
+    s.zm1 = s.os.zeta - 1;
+    s.q = s.general ? 0 : 1 << (s.os.zeta - 2);
+    s.m = s.os.m;
+    return s;
 }
-DEV int4 lift_odd(int4 x, int4 a, int4 b) {
-    return make_int4(x.x + ((a.x + b.x) >> 1), x.y + ((a.y + b.y) >> 1), x.z + ((a.z + b.z) >> 1), x.w + ((a.w + b.w) >> 1));
+DEV uint32_t out_sample8(int32_t v, const OutScale8& s) {
+    if (s.general) return out_sample(v, s.os);
+    const int32_t u = (int32_t)((uint32_t)v + s.half_bw);
+    return (uint32_t)min(max(((u >> 1) + s.q) >> s.zm1, 0), s.m);
 }
 
-/* One output row of this lane's four columns x0 .. x0 + 3 (x0 < w). */
+/* One output row of the lane's 8 columns c0 .. c0 + 7 (c0 < w): vector
+ * stores where the row is aligned and all 8 are inside. */
 template <int OUT>
-DEV void store4(const InvVJob& J, int y, int x0, int w, int4 v, const OutScale& os) {
-    const bool all4 = x0 + 3 < w;
-    if (OUT == 0) {
-        int32_t* d = (int32_t*)J.dst + (long long)y * J.dst_pitch + x0;
-        if (all4) {
-            *(int4*)d = v;
+DEV void iv_store8(const InvVJob& J, int y, int c0, int w, bool vec, const int32_t* x, const OutScale8& os) {
+    const bool all8 = vec && c0 + 8 <= w;
+    if constexpr (OUT == 0) {
+        int32_t* d = (int32_t*)J.dst + (size_t)y * J.dst_pitch + c0;
+        if (all8) {
+            *(int4*)d = make_int4(x[0], x[1], x[2], x[3]);
+            *(int4*)(d + 4) = make_int4(x[4], x[5], x[6], x[7]);
         } else {
-            d[0] = v.x;
-            if (x0 + 1 < w) d[1] = v.y;
-            if (x0 + 2 < w) d[2] = v.z;
-        }
-        return;
-    }
-    const uint32_t a = out_sample(v.x, os), b = out_sample(v.y, os), c = out_sample(v.z, os), e = out_sample(v.w, os);
-    if (OUT == 1) {
-        uint8_t* d = (uint8_t*)J.dst + (long long)y * J.dst_pitch + x0;
-        if (all4 && ((uintptr_t)d & 3) == 0) {
-            *(uint32_t*)d = a | (b << 8) | (c << 16) | (e << 24);
-        } else {
-            d[0] = (uint8_t)a;
-            if (x0 + 1 < w) d[1] = (uint8_t)b;
-            if (x0 + 2 < w) d[2] = (uint8_t)c;
-            if (x0 + 3 < w) d[3] = (uint8_t)e;
+            for (int q = 0; q < 8; q++)
+                if (c0 + q < w) d[q] = x[q];
         }
     } else {
-        uint16_t* d = (uint16_t*)J.dst + (long long)y * J.dst_pitch + x0;
-        if (all4 && ((uintptr_t)d & 7) == 0) {
-            *(uint2*)d = make_uint2(a | (b << 16), c | (e << 16));
+        uint32_t o[8];
+#pragma unroll
+        for (int q = 0; q < 8; q++) o[q] = out_sample8(x[q], os);
+        if constexpr (OUT == 1) {
+            uint8_t* d = (uint8_t*)J.dst + (size_t)y * J.dst_pitch + c0;
+            if (all8) {
+                *(uint2*)d = make_uint2(o[0] | (o[1] << 8) | (o[2] << 16) | (o[3] << 24),
+                                        o[4] | (o[5] << 8) | (o[6] << 16) | (o[7] << 24));
+            } else {
+                for (int q = 0; q < 8; q++)
+                    if (c0 + q < w) d[q] = (uint8_t)o[q];
+            }
         } else {
-            d[0] = (uint16_t)a;
-            if (x0 + 1 < w) d[1] = (uint16_t)b;
-            if (x0 + 2 < w) d[2] = (uint16_t)c;
-            if (x0 + 3 < w) d[3] = (uint16_t)e;
+            uint16_t* d = (uint16_t*)J.dst + (size_t)y * J.dst_pitch + c0;
+            if (all8) {
+                *(uint4*)d = make_uint4(o[0] | (o[1] << 16), o[2] | (o[3] << 16), o[4] | (o[5] << 16), o[6] | (o[7] << 16));
+            } else {
+                for (int q = 0; q < 8; q++)
+                    if (c0 + q < w) d[q] = (uint16_t)o[q];
+            }
         }
     }
 }
@@ -320,11 +350,13 @@ __global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant
     const int n1 = (h + 1) >> 1, n2 = h >> 1;
     const int w1 = (w + 1) >> 1, w2 = w >> 1;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int jw = (tx * IV_WARPS + warp) * IV_WPAIRS; /* first output pair of the strip */
-    if (jw >= w1) return;                              /* the whole warp */
-    const int j0 = jw - 2 + 2 * lane;
-    const int r0 = ty * IV_ROWPAIRS;
-    const int rend = min(r0 + IV_ROWPAIRS, n1);
+    const int r0 = (ty * IV_WARPS + warp) * IV_WROWPAIRS;
+    if (r0 >= n1) return; /* the whole warp */
+    const int rend = min(r0 + IV_WROWPAIRS, n1);
+    const int c0 = tx * IV_COLS - 8 + 8 * lane, j0 = c0 >> 1;
+    const bool out_lane = lane >= 1 && lane <= 30 && c0 < w;
+    const int esz = OUT == 0 ? 4 : OUT;
+    const bool vec = ((uintptr_t)J.dst & 15) == 0 && (((size_t)J.dst_pitch * esz) & 15) == 0;
     const jxs_band_t& bHL = J.bands[J.b_hl];
     const jxs_band_t& bLH = J.bands[J.b_lh];
     const jxs_band_t& bHH = J.bands[J.b_hh];
@@ -332,47 +364,94 @@ __global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant
     const int16_t* lh = J.coef + bLH.coef_off;
     const int16_t* hh = J.coef + bHH.coef_off;
     const uint32_t hl_p = bHL.pitch, lh_p = bLH.pitch, hh_p = bHH.pitch;
-    const OutScale os = out_scale(J.bw, J.depth);
-    /* low row i (LL + HL), i < n1; high row i (LH + HH) with i clamped into
-     * [0, n2) (n2 > 0), rebuilt horizontally */
-    auto lowrow = [&](int i) {
-        int32_t s0, s1, d0 = 0, d1 = 0;
-        low2(J.ll + (long long)i * J.ll_pitch, j0, w1, s0, s1);
-        if (w2) band2(hl + (uint64_t)i * hl_p, j0, w2, fq, d0, d1);
-        return hinv(s0, s1, d0, d1, j0, w1);
+    const OutScale8 os = out_scale8(J.bw, J.depth);
+    /* raw loads of low row i (i < n1) and high row i (clamped into [0, n2),
+     * n2 > 0) */
+    auto ld_low = [&](int i, IvRaw& r) {
+        r.s = iv_ld_low(J.ll + (size_t)i * J.ll_pitch, j0, w1);
+        r.d = w2 ? iv_ld_coef(hl + (size_t)i * hl_p, j0, w2) : make_uint2(0u, 0u);
     };
-    auto highrow = [&](int i) {
+    auto ld_high = [&](int i, IvRaw& r) {
         i = clampi(i, n2);
-        int32_t s0, s1, d0 = 0, d1 = 0;
-        band2(lh + (uint64_t)i * lh_p, j0, w1, fq, s0, s1);
-        if (w2) band2(hh + (uint64_t)i * hh_p, j0, w2, fq, d0, d1);
-        return hinv(s0, s1, d0, d1, j0, w1);
+        r.sc = iv_ld_coef(lh + (size_t)i * lh_p, j0, w1);
+        r.d = w2 ? iv_ld_coef(hh + (size_t)i * hh_p, j0, w2) : make_uint2(0u, 0u);
     };
-    const int4 zero = make_int4(0, 0, 0, 0);
-    int4 hp = n2 ? highrow(r0 - 1) : zero, hc = n2 ? highrow(r0) : zero;
-    int4 xe = lift_even(lowrow(r0), hp, hc);
-    const bool out_lane = lane >= 1 && lane <= 30 && 2 * j0 < w;
-    const int x0 = 2 * j0;
+    auto build = [&](const IvRaw& r, bool low, int32_t* x) {
+        int32_t sv[4], dv[4];
+        if (low) {
+            sv[0] = r.s.x; sv[1] = r.s.y; sv[2] = r.s.z; sv[3] = r.s.w;
+        } else {
+            iv_dq2(r.sc.x, fq, sv[0], sv[1]);
+            iv_dq2(r.sc.y, fq, sv[2], sv[3]);
+        }
+        iv_dq2(r.d.x, fq, dv[0], dv[1]);
+        iv_dq2(r.d.y, fq, dv[2], dv[3]);
+        iv_hrow(sv, dv, j0, w1, x);
+    };
+    /* x[2 r0] = low[r0] - ((high[r0 - 1] + high[r0] + 2) >> 2) */
+    int32_t xe[8], hc[8];
+    IvRaw nl, nh; /* the next step's low and high rows, in flight */
+    {
+        IvRaw a, b, c;
+        ld_low(r0, a);
+        if (n2) {
+            ld_high(r0 - 1, b);
+            ld_high(r0, c);
+        }
+        if (r0 + 1 < n1 && 2 * r0 + 2 < h) {
+            ld_low(r0 + 1, nl);
+            if (n2) ld_high(r0 + 1, nh);
+        }
+        int32_t hp[8];
+        build(a, true, xe);
+        if (n2) {
+            build(b, false, hp);
+            build(c, false, hc);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 8; k++) hp[k] = hc[k] = 0;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) xe[k] -= (hp[k] + hc[k] + 2) >> 2;
+    }
     for (int i = r0; i < rend; i++) {
         const int y = 2 * i;
-        int4 xo = zero, xn = xe;
-        if (y + 1 < h) {
-            const int4 hcur = hc;
-            if (y + 2 < h) {
-                const int4 hn = highrow(i + 1);
-                xn = lift_even(lowrow(i + 1), hc, hn);
-                hp = hc;
-                hc = hn;
+        int32_t xo[8], xn[8];
+        if (y + 2 < h) {
+            /* x[2i + 2] from the next low and high rows */
+            int32_t hn[8];
+            build(nl, true, xn);
+            if (n2) {
+                build(nh, false, hn);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 8; k++) hn[k] = 0;
             }
-            xo = lift_odd(hcur, xe, xn);
+            if (i + 1 < rend && y + 4 < h) {
+                ld_low(i + 2, nl);
+                if (n2) ld_high(i + 2, nh);
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                xn[k] -= (hc[k] + hn[k] + 2) >> 2;
+                xo[k] = hc[k] + ((xe[k] + xn[k]) >> 1);
+                hc[k] = hn[k];
+            }
+        } else {
+            /* the last even row is its own lower neighbour */
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                xn[k] = xe[k];
+                xo[k] = hc[k] + xe[k];
+            }
         }
         if (out_lane) {
-            store4<OUT>(J, y, x0, w, xe, os);
-            if (y + 1 < h) store4<OUT>(J, y + 1, x0, w, xo, os);
+            iv_store8<OUT>(J, y, c0, w, vec, xe, os);
+            if (y + 1 < h) iv_store8<OUT>(J, y + 1, c0, w, vec, xo, os);
         }
-        xe = xn;
+#pragma unroll
+        for (int k = 0; k < 8; k++) xe[k] = xn[k];
     }
-    (void)hp;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -58,7 +58,7 @@ struct FwdVJob {
     const void* src;        /* level input: samples (level 0) or the int32 low band of the previous level */
     long long src_pitch;    /* elements */
     int chan;               /* packed input: channel of this component */
-    int vec;                /* two adjacent samples may be read with one load */
+    int vec;                /* rows may be read 8 samples per vector load (aligned planar source) */
     int w, h;               /* level input size */
     int col_tiles, first_block;
     int32_t* ll;            /* int32 low band written for the next level */
@@ -238,6 +238,8 @@ struct DecPrecLaunch {
  * first sign bits.  `end` is the size of one precinct's area; slice-ordered
  * decoding keeps the row above's GCLIs after it (top, cap_groups bytes). */
 #define UK_ZCAP(cap_groups) ((cap_groups) + 8 * JXS_MAXPK + 32)
+/* 128 list entries per warp of a 512-thread unpacking block */
+#define UK_LIST_BYTES (4 * 128 * 16)
 struct UkLayout {
     uint32_t gcl, zend, seg, cnt, base, ex, nz, sgb, ord, end, top, top_end;
 };
@@ -247,7 +249,9 @@ static inline __host__ __device__ UkLayout uk_layout(uint32_t cap_bytes, uint32_
     L.gcl = o;
     o = (o + cap_groups + 15) & ~15u;
     L.zend = o;
-    o = (o + 2 * UK_ZCAP(cap_groups) + 15) & ~15u;
+    /* the zero-bit table; in the data pass the same area holds each warp's
+     * list of groups with data (UK_LIST_BYTES) */
+    o = (o + (2 * UK_ZCAP(cap_groups) > UK_LIST_BYTES ? 2 * UK_ZCAP(cap_groups) : UK_LIST_BYTES) + 15) & ~15u;
     L.seg = o;
     o += 8 * cap_seg;
     L.cnt = o;

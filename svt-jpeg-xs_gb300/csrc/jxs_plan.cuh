@@ -79,6 +79,11 @@ static inline void level_dims(const jxs_comp_t& cp, int v, uint32_t* w, uint32_t
 
 static inline uint32_t bytes_per_sample(const jxs_cfg_t* c) { return c->depth <= 8 ? 1 : 2; }
 
+/* Row pitch (elements) of a staged input plane w elements wide: rows start
+ * on 16-byte boundaries, so that the first transform level reads them with
+ * vector loads. */
+static inline uint32_t stage_pitch(uint32_t w, uint32_t bps) { return (uint32_t)((((uint64_t)w * bps + 15) & ~15ull) / bps); }
+
 static inline uint32_t cfg_max_dv(const jxs_cfg_t* c) {
     uint32_t m = 0;
     for (uint32_t k = 0; k < c->nc; k++) m = c->comp[k].dv > m ? c->comp[k].dv : m;
@@ -217,7 +222,8 @@ static inline int plan_fwd_v(const jxs_cfg_t* c, const jxs_cfg_t* dcfg, const Fr
             J.src = in.p[pk];
             J.src_pitch = in.pitch[pk];
             J.chan = packed ? (int)k : 0;
-            J.vec = !packed && ((uintptr_t)in.p[pk] % (2 * bps)) == 0 && (in.pitch[pk] % 2) == 0;
+            /* 8 samples per vector load: 16 bytes (16-bit) or 8 bytes (8-bit) */
+            J.vec = !packed && ((uintptr_t)in.p[pk] % (8 * bps)) == 0 && (in.pitch[pk] % 8) == 0;
         } else {
             J.src = b.ll[v - 1][k];
             J.src_pitch = b.ll_pitch[v - 1][k];
