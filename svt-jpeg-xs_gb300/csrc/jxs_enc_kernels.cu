@@ -1487,18 +1487,22 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
         for (uint32_t base = sg.g0; base < gend; base += 128) {
             const uint32_t g = base + 4 * lane;
             const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
-            const uint32_t w4 = nv ? *(const uint32_t*)(grow + g) : 0u;
+            /* the lane's GCLIs, one per byte (0 past the line's end) */
+            uint32_t w4 = nv ? *(const uint32_t*)(grow + g) : 0u;
+            w4 &= nv >= 4 ? 0xffffffffu : (1u << (8 * nv)) - 1u;
             uint4 c0 = make_uint4(0, 0, 0, 0), c1 = c0;
             if (nv && fs) {
                 c0 = *(const uint4*)(crow + 4 * g);
                 c1 = *(const uint4*)(crow + 4 * g + 8);
             }
-            uint32_t v[4], m = 0;
+            /* per byte: planes above gtli d = max(v - t, 0), and v > t */
+            const uint32_t t4 = t * 0x01010101u;
+            const uint32_t d4 = __vsubus4(w4, t4), s4 = __vcmpgtu4(w4, t4);
+            const uint32_t dsum = __vsadu4(d4, 0u), nsig = __popc(s4 & 0x01010101u);
+            uint32_t v[4];
 #pragma unroll
-            for (int k = 0; k < 4; k++) {
-                v[k] = k < (int)nv ? (w4 >> (8 * k)) & 255u : 0u;
-                m = max(m, v[k]);
-            }
+            for (int k = 0; k < 4; k++) v[k] = (w4 >> (8 * k)) & 255u;
+            const uint32_t m2 = __vmaxu4(w4, w4 >> 16), m = max(m2 & 255u, (m2 >> 8) & 255u);
             const uint32_t mx = max(m, __shfl_xor_sync(FULL, m, 1));
             /* a significance group without codes: all GCLIs <= gtli, or with
              * prediction the group's flag */
@@ -1548,28 +1552,36 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
 #pragma unroll
                         for (int k = 0; k < 4; k++) vl += n4[k];
                     } else {
-                        /* unary codes: (v - t) ones then a zero (PackPrecinct.h:25-39) */
+                        /* unary codes: d ones then a zero for each present
+                         * group (PackPrecinct.h:25-39), two groups per word */
+                        uint32_t n[4], c[4];
 #pragma unroll
                         for (int k = 0; k < 4; k++) {
-                            if (k < (int)nv) {
-                                const uint32_t n = v[k] > t ? v[k] - t + 1 : 1u;
-                                vacc = (vacc << n) | (((1ull << (n - 1)) - 1) << 1);
-                                vl += n;
-                            }
+                            const uint32_t dk = (d4 >> (8 * k)) & 255u;
+                            n[k] = k < (int)nv ? dk + 1 : 0u;
+                            c[k] = ((1u << dk) - 1u) << 1;
                         }
+                        const uint32_t l23 = n[2] + n[3];
+                        vacc = ((uint64_t)((c[0] << n[1]) | c[1]) << l23) | ((c[2] << n[3]) | c[3]);
+                        vl = dsum + nv;
                     }
                 }
             }
-            uint32_t dl = 0;
-#pragma unroll
-            for (int k = 0; k < 4; k++) dl += (k < (int)nv && v[k] > t) ? 4 * (v[k] - t + 1 - fs) : 0u;
+            /* data bits of the groups above gtli: 4 (d + 1) each (the sign
+             * nibble, unless signs go to their own sub-packet) */
+            const uint32_t dl4 = dsum + (fs ? 0u : nsig);
+            /* one scan for three running sums: data bits / 4 (12 bits), code
+             * bits (13 bits), listed groups (the exclusive sums, at most 124,
+             * in the top 7 bits) */
             uint32_t tot;
-            const uint32_t ex = warp_excl_scan((dl << 16) | vl, &tot);
+            const uint32_t ex = warp_excl_scan(dl4 | (vl << 12) | (nsig << 25), &tot);
+            const uint32_t ex_d = (ex & 0xfffu) << 2, ex_v = (ex >> 12) & 0x1fffu;
+            const uint32_t tot_d = (tot & 0xfffu) << 2, tot_v = (tot >> 12) & 0x1fffu;
             if (vl) {
                 if (VPRED && (L.meth & 1)) {
                     /* prediction codes (up to 31 bits each): n - 1 ones then
                      * a zero, joined while they fit 64 bits */
-                    uint32_t pos = vpos + (ex & 0xffffu), an = 0;
+                    uint32_t pos = vpos + ex_v, an = 0;
                     uint64_t acc = 0;
 #pragma unroll
                     for (int k = 0; k < 4; k++) {
@@ -1587,7 +1599,7 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                     }
                     if (an) put_bits(buf, words, pos, acc, an, ovf);
                 } else {
-                    put_bits(buf, words, vpos + (ex & 0xffffu), vacc, vl, ovf);
+                    put_bits(buf, words, vpos + ex_v, vacc, vl, ovf);
                 }
             }
             uint32_t sbits = 0, sn = 0;
@@ -1598,18 +1610,11 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                  * nibble and planes in one write of at most 64 bits; the
                  * coefficients of the other groups are never read */
                 uint32_t* list = &s_segw[0][0] + 128 * warp;
-                const uint32_t lt = (1u << lane) - 1u;
-                uint32_t cnt = 0, idx = 0, o = ex >> 16;
+                const uint32_t cnt = __reduce_add_sync(FULL, nsig);
+                uint32_t idx = ex >> 25, o = ex_d;
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
-                    const bool sk = k < (int)nv && v[k] > t;
-                    const uint32_t bk = __ballot_sync(FULL, sk);
-                    idx += __popc(bk & lt);
-                    cnt += __popc(bk);
-                }
-#pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    if (k < (int)nv && v[k] > t) {
+                    if ((s4 >> (8 * k)) & 1u) {
                         list[idx++] = (o << 11) | ((uint32_t)(4 * lane + k) << 4) | v[k];
                         o += 4 * (v[k] - t + 1);
                     }
@@ -1625,10 +1630,10 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                     put_bits(buf, words, dpos + (e >> 11), ch, 4 * (np + 1), ovf);
                 }
                 __syncwarp();
-            } else if (dl) {
+            } else if (dl4) {
                 /* data bits of the groups with gcli > gtli (pack_data_c,
                  * PackPrecinct.c:128-198), joined while they fit 64 bits */
-                uint32_t pos = dpos + (ex >> 16);
+                uint32_t pos = dpos + ex_d;
                 uint64_t acc = 0;
                 uint32_t an = 0;
                 const uint2 cw[4] = {make_uint2(c0.x, c0.y), make_uint2(c0.z, c0.w), make_uint2(c1.x, c1.y), make_uint2(c1.z, c1.w)};
@@ -1662,8 +1667,8 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                 }
                 if (an) put_bits(buf, words, pos, acc, an, ovf);
             }
-            vpos += tot & 0xffffu;
-            dpos += tot >> 16;
+            vpos += tot_v;
+            dpos += tot_d;
             if (fs) {
                 /* sign sub-packet (pack_sign_c, PackPrecinct.c:200-233) */
                 uint32_t stot;

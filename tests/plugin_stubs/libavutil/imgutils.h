@@ -1,0 +1,2 @@
+/* Test stand-in: see ffstub.h. */
+#include "../ffstub.h"
