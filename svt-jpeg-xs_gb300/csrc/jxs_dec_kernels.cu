@@ -557,14 +557,27 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         __syncthreads();
     }
 
-    /* zero bits of the VLC sub-packets: count, scan, record positions */
+    /* zero bits of the VLC sub-packets: count, scan, record positions.  A
+     * thread's first word finds its packet by binary search over the
+     * packets' word ranges (contiguous, in packet order; a packet without
+     * VLC words has an empty range), later words step forward. */
     const uint32_t per = (tw + blockDim.x - 1) / blockDim.x;
     const uint32_t wa = min(tw, threadIdx.x * per), we = min(tw, wa + per);
+    uint32_t k0 = 0;
+    if (wa < we) {
+        uint32_t lo = 0, hi = npk - 1; /* the first packet whose range ends past wa */
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (pk[mid].wbase + pk[mid].nwords > wa) hi = mid;
+            else lo = mid + 1;
+        }
+        k0 = lo;
+    }
     uint32_t zc = 0;
     {
-        uint32_t k = 0;
+        uint32_t k = k0;
         for (uint32_t wi = wa; wi < we; wi++) {
-            while (k + 1 < npk && (!pk[k].present || pk[k].raw || wi >= pk[k].wbase + pk[k].nwords)) k++;
+            while (k + 1 < npk && wi >= pk[k].wbase + pk[k].nwords) k++;
             const uint32_t i = wi - pk[k].wbase;
             const uint32_t valid = min(32u, pk[k].gbits - 32 * i);
             uint32_t z = ~bits32_at(pbuf, pk[k].gpos + 32 * i);
@@ -575,9 +588,9 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     uint32_t z0;
     const uint32_t ztotal = block_scan1(zc, &z0, ws);
     {
-        uint32_t k = 0;
+        uint32_t k = k0;
         for (uint32_t wi = wa; wi < we; wi++) {
-            while (k + 1 < npk && (!pk[k].present || pk[k].raw || wi >= pk[k].wbase + pk[k].nwords)) k++;
+            while (k + 1 < npk && wi >= pk[k].wbase + pk[k].nwords) k++;
             const uint32_t i = wi - pk[k].wbase;
             if (i == 0) pk[k].zbase = z0;
             const uint32_t valid = min(32u, pk[k].gbits - 32 * i);
@@ -658,23 +671,24 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
             }
             const uint32_t bal = __ballot_sync(FULL, coded);
             if (coded) {
-                /* codeword c + q ends at the (c + q)-th zero bit */
+                /* codeword c + q ends at the (c + q)-th zero bit: its value
+                 * is the distance to the zero before, less one; the four
+                 * distances as 16-bit pairs */
                 const uint32_t c = cw + 4 * __popc(bal & lt_mask);
                 const uint32_t zr = P.zbase + c;
-                int prev = c ? (int)zend[zr - 1] : -1;
+                const uint32_t zm = c ? zend[zr - 1] : 0xffffu; /* -1 */
+                uint32_t z[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    if (q < (int)nv) {
-                        const int e = (int)zend[zr + q];
-                        uint32_t v = (L.vp ? 0u : L.t) + (uint32_t)(e - prev - 1);
-                        if (v > (L.vp ? 31u : 15u)) {
-                            bad = 1;
-                            v = L.vp ? 31u : 15u;
-                        }
-                        v4 |= v << (8 * q);
-                        prev = e;
-                    }
-                }
+                for (int q = 0; q < 4; q++) z[q] = q < (int)nv ? zend[zr + q] : 0u;
+                const uint32_t r01 = __vsub2(__vsub2(z[0] | (z[1] << 16), zm | (z[0] << 16)), 0x00010001u);
+                const uint32_t r23 = __vsub2(__vsub2(z[2] | (z[3] << 16), z[1] | (z[2] << 16)), 0x00010001u);
+                /* GCLI = base + r, at most 15 (31 for a predicted line's
+                 * codeword value) */
+                const uint32_t base = L.vp ? 0u : L.t, room = (L.vp ? 31u : 15u) - base;
+                const uint32_t room2 = room * 0x00010001u, base2 = base * 0x00010001u;
+                const uint32_t keep = nv >= 4 ? 0xffffffffu : (1u << (8 * nv)) - 1u;
+                if (__byte_perm(__vcmpgtu2(r01, room2), __vcmpgtu2(r23, room2), 0x6420) & keep) bad = 1;
+                v4 = __byte_perm(__vadd2(__vminu2(r01, room2), base2), __vadd2(__vminu2(r23, room2), base2), 0x6420) & keep;
             }
             uint8_t* gdst = gcl + B.gbase + g0;
             if (nv == 4) {
@@ -683,10 +697,12 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                 for (uint32_t q = 0; q < nv; q++) gdst[q] = (uint8_t)(v4 >> (8 * q));
             }
             cw += __reduce_add_sync(FULL, coded ? nv : 0u);
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const uint32_t v = (v4 >> (8 * q)) & 255u;
-                if (!L.vp && q < (int)nv && v > L.t) dsum += 4 * (v - L.t + nib_sign);
+            if (!L.vp) {
+                /* data bits: 4 (v - t + 1) per group above gtli (4 (v - t)
+                 * with separate signs) */
+                const uint32_t t4 = L.t * 0x01010101u;
+                const uint32_t vm = v4 & (nv >= 4 ? 0xffffffffu : (1u << (8 * nv)) - 1u);
+                dsum += 4 * (__vsadu4(__vsubus4(vm, t4), 0u) + nib_sign * __popc(__vcmpgtu4(vm, t4) & 0x01010101u));
             }
         }
         dsum = __reduce_add_sync(FULL, dsum);
@@ -820,15 +836,13 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                 } else {
                     for (uint32_t q = 0; q < nv; q++) v4 |= (uint32_t)gcl[B.gbase + g + q] << (8 * q);
                 }
-                uint32_t len[4], lsum = 0;
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const uint32_t v = (v4 >> (8 * q)) & 255u;
-                    len[q] = (q < (int)nv && v > t) ? 4 * (v - t + 1) : 0u;
-                    lsum += len[q];
-                }
+                /* per byte: v > t, and the data of such a group: 4 (v - t + 1)
+                 * bits; one scan for the data bits / 4 and the listed groups */
+                const uint32_t t4 = t * 0x01010101u;
+                const uint32_t s4 = __vcmpgtu4(v4, t4), nsig = __popc(s4 & 0x01010101u);
                 uint32_t tot;
-                uint32_t o = warp_excl_scan(lsum, &tot);
+                const uint32_t ex = warp_excl_scan((__vsadu4(__vsubus4(v4, t4), 0u) + nsig) | (nsig << 24), &tot);
+                uint32_t o = (ex & 0xffffffu) << 2;
                 /* zeros for the lane's groups (those with data are written
                  * again below, after the warp barrier) */
                 if (one_col) {
@@ -843,20 +857,16 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                      * next begins: the groups' coefficients inside it only */
                     const int wl = (int)B.w - 4 * (int)g;
                     for (int c = 0; c < 4 * (int)nv && c < wl; c++)
-                        if (!len[c >> 2]) crow[4 * g + c] = 0;
+                        if (!((s4 >> (8 * (c >> 2))) & 1u)) crow[4 * g + c] = 0;
                 }
-                uint32_t idx = 0, cnt = 0;
+                const uint32_t cnt = tot >> 24;
+                uint32_t idx = ex >> 24;
 #pragma unroll
                 for (int q = 0; q < 4; q++) {
-                    const uint32_t bq = __ballot_sync(FULL, len[q] != 0);
-                    idx += __popc(bq & lt_mask);
-                    cnt += __popc(bq);
-                }
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    if (len[q]) {
-                        list[idx++] = (o << 11) | ((uint32_t)(4 * lane + q) << 4) | ((v4 >> (8 * q)) & 15u);
-                        o += len[q];
+                    if ((s4 >> (8 * q)) & 1u) {
+                        const uint32_t v = (v4 >> (8 * q)) & 255u;
+                        list[idx++] = (o << 11) | ((uint32_t)(4 * lane + q) << 4) | (v & 15u);
+                        o += 4 * (v - t + 1);
                     }
                 }
                 __syncwarp();
@@ -879,7 +889,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                     }
                 }
                 __syncwarp();
-                dpos += tot;
+                dpos += (tot & 0xffffffu) << 2;
             }
             continue;
         }

@@ -50,6 +50,39 @@ extern "C" int jxs_gpu_is_device_ptr(const void* p) {
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
+/* Host memory the copy engines reach asynchronously: page-locked
+ * (cudaMallocHost) or registered.  Ordinary (pageable) memory is not. */
+extern "C" int jxs_gpu_is_page_locked(const void* p) {
+    if (!p) return 0;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+/* A device-to-host copy into pageable memory, left for the frame's
+ * completion: cudaMemcpy*Async into pageable memory returns only once the
+ * copy is done, which would make the submitting call wait for the whole
+ * frame.  The completion thread copies once the frame's work has finished. */
+struct DeferredCopy {
+    void* dst;
+    size_t dpitch;
+    const void* src;
+    size_t spitch, width, height;
+};
+static int run_deferred(DeferredCopy* d, int* n) {
+    int ok = 1;
+    for (int i = 0; i < *n; i++)
+        if (cudaMemcpy2D(d[i].dst, d[i].dpitch, d[i].src, d[i].spitch, d[i].width, d[i].height, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            cudaGetLastError();
+            ok = 0;
+        }
+    *n = 0;
+    return ok;
+}
+
 extern "C" void* jxs_gpu_host_alloc(size_t n) {
     void* p = NULL;
     if (cudaMallocHost(&p, n) != cudaSuccess) {
@@ -98,6 +131,8 @@ struct EncSlot {
     uint8_t* out_stage;
     int* status_h;
     int busy;
+    DeferredCopy defer[1];  /* the codestream, for a pageable destination */
+    int ndefer;
     cudaEvent_t tev[6];
     cudaEvent_t kev[JXS_KEV];   /* timing mode: before the first kernel and after each */
     int nkev;
@@ -245,6 +280,7 @@ extern "C" jxs_gpu_enc_t* jxs_gpu_enc_create(const jxs_cfg_t* cfg, int nslots, i
 }
 
 static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], const uint32_t strides[4], uint8_t* out) {
+    s->ndefer = 0;
     const jxs_cfg_t* c = &e->cfg;
     const int packed = c->fmt == COLOUR_FORMAT_PACKED_YUV444_OR_RGB;
     const uint32_t bps = bytes_per_sample(c);
@@ -325,7 +361,11 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
     CK(jxs_launch_pack(e->dcfg, c->np, s->coef, s->gcli, s->rc, s->cost, dst, e->cap_words, s->status, c->vpred ? 2 : 0, st));
     KMARK();
     TMARK(4);
-    if (!out_dev) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));
+    s->ndefer = 0;
+    if (!out_dev) {
+        if (jxs_gpu_is_page_locked(out)) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));
+        else s->defer[s->ndefer++] = DeferredCopy{out, c->lcod, s->out_stage, c->lcod, c->lcod, 1};
+    }
     CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
     TMARK(5);
 #undef TMARK
@@ -344,6 +384,11 @@ extern "C" int32_t jxs_gpu_enc_wait(jxs_gpu_enc_t* e, int slot) {
     EncSlot* s = &e->slot[slot];
     if (cudaEventSynchronize(s->done) != cudaSuccess) {
         fprintf(stderr, "jxs: encode failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+        s->ndefer = 0;
+        return JXS_E_ENC_FRAME;
+    }
+    if (!run_deferred(s->defer, &s->ndefer)) {
+        fprintf(stderr, "jxs: copying the codestream to host memory failed\n");
         return JXS_E_ENC_FRAME;
     }
     s->busy = 0;
@@ -445,6 +490,8 @@ struct DecSlot {
     int arg_walked;         /* precinct offsets in prec_off_h */
     void* arg_planes[4];
     uint32_t arg_strides[4];
+    DeferredCopy defer[JXS_MAXC]; /* output planes in pageable memory */
+    int ndefer;
     cudaEvent_t tev[5];
     cudaEvent_t kev[JXS_KEV];
     int nkev;
@@ -607,6 +654,7 @@ extern "C" jxs_gpu_dec_t* jxs_gpu_dec_create(const jxs_cfg_t* cfg, int nslots, i
 
 static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t size, const uint32_t* prec_off,
                        void* const planes[4], const uint32_t strides[4]) {
+    s->ndefer = 0;
     const jxs_cfg_t* c = &d->cfg;
     const uint32_t bps = bytes_per_sample(c);
     const cudaStream_t st = dec_stream(d, s);
@@ -742,11 +790,16 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         CK(jxs_launch_nlt_out(&P, st));
     }
     TMARK(3);
+    s->ndefer = 0;
     for (uint32_t k = 0; k < c->nc; k++) {
         if (out_dev[k]) continue;
         const uint32_t ow = jxs_out_w(c, k), oh = jxs_out_h(c, k);
-        CK(cudaMemcpy2DAsync(planes[k], (size_t)strides[k] * bps, s->out_stage + s->out_off[k], (size_t)stage_pitch(ow, bps) * bps,
-                             (size_t)ow * bps, oh, cudaMemcpyDeviceToHost, st));
+        const DeferredCopy cp{planes[k], (size_t)strides[k] * bps, s->out_stage + s->out_off[k], (size_t)stage_pitch(ow, bps) * bps,
+                              (size_t)ow * bps, oh};
+        if (jxs_gpu_is_page_locked(planes[k]))
+            CK(cudaMemcpy2DAsync(cp.dst, cp.dpitch, cp.src, cp.spitch, cp.width, cp.height, cudaMemcpyDeviceToHost, st));
+        else
+            s->defer[s->ndefer++] = cp;
     }
     CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
     TMARK(4);
@@ -765,6 +818,7 @@ extern "C" int32_t jxs_gpu_dec_wait(jxs_gpu_dec_t* d, int slot) {
     DecSlot* s = &d->slot[slot];
     if (cudaEventSynchronize(s->done) != cudaSuccess) {
         fprintf(stderr, "jxs: decode failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+        s->ndefer = 0;
         return JXS_E_DEC_INTERNAL;
     }
     if (*s->status_h == JXS_E_DEC_VPRED) {
@@ -776,8 +830,13 @@ extern "C" int32_t jxs_gpu_dec_wait(jxs_gpu_dec_t* d, int slot) {
         if (r != JXS_OK) return r;
         if (cudaEventSynchronize(s->done) != cudaSuccess) {
             fprintf(stderr, "jxs: decode failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+            s->ndefer = 0;
             return JXS_E_DEC_INTERNAL;
         }
+    }
+    if (!run_deferred(s->defer, &s->ndefer)) {
+        fprintf(stderr, "jxs: copying the decoded planes to host memory failed\n");
+        return JXS_E_DEC_INTERNAL;
     }
     if (s->timed) {
         float ms[DEC_STAGES];

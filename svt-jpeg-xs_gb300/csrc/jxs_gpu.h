@@ -67,6 +67,7 @@ uint64_t jxs_gpu_dec_read_timing(jxs_gpu_dec_t* d, double* ms, int n);
 
 /* 1 if p is memory of this process's current CUDA device. */
 int jxs_gpu_is_device_ptr(const void* p);
+int jxs_gpu_is_page_locked(const void* p);
 
 /* Host and device copies of a decoder's configuration. */
 const jxs_cfg_t* jxs_gpu_dec_cfg(jxs_gpu_dec_t* d, const jxs_cfg_t** dev_cfg);
