@@ -845,11 +845,12 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     /* with sign handling each packet adds its sign sub-packet, rounded on
      * its own: fast signs in dC, full signs in dF (RateControl.c:745-756) */
     const uint32_t npk = cfg->npk;
-    for (uint32_t e = threadIdx.x; e < (uint32_t)nq * npk; e += blockDim.x) {
-        const int q = (int)(e / npk);
-        const uint32_t k = e - (uint32_t)q * npk;
+    /* a warp per packet, a lane per Q (at most 32): the packet's band lines
+     * are the same for the whole warp */
+    for (uint32_t k = warp; k < npk; k += RC_WARPS) {
+        const int q = lane;
         const uint32_t b0 = s_pkbl0[k], nb = s_pknbl[k];
-        if (!nb) continue;
+        if (!nb || q >= nq) continue;
         uint32_t db = 0, gb = 0, sb = 0, fb = 0, zb = 0;
         for (uint32_t x = b0; x < b0 + nb; x++) {
             const int g = lgain[x];

@@ -50,6 +50,17 @@ DEV int mirror_idx(int i, int n) {
     return i < n ? i : p - i;
 }
 
+/* The same for the indices a strip reads (-n < i < 2n - 1: one reflection)
+ * without a division; other indices (levels of one or two samples) take the
+ * general form out of line, so that the division is never inlined into the
+ * loops. */
+__device__ __noinline__ int mirror_far(int i, int n) { return mirror_idx(i, n); }
+DEV int mirror1(int i, int n) {
+    const int a = i < 0 ? -i : i;
+    const int m = a < n ? a : 2 * (n - 1) - a;
+    return (unsigned)m < (unsigned)n ? m : mirror_far(i, n);
+}
+
 DEV uint32_t to_sm(int32_t v) {
     const uint32_t m = ((uint32_t)abs(v) + 128u) >> 8;
     return m ? (m | (((uint32_t)v >> 16) & 0x8000u)) : 0u;
@@ -176,25 +187,34 @@ DEV uint32_t raw1(const void* row, int chan, int x) {
 
 template <int SRC> DEV size_t src_elem() { return SRC == SRC_I32 ? 4 : (SRC == SRC_U16 || SRC == SRC_PK16) ? 2 : 1; }
 
+/* A strip's input: base, row pitch in bytes, width and channel, held in
+ * registers for the whole strip. */
+struct FvSrc {
+    const char* base;
+    size_t pitch;
+    int w, chan;
+};
+
 /* Loads row y (in range) for the lane's columns c0 .. c0 + 7: one or two
- * vector loads when `fast` (all 8 columns inside, aligned), else one load per
- * column with the symmetric extension. */
-template <int SRC>
-DEV void fv_load(const FwdVJob& J, int y, int c0, bool fast, uint32_t* r) {
-    const char* row = (const char*)J.src + (size_t)y * (size_t)J.src_pitch * src_elem<SRC>();
+ * vector loads when the lane's 8 columns are inside and the rows aligned
+ * (`fast`; always so in a FAST strip), else one load per column with the
+ * symmetric extension. */
+template <int SRC, bool FAST>
+DEV void fv_load(const FvSrc& S, int y, int c0, bool fast, uint32_t* r) {
+    const char* row = S.base + (size_t)y * S.pitch;
     if constexpr (SRC == SRC_I32) {
-        if (fast) {
+        if (FAST || fast) {
             const int4 a = *(const int4*)((const int32_t*)row + c0), b = *(const int4*)((const int32_t*)row + c0 + 4);
             r[0] = a.x; r[1] = a.y; r[2] = a.z; r[3] = a.w;
             r[4] = b.x; r[5] = b.y; r[6] = b.z; r[7] = b.w;
         } else {
 #pragma unroll
-            for (int k = 0; k < 8; k++) r[k] = raw1<SRC>(row, 0, mirror_idx(c0 + k, J.w));
+            for (int k = 0; k < 8; k++) r[k] = raw1<SRC>(row, 0, mirror1(c0 + k, S.w));
         }
-    } else if (fast && SRC == SRC_U16) {
+    } else if ((FAST || fast) && SRC == SRC_U16) {
         const uint4 q = *(const uint4*)((const uint16_t*)row + c0);
         r[0] = q.x; r[1] = q.y; r[2] = q.z; r[3] = q.w;
-    } else if (fast && SRC == SRC_U8) {
+    } else if ((FAST || fast) && SRC == SRC_U8) {
         const uint2 q = *(const uint2*)((const uint8_t*)row + c0);
         r[0] = __byte_perm(q.x, 0, 0x4140);
         r[1] = __byte_perm(q.x, 0, 0x4342);
@@ -203,7 +223,7 @@ DEV void fv_load(const FwdVJob& J, int y, int c0, bool fast, uint32_t* r) {
     } else {
 #pragma unroll
         for (int k = 0; k < 4; k++)
-            r[k] = raw1<SRC>(row, J.chan, mirror_idx(c0 + 2 * k, J.w)) | (raw1<SRC>(row, J.chan, mirror_idx(c0 + 2 * k + 1, J.w)) << 16);
+            r[k] = raw1<SRC>(row, S.chan, mirror1(c0 + 2 * k, S.w)) | (raw1<SRC>(row, S.chan, mirror1(c0 + 2 * k + 1, S.w)) << 16);
     }
 }
 
@@ -258,35 +278,42 @@ DEV FvBand fv_band(const jxs_band_t& bd, int row, uint16_t* coef, uint8_t* gcli)
     b.gw = (int)bd.gcli_w;
     return b;
 }
+template <bool FAST>
 DEV void fv_emit(const FvBand& b, int j, const int32_t* v) {
-    emit4(BandRow{b.crow, b.grow, b.w, b.gw}, j, v[0], v[1], v[2], v[3]);
+    if constexpr (FAST) {
+        /* the whole group inside the band */
+        const uint32_t c0 = to_sm(v[0]), c1 = to_sm(v[1]), c2 = to_sm(v[2]), c3 = to_sm(v[3]);
+        *(uint2*)(b.crow + j) = make_uint2(c0 | (c1 << 16), c2 | (c3 << 16));
+        b.grow[j >> 2] = (uint8_t)(32 - __clz((c0 | c1 | c2 | c3) & 0x7fffu));
+    } else {
+        emit4(BandRow{b.crow, b.grow, b.w, b.gw}, j, v[0], v[1], v[2], v[3]);
+    }
 }
 DEV void fv_next(FvBand& b) {
     b.crow += b.pitch;
     b.grow += b.gpitch;
 }
 
-template <int SRC, int NJ>
-__global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant__ FwdVLaunchN<NJ> L) {
-    const FwdVJob& J = L.job[find_job<NJ>(L.job, L.njobs, (int)blockIdx.x)];
-    const int u = blockIdx.x - J.first_block;
-    const int ty = u / J.col_tiles, tx = u - ty * J.col_tiles;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int w = J.w, h = J.h, n1 = (h + 1) >> 1, n2 = h >> 1;
-    const int r0 = (ty * FV_WARPS + warp) * FV_WROWPAIRS;
-    if (r0 >= n1) return; /* the whole warp */
-    const int rend = min(r0 + FV_WROWPAIRS, n1);
-    const int c0 = tx * FV_COLS - 8 + 8 * lane;
-    const bool fast = J.vec && c0 >= 0 && c0 + 8 <= w;
+/* One warp's strip: row pairs r0 .. rend - 1 of columns c0 (this lane) of
+ * job J.  FAST: the strip is away from the level's left and right edges
+ * (every lane's 8 columns and every output group inside), so that no load
+ * or store needs a check. */
+template <int SRC, bool FAST>
+DEV void fv_strip(const FwdVJob& J, int r0, int rend, int c0) {
+    const int lane = threadIdx.x & 31;
+    const int h = J.h, n2 = h >> 1;
+    const FvSrc S{(const char*)J.src, (size_t)J.src_pitch * src_elem<SRC>(), J.w, J.chan};
+    const bool fast = J.vec && c0 >= 0 && c0 + 8 <= J.w;
     const uint32_t mask = (1u << J.depth) - 1u;
     const int32_t mul = 1 << (20 - J.depth);
     /* output: pairs jj .. jj + 3 of the level's bands (one group), lanes 1..30 */
-    const int jj = c0 >> 1, w1 = (w + 1) >> 1;
-    const bool out_lane = lane >= 1 && lane <= 30 && c0 < w;
+    const int jj = c0 >> 1, w1 = (J.w + 1) >> 1;
+    const bool out_lane = lane >= 1 && lane <= 30 && c0 < J.w;
     FvBand bhl = fv_band(J.bands[J.b_hl], r0, J.coef, J.gcli);
     FvBand blh = fv_band(J.bands[J.b_lh], r0, J.coef, J.gcli);
     FvBand bhh = fv_band(J.bands[J.b_hh], r0, J.coef, J.gcli);
-    int32_t* ll = J.ll + (size_t)r0 * J.ll_pitch + jj;
+    const int ll_pitch = J.ll_pitch;
+    int32_t* ll = J.ll + (size_t)r0 * ll_pitch + jj;
     const int N = FvRaw<SRC>::N;
 
     /* x[2 r0] and d[r0 - 1] (rows 2 r0 - 2, 2 r0 - 1 mirrored at the top);
@@ -295,11 +322,11 @@ __global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant
     uint32_t ra[N], rb[N];
     {
         uint32_t q0[N], q1[N], q2[N];
-        fv_load<SRC>(J, mirror_idx(2 * r0 - 2, h), c0, fast, q0);
-        fv_load<SRC>(J, mirror_idx(2 * r0 - 1, h), c0, fast, q1);
-        fv_load<SRC>(J, 2 * r0, c0, fast, q2);
-        fv_load<SRC>(J, mirror_idx(2 * r0 + 1, h), c0, fast, ra);
-        fv_load<SRC>(J, mirror_idx(2 * r0 + 2, h), c0, fast, rb);
+        fv_load<SRC, FAST>(S, mirror1(2 * r0 - 2, h), c0, fast, q0);
+        fv_load<SRC, FAST>(S, mirror1(2 * r0 - 1, h), c0, fast, q1);
+        fv_load<SRC, FAST>(S, 2 * r0, c0, fast, q2);
+        fv_load<SRC, FAST>(S, mirror1(2 * r0 + 1, h), c0, fast, ra);
+        fv_load<SRC, FAST>(S, mirror1(2 * r0 + 2, h), c0, fast, rb);
         int32_t xa[8], xb[8];
         fv_decode<SRC>(q0, mask, mul, xa);
         fv_decode<SRC>(q1, mask, mul, xb);
@@ -312,8 +339,10 @@ __global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant
         fv_decode<SRC>(ra, mask, mul, xo);
         fv_decode<SRC>(rb, mask, mul, xn);
         if (i + 1 < rend) {
-            fv_load<SRC>(J, mirror_idx(2 * i + 3, h), c0, fast, ra);
-            fv_load<SRC>(J, mirror_idx(2 * i + 4, h), c0, fast, rb);
+            /* rows 2i + 3, 2i + 4, mirrored past the bottom */
+            const int ya = 2 * i + 3, yb = 2 * i + 4;
+            fv_load<SRC, FAST>(S, ya < h ? ya : mirror1(ya, h), c0, fast, ra);
+            fv_load<SRC, FAST>(S, yb < h ? yb : mirror1(yb, h), c0, fast, rb);
         }
         /* vertical lifting: high d[i], low s[i] */
         int32_t d[8], s[8];
@@ -328,8 +357,8 @@ __global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant
         int32_t hs[4], hd[4];
         fv_hlift(s, hs, hd);
         if (out_lane) {
-            fv_emit(bhl, jj, hd);
-            if (jj + 3 < w1) {
+            fv_emit<FAST>(bhl, jj, hd);
+            if (FAST || jj + 3 < w1) {
                 *(int4*)ll = make_int4(hs[0], hs[1], hs[2], hs[3]);
             } else {
                 for (int q = 0; q < 4; q++)
@@ -340,15 +369,32 @@ __global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant
         if (i < n2) {
             fv_hlift(d, hs, hd);
             if (out_lane) {
-                fv_emit(blh, jj, hs);
-                fv_emit(bhh, jj, hd);
+                fv_emit<FAST>(blh, jj, hs);
+                fv_emit<FAST>(bhh, jj, hd);
             }
         }
         fv_next(bhl);
         fv_next(blh);
         fv_next(bhh);
-        ll += J.ll_pitch;
+        ll += ll_pitch;
     }
+}
+
+template <int SRC, int NJ>
+__global__ void __launch_bounds__(FV_THREADS) fwd_v_kernel(const __grid_constant__ FwdVLaunchN<NJ> L) {
+    const FwdVJob& J = L.job[find_job<NJ>(L.job, L.njobs, (int)blockIdx.x)];
+    const int u = blockIdx.x - J.first_block;
+    const int ty = u / J.col_tiles, tx = u - ty * J.col_tiles;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n1 = (J.h + 1) >> 1;
+    const int r0 = (ty * FV_WARPS + warp) * FV_WROWPAIRS;
+    if (r0 >= n1) return; /* the whole warp */
+    const int rend = min(r0 + FV_WROWPAIRS, n1);
+    const int first = tx * FV_COLS, c0 = first - 8 + 8 * lane;
+    /* the strip's 256 columns first - 8 .. first + 247 all inside: the
+     * whole warp takes the path without checks */
+    if (J.vec && first >= 8 && first + FV_COLS + 8 <= J.w) fv_strip<SRC, true>(J, r0, rend, c0);
+    else fv_strip<SRC, false>(J, r0, rend, c0);
 }
 
 /* ------------------------------------------------------------------------ */

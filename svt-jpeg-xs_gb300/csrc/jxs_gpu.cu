@@ -62,6 +62,69 @@ extern "C" int jxs_gpu_is_page_locked(const void* p) {
     return a.type == cudaMemoryTypeHost;
 }
 
+/* Copies between device memory and ordinary (pageable) host memory.  On a
+ * GB300 behind NVLink-C2C with the host's page tables shared with the GPU
+ * (cudaDevAttrPageableMemoryAccessUsesHostPageTables), a kernel reads and
+ * writes pageable memory directly: the copy is ordered in the frame's
+ * stream like any kernel and the calling thread does not wait.  The CUDA
+ * copy of pageable memory instead stages it through the driver and, from
+ * the device, returns only once the copy is done.  The caller's buffers are
+ * the library's until the frame is returned, as with the reference
+ * (EncHandle.c:1006 keeps only the input structure, and its workers read
+ * the planes later). */
+__global__ void __launch_bounds__(256) host_copy16_kernel(uint8_t* dst, size_t dpitch, const uint8_t* src, size_t spitch,
+                                                          uint32_t chunks) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x < chunks) *(uint4*)(dst + y * dpitch + 16 * (size_t)x) = *(const uint4*)(src + y * spitch + 16 * (size_t)x);
+}
+__global__ void __launch_bounds__(256) host_copy1_kernel(uint8_t* dst, size_t dpitch, const uint8_t* src, size_t spitch,
+                                                         uint32_t width) {
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+    if (x < width) dst[y * dpitch + x] = src[y * spitch + x];
+}
+
+/* 1: kernels may access this device's pageable host memory through the
+ * host's page tables (queried once per device) */
+static int pageable_direct(void) {
+    static std::atomic<int> q[JXS_MAX_DEV];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= JXS_MAX_DEV) {
+        cudaGetLastError();
+        return 0;
+    }
+    int v = q[dev].load();
+    if (v == 0) {
+        int a = 0, b = 0;
+        if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+            cudaGetLastError();
+            a = b = 0;
+        }
+        v = (a && b) ? 1 : 2;
+        q[dev].store(v);
+    }
+    return v == 1;
+}
+
+/* A 2-D copy with one side in pageable host memory by a copy kernel when
+ * the device reaches pageable memory directly; returns 0 when it does not
+ * (the caller then copies another way). */
+static int host_copy_kernel(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t rows, cudaStream_t st,
+                            cudaError_t* err) {
+    *err = cudaSuccess;
+    if (!pageable_direct()) return 0;
+    if (!width || !rows) return 1;
+    if (rows > 65535 || width > 0xffffffffull) return 0;
+    /* a thread per 16-byte chunk (or byte), a grid row per row */
+    const int v16 = (((uintptr_t)dst | (uintptr_t)src | dpitch | spitch | width) & 15) == 0;
+    const size_t items = v16 ? width / 16 : width;
+    const dim3 grid((unsigned)((items + 255) / 256), (unsigned)rows);
+    if (v16) host_copy16_kernel<<<grid, 256, 0, st>>>((uint8_t*)dst, dpitch, (const uint8_t*)src, spitch, (uint32_t)items);
+    else host_copy1_kernel<<<grid, 256, 0, st>>>((uint8_t*)dst, dpitch, (const uint8_t*)src, spitch, (uint32_t)items);
+    *err = cudaGetLastError();
+    return 1;
+}
+
 /* A device-to-host copy into pageable memory, left for the frame's
  * completion: cudaMemcpy*Async into pageable memory returns only once the
  * copy is done, which would make the submitting call wait for the whole
@@ -303,8 +366,13 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
         } else {
             uint8_t* d = s->in_stage + s->in_off[k];
             const uint32_t sp = packed ? w : stage_pitch(w, bps);
-            CK(cudaMemcpy2DAsync(d, (size_t)sp * bps, planes[k], (size_t)strides[k] * bps, (size_t)w * bps, h,
-                                 cudaMemcpyHostToDevice, st));
+            cudaError_t ce = cudaSuccess;
+            if (!jxs_gpu_is_page_locked(planes[k]) &&
+                host_copy_kernel(d, (size_t)sp * bps, planes[k], (size_t)strides[k] * bps, (size_t)w * bps, h, st, &ce))
+                CK(ce);
+            else
+                CK(cudaMemcpy2DAsync(d, (size_t)sp * bps, planes[k], (size_t)strides[k] * bps, (size_t)w * bps, h,
+                                     cudaMemcpyHostToDevice, st));
             src[k] = d;
             pitch[k] = sp;
         }
@@ -363,7 +431,9 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
     TMARK(4);
     s->ndefer = 0;
     if (!out_dev) {
+        cudaError_t ce = cudaSuccess;
         if (jxs_gpu_is_page_locked(out)) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));
+        else if (host_copy_kernel(out, c->lcod, s->out_stage, c->lcod, c->lcod, 1, st, &ce)) CK(ce);
         else s->defer[s->ndefer++] = DeferredCopy{out, c->lcod, s->out_stage, c->lcod, c->lcod, 1};
     }
     CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -682,7 +752,9 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
             s->bs_cap = size + 4096;
             CK(cudaMalloc(&s->bs, s->bs_cap + 64));
         }
-        CK(cudaMemcpyAsync(s->bs, bs, size, cudaMemcpyHostToDevice, st));
+        cudaError_t ce = cudaSuccess;
+        if (!jxs_gpu_is_page_locked(bs) && host_copy_kernel(s->bs, size, bs, size, size, 1, st, &ce)) CK(ce);
+        else CK(cudaMemcpyAsync(s->bs, bs, size, cudaMemcpyHostToDevice, st));
         dbs = s->bs;
     }
     if (prec_off) {
@@ -796,8 +868,11 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         const uint32_t ow = jxs_out_w(c, k), oh = jxs_out_h(c, k);
         const DeferredCopy cp{planes[k], (size_t)strides[k] * bps, s->out_stage + s->out_off[k], (size_t)stage_pitch(ow, bps) * bps,
                               (size_t)ow * bps, oh};
+        cudaError_t ce = cudaSuccess;
         if (jxs_gpu_is_page_locked(planes[k]))
             CK(cudaMemcpy2DAsync(cp.dst, cp.dpitch, cp.src, cp.spitch, cp.width, cp.height, cudaMemcpyDeviceToHost, st));
+        else if (host_copy_kernel(cp.dst, cp.dpitch, cp.src, cp.spitch, cp.width, cp.height, st, &ce))
+            CK(ce);
         else
             s->defer[s->ndefer++] = cp;
     }

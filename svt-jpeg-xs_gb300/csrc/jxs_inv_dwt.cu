@@ -235,16 +235,22 @@ struct IvRaw {
 };
 
 /* int16 values j0 .. j0 + 3 of a band row of n (> 0) coefficients, two per
- * word; indices outside [0, n) read the nearest inside */
+ * word; indices outside [0, n) read the nearest inside (FAST: all inside) */
+template <bool FAST>
 DEV uint2 iv_ld_coef(const int16_t* row, int j0, int n) {
-    if (j0 >= 0 && j0 + 4 <= n) return *(const uint2*)(row + j0);
-    uint32_t v[4];
+    if constexpr (FAST) {
+        return *(const uint2*)(row + j0);
+    } else {
+        if (j0 >= 0 && j0 + 4 <= n) return *(const uint2*)(row + j0);
+        uint32_t v[4];
 #pragma unroll
-    for (int q = 0; q < 4; q++) v[q] = (uint16_t)row[clampi(j0 + q, n)];
-    return make_uint2(v[0] | (v[1] << 16), v[2] | (v[3] << 16));
+        for (int q = 0; q < 4; q++) v[q] = (uint16_t)row[clampi(j0 + q, n)];
+        return make_uint2(v[0] | (v[1] << 16), v[2] | (v[3] << 16));
+    }
 }
+template <bool FAST>
 DEV int4 iv_ld_low(const int32_t* row, int j0, int n) {
-    if (j0 >= 0 && j0 + 4 <= n) return *(const int4*)(row + j0);
+    if (FAST || (j0 >= 0 && j0 + 4 <= n)) return *(const int4*)(row + j0);
     return make_int4(row[clampi(j0, n)], row[clampi(j0 + 1, n)], row[clampi(j0 + 2, n)], row[clampi(j0 + 3, n)]);
 }
 /* two int16 values of a word as int32 << fq */
@@ -259,6 +265,7 @@ DEV void iv_dq2(uint32_t w, int fq, int32_t& a, int32_t& b) {
  * x[2j] itself in place of x[2j+2] past the row (j + 1 >= w1).  The left
  * neighbour's last high value and the right neighbour's first even sample
  * come by shuffles.  x receives the lane's 8 samples. */
+template <bool FAST>
 DEV void iv_hrow(const int32_t* s, const int32_t* d, int j0, int w1, int32_t* x) {
     const int32_t dm = __shfl_up_sync(FULL, d[3], 1);
     const int32_t e0 = s[0] - ((dm + d[0] + 2) >> 2);
@@ -267,13 +274,13 @@ DEV void iv_hrow(const int32_t* s, const int32_t* d, int j0, int w1, int32_t* x)
     const int32_t e3 = s[3] - ((d[2] + d[3] + 2) >> 2);
     const int32_t en = __shfl_down_sync(FULL, e0, 1);
     x[0] = e0;
-    x[1] = d[0] + ((e0 + (j0 + 1 < w1 ? e1 : e0)) >> 1);
+    x[1] = d[0] + ((e0 + (FAST || j0 + 1 < w1 ? e1 : e0)) >> 1);
     x[2] = e1;
-    x[3] = d[1] + ((e1 + (j0 + 2 < w1 ? e2 : e1)) >> 1);
+    x[3] = d[1] + ((e1 + (FAST || j0 + 2 < w1 ? e2 : e1)) >> 1);
     x[4] = e2;
-    x[5] = d[2] + ((e2 + (j0 + 3 < w1 ? e3 : e2)) >> 1);
+    x[5] = d[2] + ((e2 + (FAST || j0 + 3 < w1 ? e3 : e2)) >> 1);
     x[6] = e3;
-    x[7] = d[3] + ((e3 + (j0 + 4 < w1 ? en : e3)) >> 1);
+    x[7] = d[3] + ((e3 + (FAST || j0 + 4 < w1 ? en : e3)) >> 1);
 }
 
 /* linear_output_scaling of one sample with zeta >= 2: the rounded value
@@ -304,9 +311,9 @@ DEV uint32_t out_sample8(int32_t v, const OutScale8& s) {
 
 /* One output row of the lane's 8 columns c0 .. c0 + 7 (c0 < w): vector
  * stores where the row is aligned and all 8 are inside. */
-template <int OUT>
+template <int OUT, bool FAST>
 DEV void iv_store8(const InvVJob& J, int y, int c0, int w, bool vec, const int32_t* x, const OutScale8& os) {
-    const bool all8 = vec && c0 + 8 <= w;
+    const bool all8 = FAST || (vec && c0 + 8 <= w);
     if constexpr (OUT == 0) {
         int32_t* d = (int32_t*)J.dst + (size_t)y * J.dst_pitch + c0;
         if (all8) {
@@ -341,22 +348,17 @@ DEV void iv_store8(const InvVJob& J, int y, int c0, int w, bool vec, const int32
     }
 }
 
-template <int OUT, int NJ>
-__global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant__ InvVLaunchN<NJ> L) {
-    const InvVJob& J = L.job[find_job<NJ>(L.job, L.njobs, (int)blockIdx.x)];
-    const int t = blockIdx.x - J.first_block;
-    const int ty = t / J.col_tiles, tx = t - ty * J.col_tiles;
+/* One warp's strip: row pairs r0 .. rend - 1 of output columns c0 (this
+ * lane) of job J.  FAST: the strip is away from the level's left and right
+ * edges and its rows are aligned, so that no load or store needs a check. */
+template <int OUT, bool FAST>
+DEV void iv_strip(const InvVJob& J, int r0, int rend, int c0, bool vec) {
+    const int lane = threadIdx.x & 31;
     const int w = J.w, h = J.h, fq = J.fq;
     const int n1 = (h + 1) >> 1, n2 = h >> 1;
     const int w1 = (w + 1) >> 1, w2 = w >> 1;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r0 = (ty * IV_WARPS + warp) * IV_WROWPAIRS;
-    if (r0 >= n1) return; /* the whole warp */
-    const int rend = min(r0 + IV_WROWPAIRS, n1);
-    const int c0 = tx * IV_COLS - 8 + 8 * lane, j0 = c0 >> 1;
+    const int j0 = c0 >> 1;
     const bool out_lane = lane >= 1 && lane <= 30 && c0 < w;
-    const int esz = OUT == 0 ? 4 : OUT;
-    const bool vec = ((uintptr_t)J.dst & 15) == 0 && (((size_t)J.dst_pitch * esz) & 15) == 0;
     const jxs_band_t& bHL = J.bands[J.b_hl];
     const jxs_band_t& bLH = J.bands[J.b_lh];
     const jxs_band_t& bHH = J.bands[J.b_hh];
@@ -364,17 +366,19 @@ __global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant
     const int16_t* lh = J.coef + bLH.coef_off;
     const int16_t* hh = J.coef + bHH.coef_off;
     const uint32_t hl_p = bHL.pitch, lh_p = bLH.pitch, hh_p = bHH.pitch;
+    const int32_t* llb = J.ll;
+    const int ll_p = J.ll_pitch;
     const OutScale8 os = out_scale8(J.bw, J.depth);
     /* raw loads of low row i (i < n1) and high row i (clamped into [0, n2),
      * n2 > 0) */
     auto ld_low = [&](int i, IvRaw& r) {
-        r.s = iv_ld_low(J.ll + (size_t)i * J.ll_pitch, j0, w1);
-        r.d = w2 ? iv_ld_coef(hl + (size_t)i * hl_p, j0, w2) : make_uint2(0u, 0u);
+        r.s = iv_ld_low<FAST>(llb + (size_t)i * ll_p, j0, w1);
+        r.d = w2 ? iv_ld_coef<FAST>(hl + (size_t)i * hl_p, j0, w2) : make_uint2(0u, 0u);
     };
     auto ld_high = [&](int i, IvRaw& r) {
         i = clampi(i, n2);
-        r.sc = iv_ld_coef(lh + (size_t)i * lh_p, j0, w1);
-        r.d = w2 ? iv_ld_coef(hh + (size_t)i * hh_p, j0, w2) : make_uint2(0u, 0u);
+        r.sc = iv_ld_coef<FAST>(lh + (size_t)i * lh_p, j0, w1);
+        r.d = w2 ? iv_ld_coef<FAST>(hh + (size_t)i * hh_p, j0, w2) : make_uint2(0u, 0u);
     };
     auto build = [&](const IvRaw& r, bool low, int32_t* x) {
         int32_t sv[4], dv[4];
@@ -386,7 +390,7 @@ __global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant
         }
         iv_dq2(r.d.x, fq, dv[0], dv[1]);
         iv_dq2(r.d.y, fq, dv[2], dv[3]);
-        iv_hrow(sv, dv, j0, w1, x);
+        iv_hrow<FAST>(sv, dv, j0, w1, x);
     };
     /* x[2 r0] = low[r0] - ((high[r0 - 1] + high[r0] + 2) >> 2) */
     int32_t xe[8], hc[8];
@@ -446,12 +450,32 @@ __global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant
             }
         }
         if (out_lane) {
-            iv_store8<OUT>(J, y, c0, w, vec, xe, os);
-            if (y + 1 < h) iv_store8<OUT>(J, y + 1, c0, w, vec, xo, os);
+            iv_store8<OUT, FAST>(J, y, c0, w, vec, xe, os);
+            if (y + 1 < h) iv_store8<OUT, FAST>(J, y + 1, c0, w, vec, xo, os);
         }
 #pragma unroll
         for (int k = 0; k < 8; k++) xe[k] = xn[k];
     }
+}
+
+template <int OUT, int NJ>
+__global__ void __launch_bounds__(IV_THREADS) inv_v_kernel(const __grid_constant__ InvVLaunchN<NJ> L) {
+    const InvVJob& J = L.job[find_job<NJ>(L.job, L.njobs, (int)blockIdx.x)];
+    const int t = blockIdx.x - J.first_block;
+    const int ty = t / J.col_tiles, tx = t - ty * J.col_tiles;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n1 = (J.h + 1) >> 1;
+    const int r0 = (ty * IV_WARPS + warp) * IV_WROWPAIRS;
+    if (r0 >= n1) return; /* the whole warp */
+    const int rend = min(r0 + IV_WROWPAIRS, n1);
+    const int first = tx * IV_COLS, c0 = first - 8 + 8 * lane;
+    const int esz = OUT == 0 ? 4 : OUT;
+    const bool vec = ((uintptr_t)J.dst & 15) == 0 && (((size_t)J.dst_pitch * esz) & 15) == 0;
+    /* the strip's 256 columns first - 8 .. first + 247 (band pairs up to
+     * first / 2 + 123) all inside, aligned rows: the whole warp takes the
+     * path without checks */
+    if (vec && first >= 8 && first + IV_COLS + 8 <= J.w) iv_strip<OUT, true>(J, r0, rend, c0, vec);
+    else iv_strip<OUT, false>(J, r0, rend, c0, vec);
 }
 
 /* ------------------------------------------------------------------------ */

@@ -16,7 +16,9 @@
  *                 Requests that arrive while every lane is
  *                 busy wait for the next free lane, so the batch size follows
  *                 the load: one request alone runs at once, a burst runs
- *                 together.  A lane keeps its working sets for its next batch;
+ *                 together.  A lane that takes a single request runs it in a
+ *                 free frame slot of the request's stream (the per-frame
+ *                 launch path, without batch planning).  A lane keeps its working sets for its next batch;
  *                 when a batch does not fit, the idle lanes give theirs back
  *                 to the arena first.
  *   per-frame     the plain drop-in path: every request goes to a free frame
@@ -31,6 +33,7 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 #include <string.h>
+#include <sys/prctl.h>
 
 #include <algorithm>
 #include <atomic>
@@ -72,6 +75,9 @@ struct SrvLane {
     cudaStream_t st = nullptr;
     std::vector<SrvReq> reqs;
     int busy = 0;
+    /* a lone request runs in a frame slot of its stream's own handle (the
+     * per-frame launch path, no batch planning): its stream and slot */
+    int single_stream = -1, single_slot = -1;
 };
 
 struct jxs_server {
@@ -106,7 +112,21 @@ static void finish(jxs_server_t* s, const SrvReq& r, int32_t status, int64_t t_d
 
 /* ---------------------------------------------------------------- batched */
 static int lane_poll(jxs_server_t* s, SrvLane& L) {
-    if (!L.busy || !jxs_gpu_batch_ready(L.b)) return 0;
+    if (!L.busy) return 0;
+    if (L.single_slot >= 0) {
+        SrvStream& S = s->streams[L.single_stream];
+        const int k = L.single_slot;
+        const int ready = S.kind == 0 ? jxs_gpu_enc_ready(S.enc, k) : jxs_gpu_dec_ready(S.dec, k);
+        if (!ready) return 0;
+        const int32_t st = S.kind == 0 ? jxs_gpu_enc_wait(S.enc, k) : jxs_gpu_dec_wait(S.dec, k);
+        finish(s, L.reqs[0], st, now_ns());
+        S.slot_busy[k] = 0;
+        L.reqs.clear();
+        L.single_slot = L.single_stream = -1;
+        L.busy = 0;
+        return 1;
+    }
+    if (!jxs_gpu_batch_ready(L.b)) return 0;
     int32_t st[JXS_BATCH_FRAMES];
     jxs_gpu_batch_wait(L.b, st);
     const int64_t t = now_ns();
@@ -128,6 +148,37 @@ static int lane_launch(jxs_server_t* s, SrvLane& L) {
         }
     }
     if (L.reqs.empty()) return 0;
+    uint64_t arena_bytes = 0, arena_used = 0, arena_peak = 0;
+    jxs_arena_stats(s->arena, &arena_bytes, &arena_used, &arena_peak);
+    if (L.reqs.size() == 1 && s->streams[L.reqs[0].io.stream].work_bytes <= arena_bytes) {
+        /* one request: a free frame slot of its stream's handle, the same
+         * launches as the per-frame path; a batch only if every slot is
+         * busy.  A request whose working set exceeds the whole budget still
+         * goes to the batch path, which refuses it. */
+        SrvReq& r = L.reqs[0];
+        SrvStream& S = s->streams[r.io.stream];
+        for (size_t k = 0; k < S.slot_busy.size(); k++) {
+            if (S.slot_busy[k]) continue;
+            r.t_start = now_ns();
+            const int32_t rc = S.kind == 0 ? jxs_gpu_enc_submit(S.enc, (int)k, r.io.planes, r.io.strides, (uint8_t*)r.io.bitstream)
+                                           : jxs_gpu_dec_submit(S.dec, (int)k, (const uint8_t*)r.io.bitstream,
+                                                                r.io.bitstream_size, nullptr, r.io.planes, r.io.strides);
+            if (rc != JXS_OK) {
+                finish(s, r, rc, now_ns());
+                L.reqs.clear();
+                return 1;
+            }
+            S.slot_busy[k] = 1;
+            L.single_stream = r.io.stream;
+            L.single_slot = (int)k;
+            L.busy = 1;
+            std::lock_guard<std::mutex> g(s->mu);
+            s->batches++;
+            s->batched_frames++;
+            if (s->max_seen_batch < 1) s->max_seen_batch = 1;
+            return 1;
+        }
+    }
     const uint32_t n0 = (uint32_t)L.reqs.size();
     std::vector<jxs_gpu_enc_t*> eh(n0);
     std::vector<jxs_gpu_dec_t*> dh(n0);
@@ -259,6 +310,9 @@ static int frame_launch(jxs_server_t* s) {
 
 /* -------------------------------------------------------------- scheduler */
 static void scheduler(jxs_server_t* s) {
+    /* the short sleeps between polls last what they ask for, not the
+     * default 50 us timer slack (completion seen sooner in both modes) */
+    prctl(PR_SET_TIMERSLACK, 1000UL, 0, 0, 0);
     while (!s->stop.load()) {
         int work = 0;
         if (s->mode == JXS_SRV_BATCHED) {
@@ -388,7 +442,12 @@ extern "C" void jxs_server_destroy(jxs_server_t* s) {
     s->cv.notify_all();
     if (s->th.joinable()) s->th.join();
     for (SrvLane& L : s->lanes) {
-        if (L.busy) {
+        if (L.busy && L.single_slot >= 0) {
+            SrvStream& S = s->streams[L.single_stream];
+            if (S.kind == 0) jxs_gpu_enc_wait(S.enc, L.single_slot);
+            else jxs_gpu_dec_wait(S.dec, L.single_slot);
+            S.slot_busy[L.single_slot] = 0;
+        } else if (L.busy) {
             int32_t st[JXS_BATCH_FRAMES];
             jxs_gpu_batch_wait(L.b, st);
         }
