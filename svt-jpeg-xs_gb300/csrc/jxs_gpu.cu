@@ -15,8 +15,12 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <sys/mman.h>
+#include <unistd.h>
+
 #include <atomic>
 #include <mutex>
+#include <vector>
 
 #include "SvtJpegxs.h"
 #include "jxs_batch.h"
@@ -106,14 +110,32 @@ static int pageable_direct(void) {
     return v == 1;
 }
 
-/* A 2-D copy with one side in pageable host memory by a copy kernel when
- * the device reaches pageable memory directly; returns 0 when it does not
- * (the caller then copies another way). */
+/* 1: every page of [p, p + bytes) is resident.  A GPU access to a page
+ * that is not (memory never touched since it was allocated, or swapped out)
+ * is a page fault served over the link, far slower than the driver's copy,
+ * which takes the faults on the CPU. */
+static int host_resident(const void* p, size_t bytes) {
+    static thread_local std::vector<unsigned char> vec;
+    const uintptr_t pg = (uintptr_t)sysconf(_SC_PAGESIZE);
+    const uintptr_t a = (uintptr_t)p & ~(pg - 1), e = ((uintptr_t)p + bytes + pg - 1) & ~(pg - 1);
+    const size_t n = (e - a) / pg;
+    if (vec.size() < n) vec.resize(n);
+    if (mincore((void*)a, e - a, vec.data()) != 0) return 0;
+    for (size_t i = 0; i < n; i++)
+        if (!(vec[i] & 1)) return 0;
+    return 1;
+}
+
+/* A 2-D copy with one side in pageable host memory (`host`) by a copy
+ * kernel, when the device reaches pageable memory directly and the host
+ * side's pages are resident; returns 0 otherwise (the caller then copies
+ * another way). */
 static int host_copy_kernel(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t rows, cudaStream_t st,
-                            cudaError_t* err) {
+                            cudaError_t* err, const void* host, size_t host_pitch) {
     *err = cudaSuccess;
     if (!pageable_direct()) return 0;
     if (!width || !rows) return 1;
+    if (!host_resident(host, (rows - 1) * host_pitch + width)) return 0;
     if (rows > 65535 || width > 0xffffffffull) return 0;
     /* a thread per 16-byte chunk (or byte), a grid row per row */
     const int v16 = (((uintptr_t)dst | (uintptr_t)src | dpitch | spitch | width) & 15) == 0;
@@ -368,7 +390,8 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
             const uint32_t sp = packed ? w : stage_pitch(w, bps);
             cudaError_t ce = cudaSuccess;
             if (!jxs_gpu_is_page_locked(planes[k]) &&
-                host_copy_kernel(d, (size_t)sp * bps, planes[k], (size_t)strides[k] * bps, (size_t)w * bps, h, st, &ce))
+                host_copy_kernel(d, (size_t)sp * bps, planes[k], (size_t)strides[k] * bps, (size_t)w * bps, h, st, &ce, planes[k],
+                                 (size_t)strides[k] * bps))
                 CK(ce);
             else
                 CK(cudaMemcpy2DAsync(d, (size_t)sp * bps, planes[k], (size_t)strides[k] * bps, (size_t)w * bps, h,
@@ -433,7 +456,7 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
     if (!out_dev) {
         cudaError_t ce = cudaSuccess;
         if (jxs_gpu_is_page_locked(out)) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));
-        else if (host_copy_kernel(out, c->lcod, s->out_stage, c->lcod, c->lcod, 1, st, &ce)) CK(ce);
+        else if (host_copy_kernel(out, c->lcod, s->out_stage, c->lcod, c->lcod, 1, st, &ce, out, c->lcod)) CK(ce);
         else s->defer[s->ndefer++] = DeferredCopy{out, c->lcod, s->out_stage, c->lcod, c->lcod, 1};
     }
     CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -753,7 +776,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
             CK(cudaMalloc(&s->bs, s->bs_cap + 64));
         }
         cudaError_t ce = cudaSuccess;
-        if (!jxs_gpu_is_page_locked(bs) && host_copy_kernel(s->bs, size, bs, size, size, 1, st, &ce)) CK(ce);
+        if (!jxs_gpu_is_page_locked(bs) && host_copy_kernel(s->bs, size, bs, size, size, 1, st, &ce, bs, size)) CK(ce);
         else CK(cudaMemcpyAsync(s->bs, bs, size, cudaMemcpyHostToDevice, st));
         dbs = s->bs;
     }
@@ -871,7 +894,7 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         cudaError_t ce = cudaSuccess;
         if (jxs_gpu_is_page_locked(planes[k]))
             CK(cudaMemcpy2DAsync(cp.dst, cp.dpitch, cp.src, cp.spitch, cp.width, cp.height, cudaMemcpyDeviceToHost, st));
-        else if (host_copy_kernel(cp.dst, cp.dpitch, cp.src, cp.spitch, cp.width, cp.height, st, &ce))
+        else if (host_copy_kernel(cp.dst, cp.dpitch, cp.src, cp.spitch, cp.width, cp.height, st, &ce, cp.dst, cp.dpitch))
             CK(ce);
         else
             s->defer[s->ndefer++] = cp;

@@ -16,9 +16,11 @@
  *                 Requests that arrive while every lane is
  *                 busy wait for the next free lane, so the batch size follows
  *                 the load: one request alone runs at once, a burst runs
- *                 together.  A lane that takes a single request runs it in a
- *                 free frame slot of the request's stream (the per-frame
- *                 launch path, without batch planning).  A lane keeps its working sets for its next batch;
+ *                 together.  A lane batches only what the idle lanes of its
+ *                 kind cannot take one by one, and a lane that takes a
+ *                 single request runs it in a free frame slot of the
+ *                 request's stream (the per-frame launch path, without batch
+ *                 planning).  A lane keeps its working sets for its next batch;
  *                 when a batch does not fit, the idle lanes give theirs back
  *                 to the arena first.
  *   per-frame     the plain drop-in path: every request goes to a free frame
@@ -140,9 +142,16 @@ static int lane_poll(jxs_server_t* s, SrvLane& L) {
  * one batch.  Returns 1 if anything was launched. */
 static int lane_launch(jxs_server_t* s, SrvLane& L) {
     {
+        /* batch only what the idle lanes cannot take one by one: with as
+         * many idle lanes of this kind as waiting requests, each lane takes
+         * one (a lone request runs as soon as a lane is free) */
+        int idle = 0;
+        for (const SrvLane& o : s->lanes) idle += o.kind == L.kind && !o.busy;
         std::lock_guard<std::mutex> g(s->mu);
         std::deque<SrvReq>& q = s->queue[L.kind];
-        while (!q.empty() && (int)L.reqs.size() < s->max_batch) {
+        const int waiting = (int)q.size();
+        const int take = waiting <= idle ? 1 : std::min(s->max_batch, waiting - idle + 1);
+        while (!q.empty() && (int)L.reqs.size() < take) {
             L.reqs.push_back(q.front());
             q.pop_front();
         }

@@ -90,13 +90,15 @@ def test_server_mixed_streams_same_alone_and_in_mix(gpu, mode):
 def test_server_device_budget_admission(gpu):
     """A budget that holds two 1080p working sets: the other requests wait
     for memory (deferred) and all complete bit-exact; a request that can
-    never fit completes with SvtJxsErrorInsufficientResources."""
+    never fit completes with SvtJxsErrorInsufficientResources.  One lane per
+    kind: the first request runs alone in its stream's frame slot, the seven
+    that arrive meanwhile then form one batch, larger than the budget."""
     torch = pytest.importorskip("torch")
     enc = gpu.Encoder(1920, 1080, 8, S.FMT_YUV422, 3)
     big = gpu.Encoder(3840, 2160, 10, S.FMT_YUV422, 3)
     planes = S.frame(1920, 1080, 8, S.FMT_YUV422, seed=9)
     want = enc.encode(planes)
-    server = gpu.Server(48 << 20, gpu.SERVER_BATCHED, lanes=2, max_batch=8)
+    server = gpu.Server(48 << 20, gpu.SERVER_BATCHED, lanes=1, max_batch=8)
     sid = server.add_encoder(enc)
     bid = server.add_encoder(big)
     _, dp = _dev_planes(torch, planes)
