@@ -16,9 +16,12 @@ value  : luma Gpixel/s of encode + decode with inputs and outputs resident in
 e2e    : the same metric through the public C API with host buffers (page-
          locked), host-to-device and device-to-host copies inside the timed
          region, several frames in flight.
-roofline: the dominant stage (per-stage CUDA-event times from a separate
-         single-stream pass) against the measured HBM copy bandwidth; bytes
-         are the algorithmic bytes of that stage.
+roofline: the dominant kernel of the headline path against the measured HBM
+         copy bandwidth: per launch of the batched step (F frames per launch;
+         CUDA events around every launch in a separate pass of the same
+         batches without graphs), or of the per-frame path when that is the
+         headline; bytes are the algorithmic bytes of that launch, traffic
+         the ncu DRAM bytes of one frame's launch scaled by the frames.
 cpu_baseline: the reference SVT-JPEG-XS library on the host cores (built from
          its own C sources by build(); threads_num = cores, frames pipelined
          through its public API), a bounded sample of the same workload;
@@ -458,9 +461,78 @@ def run_batched(args, jxs, torch, dev, frames, d_in, lcod, enc, dec, nseq):
            "enc_tune": ie["tune"], "dec_tune": idd["tune"], "launches_per_step": ie["last_launches"] + idd["last_launches"],
            "graph_hits": ie["graph_hits"] + idd["graph_hits"], "enc_batch_gpu_ms": ie["last_gpu_ms"],
            "dec_batch_gpu_ms": idd["last_gpu_ms"]}
+    # the other pair's buffers: the last step's outputs are checked afterwards
+    o = 1 - last
+    out["launch_ms"] = batched_launch_times(args, torch, streams[o], bat_e[o], bat_d[o], enc, dec, d_in, d_bs[o], d_out[o],
+                                            lcod, nseq, ie["tune"], idd["tune"], planes_of)
     for b in bat_e + bat_d:
         b.close()
     return out
+
+
+def link_rates(torch, dev, nbytes=33 << 20, reps=20):
+    """Page-locked copy rates of the host link in GB/s: host to device
+    alone, device to host alone, and both directions at once on two streams
+    (per direction)."""
+    h_a = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h_b = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d_a = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    d_b = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+    sa, sb = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+
+    def run(h2d, d2h):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            if h2d:
+                with torch.cuda.stream(sa):
+                    d_a.copy_(h_a, non_blocking=True)
+            if d2h:
+                with torch.cuda.stream(sb):
+                    h_b.copy_(d_b, non_blocking=True)
+        torch.cuda.synchronize()
+        return reps * nbytes / (time.perf_counter() - t0) / 1e9
+
+    run(True, True)
+    return {"h2d_gbs": run(True, False), "d2h_gbs": run(False, True), "both_gbs_per_direction": run(True, True)}
+
+
+def launch_name(stage, variant):
+    """Kernel name of a batched launch (as in ENC_KERNELS / DEC_KERNELS)."""
+    if stage in ("fwd_v", "inv_v"):
+        return stage + ("_level0" if variant else "_level1")
+    return "rc_cost" if stage == "rc" else stage
+
+
+def batched_launch_times(args, torch, stream, be, bd, enc, dec, d_in, d_bs, d_out, lcod, nseq, tune_e, tune_d, planes_of):
+    """Device time of each launch of the batched step (median of 5 steps):
+    the same F-frame batches as the timed region, issued as one chain without
+    graphs, with a CUDA event pair around every launch on its stream."""
+    F = args.frames
+    for b, t in ((be, tune_e), (bd, tune_d)):
+        b.set_options(use_graph=False, autotune=False)
+        b.set_tune(1, *t[1:])
+        b.set_stage_timing(True)
+    st = stream.cuda_stream
+    times = {}
+    for rep in range(6):
+        base = ((rep + 7) * F) % nseq
+        r = be.encode([enc] * F, [planes_of(d_in[(base + i) % nseq]) for i in range(F)], [t.data_ptr() for t in d_bs],
+                      out_caps=[lcod + 64] * F, stream=st)
+        assert r == 0 and be.wait()[0] == 0
+        r = bd.decode([dec] * F, [t.data_ptr() for t in d_bs], [planes_of(o) for o in d_out], sizes=[lcod] * F, stream=st)
+        assert r == 0 and bd.wait()[0] == 0
+        if rep == 0:
+            continue
+        step = {}
+        for stage, var, ms in be.read_stage_times() + bd.read_stage_times():
+            name = launch_name(stage, var)
+            step[name] = step.get(name, 0.0) + ms
+        for name, ms in step.items():
+            times.setdefault(name, []).append(ms)
+    for b in (be, bd):
+        b.set_stage_timing(False)
+    return {name: statistics.median(v) for name, v in times.items()}
 
 
 def run_ours(args, rank, world, local):
@@ -704,6 +776,12 @@ def run_ours(args, rank, world, local):
         "decode from pageable memory differs from the page-locked run"
     in_bytes = sum(p.nbytes for p in frames[0])
     out_bytes = in_bytes
+    # the host link's own bound on e2e: every frame moves in_bytes + lcod each
+    # way, both directions at once
+    link = link_rates(torch, dev)
+    per_dir = max(in_bytes + lcod, lcod + out_bytes)
+    link_bound = link["both_gbs_per_direction"] * 1e9 / per_dir * W * H / 1e9 * world
+    link.update({"bytes_per_frame_each_way": per_dir, "bound_value": link_bound, "e2e_frac_of_bound": e2e_val / link_bound})
     # per-frame latency through the API, one frame at a time (no queueing)
     lat_frame = []
     for i in range(20):
@@ -729,8 +807,16 @@ def run_ours(args, rank, world, local):
     for names, times in ((ENC_KERNELS, kenc), (DEC_KERNELS, kdec)):
         for name, t in zip(names, times):
             kern_ms[name] = t / nfr
-    dom = max((k for k in kern_ms if k in kb), key=lambda k: kern_ms[k])
-    achieved = kb[dom] / (kern_ms[dom] / 1e3) / 1e9
+    # the dominant kernel of the headline path: per launch of the batched
+    # step (F frames per launch) when that path is the headline, else of
+    # the per-frame path
+    head_batched = batched_value >= value
+    launch_ms = bat["launch_ms"] if head_batched else kern_ms
+    units = F if head_batched else 1
+    dom = max((k for k in launch_ms if k in kb), key=lambda k: launch_ms[k])
+    achieved = units * kb[dom] / (launch_ms[dom] / 1e3) / 1e9
+    dom_pf = max((k for k in kern_ms if k in kb), key=lambda k: kern_ms[k])
+    achieved_pf = kb[dom_pf] / (kern_ms[dom_pf] / 1e3) / 1e9
     pipeline_gbs = (in_bytes + lcod + lcod + out_bytes) / ((sum(stages.values()) / nfr) / 1e3) / 1e9
 
     # ---- CPU baseline, rank 0 only: the reference library on the host
@@ -754,7 +840,6 @@ def run_ours(args, rank, world, local):
     # per frame: 2 vertical + 1 horizontal transform, rate control, pack;
     # 2 precinct walks (device codestreams), unpack, 1 horizontal + 2 vertical inverse
     launches_per_frame = 5 + 6
-    head_batched = batched_value >= value
     head_ms = bat["dev_ms"] if head_batched else dev_ms
     head_clk = clk_b if head_batched else clk
     line = {
@@ -766,12 +851,17 @@ def run_ours(args, rank, world, local):
         "e2e": {"value": e2e_val, "unit": "Gpix/s", "h2d_bytes_per_step": F * (in_bytes + lcod),
                 "d2h_bytes_per_step": F * (lcod + out_bytes), "p50_step_ms": 1e3 * statistics.median(lat),
                 "frame_latency_ms_p50": statistics.median(lat_frame),
-                "frame_latency_ms_p99": float(np.percentile(lat_frame, 99))},
+                "frame_latency_ms_p99": float(np.percentile(lat_frame, 99)), "host_link": link},
         "e2e_pageable": {"value": e2e_pg_val, "unit": "Gpix/s", "frac_of_page_locked": e2e_pg_val / e2e_val,
                          "buffers": "ordinary (pageable) host memory, the same pipeline and bytes as e2e"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": KERNEL_DRAM_BYTES.get(dom), "algorithmic_bytes": kb[dom],
-                     "kernel_ms_per_frame": {k: round(v, 4) for k, v in kern_ms.items()}, "stage_ms_per_frame": stage_ms,
+                     "peak_source": peak_kind,
+                     "traffic": KERNEL_DRAM_BYTES[dom] * units if dom in KERNEL_DRAM_BYTES else None,
+                     "algorithmic_bytes": kb[dom] * units, "frames_per_launch": units,
+                     "launch_ms": {k: round(v, 4) for k, v in launch_ms.items()},
+                     "per_frame_path": {"kernel": dom_pf, "achieved": achieved_pf, "frac": achieved_pf / peak,
+                                        "kernel_ms_per_frame": {k: round(v, 4) for k, v in kern_ms.items()},
+                                        "stage_ms_per_frame": stage_ms},
                      "pipeline_algorithmic_gbs": pipeline_gbs},
         "per_frame": {"value": value, "unit": "Gpix/s", "streams": NS, "launches_per_frame": launches_per_frame},
         "batched": {"value": batched_value, "unit": "Gpix/s", "frames_per_batch": F,

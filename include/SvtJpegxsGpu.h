@@ -162,6 +162,28 @@ PREFIX_API uint32_t svt_jpeg_xs_gpu_batch_ready(svt_jpeg_xs_gpu_batch_t* batch);
 
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_get_info(svt_jpeg_xs_gpu_batch_t* batch, svt_jpeg_xs_gpu_batch_info_t* info);
 
+/* Stage timing.  While on, batches are issued without graphs, with a CUDA
+ * event pair around every kernel launch on the launch's stream (set one
+ * chain with set_tune to time the stages one after another).  After the
+ * wait of such a batch, read_stage_times gives each launch's stage
+ * (SVT_JPEGXS_GPU_STAGE_*), variant and device milliseconds, at most `max`
+ * entries, and returns their number (0 while a batch is in flight).
+ * Variant: for the transform stages the sample kind read or written (0: the
+ * 32-bit low band of the next level, 1 / 2: 8- / 16-bit planar, 3 / 4:
+ * packed); for rate control and packing bit 0 sign handling and bit 1
+ * vertical prediction. */
+#define SVT_JPEGXS_GPU_STAGE_FWD_V 0  /* vertical level and the horizontal level after it */
+#define SVT_JPEGXS_GPU_STAGE_FWD_H 1  /* horizontal-only levels */
+#define SVT_JPEGXS_GPU_STAGE_RC 2     /* rate control */
+#define SVT_JPEGXS_GPU_STAGE_PACK 3
+#define SVT_JPEGXS_GPU_STAGE_WALK 4   /* precinct offsets of device codestreams */
+#define SVT_JPEGXS_GPU_STAGE_UNPACK 5
+#define SVT_JPEGXS_GPU_STAGE_INV_H 6
+#define SVT_JPEGXS_GPU_STAGE_INV_V 7
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_set_stage_timing(svt_jpeg_xs_gpu_batch_t* batch, uint32_t on);
+PREFIX_API uint32_t svt_jpeg_xs_gpu_batch_read_stage_times(svt_jpeg_xs_gpu_batch_t* batch, int32_t* stage, int32_t* variant,
+                                                           float* ms, uint32_t max);
+
 /* ------------------------------------------------------------------------
  * Serving loop.  Encode and decode requests from many streams are run by a
  * scheduler thread of the library:

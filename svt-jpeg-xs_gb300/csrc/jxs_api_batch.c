@@ -11,6 +11,11 @@
 #include "jxs_batch.h"
 #include "jxs_server.h"
 
+_Static_assert(SVT_JPEGXS_GPU_STAGE_FWD_V == JXS_STAGE_FWD_V && SVT_JPEGXS_GPU_STAGE_RC == JXS_STAGE_RC &&
+                   SVT_JPEGXS_GPU_STAGE_PACK == JXS_STAGE_PACK && SVT_JPEGXS_GPU_STAGE_UNPACK == JXS_STAGE_UNPACK &&
+                   SVT_JPEGXS_GPU_STAGE_INV_V == JXS_STAGE_INV_V,
+               "stage numbers of the public header");
+
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_create(uint64_t device_bytes, svt_jpeg_xs_gpu_batch_t** batch) {
     if (!batch || !device_bytes) return SvtJxsErrorBadParameter;
     int32_t err = 0;
@@ -32,6 +37,17 @@ PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_set_tune(svt_jpeg_xs_gpu_batc
     const int t[5] = {tune[0], tune[1], tune[2], tune[3], tune[4]};
     jxs_gpu_batch_set_tune((jxs_gpu_batch_t*)batch, t);
     return SvtJxsErrorNone;
+}
+
+PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_set_stage_timing(svt_jpeg_xs_gpu_batch_t* batch, uint32_t on) {
+    if (!batch) return SvtJxsErrorBadParameter;
+    jxs_gpu_batch_set_stage_timing((jxs_gpu_batch_t*)batch, on != 0);
+    return SvtJxsErrorNone;
+}
+
+PREFIX_API uint32_t svt_jpeg_xs_gpu_batch_read_stage_times(svt_jpeg_xs_gpu_batch_t* batch, int32_t* stage, int32_t* variant,
+                                                           float* ms, uint32_t max) {
+    return batch ? jxs_gpu_batch_stage_times((jxs_gpu_batch_t*)batch, stage, variant, ms, max) : 0u;
 }
 
 PREFIX_API SvtJxsErrorType_t svt_jpeg_xs_gpu_batch_wait(svt_jpeg_xs_gpu_batch_t* batch, SvtJxsErrorType_t* status) {

@@ -350,6 +350,12 @@ struct jxs_gpu_batch {
     Tune last_tune = kDefaultTune;
     float last_ms = 0.f;
     uint32_t last_launches = 0;
+    /* stage timing: an event pair around every launch of the batches issued
+     * while it is on (no graphs); the stage and variant of each launch */
+    int stage_timing = 0;
+    std::vector<cudaEvent_t> tev;
+    std::vector<int> tstage, tvar;
+    uint32_t tcount = 0;
 };
 
 static void order_chains(const std::vector<uint64_t>& weight, const Tune& t, std::vector<std::vector<int>>* chains) {
@@ -604,10 +610,23 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         BCK(cudaEventRecord(b->fork, st));
         for (int c = 1; c < P.nchains; c++) BCK(cudaStreamWaitEvent(b->side[c], b->fork, 0));
     }
+    if (b->stage_timing) {
+        const size_t need = 2 * P.ops.size();
+        while (b->tev.size() < need) {
+            cudaEvent_t ev;
+            BCK(cudaEventCreate(&ev));
+            b->tev.push_back(ev);
+        }
+        b->tstage.assign(P.ops.size(), 0);
+        b->tvar.assign(P.ops.size(), 0);
+        b->tcount = 0;
+    }
     for (const Op& o : P.ops) {
         const cudaStream_t s = o.chain == 0 ? st : b->side[o.chain];
         const void* d = P.bytes.data() + o.off;
         cudaError_t e = cudaSuccess;
+        const uint32_t ti = b->tcount;
+        if (b->stage_timing) BCK(cudaEventRecord(b->tev[2 * ti], s));
         switch (o.type) {
         case OP_FWD_V: e = jxs_launch_fwd_v_batch((const FwdVLaunchB*)d, o.kind, (int)o.a, s); break;
         case OP_FWD_H: e = jxs_launch_fwd_h_batch((const FwdHLaunchB*)d, o.kind, o.nblocks, s); break;
@@ -645,6 +664,23 @@ static int32_t issue(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
         }
         }
         BCK(e);
+        if (b->stage_timing) {
+            BCK(cudaEventRecord(b->tev[2 * ti + 1], s));
+            /* the stage of each launch: the per-frame and the batched forms of
+             * a kernel report the same stage */
+            static const int kStage[] = {JXS_STAGE_FWD_V, JXS_STAGE_FWD_H, JXS_STAGE_RC,    JXS_STAGE_PACK,
+                                         JXS_STAGE_WALK,  JXS_STAGE_UNPACK, JXS_STAGE_INV_H, JXS_STAGE_INV_V,
+                                         JXS_STAGE_FWD_V, JXS_STAGE_FWD_H, JXS_STAGE_INV_H, JXS_STAGE_INV_V,
+                                         JXS_STAGE_RC,    JXS_STAGE_PACK,  JXS_STAGE_WALK,  JXS_STAGE_UNPACK};
+            b->tstage[ti] = kStage[o.type];
+            /* transforms: the sample kind read or written (0: the 32-bit low
+             * band of the next level); rate control and packing: bit 0 sign
+             * handling, bit 1 vertical prediction */
+            const int st = kStage[o.type];
+            b->tvar[ti] = st == JXS_STAGE_RC || st == JXS_STAGE_PACK ? (int)o.b
+                          : st == JXS_STAGE_WALK || st == JXS_STAGE_UNPACK ? 0 : o.kind;
+            b->tcount = ti + 1;
+        }
     }
     if (P.nchains > 1) {
         for (int c = 1; c < P.nchains; c++) {
@@ -667,7 +703,7 @@ static void plan_key(const Plan& P, std::vector<uint8_t>* key) {
 
 static int32_t run_plan(jxs_gpu_batch_t* b, const Plan& P, cudaStream_t st) {
     b->last_launches = (uint32_t)P.ops.size();
-    if (!b->use_graph) return issue(b, P, st);
+    if (!b->use_graph || b->stage_timing) return issue(b, P, st);
     std::vector<uint8_t> key;
     plan_key(P, &key);
     b->clock++;
@@ -857,6 +893,7 @@ extern "C" void jxs_gpu_batch_destroy(jxs_gpu_batch_t* b) {
     if (b->done) cudaEventDestroy(b->done);
     if (b->t0) cudaEventDestroy(b->t0);
     if (b->t1) cudaEventDestroy(b->t1);
+    for (cudaEvent_t ev : b->tev) cudaEventDestroy(ev);
     cudaFree(b->status_d);
     if (b->status_h) cudaFreeHost(b->status_h);
     if (b->hdr_pool) cudaFreeHost(b->hdr_pool);
@@ -871,6 +908,28 @@ extern "C" void jxs_gpu_batch_set_options(jxs_gpu_batch_t* b, int use_graph, int
 }
 
 extern "C" void jxs_gpu_batch_set_release(jxs_gpu_batch_t* b, int on) { b->release_after_wait = on; }
+
+extern "C" void jxs_gpu_batch_set_stage_timing(jxs_gpu_batch_t* b, int on) {
+    b->stage_timing = on;
+    b->tcount = 0;
+}
+
+extern "C" uint32_t jxs_gpu_batch_stage_times(jxs_gpu_batch_t* b, int32_t* stage, int32_t* variant, float* ms, uint32_t max) {
+    if (b->pending) return 0;
+    uint32_t n = 0;
+    for (uint32_t i = 0; i < b->tcount && n < max; i++) {
+        float t = -1.f;
+        if (cudaEventElapsedTime(&t, b->tev[2 * i], b->tev[2 * i + 1]) != cudaSuccess) {
+            cudaGetLastError();
+            t = -1.f;
+        }
+        if (stage) stage[n] = b->tstage[i];
+        if (variant) variant[n] = b->tvar[i];
+        if (ms) ms[n] = t;
+        n++;
+    }
+    return n;
+}
 
 static void release_all(jxs_gpu_batch_t* b);
 

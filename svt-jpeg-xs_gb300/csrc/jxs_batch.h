@@ -53,6 +53,23 @@ uint64_t jxs_gpu_batch_dec_work_bytes(jxs_gpu_dec_t* d);
  * a batch call on `stream`; returns how many leading positions fit in the
  * arena. */
 uint32_t jxs_gpu_batch_reserve(jxs_gpu_batch_t* b, jxs_gpu_enc_t* const* enc, jxs_gpu_dec_t* const* dec, uint32_t n, void* stream);
+/* stages of a batch's launches (the values of SVT_JPEGXS_GPU_STAGE_*) */
+enum {
+    JXS_STAGE_FWD_V = 0, /* vertical level + the horizontal level after it */
+    JXS_STAGE_FWD_H = 1, /* horizontal-only levels */
+    JXS_STAGE_RC = 2,    /* rate control */
+    JXS_STAGE_PACK = 3,
+    JXS_STAGE_WALK = 4,  /* precinct offsets of device codestreams */
+    JXS_STAGE_UNPACK = 5,
+    JXS_STAGE_INV_H = 6,
+    JXS_STAGE_INV_V = 7
+};
+/* stage timing (see svt_jpeg_xs_gpu_batch_set_stage_timing): on, batches
+ * launch without graphs with an event pair around every launch */
+void jxs_gpu_batch_set_stage_timing(jxs_gpu_batch_t* b, int on);
+/* stage (JXS_STAGE_*), variant and device milliseconds of each launch of the
+ * last batch issued with stage timing on, after its wait; returns the count */
+uint32_t jxs_gpu_batch_stage_times(jxs_gpu_batch_t* b, int32_t* stage, int32_t* variant, float* ms, uint32_t max);
 /* fixed launch shapes for every batch: chains, heavy-first, blocks per SM,
  * forward / inverse rows per block */
 void jxs_gpu_batch_set_tune(jxs_gpu_batch_t* b, const int* tune5);

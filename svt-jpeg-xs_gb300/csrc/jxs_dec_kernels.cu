@@ -292,7 +292,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     __shared__ uint8_t s_pkbl0[JXS_MAXPK], s_pknbl[JXS_MAXPK];
     __shared__ uint32_t ws[UK_WARPS];
     __shared__ int s_err;
-    __shared__ uint32_t s_total, s_lead, s_tw, s_npk;
+    __shared__ uint32_t s_total, s_lead, s_tw, s_npk, s_off;
     __shared__ uint8_t s_g2f[JXS_MAXBL];          /* global band -> flat band */
     __shared__ uint16_t s_lgp[JXS_MAXBLINES];      /* per line: band gain | priority << 8 */
     __shared__ uint32_t s_sc[9];                   /* nbands_all, npk, long headers, separate signs, precinct header bytes,
@@ -313,6 +313,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
         /* the precinct's offset and length field are read in bounds before
          * the frame status, so that the three loads do not wait in turn */
         const uint32_t off = prec_off[p], phb = cfg->prec_hdr_bytes;
+        s_off = off; /* read once: the offsets may be in host memory */
         const bool inb = (uint64_t)off + phb <= bs_size;
         const uint32_t lprc = inb ? ((uint32_t)bs[off] << 16) | ((uint32_t)bs[off + 1] << 8) | bs[off + 2] : 0u;
         int err = *(volatile int*)status; /* set: the precinct offsets could not be found */
@@ -366,7 +367,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
     }
     __syncthreads();
     if (s_err) return;
-    const uint32_t off = prec_off[p];
+    const uint32_t off = s_off;
     const uint32_t total = s_total, lead = s_lead;
     {
         /* aligned 16-byte chunks inside the precinct, single bytes at its

@@ -76,6 +76,13 @@ extern "C" int jxs_gpu_is_page_locked(const void* p) {
  * the library's until the frame is returned, as with the reference
  * (EncHandle.c:1006 keeps only the input structure, and its workers read
  * the planes later). */
+/* A frame's final status into page-locked host memory, written by the GPU
+ * after the frame's last compute kernel: no 4-byte copy waits in the copy
+ * engines' queues between the frames' large transfers. */
+__global__ void publish_status_kernel(int* __restrict__ host, const int* __restrict__ status) {
+    if (threadIdx.x == 0) *(volatile int*)host = *(const volatile int*)status;
+}
+
 __global__ void __launch_bounds__(256) host_copy16_kernel(uint8_t* dst, size_t dpitch, const uint8_t* src, size_t spitch,
                                                           uint32_t chunks) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
@@ -215,6 +222,7 @@ struct EncSlot {
     int* status;
     uint8_t* out_stage;
     int* status_h;
+    int* status_hd;       /* status_h as the device addresses it */
     int busy;
     DeferredCopy defer[1];  /* the codestream, for a pageable destination */
     int ndefer;
@@ -285,6 +293,7 @@ static int32_t enc_slot_alloc(jxs_gpu_enc_t* e, EncSlot* s) {
     CK(cudaMalloc(&s->out_stage, c->lcod + 64));
     CK(cudaMallocHost(&s->status_h, 64));
     *s->status_h = 0;
+    CK(cudaHostGetDevicePointer((void**)&s->status_hd, s->status_h, 0));
     for (int i = 0; i < 6; i++) CK(cudaEventCreate(&s->tev[i]));
     for (int i = 0; i < JXS_KEV; i++) CK(cudaEventCreate(&s->kev[i]));
     return JXS_OK;
@@ -451,6 +460,8 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
     uint8_t* dst = out_dev ? out : s->out_stage;
     CK(jxs_launch_pack(e->dcfg, c->np, s->coef, s->gcli, s->rc, s->cost, dst, e->cap_words, s->status, c->vpred ? 2 : 0, st));
     KMARK();
+    publish_status_kernel<<<1, 32, 0, st>>>(s->status_hd, s->status);
+    CK(cudaGetLastError());
     TMARK(4);
     s->ndefer = 0;
     if (!out_dev) {
@@ -459,7 +470,6 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
         else if (host_copy_kernel(out, c->lcod, s->out_stage, c->lcod, c->lcod, 1, st, &ce, out, c->lcod)) CK(ce);
         else s->defer[s->ndefer++] = DeferredCopy{out, c->lcod, s->out_stage, c->lcod, c->lcod, 1};
     }
-    CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
     TMARK(5);
 #undef TMARK
     CK(cudaEventRecord(s->done, st));
@@ -573,7 +583,9 @@ struct DecSlot {
     int mct_pitch[JXS_MAXC];
     int* status;
     int* status_h;
+    int* status_hd;       /* status_h as the device addresses it */
     uint32_t* prec_off_h;
+    const uint32_t* prec_off_hd; /* prec_off_h as the device addresses it */
     uint8_t* hdr_h;       /* header of a device-resident codestream, checked at completion */
     int hdr_check;
     /* the frame's arguments, for a second decode slice by slice when it
@@ -625,6 +637,7 @@ static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
     CK(cudaMalloc(&s->bs, s->bs_cap + 64));
     CK(cudaMalloc(&s->prec_off, (size_t)c->nprec * sizeof(uint32_t)));
     CK(cudaMallocHost(&s->prec_off_h, (size_t)c->nprec * sizeof(uint32_t)));
+    CK(cudaHostGetDevicePointer((void**)&s->prec_off_hd, s->prec_off_h, 0));
     CK(cudaMallocHost(&s->hdr_h, sizeof(c->hdr)));
     CK(cudaMalloc(&s->coef, c->coef_total * sizeof(int16_t) + 64));
     for (uint32_t k = 0; k < c->nc; k++) {
@@ -654,6 +667,7 @@ static int32_t dec_slot_alloc(jxs_gpu_dec_t* d, DecSlot* s) {
     CK(cudaMalloc(&s->status, 64));
     CK(cudaMallocHost(&s->status_h, 64));
     *s->status_h = 0;
+    CK(cudaHostGetDevicePointer((void**)&s->status_hd, s->status_h, 0));
     for (int i = 0; i < 5; i++) CK(cudaEventCreate(&s->tev[i]));
     for (int i = 0; i < JXS_KEV; i++) CK(cudaEventCreate(&s->kev[i]));
     return JXS_OK;
@@ -784,8 +798,10 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         /* the previous use of prec_off_h by this slot has completed: slots are
          * reused only after their completion was observed */
         if (prec_off != s->prec_off_h) memcpy(s->prec_off_h, prec_off, sizeof(uint32_t) * c->nprec);
-        CK(cudaMemcpyAsync(s->prec_off, s->prec_off_h, sizeof(uint32_t) * c->nprec, cudaMemcpyHostToDevice, st));
     }
+    /* host-walked offsets are read by the unpacking blocks straight from the
+     * page-locked buffer (one word per block), not copied */
+    const uint32_t* doff = prec_off ? s->prec_off_hd : s->prec_off;
     s->arg_bs = dbs;
     s->arg_size = size;
     s->arg_walked = prec_off != NULL;
@@ -796,10 +812,10 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
     TMARK(1);
     KMARK();
     if (d->vpred)
-        CK(jxs_launch_unpack_vpred(d->dcfg, dbs, size, s->prec_off, s->coef, c->nslices, d->cap_bytes, d->cap_groups, d->cap_seg,
+        CK(jxs_launch_unpack_vpred(d->dcfg, dbs, size, doff, s->coef, c->nslices, d->cap_bytes, d->cap_groups, d->cap_seg,
                                    s->status, st));
     else
-        CK(jxs_launch_unpack(d->dcfg, dbs, size, s->prec_off, s->coef, c->nprec, d->cap_bytes, d->cap_groups, d->cap_seg, s->status,
+        CK(jxs_launch_unpack(d->dcfg, dbs, size, doff, s->coef, c->nprec, d->cap_bytes, d->cap_groups, d->cap_seg, s->status,
                              st));
     KMARK();
     TMARK(2);
@@ -884,6 +900,8 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         nlt_out_params(c, tin, out, &P);
         CK(jxs_launch_nlt_out(&P, st));
     }
+    publish_status_kernel<<<1, 32, 0, st>>>(s->status_hd, s->status);
+    CK(cudaGetLastError());
     TMARK(3);
     s->ndefer = 0;
     for (uint32_t k = 0; k < c->nc; k++) {
@@ -899,7 +917,6 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
         else
             s->defer[s->ndefer++] = cp;
     }
-    CK(cudaMemcpyAsync(s->status_h, s->status, sizeof(int), cudaMemcpyDeviceToHost, st));
     TMARK(4);
 #undef TMARK
     CK(cudaEventRecord(s->done, st));

@@ -195,6 +195,11 @@ def lib():
         L.svt_jpeg_xs_gpu_batch_ready.restype = u32
         L.svt_jpeg_xs_gpu_batch_get_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchInfo)]
         L.svt_jpeg_xs_gpu_batch_get_info.restype = u32
+        L.svt_jpeg_xs_gpu_batch_set_stage_timing.argtypes = [ctypes.c_void_p, u32]
+        L.svt_jpeg_xs_gpu_batch_set_stage_timing.restype = u32
+        L.svt_jpeg_xs_gpu_batch_read_stage_times.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int32),
+                                                            ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float), u32]
+        L.svt_jpeg_xs_gpu_batch_read_stage_times.restype = u32
         L.svt_jpeg_xs_gpu_server_create.argtypes = [ctypes.c_uint64, u32, u32, u32, ctypes.POINTER(ctypes.c_void_p)]
         L.svt_jpeg_xs_gpu_server_create.restype = u32
         L.svt_jpeg_xs_gpu_server_destroy.argtypes = [ctypes.c_void_p]
@@ -500,6 +505,19 @@ class Batch:
 
     def set_options(self, use_graph=True, autotune=False):
         _check("batch_set_options", lib().svt_jpeg_xs_gpu_batch_set_options(self.h, 1 if use_graph else 0, 1 if autotune else 0))
+
+    STAGES = ("fwd_v", "fwd_h", "rc", "pack", "walk", "unpack", "inv_h", "inv_v")
+
+    def set_stage_timing(self, on=True):
+        _check("batch_set_stage_timing", lib().svt_jpeg_xs_gpu_batch_set_stage_timing(self.h, 1 if on else 0))
+
+    def read_stage_times(self):
+        """[(stage name, variant, ms)] of the launches of the last batch
+        issued with stage timing on (after its wait)."""
+        n = 256
+        st, var, ms = (ctypes.c_int32 * n)(), (ctypes.c_int32 * n)(), (ctypes.c_float * n)()
+        k = lib().svt_jpeg_xs_gpu_batch_read_stage_times(self.h, st, var, ms, n)
+        return [(self.STAGES[st[i]], var[i], ms[i]) for i in range(k)]
 
     def set_tune(self, chains=1, heavy_first=0, grid_per_sm=0, fwd_rows=4, inv_rows=4):
         t = (ctypes.c_int32 * 5)(chains, heavy_first, grid_per_sm, fwd_rows, inv_rows)
