@@ -686,12 +686,21 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
     }
     __syncthreads();
 
-    /* histograms: each lane 4 consecutive groups (one 4-byte load), 8-bit
-     * counters packed four to a register, summed over the warp per 128
-     * groups (at most 128 per bin); a segment of at most 128 groups also
-     * stores its own histograms for packing */
+    /* histograms: each lane 4 consecutive groups (one 4-byte load) in 4-bit
+     * counters, one per GCLI value (at most 4, or 8 for a significance
+     * group's weight), widened to bytes and summed over the warp per 128
+     * groups (at most 128 per bin); then lane b < 16 holds the count of
+     * GCLI b and lane 16 + b that of significance-group maximum b, adds it
+     * to the band line's histogram and, for a segment of at most 128
+     * groups, stores it as byte b / 16 + b of the segment's histograms for
+     * packing */
     uint32_t* seghist = cost + jxs_seghist_word(cfg) + (uint64_t)p * jxs_seg_cap(cfg) * JXS_SEGHIST_WORDS;
+    static_assert(JXS_SEGHIST_WORDS * 4 == 32, "a segment's histograms: one byte per lane");
     const bool export_hist = SG <= 128;
+    /* this lane's bin: byte (b >> 1) & 3 of word 2 (b >= 8) + (b & 1) of the
+     * value (lanes 0..15) or significance (16..31) words */
+    const uint32_t hb = lane & 15u, hsh = 8u * ((hb >> 1) & 3u);
+    uint32_t* htab = (lane < 16 ? &hist[0][0] : &shist[0][0]) + hb;
     for (uint32_t sidx = warp; sidx < nseg; sidx += RC_WARPS) {
         const jxs_seg_t sg = segs[sidx];
         const uint32_t x = sg.bl;
@@ -705,43 +714,39 @@ __device__ __forceinline__ void rc_cost_body(const jxs_cfg_t* __restrict__ cfg, 
         for (uint32_t base = sg.g0; base < gend; base += 128) {
             const uint32_t g = base + 4 * lane;
             const uint32_t nv = g < gend ? min(4u, gend - g) : 0u;
-            const uint32_t w4 = nv ? *(const uint32_t*)(grow + g) : 0u;
-            /* 8-bit counters of GCLIs 0..7 in lo, 8..15 in hi (GCLIs are
-             * below 16): one shift and add per group */
-            uint64_t lo = 0, hi = 0;
-            uint32_t m = 0;
+            uint32_t w4 = nv ? *(const uint32_t*)(grow + g) : 0u;
+            /* GCLIs past the line's end read as 0 and are taken off bin 0 */
+            w4 &= nv >= 4 ? 0xffffffffu : (1u << (8 * nv)) - 1u;
+            uint32_t lo = nv - 4u, hi = 0u; /* bin 0 starts at -(4 - nv) */
 #pragma unroll
             for (int k = 0; k < 4; k++) {
-                const uint32_t v = (w4 >> (8 * k)) & 255u;
-                const uint64_t inc = k < (int)nv ? 1ull << (8 * (v & 7)) : 0ull;
-                if (v & 8) hi += inc;
+                const uint32_t v = (w4 >> (8 * k)) & 15u;
+                const uint32_t inc = 1u << (4 * (v & 7u));
+                if (v & 8u) hi += inc;
                 else lo += inc;
-                if (k < (int)nv) m = max(m, v);
             }
-            const uint32_t h[4] = {(uint32_t)lo, (uint32_t)(lo >> 32), (uint32_t)hi, (uint32_t)(hi >> 32)};
+            const uint32_t m2 = __vmaxu4(w4, w4 >> 16), m = max(m2 & 255u, (m2 >> 8) & 255u);
             /* significance group: 8 groups in lanes 2i, 2i+1; its groups
              * (8, or fewer at the end of a line) counted at its maximum */
             const uint32_t mx = max(m, __shfl_xor_sync(FULL, m, 1));
             const uint32_t nvp = nv + __shfl_xor_sync(FULL, nv, 1);
-            uint64_t slo = 0, shi = 0;
+            uint32_t slo = 0u, shi = 0u;
             if (!(lane & 1) && nv) {
-                const uint64_t si = (uint64_t)nvp << (8 * (mx & 7));
-                if (mx & 8) shi = si;
+                const uint32_t si = nvp << (4 * (mx & 7u));
+                if (mx & 8u) shi = si;
                 else slo = si;
             }
-            const uint32_t sh[4] = {(uint32_t)slo, (uint32_t)(slo >> 32), (uint32_t)shi, (uint32_t)(shi >> 32)};
-            uint32_t mine = 0;
-#pragma unroll
-            for (int r = 0; r < 4; r++) {
-                const uint32_t hs = __reduce_add_sync(FULL, h[r]), ss = __reduce_add_sync(FULL, sh[r]);
-                mine = lane == r ? hs : (lane == 4 + r ? ss : mine);
-                if (lane < 4) {
-                    const uint32_t c = (hs >> (8 * lane)) & 0xffu, cs2 = (ss >> (8 * lane)) & 0xffu;
-                    if (c) atomicAdd(&hist[x][4 * r + lane], c);
-                    if (cs2) atomicAdd(&shist[x][4 * r + lane], cs2);
-                }
-            }
-            if (export_hist && lane < JXS_SEGHIST_WORDS) seghist[sidx * JXS_SEGHIST_WORDS + lane] = mine;
+            /* bytes: even bins, odd bins of 0..7 and of 8..15 */
+            const uint32_t M = 0x0f0f0f0fu;
+            const uint32_t v0 = __reduce_add_sync(FULL, lo & M), v1 = __reduce_add_sync(FULL, (lo >> 4) & M);
+            const uint32_t v2 = __reduce_add_sync(FULL, hi & M), v3 = __reduce_add_sync(FULL, (hi >> 4) & M);
+            const uint32_t s0 = __reduce_add_sync(FULL, slo & M), s1 = __reduce_add_sync(FULL, (slo >> 4) & M);
+            const uint32_t s2 = __reduce_add_sync(FULL, shi & M), s3 = __reduce_add_sync(FULL, (shi >> 4) & M);
+            const uint32_t wv = hb >= 8 ? (hb & 1 ? v3 : v2) : (hb & 1 ? v1 : v0);
+            const uint32_t ws = hb >= 8 ? (hb & 1 ? s3 : s2) : (hb & 1 ? s1 : s0);
+            const uint32_t c = ((lane < 16 ? wv : ws) >> hsh) & 255u;
+            if (c) atomicAdd(htab + 16 * x, c);
+            if (export_hist) ((uint8_t*)(seghist + sidx * JXS_SEGHIST_WORDS))[lane] = (uint8_t)c;
             if (fs) {
                 /* sign handling: the lane's 16 coefficients (inside the band
                  * width) by the number of gtli values at which they stay
