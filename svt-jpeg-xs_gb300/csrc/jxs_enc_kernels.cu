@@ -1038,6 +1038,41 @@ DEV uint64_t data_chunk(uint2 raw4, int wleft, uint32_t v, uint32_t t, uint32_t 
     return planes;
 }
 
+/* The same with the sign nibble leading the planes (signs with the data),
+ * for a group whose coefficients past the band width are stored as zero:
+ * the sign of every coefficient that stays non-zero enters as plane
+ * v - t of its magnitude, and one transpose gives sign and planes. */
+DEV uint64_t data_chunk_signed(uint2 raw4, uint32_t v, uint32_t t, uint32_t uniform) {
+    const uint32_t c01 = raw4.x, c23 = raw4.y, np = v - t;
+    uint32_t P01, P23;
+    if (t == 0) {
+        P01 = c01 & 0x7fff7fffu;
+        P23 = c23 & 0x7fff7fffu;
+    } else if (!uniform) {
+        const uint32_t keep = (0x7fffu >> t) * 0x00010001u;
+        P01 = ((c01 & 0x7fff7fffu) >> t) & keep;
+        P23 = ((c23 & 0x7fff7fffu) >> t) & keep;
+    } else {
+        uint32_t q[4];
+        const uint32_t c[4] = {c01 & 0xffffu, c01 >> 16, c23 & 0xffffu, c23 >> 16};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint32_t m = c[k] & 0x7fffu;
+            const uint32_t u = (((m << (v - t + 1)) - m + (1u << v)) >> (v + 1)) & 0xffffu;
+            q[k] = ((u << t) & 0xffffu) >> t;
+        }
+        P01 = q[0] | (q[1] << 16);
+        P23 = q[2] | (q[3] << 16);
+    }
+    /* sign bits (bits 15 and 31) of the non-zero magnitudes moved to bit np
+     * of each half (np <= 15) */
+    P01 |= (__vcmpne2(P01, 0u) & c01 & 0x80008000u) >> (15 - np);
+    P23 |= (__vcmpne2(P23, 0u) & c23 & 0x80008000u) >> (15 - np);
+    uint64_t planes = coefs_to_planes(__byte_perm(P01, P23, 0x0246));
+    if (np >= 8) planes |= (uint64_t)coefs_to_planes(__byte_perm(P01, P23, 0x1357)) << 32;
+    return planes;
+}
+
 /* Per band line of the precinct being packed. */
 struct PkLine {
     uint32_t sig_pos, gcli_pos, data_pos, sign_pos; /* bit positions in the shared-memory precinct */
@@ -1617,23 +1652,25 @@ __device__ __forceinline__ void pack_body(const jxs_cfg_t* __restrict__ cfg, con
                  * coefficients of the other groups are never read */
                 uint32_t* list = &s_segw[0][0] + 128 * warp;
                 const uint32_t cnt = __reduce_add_sync(FULL, nsig);
-                uint32_t idx = ex >> 25, o = ex_d;
+                {
+                    /* per byte: 1 for a listed group, and its data nibbles
+                     * v - t + 1; their exclusive prefix sums over the
+                     * lane's bytes give each entry's slot and offset */
+                    const uint32_t one = s4 & 0x01010101u, dd = d4 + one;
+                    const uint32_t po = dd * 0x01010100u, pi = one * 0x01010100u;
+                    const uint32_t e0 = (ex_d << 11) | ((uint32_t)lane << 6), i0 = ex >> 25;
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    if ((s4 >> (8 * k)) & 1u) {
-                        list[idx++] = (o << 11) | ((uint32_t)(4 * lane + k) << 4) | v[k];
-                        o += 4 * (v[k] - t + 1);
-                    }
+                    for (int k = 0; k < 4; k++)
+                        if ((one >> (8 * k)) & 1u)
+                            list[i0 + ((pi >> (8 * k)) & 255u)] = e0 + (((po >> (8 * k)) & 255u) << 13) + ((uint32_t)k << 4) + v[k];
                 }
                 __syncwarp();
                 for (uint32_t r = lane; r < cnt; r += 32) {
                     const uint32_t e = list[r];
                     const uint32_t gi = base + ((e >> 4) & 127u), vv = e & 15u, np = vv - t;
+                    /* the coefficients past the band width are stored as zero */
                     const uint2 raw4 = *(const uint2*)(crow + 4 * gi);
-                    uint32_t sgn, nzm;
-                    uint64_t ch = data_chunk(raw4, (int)B.w - 4 * (int)gi, vv, t, uniform, sgn, nzm);
-                    ch |= (uint64_t)sgn << (4 * np);
-                    put_bits(buf, words, dpos + (e >> 11), ch, 4 * (np + 1), ovf);
+                    put_bits(buf, words, dpos + (e >> 11), data_chunk_signed(raw4, vv, t, uniform), 4 * (np + 1), ovf);
                 }
                 __syncwarp();
             } else if (dl4) {

@@ -66,6 +66,13 @@ extern "C" int jxs_gpu_is_page_locked(const void* p) {
     return a.type == cudaMemoryTypeHost;
 }
 
+/* A frame's final status into page-locked host memory, written by the GPU
+ * after the frame's last compute kernel: no 4-byte copy waits in the copy
+ * engines' queues between the frames' large transfers. */
+__global__ void publish_status_kernel(int* __restrict__ host, const int* __restrict__ status) {
+    if (threadIdx.x == 0) *(volatile int*)host = *(const volatile int*)status;
+}
+
 /* Copies between device memory and ordinary (pageable) host memory.  On a
  * GB300 behind NVLink-C2C with the host's page tables shared with the GPU
  * (cudaDevAttrPageableMemoryAccessUsesHostPageTables), a kernel reads and
@@ -76,13 +83,6 @@ extern "C" int jxs_gpu_is_page_locked(const void* p) {
  * the library's until the frame is returned, as with the reference
  * (EncHandle.c:1006 keeps only the input structure, and its workers read
  * the planes later). */
-/* A frame's final status into page-locked host memory, written by the GPU
- * after the frame's last compute kernel: no 4-byte copy waits in the copy
- * engines' queues between the frames' large transfers. */
-__global__ void publish_status_kernel(int* __restrict__ host, const int* __restrict__ status) {
-    if (threadIdx.x == 0) *(volatile int*)host = *(const volatile int*)status;
-}
-
 __global__ void __launch_bounds__(256) host_copy16_kernel(uint8_t* dst, size_t dpitch, const uint8_t* src, size_t spitch,
                                                           uint32_t chunks) {
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
