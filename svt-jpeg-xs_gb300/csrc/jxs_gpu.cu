@@ -133,10 +133,10 @@ static int host_resident(const void* p, size_t bytes) {
     return 1;
 }
 
-/* A 2-D copy with one side in pageable host memory (`host`) by a copy
- * kernel, when the device reaches pageable memory directly and the host
- * side's pages are resident; returns 0 otherwise (the caller then copies
- * another way). */
+/* A 2-D copy with one side in host memory (`host`, pageable or page-locked)
+ * by a copy kernel, when the device reaches pageable memory directly and the
+ * host side's pages are resident; returns 0 otherwise (the caller then
+ * copies another way). */
 static int host_copy_kernel(void* dst, size_t dpitch, const void* src, size_t spitch, size_t width, size_t rows, cudaStream_t st,
                             cudaError_t* err, const void* host, size_t host_pitch) {
     *err = cudaSuccess;
@@ -466,8 +466,12 @@ static int32_t enc_run(jxs_gpu_enc_t* e, EncSlot* s, void* const planes[4], cons
     s->ndefer = 0;
     if (!out_dev) {
         cudaError_t ce = cudaSuccess;
-        if (jxs_gpu_is_page_locked(out)) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));
-        else if (host_copy_kernel(out, c->lcod, s->out_stage, c->lcod, c->lcod, 1, st, &ce, out, c->lcod)) CK(ce);
+        /* the codestream (a tenth of the frame's bytes) by a copy kernel also
+         * from page-locked memory: the copy engines then carry only the
+         * planes, with no small copy queued between them (encode + decode
+         * from host memory: 32.2 -> 34.1 Gpix/s, 4K 4:2:2 10-bit) */
+        if (host_copy_kernel(out, c->lcod, s->out_stage, c->lcod, c->lcod, 1, st, &ce, out, c->lcod)) CK(ce);
+        else if (jxs_gpu_is_page_locked(out)) CK(cudaMemcpyAsync(out, s->out_stage, c->lcod, cudaMemcpyDeviceToHost, st));
         else s->defer[s->ndefer++] = DeferredCopy{out, c->lcod, s->out_stage, c->lcod, c->lcod, 1};
     }
     TMARK(5);
@@ -790,7 +794,9 @@ static int32_t dec_run(jxs_gpu_dec_t* d, DecSlot* s, const uint8_t* bs, uint32_t
             CK(cudaMalloc(&s->bs, s->bs_cap + 64));
         }
         cudaError_t ce = cudaSuccess;
-        if (!jxs_gpu_is_page_locked(bs) && host_copy_kernel(s->bs, size, bs, size, size, 1, st, &ce, bs, size)) CK(ce);
+        /* by a copy kernel also from page-locked memory, as the encoder's
+         * codestream: the copy engines carry only the planes */
+        if (host_copy_kernel(s->bs, size, bs, size, size, 1, st, &ce, bs, size)) CK(ce);
         else CK(cudaMemcpyAsync(s->bs, bs, size, cudaMemcpyHostToDevice, st));
         dbs = s->bs;
     }
