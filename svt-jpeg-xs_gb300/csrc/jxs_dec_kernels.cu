@@ -242,6 +242,35 @@ DEV uint2 decode_group(uint64_t chunk, uint32_t np, uint32_t t, uint32_t gv, uin
     return group_finish(A, B, sgn, uniform && t != 0, wl);
 }
 
+/* The same under deadzone quantization, for a group inside its band line or
+ * at its end (`wl` remaining coefficients): the sign nibble is transposed
+ * with the planes, as the plane above the np magnitude planes, so that the
+ * signs arrive as bit np of each coefficient. */
+DEV uint2 decode_group_dz(uint64_t chunk, uint32_t np, uint32_t t, int wl) {
+    const uint32_t tl = planes_to_coefs((uint32_t)chunk);
+    uint32_t P01 = __byte_perm(tl, 0u, 0x4243), P23 = __byte_perm(tl, 0u, 0x4041);
+    if (np >= 8) {
+        const uint32_t th = planes_to_coefs((uint32_t)(chunk >> 32));
+        P01 |= __byte_perm(th, 0u, 0x4243) << 8;
+        P23 |= __byte_perm(th, 0u, 0x4041) << 8;
+    }
+    /* signs to all-ones halves; magnitudes without them */
+    const uint32_t s01 = (P01 >> np) & 0x00010001u, s23 = (P23 >> np) & 0x00010001u;
+    const uint32_t n01 = s01 * 0xffffu, n23 = s23 * 0xffffu;
+    uint32_t a = (P01 ^ (s01 << np)) << t, b = (P23 ^ (s23 << np)) << t;
+    if (t > 0) {
+        /* deadzone reconstruction (Dequant.c:9-21): half a step on non-zero magnitudes */
+        const uint32_t half = (1u << (t - 1)) * 0x00010001u;
+        a |= __vcmpne2(a, 0u) & half;
+        b |= __vcmpne2(b, 0u) & half;
+    }
+    /* two's complement of the negative ones, two per word */
+    a = __vsub2(a ^ n01, n01);
+    b = __vsub2(b ^ n23, n23);
+    const uint32_t keepA = (wl > 1 ? 0xffff0000u : 0u) | 0xffffu, keepB = (wl > 2 ? 0xffffu : 0u) | (wl > 3 ? 0xffff0000u : 0u);
+    return make_uint2(a & keepA, b & keepB);
+}
+
 /* unpack_precinct (Packing.c:513-868) for one precinct row; vertical
  * prediction and separate sign sub-packets are rejected.
  *
@@ -843,7 +872,7 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                 const uint32_t s4 = __vcmpgtu4(v4, t4), nsig = __popc(s4 & 0x01010101u);
                 uint32_t tot;
                 const uint32_t ex = warp_excl_scan((__vsadu4(__vsubus4(v4, t4), 0u) + nsig) | (nsig << 24), &tot);
-                uint32_t o = (ex & 0xffffffu) << 2;
+                const uint32_t o = (ex & 0xffffffu) << 2;
                 /* zeros for the lane's groups (those with data are written
                  * again below, after the warp barrier) */
                 if (one_col) {
@@ -861,14 +890,18 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                         if (!((s4 >> (8 * (c >> 2))) & 1u)) crow[4 * g + c] = 0;
                 }
                 const uint32_t cnt = tot >> 24;
-                uint32_t idx = ex >> 24;
+                {
+                    /* per byte: 1 for a listed group, and its data nibbles
+                     * v - t + 1; their exclusive prefix sums over the lane's
+                     * bytes give each entry's slot and offset */
+                    const uint32_t one = s4 & 0x01010101u, dd = __vsubus4(v4, t4) + one;
+                    const uint32_t po = dd * 0x01010100u, pi = one * 0x01010100u;
+                    const uint32_t e0 = (o << 11) | ((uint32_t)lane << 6), i0 = ex >> 24;
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    if ((s4 >> (8 * q)) & 1u) {
-                        const uint32_t v = (v4 >> (8 * q)) & 255u;
-                        list[idx++] = (o << 11) | ((uint32_t)(4 * lane + q) << 4) | (v & 15u);
-                        o += 4 * (v - t + 1);
-                    }
+                    for (int q = 0; q < 4; q++)
+                        if ((one >> (8 * q)) & 1u)
+                            list[i0 + ((pi >> (8 * q)) & 255u)] =
+                                e0 + (((po >> (8 * q)) & 255u) << 13) + ((uint32_t)q << 4) + ((v4 >> (8 * q)) & 15u);
                 }
                 __syncwarp();
                 for (uint32_t r = lane; r < cnt; r += 32) {
@@ -879,7 +912,8 @@ __device__ __forceinline__ void unpack_body(const jxs_cfg_t* __restrict__ cfg, c
                     const uint32_t w0 = be_word(pbuf, wi), w1 = be_word(pbuf, wi + 1), w2 = be_word(pbuf, wi + 2);
                     const uint64_t win = ((uint64_t)__funnelshift_l(w1, w0, sh) << 32) | __funnelshift_l(w2, w1, sh);
                     const int wl = (int)B.w - 4 * (int)gi;
-                    const uint2 ov = decode_group(win >> (64 - ln), np, t, v, uniform, wl);
+                    const uint2 ov = uniform ? decode_group(win >> (64 - ln), np, t, v, uniform, wl)
+                                             : decode_group_dz(win >> (64 - ln), np, t, wl);
                     if (one_col) {
                         *(uint2*)(crow + 4 * gi) = ov;
                     } else {
