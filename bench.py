@@ -494,7 +494,9 @@ def link_rates(torch, dev, nbytes=33 << 20, reps=20):
         return reps * nbytes / (time.perf_counter() - t0) / 1e9
 
     run(True, True)
-    return {"h2d_gbs": run(True, False), "d2h_gbs": run(False, True), "both_gbs_per_direction": run(True, True)}
+    # best of three: the link is the host's, and other traffic can slow one run
+    return {"h2d_gbs": max(run(True, False) for _ in range(3)), "d2h_gbs": max(run(False, True) for _ in range(3)),
+            "both_gbs_per_direction": max(run(True, True) for _ in range(3))}
 
 
 def launch_name(stage, variant):
@@ -757,21 +759,29 @@ def run_ours(args, rank, world, local):
                         marks.append(time.perf_counter())
         return marks
 
+    # the driving loop is Python: no garbage-collector pauses inside the
+    # timed pipelines (the library itself allocates nothing per frame)
     e2e_run(max(1, args.warmup) * F)
     torch.cuda.synchronize()
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
     marks = e2e_run(args.steps * F)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+    gc.enable()
     lat = list(np.diff([t0] + marks))
     e2e_val = args.steps * F * world * W * H / e2e_s / 1e9
     # the same pipeline from and to pageable host memory
     e2e_run(max(1, args.warmup) * F, p_enc_frames, p_dec_frames)
     torch.cuda.synchronize()
+    gc.collect()
+    gc.disable()
     t0 = time.perf_counter()
     e2e_run(args.steps * F, p_enc_frames, p_dec_frames)
     torch.cuda.synchronize()
     e2e_pg_val = args.steps * F * world * W * H / (time.perf_counter() - t0) / 1e9
+    gc.enable()
     assert all(np.array_equal(a, b) for i in range(R) for a, b in zip(p_out[i], h_out[i])), \
         "decode from pageable memory differs from the page-locked run"
     in_bytes = sum(p.nbytes for p in frames[0])
