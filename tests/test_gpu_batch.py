@@ -164,3 +164,45 @@ def test_batch_device_budget(gpu):
     assert r == 0 and np.array_equal(outs[0][: enc.frame_bytes], enc.encode(planes))
     batch.close()
     enc.close()
+
+
+def test_batch_stage_timing(gpu):
+    """Stage timing: with it on, a batch runs without graphs, its outputs
+    unchanged, and every launch reports its stage and a device time; the
+    golden 4:2:2 and 4:4:4 cases encode in one launch per stage, so the
+    stages come in pipeline order."""
+    names = ["c1_422_8b", "c3_444_12b"]
+    encs = [make_encoder(gpu, SMALL[n]) for n in names]
+    decs = [gpu.Decoder(SMALL[n]["bs"]) for n in names]
+    batch = gpu.Batch(1 * GB)
+    batch.set_tune(1, 0, 0, 4, 4)
+    batch.set_stage_timing(True)
+    bss = _encode_batch(gpu, batch, encs, [SMALL[n]["planes"] for n in names])
+    for n, bs in zip(names, bss):
+        assert np.array_equal(bs, SMALL[n]["bs"]), n
+    enc_t = batch.read_stage_times()
+    outs = _decode_batch(gpu, batch, decs, [SMALL[n]["bs"] for n in names])
+    for n, out in zip(names, outs):
+        assert all(np.array_equal(a, b) for a, b in zip(out, SMALL[n]["dec"])), n
+    dec_t = batch.read_stage_times()
+    order = {s: i for i, s in enumerate(gpu.Batch.STAGES)}
+    for times, allowed in ((enc_t, {"fwd_v", "fwd_h", "rc", "pack"}), (dec_t, {"walk", "unpack", "inv_h", "inv_v"})):
+        stages = [s for s, _, _ in times]
+        assert stages and set(stages) <= allowed, stages
+        assert all(ms > 0 for _, _, ms in times), times
+        # one chain: rate control after every transform launch, packing last
+        if "rc" in stages:
+            assert stages.index("rc") > max(i for i, s in enumerate(stages) if s.startswith("fwd"))
+            assert stages[-1] == "pack"
+        assert [order[s] for s in stages if s in ("unpack", "inv_h")] == sorted(order[s] for s in stages if s in ("unpack", "inv_h"))
+    assert {"fwd_v", "rc", "pack"} <= {s for s, _, _ in enc_t}
+    assert {"unpack", "inv_v"} <= {s for s, _, _ in dec_t}
+    assert batch.info()["graph_hits"] == 0
+    # off again: graphs resume and nothing more is recorded
+    batch.set_stage_timing(False)
+    _encode_batch(gpu, batch, encs, [SMALL[n]["planes"] for n in names])
+    _encode_batch(gpu, batch, encs, [SMALL[n]["planes"] for n in names])
+    assert batch.info()["graph_hits"] >= 1
+    batch.close()
+    for x in encs + decs:
+        x.close()
