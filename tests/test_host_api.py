@@ -134,3 +134,16 @@ def test_buffer_tools(jxs_lib):
     L.svt_jpeg_xs_frame_pool_release(pool, ctypes.byref(f1))
     assert L.svt_jpeg_xs_frame_pool_get(pool, ctypes.byref(f3), 0) == 0
     L.svt_jpeg_xs_frame_pool_free(pool)
+
+
+def test_batch_entry_points_reject_null(jxs_lib):
+    """The batch extension's entry points validate their handle before any
+    CUDA call: a null batch is a bad parameter (or no stage times)."""
+    L = jxs_lib.lib()
+    assert L.svt_jpeg_xs_gpu_batch_set_stage_timing(None, 1) == jxs_lib.E_BAD_PARAMETER
+    n = 4
+    st, var, ms = (ctypes.c_int32 * n)(), (ctypes.c_int32 * n)(), (ctypes.c_float * n)()
+    assert L.svt_jpeg_xs_gpu_batch_read_stage_times(None, st, var, ms, n) == 0
+    assert L.svt_jpeg_xs_gpu_batch_set_options(None, 1, 0) == jxs_lib.E_BAD_PARAMETER
+    t = (ctypes.c_int32 * 5)(1, 0, 0, 4, 4)
+    assert L.svt_jpeg_xs_gpu_batch_set_tune(None, t) == jxs_lib.E_BAD_PARAMETER
