@@ -1097,9 +1097,10 @@ struct PkLine {
  *           band (significance only if strictly cheaper), packet headers, raw
  *           fallback, packet positions by a warp scan, sub-packet positions,
  *           each segment's start in its GCLI and data sub-packets;
- *   pass B  each lane one group: significance flags, the unary GCLI code and
- *           the data bits, at positions from a warp prefix sum, OR-ed into
- *           the buffer.
+ *   pass B  each lane 4 groups: significance flags and the unary GCLI
+ *           codes at positions from a warp prefix sum; the groups above
+ *           gtli listed per warp, each lane then packing one listed group's
+ *           data bits; everything OR-ed into the buffer.
  * VPRED (frames with vertical prediction; compiled out otherwise): a
  * precinct row below another of its slice also sums, per segment, the
  * codes of its GCLIs predicted from the line above at its gtli (line 0:
